@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 traversal path: Mrays/s closest-hit.
+
+Workload (the raw-traversal configuration): a 1,048,576-triangle float32 soup
+(seed 2; centroids uniform in the unit cube, vertices at centroid + 0.005 x a
+direction uniform on the sphere) in the reference-built QBVH (binned SAH,
+leafMax 16), and 4,194,304 incoherent rays (origins uniform in the cube,
+directions uniform on the sphere, tmax = +inf).  A step = one closest-hit
+trace of all 4M rays.  Inputs are generated from seeds (no scene files ship
+with the reference).
+
+  value  : rays / device time of the trace kernel, rays already in HBM, L2
+           flushed (256 MB write) before every timed step
+  e2e    : the same trace through the C ABI with pinned host buffers: the
+           host->device copy of the rays and device->host copy of the hits
+           are inside the timed region
+  roofline: algorithmic bytes per launch = rays * 44 + 128 * node visits +
+           48 * triangle tests (visit counts from the kernel's counters, which
+           equal the oracle's), over the kernel's average duration, against
+           the measured HBM copy bandwidth
+
+`--impl reference` times the reference algorithm on the host cores: the C++
+restatement in oracle/ (the Go reference does not build here: no Go
+toolchain, and its assembly is amd64-only).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 1 << 20
+N_RAYS = 1 << 22
+SEED = 2
+METRIC = "Mrays/s closest-hit"
+CONFIG = {"workload": "raw traversal: 1,048,576-triangle soup (seed 2), 4,194,304 incoherent rays, closest-hit",
+          "triangles": N_TRIS, "rays_per_step": N_RAYS, "leaf_max": 16,
+          "l2": "flushed between timed steps (256 MB write); scene data (~55 MB) is L2-resident by design"}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the traversal kernel from the committed ncu
+    summary (profiles/traverse_soup1m_incoherent.md), or None."""
+    p = os.path.join(ROOT, "profiles", "traverse_soup1m_incoherent.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def make_workload():
+    from vermeer_gb300 import scenes
+    v, ip = scenes.triangle_soup(N_TRIS, SEED)
+    rays = scenes.incoherent_rays(N_RAYS, SEED)
+    return v, ip, rays
+
+
+def cpu_baseline(v, ip, rays, threads, sample):
+    """The oracle port on the host cores over a bounded sample of the rays."""
+    from oracle import orc
+    m = orc.Mesh(v, ip)
+    sub = rays[:sample]
+    m.trace(sub[:4096], nthreads=threads)  # warm the caches / thread pool
+    t0 = time.perf_counter()
+    m.trace(sub, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return sample / dt / 1e6, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    v, ip, rays = make_workload()
+    threads = cpu_threads()
+    sample = 1 << 18
+    from oracle import orc
+    m = orc.Mesh(v, ip)
+    for i in range(args.warmup):
+        m.trace(rays[i * sample % N_RAYS:][:sample], nthreads=threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        s = (i * sample) % N_RAYS
+        m.trace(rays[s:s + sample], nthreads=threads)
+    dt = time.perf_counter() - t0
+    value = sample * args.steps / dt / 1e6
+    line = {"metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": dict(CONFIG, rays_per_step=sample), "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} of the {N_RAYS} incoherent rays per step, {threads} threads; "
+                                       "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"},
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import vermeer_gb300 as vg
+    from vermeer_gb300 import _lib
+
+    v, ip, rays = make_workload()
+    ctx = vg.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    geom = ctx.mesh_build(v, ip)
+    soa = np.ascontiguousarray(rays[:, :7].T)  # px py pz dx dy dz tmax
+    d_rays = torch.from_numpy(soa).to(dev)
+    out = {k: torch.empty(N_RAYS, dtype=torch.int32 if k == "prim" else torch.float32, device=dev)
+           for k in ("prim", "t", "u", "v", "w")}
+    P = ctypes.c_void_p
+    r = _lib.Rays(*[P(d_rays[k].data_ptr()) for k in range(7)], None)
+    h = _lib.Hits(P(out["prim"].data_ptr()), None, *[P(out[k].data_ptr()) for k in ("t", "u", "v", "w")])
+    L = ctx.L
+
+    def trace(flags):
+        st = _lib.TraceStats()
+        rc = L.vmr_trace_mesh(ctx.h, geom, ctypes.byref(r), N_RAYS, flags, ctypes.byref(h), ctypes.byref(st))
+        if rc != 0:
+            raise vg.VmrError(rc, L.vmr_last_error(ctx.h).decode())
+        return st
+
+    # Visit counts for the algorithmic byte count: one untimed host-buffer
+    # pass with the counters on (they equal the oracle's NodesT/LeafsT sums).
+    host_soa = [np.ascontiguousarray(soa[k]) for k in range(7)]
+    hr = _lib.Rays(*[h_.ctypes.data_as(P) for h_ in host_soa], None)
+    hbuf = {k: np.empty(N_RAYS, np.int32 if k == "prim" else np.float32) for k in ("prim", "t", "u", "v", "w")}
+    hh = _lib.Hits(hbuf["prim"].ctypes.data_as(P), None, *[hbuf[k].ctypes.data_as(P) for k in ("t", "u", "v", "w")])
+    cst = _lib.TraceStats()
+    rc = L.vmr_trace_mesh(ctx.h, geom, ctypes.byref(hr), N_RAYS, 4, ctypes.byref(hh), ctypes.byref(cst))
+    if rc != 0:
+        raise vg.VmrError(rc, L.vmr_last_error(ctx.h).decode())
+    alg_bytes = N_RAYS * 44.0 + 128.0 * cst.node_visits + 48.0 * cst.tri_tests
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        flush.zero_()
+        trace(2)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            trace(2)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ctx.sync()
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(kernel_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall = t.tolist()
+    value = N_RAYS * args.steps * world / dev_s / 1e6
+    avg_launch_s = dev_s / args.steps
+
+    # End to end through the C ABI: pinned host rays in, pinned hits out.
+    pin_rays = [torch.from_numpy(host_soa[k]).pin_memory() for k in range(7)]
+    pin_out = {k: torch.empty(N_RAYS, dtype=torch.int32 if k == "prim" else torch.float32).pin_memory()
+               for k in ("prim", "t", "u", "v", "w")}
+    er = _lib.Rays(*[P(t_.data_ptr()) for t_ in pin_rays], None)
+    eh = _lib.Hits(P(pin_out["prim"].data_ptr()), None, *[P(pin_out[k].data_ptr()) for k in ("t", "u", "v", "w")])
+    est = _lib.TraceStats()
+
+    def e2e_step():
+        rc_ = L.vmr_trace_mesh(ctx.h, geom, ctypes.byref(er), N_RAYS, 0, ctypes.byref(eh), ctypes.byref(est))
+        if rc_ != 0:
+            raise vg.VmrError(rc_, L.vmr_last_error(ctx.h).decode())
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = N_RAYS * args.steps * world / e2e_s / 1e6
+    ok = np.array_equal(pin_out["prim"].numpy(), hbuf["prim"])
+
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / avg_launch_s / 1e9
+    traffic = profiled_traffic()
+    clocks = clk.summary()
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": CONFIG,
+            "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 7 * 4,
+                    "d2h_bytes_per_step": N_RAYS * 5 * 4, "hits_match_device_path": bool(ok)},
+            "gpu_launches": args.steps,
+            "kernel_ms_mean": round(avg_launch_s * 1e3, 4),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes,
+                         "node_visits_per_ray": round(cst.node_visits / N_RAYS, 3),
+                         "tri_tests_per_ray": round(cst.tri_tests / N_RAYS, 3)},
+            "clocks": clocks}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        sample = 1 << 20
+        cval, cdt = cpu_baseline(v, ip, rays, threads, sample)
+        line["cpu_baseline"] = {"value": round(cval, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                "sample": f"{sample} of the {N_RAYS} incoherent rays ({cdt:.1f} s), "
+                                          "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

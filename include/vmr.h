@@ -1,0 +1,202 @@
+/*
+ * vmr.h - C ABI of libvmr, the GB300 (sm_103a) traversal and rendering path
+ * for Vermeer scenes.
+ *
+ * The reference renderer (jamiec7919/vermeer, Go) reaches its hot path through
+ * Go interfaces: core.Scene (core/scene.go:8-24) with qbvh.Trace /
+ * qbvh.TraceMotion (qbvh/intersect.go:91, qbvh/motionintersect.go:22) calling
+ * PolyMesh.TraceElems / TraceMotionElems (builtin/geom/polymesh/trace.go:108,
+ * :520) one ray at a time, and core.Render (core/render.go:140) looping over
+ * pixels.  A per-ray callback cannot cross cgo efficiently, so this ABI takes
+ * whole batches: meshes with their reference-built QBVH, SoA ray streams, and
+ * whole render passes.  Every function returns a vmr_status; 0 is success.
+ *
+ * Threading: one context per host thread (a Go caller pins its goroutine with
+ * runtime.LockOSThread).  Calls on one context are serialised on its stream;
+ * contexts are independent.  No call invokes a host callback.
+ */
+#ifndef VMR_H
+#define VMR_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VMR_ABI_VERSION 1
+
+typedef enum {
+    VMR_OK = 0,
+    VMR_ERR_INVALID = -1,        /* bad argument or handle */
+    VMR_ERR_CUDA = -2,           /* a CUDA runtime call failed */
+    VMR_ERR_OOM = -3,            /* device or host allocation failed */
+    VMR_ERR_TIMEOUT = -4,        /* a device loop hit its iteration cap */
+    VMR_ERR_STACK_OVERFLOW = -5, /* a ray needed more than 90 traversal stack
+                                    entries (RenderTask.Traversal.Stack,
+                                    core/ray.go:158) */
+    VMR_ERR_QUEUE_OVERFLOW = -6, /* a wavefront queue exceeded its capacity */
+    VMR_ERR_UNSUPPORTED = -7     /* input the path does not handle */
+} vmr_status;
+
+typedef struct vmr_ctx vmr_ctx;
+
+/* ---------------------------------------------------------------- context */
+/* Replaces the process-global state of core (core/core.go:10-15): a Go host
+ * creates one context per render.  device < 0 creates a host-only context
+ * that builds and exports accelerators but cannot trace. */
+int vmr_create(int device, vmr_ctx** out);
+int vmr_destroy(vmr_ctx* ctx);
+/* Message of the last failing call on ctx (owned by ctx, never NULL). */
+const char* vmr_last_error(const vmr_ctx* ctx);
+/* Use an external CUDA stream (a cudaStream_t) for all work of ctx; NULL
+ * restores the context's own stream. */
+int vmr_set_stream(vmr_ctx* ctx, void* cuda_stream);
+/* Wait for the context's stream and report any device-side status
+ * (stack overflow, iteration caps) raised since the last call. */
+int vmr_sync(vmr_ctx* ctx);
+int vmr_abi_version(void);
+
+/* ------------------------------------------------------------ QBVH nodes */
+/* qbvh.Node (qbvh/qbvh.go:31-36), 128 bytes, identical memory layout:
+ * boxes[child + 12*(0 min|1 max) + 4*axis]; children >= 0 inner node,
+ * -1 empty, else leaf (1<<31)|(first<<4)|(count-1). */
+typedef struct {
+    float boxes[24];
+    uint32_t axis0, axis1, axis2;
+    int32_t children[4];
+    int32_t parent;
+} vmr_qbvh_node;
+
+/* qbvh.MotionNode (qbvh/mqbvh.go:24-29), 40 bytes. */
+typedef struct {
+    int32_t axis0, axis1, axis2;
+    int32_t children[4];
+    int32_t parent;
+    uint32_t pad[2];
+} vmr_mqbvh_node;
+
+typedef enum {
+    VMR_MOTION_FAITHFUL = 0, /* leaf test reads idxp at the leaf position, as
+                                TraceMotionElems does (trace.go:532-537) */
+    VMR_MOTION_FIXED = 1     /* leaf position mapped through accel idx, the
+                                face the leaf boxes were built from */
+} vmr_motion_mode;
+
+/* --------------------------------------------------------------- meshes */
+/* Raw mesh input (the PolyMesh fields after init(), polymesh/init.go):
+ * verts is a key-major PointArray (motion_keys * n_verts * 3 floats), idxp
+ * holds 3 vertex indices per triangle in face order. */
+typedef struct {
+    const float* verts;
+    uint32_t n_verts;
+    uint32_t motion_keys;
+    const uint32_t* idxp;
+    uint32_t n_tris;
+    float ray_bias;               /* PolyMesh.RayBias */
+    int motion_mode;              /* vmr_motion_mode */
+    const uint8_t* shader_idx;    /* optional, per face in face order */
+} vmr_mesh_input;
+
+/* A mesh whose QBVH was built by the caller (the reference's
+ * PolyMesh.initAccel, buildqbvh.go:14-144).  Static: nodes + accel_idx and
+ * idxp already permuted to leaf order.  Motion: mnodes + mboxes
+ * ([keys][n_mnodes][24]) + accel_idx, idxp in face order, plus the per-key
+ * bounds (PolyMesh.motionBounds) used by the top level. */
+typedef struct {
+    const float* verts;
+    uint32_t n_verts;
+    uint32_t motion_keys;
+    const uint32_t* idxp;
+    uint32_t n_tris;
+    const int32_t* accel_idx;
+    float ray_bias;
+    int motion_mode;
+    const vmr_qbvh_node* nodes;
+    uint32_t n_nodes;
+    const vmr_mqbvh_node* mnodes;
+    uint32_t n_mnodes;
+    const float* mboxes;
+    const float* bounds;          /* 6 floats (static) or 6*motion_keys */
+    const uint8_t* shader_idx;    /* optional, per face in leaf order */
+} vmr_mesh_desc;
+
+/* Build the mesh's QBVH on the host exactly as PolyMesh.initAccel does
+ * (binned SAH, qbvh/build.go:28-307, leafMax 16) and upload it. */
+int vmr_mesh_build(vmr_ctx* ctx, const vmr_mesh_input* in, uint32_t* out_geom);
+/* Upload a caller-built (reference-built) accelerator; the data is copied. */
+int vmr_mesh_upload(vmr_ctx* ctx, const vmr_mesh_desc* desc, uint32_t* out_geom);
+/* Sizes of a mesh's accelerator: static node count, motion node count. */
+int vmr_mesh_info(vmr_ctx* ctx, uint32_t geom, uint32_t* n_nodes, uint32_t* n_mnodes,
+                  uint32_t* n_tris, uint32_t* motion_keys);
+/* Copy the host-side accelerator of a mesh (what the builder produced or the
+ * caller uploaded).  Any pointer may be NULL.  bounds: 6 floats per key. */
+int vmr_mesh_export(vmr_ctx* ctx, uint32_t geom, vmr_qbvh_node* nodes, int32_t* accel_idx,
+                    uint32_t* idxp, vmr_mqbvh_node* mnodes, float* mboxes, float* bounds);
+
+/* ---------------------------------------------------------------- scene */
+/* Two-level scene (builtin/scene/scene.go): a top-level QBVH with leafMax 1
+ * over the listed geoms (Scene.initAccel, scene.go:135-203).  Replaces any
+ * previous scene of ctx. */
+int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n_geoms);
+/* Caller-built top level: static nodes, or motion nodes + boxes; geom_order
+ * maps leaf position -> geom id. */
+int vmr_scene_upload(vmr_ctx* ctx, const vmr_qbvh_node* nodes, uint32_t n_nodes,
+                     const vmr_mqbvh_node* mnodes, uint32_t n_mnodes, const float* mboxes,
+                     uint32_t motion_keys, const uint32_t* geom_order, uint32_t n_geoms);
+/* Top-level export: geom_order (leaf position -> geom id), nodes or motion
+ * nodes + boxes.  Any pointer may be NULL. */
+int vmr_scene_export(vmr_ctx* ctx, uint32_t* geom_order, vmr_qbvh_node* nodes,
+                     vmr_mqbvh_node* mnodes, float* mboxes, uint32_t* n_nodes,
+                     uint32_t* n_mnodes, uint32_t* motion_keys);
+
+/* ---------------------------------------------------------------- trace */
+/* Structure-of-arrays ray stream (the traversal inputs of core.Ray,
+ * core/ray.go:27-51).  time may be NULL (time 0). */
+typedef struct {
+    const float *px, *py, *pz;
+    const float *dx, *dy, *dz;
+    const float *tmax;
+    const float *time;
+} vmr_rays;
+
+/* Hit stream.  prim = ShaderContext.ElemID (leaf-order triangle index for
+ * static meshes, -1 on a miss); geom = hit geom id (scene traces); t =
+ * Ray.Tclosest after the trace; u,v,w = barycentrics of the accepted hit.
+ * Any pointer may be NULL. */
+typedef struct {
+    int32_t* prim;
+    int32_t* geom;
+    float *t, *u, *v, *w;
+} vmr_hits;
+
+typedef enum {
+    VMR_TRACE_CLOSEST = 0,
+    VMR_TRACE_ANY_HIT = 1,   /* RayTypeShadow: stop at the first hit leaf
+                                (intersect.go:231-236) */
+    VMR_TRACE_DEVICE = 2,    /* ray and hit pointers are device pointers;
+                                the call is asynchronous on ctx's stream */
+    VMR_TRACE_COUNT = 4      /* fill the visit counters of vmr_trace_stats */
+} vmr_trace_flags;
+
+typedef struct {
+    uint64_t rays;
+    uint64_t node_visits;    /* Ray.NodesT summed over rays */
+    uint64_t leaf_visits;    /* Ray.LeafsT summed over rays */
+    uint64_t tri_tests;
+    float kernel_ms;         /* device time of the traversal kernel */
+} vmr_trace_stats;
+
+/* Closest-hit / any-hit traversal of one mesh (PolyMesh.Trace without a
+ * transform, trace.go:57-101).  Host pointers (default): the call copies
+ * rays in and hits out and returns when done.  stats may be NULL. */
+int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags,
+                   const vmr_hits* hits, vmr_trace_stats* stats);
+/* Traversal of the two-level scene (Scene.Trace, scene.go:30-58). */
+int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags,
+                    const vmr_hits* hits, vmr_trace_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,217 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liborc.so).
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA path.  Only the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import
+this module.  The product package ``vermeer_gb300`` never does.
+
+Every entry point restates a reference function; the C++ sources cite the
+file:line of each (oracle/orc_core.cpp, oracle/orc_ldseq.cpp,
+oracle/orc_render.cpp).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liborc.so")
+_lib = None
+
+ORC_NODE_DTYPE = np.dtype([
+    ("boxes", "<f4", (24,)),
+    ("axis", "<u4", (3,)),
+    ("children", "<i4", (4,)),
+    ("parent", "<i4"),
+])
+ORC_MNODE_DTYPE = np.dtype([
+    ("axis", "<i4", (3,)),
+    ("children", "<i4", (4,)),
+    ("parent", "<i4"),
+    ("pad", "<u4", (2,)),
+])
+assert ORC_NODE_DTYPE.itemsize == 128 and ORC_MNODE_DTYPE.itemsize == 40
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++, -ffp-contract=off)."""
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        L.orc_mesh_create.restype = P
+        L.orc_mesh_create.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_uint32,
+                                      ctypes.c_float, ctypes.c_int]
+        L.orc_mesh_destroy.argtypes = [P]
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_mesh_info.argtypes = [P, P, P, P]
+        L.orc_mesh_export.argtypes = [P, P, P, P, P, P]
+        L.orc_trace_mesh.restype = ctypes.c_int
+        L.orc_trace_mesh.argtypes = [P, P, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+                                     P, P, P, P, P, P]
+        L.orc_scene_create.restype = P
+        L.orc_scene_create.argtypes = [P, ctypes.c_uint32]
+        L.orc_scene_destroy.argtypes = [P]
+        L.orc_scene_info.argtypes = [P, P, P, P]
+        L.orc_scene_export.argtypes = [P, P, P, P, P]
+        L.orc_trace_scene.restype = ctypes.c_int
+        L.orc_trace_scene.argtypes = [P, P, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+                                      P, P, P, P, P, P, P]
+        L.orc_vdc.restype = ctypes.c_uint64
+        L.orc_vdc.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_sobol.restype = ctypes.c_uint64
+        L.orc_sobol.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_raster_xy.restype = ctypes.c_uint64
+        L.orc_raster_xy.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
+                                    ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]
+        L.orc_vdc_sobol_tables.argtypes = [ctypes.c_uint32, P, P]
+        _register_render(L)
+        _lib = L
+    return _lib
+
+
+def _register_render(L):
+    if hasattr(L, "orc_render"):
+        P = ctypes.c_void_p
+        L.orc_render.restype = ctypes.c_int
+        L.orc_render.argtypes = [P, P, P, ctypes.c_int]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Mesh:
+    """A PolyMesh with its accelerator built by the oracle."""
+
+    def __init__(self, verts, idxp, keys=1, ray_bias=0.0, motion_fixed=False):
+        verts = np.ascontiguousarray(verts, dtype=np.float32)
+        idxp = np.ascontiguousarray(idxp, dtype=np.uint32)
+        assert verts.size % (3 * keys) == 0 and idxp.size % 3 == 0
+        self.nverts = verts.size // (3 * keys)
+        self.keys = keys
+        self.ntris = idxp.size // 3
+        self.verts, self.idxp_in = verts, idxp
+        self.h = lib().orc_mesh_create(_ptr(verts), self.nverts, keys, _ptr(idxp), self.ntris,
+                                       float(ray_bias), int(bool(motion_fixed)))
+        if not self.h:
+            raise ValueError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mesh_destroy(self.h)
+            self.h = None
+
+    def info(self):
+        n = ctypes.c_uint32()
+        nm = ctypes.c_uint32()
+        b = np.zeros(6, np.float32)
+        lib().orc_mesh_info(self.h, ctypes.byref(n), ctypes.byref(nm), _ptr(b))
+        return n.value, nm.value, b
+
+    def export(self):
+        n, nm, b = self.info()
+        nodes = np.zeros(n, ORC_NODE_DTYPE)
+        accel_idx = np.zeros(self.ntris, np.int32)
+        idxp = np.zeros(self.ntris * 3, np.uint32)
+        mnodes = np.zeros(nm, ORC_MNODE_DTYPE)
+        mboxes = np.zeros((self.keys if nm else 0, nm, 24), np.float32)
+        lib().orc_mesh_export(self.h, _ptr(nodes), _ptr(accel_idx), _ptr(idxp), _ptr(mnodes),
+                              _ptr(mboxes))
+        return dict(nodes=nodes, accel_idx=accel_idx, idxp=idxp, mnodes=mnodes, mboxes=mboxes,
+                    bounds=b)
+
+    def trace(self, rays, shadow=False, nthreads=0, counters=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        u = np.empty(n, np.float32)
+        v = np.empty(n, np.float32)
+        w = np.empty(n, np.float32)
+        cnt = np.empty((n, 3), np.uint32) if counters else None
+        st = lib().orc_trace_mesh(self.h, _ptr(rays), n, int(bool(shadow)), int(nthreads),
+                                  _ptr(prim), _ptr(t), _ptr(u), _ptr(v), _ptr(w), _ptr(cnt))
+        out = dict(prim=prim, t=t, u=u, v=v, w=w, status=st)
+        if counters:
+            out["counters"] = cnt
+        return out
+
+
+class Scene:
+    """The two-level scene of builtin/scene over oracle meshes."""
+
+    def __init__(self, meshes):
+        self.meshes = list(meshes)
+        arr = (ctypes.c_void_p * len(self.meshes))(*[m.h for m in self.meshes])
+        self.h = lib().orc_scene_create(arr, len(self.meshes))
+        if not self.h:
+            raise ValueError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_scene_destroy(self.h)
+            self.h = None
+
+    def export(self):
+        n = ctypes.c_uint32()
+        nm = ctypes.c_uint32()
+        keys = ctypes.c_uint32()
+        lib().orc_scene_info(self.h, ctypes.byref(n), ctypes.byref(nm), ctypes.byref(keys))
+        nodes = np.zeros(n.value, ORC_NODE_DTYPE)
+        order = np.zeros(len(self.meshes), np.int32)
+        mnodes = np.zeros(nm.value, ORC_MNODE_DTYPE)
+        mboxes = np.zeros((keys.value if nm.value else 0, nm.value, 24), np.float32)
+        lib().orc_scene_export(self.h, _ptr(nodes), _ptr(order), _ptr(mnodes), _ptr(mboxes))
+        return dict(nodes=nodes, geom_order=order, mnodes=mnodes, mboxes=mboxes, keys=keys.value)
+
+    def trace(self, rays, shadow=False, nthreads=0, counters=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        geom = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        u = np.empty(n, np.float32)
+        v = np.empty(n, np.float32)
+        w = np.empty(n, np.float32)
+        cnt = np.empty((n, 3), np.uint32) if counters else None
+        st = lib().orc_trace_scene(self.h, _ptr(rays), n, int(bool(shadow)), int(nthreads),
+                                   _ptr(prim), _ptr(geom), _ptr(t), _ptr(u), _ptr(v), _ptr(w),
+                                   _ptr(cnt))
+        out = dict(prim=prim, geom=geom, t=t, u=u, v=v, w=w, status=st)
+        if counters:
+            out["counters"] = cnt
+        return out
+
+
+def vdc(i, scramble=0):
+    return lib().orc_vdc(i, scramble)
+
+
+def sobol(i, scramble=0):
+    return lib().orc_sobol(i, scramble)
+
+
+def raster_xy(m, frame, px, py, sx=0, sy=0):
+    rx = ctypes.c_double()
+    ry = ctypes.c_double()
+    idx = lib().orc_raster_xy(m, frame, px, py, sx, sy, ctypes.byref(rx), ctypes.byref(ry))
+    return idx, rx.value, ry.value
+
+
+def vdc_sobol_tables(m):
+    f = np.zeros(52, np.uint64)
+    v = np.zeros(52, np.uint64)
+    lib().orc_vdc_sobol_tables(m, _ptr(f), _ptr(v))
+    return f, v

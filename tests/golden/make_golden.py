@@ -1,0 +1,106 @@
+"""Regenerate the golden fixtures under tests/golden/.
+
+Run from the repository root:  python tests/golden/make_golden.py [REFERENCE_DIR]
+
+1. vdc_sobol_tables.npz - the two Grunschloss enumeration tables exactly as
+   the reference holds them (math/ldseq/vdc_sobol_matrices52.go), parsed from
+   the reference source.  Needs the reference checkout (default: the
+   VERMEER_REFERENCE environment variable); skipped when it is absent.
+2. traversal_small.npz - small triangle soups, rays with awkward directions
+   (axis-parallel, zero components, through vertices and edges, finite
+   tmax) and the oracle's closest-hit and any-hit answers.  This pins the
+   oracle itself, so a rebuild on another machine (x86_64 or aarch64) must
+   reproduce it bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def parse_tables(ref_dir: str):
+    src = open(os.path.join(ref_dir, "math", "ldseq", "vdc_sobol_matrices52.go")).read()
+
+    def parse(name):
+        i = src.index("var " + name)
+        j = src.index("\n}\n", i)
+        out = np.zeros((27, 52), np.uint64)
+        for m, body in re.findall(r"\{ // m = (\d+)\n(.*?)\n\t\}", src[i:j], re.S):
+            vals = [int(x, 16) for x in re.findall(r"0x[0-9a-fA-F]+", body)]
+            out[int(m), :len(vals)] = vals
+        return out
+
+    return parse("vdcSobolMatrices"), parse("vdcSobolMatricesInv")
+
+
+def edge_rays(verts: np.ndarray, seed: int, n_random: int) -> np.ndarray:
+    """Rays aimed at vertices and edge midpoints of the soup, rays with zero
+    direction components, and random rays with finite tmax."""
+    from vermeer_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    tri = verts.reshape(-1, 3, 3)
+    rays = []
+    # through vertices and edge midpoints, from random origins
+    for k in range(min(200, tri.shape[0])):
+        for tgt in (tri[k, 0], tri[k, 1], 0.5 * (tri[k, 0] + tri[k, 2])):
+            o = rng.uniform(-0.5, 1.5, 3).astype(np.float32)
+            d = (tgt.astype(np.float64) - o)
+            d /= np.linalg.norm(d)
+            rays.append([*o, *d, np.inf, 0.0])
+    # axis-parallel rays (two zero direction components) from vertex-aligned origins
+    for k in range(min(100, tri.shape[0])):
+        v = tri[k, 0]
+        for axis in range(3):
+            for s in (1.0, -1.0):
+                o = v.copy()
+                o[axis] = -0.5 if s > 0 else 1.5
+                d = np.zeros(3)
+                d[axis] = s
+                rays.append([*o, *d, np.inf, 0.0])
+    # one zero component, origin on a vertex plane
+    for k in range(min(100, tri.shape[0])):
+        v = tri[k, 1]
+        o = np.array([v[0], rng.uniform(-0.5, 1.5), rng.uniform(-0.5, 1.5)], np.float32)
+        d = np.array([0.0, rng.normal(), rng.normal()])
+        d /= np.linalg.norm(d)
+        rays.append([*o, *d, np.inf, 0.0])
+    rnd = scenes.incoherent_rays(n_random, seed)
+    rnd[:, 6] = rng.uniform(0.0, 0.3, n_random).astype(np.float32)  # finite tmax
+    out = np.concatenate([np.asarray(rays, np.float32), rnd], axis=0)
+    return out
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VERMEER_REFERENCE", "")
+    if ref and os.path.isdir(ref):
+        fwd, inv = parse_tables(ref)
+        np.savez_compressed(os.path.join(HERE, "vdc_sobol_tables.npz"), fwd=fwd, inv=inv)
+        print("wrote vdc_sobol_tables.npz")
+    else:
+        print("reference checkout not given: keeping vdc_sobol_tables.npz")
+
+    from oracle import orc
+    from vermeer_gb300 import scenes
+    cases = {}
+    for name, n, seed, edge in (("soup64", 64, 11, 0.2), ("soup2k", 2000, 12, 0.05), ("soup8k", 8000, 13, 0.02)):
+        v, ip = scenes.triangle_soup(n, seed, edge=edge)
+        rays = edge_rays(v, seed, 3000)
+        m = orc.Mesh(v, ip)
+        ch = m.trace(rays)
+        an = m.trace(rays, shadow=True)
+        cases[name] = dict(verts=v, idxp=ip, rays=rays, **{f"ch_{k}": ch[k] for k in ("prim", "t", "u", "v", "w")},
+                           **{f"any_{k}": an[k] for k in ("prim", "t", "u", "v", "w")})
+    flat = {f"{c}__{k}": a for c, d in cases.items() for k, a in d.items()}
+    np.savez_compressed(os.path.join(HERE, "traversal_small.npz"), **flat)
+    print("wrote traversal_small.npz", {c: d["rays"].shape[0] for c, d in cases.items()})
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,66 @@
+"""The C-ABI library loads and exports every function include/vmr.h declares;
+host-only contexts report errors with the documented status codes."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"^\s*(?:int|const char\s*\*|void)\s+(vmr_\w+)\s*\(", src, re.M))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    from vermeer_gb300 import _lib
+    L = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), f"libvmr does not export {n}"
+    assert L.vmr_abi_version() == 1
+
+
+def test_binding_covers_header():
+    from vermeer_gb300 import _lib
+    assert set(declared_functions()) <= set(_lib.exported_symbols()) | set(_lib.extra_symbols())
+
+
+def test_host_only_context_refuses_trace(host_ctx):
+    import vermeer_gb300 as vg
+    from vermeer_gb300 import scenes
+    v, ip = scenes.triangle_soup(50, 1)
+    g = host_ctx.mesh_build(v, ip)
+    with pytest.raises(vg.VmrError) as e:
+        host_ctx.trace_mesh(g, scenes.incoherent_rays(10, 1))
+    assert e.value.code == -7
+
+
+def test_upload_validates_reference_nodes(host_ctx, orc):
+    """vmr_mesh_upload accepts the oracle-built (reference-layout) tree and
+    rejects out-of-range leaf ranges."""
+    import vermeer_gb300 as vg
+    from vermeer_gb300 import scenes
+    v, ip = scenes.triangle_soup(300, 2)
+    ex = orc.Mesh(v, ip).export()
+    host_ctx.mesh_upload(v, ex["idxp"], ex["accel_idx"], nodes=ex["nodes"], bounds=ex["bounds"])
+    bad = ex["accel_idx"].copy()
+    bad[0] = 300
+    with pytest.raises(vg.VmrError):
+        host_ctx.mesh_upload(v, ex["idxp"], bad, nodes=ex["nodes"], bounds=ex["bounds"])
+
+
+def test_null_context_is_rejected():
+    from vermeer_gb300 import _lib
+    L = _lib.load()
+    assert L.vmr_destroy(None) == -1
+    assert L.vmr_sync(None) == -1

@@ -1,0 +1,138 @@
+"""Bit-exact parity of the CUDA traversal (through the C ABI) with the CPU
+oracle: closest-hit and any-hit, static, motion (faithful and fixed) and
+two-level scenes, host and device buffers, golden fixtures and the full
+1M-triangle / 4M-ray workload."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import assert_hits_equal
+from vermeer_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_golden_fixture_static(ctx):
+    g = np.load(os.path.join(GOLDEN, "traversal_small.npz"))
+    for case in ("soup64", "soup2k", "soup8k"):
+        geom = ctx.mesh_build(g[f"{case}__verts"], g[f"{case}__idxp"])
+        rays = g[f"{case}__rays"]
+        for mode, shadow in (("ch", False), ("any", True)):
+            got = ctx.trace_mesh(geom, rays, shadow=shadow)
+            ref = {k: g[f"{case}__{mode}_{k}"] for k in ("prim", "t", "u", "v", "w")}
+            assert_hits_equal(got, ref, what=f"{case}/{mode}")
+
+
+@pytest.mark.parametrize("n,seed,edge", [(1, 1, 0.3), (17, 2, 0.2), (5000, 3, 0.02), (100000, 4, 0.005)])
+def test_static_parity_incoherent(ctx, orc, n, seed, edge):
+    v, ip = scenes.triangle_soup(n, seed, edge=edge)
+    rays = scenes.incoherent_rays(200000, seed + 50)
+    geom = ctx.mesh_build(v, ip)
+    om = orc.Mesh(v, ip)
+    for shadow in (False, True):
+        assert_hits_equal(ctx.trace_mesh(geom, rays, shadow=shadow), om.trace(rays, shadow=shadow),
+                          what=f"n={n} shadow={shadow}")
+
+
+def test_static_parity_coherent_and_finite_tmax(ctx, orc):
+    v, ip = scenes.triangle_soup(200000, 8)
+    geom = ctx.mesh_build(v, ip)
+    om = orc.Mesh(v, ip)
+    rays = scenes.coherent_rays(384)
+    assert_hits_equal(ctx.trace_mesh(geom, rays), om.trace(rays), what="coherent")
+    rays = scenes.incoherent_rays(100000, 9)
+    rays[:, 6] = np.random.default_rng(0).uniform(0, 0.05, rays.shape[0]).astype(np.float32)
+    for shadow in (False, True):
+        assert_hits_equal(ctx.trace_mesh(geom, rays, shadow=shadow), om.trace(rays, shadow=shadow),
+                          what=f"finite tmax shadow={shadow}")
+
+
+def test_uploaded_reference_tree_equals_built(ctx, orc):
+    """A reference-built tree uploaded through vmr_mesh_upload traces the
+    same as the tree libvmr builds itself."""
+    v, ip = scenes.triangle_soup(30000, 10)
+    ex = orc.Mesh(v, ip).export()
+    g_up = ctx.mesh_upload(v, ex["idxp"], ex["accel_idx"], nodes=ex["nodes"], bounds=ex["bounds"])
+    g_b = ctx.mesh_build(v, ip)
+    rays = scenes.incoherent_rays(50000, 11)
+    assert_hits_equal(ctx.trace_mesh(g_up, rays), ctx.trace_mesh(g_b, rays), what="upload vs build")
+
+
+def test_device_buffers_equal_host_buffers(ctx):
+    import torch
+    v, ip = scenes.triangle_soup(50000, 12)
+    geom = ctx.mesh_build(v, ip)
+    rays = scenes.incoherent_rays(100000, 13)
+    host = ctx.trace_mesh(geom, rays)
+    dev_rays = torch.from_numpy(np.ascontiguousarray(rays.T)).cuda()
+    dev = ctx.trace_mesh(geom, dev_rays)
+    ctx.sync()
+    got = {k: dev[k].cpu().numpy() for k in ("prim", "t", "u", "v", "w")}
+    assert_hits_equal(got, host, what="device vs host")
+
+
+def test_counters_match_oracle_visit_counts(ctx, orc):
+    """The visit counters report the reference's NodesT / LeafsT totals
+    (the GPU skips only pops the reference culls)."""
+    v, ip = scenes.triangle_soup(20000, 14)
+    geom = ctx.mesh_build(v, ip)
+    rays = scenes.incoherent_rays(20000, 15)
+    got = ctx.trace_mesh(geom, rays, counters=True)["stats"]
+    ref = orc.Mesh(v, ip).trace(rays, counters=True)["counters"].astype(np.uint64).sum(axis=0)
+    assert got["node_visits"] == ref[0] and got["leaf_visits"] == ref[1] and got["tri_tests"] == ref[2]
+
+
+@pytest.mark.parametrize("fixed", [False, True])
+@pytest.mark.parametrize("n,seed", [(12, 1), (3000, 2), (60000, 3)])
+def test_motion_parity(ctx, orc, n, seed, fixed):
+    v, ip = scenes.motion_soup(n, seed, edge=0.01)
+    rays = scenes.incoherent_rays(100000, seed + 7)
+    rays[:, 7] = scenes.uniform(seed, rays.shape[0], 77).astype(np.float32)
+    rays[:3, 7] = [0.0, 1.0, 0.5]
+    mode = 1 if fixed else 0
+    geom = ctx.mesh_build(v, ip, keys=2, motion_mode=mode)
+    om = orc.Mesh(v, ip, keys=2, motion_fixed=fixed)
+    for shadow in (False, True):
+        assert_hits_equal(ctx.trace_mesh(geom, rays, shadow=shadow), om.trace(rays, shadow=shadow),
+                          what=f"motion fixed={fixed} shadow={shadow}")
+
+
+@pytest.mark.parametrize("motion_every", [0, 2])
+def test_two_level_scene_parity(ctx, orc, motion_every):
+    rng = np.random.default_rng(5 + motion_every)
+    ms = []
+    for i in range(24):
+        n = int(rng.integers(1, 5000))
+        if motion_every and i % motion_every == 0:
+            v, ip = scenes.motion_soup(n, 500 + i, edge=0.01)
+            k = 2
+        else:
+            v, ip = scenes.triangle_soup(n, 500 + i, edge=0.01)
+            k = 1
+        off = rng.uniform(-1, 1, 3).astype(np.float32)
+        ms.append(((v * 0.5 + off).astype(np.float32), ip, k))
+    oms = [orc.Mesh(v, ip, keys=k, motion_fixed=True) for v, ip, k in ms]
+    osc = orc.Scene(oms)
+    ids = [ctx.mesh_build(v, ip, keys=k, motion_mode=1) for v, ip, k in ms]
+    ctx.scene_build(ids)
+    rays = scenes.incoherent_rays(100000, 60, lo=-1.5, hi=1.5)
+    rays[:, 7] = scenes.uniform(61, rays.shape[0], 3).astype(np.float32)
+    for shadow in (False, True):
+        got = ctx.trace_scene(rays, shadow=shadow)
+        ref = osc.trace(rays, shadow=shadow)
+        ref["geom"] = np.where(ref["geom"] >= 0, np.asarray(ids, np.int32)[np.maximum(ref["geom"], 0)], -1)
+        assert_hits_equal(got, ref, keys=("prim", "geom", "t", "u", "v", "w"), what=f"scene shadow={shadow}")
+
+
+def test_full_size_soup_parity(ctx, orc):
+    """The benchmark workload: 1,048,576-triangle soup, 4M incoherent rays,
+    every hit compared with the oracle (multithreaded on the host)."""
+    v, ip = scenes.triangle_soup(1 << 20, 2)
+    geom = ctx.mesh_build(v, ip)
+    rays = scenes.incoherent_rays(1 << 22, 2)
+    om = orc.Mesh(v, ip)
+    assert_hits_equal(ctx.trace_mesh(geom, rays), om.trace(rays), what="1M soup closest")
+    sub = rays[: 1 << 20]
+    assert_hits_equal(ctx.trace_mesh(geom, sub, shadow=True), om.trace(sub, shadow=True), what="1M soup any")

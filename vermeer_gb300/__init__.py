@@ -1,0 +1,11 @@
+"""vermeer_gb300 - GB300-native (sm_103a) traversal and rendering path for
+Vermeer scenes.
+
+The compute path is libvmr (hand-written CUDA behind the C ABI in
+include/vmr.h).  This package builds and binds it; there is no CPU fallback:
+every entry point raises if the library or a CUDA device is missing.
+"""
+from .api import (MOTION_FAITHFUL, MOTION_FIXED, MNODE_DTYPE, NODE_DTYPE, Context, VmrError)  # noqa: F401
+from . import scenes  # noqa: F401
+
+__all__ = ["Context", "VmrError", "NODE_DTYPE", "MNODE_DTYPE", "MOTION_FAITHFUL", "MOTION_FIXED", "scenes"]

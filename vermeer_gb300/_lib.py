@@ -1,0 +1,102 @@
+"""ctypes declarations of libvmr's C ABI (include/vmr.h)."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+P = ctypes.c_void_p
+U32 = ctypes.c_uint32
+I32 = ctypes.c_int32
+
+
+class QbvhNode(ctypes.Structure):
+    """qbvh.Node (qbvh/qbvh.go:31-36)."""
+    _fields_ = [("boxes", ctypes.c_float * 24), ("axis0", U32), ("axis1", U32), ("axis2", U32),
+                ("children", I32 * 4), ("parent", I32)]
+
+
+class MqbvhNode(ctypes.Structure):
+    """qbvh.MotionNode (qbvh/mqbvh.go:24-29)."""
+    _fields_ = [("axis0", I32), ("axis1", I32), ("axis2", I32), ("children", I32 * 4), ("parent", I32),
+                ("pad", U32 * 2)]
+
+
+class MeshInput(ctypes.Structure):
+    _fields_ = [("verts", P), ("n_verts", U32), ("motion_keys", U32), ("idxp", P), ("n_tris", U32),
+                ("ray_bias", ctypes.c_float), ("motion_mode", ctypes.c_int), ("shader_idx", P)]
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("verts", P), ("n_verts", U32), ("motion_keys", U32), ("idxp", P), ("n_tris", U32),
+                ("accel_idx", P), ("ray_bias", ctypes.c_float), ("motion_mode", ctypes.c_int),
+                ("nodes", P), ("n_nodes", U32), ("mnodes", P), ("n_mnodes", U32), ("mboxes", P),
+                ("bounds", P), ("shader_idx", P)]
+
+
+class Rays(ctypes.Structure):
+    _fields_ = [(n, P) for n in ("px", "py", "pz", "dx", "dy", "dz", "tmax", "time")]
+
+
+class Hits(ctypes.Structure):
+    _fields_ = [(n, P) for n in ("prim", "geom", "t", "u", "v", "w")]
+
+
+class TraceStats(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_uint64), ("node_visits", ctypes.c_uint64), ("leaf_visits", ctypes.c_uint64),
+                ("tri_tests", ctypes.c_uint64), ("kernel_ms", ctypes.c_float)]
+
+
+assert ctypes.sizeof(QbvhNode) == 128 and ctypes.sizeof(MqbvhNode) == 40
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vmr_abi_version": (ctypes.c_int, []),
+    "vmr_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(P)]),
+    "vmr_destroy": (ctypes.c_int, [P]),
+    "vmr_last_error": (ctypes.c_char_p, [P]),
+    "vmr_set_stream": (ctypes.c_int, [P, P]),
+    "vmr_sync": (ctypes.c_int, [P]),
+    "vmr_mesh_build": (ctypes.c_int, [P, ctypes.POINTER(MeshInput), ctypes.POINTER(U32)]),
+    "vmr_mesh_upload": (ctypes.c_int, [P, ctypes.POINTER(MeshDesc), ctypes.POINTER(U32)]),
+    "vmr_mesh_info": (ctypes.c_int, [P, U32, P, P, P, P]),
+    "vmr_mesh_export": (ctypes.c_int, [P, U32, P, P, P, P, P, P]),
+    "vmr_scene_build": (ctypes.c_int, [P, P, U32]),
+    "vmr_scene_upload": (ctypes.c_int, [P, P, U32, P, U32, P, U32, P, U32]),
+    "vmr_scene_export": (ctypes.c_int, [P, P, P, P, P, P, P, P]),
+    "vmr_trace_mesh": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
+                                      ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
+    "vmr_trace_scene": (ctypes.c_int, [P, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
+                                       ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
+}
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libvmr.  Raises if it cannot be built or loaded: there is no
+    fallback implementation."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"libvmr not built ({path}); run vermeer_gb300.build.build()")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(SIGNATURES)
+
+
+def extra_symbols():
+    """Declared functions bound by other modules of the package."""
+    return []

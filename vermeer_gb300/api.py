@@ -1,0 +1,185 @@
+"""Host-side interface over libvmr's C ABI.
+
+Mirrors the reference's traversal boundary: a PolyMesh is built
+(PolyMesh.PreRender -> initAccel, builtin/geom/polymesh/buildqbvh.go:14-144)
+or uploaded with a reference-built QBVH, a Scene gets its top level
+(Scene.PreRender -> initAccel, builtin/scene/scene.go:131-203), and rays are
+traced closest-hit or as shadow rays (qbvh.Trace, qbvh/intersect.go:91;
+Scene.Trace, scene.go:30).  Errors raise VmrError carrying the vmr_status.
+
+Ray batches are float32 arrays of shape [n, 8] (px py pz dx dy dz tmax time)
+in host memory, or CUDA tensors of shape [8, n] (one row per field, already
+in HBM) for the device path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+STATUS = {0: "VMR_OK", -1: "VMR_ERR_INVALID", -2: "VMR_ERR_CUDA", -3: "VMR_ERR_OOM", -4: "VMR_ERR_TIMEOUT",
+          -5: "VMR_ERR_STACK_OVERFLOW", -6: "VMR_ERR_QUEUE_OVERFLOW", -7: "VMR_ERR_UNSUPPORTED"}
+TRACE_ANY_HIT, TRACE_DEVICE, TRACE_COUNT = 1, 2, 4
+MOTION_FAITHFUL, MOTION_FIXED = 0, 1
+
+NODE_DTYPE = np.dtype([("boxes", "<f4", (24,)), ("axis", "<u4", (3,)), ("children", "<i4", (4,)),
+                       ("parent", "<i4")])
+MNODE_DTYPE = np.dtype([("axis", "<i4", (3,)), ("children", "<i4", (4,)), ("parent", "<i4"),
+                        ("pad", "<u4", (2,))])
+
+
+class VmrError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _p(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(ctypes.c_void_p)
+    return ctypes.c_void_p(a.data_ptr())  # torch tensor
+
+
+class Context:
+    """One libvmr context on one GPU (vmr_create)."""
+
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.L.vmr_create(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise VmrError(rc, "vmr_create failed (no usable CUDA device?)")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.vmr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise VmrError(rc, self.L.vmr_last_error(self.h).decode(errors="replace"))
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.L.vmr_set_stream(self.h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+
+    def sync(self):
+        self._check(self.L.vmr_sync(self.h))
+
+    # ------------------------------------------------------------ meshes
+    def mesh_build(self, verts, idxp, keys: int = 1, ray_bias: float = 0.0, motion_mode: int = MOTION_FAITHFUL,
+                   shader_idx=None) -> int:
+        verts = np.ascontiguousarray(verts, np.float32)
+        idxp = np.ascontiguousarray(idxp, np.uint32)
+        sidx = None if shader_idx is None else np.ascontiguousarray(shader_idx, np.uint8)
+        mi = _lib.MeshInput(_p(verts), verts.size // (3 * keys), keys, _p(idxp), idxp.size // 3,
+                            float(ray_bias), int(motion_mode), _p(sidx))
+        g = ctypes.c_uint32()
+        self._check(self.L.vmr_mesh_build(self.h, ctypes.byref(mi), ctypes.byref(g)))
+        return g.value
+
+    def mesh_upload(self, verts, idxp, accel_idx, nodes=None, mnodes=None, mboxes=None, bounds=None, keys: int = 1,
+                    ray_bias: float = 0.0, motion_mode: int = MOTION_FAITHFUL) -> int:
+        verts = np.ascontiguousarray(verts, np.float32)
+        idxp = np.ascontiguousarray(idxp, np.uint32)
+        accel_idx = np.ascontiguousarray(accel_idx, np.int32)
+        nodes = None if nodes is None else np.ascontiguousarray(nodes, NODE_DTYPE)
+        mnodes = None if mnodes is None else np.ascontiguousarray(mnodes, MNODE_DTYPE)
+        mboxes = None if mboxes is None else np.ascontiguousarray(mboxes, np.float32)
+        bounds = None if bounds is None else np.ascontiguousarray(bounds, np.float32)
+        d = _lib.MeshDesc(_p(verts), verts.size // (3 * keys), keys, _p(idxp), idxp.size // 3, _p(accel_idx),
+                          float(ray_bias), int(motion_mode), _p(nodes), 0 if nodes is None else len(nodes),
+                          _p(mnodes), 0 if mnodes is None else len(mnodes), _p(mboxes), _p(bounds), None)
+        g = ctypes.c_uint32()
+        self._check(self.L.vmr_mesh_upload(self.h, ctypes.byref(d), ctypes.byref(g)))
+        return g.value
+
+    def mesh_info(self, geom: int):
+        a, b, c, d = (ctypes.c_uint32() for _ in range(4))
+        self._check(self.L.vmr_mesh_info(self.h, geom, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                         ctypes.byref(d)))
+        return dict(n_nodes=a.value, n_mnodes=b.value, n_tris=c.value, keys=d.value)
+
+    def mesh_export(self, geom: int):
+        i = self.mesh_info(geom)
+        nodes = np.zeros(i["n_nodes"], NODE_DTYPE)
+        mnodes = np.zeros(i["n_mnodes"], MNODE_DTYPE)
+        mboxes = np.zeros((i["keys"] if i["n_mnodes"] else 0, i["n_mnodes"], 24), np.float32)
+        accel_idx = np.zeros(i["n_tris"], np.int32)
+        idxp = np.zeros(i["n_tris"] * 3, np.uint32)
+        bounds = np.zeros(6 * i["keys"], np.float32)
+        self._check(self.L.vmr_mesh_export(self.h, geom, _p(nodes), _p(accel_idx), _p(idxp), _p(mnodes),
+                                           _p(mboxes), _p(bounds)))
+        return dict(nodes=nodes, accel_idx=accel_idx, idxp=idxp, mnodes=mnodes, mboxes=mboxes, bounds=bounds)
+
+    # ------------------------------------------------------------- scene
+    def scene_build(self, geoms):
+        g = np.ascontiguousarray(geoms, np.uint32)
+        self._check(self.L.vmr_scene_build(self.h, _p(g), g.size))
+
+    def scene_upload(self, geom_order, nodes=None, mnodes=None, mboxes=None, keys: int = 1):
+        order = np.ascontiguousarray(geom_order, np.uint32)
+        nodes = None if nodes is None else np.ascontiguousarray(nodes, NODE_DTYPE)
+        mnodes = None if mnodes is None else np.ascontiguousarray(mnodes, MNODE_DTYPE)
+        mboxes = None if mboxes is None else np.ascontiguousarray(mboxes, np.float32)
+        self._check(self.L.vmr_scene_upload(self.h, _p(nodes), 0 if nodes is None else len(nodes), _p(mnodes),
+                                            0 if mnodes is None else len(mnodes), _p(mboxes), keys, _p(order),
+                                            order.size))
+
+    def scene_export(self, n_geoms: int):
+        nn, nm, k = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.L.vmr_scene_export(self.h, None, None, None, None, ctypes.byref(nn), ctypes.byref(nm),
+                                            ctypes.byref(k)))
+        order = np.zeros(n_geoms, np.uint32)
+        nodes = np.zeros(nn.value, NODE_DTYPE)
+        mnodes = np.zeros(nm.value, MNODE_DTYPE)
+        mboxes = np.zeros((k.value if nm.value else 0, nm.value, 24), np.float32)
+        self._check(self.L.vmr_scene_export(self.h, _p(order), _p(nodes), _p(mnodes), _p(mboxes), None, None, None))
+        return dict(geom_order=order, nodes=nodes, mnodes=mnodes, mboxes=mboxes, keys=k.value)
+
+    # ------------------------------------------------------------- trace
+    def _trace(self, geom, rays, shadow, counters, outputs):
+        flags = (TRACE_ANY_HIT if shadow else 0) | (TRACE_COUNT if counters else 0)
+        st = _lib.TraceStats()
+        if isinstance(rays, np.ndarray):
+            rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+            n = rays.shape[0]
+            soa = np.ascontiguousarray(rays.T)
+            r = _lib.Rays(*[_p(soa[k]) for k in range(8)])
+            out = {k: np.empty(n, np.int32 if k in ("prim", "geom") else np.float32) for k in outputs}
+            h = _lib.Hits(*[_p(out.get(k)) for k in ("prim", "geom", "t", "u", "v", "w")])
+        else:  # CUDA tensor [8, n], rows already in HBM
+            import torch
+            assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[0] == 8 and rays.is_contiguous()
+            n = rays.shape[1]
+            r = _lib.Rays(*[ctypes.c_void_p(rays[k].data_ptr()) for k in range(8)])
+            out = {k: torch.empty(n, dtype=torch.int32 if k in ("prim", "geom") else torch.float32,
+                                  device=rays.device) for k in outputs}
+            h = _lib.Hits(*[_p(out.get(k)) for k in ("prim", "geom", "t", "u", "v", "w")])
+            flags |= TRACE_DEVICE
+        if geom is None:
+            rc = self.L.vmr_trace_scene(self.h, ctypes.byref(r), n, flags, ctypes.byref(h), ctypes.byref(st))
+        else:
+            rc = self.L.vmr_trace_mesh(self.h, geom, ctypes.byref(r), n, flags, ctypes.byref(h), ctypes.byref(st))
+        self._check(rc)
+        out["stats"] = dict(rays=st.rays, node_visits=st.node_visits, leaf_visits=st.leaf_visits,
+                            tri_tests=st.tri_tests, kernel_ms=st.kernel_ms)
+        return out
+
+    def trace_mesh(self, geom: int, rays, shadow: bool = False, counters: bool = False,
+                   outputs=("prim", "t", "u", "v", "w")):
+        """PolyMesh.Trace over one mesh: closest hit, or any hit for shadow rays."""
+        return self._trace(geom, rays, shadow, counters, outputs)
+
+    def trace_scene(self, rays, shadow: bool = False, counters: bool = False,
+                    outputs=("prim", "geom", "t", "u", "v", "w")):
+        """Scene.Trace over the two-level scene."""
+        return self._trace(None, rays, shadow, counters, outputs)

@@ -1,0 +1,100 @@
+"""Compile libvmr (vermeer_gb300/_build/libvmr.so) for sm_103a.
+
+Host C++ sources are compiled with g++ -ffp-contract=off (the accelerator
+builder must round exactly as the reference does); CUDA sources with nvcc for
+sm_103a only.  Translation units compile in parallel; the CUDA runtime is
+linked statically so the library has no runtime search-path needs.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libvmr.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+             "-Wno-unused-function"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr"] + ARCH
+
+
+def _cuda_home() -> str:
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    return os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def sources():
+    cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return cpp, cu
+
+
+def _digest() -> str:
+    h = hashlib.sha256()
+    for d in (CSRC, INCLUDE):
+        for f in sorted(os.listdir(d)):
+            p = os.path.join(d, f)
+            if os.path.isfile(p):
+                h.update(f.encode())
+                with open(p, "rb") as fh:
+                    h.update(fh.read())
+    h.update(" ".join(CXX_FLAGS + NVCC_FLAGS).encode())
+    return h.hexdigest()
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Build libvmr if its sources changed; returns the library path."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    stamp = os.path.join(OUT_DIR, "libvmr.sha256")
+    dig = _digest()
+    if not force and os.path.exists(LIB) and os.path.exists(stamp):
+        with open(stamp) as fh:
+            if fh.read().strip() == dig:
+                return LIB
+    cuda = _cuda_home()
+    inc = ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(cuda, "include")]
+    cpp, cu = sources()
+    jobs = []
+    objs = []
+    for f in cpp:
+        o = os.path.join(OUT_DIR, f + ".o")
+        objs.append(o)
+        jobs.append(["g++"] + CXX_FLAGS + inc + ["-c", os.path.join(CSRC, f), "-o", o])
+    for f in cu:
+        o = os.path.join(OUT_DIR, f + ".o")
+        objs.append(o)
+        jobs.append(["nvcc"] + NVCC_FLAGS + inc + ["-c", os.path.join(CSRC, f), "-o", o])
+    procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for j in jobs]
+    failed = []
+    for j, p in procs:
+        out, _ = p.communicate()
+        if verbose or p.returncode != 0:
+            sys.stderr.write(out.decode(errors="replace"))
+        if p.returncode != 0:
+            failed.append(" ".join(j))
+    if failed:
+        raise RuntimeError("libvmr build failed:\n" + "\n".join(failed))
+    tmp = LIB + ".tmp"
+    link = ["nvcc", "-shared"] + ARCH + ["-cudart", "static", "-o", tmp] + objs + ["-lpthread"]
+    r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("libvmr link failed:\n" + r.stdout.decode(errors="replace"))
+    os.replace(tmp, LIB)
+    with open(stamp, "w") as fh:
+        fh.write(dig)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

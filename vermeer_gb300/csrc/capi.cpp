@@ -1,0 +1,559 @@
+// capi.cpp - the C ABI of libvmr (include/vmr.h).
+//
+// Host side of the traversal path: contexts, mesh and scene upload (the
+// reference's 128-byte qbvh.Node repacked into the device GNode layout),
+// batched traces with host or device buffers, and status reporting.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "accel.h"
+#include "device.h"
+#include "vmr.h"
+
+using vmr::DMesh;
+using vmr::DScratch;
+using vmr::DTop;
+using vmr::GNode;
+using vmr::HostMesh;
+using vmr::HostTop;
+using vmr::MNode;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct MeshRec {
+  HostMesh host;
+  DevBuf nodes, tris, mnodes, mboxes, mtris, elem;
+  DMesh dmesh{};
+};
+
+struct TopRec {
+  HostTop host;
+  DevBuf nodes, mnodes, mboxes, order, meshes;
+  DTop dtop{};
+  bool valid = false;
+};
+
+}  // namespace
+
+struct vmr_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  DevBuf scratch;                 // DScratch
+  DevBuf io;                      // rays + hits for host-pointer traces
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<std::unique_ptr<MeshRec>> meshes;
+  TopRec top;
+};
+
+namespace {
+
+int fail(vmr_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_fail(vmr_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? VMR_ERR_OOM : VMR_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define VMR_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);  \
+  } while (0)
+
+template <class T>
+cudaError_t upload(vmr_ctx* ctx, DevBuf& buf, const std::vector<T>& v) {
+  if (v.empty()) return cudaSuccess;
+  cudaError_t e = buf.ensure(v.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+}
+
+// Reference leaf code -> device leaf code (see device.h).
+bool repack_child(int32_t c, uint32_t n_inner, uint32_t n_elems, int32_t& out) {
+  if (c >= 0) {
+    if ((uint32_t)c >= n_inner) return false;
+    out = c;
+    return true;
+  }
+  if (c == -1) { out = vmr::kEmptyChild; return true; }
+  uint32_t first = ((uint32_t)c & 0x7ffffffu) >> 4;  // LeafBase (qbvh/qbvh.go:64)
+  uint32_t count = ((uint32_t)c & 0xfu) + 1u;         // LeafCount (qbvh.go:61)
+  if ((uint64_t)first + count > n_elems) return false;
+  out = (int32_t)(0x80000000u | (first << 4) | (count - 1u));
+  return true;
+}
+
+uint32_t pack_axes(uint32_t a0, uint32_t a1, uint32_t a2) { return (a0 & 3u) | ((a1 & 3u) << 2) | ((a2 & 3u) << 4); }
+
+bool repack_nodes(const std::vector<vmr_qbvh_node>& in, uint32_t n_elems, std::vector<GNode>& out) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); ++i) {
+    GNode g;
+    std::memset(&g, 0, sizeof(g));
+    std::memcpy(g.box, in[i].boxes, sizeof(g.box));
+    for (int c = 0; c < 4; ++c)
+      if (!repack_child(in[i].children[c], (uint32_t)in.size(), n_elems, g.child[c])) return false;
+    if (in[i].axis0 > 2 || in[i].axis1 > 2 || in[i].axis2 > 2) return false;
+    g.axes = pack_axes(in[i].axis0, in[i].axis1, in[i].axis2);
+    out[i] = g;
+  }
+  return true;
+}
+
+bool repack_mnodes(const std::vector<vmr_mqbvh_node>& in, uint32_t n_elems, std::vector<MNode>& out) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); ++i) {
+    MNode g;
+    std::memset(&g, 0, sizeof(g));
+    for (int c = 0; c < 4; ++c)
+      if (!repack_child(in[i].children[c], (uint32_t)in.size(), n_elems, g.child[c])) return false;
+    if ((uint32_t)in[i].axis0 > 2 || (uint32_t)in[i].axis1 > 2 || (uint32_t)in[i].axis2 > 2) return false;
+    g.axes = pack_axes((uint32_t)in[i].axis0, (uint32_t)in[i].axis1, (uint32_t)in[i].axis2);
+    out[i] = g;
+  }
+  return true;
+}
+
+struct F4 { float x, y, z, w; };
+
+// Host accelerator -> device arrays (layout in device.h).
+int upload_mesh(vmr_ctx* ctx, MeshRec& rec) {
+  HostMesh& m = rec.host;
+  if (ctx->device < 0) return VMR_OK;
+  DMesh d{};
+  d.n_tris = m.n_tris;
+  d.keys = m.motion() ? m.keys : 1u;
+  d.lower_static = 1.19209290e-07f + m.ray_bias;  // EpsilonFloat32 + RayBias
+  d.ray_bias = m.ray_bias;
+  if (!m.motion()) {
+    std::vector<GNode> g;
+    if (!repack_nodes(m.nodes, m.n_tris, g)) return fail(ctx, VMR_ERR_INVALID, "malformed QBVH nodes");
+    std::vector<F4> tris((size_t)m.n_tris * 3);
+    for (size_t i = 0; i < (size_t)m.n_tris * 3; ++i) {
+      const float* v = &m.verts[(size_t)m.idxp[i] * 3];
+      tris[i] = F4{v[0], v[1], v[2], 0.0f};
+    }
+    VMR_CUDA(ctx, upload(ctx, rec.nodes, g));
+    VMR_CUDA(ctx, upload(ctx, rec.tris, tris));
+    d.nodes = rec.nodes.as<GNode>();
+    d.tris = rec.tris.p;
+  } else {
+    std::vector<MNode> g;
+    if (!repack_mnodes(m.mnodes, m.n_tris, g)) return fail(ctx, VMR_ERR_INVALID, "malformed motion QBVH nodes");
+    const bool fixed = m.motion_mode == VMR_MOTION_FIXED;
+    std::vector<F4> tris((size_t)m.keys * m.n_tris * 3);
+    std::vector<int32_t> elem(m.n_tris);
+    for (uint32_t i = 0; i < m.n_tris; ++i) {
+      // Faithful: idxp read at the leaf position (trace.go:532-537).
+      // Fixed: the face the leaf boxes were built from.
+      const uint32_t face = fixed ? (uint32_t)m.accel_idx[i] : i;
+      elem[i] = (int32_t)face;
+      for (uint32_t key = 0; key < m.keys; ++key)
+        for (int j = 0; j < 3; ++j) {
+          const float* v = &m.verts[((size_t)key * m.n_verts + m.idxp[(size_t)face * 3 + j]) * 3];
+          tris[((size_t)key * m.n_tris + i) * 3 + j] = F4{v[0], v[1], v[2], 0.0f};
+        }
+    }
+    VMR_CUDA(ctx, upload(ctx, rec.mnodes, g));
+    VMR_CUDA(ctx, upload(ctx, rec.mboxes, m.mboxes));
+    VMR_CUDA(ctx, upload(ctx, rec.mtris, tris));
+    VMR_CUDA(ctx, upload(ctx, rec.elem, elem));
+    d.mnodes = rec.mnodes.as<MNode>();
+    d.mboxes = rec.mboxes.p;
+    d.mtris = rec.mtris.p;
+    d.elem = rec.elem.as<int32_t>();
+    d.n_mnodes = (uint32_t)m.mnodes.size();
+  }
+  VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  rec.dmesh = d;
+  return VMR_OK;
+}
+
+bool valid_mesh_input(const vmr_mesh_input* in, std::string& why) {
+  if (!in || in->motion_keys < 1) { why = "motion_keys must be >= 1"; return false; }
+  if (in->n_tris > 0 && (!in->verts || !in->idxp)) { why = "null verts or idxp"; return false; }
+  if (in->n_tris >= (1u << 23)) { why = "a mesh holds at most 2^23-1 triangles (qbvh.LeafBase)"; return false; }
+  for (size_t i = 0; i < (size_t)in->n_tris * 3; ++i)
+    if (in->idxp[i] >= in->n_verts) { why = "vertex index out of range"; return false; }
+  return true;
+}
+
+int refresh_top(vmr_ctx* ctx) {
+  TopRec& t = ctx->top;
+  if (ctx->device < 0) return VMR_OK;
+  // Device mesh table indexed by geom id.
+  std::vector<DMesh> table(ctx->meshes.size());
+  for (size_t i = 0; i < ctx->meshes.size(); ++i) table[i] = ctx->meshes[i]->dmesh;
+  VMR_CUDA(ctx, upload(ctx, t.meshes, table));
+  DTop d{};
+  if (t.host.keys <= 1) {
+    std::vector<GNode> g;
+    if (!repack_nodes(t.host.nodes, (uint32_t)t.host.geom_order.size(), g))
+      return fail(ctx, VMR_ERR_INVALID, "malformed top-level nodes");
+    VMR_CUDA(ctx, upload(ctx, t.nodes, g));
+    d.nodes = t.nodes.as<GNode>();
+    d.keys = 1;
+  } else {
+    std::vector<MNode> g;
+    if (!repack_mnodes(t.host.mnodes, (uint32_t)t.host.geom_order.size(), g))
+      return fail(ctx, VMR_ERR_INVALID, "malformed top-level motion nodes");
+    VMR_CUDA(ctx, upload(ctx, t.mnodes, g));
+    VMR_CUDA(ctx, upload(ctx, t.mboxes, t.host.mboxes));
+    d.mnodes = t.mnodes.as<MNode>();
+    d.mboxes = t.mboxes.p;
+    d.keys = t.host.keys;
+    d.n_mnodes = (uint32_t)t.host.mnodes.size();
+  }
+  VMR_CUDA(ctx, upload(ctx, t.order, t.host.geom_order));
+  VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  d.geom_order = t.order.as<uint32_t>();
+  d.meshes = t.meshes.as<DMesh>();
+  d.n_geoms = (uint32_t)t.host.geom_order.size();
+  t.dtop = d;
+  t.valid = !t.host.geom_order.empty();
+  return VMR_OK;
+}
+
+int read_status(vmr_ctx* ctx, vmr_trace_stats* stats) {
+  DScratch s;
+  VMR_CUDA(ctx, cudaMemcpyAsync(&s, ctx->scratch.p, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
+  VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (stats) {
+    stats->node_visits = s.node_visits;
+    stats->leaf_visits = s.leaf_visits;
+    stats->tri_tests = s.tri_tests;
+  }
+  if (s.status == vmr::kStatusStackOverflow)
+    return fail(ctx, VMR_ERR_STACK_OVERFLOW, "a ray needed more than 90 traversal stack entries");
+  if (s.status == vmr::kStatusIterationCap)
+    return fail(ctx, VMR_ERR_TIMEOUT, "a traversal loop hit its iteration cap");
+  return VMR_OK;
+}
+
+// One traversal launch: rays/hits are device pointers here.
+int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int flags, const vmr_hits& h,
+              vmr_trace_stats* stats) {
+  vmr::TraceLaunch l{};
+  l.rays = vmr::RaySoA{r.px, r.py, r.pz, r.dx, r.dy, r.dz, r.tmax, r.time};
+  l.hits = vmr::HitSoA{h.prim, h.geom, h.t, h.u, h.v, h.w};
+  l.n = n;
+  l.any_hit = (flags & VMR_TRACE_ANY_HIT) ? 1 : 0;
+  l.count = (flags & VMR_TRACE_COUNT) ? 1 : 0;
+  l.scratch = ctx->scratch.as<DScratch>();
+  l.stream = ctx->stream;
+  VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
+  VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  int e = mesh ? vmr::launch_trace_mesh(*mesh, l) : vmr::launch_trace_scene(ctx->top.dtop, l);
+  if (e != 0) return cuda_fail(ctx, (cudaError_t)e, "trace kernel launch");
+  VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  if (stats) stats->rays = n;
+  if (flags & VMR_TRACE_DEVICE) return VMR_OK;
+  int st = read_status(ctx, stats);
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    stats->kernel_ms = ms;
+  }
+  return st;
+}
+
+// Host-pointer trace: stage rays in, run, copy hits out.
+int trace_host(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays* rays, size_t n, int flags, const vmr_hits* hits,
+               vmr_trace_stats* stats) {
+  const size_t fb = n * sizeof(float);
+  const int n_in = rays->time ? 8 : 7;
+  const size_t bytes = fb * (size_t)n_in + fb * 6;
+  VMR_CUDA(ctx, ctx->io.ensure(bytes == 0 ? 16 : bytes));
+  char* base = ctx->io.as<char>();
+  const float* src[8] = {rays->px, rays->py, rays->pz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->time};
+  float* dst[8];
+  for (int k = 0; k < n_in; ++k) {
+    dst[k] = reinterpret_cast<float*>(base + fb * k);
+    if (!src[k]) return fail(ctx, VMR_ERR_INVALID, "null ray array");
+    if (n) VMR_CUDA(ctx, cudaMemcpyAsync(dst[k], src[k], fb, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  vmr_rays dr{dst[0], dst[1], dst[2], dst[3], dst[4], dst[5], dst[6], n_in == 8 ? dst[7] : nullptr};
+  char* hb = base + fb * n_in;
+  vmr_hits dh{hits->prim ? reinterpret_cast<int32_t*>(hb) : nullptr,
+              hits->geom ? reinterpret_cast<int32_t*>(hb + fb) : nullptr,
+              hits->t ? reinterpret_cast<float*>(hb + 2 * fb) : nullptr,
+              hits->u ? reinterpret_cast<float*>(hb + 3 * fb) : nullptr,
+              hits->v ? reinterpret_cast<float*>(hb + 4 * fb) : nullptr,
+              hits->w ? reinterpret_cast<float*>(hb + 5 * fb) : nullptr};
+  int st = run_trace(ctx, mesh, dr, n, flags & ~VMR_TRACE_DEVICE, dh, stats);
+  void* outs[6] = {hits->prim, hits->geom, hits->t, hits->u, hits->v, hits->w};
+  void* douts[6] = {dh.prim, dh.geom, dh.t, dh.u, dh.v, dh.w};
+  for (int k = 0; k < 6; ++k)
+    if (outs[k] && n) VMR_CUDA(ctx, cudaMemcpyAsync(outs[k], douts[k], fb, cudaMemcpyDeviceToHost, ctx->stream));
+  VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vmr_abi_version(void) { return VMR_ABI_VERSION; }
+
+int vmr_create(int device, vmr_ctx** out) {
+  if (!out) return VMR_ERR_INVALID;
+  *out = nullptr;
+  if (device < 0) {  // host-only: builds accelerators, cannot trace
+    auto* ctx = new vmr_ctx();
+    ctx->device = -1;
+    *out = ctx;
+    return VMR_OK;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return VMR_ERR_CUDA;
+  if (device < 0 || device >= ndev) return VMR_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return VMR_ERR_CUDA;
+  auto* ctx = new vmr_ctx();
+  ctx->device = device;
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+      ctx->scratch.ensure(sizeof(DScratch)) != cudaSuccess) {
+    delete ctx;
+    return VMR_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  *out = ctx;
+  return VMR_OK;
+}
+
+int vmr_destroy(vmr_ctx* ctx) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (ctx->device < 0) { delete ctx; return VMR_OK; }
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  cudaStream_t s = ctx->own_stream;
+  delete ctx;
+  if (s) cudaStreamDestroy(s);
+  return VMR_OK;
+}
+
+const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int vmr_set_stream(vmr_ctx* ctx, void* s) {
+  if (!ctx) return VMR_ERR_INVALID;
+  ctx->stream = s ? (cudaStream_t)s : ctx->own_stream;
+  return VMR_OK;
+}
+
+int vmr_sync(vmr_ctx* ctx) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (ctx->device < 0) return VMR_OK;
+  cudaSetDevice(ctx->device);
+  return read_status(ctx, nullptr);
+}
+
+int vmr_mesh_build(vmr_ctx* ctx, const vmr_mesh_input* in, uint32_t* out_geom) {
+  if (!ctx) return VMR_ERR_INVALID;
+  std::string why;
+  if (!valid_mesh_input(in, why)) return fail(ctx, VMR_ERR_INVALID, why);
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  auto rec = std::make_unique<MeshRec>();
+  HostMesh& m = rec->host;
+  m.n_verts = in->n_verts;
+  m.keys = in->motion_keys;
+  m.n_tris = in->n_tris;
+  m.verts.assign(in->verts, in->verts + (size_t)in->n_verts * in->motion_keys * 3);
+  m.idxp.assign(in->idxp, in->idxp + (size_t)in->n_tris * 3);
+  m.ray_bias = in->ray_bias;
+  m.motion_mode = in->motion_mode;
+  if (in->shader_idx) m.shader_idx.assign(in->shader_idx, in->shader_idx + in->n_tris);
+  if (!vmr::build_mesh_accel(m, why)) return fail(ctx, VMR_ERR_INVALID, why);
+  int st = upload_mesh(ctx, *rec);
+  if (st != VMR_OK) return st;
+  if (out_geom) *out_geom = (uint32_t)ctx->meshes.size();
+  ctx->meshes.push_back(std::move(rec));
+  return VMR_OK;
+}
+
+int vmr_mesh_upload(vmr_ctx* ctx, const vmr_mesh_desc* d, uint32_t* out_geom) {
+  if (!ctx || !d) return VMR_ERR_INVALID;
+  if (d->motion_keys < 1 || (d->n_tris && (!d->verts || !d->idxp || !d->accel_idx)))
+    return fail(ctx, VMR_ERR_INVALID, "incomplete mesh description");
+  if (d->n_tris >= (1u << 23)) return fail(ctx, VMR_ERR_INVALID, "a mesh holds at most 2^23-1 triangles");
+  for (size_t i = 0; i < (size_t)d->n_tris * 3; ++i)
+    if (d->idxp[i] >= d->n_verts) return fail(ctx, VMR_ERR_INVALID, "vertex index out of range");
+  for (size_t i = 0; i < d->n_tris; ++i)
+    if (d->accel_idx[i] < 0 || (uint32_t)d->accel_idx[i] >= d->n_tris)
+      return fail(ctx, VMR_ERR_INVALID, "accel_idx out of range");
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  auto rec = std::make_unique<MeshRec>();
+  HostMesh& m = rec->host;
+  m.n_verts = d->n_verts;
+  m.keys = d->motion_keys;
+  m.n_tris = d->n_tris;
+  m.verts.assign(d->verts, d->verts + (size_t)d->n_verts * d->motion_keys * 3);
+  m.idxp.assign(d->idxp, d->idxp + (size_t)d->n_tris * 3);
+  m.accel_idx.assign(d->accel_idx, d->accel_idx + d->n_tris);
+  m.ray_bias = d->ray_bias;
+  m.motion_mode = d->motion_mode;
+  if (d->shader_idx) m.shader_idx.assign(d->shader_idx, d->shader_idx + d->n_tris);
+  if (m.motion()) {
+    if (!d->mnodes || !d->mboxes || !d->bounds || d->n_mnodes == 0)
+      return fail(ctx, VMR_ERR_INVALID, "motion mesh needs mnodes, mboxes and per-key bounds");
+    m.mnodes.assign(d->mnodes, d->mnodes + d->n_mnodes);
+    m.mboxes.assign(d->mboxes, d->mboxes + (size_t)d->motion_keys * d->n_mnodes * 24);
+    m.key_bounds.resize(d->motion_keys);
+    vmr::Bounds full{{__builtin_huge_valf(), __builtin_huge_valf(), __builtin_huge_valf()},
+                     {-__builtin_huge_valf(), -__builtin_huge_valf(), -__builtin_huge_valf()}};
+    for (uint32_t k = 0; k < d->motion_keys; ++k) {
+      for (int a = 0; a < 3; ++a) {
+        m.key_bounds[k].lo[a] = d->bounds[6 * k + a];
+        m.key_bounds[k].hi[a] = d->bounds[6 * k + 3 + a];
+        full.lo[a] = full.lo[a] < m.key_bounds[k].lo[a] ? full.lo[a] : m.key_bounds[k].lo[a];
+        full.hi[a] = full.hi[a] > m.key_bounds[k].hi[a] ? full.hi[a] : m.key_bounds[k].hi[a];
+      }
+    }
+    m.bounds = full;
+  } else {
+    if ((!d->nodes && d->n_tris) || !d->bounds) return fail(ctx, VMR_ERR_INVALID, "static mesh needs nodes and bounds");
+    if (d->nodes) m.nodes.assign(d->nodes, d->nodes + d->n_nodes);
+    for (int a = 0; a < 3; ++a) { m.bounds.lo[a] = d->bounds[a]; m.bounds.hi[a] = d->bounds[3 + a]; }
+  }
+  int st = upload_mesh(ctx, *rec);
+  if (st != VMR_OK) return st;
+  if (out_geom) *out_geom = (uint32_t)ctx->meshes.size();
+  ctx->meshes.push_back(std::move(rec));
+  return VMR_OK;
+}
+
+int vmr_mesh_info(vmr_ctx* ctx, uint32_t geom, uint32_t* n_nodes, uint32_t* n_mnodes, uint32_t* n_tris,
+                  uint32_t* motion_keys) {
+  if (!ctx || geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+  const HostMesh& m = ctx->meshes[geom]->host;
+  if (n_nodes) *n_nodes = (uint32_t)m.nodes.size();
+  if (n_mnodes) *n_mnodes = (uint32_t)m.mnodes.size();
+  if (n_tris) *n_tris = m.n_tris;
+  if (motion_keys) *motion_keys = m.keys;
+  return VMR_OK;
+}
+
+int vmr_mesh_export(vmr_ctx* ctx, uint32_t geom, vmr_qbvh_node* nodes, int32_t* accel_idx, uint32_t* idxp,
+                    vmr_mqbvh_node* mnodes, float* mboxes, float* bounds) {
+  if (!ctx || geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+  const HostMesh& m = ctx->meshes[geom]->host;
+  if (nodes && !m.nodes.empty()) std::memcpy(nodes, m.nodes.data(), m.nodes.size() * sizeof(vmr_qbvh_node));
+  if (accel_idx && !m.accel_idx.empty()) std::memcpy(accel_idx, m.accel_idx.data(), m.accel_idx.size() * 4);
+  if (idxp && !m.idxp.empty()) std::memcpy(idxp, m.idxp.data(), m.idxp.size() * 4);
+  if (mnodes && !m.mnodes.empty()) std::memcpy(mnodes, m.mnodes.data(), m.mnodes.size() * sizeof(vmr_mqbvh_node));
+  if (mboxes && !m.mboxes.empty()) std::memcpy(mboxes, m.mboxes.data(), m.mboxes.size() * 4);
+  if (bounds) {
+    if (m.motion()) {
+      for (size_t k = 0; k < m.key_bounds.size(); ++k)
+        for (int a = 0; a < 3; ++a) { bounds[6 * k + a] = m.key_bounds[k].lo[a]; bounds[6 * k + 3 + a] = m.key_bounds[k].hi[a]; }
+    } else {
+      for (int a = 0; a < 3; ++a) { bounds[a] = m.bounds.lo[a]; bounds[3 + a] = m.bounds.hi[a]; }
+    }
+  }
+  return VMR_OK;
+}
+
+int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n) {
+  if (!ctx || (n && !geoms)) return VMR_ERR_INVALID;
+  std::vector<const HostMesh*> ms(n);
+  std::vector<uint32_t> ids(geoms, geoms + n);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (geoms[i] >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+    ms[i] = &ctx->meshes[geoms[i]]->host;
+  }
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  std::string why;
+  HostTop top;
+  if (!vmr::build_top_level(ms, ids, top, why)) return fail(ctx, VMR_ERR_INVALID, why);
+  ctx->top.host = std::move(top);
+  return refresh_top(ctx);
+}
+
+int vmr_scene_upload(vmr_ctx* ctx, const vmr_qbvh_node* nodes, uint32_t n_nodes, const vmr_mqbvh_node* mnodes,
+                     uint32_t n_mnodes, const float* mboxes, uint32_t keys, const uint32_t* order, uint32_t n_geoms) {
+  if (!ctx || !order || keys < 1) return VMR_ERR_INVALID;
+  for (uint32_t i = 0; i < n_geoms; ++i)
+    if (order[i] >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id in order");
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  HostTop top;
+  top.keys = keys;
+  top.geom_order.assign(order, order + n_geoms);
+  if (keys == 1) {
+    if (!nodes) return fail(ctx, VMR_ERR_INVALID, "static top level needs nodes");
+    top.nodes.assign(nodes, nodes + n_nodes);
+  } else {
+    if (!mnodes || !mboxes) return fail(ctx, VMR_ERR_INVALID, "motion top level needs mnodes and mboxes");
+    top.mnodes.assign(mnodes, mnodes + n_mnodes);
+    top.mboxes.assign(mboxes, mboxes + (size_t)keys * n_mnodes * 24);
+  }
+  ctx->top.host = std::move(top);
+  return refresh_top(ctx);
+}
+
+int vmr_scene_export(vmr_ctx* ctx, uint32_t* order, vmr_qbvh_node* nodes, vmr_mqbvh_node* mnodes, float* mboxes,
+                     uint32_t* n_nodes, uint32_t* n_mnodes, uint32_t* keys) {
+  if (!ctx) return VMR_ERR_INVALID;
+  const HostTop& t = ctx->top.host;
+  if (order && !t.geom_order.empty()) std::memcpy(order, t.geom_order.data(), t.geom_order.size() * 4);
+  if (nodes && !t.nodes.empty()) std::memcpy(nodes, t.nodes.data(), t.nodes.size() * sizeof(vmr_qbvh_node));
+  if (mnodes && !t.mnodes.empty()) std::memcpy(mnodes, t.mnodes.data(), t.mnodes.size() * sizeof(vmr_mqbvh_node));
+  if (mboxes && !t.mboxes.empty()) std::memcpy(mboxes, t.mboxes.data(), t.mboxes.size() * 4);
+  if (n_nodes) *n_nodes = (uint32_t)t.nodes.size();
+  if (n_mnodes) *n_mnodes = (uint32_t)t.mnodes.size();
+  if (keys) *keys = t.keys;
+  return VMR_OK;
+}
+
+int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags, const vmr_hits* hits,
+                   vmr_trace_stats* stats) {
+  if (ctx && ctx->device < 0) return fail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (!ctx || !rays || !hits) return VMR_ERR_INVALID;
+  if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+  cudaSetDevice(ctx->device);
+  const DMesh* m = &ctx->meshes[geom]->dmesh;
+  if (ctx->meshes[geom]->host.n_tris == 0) return fail(ctx, VMR_ERR_INVALID, "empty mesh");
+  if (flags & VMR_TRACE_DEVICE) return run_trace(ctx, m, *rays, n, flags, *hits, stats);
+  return trace_host(ctx, m, rays, n, flags, hits, stats);
+}
+
+int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags, const vmr_hits* hits,
+                    vmr_trace_stats* stats) {
+  if (ctx && ctx->device < 0) return fail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (!ctx || !rays || !hits) return VMR_ERR_INVALID;
+  if (!ctx->top.valid) return fail(ctx, VMR_ERR_INVALID, "no scene: call vmr_scene_build first");
+  cudaSetDevice(ctx->device);
+  if (flags & VMR_TRACE_DEVICE) return run_trace(ctx, nullptr, *rays, n, flags, *hits, stats);
+  return trace_host(ctx, nullptr, rays, n, flags, hits, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+// device.h - device-side data layout of libvmr (shared by host and kernels).
+//
+// HBM layout of one mesh (all arrays 128-byte aligned, resident for the
+// lifetime of the context):
+//   static mesh
+//     GNode   nodes[n_nodes]       128 B: the 24 child-box floats of qbvh.Node
+//                                  as 6 float4 (minx,miny,minz,maxx,maxy,maxz
+//                                  over the 4 children), children as int4,
+//                                  split axes packed in one word
+//     float4  tris[3*n_tris]       leaf order: v0,v1,v2 (w unused), 48 B per
+//                                  triangle, so a leaf is one contiguous run
+//   motion mesh
+//     MNode   mnodes[n_mnodes]     32 B: children int4 + packed axes
+//     float4  mboxes[keys][n][6]   96 B per node per key
+//     float4  mtris[keys][3*n]     leaf-position order, per key
+//     int32   elem[n]              leaf position -> reported ElemID
+#pragma once
+#include <cstdint>
+
+#ifndef __CUDACC__
+struct float4_host { float x, y, z, w; };
+#endif
+
+namespace vmr {
+
+// Leaf code in GNode/MNode children: bit 31 set, bits 4..30 first element,
+// bits 0..3 count-1.  -1 is an empty child.  The reference packs the first
+// element into 23 bits (LeafBase, qbvh/qbvh.go:64); the device format keeps
+// 27, the upload path checks that reference trees decode unchanged.
+constexpr int32_t kEmptyChild = -1;
+
+struct alignas(128) GNode {
+  float box[24];        // box[c + 4*axis] = min, box[12 + c + 4*axis] = max
+  int32_t child[4];
+  uint32_t axes;        // axis0 | axis1<<2 | axis2<<4
+  uint32_t pad[3];
+};
+static_assert(sizeof(GNode) == 128, "GNode must be 128 bytes");
+
+struct alignas(32) MNode {
+  int32_t child[4];
+  uint32_t axes;
+  uint32_t pad[3];
+};
+static_assert(sizeof(MNode) == 32, "MNode must be 32 bytes");
+
+// One mesh as the kernels see it.
+struct DMesh {
+  const GNode* nodes;       // static
+  const void* tris;         // float4[3*n_tris] (static)
+  const MNode* mnodes;      // motion
+  const void* mboxes;       // float4[keys][n_mnodes][6]
+  const void* mtris;        // float4[keys][3*n_tris]
+  const int32_t* elem;      // motion: leaf position -> ElemID
+  uint32_t n_tris;
+  uint32_t n_mnodes;
+  uint32_t keys;            // 1 = static
+  float lower_static;       // EpsilonFloat32 + RayBias (trace.go:182)
+  float ray_bias;           // motion lower bound (trace.go:612)
+  uint32_t pad[3];
+};
+
+// Top level of a scene (builtin/scene): static GNodes or motion MNodes with
+// boxes; leaves index geom_order (leaf position -> geom id).
+struct DTop {
+  const GNode* nodes;
+  const MNode* mnodes;
+  const void* mboxes;
+  const uint32_t* geom_order;
+  const DMesh* meshes;      // indexed by geom id
+  uint32_t keys;
+  uint32_t n_mnodes;
+  uint32_t n_geoms;
+  uint32_t pad;
+};
+
+struct RaySoA {
+  const float *px, *py, *pz, *dx, *dy, *dz, *tmax, *time;
+};
+struct HitSoA {
+  int32_t* prim;
+  int32_t* geom;
+  float *t, *u, *v, *w;
+};
+
+// Device scratch of one context: the persistent kernels' work counter, the
+// status word and the visit counters (reset before every launch).
+struct DScratch {
+  unsigned long long next_ray;
+  int status;
+  int pad;
+  unsigned long long node_visits;
+  unsigned long long leaf_visits;
+  unsigned long long tri_tests;
+};
+
+enum DeviceStatus : int {
+  kStatusOk = 0,
+  kStatusStackOverflow = 1,
+  kStatusIterationCap = 2,
+};
+
+constexpr int kStackCapacity = 90;  // RenderTask.Traversal.Stack (core/ray.go:158)
+
+// Launch entry points (traverse.cu).
+struct TraceLaunch {
+  RaySoA rays;
+  HitSoA hits;
+  uint64_t n;
+  int any_hit;
+  int count;
+  DScratch* scratch;
+  int grid;
+  int block;
+  void* stream;
+};
+int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);
+int launch_trace_scene(const DTop& top, const TraceLaunch& l);
+int device_sm_count();
+
+}  // namespace vmr

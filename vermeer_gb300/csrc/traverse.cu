@@ -1,0 +1,629 @@
+// traverse.cu - QBVH traversal and watertight ray/triangle kernels (sm_103a).
+//
+// Bit-exactness contract: for the same QBVH and rays, the hit element id, t
+// and barycentrics equal those of the reference's qbvh.Trace +
+// PolyMesh.TraceElems (qbvh/intersect.go:91-246, qbvh/intersect_amd64.s,
+// builtin/geom/polymesh/trace.go:108-194), motion traversal
+// (qbvh/motionintersect.go:22-127, trace.go:520-719) and the two-level scene
+// (builtin/scene/scene.go:30-97).  To get there:
+//   * every float operation of the box and triangle tests is an explicit
+//     round-to-nearest intrinsic (__fadd_rn/__fsub_rn/__fmul_rn never fuse
+//     into FMA), in the reference's operation order;
+//   * divisions are IEEE (__fdiv_rn/__frcp_rn), which equal the reference's
+//     float32(float64(a)/float64(b));
+//   * the FP64 edge fallback is kept (__dmul_rn/__dsub_rn/__double2float_rn);
+//   * children are visited in the reference's order, pops are culled with
+//     the reference's test (Tclosest < T), leaves are scanned in order.
+// The traversal may skip work the reference does without effect: children
+// that would be culled when popped are never pushed, and the child popped
+// next stays in registers instead of a stack round trip.
+//
+// Execution model: persistent warps (grid = SMs x resident blocks) pull
+// 32-ray batches from a global counter with one atomic per warp; each lane
+// owns one ray and a private stack in local memory (L1-resident, interleaved
+// per lane by the hardware so same-depth accesses coalesce).
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace vmr {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kIterationCap = 1 << 24;
+
+__device__ __forceinline__ float pick3(float x, float y, float z, int k) {
+  return k == 0 ? x : (k == 1 ? y : z);
+}
+
+// Traversal inputs of core.Ray after Ray.Setup (core/ray.go:103-148).
+struct TRay {
+  float ox, oy, oz;
+  float dx, dy, dz;
+  float ix, iy, iz;     // Dinv
+  float tclosest;       // Tclosest
+  float s0, s1, s2;     // S
+  float pkx, pky, pkz;  // P[Kx], P[Ky], P[Kz]
+  int kx, ky, kz;
+  unsigned oct;         // bit k set when D[k] < 0
+  bool exact;           // a NaN can arise in the slab test
+  float time;
+};
+
+__device__ __forceinline__ void ray_setup(TRay& r) {
+  float ax = fabsf(r.dx), ay = fabsf(r.dy), az = fabsf(r.dz);
+  int kz = 0;
+  if (ay > az) {
+    if (ay > ax) kz = 1;
+  } else {
+    if (az > ax) kz = 2;
+  }
+  int kx = kz + 1;
+  if (kx == 3) kx = 0;
+  int ky = kx + 1;
+  if (ky == 3) ky = 0;
+  float dkz = pick3(r.dx, r.dy, r.dz, kz);
+  if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
+  r.kx = kx; r.ky = ky; r.kz = kz;
+  r.s2 = __frcp_rn(dkz);
+  r.s0 = __fdiv_rn(pick3(r.dx, r.dy, r.dz, kx), dkz);
+  r.s1 = __fdiv_rn(pick3(r.dx, r.dy, r.dz, ky), dkz);
+  r.ix = __frcp_rn(r.dx);
+  r.iy = __frcp_rn(r.dy);
+  r.iz = __frcp_rn(r.dz);
+  r.pkx = pick3(r.ox, r.oy, r.oz, kx);
+  r.pky = pick3(r.ox, r.oy, r.oz, ky);
+  r.pkz = pick3(r.ox, r.oy, r.oz, kz);
+  r.oct = (r.dx < 0.0f ? 1u : 0u) | (r.dy < 0.0f ? 2u : 0u) | (r.dz < 0.0f ? 4u : 0u);
+  // (b - o) * Dinv can only be NaN when Dinv is infinite or zero or an
+  // input is not finite; otherwise the ternary min/max of the reference
+  // and fminf/fmaxf agree (up to the sign of zero, which no comparison sees).
+  r.exact = !(isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz) && r.ix != 0.0f && r.iy != 0.0f &&
+              r.iz != 0.0f && isfinite(r.ox) && isfinite(r.oy) && isfinite(r.oz));
+}
+
+// Slab test of the 4 children against boxes b[6] (intersect_amd64.s).
+// Returns the 4-bit hit mask, tNear per child in tn[].
+template <bool EXACT>
+__device__ __forceinline__ unsigned box4(const TRay& r, const float4 (&b)[6], float (&tn)[4]) {
+  unsigned mask = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float bminx = (&b[0].x)[c], bminy = (&b[1].x)[c], bminz = (&b[2].x)[c];
+    const float bmaxx = (&b[3].x)[c], bmaxy = (&b[4].x)[c], bmaxz = (&b[5].x)[c];
+    float x1 = __fmul_rn(__fsub_rn(bminx, r.ox), r.ix);
+    float x2 = __fmul_rn(__fsub_rn(bmaxx, r.ox), r.ix);
+    float y1 = __fmul_rn(__fsub_rn(bminy, r.oy), r.iy);
+    float y2 = __fmul_rn(__fsub_rn(bmaxy, r.oy), r.iy);
+    float z1 = __fmul_rn(__fsub_rn(bminz, r.oz), r.iz);
+    float z2 = __fmul_rn(__fsub_rn(bmaxz, r.oz), r.iz);
+    float lo, hi;
+    if (EXACT) {
+      // MINPS/MAXPS operand order: the second source wins unless the first
+      // compares strictly smaller/larger, so a NaN propagates as the SSE
+      // code does.
+      lo = x2 < x1 ? x2 : x1;
+      hi = x2 > x1 ? x2 : x1;
+      float ylo = y2 < y1 ? y2 : y1, yhi = y2 > y1 ? y2 : y1;
+      lo = lo > ylo ? lo : ylo;
+      hi = hi < yhi ? hi : yhi;
+      float zlo = z2 < z1 ? z2 : z1, zhi = z2 > z1 ? z2 : z1;
+      lo = lo > zlo ? lo : zlo;
+      hi = hi < zhi ? hi : zhi;
+      float t = 0.0f > lo ? 0.0f : lo;
+      tn[c] = t;
+      if (t <= hi) mask |= 1u << c;
+    } else {
+      lo = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fminf(z1, z2));
+      hi = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fmaxf(z1, z2));
+      float t = fmaxf(0.0f, lo);
+      tn[c] = t;
+      if (t <= hi) mask |= 1u << c;
+    }
+  }
+  return mask;
+}
+
+// Result of the accepted triangle (ShaderContext fields the trace fills).
+struct HitRec {
+  int32_t elem;
+  int32_t geom;
+  float u, v, w;
+};
+
+// The watertight test (trace.go:123-193).  STRICT: static idxp path
+// (xT < lower*xdet); otherwise the motion path (xT <= lower*xdet).
+template <bool STRICT>
+__device__ __forceinline__ bool tri_test(TRay& r, float4 v0, float4 v1, float4 v2, float lower, float& U,
+                                         float& V, float& W) {
+  const float AKz = __fsub_rn(pick3(v0.x, v0.y, v0.z, r.kz), r.pkz);
+  const float BKz = __fsub_rn(pick3(v1.x, v1.y, v1.z, r.kz), r.pkz);
+  const float CKz = __fsub_rn(pick3(v2.x, v2.y, v2.z, r.kz), r.pkz);
+  const float Cx = __fsub_rn(__fsub_rn(pick3(v2.x, v2.y, v2.z, r.kx), r.pkx), __fmul_rn(r.s0, CKz));
+  const float By = __fsub_rn(__fsub_rn(pick3(v1.x, v1.y, v1.z, r.ky), r.pky), __fmul_rn(r.s1, BKz));
+  const float Cy = __fsub_rn(__fsub_rn(pick3(v2.x, v2.y, v2.z, r.ky), r.pky), __fmul_rn(r.s1, CKz));
+  const float Bx = __fsub_rn(__fsub_rn(pick3(v1.x, v1.y, v1.z, r.kx), r.pkx), __fmul_rn(r.s0, BKz));
+  const float Ax = __fsub_rn(__fsub_rn(pick3(v0.x, v0.y, v0.z, r.kx), r.pkx), __fmul_rn(r.s0, AKz));
+  const float Ay = __fsub_rn(__fsub_rn(pick3(v0.x, v0.y, v0.z, r.ky), r.pky), __fmul_rn(r.s1, AKz));
+  float fU = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+  float fV = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+  float fW = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+  if (fU == 0.0f || fV == 0.0f || fW == 0.0f) {
+    // FP64 fallback (trace.go:142-155): exact products, one rounding in the
+    // double subtraction, one in the conversion.
+    fU = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
+    fV = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
+    fW = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
+  }
+  if ((fU < 0.0f || fV < 0.0f || fW < 0.0f) && (fU > 0.0f || fV > 0.0f || fW > 0.0f)) return false;
+  const float det = __fadd_rn(__fadd_rn(fU, fV), fW);
+  if (det == 0.0f) return false;
+  const float T = __fmul_rn(r.s2, __fadd_rn(__fadd_rn(__fmul_rn(fU, AKz), __fmul_rn(fV, BKz)), __fmul_rn(fW, CKz)));
+  const unsigned sgn = __float_as_uint(det) & 0x80000000u;
+  const float xT = __uint_as_float(__float_as_uint(T) ^ sgn);
+  const float xdet = __uint_as_float(__float_as_uint(det) ^ sgn);
+  const float lo = __fmul_rn(lower, xdet);
+  const bool below = STRICT ? (xT < lo) : (xT <= lo);
+  if (below || xT > __fmul_rn(r.tclosest, xdet)) return false;
+  const float rcp = __frcp_rn(det);
+  U = __fmul_rn(fU, rcp);
+  V = __fmul_rn(fV, rcp);
+  W = __fmul_rn(fW, rcp);
+  r.tclosest = __fmul_rn(T, rcp);
+  return true;
+}
+
+struct Counters {
+  uint32_t nodes, leafs, tris;
+};
+
+__device__ __forceinline__ void leaf_decode(int32_t c, uint32_t& first, uint32_t& count) {
+  first = ((uint32_t)c & 0x7fffffffu) >> 4;
+  count = ((uint32_t)c & 15u) + 1u;
+}
+
+// Push-order rank of each child (intersect.go:137-216): pairs (0,1) and
+// (2,3) each ordered by the sign of D along their split axis, the pair
+// order by the sign of D[Axis0].  Rank 0 is pushed first (popped last).
+__device__ __forceinline__ void child_ranks(unsigned axes, unsigned oct, unsigned (&rk)[4]) {
+  const unsigned s0 = (oct >> (axes & 3u)) & 1u;
+  const unsigned s1 = (oct >> ((axes >> 2) & 3u)) & 1u;
+  const unsigned s2 = (oct >> ((axes >> 4) & 3u)) & 1u;
+  rk[0] = 2u * (1u - s0) + (1u - s1);
+  rk[1] = 2u * (1u - s0) + s1;
+  rk[2] = 2u * s0 + (1u - s2);
+  rk[3] = 2u * s0 + s2;
+}
+
+// Push the hit children of a node in the reference order.  The child that
+// would be popped first is returned in (next, nextT) instead of being
+// stored.  Returns false when there is no child to visit.
+__device__ __forceinline__ bool push_children(int2* stk, int& sp, int cap, unsigned mask, const int4& ch,
+                                              const float (&tn)[4], unsigned axes, unsigned oct, int& next,
+                                              float& nextT, int& status) {
+  if (mask == 0) return false;
+  unsigned rk[4];
+  child_ranks(axes, oct, rk);
+  unsigned rmask = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    if (mask & (1u << c)) rmask |= 1u << rk[c];
+  const unsigned rtop = 31u - __clz(rmask);
+  const int npush = __popc(rmask) - 1;
+  if (sp + npush > cap) {
+    status = kStatusStackOverflow;
+    return false;
+  }
+  const int chv[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (mask & (1u << c)) {
+      if (rk[c] == rtop) {
+        next = chv[c];
+        nextT = tn[c];
+      } else {
+        const int slot = sp + __popc(rmask & ((1u << rk[c]) - 1u));
+        stk[slot] = make_int2(chv[c], __float_as_int(tn[c]));
+      }
+    }
+  }
+  sp += npush;
+  return true;
+}
+
+// qbvh.Trace over a static mesh (intersect.go:91-246) with
+// PolyMesh.TraceElems at the leaves.  Returns true if some leaf accepted a
+// triangle.  stk/cap: the free part of the ray's stack.
+template <bool ANY, bool COUNT>
+__device__ bool trace_static(const DMesh& m, TRay& r, int2* stk, int cap, HitRec& h, Counters& cnt,
+                             int& status) {
+  const float4* __restrict__ tris = reinterpret_cast<const float4*>(m.tris);
+  bool hit = false;
+  int sp = 0;
+  int node = 0;
+  float nodeT = r.tclosest;
+  for (int iter = 0;; ++iter) {
+    if (iter >= kIterationCap) { status = kStatusIterationCap; break; }
+    if (!(r.tclosest < nodeT) && node != kEmptyChild) {
+      if (node >= 0) {
+        if (COUNT) cnt.nodes++;
+        const float4* nb = reinterpret_cast<const float4*>(m.nodes + node);
+        float4 b[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) b[k] = __ldg(nb + k);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(nb + 6));
+        const unsigned axes = __ldg(reinterpret_cast<const unsigned*>(nb + 7));
+        float tn[4];
+        unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
+        // Children culled at pop time in the reference are dropped here.
+        if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
+        if (ch.y == kEmptyChild || r.tclosest < tn[1]) mask &= ~2u;
+        if (ch.z == kEmptyChild || r.tclosest < tn[2]) mask &= ~4u;
+        if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
+        int next;
+        float nextT;
+        if (push_children(stk, sp, cap, mask, ch, tn, axes, r.oct, next, nextT, status)) {
+          node = next;
+          nodeT = nextT;
+          continue;
+        }
+        if (status != kStatusOk) break;
+      } else {
+        uint32_t first, count;
+        leaf_decode(node, first, count);
+        if (COUNT) { cnt.leafs++; cnt.tris += count; }
+        int32_t idx = -1;
+        float U = 0.f, V = 0.f, W = 0.f;
+        for (uint32_t i = first; i < first + count; ++i) {
+          const float4 v0 = __ldg(tris + 3 * (size_t)i);
+          const float4 v1 = __ldg(tris + 3 * (size_t)i + 1);
+          const float4 v2 = __ldg(tris + 3 * (size_t)i + 2);
+          if (tri_test<true>(r, v0, v1, v2, m.lower_static, U, V, W)) idx = (int32_t)i;
+        }
+        if (idx != -1) {
+          h.elem = idx;
+          h.u = U; h.v = V; h.w = W;
+          hit = true;
+          if (ANY) break;
+        }
+      }
+    }
+    if (sp == 0) break;
+    --sp;
+    const int2 e = stk[sp];
+    node = e.x;
+    nodeT = __int_as_float(e.y);
+  }
+  return hit;
+}
+
+// qbvh.TraceMotion (motionintersect.go:22-127) with TraceMotionElems
+// (trace.go:520-719): per-key boxes and vertices lerped with the ray's time.
+template <bool ANY, bool COUNT>
+__device__ bool trace_motion(const DMesh& m, TRay& r, int2* stk, int cap, HitRec& h, Counters& cnt,
+                             int& status) {
+  // k = Time*float32(keys-1); time = k - Floor(k); key = Floor, key2 = Ceil
+  const float k = __fmul_rn(r.time, (float)(m.keys - 1));
+  const float fk = floorf(k);
+  const float tm = __fsub_rn(k, fk);
+  const int key = (int)fk, key2 = (int)ceilf(k);
+  if (key < 0 || key2 >= (int)m.keys) return false;  // the reference indexes out of range here
+  const float omt = __fsub_rn(1.0f, tm);
+  const float4* __restrict__ bx0 = reinterpret_cast<const float4*>(m.mboxes) + (size_t)key * m.n_mnodes * 6;
+  const float4* __restrict__ bx1 = reinterpret_cast<const float4*>(m.mboxes) + (size_t)key2 * m.n_mnodes * 6;
+  const float4* __restrict__ t0 = reinterpret_cast<const float4*>(m.mtris) + (size_t)key * m.n_tris * 3;
+  const float4* __restrict__ t1 = reinterpret_cast<const float4*>(m.mtris) + (size_t)key2 * m.n_tris * 3;
+  bool hit = false;
+  int sp = 0;
+  int node = 0;
+  float nodeT = r.tclosest;
+  for (int iter = 0;; ++iter) {
+    if (iter >= kIterationCap) { status = kStatusIterationCap; break; }
+    if (!(r.tclosest < nodeT) && node != kEmptyChild) {
+      if (node >= 0) {
+        if (COUNT) cnt.nodes++;
+        float4 b[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          const float4 a = __ldg(bx0 + (size_t)node * 6 + q);
+          const float4 c = __ldg(bx1 + (size_t)node * 6 + q);
+          // (1.0-time)*Boxes[key] + time*Boxes[key2] (motionintersect.go:47-49)
+          b[q].x = __fadd_rn(__fmul_rn(omt, a.x), __fmul_rn(tm, c.x));
+          b[q].y = __fadd_rn(__fmul_rn(omt, a.y), __fmul_rn(tm, c.y));
+          b[q].z = __fadd_rn(__fmul_rn(omt, a.z), __fmul_rn(tm, c.z));
+          b[q].w = __fadd_rn(__fmul_rn(omt, a.w), __fmul_rn(tm, c.w));
+        }
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(m.mnodes + node));
+        const unsigned axes = __ldg(reinterpret_cast<const unsigned*>(m.mnodes + node) + 4);
+        float tn[4];
+        unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
+        if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
+        if (ch.y == kEmptyChild || r.tclosest < tn[1]) mask &= ~2u;
+        if (ch.z == kEmptyChild || r.tclosest < tn[2]) mask &= ~4u;
+        if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
+        int next;
+        float nextT;
+        if (push_children(stk, sp, cap, mask, ch, tn, axes, r.oct, next, nextT, status)) {
+          node = next;
+          nodeT = nextT;
+          continue;
+        }
+        if (status != kStatusOk) break;
+      } else {
+        uint32_t first, count;
+        leaf_decode(node, first, count);
+        if (COUNT) { cnt.leafs++; cnt.tris += count; }
+        int32_t idx = -1;
+        float U = 0.f, V = 0.f, W = 0.f;
+        for (uint32_t i = first; i < first + count; ++i) {
+          float4 v[3];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const float4 a = __ldg(t0 + 3 * (size_t)i + j);
+            const float4 c = __ldg(t1 + 3 * (size_t)i + j);
+            // Vec3Lerp (math/vec3.go:52-58)
+            v[j].x = __fadd_rn(__fmul_rn(omt, a.x), __fmul_rn(tm, c.x));
+            v[j].y = __fadd_rn(__fmul_rn(omt, a.y), __fmul_rn(tm, c.y));
+            v[j].z = __fadd_rn(__fmul_rn(omt, a.z), __fmul_rn(tm, c.z));
+            v[j].w = 0.0f;
+          }
+          if (tri_test<false>(r, v[0], v[1], v[2], m.ray_bias, U, V, W)) idx = (int32_t)i;
+        }
+        if (idx != -1) {
+          h.elem = __ldg(m.elem + idx);
+          h.u = U; h.v = V; h.w = W;
+          hit = true;
+          if (ANY) break;
+        }
+      }
+    }
+    if (sp == 0) break;
+    --sp;
+    const int2 e = stk[sp];
+    node = e.x;
+    nodeT = __int_as_float(e.y);
+  }
+  return hit;
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trace_any_mesh(const DMesh& m, TRay& r, int2* stk, int cap, HitRec& h,
+                                               Counters& cnt, int& status) {
+  if (m.n_tris == 0) return false;
+  if (m.keys > 1) return trace_motion<ANY, COUNT>(m, r, stk, cap, h, cnt, status);
+  return trace_static<ANY, COUNT>(m, r, stk, cap, h, cnt, status);
+}
+
+__device__ __forceinline__ void load_ray(const RaySoA& rs, uint64_t i, TRay& r) {
+  r.ox = __ldg(rs.px + i); r.oy = __ldg(rs.py + i); r.oz = __ldg(rs.pz + i);
+  r.dx = __ldg(rs.dx + i); r.dy = __ldg(rs.dy + i); r.dz = __ldg(rs.dz + i);
+  r.tclosest = __ldg(rs.tmax + i);
+  r.time = rs.time ? __ldg(rs.time + i) : 0.0f;
+  ray_setup(r);
+}
+
+__device__ __forceinline__ void store_hit(const HitSoA& hs, uint64_t i, const TRay& r, bool hit, const HitRec& h) {
+  if (hs.prim) hs.prim[i] = hit ? h.elem : -1;
+  if (hs.geom) hs.geom[i] = hit ? h.geom : -1;
+  if (hs.t) hs.t[i] = r.tclosest;
+  if (hs.u) hs.u[i] = hit ? h.u : 0.0f;
+  if (hs.v) hs.v[i] = hit ? h.v : 0.0f;
+  if (hs.w) hs.w[i] = hit ? h.w : 0.0f;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void flush_counters(DScratch* s, const Counters& c) {
+  if (!COUNT) return;
+  unsigned long long a = c.nodes, b = c.leafs, d = c.tris;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(kFull, a, o);
+    b += __shfl_down_sync(kFull, b, o);
+    d += __shfl_down_sync(kFull, d, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s->node_visits, a);
+    atomicAdd(&s->leaf_visits, b);
+    atomicAdd(&s->tri_tests, d);
+  }
+}
+
+// Persistent kernel over one mesh.
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_mesh(const DMesh mesh, RaySoA rays, HitSoA hits, uint64_t n,
+                                                    DScratch* scratch) {
+  int2 stk[kStackCapacity];
+  Counters cnt{0, 0, 0};
+  const unsigned lane = threadIdx.x & 31u;
+  int status = kStatusOk;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&scratch->next_ray, 32ull);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= n) break;
+    const uint64_t i = base + lane;
+    if (i < n) {
+      TRay r;
+      load_ray(rays, i, r);
+      HitRec h{-1, 0, 0.f, 0.f, 0.f};
+      bool hit = trace_any_mesh<ANY, COUNT>(mesh, r, stk, kStackCapacity, h, cnt, status);
+      store_hit(hits, i, r, hit, h);
+    }
+  }
+  flush_counters<COUNT>(scratch, cnt);
+  if (status != kStatusOk) atomicMax(&scratch->status, status);
+}
+
+// Scene.Trace (scene.go:30-58): top-level QBVH (leafMax 1) whose leaves run
+// the per-mesh traversal on the remaining part of the same stack, sharing
+// Tclosest, as Scene.TraceElems calls Geom.Trace (scene.go:61-97).
+template <bool ANY, bool COUNT>
+__device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, Counters& cnt, int& status) {
+  bool hit = false;
+  const bool motion = top.keys > 1;
+  float tm = 0.f, omt = 1.f;
+  int key = 0, key2 = 0;
+  if (motion) {
+    const float k = __fmul_rn(r.time, (float)(top.keys - 1));
+    const float fk = floorf(k);
+    tm = __fsub_rn(k, fk);
+    omt = __fsub_rn(1.0f, tm);
+    key = (int)fk;
+    key2 = (int)ceilf(k);
+    if (key < 0 || key2 >= (int)top.keys) return false;
+  }
+  int sp = 0;
+  int node = 0;
+  float nodeT = r.tclosest;
+  for (int iter = 0;; ++iter) {
+    if (iter >= kIterationCap) { status = kStatusIterationCap; break; }
+    if (!(r.tclosest < nodeT) && node != kEmptyChild) {
+      if (node >= 0) {
+        if (COUNT) cnt.nodes++;
+        float4 b[6];
+        int4 ch;
+        unsigned axes;
+        if (!motion) {
+          const float4* nb = reinterpret_cast<const float4*>(top.nodes + node);
+#pragma unroll
+          for (int q = 0; q < 6; ++q) b[q] = __ldg(nb + q);
+          ch = __ldg(reinterpret_cast<const int4*>(nb + 6));
+          axes = __ldg(reinterpret_cast<const unsigned*>(nb + 7));
+        } else {
+          const float4* bk = reinterpret_cast<const float4*>(top.mboxes);
+          const float4* pa = bk + ((size_t)key * top.n_mnodes + node) * 6;
+          const float4* pb = bk + ((size_t)key2 * top.n_mnodes + node) * 6;
+#pragma unroll
+          for (int q = 0; q < 6; ++q) {
+            const float4 a = __ldg(pa + q), c = __ldg(pb + q);
+            b[q].x = __fadd_rn(__fmul_rn(omt, a.x), __fmul_rn(tm, c.x));
+            b[q].y = __fadd_rn(__fmul_rn(omt, a.y), __fmul_rn(tm, c.y));
+            b[q].z = __fadd_rn(__fmul_rn(omt, a.z), __fmul_rn(tm, c.z));
+            b[q].w = __fadd_rn(__fmul_rn(omt, a.w), __fmul_rn(tm, c.w));
+          }
+          ch = __ldg(reinterpret_cast<const int4*>(top.mnodes + node));
+          axes = __ldg(reinterpret_cast<const unsigned*>(top.mnodes + node) + 4);
+        }
+        float tn[4];
+        unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
+        if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
+        if (ch.y == kEmptyChild || r.tclosest < tn[1]) mask &= ~2u;
+        if (ch.z == kEmptyChild || r.tclosest < tn[2]) mask &= ~4u;
+        if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
+        int next;
+        float nextT;
+        if (push_children(stk, sp, kStackCapacity, mask, ch, tn, axes, r.oct, next, nextT, status)) {
+          node = next;
+          nodeT = nextT;
+          continue;
+        }
+        if (status != kStatusOk) break;
+      } else {
+        uint32_t first, count;
+        leaf_decode(node, first, count);
+        if (COUNT) cnt.leafs++;
+        bool leaf_hit = false;
+        for (uint32_t i = first; i < first + count; ++i) {
+          const uint32_t g = __ldg(top.geom_order + i);
+          HitRec hm = h;
+          // The mesh traversal starts one slot above the free stack top,
+          // as Traversal.StackTop = stackTop + 1 does (intersect.go:226).
+          const int base = sp + 1;
+          if (base >= kStackCapacity) { status = kStatusStackOverflow; break; }
+          if (trace_any_mesh<ANY, COUNT>(top.meshes[g], r, stk + base, kStackCapacity - base, hm, cnt, status)) {
+            h = hm;
+            h.geom = (int32_t)g;
+            leaf_hit = true;
+            if (ANY) break;
+          }
+          if (status != kStatusOk) break;
+        }
+        if (status != kStatusOk) break;
+        if (leaf_hit) {
+          hit = true;
+          if (ANY) break;
+        }
+      }
+    }
+    if (sp == 0) break;
+    --sp;
+    const int2 e = stk[sp];
+    node = e.x;
+    nodeT = __int_as_float(e.y);
+  }
+  return hit;
+}
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays, HitSoA hits, uint64_t n,
+                                                     DScratch* scratch) {
+  int2 stk[kStackCapacity];
+  Counters cnt{0, 0, 0};
+  const unsigned lane = threadIdx.x & 31u;
+  int status = kStatusOk;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&scratch->next_ray, 32ull);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= n) break;
+    const uint64_t i = base + lane;
+    if (i < n) {
+      TRay r;
+      load_ray(rays, i, r);
+      HitRec h{-1, -1, 0.f, 0.f, 0.f};
+      bool hit = trace_scene_ray<ANY, COUNT>(top, r, stk, h, cnt, status);
+      store_hit(hits, i, r, hit, h);
+    }
+  }
+  flush_counters<COUNT>(scratch, cnt);
+  if (status != kStatusOk) atomicMax(&scratch->status, status);
+}
+
+template <class K>
+int persistent_grid(K kernel, int block) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
+}
+
+template <bool ANY, bool COUNT>
+int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
+  auto k = k_trace_mesh<ANY, COUNT>;
+  const int block = 128;
+  const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
+  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch);
+  return (int)cudaGetLastError();
+}
+
+template <bool ANY, bool COUNT>
+int launch_scene_t(const DTop& top, const TraceLaunch& l) {
+  auto k = k_trace_scene<ANY, COUNT>;
+  const int block = 128;
+  const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
+  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l) {
+  if (l.any_hit) return l.count ? launch_mesh_t<true, true>(mesh, l) : launch_mesh_t<true, false>(mesh, l);
+  return l.count ? launch_mesh_t<false, true>(mesh, l) : launch_mesh_t<false, false>(mesh, l);
+}
+
+int launch_trace_scene(const DTop& top, const TraceLaunch& l) {
+  if (l.any_hit) return l.count ? launch_scene_t<true, true>(top, l) : launch_scene_t<true, false>(top, l);
+  return l.count ? launch_scene_t<false, true>(top, l) : launch_scene_t<false, false>(top, l);
+}
+
+int device_sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+}  // namespace vmr
