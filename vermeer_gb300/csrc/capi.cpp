@@ -165,6 +165,7 @@ int upload_mesh(vmr_ctx* ctx, MeshRec& rec) {
     VMR_CUDA(ctx, upload(ctx, rec.tris, tris));
     d.nodes = rec.nodes.as<GNode>();
     d.tris = rec.tris.p;
+    d.iter_cap = 4u * (uint32_t)m.nodes.size() + 2u;
   } else {
     std::vector<MNode> g;
     if (!repack_mnodes(m.mnodes, m.n_tris, g)) return fail(ctx, VMR_ERR_INVALID, "malformed motion QBVH nodes");
@@ -191,6 +192,7 @@ int upload_mesh(vmr_ctx* ctx, MeshRec& rec) {
     d.mtris = rec.mtris.p;
     d.elem = rec.elem.as<int32_t>();
     d.n_mnodes = (uint32_t)m.mnodes.size();
+    d.iter_cap = 4u * (uint32_t)m.mnodes.size() + 2u;
   }
   VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   rec.dmesh = d;
@@ -221,6 +223,7 @@ int refresh_top(vmr_ctx* ctx) {
     VMR_CUDA(ctx, upload(ctx, t.nodes, g));
     d.nodes = t.nodes.as<GNode>();
     d.keys = 1;
+    d.iter_cap = 4u * (uint32_t)t.host.nodes.size() + 2u;
   } else {
     std::vector<MNode> g;
     if (!repack_mnodes(t.host.mnodes, (uint32_t)t.host.geom_order.size(), g))
@@ -231,6 +234,7 @@ int refresh_top(vmr_ctx* ctx) {
     d.mboxes = t.mboxes.p;
     d.keys = t.host.keys;
     d.n_mnodes = (uint32_t)t.host.mnodes.size();
+    d.iter_cap = 4u * (uint32_t)t.host.mnodes.size() + 2u;
   }
   VMR_CUDA(ctx, upload(ctx, t.order, t.host.geom_order));
   VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

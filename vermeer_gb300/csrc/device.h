@@ -57,7 +57,8 @@ struct DMesh {
   uint32_t keys;            // 1 = static
   float lower_static;       // EpsilonFloat32 + RayBias (trace.go:182)
   float ray_bias;           // motion lower bound (trace.go:612)
-  uint32_t pad[3];
+  uint32_t iter_cap;        // 4 * nodes + 2: a traversal pops each entry once
+  uint32_t pad[2];
 };
 
 // Top level of a scene (builtin/scene): static GNodes or motion MNodes with
@@ -71,7 +72,7 @@ struct DTop {
   uint32_t keys;
   uint32_t n_mnodes;
   uint32_t n_geoms;
-  uint32_t pad;
+  uint32_t iter_cap;
 };
 
 struct RaySoA {

@@ -30,7 +30,6 @@ namespace vmr {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kIterationCap = 1 << 24;
 
 __device__ __forceinline__ float pick3(float x, float y, float z, int k) {
   return k == 0 ? x : (k == 1 ? y : z);
@@ -237,13 +236,14 @@ __device__ __forceinline__ bool push_children(int2* stk, int& sp, int cap, unsig
 template <bool ANY, bool COUNT>
 __device__ bool trace_static(const DMesh& m, TRay& r, int2* stk, int cap, HitRec& h, Counters& cnt,
                              int& status) {
+  const uint32_t CAP = m.iter_cap;
   const float4* __restrict__ tris = reinterpret_cast<const float4*>(m.tris);
   bool hit = false;
   int sp = 0;
   int node = 0;
   float nodeT = r.tclosest;
-  for (int iter = 0;; ++iter) {
-    if (iter >= kIterationCap) { status = kStatusIterationCap; break; }
+  for (uint32_t iter = 0;; ++iter) {
+    if (iter >= CAP) { status = kStatusIterationCap; break; }
     if (!(r.tclosest < nodeT) && node != kEmptyChild) {
       if (node >= 0) {
         if (COUNT) cnt.nodes++;
@@ -302,6 +302,7 @@ __device__ bool trace_static(const DMesh& m, TRay& r, int2* stk, int cap, HitRec
 template <bool ANY, bool COUNT>
 __device__ bool trace_motion(const DMesh& m, TRay& r, int2* stk, int cap, HitRec& h, Counters& cnt,
                              int& status) {
+  const uint32_t CAP = m.iter_cap;
   // k = Time*float32(keys-1); time = k - Floor(k); key = Floor, key2 = Ceil
   const float k = __fmul_rn(r.time, (float)(m.keys - 1));
   const float fk = floorf(k);
@@ -317,8 +318,8 @@ __device__ bool trace_motion(const DMesh& m, TRay& r, int2* stk, int cap, HitRec
   int sp = 0;
   int node = 0;
   float nodeT = r.tclosest;
-  for (int iter = 0;; ++iter) {
-    if (iter >= kIterationCap) { status = kStatusIterationCap; break; }
+  for (uint32_t iter = 0;; ++iter) {
+    if (iter >= CAP) { status = kStatusIterationCap; break; }
     if (!(r.tclosest < nodeT) && node != kEmptyChild) {
       if (node >= 0) {
         if (COUNT) cnt.nodes++;
@@ -438,7 +439,11 @@ __global__ void __launch_bounds__(128) k_trace_mesh(const DMesh mesh, RaySoA ray
   int status = kStatusOk;
   for (;;) {
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&scratch->next_ray, 32ull);
+    if (lane == 0) {
+      base = atomicAdd(&scratch->next_ray, 32ull);
+      // A ray that hit a bound stops the whole launch at the next fetch.
+      if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) base = n;
+    }
     base = __shfl_sync(kFull, base, 0);
     if (base >= n) break;
     const uint64_t i = base + lane;
@@ -448,10 +453,13 @@ __global__ void __launch_bounds__(128) k_trace_mesh(const DMesh mesh, RaySoA ray
       HitRec h{-1, 0, 0.f, 0.f, 0.f};
       bool hit = trace_any_mesh<ANY, COUNT>(mesh, r, stk, kStackCapacity, h, cnt, status);
       store_hit(hits, i, r, hit, h);
+      if (status != kStatusOk) {
+        atomicMax(&scratch->status, status);
+        status = kStatusOk;
+      }
     }
   }
   flush_counters<COUNT>(scratch, cnt);
-  if (status != kStatusOk) atomicMax(&scratch->status, status);
 }
 
 // Scene.Trace (scene.go:30-58): top-level QBVH (leafMax 1) whose leaves run
@@ -459,6 +467,7 @@ __global__ void __launch_bounds__(128) k_trace_mesh(const DMesh mesh, RaySoA ray
 // Tclosest, as Scene.TraceElems calls Geom.Trace (scene.go:61-97).
 template <bool ANY, bool COUNT>
 __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, Counters& cnt, int& status) {
+  const uint32_t CAP = top.iter_cap;
   bool hit = false;
   const bool motion = top.keys > 1;
   float tm = 0.f, omt = 1.f;
@@ -475,8 +484,8 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
   int sp = 0;
   int node = 0;
   float nodeT = r.tclosest;
-  for (int iter = 0;; ++iter) {
-    if (iter >= kIterationCap) { status = kStatusIterationCap; break; }
+  for (uint32_t iter = 0;; ++iter) {
+    if (iter >= CAP) { status = kStatusIterationCap; break; }
     if (!(r.tclosest < nodeT) && node != kEmptyChild) {
       if (node >= 0) {
         if (COUNT) cnt.nodes++;
@@ -563,7 +572,11 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
   int status = kStatusOk;
   for (;;) {
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&scratch->next_ray, 32ull);
+    if (lane == 0) {
+      base = atomicAdd(&scratch->next_ray, 32ull);
+      // A ray that hit a bound stops the whole launch at the next fetch.
+      if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) base = n;
+    }
     base = __shfl_sync(kFull, base, 0);
     if (base >= n) break;
     const uint64_t i = base + lane;
@@ -573,10 +586,13 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
       HitRec h{-1, -1, 0.f, 0.f, 0.f};
       bool hit = trace_scene_ray<ANY, COUNT>(top, r, stk, h, cnt, status);
       store_hit(hits, i, r, hit, h);
+      if (status != kStatusOk) {
+        atomicMax(&scratch->status, status);
+        status = kStatusOk;
+      }
     }
   }
   flush_counters<COUNT>(scratch, cnt);
-  if (status != kStatusOk) atomicMax(&scratch->status, status);
 }
 
 template <class K>
