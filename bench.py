@@ -196,9 +196,14 @@ def run_gpu(args):
     import vermeer_gb300 as vg
     from vermeer_gb300 import _lib
 
+    global N_RAYS
+    N_RAYS = args.rays
+    CONFIG["rays_per_step"] = N_RAYS
     v, ip, rays = make_workload()
     ctx = vg.Context(local)
-    stream = torch.cuda.current_stream(dev)
+    # A dedicated stream: the kernels and the CUDA events share it.
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     geom = ctx.mesh_build(v, ip)
     soa = np.ascontiguousarray(rays[:, :7].T)  # px py pz dx dy dz tmax
@@ -257,7 +262,48 @@ def run_gpu(args):
     value = N_RAYS * args.steps * world / dev_s / 1e6
     avg_launch_s = dev_s / args.steps
 
-    # End to end through the C ABI: pinned host rays in, pinned hits out.
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / avg_launch_s / 1e9
+    traffic = profiled_traffic()
+    clocks = clk.summary()
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world)
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": CONFIG, "e2e": e2e,
+            "gpu_launches": args.steps,
+            "kernel_ms_mean": round(avg_launch_s * 1e3, 4),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes,
+                         "node_visits_per_ray": round(cst.node_visits / N_RAYS, 3),
+                         "tri_tests_per_ray": round(cst.tri_tests / N_RAYS, 3)},
+            "clocks": clocks}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = cpu_threads()
+        sample = min(1 << 20, N_RAYS)
+        cval, cdt = cpu_baseline(v, ip, rays, threads, sample)
+        line["cpu_baseline"] = {"value": round(cval, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                "sample": f"{sample} of the {N_RAYS} incoherent rays ({cdt:.1f} s), "
+                                          "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world):
+    """End to end through the C ABI: pinned host rays in, pinned hits out,
+    both copies inside the timed region."""
+    import torch
+    import vermeer_gb300 as vg
+    from vermeer_gb300 import _lib
+    P = ctypes.c_void_p
+    L = ctx.L
     pin_rays = [torch.from_numpy(host_soa[k]).pin_memory() for k in range(7)]
     pin_out = {k: torch.empty(N_RAYS, dtype=torch.int32 if k == "prim" else torch.float32).pin_memory()
                for k in ("prim", "t", "u", "v", "w")}
@@ -281,38 +327,8 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     e2e_value = N_RAYS * args.steps * world / e2e_s / 1e6
     ok = np.array_equal(pin_out["prim"].numpy(), hbuf["prim"])
-
-    peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / avg_launch_s / 1e9
-    traffic = profiled_traffic()
-    clocks = clk.summary()
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": CONFIG,
-            "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 7 * 4,
-                    "d2h_bytes_per_step": N_RAYS * 5 * 4, "hits_match_device_path": bool(ok)},
-            "gpu_launches": args.steps,
-            "kernel_ms_mean": round(avg_launch_s * 1e3, 4),
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes,
-                         "node_visits_per_ray": round(cst.node_visits / N_RAYS, 3),
-                         "tri_tests_per_ray": round(cst.tri_tests / N_RAYS, 3)},
-            "clocks": clocks}
-    if rank == 0 and not args.no_cpu_baseline:
-        threads = cpu_threads()
-        sample = 1 << 20
-        cval, cdt = cpu_baseline(v, ip, rays, threads, sample)
-        line["cpu_baseline"] = {"value": round(cval, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                                "sample": f"{sample} of the {N_RAYS} incoherent rays ({cdt:.1f} s), "
-                                          "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"}
-    if rank == 0:
-        print(json.dumps(line))
-    ctx.close()
-    if world > 1:
-        dist.destroy_process_group()
-    return 0
+    return {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 7 * 4,
+            "d2h_bytes_per_step": N_RAYS * 5 * 4, "hits_match_device_path": bool(ok)}
 
 
 def main():
@@ -322,6 +338,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling runs use fewer)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
