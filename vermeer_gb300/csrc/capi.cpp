@@ -113,6 +113,20 @@ bool repack_child(int32_t c, uint32_t n_inner, uint32_t n_elems, int32_t& out) {
 
 uint32_t pack_axes(uint32_t a0, uint32_t a1, uint32_t a2) { return (a0 & 3u) | ((a1 & 3u) << 2) | ((a2 & 3u) << 4); }
 
+// Push rank of each child for every ray octant (bit k of o set when D[k] < 0),
+// following qbvh.Trace (qbvh/intersect.go:137-216): the pairs (0,1) and
+// (2,3) are each ordered by the sign of D along their split axis and the
+// pair order by D[Axis0].  Rank 0 is pushed first, so it is popped last.
+void push_ranks(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t rank[2]) {
+  rank[0] = rank[1] = 0;
+  for (uint32_t o = 0; o < 8; ++o) {
+    const uint32_t s0 = (o >> a0) & 1u, s1 = (o >> a1) & 1u, s2 = (o >> a2) & 1u;
+    const uint32_t r[4] = {2u * (1u - s0) + (1u - s1), 2u * (1u - s0) + s1, 2u * s0 + (1u - s2), 2u * s0 + s2};
+    uint32_t byte = r[0] | (r[1] << 2) | (r[2] << 4) | (r[3] << 6);
+    rank[o >> 2] |= byte << (8u * (o & 3u));
+  }
+}
+
 bool repack_nodes(const std::vector<vmr_qbvh_node>& in, uint32_t n_elems, std::vector<GNode>& out) {
   out.resize(in.size());
   for (size_t i = 0; i < in.size(); ++i) {
@@ -123,6 +137,7 @@ bool repack_nodes(const std::vector<vmr_qbvh_node>& in, uint32_t n_elems, std::v
       if (!repack_child(in[i].children[c], (uint32_t)in.size(), n_elems, g.child[c])) return false;
     if (in[i].axis0 > 2 || in[i].axis1 > 2 || in[i].axis2 > 2) return false;
     g.axes = pack_axes(in[i].axis0, in[i].axis1, in[i].axis2);
+    push_ranks(in[i].axis0, in[i].axis1, in[i].axis2, g.rank);
     out[i] = g;
   }
   return true;
@@ -137,6 +152,7 @@ bool repack_mnodes(const std::vector<vmr_mqbvh_node>& in, uint32_t n_elems, std:
       if (!repack_child(in[i].children[c], (uint32_t)in.size(), n_elems, g.child[c])) return false;
     if ((uint32_t)in[i].axis0 > 2 || (uint32_t)in[i].axis1 > 2 || (uint32_t)in[i].axis2 > 2) return false;
     g.axes = pack_axes((uint32_t)in[i].axis0, (uint32_t)in[i].axis1, (uint32_t)in[i].axis2);
+    push_ranks((uint32_t)in[i].axis0, (uint32_t)in[i].axis1, (uint32_t)in[i].axis2, g.rank);
     out[i] = g;
   }
   return true;

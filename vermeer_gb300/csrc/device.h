@@ -33,14 +33,17 @@ struct alignas(128) GNode {
   float box[24];        // box[c + 4*axis] = min, box[12 + c + 4*axis] = max
   int32_t child[4];
   uint32_t axes;        // axis0 | axis1<<2 | axis2<<4
-  uint32_t pad[3];
+  uint32_t rank[2];     // push rank of each child per ray octant: byte o
+                        // (o = sign bits of D) holds rank(c) at bits 2c
+  uint32_t pad;
 };
 static_assert(sizeof(GNode) == 128, "GNode must be 128 bytes");
 
 struct alignas(32) MNode {
   int32_t child[4];
   uint32_t axes;
-  uint32_t pad[3];
+  uint32_t rank[2];
+  uint32_t pad;
 };
 static_assert(sizeof(MNode) == 32, "MNode must be 32 bytes");
 

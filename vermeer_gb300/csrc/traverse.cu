@@ -429,39 +429,6 @@ __device__ __forceinline__ void flush_counters(DScratch* s, const Counters& c) {
   }
 }
 
-// Persistent kernel over one mesh.
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_mesh(const DMesh mesh, RaySoA rays, HitSoA hits, uint64_t n,
-                                                    DScratch* scratch) {
-  int2 stk[kStackCapacity];
-  Counters cnt{0, 0, 0};
-  const unsigned lane = threadIdx.x & 31u;
-  int status = kStatusOk;
-  for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) {
-      base = atomicAdd(&scratch->next_ray, 32ull);
-      // A ray that hit a bound stops the whole launch at the next fetch.
-      if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) base = n;
-    }
-    base = __shfl_sync(kFull, base, 0);
-    if (base >= n) break;
-    const uint64_t i = base + lane;
-    if (i < n) {
-      TRay r;
-      load_ray(rays, i, r);
-      HitRec h{-1, 0, 0.f, 0.f, 0.f};
-      bool hit = trace_any_mesh<ANY, COUNT>(mesh, r, stk, kStackCapacity, h, cnt, status);
-      store_hit(hits, i, r, hit, h);
-      if (status != kStatusOk) {
-        atomicMax(&scratch->status, status);
-        status = kStatusOk;
-      }
-    }
-  }
-  flush_counters<COUNT>(scratch, cnt);
-}
-
 // Scene.Trace (scene.go:30-58): top-level QBVH (leafMax 1) whose leaves run
 // the per-mesh traversal on the remaining part of the same stack, sharing
 // Tclosest, as Scene.TraceElems calls Geom.Trace (scene.go:61-97).
@@ -595,6 +562,251 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
   flush_counters<COUNT>(scratch, cnt);
 }
 
+// ------------------------------------------------------------------------
+// While-while persistent kernel for one mesh (the hot path).
+//
+// Each lane owns one ray.  An outer iteration runs a node phase (visit
+// inner nodes until the current entry is a leaf or the ray is done) and a
+// leaf phase (scan the leaf's triangles in order), so the warp executes the
+// two code paths one after the other instead of interleaving them per lane.
+// Lanes whose ray finished are refilled at the top of the next iteration
+// with one warp-aggregated atomic (ballot of idle lanes, leader adds the
+// count, lanes take base + their rank among the idle lanes), which keeps the
+// warp full until the ray pool runs dry.
+
+// Fetch a static node: 6 box float4, children, and this octant's push ranks.
+__device__ __forceinline__ void fetch_node(const DMesh& m, int node, unsigned oct, float4 (&b)[6], int4& ch,
+                                           unsigned& rk) {
+  const float4* nb = reinterpret_cast<const float4*>(m.nodes + node);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) b[k] = __ldg(nb + k);
+  ch = __ldg(reinterpret_cast<const int4*>(nb + 6));
+  const uint4 meta = __ldg(reinterpret_cast<const uint4*>(nb + 7));
+  rk = (((oct & 4u) ? meta.z : meta.y) >> ((oct & 3u) * 8u)) & 0xffu;
+}
+
+// Fetch a motion node: boxes of both keys lerped per float
+// ((1.0-time)*Boxes[key] + time*Boxes[key2], motionintersect.go:47-49).
+__device__ __forceinline__ void fetch_mnode(const DMesh& m, int node, unsigned oct, const float4* bx0,
+                                            const float4* bx1, float tm, float omt, float4 (&b)[6], int4& ch,
+                                            unsigned& rk) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const float4 a = __ldg(bx0 + (size_t)node * 6 + q);
+    const float4 c = __ldg(bx1 + (size_t)node * 6 + q);
+    b[q].x = __fadd_rn(__fmul_rn(omt, a.x), __fmul_rn(tm, c.x));
+    b[q].y = __fadd_rn(__fmul_rn(omt, a.y), __fmul_rn(tm, c.y));
+    b[q].z = __fadd_rn(__fmul_rn(omt, a.z), __fmul_rn(tm, c.z));
+    b[q].w = __fadd_rn(__fmul_rn(omt, a.w), __fmul_rn(tm, c.w));
+  }
+  const uint4* mn = reinterpret_cast<const uint4*>(m.mnodes + node);
+  const uint4 c4 = __ldg(mn);
+  ch = make_int4((int)c4.x, (int)c4.y, (int)c4.z, (int)c4.w);
+  const uint4 meta = __ldg(mn + 1);
+  rk = (((oct & 4u) ? meta.z : meta.y) >> ((oct & 3u) * 8u)) & 0xffu;
+}
+
+// Push the hit children in rank order (rank r_c = bits 2c..2c+1 of rk);
+// the highest-ranked child is returned as the next entry instead.
+__device__ __forceinline__ bool push_ranked(int2* stk, int& sp, unsigned mask, const int4& ch, const float (&tn)[4],
+                                            unsigned rk, int& next, float& nextT, int& status) {
+  if (mask == 0) return false;
+  const unsigned r0 = rk & 3u, r1 = (rk >> 2) & 3u, r2 = (rk >> 4) & 3u, r3 = (rk >> 6) & 3u;
+  const unsigned rmask = ((mask & 1u) << r0) | (((mask >> 1) & 1u) << r1) | (((mask >> 2) & 1u) << r2) |
+                         (((mask >> 3) & 1u) << r3);
+  const unsigned rtop = 31u - __clz(rmask);
+  const int npush = __popc(rmask) - 1;
+  if (sp + npush > kStackCapacity) {
+    status = kStatusStackOverflow;
+    return false;
+  }
+  const unsigned rr[4] = {r0, r1, r2, r3};
+  const int cv[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (mask & (1u << c)) {
+      if (rr[c] == rtop) {
+        next = cv[c];
+        nextT = tn[c];
+      } else {
+        stk[sp + __popc(rmask & ((1u << rr[c]) - 1u))] = make_int2(cv[c], __float_as_int(tn[c]));
+      }
+    }
+  }
+  sp += npush;
+  return true;
+}
+
+template <bool MOTION, bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
+                                                       DScratch* scratch) {
+  int2 stk[kStackCapacity];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  TRay r;
+  HitRec h{-1, -1, 0.f, 0.f, 0.f};
+  int node = 0, sp = 0;
+  float nodeT = 0.f;
+  uint64_t rid = 0;
+  uint32_t iter = 0;
+  bool alive = false, hit = false;
+  bool more = true;  // warp-uniform: the pool may still hold rays
+  int status = kStatusOk;
+  Counters cnt{0, 0, 0};
+  float tm = 0.f, omt = 1.f;
+  const float4* bx0 = nullptr;
+  const float4* bx1 = nullptr;
+  const float4* tr0 = reinterpret_cast<const float4*>(MOTION ? m.mtris : m.tris);
+  const float4* tr1 = tr0;
+  for (;;) {
+    const unsigned need = __ballot_sync(kFull, !alive);
+    if (need != 0u && more) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) {
+        base = atomicAdd(&scratch->next_ray, (unsigned long long)__popc(need));
+        // A ray that hit a bound stops the whole launch at the next fetch.
+        if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) base = n;
+      }
+      base = __shfl_sync(kFull, base, leader);
+      if (base + __popc(need) >= n) more = false;
+      if (!alive) {
+        const uint64_t i = base + __popc(need & lanes_below);
+        if (i < n) {
+          rid = i;
+          load_ray(rays, i, r);
+          h = HitRec{-1, -1, 0.f, 0.f, 0.f};
+          hit = false;
+          node = 0;
+          nodeT = r.tclosest;
+          sp = 0;
+          iter = 0;
+          alive = true;
+          if (MOTION) {
+            // k = Time*float32(keys-1); time = k-Floor(k); key = Floor(k),
+            // key2 = Ceil(k) (builtin/geom/polymesh/trace.go:79-84)
+            const float k = __fmul_rn(r.time, (float)(m.keys - 1));
+            const float fk = floorf(k);
+            tm = __fsub_rn(k, fk);
+            omt = __fsub_rn(1.0f, tm);
+            const int key = (int)fk, key2 = (int)ceilf(k);
+            if (key < 0 || key2 >= (int)m.keys) {
+              // out of the key range: the reference indexes out of bounds; miss
+              store_hit(hits, rid, r, false, h);
+              alive = false;
+            } else {
+              bx0 = reinterpret_cast<const float4*>(m.mboxes) + (size_t)key * m.n_mnodes * 6;
+              bx1 = reinterpret_cast<const float4*>(m.mboxes) + (size_t)key2 * m.n_mnodes * 6;
+              tr0 = reinterpret_cast<const float4*>(m.mtris) + (size_t)key * m.n_tris * 3;
+              tr1 = reinterpret_cast<const float4*>(m.mtris) + (size_t)key2 * m.n_tris * 3;
+            }
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, alive)) {
+      if (!more) break;
+      continue;
+    }
+    if (alive) {
+      bool done = false;
+      // ---- node phase: inner nodes until a leaf or the stack runs dry
+      for (;;) {
+        if (++iter > m.iter_cap) { status = kStatusIterationCap; done = true; break; }
+        if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
+          if (sp == 0) { done = true; break; }
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+          continue;
+        }
+        if (node < 0) break;  // a leaf: the leaf phase handles it
+        if (COUNT) cnt.nodes++;
+        float4 b[6];
+        int4 ch;
+        unsigned rk;
+        if (MOTION) fetch_mnode(m, node, r.oct, bx0, bx1, tm, omt, b, ch, rk);
+        else fetch_node(m, node, r.oct, b, ch, rk);
+        float tn[4];
+        unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
+        if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
+        if (ch.y == kEmptyChild || r.tclosest < tn[1]) mask &= ~2u;
+        if (ch.z == kEmptyChild || r.tclosest < tn[2]) mask &= ~4u;
+        if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
+        int next = 0;
+        float nextT = 0.f;
+        if (push_ranked(stk, sp, mask, ch, tn, rk, next, nextT, status)) {
+          node = next;
+          nodeT = nextT;
+        } else {
+          if (status != kStatusOk || sp == 0) { done = true; break; }
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+        }
+      }
+      // ---- leaf phase: TraceElems / TraceMotionElems over [first, first+count)
+      if (!done) {
+        uint32_t first, count;
+        leaf_decode(node, first, count);
+        if (COUNT) { cnt.leafs++; cnt.tris += count; }
+        int32_t idx = -1;
+        float U = 0.f, V = 0.f, W = 0.f;
+        for (uint32_t i = first; i < first + count; ++i) {
+          float4 v0, v1, v2;
+          if (MOTION) {
+            float4 a[3], c[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              a[j] = __ldg(tr0 + 3 * (size_t)i + j);
+              c[j] = __ldg(tr1 + 3 * (size_t)i + j);
+            }
+            // Vec3Lerp (math/vec3.go:52-58)
+            v0 = make_float4(__fadd_rn(__fmul_rn(omt, a[0].x), __fmul_rn(tm, c[0].x)),
+                             __fadd_rn(__fmul_rn(omt, a[0].y), __fmul_rn(tm, c[0].y)),
+                             __fadd_rn(__fmul_rn(omt, a[0].z), __fmul_rn(tm, c[0].z)), 0.f);
+            v1 = make_float4(__fadd_rn(__fmul_rn(omt, a[1].x), __fmul_rn(tm, c[1].x)),
+                             __fadd_rn(__fmul_rn(omt, a[1].y), __fmul_rn(tm, c[1].y)),
+                             __fadd_rn(__fmul_rn(omt, a[1].z), __fmul_rn(tm, c[1].z)), 0.f);
+            v2 = make_float4(__fadd_rn(__fmul_rn(omt, a[2].x), __fmul_rn(tm, c[2].x)),
+                             __fadd_rn(__fmul_rn(omt, a[2].y), __fmul_rn(tm, c[2].y)),
+                             __fadd_rn(__fmul_rn(omt, a[2].z), __fmul_rn(tm, c[2].z)), 0.f);
+            if (tri_test<false>(r, v0, v1, v2, m.ray_bias, U, V, W)) idx = (int32_t)i;
+          } else {
+            v0 = __ldg(tr0 + 3 * (size_t)i);
+            v1 = __ldg(tr0 + 3 * (size_t)i + 1);
+            v2 = __ldg(tr0 + 3 * (size_t)i + 2);
+            if (tri_test<true>(r, v0, v1, v2, m.lower_static, U, V, W)) idx = (int32_t)i;
+          }
+        }
+        if (idx != -1) {
+          h.elem = MOTION ? __ldg(m.elem + idx) : idx;
+          h.u = U;
+          h.v = V;
+          h.w = W;
+          hit = true;
+        }
+        if ((ANY && idx != -1) || sp == 0) {
+          done = true;
+        } else {
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+        }
+      }
+      if (done) {
+        store_hit(hits, rid, r, hit, h);
+        alive = false;
+        if (status != kStatusOk) {
+          atomicMax(&scratch->status, status);
+          status = kStatusOk;
+        }
+      }
+    }
+  }
+  flush_counters<COUNT>(scratch, cnt);
+}
+
 template <class K>
 int persistent_grid(K kernel, int block) {
   int dev = 0, sms = 0, per_sm = 0;
@@ -605,13 +817,19 @@ int persistent_grid(K kernel, int block) {
   return sms * per_sm;
 }
 
-template <bool ANY, bool COUNT>
+template <bool MOTION, bool ANY, bool COUNT>
 int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
-  auto k = k_trace_mesh<ANY, COUNT>;
+  auto k = k_trace_mesh_ww<MOTION, ANY, COUNT>;
   const int block = 128;
   const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
   k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch);
   return (int)cudaGetLastError();
+}
+
+template <bool MOTION>
+int launch_mesh_m(const DMesh& mesh, const TraceLaunch& l) {
+  if (l.any_hit) return l.count ? launch_mesh_t<MOTION, true, true>(mesh, l) : launch_mesh_t<MOTION, true, false>(mesh, l);
+  return l.count ? launch_mesh_t<MOTION, false, true>(mesh, l) : launch_mesh_t<MOTION, false, false>(mesh, l);
 }
 
 template <bool ANY, bool COUNT>
@@ -626,8 +844,7 @@ int launch_scene_t(const DTop& top, const TraceLaunch& l) {
 }  // namespace
 
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l) {
-  if (l.any_hit) return l.count ? launch_mesh_t<true, true>(mesh, l) : launch_mesh_t<true, false>(mesh, l);
-  return l.count ? launch_mesh_t<false, true>(mesh, l) : launch_mesh_t<false, false>(mesh, l);
+  return mesh.keys > 1 ? launch_mesh_m<true>(mesh, l) : launch_mesh_m<false>(mesh, l);
 }
 
 int launch_trace_scene(const DTop& top, const TraceLaunch& l) {
