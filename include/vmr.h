@@ -57,6 +57,18 @@ int vmr_set_stream(vmr_ctx* ctx, void* cuda_stream);
 int vmr_sync(vmr_ctx* ctx);
 int vmr_abi_version(void);
 
+/* Launch parameters of the traversal kernels, chosen per scene (by hand or
+ * by vmr_autotune).  Results never depend on them: they only change how
+ * rays are scheduled onto warps.  Zero fields take the defaults. */
+typedef struct {
+    int kernel;          /* 0 = step-scheduled (default), 1 = while-while */
+    int block;           /* threads per block, multiple of 32, <= 256 (128) */
+    int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
+    int refill_min;      /* idle lanes that trigger a warp refill, 1..32 (4) */
+} vmr_tuning;
+int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* tuning);
+int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* tuning);
+
 /* ------------------------------------------------------------ QBVH nodes */
 /* qbvh.Node (qbvh/qbvh.go:31-36), 128 bytes, identical memory layout:
  * boxes[child + 12*(0 min|1 max) + 4*axis]; children >= 0 inner node,

@@ -43,6 +43,11 @@ class Hits(ctypes.Structure):
     _fields_ = [(n, P) for n in ("prim", "geom", "t", "u", "v", "w")]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("kernel", ctypes.c_int), ("block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
+                ("refill_min", ctypes.c_int)]
+
+
 class TraceStats(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_uint64), ("node_visits", ctypes.c_uint64), ("leaf_visits", ctypes.c_uint64),
                 ("tri_tests", ctypes.c_uint64), ("kernel_ms", ctypes.c_float)]
@@ -58,6 +63,8 @@ SIGNATURES = {
     "vmr_last_error": (ctypes.c_char_p, [P]),
     "vmr_set_stream": (ctypes.c_int, [P, P]),
     "vmr_sync": (ctypes.c_int, [P]),
+    "vmr_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
+    "vmr_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
     "vmr_mesh_build": (ctypes.c_int, [P, ctypes.POINTER(MeshInput), ctypes.POINTER(U32)]),
     "vmr_mesh_upload": (ctypes.c_int, [P, ctypes.POINTER(MeshDesc), ctypes.POINTER(U32)]),
     "vmr_mesh_info": (ctypes.c_int, [P, U32, P, P, P, P]),

@@ -68,6 +68,7 @@ struct vmr_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
+  vmr_tuning tuning{0, 0, 0, 0};
 };
 
 namespace {
@@ -289,6 +290,10 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   l.count = (flags & VMR_TRACE_COUNT) ? 1 : 0;
   l.scratch = ctx->scratch.as<DScratch>();
   l.stream = ctx->stream;
+  l.kernel = ctx->tuning.kernel;
+  l.block = ctx->tuning.block;
+  l.grid = ctx->tuning.blocks_per_sm;
+  l.refill_min = ctx->tuning.refill_min;
   VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   int e = mesh ? vmr::launch_trace_mesh(*mesh, l) : vmr::launch_trace_scene(ctx->top.dtop, l);
@@ -384,6 +389,23 @@ int vmr_destroy(vmr_ctx* ctx) {
 }
 
 const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
+  if (!ctx || !t) return VMR_ERR_INVALID;
+  if (t->kernel < 0 || t->kernel > 1) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be 0 or 1");
+  if (t->block != 0 && (t->block < 32 || t->block > 256 || t->block % 32 != 0))
+    return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
+  if (t->blocks_per_sm < 0 || t->refill_min < 0 || t->refill_min > 32)
+    return fail(ctx, VMR_ERR_INVALID, "tuning.blocks_per_sm >= 0 and refill_min in [0, 32]");
+  ctx->tuning = *t;
+  return VMR_OK;
+}
+
+int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* t) {
+  if (!ctx || !t) return VMR_ERR_INVALID;
+  *t = ctx->tuning;
+  return VMR_OK;
+}
 
 int vmr_set_stream(vmr_ctx* ctx, void* s) {
   if (!ctx) return VMR_ERR_INVALID;

@@ -106,6 +106,9 @@ enum DeviceStatus : int {
 
 constexpr int kStackCapacity = 90;  // RenderTask.Traversal.Stack (core/ray.go:158)
 
+// Traversal kernel variants (vmr_tuning.kernel).
+enum TraceKernel : int { kKernelScheduled = 0, kKernelWhileWhile = 1 };
+
 // Launch entry points (traverse.cu).
 struct TraceLaunch {
   RaySoA rays;
@@ -114,8 +117,10 @@ struct TraceLaunch {
   int any_hit;
   int count;
   DScratch* scratch;
-  int grid;
+  int grid;             // resident blocks per SM wanted (0 = occupancy maximum)
   int block;
+  int kernel;
+  int refill_min;
   void* stream;
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);

@@ -638,7 +638,7 @@ __device__ __forceinline__ bool push_ranked(int2* stk, int& sp, unsigned mask, c
 }
 
 template <bool MOTION, bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
+__global__ void __launch_bounds__(256) k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
                                                        DScratch* scratch) {
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
@@ -807,22 +807,215 @@ __global__ void __launch_bounds__(128) k_trace_mesh_ww(const DMesh m, RaySoA ray
   flush_counters<COUNT>(scratch, cnt);
 }
 
+// ------------------------------------------------------------------------
+// Step-scheduled persistent kernel.  Each lane is IDLE, at an inner-node
+// entry (NODE) or inside a leaf (LEAF, next triangle ti of [ti, tend)).  A
+// step runs ONE node visit for the NODE lanes or ONE triangle test for the
+// LEAF lanes, whichever group holds more lanes (one ballot per step), so a
+// lane never waits for another lane's whole node walk or whole leaf.  Idle
+// lanes are refilled once at least `refill_min` of them are idle.  Per ray
+// the sequence of pops, visits, culls and triangle tests is the
+// reference's.
+enum LaneState : int { kIdle = 0, kNode = 1, kLeaf = 2 };
+
+template <bool MOTION>
+__device__ __forceinline__ bool test_tri(const DMesh& m, TRay& r, uint32_t i, const float4* tr0, const float4* tr1,
+                                         float tm, float omt, float& U, float& V, float& W) {
+  if (MOTION) {
+    float4 a[3], c[3], v[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      a[j] = __ldg(tr0 + 3 * (size_t)i + j);
+      c[j] = __ldg(tr1 + 3 * (size_t)i + j);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)  // Vec3Lerp (math/vec3.go:52-58)
+      v[j] = make_float4(__fadd_rn(__fmul_rn(omt, a[j].x), __fmul_rn(tm, c[j].x)),
+                         __fadd_rn(__fmul_rn(omt, a[j].y), __fmul_rn(tm, c[j].y)),
+                         __fadd_rn(__fmul_rn(omt, a[j].z), __fmul_rn(tm, c[j].z)), 0.f);
+    return tri_test<false>(r, v[0], v[1], v[2], m.ray_bias, U, V, W);
+  }
+  const float4 v0 = __ldg(tr0 + 3 * (size_t)i);
+  const float4 v1 = __ldg(tr0 + 3 * (size_t)i + 1);
+  const float4 v2 = __ldg(tr0 + 3 * (size_t)i + 2);
+  return tri_test<true>(r, v0, v1, v2, m.lower_static, U, V, W);
+}
+
+template <bool MOTION, bool ANY, bool COUNT>
+__global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
+                                                          DScratch* scratch, int refill_min) {
+  int2 stk[kStackCapacity];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  TRay r;
+  HitRec h{-1, -1, 0.f, 0.f, 0.f};
+  int state = kIdle;
+  int node = 0, sp = 0;
+  float nodeT = 0.f;
+  uint32_t ti = 0, tend = 0;
+  uint64_t rid = 0;
+  uint32_t iter = 0;
+  bool hit = false, leafhit = false;
+  bool more = true;
+  int status = kStatusOk;
+  Counters cnt{0, 0, 0};
+  float tm = 0.f, omt = 1.f;
+  const float4* bx0 = nullptr;
+  const float4* bx1 = nullptr;
+  const float4* tr0 = reinterpret_cast<const float4*>(MOTION ? m.mtris : m.tris);
+  const float4* tr1 = tr0;
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, state == kIdle);
+    if (more && idle != 0u && (__popc(idle) >= refill_min || idle == kFull)) {
+      const int leader = __ffs(idle) - 1;
+      unsigned long long base = 0;
+      if ((int)lane == leader) {
+        base = atomicAdd(&scratch->next_ray, (unsigned long long)__popc(idle));
+        if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) base = n;
+      }
+      base = __shfl_sync(kFull, base, leader);
+      if (base + __popc(idle) >= n) more = false;
+      if (state == kIdle) {
+        const uint64_t i = base + __popc(idle & lanes_below);
+        if (i < n) {
+          rid = i;
+          load_ray(rays, i, r);
+          h = HitRec{-1, -1, 0.f, 0.f, 0.f};
+          hit = false;
+          node = 0;
+          nodeT = r.tclosest;
+          sp = 0;
+          iter = 0;
+          state = kNode;
+          if (MOTION) {
+            const float k = __fmul_rn(r.time, (float)(m.keys - 1));
+            const float fk = floorf(k);
+            tm = __fsub_rn(k, fk);
+            omt = __fsub_rn(1.0f, tm);
+            const int key = (int)fk, key2 = (int)ceilf(k);
+            if (key < 0 || key2 >= (int)m.keys) {
+              store_hit(hits, rid, r, false, h);
+              state = kIdle;
+            } else {
+              bx0 = reinterpret_cast<const float4*>(m.mboxes) + (size_t)key * m.n_mnodes * 6;
+              bx1 = reinterpret_cast<const float4*>(m.mboxes) + (size_t)key2 * m.n_mnodes * 6;
+              tr0 = reinterpret_cast<const float4*>(m.mtris) + (size_t)key * m.n_tris * 3;
+              tr1 = reinterpret_cast<const float4*>(m.mtris) + (size_t)key2 * m.n_tris * 3;
+            }
+          }
+        }
+      }
+    }
+    const unsigned leafm = __ballot_sync(kFull, state == kLeaf);
+    const unsigned nodem = __ballot_sync(kFull, state == kNode);
+    if ((leafm | nodem) == 0u) {
+      if (!more) break;
+      continue;
+    }
+    bool finish = false;
+    if (__popc(leafm) >= __popc(nodem)) {
+      if (state == kLeaf) {
+        float U, V, W;
+        if (test_tri<MOTION>(m, r, ti, tr0, tr1, tm, omt, U, V, W)) {
+          h.elem = MOTION ? __ldg(m.elem + ti) : (int32_t)ti;
+          h.u = U;
+          h.v = V;
+          h.w = W;
+          hit = true;
+          leafhit = true;
+        }
+        if (++ti == tend) {
+          if ((ANY && leafhit) || sp == 0) {
+            finish = true;
+          } else {
+            const int2 e = stk[--sp];
+            node = e.x;
+            nodeT = __int_as_float(e.y);
+            state = kNode;
+          }
+        }
+      }
+    } else if (state == kNode) {
+      if (++iter > m.iter_cap) {
+        status = kStatusIterationCap;
+        finish = true;
+      } else if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
+        if (sp == 0) {
+          finish = true;
+        } else {
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+        }
+      } else if (node < 0) {
+        leaf_decode(node, ti, tend);
+        tend += ti;
+        leafhit = false;
+        state = kLeaf;
+        if (COUNT) { cnt.leafs++; cnt.tris += tend - ti; }
+      } else {
+        if (COUNT) cnt.nodes++;
+        float4 b[6];
+        int4 ch;
+        unsigned rk;
+        if (MOTION) fetch_mnode(m, node, r.oct, bx0, bx1, tm, omt, b, ch, rk);
+        else fetch_node(m, node, r.oct, b, ch, rk);
+        float tn[4];
+        unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
+        if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
+        if (ch.y == kEmptyChild || r.tclosest < tn[1]) mask &= ~2u;
+        if (ch.z == kEmptyChild || r.tclosest < tn[2]) mask &= ~4u;
+        if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
+        int next = 0;
+        float nextT = 0.f;
+        if (push_ranked(stk, sp, mask, ch, tn, rk, next, nextT, status)) {
+          node = next;
+          nodeT = nextT;
+        } else if (status != kStatusOk || sp == 0) {
+          finish = true;
+        } else {
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+        }
+      }
+    }
+    if (finish) {
+      store_hit(hits, rid, r, hit, h);
+      state = kIdle;
+      if (status != kStatusOk) {
+        atomicMax(&scratch->status, status);
+        status = kStatusOk;
+      }
+    }
+  }
+  flush_counters<COUNT>(scratch, cnt);
+}
+
 template <class K>
-int persistent_grid(K kernel, int block) {
+int persistent_grid(K kernel, int block, int want_per_sm = 0) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
   if (per_sm < 1) per_sm = 1;
+  if (want_per_sm > 0 && want_per_sm < per_sm) per_sm = want_per_sm;
   return sms * per_sm;
 }
 
 template <bool MOTION, bool ANY, bool COUNT>
 int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
-  auto k = k_trace_mesh_ww<MOTION, ANY, COUNT>;
-  const int block = 128;
-  const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
-  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch);
+  const int block = l.block > 0 ? l.block : 128;
+  if (l.kernel == kKernelWhileWhile) {
+    auto k = k_trace_mesh_ww<MOTION, ANY, COUNT>;
+    const int grid = persistent_grid(k, block, l.grid);
+    k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch);
+  } else {
+    auto k = k_trace_mesh_sched<MOTION, ANY, COUNT>;
+    const int grid = persistent_grid(k, block, l.grid);
+    k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch,
+                                                  l.refill_min > 0 ? l.refill_min : 4);
+  }
   return (int)cudaGetLastError();
 }
 
