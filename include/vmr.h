@@ -61,7 +61,9 @@ int vmr_abi_version(void);
  * by vmr_autotune).  Results never depend on them: they only change how
  * rays are scheduled onto warps.  Zero fields take the defaults. */
 typedef struct {
-    int kernel;          /* 0 = step-scheduled (default), 1 = while-while */
+    int kernel;          /* bit 0: while-while (else step-scheduled); bit 1:
+                            L1 prefetch of the next leaf/node; bit 2: 64-register
+                            cap (while-while only) */
     int block;           /* threads per block, multiple of 32, <= 256 (128) */
     int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
     int refill_min;      /* idle lanes that trigger a warp refill, 1..32 (4) */

@@ -68,7 +68,7 @@ struct vmr_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
-  vmr_tuning tuning{0, 0, 0, 0};
+  vmr_tuning tuning{1, 0, 0, 0};
 };
 
 namespace {
@@ -392,7 +392,7 @@ const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
   if (!ctx || !t) return VMR_ERR_INVALID;
-  if (t->kernel < 0 || t->kernel > 1) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be 0 or 1");
+  if (t->kernel < 0 || t->kernel > 7) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 7]");
   if (t->block != 0 && (t->block < 32 || t->block > 256 || t->block % 32 != 0))
     return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
   if (t->blocks_per_sm < 0 || t->refill_min < 0 || t->refill_min > 32)

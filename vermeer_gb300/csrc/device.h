@@ -107,7 +107,7 @@ enum DeviceStatus : int {
 constexpr int kStackCapacity = 90;  // RenderTask.Traversal.Stack (core/ray.go:158)
 
 // Traversal kernel variants (vmr_tuning.kernel).
-enum TraceKernel : int { kKernelScheduled = 0, kKernelWhileWhile = 1 };
+enum TraceKernel : int { kKernelScheduled = 0, kKernelWhileWhile = 1, kKernelPrefetch = 2, kKernelRegCap = 4 };
 
 // Launch entry points (traverse.cu).
 struct TraceLaunch {

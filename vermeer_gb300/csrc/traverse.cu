@@ -123,6 +123,18 @@ __device__ __forceinline__ unsigned box4(const TRay& r, const float4 (&b)[6], fl
   return mask;
 }
 
+// L1 prefetch hints (no register result).  Only issued for addresses inside
+// the node and triangle arrays.
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+// The lines holding triangles [first, first+count) (48 bytes each).
+__device__ __forceinline__ void prefetch_leaf(const float4* tris, uint32_t first, uint32_t count) {
+  const char* a = reinterpret_cast<const char*>(tris + 3 * (size_t)first);
+  const char* e = reinterpret_cast<const char*>(tris + 3 * (size_t)(first + count));
+  for (const char* q = reinterpret_cast<const char*>((uintptr_t)a & ~(uintptr_t)127); q < e; q += 128) prefetch_l1(q);
+}
+
 // Result of the accepted triangle (ShaderContext fields the trace fills).
 struct HitRec {
   int32_t elem;
@@ -637,9 +649,9 @@ __device__ __forceinline__ bool push_ranked(int2* stk, int& sp, unsigned mask, c
   return true;
 }
 
-template <bool MOTION, bool ANY, bool COUNT>
-__global__ void __launch_bounds__(256) k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
-                                                       DScratch* scratch) {
+template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB>
+__global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
+    k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch) {
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
@@ -720,7 +732,16 @@ __global__ void __launch_bounds__(256) k_trace_mesh_ww(const DMesh m, RaySoA ray
           nodeT = __int_as_float(e.y);
           continue;
         }
-        if (node < 0) break;  // a leaf: the leaf phase handles it
+        if (node < 0) {  // a leaf: the leaf phase handles it
+          if (PF && !MOTION) {
+            // The lane now waits for the warp's other node walks: fetch
+            // its triangles into L1 meanwhile.
+            uint32_t f, c;
+            leaf_decode(node, f, c);
+            prefetch_leaf(tr0, f, c);
+          }
+          break;
+        }
         if (COUNT) cnt.nodes++;
         float4 b[6];
         int4 ch;
@@ -792,6 +813,7 @@ __global__ void __launch_bounds__(256) k_trace_mesh_ww(const DMesh m, RaySoA ray
           const int2 e = stk[--sp];
           node = e.x;
           nodeT = __int_as_float(e.y);
+          if (PF && !MOTION && node >= 0) prefetch_l1(m.nodes + node);
         }
       }
       if (done) {
@@ -841,7 +863,7 @@ __device__ __forceinline__ bool test_tri(const DMesh& m, TRay& r, uint32_t i, co
   return tri_test<true>(r, v0, v1, v2, m.lower_static, U, V, W);
 }
 
-template <bool MOTION, bool ANY, bool COUNT>
+template <bool MOTION, bool ANY, bool COUNT, bool PF>
 __global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
                                                           DScratch* scratch, int refill_min) {
   int2 stk[kStackCapacity];
@@ -932,6 +954,7 @@ __global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA 
             node = e.x;
             nodeT = __int_as_float(e.y);
             state = kNode;
+            if (PF && !MOTION && node >= 0) prefetch_l1(m.nodes + node);
           }
         }
       }
@@ -949,6 +972,7 @@ __global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA 
         }
       } else if (node < 0) {
         leaf_decode(node, ti, tend);
+        if (PF && !MOTION) prefetch_leaf(tr0, ti, tend);
         tend += ti;
         leafhit = false;
         state = kLeaf;
@@ -1003,20 +1027,34 @@ int persistent_grid(K kernel, int block, int want_per_sm = 0) {
   return sms * per_sm;
 }
 
+template <class K, class... A>
+int launch_persistent(K k, const TraceLaunch& l, int block, A... args) {
+  const int grid = persistent_grid(k, block, l.grid);
+  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(args...);
+  return (int)cudaGetLastError();
+}
+
+// tuning.kernel: bit 0 = while-while (else step-scheduled), bit 1 = L1
+// prefetch of the next leaf / node, bit 2 = 64-register cap (while-while,
+// 128 threads, 8 resident blocks).
 template <bool MOTION, bool ANY, bool COUNT>
 int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
   const int block = l.block > 0 ? l.block : 128;
-  if (l.kernel == kKernelWhileWhile) {
-    auto k = k_trace_mesh_ww<MOTION, ANY, COUNT>;
-    const int grid = persistent_grid(k, block, l.grid);
-    k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch);
-  } else {
-    auto k = k_trace_mesh_sched<MOTION, ANY, COUNT>;
-    const int grid = persistent_grid(k, block, l.grid);
-    k<<<grid, block, 0, (cudaStream_t)l.stream>>>(mesh, l.rays, l.hits, l.n, l.scratch,
-                                                  l.refill_min > 0 ? l.refill_min : 4);
+  const int v = l.kernel;
+  if (v & kKernelWhileWhile) {
+    if (v & kKernelRegCap) {
+      if (v & kKernelPrefetch)
+        return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch);
+      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch);
+    }
+    if (v & kKernelPrefetch)
+      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch);
+    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch);
   }
-  return (int)cudaGetLastError();
+  const int refill = l.refill_min > 0 ? l.refill_min : 4;
+  if (v & kKernelPrefetch)
+    return launch_persistent(k_trace_mesh_sched<MOTION, ANY, COUNT, true>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, refill);
+  return launch_persistent(k_trace_mesh_sched<MOTION, ANY, COUNT, false>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, refill);
 }
 
 template <bool MOTION>
