@@ -63,7 +63,9 @@ int vmr_abi_version(void);
 typedef struct {
     int kernel;          /* bit 0: while-while (else step-scheduled); bit 1:
                             L1 prefetch of the next leaf/node; bit 2: 64-register
-                            cap (while-while only) */
+                            cap (while-while only); bit 3: reorder rays by
+                            permutation class and origin cell before a mesh
+                            trace of >= 65536 rays */
     int block;           /* threads per block, multiple of 32, <= 256 (128) */
     int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
     int refill_min;      /* idle lanes that trigger a warp refill, 1..32 (4) */

@@ -136,3 +136,27 @@ def test_full_size_soup_parity(ctx, orc):
     assert_hits_equal(ctx.trace_mesh(geom, rays), om.trace(rays), what="1M soup closest")
     sub = rays[: 1 << 20]
     assert_hits_equal(ctx.trace_mesh(geom, sub, shadow=True), om.trace(sub, shadow=True), what="1M soup any")
+
+
+@pytest.mark.parametrize("tuning", [(0, 0, 0, 0), (1, 0, 0, 0), (3, 0, 0, 0), (5, 0, 0, 0), (8, 0, 0, 4),
+                                    (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0)])
+def test_every_tuning_is_bit_exact(ctx, orc, tuning):
+    """Launch parameters (kernel variant, ray reordering, block size,
+    resident blocks) only change scheduling: hits stay bit-exact."""
+    v, ip = scenes.triangle_soup(100000, 17, edge=0.006)
+    rays = scenes.incoherent_rays(150000, 18)
+    geom = ctx.mesh_build(v, ip)
+    om = orc.Mesh(v, ip)
+    try:
+        ctx.set_tuning(*tuning)
+        for shadow in (False, True):
+            assert_hits_equal(ctx.trace_mesh(geom, rays, shadow=shadow), om.trace(rays, shadow=shadow),
+                              what=f"tuning={tuning} shadow={shadow}")
+        mv, mip = scenes.motion_soup(20000, 19, edge=0.01)
+        mg = ctx.mesh_build(mv, mip, keys=2, motion_mode=1)
+        mrays = rays.copy()
+        mrays[:, 7] = scenes.uniform(20, mrays.shape[0], 1).astype(np.float32)
+        assert_hits_equal(ctx.trace_mesh(mg, mrays), orc.Mesh(mv, mip, keys=2, motion_fixed=True).trace(mrays),
+                          what=f"motion tuning={tuning}")
+    finally:
+        ctx.set_tuning(1, 0, 0, 0)

@@ -47,6 +47,7 @@ struct MeshRec {
   HostMesh host;
   DevBuf nodes, tris, mnodes, mboxes, mtris, elem;
   DMesh dmesh{};
+  float bounds6[6];
 };
 
 struct TopRec {
@@ -65,10 +66,17 @@ struct vmr_ctx {
   std::string err;
   DevBuf scratch;                 // DScratch
   DevBuf io;                      // rays + hits for host-pointer traces
+  DevBuf sortbuf;                 // ray keys, bucket offsets, order, key-ordered rays
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
   vmr_tuning tuning{1, 0, 0, 0};
+  // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
+  const float* mesh_bounds_of(const DMesh* d) const {
+    for (const auto& m : meshes)
+      if (&m->dmesh == d) return m->bounds6;
+    return nullptr;
+  }
 };
 
 namespace {
@@ -213,6 +221,10 @@ int upload_mesh(vmr_ctx* ctx, MeshRec& rec) {
   }
   VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   rec.dmesh = d;
+  for (int a = 0; a < 3; ++a) {
+    rec.bounds6[a] = m.bounds.lo[a];
+    rec.bounds6[3 + a] = m.bounds.hi[a];
+  }
   return VMR_OK;
 }
 
@@ -296,6 +308,24 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   l.refill_min = ctx->tuning.refill_min;
   VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  if (mesh && (ctx->tuning.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
+    // Key-ordered copy of the rays (raysort.cu); hits go back through order[].
+    const size_t nf = ((n + 31) / 32) * 32;
+    const int nfield = r.time ? 8 : 7;
+    const size_t bytes = nf * 4 * (2 + nfield) + sizeof(uint32_t) * vmr::kSortBuckets;
+    VMR_CUDA(ctx, ctx->sortbuf.ensure(bytes));
+    uint32_t* keys = ctx->sortbuf.as<uint32_t>();
+    uint32_t* order = keys + nf;
+    float* f = reinterpret_cast<float*>(order + nf);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(f + nf * nfield);
+    vmr::RaySoA sorted{f, f + nf, f + 2 * nf, f + 3 * nf, f + 4 * nf, f + 5 * nf, f + 6 * nf,
+                       nfield == 8 ? f + 7 * nf : nullptr};
+    const float* mb = ctx->mesh_bounds_of(mesh);
+    int se = vmr::launch_ray_sort(l.rays, n, mb, keys, hist, order, sorted, ctx->stream);
+    if (se != 0) return cuda_fail(ctx, (cudaError_t)se, "ray sort launch");
+    l.rays = sorted;
+    l.order = order;
+  }
   int e = mesh ? vmr::launch_trace_mesh(*mesh, l) : vmr::launch_trace_scene(ctx->top.dtop, l);
   if (e != 0) return cuda_fail(ctx, (cudaError_t)e, "trace kernel launch");
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
@@ -392,7 +422,7 @@ const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
   if (!ctx || !t) return VMR_ERR_INVALID;
-  if (t->kernel < 0 || t->kernel > 7) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 7]");
+  if (t->kernel < 0 || t->kernel > 15) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 15]");
   if (t->block != 0 && (t->block < 32 || t->block > 256 || t->block % 32 != 0))
     return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
   if (t->blocks_per_sm < 0 || t->refill_min < 0 || t->refill_min > 32)

@@ -106,13 +106,25 @@ enum DeviceStatus : int {
 
 constexpr int kStackCapacity = 90;  // RenderTask.Traversal.Stack (core/ray.go:158)
 
-// Traversal kernel variants (vmr_tuning.kernel).
-enum TraceKernel : int { kKernelScheduled = 0, kKernelWhileWhile = 1, kKernelPrefetch = 2, kKernelRegCap = 4 };
+// Traversal kernel variants (vmr_tuning.kernel bits).
+enum TraceKernel : int {
+  kKernelScheduled = 0,
+  kKernelWhileWhile = 1,
+  kKernelPrefetch = 2,
+  kKernelRegCap = 4,
+  kKernelSort = 8,
+};
+
+// Ray reordering (raysort.cu): 6 permutation classes x 16^3 origin cells.
+constexpr int kSortCells = 4096;
+constexpr int kSortBuckets = 6 * kSortCells;
+constexpr uint64_t kSortMinRays = 1u << 16;  // smaller batches are traced unsorted
 
 // Launch entry points (traverse.cu).
 struct TraceLaunch {
   RaySoA rays;
   HitSoA hits;
+  const uint32_t* order;  // rays[i] is input ray order[i] (nullptr: identity)
   uint64_t n;
   int any_hit;
   int count;
@@ -124,6 +136,8 @@ struct TraceLaunch {
   void* stream;
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);
+int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], uint32_t* keys, uint32_t* hist,
+                    uint32_t* order, const RaySoA& sorted_out, void* stream);
 int launch_trace_scene(const DTop& top, const TraceLaunch& l);
 int device_sm_count();
 

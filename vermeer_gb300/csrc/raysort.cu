@@ -1,0 +1,134 @@
+// raysort.cu - ray reordering before traversal.
+//
+// Each ray gets the key  class * 4096 + morton12(origin),  where class =
+// 2*Kz + (D[Kz] < 0) is the permutation the watertight test uses (Ray.Setup,
+// core/ray.go:103-135) and morton12 interleaves a 16^3 grid cell of the
+// origin inside the scene bounds.  A one-pass bucket sort (histogram,
+// exclusive scan, scatter) gathers the rays into key order: warps then trace
+// rays that start close together and head into the same sixth of the
+// sphere, and the triangle test can use one compile-time permutation per
+// warp.  Order inside a bucket is whatever the atomics give; every ray is
+// traced independently, so results do not depend on it.
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace vmr {
+namespace {
+
+__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // abcd -> a..b..c..d
+  v &= 15u;
+  v = (v | (v << 4)) & 0x0c3u;
+  v = (v | (v << 2)) & 0x249u;
+  return v;
+}
+
+__device__ __forceinline__ uint32_t cell(float p, float lo, float inv) {
+  const float q = fminf(fmaxf((p - lo) * inv, 0.0f), 15.0f);  // NaN -> 0
+  return (uint32_t)q;
+}
+
+// The permutation class of Ray.Setup: Kz chosen by the strict |D|
+// comparisons, and whether Kx/Ky were swapped because D[Kz] < 0.
+__device__ __forceinline__ uint32_t ray_class(float dx, float dy, float dz) {
+  const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+  int kz = 0;
+  if (ay > az) {
+    if (ay > ax) kz = 1;
+  } else {
+    if (az > ax) kz = 2;
+  }
+  const float dkz = kz == 0 ? dx : (kz == 1 ? dy : dz);
+  return 2u * (uint32_t)kz + (dkz < 0.0f ? 1u : 0u);
+}
+
+__global__ void k_ray_keys(RaySoA rays, uint64_t n, float3 lo, float3 inv, uint32_t* keys, uint32_t* hist) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = ray_class(rays.dx[i], rays.dy[i], rays.dz[i]);
+    const uint32_t m = spread4(cell(rays.px[i], lo.x, inv.x)) << 2 | spread4(cell(rays.py[i], lo.y, inv.y)) << 1 |
+                       spread4(cell(rays.pz[i], lo.z, inv.z));
+    const uint32_t k = c * kSortCells + m;
+    keys[i] = k;
+    atomicAdd(hist + k, 1u);
+  }
+}
+
+// Exclusive scan of kSortBuckets counters in one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* hist) {
+  constexpr int kPer = (kSortBuckets + 1023) / 1024;
+  __shared__ uint32_t part[1024];
+  const int t = threadIdx.x;
+  uint32_t local[kPer];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int b = t * kPer + j;
+    local[j] = b < kSortBuckets ? hist[b] : 0u;
+    sum += local[j];
+  }
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const uint32_t v = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - sum;  // exclusive prefix of this thread's range
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int b = t * kPer + j;
+    if (b < kSortBuckets) hist[b] = run;
+    run += local[j];
+  }
+}
+
+__global__ void k_ray_scatter(RaySoA rays, uint64_t n, const uint32_t* keys, uint32_t* offsets, uint32_t* order,
+                              RaySoA sorted_out) {
+  float* px = const_cast<float*>(sorted_out.px);
+  float* py = const_cast<float*>(sorted_out.py);
+  float* pz = const_cast<float*>(sorted_out.pz);
+  float* dx = const_cast<float*>(sorted_out.dx);
+  float* dy = const_cast<float*>(sorted_out.dy);
+  float* dz = const_cast<float*>(sorted_out.dz);
+  float* tm = const_cast<float*>(sorted_out.tmax);
+  float* ti = const_cast<float*>(sorted_out.time);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t pos = atomicAdd(offsets + keys[i], 1u);
+    order[pos] = (uint32_t)i;
+    px[pos] = rays.px[i];
+    py[pos] = rays.py[i];
+    pz[pos] = rays.pz[i];
+    dx[pos] = rays.dx[i];
+    dy[pos] = rays.dy[i];
+    dz[pos] = rays.dz[i];
+    tm[pos] = rays.tmax[i];
+    if (ti) ti[pos] = rays.time ? rays.time[i] : 0.0f;
+  }
+}
+
+}  // namespace
+
+int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], uint32_t* keys, uint32_t* hist,
+                    uint32_t* order, const RaySoA& sorted_out, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  float3 lo = make_float3(bounds[0], bounds[1], bounds[2]);
+  float3 inv;
+  const float ext[3] = {bounds[3] - bounds[0], bounds[4] - bounds[1], bounds[5] - bounds[2]};
+  inv.x = ext[0] > 0.f ? 16.0f / ext[0] : 0.f;
+  inv.y = ext[1] > 0.f ? 16.0f / ext[1] : 0.f;
+  inv.z = ext[2] > 0.f ? 16.0f / ext[2] : 0.f;
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * kSortBuckets, s);
+  if (e != cudaSuccess) return (int)e;
+  const int block = 256;
+  int grid = (int)((n + block - 1) / block);
+  const int cap = device_sm_count() * 16;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  k_ray_keys<<<grid, block, 0, s>>>(rays, n, lo, inv, keys, hist);
+  k_bucket_scan<<<1, 1024, 0, s>>>(hist);
+  k_ray_scatter<<<grid, block, 0, s>>>(rays, n, keys, hist, order, sorted_out);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace vmr

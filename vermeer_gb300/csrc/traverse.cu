@@ -45,6 +45,7 @@ struct TRay {
   float pkx, pky, pkz;  // P[Kx], P[Ky], P[Kz]
   int kx, ky, kz;
   unsigned oct;         // bit k set when D[k] < 0
+  int cls;              // 2*Kz + (D[Kz] < 0): selects (Kx, Ky, Kz)
   bool exact;           // a NaN can arise in the slab test
   float time;
 };
@@ -64,6 +65,7 @@ __device__ __forceinline__ void ray_setup(TRay& r) {
   float dkz = pick3(r.dx, r.dy, r.dz, kz);
   if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
   r.kx = kx; r.ky = ky; r.kz = kz;
+  r.cls = 2 * kz + (dkz < 0.0f ? 1 : 0);
   r.s2 = __frcp_rn(dkz);
   r.s0 = __fdiv_rn(pick3(r.dx, r.dy, r.dz, kx), dkz);
   r.s1 = __fdiv_rn(pick3(r.dx, r.dy, r.dz, ky), dkz);
@@ -142,20 +144,43 @@ struct HitRec {
   float u, v, w;
 };
 
+// Component k of a vertex: compile-time for a known permutation class,
+// selected at run time otherwise (C < 0).
+template <int C>
+struct Perm {
+  static constexpr int KZ = C >> 1;
+  static constexpr int KX0 = (KZ + 1) % 3;
+  static constexpr int KY0 = (KX0 + 1) % 3;
+  static constexpr int KX = (C & 1) ? KY0 : KX0;
+  static constexpr int KY = (C & 1) ? KX0 : KY0;
+};
+template <int K>
+__device__ __forceinline__ float comp(const float4& v) {
+  return K == 0 ? v.x : (K == 1 ? v.y : v.z);
+}
+template <int C, int AXIS>  // AXIS: 0 = Kx, 1 = Ky, 2 = Kz
+__device__ __forceinline__ float kcomp(const TRay& r, const float4& v) {
+  if constexpr (C >= 0) {
+    return comp<AXIS == 0 ? Perm<C>::KX : (AXIS == 1 ? Perm<C>::KY : Perm<C>::KZ)>(v);
+  } else {
+    return pick3(v.x, v.y, v.z, AXIS == 0 ? r.kx : (AXIS == 1 ? r.ky : r.kz));
+  }
+}
+
 // The watertight test (trace.go:123-193).  STRICT: static idxp path
 // (xT < lower*xdet); otherwise the motion path (xT <= lower*xdet).
-template <bool STRICT>
+template <bool STRICT, int C = -1>
 __device__ __forceinline__ bool tri_test(TRay& r, float4 v0, float4 v1, float4 v2, float lower, float& U,
                                          float& V, float& W) {
-  const float AKz = __fsub_rn(pick3(v0.x, v0.y, v0.z, r.kz), r.pkz);
-  const float BKz = __fsub_rn(pick3(v1.x, v1.y, v1.z, r.kz), r.pkz);
-  const float CKz = __fsub_rn(pick3(v2.x, v2.y, v2.z, r.kz), r.pkz);
-  const float Cx = __fsub_rn(__fsub_rn(pick3(v2.x, v2.y, v2.z, r.kx), r.pkx), __fmul_rn(r.s0, CKz));
-  const float By = __fsub_rn(__fsub_rn(pick3(v1.x, v1.y, v1.z, r.ky), r.pky), __fmul_rn(r.s1, BKz));
-  const float Cy = __fsub_rn(__fsub_rn(pick3(v2.x, v2.y, v2.z, r.ky), r.pky), __fmul_rn(r.s1, CKz));
-  const float Bx = __fsub_rn(__fsub_rn(pick3(v1.x, v1.y, v1.z, r.kx), r.pkx), __fmul_rn(r.s0, BKz));
-  const float Ax = __fsub_rn(__fsub_rn(pick3(v0.x, v0.y, v0.z, r.kx), r.pkx), __fmul_rn(r.s0, AKz));
-  const float Ay = __fsub_rn(__fsub_rn(pick3(v0.x, v0.y, v0.z, r.ky), r.pky), __fmul_rn(r.s1, AKz));
+  const float AKz = __fsub_rn(kcomp<C, 2>(r, v0), r.pkz);
+  const float BKz = __fsub_rn(kcomp<C, 2>(r, v1), r.pkz);
+  const float CKz = __fsub_rn(kcomp<C, 2>(r, v2), r.pkz);
+  const float Cx = __fsub_rn(__fsub_rn(kcomp<C, 0>(r, v2), r.pkx), __fmul_rn(r.s0, CKz));
+  const float By = __fsub_rn(__fsub_rn(kcomp<C, 1>(r, v1), r.pky), __fmul_rn(r.s1, BKz));
+  const float Cy = __fsub_rn(__fsub_rn(kcomp<C, 1>(r, v2), r.pky), __fmul_rn(r.s1, CKz));
+  const float Bx = __fsub_rn(__fsub_rn(kcomp<C, 0>(r, v1), r.pkx), __fmul_rn(r.s0, BKz));
+  const float Ax = __fsub_rn(__fsub_rn(kcomp<C, 0>(r, v0), r.pkx), __fmul_rn(r.s0, AKz));
+  const float Ay = __fsub_rn(__fsub_rn(kcomp<C, 1>(r, v0), r.pky), __fmul_rn(r.s1, AKz));
   float fU = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
   float fV = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
   float fW = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
@@ -649,9 +674,61 @@ __device__ __forceinline__ bool push_ranked(int2* stk, int& sp, unsigned mask, c
   return true;
 }
 
+// One leaf of TraceElems / TraceMotionElems: triangles [first, first+count)
+// in order; returns the position of the last accepted triangle or -1.
+template <bool MOTION, int C>
+__device__ __forceinline__ int32_t leaf_scan(const DMesh& m, TRay& r, uint32_t first, uint32_t count,
+                                             const float4* tr0, const float4* tr1, float tm, float omt, float& U,
+                                             float& V, float& W) {
+  int32_t idx = -1;
+  for (uint32_t i = first; i < first + count; ++i) {
+    if (MOTION) {
+      float4 a[3], c[3], v[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        a[j] = __ldg(tr0 + 3 * (size_t)i + j);
+        c[j] = __ldg(tr1 + 3 * (size_t)i + j);
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j)  // Vec3Lerp (math/vec3.go:52-58)
+        v[j] = make_float4(__fadd_rn(__fmul_rn(omt, a[j].x), __fmul_rn(tm, c[j].x)),
+                           __fadd_rn(__fmul_rn(omt, a[j].y), __fmul_rn(tm, c[j].y)),
+                           __fadd_rn(__fmul_rn(omt, a[j].z), __fmul_rn(tm, c[j].z)), 0.f);
+      if (tri_test<false, C>(r, v[0], v[1], v[2], m.ray_bias, U, V, W)) idx = (int32_t)i;
+    } else {
+      const float4 v0 = __ldg(tr0 + 3 * (size_t)i);
+      const float4 v1 = __ldg(tr0 + 3 * (size_t)i + 1);
+      const float4 v2 = __ldg(tr0 + 3 * (size_t)i + 2);
+      if (tri_test<true, C>(r, v0, v1, v2, m.lower_static, U, V, W)) idx = (int32_t)i;
+    }
+  }
+  return idx;
+}
+
+// Warp-uniform permutation class -> the compile-time instance; mixed warps
+// take the run-time-select instance.  Both compute the same bits.
+template <bool MOTION>
+__device__ __forceinline__ int32_t leaf_scan_dispatch(const DMesh& m, TRay& r, uint32_t first, uint32_t count,
+                                                      const float4* tr0, const float4* tr1, float tm, float omt,
+                                                      float& U, float& V, float& W) {
+  const unsigned act = __activemask();
+  const int c0 = __shfl_sync(act, r.cls, __ffs(act) - 1);
+  if (__all_sync(act, r.cls == c0)) {
+    switch (c0) {
+      case 0: return leaf_scan<MOTION, 0>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+      case 1: return leaf_scan<MOTION, 1>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+      case 2: return leaf_scan<MOTION, 2>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+      case 3: return leaf_scan<MOTION, 3>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+      case 4: return leaf_scan<MOTION, 4>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+      default: return leaf_scan<MOTION, 5>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+    }
+  }
+  return leaf_scan<MOTION, -1>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+}
+
 template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
-    k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch) {
+    k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order) {
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
@@ -685,7 +762,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
       if (!alive) {
         const uint64_t i = base + __popc(need & lanes_below);
         if (i < n) {
-          rid = i;
+          rid = order ? (uint64_t)__ldg(order + i) : i;
           load_ray(rays, i, r);
           h = HitRec{-1, -1, 0.f, 0.f, 0.f};
           hit = false;
@@ -771,35 +848,8 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         uint32_t first, count;
         leaf_decode(node, first, count);
         if (COUNT) { cnt.leafs++; cnt.tris += count; }
-        int32_t idx = -1;
         float U = 0.f, V = 0.f, W = 0.f;
-        for (uint32_t i = first; i < first + count; ++i) {
-          float4 v0, v1, v2;
-          if (MOTION) {
-            float4 a[3], c[3];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-              a[j] = __ldg(tr0 + 3 * (size_t)i + j);
-              c[j] = __ldg(tr1 + 3 * (size_t)i + j);
-            }
-            // Vec3Lerp (math/vec3.go:52-58)
-            v0 = make_float4(__fadd_rn(__fmul_rn(omt, a[0].x), __fmul_rn(tm, c[0].x)),
-                             __fadd_rn(__fmul_rn(omt, a[0].y), __fmul_rn(tm, c[0].y)),
-                             __fadd_rn(__fmul_rn(omt, a[0].z), __fmul_rn(tm, c[0].z)), 0.f);
-            v1 = make_float4(__fadd_rn(__fmul_rn(omt, a[1].x), __fmul_rn(tm, c[1].x)),
-                             __fadd_rn(__fmul_rn(omt, a[1].y), __fmul_rn(tm, c[1].y)),
-                             __fadd_rn(__fmul_rn(omt, a[1].z), __fmul_rn(tm, c[1].z)), 0.f);
-            v2 = make_float4(__fadd_rn(__fmul_rn(omt, a[2].x), __fmul_rn(tm, c[2].x)),
-                             __fadd_rn(__fmul_rn(omt, a[2].y), __fmul_rn(tm, c[2].y)),
-                             __fadd_rn(__fmul_rn(omt, a[2].z), __fmul_rn(tm, c[2].z)), 0.f);
-            if (tri_test<false>(r, v0, v1, v2, m.ray_bias, U, V, W)) idx = (int32_t)i;
-          } else {
-            v0 = __ldg(tr0 + 3 * (size_t)i);
-            v1 = __ldg(tr0 + 3 * (size_t)i + 1);
-            v2 = __ldg(tr0 + 3 * (size_t)i + 2);
-            if (tri_test<true>(r, v0, v1, v2, m.lower_static, U, V, W)) idx = (int32_t)i;
-          }
-        }
+        const int32_t idx = leaf_scan_dispatch<MOTION>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
         if (idx != -1) {
           h.elem = MOTION ? __ldg(m.elem + idx) : idx;
           h.u = U;
@@ -865,7 +915,7 @@ __device__ __forceinline__ bool test_tri(const DMesh& m, TRay& r, uint32_t i, co
 
 template <bool MOTION, bool ANY, bool COUNT, bool PF>
 __global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n,
-                                                          DScratch* scratch, int refill_min) {
+                                                          DScratch* scratch, int refill_min, const uint32_t* order) {
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
@@ -900,7 +950,7 @@ __global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA 
       if (state == kIdle) {
         const uint64_t i = base + __popc(idle & lanes_below);
         if (i < n) {
-          rid = i;
+          rid = order ? (uint64_t)__ldg(order + i) : i;
           load_ray(rays, i, r);
           h = HitRec{-1, -1, 0.f, 0.f, 0.f};
           hit = false;
@@ -1044,17 +1094,17 @@ int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
   if (v & kKernelWhileWhile) {
     if (v & kKernelRegCap) {
       if (v & kKernelPrefetch)
-        return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch);
-      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch);
+        return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
+      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
     }
     if (v & kKernelPrefetch)
-      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch);
-    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch);
+      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
+    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
   }
   const int refill = l.refill_min > 0 ? l.refill_min : 4;
   if (v & kKernelPrefetch)
-    return launch_persistent(k_trace_mesh_sched<MOTION, ANY, COUNT, true>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, refill);
-  return launch_persistent(k_trace_mesh_sched<MOTION, ANY, COUNT, false>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, refill);
+    return launch_persistent(k_trace_mesh_sched<MOTION, ANY, COUNT, true>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, refill, l.order);
+  return launch_persistent(k_trace_mesh_sched<MOTION, ANY, COUNT, false>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, refill, l.order);
 }
 
 template <bool MOTION>
