@@ -729,13 +729,20 @@ __device__ __forceinline__ int32_t leaf_scan_dispatch(const DMesh& m, TRay& r, u
 template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order) {
+  // Speculation changes how many nodes are visited (never the result), so
+  // runs that report the reference's visit counters do not speculate.
+  constexpr bool SPEC = !COUNT;
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
   TRay r;
   HitRec h{-1, -1, 0.f, 0.f, 0.f};
-  int node = 0, sp = 0;
+  // Current entry (as if just popped); -1 = no entry left.
+  int node = -1, sp = 0;
   float nodeT = 0.f;
+  // Postponed leaf (SPEC): found while other lanes still walk nodes.
+  int pleaf = -1;
+  float pleafT = 0.f;
   uint64_t rid = 0;
   uint32_t iter = 0;
   bool alive = false, hit = false;
@@ -766,8 +773,9 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
           load_ray(rays, i, r);
           h = HitRec{-1, -1, 0.f, 0.f, 0.f};
           hit = false;
-          node = 0;
+          node = 0;  // the root, pushed with T = Tclosest (intersect.go:93-95)
           nodeT = r.tclosest;
+          pleaf = -1;
           sp = 0;
           iter = 0;
           alive = true;
@@ -799,23 +807,28 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     }
     if (alive) {
       bool done = false;
-      // ---- node phase: inner nodes until a leaf or the stack runs dry
+      // ---- node phase: walk inner nodes until the current entry is a leaf
+      // (SPEC: until a second leaf, or every walking lane holds a leaf).
       for (;;) {
+        if (node == -1) break;
         if (++iter > m.iter_cap) { status = kStatusIterationCap; done = true; break; }
         if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
-          if (sp == 0) { done = true; break; }
+          if (sp == 0) { node = -1; break; }
           const int2 e = stk[--sp];
           node = e.x;
           nodeT = __int_as_float(e.y);
           continue;
         }
-        if (node < 0) {  // a leaf: the leaf phase handles it
-          if (PF && !MOTION) {
-            // The lane now waits for the warp's other node walks: fetch
-            // its triangles into L1 meanwhile.
-            uint32_t f, c;
-            leaf_decode(node, f, c);
-            prefetch_leaf(tr0, f, c);
+        if (node < 0) {  // a leaf
+          if (SPEC && pleaf == -1) {
+            pleaf = node;
+            pleafT = nodeT;
+            if (sp == 0) { node = -1; break; }
+            const int2 e = stk[--sp];
+            node = e.x;
+            nodeT = __int_as_float(e.y);
+            if (!__any_sync(__activemask(), pleaf == -1)) break;
+            continue;
           }
           break;
         }
@@ -836,35 +849,61 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         if (push_ranked(stk, sp, mask, ch, tn, rk, next, nextT, status)) {
           node = next;
           nodeT = nextT;
-        } else {
-          if (status != kStatusOk || sp == 0) { done = true; break; }
-          const int2 e = stk[--sp];
-          node = e.x;
-          nodeT = __int_as_float(e.y);
-        }
-      }
-      // ---- leaf phase: TraceElems / TraceMotionElems over [first, first+count)
-      if (!done) {
-        uint32_t first, count;
-        leaf_decode(node, first, count);
-        if (COUNT) { cnt.leafs++; cnt.tris += count; }
-        float U = 0.f, V = 0.f, W = 0.f;
-        const int32_t idx = leaf_scan_dispatch<MOTION>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
-        if (idx != -1) {
-          h.elem = MOTION ? __ldg(m.elem + idx) : idx;
-          h.u = U;
-          h.v = V;
-          h.w = W;
-          hit = true;
-        }
-        if ((ANY && idx != -1) || sp == 0) {
+        } else if (status != kStatusOk) {
           done = true;
+          break;
+        } else if (sp == 0) {
+          node = -1;
+          break;
         } else {
           const int2 e = stk[--sp];
           node = e.x;
           nodeT = __int_as_float(e.y);
-          if (PF && !MOTION && node >= 0) prefetch_l1(m.nodes + node);
         }
+        if (SPEC && !__any_sync(__activemask(), pleaf == -1)) break;
+      }
+      // ---- leaf phase: the postponed leaf, then the current entry if it is
+      // a leaf, in the order the reference pops them.  Each is re-checked
+      // against the current Tclosest first: a leaf met while speculating was
+      // checked against an older, larger Tclosest.
+      if (!done) {
+        const int q0 = pleaf;
+        const float q0T = pleafT;
+        int q1 = -1;
+        float q1T = 0.f;
+        if (node < -1) {  // the current entry is a leaf: take it, pop the next
+          q1 = node;
+          q1T = nodeT;
+          if (sp == 0) {
+            node = -1;
+          } else {
+            const int2 e = stk[--sp];
+            node = e.x;
+            nodeT = __int_as_float(e.y);
+          }
+        }
+        pleaf = -1;
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+          const int L = q == 0 ? q0 : q1;
+          const float LT = q == 0 ? q0T : q1T;
+          if (L == -1 || done || r.tclosest < LT) continue;
+          uint32_t first, count;
+          leaf_decode(L, first, count);
+          if (COUNT) { cnt.leafs++; cnt.tris += count; }
+          float U = 0.f, V = 0.f, W = 0.f;
+          const int32_t idx = leaf_scan_dispatch<MOTION>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+          if (idx != -1) {
+            h.elem = MOTION ? __ldg(m.elem + idx) : idx;
+            h.u = U;
+            h.v = V;
+            h.w = W;
+            hit = true;
+            if (ANY) done = true;  // shadow rays stop at the first hit leaf (intersect.go:231-236)
+          }
+        }
+        if (node == -1) done = true;
+        if (PF && !MOTION && !done && node >= 0) prefetch_l1(m.nodes + node);
       }
       if (done) {
         store_hit(hits, rid, r, hit, h);
