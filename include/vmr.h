@@ -58,14 +58,16 @@ int vmr_sync(vmr_ctx* ctx);
 int vmr_abi_version(void);
 
 /* Launch parameters of the traversal kernels, chosen per scene (by hand or
- * by vmr_autotune).  Results never depend on them: they only change how
- * rays are scheduled onto warps.  Zero fields take the defaults. */
+ * by an autotuner).  Results never depend on them: they only change how
+ * rays are scheduled onto warps.  Zero block/blocks_per_sm/refill_min take
+ * the defaults. */
 typedef struct {
     int kernel;          /* bit 0: while-while (else step-scheduled); bit 1:
                             L1 prefetch of the next leaf/node; bit 2: 64-register
                             cap (while-while only); bit 3: reorder rays by
                             permutation class and origin cell before a mesh
-                            trace of >= 65536 rays */
+                            trace of >= 65536 rays; bit 4: speculative leaf
+                            postponing (while-while).  Default 13. */
     int block;           /* threads per block, multiple of 32, <= 256 (128) */
     int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
     int refill_min;      /* idle lanes that trigger a warp refill, 1..32 (4) */

@@ -113,6 +113,7 @@ enum TraceKernel : int {
   kKernelPrefetch = 2,
   kKernelRegCap = 4,
   kKernelSort = 8,
+  kKernelSpeculate = 16,
 };
 
 // Ray reordering (raysort.cu): 6 permutation classes x 16^3 origin cells.

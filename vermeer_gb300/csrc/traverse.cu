@@ -726,12 +726,12 @@ __device__ __forceinline__ int32_t leaf_scan_dispatch(const DMesh& m, TRay& r, u
   return leaf_scan<MOTION, -1>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
 }
 
-template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB>
+template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB, bool SPEC_>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order) {
   // Speculation changes how many nodes are visited (never the result), so
   // runs that report the reference's visit counters do not speculate.
-  constexpr bool SPEC = !COUNT;
+  constexpr bool SPEC = SPEC_ && !COUNT;
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
@@ -1126,19 +1126,28 @@ int launch_persistent(K k, const TraceLaunch& l, int block, A... args) {
 // tuning.kernel: bit 0 = while-while (else step-scheduled), bit 1 = L1
 // prefetch of the next leaf / node, bit 2 = 64-register cap (while-while,
 // 128 threads, 8 resident blocks).
+// tuning.kernel: bit 0 = while-while (else step-scheduled), bit 1 = L1
+// prefetch of the next leaf / node, bit 2 = 64-register cap (while-while,
+// 128 threads, 8 resident blocks), bit 3 = ray reordering (host side),
+// bit 4 = speculative leaf postponing (while-while).
+template <bool MOTION, bool ANY, bool COUNT, int MINB, bool SPEC>
+int launch_ww(const DMesh& mesh, const TraceLaunch& l, int block) {
+  if (l.kernel & kKernelPrefetch)
+    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, MINB, SPEC>, l, block, mesh, l.rays, l.hits,
+                             l.n, l.scratch, l.order);
+  return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, SPEC>, l, block, mesh, l.rays, l.hits,
+                           l.n, l.scratch, l.order);
+}
+
 template <bool MOTION, bool ANY, bool COUNT>
 int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
   const int block = l.block > 0 ? l.block : 128;
   const int v = l.kernel;
   if (v & kKernelWhileWhile) {
-    if (v & kKernelRegCap) {
-      if (v & kKernelPrefetch)
-        return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
-      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 8>, l, 128, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
-    }
-    if (v & kKernelPrefetch)
-      return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
-    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, 0>, l, block, mesh, l.rays, l.hits, l.n, l.scratch, l.order);
+    const bool spec = (v & kKernelSpeculate) != 0;
+    if (v & kKernelRegCap)
+      return spec ? launch_ww<MOTION, ANY, COUNT, 8, true>(mesh, l, 128) : launch_ww<MOTION, ANY, COUNT, 8, false>(mesh, l, 128);
+    return spec ? launch_ww<MOTION, ANY, COUNT, 0, true>(mesh, l, block) : launch_ww<MOTION, ANY, COUNT, 0, false>(mesh, l, block);
   }
   const int refill = l.refill_min > 0 ? l.refill_min : 4;
   if (v & kKernelPrefetch)
