@@ -675,16 +675,14 @@ __device__ __forceinline__ bool push_ranked(int2* stk, int& sp, unsigned mask, c
 }
 
 // One leaf of TraceElems / TraceMotionElems: triangles [first, first+count)
-// in order; returns the position of the last accepted triangle or -1.  The
-// static path loads triangle i+1 before testing triangle i, so the leaf
-// costs about one memory round trip instead of one per triangle.
+// in order; returns the position of the last accepted triangle or -1.
 template <bool MOTION, int C>
 __device__ __forceinline__ int32_t leaf_scan(const DMesh& m, TRay& r, uint32_t first, uint32_t count,
                                              const float4* tr0, const float4* tr1, float tm, float omt, float& U,
                                              float& V, float& W) {
   int32_t idx = -1;
-  if (MOTION) {
-    for (uint32_t i = first; i < first + count; ++i) {
+  for (uint32_t i = first; i < first + count; ++i) {
+    if (MOTION) {
       float4 a[3], c[3], v[3];
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
@@ -697,20 +695,12 @@ __device__ __forceinline__ int32_t leaf_scan(const DMesh& m, TRay& r, uint32_t f
                            __fadd_rn(__fmul_rn(omt, a[j].y), __fmul_rn(tm, c[j].y)),
                            __fadd_rn(__fmul_rn(omt, a[j].z), __fmul_rn(tm, c[j].z)), 0.f);
       if (tri_test<false, C>(r, v[0], v[1], v[2], m.ray_bias, U, V, W)) idx = (int32_t)i;
+    } else {
+      const float4 v0 = __ldg(tr0 + 3 * (size_t)i);
+      const float4 v1 = __ldg(tr0 + 3 * (size_t)i + 1);
+      const float4 v2 = __ldg(tr0 + 3 * (size_t)i + 2);
+      if (tri_test<true, C>(r, v0, v1, v2, m.lower_static, U, V, W)) idx = (int32_t)i;
     }
-    return idx;
-  }
-  const float4* t = tr0 + 3 * (size_t)first;
-  float4 v0 = __ldg(t), v1 = __ldg(t + 1), v2 = __ldg(t + 2);
-  for (uint32_t k = 0; k < count; ++k) {
-    // The next triangle (the leaf's last one again at the end: a valid
-    // address, never tested).
-    const uint32_t kn = k + 1 < count ? k + 1 : k;
-    const float4 n0 = __ldg(t + 3 * kn), n1 = __ldg(t + 3 * kn + 1), n2 = __ldg(t + 3 * kn + 2);
-    if (tri_test<true, C>(r, v0, v1, v2, m.lower_static, U, V, W)) idx = (int32_t)(first + k);
-    v0 = n0;
-    v1 = n1;
-    v2 = n2;
   }
   return idx;
 }
