@@ -801,7 +801,8 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         }
       }
     }
-    if (!__any_sync(kFull, alive)) {
+    const unsigned alive_mask = __ballot_sync(kFull, alive);
+    if (alive_mask == 0u) {
       if (!more) break;
       continue;
     }
@@ -862,6 +863,10 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         }
         if (SPEC && !__any_sync(__activemask(), pleaf == -1)) break;
       }
+      // Lanes leave the node walk at different times; reconverge them so
+      // the leaf scans below run as one pass over the warp, not one pass
+      // per group of lanes that happened to exit together.
+      __syncwarp(alive_mask);
       // ---- leaf phase: the postponed leaf, then the current entry if it is
       // a leaf, in the order the reference pops them.  Each is re-checked
       // against the current Tclosest first: a leaf met while speculating was
