@@ -63,14 +63,17 @@ int vmr_abi_version(void);
  * the defaults. */
 typedef struct {
     int kernel;          /* bit 0: while-while (else step-scheduled); bit 1:
-                            L1 prefetch of the next leaf/node; bit 2: 64-register
+                            L1 prefetch of the next node; bit 2: 64-register
                             cap (while-while only); bit 3: reorder rays by
                             permutation class and origin cell before a mesh
-                            trace of >= 65536 rays; bit 4: speculative leaf
-                            postponing (while-while).  Default 13. */
+                            trace of >= 65536 rays.  Default 13. */
     int block;           /* threads per block, multiple of 32, <= 256 (128) */
     int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
-    int refill_min;      /* idle lanes that trigger a warp refill, 1..32 (4) */
+    int refill_min;      /* step-scheduled: idle lanes that trigger a warp
+                            refill, 1..32 (4) */
+    int walk_tail;       /* while-while: end a node walk early once at most
+                            this many lanes still walk and a lane holds a
+                            leaf, 0..31 (0 = wait for every lane) */
 } vmr_tuning;
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* tuning);
 int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* tuning);

@@ -139,7 +139,7 @@ def test_full_size_soup_parity(ctx, orc):
 
 
 @pytest.mark.parametrize("tuning", [(0, 0, 0, 0), (1, 0, 0, 0), (3, 0, 0, 0), (5, 0, 0, 0), (8, 0, 0, 4),
-                                    (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0), (25, 0, 0, 0), (29, 0, 0, 0)])
+                                    (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0), (13, 0, 0, 0, 4), (9, 0, 0, 0, 12)])
 def test_every_tuning_is_bit_exact(ctx, orc, tuning):
     """Launch parameters (kernel variant, ray reordering, block size,
     resident blocks) only change scheduling: hits stay bit-exact."""

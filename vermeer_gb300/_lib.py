@@ -45,7 +45,7 @@ class Hits(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("kernel", ctypes.c_int), ("block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("refill_min", ctypes.c_int)]
+                ("refill_min", ctypes.c_int), ("walk_tail", ctypes.c_int)]
 
 
 class TraceStats(ctypes.Structure):

@@ -74,15 +74,17 @@ class Context:
     def sync(self):
         self._check(self.L.vmr_sync(self.h))
 
-    def set_tuning(self, kernel: int = 0, block: int = 0, blocks_per_sm: int = 0, refill_min: int = 0):
+    def set_tuning(self, kernel: int = 13, block: int = 0, blocks_per_sm: int = 0, refill_min: int = 0,
+                   walk_tail: int = 0):
         """Launch parameters of the traversal kernels (vmr_set_tuning)."""
-        t = _lib.Tuning(kernel, block, blocks_per_sm, refill_min)
+        t = _lib.Tuning(kernel, block, blocks_per_sm, refill_min, walk_tail)
         self._check(self.L.vmr_set_tuning(self.h, ctypes.byref(t)))
 
     def get_tuning(self):
         t = _lib.Tuning()
         self._check(self.L.vmr_get_tuning(self.h, ctypes.byref(t)))
-        return dict(kernel=t.kernel, block=t.block, blocks_per_sm=t.blocks_per_sm, refill_min=t.refill_min)
+        return dict(kernel=t.kernel, block=t.block, blocks_per_sm=t.blocks_per_sm, refill_min=t.refill_min,
+                    walk_tail=t.walk_tail)
 
     # ------------------------------------------------------------ meshes
     def mesh_build(self, verts, idxp, keys: int = 1, ray_bias: float = 0.0, motion_mode: int = MOTION_FAITHFUL,

@@ -70,7 +70,7 @@ struct vmr_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
-  vmr_tuning tuning{13, 0, 0, 0};
+  vmr_tuning tuning{13, 0, 0, 0, 0};
   // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
   const float* mesh_bounds_of(const DMesh* d) const {
     for (const auto& m : meshes)
@@ -306,6 +306,7 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   l.block = ctx->tuning.block;
   l.grid = ctx->tuning.blocks_per_sm;
   l.refill_min = ctx->tuning.refill_min;
+  l.walk_tail = ctx->tuning.walk_tail;
   VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   if (mesh && (ctx->tuning.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
@@ -422,7 +423,8 @@ const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
   if (!ctx || !t) return VMR_ERR_INVALID;
-  if (t->kernel < 0 || t->kernel > 31) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 31]");
+  if (t->kernel < 0 || t->kernel > 15) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 15]");
+  if (t->walk_tail < 0 || t->walk_tail > 31) return fail(ctx, VMR_ERR_INVALID, "tuning.walk_tail must be in [0, 31]");
   if (t->block != 0 && (t->block < 32 || t->block > 256 || t->block % 32 != 0))
     return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
   if (t->blocks_per_sm < 0 || t->refill_min < 0 || t->refill_min > 32)

@@ -113,7 +113,6 @@ enum TraceKernel : int {
   kKernelPrefetch = 2,
   kKernelRegCap = 4,
   kKernelSort = 8,
-  kKernelSpeculate = 16,
 };
 
 // Ray reordering (raysort.cu): 6 permutation classes x 16^3 origin cells.
@@ -134,6 +133,7 @@ struct TraceLaunch {
   int block;
   int kernel;
   int refill_min;
+  int walk_tail;
   void* stream;
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);

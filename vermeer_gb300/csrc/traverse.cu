@@ -726,12 +726,10 @@ __device__ __forceinline__ int32_t leaf_scan_dispatch(const DMesh& m, TRay& r, u
   return leaf_scan<MOTION, -1>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
 }
 
-template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB, bool SPEC_>
+template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
-    k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order) {
-  // Speculation changes how many nodes are visited (never the result), so
-  // runs that report the reference's visit counters do not speculate.
-  constexpr bool SPEC = SPEC_ && !COUNT;
+    k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order,
+                    int walk_tail) {
   int2 stk[kStackCapacity];
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
@@ -740,9 +738,6 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
   // Current entry (as if just popped); -1 = no entry left.
   int node = -1, sp = 0;
   float nodeT = 0.f;
-  // Postponed leaf (SPEC): found while other lanes still walk nodes.
-  int pleaf = -1;
-  float pleafT = 0.f;
   uint64_t rid = 0;
   uint32_t iter = 0;
   bool alive = false, hit = false;
@@ -775,7 +770,6 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
           hit = false;
           node = 0;  // the root, pushed with T = Tclosest (intersect.go:93-95)
           nodeT = r.tclosest;
-          pleaf = -1;
           sp = 0;
           iter = 0;
           alive = true;
@@ -808,30 +802,40 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     }
     if (alive) {
       bool done = false;
-      // ---- node phase: walk inner nodes until the current entry is a leaf
-      // (SPEC: until a second leaf, or every walking lane holds a leaf).
+      // ---- node phase: one entry per step (a cull-pop, a leaf found, or an
+      // inner-node visit) for every lane still walking.  The warp steps in
+      // lock-step; it stops when no lane walks, or when at most walk_tail
+      // lanes walk and some lane holds a leaf (the stragglers resume in the
+      // next node phase).
+      bool walking = node != -1;
       for (;;) {
-        if (node == -1) break;
-        if (++iter > m.iter_cap) { status = kStatusIterationCap; done = true; break; }
-        if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
-          if (sp == 0) { node = -1; break; }
-          const int2 e = stk[--sp];
-          node = e.x;
-          nodeT = __int_as_float(e.y);
+        const unsigned wmask = __ballot_sync(alive_mask, walking);
+        if (wmask == 0u) break;
+        if (walk_tail > 0 && __popc(wmask) <= walk_tail) {
+          const unsigned leafy = __ballot_sync(alive_mask, !walking && node < -1);
+          if (leafy != 0u) break;
+        }
+        if (!walking) continue;
+        if (++iter > m.iter_cap) {
+          status = kStatusIterationCap;
+          done = true;
+          walking = false;
           continue;
         }
-        if (node < 0) {  // a leaf
-          if (SPEC && pleaf == -1) {
-            pleaf = node;
-            pleafT = nodeT;
-            if (sp == 0) { node = -1; break; }
+        if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
+          if (sp == 0) {
+            node = -1;
+            walking = false;
+          } else {
             const int2 e = stk[--sp];
             node = e.x;
             nodeT = __int_as_float(e.y);
-            if (!__any_sync(__activemask(), pleaf == -1)) break;
-            continue;
           }
-          break;
+          continue;
+        }
+        if (node < 0) {  // a leaf: the leaf phase scans it
+          walking = false;
+          continue;
         }
         if (COUNT) cnt.nodes++;
         float4 b[6];
@@ -852,64 +856,41 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
           nodeT = nextT;
         } else if (status != kStatusOk) {
           done = true;
-          break;
+          walking = false;
         } else if (sp == 0) {
           node = -1;
-          break;
+          walking = false;
         } else {
           const int2 e = stk[--sp];
           node = e.x;
           nodeT = __int_as_float(e.y);
         }
-        if (SPEC && !__any_sync(__activemask(), pleaf == -1)) break;
       }
-      // Lanes leave the node walk at different times; reconverge them so
-      // the leaf scans below run as one pass over the warp, not one pass
-      // per group of lanes that happened to exit together.
-      __syncwarp(alive_mask);
-      // ---- leaf phase: the postponed leaf, then the current entry if it is
-      // a leaf, in the order the reference pops them.  Each is re-checked
-      // against the current Tclosest first: a leaf met while speculating was
-      // checked against an older, larger Tclosest.
-      if (!done) {
-        const int q0 = pleaf;
-        const float q0T = pleafT;
-        int q1 = -1;
-        float q1T = 0.f;
-        if (node < -1) {  // the current entry is a leaf: take it, pop the next
-          q1 = node;
-          q1T = nodeT;
-          if (sp == 0) {
-            node = -1;
-          } else {
-            const int2 e = stk[--sp];
-            node = e.x;
-            nodeT = __int_as_float(e.y);
-          }
+      // ---- leaf phase: lanes whose current entry is a leaf scan it, in the
+      // order the reference pops it, then pop the next entry.
+      if (!done && !walking && node < -1) {
+        uint32_t first, count;
+        leaf_decode(node, first, count);
+        if (COUNT) { cnt.leafs++; cnt.tris += count; }
+        float U = 0.f, V = 0.f, W = 0.f;
+        const int32_t idx = leaf_scan_dispatch<MOTION>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
+        if (idx != -1) {
+          h.elem = MOTION ? __ldg(m.elem + idx) : idx;
+          h.u = U;
+          h.v = V;
+          h.w = W;
+          hit = true;
         }
-        pleaf = -1;
-#pragma unroll 1
-        for (int q = 0; q < 2; ++q) {
-          const int L = q == 0 ? q0 : q1;
-          const float LT = q == 0 ? q0T : q1T;
-          if (L == -1 || done || r.tclosest < LT) continue;
-          uint32_t first, count;
-          leaf_decode(L, first, count);
-          if (COUNT) { cnt.leafs++; cnt.tris += count; }
-          float U = 0.f, V = 0.f, W = 0.f;
-          const int32_t idx = leaf_scan_dispatch<MOTION>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
-          if (idx != -1) {
-            h.elem = MOTION ? __ldg(m.elem + idx) : idx;
-            h.u = U;
-            h.v = V;
-            h.w = W;
-            hit = true;
-            if (ANY) done = true;  // shadow rays stop at the first hit leaf (intersect.go:231-236)
-          }
+        if ((ANY && idx != -1) || sp == 0) {  // shadow rays stop at the first hit leaf (intersect.go:231-236)
+          done = true;
+        } else {
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+          if (PF && !MOTION && node >= 0) prefetch_l1(m.nodes + node);
         }
-        if (node == -1) done = true;
-        if (PF && !MOTION && !done && node >= 0) prefetch_l1(m.nodes + node);
       }
+      if (!walking && node == -1) done = true;
       if (done) {
         store_hit(hits, rid, r, hit, h);
         alive = false;
@@ -1129,19 +1110,16 @@ int launch_persistent(K k, const TraceLaunch& l, int block, A... args) {
 }
 
 // tuning.kernel: bit 0 = while-while (else step-scheduled), bit 1 = L1
-// prefetch of the next leaf / node, bit 2 = 64-register cap (while-while,
-// 128 threads, 8 resident blocks).
-// tuning.kernel: bit 0 = while-while (else step-scheduled), bit 1 = L1
-// prefetch of the next leaf / node, bit 2 = 64-register cap (while-while,
-// 128 threads, 8 resident blocks), bit 3 = ray reordering (host side),
-// bit 4 = speculative leaf postponing (while-while).
-template <bool MOTION, bool ANY, bool COUNT, int MINB, bool SPEC>
+// prefetch of the next node, bit 2 = 64-register cap (while-while, 128
+// threads, 8 resident blocks), bit 3 = ray reordering (host side).
+template <bool MOTION, bool ANY, bool COUNT, int MINB>
 int launch_ww(const DMesh& mesh, const TraceLaunch& l, int block) {
+  const int tail = l.walk_tail;
   if (l.kernel & kKernelPrefetch)
-    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, MINB, SPEC>, l, block, mesh, l.rays, l.hits,
-                             l.n, l.scratch, l.order);
-  return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, SPEC>, l, block, mesh, l.rays, l.hits,
-                           l.n, l.scratch, l.order);
+    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, MINB>, l, block, mesh, l.rays, l.hits, l.n,
+                             l.scratch, l.order, tail);
+  return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB>, l, block, mesh, l.rays, l.hits, l.n,
+                           l.scratch, l.order, tail);
 }
 
 template <bool MOTION, bool ANY, bool COUNT>
@@ -1149,10 +1127,8 @@ int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
   const int block = l.block > 0 ? l.block : 128;
   const int v = l.kernel;
   if (v & kKernelWhileWhile) {
-    const bool spec = (v & kKernelSpeculate) != 0;
-    if (v & kKernelRegCap)
-      return spec ? launch_ww<MOTION, ANY, COUNT, 8, true>(mesh, l, 128) : launch_ww<MOTION, ANY, COUNT, 8, false>(mesh, l, 128);
-    return spec ? launch_ww<MOTION, ANY, COUNT, 0, true>(mesh, l, block) : launch_ww<MOTION, ANY, COUNT, 0, false>(mesh, l, block);
+    if (v & kKernelRegCap) return launch_ww<MOTION, ANY, COUNT, 8>(mesh, l, 128);
+    return launch_ww<MOTION, ANY, COUNT, 0>(mesh, l, block);
   }
   const int refill = l.refill_min > 0 ? l.refill_min : 4;
   if (v & kKernelPrefetch)
