@@ -73,7 +73,7 @@ typedef struct {
                             refill, 1..32 (4) */
     int walk_tail;       /* while-while: end a node walk early once at most
                             this many lanes still walk and a lane holds a
-                            leaf, 0..31 (0 = wait for every lane) */
+                            leaf, 0..31 (default 4; 0 = wait for every lane) */
 } vmr_tuning;
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* tuning);
 int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* tuning);

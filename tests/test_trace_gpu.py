@@ -159,4 +159,4 @@ def test_every_tuning_is_bit_exact(ctx, orc, tuning):
         assert_hits_equal(ctx.trace_mesh(mg, mrays), orc.Mesh(mv, mip, keys=2, motion_fixed=True).trace(mrays),
                           what=f"motion tuning={tuning}")
     finally:
-        ctx.set_tuning(13, 0, 0, 0)
+        ctx.set_tuning(13, 0, 0, 0, 4)

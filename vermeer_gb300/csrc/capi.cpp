@@ -70,7 +70,7 @@ struct vmr_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
-  vmr_tuning tuning{13, 0, 0, 0, 0};
+  vmr_tuning tuning{13, 0, 0, 0, 4};
   // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
   const float* mesh_bounds_of(const DMesh* d) const {
     for (const auto& m : meshes)
