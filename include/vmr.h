@@ -77,6 +77,9 @@ typedef struct {
 } vmr_tuning;
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* tuning);
 int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* tuning);
+/* Device time of the last trace call on ctx: the ray reordering kernels and
+ * the traversal kernel, in milliseconds (waits for the trace to finish). */
+int vmr_trace_timing(vmr_ctx* ctx, float* sort_ms, float* traverse_ms);
 
 /* ------------------------------------------------------------ QBVH nodes */
 /* qbvh.Node (qbvh/qbvh.go:31-36), 128 bytes, identical memory layout:
@@ -205,7 +208,8 @@ typedef struct {
     uint64_t node_visits;    /* Ray.NodesT summed over rays */
     uint64_t leaf_visits;    /* Ray.LeafsT summed over rays */
     uint64_t tri_tests;
-    float kernel_ms;         /* device time of the traversal kernel */
+    float kernel_ms;         /* device time of the traversal kernel (host-pointer
+                                calls; use vmr_trace_timing for device ones) */
 } vmr_trace_stats;
 
 /* Closest-hit / any-hit traversal of one mesh (PolyMesh.Trace without a

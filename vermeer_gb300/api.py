@@ -80,6 +80,12 @@ class Context:
         t = _lib.Tuning(kernel, block, blocks_per_sm, refill_min, walk_tail)
         self._check(self.L.vmr_set_tuning(self.h, ctypes.byref(t)))
 
+    def trace_timing(self):
+        """(sort_ms, traverse_ms) of the last trace call (vmr_trace_timing)."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        self._check(self.L.vmr_trace_timing(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def get_tuning(self):
         t = _lib.Tuning()
         self._check(self.L.vmr_get_tuning(self.h, ctypes.byref(t)))

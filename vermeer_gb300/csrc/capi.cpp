@@ -67,7 +67,7 @@ struct vmr_ctx {
   DevBuf scratch;                 // DScratch
   DevBuf io;                      // rays + hits for host-pointer traces
   DevBuf sortbuf;                 // ray keys, bucket offsets, order, key-ordered rays
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;  // start, after the sort, end
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
   vmr_tuning tuning{13, 0, 0, 0, 4};
@@ -327,6 +327,7 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
     l.rays = sorted;
     l.order = order;
   }
+  VMR_CUDA(ctx, cudaEventRecord(ctx->evm, ctx->stream));
   int e = mesh ? vmr::launch_trace_mesh(*mesh, l) : vmr::launch_trace_scene(ctx->top.dtop, l);
   if (e != 0) return cuda_fail(ctx, (cudaError_t)e, "trace kernel launch");
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
@@ -335,7 +336,7 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   int st = read_status(ctx, stats);
   if (stats) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&ms, ctx->evm, ctx->ev1);
     stats->kernel_ms = ms;
   }
   return st;
@@ -397,6 +398,7 @@ int vmr_create(int device, vmr_ctx** out) {
   ctx->device = device;
   if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+      cudaEventCreate(&ctx->evm) != cudaSuccess ||
       ctx->scratch.ensure(sizeof(DScratch)) != cudaSuccess) {
     delete ctx;
     return VMR_ERR_CUDA;
@@ -413,6 +415,7 @@ int vmr_destroy(vmr_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->evm) cudaEventDestroy(ctx->evm);
   cudaStream_t s = ctx->own_stream;
   delete ctx;
   if (s) cudaStreamDestroy(s);
@@ -436,6 +439,18 @@ int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
 int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* t) {
   if (!ctx || !t) return VMR_ERR_INVALID;
   *t = ctx->tuning;
+  return VMR_OK;
+}
+
+int vmr_trace_timing(vmr_ctx* ctx, float* sort_ms, float* traverse_ms) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, VMR_ERR_UNSUPPORTED, "host-only context");
+  VMR_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+  float a = 0.f, b = 0.f;
+  VMR_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev0, ctx->evm));
+  VMR_CUDA(ctx, cudaEventElapsedTime(&b, ctx->evm, ctx->ev1));
+  if (sort_ms) *sort_ms = a;
+  if (traverse_ms) *traverse_ms = b;
   return VMR_OK;
 }
 
