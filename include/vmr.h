@@ -221,6 +221,27 @@ int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, 
 int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags,
                     const vmr_hits* hits, vmr_trace_stats* stats);
 
+/* -------------------------------------------------------------- no-alloc */
+/* No counterpart in the reference.  For callers that must not have a library
+ * allocate device memory while they run (they manage the whole device
+ * themselves, or cannot afford an allocation's synchronisation in their
+ * loop): the same trace as vmr_trace_mesh with device pointers, but every
+ * scratch buffer (work counter, status word, ray-reordering buffers) lives in
+ * one static device array of about 10 MB, present on every GPU that loads
+ * libvmr until the process exits.  The call allocates nothing.
+ *   - rays and hits are device pointers; at most VMR_NOALLOC_MAX_RAYS rays per
+ *     call (larger batches fail with VMR_ERR_INVALID); flags may hold only
+ *     VMR_TRACE_ANY_HIT and VMR_TRACE_DEVICE;
+ *   - the first call on a device looks up the array's device address, so make
+ *     that first call before any stream capture;
+ *   - all calls share the one array: calls that overlap on the GPU (other
+ *     host threads, other streams, other contexts of the process on the same
+ *     device) race and corrupt each other's results;
+ *   - the call returns when the trace has finished. */
+#define VMR_NOALLOC_MAX_RAYS 262144
+int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags,
+                           const vmr_hits* hits);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,8 @@ SIGNATURES = {
                                       ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
     "vmr_trace_scene": (ctypes.c_int, [P, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                        ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
+    "vmr_trace_mesh_noalloc": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
+                                              ctypes.POINTER(Hits)]),
 }
 
 _lib = None

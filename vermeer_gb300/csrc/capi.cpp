@@ -376,6 +376,22 @@ int trace_host(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays* rays, size_t n, 
 
 }  // namespace
 
+namespace vmr {
+// Read-only view of a context's mesh and settings for vmr_trace_mesh_noalloc
+// (noalloc.cu), which keeps its own scratch and launches the same kernels.
+bool ctx_noalloc_view(vmr_ctx* ctx, uint32_t geom, const DMesh** mesh, const float** bounds, void** stream,
+                      int* device, vmr_tuning* tuning) {
+  if (!ctx || ctx->device < 0 || geom >= ctx->meshes.size()) return false;
+  *mesh = &ctx->meshes[geom]->dmesh;
+  *bounds = ctx->meshes[geom]->bounds6;
+  *stream = ctx->stream;
+  *device = ctx->device;
+  *tuning = ctx->tuning;
+  return ctx->meshes[geom]->host.n_tris > 0;
+}
+int ctx_fail(vmr_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
+}  // namespace vmr
+
 extern "C" {
 
 int vmr_abi_version(void) { return VMR_ABI_VERSION; }
