@@ -221,6 +221,72 @@ int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, 
 int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags,
                     const vmr_hits* hits, vmr_trace_stats* stats);
 
+/* ----------------------------------------------------------------- render */
+/* ShaderStd parameters (builtin/shader/std.go:25-47).  The reference leaves
+ * an unset parameter nil, which changes its default; flags say which are
+ * set.  spec1_fresnel: 0 Dielectric (also the default), 1 Metal. */
+enum {
+    VMR_SH_EMISSION_COLOUR = 1, VMR_SH_EMISSION_STRENGTH = 2,
+    VMR_SH_DIFFUSE_COLOUR = 4, VMR_SH_DIFFUSE_STRENGTH = 8, VMR_SH_DIFFUSE_ROUGHNESS = 16,
+    VMR_SH_SPEC1_COLOUR = 32, VMR_SH_SPEC1_STRENGTH = 64, VMR_SH_SPEC1_ROUGHNESS = 128,
+    VMR_SH_FRESNEL_REFL = 256, VMR_SH_FRESNEL_EDGE = 512, VMR_SH_IOR = 1024
+};
+typedef struct {
+    uint32_t flags;
+    float emission_colour[3], emission_strength;
+    float diffuse_colour[3], diffuse_strength, diffuse_roughness;
+    float spec1_colour[3], spec1_strength, spec1_roughness;
+    int spec1_fresnel;
+    float spec1_fresnel_refl[3], spec1_fresnel_edge[3];
+    float ior;
+} vmr_shader_std;
+
+/* TriLight (builtin/light/triangle.go:18-28): geom is the light's own
+ * emissive mesh (Tri.createMesh, triangle.go:537-565), which shading
+ * excludes from the light list when it is the hit geom (scene.go:100-116). */
+typedef struct {
+    float p0[3], p1[3], p2[3];
+    int samples;           /* NumSamples = 1 << samples (default 1) */
+    uint32_t shader;
+    uint32_t geom;
+} vmr_tri_light;
+
+/* Pinhole camera (builtin/camera/camera.go): m = LocalToWorld,
+ * column-major; tan_theta_focal = tan(fov/2) * focal. */
+typedef struct {
+    float m[16];
+    float tan_theta_focal, aspect, focal, radius;
+} vmr_camera;
+
+typedef struct {
+    uint32_t width, height;
+    uint32_t iter_begin, iter_count;  /* core.Render loop iterations */
+    uint64_t seed;                    /* per-pixel scrambles */
+    uint32_t max_batch_samples;       /* samples per wavefront batch (0: 4M) */
+} vmr_render_params;
+
+typedef struct {
+    uint64_t samples;      /* pixel samples rendered */
+    uint64_t camera_rays;  /* primary rays traced */
+    uint64_t shadow_rays;  /* shadow rays traced */
+    float ms;              /* device time of the render */
+} vmr_render_stats;
+
+/* Material table (index = shader id). */
+int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n);
+/* PolyMesh.Shader (the mesh's shader ids; faces pick one through the
+ * shader_idx given at build) and optional per-vertex normals (key 0). */
+int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, uint32_t n_shaders,
+                         const float* normals);
+int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n);
+int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* camera);
+/* core.Render in reference mode (core/render.go:140-218 with ShaderStd's
+ * direct lighting): iterations iter_begin..iter_begin+iter_count-1 of every
+ * pixel, folded into fb (host, width*height*3 floats, in/out) as
+ * buf = (buf*(iter+1) + c)/(iter+2).  Needs the scene (vmr_scene_build)
+ * over every mesh, light meshes included. */
+int vmr_render(vmr_ctx* ctx, const vmr_render_params* params, float* fb, vmr_render_stats* stats);
+
 /* -------------------------------------------------------------- no-alloc */
 /* No counterpart in the reference.  For callers that must not have a library
  * allocate device memory while they run (they manage the whole device

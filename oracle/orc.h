@@ -106,6 +106,65 @@ uint64_t orc_raster_xy(uint32_t m, uint32_t frame, uint32_t px, uint32_t py,
  * generator matrices: 52 uint64 each. */
 void orc_vdc_sobol_tables(uint32_t m, uint64_t* fwd52, uint64_t* inv52);
 
+/* ------------------------------------------------------ reference render */
+/* ShaderStd parameters (builtin/shader/std.go:25-47).  A parameter the scene
+ * does not set is absent (nil in the reference), which changes defaults:
+ * flags say which are present. */
+enum {
+    ORC_SH_EMISSION_COLOUR = 1, ORC_SH_EMISSION_STRENGTH = 2,
+    ORC_SH_DIFFUSE_COLOUR = 4, ORC_SH_DIFFUSE_STRENGTH = 8, ORC_SH_DIFFUSE_ROUGHNESS = 16,
+    ORC_SH_SPEC1_COLOUR = 32, ORC_SH_SPEC1_STRENGTH = 64, ORC_SH_SPEC1_ROUGHNESS = 128,
+    ORC_SH_FRESNEL_REFL = 256, ORC_SH_FRESNEL_EDGE = 512, ORC_SH_IOR = 1024
+};
+typedef struct {
+    uint32_t flags;
+    float emission_colour[3], emission_strength;
+    float diffuse_colour[3], diffuse_strength, diffuse_roughness;
+    float spec1_colour[3], spec1_strength, spec1_roughness;
+    int spec1_fresnel; /* 0 Dielectric (also the unset default), 1 Metal */
+    float spec1_fresnel_refl[3], spec1_fresnel_edge[3];
+    float ior;
+} orc_shader;
+
+/* TriLight (builtin/light/triangle.go:18-28); mesh = index, among the
+ * meshes given to orc_scene_create, of the light's own emissive mesh. */
+typedef struct {
+    float p0[3], p1[3], p2[3];
+    int samples;
+    uint32_t shader;
+    uint32_t mesh;
+} orc_trilight;
+
+/* Camera (builtin/camera/camera.go): m = LocalToWorld, column-major. */
+typedef struct {
+    float m[16];
+    float tan_theta_focal, aspect, focal, radius;
+} orc_camera;
+
+typedef struct orc_render orc_render;
+
+/* Per-mesh shading data: shader index per face (face order, may be NULL)
+ * and per-vertex normals of key 0 (may be NULL). */
+int orc_mesh_set_shading(orc_mesh* m, const uint8_t* face_shader, const float* normals);
+
+/* shader_list[mesh_shader_offset[m] .. + mesh_shader_count[m]] are the
+ * shaders of mesh m (PolyMesh.Shader). */
+orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, uint32_t n_meshes,
+                              const uint32_t* mesh_shader_offset, const uint32_t* mesh_shader_count,
+                              const uint32_t* shader_list, const orc_shader* shaders, uint32_t n_shaders,
+                              const orc_trilight* lights, uint32_t n_lights, const orc_camera* cam);
+void orc_render_destroy(orc_render* r);
+/* Runs core.Render iterations iter_begin .. iter_begin+iter_count-1 (the
+ * reference's 0-based loop variable; each renders sample iter+1 and folds
+ * it into fb as buf = (buf*(iter+1) + c)/(iter+2), core/render.go:127-129).
+ * fb: w*h*3 floats, in/out.  seed: per-pixel scrambles (see orc_scramble). */
+int orc_render_run(orc_render* r, uint32_t w, uint32_t h, uint32_t iter_begin, uint32_t iter_count,
+                   uint64_t seed, float* fb, int nthreads);
+/* The scramble k (0 lensU, 1 lensV, 2 time, 3 lambda, 4 light/glossy 0,
+ * 5 light/glossy 1) of pixel pix: replaces the reference's draws from
+ * math/rand (core/render.go:166-176). */
+uint64_t orc_scramble(uint64_t seed, uint64_t pix, uint32_t k);
+
 #ifdef __cplusplus
 }
 #endif

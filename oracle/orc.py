@@ -81,11 +81,102 @@ def lib():
     return _lib
 
 
+class OrcShader(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_uint32), ("emission_colour", ctypes.c_float * 3),
+                ("emission_strength", ctypes.c_float), ("diffuse_colour", ctypes.c_float * 3),
+                ("diffuse_strength", ctypes.c_float), ("diffuse_roughness", ctypes.c_float),
+                ("spec1_colour", ctypes.c_float * 3), ("spec1_strength", ctypes.c_float),
+                ("spec1_roughness", ctypes.c_float), ("spec1_fresnel", ctypes.c_int),
+                ("spec1_fresnel_refl", ctypes.c_float * 3), ("spec1_fresnel_edge", ctypes.c_float * 3),
+                ("ior", ctypes.c_float)]
+
+
+class OrcTriLight(ctypes.Structure):
+    _fields_ = [("p0", ctypes.c_float * 3), ("p1", ctypes.c_float * 3), ("p2", ctypes.c_float * 3),
+                ("samples", ctypes.c_int), ("shader", ctypes.c_uint32), ("mesh", ctypes.c_uint32)]
+
+
+class OrcCamera(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_float * 16), ("tan_theta_focal", ctypes.c_float), ("aspect", ctypes.c_float),
+                ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
+
+
+_SH_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
+             "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
+             "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
+
+
 def _register_render(L):
-    if hasattr(L, "orc_render"):
-        P = ctypes.c_void_p
-        L.orc_render.restype = ctypes.c_int
-        L.orc_render.argtypes = [P, P, P, ctypes.c_int]
+    P = ctypes.c_void_p
+    L.orc_mesh_set_shading.restype = ctypes.c_int
+    L.orc_mesh_set_shading.argtypes = [P, P, P]
+    L.orc_render_create.restype = P
+    L.orc_render_create.argtypes = [P, P, ctypes.c_uint32, P, P, P, P, ctypes.c_uint32, P, ctypes.c_uint32, P]
+    L.orc_render_destroy.argtypes = [P]
+    L.orc_render_run.restype = ctypes.c_int
+    L.orc_render_run.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                 ctypes.c_uint64, P, ctypes.c_int]
+    L.orc_scramble.restype = ctypes.c_uint64
+    L.orc_scramble.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32]
+
+
+class Render:
+    """The oracle's reference-mode renderer over a render scene
+    (vermeer_gb300.scenes format)."""
+
+    def __init__(self, scene):
+        self.meshes = []
+        for m in scene["meshes"]:
+            om = Mesh(m["verts"], m["idxp"])
+            fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
+            nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
+            lib().orc_mesh_set_shading(om.h, _ptr(fs), _ptr(nr))
+            self.meshes.append(om)
+        self.scene = Scene(self.meshes)
+        counts = np.asarray([len(m["shaders"]) for m in scene["meshes"]], np.uint32)
+        offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32)
+        lst = np.asarray([s for m in scene["meshes"] for s in m["shaders"]], np.uint32)
+        shs = (OrcShader * len(scene["shaders"]))()
+        for i, d in enumerate(scene["shaders"]):
+            fl = 0
+            for k, bit in _SH_FLAGS.items():
+                if k in d:
+                    fl |= bit
+                    if isinstance(getattr(shs[i], k), float):
+                        setattr(shs[i], k, float(d[k]))
+                    else:
+                        for c in range(3):
+                            getattr(shs[i], k)[c] = float(d[k][c])
+            shs[i].flags = fl
+            shs[i].spec1_fresnel = 1 if d.get("spec1_fresnel") == "Metal" else 0
+        lts = (OrcTriLight * len(scene["lights"]))()
+        for i, d in enumerate(scene["lights"]):
+            for k in ("p0", "p1", "p2"):
+                for c in range(3):
+                    getattr(lts[i], k)[c] = float(d[k][c])
+            lts[i].samples, lts[i].shader, lts[i].mesh = int(d.get("samples", 1)), int(d["shader"]), int(d["mesh"])
+        cam = OrcCamera()
+        for i in range(16):
+            cam.m[i] = float(scene["camera"]["m"][i])
+        c = scene["camera"]
+        cam.tan_theta_focal, cam.aspect, cam.focal, cam.radius = (float(c[k]) for k in
+                                                               ("tan_theta_focal", "aspect", "focal", "radius"))
+        arr = (ctypes.c_void_p * len(self.meshes))(*[m.h for m in self.meshes])
+        self._keep = (counts, offs, lst, shs, lts, cam, arr)
+        self.h = lib().orc_render_create(self.scene.h, arr, len(self.meshes), _ptr(offs), _ptr(counts), _ptr(lst),
+                                         shs, len(scene["shaders"]), lts, len(scene["lights"]), ctypes.byref(cam))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_render_destroy(self.h)
+            self.h = None
+
+    def run(self, width, height, iter_begin, iter_count, seed, fb=None, nthreads=0):
+        if fb is None:
+            fb = np.zeros((height, width, 3), np.float32)
+        fb = np.ascontiguousarray(fb, np.float32)
+        lib().orc_render_run(self.h, width, height, iter_begin, iter_count, seed, _ptr(fb), int(nthreads))
+        return fb
 
 
 def _ptr(a):

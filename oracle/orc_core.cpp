@@ -361,6 +361,8 @@ struct Mesh {
   std::vector<std::vector<float>> mboxes;       // [key][node*24]
   std::vector<Box> motion_bounds;
   Box bounds;
+  std::vector<uint8_t> shaderidx;  // leaf order (static) / face order (motion)
+  std::vector<float> normals;      // per vertex, key 0
 
   const float* vert(uint32_t i, int key) const { return &verts[((size_t)key * nverts + i) * 3]; }
   int motion_keys() const { return nodes.empty() ? (int)mboxes.size() : 1; }  // polymesh.go:103-112
@@ -806,6 +808,41 @@ void parallel_for(size_t n, int nthreads, F&& f) {
 struct orc_mesh { Mesh m; };
 struct orc_scene { Scene s; };
 
+#include "orc_internal.h"
+
+namespace orc_internal {
+
+Hit trace(const orc_scene* s, const float P[3], const float D[3], float tmax, float time, bool shadow) {
+  float in[8] = {P[0], P[1], P[2], D[0], D[1], D[2], tmax, time};
+  Ray r = make_ray(in, shadow);
+  Task tk;
+  Hit h;
+  h.hit = scene_trace(s->s, r, tk);
+  h.elem = tk.elem;
+  h.geom = tk.geom;
+  h.t = r.Tclosest;
+  h.u = tk.bu;
+  h.v = tk.bv;
+  h.w = tk.bw;
+  h.overflow = tk.overflow;
+  return h;
+}
+
+MeshView mesh_view(const orc_mesh* om) {
+  const Mesh& m = om->m;
+  MeshView v;
+  v.verts = m.verts.data();
+  v.nverts = m.nverts;
+  v.keys = m.keys;
+  v.idxp = m.idxp.data();
+  v.shaderidx = m.shaderidx.empty() ? nullptr : m.shaderidx.data();
+  v.normals = m.normals.empty() ? nullptr : m.normals.data();
+  v.motion = m.keys > 1;
+  return v;
+}
+
+}  // namespace orc_internal
+
 extern "C" {
 
 const char* orc_last_error(void) { return g_err.c_str(); }
@@ -833,6 +870,22 @@ orc_mesh* orc_mesh_create(const float* verts, uint32_t nverts, uint32_t keys, co
 }
 
 void orc_mesh_destroy(orc_mesh* m) { delete m; }
+
+// Shading data as PolyMesh holds it after initAccel (buildqbvh.go:98-104):
+// shader indices permuted to leaf order for a static mesh, face order for a
+// motion mesh; normals indexed by vertex (NormalIdx = FaceIdx).
+int orc_mesh_set_shading(orc_mesh* om, const uint8_t* face_shader, const float* normals) {
+  Mesh& m = om->m;
+  m.shaderidx.clear();
+  if (face_shader) {
+    m.shaderidx.resize(m.ntris);
+    for (uint32_t i = 0; i < m.ntris; ++i)
+      m.shaderidx[i] = m.nodes.empty() ? face_shader[i] : face_shader[m.accel_idx[i]];
+  }
+  m.normals.clear();
+  if (normals) m.normals.assign(normals, normals + (size_t)m.nverts * 3);
+  return 0;
+}
 
 void orc_mesh_info(const orc_mesh* om, uint32_t* n_nodes, uint32_t* n_mnodes, float* bounds6) {
   const Mesh& m = om->m;

@@ -1,0 +1,825 @@
+// orc_render.cpp - CPU oracle of the reference render path (reference mode).
+//
+// TEST INFRASTRUCTURE ONLY (see orc.h).  Restates core.Render / render
+// (core/render.go:66-218), Camera.ComputeRay for a pinhole
+// (builtin/camera/camera.go:221-323), core.Trace (core/trace.go:40-83), the
+// static hit attributes of PolyMesh.TraceElems (trace.go:276-515),
+// ShaderStd.Eval (builtin/shader/std.go:77-316), EvaluateLightSamples
+// (core/shader.go:203-402), the OrenNayar and GGX BSDFs, the Fresnel models,
+// TriLight sampling (builtin/light/triangle.go) and the hero-wavelength
+// spectrum (colour/*.go).
+//
+// Deliberate, documented departures from the Go code (the CUDA path does the
+// same, so the two agree closely):
+//  * Vec3Normalize is a * (1/sqrt(a.a)) with IEEE sqrt and division; the
+//    reference's RSQRTSS estimate is machine-dependent (math/vec3_amd64.s).
+//  * acos arguments are clamped to [-1, 1]: a normalised dot product can
+//    exceed 1 by an ulp, where the reference yields NaN.
+//  * per-pixel scrambles come from a hash of (seed, pixel) instead of the
+//    unseeded math/rand stream (core/render.go:166-176).
+//  * the camera uses LocalToWorld directly instead of its SRT decomposition
+//    round trip (camera.go:223-236), which is not exact for one key.
+// Transcendentals follow math/sincos.go: evaluated in float64, rounded to
+// float32.
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "orc.h"
+#include "orc_colour_tables.h"
+#include "orc_internal.h"
+
+namespace {
+
+using orc_internal::Hit;
+
+struct V3 {
+  float x, y, z;
+};
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 scale(float s, V3 a) { return v3(a.x * s, a.y * s, a.z * s); }  // Vec3Scale
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {  // Vec3Cross (math/vec3.go:69-74)
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline float len2(V3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+inline float gabs(float x) { return std::fabs(x); }
+inline V3 normalize(V3 a) {
+  const float r = 1.0f / std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  return v3(a.x * r, a.y * r, a.z * r);
+}
+inline float length(V3 a) { return std::sqrt((a.x * a.x + a.y * a.y) + a.z * a.z); }  // Vec3Length
+inline float gmax(float x, float y) { return x > y ? x : y; }
+inline float gmin(float x, float y) { return x < y ? x : y; }
+const float kPi = 3.14159265358f;  // math.Pi (math/const.go:8) as float32
+// math/sincos.go: float64 evaluation, float32 result.
+inline float gsin(float x) { return (float)std::sin((double)x); }
+inline float gcos(float x) { return (float)std::cos((double)x); }
+inline float gtan(float x) { return (float)std::tan((double)x); }
+inline float gatan(float x) { return (float)std::atan((double)x); }
+inline float gatan2(float y, float x) { return (float)std::atan2((double)y, (double)x); }
+inline float gacos(float x) { return (float)std::acos((double)(x > 1.0f ? 1.0f : (x < -1.0f ? -1.0f : x))); }
+// Vec3BasisProject / Vec3BasisExpand (math/vec3.go:122-137).
+inline V3 project(V3 U, V3 V, V3 W, V3 s) { return v3(dot(U, s), dot(V, s), dot(W, s)); }
+inline V3 expand(V3 U, V3 V, V3 W, V3 s) {
+  return v3(U.x * s.x + V.x * s.y + W.x * s.z, U.y * s.x + V.y * s.y + W.y * s.z, U.z * s.x + V.z * s.y + W.z * s.z);
+}
+
+// ---------------------------------------------------------------- QMC ----
+uint64_t vdc_bits(uint64_t i, uint64_t s) {  // ldseq.vanDerCorput
+  uint64_t b = (i << 32) | (i >> 32);
+  b = ((b & 0x0000ffff0000ffffull) << 16) | ((b & 0xffff0000ffff0000ull) >> 16);
+  b = ((b & 0x00ff00ff00ff00ffull) << 8) | ((b & 0xff00ff00ff00ff00ull) >> 8);
+  b = ((b & 0x0f0f0f0f0f0f0f0full) << 4) | ((b & 0xf0f0f0f0f0f0f0f0ull) >> 4);
+  b = ((b & 0x3333333333333333ull) << 2) | ((b & 0xccccccccccccccccull) >> 2);
+  b = ((b & 0x5555555555555555ull) << 1) | ((b & 0xaaaaaaaaaaaaaaaaull) >> 1);
+  return (s ^ b) >> 12;
+}
+uint64_t sobol_bits(uint64_t i, uint64_t s) {  // ldseq.sobol
+  uint64_t r = s >> 12;
+  for (uint64_t v = 1ull << 51; i != 0; i >>= 1) {
+    if (i & 1) r ^= v;
+    v ^= v >> 1;
+  }
+  return r;
+}
+const double kTwo52 = 4503599627370496.0;
+inline double vdc(uint64_t i, uint64_t s) { return (double)vdc_bits(i, s) / kTwo52; }
+inline double sobol(uint64_t i, uint64_t s) { return (double)sobol_bits(i, s) / kTwo52; }
+
+// ----------------------------------------------------------- spectrum ----
+struct RGB {
+  float c[3];
+};
+struct Spectrum {
+  float c[4];
+  float lambda;
+};
+// Spectrum.Wavelength (colour/spectrum.go:102-112).
+float wavelength(float lambda, int j) {
+  float v = (lambda - 450.0f + ((float)j / 4.0f) * 300.0f);
+  if (v >= 300.0f) v -= 300.0f;
+  v += 450.0f;
+  return v;
+}
+float smits_eval(const float* s, float lambda) {  // smitsSpectrum.eval
+  if (lambda < 380.0f || lambda >= 720.0f) return 0.0f;
+  int bin = (int)(((lambda - 380.0f) / (720.0f - 380.0f)) * 10.0f);
+  return s[bin];
+}
+// RGBToSpectrumSmits99 (colour/spectrum_smits9.go:48-84).
+float smits(float r, float g, float b, float l) {
+  float c = 0.0f;
+  if (r <= g && r <= b) {
+    c += r * smits_eval(kSmitsWhite, l);
+    if (g <= b) {
+      c += (g - r) * smits_eval(kSmitsCyan, l);
+      c += (b - g) * smits_eval(kSmitsBlue, l);
+    } else {
+      c += (b - r) * smits_eval(kSmitsCyan, l);
+      c += (g - b) * smits_eval(kSmitsGreen, l);
+    }
+  } else if (g <= r && g <= b) {
+    c += g * smits_eval(kSmitsWhite, l);
+    if (r <= b) {
+      c += (r - g) * smits_eval(kSmitsMagenta, l);
+      c += (b - r) * smits_eval(kSmitsBlue, l);
+    } else {
+      c += (b - g) * smits_eval(kSmitsMagenta, l);
+      c += (r - b) * smits_eval(kSmitsRed, l);
+    }
+  } else {
+    c += b * smits_eval(kSmitsWhite, l);
+    if (r <= g) {
+      c += (r - b) * smits_eval(kSmitsYellow, l);
+      c += (g - r) * smits_eval(kSmitsGreen, l);
+    } else {
+      c += (g - b) * smits_eval(kSmitsYellow, l);
+      c += (r - g) * smits_eval(kSmitsRed, l);
+    }
+  }
+  return c;
+}
+Spectrum from_rgb(RGB rgb, float lambda) {  // Spectrum.FromRGB
+  Spectrum s;
+  s.lambda = lambda;
+  for (int k = 0; k < 4; ++k) s.c[k] = smits(rgb.c[0], rgb.c[1], rgb.c[2], wavelength(lambda, k));
+  return s;
+}
+float cie(const float* t, float l) {  // CieObserverData.X/Y/Z
+  if (l < 360.0f || l >= 830.0f) return -1.0f;
+  int bin = (int)(((l - 360.0f) / (830.0f - 360.0f)) * 95.0f);
+  return t[bin];
+}
+RGB to_rgb(const Spectrum& s) {  // Spectrum.ToRGB + sRGB.XYZToRGB
+  float x = 0, y = 0, z = 0;
+  for (int i = 0; i < 4; ++i) {
+    const float l = wavelength(s.lambda, i);
+    x += s.c[i] * cie(kCieX, l);
+    y += s.c[i] * cie(kCieY, l);
+    z += s.c[i] * cie(kCieZ, l);
+  }
+  const float* m = kSrgbFromXyz;
+  return RGB{{x * m[0] + y * m[1] + z * m[2], x * m[3] + y * m[4] + z * m[5], x * m[6] + y * m[7] + z * m[8]}};
+}
+inline void sscale(Spectrum& s, float f) {
+  for (float& c : s.c) c *= f;
+}
+inline void smul(Spectrum& s, const Spectrum& o) {
+  for (int k = 0; k < 4; ++k) s.c[k] *= o.c[k];
+}
+inline void radd(RGB& a, RGB b) {
+  for (int k = 0; k < 3; ++k) a.c[k] += b.c[k];
+}
+inline void rmul(RGB& a, RGB b) {
+  for (int k = 0; k < 3; ++k) a.c[k] *= b.c[k];
+}
+inline void rscale(RGB& a, float f) {
+  for (float& c : a.c) c *= f;
+}
+
+// ------------------------------------------------------------ fresnel ----
+struct Fresnel {
+  int model;  // 0 dielectric, 1 conductor
+  float eta;
+  RGB r, g;
+};
+inline float sqr(float v) { return v * v; }
+RGB fresnel_kr(const Fresnel& f, float c) {
+  if (f.model == 0) {  // Dielectric.Kr (fresnel/dielectric.go:34-47)
+    float g = (f.eta * f.eta) - 1 + (c * c);
+    if (g < 0.0f) return RGB{{1, 1, 1}};
+    g = std::sqrt(g);
+    float fr = 0.5f * sqr((g - c) / (g + c)) * (1 + sqr((c * (g + c) - 1) / (c * (g - c) + 1)));
+    return RGB{{fr, fr, fr}};
+  }
+  RGB out;  // Conductor.Kr (fresnel/conductor.go:58-89)
+  for (int k = 0; k < 3; ++k) {
+    const float r = gmax(0.0f, gmin(f.r.c[k], 0.99f));  // Clamp(r, 0, 0.99)
+    const float g = f.g.c[k];
+    const float nmin = (1 - r) / (1 + r);
+    const float nmax = (1 + std::sqrt(r)) / (1 - std::sqrt(r));
+    const float n = nmin * g + (1 - g) * nmax;
+    const float k2 = ((n + 1) * (n + 1) * r - (n - 1) * (n - 1)) / (1 - r);
+    const float rs = (n * n + k2 - 2 * n * c + c * c) / (n * n + k2 + 2 * n * c + c * c);
+    const float rp = ((n * n + k2) * c * c - 2 * n * c + 1) / ((n * n + k2) * c * c + 2 * n * c + 1);
+    out.c[k] = 0.5f * (rs + rp);
+  }
+  return out;
+}
+
+// --------------------------------------------------------------- BSDFs ----
+struct Bsdf {
+  int kind;  // 0 OrenNayar, 1 GGX, 2 specular
+  float lambda;
+  V3 wi;       // OmegaI / OmegaR in the local frame
+  float rough; // roughness^2 as the constructors store it
+  Fresnel fr;
+  V3 U, V, N;
+};
+// sample.CosineHemisphere (math/sample/sample.go:18-27)
+V3 cosine_hemisphere(double u0, double u1) {
+  double r = std::sqrt(1 - u0);
+  double th = 2 * M_PI * u1;
+  return v3((float)(r * std::cos(th)), (float)(r * std::sin(th)), (float)std::sqrt(u0));
+}
+inline float chi(float x) { return x > 0.0f ? 1.0f : 0.0f; }
+float ggx_g1(V3 w, V3 m, float alpha) {
+  float odn = dot(w, m);
+  float denom = 1 + std::sqrt(1 + (alpha * alpha) * ((1.0f / (w.z * w.z)) - 1));
+  return chi(odn / w.z) * 2 / denom;
+}
+float ggx_d(V3 m, float alpha) {
+  float numer = alpha * alpha * chi(m.z);
+  if (m.z == 1.0f) return 1.0f / (kPi * alpha * alpha);
+  float denom = kPi * sqr(m.z * m.z) * sqr(alpha * alpha + ((1.0f / (m.z * m.z)) - 1));
+  return numer / denom;
+}
+inline float signf(float v) { return v < 0 ? -1.0f : 1.0f; }
+inline V3 reflect_z(V3 w) {  // reflect(omegaR, (0,0,1)) (bsdf/specular.go:13-19)
+  const float d = 0.0f * w.x + 0.0f * w.y + 1.0f * w.z;
+  return sub(scale(2.0f * d, v3(0, 0, 1)), w);
+}
+
+V3 bsdf_sample(const Bsdf& b, double r0, double r1) {
+  if (b.kind == 0) return expand(b.U, b.V, b.N, cosine_hemisphere(r0, r1));
+  if (b.kind == 1) {  // MicrofacetGGX.Sample (bsdf/microfacetggx.go:82-100)
+    const float alpha = sqr(b.rough);
+    const double thetaM = std::atan2((double)alpha * std::sqrt(r0), std::sqrt(1 - r0));
+    const double phiM = 2.0 * M_PI * r1;
+    const V3 m = v3(gsin((float)thetaM) * gcos((float)phiM), gsin((float)thetaM) * gsin((float)phiM), gcos((float)thetaM));
+    const V3 wo = sub(scale(2.0f * gabs(dot(m, b.wi)), m), b.wi);
+    return expand(b.U, b.V, b.N, normalize(wo));
+  }
+  return expand(b.U, b.V, b.N, normalize(reflect_z(b.wi)));  // Specular.Sample
+}
+
+double bsdf_pdf(const Bsdf& b, V3 wo_world) {
+  const V3 wo = project(b.U, b.V, b.N, wo_world);
+  if (b.kind == 0) return (double)gmax(0.0f, wo.z) / M_PI;
+  if (b.kind == 1) {
+    const float alpha = sqr(b.rough);
+    const V3 m = scale(signf(b.wi.z), normalize(add(b.wi, wo)));
+    const double pdf = (double)(ggx_d(m, alpha) * m.z);
+    return std::isnan(pdf) ? 0.0 : pdf;
+  }
+  return dot(wo, reflect_z(b.wi)) < 0.9999f ? 0.0 : 1.0;
+}
+
+Spectrum bsdf_eval(const Bsdf& b, V3 wo_world) {
+  Spectrum rho;
+  rho.lambda = b.lambda;
+  for (float& c : rho.c) c = 0.0f;
+  const V3 wo = project(b.U, b.V, b.N, wo_world);
+  if (b.kind == 0) {  // OrenNayar.Eval (bsdf/orennayar.go:42-73)
+    const float sigma = b.rough;
+    const float A = 1 - (0.5f * (sigma * sigma) / ((sigma * sigma) + 0.57f));
+    const float B = 0.45f * (sigma * sigma) / ((sigma * sigma) + 0.09f);
+    const float phiI = gatan2(b.wi.y, b.wi.x);
+    const float phiO = gatan2(wo.y, wo.x);
+    const float thetaI = gacos(b.wi.z);
+    const float thetaO = gacos(wo.z);
+    const float alpha = gmax(thetaI, thetaO);
+    const float beta = gmin(thetaI, thetaO);
+    const float C = gsin(alpha) * gtan(beta);
+    const float gamma = gcos(phiO - phiI);
+    const float s = wo.z * (A + (B * gmax(0.0f, gamma) * C));
+    rho = from_rgb(RGB{{1, 1, 1}}, b.lambda);
+    sscale(rho, s / kPi);
+    return rho;
+  }
+  if (b.kind == 1) {  // MicrofacetGGX.Eval (microfacetggx.go:119-145)
+    const float alpha = sqr(b.rough);
+    const V3 h = scale(signf(b.wi.z), normalize(add(b.wi, wo)));
+    const RGB f = fresnel_kr(b.fr, gabs(dot(b.wi, h)));
+    const float numer = ggx_g1(b.wi, h, alpha) * ggx_g1(wo, h, alpha) * ggx_d(h, alpha);
+    const float denom = 4 * gabs(b.wi.z) * gabs(wo.z);
+    rho = from_rgb(f, b.lambda);
+    sscale(rho, gabs(wo.z) * numer / denom);
+    for (float& c : rho.c)
+      if (c < 0 || std::isnan(c)) c = 0;
+    return rho;
+  }
+  if (dot(wo, reflect_z(b.wi)) < 0.9999f) return rho;  // Specular.Eval
+  rho = from_rgb(fresnel_kr(b.fr, b.wi.z), b.lambda);
+  sscale(rho, gabs(dot(wo, v3(0, 0, 1))));
+  return rho;
+}
+
+// -------------------------------------------------------------- scene ----
+struct Shader {
+  orc_shader p;
+  bool has(uint32_t f) const { return (p.flags & f) != 0; }
+};
+
+struct Ctx {  // the ShaderContext fields the path reads
+  V3 P, N, Ng, Poffset, DdPdu, DdPdv, Rd;
+  float lambda, time;
+  int level;
+  uint64_t I;
+  uint64_t scr0, scr1;
+  int32_t geom;
+  const Shader* shader;
+};
+
+struct LightSample {
+  V3 Ld;
+  float Ldist, pdf;
+  Spectrum Liu;
+};
+struct BsdfSample {
+  V3 D, Ld;
+  double pdf;
+  float pdf_light, Ldist;
+  Spectrum Liu;
+};
+
+struct Render {
+  const orc_scene* scene = nullptr;
+  std::vector<orc_internal::MeshView> meshes;
+  std::vector<std::vector<uint32_t>> mesh_shaders;
+  std::vector<Shader> shaders;
+  std::vector<orc_trilight> lights;
+  orc_camera cam;
+};
+
+// EvalEmission (std.go:299-316).
+RGB emission(const Shader& s) {
+  if (!s.has(ORC_SH_EMISSION_STRENGTH)) return RGB{{0, 0, 0}};
+  RGB e = s.has(ORC_SH_EMISSION_COLOUR) ? RGB{{s.p.emission_colour[0], s.p.emission_colour[1], s.p.emission_colour[2]}}
+                                        : RGB{{0, 0, 0}};
+  rscale(e, s.p.emission_strength);
+  return e;
+}
+
+// OffsetP (core/shader.go:139-163).
+float next_up(float v) {
+  if (std::isinf(v) && v > 0) return v;
+  if (v == 0.0f) v = 0.0f;
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  if (v >= 0.0f) ++u; else --u;
+  std::memcpy(&v, &u, 4);
+  return v;
+}
+float next_down(float v) {
+  if (std::isinf(v) && v < 0) return v;
+  if (v == 0.0f) v = 0.0f;
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  if (v >= 0.0f) --u; else ++u;
+  std::memcpy(&v, &u, 4);
+  return v;
+}
+V3 offset_p(const Ctx& sc, int dir) {
+  const V3 pofs = dir < 0 ? v3(-sc.Poffset.x, -sc.Poffset.y, -sc.Poffset.z) : sc.Poffset;
+  V3 po = add(sc.P, pofs);
+  float* p = &po.x;
+  const float* o = &pofs.x;
+  for (int i = 0; i < 3; ++i) {
+    if (o[i] > 0) p[i] = next_up(p[i]);
+    else if (o[i] < -0.0f) p[i] = next_down(p[i]);
+  }
+  return po;
+}
+
+// Triangle-light helpers (builtin/light/triangle.go).
+V3 tri_normal(const orc_trilight& L) {
+  const V3 p0 = v3(L.p0[0], L.p0[1], L.p0[2]), p1 = v3(L.p1[0], L.p1[1], L.p1[2]), p2 = v3(L.p2[0], L.p2[1], L.p2[2]);
+  return normalize(cross(sub(p1, p0), sub(p2, p0)));
+}
+float tri_area(V3 p0, V3 p1, V3 p2) { return 0.5f * length(cross(sub(p1, p0), sub(p2, p0))); }
+void sides_to_angles(float as, float bs, float cs, float& a, float& b, float& c) {
+  const float ssu = (as + bs + cs) / 2;
+  const float sa = gsin(ssu - as), sb = gsin(ssu - bs), sc2 = gsin(ssu - cs), s = gsin(ssu);
+  a = 2 * gatan(std::sqrt(sb * sc2 / (s * sa)));
+  b = 2 * gatan(std::sqrt(sa * sc2 / (s * sb)));
+  c = 2 * gatan(std::sqrt(sa * sb / (s * sc2)));
+}
+float spherical_area(V3 pa, V3 pb, V3 pc, float& a_side_c) {
+  const float a = gacos(dot(pb, pc)), b = gacos(dot(pc, pa)), c = gacos(dot(pa, pb));
+  float al, be, ga;
+  sides_to_angles(a, b, c, al, be, ga);
+  a_side_c = c;
+  return al + be + ga - kPi;
+}
+// sampleSphericalTriangle (triangle.go:474-535), Arvo's method.
+V3 sample_spherical(V3 p0, V3 p1, V3 p2, V3 p, double r0, double r1, double& pdf) {
+  const V3 pa = normalize(sub(p0, p)), pb = normalize(sub(p1, p)), pc = normalize(sub(p2, p));
+  const float a = gacos(dot(pb, pc)), b = gacos(dot(pc, pa)), c = gacos(dot(pa, pb));
+  float alpha, beta, gamma;
+  sides_to_angles(a, b, c, alpha, beta, gamma);
+  const float area = alpha + beta + gamma - kPi;
+  const float areaHat = (float)r0 * area;
+  const float s = gsin(areaHat - alpha), t = gcos(areaHat - alpha);
+  const float sinA = gsin(alpha), cosA = gcos(alpha);
+  const float u = t - cosA;
+  const float v = s + sinA * gcos(c);
+  float q = ((v * t - u * s) * cosA - v) / ((v * s + u * t) * sinA);
+  q = gmax(-1.0f, gmin(q, 1.0f));
+  float w = dot(pc, pa);
+  V3 v31 = normalize(v3(pc.x - w * pa.x, pc.y - w * pa.y, pc.z - w * pa.z));
+  const float sq = std::sqrt(1 - q * q);
+  const V3 v4 = v3(q * pa.x + sq * v31.x, q * pa.y + sq * v31.y, q * pa.z + sq * v31.z);
+  const float z = 1 - (float)r1 * (1 - dot(v4, pb));
+  w = dot(v4, pb);
+  const V3 v42 = normalize(v3(v4.x - w * pb.x, v4.y - w * pb.y, v4.z - w * pb.z));
+  pdf = 1 / (double)area;
+  return add(scale(z, pb), scale(std::sqrt(1 - z * z), v42));
+}
+// rayPlaneIntersect (builtin/light/disk.go:38-51)
+bool ray_plane(V3 Ro, V3 Rd, V3 P, V3 N, float& t) {
+  const float denom = dot(N, Rd);
+  if (gabs(denom) > 1e-6f) {
+    t = dot(sub(P, Ro), N) / denom;
+    return t >= 0;
+  }
+  t = 0;
+  return false;
+}
+// rayTriangleIntersect, Moller-Trumbore (triangle.go:79-129)
+bool ray_tri(V3 Ro, V3 Rd, V3 P0, V3 P1, V3 P2, V3& out) {
+  const V3 e1 = sub(P1, P0), e2 = sub(P2, P0);
+  const V3 P = cross(Rd, e2);
+  const float det = dot(e1, P);
+  if (det > -1e-6f && det < 1e-6f) return false;
+  const float inv = 1 / det;
+  const V3 T = sub(Ro, P0);
+  const float u = dot(T, P) * inv;
+  if (u < 0 || u > 1) return false;
+  const V3 Q = cross(T, e1);
+  const float v = dot(Rd, Q) * inv;
+  if (v < 0 || u + v > 1) return false;
+  const float t = dot(e2, Q) * inv;
+  if (t > 1e-6f) {
+    out = add(add(scale(1 - u - v, P0), scale(u, P1)), scale(v, P2));
+    return true;
+  }
+  return false;
+}
+
+struct Renderer {
+  const Render& R;
+
+  Spectrum light_liu(const orc_trilight& L, const Ctx& sc) const {
+    return from_rgb(emission(R.shaders[L.shader]), sc.lambda);
+  }
+
+  // Tri.SampleArea (triangle.go:285-343) with the area fallback (:232-282).
+  void sample_area(const orc_trilight& L, const Ctx& sc, int n, std::vector<LightSample>& out) const {
+    const V3 p0 = v3(L.p0[0], L.p0[1], L.p0[2]), p1 = v3(L.p1[0], L.p1[1], L.p1[2]), p2 = v3(L.p2[0], L.p2[1], L.p2[2]);
+    const V3 N = tri_normal(L);
+    const bool area_only = dot(sc.Ng, sub(p0, sc.P)) < 0 || dot(sc.Ng, sub(p1, sc.P)) < 0 || dot(sc.Ng, sub(p2, sc.P)) < 0;
+    for (int i = 0; i < n; ++i) {
+      const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;
+      const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
+      LightSample ls;
+      if (area_only) {
+        const double pdf = (double)(1 / tri_area(p0, p1, p2));
+        const float a = (float)(r1 * std::sqrt(1 - r0)), b = (float)(1 - std::sqrt(1 - r0));
+        const V3 P = add(add(p0, scale(a, sub(p1, p0))), scale(b, sub(p2, p0)));
+        const V3 D = sub(P, sc.P);
+        ls.Ldist = length(D);
+        ls.Ld = normalize(D);
+        if (dot(ls.Ld, N) > 0 || dot(ls.Ld, sc.Ng) < 0) continue;
+        ls.Liu = light_liu(L, sc);
+        ls.pdf = (float)pdf * sqr(ls.Ldist) / gabs(dot(ls.Ld, N));
+      } else {
+        double pdf;
+        const V3 x = sample_spherical(p0, p1, p2, sc.P, r0, r1, pdf);
+        float t;
+        ray_plane(sc.P, x, p0, N, t);
+        const V3 P = add(sc.P, scale(t, x));  // Vec3Mad
+        const V3 D = sub(P, sc.P);
+        ls.Ldist = length(D);
+        ls.Ld = normalize(D);
+        if (dot(ls.Ld, N) > 0 || dot(ls.Ld, sc.Ng) < 0) continue;
+        ls.Liu = light_liu(L, sc);
+        ls.pdf = (float)pdf;
+      }
+      out.push_back(ls);
+    }
+  }
+
+  // Tri.ValidSample (triangle.go:136-230).
+  bool valid_sample(const orc_trilight& L, const Ctx& sc, BsdfSample& s) const {
+    const V3 p0 = v3(L.p0[0], L.p0[1], L.p0[2]), p1 = v3(L.p1[0], L.p1[1], L.p1[2]), p2 = v3(L.p2[0], L.p2[1], L.p2[2]);
+    V3 P;
+    if (!ray_tri(sc.P, s.D, p0, p1, p2, P)) return false;
+    const V3 N = tri_normal(L);
+    const bool area_only = dot(sc.Ng, sub(p0, P)) < 0 || dot(sc.Ng, sub(p1, P)) < 0 || dot(sc.Ng, sub(p2, P)) < 0;
+    const V3 D = sub(P, sc.P);
+    s.Ldist = length(D);
+    s.Ld = normalize(D);
+    if (dot(s.Ld, N) > 0 || dot(s.Ld, sc.Ng) < 0) return false;
+    s.Liu = light_liu(L, sc);
+    if (area_only) {
+      const double pdf = (double)(1 / tri_area(p0, p1, p2));
+      s.pdf_light = (float)pdf * sqr(s.Ldist) / gabs(dot(s.Ld, N));
+    } else {
+      float cside;
+      const float area = spherical_area(normalize(sub(p0, sc.P)), normalize(sub(p1, sc.P)), normalize(sub(p2, sc.P)), cside);
+      s.pdf_light = (float)(1 / (double)area);
+    }
+    return true;
+  }
+
+  bool occluded(const Ctx& sc, V3 Ld, float Ldist) const {
+    const V3 o = offset_p(sc, dot(Ld, sc.Ng) < 0 ? -1 : 1);
+    const V3 d = scale(Ldist * 0.9999f, Ld);  // ShadowRayEpsilon (core/ray.go:22)
+    const float P[3] = {o.x, o.y, o.z}, D[3] = {d.x, d.y, d.z};
+    return orc_internal::trace(R.scene, P, D, 1.0f, sc.time, true).hit;
+  }
+
+  // EvaluateLightSamples (core/shader.go:203-402).
+  RGB evaluate_light_samples(const Ctx& sc, const orc_trilight& L, int NS, const Bsdf& bsdf) const {
+    RGB col{{0, 0, 0}};
+    if (NS > 1) {
+      std::vector<BsdfSample> bsdf_samples;
+      for (int i = 0; i < NS / 2; ++i) {
+        const uint64_t idx = sc.I * (uint64_t)(NS / 2) + (uint64_t)i;
+        const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
+        BsdfSample s;
+        s.D = normalize(bsdf_sample(bsdf, r0, r1));
+        s.pdf = bsdf_pdf(bsdf, s.D);
+        if (s.pdf <= 0) continue;
+        if (valid_sample(L, sc, s)) bsdf_samples.push_back(s);
+      }
+      std::vector<LightSample> ls;
+      sample_area(L, sc, NS / 2, ls);
+      int nB = NS / 2, nL = NS / 2;
+      if (ls.empty()) nL = 0;
+      if (bsdf_samples.empty()) nB = 0;
+      const int total = nB + nL;
+      if (total == 0) return col;
+      for (const LightSample& l : ls) {
+        if (dot(l.Ld, sc.N) <= 0) continue;
+        if (occluded(sc, l.Ld, l.Ldist)) continue;
+        Spectrum rho = bsdf_eval(bsdf, l.Ld);
+        smul(rho, l.Liu);
+        float p_hat = (float)nB * (float)bsdf_pdf(bsdf, l.Ld) / (float)total;
+        p_hat += (float)nL * l.pdf / (float)total;
+        sscale(rho, 1.0f / p_hat);
+        RGB rgb = to_rgb(rho);
+        for (float& c : rgb.c)
+          if (c < 0) c = 0;
+        radd(col, rgb);
+      }
+      for (const BsdfSample& b : bsdf_samples) {
+        if (dot(b.Ld, sc.N) <= 0) continue;
+        if (occluded(sc, b.Ld, b.Ldist)) continue;
+        Spectrum rho = bsdf_eval(bsdf, b.Ld);
+        smul(rho, b.Liu);
+        float p_hat = (float)nB * (float)b.pdf / (float)total;
+        p_hat += (float)nL * b.pdf_light / (float)total;
+        sscale(rho, 1.0f / p_hat);
+        RGB rgb = to_rgb(rho);
+        for (float& c : rgb.c)
+          if (c < 0) c = 0;
+        radd(col, rgb);
+      }
+      rscale(col, 1.0f / (float)total);
+      return col;
+    }
+    std::vector<LightSample> ls;
+    sample_area(L, sc, NS, ls);
+    for (const LightSample& l : ls) {
+      if (dot(l.Ld, sc.N) <= 0) continue;
+      if (occluded(sc, l.Ld, l.Ldist)) continue;
+      Spectrum rho = bsdf_eval(bsdf, l.Ld);
+      smul(rho, l.Liu);
+      sscale(rho, 1.0f / l.pdf);
+      radd(col, to_rgb(rho));
+    }
+    return col;
+  }
+
+  // Hit attributes for a static mesh (trace.go:276-515) followed by
+  // ShaderContext.ApplyTransform with the identity (core/shader.go:129-135).
+  bool hit_context(const Hit& h, Ctx& sc) const {
+    const orc_internal::MeshView& m = R.meshes[h.geom];
+    const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
+    auto vert = [&](uint32_t i) { return v3(m.verts[i * 3], m.verts[i * 3 + 1], m.verts[i * 3 + 2]); };
+    const V3 V0 = vert(i0), V1 = vert(i1), V2 = vert(i2);
+    const float U = h.u, V = h.v, W = h.w;
+    const float xs = gabs(U * V0.x) + gabs(V * V1.x) + gabs(W * V2.x);
+    const float ys = gabs(U * V0.y) + gabs(V * V1.y) + gabs(W * V2.y);
+    const float zs = gabs(U * V0.z) + gabs(V * V1.z) + gabs(W * V2.z);
+    const uint8_t sidx = m.shaderidx ? m.shaderidx[h.elem] : 0;
+    const auto& list = R.mesh_shaders[h.geom];
+    if (sidx >= list.size()) return false;
+    sc.shader = &R.shaders[list[sidx]];
+    const V3 e0 = sub(V1, V0), e1 = sub(V2, V0);
+    V3 Ng = normalize(v3(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x));
+    V3 N;
+    if (m.normals) {
+      auto nrm = [&](uint32_t i) { return v3(m.normals[i * 3], m.normals[i * 3 + 1], m.normals[i * 3 + 2]); };
+      const V3 N0 = nrm(i0), N1 = nrm(i1), N2 = nrm(i2);
+      N = normalize(v3(U * N0.x + V * N1.x + W * N2.x, U * N0.y + V * N1.y + W * N2.y, U * N0.z + V * N1.z + W * N2.z));
+    } else {
+      N = Ng;
+    }
+    const float g7 = (7.0f * 5.96046448e-08f) / (1 - 7.0f * 5.96046448e-08f);  // Gamma(7)
+    const float d = g7 * xs * gabs(Ng.x) + g7 * ys * gabs(Ng.y) + g7 * zs * gabs(Ng.z);
+    sc.Poffset = scale(d, Ng);
+    sc.P = v3(U * V0.x + V * V1.x + W * V2.x, U * V0.y + V * V1.y + W * V2.y, U * V0.z + V * V1.z + W * V2.z);
+    V3 axisu = sub(v3(1, 0, 0), scale(dot(v3(1, 0, 0), Ng), Ng));
+    if (len2(axisu) < 0.1f || gabs(dot(axisu, Ng)) > 0.3f) axisu = sub(v3(0, 0, 1), scale(dot(v3(0, 0, 1), Ng), Ng));
+    const V3 dpdu = normalize(axisu);
+    const V3 dpdv = cross(Ng, dpdu);
+    sc.N = normalize(N);
+    sc.Ng = normalize(Ng);
+    sc.DdPdu = normalize(dpdu);
+    sc.DdPdv = normalize(dpdv);
+    sc.geom = h.geom;
+    return true;
+  }
+
+  // core.Trace (core/trace.go:40-83).
+  bool trace(V3 P, V3 D, int level, const Ctx& parent, RGB& out) const {
+    const float Pa[3] = {P.x, P.y, P.z}, Da[3] = {D.x, D.y, D.z};
+    const Hit h = orc_internal::trace(R.scene, Pa, Da, INFINITY, parent.time, false);
+    if (!h.hit) return false;
+    Ctx sc = parent;
+    sc.level = level;
+    sc.Rd = D;
+    if (!hit_context(h, sc)) return false;
+    out = shade(sc);
+    return true;
+  }
+
+  // ShaderStd.Eval (builtin/shader/std.go:77-296).
+  RGB shade(const Ctx& sg) const {
+    RGB zero{{0, 0, 0}};
+    if (sg.level > 3) return zero;
+    const Shader& sh = *sg.shader;
+    V3 Vt = cross(sg.N, sg.DdPdu);
+    if (len2(Vt) < 0.1f) Vt = cross(sg.N, sg.DdPdv);
+    Vt = normalize(Vt);
+    const V3 Ut = normalize(cross(sg.N, Vt));
+    const float diff_rough = sh.has(ORC_SH_DIFFUSE_ROUGHNESS) ? sh.p.diffuse_roughness : 0.5f;
+    const V3 wi = v3(-sg.Rd.x, -sg.Rd.y, -sg.Rd.z);
+    Bsdf diff{0, sg.lambda, project(Ut, Vt, sg.N, wi), diff_rough * diff_rough, Fresnel{}, Ut, Vt, sg.N};
+    RGB diff_col = sh.has(ORC_SH_DIFFUSE_COLOUR) ? RGB{{sh.p.diffuse_colour[0], sh.p.diffuse_colour[1], sh.p.diffuse_colour[2]}} : zero;
+    float dw = sh.has(ORC_SH_DIFFUSE_STRENGTH) ? sh.p.diffuse_strength : 0.0f;
+    float sw = sh.has(ORC_SH_SPEC1_STRENGTH) ? sh.p.spec1_strength : 0.0f;
+    const float total = dw + sw;
+    dw /= total;
+    sw /= total;
+    RGB diff_contrib = zero;
+    if (total == 0.0f) return zero;  // the reference panics ("Shader has no weight")
+    if (dw > 0.0f) {
+      for (const orc_trilight& L : R.lights) {
+        if ((int32_t)L.mesh == sg.geom) continue;  // LightsPrepare (scene.go:100-116)
+        const int NS = sg.level > 0 ? 1 : (1 << L.samples);
+        RGB col = evaluate_light_samples(sg, L, NS, diff);
+        rmul(col, diff_col);
+        radd(diff_contrib, col);
+      }
+      rscale(diff_contrib, dw);
+    }
+    Fresnel fr{0, sh.has(ORC_SH_IOR) ? sh.p.ior : 1.7f, {}, {}};
+    if (sh.p.spec1_fresnel == 1) {
+      RGB refl{{0.5f, 0.5f, 0.5f}}, edge{{0.5f, 0.5f, 0.5f}};
+      if (sh.has(ORC_SH_FRESNEL_REFL)) refl = RGB{{sh.p.spec1_fresnel_refl[0], sh.p.spec1_fresnel_refl[1], sh.p.spec1_fresnel_refl[2]}};
+      if (sh.has(ORC_SH_FRESNEL_EDGE))  // the reference assigns the edge colour to refl (std.go:185-187)
+        refl = RGB{{sh.p.spec1_fresnel_edge[0], sh.p.spec1_fresnel_edge[1], sh.p.spec1_fresnel_edge[2]}};
+      fr = Fresnel{1, 0, refl, edge};
+    }
+    RGB spec_contrib = zero;
+    if (sw > 0.0f) {
+      const float rough = sh.has(ORC_SH_SPEC1_ROUGHNESS) ? sh.p.spec1_roughness : 0.5f;
+      const RGB spec_col = sh.has(ORC_SH_SPEC1_COLOUR) ? RGB{{sh.p.spec1_colour[0], sh.p.spec1_colour[1], sh.p.spec1_colour[2]}} : zero;
+      Bsdf spec{rough == 0.0f ? 2 : 1, sg.lambda, project(Ut, Vt, sg.N, wi), rough * rough, fr, Ut, Vt, sg.N};
+      const int spec_samples = rough == 0.0f ? 1 : 0;
+      for (int i = 0; i < spec_samples; ++i) {
+        const uint64_t idx = sg.I * (uint64_t)spec_samples + (uint64_t)i;
+        const double r0 = vdc(idx, sg.scr0), r1 = sobol(idx, sg.scr1);
+        const V3 wo = bsdf_sample(spec, r0, r1);
+        const double pdf = bsdf_pdf(spec, wo);
+        if (dot(wo, sg.Ng) <= 0.0f) continue;
+        RGB child;
+        if (trace(offset_p(sg, 1), wo, sg.level + 1, sg, child)) {
+          Spectrum rho = bsdf_eval(spec, wo);
+          sscale(rho, 1.0f / (float)pdf);
+          RGB col = to_rgb(rho);
+          rmul(col, spec_col);
+          rmul(col, child);
+          for (float& c : col.c)
+            if (c < 0 || std::isnan(c)) c = 0;
+          radd(spec_contrib, col);
+        }
+      }
+      if (spec_samples > 0) rscale(spec_contrib, sw / (float)spec_samples);
+      if (rough > 0.0f) {
+        for (const orc_trilight& L : R.lights) {
+          if ((int32_t)L.mesh == sg.geom) continue;
+          const int NS = sg.level > 0 ? 1 : (1 << L.samples);
+          RGB col = evaluate_light_samples(sg, L, NS, spec);
+          rmul(col, spec_col);
+          radd(spec_contrib, col);
+        }
+      }
+    }
+    RGB contrib = zero;
+    radd(contrib, emission(sh));
+    radd(contrib, diff_contrib);
+    radd(contrib, spec_contrib);
+    return contrib;
+  }
+};
+
+// Per-pixel scramble: SplitMix64 of (seed, pixel, k).
+uint64_t scramble(uint64_t seed, uint64_t pix, uint32_t k) {
+  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (pix * 8ull + k + 1ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+struct orc_render {
+  Render r;
+};
+
+extern "C" {
+
+uint64_t orc_scramble(uint64_t seed, uint64_t pix, uint32_t k) { return scramble(seed, pix, k); }
+
+orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, uint32_t n_meshes,
+                              const uint32_t* off, const uint32_t* cnt, const uint32_t* list, const orc_shader* shaders,
+                              uint32_t n_shaders, const orc_trilight* lights, uint32_t n_lights, const orc_camera* cam) {
+  auto* o = new orc_render();
+  Render& r = o->r;
+  r.scene = scene;
+  for (uint32_t i = 0; i < n_meshes; ++i) {
+    r.meshes.push_back(orc_internal::mesh_view(meshes[i]));
+    r.mesh_shaders.emplace_back(list + off[i], list + off[i] + cnt[i]);
+  }
+  for (uint32_t i = 0; i < n_shaders; ++i) r.shaders.push_back(Shader{shaders[i]});
+  r.lights.assign(lights, lights + n_lights);
+  r.cam = *cam;
+  return o;
+}
+
+void orc_render_destroy(orc_render* r) { delete r; }
+
+int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, uint32_t iter_count, uint64_t seed,
+                   float* fb, int nthreads) {
+  const Render& R = o->r;
+  Renderer rr{R};
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  const size_t npix = (size_t)w * h;
+  for (uint32_t it = iter_begin; it < iter_begin + iter_count; ++it) {
+    const uint32_t j = it + 1;  // render(iter+1, ...) (core/render.go:192)
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+      for (;;) {
+        const size_t s = next.fetch_add(256);
+        if (s >= npix) break;
+        for (size_t pix = s; pix < std::min(npix, s + 256); ++pix) {
+          const uint32_t x = (uint32_t)(pix % w), y = (uint32_t)(pix / w);
+          double rx, ry;
+          orc_raster_xy(12, j, x, y, 0, 0, &rx, &ry);  // render.go:89
+          const double time = vdc(j, scramble(seed, pix, 2));
+          const double lambda = (720.0 - 450.0) * vdc(j, scramble(seed, pix, 3)) + 450.0;
+          const float Sx = (float)(-1.0 + 2.0 * (rx / (double)w));
+          const float Sy = -(float)(-1.0 + 2.0 * (ry / (double)h));
+          // Camera.ComputeRay, pinhole (camera.go:244-284)
+          const orc_camera& c = R.cam;
+          const float camu = Sx * c.tan_theta_focal;
+          const float camv = Sy * (c.tan_theta_focal / c.aspect);
+          const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
+          const float* M = c.m;
+          const V3 d = v3(M[0] * s3.x + M[4] * s3.y + M[8] * s3.z, M[1] * s3.x + M[5] * s3.y + M[9] * s3.z,
+                          M[2] * s3.x + M[6] * s3.y + M[10] * s3.z);
+          const V3 D = normalize(d);
+          const V3 P = v3(M[0] * 0.0f + M[4] * 0.0f + M[8] * 0.0f + M[12], M[1] * 0.0f + M[5] * 0.0f + M[9] * 0.0f + M[13],
+                          M[2] * 0.0f + M[6] * 0.0f + M[10] * 0.0f + M[14]);
+          Ctx sc{};
+          sc.lambda = (float)lambda;
+          sc.time = (float)time;
+          sc.I = j;
+          sc.scr0 = scramble(seed, pix, 4);
+          sc.scr1 = scramble(seed, pix, 5);
+          sc.level = 0;
+          RGB col{{0, 0, 0}};
+          rr.trace(P, D, 0, sc, col);
+          for (int k = 0; k < 3; ++k)
+            fb[pix * 3 + k] = (fb[pix * 3 + k] * (float)j + col.c[k]) / (float)(j + 1);  // render.go:127-129
+        }
+      }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) th.emplace_back(work);
+    for (auto& t : th) t.join();
+  }
+  return 0;
+}
+
+}  // extern "C"

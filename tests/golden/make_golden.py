@@ -6,7 +6,10 @@ Run from the repository root:  python tests/golden/make_golden.py [REFERENCE_DIR
    the reference holds them (math/ldseq/vdc_sobol_matrices52.go), parsed from
    the reference source.  Needs the reference checkout (default: the
    VERMEER_REFERENCE environment variable); skipped when it is absent.
-2. traversal_small.npz - small triangle soups, rays with awkward directions
+2. colour_tables.npz plus oracle/orc_colour_tables.h and
+   vermeer_gb300/csrc/colour_tables.h - the spectral tables of colour/*.go
+   (CIE observer bins, Smits spectra, sRGB matrix); same reference checkout.
+3. traversal_small.npz - small triangle soups, rays with awkward directions
    (axis-parallel, zero components, through vertices and edges, finite
    tmax) and the oracle's closest-hit and any-hit answers.  This pins the
    oracle itself, so a rebuild on another machine (x86_64 or aarch64) must
@@ -38,6 +41,53 @@ def parse_tables(ref_dir: str):
         return out
 
     return parse("vdcSobolMatrices"), parse("vdcSobolMatricesInv")
+
+
+def parse_colour_tables(ref_dir: str):
+    """CIE 1931 2-degree observer bins, the Smits basis spectra and the sRGB
+    matrix as the reference holds them (colour/*.go)."""
+    src = open(os.path.join(ref_dir, "colour", "cie1931_2deg.go")).read()
+
+    def bar(name):
+        i = src.index(name + ": []float32{")
+        j = src.index("},", i)
+        body = src[i + len(name) + 12:j]
+        return np.array([float(x) for x in re.findall(r"[-+]?\d*\.?\d+(?:[eE][-+]?\d+)?", body)], np.float32)
+
+    sm = open(os.path.join(ref_dir, "colour", "spectrum_smits9.go")).read()
+    smits = {}
+    for n in ("white", "cyan", "magenta", "yellow", "red", "green", "blue"):
+        mm = re.search(n + r"\s*=\s*smitsSpectrum\{([^}]*)\}", sm)
+        smits[n] = np.array([float(x) for x in mm.group(1).split(",")], np.float32)
+    srgb = open(os.path.join(ref_dir, "colour", "space_srgb.go")).read()
+    mat = np.array([float(x) for x in re.findall(r"-?\d+\.\d+", srgb)], np.float32)
+    return dict(cie_x=bar("xBar"), cie_y=bar("yBar"), cie_z=bar("zBar"), srgb=mat,
+                **{"smits_" + k: v for k, v in smits.items()})
+
+
+def write_colour_headers(t):
+    """The same data as C arrays for the oracle and for libvmr."""
+    def arr(name, vals, per=6):
+        rows = []
+        for i in range(0, len(vals), per):
+            rows.append("    " + ", ".join(repr(float(v)) + "f" for v in vals[i:i + per]) + ",")
+        return f"{name}[{len(vals)}] = {{\n" + "\n".join(rows) + "\n};\n"
+
+    body = ("// Generated by tests/golden/make_golden.py.  CIE 1931 2-degree standard\n"
+            "// observer in 5 nm bins from 360 nm, the Smits (1999) RGB->spectrum basis\n"
+            "// spectra in 10 bins over [380, 720) nm, and the sRGB XYZ->RGB matrix: the\n"
+            "// values of colour/cie1931_2deg.go, colour/spectrum_smits9.go and\n"
+            "// colour/space_srgb.go, which spectral parity requires.\n")
+    decl = {"oracle": "static const float ", "csrc": "static __constant__ const float "}
+    for where, path in (("oracle", os.path.join(ROOT, "oracle", "orc_colour_tables.h")),
+                        ("csrc", os.path.join(ROOT, "vermeer_gb300", "csrc", "colour_tables.h"))):
+        d = decl[where]
+        txt = body + "#pragma once\n"
+        txt += d + arr("kCieX", t["cie_x"]) + d + arr("kCieY", t["cie_y"]) + d + arr("kCieZ", t["cie_z"])
+        for k in ("white", "cyan", "magenta", "yellow", "red", "green", "blue"):
+            txt += d + arr("kSmits" + k.capitalize(), t["smits_" + k], per=10)
+        txt += d + arr("kSrgbFromXyz", t["srgb"], per=3)
+        open(path, "w").write(txt)
 
 
 def edge_rays(verts: np.ndarray, seed: int, n_random: int) -> np.ndarray:
@@ -82,7 +132,10 @@ def main():
     if ref and os.path.isdir(ref):
         fwd, inv = parse_tables(ref)
         np.savez_compressed(os.path.join(HERE, "vdc_sobol_tables.npz"), fwd=fwd, inv=inv)
-        print("wrote vdc_sobol_tables.npz")
+        ct = parse_colour_tables(ref)
+        np.savez_compressed(os.path.join(HERE, "colour_tables.npz"), **ct)
+        write_colour_headers(ct)
+        print("wrote vdc_sobol_tables.npz, colour_tables.npz and the colour table headers")
     else:
         print("reference checkout not given: keeping vdc_sobol_tables.npz")
 

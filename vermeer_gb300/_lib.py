@@ -53,6 +53,40 @@ class TraceStats(ctypes.Structure):
                 ("tri_tests", ctypes.c_uint64), ("kernel_ms", ctypes.c_float)]
 
 
+class ShaderStd(ctypes.Structure):
+    """vmr_shader_std (builtin/shader/std.go:25-47)."""
+    _fields_ = [("flags", U32), ("emission_colour", ctypes.c_float * 3), ("emission_strength", ctypes.c_float),
+                ("diffuse_colour", ctypes.c_float * 3), ("diffuse_strength", ctypes.c_float),
+                ("diffuse_roughness", ctypes.c_float), ("spec1_colour", ctypes.c_float * 3),
+                ("spec1_strength", ctypes.c_float), ("spec1_roughness", ctypes.c_float),
+                ("spec1_fresnel", ctypes.c_int), ("spec1_fresnel_refl", ctypes.c_float * 3),
+                ("spec1_fresnel_edge", ctypes.c_float * 3), ("ior", ctypes.c_float)]
+
+
+class TriLight(ctypes.Structure):
+    _fields_ = [("p0", ctypes.c_float * 3), ("p1", ctypes.c_float * 3), ("p2", ctypes.c_float * 3),
+                ("samples", ctypes.c_int), ("shader", U32), ("geom", U32)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_float * 16), ("tan_theta_focal", ctypes.c_float), ("aspect", ctypes.c_float),
+                ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
+
+
+class RenderParams(ctypes.Structure):
+    _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
+                ("seed", ctypes.c_uint64), ("max_batch_samples", U32)]
+
+
+class RenderStats(ctypes.Structure):
+    _fields_ = [("samples", ctypes.c_uint64), ("camera_rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
+                ("ms", ctypes.c_float)]
+
+
+SHADER_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
+                "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
+                "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
+
 assert ctypes.sizeof(QbvhNode) == 128 and ctypes.sizeof(MqbvhNode) == 40
 
 # name -> (restype, argtypes)
@@ -77,6 +111,11 @@ SIGNATURES = {
                                       ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
     "vmr_trace_scene": (ctypes.c_int, [P, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                        ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
+    "vmr_set_shaders": (ctypes.c_int, [P, P, U32]),
+    "vmr_mesh_set_shading": (ctypes.c_int, [P, U32, P, U32, P]),
+    "vmr_set_lights": (ctypes.c_int, [P, P, U32]),
+    "vmr_set_camera": (ctypes.c_int, [P, ctypes.POINTER(Camera)]),
+    "vmr_render": (ctypes.c_int, [P, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
     "vmr_trace_mesh_noalloc": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                               ctypes.POINTER(Hits)]),
 }
@@ -101,6 +140,25 @@ def load(build_if_missing: bool = True):
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def shader_struct(d: dict) -> ShaderStd:
+    """A ShaderStd parameter dict (keys as in SHADER_FLAGS, plus
+    'spec1_fresnel': 'Dielectric' | 'Metal') as the C struct."""
+    sh = ShaderStd()
+    flags = 0
+    for k, bit in SHADER_FLAGS.items():
+        if k in d:
+            flags |= bit
+            v = d[k]
+            if isinstance(getattr(sh, k), float):
+                setattr(sh, k, float(v))
+            else:
+                for i in range(3):
+                    getattr(sh, k)[i] = float(v[i])
+    sh.flags = flags
+    sh.spec1_fresnel = 1 if d.get("spec1_fresnel") == "Metal" else 0
+    return sh
 
 
 def exported_symbols():

@@ -201,3 +201,60 @@ class Context:
                     outputs=("prim", "geom", "t", "u", "v", "w")):
         """Scene.Trace over the two-level scene."""
         return self._trace(None, rays, shadow, counters, outputs)
+
+    # ------------------------------------------------------------ render
+    def set_shaders(self, shaders):
+        """Material table: ShaderStd parameter dicts (see _lib.SHADER_FLAGS)."""
+        arr = (_lib.ShaderStd * len(shaders))(*[_lib.shader_struct(d) for d in shaders])
+        self._check(self.L.vmr_set_shaders(self.h, arr, len(shaders)))
+
+    def mesh_set_shading(self, geom: int, shader_ids, normals=None):
+        ids = np.ascontiguousarray(shader_ids, np.uint32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        self._check(self.L.vmr_mesh_set_shading(self.h, geom, _p(ids), ids.size, _p(nrm)))
+
+    def set_lights(self, lights):
+        """TriLights: dicts with p0, p1, p2, samples, shader, geom."""
+        arr = (_lib.TriLight * len(lights))()
+        for i, d in enumerate(lights):
+            for k in ("p0", "p1", "p2"):
+                for c in range(3):
+                    getattr(arr[i], k)[c] = float(d[k][c])
+            arr[i].samples, arr[i].shader, arr[i].geom = int(d.get("samples", 1)), int(d["shader"]), int(d["geom"])
+        self._check(self.L.vmr_set_lights(self.h, arr, len(lights)))
+
+    def set_camera(self, cam: dict):
+        c = _lib.Camera()
+        for i in range(16):
+            c.m[i] = float(cam["m"][i])
+        c.tan_theta_focal, c.aspect, c.focal, c.radius = (float(cam[k]) for k in
+                                                         ("tan_theta_focal", "aspect", "focal", "radius"))
+        self._check(self.L.vmr_set_camera(self.h, ctypes.byref(c)))
+
+    def render(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, fb=None,
+               max_batch_samples: int = 0):
+        """core.Render iterations [iter_begin, iter_begin+iter_count) folded
+        into fb (float32 [height, width, 3]); returns (fb, stats)."""
+        if fb is None:
+            fb = np.zeros((height, width, 3), np.float32)
+        fb = np.ascontiguousarray(fb, np.float32)
+        p = _lib.RenderParams(width, height, iter_begin, iter_count, seed, max_batch_samples)
+        st = _lib.RenderStats()
+        self._check(self.L.vmr_render(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
+        return fb, dict(samples=st.samples, camera_rays=st.camera_rays, shadow_rays=st.shadow_rays, ms=st.ms)
+
+    def load_scene(self, scene: dict):
+        """Upload a render scene (vermeer_gb300.scenes format): meshes with
+        their shading, the two-level scene, materials, lights, camera.
+        Returns the geom ids."""
+        ids = []
+        for m in scene["meshes"]:
+            g = self.mesh_build(m["verts"], m["idxp"], shader_idx=m.get("face_shader"))
+            ids.append(g)
+        self.scene_build(ids)
+        self.set_shaders(scene["shaders"])
+        for g, m in zip(ids, scene["meshes"]):
+            self.mesh_set_shading(g, m["shaders"], m.get("normals"))
+        self.set_lights([dict(l, geom=ids[l["mesh"]]) for l in scene["lights"]])
+        self.set_camera(scene["camera"])
+        return ids

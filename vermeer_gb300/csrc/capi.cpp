@@ -13,71 +13,9 @@
 #include <vector>
 
 #include "accel.h"
+#include "ctx.h"
 #include "device.h"
 #include "vmr.h"
-
-using vmr::DMesh;
-using vmr::DScratch;
-using vmr::DTop;
-using vmr::GNode;
-using vmr::HostMesh;
-using vmr::HostTop;
-using vmr::MNode;
-
-namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-  ~DevBuf() { if (p) cudaFree(p); }
-  cudaError_t ensure(size_t n) {
-    if (n <= bytes) return cudaSuccess;
-    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e == cudaSuccess) bytes = n;
-    return e;
-  }
-  template <class T> T* as() const { return static_cast<T*>(p); }
-};
-
-struct MeshRec {
-  HostMesh host;
-  DevBuf nodes, tris, mnodes, mboxes, mtris, elem;
-  DMesh dmesh{};
-  float bounds6[6];
-};
-
-struct TopRec {
-  HostTop host;
-  DevBuf nodes, mnodes, mboxes, order, meshes;
-  DTop dtop{};
-  bool valid = false;
-};
-
-}  // namespace
-
-struct vmr_ctx {
-  int device = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  DevBuf scratch;                 // DScratch
-  DevBuf io;                      // rays + hits for host-pointer traces
-  DevBuf sortbuf;                 // ray keys, bucket offsets, order, key-ordered rays
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;  // start, after the sort, end
-  std::vector<std::unique_ptr<MeshRec>> meshes;
-  TopRec top;
-  vmr_tuning tuning{13, 0, 0, 0, 4};
-  // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
-  const float* mesh_bounds_of(const DMesh* d) const {
-    for (const auto& m : meshes)
-      if (&m->dmesh == d) return m->bounds6;
-    return nullptr;
-  }
-};
 
 namespace {
 

@@ -1,0 +1,93 @@
+// ctx.h - the context record behind vmr_ctx (shared by the C-ABI sources).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "accel.h"
+#include "device.h"
+#include "vmr.h"
+
+using vmr::DMesh;
+using vmr::DScratch;
+using vmr::DTop;
+using vmr::GNode;
+using vmr::HostMesh;
+using vmr::HostTop;
+using vmr::MNode;
+
+namespace vmr {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct MeshRec {
+  HostMesh host;
+  DevBuf nodes, tris, mnodes, mboxes, mtris, elem;
+  DMesh dmesh{};
+  float bounds6[6];
+  // shading (render.cu): PolyMesh.Shader, shader index and normals per
+  // leaf-order triangle
+  std::vector<uint32_t> shader_list;
+  bool has_normals = false;
+  DevBuf shlist, sidx, nrm;
+};
+
+struct RenderState {
+  std::vector<vmr_shader_std> shaders;
+  std::vector<vmr_tri_light> lights;
+  vmr_camera camera{};
+  bool has_camera = false;
+  DevBuf buf;
+};
+
+struct TopRec {
+  HostTop host;
+  DevBuf nodes, mnodes, mboxes, order, meshes;
+  DTop dtop{};
+  bool valid = false;
+};
+
+}  // namespace vmr
+
+using vmr::DevBuf;
+using vmr::MeshRec;
+using vmr::TopRec;
+
+struct vmr_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  DevBuf scratch;                 // DScratch
+  DevBuf io;                      // rays + hits for host-pointer traces
+  DevBuf sortbuf;                 // ray keys, bucket offsets, order, key-ordered rays
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;  // start, after the sort, end
+  std::vector<std::unique_ptr<MeshRec>> meshes;
+  TopRec top;
+  vmr::RenderState render;
+  vmr_tuning tuning{13, 0, 0, 0, 4};
+  // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
+  const float* mesh_bounds_of(const DMesh* d) const {
+    for (const auto& m : meshes)
+      if (&m->dmesh == d) return m->bounds6;
+    return nullptr;
+  }
+};
+
