@@ -287,6 +287,69 @@ int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* camera);
  * over every mesh, light meshes included. */
 int vmr_render(vmr_ctx* ctx, const vmr_render_params* params, float* fb, vmr_render_stats* stats);
 
+/* ------------------------------------------------- extended path tracing */
+/* No counterpart in the reference, which renders direct light only (plus
+ * mirror recursion) and has no environment light; its QuadLight panics in
+ * ValidSample (builtin/light/quad.go:87-89).  The extended mode is a unidirectional
+ * path tracer over the same scene, materials, TriLights and camera:
+ *   - indirect bounces up to max_depth scattering events, Russian roulette
+ *     from rr_depth on (survival min(0.95, max throughput));
+ *   - next-event estimation with one light picked uniformly from TriLights,
+ *     quad lights and the environment, combined with BSDF sampling by the
+ *     power heuristic;
+ *   - ShaderStd as the mixture dw*Diffuse + sw*GGX (weights normalised;
+ *     diffuse roughness 0 = Lambert, else OrenNayar; GGX alpha =
+ *     Spec1Roughness^4 as the reference's, sampled by the visible-normal-free
+ *     D(m)cos(m) method with the correct 1/(4|wo.m|) Jacobian; roughness 0
+ *     = a perfect mirror); surfaces are two-sided, emitters one-sided;
+ *   - RGB throughout (no hero wavelength); camera rays equal reference mode's;
+ *   - per-sample random numbers from a counter-based SplitMix64 hash of
+ *     (seed, pixel, iteration, dimension).
+ * A quad light is the parallelogram p0, p0+e1, p0+e1+e2, p0+e2 emitting on the
+ * side of e1 x e2; geom is its emissive mesh (two triangles with that
+ * winding), uploaded by the caller. */
+typedef struct {
+    float p0[3], e1[3], e2[3];
+    uint32_t shader;
+    uint32_t geom;
+} vmr_quad_light;
+
+int vmr_set_quad_lights(vmr_ctx* ctx, const vmr_quad_light* lights, uint32_t n);
+/* Constant environment radiance seen by rays that leave the scene (0,0,0:
+ * no environment light). */
+int vmr_set_env_light(vmr_ctx* ctx, const float radiance[3]);
+
+typedef struct {
+    uint32_t width, height;
+    uint32_t iter_begin, iter_count;  /* iterations (one sample per pixel each) */
+    uint64_t seed;
+    uint32_t max_depth;               /* scattering events per path */
+    uint32_t rr_depth;                /* Russian roulette from this event on */
+    uint32_t max_batch_samples;       /* paths per wavefront batch (0: 2M) */
+    uint32_t flags;                   /* VMR_PATH_* */
+    double* fb64;                     /* optional host width*height*3: the same
+                                         running mean folded in float64 */
+} vmr_path_params;
+
+enum {
+    VMR_PATH_NO_GRAPH = 1   /* launch the bounce loop stage by stage instead
+                               of replaying its CUDA graph */
+};
+
+typedef struct {
+    uint64_t samples;        /* pixel samples (paths) */
+    uint64_t rays;           /* extension rays traced (camera rays included) */
+    uint64_t shadow_rays;
+    uint32_t graph_replays;  /* batches run by replaying the captured graph */
+    float ms;                /* device time */
+} vmr_path_stats;
+
+/* Iterations iter_begin..iter_begin+iter_count-1 of every pixel folded into
+ * fb (host, width*height*3 floats, in/out) as buf = (buf*i + L)/(i+1),
+ * i = the 0-based iteration: the exact mean of the samples (the reference's
+ * fold starts at i+1 and so counts the initial buffer as a sample, F6). */
+int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* params, float* fb, vmr_path_stats* stats);
+
 /* -------------------------------------------------------------- no-alloc */
 /* No counterpart in the reference.  For callers that must not have a library
  * allocate device memory while they run (they manage the whole device

@@ -165,6 +165,27 @@ int orc_render_run(orc_render* r, uint32_t w, uint32_t h, uint32_t iter_begin, u
  * math/rand (core/render.go:166-176). */
 uint64_t orc_scramble(uint64_t seed, uint64_t pix, uint32_t k);
 
+/* Extended path tracer (no reference counterpart; orc_pt.cpp restates the
+ * project's own estimator).  Quad light: parallelogram p0, p0+e1, p0+e1+e2,
+ * p0+e2 emitting toward e1 x e2, mesh = its emissive mesh's index. */
+typedef struct {
+    float p0[3], e1[3], e2[3];
+    uint32_t shader, mesh;
+} orc_quad_light;
+typedef struct {
+    uint32_t width, height, iter_begin, iter_count;
+    uint64_t seed;
+    uint32_t max_depth, rr_depth;
+    float env[3];
+} orc_pt_params;
+/* precision 32: float32 shading in the CUDA kernels' operation order;
+ * 64: float64 shading.  fb (float, may be NULL) and fb64 (double, may be
+ * NULL) both receive the running mean buf = (buf*j + L)/(j+1). */
+int orc_pt_run(const orc_render* r, const orc_quad_light* quads, uint32_t n_quads, const orc_pt_params* p,
+               float* fb, double* fb64, int precision, int nthreads);
+/* Random number `dim` of pixel sample (pix, j = iteration + 1). */
+float orc_pt_rnd(uint64_t seed, uint64_t pix, uint32_t j, uint32_t dim);
+
 #ifdef __cplusplus
 }
 #endif

@@ -118,6 +118,21 @@ def _register_render(L):
                                  ctypes.c_uint64, P, ctypes.c_int]
     L.orc_scramble.restype = ctypes.c_uint64
     L.orc_scramble.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32]
+    L.orc_pt_run.restype = ctypes.c_int
+    L.orc_pt_run.argtypes = [P, P, ctypes.c_uint32, P, P, P, ctypes.c_int, ctypes.c_int]
+    L.orc_pt_rnd.restype = ctypes.c_float
+    L.orc_pt_rnd.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
+
+
+class OrcQuadLight(ctypes.Structure):
+    _fields_ = [("p0", ctypes.c_float * 3), ("e1", ctypes.c_float * 3), ("e2", ctypes.c_float * 3),
+                ("shader", ctypes.c_uint32), ("mesh", ctypes.c_uint32)]
+
+
+class OrcPtParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("iter_begin", ctypes.c_uint32),
+                ("iter_count", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("max_depth", ctypes.c_uint32),
+                ("rr_depth", ctypes.c_uint32), ("env", ctypes.c_float * 3)]
 
 
 class Render:
@@ -161,6 +176,14 @@ class Render:
         c = scene["camera"]
         cam.tan_theta_focal, cam.aspect, cam.focal, cam.radius = (float(c[k]) for k in
                                                                ("tan_theta_focal", "aspect", "focal", "radius"))
+        qs = scene.get("quad_lights", [])
+        self._quads = (OrcQuadLight * len(qs))()
+        for i, d in enumerate(qs):
+            for k in ("p0", "e1", "e2"):
+                for c in range(3):
+                    getattr(self._quads[i], k)[c] = float(d[k][c])
+            self._quads[i].shader, self._quads[i].mesh = int(d["shader"]), int(d["mesh"])
+        self._env = tuple(float(x) for x in scene.get("env", (0.0, 0.0, 0.0)))
         arr = (ctypes.c_void_p * len(self.meshes))(*[m.h for m in self.meshes])
         self._keep = (counts, offs, lst, shs, lts, cam, arr)
         self.h = lib().orc_render_create(self.scene.h, arr, len(self.meshes), _ptr(offs), _ptr(counts), _ptr(lst),
@@ -170,6 +193,25 @@ class Render:
         if getattr(self, "h", None):
             lib().orc_render_destroy(self.h)
             self.h = None
+
+    def run_path(self, width, height, iter_begin, iter_count, seed, max_depth=4, rr_depth=3, precision=32, fb=None,
+                 fb64=None, nthreads=0):
+        """The extended path tracer (orc_pt.cpp) over this scene plus its
+        'quad_lights' and 'env'.  Returns (fb float32, fb64 float64)."""
+        if fb is None:
+            fb = np.zeros((height, width, 3), np.float32)
+        if fb64 is None:
+            fb64 = np.zeros((height, width, 3), np.float64)
+        fb = np.ascontiguousarray(fb, np.float32)
+        fb64 = np.ascontiguousarray(fb64, np.float64)
+        quads = self._quads
+        p = OrcPtParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth,
+                        (ctypes.c_float * 3)(*[float(x) for x in self._env]))
+        rc = lib().orc_pt_run(self.h, quads, len(quads), ctypes.byref(p), _ptr(fb), _ptr(fb64), int(precision),
+                              int(nthreads))
+        if rc != 0:
+            raise RuntimeError("orc_pt_run failed")
+        return fb, fb64
 
     def run(self, width, height, iter_begin, iter_count, seed, fb=None, nthreads=0):
         if fb is None:

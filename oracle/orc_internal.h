@@ -2,6 +2,7 @@
 // TEST INFRASTRUCTURE ONLY (see orc.h).
 #pragma once
 #include <cstdint>
+#include <vector>
 
 #include "orc.h"
 
@@ -27,5 +28,22 @@ struct MeshView {
   bool motion;
 };
 MeshView mesh_view(const orc_mesh* m);
+
+// What orc_render_create was given, for the extended path tracer (orc_pt.cpp).
+struct RenderScene {
+  const orc_scene* scene;
+  std::vector<MeshView> meshes;
+  std::vector<std::vector<uint32_t>> mesh_shaders;  // PolyMesh.Shader per mesh
+  std::vector<orc_shader> shaders;
+  std::vector<orc_trilight> lights;
+  orc_camera cam;
+};
+RenderScene render_scene(const orc_render* r);
+
+// core.Render's per-sample setup and the pinhole Camera.ComputeRay
+// (core/render.go:89-120, builtin/camera/camera.go:244-284) for iteration j
+// (render(iter+1)) of pixel pix: ray origin, direction and time.
+void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uint64_t pix, uint64_t seed, float P[3],
+                    float D[3], float* time);
 
 }  // namespace orc_internal

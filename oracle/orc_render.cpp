@@ -747,6 +747,44 @@ struct orc_render {
   Render r;
 };
 
+namespace orc_internal {
+
+void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uint64_t pix, uint64_t seed, float Po[3],
+                    float Do[3], float* time) {
+  const uint32_t x = (uint32_t)(pix % w), y = (uint32_t)(pix / w);
+  double rx, ry;
+  orc_raster_xy(12, j, x, y, 0, 0, &rx, &ry);  // render.go:89
+  *time = (float)vdc(j, scramble(seed, pix, 2));
+  const float Sx = (float)(-1.0 + 2.0 * (rx / (double)w));
+  const float Sy = -(float)(-1.0 + 2.0 * (ry / (double)h));
+  // Camera.ComputeRay, pinhole (camera.go:244-284)
+  const float camu = Sx * c.tan_theta_focal;
+  const float camv = Sy * (c.tan_theta_focal / c.aspect);
+  const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
+  const float* M = c.m;
+  const V3 d = v3(M[0] * s3.x + M[4] * s3.y + M[8] * s3.z, M[1] * s3.x + M[5] * s3.y + M[9] * s3.z,
+                  M[2] * s3.x + M[6] * s3.y + M[10] * s3.z);
+  const V3 D = normalize(d);
+  const V3 P = v3(M[0] * 0.0f + M[4] * 0.0f + M[8] * 0.0f + M[12], M[1] * 0.0f + M[5] * 0.0f + M[9] * 0.0f + M[13],
+                  M[2] * 0.0f + M[6] * 0.0f + M[10] * 0.0f + M[14]);
+  Po[0] = P.x; Po[1] = P.y; Po[2] = P.z;
+  Do[0] = D.x; Do[1] = D.y; Do[2] = D.z;
+}
+
+RenderScene render_scene(const orc_render* o) {
+  const Render& r = o->r;
+  RenderScene s;
+  s.scene = r.scene;
+  s.meshes = r.meshes;
+  s.mesh_shaders = r.mesh_shaders;
+  for (const Shader& sh : r.shaders) s.shaders.push_back(sh.p);
+  s.lights = r.lights;
+  s.cam = r.cam;
+  return s;
+}
+
+}  // namespace orc_internal
+
 extern "C" {
 
 uint64_t orc_scramble(uint64_t seed, uint64_t pix, uint32_t k) { return scramble(seed, pix, k); }
@@ -783,24 +821,11 @@ int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, u
         const size_t s = next.fetch_add(256);
         if (s >= npix) break;
         for (size_t pix = s; pix < std::min(npix, s + 256); ++pix) {
-          const uint32_t x = (uint32_t)(pix % w), y = (uint32_t)(pix / w);
-          double rx, ry;
-          orc_raster_xy(12, j, x, y, 0, 0, &rx, &ry);  // render.go:89
-          const double time = vdc(j, scramble(seed, pix, 2));
+          float Pf[3], Df[3], tf;
+          orc_internal::camera_primary(R.cam, w, h, j, pix, seed, Pf, Df, &tf);
+          const V3 P = v3(Pf[0], Pf[1], Pf[2]), D = v3(Df[0], Df[1], Df[2]);
+          const double time = (double)tf;
           const double lambda = (720.0 - 450.0) * vdc(j, scramble(seed, pix, 3)) + 450.0;
-          const float Sx = (float)(-1.0 + 2.0 * (rx / (double)w));
-          const float Sy = -(float)(-1.0 + 2.0 * (ry / (double)h));
-          // Camera.ComputeRay, pinhole (camera.go:244-284)
-          const orc_camera& c = R.cam;
-          const float camu = Sx * c.tan_theta_focal;
-          const float camv = Sy * (c.tan_theta_focal / c.aspect);
-          const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
-          const float* M = c.m;
-          const V3 d = v3(M[0] * s3.x + M[4] * s3.y + M[8] * s3.z, M[1] * s3.x + M[5] * s3.y + M[9] * s3.z,
-                          M[2] * s3.x + M[6] * s3.y + M[10] * s3.z);
-          const V3 D = normalize(d);
-          const V3 P = v3(M[0] * 0.0f + M[4] * 0.0f + M[8] * 0.0f + M[12], M[1] * 0.0f + M[5] * 0.0f + M[9] * 0.0f + M[13],
-                          M[2] * 0.0f + M[6] * 0.0f + M[10] * 0.0f + M[14]);
           Ctx sc{};
           sc.lambda = (float)lambda;
           sc.time = (float)time;

@@ -1,0 +1,182 @@
+"""Extended path tracer (vmr_render_path): indirect bounces, NEE with the
+power heuristic, Russian roulette, TriLights, quad lights and a constant
+environment.  No reference counterpart: the oracle (oracle/orc_pt.cpp)
+restates the project's own estimator in float32 (the CUDA operation order)
+and in float64.
+
+Tolerances.
+* CUDA vs the float32 oracle at equal samples: the same float32 operations;
+  float64 transcendentals may differ by one float32 ulp after rounding in rare
+  cases, which can flip a path decision (Russian roulette, lobe choice) for
+  that sample.  99.5% of pixels agree within 1e-5 relative and the image
+  means within 1e-4 relative.
+* Unbiasedness: the furnace (convex Lambert sphere under a constant
+  environment) converges to albedo x environment; the sphere pixels' mean
+  must be within 5 standard errors of it and environment pixels exactly equal
+  to the environment.
+* Convergence against the float64 oracle with independent seeds: the image
+  means agree within 5 combined standard errors and the 4x4-block relMSE is
+  below 0.01.
+"""
+import numpy as np
+import pytest
+
+from vermeer_gb300 import scenes
+
+REL = 1e-5
+FRAC_EQUAL = 0.995
+
+
+@pytest.fixture(scope="module")
+def room():
+    return scenes.small_room_ext(2048, seed=3)
+
+
+@pytest.fixture(scope="module")
+def oracle_room(orc, room):
+    return orc.Render(room)
+
+
+def _disc_masks(w, h, inner=0.55, outer=0.85):
+    """Pixels certainly on / certainly off the furnace sphere (image-plane
+    radius relative to half the image; the sphere spans ~0.71)."""
+    y, x = np.mgrid[0:h, 0:w]
+    r = np.hypot((x + 0.5) / w * 2 - 1, (y + 0.5) / h * 2 - 1)
+    return r < inner, r > outer
+
+
+def _block_relmse(a, b, k=4):
+    h, w, _ = a.shape
+    a = a[: h // k * k, : w // k * k].reshape(h // k, k, w // k, k, 3).mean((1, 3))
+    b = b[: h // k * k, : w // k * k].reshape(h // k, k, w // k, k, 3).mean((1, 3))
+    return float(np.mean((a - b) ** 2 / (b * b + 1e-2)))
+
+
+# ------------------------------------------------------------------ CPU ----
+def test_oracle_pt_random_numbers(orc):
+    lib = orc.lib()
+    vals = np.array([lib.orc_pt_rnd(7, p, j, d) for p in range(4) for j in (1, 2) for d in range(16)])
+    assert ((vals >= 0) & (vals < 1)).all()
+    assert np.all(vals * (1 << 24) == np.floor(vals * (1 << 24)))  # 24-bit grid
+    assert len(set(vals.tolist())) > 120
+
+
+def test_oracle_pt_deterministic(oracle_room):
+    a, _ = oracle_room.run_path(24, 24, 0, 2, 9, nthreads=1)
+    b, _ = oracle_room.run_path(24, 24, 0, 2, 9, nthreads=5)
+    assert a.tobytes() == b.tobytes()
+
+
+def test_oracle_pt_iterations_fold(oracle_room):
+    full, full64 = oracle_room.run_path(16, 16, 0, 4, 9)
+    part, part64 = oracle_room.run_path(16, 16, 0, 1, 9)
+    part, part64 = oracle_room.run_path(16, 16, 1, 3, 9, fb=part, fb64=part64)
+    assert full.tobytes() == part.tobytes() and full64.tobytes() == part64.tobytes()
+
+
+def test_oracle_pt_furnace_unbiased(orc):
+    sc = scenes.furnace(0.5, 1.0, subdiv=8)
+    r = orc.Render(sc)
+    _, fb64 = r.run_path(32, 32, 0, 128, 11, max_depth=6, rr_depth=1, precision=64)
+    on, off = _disc_masks(32, 32)
+    v = fb64[on][:, 0]
+    assert abs(v.mean() - 0.5) < 5 * v.std() / np.sqrt(v.size), (v.mean(), v.std())
+    assert np.all(fb64[off] == 1.0)
+
+
+def test_oracle_pt_float_close_to_double(oracle_room):
+    f32, _ = oracle_room.run_path(24, 24, 0, 8, 13, precision=32)
+    _, f64 = oracle_room.run_path(24, 24, 0, 8, 13, precision=64)
+    close = np.abs(f32 - f64) <= 1e-3 * (1 + np.abs(f64))
+    assert close.all(-1).mean() > 0.97
+    assert abs(f32.mean() - f64.mean()) < 1e-3 * f64.mean()
+
+
+def test_oracle_pt_light_kinds_contribute(orc, room):
+    """Each light kind alone gives a non-black image, and the sum of the
+    three single-kind images matches the full image statistically."""
+    base = dict(room)
+    full = orc.Render(base).run_path(24, 24, 0, 64, 5, max_depth=1, precision=64)[1].mean()
+    parts = []
+    for keep in ("tri", "quad", "env"):
+        sc = dict(base)
+        sc["lights"] = base["lights"] if keep == "tri" else []
+        sc["quad_lights"] = base["quad_lights"] if keep == "quad" else []
+        sc["env"] = base["env"] if keep == "env" else (0.0, 0.0, 0.0)
+        if keep != "tri":  # remove the tri panels' emission too
+            sc["shaders"] = [dict(s) for s in base["shaders"]]
+            for l in base["lights"]:
+                sc["shaders"][l["shader"]]["emission_strength"] = 0.0
+        if keep != "quad":
+            sc["shaders"] = [dict(s) for s in sc["shaders"]]
+            for q in base["quad_lights"]:
+                sc["shaders"][q["shader"]]["emission_strength"] = 0.0
+        m = orc.Render(sc).run_path(24, 24, 0, 64, 5, max_depth=1, precision=64)[1].mean()
+        assert m > 0, keep
+        parts.append(m)
+    assert abs(sum(parts) - full) < 0.05 * full, (parts, full)
+
+
+# ------------------------------------------------------------------ GPU ----
+@pytest.mark.gpu
+def test_pt_matches_float_oracle(ctx, room, oracle_room):
+    ctx.load_scene(room)
+    ref, _ = oracle_room.run_path(48, 40, 0, 4, 21, max_depth=5, rr_depth=2, precision=32)
+    got, st = ctx.render_path(48, 40, 0, 4, 21, max_depth=5, rr_depth=2)
+    assert np.isfinite(got).all()
+    ok = (np.abs(got - ref) <= REL * (1 + np.abs(ref))).all(-1)
+    assert ok.mean() >= FRAC_EQUAL, ok.mean()
+    assert abs(got.mean() - ref.mean()) <= 1e-4 * ref.mean()
+    assert st["samples"] == 48 * 40 * 4
+    assert st["rays"] >= 48 * 40 * 4 and st["shadow_rays"] > 0
+
+
+@pytest.mark.gpu
+def test_pt_graph_batches_and_calls_are_exact(ctx, room):
+    ctx.load_scene(room)
+    a, sa = ctx.render_path(32, 32, 0, 6, 4)
+    b, sb = ctx.render_path(32, 32, 0, 6, 4, graph=False)
+    c, sc_ = ctx.render_path(32, 32, 0, 6, 4, max_batch_samples=32 * 32 * 2)
+    d, _ = ctx.render_path(32, 32, 0, 2, 4)
+    d, _ = ctx.render_path(32, 32, 2, 4, 4, fb=d)
+    assert a.tobytes() == b.tobytes() == c.tobytes() == d.tobytes()
+    assert sa["graph_replays"] == 1 and sb["graph_replays"] == 0 and sc_["graph_replays"] == 3
+    assert sa["rays"] == sb["rays"] == sc_["rays"]
+
+
+@pytest.mark.gpu
+def test_pt_fp64_accumulation(ctx, room):
+    ctx.load_scene(room)
+    fb64 = np.zeros((16, 16, 3), np.float64)
+    fb, _ = ctx.render_path(16, 16, 0, 8, 4, fb64=fb64)
+    assert np.abs(fb - fb64).max() < 1e-5 * (1 + np.abs(fb64).max())
+
+
+@pytest.mark.gpu
+def test_pt_furnace_unbiased(ctx):
+    sc = scenes.furnace(0.5, 1.0, subdiv=12)
+    ctx.load_scene(sc)
+    fb64 = np.zeros((64, 64, 3), np.float64)
+    ctx.render_path(64, 64, 0, 512, 17, max_depth=8, rr_depth=1, fb64=fb64)
+    on, off = _disc_masks(64, 64)
+    v = fb64[on][:, 0]
+    assert abs(v.mean() - 0.5) < 5 * v.std() / np.sqrt(v.size), (v.mean(), v.std())
+    assert np.all(fb64[off] == 1.0)
+
+
+@pytest.mark.gpu
+def test_pt_converges_to_fp64_oracle(ctx, room, oracle_room):
+    """Independent seeds: the GPU image and the float64 oracle image estimate
+    the same expectation."""
+    ctx.load_scene(room)
+    n = 256
+    g64 = np.zeros((32, 32, 3), np.float64)
+    ctx.render_path(32, 32, 0, n, 1001, max_depth=4, fb64=g64)
+    _, o64 = oracle_room.run_path(32, 32, 0, n, 2002, max_depth=4, precision=64)
+    # per-pixel standard errors are not known; compare image means with the
+    # spread of 8x8-block means as the noise estimate
+    bg = g64.reshape(4, 8, 4, 8, 3).mean((1, 3)).ravel()
+    bo = o64.reshape(4, 8, 4, 8, 3).mean((1, 3)).ravel()
+    se = np.sqrt(np.var(bg - bo) / bg.size)
+    assert abs(bg.mean() - bo.mean()) < 5 * se + 1e-6, (bg.mean(), bo.mean(), se)
+    assert _block_relmse(g64, o64) < 0.01

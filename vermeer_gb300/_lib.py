@@ -83,6 +83,24 @@ class RenderStats(ctypes.Structure):
                 ("ms", ctypes.c_float)]
 
 
+class QuadLight(ctypes.Structure):
+    _fields_ = [("p0", ctypes.c_float * 3), ("e1", ctypes.c_float * 3), ("e2", ctypes.c_float * 3),
+                ("shader", U32), ("geom", U32)]
+
+
+class PathParams(ctypes.Structure):
+    _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
+                ("seed", ctypes.c_uint64), ("max_depth", U32), ("rr_depth", U32), ("max_batch_samples", U32),
+                ("flags", U32), ("fb64", P)]
+
+
+class PathStats(ctypes.Structure):
+    _fields_ = [("samples", ctypes.c_uint64), ("rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
+                ("graph_replays", U32), ("ms", ctypes.c_float)]
+
+
+PATH_NO_GRAPH = 1
+
 SHADER_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
                 "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
                 "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
@@ -116,6 +134,9 @@ SIGNATURES = {
     "vmr_set_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_camera": (ctypes.c_int, [P, ctypes.POINTER(Camera)]),
     "vmr_render": (ctypes.c_int, [P, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
+    "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),
+    "vmr_set_env_light": (ctypes.c_int, [P, P]),
+    "vmr_render_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, ctypes.POINTER(PathStats)]),
     "vmr_trace_mesh_noalloc": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                               ctypes.POINTER(Hits)]),
 }

@@ -223,6 +223,37 @@ class Context:
             arr[i].samples, arr[i].shader, arr[i].geom = int(d.get("samples", 1)), int(d["shader"]), int(d["geom"])
         self._check(self.L.vmr_set_lights(self.h, arr, len(lights)))
 
+    def set_quad_lights(self, lights):
+        """Quad lights: dicts with p0, e1, e2, shader, geom."""
+        arr = (_lib.QuadLight * len(lights))()
+        for i, d in enumerate(lights):
+            for k in ("p0", "e1", "e2"):
+                for c in range(3):
+                    getattr(arr[i], k)[c] = float(d[k][c])
+            arr[i].shader, arr[i].geom = int(d["shader"]), int(d["geom"])
+        self._check(self.L.vmr_set_quad_lights(self.h, arr, len(lights)))
+
+    def set_env_light(self, radiance):
+        r = (ctypes.c_float * 3)(*[float(x) for x in radiance])
+        self._check(self.L.vmr_set_env_light(self.h, r))
+
+    def render_path(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, max_depth: int = 4,
+                    rr_depth: int = 3, fb=None, fb64=None, max_batch_samples: int = 0, graph: bool = True):
+        """The extended path tracer: iterations [iter_begin, iter_begin +
+        iter_count) folded into fb (float32 [height, width, 3]) and, when
+        given, fb64 (float64).  Returns (fb, stats)."""
+        if fb is None:
+            fb = np.zeros((height, width, 3), np.float32)
+        fb = np.ascontiguousarray(fb, np.float32)
+        if fb64 is not None:
+            assert fb64.dtype == np.float64 and fb64.flags.c_contiguous and fb64.shape == (height, width, 3)
+        p = _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
+                            0 if graph else _lib.PATH_NO_GRAPH, None if fb64 is None else _p(fb64))
+        st = _lib.PathStats()
+        self._check(self.L.vmr_render_path(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
+        return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,
+                        graph_replays=st.graph_replays, ms=st.ms)
+
     def set_camera(self, cam: dict):
         c = _lib.Camera()
         for i in range(16):
@@ -256,5 +287,7 @@ class Context:
         for g, m in zip(ids, scene["meshes"]):
             self.mesh_set_shading(g, m["shaders"], m.get("normals"))
         self.set_lights([dict(l, geom=ids[l["mesh"]]) for l in scene["lights"]])
+        self.set_quad_lights([dict(q, geom=ids[q["mesh"]]) for q in scene.get("quad_lights", [])])
+        self.set_env_light(scene.get("env", (0.0, 0.0, 0.0)))
         self.set_camera(scene["camera"])
         return ids

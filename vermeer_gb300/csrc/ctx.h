@@ -49,12 +49,27 @@ struct MeshRec {
   DevBuf shlist, sidx, nrm;
 };
 
+// The extended path tracer's captured bounce loop (pathtrace.cu): valid for
+// the buffers, scene tables and launch shapes it was captured with.
+struct PathGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> key;
+  ~PathGraph() { if (exec) cudaGraphExecDestroy(exec); }
+};
+
 struct RenderState {
   std::vector<vmr_shader_std> shaders;
   std::vector<vmr_tri_light> lights;
+  std::vector<vmr_quad_light> quads;
+  float env[3] = {0.f, 0.f, 0.f};
   vmr_camera camera{};
   bool has_camera = false;
-  DevBuf buf;
+  DevBuf buf;      // reference mode batch buffers
+  DevBuf ptbuf;    // extended mode batch buffers
+  void* pt_host = nullptr;  // pinned per-batch parameters (extended mode)
+  size_t pt_host_bytes = 0;
+  PathGraph graph;
+  ~RenderState() { if (pt_host) cudaFreeHost(pt_host); }
 };
 
 struct TopRec {

@@ -1,0 +1,850 @@
+// pathtrace.cu - extended path tracer (vmr_render_path): indirect bounces,
+// next-event estimation with the power heuristic, Russian roulette, quad and
+// environment lights.  No reference counterpart (the reference renders
+// direct light only); the estimator is specified in include/vmr.h and
+// restated independently by the float32/float64 oracle.
+//
+// Wavefront per batch of whole iterations (n paths, one per (iteration,
+// pixel)):
+//   k_pt_generate            camera rays (the reference mode's) into queue 0
+//   for d = 0 .. max_depth:
+//     trace                  closest hit of queue d (count read on the device)
+//     k_pt_shade<d>          emission / environment with MIS, light sample +
+//                            shadow ray into the shadow queue, BSDF sample +
+//                            continuation into queue d+1 (warp-aggregated
+//                            appends), Russian roulette
+//     trace (d < max_depth)  any hit of the shadow queue
+//     k_pt_resolve           unoccluded shadow rays add their contribution
+//   k_pt_accumulate          per pixel, the batch's iterations in order:
+//                            buf = (buf*i + L)/(i+1), i the 0-based iteration
+//                            (float, optional float64)
+// Every queue length lives in device memory and every kernel reads it there,
+// so a batch runs without host synchronisation; the whole sequence is
+// captured once as a CUDA graph and replayed per batch (the batch's first
+// iteration and path count are copied in before each replay).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+#include "device.h"
+#include "shade_common.cuh"
+#include "vmr.h"
+
+namespace vmr {
+namespace {
+
+constexpr int kPtMaxDepth = 32;
+constexpr int kPtBlock = 256;
+
+// One light of the path tracer's light list (TriLights, quad lights, the
+// environment, in that order).
+struct PtLight {
+  int kind;  // 0 triangle (p0, a = p1, b = p2), 1 quad (p0, a = e1, b = e2), 2 environment
+  float p0[3], a[3], b[3];
+  float N[3];  // emitting side
+  float area;
+  float Le[3];
+  int32_t geom;
+};
+
+// Per-batch values copied in before each replay.
+struct PtIter {
+  uint32_t iter0;  // first iteration of the batch
+  uint32_t iters;  // iterations in the batch
+  unsigned long long n;  // paths = iters * npix
+};
+
+struct PtBatch {
+  uint32_t width, height, npix;
+  uint32_t nl;        // lights
+  uint32_t max_depth, rr_depth;
+  uint32_t has_env;
+  uint32_t cap;       // path capacity of the buffers
+  float env[3];
+  float sel;          // 1/nl
+  uint64_t seed;
+  vmr_camera cam;
+  const PtIter* it;
+  const vmr_shader_std* shaders;
+  const PtLight* lights;
+  const RMesh* meshes;
+  const int32_t* light_of_geom;
+  uint32_t n_geoms;
+  // per path
+  float *bx, *by, *bz;   // throughput
+  float *lx, *ly, *lz;   // radiance
+  float* pdf;            // pdf of the last BSDF sample (0: camera or mirror)
+  unsigned long long* key;
+  // extension queues (ping-pong) and the hit record of the current one
+  float* qray[2];        // 8 * cap floats: px py pz dx dy dz tmax time
+  uint32_t* qpath[2];
+  int32_t *hprim, *hgeom;
+  float *ht, *hu, *hv, *hw;
+  // shadow queue
+  float* sray;           // 8 * cap
+  uint32_t* spath;
+  float* scontrib;       // 3 * cap
+  int32_t* shit;
+  unsigned long long* qlen;  // [kPtMaxDepth + 2]
+  unsigned long long* slen;  // [kPtMaxDepth + 1]
+  unsigned long long* totals;  // [2]: extension rays, shadow rays
+  const DScratch* scr;         // the traversal launches' scratch, 2 per bounce
+  int* status;                 // worst traversal status over all batches
+  float* fb;
+  double* fb64;
+};
+
+// ------------------------------------------------------------- random ----
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+constexpr uint64_t kGold = 0x9E3779B97F4A7C15ull;
+__device__ __forceinline__ uint64_t sample_key(uint64_t seed, uint64_t pix, uint64_t j) {
+  return mix64(mix64(seed + kGold * (pix + 1)) + kGold * (j + 1));
+}
+// 24 random bits as a float in [0, 1), exact in float32.
+__device__ __forceinline__ float rnd(uint64_t key, uint32_t dim) {
+  return (float)(mix64(key + kGold * (uint64_t)(dim + 1)) >> 40) * 5.9604644775390625e-08f;
+}
+
+constexpr float kInv4Pi = 0.0795774715f;  // float32(1/(4 pi))
+
+// ----------------------------------------------------------- material ----
+struct Mat {
+  float dw, sw;
+  V3 cd, cs;
+  float rd, alpha;
+  bool mirror;
+  Fresnel fr;
+};
+
+__device__ __forceinline__ Mat material(const vmr_shader_std& s) {
+  Mat m;
+  const float dw = (s.flags & VMR_SH_DIFFUSE_STRENGTH) ? s.diffuse_strength : 0.0f;
+  const float sw = (s.flags & VMR_SH_SPEC1_STRENGTH) ? s.spec1_strength : 0.0f;
+  const float tw = dw + sw;
+  m.dw = dw / tw;
+  m.sw = sw / tw;
+  m.cd = (s.flags & VMR_SH_DIFFUSE_COLOUR) ? v3(s.diffuse_colour[0], s.diffuse_colour[1], s.diffuse_colour[2])
+                                           : v3(0, 0, 0);
+  m.cs = (s.flags & VMR_SH_SPEC1_COLOUR) ? v3(s.spec1_colour[0], s.spec1_colour[1], s.spec1_colour[2]) : v3(0, 0, 0);
+  m.rd = (s.flags & VMR_SH_DIFFUSE_ROUGHNESS) ? s.diffuse_roughness : 0.5f;
+  const float rs = (s.flags & VMR_SH_SPEC1_ROUGHNESS) ? s.spec1_roughness : 0.5f;
+  m.mirror = rs == 0.0f;
+  m.alpha = sqr(rs * rs);
+  m.fr = Fresnel{0, (s.flags & VMR_SH_IOR) ? s.ior : 1.7f, {}, {}};
+  if (s.spec1_fresnel == 1) {
+    RGB refl{{0.5f, 0.5f, 0.5f}}, edge{{0.5f, 0.5f, 0.5f}};
+    if (s.flags & VMR_SH_FRESNEL_REFL) refl = RGB{{s.spec1_fresnel_refl[0], s.spec1_fresnel_refl[1], s.spec1_fresnel_refl[2]}};
+    if (s.flags & VMR_SH_FRESNEL_EDGE)  // the reference's assignment (std.go:185-187)
+      refl = RGB{{s.spec1_fresnel_edge[0], s.spec1_fresnel_edge[1], s.spec1_fresnel_edge[2]}};
+    m.fr = Fresnel{1, 0, refl, edge};
+  }
+  return m;
+}
+
+__device__ __forceinline__ float ggx_d_pt(V3 m, float alpha) {
+  if (m.z <= 0.0f) return 0.0f;
+  if (m.z == 1.0f) return 1.0f / (kPi * alpha * alpha);
+  const float denom = kPi * sqr(m.z * m.z) * sqr(alpha * alpha + ((1.0f / (m.z * m.z)) - 1));
+  return (alpha * alpha) / denom;
+}
+
+// f(wi, wo)*|cos wo| in the local frame (wi.z > 0: the frame faces wi).
+__device__ V3 bsdf_f(const Mat& m, V3 wi, V3 wo) {
+  V3 f = v3(0, 0, 0);
+  if (wo.z <= 0.0f) return f;
+  if (m.dw > 0.0f) {
+    float s;
+    if (m.rd == 0.0f) {
+      s = wo.z / kPi;
+    } else {  // OrenNayar (bsdf/orennayar.go:42-73), sigma = roughness^2
+      const float sigma = m.rd * m.rd;
+      const float A = 1 - (0.5f * (sigma * sigma) / ((sigma * sigma) + 0.57f));
+      const float B = 0.45f * (sigma * sigma) / ((sigma * sigma) + 0.09f);
+      const float phiI = gatan2(wi.y, wi.x), phiO = gatan2(wo.y, wo.x);
+      const float thetaI = gacos(wi.z), thetaO = gacos(wo.z);
+      const float al = thetaI > thetaO ? thetaI : thetaO, be = thetaI < thetaO ? thetaI : thetaO;
+      const float C = gsin(al) * gtan(be);
+      const float gm = gcos(phiO - phiI);
+      s = wo.z * (A + (B * (gm > 0.0f ? gm : 0.0f) * C)) / kPi;
+    }
+    const float k = m.dw * s;
+    f = v3(k * m.cd.x, k * m.cd.y, k * m.cd.z);
+  }
+  if (m.sw > 0.0f && !m.mirror) {
+    const V3 h = normalize(add(wi, wo));
+    const RGB F = fresnel_kr(m.fr, fabsf(dot(wi, h)));
+    const float numer = ggx_g1(wi, h, m.alpha) * ggx_g1(wo, h, m.alpha) * ggx_d_pt(h, m.alpha);
+    const float denom = 4 * wi.z * wo.z;
+    float s = wo.z * numer / denom;
+    if (!(s > 0.0f)) s = 0.0f;
+    const float k = m.sw * s;
+    f = add(f, v3(k * m.cs.x * F.c[0], k * m.cs.y * F.c[1], k * m.cs.z * F.c[2]));
+  }
+  return f;
+}
+
+__device__ float bsdf_pdf_pt(const Mat& m, V3 wi, V3 wo) {
+  if (wo.z <= 0.0f) return 0.0f;
+  float p = m.dw * (wo.z / kPi);
+  if (m.sw > 0.0f && !m.mirror) {
+    const V3 h = normalize(add(wi, wo));
+    const float d = fabsf(dot(wo, h));
+    if (d > 0.0f) p = p + m.sw * (ggx_d_pt(h, m.alpha) * h.z / (4 * d));
+  }
+  return p;
+}
+
+__device__ __forceinline__ float power_w(float a, float b) { return (a * a) / (a * a + b * b); }
+__device__ __forceinline__ float tmax3(float a, float b, float c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
+
+// Warp-aggregated append: one atomic per warp for the lanes that want a slot.
+__device__ __forceinline__ unsigned long long warp_append(unsigned long long* counter, bool want) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, want);
+  if (m == 0u) return ~0ull;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
+  base = __shfl_sync(act, base, leader);
+  return want ? base + __popc(m & ((1u << lane) - 1u)) : ~0ull;
+}
+
+__device__ __forceinline__ void put_ray(float* q, uint32_t cap, uint64_t i, const float o[3], V3 d, float tmax,
+                                        float time) {
+  q[i] = o[0];
+  q[cap + i] = o[1];
+  q[2 * (size_t)cap + i] = o[2];
+  q[3 * (size_t)cap + i] = d.x;
+  q[4 * (size_t)cap + i] = d.y;
+  q[5 * (size_t)cap + i] = d.z;
+  q[6 * (size_t)cap + i] = tmax;
+  q[7 * (size_t)cap + i] = time;
+}
+
+__global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
+  const uint64_t n = b.it->n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.qlen[0] = n;
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t pix = (uint32_t)(s % b.npix);
+    const uint32_t j = b.it->iter0 + (uint32_t)(s / b.npix) + 1;
+    V3 P, D;
+    float time, lambda;
+    camera_primary(b.cam, b.width, b.height, j, pix, b.seed, P, D, time, lambda);
+    const float o[3] = {P.x, P.y, P.z};
+    put_ray(b.qray[0], b.cap, s, o, D, __int_as_float(0x7f800000), time);
+    b.qpath[0][s] = (uint32_t)s;
+    b.bx[s] = 1.0f; b.by[s] = 1.0f; b.bz[s] = 1.0f;
+    b.lx[s] = 0.0f; b.ly[s] = 0.0f; b.lz[s] = 0.0f;
+    b.pdf[s] = 0.0f;
+    b.key[s] = sample_key(b.seed, pix, j);
+  }
+}
+
+// One bounce of every path in queue d.
+__global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
+  const uint64_t n = b.qlen[d];
+  const float* q = b.qray[d & 1];
+  const uint32_t* qp = b.qpath[d & 1];
+  float* nq = b.qray[(d + 1) & 1];
+  uint32_t* nqp = b.qpath[(d + 1) & 1];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // Every lane of a warp runs the same number of iterations so the
+  // warp-aggregated appends see whole warps.
+  const uint64_t nround = (n + stride - 1) / stride;
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  for (uint64_t r = 0; r < nround; ++r) {
+    const uint64_t i = r * stride + tid;
+    const bool active = i < n;
+    bool want_shadow = false, want_next = false;
+    uint32_t p = 0;
+    float so[3] = {0, 0, 0}, no[3] = {0, 0, 0};
+    V3 sd = v3(0, 0, 0), nd = v3(0, 0, 0), sc3 = v3(0, 0, 0);
+    float stmax = 0.f, time = 0.f;
+    if (active) {
+      p = qp[i];
+      const V3 D = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
+      time = q[7 * (size_t)b.cap + i];
+      V3 beta = v3(b.bx[p], b.by[p], b.bz[p]);
+      V3 L = v3(b.lx[p], b.ly[p], b.lz[p]);
+      const float pdf_prev = b.pdf[p];
+      const uint64_t key = b.key[p];
+      const int32_t prim = b.hprim[i];
+      bool cont = false;
+      if (prim < 0) {
+        if (b.has_env) {
+          const float w = pdf_prev == 0.0f ? 1.0f : power_w(pdf_prev, b.sel * kInv4Pi);
+          L = add(L, v3(beta.x * b.env[0] * w, beta.y * b.env[1] * w, beta.z * b.env[2] * w));
+        }
+      } else {
+        const int32_t geom = b.hgeom[i];
+        Ctx sc;
+        uint32_t shid = 0;
+        if (hit_attributes(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], sc, shid)) {
+          const vmr_shader_std& sh = b.shaders[shid];
+          const V3 wi = v3(-D.x, -D.y, -D.z);
+          const bool front = dot(sc.Ng, wi) > 0.0f;
+          const RGB e = emission(sh);
+          const V3 Le = v3(e.c[0], e.c[1], e.c[2]);
+          if (front && (Le.x != 0.0f || Le.y != 0.0f || Le.z != 0.0f)) {
+            float w = 1.0f;
+            const int32_t li = (uint32_t)geom < b.n_geoms ? b.light_of_geom[geom] : -1;
+            if (pdf_prev != 0.0f && li >= 0) {
+              const PtLight& l = b.lights[li];
+              const float t = b.ht[i];
+              const float pl = b.sel * (t * t) / (l.area * fabsf(dot(D, sc.Ng)));
+              w = power_w(pdf_prev, pl);
+            }
+            L = add(L, v3(beta.x * Le.x * w, beta.y * Le.y * w, beta.z * Le.z * w));
+          }
+          const float tw = ((sh.flags & VMR_SH_DIFFUSE_STRENGTH) ? sh.diffuse_strength : 0.0f) +
+                           ((sh.flags & VMR_SH_SPEC1_STRENGTH) ? sh.spec1_strength : 0.0f);
+          if (d < b.max_depth && tw != 0.0f) {
+            if (!front) {  // two-sided: face the incoming ray
+              sc.N = v3(-sc.N.x, -sc.N.y, -sc.N.z);
+              sc.Ng = v3(-sc.Ng.x, -sc.Ng.y, -sc.Ng.z);
+              sc.Poffset = v3(-sc.Poffset.x, -sc.Poffset.y, -sc.Poffset.z);
+            }
+            V3 Vt = cross(sc.N, sc.DdPdu);
+            if (len2(Vt) < 0.1f) Vt = cross(sc.N, sc.DdPdv);
+            Vt = normalize(Vt);
+            const V3 Ut = normalize(cross(sc.N, Vt));
+            const Mat m = material(sh);
+            const V3 wil = project(Ut, Vt, sc.N, wi);
+            const uint32_t base = 8 * d;
+            const int nL = (int)b.nl;
+            // ---- next-event estimation
+            if (nL > 0 && (m.dw > 0.0f || !m.mirror)) {
+              const float u = rnd(key, base + 0);
+              int li = (int)(u * (float)nL);
+              if (li > nL - 1) li = nL - 1;
+              const float u0 = rnd(key, base + 1), u1 = rnd(key, base + 2);
+              const PtLight& l = b.lights[li];
+              V3 Ld;
+              float dist = 0.f, pl = 0.f;
+              bool ok = true;
+              if (l.kind == 2) {
+                const float z = 1 - 2 * u0;
+                const float rr = sqrtf((1 - z * z) > 0.0f ? (1 - z * z) : 0.0f);
+                const float phi = 2 * kPi * u1;
+                Ld = v3(rr * gcos(phi), rr * gsin(phi), z);
+                pl = b.sel * kInv4Pi;
+              } else {
+                const V3 p0 = v3(l.p0[0], l.p0[1], l.p0[2]), la = v3(l.a[0], l.a[1], l.a[2]),
+                         lb = v3(l.b[0], l.b[1], l.b[2]);
+                V3 Pl;
+                if (l.kind == 0) {
+                  const float su = sqrtf(u0);
+                  const float b0 = 1 - su, b1 = su * (1 - u1), b2 = su * u1;
+                  Pl = add(add(scale(b0, p0), scale(b1, la)), scale(b2, lb));
+                } else {
+                  Pl = add(add(p0, scale(u0, la)), scale(u1, lb));
+                }
+                const V3 Dv = sub(Pl, sc.P);
+                dist = length(Dv);
+                Ld = normalize(Dv);
+                const float cl = dot(Ld, v3(l.N[0], l.N[1], l.N[2]));
+                if (!(cl < 0.0f)) ok = false;
+                else pl = b.sel * (dist * dist) / (l.area * (-cl));
+              }
+              if (ok && dot(Ld, sc.Ng) > 0.0f && dot(Ld, sc.N) > 0.0f && pl > 0.0f && !isinf(pl)) {
+                const V3 wol = project(Ut, Vt, sc.N, Ld);
+                const V3 f = bsdf_f(m, wil, wol);
+                const float pb = bsdf_pdf_pt(m, wil, wol);
+                const float w = power_w(pl, pb);
+                const float k = w / pl;
+                const V3 c = v3(beta.x * f.x * l.Le[0] * k, beta.y * f.y * l.Le[1] * k, beta.z * f.z * l.Le[2] * k);
+                if (c.x > 0.0f || c.y > 0.0f || c.z > 0.0f) {
+                  const V3 o = offset_p(sc, 1);
+                  so[0] = o.x; so[1] = o.y; so[2] = o.z;
+                  if (l.kind == 2) {
+                    sd = Ld;
+                    stmax = __int_as_float(0x7f800000);
+                  } else {
+                    const float sl = dist * 0.9999f;
+                    sd = v3(Ld.x * sl, Ld.y * sl, Ld.z * sl);
+                    stmax = 1.0f;
+                  }
+                  sc3 = c;
+                  want_shadow = true;
+                }
+              }
+            }
+            // ---- BSDF sample
+            const float ul = rnd(key, base + 3);
+            const double r0 = (double)rnd(key, base + 4), r1 = (double)rnd(key, base + 5);
+            V3 wol;
+            bool delta = false;
+            if (ul < m.dw) {  // CosineHemisphere (math/sample/sample.go:18-27)
+              const double r = sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
+              wol = v3((float)(r * cos(th)), (float)(r * sin(th)), (float)sqrt(r0));
+            } else if (m.mirror) {
+              wol = v3(-wil.x, -wil.y, wil.z);
+              delta = true;
+            } else {  // GGX D(m)cos(m) (microfacetggx.go:82-100)
+              const double thetaM = atan2((double)m.alpha * sqrt(r0), sqrt(1 - r0));
+              const double phiM = 2.0 * 3.14159265358979323846 * r1;
+              const float st = gsin((float)thetaM), ct = gcos((float)thetaM);
+              const V3 mh = v3(st * gcos((float)phiM), st * gsin((float)phiM), ct);
+              wol = normalize(sub(scale(2 * fabsf(dot(mh, wil)), mh), wil));
+            }
+            const V3 wo = expand(Ut, Vt, sc.N, wol);
+            if (dot(wo, sc.Ng) > 0.0f) {
+              bool alive = true;
+              float pb = 0.0f;
+              if (delta) {
+                const RGB F = fresnel_kr(m.fr, wil.z);
+                beta = v3(beta.x * (m.cs.x * F.c[0]), beta.y * (m.cs.y * F.c[1]), beta.z * (m.cs.z * F.c[2]));
+              } else {
+                const V3 f = bsdf_f(m, wil, wol);
+                pb = bsdf_pdf_pt(m, wil, wol);
+                if (!(pb > 0.0f)) alive = false;
+                else beta = v3(beta.x * (f.x / pb), beta.y * (f.y / pb), beta.z * (f.z / pb));
+              }
+              if (alive && d + 1 >= b.rr_depth) {  // Russian roulette
+                float qq = tmax3(beta.x, beta.y, beta.z);
+                if (qq > 0.95f) qq = 0.95f;
+                const float ur = rnd(key, base + 6);
+                if (!(ur < qq)) alive = false;
+                else beta = v3(beta.x / qq, beta.y / qq, beta.z / qq);
+              }
+              if (alive) {
+                const V3 o = offset_p(sc, 1);
+                no[0] = o.x; no[1] = o.y; no[2] = o.z;
+                nd = wo;
+                b.pdf[p] = delta ? 0.0f : pb;
+                cont = true;
+              }
+            }
+          }
+        }
+      }
+      b.lx[p] = L.x; b.ly[p] = L.y; b.lz[p] = L.z;
+      if (cont) {
+        b.bx[p] = beta.x; b.by[p] = beta.y; b.bz[p] = beta.z;
+        want_next = true;
+      }
+    }
+    __syncwarp();
+    const unsigned long long si = warp_append(&b.slen[d], want_shadow);
+    if (want_shadow && si < b.cap) {
+      put_ray(b.sray, b.cap, si, so, sd, stmax, time);
+      b.spath[si] = p;
+      b.scontrib[si] = sc3.x;
+      b.scontrib[b.cap + si] = sc3.y;
+      b.scontrib[2 * (size_t)b.cap + si] = sc3.z;
+    }
+    const unsigned long long ni = warp_append(&b.qlen[d + 1], want_next);
+    if (want_next && ni < b.cap) {
+      put_ray(nq, b.cap, ni, no, nd, __int_as_float(0x7f800000), time);
+      nqp[ni] = p;
+    }
+  }
+}
+
+// Unoccluded shadow rays add their contribution, in queue order (each path
+// has at most one shadow ray per bounce, so no two threads touch one path).
+__global__ void __launch_bounds__(kPtBlock) k_pt_resolve(PtBatch b, uint32_t d) {
+  const uint64_t n = b.slen[d];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (b.shit[i] >= 0) continue;
+    const uint32_t p = b.spath[i];
+    b.lx[p] = b.lx[p] + b.scontrib[i];
+    b.ly[p] = b.ly[p] + b.scontrib[b.cap + i];
+    b.lz[p] = b.lz[p] + b.scontrib[2 * (size_t)b.cap + i];
+  }
+}
+
+__global__ void __launch_bounds__(kPtBlock) k_pt_accumulate(PtBatch b) {
+  const uint32_t iters = b.it->iters;
+  for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < b.npix; pix += gridDim.x * blockDim.x) {
+    float f[3] = {b.fb[pix * 3], b.fb[pix * 3 + 1], b.fb[pix * 3 + 2]};
+    double g[3] = {0, 0, 0};
+    if (b.fb64)
+      for (int k = 0; k < 3; ++k) g[k] = b.fb64[(size_t)pix * 3 + k];
+    for (uint32_t t = 0; t < iters; ++t) {
+      const uint64_t s = (uint64_t)t * b.npix + pix;
+      const uint32_t i = b.it->iter0 + t;  // 0-based: the exact running mean
+      const float L[3] = {b.lx[s], b.ly[s], b.lz[s]};
+      for (int k = 0; k < 3; ++k) {
+        f[k] = (f[k] * (float)i + L[k]) / (float)(i + 1);
+        g[k] = (g[k] * (double)i + (double)L[k]) / (double)(i + 1);
+      }
+    }
+    for (int k = 0; k < 3; ++k) b.fb[pix * 3 + k] = f[k];
+    if (b.fb64)
+      for (int k = 0; k < 3; ++k) b.fb64[(size_t)pix * 3 + k] = g[k];
+  }
+}
+
+// Ray counts and traversal status of the batch, kept across batches (the
+// next batch clears the per-launch scratch).
+__global__ void k_pt_tally(PtBatch b) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  unsigned long long r = 0, s = 0;
+  int st = *b.status;
+  for (uint32_t d = 0; d <= b.max_depth; ++d) {
+    r += b.qlen[d];
+    s += b.slen[d];
+    st = max(st, max(b.scr[2 * d].status, b.scr[2 * d + 1].status));
+  }
+  b.totals[0] += r;
+  b.totals[1] += s;
+  *b.status = st;
+}
+
+// ---------------------------------------------------- host: light table ---
+// Host float math in the oracle's operation order (compiled without
+// contraction), so the device sees the same light table as the oracle.
+struct HV {
+  float x, y, z;
+};
+inline HV hv(const float* p) { return HV{p[0], p[1], p[2]}; }
+inline HV hsub(HV a, HV b) { return HV{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline HV hcross(HV a, HV b) { return HV{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float hlen(HV a) { return std::sqrt((a.x * a.x + a.y * a.y) + a.z * a.z); }
+inline HV hnrm(HV a) {
+  const float r = 1.0f / std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  return HV{a.x * r, a.y * r, a.z * r};
+}
+void host_emission(const vmr_shader_std& s, float out[3]) {
+  out[0] = out[1] = out[2] = 0.0f;
+  if (!(s.flags & VMR_SH_EMISSION_STRENGTH)) return;
+  for (int k = 0; k < 3; ++k)
+    out[k] = ((s.flags & VMR_SH_EMISSION_COLOUR) ? s.emission_colour[k] : 0.0f) * s.emission_strength;
+}
+
+int pfail(vmr_ctx* ctx, int code, const std::string& msg) {
+  ctx->err = msg;
+  return code;
+}
+
+#define PCUDA(x)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) return pfail(ctx, VMR_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+// Launches one batch's stages on the context's stream (also used while
+// capturing the graph).  Every count is read on the device.
+int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid) {
+  cudaStream_t st = ctx->stream;
+  const size_t nq = kPtMaxDepth + 2, ns = kPtMaxDepth + 1;
+  PCUDA(cudaMemsetAsync(b.qlen, 0, nq * sizeof(unsigned long long), st));
+  PCUDA(cudaMemsetAsync(b.slen, 0, ns * sizeof(unsigned long long), st));
+  PCUDA(cudaMemsetAsync(scr, 0, sizeof(DScratch) * 2 * (b.max_depth + 1), st));
+  k_pt_generate<<<grid, kPtBlock, 0, st>>>(b);
+  PCUDA(cudaGetLastError());
+  for (uint32_t d = 0; d <= b.max_depth; ++d) {
+    TraceLaunch l{};
+    l.rays = RaySoA{b.qray[d & 1], b.qray[d & 1] + b.cap, b.qray[d & 1] + 2 * (size_t)b.cap,
+                    b.qray[d & 1] + 3 * (size_t)b.cap, b.qray[d & 1] + 4 * (size_t)b.cap,
+                    b.qray[d & 1] + 5 * (size_t)b.cap, b.qray[d & 1] + 6 * (size_t)b.cap,
+                    b.qray[d & 1] + 7 * (size_t)b.cap};
+    l.hits = HitSoA{b.hprim, b.hgeom, b.ht, b.hu, b.hv, b.hw};
+    l.n = b.cap;
+    l.n_dev = &b.qlen[d];
+    l.scratch = scr + 2 * d;
+    l.stream = st;
+    if (launch_trace_scene(ctx->top.dtop, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+    k_pt_shade<<<grid, kPtBlock, 0, st>>>(b, d);
+    PCUDA(cudaGetLastError());
+    if (d < b.max_depth) {
+      TraceLaunch s{};
+      s.rays = RaySoA{b.sray, b.sray + b.cap, b.sray + 2 * (size_t)b.cap, b.sray + 3 * (size_t)b.cap,
+                      b.sray + 4 * (size_t)b.cap, b.sray + 5 * (size_t)b.cap, b.sray + 6 * (size_t)b.cap,
+                      b.sray + 7 * (size_t)b.cap};
+      s.hits = HitSoA{b.shit, nullptr, nullptr, nullptr, nullptr, nullptr};
+      s.n = b.cap;
+      s.n_dev = &b.slen[d];
+      s.any_hit = 1;
+      s.scratch = scr + 2 * d + 1;
+      s.stream = st;
+      if (launch_trace_scene(ctx->top.dtop, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+      k_pt_resolve<<<grid, kPtBlock, 0, st>>>(b, d);
+      PCUDA(cudaGetLastError());
+    }
+  }
+  k_pt_accumulate<<<grid, kPtBlock, 0, st>>>(b);
+  PCUDA(cudaGetLastError());
+  k_pt_tally<<<1, 32, 0, st>>>(b);
+  PCUDA(cudaGetLastError());
+  return VMR_OK;
+}
+
+}  // namespace
+}  // namespace vmr
+
+extern "C" {
+
+int vmr_set_quad_lights(vmr_ctx* ctx, const vmr_quad_light* lights, uint32_t n) {
+  if (!ctx || (n && !lights)) return VMR_ERR_INVALID;
+  ctx->render.quads.assign(lights, lights + n);
+  return VMR_OK;
+}
+
+int vmr_set_env_light(vmr_ctx* ctx, const float radiance[3]) {
+  if (!ctx || !radiance) return VMR_ERR_INVALID;
+  for (int k = 0; k < 3; ++k) {
+    if (!(radiance[k] >= 0.0f) || std::isinf(radiance[k]))
+      return vmr::pfail(ctx, VMR_ERR_INVALID, "environment radiance must be finite and non-negative");
+    ctx->render.env[k] = radiance[k];
+  }
+  return VMR_OK;
+}
+
+int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_stats* stats) {
+  using namespace vmr;
+  if (!ctx || !p || !fb) return VMR_ERR_INVALID;
+  if (ctx->device < 0) return pfail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot render");
+  if (!ctx->top.valid) return pfail(ctx, VMR_ERR_INVALID, "no scene: call vmr_scene_build first");
+  if (!ctx->render.has_camera) return pfail(ctx, VMR_ERR_INVALID, "no camera");
+  if (p->width == 0 || p->height == 0 || p->width > 4096 || p->height > 4096)
+    return pfail(ctx, VMR_ERR_INVALID, "image size must be in [1, 4096] (RasterXY uses m = 12)");
+  if (p->max_depth > (uint32_t)kPtMaxDepth) return pfail(ctx, VMR_ERR_INVALID, "max_depth must be <= 32");
+  auto& R = ctx->render;
+  for (uint32_t g : ctx->top.host.geom_order) {
+    const auto& mr = ctx->meshes[g];
+    if (mr->host.motion()) return pfail(ctx, VMR_ERR_UNSUPPORTED, "rendering motion meshes is not supported yet");
+    for (uint32_t sid : mr->shader_list)
+      if (sid >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "mesh shader id out of range");
+  }
+  // Light list: TriLights, quad lights, environment.
+  const uint32_t n_geoms = (uint32_t)ctx->meshes.size();
+  std::vector<PtLight> lights;
+  std::vector<int32_t> log(std::max<uint32_t>(1, n_geoms), -1);
+  for (const auto& t : R.lights) {
+    if (t.shader >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "light shader out of range");
+    PtLight l{};
+    l.kind = 0;
+    std::memcpy(l.p0, t.p0, 12);
+    std::memcpy(l.a, t.p1, 12);
+    std::memcpy(l.b, t.p2, 12);
+    const HV c = hcross(hsub(hv(t.p1), hv(t.p0)), hsub(hv(t.p2), hv(t.p0)));
+    const HV N = hnrm(c);
+    l.N[0] = N.x; l.N[1] = N.y; l.N[2] = N.z;
+    l.area = 0.5f * hlen(c);
+    host_emission(R.shaders[t.shader], l.Le);
+    l.geom = (int32_t)t.geom;
+    if (t.geom < n_geoms) log[t.geom] = (int32_t)lights.size();
+    lights.push_back(l);
+  }
+  for (const auto& qd : R.quads) {
+    if (qd.shader >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "quad light shader out of range");
+    PtLight l{};
+    l.kind = 1;
+    std::memcpy(l.p0, qd.p0, 12);
+    std::memcpy(l.a, qd.e1, 12);
+    std::memcpy(l.b, qd.e2, 12);
+    const HV c = hcross(hv(qd.e1), hv(qd.e2));
+    const HV N = hnrm(c);
+    l.N[0] = N.x; l.N[1] = N.y; l.N[2] = N.z;
+    l.area = hlen(c);
+    host_emission(R.shaders[qd.shader], l.Le);
+    l.geom = (int32_t)qd.geom;
+    if (qd.geom < n_geoms) log[qd.geom] = (int32_t)lights.size();
+    lights.push_back(l);
+  }
+  const bool has_env = R.env[0] != 0.0f || R.env[1] != 0.0f || R.env[2] != 0.0f;
+  if (has_env) {
+    PtLight l{};
+    l.kind = 2;
+    std::memcpy(l.Le, R.env, 12);
+    l.geom = -1;
+    lights.push_back(l);
+  }
+  const uint32_t nl = (uint32_t)lights.size();
+  std::vector<RMesh> rm(ctx->meshes.size());
+  for (size_t g = 0; g < ctx->meshes.size(); ++g) {
+    MeshRec& mr = *ctx->meshes[g];
+    rm[g].tris = reinterpret_cast<const float4*>(mr.tris.p);
+    rm[g].nrm = mr.has_normals ? reinterpret_cast<const float4*>(mr.nrm.p) : nullptr;
+    rm[g].sidx = mr.host.shader_idx.empty() ? nullptr : mr.sidx.as<uint8_t>();
+    rm[g].shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
+    rm[g].n_shaders = (uint32_t)mr.shader_list.size();
+  }
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const uint32_t npix = p->width * p->height;
+  const uint32_t per_batch = p->max_batch_samples ? p->max_batch_samples : (2u << 20);
+  uint32_t ipb = std::max<uint32_t>(1, per_batch / npix);
+  if (p->iter_count > 0 && ipb > p->iter_count) ipb = p->iter_count;
+  const uint64_t cap = (uint64_t)ipb * npix;
+  if (cap > 0xffffffffull) return pfail(ctx, VMR_ERR_INVALID, "batch too large");
+  // One device block, carved.
+  size_t bytes = 0;
+  auto carve = [&](size_t nb) { size_t o = bytes; bytes += (nb + 255) / 256 * 256; return o; };
+  const size_t o_state = carve(cap * 7 * 4), o_key = carve(cap * 8), o_q0 = carve(cap * 8 * 4),
+               o_q1 = carve(cap * 8 * 4), o_qp0 = carve(cap * 4), o_qp1 = carve(cap * 4), o_hit = carve(cap * 6 * 4),
+               o_s = carve(cap * 8 * 4), o_sp = carve(cap * 4), o_sc = carve(cap * 3 * 4), o_sh = carve(cap * 4),
+               o_cnt = carve((2 * kPtMaxDepth + 6) * 8), o_scr = carve(sizeof(DScratch) * 2 * (kPtMaxDepth + 1)),
+               o_it = carve(sizeof(PtIter)), o_fb = carve((size_t)npix * 3 * 4),
+               o_fb64 = carve(p->fb64 ? (size_t)npix * 3 * 8 : 0), o_mesh = carve(rm.size() * sizeof(RMesh)),
+               o_light = carve(std::max<size_t>(1, lights.size()) * sizeof(PtLight)),
+               o_shader = carve(std::max<size_t>(1, R.shaders.size()) * sizeof(vmr_shader_std)),
+               o_log = carve(log.size() * 4);
+  PCUDA(R.ptbuf.ensure(bytes));
+  char* base = R.ptbuf.as<char>();
+  uint64_t fwd[52], inv[52];
+  raster_tables_m12(fwd, inv);
+  PCUDA(cudaMemcpyToSymbolAsync(c_raster_fwd, fwd, sizeof(fwd), 0, cudaMemcpyHostToDevice, st));
+  PCUDA(cudaMemcpyToSymbolAsync(c_raster_inv, inv, sizeof(inv), 0, cudaMemcpyHostToDevice, st));
+  PCUDA(cudaMemcpyAsync(base + o_mesh, rm.data(), rm.size() * sizeof(RMesh), cudaMemcpyHostToDevice, st));
+  if (!lights.empty())
+    PCUDA(cudaMemcpyAsync(base + o_light, lights.data(), lights.size() * sizeof(PtLight), cudaMemcpyHostToDevice, st));
+  if (!R.shaders.empty())
+    PCUDA(cudaMemcpyAsync(base + o_shader, R.shaders.data(), R.shaders.size() * sizeof(vmr_shader_std),
+                          cudaMemcpyHostToDevice, st));
+  PCUDA(cudaMemcpyAsync(base + o_log, log.data(), log.size() * 4, cudaMemcpyHostToDevice, st));
+  PCUDA(cudaMemcpyAsync(base + o_fb, fb, (size_t)npix * 3 * 4, cudaMemcpyHostToDevice, st));
+  if (p->fb64) PCUDA(cudaMemcpyAsync(base + o_fb64, p->fb64, (size_t)npix * 3 * 8, cudaMemcpyHostToDevice, st));
+  PtBatch b{};
+  b.width = p->width;
+  b.height = p->height;
+  b.npix = npix;
+  b.nl = nl;
+  b.max_depth = p->max_depth;
+  b.rr_depth = p->rr_depth;
+  b.has_env = has_env ? 1u : 0u;
+  b.cap = (uint32_t)cap;
+  std::memcpy(b.env, R.env, 12);
+  b.sel = nl > 0 ? 1.0f / (float)nl : 0.0f;
+  b.seed = p->seed;
+  b.cam = R.camera;
+  b.it = reinterpret_cast<const PtIter*>(base + o_it);
+  b.shaders = reinterpret_cast<const vmr_shader_std*>(base + o_shader);
+  b.lights = reinterpret_cast<const PtLight*>(base + o_light);
+  b.meshes = reinterpret_cast<const RMesh*>(base + o_mesh);
+  b.light_of_geom = reinterpret_cast<const int32_t*>(base + o_log);
+  b.n_geoms = n_geoms;
+  float* stt = reinterpret_cast<float*>(base + o_state);
+  b.bx = stt; b.by = stt + cap; b.bz = stt + 2 * cap;
+  b.lx = stt + 3 * cap; b.ly = stt + 4 * cap; b.lz = stt + 5 * cap;
+  b.pdf = stt + 6 * cap;
+  b.key = reinterpret_cast<unsigned long long*>(base + o_key);
+  b.qray[0] = reinterpret_cast<float*>(base + o_q0);
+  b.qray[1] = reinterpret_cast<float*>(base + o_q1);
+  b.qpath[0] = reinterpret_cast<uint32_t*>(base + o_qp0);
+  b.qpath[1] = reinterpret_cast<uint32_t*>(base + o_qp1);
+  int32_t* hit = reinterpret_cast<int32_t*>(base + o_hit);
+  b.hprim = hit;
+  b.hgeom = hit + cap;
+  b.ht = reinterpret_cast<float*>(hit + 2 * cap);
+  b.hu = reinterpret_cast<float*>(hit + 3 * cap);
+  b.hv = reinterpret_cast<float*>(hit + 4 * cap);
+  b.hw = reinterpret_cast<float*>(hit + 5 * cap);
+  b.sray = reinterpret_cast<float*>(base + o_s);
+  b.spath = reinterpret_cast<uint32_t*>(base + o_sp);
+  b.scontrib = reinterpret_cast<float*>(base + o_sc);
+  b.shit = reinterpret_cast<int32_t*>(base + o_sh);
+  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(base + o_cnt);
+  b.qlen = cnt;
+  b.slen = cnt + kPtMaxDepth + 2;
+  b.totals = cnt + 2 * kPtMaxDepth + 3;
+  b.status = reinterpret_cast<int*>(cnt + 2 * kPtMaxDepth + 5);
+  b.fb = reinterpret_cast<float*>(base + o_fb);
+  b.fb64 = p->fb64 ? reinterpret_cast<double*>(base + o_fb64) : nullptr;
+  DScratch* scr = reinterpret_cast<DScratch*>(base + o_scr);
+  b.scr = scr;
+  PCUDA(cudaMemsetAsync(b.totals, 0, 24, st));
+  PCUDA(cudaMemsetAsync(scr, 0, sizeof(DScratch) * 2 * (kPtMaxDepth + 1), st));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const int grid = std::max(1, sms) * 8;
+  // Per-batch parameters, pinned so that each copy has its own stable source.
+  const uint32_t nbatch = p->iter_count == 0 ? 0 : (p->iter_count + ipb - 1) / ipb;
+  const size_t hbytes = std::max<size_t>(1, nbatch) * sizeof(PtIter);
+  if (R.pt_host_bytes < hbytes) {
+    PCUDA(cudaStreamSynchronize(st));
+    if (R.pt_host) cudaFreeHost(R.pt_host);
+    R.pt_host = nullptr;
+    R.pt_host_bytes = 0;
+    PCUDA(cudaMallocHost(&R.pt_host, hbytes));
+    R.pt_host_bytes = hbytes;
+  }
+  PtIter* batches = static_cast<PtIter*>(R.pt_host);
+  for (uint32_t k = 0; k < nbatch; ++k) {
+    const uint32_t it0 = k * ipb;
+    batches[k].iter0 = p->iter_begin + it0;
+    batches[k].iters = std::min(ipb, p->iter_count - it0);
+    batches[k].n = (unsigned long long)batches[k].iters * npix;
+  }
+  // The captured graph depends on every pointer and launch parameter above.
+  const bool use_graph = !(p->flags & VMR_PATH_NO_GRAPH);
+  std::vector<uint64_t> key = {(uint64_t)(uintptr_t)base, bytes, cap, npix, p->width, p->height, nl, p->max_depth,
+                               p->rr_depth, p->seed, (uint64_t)(p->fb64 != nullptr), (uint64_t)(uintptr_t)st,
+                               (uint64_t)(uintptr_t)ctx->top.nodes.p, (uint64_t)grid};
+  {
+    uint64_t h = 1469598103934665603ull;
+    auto fold = [&](const void* d, size_t nb) {
+      const unsigned char* c = static_cast<const unsigned char*>(d);
+      for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    };
+    fold(&b.cam, sizeof(b.cam));
+    fold(b.env, sizeof(b.env));
+    fold(&b.sel, sizeof(b.sel));
+    fold(&ctx->top.dtop, sizeof(ctx->top.dtop));
+    key.push_back(h);
+  }
+  uint32_t replays = 0;
+  if (use_graph && nbatch > 0 && !(R.graph.exec && R.graph.key == key)) {
+    if (R.graph.exec) {
+      cudaGraphExecDestroy(R.graph.exec);
+      R.graph.exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    PCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const int rc = launch_batch(ctx, b, scr, grid);
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rc != VMR_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    PCUDA(ec);
+    const cudaError_t ei = cudaGraphInstantiate(&R.graph.exec, g, 0);
+    cudaGraphDestroy(g);
+    PCUDA(ei);
+    R.graph.key = key;
+  }
+  PCUDA(cudaEventRecord(ctx->ev0, st));
+  for (uint32_t k = 0; k < nbatch; ++k) {
+    PCUDA(cudaMemcpyAsync((void*)b.it, &batches[k], sizeof(PtIter), cudaMemcpyHostToDevice, st));
+    if (use_graph) {
+      PCUDA(cudaGraphLaunch(R.graph.exec, st));
+      ++replays;
+    } else {
+      const int rc = launch_batch(ctx, b, scr, grid);
+      if (rc != VMR_OK) return rc;
+    }
+  }
+  PCUDA(cudaEventRecord(ctx->ev1, st));
+  PCUDA(cudaMemcpyAsync(fb, b.fb, (size_t)npix * 3 * 4, cudaMemcpyDeviceToHost, st));
+  if (p->fb64) PCUDA(cudaMemcpyAsync(p->fb64, b.fb64, (size_t)npix * 3 * 8, cudaMemcpyDeviceToHost, st));
+  unsigned long long tot[2] = {0, 0};
+  PCUDA(cudaMemcpyAsync(tot, b.totals, 16, cudaMemcpyDeviceToHost, st));
+  int status = 0;
+  PCUDA(cudaMemcpyAsync(&status, b.status, 4, cudaMemcpyDeviceToHost, st));
+  PCUDA(cudaStreamSynchronize(st));
+  if (status == kStatusStackOverflow) return pfail(ctx, VMR_ERR_STACK_OVERFLOW, "traversal stack overflow");
+  if (status != kStatusOk) return pfail(ctx, VMR_ERR_TIMEOUT, "traversal iteration cap");
+  if (stats) {
+    stats->samples = (uint64_t)npix * p->iter_count;
+    stats->rays = tot[0];
+    stats->shadow_rays = tot[1];
+    stats->graph_replays = replays;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    stats->ms = ms;
+  }
+  return VMR_OK;
+}
+
+}  // extern "C"

@@ -25,380 +25,13 @@
 #include <string>
 #include <vector>
 
-#include "colour_tables.h"
 #include "ctx.h"
 #include "device.h"
+#include "shade_common.cuh"
 #include "vmr.h"
 
 namespace vmr {
 namespace {
-
-// -------------------------------------------------------------- vectors ---
-struct V3 {
-  float x, y, z;
-};
-__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
-__device__ __forceinline__ V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ V3 scale(float s, V3 a) { return v3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V3 cross(V3 a, V3 b) {
-  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ float len2(V3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
-__device__ __forceinline__ V3 normalize(V3 a) {
-  const float r = 1.0f / sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
-  return v3(a.x * r, a.y * r, a.z * r);
-}
-__device__ __forceinline__ float length(V3 a) { return sqrtf((a.x * a.x + a.y * a.y) + a.z * a.z); }
-__device__ __forceinline__ float gmax(float x, float y) { return x > y ? x : y; }
-__device__ __forceinline__ float gmin(float x, float y) { return x < y ? x : y; }
-__device__ __forceinline__ float sqr(float v) { return v * v; }
-constexpr float kPi = 3.14159265358f;  // math.Pi (math/const.go:8) as float32
-__device__ __forceinline__ float gsin(float x) { return (float)sin((double)x); }
-__device__ __forceinline__ float gcos(float x) { return (float)cos((double)x); }
-__device__ __forceinline__ float gtan(float x) { return (float)tan((double)x); }
-__device__ __forceinline__ float gatan(float x) { return (float)atan((double)x); }
-__device__ __forceinline__ float gatan2(float y, float x) { return (float)atan2((double)y, (double)x); }
-__device__ __forceinline__ float gacos(float x) {
-  return (float)acos((double)(x > 1.0f ? 1.0f : (x < -1.0f ? -1.0f : x)));
-}
-__device__ __forceinline__ V3 project(V3 U, V3 V, V3 W, V3 s) { return v3(dot(U, s), dot(V, s), dot(W, s)); }
-__device__ __forceinline__ V3 expand(V3 U, V3 V, V3 W, V3 s) {
-  return v3(U.x * s.x + V.x * s.y + W.x * s.z, U.y * s.x + V.y * s.y + W.y * s.z, U.z * s.x + V.z * s.y + W.z * s.z);
-}
-
-// ------------------------------------------------------------------ QMC ---
-__device__ __forceinline__ uint64_t vdc_bits(uint64_t i, uint64_t s) { return (s ^ __brevll(i)) >> 12; }
-__device__ __forceinline__ uint64_t sobol_bits(uint64_t i, uint64_t s) {
-  uint64_t r = s >> 12;
-  for (uint64_t v = 1ull << 51; i != 0; i >>= 1) {
-    if (i & 1) r ^= v;
-    v ^= v >> 1;
-  }
-  return r;
-}
-constexpr double kTwo52 = 4503599627370496.0;
-__device__ __forceinline__ double vdc(uint64_t i, uint64_t s) { return (double)vdc_bits(i, s) / kTwo52; }
-__device__ __forceinline__ double sobol(uint64_t i, uint64_t s) { return (double)sobol_bits(i, s) / kTwo52; }
-__device__ __forceinline__ uint64_t scramble(uint64_t seed, uint64_t pix, uint32_t k) {
-  uint64_t z = seed + 0x9E3779B97F4A7C15ull * (pix * 8ull + k + 1ull);
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-
-// RasterXY tables for m = 12 (the Grunschloss enumeration, computed on the
-// host from the generator matrices).
-__constant__ uint64_t c_raster_fwd[52];
-__constant__ uint64_t c_raster_inv[52];
-
-// ldseq.RasterXY(12, frame, px, py, 0, 0) (math/ldseq/raster.go:10-57).
-__device__ void raster_xy(uint32_t frame, uint32_t px, uint32_t py, double& rx, double& ry) {
-  const uint32_t m = 12;
-  uint64_t index = (uint64_t)frame << (2 * m);
-  uint64_t delta = 0;
-  for (uint32_t c = 0; frame != 0; frame >>= 1, ++c)
-    if (frame & 1) delta ^= c_raster_fwd[c];
-  uint64_t b = (((uint64_t)px << m) | (uint64_t)py) ^ delta;
-  for (uint32_t c = 0; b != 0; b >>= 1, ++c)
-    if (b & 1) index ^= c_raster_inv[c];
-  const double sc = (double)(1ull << (52 - m));
-  rx = (double)vdc_bits(index, 0) / sc;
-  ry = (double)sobol_bits(index, 0) / sc;
-}
-
-// ------------------------------------------------------------- spectrum ---
-struct RGB {
-  float c[3];
-};
-struct Spec {
-  float c[4];
-};
-__device__ __forceinline__ float wavelength(float lambda, int j) {  // Spectrum.Wavelength
-  float v = (lambda - 450.0f + ((float)j / 4.0f) * 300.0f);
-  if (v >= 300.0f) v -= 300.0f;
-  return v + 450.0f;
-}
-__device__ __forceinline__ float smits_eval(const float* s, float l) {
-  if (l < 380.0f || l >= 720.0f) return 0.0f;
-  return s[(int)(((l - 380.0f) / (720.0f - 380.0f)) * 10.0f)];
-}
-__device__ float smits(float r, float g, float b, float l) {  // RGBToSpectrumSmits99
-  float c = 0.0f;
-  if (r <= g && r <= b) {
-    c += r * smits_eval(kSmitsWhite, l);
-    if (g <= b) {
-      c += (g - r) * smits_eval(kSmitsCyan, l);
-      c += (b - g) * smits_eval(kSmitsBlue, l);
-    } else {
-      c += (b - r) * smits_eval(kSmitsCyan, l);
-      c += (g - b) * smits_eval(kSmitsGreen, l);
-    }
-  } else if (g <= r && g <= b) {
-    c += g * smits_eval(kSmitsWhite, l);
-    if (r <= b) {
-      c += (r - g) * smits_eval(kSmitsMagenta, l);
-      c += (b - r) * smits_eval(kSmitsBlue, l);
-    } else {
-      c += (b - g) * smits_eval(kSmitsMagenta, l);
-      c += (r - b) * smits_eval(kSmitsRed, l);
-    }
-  } else {
-    c += b * smits_eval(kSmitsWhite, l);
-    if (r <= g) {
-      c += (r - b) * smits_eval(kSmitsYellow, l);
-      c += (g - r) * smits_eval(kSmitsGreen, l);
-    } else {
-      c += (g - b) * smits_eval(kSmitsYellow, l);
-      c += (r - g) * smits_eval(kSmitsRed, l);
-    }
-  }
-  return c;
-}
-__device__ __forceinline__ Spec from_rgb(RGB rgb, float lambda) {
-  Spec s;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) s.c[k] = smits(rgb.c[0], rgb.c[1], rgb.c[2], wavelength(lambda, k));
-  return s;
-}
-__device__ __forceinline__ float cie(const float* t, float l) {
-  if (l < 360.0f || l >= 830.0f) return -1.0f;
-  return t[(int)(((l - 360.0f) / (830.0f - 360.0f)) * 95.0f)];
-}
-__device__ RGB to_rgb(const Spec& s, float lambda) {
-  float x = 0, y = 0, z = 0;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const float l = wavelength(lambda, i);
-    x += s.c[i] * cie(kCieX, l);
-    y += s.c[i] * cie(kCieY, l);
-    z += s.c[i] * cie(kCieZ, l);
-  }
-  const float* m = kSrgbFromXyz;
-  return RGB{{x * m[0] + y * m[1] + z * m[2], x * m[3] + y * m[4] + z * m[5], x * m[6] + y * m[7] + z * m[8]}};
-}
-
-// -------------------------------------------------------------- fresnel ---
-struct Fresnel {
-  int model;
-  float eta;
-  RGB r, g;
-};
-__device__ RGB fresnel_kr(const Fresnel& f, float c) {
-  if (f.model == 0) {  // Dielectric.Kr (fresnel/dielectric.go:34-47)
-    float g = (f.eta * f.eta) - 1 + (c * c);
-    if (g < 0.0f) return RGB{{1, 1, 1}};
-    g = sqrtf(g);
-    const float fr = 0.5f * sqr((g - c) / (g + c)) * (1 + sqr((c * (g + c) - 1) / (c * (g - c) + 1)));
-    return RGB{{fr, fr, fr}};
-  }
-  RGB out;  // Conductor.Kr (fresnel/conductor.go:58-89)
-  for (int k = 0; k < 3; ++k) {
-    const float r = gmax(0.0f, gmin(f.r.c[k], 0.99f));
-    const float g = f.g.c[k];
-    const float nmin = (1 - r) / (1 + r);
-    const float nmax = (1 + sqrtf(r)) / (1 - sqrtf(r));
-    const float n = nmin * g + (1 - g) * nmax;
-    const float k2 = ((n + 1) * (n + 1) * r - (n - 1) * (n - 1)) / (1 - r);
-    const float rs = (n * n + k2 - 2 * n * c + c * c) / (n * n + k2 + 2 * n * c + c * c);
-    const float rp = ((n * n + k2) * c * c - 2 * n * c + 1) / ((n * n + k2) * c * c + 2 * n * c + 1);
-    out.c[k] = 0.5f * (rs + rp);
-  }
-  return out;
-}
-
-// ---------------------------------------------------------------- BSDFs ---
-struct Bsdf {
-  int kind;  // 0 OrenNayar, 1 GGX
-  float lambda;
-  V3 wi;
-  float rough;  // roughness^2 as the constructors store it
-  Fresnel fr;
-  V3 U, V, N;
-};
-__device__ __forceinline__ float chi(float x) { return x > 0.0f ? 1.0f : 0.0f; }
-__device__ __forceinline__ float signf(float v) { return v < 0 ? -1.0f : 1.0f; }
-__device__ float ggx_g1(V3 w, V3 m, float alpha) {
-  const float odn = dot(w, m);
-  const float denom = 1 + sqrtf(1 + (alpha * alpha) * ((1.0f / (w.z * w.z)) - 1));
-  return chi(odn / w.z) * 2 / denom;
-}
-__device__ float ggx_d(V3 m, float alpha) {
-  const float numer = alpha * alpha * chi(m.z);
-  if (m.z == 1.0f) return 1.0f / (kPi * alpha * alpha);
-  const float denom = kPi * sqr(m.z * m.z) * sqr(alpha * alpha + ((1.0f / (m.z * m.z)) - 1));
-  return numer / denom;
-}
-__device__ V3 bsdf_sample(const Bsdf& b, double r0, double r1) {
-  if (b.kind == 0) {  // CosineHemisphere (math/sample/sample.go:18-27)
-    const double r = sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
-    return expand(b.U, b.V, b.N, v3((float)(r * cos(th)), (float)(r * sin(th)), (float)sqrt(r0)));
-  }
-  const float alpha = sqr(b.rough);  // MicrofacetGGX.Sample
-  const double thetaM = atan2((double)alpha * sqrt(r0), sqrt(1 - r0));
-  const double phiM = 2.0 * 3.14159265358979323846 * r1;
-  const V3 m = v3(gsin((float)thetaM) * gcos((float)phiM), gsin((float)thetaM) * gsin((float)phiM), gcos((float)thetaM));
-  const V3 wo = sub(scale(2.0f * fabsf(dot(m, b.wi)), m), b.wi);
-  return expand(b.U, b.V, b.N, normalize(wo));
-}
-__device__ double bsdf_pdf(const Bsdf& b, V3 wo_world) {
-  const V3 wo = project(b.U, b.V, b.N, wo_world);
-  if (b.kind == 0) return (double)gmax(0.0f, wo.z) / 3.14159265358979323846;
-  const float alpha = sqr(b.rough);
-  const V3 m = scale(signf(b.wi.z), normalize(add(b.wi, wo)));
-  const double pdf = (double)(ggx_d(m, alpha) * m.z);
-  return isnan(pdf) ? 0.0 : pdf;
-}
-__device__ Spec bsdf_eval(const Bsdf& b, V3 wo_world) {
-  const V3 wo = project(b.U, b.V, b.N, wo_world);
-  if (b.kind == 0) {  // OrenNayar.Eval (bsdf/orennayar.go:42-73)
-    const float sigma = b.rough;
-    const float A = 1 - (0.5f * (sigma * sigma) / ((sigma * sigma) + 0.57f));
-    const float B = 0.45f * (sigma * sigma) / ((sigma * sigma) + 0.09f);
-    const float phiI = gatan2(b.wi.y, b.wi.x), phiO = gatan2(wo.y, wo.x);
-    const float thetaI = gacos(b.wi.z), thetaO = gacos(wo.z);
-    const float alpha = gmax(thetaI, thetaO), beta = gmin(thetaI, thetaO);
-    const float C = gsin(alpha) * gtan(beta);
-    const float gamma = gcos(phiO - phiI);
-    const float s = wo.z * (A + (B * gmax(0.0f, gamma) * C));
-    Spec rho = from_rgb(RGB{{1, 1, 1}}, b.lambda);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) rho.c[k] *= s / kPi;
-    return rho;
-  }
-  const float alpha = sqr(b.rough);  // MicrofacetGGX.Eval (microfacetggx.go:119-145)
-  const V3 h = scale(signf(b.wi.z), normalize(add(b.wi, wo)));
-  const RGB f = fresnel_kr(b.fr, fabsf(dot(b.wi, h)));
-  const float numer = ggx_g1(b.wi, h, alpha) * ggx_g1(wo, h, alpha) * ggx_d(h, alpha);
-  const float denom = 4 * fabsf(b.wi.z) * fabsf(wo.z);
-  Spec rho = from_rgb(f, b.lambda);
-  const float s = fabsf(wo.z) * numer / denom;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    rho.c[k] *= s;
-    if (rho.c[k] < 0 || isnan(rho.c[k])) rho.c[k] = 0;
-  }
-  return rho;
-}
-
-// ----------------------------------------------------------- scene data ---
-struct RMesh {
-  const float4* tris;      // leaf order, as the traversal holds them
-  const float4* nrm;       // per corner (leaf order) or null
-  const uint8_t* sidx;     // per leaf-order triangle or null
-  const uint32_t* shaders; // PolyMesh.Shader
-  uint32_t n_shaders;
-  uint32_t pad;
-};
-struct RLight {
-  float p[9];
-  int samples;
-  uint32_t shader;
-  uint32_t geom;
-};
-
-struct Ctx {
-  V3 P, N, Ng, Poffset, DdPdu, DdPdv, Rd;
-  float lambda, time;
-  uint64_t I, scr0, scr1;
-  int32_t geom;
-};
-
-__device__ RGB emission(const vmr_shader_std& s) {
-  if (!(s.flags & VMR_SH_EMISSION_STRENGTH)) return RGB{{0, 0, 0}};
-  RGB e = (s.flags & VMR_SH_EMISSION_COLOUR) ? RGB{{s.emission_colour[0], s.emission_colour[1], s.emission_colour[2]}}
-                                            : RGB{{0, 0, 0}};
-  for (float& c : e.c) c *= s.emission_strength;
-  return e;
-}
-__device__ __forceinline__ float next_up(float v) {
-  if (isinf(v) && v > 0) return v;
-  if (v == 0.0f) v = 0.0f;
-  unsigned u = __float_as_uint(v);
-  u = v >= 0.0f ? u + 1 : u - 1;
-  return __uint_as_float(u);
-}
-__device__ __forceinline__ float next_down(float v) {
-  if (isinf(v) && v < 0) return v;
-  if (v == 0.0f) v = 0.0f;
-  unsigned u = __float_as_uint(v);
-  u = v >= 0.0f ? u - 1 : u + 1;
-  return __uint_as_float(u);
-}
-__device__ V3 offset_p(const Ctx& sc, int dir) {  // OffsetP (core/shader.go:139-163)
-  const V3 pofs = dir < 0 ? v3(-sc.Poffset.x, -sc.Poffset.y, -sc.Poffset.z) : sc.Poffset;
-  V3 po = add(sc.P, pofs);
-  float* p = &po.x;
-  const float* o = &pofs.x;
-  for (int i = 0; i < 3; ++i) {
-    if (o[i] > 0) p[i] = next_up(p[i]);
-    else if (o[i] < -0.0f) p[i] = next_down(p[i]);
-  }
-  return po;
-}
-
-__device__ __forceinline__ V3 lp(const RLight& L, int k) { return v3(L.p[3 * k], L.p[3 * k + 1], L.p[3 * k + 2]); }
-__device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) { return 0.5f * length(cross(sub(p1, p0), sub(p2, p0))); }
-__device__ void sides_to_angles(float as, float bs, float cs, float& a, float& b, float& c) {
-  const float ssu = (as + bs + cs) / 2;
-  const float sa = gsin(ssu - as), sb = gsin(ssu - bs), sc2 = gsin(ssu - cs), s = gsin(ssu);
-  a = 2 * gatan(sqrtf(sb * sc2 / (s * sa)));
-  b = 2 * gatan(sqrtf(sa * sc2 / (s * sb)));
-  c = 2 * gatan(sqrtf(sa * sb / (s * sc2)));
-}
-// sampleSphericalTriangle (triangle.go:474-535)
-__device__ V3 sample_spherical(V3 p0, V3 p1, V3 p2, V3 p, double r0, double r1, double& pdf) {
-  const V3 pa = normalize(sub(p0, p)), pb = normalize(sub(p1, p)), pc = normalize(sub(p2, p));
-  const float a = gacos(dot(pb, pc)), b = gacos(dot(pc, pa)), c = gacos(dot(pa, pb));
-  float alpha, beta, gamma;
-  sides_to_angles(a, b, c, alpha, beta, gamma);
-  const float area = alpha + beta + gamma - kPi;
-  const float areaHat = (float)r0 * area;
-  const float s = gsin(areaHat - alpha), t = gcos(areaHat - alpha);
-  const float sinA = gsin(alpha), cosA = gcos(alpha);
-  const float u = t - cosA;
-  const float v = s + sinA * gcos(c);
-  float q = ((v * t - u * s) * cosA - v) / ((v * s + u * t) * sinA);
-  q = gmax(-1.0f, gmin(q, 1.0f));
-  float w = dot(pc, pa);
-  const V3 v31 = normalize(v3(pc.x - w * pa.x, pc.y - w * pa.y, pc.z - w * pa.z));
-  const float sq = sqrtf(1 - q * q);
-  const V3 v4 = v3(q * pa.x + sq * v31.x, q * pa.y + sq * v31.y, q * pa.z + sq * v31.z);
-  const float z = 1 - (float)r1 * (1 - dot(v4, pb));
-  w = dot(v4, pb);
-  const V3 v42 = normalize(v3(v4.x - w * pb.x, v4.y - w * pb.y, v4.z - w * pb.z));
-  pdf = 1 / (double)area;
-  return add(scale(z, pb), scale(sqrtf(1 - z * z), v42));
-}
-__device__ bool ray_plane(V3 Ro, V3 Rd, V3 P, V3 N, float& t) {
-  const float denom = dot(N, Rd);
-  if (fabsf(denom) > 1e-6f) {
-    t = dot(sub(P, Ro), N) / denom;
-    return t >= 0;
-  }
-  t = 0;
-  return false;
-}
-__device__ bool ray_tri(V3 Ro, V3 Rd, V3 P0, V3 P1, V3 P2, V3& out) {  // Moller-Trumbore
-  const V3 e1 = sub(P1, P0), e2 = sub(P2, P0);
-  const V3 P = cross(Rd, e2);
-  const float det = dot(e1, P);
-  if (det > -1e-6f && det < 1e-6f) return false;
-  const float inv = 1 / det;
-  const V3 T = sub(Ro, P0);
-  const float u = dot(T, P) * inv;
-  if (u < 0 || u > 1) return false;
-  const V3 Q = cross(T, e1);
-  const float v = dot(Rd, Q) * inv;
-  if (v < 0 || u + v > 1) return false;
-  const float t = dot(e2, Q) * inv;
-  if (t > 1e-6f) {
-    out = add(add(scale(1 - u - v, P0), scale(u, P1)), scale(v, P2));
-    return true;
-  }
-  return false;
-}
 
 // A light-sample candidate: direction, distance, pdf, spectrum.
 struct Cand {
@@ -518,28 +151,14 @@ __global__ void k_generate(RenderBatch b) {
   if (s >= b.n) return;
   const uint32_t pix = (uint32_t)(s % b.npix);
   const uint32_t j = b.iter0 + (uint32_t)(s / b.npix) + 1;  // render(iter+1)
-  const uint32_t x = pix % b.width, y = pix / b.width;
-  double rx, ry;
-  raster_xy(j, x, y, rx, ry);
-  const double time = vdc(j, scramble(b.seed, pix, 2));
-  const double lambda = (720.0 - 450.0) * vdc(j, scramble(b.seed, pix, 3)) + 450.0;
-  const float Sx = (float)(-1.0 + 2.0 * (rx / (double)b.width));
-  const float Sy = -(float)(-1.0 + 2.0 * (ry / (double)b.height));
-  const vmr_camera& c = b.cam;
-  const float camu = Sx * c.tan_theta_focal;
-  const float camv = Sy * (c.tan_theta_focal / c.aspect);
-  const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
-  const float* M = c.m;
-  const V3 d = v3(M[0] * s3.x + M[4] * s3.y + M[8] * s3.z, M[1] * s3.x + M[5] * s3.y + M[9] * s3.z,
-                  M[2] * s3.x + M[6] * s3.y + M[10] * s3.z);
-  const V3 D = normalize(d);
-  const V3 P = v3(M[0] * 0.0f + M[4] * 0.0f + M[8] * 0.0f + M[12], M[1] * 0.0f + M[5] * 0.0f + M[9] * 0.0f + M[13],
-                  M[2] * 0.0f + M[6] * 0.0f + M[10] * 0.0f + M[14]);
+  V3 P, D;
+  float time, lambda;
+  camera_primary(b.cam, b.width, b.height, j, pix, b.seed, P, D, time, lambda);
   b.px[s] = P.x; b.py[s] = P.y; b.pz[s] = P.z;
   b.dx[s] = D.x; b.dy[s] = D.y; b.dz[s] = D.z;
   b.tmax[s] = __int_as_float(0x7f800000);
-  b.time[s] = (float)time;
-  b.lambda[s] = (float)lambda;
+  b.time[s] = time;
+  b.lambda[s] = lambda;
 }
 
 // Queues one shadow ray (one atomic per warp for the lanes that want one).
@@ -646,37 +265,10 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b) {
   if (prim < 0) return;
   const int32_t geom = b.hgeom[s];
   const RMesh& m = b.meshes[geom];
-  const float U = b.hu[s], V = b.hv[s], W = b.hw[s];
-  const float4 a0 = m.tris[3 * (size_t)prim], a1 = m.tris[3 * (size_t)prim + 1], a2 = m.tris[3 * (size_t)prim + 2];
-  const V3 V0 = v3(a0.x, a0.y, a0.z), V1 = v3(a1.x, a1.y, a1.z), V2 = v3(a2.x, a2.y, a2.z);
-  const uint32_t sidx = m.sidx ? m.sidx[prim] : 0u;
-  if (sidx >= m.n_shaders) return;  // no shader: core.Trace returns false (trace.go:281-283)
-  const uint32_t shid = m.shaders[sidx];
-  const vmr_shader_std& sh = b.shaders[shid];
   Ctx sc;
-  const float xs = fabsf(U * V0.x) + fabsf(V * V1.x) + fabsf(W * V2.x);
-  const float ys = fabsf(U * V0.y) + fabsf(V * V1.y) + fabsf(W * V2.y);
-  const float zs = fabsf(U * V0.z) + fabsf(V * V1.z) + fabsf(W * V2.z);
-  const V3 e0 = sub(V1, V0), e1 = sub(V2, V0);
-  const V3 Ng = normalize(v3(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x));
-  V3 N = Ng;
-  if (m.nrm) {
-    const float4 n0 = m.nrm[3 * (size_t)prim], n1 = m.nrm[3 * (size_t)prim + 1], n2 = m.nrm[3 * (size_t)prim + 2];
-    N = normalize(v3(U * n0.x + V * n1.x + W * n2.x, U * n0.y + V * n1.y + W * n2.y, U * n0.z + V * n1.z + W * n2.z));
-  }
-  const float g7 = (7.0f * 5.96046448e-08f) / (1 - 7.0f * 5.96046448e-08f);  // Gamma(7) (math/ferror.go:22-24)
-  const float d = g7 * xs * fabsf(Ng.x) + g7 * ys * fabsf(Ng.y) + g7 * zs * fabsf(Ng.z);
-  sc.Poffset = scale(d, Ng);
-  sc.P = v3(U * V0.x + V * V1.x + W * V2.x, U * V0.y + V * V1.y + W * V2.y, U * V0.z + V * V1.z + W * V2.z);
-  V3 axisu = sub(v3(1, 0, 0), scale(dot(v3(1, 0, 0), Ng), Ng));
-  if (len2(axisu) < 0.1f || fabsf(dot(axisu, Ng)) > 0.3f) axisu = sub(v3(0, 0, 1), scale(dot(v3(0, 0, 1), Ng), Ng));
-  const V3 dpdu = normalize(axisu);
-  const V3 dpdv = cross(Ng, dpdu);
-  // ApplyTransform with the identity transform renormalises (core/shader.go:129-135)
-  sc.N = normalize(N);
-  sc.Ng = normalize(Ng);
-  sc.DdPdu = normalize(dpdu);
-  sc.DdPdv = normalize(dpdv);
+  uint32_t shid;
+  if (!hit_attributes(m, prim, b.hu[s], b.hv[s], b.hw[s], sc, shid)) return;
+  const vmr_shader_std& sh = b.shaders[shid];
   sc.Rd = v3(b.dx[s], b.dy[s], b.dz[s]);
   sc.lambda = b.lambda[s];
   sc.time = b.time[s];

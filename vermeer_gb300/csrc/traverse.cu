@@ -569,7 +569,11 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
 
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays, HitSoA hits, uint64_t n,
-                                                     DScratch* scratch) {
+                                                     DScratch* scratch, const unsigned long long* n_dev) {
+  if (n_dev) {
+    const uint64_t nd = *n_dev;
+    n = nd < n ? nd : n;
+  }
   int2 stk[kStackCapacity];
   Counters cnt{0, 0, 0};
   const unsigned lane = threadIdx.x & 31u;
@@ -1147,7 +1151,7 @@ int launch_scene_t(const DTop& top, const TraceLaunch& l) {
   auto k = k_trace_scene<ANY, COUNT>;
   const int block = 128;
   const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
-  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch);
+  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev);
   return (int)cudaGetLastError();
 }
 

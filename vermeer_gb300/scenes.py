@@ -193,3 +193,163 @@ def small_room(n_tris: int = 16384, seed: int = 1, res: int = 256, n_albedo: int
                            mesh=len(meshes) - 1))
     cam = lookat_camera((0.0, 0.0, -3.4), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, 1.0)
     return dict(meshes=meshes, shaders=shaders, lights=lights, camera=cam, res=res)
+
+
+# -------------------------------------------------- extended-mode scenes ---
+def _lattice(seed: int, ix, iy, iz) -> np.ndarray:
+    """Value of the noise lattice at integer points: uniform in [-1, 1) from
+    a SplitMix64 hash of (seed, ix, iy, iz)."""
+    with np.errstate(over="ignore"):
+        k = (np.asarray(ix, np.int64).astype(np.uint64) * np.uint64(0x8DA6B343)
+             ^ np.asarray(iy, np.int64).astype(np.uint64) * np.uint64(0xD8163841)
+             ^ np.asarray(iz, np.int64).astype(np.uint64) * np.uint64(0xCB1AB31F))
+        z = np.uint64(seed) * _GOLD + k
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(40)).astype(np.float64) * (2.0 ** -23) - 1.0
+
+
+def value_noise(p: np.ndarray, seed: int) -> np.ndarray:
+    """3-D value noise in [-1, 1): lattice values interpolated trilinearly
+    with smoothstep weights."""
+    f = np.floor(p)
+    i = f.astype(np.int64)
+    t = p - f
+    w = t * t * (3.0 - 2.0 * t)
+    out = np.zeros(p.shape[0])
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                c = _lattice(seed, i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz)
+                wx = w[:, 0] if dx else 1 - w[:, 0]
+                wy = w[:, 1] if dy else 1 - w[:, 1]
+                wz = w[:, 2] if dz else 1 - w[:, 2]
+                out += c * wx * wy * wz
+    return out
+
+
+def octasphere(center, radius: float, subdiv: int, displace: float = 0.0, seed: int = 0, freq: float = 4.0):
+    """A sphere of 8*subdiv^2 triangles: each face of an octahedron split
+    into a subdiv x subdiv triangle grid, vertices projected to the sphere and
+    moved radially by radius*displace*value_noise(freq*unit_dir).  Wound
+    so geometric normals point outward.  Returns (verts [3n,3] float32, idxp,
+    normals [3n,3] float32 of the undisplaced sphere)."""
+    n = subdiv
+    ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    keep = ii + jj <= n
+    gi, gj = ii[keep], jj[keep]
+    index = -np.ones((n + 1, n + 1), np.int64)
+    index[gi, gj] = np.arange(gi.size)
+    tris = []
+    for i in range(n):
+        for j in range(n - i):
+            tris.append((index[i, j], index[i + 1, j], index[i, j + 1]))
+            if i + j < n - 1:
+                tris.append((index[i + 1, j], index[i + 1, j + 1], index[i, j + 1]))
+    tris = np.asarray(tris, np.int64)
+    all_v = []
+    for sx in (1, -1):
+        for sy in (1, -1):
+            for sz in (1, -1):
+                A, B, C = np.array([sx, 0, 0.0]), np.array([0, sy, 0.0]), np.array([0, 0, sz * 1.0])
+                if sx * sy * sz < 0:
+                    B, C = C, B
+                pts = (A[None] * (n - gi - gj)[:, None] + B[None] * gi[:, None] + C[None] * gj[:, None]) / n
+                all_v.append(pts[tris].reshape(-1, 3))
+    u = np.concatenate(all_v)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = radius * (1.0 + displace * value_noise(freq * u, seed)) if displace else np.full(u.shape[0], radius)
+    verts = (np.asarray(center, np.float64)[None] + u * r[:, None]).astype(np.float32)
+    return verts, np.arange(verts.shape[0], dtype=np.uint32), u.astype(np.float32)
+
+
+def quad_light_mesh(p0, e1, e2):
+    """The emissive mesh of a quad light: triangles (p0, p0+e1, p0+e1+e2)
+    and (p0, p0+e1+e2, p0+e2), whose geometric normals point along e1 x e2."""
+    p0, e1, e2 = (np.asarray(a, np.float32) for a in (p0, e1, e2))
+    v = np.stack([p0, p0 + e1, p0 + e1 + e2, p0, p0 + e1 + e2, p0 + e2]).astype(np.float32)
+    return v, np.arange(6, dtype=np.uint32)
+
+
+def furnace(albedo: float = 0.5, env: float = 1.0, subdiv: int = 12) -> dict:
+    """A flat-shaded (convex) tessellated unit sphere, Lambert albedo
+    `albedo`, under a constant environment `env` and nothing else.  Every
+    pixel that sees the sphere converges to albedo*env exactly (each bounce
+    off a convex object sees only the environment), every other pixel to
+    env."""
+    v, i, _ = octasphere((0.0, 0.0, 0.0), 1.0, subdiv)
+    shaders = [dict(diffuse_colour=(albedo, albedo, albedo), diffuse_strength=1.0, diffuse_roughness=0.0)]
+    cam = lookat_camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, 1.0)
+    return dict(meshes=[dict(verts=v, idxp=i, shaders=[0])], shaders=shaders, lights=[], quad_lights=[],
+                env=(env, env, env), camera=cam)
+
+
+def sphere_grid(per_side: int = 16, subdiv: int = 32, seed: int = 3, width: int = 1920, height: int = 1080,
+                env=(0.05, 0.06, 0.08)) -> dict:
+    """The full-render configuration: per_side^2 noise-displaced spheres of
+    8*subdiv^2 triangles (16x16 x 8,192 = 2,097,152 by default; radius 0.4,
+    radial displacement 0.05 x value noise, seed 3) on a 40x40 ground plane,
+    each with a mixed diffuse + GGX ShaderStd (diffuse colour uniform in
+    [0.2, 0.8], weights 0.7/0.3, GGX roughness uniform in [0.05, 0.6],
+    dielectric Fresnel with IOR 1.5, i.e. F0 = 0.04), four 2x2 quad lights of
+    radiance 15 at height 8, a constant environment light, and a pinhole
+    camera at the image's aspect."""
+    meshes, shaders = [], []
+    ns = per_side * per_side
+    col = 0.2 + 0.6 * np.stack([uniform(seed, ns, 400 + k) for k in range(3)], axis=1)
+    rough = 0.05 + 0.55 * uniform(seed, ns, 410)
+    off = (per_side - 1) / 2.0
+    for k in range(ns):
+        gx, gz = k % per_side, k // per_side
+        c = (gx - off, 0.4, gz - off)
+        v, i, nrm = octasphere(c, 0.4, subdiv, displace=0.05, seed=seed * 1000 + k)
+        shaders.append(dict(diffuse_colour=col[k], diffuse_strength=0.7, diffuse_roughness=0.0,
+                            spec1_colour=(1.0, 1.0, 1.0), spec1_strength=0.3, spec1_roughness=float(rough[k]),
+                            ior=1.5))
+        meshes.append(dict(verts=v, idxp=i, shaders=[k]))
+    g = 20.0
+    gv = np.asarray([(-g, 0, -g), (-g, 0, g), (g, 0, g), (-g, 0, -g), (g, 0, g), (g, 0, -g)], np.float32)
+    shaders.append(dict(diffuse_colour=(0.5, 0.5, 0.5), diffuse_strength=1.0, diffuse_roughness=0.0))
+    meshes.append(dict(verts=gv, idxp=np.arange(6, dtype=np.uint32), shaders=[len(shaders) - 1]))
+    light_shader = len(shaders)
+    shaders.append(dict(emission_colour=(1.0, 1.0, 1.0), emission_strength=15.0, diffuse_colour=(0.0, 0.0, 0.0),
+                        diffuse_strength=1.0, diffuse_roughness=0.0))
+    quads = []
+    for x, z in ((-4.0, -4.0), (4.0, -4.0), (-4.0, 4.0), (4.0, 4.0)):
+        p0, e1, e2 = (x - 1.0, 8.0, z - 1.0), (2.0, 0.0, 0.0), (0.0, 0.0, 2.0)
+        v, i = quad_light_mesh(p0, e1, e2)
+        meshes.append(dict(verts=v, idxp=i, shaders=[light_shader]))
+        quads.append(dict(p0=p0, e1=e1, e2=e2, shader=light_shader, mesh=len(meshes) - 1))
+    cam = lookat_camera((0.0, 7.0, -16.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 45.0, width / height)
+    return dict(meshes=meshes, shaders=shaders, lights=[], quad_lights=quads, env=tuple(env), camera=cam,
+                width=width, height=height)
+
+
+def small_room_ext(n_tris: int = 4096, seed: int = 1, env=(0.2, 0.25, 0.3)) -> dict:
+    """The small room for the extended path tracer, with every light kind
+    and lobe: the two TriLight panels, a 0.4 x 0.3 quad light recessed in the
+    ceiling opening (radiance 5), a constant environment seen through the
+    open side, and the soup's eight materials cycling through Lambert,
+    OrenNayar (roughness 0.6), diffuse + GGX (roughness 0.3 and 0.7) and
+    diffuse + mirror (Spec1Roughness 0)."""
+    sc = small_room(n_tris, seed=seed)
+    kinds = [
+        dict(diffuse_roughness=0.0),
+        dict(diffuse_roughness=0.6),
+        dict(diffuse_roughness=0.0, spec1_colour=(1.0, 1.0, 1.0), spec1_strength=0.5, spec1_roughness=0.3, ior=1.5),
+        dict(diffuse_roughness=0.0, spec1_colour=(0.9, 0.8, 0.6), spec1_strength=0.4, spec1_roughness=0.7,
+             spec1_fresnel="Metal", spec1_fresnel_refl=(0.9, 0.6, 0.3)),
+        dict(diffuse_roughness=0.0, spec1_colour=(1.0, 1.0, 1.0), spec1_strength=0.3, spec1_roughness=0.0, ior=1.5),
+    ]
+    for k, sid in enumerate(range(5, 13)):
+        sc["shaders"][sid] = dict(sc["shaders"][sid], **kinds[k % len(kinds)])
+    light_shader = len(sc["shaders"])
+    sc["shaders"].append(dict(emission_colour=(1.0, 0.9, 0.8), emission_strength=5.0, diffuse_colour=(0.0, 0.0, 0.0),
+                              diffuse_strength=1.0, diffuse_roughness=0.0))
+    p0, e1, e2 = (-0.2, 1.15, -0.15), (0.4, 0.0, 0.0), (0.0, 0.0, 0.3)
+    v, i = quad_light_mesh(p0, e1, e2)
+    sc["meshes"].append(dict(verts=v, idxp=i, shaders=[light_shader]))
+    sc["quad_lights"] = [dict(p0=p0, e1=e1, e2=e2, shader=light_shader, mesh=len(sc["meshes"]) - 1)]
+    sc["env"] = tuple(env)
+    return sc
