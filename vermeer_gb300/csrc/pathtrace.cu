@@ -231,7 +231,7 @@ __device__ __forceinline__ void put_ray(float* q, uint32_t cap, uint64_t i, cons
 }
 
 __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
-  const uint64_t n = b.it->n;
+  const uint64_t n = b.it->n < b.cap ? b.it->n : b.cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) b.qlen[0] = n;
   for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t pix = (uint32_t)(s % b.npix);
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
 
 // One bounce of every path in queue d.
 __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
-  const uint64_t n = b.qlen[d];
+  const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
   const float* q = b.qray[d & 1];
   const uint32_t* qp = b.qpath[d & 1];
   float* nq = b.qray[(d + 1) & 1];
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
 // Unoccluded shadow rays add their contribution, in queue order (each path
 // has at most one shadow ray per bounce, so no two threads touch one path).
 __global__ void __launch_bounds__(kPtBlock) k_pt_resolve(PtBatch b, uint32_t d) {
-  const uint64_t n = b.slen[d];
+  const uint64_t n = b.slen[d] < b.cap ? b.slen[d] : b.cap;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     if (b.shit[i] >= 0) continue;
     const uint32_t p = b.spath[i];
