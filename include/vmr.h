@@ -350,6 +350,41 @@ typedef struct {
  * fold starts at i+1 and so counts the initial buffer as a sample, F6). */
 int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* params, float* fb, vmr_path_stats* stats);
 
+/* ------------------------------------------------------------ path guide */
+/* No counterpart in the reference.  A small MLP proposes directions at path
+ * vertices: inputs = the hit point normalised to the scene bounds [lo, hi]
+ * encoded with 12 sin/cos frequencies per axis, the shading normal and the
+ * direction toward the previous vertex (78 values, plus a constant 1);
+ * 4 hidden ReLU layers of 64; outputs = 8 von Mises-Fisher lobes (direction,
+ * concentration, mixture logit).  Weights: W0 [64][80], W1..W3 [64][64],
+ * W4 [40][64] row-major, concatenated (VMR_GUIDE_WEIGHTS floats); the
+ * kernels run them on the tensor cores in bf16 with float32 accumulation.
+ * Vertex arrays are host pointers to n x 3 floats. */
+#define VMR_GUIDE_WEIGHTS 19968
+
+typedef struct {
+    float lr, beta1, beta2, eps;
+} vmr_adam;
+
+/* He-uniform initial weights from a seed (the output layer scaled by 0.1);
+ * resets the optimiser. */
+int vmr_guide_init(vmr_ctx* ctx, uint64_t seed);
+int vmr_guide_set_weights(vmr_ctx* ctx, const float* weights);
+int vmr_guide_get_weights(vmr_ctx* ctx, float* weights);
+/* The 40 outputs of n vertices (out: n x 40 floats). */
+int vmr_guide_forward(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, size_t n,
+                      const float lo[3], const float hi[3], float* out);
+/* Gradient of sum_i -weight_i * log p_i(omega_i) with respect to the weights
+ * (grad: VMR_GUIDE_WEIGHTS floats) and the loss itself; omega: n x 3 unit
+ * directions, weight: n floats.  The weights are not changed. */
+int vmr_guide_gradient(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
+                       const float* weight, size_t n, const float lo[3], const float hi[3], float* grad,
+                       float* loss);
+/* One Adam step on that loss divided by the sum of the weights. */
+int vmr_guide_train_step(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
+                         const float* weight, size_t n, const float lo[3], const float hi[3], const vmr_adam* opt,
+                         float* loss);
+
 /* -------------------------------------------------------------- no-alloc */
 /* No counterpart in the reference.  For callers that must not have a library
  * allocate device memory while they run (they manage the whole device

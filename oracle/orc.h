@@ -186,6 +186,19 @@ int orc_pt_run(const orc_render* r, const orc_quad_light* quads, uint32_t n_quad
 /* Random number `dim` of pixel sample (pix, j = iteration + 1). */
 float orc_pt_rnd(uint64_t seed, uint64_t pix, uint32_t j, uint32_t dim);
 
+/* Path-guiding network (orc_mlp.cpp; no reference counterpart).  Weights:
+ * W0 [64][80], W1..W3 [64][64], W4 [40][64] concatenated, row-major.
+ * precision: 64, 32, or 16 (the CUDA kernels' bfloat16 roundings with
+ * float32 accumulation). */
+int orc_guide_n_weights(void);
+void orc_guide_features(const float* pos, const float* nrm, const float* wo, const float* lo, const float* hi, int n,
+                        double* feat);
+void orc_guide_forward(const float* W, const double* feat, int n, int precision, double* out);
+double orc_guide_pdf(const double* out40, const double* w);
+void orc_guide_out_grad(const double* out40, const double* w, double weight, double* g40, double* loss);
+double orc_guide_loss_grad(const float* W, const double* feat, const float* omega, const float* weight, int n,
+                           int precision, double* gW);
+
 #ifdef __cplusplus
 }
 #endif

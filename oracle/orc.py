@@ -122,6 +122,67 @@ def _register_render(L):
     L.orc_pt_run.argtypes = [P, P, ctypes.c_uint32, P, P, P, ctypes.c_int, ctypes.c_int]
     L.orc_pt_rnd.restype = ctypes.c_float
     L.orc_pt_rnd.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
+    L.orc_guide_n_weights.restype = ctypes.c_int
+    L.orc_guide_features.argtypes = [P, P, P, P, P, ctypes.c_int, P]
+    L.orc_guide_forward.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P]
+    L.orc_guide_pdf.restype = ctypes.c_double
+    L.orc_guide_pdf.argtypes = [P, P]
+    L.orc_guide_out_grad.argtypes = [P, P, ctypes.c_double, P, P]
+    L.orc_guide_loss_grad.restype = ctypes.c_double
+    L.orc_guide_loss_grad.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, P]
+
+
+class Guide:
+    """The path-guiding network's oracle (orc_mlp.cpp)."""
+
+    N_IN, N_OUT = 80, 40
+
+    @staticmethod
+    def n_weights():
+        return lib().orc_guide_n_weights()
+
+    @staticmethod
+    def features(pos, nrm, wo, lo, hi):
+        pos, nrm, wo = (np.ascontiguousarray(a, np.float32) for a in (pos, nrm, wo))
+        lo, hi = np.ascontiguousarray(lo, np.float32), np.ascontiguousarray(hi, np.float32)
+        n = pos.shape[0]
+        f = np.zeros((n, 80), np.float64)
+        lib().orc_guide_features(_ptr(pos), _ptr(nrm), _ptr(wo), _ptr(lo), _ptr(hi), n, _ptr(f))
+        return f
+
+    @staticmethod
+    def forward(W, feat, precision=64):
+        W = np.ascontiguousarray(W, np.float32)
+        feat = np.ascontiguousarray(feat, np.float64)
+        out = np.zeros((feat.shape[0], 40), np.float64)
+        lib().orc_guide_forward(_ptr(W), _ptr(feat), feat.shape[0], int(precision), _ptr(out))
+        return out
+
+    @staticmethod
+    def pdf(out40, w):
+        o = np.ascontiguousarray(out40, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        return lib().orc_guide_pdf(_ptr(o), _ptr(w))
+
+    @staticmethod
+    def out_grad(out40, w, weight):
+        o = np.ascontiguousarray(out40, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        g = np.zeros(40, np.float64)
+        loss = ctypes.c_double()
+        lib().orc_guide_out_grad(_ptr(o), _ptr(w), float(weight), _ptr(g), ctypes.byref(loss))
+        return g, loss.value
+
+    @staticmethod
+    def loss_grad(W, feat, omega, weight, precision=64):
+        W = np.ascontiguousarray(W, np.float32)
+        feat = np.ascontiguousarray(feat, np.float64)
+        omega = np.ascontiguousarray(omega, np.float32)
+        weight = np.ascontiguousarray(weight, np.float32)
+        g = np.zeros(W.size, np.float64)
+        loss = lib().orc_guide_loss_grad(_ptr(W), _ptr(feat), _ptr(omega), _ptr(weight), feat.shape[0],
+                                         int(precision), _ptr(g))
+        return loss, g
 
 
 class OrcQuadLight(ctypes.Structure):

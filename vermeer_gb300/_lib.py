@@ -101,6 +101,12 @@ class PathStats(ctypes.Structure):
 
 PATH_NO_GRAPH = 1
 
+GUIDE_WEIGHTS = 19968
+
+
+class Adam(ctypes.Structure):
+    _fields_ = [("lr", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("eps", ctypes.c_float)]
+
 SHADER_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
                 "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
                 "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
@@ -137,6 +143,14 @@ SIGNATURES = {
     "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_env_light": (ctypes.c_int, [P, P]),
     "vmr_render_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, ctypes.POINTER(PathStats)]),
+    "vmr_guide_init": (ctypes.c_int, [P, ctypes.c_uint64]),
+    "vmr_guide_set_weights": (ctypes.c_int, [P, P]),
+    "vmr_guide_get_weights": (ctypes.c_int, [P, P]),
+    "vmr_guide_forward": (ctypes.c_int, [P, P, P, P, ctypes.c_size_t, P, P, P]),
+    "vmr_guide_gradient": (ctypes.c_int, [P, P, P, P, P, P, ctypes.c_size_t, P, P, P,
+                                          ctypes.POINTER(ctypes.c_float)]),
+    "vmr_guide_train_step": (ctypes.c_int, [P, P, P, P, P, P, ctypes.c_size_t, P, P, ctypes.POINTER(Adam),
+                                            ctypes.POINTER(ctypes.c_float)]),
     "vmr_trace_mesh_noalloc": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                               ctypes.POINTER(Hits)]),
 }

@@ -254,6 +254,47 @@ class Context:
         return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,
                         graph_replays=st.graph_replays, ms=st.ms)
 
+    # ------------------------------------------------------------ guide ---
+    def guide_init(self, seed: int = 0):
+        self._check(self.L.vmr_guide_init(self.h, int(seed)))
+
+    def guide_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        assert w.size == _lib.GUIDE_WEIGHTS
+        self._check(self.L.vmr_guide_set_weights(self.h, _p(w)))
+
+    def guide_get_weights(self):
+        w = np.zeros(_lib.GUIDE_WEIGHTS, np.float32)
+        self._check(self.L.vmr_guide_get_weights(self.h, _p(w)))
+        return w
+
+    @staticmethod
+    def _rows(*arrs):
+        return [np.ascontiguousarray(a, np.float32) for a in arrs]
+
+    def guide_forward(self, pos, nrm, wo, lo, hi):
+        pos, nrm, wo, lo, hi = self._rows(pos, nrm, wo, lo, hi)
+        n = pos.shape[0]
+        out = np.zeros((n, 40), np.float32)
+        self._check(self.L.vmr_guide_forward(self.h, _p(pos), _p(nrm), _p(wo), n, _p(lo), _p(hi), _p(out)))
+        return out
+
+    def guide_gradient(self, pos, nrm, wo, omega, weight, lo, hi):
+        pos, nrm, wo, omega, weight, lo, hi = self._rows(pos, nrm, wo, omega, weight, lo, hi)
+        g = np.zeros(_lib.GUIDE_WEIGHTS, np.float32)
+        loss = ctypes.c_float()
+        self._check(self.L.vmr_guide_gradient(self.h, _p(pos), _p(nrm), _p(wo), _p(omega), _p(weight), pos.shape[0],
+                                              _p(lo), _p(hi), _p(g), ctypes.byref(loss)))
+        return g.astype(np.float64), loss.value
+
+    def guide_train_step(self, pos, nrm, wo, omega, weight, lo, hi, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        pos, nrm, wo, omega, weight, lo, hi = self._rows(pos, nrm, wo, omega, weight, lo, hi)
+        a = _lib.Adam(lr, beta1, beta2, eps)
+        loss = ctypes.c_float()
+        self._check(self.L.vmr_guide_train_step(self.h, _p(pos), _p(nrm), _p(wo), _p(omega), _p(weight),
+                                                pos.shape[0], _p(lo), _p(hi), ctypes.byref(a), ctypes.byref(loss)))
+        return loss.value
+
     def set_camera(self, cam: dict):
         c = _lib.Camera()
         for i in range(16):

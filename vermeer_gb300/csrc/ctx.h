@@ -72,6 +72,17 @@ struct RenderState {
   ~RenderState() { if (pt_host) cudaFreeHost(pt_host); }
 };
 
+// The path-guiding network (guide.cu): float32 master weights with Adam
+// state, bf16 forward and transposed copies, and training scratch.
+struct GuideState {
+  bool ready = false;
+  int step = 0;
+  DevBuf W, m, v, grad, wf, wb, sums, err;
+  DevBuf save;          // bf16 feature-major activations and deltas
+  uint32_t save_rows = 0;
+  DevBuf io;            // host-call staging (SoA rows, outputs)
+};
+
 struct TopRec {
   HostTop host;
   DevBuf nodes, mnodes, mboxes, order, meshes;
@@ -97,6 +108,7 @@ struct vmr_ctx {
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
   vmr::RenderState render;
+  vmr::GuideState guide;
   vmr_tuning tuning{13, 0, 0, 0, 4};
   // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
   const float* mesh_bounds_of(const DMesh* d) const {

@@ -1,0 +1,46 @@
+// guide.h - launch interface of the path-guiding network (guide.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace vmr {
+namespace guide {
+
+constexpr int kGuideWeights = 19968;  // W0 64x80, W1..W3 64x64, W4 40x64
+constexpr uint32_t kSaveRows = 640;   // feature-major rows saved per training record
+
+// Path vertices (SoA, device pointers): hit point, shading normal, direction
+// toward the previous vertex; n rows, or *n_dev rows when n_dev is set.
+struct GuideRows {
+  const float *px, *py, *pz, *nx, *ny, *nz, *wx, *wy, *wz;
+  uint64_t n;
+  const unsigned long long* n_dev;
+  float lo[3], inv_ext[3];  // scene bounds: q = (p - lo) * inv_ext
+};
+
+// Training records: the rows plus the sampled direction and its weight
+// (incident radiance over the density it was sampled with).
+struct GuideTrain {
+  GuideRows rows;
+  const float *ox, *oy, *oz, *weight;
+  uint32_t stride;  // rows of the save buffer's feature-major arrays
+};
+
+struct GuideAdam {
+  float lr, beta1, beta2, eps;
+  int step;  // 0: only refresh the bf16 copies
+};
+
+size_t wf_elems();
+size_t wb_elems();
+int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int grid, cudaStream_t st);
+int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int grid,
+                 cudaStream_t st);
+int launch_wgrad(const void* save, uint32_t B, uint64_t n, float* grad, int* err, int chunks, cudaStream_t st);
+int launch_adam(float* W, float* m, float* v, float* grad, const float* sums, const GuideAdam& a, void* wf, void* wb,
+                cudaStream_t st);
+
+}  // namespace guide
+}  // namespace vmr
