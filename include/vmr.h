@@ -329,11 +329,24 @@ typedef struct {
     uint32_t flags;                   /* VMR_PATH_* */
     double* fb64;                     /* optional host width*height*3: the same
                                          running mean folded in float64 */
+    float guide_fraction;             /* VMR_PATH_GUIDED: probability of sampling
+                                         the guide at a vertex (0: 0.5) */
+    uint32_t train_steps;             /* VMR_PATH_TRAIN: Adam steps after each
+                                         batch (0: 4) */
+    uint32_t train_batch;             /* training records per step (0: 65536) */
+    float train_lr;                   /* Adam learning rate (0: 1e-3) */
 } vmr_path_params;
 
 enum {
-    VMR_PATH_NO_GRAPH = 1   /* launch the bounce loop stage by stage instead
+    VMR_PATH_NO_GRAPH = 1,  /* launch the bounce loop stage by stage instead
                                of replaying its CUDA graph */
+    VMR_PATH_GUIDED = 2,    /* one-sample MIS of the guide (vmr_guide_*) and the
+                               BSDF at every non-mirror vertex; the density of
+                               the mixture enters the NEE and emission weights,
+                               so the estimator stays unbiased */
+    VMR_PATH_TRAIN = 4      /* record (vertex, sampled direction, density,
+                               incident radiance) and train the guide on them
+                               after each batch (online) */
 };
 
 typedef struct {
@@ -342,6 +355,9 @@ typedef struct {
     uint64_t shadow_rays;
     uint32_t graph_replays;  /* batches run by replaying the captured graph */
     float ms;                /* device time */
+    uint64_t train_records;  /* training records collected */
+    uint32_t train_steps;    /* Adam steps taken */
+    float train_loss;        /* loss of the last step over its weight sum */
 } vmr_path_stats;
 
 /* Iterations iter_begin..iter_begin+iter_count-1 of every pixel folded into

@@ -180,3 +180,48 @@ def test_pt_converges_to_fp64_oracle(ctx, room, oracle_room):
     se = np.sqrt(np.var(bg - bo) / bg.size)
     assert abs(bg.mean() - bo.mean()) < 5 * se + 1e-6, (bg.mean(), bo.mean(), se)
     assert _block_relmse(g64, o64) < 0.01
+
+
+# --------------------------------------------------------- guided mode ----
+@pytest.mark.gpu
+def test_pt_guided_furnace_unbiased(ctx):
+    """One-sample MIS of an untrained (random) guide and the BSDF stays
+    unbiased: the furnace still converges to albedo x environment."""
+    sc = scenes.furnace(0.5, 1.0, subdiv=12)
+    ctx.load_scene(sc)
+    ctx.guide_init(3)
+    fb64 = np.zeros((64, 64, 3), np.float64)
+    ctx.render_path(64, 64, 0, 512, 19, max_depth=8, rr_depth=1, fb64=fb64, guided=True)
+    on, off = _disc_masks(64, 64)
+    v = fb64[on][:, 0]
+    assert abs(v.mean() - 0.5) < 5 * v.std() / np.sqrt(v.size), (v.mean(), v.std())
+    assert np.all(fb64[off] == 1.0)
+
+
+@pytest.mark.gpu
+def test_pt_guided_graph_equals_direct(ctx, room):
+    ctx.load_scene(room)
+    ctx.guide_init(4)
+    a, sa = ctx.render_path(32, 32, 0, 4, 6, guided=True)
+    b, sb = ctx.render_path(32, 32, 0, 4, 6, guided=True, graph=False)
+    assert a.tobytes() == b.tobytes()
+    assert sa["graph_replays"] == 1 and sb["graph_replays"] == 0
+
+
+@pytest.mark.gpu
+def test_pt_guided_training_matches_plain(ctx, room):
+    """Online training changes the sampling, not the expectation: the
+    guided+trained image and the plain one agree statistically."""
+    ctx.load_scene(room)
+    ctx.guide_init(5)
+    g64 = np.zeros((32, 32, 3), np.float64)
+    _, st = ctx.render_path(32, 32, 0, 256, 71, max_depth=4, fb64=g64, guided=True, train=True,
+                            max_batch_samples=32 * 32 * 16, train_steps=2, train_batch=8192)
+    assert st["train_records"] > 0 and st["train_steps"] > 0 and np.isfinite(st["train_loss"])
+    p64 = np.zeros((32, 32, 3), np.float64)
+    ctx.render_path(32, 32, 0, 256, 72, max_depth=4, fb64=p64)
+    bg = g64.reshape(4, 8, 4, 8, 3).mean((1, 3)).ravel()
+    bp = p64.reshape(4, 8, 4, 8, 3).mean((1, 3)).ravel()
+    se = np.sqrt(np.var(bg - bp) / bg.size)
+    assert abs(bg.mean() - bp.mean()) < 5 * se + 1e-6, (bg.mean(), bp.mean(), se)
+    assert _block_relmse(g64, p64) < 0.02

@@ -91,15 +91,19 @@ class QuadLight(ctypes.Structure):
 class PathParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
                 ("seed", ctypes.c_uint64), ("max_depth", U32), ("rr_depth", U32), ("max_batch_samples", U32),
-                ("flags", U32), ("fb64", P)]
+                ("flags", U32), ("fb64", P), ("guide_fraction", ctypes.c_float), ("train_steps", U32),
+                ("train_batch", U32), ("train_lr", ctypes.c_float)]
 
 
 class PathStats(ctypes.Structure):
     _fields_ = [("samples", ctypes.c_uint64), ("rays", ctypes.c_uint64), ("shadow_rays", ctypes.c_uint64),
-                ("graph_replays", U32), ("ms", ctypes.c_float)]
+                ("graph_replays", U32), ("ms", ctypes.c_float), ("train_records", ctypes.c_uint64),
+                ("train_steps", U32), ("train_loss", ctypes.c_float)]
 
 
 PATH_NO_GRAPH = 1
+PATH_GUIDED = 2
+PATH_TRAIN = 4
 
 GUIDE_WEIGHTS = 19968
 

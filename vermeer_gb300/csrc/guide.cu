@@ -481,11 +481,12 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideTrain tr, const __nv_b
 // blockIdx.y = layer, blockIdx.x strides the chunks; partial sums go to the
 // float32 gradient with atomics.
 constexpr uint32_t kGA = 0, kGB = 128 * 128 * 2, kWgradSmem = kGB + 80 * 128 * 2 + 64;
-__global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, uint32_t B, uint64_t n, float* grad,
-                                                     int* err) {
+__global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, uint32_t B, uint64_t n,
+                                                     const unsigned long long* n_dev, float* grad, int* err) {
   extern __shared__ __align__(1024) char sm[];
   __shared__ Shared sh;
   const uint32_t r = threadIdx.x;
+  if (n_dev) n = *n_dev < n ? *n_dev : n;
   const int l = blockIdx.y;
   // layer l: output deltas at row dz0 (M of them), inputs at row in0 (N)
   const uint32_t M = l == 4 ? 40u : 64u;
@@ -605,33 +606,29 @@ __global__ void k_guide_adam(float* W, float* m, float* v, float* grad, const fl
 
 }  // namespace
 
+void prepare_kernels() {
+  cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+  cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
+  cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgradSmem);
+}
+
 int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int grid, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
-    attr = true;
-  }
   k_guide_infer<<<grid, 128, kInferSmem, st>>>(rows, static_cast<const __nv_bfloat16*>(wf), out, err);
   return (int)cudaGetLastError();
 }
 
 int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int grid,
                  cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
-    cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgradSmem);
-    attr = true;
-  }
   k_guide_train<<<grid, 128, kTrainSmem, st>>>(tr, static_cast<const __nv_bfloat16*>(wf),
                                                 static_cast<const __nv_bfloat16*>(wb),
                                                 static_cast<__nv_bfloat16*>(save), sums, err);
   return (int)cudaGetLastError();
 }
 
-int launch_wgrad(const void* save, uint32_t B, uint64_t n, float* grad, int* err, int chunks, cudaStream_t st) {
+int launch_wgrad(const void* save, uint32_t B, uint64_t n, const unsigned long long* n_dev, float* grad, int* err,
+                 int chunks, cudaStream_t st) {
   dim3 g(chunks, 5);
-  k_guide_wgrad<<<g, 128, kWgradSmem, st>>>(static_cast<const __nv_bfloat16*>(save), B, n, grad, err);
+  k_guide_wgrad<<<g, 128, kWgradSmem, st>>>(static_cast<const __nv_bfloat16*>(save), B, n, n_dev, grad, err);
   return (int)cudaGetLastError();
 }
 
@@ -640,6 +637,11 @@ int launch_adam(float* W, float* m, float* v, float* grad, const float* sums, co
   k_guide_adam<<<(kGuideWeights + 255) / 256, 256, 0, st>>>(W, m, v, grad, sums, a, static_cast<__nv_bfloat16*>(wf),
                                                            static_cast<__nv_bfloat16*>(wb));
   return (int)cudaGetLastError();
+}
+
+int ensure_ready(vmr_ctx* ctx) {
+  if (ctx->guide.ready) return VMR_OK;
+  return vmr_guide_init(ctx, 0);
 }
 
 size_t wf_elems() { return kWfSize; }
@@ -669,6 +671,7 @@ using vmr::guide::kGuideWeights;
 int guide_alloc(vmr_ctx* ctx) {
   auto& G = ctx->guide;
   if (G.ready) return VMR_OK;
+  vmr::guide::prepare_kernels();
   const size_t nw = kGuideWeights * sizeof(float);
   GCUDA(G.W.ensure(nw));
   GCUDA(G.m.ensure(nw));
@@ -771,7 +774,7 @@ int guide_backprop(vmr_ctx* ctx, const GuideTrain& tr, size_t n) {
                                ctx->stream) != 0)
     return gfail(ctx, VMR_ERR_CUDA, "guide training kernel launch failed");
   const int chunks = (int)std::min<uint64_t>(tiles, (uint64_t)sms);
-  if (vmr::guide::launch_wgrad(G.save.p, (uint32_t)stride, n, G.grad.as<float>(), G.err.as<int>(), chunks,
+  if (vmr::guide::launch_wgrad(G.save.p, (uint32_t)stride, n, nullptr, G.grad.as<float>(), G.err.as<int>(), chunks,
                                ctx->stream) != 0)
     return gfail(ctx, VMR_ERR_CUDA, "guide weight-gradient kernel launch failed");
   return VMR_OK;

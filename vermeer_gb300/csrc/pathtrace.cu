@@ -31,6 +31,7 @@
 
 #include "ctx.h"
 #include "device.h"
+#include "guide.h"
 #include "shade_common.cuh"
 #include "vmr.h"
 
@@ -96,7 +97,22 @@ struct PtBatch {
   int* status;                 // worst traversal status over all batches
   float* fb;
   double* fb64;
+  // path guiding
+  float alpha;                 // probability of sampling the guide at a vertex
+  float glo[3];                // scene bounds for the guide's inputs
+  float* grow;                 // 9 * cap: guide input rows per queue entry
+  float* gout;                 // 40 * cap: guide outputs per queue entry
+  float* rec;                  // kRecCols * rcap training records (SoA)
+  uint32_t rcap;
+  unsigned long long* rcount;  // [2]: records this batch, records in total
+  uint32_t* last_rec;          // per path: its last record awaiting L_mark
 };
+
+// Training record columns: vertex (p, n, wo), sampled direction, weight
+// (filled after the bounce loop), density, throughput after the vertex,
+// radiance before the next vertex, path.
+constexpr int kRecCols = 21;
+enum RecCol { kRP = 0, kRN = 3, kRWo = 6, kROm = 9, kRW = 12, kRQ = 13, kRBeta = 14, kRMark = 17, kRPath = 20 };
 
 // ------------------------------------------------------------- random ----
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
@@ -230,6 +246,67 @@ __device__ __forceinline__ void put_ray(float* q, uint32_t cap, uint64_t i, cons
   q[7 * (size_t)cap + i] = time;
 }
 
+// ------------------------------------------------------- guide mixture ---
+// The 40 network outputs as 8 vMF lobes (the same decoding the trainer
+// differentiates): mu = normalize, kappa = min(softplus + 0.01, 1000),
+// pi = softmax; c = kappa / (2 pi (1 - exp(-2 kappa))).
+struct GMix {
+  float mu[8][3], kap[8], c[8], pi[8];
+};
+__device__ void gmix_decode(const float* o, GMix& g) {
+  float mx = -INFINITY;
+  for (int k = 0; k < 8; ++k) mx = fmaxf(mx, o[5 * k + 4]);
+  float z = 0.f;
+  for (int k = 0; k < 8; ++k) {
+    const float* r = o + 5 * k;
+    float n = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    n = n < 1e-6f ? 1e-6f : n;
+    for (int c = 0; c < 3; ++c) g.mu[k][c] = r[c] / n;
+    const float s = r[3];
+    const float kk = (s > 20.f ? s : log1pf(expf(s))) + 0.01f;
+    g.kap[k] = kk > 1000.f ? 1000.f : kk;
+    g.c[k] = g.kap[k] / (6.28318530718f * (-expm1f(-2.f * g.kap[k])));
+    g.pi[k] = expf(r[4] - mx);
+    z += g.pi[k];
+  }
+  for (int k = 0; k < 8; ++k) g.pi[k] /= z;
+}
+__device__ float gmix_pdf(const GMix& g, V3 w) {
+  float p = 0.f;
+  for (int k = 0; k < 8; ++k) {
+    const float d = g.mu[k][0] * w.x + g.mu[k][1] * w.y + g.mu[k][2] * w.z;
+    p += g.pi[k] * g.c[k] * expf(g.kap[k] * (d - 1.f));
+  }
+  return p;
+}
+// A direction from the mixture: lobe by u (cumulative pi), then the vMF
+// inversion w = 1 + log(u1 + (1-u1) e^{-2 kappa}) / kappa around mu.
+__device__ V3 gmix_sample(const GMix& g, float u, float u1, float u2) {
+  int k = 7;
+  float acc = 0.f;
+  for (int j = 0; j < 8; ++j) {
+    acc += g.pi[j];
+    if (u < acc) {
+      k = j;
+      break;
+    }
+  }
+  const float kap = g.kap[k];
+  float w = 1.f + logf(u1 + (1.f - u1) * expf(-2.f * kap)) / kap;
+  w = fminf(1.f, fmaxf(-1.f, w));
+  const float st = sqrtf(fmaxf(0.f, 1.f - w * w));
+  const float phi = 6.28318530718f * u2;
+  const V3 mu = v3(g.mu[k][0], g.mu[k][1], g.mu[k][2]);
+  const float sgn = mu.z >= 0.f ? 1.f : -1.f;  // orthonormal basis (Duff et al. 2017)
+  const float a = -1.f / (sgn + mu.z);
+  const float bb = mu.x * mu.y * a;
+  const V3 t1 = v3(1.f + sgn * mu.x * mu.x * a, sgn * bb, -sgn * mu.x);
+  const V3 t2 = v3(bb, sgn + mu.y * mu.y * a, -mu.y);
+  const float cp = cosf(phi), sp = sinf(phi);
+  return normalize(v3(w * mu.x + st * (cp * t1.x + sp * t2.x), w * mu.y + st * (cp * t1.y + sp * t2.y),
+                      w * mu.z + st * (cp * t1.z + sp * t2.z)));
+}
+
 __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
   const uint64_t n = b.it->n < b.cap ? b.it->n : b.cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) b.qlen[0] = n;
@@ -246,10 +323,40 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
     b.lx[s] = 0.0f; b.ly[s] = 0.0f; b.lz[s] = 0.0f;
     b.pdf[s] = 0.0f;
     b.key[s] = sample_key(b.seed, pix, j);
+    if (b.last_rec) b.last_rec[s] = 0xffffffffu;
   }
 }
 
-// One bounce of every path in queue d.
+// Guide inputs of queue d: the hit point, the shading normal facing the
+// incoming ray and the direction toward the previous vertex (misses and
+// faces without a shader get a placeholder row the shade kernel ignores).
+__global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
+  const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
+  const float* q = b.qray[d & 1];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    V3 P = v3(b.glo[0], b.glo[1], b.glo[2]), N = v3(0, 0, 1), wi = v3(0, 0, 1);
+    const int32_t prim = b.hprim[i];
+    if (prim >= 0) {
+      Ctx sc;
+      uint32_t shid = 0;
+      if (hit_attributes(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], sc, shid)) {
+        wi = v3(-q[3 * (size_t)b.cap + i], -q[4 * (size_t)b.cap + i], -q[5 * (size_t)b.cap + i]);
+        P = sc.P;
+        N = dot(sc.Ng, wi) > 0.0f ? sc.N : v3(-sc.N.x, -sc.N.y, -sc.N.z);
+      }
+    }
+    float* g = b.grow;
+    const size_t c = b.cap;
+    g[i] = P.x; g[c + i] = P.y; g[2 * c + i] = P.z;
+    g[3 * c + i] = N.x; g[4 * c + i] = N.y; g[5 * c + i] = N.z;
+    g[6 * c + i] = wi.x; g[7 * c + i] = wi.y; g[8 * c + i] = wi.z;
+  }
+}
+
+// One bounce of every path in queue d.  GUIDED: one-sample MIS of the guide
+// (probability alpha) and the BSDF at non-mirror vertices; TRAIN: training
+// records of the guided continuations.
+template <bool GUIDED, bool TRAIN>
 __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
   const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
   const float* q = b.qray[d & 1];
@@ -269,12 +376,24 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
     float so[3] = {0, 0, 0}, no[3] = {0, 0, 0};
     V3 sd = v3(0, 0, 0), nd = v3(0, 0, 0), sc3 = v3(0, 0, 0);
     float stmax = 0.f, time = 0.f;
+    bool want_rec = false;
+    V3 rP = v3(0, 0, 0), rN = v3(0, 0, 0), rWi = v3(0, 0, 0);
+    float rQ = 0.f;
     if (active) {
       p = qp[i];
       const V3 D = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
       time = q[7 * (size_t)b.cap + i];
       V3 beta = v3(b.bx[p], b.by[p], b.bz[p]);
       V3 L = v3(b.lx[p], b.ly[p], b.lz[p]);
+      if (TRAIN) {  // the radiance before this vertex closes the previous record
+        const uint32_t lr = b.last_rec[p];
+        if (lr != 0xffffffffu) {
+          b.rec[(size_t)(kRMark + 0) * b.rcap + lr] = L.x;
+          b.rec[(size_t)(kRMark + 1) * b.rcap + lr] = L.y;
+          b.rec[(size_t)(kRMark + 2) * b.rcap + lr] = L.z;
+          b.last_rec[p] = 0xffffffffu;
+        }
+      }
       const float pdf_prev = b.pdf[p];
       const uint64_t key = b.key[p];
       const int32_t prim = b.hprim[i];
@@ -321,6 +440,9 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
             const V3 wil = project(Ut, Vt, sc.N, wi);
             const uint32_t base = 8 * d;
             const int nL = (int)b.nl;
+            const bool guided = GUIDED && (m.dw > 0.0f || !m.mirror);
+            GMix gm;
+            if (guided) gmix_decode(b.gout + i * 40, gm);
             // ---- next-event estimation
             if (nL > 0 && (m.dw > 0.0f || !m.mirror)) {
               const float u = rnd(key, base + 0);
@@ -358,7 +480,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
               if (ok && dot(Ld, sc.Ng) > 0.0f && dot(Ld, sc.N) > 0.0f && pl > 0.0f && !isinf(pl)) {
                 const V3 wol = project(Ut, Vt, sc.N, Ld);
                 const V3 f = bsdf_f(m, wil, wol);
-                const float pb = bsdf_pdf_pt(m, wil, wol);
+                float pb = bsdf_pdf_pt(m, wil, wol);
+                if (guided) pb = b.alpha * gmix_pdf(gm, Ld) + (1.0f - b.alpha) * pb;
                 const float w = power_w(pl, pb);
                 const float k = w / pl;
                 const V3 c = v3(beta.x * f.x * l.Le[0] * k, beta.y * f.y * l.Le[1] * k, beta.z * f.z * l.Le[2] * k);
@@ -378,12 +501,16 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
                 }
               }
             }
-            // ---- BSDF sample
+            // ---- continuation: the guide (probability alpha) or the BSDF
             const float ul = rnd(key, base + 3);
             const double r0 = (double)rnd(key, base + 4), r1 = (double)rnd(key, base + 5);
-            V3 wol;
+            V3 wol, wo;
             bool delta = false;
-            if (ul < m.dw) {  // CosineHemisphere (math/sample/sample.go:18-27)
+            const bool from_guide = guided && rnd(key, base + 7) < b.alpha;
+            if (from_guide) {
+              wo = gmix_sample(gm, ul, (float)r0, (float)r1);
+              wol = project(Ut, Vt, sc.N, wo);
+            } else if (ul < m.dw) {  // CosineHemisphere (math/sample/sample.go:18-27)
               const double r = sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
               wol = v3((float)(r * cos(th)), (float)(r * sin(th)), (float)sqrt(r0));
             } else if (m.mirror) {
@@ -396,16 +523,21 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
               const V3 mh = v3(st * gcos((float)phiM), st * gsin((float)phiM), ct);
               wol = normalize(sub(scale(2 * fabsf(dot(mh, wil)), mh), wil));
             }
-            const V3 wo = expand(Ut, Vt, sc.N, wol);
+            if (!from_guide) wo = expand(Ut, Vt, sc.N, wol);
             if (dot(wo, sc.Ng) > 0.0f) {
               bool alive = true;
               float pb = 0.0f;
               if (delta) {
                 const RGB F = fresnel_kr(m.fr, wil.z);
                 beta = v3(beta.x * (m.cs.x * F.c[0]), beta.y * (m.cs.y * F.c[1]), beta.z * (m.cs.z * F.c[2]));
+                if (guided) {  // the mirror lobe is taken with probability (1-alpha)*sw
+                  const float inv = 1.0f / (1.0f - b.alpha);
+                  beta = v3(beta.x * inv, beta.y * inv, beta.z * inv);
+                }
               } else {
                 const V3 f = bsdf_f(m, wil, wol);
                 pb = bsdf_pdf_pt(m, wil, wol);
+                if (guided) pb = b.alpha * gmix_pdf(gm, wo) + (1.0f - b.alpha) * pb;
                 if (!(pb > 0.0f)) alive = false;
                 else beta = v3(beta.x * (f.x / pb), beta.y * (f.y / pb), beta.z * (f.z / pb));
               }
@@ -422,6 +554,13 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
                 nd = wo;
                 b.pdf[p] = delta ? 0.0f : pb;
                 cont = true;
+                if (TRAIN && guided && !delta) {
+                  want_rec = true;
+                  rP = sc.P;
+                  rN = sc.N;
+                  rWi = wi;
+                  rQ = pb;
+                }
               }
             }
           }
@@ -447,7 +586,51 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
       put_ray(nq, b.cap, ni, no, nd, __int_as_float(0x7f800000), time);
       nqp[ni] = p;
     }
+    if (TRAIN) {
+      const unsigned long long ri = warp_append(&b.rcount[0], want_rec);
+      if (want_rec && ri < b.rcap) {
+        float* R = b.rec;
+        const size_t c = b.rcap;
+        const float v[20] = {rP.x, rP.y, rP.z, rN.x, rN.y, rN.z, rWi.x, rWi.y, rWi.z, nd.x, nd.y, nd.z, 0.f, rQ,
+                             b.bx[p], b.by[p], b.bz[p], 0.f, 0.f, 0.f};
+        for (int k = 0; k < 20; ++k) R[(size_t)k * c + ri] = v[k];
+        R[(size_t)kRPath * c + ri] = __uint_as_float(p);
+        b.last_rec[p] = (uint32_t)ri;
+      }
+    }
   }
+}
+
+// Training weights: incident radiance along the sampled direction,
+// (L_final - L_mark) / beta per channel, as luminance over the density it
+// was sampled with (clamped to 1e4).
+__global__ void __launch_bounds__(kPtBlock) k_pt_targets(PtBatch b) {
+  const uint64_t n = b.rcount[0] < b.rcap ? b.rcount[0] : b.rcap;
+  const size_t c = b.rcap;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = __float_as_uint(b.rec[(size_t)kRPath * c + i]);
+    const float Lf[3] = {b.lx[p], b.ly[p], b.lz[p]};
+    float lin[3];
+    for (int k = 0; k < 3; ++k) {
+      const float bt = b.rec[(size_t)(kRBeta + k) * c + i];
+      const float v = bt > 0.f ? (Lf[k] - b.rec[(size_t)(kRMark + k) * c + i]) / bt : 0.f;
+      lin[k] = v > 0.f ? v : 0.f;
+    }
+    const float lum = 0.2126f * lin[0] + 0.7152f * lin[1] + 0.0722f * lin[2];
+    const float q = b.rec[(size_t)kRQ * c + i];
+    float w = q > 0.f ? lum / q : 0.f;
+    w = isfinite(w) ? fminf(w, 1e4f) : 0.f;
+    b.rec[(size_t)kRW * c + i] = w;
+  }
+}
+
+// Records of training step s: [s*B, s*B + B) clipped to the batch's count.
+__global__ void k_pt_train_count(const unsigned long long* rcount, uint32_t rcap, uint64_t off, uint64_t B,
+                                 unsigned long long* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint64_t n = rcount[0] < rcap ? rcount[0] : rcap;
+  const uint64_t m = n > off ? n - off : 0;
+  *out = m < B ? m : B;
 }
 
 // Unoccluded shadow rays add their contribution, in queue order (each path
@@ -499,6 +682,7 @@ __global__ void k_pt_tally(PtBatch b) {
   b.totals[0] += r;
   b.totals[1] += s;
   *b.status = st;
+  if (b.rcount) b.rcount[1] += b.rcount[0] < b.rcap ? b.rcount[0] : b.rcap;
 }
 
 // ---------------------------------------------------- host: light table ---
@@ -535,12 +719,14 @@ int pfail(vmr_ctx* ctx, int code, const std::string& msg) {
 
 // Launches one batch's stages on the context's stream (also used while
 // capturing the graph).  Every count is read on the device.
-int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid) {
+int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool guided, bool train,
+                 const guide::GuideRows& grows) {
   cudaStream_t st = ctx->stream;
   const size_t nq = kPtMaxDepth + 2, ns = kPtMaxDepth + 1;
   PCUDA(cudaMemsetAsync(b.qlen, 0, nq * sizeof(unsigned long long), st));
   PCUDA(cudaMemsetAsync(b.slen, 0, ns * sizeof(unsigned long long), st));
   PCUDA(cudaMemsetAsync(scr, 0, sizeof(DScratch) * 2 * (b.max_depth + 1), st));
+  if (train) PCUDA(cudaMemsetAsync(b.rcount, 0, sizeof(unsigned long long), st));
   k_pt_generate<<<grid, kPtBlock, 0, st>>>(b);
   PCUDA(cudaGetLastError());
   for (uint32_t d = 0; d <= b.max_depth; ++d) {
@@ -555,7 +741,18 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid) {
     l.scratch = scr + 2 * d;
     l.stream = st;
     if (launch_trace_scene(ctx->top.dtop, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
-    k_pt_shade<<<grid, kPtBlock, 0, st>>>(b, d);
+    if (guided) {
+      k_pt_prep<<<grid, kPtBlock, 0, st>>>(b, d);
+      PCUDA(cudaGetLastError());
+      guide::GuideRows r = grows;
+      r.n_dev = &b.qlen[d];
+      if (guide::launch_infer(r, ctx->guide.wf.p, b.gout, ctx->guide.err.as<int>(), grid / 4, st) != 0)
+        return pfail(ctx, VMR_ERR_CUDA, "guide inference launch failed");
+      if (train) k_pt_shade<true, true><<<grid, kPtBlock, 0, st>>>(b, d);
+      else k_pt_shade<true, false><<<grid, kPtBlock, 0, st>>>(b, d);
+    } else {
+      k_pt_shade<false, false><<<grid, kPtBlock, 0, st>>>(b, d);
+    }
     PCUDA(cudaGetLastError());
     if (d < b.max_depth) {
       TraceLaunch s{};
@@ -575,6 +772,10 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid) {
   }
   k_pt_accumulate<<<grid, kPtBlock, 0, st>>>(b);
   PCUDA(cudaGetLastError());
+  if (train) {
+    k_pt_targets<<<grid, kPtBlock, 0, st>>>(b);
+    PCUDA(cudaGetLastError());
+  }
   k_pt_tally<<<1, 32, 0, st>>>(b);
   PCUDA(cudaGetLastError());
   return VMR_OK;
@@ -679,6 +880,28 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   if (p->iter_count > 0 && ipb > p->iter_count) ipb = p->iter_count;
   const uint64_t cap = (uint64_t)ipb * npix;
   if (cap > 0xffffffffull) return pfail(ctx, VMR_ERR_INVALID, "batch too large");
+  const bool guided = (p->flags & VMR_PATH_GUIDED) != 0;
+  const bool train = guided && (p->flags & VMR_PATH_TRAIN) != 0;
+  if (guided) {
+    const int rc = guide::ensure_ready(ctx);
+    if (rc != VMR_OK) return rc;
+    guide::prepare_kernels();
+  }
+  const float alpha = p->guide_fraction > 0.0f ? p->guide_fraction : 0.5f;
+  if (guided && !(alpha < 1.0f)) return pfail(ctx, VMR_ERR_INVALID, "guide_fraction must be below 1");
+  const uint64_t rcap = train ? std::min<uint64_t>(cap * std::max<uint32_t>(1, p->max_depth), 0xffffffffull) : 0;
+  const uint32_t tsteps = p->train_steps ? p->train_steps : 4;
+  const uint32_t tbatch = p->train_batch ? p->train_batch : 65536;
+  const float tlr = p->train_lr > 0.0f ? p->train_lr : 1e-3f;
+  // scene bounds for the guide's inputs
+  float glo[3] = {INFINITY, INFINITY, INFINITY}, ghi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t g : ctx->top.host.geom_order)
+    for (int k = 0; k < 3; ++k) {
+      glo[k] = std::min(glo[k], ctx->meshes[g]->bounds6[k]);
+      ghi[k] = std::max(ghi[k], ctx->meshes[g]->bounds6[3 + k]);
+    }
+  for (int k = 0; k < 3; ++k)
+    if (!(ghi[k] > glo[k])) ghi[k] = glo[k] + 1.0f;
   // One device block, carved.
   size_t bytes = 0;
   auto carve = [&](size_t nb) { size_t o = bytes; bytes += (nb + 255) / 256 * 256; return o; };
@@ -690,7 +913,9 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
                o_fb64 = carve(p->fb64 ? (size_t)npix * 3 * 8 : 0), o_mesh = carve(rm.size() * sizeof(RMesh)),
                o_light = carve(std::max<size_t>(1, lights.size()) * sizeof(PtLight)),
                o_shader = carve(std::max<size_t>(1, R.shaders.size()) * sizeof(vmr_shader_std)),
-               o_log = carve(log.size() * 4);
+               o_log = carve(log.size() * 4), o_grow = carve(guided ? cap * 9 * 4 : 0),
+               o_gout = carve(guided ? cap * 40 * 4 : 0), o_rec = carve(rcap * kRecCols * 4),
+               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32);
   PCUDA(R.ptbuf.ensure(bytes));
   char* base = R.ptbuf.as<char>();
   uint64_t fwd[52], inv[52];
@@ -754,6 +979,22 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   b.fb64 = p->fb64 ? reinterpret_cast<double*>(base + o_fb64) : nullptr;
   DScratch* scr = reinterpret_cast<DScratch*>(base + o_scr);
   b.scr = scr;
+  b.alpha = alpha;
+  std::memcpy(b.glo, glo, 12);
+  b.grow = guided ? reinterpret_cast<float*>(base + o_grow) : nullptr;
+  b.gout = guided ? reinterpret_cast<float*>(base + o_gout) : nullptr;
+  b.rec = train ? reinterpret_cast<float*>(base + o_rec) : nullptr;
+  b.rcap = (uint32_t)rcap;
+  b.rcount = train ? reinterpret_cast<unsigned long long*>(base + o_rcnt) : nullptr;
+  b.last_rec = train ? reinterpret_cast<uint32_t*>(base + o_last) : nullptr;
+  if (train) PCUDA(cudaMemsetAsync(b.rcount, 0, 32, st));
+  guide::GuideRows grows{};
+  if (guided) {
+    const float* g = b.grow;
+    grows = guide::GuideRows{g, g + cap, g + 2 * cap, g + 3 * cap, g + 4 * cap, g + 5 * cap, g + 6 * cap,
+                             g + 7 * cap, g + 8 * cap, cap, nullptr, {glo[0], glo[1], glo[2]},
+                             {1.0f / (ghi[0] - glo[0]), 1.0f / (ghi[1] - glo[1]), 1.0f / (ghi[2] - glo[2])}};
+  }
   PCUDA(cudaMemsetAsync(b.totals, 0, 24, st));
   PCUDA(cudaMemsetAsync(scr, 0, sizeof(DScratch) * 2 * (kPtMaxDepth + 1), st));
   int sms = 0;
@@ -781,7 +1022,8 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   const bool use_graph = !(p->flags & VMR_PATH_NO_GRAPH);
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)base, bytes, cap, npix, p->width, p->height, nl, p->max_depth,
                                p->rr_depth, p->seed, (uint64_t)(p->fb64 != nullptr), (uint64_t)(uintptr_t)st,
-                               (uint64_t)(uintptr_t)ctx->top.nodes.p, (uint64_t)grid};
+                               (uint64_t)(uintptr_t)ctx->top.nodes.p, (uint64_t)grid, (uint64_t)guided,
+                               (uint64_t)train, (uint64_t)(uintptr_t)ctx->guide.wf.p, rcap};
   {
     uint64_t h = 1469598103934665603ull;
     auto fold = [&](const void* d, size_t nb) {
@@ -792,9 +1034,12 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     fold(b.env, sizeof(b.env));
     fold(&b.sel, sizeof(b.sel));
     fold(&ctx->top.dtop, sizeof(ctx->top.dtop));
+    fold(&b.alpha, sizeof(b.alpha));
+    fold(b.glo, sizeof(b.glo));
+    fold(grows.inv_ext, sizeof(grows.inv_ext));
     key.push_back(h);
   }
-  uint32_t replays = 0;
+  uint32_t replays = 0, tsteps_done = 0;
   if (use_graph && nbatch > 0 && !(R.graph.exec && R.graph.key == key)) {
     if (R.graph.exec) {
       cudaGraphExecDestroy(R.graph.exec);
@@ -802,7 +1047,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     }
     cudaGraph_t g = nullptr;
     PCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-    const int rc = launch_batch(ctx, b, scr, grid);
+    const int rc = launch_batch(ctx, b, scr, grid, guided, train, grows);
     const cudaError_t ec = cudaStreamEndCapture(st, &g);
     if (rc != VMR_OK) {
       if (g) cudaGraphDestroy(g);
@@ -821,8 +1066,47 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
       PCUDA(cudaGraphLaunch(R.graph.exec, st));
       ++replays;
     } else {
-      const int rc = launch_batch(ctx, b, scr, grid);
+      const int rc = launch_batch(ctx, b, scr, grid, guided, train, grows);
       if (rc != VMR_OK) return rc;
+    }
+    if (train) {  // online training on this batch's records (device counts)
+      auto& G = ctx->guide;
+      const uint32_t stride = (tbatch + 127) / 128 * 128;
+      if (G.save_rows < stride) {
+        PCUDA(G.save.ensure((size_t)guide::kSaveRows * stride * 2));
+        G.save_rows = stride;
+      }
+      unsigned long long* ncount = b.rcount + 2;
+      for (uint32_t s = 0; s < tsteps; ++s) {
+        const uint64_t off = (uint64_t)s * tbatch;
+        k_pt_train_count<<<1, 32, 0, st>>>(b.rcount, b.rcap, off, tbatch, ncount);
+        PCUDA(cudaGetLastError());
+        guide::GuideTrain tr{};
+        tr.rows = grows;
+        const float* R = b.rec;
+        const size_t c = b.rcap;
+        tr.rows.px = R + kRP * c + off; tr.rows.py = R + (kRP + 1) * c + off; tr.rows.pz = R + (kRP + 2) * c + off;
+        tr.rows.nx = R + kRN * c + off; tr.rows.ny = R + (kRN + 1) * c + off; tr.rows.nz = R + (kRN + 2) * c + off;
+        tr.rows.wx = R + kRWo * c + off; tr.rows.wy = R + (kRWo + 1) * c + off; tr.rows.wz = R + (kRWo + 2) * c + off;
+        tr.rows.n = tbatch;
+        tr.rows.n_dev = ncount;
+        tr.ox = R + kROm * c + off; tr.oy = R + (kROm + 1) * c + off; tr.oz = R + (kROm + 2) * c + off;
+        tr.weight = R + kRW * c + off;
+        tr.stride = stride;
+        if (off >= rcap) break;
+        PCUDA(cudaMemsetAsync(G.sums.p, 0, 16, st));
+        const int tgrid = std::min<int>(grid / 4, (int)((tbatch + 127) / 128));
+        if (guide::launch_train(tr, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), tgrid, st) != 0)
+          return pfail(ctx, VMR_ERR_CUDA, "guide training launch failed");
+        if (guide::launch_wgrad(G.save.p, stride, tbatch, ncount, G.grad.as<float>(), G.err.as<int>(),
+                                std::max(1, std::min(sms, (int)((tbatch + 127) / 128))), st) != 0)
+          return pfail(ctx, VMR_ERR_CUDA, "guide weight-gradient launch failed");
+        guide::GuideAdam a{tlr, 0.9f, 0.999f, 1e-8f, ++G.step};
+        if (guide::launch_adam(G.W.as<float>(), G.m.as<float>(), G.v.as<float>(), G.grad.as<float>(),
+                               G.sums.as<float>(), a, G.wf.p, G.wb.p, st) != 0)
+          return pfail(ctx, VMR_ERR_CUDA, "guide Adam launch failed");
+        ++tsteps_done;
+      }
     }
   }
   PCUDA(cudaEventRecord(ctx->ev1, st));
@@ -830,16 +1114,30 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   if (p->fb64) PCUDA(cudaMemcpyAsync(p->fb64, b.fb64, (size_t)npix * 3 * 8, cudaMemcpyDeviceToHost, st));
   unsigned long long tot[2] = {0, 0};
   PCUDA(cudaMemcpyAsync(tot, b.totals, 16, cudaMemcpyDeviceToHost, st));
-  int status = 0;
+  int status = 0, gerr = 0;
   PCUDA(cudaMemcpyAsync(&status, b.status, 4, cudaMemcpyDeviceToHost, st));
+  unsigned long long recs[2] = {0, 0};
+  float gsums[2] = {0.f, 0.f};
+  if (train) {
+    PCUDA(cudaMemcpyAsync(recs, b.rcount, 16, cudaMemcpyDeviceToHost, st));
+    PCUDA(cudaMemcpyAsync(gsums, ctx->guide.sums.p, 8, cudaMemcpyDeviceToHost, st));
+  }
+  if (guided) PCUDA(cudaMemcpyAsync(&gerr, ctx->guide.err.p, 4, cudaMemcpyDeviceToHost, st));
   PCUDA(cudaStreamSynchronize(st));
   if (status == kStatusStackOverflow) return pfail(ctx, VMR_ERR_STACK_OVERFLOW, "traversal stack overflow");
   if (status != kStatusOk) return pfail(ctx, VMR_ERR_TIMEOUT, "traversal iteration cap");
+  if (gerr) {
+    cudaMemsetAsync(ctx->guide.err.p, 0, 4, st);
+    return pfail(ctx, VMR_ERR_TIMEOUT, "a guide kernel's tensor-core wait ran out");
+  }
   if (stats) {
     stats->samples = (uint64_t)npix * p->iter_count;
     stats->rays = tot[0];
     stats->shadow_rays = tot[1];
     stats->graph_replays = replays;
+    stats->train_records = recs[1];
+    stats->train_steps = tsteps_done;
+    stats->train_loss = gsums[1] > 0.f ? gsums[0] / gsums[1] : 0.f;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     stats->ms = ms;

@@ -353,3 +353,58 @@ def small_room_ext(n_tris: int = 4096, seed: int = 1, env=(0.2, 0.25, 0.3)) -> d
     sc["quad_lights"] = [dict(p0=p0, e1=e1, e2=e2, shader=light_shader, mesh=len(sc["meshes"]) - 1)]
     sc["env"] = tuple(env)
     return sc
+
+
+def _box_faces(lo, hi, skip=()):
+    """Triangles of the faces of an axis-aligned box (names: x0 x1 y0 y1 z0
+    z1 for the faces at lo/hi of each axis), wound so normals point inward."""
+    (x0, y0, z0), (x1, y1, z1) = lo, hi
+    faces = {
+        "y0": [(x0, y0, z0), (x0, y0, z1), (x1, y0, z1), (x1, y0, z0)],
+        "y1": [(x0, y1, z0), (x1, y1, z0), (x1, y1, z1), (x0, y1, z1)],
+        "z0": [(x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0)],
+        "z1": [(x0, y0, z1), (x0, y1, z1), (x1, y1, z1), (x1, y0, z1)],
+        "x0": [(x0, y0, z0), (x0, y1, z0), (x0, y1, z1), (x0, y0, z1)],
+        "x1": [(x1, y0, z0), (x1, y0, z1), (x1, y1, z1), (x1, y1, z0)],
+    }
+    tris = []
+    for name, (a, b, c, d) in faces.items():
+        if name in skip:
+            continue
+        tris += [a, b, c, a, c, d]
+    return tris
+
+
+def slit_room(n_tris: int = 200_000, seed: int = 5, width: int = 1024, height: int = 1024) -> dict:
+    """The path-guiding configuration: a 4 x 3 x 3 room (x in [-2, 2], y in
+    [0, 3], z in [0, 3]) whose only light, a quad of radiance 200 facing the
+    room, sits in a 0.4-deep chamber behind the x = 2 wall; the wall is cut
+    by a horizontal slit 0.06 high across its whole depth (2% of its area),
+    the only way the light reaches the room.  n_tris random diffuse
+    triangles (centroids uniform in the room's interior, vertices at
+    centroid + 0.03 x a direction on the sphere), every surface Lambert with
+    albedo 0.7, pinhole camera inside the room at the image's aspect."""
+    f = np.float32
+    tris = _box_faces((-2.0, 0.0, 0.0), (2.0, 3.0, 3.0), skip=("x1",))
+    # the x = 2 wall below and above the slit (normals toward -x)
+    for ya, yb in ((0.0, 2.0), (2.06, 3.0)):
+        tris += [(2.0, ya, 0.0), (2.0, ya, 3.0), (2.0, yb, 3.0), (2.0, ya, 0.0), (2.0, yb, 3.0), (2.0, yb, 0.0)]
+    # the light chamber (open toward the room)
+    tris += _box_faces((2.0, 0.0, 0.0), (2.4, 3.0, 3.0), skip=("x0",))
+    room = np.asarray(tris, f)
+    sv, sidx = triangle_soup(n_tris, seed, lo=0.0, hi=1.0, edge=0.03)
+    c = np.asarray([[-1.8, 0.2, 0.3]], f)
+    e = np.asarray([[3.6, 2.6, 2.5]], f)
+    sv = (c + sv * e).astype(f)  # centroids spread over the interior box
+    shaders = [dict(diffuse_colour=(0.7, 0.7, 0.7), diffuse_strength=1.0, diffuse_roughness=0.0),
+               dict(emission_colour=(1.0, 1.0, 1.0), emission_strength=200.0, diffuse_colour=(0.0, 0.0, 0.0),
+                    diffuse_strength=1.0, diffuse_roughness=0.0)]
+    p0, e1, e2 = (2.35, 0.5, 2.5), (0.0, 2.0, 0.0), (0.0, 0.0, -2.0)
+    lv, li = quad_light_mesh(p0, e1, e2)
+    meshes = [dict(verts=room, idxp=np.arange(room.shape[0], dtype=np.uint32), shaders=[0]),
+              dict(verts=sv, idxp=sidx, shaders=[0]),
+              dict(verts=lv, idxp=li, shaders=[1])]
+    quads = [dict(p0=p0, e1=e1, e2=e2, shader=1, mesh=2)]
+    cam = lookat_camera((-1.2, 1.4, 0.15), (1.0, 1.3, 2.2), (0.0, 1.0, 0.0), 70.0, width / height)
+    return dict(meshes=meshes, shaders=shaders, lights=[], quad_lights=quads, env=(0.0, 0.0, 0.0), camera=cam,
+                width=width, height=height)
