@@ -602,8 +602,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
 }
 
 // Training weights: incident radiance along the sampled direction,
-// (L_final - L_mark) / beta per channel, as luminance over the density it
-// was sampled with (clamped to 1e4).
+// (L_final - L_mark) / beta per channel, as luminance, times |cos| with the
+// shading normal, over the density it was sampled with (clamped to 1e4).
 __global__ void __launch_bounds__(kPtBlock) k_pt_targets(PtBatch b) {
   const uint64_t n = b.rcount[0] < b.rcap ? b.rcount[0] : b.rcap;
   const size_t c = b.rcap;
@@ -618,7 +618,11 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_targets(PtBatch b) {
     }
     const float lum = 0.2126f * lin[0] + 0.7152f * lin[1] + 0.0722f * lin[2];
     const float q = b.rec[(size_t)kRQ * c + i];
-    float w = q > 0.f ? lum / q : 0.f;
+    // the product the vertex integrates: incident radiance x |cos| with the normal
+    const float cs = fabsf(b.rec[(size_t)kRN * c + i] * b.rec[(size_t)kROm * c + i] +
+                           b.rec[(size_t)(kRN + 1) * c + i] * b.rec[(size_t)(kROm + 1) * c + i] +
+                           b.rec[(size_t)(kRN + 2) * c + i] * b.rec[(size_t)(kROm + 2) * c + i]);
+    float w = q > 0.f ? lum * cs / q : 0.f;
     w = isfinite(w) ? fminf(w, 1e4f) : 0.f;
     b.rec[(size_t)kRW * c + i] = w;
   }
