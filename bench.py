@@ -298,12 +298,99 @@ def run_gpu(args):
         line["cpu_baseline"] = {"value": round(cval, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
                                 "sample": f"{sample} of the {N_RAYS} incoherent rays ({cdt:.1f} s), "
                                           "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"}
+    if rank == 0 and not args.no_render:
+        line["render"] = render_extras(ctx, args)
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def _relmse(a, ref):
+    return float(np.mean((a - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def render_extras(ctx, args):
+    """The render configurations, measured on the same GPU after the
+    headline (each on its own seeded synthetic scene):
+      reference_small_room   reference-mode core.Render (direct light, hero
+                             wavelength), 256x256 x 16 iterations, bit-parity
+                             with the oracle on a 64x64 sample, and the oracle's
+                             C++ restatement of the Go renderer timed on the
+                             host cores
+      extended_sphere_grid   the extended path tracer on the 2,097,152-triangle
+                             sphere grid, 1920x1080, depth 8 (16 of the
+                             configuration's 64 spp timed)
+      guided_slit            equal-wall-time relMSE on the slit-light room
+                             against a 4096-spp float64 plain render, at
+                             256x256 instead of 1024x1024 so that the reference
+                             render fits the benchmark's time"""
+    from oracle import orc
+    from vermeer_gb300 import scenes
+    out = {}
+    # reference mode, small room
+    sc = scenes.small_room(16384, seed=1)
+    ctx.load_scene(sc)
+    ctx.render(256, 256, 0, 2, 7)
+    fb, st = ctx.render(256, 256, 0, 16, 7)
+    r = orc.Render(sc)
+    ref = r.run(64, 64, 0, 2, 7)
+    got, _ = ctx.render(64, 64, 0, 2, 7)
+    threads = cpu_threads()
+    t0 = time.perf_counter()
+    r.run(128, 128, 0, 4, 7, nthreads=threads)
+    cdt = time.perf_counter() - t0
+    out["reference_small_room"] = {
+        "workload": "small room, 16,384-triangle soup + 10-triangle box, 2 TriLights, 256x256, 16 iterations",
+        "samples_per_s": round(256 * 256 * 16 / (st["ms"] / 1e3), 1), "device_ms": round(st["ms"], 3),
+        "camera_rays": st["camera_rays"], "shadow_rays": st["shadow_rays"],
+        "bit_equal_to_oracle_frac": float((got.view(np.uint32) == ref.view(np.uint32)).all(-1).mean()),
+        "cpu_baseline": {"samples_per_s": round(128 * 128 * 4 / cdt, 1), "cores": threads, "kind": "port",
+                         "sample": "128x128 x 4 iterations, oracle/orc_render.cpp (C++ restatement of core.Render)"}}
+    # extended mode, sphere grid
+    sc = scenes.sphere_grid()
+    ctx.load_scene(sc)
+    W, H = sc["width"], sc["height"]
+    ctx.render_path(W, H, 0, 2, 3, max_depth=8)
+    fb, st = ctx.render_path(W, H, 0, 16, 3, max_depth=8)
+    out["extended_sphere_grid"] = {
+        "workload": "16x16 displaced spheres x 8,192 tris + ground, 4 quad lights + environment, 1920x1080, "
+                    "depth 8, RR from 3, 16 spp",
+        "samples_per_s": round(W * H * 16 / (st["ms"] / 1e3), 1),
+        "mrays_per_s": round((st["rays"] + st["shadow_rays"]) / (st["ms"] / 1e3) / 1e6, 2),
+        "device_ms": round(st["ms"], 3), "rays": st["rays"], "shadow_rays": st["shadow_rays"],
+        "graph_replays": st["graph_replays"]}
+    # guided vs plain, equal wall time
+    W = H = 256
+    sc = scenes.slit_room(200_000, width=W, height=H)
+    ctx.load_scene(sc)
+    ref = np.zeros((H, W, 3), np.float64)
+    for k in range(16):
+        ctx.render_path(W, H, 256 * k, 256, 99, max_depth=8, fb64=ref)
+    ctx.render_path(W, H, 0, 4, 1, max_depth=8)
+    t0 = time.perf_counter()
+    plain, _ = ctx.render_path(W, H, 0, 512, 1, max_depth=8)
+    tp = time.perf_counter() - t0
+    ctx.guide_init(7)
+    g = np.zeros((H, W, 3), np.float32)
+    spp = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < tp:
+        train = time.perf_counter() - t0 < 0.3 * tp
+        g, gst = ctx.render_path(W, H, spp, 8, 1, max_depth=8, fb=g, guided=True, train=train, guide_fraction=0.5,
+                                 train_steps=16, train_batch=65536, train_lr=3e-3)
+        spp += 8
+    tg = time.perf_counter() - t0
+    out["guided_slit"] = {
+        "workload": "slit-light room, 200,000 diffuse triangles, 256x256, depth 8; plain 512 spp vs guided "
+                    "(online training for the first 30% of the time, 16 Adam steps of 65,536 records per 8-spp "
+                    "batch) for the same wall time",
+        "plain": {"spp": 512, "wall_s": round(tp, 4), "relmse": round(_relmse(plain, ref), 5)},
+        "guided": {"spp": spp, "wall_s": round(tg, 4), "relmse": round(_relmse(g, ref), 5)},
+        "reference_spp": 4096}
+    return out
 
 
 def measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world):
@@ -349,6 +436,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-render", action="store_true", help="skip the render configurations")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling runs use fewer)")
     args = ap.parse_args()
     if args.warmup < 3:
