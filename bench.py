@@ -323,6 +323,9 @@ def render_extras(ctx, args):
       extended_sphere_grid   the extended path tracer on the 2,097,152-triangle
                              sphere grid, 1920x1080, depth 8 (16 of the
                              configuration's 64 spp timed)
+      batched_jobs           64 uneven static/motion jobs traced in one launch,
+                             against one launch per job (default and
+                             autotuned launch parameters)
       guided_slit            equal-wall-time relMSE on the slit-light room
                              against a 4096-spp float64 plain render, at
                              256x256 instead of 1024x1024 so that the reference
@@ -362,6 +365,52 @@ def render_extras(ctx, args):
         "mrays_per_s": round((st["rays"] + st["shadow_rays"]) / (st["ms"] / 1e3) / 1e6, 2),
         "device_ms": round(st["ms"], 3), "rays": st["rays"], "shadow_rays": st["shadow_rays"],
         "graph_replays": st["graph_replays"]}
+    # batched uneven jobs: one launch vs one launch per job
+    import torch
+    rng_sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)
+    cam = scenes.coherent_rays(256)
+    jobs = []
+    for j, nt in enumerate(rng_sizes):
+        motion = j % 2 == 1
+        if motion:
+            v, ip = scenes.motion_soup(int(nt), 400 + j, velocity=0.05)
+        else:
+            v, ip = scenes.triangle_soup(int(nt), 400 + j)
+        g = ctx.mesh_build(v, ip, keys=2 if motion else 1, motion_mode=1)
+        rays = cam.copy()
+        rays[:, 7] = scenes.uniform(500 + j, rays.shape[0], 7).astype(np.float32) if motion else 0.0
+        jobs.append((g, torch.from_numpy(np.ascontiguousarray(rays.T)).cuda()))
+    nrays = sum(r.shape[1] for _, r in jobs)
+    ctx.trace_jobs(jobs)
+    _, jst = ctx.trace_jobs(jobs)
+
+    def per_job_ms():
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(torch.cuda.current_stream())
+        for g, r in jobs:
+            ctx.trace_mesh(g, r)
+        b.record(torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+    per_job_ms()
+    seq_default = per_job_ms()
+    t0 = time.perf_counter()
+    for g, r in jobs:
+        ctx.autotune(g, r)
+    tune_s = time.perf_counter() - t0
+    seq_tuned = per_job_ms()
+    for g, _ in jobs:
+        ctx.clear_tuning(g)
+    out["batched_jobs"] = {
+        "workload": "64 triangle soups, sizes log-uniform in [1k, 200k] (seed 4), every other one with two-key "
+                    "linear motion (velocity in a 0.05 ball), 256x256 camera rays each (times uniform in [0, 1) "
+                    "for the motion jobs), closest hit",
+        "triangles": int(rng_sizes.sum()), "rays": int(nrays),
+        "one_launch_mrays_per_s": round(nrays / (jst["kernel_ms"] / 1e3) / 1e6, 2),
+        "per_job_launches_mrays_per_s": round(nrays / (seq_default / 1e3) / 1e6, 2),
+        "per_job_autotuned_mrays_per_s": round(nrays / (seq_tuned / 1e3) / 1e6, 2),
+        "autotune_s": round(tune_s, 2)}
     # guided vs plain, equal wall time
     W = H = 256
     sc = scenes.slit_room(200_000, width=W, height=H)

@@ -74,6 +74,8 @@ typedef struct {
     int walk_tail;       /* while-while: end a node walk early once at most
                             this many lanes still walk and a lane holds a
                             leaf, 0..31 (default 4; 0 = wait for every lane) */
+    int sort_bits;       /* sort-key width: the ray reordering groups origins
+                            in (2^b)^3 cells, b = 3, 4 or 5 (0: 4) */
 } vmr_tuning;
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* tuning);
 int vmr_get_tuning(vmr_ctx* ctx, vmr_tuning* tuning);
@@ -220,6 +222,35 @@ int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, 
 /* Traversal of the two-level scene (Scene.Trace, scene.go:30-58). */
 int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags,
                     const vmr_hits* hits, vmr_trace_stats* stats);
+
+/* Batched jobs (no reference counterpart: the reference renders one scene
+ * per process).  Each job traces n rays against one mesh, static or motion;
+ * all jobs of the call run in a single persistent launch whose warps take
+ * 32-ray chunks of any job from one work counter, so jobs of very uneven size
+ * share the GPU without one launch each.  Results equal vmr_trace_mesh per
+ * job.  Rays and hits are device pointers (the call is asynchronous unless
+ * stats is given). */
+typedef struct {
+    uint32_t geom;
+    uint32_t pad;
+    size_t n;
+    vmr_rays rays;
+    vmr_hits hits;
+} vmr_trace_job;
+int vmr_trace_jobs(vmr_ctx* ctx, const vmr_trace_job* jobs, uint32_t n_jobs, int flags, vmr_trace_stats* stats);
+
+/* The autotuner: times every candidate launch configuration (kernel variant,
+ * block size, resident blocks, walk-tail cutoff, sort-key width) on a sample
+ * of rays for one mesh, keeps the fastest for that mesh (vmr_trace_mesh uses
+ * it from then on instead of the context's tuning) and
+ * returns it.  rays: host pointers, or device pointers with
+ * VMR_TRACE_DEVICE in flags; the sample should be a few hundred thousand
+ * rays of the kind the mesh will see.  best_ms (may be NULL) receives the
+ * winner's traversal time; n_tried (may be NULL) the candidates timed. */
+int vmr_autotune(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags, vmr_tuning* best,
+                 float* best_ms, uint32_t* n_tried);
+/* Forget a mesh's own tuning (it falls back to the context's). */
+int vmr_clear_tuning(vmr_ctx* ctx, uint32_t geom);
 
 /* ----------------------------------------------------------------- render */
 /* ShaderStd parameters (builtin/shader/std.go:25-47).  The reference leaves

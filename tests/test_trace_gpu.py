@@ -139,10 +139,12 @@ def test_full_size_soup_parity(ctx, orc):
 
 
 @pytest.mark.parametrize("tuning", [(0, 0, 0, 0), (1, 0, 0, 0), (3, 0, 0, 0), (5, 0, 0, 0), (8, 0, 0, 4),
-                                    (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0), (13, 0, 0, 0, 4), (9, 0, 0, 0, 12)])
+                                    (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0), (13, 0, 0, 0, 4), (9, 0, 0, 0, 12),
+                                    (13, 0, 0, 0, 4, 3), (13, 0, 0, 0, 4, 5), (8, 256, 0, 4, 4, 5)])
 def test_every_tuning_is_bit_exact(ctx, orc, tuning):
-    """Launch parameters (kernel variant, ray reordering, block size,
-    resident blocks) only change scheduling: hits stay bit-exact."""
+    """Launch parameters (kernel variant, ray reordering and its key width,
+    block size, resident blocks) only change scheduling: hits stay
+    bit-exact."""
     v, ip = scenes.triangle_soup(100000, 17, edge=0.006)
     rays = scenes.incoherent_rays(150000, 18)
     geom = ctx.mesh_build(v, ip)

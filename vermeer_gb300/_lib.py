@@ -45,7 +45,11 @@ class Hits(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("kernel", ctypes.c_int), ("block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("refill_min", ctypes.c_int), ("walk_tail", ctypes.c_int)]
+                ("refill_min", ctypes.c_int), ("walk_tail", ctypes.c_int), ("sort_bits", ctypes.c_int)]
+
+
+class TraceJob(ctypes.Structure):
+    _fields_ = [("geom", U32), ("pad", U32), ("n", ctypes.c_size_t), ("rays", Rays), ("hits", Hits)]
 
 
 class TraceStats(ctypes.Structure):
@@ -155,6 +159,10 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_float)]),
     "vmr_guide_train_step": (ctypes.c_int, [P, P, P, P, P, P, ctypes.c_size_t, P, P, ctypes.POINTER(Adam),
                                             ctypes.POINTER(ctypes.c_float)]),
+    "vmr_autotune": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
+                                    ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(U32)]),
+    "vmr_clear_tuning": (ctypes.c_int, [P, U32]),
+    "vmr_trace_jobs": (ctypes.c_int, [P, P, U32, ctypes.c_int, ctypes.POINTER(TraceStats)]),
     "vmr_trace_mesh_noalloc": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                               ctypes.POINTER(Hits)]),
 }

@@ -75,10 +75,54 @@ class Context:
         self._check(self.L.vmr_sync(self.h))
 
     def set_tuning(self, kernel: int = 13, block: int = 0, blocks_per_sm: int = 0, refill_min: int = 0,
-                   walk_tail: int = 4):
+                   walk_tail: int = 4, sort_bits: int = 0):
         """Launch parameters of the traversal kernels (vmr_set_tuning)."""
-        t = _lib.Tuning(kernel, block, blocks_per_sm, refill_min, walk_tail)
+        t = _lib.Tuning(kernel, block, blocks_per_sm, refill_min, walk_tail, sort_bits)
         self._check(self.L.vmr_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, geom: int, rays, shadow: bool = False):
+        """vmr_autotune on a sample (numpy [n, 8] or CUDA tensor [8, n]);
+        returns (tuning dict, best_ms, candidates tried)."""
+        flags = TRACE_ANY_HIT if shadow else 0
+        if isinstance(rays, np.ndarray):
+            soa = np.ascontiguousarray(np.ascontiguousarray(rays, np.float32).reshape(-1, 8).T)
+            n = soa.shape[1]
+            r = _lib.Rays(*[_p(soa[k]) for k in range(8)])
+        else:
+            n = rays.shape[1]
+            r = _lib.Rays(*[ctypes.c_void_p(rays[k].data_ptr()) for k in range(8)])
+            flags |= TRACE_DEVICE
+        t = _lib.Tuning()
+        ms = ctypes.c_float()
+        nt = ctypes.c_uint32()
+        self._check(self.L.vmr_autotune(self.h, geom, ctypes.byref(r), n, flags, ctypes.byref(t), ctypes.byref(ms),
+                                        ctypes.byref(nt)))
+        return (dict(kernel=t.kernel, block=t.block, blocks_per_sm=t.blocks_per_sm, refill_min=t.refill_min,
+                     walk_tail=t.walk_tail, sort_bits=t.sort_bits), ms.value, nt.value)
+
+    def clear_tuning(self, geom: int):
+        self._check(self.L.vmr_clear_tuning(self.h, geom))
+
+    def trace_jobs(self, jobs, shadow: bool = False, outputs=("prim", "t", "u", "v", "w")):
+        """vmr_trace_jobs: jobs = [(geom, CUDA tensor [8, n]), ...], all in one
+        launch.  Returns (list of hit dicts, stats)."""
+        import torch
+        arr = (_lib.TraceJob * len(jobs))()
+        outs = []
+        for i, (geom, rays) in enumerate(jobs):
+            assert rays.is_cuda and rays.dtype == torch.float32 and rays.shape[0] == 8 and rays.is_contiguous()
+            n = rays.shape[1]
+            out = {k: torch.empty(n, dtype=torch.int32 if k in ("prim", "geom") else torch.float32,
+                                  device=rays.device) for k in outputs}
+            arr[i].geom = geom
+            arr[i].n = n
+            arr[i].rays = _lib.Rays(*[ctypes.c_void_p(rays[k].data_ptr()) for k in range(8)])
+            arr[i].hits = _lib.Hits(*[_p(out.get(k)) for k in ("prim", "geom", "t", "u", "v", "w")])
+            outs.append(out)
+        st = _lib.TraceStats()
+        flags = TRACE_DEVICE | (TRACE_ANY_HIT if shadow else 0)
+        self._check(self.L.vmr_trace_jobs(self.h, arr, len(jobs), flags, ctypes.byref(st)))
+        return outs, dict(rays=st.rays, kernel_ms=st.kernel_ms)
 
     def trace_timing(self):
         """(sort_ms, traverse_ms) of the last trace call (vmr_trace_timing)."""
@@ -90,7 +134,7 @@ class Context:
         t = _lib.Tuning()
         self._check(self.L.vmr_get_tuning(self.h, ctypes.byref(t)))
         return dict(kernel=t.kernel, block=t.block, blocks_per_sm=t.blocks_per_sm, refill_min=t.refill_min,
-                    walk_tail=t.walk_tail)
+                    walk_tail=t.walk_tail, sort_bits=t.sort_bits)
 
     # ------------------------------------------------------------ meshes
     def mesh_build(self, verts, idxp, keys: int = 1, ray_bias: float = 0.0, motion_mode: int = MOTION_FAITHFUL,

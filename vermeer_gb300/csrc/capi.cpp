@@ -5,6 +5,7 @@
 // batched traces with host or device buffers, and status reporting.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -240,18 +241,19 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   l.count = (flags & VMR_TRACE_COUNT) ? 1 : 0;
   l.scratch = ctx->scratch.as<DScratch>();
   l.stream = ctx->stream;
-  l.kernel = ctx->tuning.kernel;
-  l.block = ctx->tuning.block;
-  l.grid = ctx->tuning.blocks_per_sm;
-  l.refill_min = ctx->tuning.refill_min;
-  l.walk_tail = ctx->tuning.walk_tail;
+  const vmr_tuning& tn = ctx->tuning_for(mesh);
+  l.kernel = tn.kernel;
+  l.block = tn.block;
+  l.grid = tn.blocks_per_sm;
+  l.refill_min = tn.refill_min;
+  l.walk_tail = tn.walk_tail;
   VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-  if (mesh && (ctx->tuning.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
+  if (mesh && (tn.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
     // Key-ordered copy of the rays (raysort.cu); hits go back through order[].
     const size_t nf = ((n + 31) / 32) * 32;
     const int nfield = r.time ? 8 : 7;
-    const size_t bytes = nf * 4 * (2 + nfield) + sizeof(uint32_t) * vmr::kSortBuckets;
+    const size_t bytes = nf * 4 * (2 + nfield) + sizeof(uint32_t) * vmr::kSortBucketsMax;
     VMR_CUDA(ctx, ctx->sortbuf.ensure(bytes));
     uint32_t* keys = ctx->sortbuf.as<uint32_t>();
     uint32_t* order = keys + nf;
@@ -260,7 +262,8 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
     vmr::RaySoA sorted{f, f + nf, f + 2 * nf, f + 3 * nf, f + 4 * nf, f + 5 * nf, f + 6 * nf,
                        nfield == 8 ? f + 7 * nf : nullptr};
     const float* mb = ctx->mesh_bounds_of(mesh);
-    int se = vmr::launch_ray_sort(l.rays, n, mb, keys, hist, order, sorted, ctx->stream);
+    int se = vmr::launch_ray_sort(l.rays, n, mb, tn.sort_bits ? tn.sort_bits : 4, keys, hist, order, sorted,
+                                  ctx->stream);
     if (se != 0) return cuda_fail(ctx, (cudaError_t)se, "ray sort launch");
     l.rays = sorted;
     l.order = order;
@@ -386,6 +389,8 @@ int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
     return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
   if (t->blocks_per_sm < 0 || t->refill_min < 0 || t->refill_min > 32)
     return fail(ctx, VMR_ERR_INVALID, "tuning.blocks_per_sm >= 0 and refill_min in [0, 32]");
+  if (t->sort_bits != 0 && (t->sort_bits < 3 || t->sort_bits > vmr::kSortMaxBits))
+    return fail(ctx, VMR_ERR_INVALID, "tuning.sort_bits must be 0, 3, 4 or 5");
   ctx->tuning = *t;
   return VMR_OK;
 }
@@ -597,6 +602,131 @@ int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags, con
   cudaSetDevice(ctx->device);
   if (flags & VMR_TRACE_DEVICE) return run_trace(ctx, nullptr, *rays, n, flags, *hits, stats);
   return trace_host(ctx, nullptr, rays, n, flags, hits, stats);
+}
+
+
+int vmr_clear_tuning(vmr_ctx* ctx, uint32_t geom) {
+  if (!ctx || geom >= ctx->meshes.size()) return VMR_ERR_INVALID;
+  ctx->meshes[geom]->tuned = false;
+  return VMR_OK;
+}
+
+int vmr_autotune(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags, vmr_tuning* best,
+                 float* best_ms, uint32_t* n_tried) {
+  if (!ctx || !rays || !best || n == 0) return VMR_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "no such geom");
+  MeshRec& mr = *ctx->meshes[geom];
+  if (mr.host.n_tris == 0) return fail(ctx, VMR_ERR_INVALID, "empty mesh");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  // device copies of the sample and a hit buffer
+  DevBuf buf;
+  const size_t nf = (n + 63) / 64 * 64;
+  VMR_CUDA(ctx, buf.ensure(nf * 4 * 13));
+  float* f = buf.as<float>();
+  vmr_rays dr{f, f + nf, f + 2 * nf, f + 3 * nf, f + 4 * nf, f + 5 * nf, f + 6 * nf, rays->time ? f + 7 * nf : nullptr};
+  const float* src[8] = {rays->px, rays->py, rays->pz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->time};
+  const cudaMemcpyKind kind = (flags & VMR_TRACE_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  for (int k = 0; k < 8; ++k)
+    if (src[k]) VMR_CUDA(ctx, cudaMemcpyAsync(f + k * nf, src[k], n * 4, kind, st));
+  int32_t* hb = reinterpret_cast<int32_t*>(f + 8 * nf);
+  vmr_hits dh{hb, nullptr, f + 9 * nf, f + 10 * nf, f + 11 * nf, f + 12 * nf};
+  // candidates: while-while (with/without reordering, register cap, tail
+  // cutoff, key width) and the step-scheduled kernel
+  std::vector<vmr_tuning> cands;
+  for (int k : {13, 9})
+    for (int tail : {0, 2, 4, 8})
+      for (int bits : {3, 4, 5}) cands.push_back(vmr_tuning{k, 0, 0, 0, tail, bits});
+  for (int k : {5, 1})
+    for (int tail : {0, 4}) cands.push_back(vmr_tuning{k, 0, 0, 0, tail, 0});
+  for (int bits : {3, 4, 5}) cands.push_back(vmr_tuning{8, 256, 0, 4, 4, bits});
+  cands.push_back(vmr_tuning{0, 256, 0, 4, 4, 0});
+  const bool had = mr.tuned;
+  const vmr_tuning old = mr.tuning;
+  float best_t = INFINITY;
+  vmr_tuning win = ctx->tuning;
+  const int tflags = (flags & VMR_TRACE_ANY_HIT) | VMR_TRACE_DEVICE;
+  for (const vmr_tuning& c : cands) {
+    mr.tuned = true;
+    mr.tuning = c;
+    float tmin = INFINITY;
+    for (int rep = 0; rep < 3; ++rep) {
+      int rc = run_trace(ctx, &mr.dmesh, dr, n, tflags, dh, nullptr);
+      if (rc != VMR_OK) {
+        mr.tuned = had;
+        mr.tuning = old;
+        return rc;
+      }
+      VMR_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+      if (rep > 0) tmin = std::min(tmin, ms);
+    }
+    int rc = read_status(ctx, nullptr);
+    if (rc != VMR_OK) {
+      mr.tuned = had;
+      mr.tuning = old;
+      return rc;
+    }
+    if (tmin < best_t) {
+      best_t = tmin;
+      win = c;
+    }
+  }
+  mr.tuned = true;
+  mr.tuning = win;
+  *best = win;
+  if (best_ms) *best_ms = best_t;
+  if (n_tried) *n_tried = (uint32_t)cands.size();
+  return VMR_OK;
+}
+
+int vmr_trace_jobs(vmr_ctx* ctx, const vmr_trace_job* jobs, uint32_t n_jobs, int flags, vmr_trace_stats* stats) {
+  if (!ctx || (n_jobs && !jobs)) return VMR_ERR_INVALID;
+  if (ctx->device < 0) return fail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot trace");
+  if (!(flags & VMR_TRACE_DEVICE)) return fail(ctx, VMR_ERR_INVALID, "vmr_trace_jobs takes device pointers");
+  if (flags & VMR_TRACE_COUNT) return fail(ctx, VMR_ERR_UNSUPPORTED, "vmr_trace_jobs has no visit counters");
+  cudaSetDevice(ctx->device);
+  std::vector<vmr::JobDesc> t(n_jobs);
+  uint64_t chunks = 0, rays = 0;
+  for (uint32_t j = 0; j < n_jobs; ++j) {
+    const vmr_trace_job& J = jobs[j];
+    if (J.geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "job geom out of range");
+    const vmr_rays& r = J.rays;
+    const vmr_hits& h = J.hits;
+    if (J.n && (!r.px || !r.py || !r.pz || !r.dx || !r.dy || !r.dz || !r.tmax))
+      return fail(ctx, VMR_ERR_INVALID, "job rays need px..tmax");
+    t[j].mesh = ctx->meshes[J.geom]->dmesh;
+    t[j].rays = vmr::RaySoA{r.px, r.py, r.pz, r.dx, r.dy, r.dz, r.tmax, r.time};
+    t[j].hits = vmr::HitSoA{h.prim, h.geom, h.t, h.u, h.v, h.w};
+    t[j].n = J.n;
+    t[j].chunk0 = chunks;
+    t[j].geom = (int32_t)J.geom;
+    chunks += (J.n + 31) / 32;
+    rays += J.n;
+  }
+  if (stats) *stats = vmr_trace_stats{rays, 0, 0, 0, 0.f};
+  if (chunks == 0) return VMR_OK;
+  // The table is read by the launch; a pending launch of an earlier call may
+  // still read the old one, so wait before overwriting it.
+  VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  VMR_CUDA(ctx, ctx->jobs.ensure(t.size() * sizeof(vmr::JobDesc)));
+  VMR_CUDA(ctx, cudaMemcpyAsync(ctx->jobs.p, t.data(), t.size() * sizeof(vmr::JobDesc), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
+  VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  VMR_CUDA(ctx, cudaEventRecord(ctx->evm, ctx->stream));
+  const int e = vmr::launch_trace_jobs(ctx->jobs.as<vmr::JobDesc>(), n_jobs, chunks,
+                                       (flags & VMR_TRACE_ANY_HIT) ? 1 : 0, ctx->scratch.as<DScratch>(), ctx->stream);
+  if (e != 0) return cuda_fail(ctx, (cudaError_t)e, "jobs kernel launch");
+  VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  if (!stats) return VMR_OK;
+  const int st = read_status(ctx, nullptr);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->evm, ctx->ev1);
+  stats->kernel_ms = ms;
+  return st;
 }
 
 }  // extern "C"

@@ -47,6 +47,9 @@ struct MeshRec {
   std::vector<uint32_t> shader_list;
   bool has_normals = false;
   DevBuf shlist, sidx, nrm;
+  // the autotuner's choice for this mesh (vmr_autotune)
+  bool tuned = false;
+  vmr_tuning tuning{};
 };
 
 // The extended path tracer's captured bounce loop (pathtrace.cu): valid for
@@ -109,12 +112,20 @@ struct vmr_ctx {
   TopRec top;
   vmr::RenderState render;
   vmr::GuideState guide;
-  vmr_tuning tuning{13, 0, 0, 0, 4};
+  vmr_tuning tuning{13, 0, 0, 0, 4, 0};
+  DevBuf jobs;                    // vmr_trace_jobs tables
   // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.
   const float* mesh_bounds_of(const DMesh* d) const {
     for (const auto& m : meshes)
       if (&m->dmesh == d) return m->bounds6;
     return nullptr;
+  }
+  // The tuning a trace of this mesh uses: its own (autotuned) or the context's.
+  const vmr_tuning& tuning_for(const DMesh* d) const {
+    if (d)
+      for (const auto& m : meshes)
+        if (&m->dmesh == d) return m->tuned ? m->tuning : tuning;
+    return tuning;
   }
 };
 

@@ -115,9 +115,13 @@ enum TraceKernel : int {
   kKernelSort = 8,
 };
 
-// Ray reordering (raysort.cu): 6 permutation classes x 16^3 origin cells.
+// Ray reordering (raysort.cu): 6 permutation classes x (2^b)^3 origin cells,
+// b = 3..5 (default 4: 16^3 cells).
 constexpr int kSortCells = 4096;
 constexpr int kSortBuckets = 6 * kSortCells;
+constexpr int kSortMaxBits = 5;
+constexpr int kSortBucketsMax = 6 << (3 * kSortMaxBits);
+constexpr uint32_t sort_buckets(int bits) { return 6u << (3 * bits); }
 constexpr uint64_t kSortMinRays = 1u << 16;  // smaller batches are traced unsorted
 
 // Launch entry points (traverse.cu).
@@ -140,9 +144,23 @@ struct TraceLaunch {
   void* stream;
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);
-int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], uint32_t* keys, uint32_t* hist,
+int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int bits, uint32_t* keys, uint32_t* hist,
                     uint32_t* order, const RaySoA& sorted_out, void* stream);
 int launch_trace_scene(const DTop& top, const TraceLaunch& l);
 int device_sm_count();
+
+// One job of a batched trace (vmr_trace_jobs): its mesh, rays, hits, and the
+// first 32-ray chunk it owns in the launch's chunk sequence.
+struct JobDesc {
+  DMesh mesh;
+  RaySoA rays;
+  HitSoA hits;
+  uint64_t n;
+  uint64_t chunk0;
+  int32_t geom;
+  int32_t pad;
+};
+int launch_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_chunks, int any_hit, DScratch* scratch,
+                      void* stream);
 
 }  // namespace vmr

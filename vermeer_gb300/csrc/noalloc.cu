@@ -109,7 +109,7 @@ extern "C" int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_ray
   if ((tuning.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
     const vmr::RaySoA sorted{f, f + kMaxRays, f + 2 * kMaxRays, f + 3 * kMaxRays, f + 4 * kMaxRays,
                              f + 5 * kMaxRays, f + 6 * kMaxRays, rays->time ? f + 7 * kMaxRays : nullptr};
-    if (vmr::launch_ray_sort(l.rays, n, bounds, keys, hist, order, sorted, stream) != 0)
+    if (vmr::launch_ray_sort(l.rays, n, bounds, 4, keys, hist, order, sorted, stream) != 0)
       return vmr::ctx_fail(ctx, VMR_ERR_CUDA, "vmr_trace_mesh_noalloc: ray reordering launch failed");
     l.rays = sorted;
     l.order = order;

@@ -1,9 +1,10 @@
 // raysort.cu - ray reordering before traversal.
 //
-// Each ray gets the key  class * 4096 + morton12(origin),  where class =
+// Each ray gets the key  class * 2^(3b) + morton(origin),  where class =
 // 2*Kz + (D[Kz] < 0) is the permutation the watertight test uses (Ray.Setup,
-// core/ray.go:103-135) and morton12 interleaves a 16^3 grid cell of the
-// origin inside the scene bounds.  A one-pass bucket sort (histogram,
+// core/ray.go:103-135) and morton interleaves a 2^b x 2^b x 2^b grid cell of
+// the origin inside the scene bounds (b = 3, 4 or 5: the sort-key width the
+// tuning chooses).  A one-pass bucket sort (histogram,
 // exclusive scan, scatter) gathers the rays into key order: warps then trace
 // rays that start close together and head into the same sixth of the
 // sphere, and the triangle test can use one compile-time permutation per
@@ -16,15 +17,16 @@
 namespace vmr {
 namespace {
 
-__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // abcd -> a..b..c..d
-  v &= 15u;
-  v = (v | (v << 4)) & 0x0c3u;
-  v = (v | (v << 2)) & 0x249u;
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {  // abcde -> a..b..c..d..e
+  v &= 31u;
+  v = (v | (v << 8)) & 0x100fu;
+  v = (v | (v << 4)) & 0x10c3u;
+  v = (v | (v << 2)) & 0x1249u;
   return v;
 }
 
-__device__ __forceinline__ uint32_t cell(float p, float lo, float inv) {
-  const float q = fminf(fmaxf((p - lo) * inv, 0.0f), 15.0f);  // NaN -> 0
+__device__ __forceinline__ uint32_t cell(float p, float lo, float inv, float top) {
+  const float q = fminf(fmaxf((p - lo) * inv, 0.0f), top);  // NaN -> 0
   return (uint32_t)q;
 }
 
@@ -42,29 +44,29 @@ __device__ __forceinline__ uint32_t ray_class(float dx, float dy, float dz) {
   return 2u * (uint32_t)kz + (dkz < 0.0f ? 1u : 0u);
 }
 
-__global__ void k_ray_keys(RaySoA rays, uint64_t n, float3 lo, float3 inv, uint32_t* keys, uint32_t* hist) {
+__global__ void k_ray_keys(RaySoA rays, uint64_t n, float3 lo, float3 inv, uint32_t bits, uint32_t* keys,
+                           uint32_t* hist) {
+  const float top = (float)((1u << bits) - 1u);
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = ray_class(rays.dx[i], rays.dy[i], rays.dz[i]);
-    const uint32_t m = spread4(cell(rays.px[i], lo.x, inv.x)) << 2 | spread4(cell(rays.py[i], lo.y, inv.y)) << 1 |
-                       spread4(cell(rays.pz[i], lo.z, inv.z));
-    const uint32_t k = c * kSortCells + m;
+    const uint32_t m = spread5(cell(rays.px[i], lo.x, inv.x, top)) << 2 | spread5(cell(rays.py[i], lo.y, inv.y, top)) << 1 |
+                       spread5(cell(rays.pz[i], lo.z, inv.z, top));
+    const uint32_t k = (c << (3 * bits)) + m;
     keys[i] = k;
     atomicAdd(hist + k, 1u);
   }
 }
 
-// Exclusive scan of kSortBuckets counters in one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* hist) {
-  constexpr int kPer = (kSortBuckets + 1023) / 1024;
+// Exclusive scan of nb counters in one block of 1024 threads (each thread a
+// contiguous range, read twice).
+__global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* hist, uint32_t nb) {
   __shared__ uint32_t part[1024];
-  const int t = threadIdx.x;
-  uint32_t local[kPer];
+  const uint32_t t = threadIdx.x;
+  const uint32_t per = (nb + 1023) / 1024;
   uint32_t sum = 0;
-#pragma unroll
-  for (int j = 0; j < kPer; ++j) {
-    const int b = t * kPer + j;
-    local[j] = b < kSortBuckets ? hist[b] : 0u;
-    sum += local[j];
+  for (uint32_t j = 0; j < per; ++j) {
+    const uint32_t b = t * per + j;
+    sum += b < nb ? hist[b] : 0u;
   }
   part[t] = sum;
   __syncthreads();
@@ -75,11 +77,13 @@ __global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* hist) {
     __syncthreads();
   }
   uint32_t run = part[t] - sum;  // exclusive prefix of this thread's range
-#pragma unroll
-  for (int j = 0; j < kPer; ++j) {
-    const int b = t * kPer + j;
-    if (b < kSortBuckets) hist[b] = run;
-    run += local[j];
+  for (uint32_t j = 0; j < per; ++j) {
+    const uint32_t b = t * per + j;
+    if (b < nb) {
+      const uint32_t v = hist[b];
+      hist[b] = run;
+      run += v;
+    }
   }
 }
 
@@ -109,24 +113,27 @@ __global__ void k_ray_scatter(RaySoA rays, uint64_t n, const uint32_t* keys, uin
 
 }  // namespace
 
-int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], uint32_t* keys, uint32_t* hist,
+int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int bits, uint32_t* keys, uint32_t* hist,
                     uint32_t* order, const RaySoA& sorted_out, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  if (bits < 3 || bits > kSortMaxBits) bits = 4;
+  const uint32_t nb = sort_buckets(bits);
+  const float side = (float)(1u << bits);
   float3 lo = make_float3(bounds[0], bounds[1], bounds[2]);
   float3 inv;
   const float ext[3] = {bounds[3] - bounds[0], bounds[4] - bounds[1], bounds[5] - bounds[2]};
-  inv.x = ext[0] > 0.f ? 16.0f / ext[0] : 0.f;
-  inv.y = ext[1] > 0.f ? 16.0f / ext[1] : 0.f;
-  inv.z = ext[2] > 0.f ? 16.0f / ext[2] : 0.f;
-  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * kSortBuckets, s);
+  inv.x = ext[0] > 0.f ? side / ext[0] : 0.f;
+  inv.y = ext[1] > 0.f ? side / ext[1] : 0.f;
+  inv.z = ext[2] > 0.f ? side / ext[2] : 0.f;
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * nb, s);
   if (e != cudaSuccess) return (int)e;
   const int block = 256;
   int grid = (int)((n + block - 1) / block);
   const int cap = device_sm_count() * 16;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
-  k_ray_keys<<<grid, block, 0, s>>>(rays, n, lo, inv, keys, hist);
-  k_bucket_scan<<<1, 1024, 0, s>>>(hist);
+  k_ray_keys<<<grid, block, 0, s>>>(rays, n, lo, inv, (uint32_t)bits, keys, hist);
+  k_bucket_scan<<<1, 1024, 0, s>>>(hist, nb);
   k_ray_scatter<<<grid, block, 0, s>>>(rays, n, keys, hist, order, sorted_out);
   return (int)cudaGetLastError();
 }

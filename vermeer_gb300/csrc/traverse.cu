@@ -603,6 +603,48 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
   flush_counters<COUNT>(scratch, cnt);
 }
 
+// Batched jobs: persistent warps take 32-ray chunks of the launch's chunk
+// sequence; a chunk belongs to one job (found by binary search over the
+// jobs' first chunks), so the warp's mesh and its static/motion path are
+// uniform.  Each lane runs the per-ray traversal of its ray.
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_chunks,
+                                                    DScratch* scratch) {
+  int2 stk[kStackCapacity];
+  Counters cnt{0, 0, 0};
+  const unsigned lane = threadIdx.x & 31u;
+  int status = kStatusOk;
+  for (;;) {
+    unsigned long long c = 0;
+    if (lane == 0) {
+      c = atomicAdd(&scratch->next_ray, 1ull);
+      if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) c = n_chunks;
+    }
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= n_chunks) break;
+    uint32_t lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) / 2;
+      if (jobs[mid].chunk0 <= c) lo = mid;
+      else hi = mid - 1;
+    }
+    const JobDesc& J = jobs[lo];
+    const uint64_t i = (c - J.chunk0) * 32 + lane;
+    if (i < J.n) {
+      TRay r;
+      load_ray(J.rays, i, r);
+      HitRec h{-1, J.geom, 0.f, 0.f, 0.f};
+      const bool hit = trace_any_mesh<ANY, false>(J.mesh, r, stk, kStackCapacity, h, cnt, status);
+      h.geom = J.geom;
+      store_hit(J.hits, i, r, hit, h);
+      if (status != kStatusOk) {
+        atomicMax(&scratch->status, status);
+        status = kStatusOk;
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------------
 // While-while persistent kernel for one mesh (the hot path).
 //
@@ -1164,6 +1206,20 @@ int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l) {
 int launch_trace_scene(const DTop& top, const TraceLaunch& l) {
   if (l.any_hit) return l.count ? launch_scene_t<true, true>(top, l) : launch_scene_t<true, false>(top, l);
   return l.count ? launch_scene_t<false, true>(top, l) : launch_scene_t<false, false>(top, l);
+}
+
+int launch_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_chunks, int any_hit, DScratch* scratch,
+                      void* stream) {
+  if (n_jobs == 0 || n_chunks == 0) return 0;
+  const int block = 128;
+  if (any_hit) {
+    const int grid = persistent_grid(k_trace_jobs<true>, block);
+    k_trace_jobs<true><<<grid, block, 0, (cudaStream_t)stream>>>(jobs, n_jobs, n_chunks, scratch);
+  } else {
+    const int grid = persistent_grid(k_trace_jobs<false>, block);
+    k_trace_jobs<false><<<grid, block, 0, (cudaStream_t)stream>>>(jobs, n_jobs, n_chunks, scratch);
+  }
+  return (int)cudaGetLastError();
 }
 
 int device_sm_count() {
