@@ -1,0 +1,82 @@
+"""Named workloads for kernel profiling (each runs once and exits 0):
+
+    python -m vermeer_gb300.profile_cases guide        guide inference on 1M vertices
+                                                       and one training step of 256K
+    python -m vermeer_gb300.profile_cases render_ext   extended path tracer, sphere grid,
+                                                       1920x1080, 2 spp, depth 8
+    python -m vermeer_gb300.profile_cases render_ref   reference-mode render, small room,
+                                                       256x256, 16 iterations
+    python -m vermeer_gb300.profile_cases jobs         64 uneven jobs in one launch
+
+Inputs are the seeded synthetic scenes of vermeer_gb300.scenes.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+
+def guide(ctx):
+    rng = np.random.default_rng(1)
+    n = 1 << 20
+    pos = rng.random((n, 3)).astype(np.float32)
+    nrm = rng.standard_normal((n, 3)).astype(np.float32)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    wo = rng.standard_normal((n, 3)).astype(np.float32)
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    lo, hi = np.zeros(3, np.float32), np.ones(3, np.float32)
+    ctx.guide_init(1)
+    ctx.guide_forward(pos, nrm, wo, lo, hi)
+    m = 1 << 18
+    ctx.guide_train_step(pos[:m], nrm[:m], wo[:m], wo[:m], np.ones(m, np.float32), lo, hi)
+
+
+def render_ext(ctx):
+    from . import scenes
+    sc = scenes.sphere_grid()
+    ctx.load_scene(sc)
+    ctx.render_path(sc["width"], sc["height"], 0, 2, 3, max_depth=8)
+
+
+def render_ref(ctx):
+    from . import scenes
+    sc = scenes.small_room(16384, seed=1)
+    ctx.load_scene(sc)
+    ctx.render(256, 256, 0, 16, 7)
+
+
+def jobs(ctx):
+    import torch
+    from . import scenes
+    sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)
+    cam = scenes.coherent_rays(256)
+    js = []
+    for j, nt in enumerate(sizes):
+        motion = j % 2 == 1
+        v, ip = scenes.motion_soup(int(nt), 400 + j) if motion else scenes.triangle_soup(int(nt), 400 + j)
+        g = ctx.mesh_build(v, ip, keys=2 if motion else 1, motion_mode=1)
+        rays = cam.copy()
+        if motion:
+            rays[:, 7] = scenes.uniform(500 + j, rays.shape[0], 7).astype(np.float32)
+        js.append((g, torch.from_numpy(np.ascontiguousarray(rays.T)).cuda()))
+    ctx.trace_jobs(js)
+
+
+CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "jobs": jobs}
+
+
+def main(argv):
+    if len(argv) != 1 or argv[0] not in CASES:
+        print(__doc__)
+        return 2
+    import vermeer_gb300 as vg
+    ctx = vg.Context(0)
+    CASES[argv[0]](ctx)
+    ctx.sync()
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
