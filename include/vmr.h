@@ -282,8 +282,20 @@ typedef struct {
     uint32_t geom;
 } vmr_tri_light;
 
-/* Pinhole camera (builtin/camera/camera.go): m = LocalToWorld,
- * column-major; tan_theta_focal = tan(fov/2) * focal. */
+/* DiskLight (builtin/light/disk.go:18-31): a disk of the given radius at P
+ * facing LookAt; geom is its emissive fan mesh (Disk.createMesh, 20 segments
+ * by default).  Lights are used in the order TriLights, DiskLights. */
+typedef struct {
+    float P[3], up[3], lookat[3];
+    float radius;
+    int samples;           /* NumSamples = 1 << samples (default 1) */
+    uint32_t shader;
+    uint32_t geom;
+} vmr_disk_light;
+
+/* Camera (builtin/camera/camera.go): m = LocalToWorld, column-major;
+ * tan_theta_focal = tan(fov/2) * focal; radius > 0 is a thin lens sampled
+ * with UniformDisk2D (math/sample/sample.go:105-129). */
 typedef struct {
     float m[16];
     float tan_theta_focal, aspect, focal, radius;
@@ -310,6 +322,7 @@ int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n);
 int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, uint32_t n_shaders,
                          const float* normals);
 int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n);
+int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n);
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* camera);
 /* core.Render in reference mode (core/render.go:140-218 with ShaderStd's
  * direct lighting): iterations iter_begin..iter_begin+iter_count-1 of every

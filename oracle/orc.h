@@ -141,6 +141,15 @@ typedef struct {
     float tan_theta_focal, aspect, focal, radius;
 } orc_camera;
 
+/* DiskLight (builtin/light/disk.go:18-31): N = normalize(LookAt - P),
+ * T = normalize(N x Up), B = N x T; mesh = its emissive fan (createMesh). */
+typedef struct {
+    float P[3], up[3], lookat[3];
+    float radius;
+    int samples;
+    uint32_t shader, mesh;
+} orc_disklight;
+
 typedef struct orc_render orc_render;
 
 /* Per-mesh shading data: shader index per face (face order, may be NULL)
@@ -154,6 +163,8 @@ orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, u
                               const uint32_t* shader_list, const orc_shader* shaders, uint32_t n_shaders,
                               const orc_trilight* lights, uint32_t n_lights, const orc_camera* cam);
 void orc_render_destroy(orc_render* r);
+/* Append DiskLights to the light list (after the TriLights). */
+int orc_render_add_disk_lights(orc_render* r, const orc_disklight* lights, uint32_t n);
 /* Runs core.Render iterations iter_begin .. iter_begin+iter_count-1 (the
  * reference's 0-based loop variable; each renders sample iter+1 and folds
  * it into fb as buf = (buf*(iter+1) + c)/(iter+2), core/render.go:127-129).

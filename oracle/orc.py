@@ -96,6 +96,12 @@ class OrcTriLight(ctypes.Structure):
                 ("samples", ctypes.c_int), ("shader", ctypes.c_uint32), ("mesh", ctypes.c_uint32)]
 
 
+class OrcDiskLight(ctypes.Structure):
+    _fields_ = [("P", ctypes.c_float * 3), ("up", ctypes.c_float * 3), ("lookat", ctypes.c_float * 3),
+                ("radius", ctypes.c_float), ("samples", ctypes.c_int), ("shader", ctypes.c_uint32),
+                ("mesh", ctypes.c_uint32)]
+
+
 class OrcCamera(ctypes.Structure):
     _fields_ = [("m", ctypes.c_float * 16), ("tan_theta_focal", ctypes.c_float), ("aspect", ctypes.c_float),
                 ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
@@ -113,6 +119,8 @@ def _register_render(L):
     L.orc_render_create.restype = P
     L.orc_render_create.argtypes = [P, P, ctypes.c_uint32, P, P, P, P, ctypes.c_uint32, P, ctypes.c_uint32, P]
     L.orc_render_destroy.argtypes = [P]
+    L.orc_render_add_disk_lights.restype = ctypes.c_int
+    L.orc_render_add_disk_lights.argtypes = [P, P, ctypes.c_uint32]
     L.orc_render_run.restype = ctypes.c_int
     L.orc_render_run.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                  ctypes.c_uint64, P, ctypes.c_int]
@@ -249,6 +257,16 @@ class Render:
         self._keep = (counts, offs, lst, shs, lts, cam, arr)
         self.h = lib().orc_render_create(self.scene.h, arr, len(self.meshes), _ptr(offs), _ptr(counts), _ptr(lst),
                                          shs, len(scene["shaders"]), lts, len(scene["lights"]), ctypes.byref(cam))
+        dls = scene.get("disk_lights", [])
+        if dls:
+            darr = (OrcDiskLight * len(dls))()
+            for i, d in enumerate(dls):
+                for k in ("P", "up", "lookat"):
+                    for c in range(3):
+                        getattr(darr[i], k)[c] = float(d[k][c])
+                darr[i].radius = float(d["radius"])
+                darr[i].samples, darr[i].shader, darr[i].mesh = int(d.get("samples", 1)), int(d["shader"]), int(d["mesh"])
+            lib().orc_render_add_disk_lights(self.h, darr, len(dls))
 
     def __del__(self):
         if getattr(self, "h", None):

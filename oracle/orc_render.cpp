@@ -227,6 +227,27 @@ V3 cosine_hemisphere(double u0, double u1) {
   double th = 2 * M_PI * u1;
   return v3((float)(r * std::cos(th)), (float)(r * std::sin(th)), (float)std::sqrt(u0));
 }
+// sample.UniformDisk2D (math/sample/sample.go:105-129), concentric warp.
+void uniform_disk(float radius, float r0, float r1, float& xo, float& yo) {
+  const float x = -1 + 2 * r0, y = -1 + 2 * r1;
+  float r = 0, theta = 0;
+  const float q = kPi / 4;
+  if (x > -y && x > y) {
+    r = x;
+    theta = q * y / x;
+  } else if (x > -y && x < y) {
+    r = y;
+    theta = q * (2 - x / y);
+  } else if (x < y && x < -y) {
+    r = -x;
+    theta = q * (4 + y / x);
+  } else if (x > y && x < -y) {
+    r = -y;
+    theta = q * (6 - x / y);
+  }
+  xo = radius * r * gcos(theta);
+  yo = radius * r * gsin(theta);
+}
 inline float chi(float x) { return x > 0.0f ? 1.0f : 0.0f; }
 float ggx_g1(V3 w, V3 m, float alpha) {
   float odn = dot(w, m);
@@ -338,12 +359,24 @@ struct BsdfSample {
   Spectrum Liu;
 };
 
+// A light of the list: a TriLight (kind 0) or a DiskLight (kind 1, with its
+// frame from Disk.PreRender, builtin/light/disk.go:79-104).
+struct Light {
+  int kind;
+  orc_trilight tri;
+  V3 P, T, B, N;
+  float radius;
+  int samples;
+  uint32_t shader, mesh;
+};
+
 struct Render {
   const orc_scene* scene = nullptr;
   std::vector<orc_internal::MeshView> meshes;
   std::vector<std::vector<uint32_t>> mesh_shaders;
   std::vector<Shader> shaders;
-  std::vector<orc_trilight> lights;
+  std::vector<orc_trilight> tri_lights;
+  std::vector<Light> lights;
   orc_camera cam;
 };
 
@@ -465,12 +498,38 @@ bool ray_tri(V3 Ro, V3 Rd, V3 P0, V3 P1, V3 P2, V3& out) {
 struct Renderer {
   const Render& R;
 
-  Spectrum light_liu(const orc_trilight& L, const Ctx& sc) const {
+  Spectrum light_liu(const Light& L, const Ctx& sc) const {
     return from_rgb(emission(R.shaders[L.shader]), sc.lambda);
   }
 
   // Tri.SampleArea (triangle.go:285-343) with the area fallback (:232-282).
-  void sample_area(const orc_trilight& L, const Ctx& sc, int n, std::vector<LightSample>& out) const {
+  // Disk.SampleArea (builtin/light/disk.go:154-204).
+  void sample_area_disk(const Light& L, const Ctx& sc, int n, std::vector<LightSample>& out) const {
+    for (int i = 0; i < n; ++i) {
+      const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;
+      const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
+      const float u = L.radius * std::sqrt((float)r0) * gcos(2 * kPi * (float)r1);
+      const float v = L.radius * std::sqrt((float)r0) * gsin(2 * kPi * (float)r1);
+      const double pdf = (double)(1.0f / (kPi * L.radius * L.radius));
+      const V3 P = add(add(L.P, scale(u, L.B)), scale(v, L.T));  // Vec3Add3
+      const V3 V = sub(P, sc.P);
+      if (dot(V, sc.Ng) > 0.0f && dot(V, L.N) < 0.0f) {
+        LightSample ls;
+        ls.Ldist = length(V);
+        ls.Ld = normalize(V);
+        ls.Liu = light_liu(L, sc);
+        ls.pdf = (float)pdf * (ls.Ldist * ls.Ldist) / gabs(dot(ls.Ld, L.N));
+        out.push_back(ls);
+      }
+    }
+  }
+
+  void sample_area(const Light& LL, const Ctx& sc, int n, std::vector<LightSample>& out) const {
+    if (LL.kind == 1) {
+      sample_area_disk(LL, sc, n, out);
+      return;
+    }
+    const orc_trilight& L = LL.tri;
     const V3 p0 = v3(L.p0[0], L.p0[1], L.p0[2]), p1 = v3(L.p1[0], L.p1[1], L.p1[2]), p2 = v3(L.p2[0], L.p2[1], L.p2[2]);
     const V3 N = tri_normal(L);
     const bool area_only = dot(sc.Ng, sub(p0, sc.P)) < 0 || dot(sc.Ng, sub(p1, sc.P)) < 0 || dot(sc.Ng, sub(p2, sc.P)) < 0;
@@ -486,7 +545,7 @@ struct Renderer {
         ls.Ldist = length(D);
         ls.Ld = normalize(D);
         if (dot(ls.Ld, N) > 0 || dot(ls.Ld, sc.Ng) < 0) continue;
-        ls.Liu = light_liu(L, sc);
+        ls.Liu = light_liu(LL, sc);
         ls.pdf = (float)pdf * sqr(ls.Ldist) / gabs(dot(ls.Ld, N));
       } else {
         double pdf;
@@ -498,15 +557,35 @@ struct Renderer {
         ls.Ldist = length(D);
         ls.Ld = normalize(D);
         if (dot(ls.Ld, N) > 0 || dot(ls.Ld, sc.Ng) < 0) continue;
-        ls.Liu = light_liu(L, sc);
+        ls.Liu = light_liu(LL, sc);
         ls.pdf = (float)pdf;
       }
       out.push_back(ls);
     }
   }
 
+  // Disk.ValidSample (disk.go:119-151) with rayDiskIntersect (disk.go:53-68).
+  bool valid_sample_disk(const Light& L, const Ctx& sc, BsdfSample& s) const {
+    const double pdf = (double)(1.0f / (kPi * L.radius * L.radius));
+    float t;
+    if (!ray_plane(sc.P, s.D, L.P, L.N, t)) return false;
+    const V3 pp = add(sc.P, scale(t, s.D));  // Vec3Mad(Ro, Rd, t)
+    const V3 vv = sub(pp, L.P);
+    if (!(std::sqrt(dot(vv, vv)) <= L.radius)) return false;
+    const V3 p = add(sc.P, scale(t, s.D));
+    const V3 V = sub(p, sc.P);
+    if (dot(V, sc.Ng) <= 0.0f || dot(V, L.N) >= 0.0f) return false;
+    s.Ldist = length(V);
+    s.Ld = normalize(V);
+    s.Liu = light_liu(L, sc);
+    s.pdf_light = (float)pdf * (s.Ldist * s.Ldist) / gabs(dot(s.Ld, L.N));
+    return true;
+  }
+
   // Tri.ValidSample (triangle.go:136-230).
-  bool valid_sample(const orc_trilight& L, const Ctx& sc, BsdfSample& s) const {
+  bool valid_sample(const Light& LL, const Ctx& sc, BsdfSample& s) const {
+    if (LL.kind == 1) return valid_sample_disk(LL, sc, s);
+    const orc_trilight& L = LL.tri;
     const V3 p0 = v3(L.p0[0], L.p0[1], L.p0[2]), p1 = v3(L.p1[0], L.p1[1], L.p1[2]), p2 = v3(L.p2[0], L.p2[1], L.p2[2]);
     V3 P;
     if (!ray_tri(sc.P, s.D, p0, p1, p2, P)) return false;
@@ -516,7 +595,7 @@ struct Renderer {
     s.Ldist = length(D);
     s.Ld = normalize(D);
     if (dot(s.Ld, N) > 0 || dot(s.Ld, sc.Ng) < 0) return false;
-    s.Liu = light_liu(L, sc);
+    s.Liu = light_liu(LL, sc);
     if (area_only) {
       const double pdf = (double)(1 / tri_area(p0, p1, p2));
       s.pdf_light = (float)pdf * sqr(s.Ldist) / gabs(dot(s.Ld, N));
@@ -536,7 +615,7 @@ struct Renderer {
   }
 
   // EvaluateLightSamples (core/shader.go:203-402).
-  RGB evaluate_light_samples(const Ctx& sc, const orc_trilight& L, int NS, const Bsdf& bsdf) const {
+  RGB evaluate_light_samples(const Ctx& sc, const Light& L, int NS, const Bsdf& bsdf) const {
     RGB col{{0, 0, 0}};
     if (NS > 1) {
       std::vector<BsdfSample> bsdf_samples;
@@ -673,7 +752,7 @@ struct Renderer {
     RGB diff_contrib = zero;
     if (total == 0.0f) return zero;  // the reference panics ("Shader has no weight")
     if (dw > 0.0f) {
-      for (const orc_trilight& L : R.lights) {
+      for (const Light& L : R.lights) {
         if ((int32_t)L.mesh == sg.geom) continue;  // LightsPrepare (scene.go:100-116)
         const int NS = sg.level > 0 ? 1 : (1 << L.samples);
         RGB col = evaluate_light_samples(sg, L, NS, diff);
@@ -716,7 +795,7 @@ struct Renderer {
       }
       if (spec_samples > 0) rscale(spec_contrib, sw / (float)spec_samples);
       if (rough > 0.0f) {
-        for (const orc_trilight& L : R.lights) {
+        for (const Light& L : R.lights) {
           if ((int32_t)L.mesh == sg.geom) continue;
           const int NS = sg.level > 0 ? 1 : (1 << L.samples);
           RGB col = evaluate_light_samples(sg, L, NS, spec);
@@ -757,16 +836,26 @@ void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uin
   *time = (float)vdc(j, scramble(seed, pix, 2));
   const float Sx = (float)(-1.0 + 2.0 * (rx / (double)w));
   const float Sy = -(float)(-1.0 + 2.0 * (ry / (double)h));
-  // Camera.ComputeRay, pinhole (camera.go:244-284)
+  // Camera.ComputeRay (camera.go:244-284): pinhole, or a thin lens of
+  // radius c.radius sampled with UniformDisk2D at (lensU, lensV)
   const float camu = Sx * c.tan_theta_focal;
   const float camv = Sy * (c.tan_theta_focal / c.aspect);
   const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
   const float* M = c.m;
-  const V3 d = v3(M[0] * s3.x + M[4] * s3.y + M[8] * s3.z, M[1] * s3.x + M[5] * s3.y + M[9] * s3.z,
-                  M[2] * s3.x + M[6] * s3.y + M[10] * s3.z);
+  V3 e = v3(0, 0, 0);
+  V3 sv = s3;
+  if (c.radius > 0.0f) {
+    const double lensU = vdc(j, scramble(seed, pix, 0)), lensV = sobol(j, scramble(seed, pix, 1));
+    float x, y;
+    uniform_disk(c.radius, (float)lensU, (float)lensV, x, y);
+    e = add(scale(x, v3(1, 0, 0)), scale(y, v3(0, 1, 0)));
+    sv = sub(s3, e);
+  }
+  const V3 d = v3(M[0] * sv.x + M[4] * sv.y + M[8] * sv.z, M[1] * sv.x + M[5] * sv.y + M[9] * sv.z,
+                  M[2] * sv.x + M[6] * sv.y + M[10] * sv.z);
   const V3 D = normalize(d);
-  const V3 P = v3(M[0] * 0.0f + M[4] * 0.0f + M[8] * 0.0f + M[12], M[1] * 0.0f + M[5] * 0.0f + M[9] * 0.0f + M[13],
-                  M[2] * 0.0f + M[6] * 0.0f + M[10] * 0.0f + M[14]);
+  const V3 P = v3(M[0] * e.x + M[4] * e.y + M[8] * e.z + M[12], M[1] * e.x + M[5] * e.y + M[9] * e.z + M[13],
+                  M[2] * e.x + M[6] * e.y + M[10] * e.z + M[14]);
   Po[0] = P.x; Po[1] = P.y; Po[2] = P.z;
   Do[0] = D.x; Do[1] = D.y; Do[2] = D.z;
 }
@@ -778,7 +867,7 @@ RenderScene render_scene(const orc_render* o) {
   s.meshes = r.meshes;
   s.mesh_shaders = r.mesh_shaders;
   for (const Shader& sh : r.shaders) s.shaders.push_back(sh.p);
-  s.lights = r.lights;
+  s.lights = r.tri_lights;
   s.cam = r.cam;
   return s;
 }
@@ -800,7 +889,16 @@ orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, u
     r.mesh_shaders.emplace_back(list + off[i], list + off[i] + cnt[i]);
   }
   for (uint32_t i = 0; i < n_shaders; ++i) r.shaders.push_back(Shader{shaders[i]});
-  r.lights.assign(lights, lights + n_lights);
+  r.tri_lights.assign(lights, lights + n_lights);
+  for (uint32_t i = 0; i < n_lights; ++i) {
+    Light L{};
+    L.kind = 0;
+    L.tri = lights[i];
+    L.samples = lights[i].samples;
+    L.shader = lights[i].shader;
+    L.mesh = lights[i].mesh;
+    r.lights.push_back(L);
+  }
   r.cam = *cam;
   return o;
 }
@@ -843,6 +941,25 @@ int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, u
     std::vector<std::thread> th;
     for (int t = 0; t < nthreads; ++t) th.emplace_back(work);
     for (auto& t : th) t.join();
+  }
+  return 0;
+}
+
+int orc_render_add_disk_lights(orc_render* o, const orc_disklight* lights, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    const orc_disklight& d = lights[i];
+    Light L{};
+    L.kind = 1;
+    L.P = v3(d.P[0], d.P[1], d.P[2]);
+    const V3 up = v3(d.up[0], d.up[1], d.up[2]), at = v3(d.lookat[0], d.lookat[1], d.lookat[2]);
+    L.N = normalize(sub(at, L.P));  // Disk.PreRender (disk.go:88-90)
+    L.T = normalize(cross(L.N, up));
+    L.B = cross(L.N, L.T);
+    L.radius = d.radius;
+    L.samples = d.samples;
+    L.shader = d.shader;
+    L.mesh = d.mesh;
+    o->r.lights.push_back(L);
   }
   return 0;
 }

@@ -123,3 +123,24 @@ def test_render_non_square_matches_oracle(ctx, orc):
     got, _ = ctx.render(48, 32, 3, 2, 11)
     frac, mean_abs = _compare(got, ref)
     assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)
+
+
+# ----------------------------------------------- DiskLight and thin lens ----
+def test_oracle_disk_light_room_sane(orc):
+    sc = scenes.small_room_disk(2048, seed=4)
+    fb = orc.Render(sc).run(32, 32, 0, 8, 5)
+    assert np.isfinite(fb).all() and (fb >= 0).all()
+    assert 0.3 < (fb.sum(-1) > 0).mean() <= 1.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("samples", [0, 1, 2])
+def test_render_disk_light_thin_lens_matches_oracle(ctx, orc, samples):
+    """DiskLight area sampling and ValidSample (one light sample without MIS
+    at samples=0, MIS with 1+1 and 2+2) through a thin-lens camera."""
+    sc = scenes.small_room_disk(2048, seed=4, light_samples=samples)
+    ctx.load_scene(sc)
+    ref = orc.Render(sc).run(40, 40, 0, 3, 9)
+    got, _ = ctx.render(40, 40, 0, 3, 9)
+    frac, mean_abs = _compare(got, ref)
+    assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)

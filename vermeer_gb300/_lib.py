@@ -72,6 +72,11 @@ class TriLight(ctypes.Structure):
                 ("samples", ctypes.c_int), ("shader", U32), ("geom", U32)]
 
 
+class DiskLight(ctypes.Structure):
+    _fields_ = [("P", ctypes.c_float * 3), ("up", ctypes.c_float * 3), ("lookat", ctypes.c_float * 3),
+                ("radius", ctypes.c_float), ("samples", ctypes.c_int), ("shader", U32), ("geom", U32)]
+
+
 class Camera(ctypes.Structure):
     _fields_ = [("m", ctypes.c_float * 16), ("tan_theta_focal", ctypes.c_float), ("aspect", ctypes.c_float),
                 ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
@@ -146,6 +151,7 @@ SIGNATURES = {
     "vmr_set_shaders": (ctypes.c_int, [P, P, U32]),
     "vmr_mesh_set_shading": (ctypes.c_int, [P, U32, P, U32, P]),
     "vmr_set_lights": (ctypes.c_int, [P, P, U32]),
+    "vmr_set_disk_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_camera": (ctypes.c_int, [P, ctypes.POINTER(Camera)]),
     "vmr_render": (ctypes.c_int, [P, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
     "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),

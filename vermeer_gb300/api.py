@@ -267,6 +267,17 @@ class Context:
             arr[i].samples, arr[i].shader, arr[i].geom = int(d.get("samples", 1)), int(d["shader"]), int(d["geom"])
         self._check(self.L.vmr_set_lights(self.h, arr, len(lights)))
 
+    def set_disk_lights(self, lights):
+        """DiskLights: dicts with P, up, lookat, radius, samples, shader, geom."""
+        arr = (_lib.DiskLight * len(lights))()
+        for i, d in enumerate(lights):
+            for k in ("P", "up", "lookat"):
+                for c in range(3):
+                    getattr(arr[i], k)[c] = float(d[k][c])
+            arr[i].radius = float(d["radius"])
+            arr[i].samples, arr[i].shader, arr[i].geom = int(d.get("samples", 1)), int(d["shader"]), int(d["geom"])
+        self._check(self.L.vmr_set_disk_lights(self.h, arr, len(lights)))
+
     def set_quad_lights(self, lights):
         """Quad lights: dicts with p0, e1, e2, shader, geom."""
         arr = (_lib.QuadLight * len(lights))()
@@ -379,6 +390,7 @@ class Context:
         for g, m in zip(ids, scene["meshes"]):
             self.mesh_set_shading(g, m["shaders"], m.get("normals"))
         self.set_lights([dict(l, geom=ids[l["mesh"]]) for l in scene["lights"]])
+        self.set_disk_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("disk_lights", [])])
         self.set_quad_lights([dict(q, geom=ids[q["mesh"]]) for q in scene.get("quad_lights", [])])
         self.set_env_light(scene.get("env", (0.0, 0.0, 0.0)))
         self.set_camera(scene["camera"])

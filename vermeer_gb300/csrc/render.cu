@@ -21,6 +21,7 @@
 // division (the reference's RSQRTSS estimate is machine-dependent).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -43,8 +44,29 @@ struct Cand {
   bool ok;
 };
 
+// Disk.SampleArea, sample i of n (builtin/light/disk.go:154-204).
+__device__ Cand disk_sample(const RLight& L, const Ctx& sc, int n, int i) {
+  Cand c{};
+  const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;
+  const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
+  const float u = L.radius * sqrtf((float)r0) * gcos(2 * kPi * (float)r1);
+  const float v = L.radius * sqrtf((float)r0) * gsin(2 * kPi * (float)r1);
+  const double pdf = (double)(1.0f / (kPi * L.radius * L.radius));
+  const V3 LP = v3(L.P[0], L.P[1], L.P[2]), LT = v3(L.T[0], L.T[1], L.T[2]), LB = v3(L.B[0], L.B[1], L.B[2]),
+           LN = v3(L.N[0], L.N[1], L.N[2]);
+  const V3 P = add(add(LP, scale(u, LB)), scale(v, LT));
+  const V3 V = sub(P, sc.P);
+  if (!(dot(V, sc.Ng) > 0.0f && dot(V, LN) < 0.0f)) return c;
+  c.Ldist = length(V);
+  c.Ld = normalize(V);
+  c.pdf_own = (float)pdf * (c.Ldist * c.Ldist) / fabsf(dot(c.Ld, LN));
+  c.ok = true;
+  return c;
+}
+
 // Tri.SampleArea, sample i of n (triangle.go:232-343).
 __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
+  if (L.kind == 1) return disk_sample(L, sc, n, i);
   Cand c{};
   const V3 p0 = lp(L, 0), p1 = lp(L, 1), p2 = lp(L, 2);
   const V3 N = normalize(cross(sub(p1, p0), sub(p2, p0)));
@@ -76,7 +98,8 @@ __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
   return c;
 }
 
-// BSDF sample i then Tri.ValidSample (core/shader.go:211-228, triangle.go:136-230).
+// BSDF sample i then Tri.ValidSample / Disk.ValidSample (core/shader.go:211-228,
+// triangle.go:136-230, disk.go:119-151).
 __device__ Cand bsdf_candidate(const RLight& L, const Ctx& sc, const Bsdf& bsdf, int half, int i) {
   Cand c{};
   const uint64_t idx = sc.I * (uint64_t)half + (uint64_t)i;
@@ -84,6 +107,22 @@ __device__ Cand bsdf_candidate(const RLight& L, const Ctx& sc, const Bsdf& bsdf,
   const V3 D = normalize(bsdf_sample(bsdf, r0, r1));
   c.pdf_bsdf = bsdf_pdf(bsdf, D);
   if (c.pdf_bsdf <= 0) return c;
+  if (L.kind == 1) {
+    const double pdf = (double)(1.0f / (kPi * L.radius * L.radius));
+    const V3 LP = v3(L.P[0], L.P[1], L.P[2]), LN = v3(L.N[0], L.N[1], L.N[2]);
+    float t;
+    if (!ray_plane(sc.P, D, LP, LN, t)) return c;  // rayDiskIntersect (disk.go:53-68)
+    const V3 pp = add(sc.P, scale(t, D));
+    const V3 vv = sub(pp, LP);
+    if (!(sqrtf(dot(vv, vv)) <= L.radius)) return c;
+    const V3 V = sub(add(sc.P, scale(t, D)), sc.P);
+    if (dot(V, sc.Ng) <= 0.0f || dot(V, LN) >= 0.0f) return c;
+    c.Ldist = length(V);
+    c.Ld = normalize(V);
+    c.pdf_light = (float)pdf * (c.Ldist * c.Ldist) / fabsf(dot(c.Ld, LN));
+    c.ok = true;
+    return c;
+  }
   const V3 p0 = lp(L, 0), p1 = lp(L, 1), p2 = lp(L, 2);
   V3 P;
   if (!ray_tri(sc.P, D, p0, p1, p2, P)) return c;
@@ -500,9 +539,20 @@ int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n) {
   return VMR_OK;
 }
 
+int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n) {
+  if (!ctx || (n && !lights)) return VMR_ERR_INVALID;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (lights[i].samples < 0 || (1 << lights[i].samples) > 2 * vmr::kMaxHalf)
+      return rfail(ctx, VMR_ERR_UNSUPPORTED, "DiskLight samples must be in [0, 4]");
+    if (!(lights[i].radius > 0.0f)) return rfail(ctx, VMR_ERR_INVALID, "DiskLight radius must be positive");
+  }
+  ctx->render.disks.assign(lights, lights + n);
+  return VMR_OK;
+}
+
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* cam) {
   if (!ctx || !cam) return VMR_ERR_INVALID;
-  if (cam->radius > 0.0f) return rfail(ctx, VMR_ERR_UNSUPPORTED, "thin-lens cameras are not supported yet");
+  if (!(cam->radius >= 0.0f)) return rfail(ctx, VMR_ERR_INVALID, "camera radius must be >= 0");
   ctx->render.camera = *cam;
   ctx->render.has_camera = true;
   return VMR_OK;
@@ -524,6 +574,9 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   for (const auto& L : R.lights)
     if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
       return rfail(ctx, VMR_ERR_INVALID, "light shader or geom out of range");
+  for (const auto& L : R.disks)
+    if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
+      return rfail(ctx, VMR_ERR_INVALID, "disk light shader or geom out of range");
   for (uint32_t g : ctx->top.host.geom_order) {
     const auto& mr = ctx->meshes[g];
     if (mr->host.motion()) return rfail(ctx, VMR_ERR_UNSUPPORTED, "rendering motion meshes is not supported yet");
@@ -542,18 +595,47 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     rm[g].shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
     rm[g].n_shaders = (uint32_t)mr.shader_list.size();
   }
-  std::vector<RLight> rl(R.lights.size());
+  std::vector<RLight> rl(R.lights.size() + R.disks.size());
   uint32_t ns = 1;
   for (size_t i = 0; i < R.lights.size(); ++i) {
+    rl[i] = RLight{};
     std::memcpy(rl[i].p, R.lights[i].p0, 12);
     std::memcpy(rl[i].p + 3, R.lights[i].p1, 12);
     std::memcpy(rl[i].p + 6, R.lights[i].p2, 12);
     rl[i].samples = R.lights[i].samples;
     rl[i].shader = R.lights[i].shader;
     rl[i].geom = R.lights[i].geom;
+    rl[i].kind = 0;
     ns = std::max<uint32_t>(ns, 1u << R.lights[i].samples);
   }
-  const uint32_t nl = (uint32_t)R.lights.size();
+  for (size_t k = 0; k < R.disks.size(); ++k) {  // Disk.PreRender frame (disk.go:88-90), host float math
+    const vmr_disk_light& d = R.disks[k];
+    RLight& L = rl[R.lights.size() + k];
+    L = RLight{};
+    L.kind = 1;
+    L.samples = d.samples;
+    L.shader = d.shader;
+    L.geom = d.geom;
+    L.radius = d.radius;
+    std::memcpy(L.P, d.P, 12);
+    auto nrm = [](const float* a, float* o) {
+      const float r = 1.0f / std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+      o[0] = a[0] * r; o[1] = a[1] * r; o[2] = a[2] * r;
+    };
+    auto crs = [](const float* a, const float* b, float* o) {
+      o[0] = a[1] * b[2] - a[2] * b[1];
+      o[1] = a[2] * b[0] - a[0] * b[2];
+      o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    const float dn[3] = {d.lookat[0] - d.P[0], d.lookat[1] - d.P[1], d.lookat[2] - d.P[2]};
+    nrm(dn, L.N);
+    float t[3];
+    crs(L.N, d.up, t);
+    nrm(t, L.T);
+    crs(L.N, L.T, L.B);
+    ns = std::max<uint32_t>(ns, 1u << d.samples);
+  }
+  const uint32_t nl = (uint32_t)rl.size();
   const uint32_t npix = p->width * p->height;
   uint32_t per_batch = p->max_batch_samples ? p->max_batch_samples : (4u << 20);
   uint32_t iters_per_batch = std::max<uint32_t>(1, per_batch / npix);

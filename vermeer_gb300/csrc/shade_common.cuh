@@ -278,10 +278,12 @@ struct RMesh {
   uint32_t pad;
 };
 struct RLight {
-  float p[9];
+  float p[9];        // TriLight: p0, p1, p2
   int samples;
   uint32_t shader;
   uint32_t geom;
+  int kind;          // 0 TriLight, 1 DiskLight
+  float P[3], T[3], B[3], N[3], radius;  // DiskLight frame (Disk.PreRender)
 };
 
 struct Ctx {
@@ -423,6 +425,28 @@ __device__ __forceinline__ bool hit_attributes(const RMesh& m, int32_t prim, flo
   return true;
 }
 
+// sample.UniformDisk2D (math/sample/sample.go:105-129), concentric warp.
+__device__ __forceinline__ void uniform_disk(float radius, float r0, float r1, float& xo, float& yo) {
+  const float x = -1 + 2 * r0, y = -1 + 2 * r1;
+  float r = 0, theta = 0;
+  const float q = kPi / 4;
+  if (x > -y && x > y) {
+    r = x;
+    theta = q * y / x;
+  } else if (x > -y && x < y) {
+    r = y;
+    theta = q * (2 - x / y);
+  } else if (x < y && x < -y) {
+    r = -x;
+    theta = q * (4 + y / x);
+  } else if (x > y && x < -y) {
+    r = -y;
+    theta = q * (6 - x / y);
+  }
+  xo = radius * r * gcos(theta);
+  yo = radius * r * gsin(theta);
+}
+
 // core.Render's per-sample setup (core/render.go:89-120) and a pinhole
 // Camera.ComputeRay (builtin/camera/camera.go:244-284) for iteration j
 // (render(iter+1)) of pixel pix: RasterXY position, VdC time and hero
@@ -441,11 +465,19 @@ __device__ __forceinline__ void camera_primary(const vmr_camera& c, uint32_t wid
   const float camv = Sy * (c.tan_theta_focal / c.aspect);
   const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
   const float* M = c.m;
-  const V3 d = v3(M[0] * s3.x + M[4] * s3.y + M[8] * s3.z, M[1] * s3.x + M[5] * s3.y + M[9] * s3.z,
-                  M[2] * s3.x + M[6] * s3.y + M[10] * s3.z);
+  V3 e = v3(0, 0, 0), sv = s3;
+  if (c.radius > 0.0f) {  // thin lens: UniformDisk2D at (lensU, lensV)
+    const double lensU = vdc(j, scramble(seed, pix, 0)), lensV = sobol(j, scramble(seed, pix, 1));
+    float x, y;
+    uniform_disk(c.radius, (float)lensU, (float)lensV, x, y);
+    e = add(scale(x, v3(1, 0, 0)), scale(y, v3(0, 1, 0)));
+    sv = sub(s3, e);
+  }
+  const V3 d = v3(M[0] * sv.x + M[4] * sv.y + M[8] * sv.z, M[1] * sv.x + M[5] * sv.y + M[9] * sv.z,
+                  M[2] * sv.x + M[6] * sv.y + M[10] * sv.z);
   D = normalize(d);
-  P = v3(M[0] * 0.0f + M[4] * 0.0f + M[8] * 0.0f + M[12], M[1] * 0.0f + M[5] * 0.0f + M[9] * 0.0f + M[13],
-         M[2] * 0.0f + M[6] * 0.0f + M[10] * 0.0f + M[14]);
+  P = v3(M[0] * e.x + M[4] * e.y + M[8] * e.z + M[12], M[1] * e.x + M[5] * e.y + M[9] * e.z + M[13],
+         M[2] * e.x + M[6] * e.y + M[10] * e.z + M[14]);
 }
 
 }  // namespace

@@ -408,3 +408,54 @@ def slit_room(n_tris: int = 200_000, seed: int = 5, width: int = 1024, height: i
     cam = lookat_camera((-1.2, 1.4, 0.15), (1.0, 1.3, 2.2), (0.0, 1.0, 0.0), 70.0, width / height)
     return dict(meshes=meshes, shaders=shaders, lights=[], quad_lights=quads, env=(0.0, 0.0, 0.0), camera=cam,
                 width=width, height=height)
+
+
+def disk_light_mesh(P, up, lookat, radius: float, segments: int = 20):
+    """The emissive fan a DiskLight adds (builtin/light/disk.go:214-258): per
+    segment (P, P + R cos(a) B + R sin(a) T, P + R cos(a+da) B + R sin(a+da) T),
+    the angle advanced in float32, every vertex normal N; N, T, B from
+    Disk.PreRender (disk.go:88-90) in float32."""
+    f = np.float32
+
+    def norm(a):
+        a = np.asarray(a, f)
+        return (a * (f(1.0) / np.sqrt(np.dot(a, a), dtype=f))).astype(f)
+
+    P, up, lookat = (np.asarray(a, f) for a in (P, up, lookat))
+    N = norm(lookat - P)
+    T = norm(np.cross(N, up).astype(f))
+    B = np.cross(N, T).astype(f)
+    R = f(radius)
+    pi = f(3.14159265358)
+    dv = f(f(2) * pi) / f(segments)
+    ang = f(0)
+    verts = []
+    for _ in range(segments):
+        a1 = f(ang + dv)
+        c0, s0 = f(np.cos(np.float64(ang))), f(np.sin(np.float64(ang)))
+        c1, s1 = f(np.cos(np.float64(a1))), f(np.sin(np.float64(a1)))
+        verts += [P, P + ((R * c0) * B + (R * s0) * T), P + ((R * c1) * B + (R * s1) * T)]
+        ang = f(ang + dv)
+    v = np.asarray(verts, f)
+    return v, np.arange(v.shape[0], dtype=np.uint32), np.tile(N, (v.shape[0], 1)).astype(f)
+
+
+def small_room_disk(n_tris: int = 4096, seed: int = 1, lens_radius: float = 0.05, light_samples: int = 1) -> dict:
+    """The small room lit by one DiskLight (radius 0.2, facing down through
+    the ceiling opening, radiance 10) instead of the TriLight panels, seen
+    through a thin-lens camera of the given lens radius focused at the
+    room's centre."""
+    sc = small_room(n_tris, seed=seed, light_samples=light_samples)
+    light_shader = sc["lights"][0]["shader"]
+    keep = [m for i, m in enumerate(sc["meshes"]) if i not in {l["mesh"] for l in sc["lights"]}]
+    P, up, at = (0.0, 1.08, 0.0), (0.0, 0.0, 1.0), (0.0, 0.0, 0.0)
+    v, i, n = disk_light_mesh(P, up, at, 0.2)
+    keep.append(dict(verts=v, idxp=i, normals=n, shaders=[light_shader]))
+    sc["meshes"] = keep
+    sc["lights"] = []
+    sc["disk_lights"] = [dict(P=P, up=up, lookat=at, radius=0.2, samples=light_samples, shader=light_shader,
+                              mesh=len(keep) - 1)]
+    cam = lookat_camera((0.0, 0.0, -3.4), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, 1.0, focal=3.4)
+    cam["radius"] = np.float32(lens_radius)
+    sc["camera"] = cam
+    return sc
