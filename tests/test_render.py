@@ -144,3 +144,24 @@ def test_render_disk_light_thin_lens_matches_oracle(ctx, orc, samples):
     got, _ = ctx.render(40, 40, 0, 3, 9)
     frac, mean_abs = _compare(got, ref)
     assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)
+
+
+# ------------------------------------------------------ mirror recursion ----
+def test_oracle_mirror_room_sane(orc):
+    sc = scenes.small_room_mirror(2048, seed=6)
+    fb = orc.Render(sc).run(32, 32, 0, 4, 5)
+    assert np.isfinite(fb).all() and (fb >= 0).all() and fb.mean() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("samples", [0, 1])
+def test_render_mirror_recursion_matches_oracle(ctx, orc, samples):
+    """Mirror reflections (core.Trace recursion, one light sample per light
+    below the camera level) down to level 3."""
+    sc = scenes.small_room_mirror(2048, seed=6, light_samples=samples)
+    ctx.load_scene(sc)
+    ref = orc.Render(sc).run(48, 48, 0, 3, 13)
+    got, st = ctx.render(48, 48, 0, 3, 13)
+    frac, mean_abs = _compare(got, ref)
+    assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)
+    assert st["camera_rays"] == 48 * 48 * 3

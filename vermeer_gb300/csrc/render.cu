@@ -148,42 +148,57 @@ __device__ Cand bsdf_candidate(const RLight& L, const Ctx& sc, const Bsdf& bsdf,
 }
 
 // --------------------------------------------------------------- layout ---
-constexpr int kMaxHalf = 8;  // NumSamples up to 16 per light (TriLight.Samples <= 4)
+constexpr int kMaxHalf = 8;    // NumSamples up to 16 per light (Samples <= 4)
+constexpr int kMaxLevel = 3;   // ShaderStd.Eval returns nothing above level 3 (std.go:96-98)
 
-// Per sample s of a batch: slots[s][lobe][light][k] hold a contribution (rgb)
-// that counts when its shadow ray is unoccluded.  k < half: light samples;
-// half <= k < 2*half: BSDF samples (the order EvaluateLightSamples adds
-// them).  lscale[s][lobe][light] = 1/float32(total), -1 when the light takes
-// one sample (no MIS, no scale), 0 when nothing was taken.
+// One recursion level of a batch (level 0: the camera rays, one entry per
+// sample; level l > 0: the mirror reflections of level l-1, one entry per
+// reflection, compacted).  Per entry e: slots[e][lobe][light][k] hold a
+// contribution (rgb) that counts when its shadow ray is unoccluded (k < half:
+// light samples, then BSDF samples: the order EvaluateLightSamples adds
+// them); lscale[e][lobe][light] = 1/float32(total), -1 when the light takes
+// one sample (no MIS, no scale), 0 when nothing was taken; mw[e] = the mirror
+// weight to_rgb(rho/pdf)*Spec1Colour and Spec1Weight (w = -1: not a mirror).
+struct Level {
+  float* ray;          // 8 * cap: px py pz dx dy dz tmax time
+  uint32_t* samp;      // entry -> sample (null at level 0: the identity)
+  int32_t* hit;        // 6 * cap: prim geom t u v w
+  int32_t* shader;     // shader id of the hit, -1 none
+  float* emis;         // 3 per entry
+  float* slot_rgb;     // [cap][2][nl][ns][3]
+  uint8_t* slot_live;  // [cap][2][nl][ns]
+  float* lscale;       // [cap][2][nl]
+  float* mw;           // 4 per entry: w.rgb, Spec1Weight (-1: not a mirror)
+  int32_t* child;      // entry at level + 1, -1 none
+  uint32_t ns;         // slots per (lobe, light)
+  uint32_t cap;
+  unsigned long long* count;  // entries (levels > 0; appended by the level below)
+};
+
 struct RenderBatch {
   uint32_t width, height, npix;
   uint32_t iter0;  // first core.Render loop iteration of the batch
   uint32_t n;      // samples in the batch
   uint32_t nl;     // lights
-  uint32_t ns;     // slots per (lobe, light)
+  uint32_t levels; // levels with storage (1 + mirror depth)
   uint32_t pad;
   uint64_t seed;
   vmr_camera cam;
   const vmr_shader_std* shaders;
   const RLight* lights;
   const RMesh* meshes;
-  float *px, *py, *pz, *dx, *dy, *dz, *tmax, *time;
-  float* lambda;
-  int32_t *hprim, *hgeom;
-  float *ht, *hu, *hv, *hw;
-  int32_t* shader;    // per sample: shader id of the hit, -1 none
-  float* emis;        // per sample rgb
-  float* slot_rgb;    // [n][2][nl][ns][3]
-  uint8_t* slot_live; // [n][2][nl][ns]
-  float* lscale;      // [n][2][nl]
+  float* lambda;      // per sample
+  Level lv[kMaxLevel + 1];
   float *sx, *sy, *sz, *sdx, *sdy, *sdz, *stmax, *stime;
-  uint32_t* sback;    // queue entry -> slot index
+  uint32_t* sback;    // queue entry -> slot index (of the level being shaded)
   int32_t* shit;      // any-hit prim per queue entry
   unsigned long long* queue_len;
   uint32_t queue_cap;
   int* status;
   float* fb;          // framebuffer (device), w*h*3
 };
+
+__device__ __forceinline__ float* ray_f(const Level& L, int k, uint64_t e) { return L.ray + (size_t)k * L.cap + e; }
 
 __global__ void k_generate(RenderBatch b) {
   const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -193,15 +208,17 @@ __global__ void k_generate(RenderBatch b) {
   V3 P, D;
   float time, lambda;
   camera_primary(b.cam, b.width, b.height, j, pix, b.seed, P, D, time, lambda);
-  b.px[s] = P.x; b.py[s] = P.y; b.pz[s] = P.z;
-  b.dx[s] = D.x; b.dy[s] = D.y; b.dz[s] = D.z;
-  b.tmax[s] = __int_as_float(0x7f800000);
-  b.time[s] = time;
+  const Level& L = b.lv[0];
+  *ray_f(L, 0, s) = P.x; *ray_f(L, 1, s) = P.y; *ray_f(L, 2, s) = P.z;
+  *ray_f(L, 3, s) = D.x; *ray_f(L, 4, s) = D.y; *ray_f(L, 5, s) = D.z;
+  *ray_f(L, 6, s) = __int_as_float(0x7f800000);
+  *ray_f(L, 7, s) = time;
   b.lambda[s] = lambda;
 }
 
 // Queues one shadow ray (one atomic per warp for the lanes that want one).
-__device__ void emit_shadow(const RenderBatch& b, const Ctx& sc, V3 Ld, float Ldist, uint32_t slot, bool want) {
+__device__ void emit_shadow(const RenderBatch& b, const Level& lv, const Ctx& sc, V3 Ld, float Ldist, uint32_t slot,
+                            bool want) {
   const unsigned act = __activemask();
   const unsigned m = __ballot_sync(act, want);
   if (m == 0u) return;
@@ -213,7 +230,7 @@ __device__ void emit_shadow(const RenderBatch& b, const Ctx& sc, V3 Ld, float Ld
   if (!want) return;
   const unsigned long long q = base + __popc(m & ((1u << lane) - 1u));
   if (q >= b.queue_cap) {  // counted by the host from queue_len; never written
-    b.slot_live[slot] = 0;
+    lv.slot_live[slot] = 0;
     return;
   }
   const V3 o = offset_p(sc, dot(Ld, sc.Ng) < 0 ? -1 : 1);
@@ -228,8 +245,8 @@ __device__ void emit_shadow(const RenderBatch& b, const Ctx& sc, V3 Ld, float Ld
 // EvaluateLightSamples (core/shader.go:203-402) for one (lobe, light):
 // writes the slot contributions, queues their shadow rays and returns the
 // scale the accumulate pass applies.
-__device__ float light_lobe(const RenderBatch& b, const Ctx& sc, const RLight& L, const Bsdf& bsdf, int NS,
-                            uint32_t slot0) {
+__device__ float light_lobe(const RenderBatch& b, const Level& lv, const Ctx& sc, const RLight& L, const Bsdf& bsdf,
+                            int NS, uint32_t slot0) {
   const int half = NS > 1 ? NS / 2 : 0;
   const int nls = NS > 1 ? half : NS;
   Cand cl[kMaxHalf], cb[kMaxHalf];
@@ -253,7 +270,7 @@ __device__ float light_lobe(const RenderBatch& b, const Ctx& sc, const RLight& L
       const Cand& c = pass == 0 ? cl[i] : cb[i];
       const uint32_t slot = slot0 + (pass == 0 ? 0 : half) + i;
       const bool want = c.ok && dot(c.Ld, sc.N) > 0 && !(mis && total == 0);
-      float* out = b.slot_rgb + (size_t)slot * 3;
+      float* out = lv.slot_rgb + (size_t)slot * 3;
       out[0] = out[1] = out[2] = 0.0f;
       if (want) {
         Spec rho = bsdf_eval(bsdf, c.Ld);
@@ -281,8 +298,8 @@ __device__ float light_lobe(const RenderBatch& b, const Ctx& sc, const RLight& L
         out[1] = rgb.c[1];
         out[2] = rgb.c[2];
       }
-      b.slot_live[slot] = want ? 1 : 0;
-      emit_shadow(b, sc, c.Ld, c.Ldist, slot, want);
+      lv.slot_live[slot] = want ? 1 : 0;
+      emit_shadow(b, lv, sc, c.Ld, c.Ldist, slot, want);
     }
   }
   if (!mis) return -1.0f;
@@ -290,94 +307,191 @@ __device__ float light_lobe(const RenderBatch& b, const Ctx& sc, const RLight& L
 }
 
 // Hit attributes (builtin/geom/polymesh/trace.go:276-515, static meshes) and
-// ShaderStd.Eval's direct lighting (builtin/shader/std.go:77-296).
-__global__ void __launch_bounds__(128) k_shade(RenderBatch b) {
-  const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (s >= b.n) return;
-  const int32_t prim = b.hprim[s];
-  float* em = b.emis + s * 3;
-  em[0] = em[1] = em[2] = 0.0f;
-  const size_t nslot = (size_t)2 * b.nl * b.ns;
-  for (size_t k = 0; k < nslot; ++k) b.slot_live[s * nslot + k] = 0;
-  for (size_t k = 0; k < (size_t)2 * b.nl; ++k) b.lscale[s * 2 * b.nl + k] = 0.0f;
-  b.shader[s] = -1;
-  if (prim < 0) return;
-  const int32_t geom = b.hgeom[s];
-  const RMesh& m = b.meshes[geom];
-  Ctx sc;
-  uint32_t shid;
-  if (!hit_attributes(m, prim, b.hu[s], b.hv[s], b.hw[s], sc, shid)) return;
-  const vmr_shader_std& sh = b.shaders[shid];
-  sc.Rd = v3(b.dx[s], b.dy[s], b.dz[s]);
-  sc.lambda = b.lambda[s];
-  sc.time = b.time[s];
-  const uint32_t pix = (uint32_t)(s % b.npix);
-  sc.I = b.iter0 + (uint64_t)(s / b.npix) + 1;
-  sc.scr0 = scramble(b.seed, pix, 4);
-  sc.scr1 = scramble(b.seed, pix, 5);
-  sc.geom = geom;
-  b.shader[s] = (int32_t)shid;
-  const RGB e = emission(sh);
-  em[0] = e.c[0];
-  em[1] = e.c[1];
-  em[2] = e.c[2];
-  // tangent frame (std.go:101-108)
-  V3 Vt = cross(sc.N, sc.DdPdu);
-  if (len2(Vt) < 0.1f) Vt = cross(sc.N, sc.DdPdv);
-  Vt = normalize(Vt);
-  const V3 Ut = normalize(cross(sc.N, Vt));
-  const V3 wi = v3(-sc.Rd.x, -sc.Rd.y, -sc.Rd.z);
-  float dw = (sh.flags & VMR_SH_DIFFUSE_STRENGTH) ? sh.diffuse_strength : 0.0f;
-  float sw = (sh.flags & VMR_SH_SPEC1_STRENGTH) ? sh.spec1_strength : 0.0f;
-  const float total = dw + sw;
-  if (total == 0.0f) {  // the reference panics: no weight (std.go:141-143)
-    atomicMax(b.status, kStatusIterationCap + 1);
-    return;
-  }
-  dw /= total;
-  sw /= total;
-  if (dw > 0.0f) {
-    const float rough = (sh.flags & VMR_SH_DIFFUSE_ROUGHNESS) ? sh.diffuse_roughness : 0.5f;
-    const Bsdf diff{0, sc.lambda, project(Ut, Vt, sc.N, wi), rough * rough, Fresnel{0, 0, {}, {}}, Ut, Vt, sc.N};
-    for (uint32_t l = 0; l < b.nl; ++l) {
-      const RLight& L = b.lights[l];
-      if ((int32_t)L.geom == geom) continue;  // LightsPrepare (scene.go:100-116)
-      const int NS = 1 << L.samples;
-      const uint32_t slot0 = (uint32_t)((s * 2 + 0) * b.nl + l) * b.ns;
-      b.lscale[(s * 2 + 0) * b.nl + l] = light_lobe(b, sc, L, diff, NS, slot0);
+// ShaderStd.Eval (builtin/shader/std.go:77-296) for the entries of one
+// level: emission, the diffuse and glossy lobes' light samples, and the
+// mirror (Spec1Roughness 0) reflection queued for the next level with the
+// sample's I and scrambles (a child ShaderContext copies them).
+__global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
+  const Level& lv = b.lv[level];
+  const uint64_t n = level == 0 ? (uint64_t)b.n : (*lv.count < lv.cap ? *lv.count : lv.cap);
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = level == 0 ? e : lv.samp[e];
+    const int32_t prim = lv.hit[e];
+    float* em = lv.emis + e * 3;
+    em[0] = em[1] = em[2] = 0.0f;
+    const size_t nslot = (size_t)2 * b.nl * lv.ns;
+    for (size_t k = 0; k < nslot; ++k) lv.slot_live[e * nslot + k] = 0;
+    for (size_t k = 0; k < (size_t)2 * b.nl; ++k) lv.lscale[e * 2 * b.nl + k] = 0.0f;
+    lv.shader[e] = -1;
+    lv.mw[e * 4 + 3] = -1.0f;
+    lv.child[e] = -1;
+    if (prim < 0) continue;
+    const int32_t geom = lv.hit[lv.cap + e];
+    const RMesh& m = b.meshes[geom];
+    Ctx sc;
+    uint32_t shid;
+    const float* hf = reinterpret_cast<const float*>(lv.hit);
+    if (!hit_attributes(m, prim, hf[3 * (size_t)lv.cap + e], hf[4 * (size_t)lv.cap + e], hf[5 * (size_t)lv.cap + e],
+                        sc, shid))
+      continue;
+    const vmr_shader_std& sh = b.shaders[shid];
+    sc.Rd = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
+    sc.lambda = b.lambda[s];
+    sc.time = *ray_f(lv, 7, e);
+    const uint32_t pix = (uint32_t)(s % b.npix);
+    sc.I = b.iter0 + (uint64_t)(s / b.npix) + 1;
+    sc.scr0 = scramble(b.seed, pix, 4);
+    sc.scr1 = scramble(b.seed, pix, 5);
+    sc.geom = geom;
+    lv.shader[e] = (int32_t)shid;
+    const RGB ec = emission(sh);
+    em[0] = ec.c[0];
+    em[1] = ec.c[1];
+    em[2] = ec.c[2];
+    // tangent frame (std.go:101-108)
+    V3 Vt = cross(sc.N, sc.DdPdu);
+    if (len2(Vt) < 0.1f) Vt = cross(sc.N, sc.DdPdv);
+    Vt = normalize(Vt);
+    const V3 Ut = normalize(cross(sc.N, Vt));
+    const V3 wi = v3(-sc.Rd.x, -sc.Rd.y, -sc.Rd.z);
+    float dw = (sh.flags & VMR_SH_DIFFUSE_STRENGTH) ? sh.diffuse_strength : 0.0f;
+    float sw = (sh.flags & VMR_SH_SPEC1_STRENGTH) ? sh.spec1_strength : 0.0f;
+    const float total = dw + sw;
+    if (total == 0.0f) {  // the reference panics: no weight (std.go:141-143)
+      atomicMax(b.status, kStatusIterationCap + 1);
+      continue;
     }
-  }
-  if (sw > 0.0f) {
-    const float rough = (sh.flags & VMR_SH_SPEC1_ROUGHNESS) ? sh.spec1_roughness : 0.5f;
-    Fresnel fr{0, (sh.flags & VMR_SH_IOR) ? sh.ior : 1.7f, {}, {}};
-    if (sh.spec1_fresnel == 1) {
-      RGB refl{{0.5f, 0.5f, 0.5f}}, edge{{0.5f, 0.5f, 0.5f}};
-      if (sh.flags & VMR_SH_FRESNEL_REFL) refl = RGB{{sh.spec1_fresnel_refl[0], sh.spec1_fresnel_refl[1], sh.spec1_fresnel_refl[2]}};
-      if (sh.flags & VMR_SH_FRESNEL_EDGE)  // assigned to refl, as std.go:185-187 does
-        refl = RGB{{sh.spec1_fresnel_edge[0], sh.spec1_fresnel_edge[1], sh.spec1_fresnel_edge[2]}};
-      fr = Fresnel{1, 0, refl, edge};
-    }
-    if (rough > 0.0f) {
-      const Bsdf spec{1, sc.lambda, project(Ut, Vt, sc.N, wi), rough * rough, fr, Ut, Vt, sc.N};
+    dw /= total;
+    sw /= total;
+    if (dw > 0.0f) {
+      const float rough = (sh.flags & VMR_SH_DIFFUSE_ROUGHNESS) ? sh.diffuse_roughness : 0.5f;
+      const Bsdf diff{0, sc.lambda, project(Ut, Vt, sc.N, wi), rough * rough, Fresnel{0, 0, {}, {}}, Ut, Vt, sc.N};
       for (uint32_t l = 0; l < b.nl; ++l) {
         const RLight& L = b.lights[l];
-        if ((int32_t)L.geom == geom) continue;
-        const int NS = 1 << L.samples;
-        const uint32_t slot0 = (uint32_t)((s * 2 + 1) * b.nl + l) * b.ns;
-        b.lscale[(s * 2 + 1) * b.nl + l] = light_lobe(b, sc, L, spec, NS, slot0);
+        if ((int32_t)L.geom == geom) continue;  // LightsPrepare (scene.go:100-116)
+        const int NS = level > 0 ? 1 : 1 << L.samples;  // level > 0: one sample (shader.go:189-191)
+        const uint32_t slot0 = (uint32_t)((e * 2 + 0) * b.nl + l) * lv.ns;
+        lv.lscale[(e * 2 + 0) * b.nl + l] = light_lobe(b, lv, sc, L, diff, NS, slot0);
+      }
+    }
+    if (sw > 0.0f) {
+      const float rough = (sh.flags & VMR_SH_SPEC1_ROUGHNESS) ? sh.spec1_roughness : 0.5f;
+      Fresnel fr{0, (sh.flags & VMR_SH_IOR) ? sh.ior : 1.7f, {}, {}};
+      if (sh.spec1_fresnel == 1) {
+        RGB refl{{0.5f, 0.5f, 0.5f}}, edge{{0.5f, 0.5f, 0.5f}};
+        if (sh.flags & VMR_SH_FRESNEL_REFL) refl = RGB{{sh.spec1_fresnel_refl[0], sh.spec1_fresnel_refl[1], sh.spec1_fresnel_refl[2]}};
+        if (sh.flags & VMR_SH_FRESNEL_EDGE)  // assigned to refl, as std.go:185-187 does
+          refl = RGB{{sh.spec1_fresnel_edge[0], sh.spec1_fresnel_edge[1], sh.spec1_fresnel_edge[2]}};
+        fr = Fresnel{1, 0, refl, edge};
+      }
+      if (rough > 0.0f) {
+        const Bsdf spec{1, sc.lambda, project(Ut, Vt, sc.N, wi), rough * rough, fr, Ut, Vt, sc.N};
+        for (uint32_t l = 0; l < b.nl; ++l) {
+          const RLight& L = b.lights[l];
+          if ((int32_t)L.geom == geom) continue;
+          const int NS = level > 0 ? 1 : 1 << L.samples;
+          const uint32_t slot0 = (uint32_t)((e * 2 + 1) * b.nl + l) * lv.ns;
+          lv.lscale[(e * 2 + 1) * b.nl + l] = light_lobe(b, lv, sc, L, spec, NS, slot0);
+        }
+      } else {
+        // the mirror: one sample at idx = I (std.go:216-259)
+        const Bsdf spec{2, sc.lambda, project(Ut, Vt, sc.N, wi), rough * rough, fr, Ut, Vt, sc.N};
+        const double r0 = vdc(sc.I, sc.scr0), r1 = sobol(sc.I, sc.scr1);
+        const V3 wo = bsdf_sample(spec, r0, r1);
+        const double pdf = bsdf_pdf(spec, wo);
+        float* w = lv.mw + e * 4;
+        w[0] = w[1] = w[2] = 0.0f;
+        w[3] = sw;
+        if (dot(wo, sc.Ng) > 0.0f) {
+          Spec rho = bsdf_eval(spec, wo);
+          const float inv = 1.0f / (float)pdf;
+          for (int k = 0; k < 4; ++k) rho.c[k] *= inv;
+          const RGB col = to_rgb(rho, sc.lambda);
+          const RGB scol = (sh.flags & VMR_SH_SPEC1_COLOUR)
+                               ? RGB{{sh.spec1_colour[0], sh.spec1_colour[1], sh.spec1_colour[2]}}
+                               : RGB{{0, 0, 0}};
+          for (int k = 0; k < 3; ++k) w[k] = col.c[k] * scol.c[k];
+          // level 3's reflection reaches level 4, whose ShaderStd.Eval adds
+          // nothing: it would contribute w*0, clamped to 0, so it is not traced
+          if (level < (uint32_t)kMaxLevel && level + 1 < b.levels) {
+            const Level& nx = b.lv[level + 1];
+            const unsigned long long c = atomicAdd(nx.count, 1ull);
+            if (c < nx.cap) {
+              const V3 o = offset_p(sc, 1);
+              *ray_f(nx, 0, c) = o.x; *ray_f(nx, 1, c) = o.y; *ray_f(nx, 2, c) = o.z;
+              *ray_f(nx, 3, c) = wo.x; *ray_f(nx, 4, c) = wo.y; *ray_f(nx, 5, c) = wo.z;
+              *ray_f(nx, 6, c) = __int_as_float(0x7f800000);
+              *ray_f(nx, 7, c) = sc.time;
+              nx.samp[c] = (uint32_t)s;
+              lv.child[e] = (int32_t)c;
+            }
+          }
+        }
       }
     }
   }
 }
 
 // Occluded shadow rays switch their slot off.
-__global__ void k_resolve(RenderBatch b, uint32_t nq) {
+__global__ void k_resolve(RenderBatch b, uint32_t level, uint32_t nq) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < nq && b.shit[q] >= 0) b.slot_live[b.sback[q]] = 0;
+  if (q < nq && b.shit[q] >= 0) b.lv[level].slot_live[b.sback[q]] = 0;
 }
 
-// Per pixel, the batch's iterations in order: the sample colour assembled
-// as ShaderStd.Eval adds its parts, then buf = (buf*iter + c)/(iter+1).
+// ShaderStd.Eval's sum for one entry: ((0 + emission) + diffuse) + spec, the
+// spec part being the glossy lobes' light samples or, for a mirror,
+// clamp(w * child) * Spec1Weight (0 when the reflection found nothing).
+__device__ RGB entry_colour(const RenderBatch& b, const Level& lv, uint64_t e, bool child_hit, RGB child) {
+  RGB c{{0, 0, 0}};
+  const vmr_shader_std& sh = b.shaders[lv.shader[e]];
+  float dw = (sh.flags & VMR_SH_DIFFUSE_STRENGTH) ? sh.diffuse_strength : 0.0f;
+  float sw = (sh.flags & VMR_SH_SPEC1_STRENGTH) ? sh.spec1_strength : 0.0f;
+  const float tw = dw + sw;
+  dw /= tw;
+  sw /= tw;
+  RGB lobe[2] = {{{0, 0, 0}}, {{0, 0, 0}}};
+  const RGB colour[2] = {
+      (sh.flags & VMR_SH_DIFFUSE_COLOUR) ? RGB{{sh.diffuse_colour[0], sh.diffuse_colour[1], sh.diffuse_colour[2]}} : RGB{{0, 0, 0}},
+      (sh.flags & VMR_SH_SPEC1_COLOUR) ? RGB{{sh.spec1_colour[0], sh.spec1_colour[1], sh.spec1_colour[2]}} : RGB{{0, 0, 0}}};
+  for (int lb = 0; lb < 2; ++lb) {
+    for (uint32_t l = 0; l < b.nl; ++l) {
+      const float sc = lv.lscale[(e * 2 + lb) * b.nl + l];
+      if (sc == 0.0f) continue;
+      RGB col{{0, 0, 0}};
+      const uint32_t slot0 = (uint32_t)((e * 2 + lb) * b.nl + l) * lv.ns;
+      for (uint32_t k = 0; k < lv.ns; ++k) {
+        if (!lv.slot_live[slot0 + k]) continue;
+        const float* v = lv.slot_rgb + (size_t)(slot0 + k) * 3;
+        col.c[0] += v[0];
+        col.c[1] += v[1];
+        col.c[2] += v[2];
+      }
+      if (sc > 0.0f)
+        for (float& v : col.c) v *= sc;
+      for (int k = 0; k < 3; ++k) col.c[k] *= colour[lb].c[k];
+      for (int k = 0; k < 3; ++k) lobe[lb].c[k] += col.c[k];
+    }
+    if (lb == 0 && dw > 0.0f)
+      for (float& v : lobe[0].c) v *= dw;
+  }
+  const float* w = lv.mw + e * 4;
+  if (w[3] >= 0.0f) {  // mirror
+    RGB sp{{0, 0, 0}};
+    if (child_hit)
+      for (int k = 0; k < 3; ++k) {
+        float v = w[k] * child.c[k];
+        if (v < 0 || isnan(v)) v = 0;
+        sp.c[k] = 0.0f + v;
+      }
+    for (int k = 0; k < 3; ++k) lobe[1].c[k] = sp.c[k] * (w[3] / 1.0f);
+  }
+  for (int k = 0; k < 3; ++k) c.c[k] = ((0.0f + lv.emis[e * 3 + k]) + lobe[0].c[k]) + lobe[1].c[k];
+  return c;
+}
+
+// Per pixel, the batch's iterations in order: each sample's chain of mirror
+// reflections evaluated from the deepest level up, then
+// buf = (buf*iter + c)/(iter+1).
 __global__ void k_accumulate(RenderBatch b, uint32_t iters) {
   const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= b.npix) return;
@@ -385,42 +499,27 @@ __global__ void k_accumulate(RenderBatch b, uint32_t iters) {
   for (uint32_t it = 0; it < iters; ++it) {
     const uint64_t s = (uint64_t)it * b.npix + pix;
     const uint32_t j = b.iter0 + it + 1;
-    RGB c{{0, 0, 0}};
-    const int32_t shid = b.shader[s];
-    if (shid >= 0) {
-      const vmr_shader_std& sh = b.shaders[shid];
-      float dw = (sh.flags & VMR_SH_DIFFUSE_STRENGTH) ? sh.diffuse_strength : 0.0f;
-      float sw = (sh.flags & VMR_SH_SPEC1_STRENGTH) ? sh.spec1_strength : 0.0f;
-      const float tw = dw + sw;
-      dw /= tw;
-      sw /= tw;
-      RGB lobe[2] = {{{0, 0, 0}}, {{0, 0, 0}}};
-      const RGB colour[2] = {
-          (sh.flags & VMR_SH_DIFFUSE_COLOUR) ? RGB{{sh.diffuse_colour[0], sh.diffuse_colour[1], sh.diffuse_colour[2]}} : RGB{{0, 0, 0}},
-          (sh.flags & VMR_SH_SPEC1_COLOUR) ? RGB{{sh.spec1_colour[0], sh.spec1_colour[1], sh.spec1_colour[2]}} : RGB{{0, 0, 0}}};
-      for (int lb = 0; lb < 2; ++lb) {
-        for (uint32_t l = 0; l < b.nl; ++l) {
-          const float sc = b.lscale[(s * 2 + lb) * b.nl + l];
-          if (sc == 0.0f) continue;
-          RGB col{{0, 0, 0}};
-          const uint32_t slot0 = (uint32_t)((s * 2 + lb) * b.nl + l) * b.ns;
-          for (uint32_t k = 0; k < b.ns; ++k) {
-            if (!b.slot_live[slot0 + k]) continue;
-            const float* v = b.slot_rgb + (size_t)(slot0 + k) * 3;
-            col.c[0] += v[0];
-            col.c[1] += v[1];
-            col.c[2] += v[2];
-          }
-          if (sc > 0.0f)
-            for (float& v : col.c) v *= sc;
-          for (int k = 0; k < 3; ++k) col.c[k] *= colour[lb].c[k];
-          for (int k = 0; k < 3; ++k) lobe[lb].c[k] += col.c[k];
-        }
-        if (lb == 0 && dw > 0.0f)
-          for (float& v : lobe[0].c) v *= dw;
-      }
-      for (int k = 0; k < 3; ++k) c.c[k] = ((0.0f + b.emis[s * 3 + k]) + lobe[0].c[k]) + lobe[1].c[k];
+    int64_t chain[kMaxLevel + 1];
+    int depth = 0;
+    chain[0] = (int64_t)s;
+    while (depth < kMaxLevel && depth + 1 < (int)b.levels && b.lv[depth].shader[chain[depth]] >= 0 &&
+           b.lv[depth].child[chain[depth]] >= 0) {
+      chain[depth + 1] = b.lv[depth].child[chain[depth]];
+      ++depth;
     }
+    RGB res{{0, 0, 0}};
+    bool hit = false;
+    for (int l = depth; l >= 0; --l) {
+      const Level& lv = b.lv[l];
+      if (lv.shader[chain[l]] < 0) {  // core.Trace returned false
+        hit = false;
+        res = RGB{{0, 0, 0}};
+        continue;
+      }
+      res = entry_colour(b, lv, (uint64_t)chain[l], hit, res);
+      hit = true;
+    }
+    const RGB c = hit ? res : RGB{{0, 0, 0}};
     f0 = (f0 * (float)j + c.c[0]) / (float)(j + 1);
     f1 = (f1 * (float)j + c.c[1]) / (float)(j + 1);
     f2 = (f2 * (float)j + c.c[2]) / (float)(j + 1);
@@ -567,10 +666,6 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   if (p->width == 0 || p->height == 0 || p->width > 4096 || p->height > 4096)
     return rfail(ctx, VMR_ERR_INVALID, "image size must be in [1, 4096] (RasterXY uses m = 12)");
   auto& R = ctx->render;
-  for (const auto& sh : R.shaders)
-    if ((sh.flags & VMR_SH_SPEC1_STRENGTH) && sh.spec1_strength > 0.0f && (sh.flags & VMR_SH_SPEC1_ROUGHNESS) &&
-        sh.spec1_roughness == 0.0f)
-      return rfail(ctx, VMR_ERR_UNSUPPORTED, "mirror (Spec1Roughness 0) shaders are not supported yet");
   for (const auto& L : R.lights)
     if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
       return rfail(ctx, VMR_ERR_INVALID, "light shader or geom out of range");
@@ -642,15 +737,36 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   if (iters_per_batch > p->iter_count) iters_per_batch = std::max<uint32_t>(1, p->iter_count);
   const uint64_t nmax = (uint64_t)iters_per_batch * npix;
   const uint64_t nslots = nmax * 2 * nl * ns;
+  // Mirror levels get storage only when a shader is a mirror.
+  bool has_mirror = false;
+  for (const auto& sh : R.shaders)
+    if ((sh.flags & VMR_SH_SPEC1_STRENGTH) && sh.spec1_strength > 0.0f && (sh.flags & VMR_SH_SPEC1_ROUGHNESS) &&
+        sh.spec1_roughness == 0.0f)
+      has_mirror = true;
+  const uint32_t levels = has_mirror ? (uint32_t)kMaxLevel + 1 : 1u;
   // Device buffers (one block, carved).
   const size_t fsz = 4;
   size_t bytes = 0;
   auto carve = [&](size_t nbytes) { size_t o = bytes; bytes += (nbytes + 255) / 256 * 256; return o; };
-  const size_t o_ray = carve(nmax * 9 * fsz), o_hit = carve(nmax * 6 * fsz), o_sh = carve(nmax * 4),
-               o_em = carve(nmax * 3 * fsz), o_srgb = carve(nslots * 3 * fsz), o_live = carve(nslots),
-               o_lsc = carve(nmax * 2 * nl * fsz), o_q = carve(std::max<uint64_t>(1, nslots) * 8 * fsz),
+  size_t o_lv[kMaxLevel + 1][10];
+  for (uint32_t l = 0; l < levels; ++l) {
+    const uint64_t cap = nmax;
+    const uint32_t lns = l == 0 ? ns : 1u;
+    const uint64_t lslots = cap * 2 * nl * lns;
+    o_lv[l][0] = carve(cap * 8 * fsz);                 // rays
+    o_lv[l][1] = carve(l == 0 ? 0 : cap * 4);          // samp
+    o_lv[l][2] = carve(cap * 6 * 4);                   // hits
+    o_lv[l][3] = carve(cap * 4);                       // shader
+    o_lv[l][4] = carve(cap * 3 * fsz);                 // emis
+    o_lv[l][5] = carve(lslots * 3 * fsz);              // slot rgb
+    o_lv[l][6] = carve(lslots);                        // slot live
+    o_lv[l][7] = carve(cap * 2 * nl * fsz);            // lscale
+    o_lv[l][8] = carve(cap * 4 * fsz);                 // mirror weight
+    o_lv[l][9] = carve(cap * 4);                       // child
+  }
+  const size_t o_lambda = carve(nmax * fsz), o_q = carve(std::max<uint64_t>(1, nslots) * 8 * fsz),
                o_back = carve(std::max<uint64_t>(1, nslots) * 4), o_shit = carve(std::max<uint64_t>(1, nslots) * 4),
-               o_cnt = carve(64), o_fb = carve((size_t)npix * 3 * fsz), o_meshes = carve(rm.size() * sizeof(RMesh)),
+               o_cnt = carve(128), o_fb = carve((size_t)npix * 3 * fsz), o_meshes = carve(rm.size() * sizeof(RMesh)),
                o_lights = carve(std::max<size_t>(1, rl.size()) * sizeof(RLight)),
                o_shaders = carve(std::max<size_t>(1, R.shaders.size()) * sizeof(vmr_shader_std));
   RCUDA(R.buf.ensure(bytes));
@@ -669,35 +785,38 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   b.height = p->height;
   b.npix = npix;
   b.nl = nl;
-  b.ns = ns;
+  b.levels = levels;
   b.seed = p->seed;
   b.cam = R.camera;
   b.shaders = reinterpret_cast<const vmr_shader_std*>(base + o_shaders);
   b.lights = reinterpret_cast<const RLight*>(base + o_lights);
   b.meshes = reinterpret_cast<const RMesh*>(base + o_meshes);
-  float* ray = reinterpret_cast<float*>(base + o_ray);
-  b.px = ray; b.py = ray + nmax; b.pz = ray + 2 * nmax; b.dx = ray + 3 * nmax; b.dy = ray + 4 * nmax;
-  b.dz = ray + 5 * nmax; b.tmax = ray + 6 * nmax; b.time = ray + 7 * nmax; b.lambda = ray + 8 * nmax;
-  char* hit = base + o_hit;
-  b.hprim = reinterpret_cast<int32_t*>(hit);
-  b.hgeom = reinterpret_cast<int32_t*>(hit) + nmax;
-  b.ht = reinterpret_cast<float*>(hit) + 2 * nmax;
-  b.hu = reinterpret_cast<float*>(hit) + 3 * nmax;
-  b.hv = reinterpret_cast<float*>(hit) + 4 * nmax;
-  b.hw = reinterpret_cast<float*>(hit) + 5 * nmax;
-  b.shader = reinterpret_cast<int32_t*>(base + o_sh);
-  b.emis = reinterpret_cast<float*>(base + o_em);
-  b.slot_rgb = reinterpret_cast<float*>(base + o_srgb);
-  b.slot_live = reinterpret_cast<uint8_t*>(base + o_live);
-  b.lscale = reinterpret_cast<float*>(base + o_lsc);
+  b.lambda = reinterpret_cast<float*>(base + o_lambda);
+  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(base + o_cnt);
+  for (uint32_t l = 0; l < levels; ++l) {
+    Level& L = b.lv[l];
+    L.ray = reinterpret_cast<float*>(base + o_lv[l][0]);
+    L.samp = l == 0 ? nullptr : reinterpret_cast<uint32_t*>(base + o_lv[l][1]);
+    L.hit = reinterpret_cast<int32_t*>(base + o_lv[l][2]);
+    L.shader = reinterpret_cast<int32_t*>(base + o_lv[l][3]);
+    L.emis = reinterpret_cast<float*>(base + o_lv[l][4]);
+    L.slot_rgb = reinterpret_cast<float*>(base + o_lv[l][5]);
+    L.slot_live = reinterpret_cast<uint8_t*>(base + o_lv[l][6]);
+    L.lscale = reinterpret_cast<float*>(base + o_lv[l][7]);
+    L.mw = reinterpret_cast<float*>(base + o_lv[l][8]);
+    L.child = reinterpret_cast<int32_t*>(base + o_lv[l][9]);
+    L.ns = l == 0 ? ns : 1u;
+    L.cap = (uint32_t)nmax;
+    L.count = cnt + 2 + l;
+  }
   const uint64_t qcap = std::max<uint64_t>(1, nslots);
   float* q = reinterpret_cast<float*>(base + o_q);
   b.sx = q; b.sy = q + qcap; b.sz = q + 2 * qcap; b.sdx = q + 3 * qcap; b.sdy = q + 4 * qcap;
   b.sdz = q + 5 * qcap; b.stmax = q + 6 * qcap; b.stime = q + 7 * qcap;
   b.sback = reinterpret_cast<uint32_t*>(base + o_back);
   b.shit = reinterpret_cast<int32_t*>(base + o_shit);
-  b.queue_len = reinterpret_cast<unsigned long long*>(base + o_cnt);
-  b.status = reinterpret_cast<int*>(base + o_cnt + 8);
+  b.queue_len = cnt;
+  b.status = reinterpret_cast<int*>(cnt + 1);
   b.queue_cap = (uint32_t)std::min<uint64_t>(qcap, 0xffffffffu);
   b.fb = reinterpret_cast<float*>(base + o_fb);
   RCUDA(cudaMemsetAsync(b.status, 0, 4, st));
@@ -709,31 +828,46 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     b.n = iters * npix;
     const int blk = 128;
     const int grid = (int)((b.n + blk - 1) / blk);
+    RCUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(unsigned long long) * (kMaxLevel + 1), st));
     k_generate<<<grid, blk, 0, st>>>(b);
     RCUDA(cudaGetLastError());
-    vmr_rays rr{b.px, b.py, b.pz, b.dx, b.dy, b.dz, b.tmax, b.time};
-    vmr_hits hh{b.hprim, b.hgeom, b.ht, b.hu, b.hv, b.hw};
-    int rc = vmr_trace_scene(ctx, &rr, b.n, VMR_TRACE_DEVICE, &hh, nullptr);
-    if (rc != VMR_OK) return rc;
-    RCUDA(cudaMemsetAsync(b.queue_len, 0, 8, st));
-    k_shade<<<grid, blk, 0, st>>>(b);
-    RCUDA(cudaGetLastError());
-    unsigned long long nq = 0;
-    RCUDA(cudaMemcpyAsync(&nq, b.queue_len, 8, cudaMemcpyDeviceToHost, st));
-    RCUDA(cudaStreamSynchronize(st));
-    if (nq > b.queue_cap) return rfail(ctx, VMR_ERR_QUEUE_OVERFLOW, "shadow-ray queue overflow");
-    if (nq) {
-      vmr_rays sr{b.sx, b.sy, b.sz, b.sdx, b.sdy, b.sdz, b.stmax, b.stime};
-      vmr_hits sh{b.shit, nullptr, nullptr, nullptr, nullptr, nullptr};
-      rc = vmr_trace_scene(ctx, &sr, nq, VMR_TRACE_DEVICE | VMR_TRACE_ANY_HIT, &sh, nullptr);
+    for (uint32_t l = 0; l < levels; ++l) {
+      const Level& L = b.lv[l];
+      uint64_t ne = b.n;
+      if (l > 0) {  // mirror reflections queued by the level below
+        unsigned long long c = 0;
+        RCUDA(cudaMemcpyAsync(&c, L.count, 8, cudaMemcpyDeviceToHost, st));
+        RCUDA(cudaStreamSynchronize(st));
+        ne = std::min<uint64_t>(c, L.cap);
+        if (ne == 0) break;
+      }
+      const uint64_t cap = L.cap;
+      vmr_rays rr{L.ray, L.ray + cap, L.ray + 2 * cap, L.ray + 3 * cap, L.ray + 4 * cap, L.ray + 5 * cap,
+                  L.ray + 6 * cap, L.ray + 7 * cap};
+      float* hf = reinterpret_cast<float*>(L.hit);
+      vmr_hits hh{L.hit, L.hit + cap, hf + 2 * cap, hf + 3 * cap, hf + 4 * cap, hf + 5 * cap};
+      int rc = vmr_trace_scene(ctx, &rr, ne, VMR_TRACE_DEVICE, &hh, nullptr);
       if (rc != VMR_OK) return rc;
-      k_resolve<<<(int)((nq + 255) / 256), 256, 0, st>>>(b, (uint32_t)nq);
+      RCUDA(cudaMemsetAsync(b.queue_len, 0, 8, st));
+      k_shade<<<(int)((ne + blk - 1) / blk), blk, 0, st>>>(b, l);
       RCUDA(cudaGetLastError());
+      unsigned long long nq = 0;
+      RCUDA(cudaMemcpyAsync(&nq, b.queue_len, 8, cudaMemcpyDeviceToHost, st));
+      RCUDA(cudaStreamSynchronize(st));
+      if (nq > b.queue_cap) return rfail(ctx, VMR_ERR_QUEUE_OVERFLOW, "shadow-ray queue overflow");
+      if (nq) {
+        vmr_rays sr{b.sx, b.sy, b.sz, b.sdx, b.sdy, b.sdz, b.stmax, b.stime};
+        vmr_hits sh{b.shit, nullptr, nullptr, nullptr, nullptr, nullptr};
+        rc = vmr_trace_scene(ctx, &sr, nq, VMR_TRACE_DEVICE | VMR_TRACE_ANY_HIT, &sh, nullptr);
+        if (rc != VMR_OK) return rc;
+        k_resolve<<<(int)((nq + 255) / 256), 256, 0, st>>>(b, l, (uint32_t)nq);
+        RCUDA(cudaGetLastError());
+      }
+      n_shadow += nq;
+      if (l == 0) n_cam += ne;
     }
     k_accumulate<<<(int)((npix + 127) / 128), 128, 0, st>>>(b, iters);
     RCUDA(cudaGetLastError());
-    n_shadow += nq;
-    n_cam += b.n;
   }
   RCUDA(cudaEventRecord(ctx->ev1, st));
   RCUDA(cudaMemcpyAsync(fb, b.fb, (size_t)npix * 3 * fsz, cudaMemcpyDeviceToHost, st));

@@ -196,7 +196,7 @@ __device__ RGB fresnel_kr(const Fresnel& f, float c) {
 
 // ---------------------------------------------------------------- BSDFs ---
 struct Bsdf {
-  int kind;  // 0 OrenNayar, 1 GGX
+  int kind;  // 0 OrenNayar, 1 GGX, 2 Specular
   float lambda;
   V3 wi;
   float rough;  // roughness^2 as the constructors store it
@@ -216,7 +216,13 @@ __device__ float ggx_d(V3 m, float alpha) {
   const float denom = kPi * sqr(m.z * m.z) * sqr(alpha * alpha + ((1.0f / (m.z * m.z)) - 1));
   return numer / denom;
 }
+// reflect(omegaR, (0,0,1)) (bsdf/specular.go:13-19): 2*dot(N, w)*N - w.
+__device__ __forceinline__ V3 reflect_z(V3 w) {
+  const float d = 0.0f * w.x + 0.0f * w.y + 1.0f * w.z;
+  return sub(scale(2.0f * d, v3(0, 0, 1)), w);
+}
 __device__ V3 bsdf_sample(const Bsdf& b, double r0, double r1) {
+  if (b.kind == 2) return expand(b.U, b.V, b.N, normalize(reflect_z(b.wi)));  // Specular.Sample
   if (b.kind == 0) {  // CosineHemisphere (math/sample/sample.go:18-27)
     const double r = sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
     return expand(b.U, b.V, b.N, v3((float)(r * cos(th)), (float)(r * sin(th)), (float)sqrt(r0)));
@@ -230,6 +236,7 @@ __device__ V3 bsdf_sample(const Bsdf& b, double r0, double r1) {
 }
 __device__ double bsdf_pdf(const Bsdf& b, V3 wo_world) {
   const V3 wo = project(b.U, b.V, b.N, wo_world);
+  if (b.kind == 2) return dot(wo, reflect_z(b.wi)) < 0.9999f ? 0.0 : 1.0;  // Specular.PDF
   if (b.kind == 0) return (double)gmax(0.0f, wo.z) / 3.14159265358979323846;
   const float alpha = sqr(b.rough);
   const V3 m = scale(signf(b.wi.z), normalize(add(b.wi, wo)));
@@ -238,6 +245,15 @@ __device__ double bsdf_pdf(const Bsdf& b, V3 wo_world) {
 }
 __device__ Spec bsdf_eval(const Bsdf& b, V3 wo_world) {
   const V3 wo = project(b.U, b.V, b.N, wo_world);
+  if (b.kind == 2) {  // Specular.Eval (bsdf/specular.go:77-101)
+    Spec rho;
+    for (int k = 0; k < 4; ++k) rho.c[k] = 0.0f;
+    if (dot(wo, reflect_z(b.wi)) < 0.9999f) return rho;
+    rho = from_rgb(fresnel_kr(b.fr, b.wi.z), b.lambda);
+    const float s = fabsf(dot(wo, v3(0, 0, 1)));
+    for (int k = 0; k < 4; ++k) rho.c[k] *= s;
+    return rho;
+  }
   if (b.kind == 0) {  // OrenNayar.Eval (bsdf/orennayar.go:42-73)
     const float sigma = b.rough;
     const float A = 1 - (0.5f * (sigma * sigma) / ((sigma * sigma) + 0.57f));

@@ -459,3 +459,21 @@ def small_room_disk(n_tris: int = 4096, seed: int = 1, lens_radius: float = 0.05
     cam["radius"] = np.float32(lens_radius)
     sc["camera"] = cam
     return sc
+
+
+def small_room_mirror(n_tris: int = 4096, seed: int = 1, light_samples: int = 1) -> dict:
+    """The small room with mirrors (ShaderStd with Spec1Roughness 0): the back
+    and side walls pure mirrors (no diffuse weight) facing each other, so
+    reflections chain to the deepest level core.Trace evaluates, and half of
+    the soup's materials diffuse + mirror (Spec1Strength 0.4, dielectric IOR
+    1.5 or a Metal Fresnel)."""
+    sc = small_room(n_tris, seed=seed, light_samples=light_samples)
+    sh = sc["shaders"]
+    for wall in (2, 3, 4):
+        sh[wall] = dict(spec1_colour=(0.95, 0.9, 0.85), spec1_strength=1.0, spec1_roughness=0.0,
+                        spec1_fresnel="Metal", spec1_fresnel_refl=(0.9, 0.9, 0.9))
+    for k, sid in enumerate(range(5, 13)):
+        if k % 2 == 0:
+            extra = dict(spec1_colour=(1.0, 1.0, 1.0), spec1_strength=0.4, spec1_roughness=0.0, ior=1.5)
+            sh[sid] = dict(sh[sid], **extra)
+    return sc
