@@ -162,3 +162,34 @@ def test_every_tuning_is_bit_exact(ctx, orc, tuning):
                           what=f"motion tuning={tuning}")
     finally:
         ctx.set_tuning(13, 0, 0, 0, 4)
+
+
+@pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (1, 0, 0, 0, 0), (5, 0, 0, 0, 8), (0, 0, 0, 4, 4),
+                                    (13, 0, 0, 0, 2, 5)])
+def test_two_level_scene_every_tuning(ctx, orc, tuning):
+    """The static two-level scene traced by the while-while scene kernel (with
+    and without ray reordering, several tail cutoffs) and by the single-loop
+    kernel: all bit-exact with the oracle, closest and any hit."""
+    rng = np.random.default_rng(77)
+    ms = []
+    for i in range(30):
+        n = int(rng.integers(1, 8000))
+        v, ip = scenes.triangle_soup(n, 700 + i, edge=0.01)
+        off = rng.uniform(-1, 1, 3).astype(np.float32)
+        ms.append(((v * 0.6 + off).astype(np.float32), ip))
+    oms = [orc.Mesh(v, ip) for v, ip in ms]
+    osc = orc.Scene(oms)
+    ids = [ctx.mesh_build(v, ip) for v, ip in ms]
+    ctx.scene_build(ids)
+    rays = np.concatenate([scenes.incoherent_rays(70000, 78, lo=-1.5, hi=1.5),
+                           scenes.coherent_rays(200, eye=(0.0, 0.0, -3.0), target=(0.0, 0.0, 0.0))])
+    try:
+        ctx.set_tuning(*tuning)
+        for shadow in (False, True):
+            got = ctx.trace_scene(rays, shadow=shadow)
+            ref = osc.trace(rays, shadow=shadow)
+            ref["geom"] = np.where(ref["geom"] >= 0, np.asarray(ids, np.int32)[np.maximum(ref["geom"], 0)], -1)
+            assert_hits_equal(got, ref, keys=("prim", "geom", "t", "u", "v", "w"),
+                              what=f"scene tuning={tuning} shadow={shadow}")
+    finally:
+        ctx.set_tuning(13, 0, 0, 0, 4)

@@ -209,6 +209,18 @@ int refresh_top(vmr_ctx* ctx) {
   d.geom_order = t.order.as<uint32_t>();
   d.meshes = t.meshes.as<DMesh>();
   d.n_geoms = (uint32_t)t.host.geom_order.size();
+  d.all_static = d.keys == 1 ? 1u : 0u;
+  for (int k = 0; k < 3; ++k) {
+    t.bounds6[k] = INFINITY;
+    t.bounds6[3 + k] = -INFINITY;
+  }
+  for (uint32_t g : t.host.geom_order) {
+    if (ctx->meshes[g]->host.motion()) d.all_static = 0u;
+    for (int k = 0; k < 3; ++k) {
+      t.bounds6[k] = std::min(t.bounds6[k], ctx->meshes[g]->bounds6[k]);
+      t.bounds6[3 + k] = std::max(t.bounds6[3 + k], ctx->meshes[g]->bounds6[3 + k]);
+    }
+  }
   t.dtop = d;
   t.valid = !t.host.geom_order.empty();
   return VMR_OK;
@@ -249,7 +261,8 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   l.walk_tail = tn.walk_tail;
   VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-  if (mesh && (tn.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
+  const bool scene_sort = !mesh && ctx->top.dtop.all_static && !(flags & VMR_TRACE_COUNT);
+  if ((mesh || scene_sort) && (tn.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
     // Key-ordered copy of the rays (raysort.cu); hits go back through order[].
     const size_t nf = ((n + 31) / 32) * 32;
     const int nfield = r.time ? 8 : 7;
@@ -261,7 +274,7 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
     uint32_t* hist = reinterpret_cast<uint32_t*>(f + nf * nfield);
     vmr::RaySoA sorted{f, f + nf, f + 2 * nf, f + 3 * nf, f + 4 * nf, f + 5 * nf, f + 6 * nf,
                        nfield == 8 ? f + 7 * nf : nullptr};
-    const float* mb = ctx->mesh_bounds_of(mesh);
+    const float* mb = mesh ? ctx->mesh_bounds_of(mesh) : ctx->top.bounds6;
     int se = vmr::launch_ray_sort(l.rays, n, mb, tn.sort_bits ? tn.sort_bits : 4, keys, hist, order, sorted,
                                   ctx->stream);
     if (se != 0) return cuda_fail(ctx, (cudaError_t)se, "ray sort launch");

@@ -91,6 +91,7 @@ struct TopRec {
   HostTop host;
   DevBuf nodes, mnodes, mboxes, order, meshes;
   DTop dtop{};
+  float bounds6[6] = {0, 0, 0, 0, 0, 0};  // union of the geoms' bounds (ray reordering)
   bool valid = false;
 };
 

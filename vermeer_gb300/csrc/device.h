@@ -76,6 +76,9 @@ struct DTop {
   uint32_t n_mnodes;
   uint32_t n_geoms;
   uint32_t iter_cap;
+  uint32_t all_static;  // static top level and only static meshes: the
+                        // while-while scene kernel applies
+  uint32_t pad;
 };
 
 struct RaySoA {

@@ -744,6 +744,8 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool g
     l.n_dev = &b.qlen[d];
     l.scratch = scr + 2 * d;
     l.stream = st;
+    l.kernel = ctx->tuning.kernel;
+    l.walk_tail = ctx->tuning.walk_tail;
     if (launch_trace_scene(ctx->top.dtop, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
     if (guided) {
       k_pt_prep<<<grid, kPtBlock, 0, st>>>(b, d);
@@ -769,6 +771,8 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool g
       s.any_hit = 1;
       s.scratch = scr + 2 * d + 1;
       s.stream = st;
+      s.kernel = ctx->tuning.kernel;
+      s.walk_tail = ctx->tuning.walk_tail;
       if (launch_trace_scene(ctx->top.dtop, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
       k_pt_resolve<<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());

@@ -951,6 +951,269 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
 }
 
 // ------------------------------------------------------------------------
+// While-while persistent kernel for a static two-level scene.
+//
+// As k_trace_mesh_ww, with the lane's current entry in either the top level
+// (geom < 0) or the mesh it entered at a top-level leaf.  A top-level leaf
+// enters its geoms one after the other (Scene.TraceElems, scene.go:61-97):
+// the mesh traversal starts one slot above the top-level entries on the
+// same stack with its root at T = Tclosest (Traversal.StackTop = stackTop+1,
+// intersect.go:226) and ends when its part of the stack is empty, after
+// which the next geom of the leaf, or the top level, continues.  Node
+// visits, pops, culls and triangle tests per ray are the reference's.
+template <bool ANY>
+__global__ void __launch_bounds__(128, 8)
+    k_trace_scene_ww(const DTop top, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch,
+                     const unsigned long long* n_dev, const uint32_t* order, int walk_tail) {
+  if (n_dev) {
+    const uint64_t nd = *n_dev;
+    n = nd < n ? nd : n;
+  }
+  int2 stk[kStackCapacity];
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  TRay r;
+  HitRec h{-1, -1, 0.f, 0.f, 0.f};
+  int node = -1, sp = 0;
+  float nodeT = 0.f;
+  uint64_t rid = 0;
+  uint32_t iter = 0, miter = 0;
+  bool alive = false, hit = false, more = true;
+  int status = kStatusOk;
+  // current mesh (geom >= 0) and the top-level leaf's remaining geoms
+  int geom = -1, base = 0;
+  uint32_t leaf_next = 0, leaf_left = 0;
+  const GNode* mnodes = nullptr;
+  const float4* mtris = nullptr;
+  float lower = 0.f;
+  uint32_t mcap = 0;
+  for (;;) {
+    const unsigned need = __ballot_sync(kFull, !alive);
+    if (need != 0u && more) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long b0 = 0;
+      if ((int)lane == leader) {
+        b0 = atomicAdd(&scratch->next_ray, (unsigned long long)__popc(need));
+        if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) b0 = n;
+      }
+      b0 = __shfl_sync(kFull, b0, leader);
+      if (b0 + __popc(need) >= n) more = false;
+      if (!alive) {
+        const uint64_t i = b0 + __popc(need & lanes_below);
+        if (i < n) {
+          rid = order ? (uint64_t)__ldg(order + i) : i;
+          load_ray(rays, i, r);
+          h = HitRec{-1, -1, 0.f, 0.f, 0.f};
+          hit = false;
+          node = 0;  // the top-level root, pushed with T = Tclosest
+          nodeT = r.tclosest;
+          sp = 0;
+          iter = 0;
+          geom = -1;
+          leaf_left = 0;
+          alive = true;
+        }
+      }
+    }
+    const unsigned alive_mask = __ballot_sync(kFull, alive);
+    if (alive_mask == 0u) {
+      if (!more) break;
+      continue;
+    }
+    if (alive) {
+      bool done = false;
+      bool walking = node != -1;
+      for (;;) {
+        const unsigned wmask = __ballot_sync(alive_mask, walking);
+        if (wmask == 0u) break;
+        if (walk_tail > 0 && __popc(wmask) <= walk_tail) {
+          const unsigned leafy = __ballot_sync(alive_mask, !walking && node < -1 && geom >= 0);
+          if (leafy != 0u) break;
+        }
+        if (!walking) continue;
+        if (geom < 0 ? ++iter > top.iter_cap : ++miter > mcap) {
+          status = kStatusIterationCap;
+          done = true;
+          walking = false;
+          continue;
+        }
+        // next entry: a pop, the next geom of the leaf, or the end
+        bool need_pop = false;
+        if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
+          need_pop = true;
+        } else if (node >= 0) {
+          const GNode* nb = geom < 0 ? top.nodes : mnodes;
+          float4 b[6];
+          int4 ch;
+          unsigned rk;
+          const float4* np = reinterpret_cast<const float4*>(nb + node);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) b[k] = __ldg(np + k);
+          ch = __ldg(reinterpret_cast<const int4*>(np + 6));
+          const uint4 meta = __ldg(reinterpret_cast<const uint4*>(np + 7));
+          rk = (((r.oct & 4u) ? meta.z : meta.y) >> ((r.oct & 3u) * 8u)) & 0xffu;
+          float tn[4];
+          unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
+          if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
+          if (ch.y == kEmptyChild || r.tclosest < tn[1]) mask &= ~2u;
+          if (ch.z == kEmptyChild || r.tclosest < tn[2]) mask &= ~4u;
+          if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
+          int next = 0;
+          float nextT = 0.f;
+          if (push_ranked(stk, sp, mask, ch, tn, rk, next, nextT, status)) {
+            node = next;
+            nodeT = nextT;
+            continue;
+          }
+          if (status != kStatusOk) {
+            done = true;
+            walking = false;
+            continue;
+          }
+          need_pop = true;
+        } else if (node == kEmptyChild) {
+          need_pop = true;
+        } else if (geom >= 0) {  // a mesh leaf: the leaf phase scans it
+          walking = false;
+          continue;
+        } else {  // a top-level leaf: its geoms, in order
+          uint32_t first, count;
+          leaf_decode(node, first, count);
+          leaf_next = first;
+          leaf_left = count;
+          need_pop = true;  // handled below: enter the first geom
+        }
+        // pop / enter the next geom / leave a finished mesh
+        for (;;) {
+          if (geom >= 0 && sp > base) {  // the mesh's own entries
+            const int2 e = stk[--sp];
+            node = e.x;
+            nodeT = __int_as_float(e.y);
+            break;
+          }
+          if (geom >= 0) {  // the mesh traversal is done
+            geom = -1;
+            sp = base - 1;
+          }
+          if (leaf_left > 0) {  // enter the next geom of the top-level leaf
+            const uint32_t g = __ldg(top.geom_order + leaf_next);
+            ++leaf_next;
+            --leaf_left;
+            const DMesh& M = top.meshes[g];
+            if (M.n_tris == 0) continue;
+            base = sp + 1;
+            if (base >= kStackCapacity) {
+              status = kStatusStackOverflow;
+              break;
+            }
+            geom = (int)g;
+            mnodes = M.nodes;
+            mtris = reinterpret_cast<const float4*>(M.tris);
+            lower = M.lower_static;
+            mcap = M.iter_cap;
+            miter = 0;
+            sp = base;
+            node = 0;
+            nodeT = r.tclosest;
+            break;
+          }
+          if (hit && ANY) {  // shadow rays stop after the leaf that hit (intersect.go:231-236)
+            node = -1;
+            break;
+          }
+          if (sp == 0) {
+            node = -1;
+            break;
+          }
+          const int2 e = stk[--sp];
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+          break;
+        }
+        if (status != kStatusOk) {
+          done = true;
+          walking = false;
+          continue;
+        }
+        (void)need_pop;
+        if (node == -1) walking = false;
+      }
+      // ---- leaf phase: a mesh leaf, scanned in the reference's order
+      if (!done && !walking && node < -1 && geom >= 0) {
+        uint32_t first, count;
+        leaf_decode(node, first, count);
+        float U = 0.f, V = 0.f, W = 0.f;
+        DMesh M;
+        M.lower_static = lower;
+        const int32_t idx = leaf_scan_dispatch<false>(M, r, first, count, mtris, mtris, 0.f, 1.f, U, V, W);
+        if (idx != -1) {
+          h.elem = idx;
+          h.geom = geom;
+          h.u = U;
+          h.v = V;
+          h.w = W;
+          hit = true;
+        }
+        if (ANY && idx != -1) {
+          done = true;
+        } else {
+          // the rest of the mesh, then the leaf's next geom or the top level
+          for (;;) {
+            if (sp > base) {
+              const int2 e = stk[--sp];
+              node = e.x;
+              nodeT = __int_as_float(e.y);
+              break;
+            }
+            geom = -1;
+            sp = base - 1;
+            if (leaf_left > 0) {
+              const uint32_t g = __ldg(top.geom_order + leaf_next);
+              ++leaf_next;
+              --leaf_left;
+              const DMesh& MM = top.meshes[g];
+              if (MM.n_tris == 0) continue;
+              base = sp + 1;
+              geom = (int)g;
+              mnodes = MM.nodes;
+              mtris = reinterpret_cast<const float4*>(MM.tris);
+              lower = MM.lower_static;
+              mcap = MM.iter_cap;
+              miter = 0;
+              sp = base;
+              node = 0;
+              nodeT = r.tclosest;
+              break;
+            }
+            if (hit && ANY) {
+              node = -1;
+              break;
+            }
+            if (sp == 0) {
+              node = -1;
+              break;
+            }
+            const int2 e = stk[--sp];
+            node = e.x;
+            nodeT = __int_as_float(e.y);
+            break;
+          }
+        }
+      }
+      if (!walking && node == -1) done = true;
+      if (done) {
+        store_hit(hits, rid, r, hit, h);
+        alive = false;
+        if (status != kStatusOk) {
+          atomicMax(&scratch->status, status);
+          status = kStatusOk;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
 // Step-scheduled persistent kernel.  Each lane is IDLE, at an inner-node
 // entry (NODE) or inside a leaf (LEAF, next triangle ti of [ti, tend)).  A
 // step runs ONE node visit for the NODE lanes or ONE triangle test for the
@@ -1190,6 +1453,12 @@ int launch_mesh_m(const DMesh& mesh, const TraceLaunch& l) {
 
 template <bool ANY, bool COUNT>
 int launch_scene_t(const DTop& top, const TraceLaunch& l) {
+  if (!COUNT && top.all_static && (l.kernel & kKernelWhileWhile)) {
+    auto k = k_trace_scene_ww<ANY>;
+    const int grid = persistent_grid(k, 128, l.grid);
+    k<<<grid, 128, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order, l.walk_tail);
+    return (int)cudaGetLastError();
+  }
   auto k = k_trace_scene<ANY, COUNT>;
   const int block = 128;
   const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
