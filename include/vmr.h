@@ -147,6 +147,12 @@ typedef struct {
     const uint8_t* shader_idx;    /* optional, per face in leaf order */
 } vmr_mesh_desc;
 
+/* An analytic sphere geom (builtin/geom/sphere: Sphere.Trace with
+ * raySphereIntersect; hit attributes N = normalize(P - centre), Poffset =
+ * 0.001 N).  It joins scenes and renders like a mesh (its shader is the
+ * first of vmr_mesh_set_shading's list); vmr_trace_mesh does not take it. */
+int vmr_sphere_add(vmr_ctx* ctx, const float center[3], float radius, uint32_t* out_geom);
+
 /* Build the mesh's QBVH on the host exactly as PolyMesh.initAccel does
  * (binned SAH, qbvh/build.go:28-307, leafMax 16) and upload it. */
 int vmr_mesh_build(vmr_ctx* ctx, const vmr_mesh_input* in, uint32_t* out_geom);
@@ -284,7 +290,7 @@ typedef struct {
 
 /* DiskLight (builtin/light/disk.go:18-31): a disk of the given radius at P
  * facing LookAt; geom is its emissive fan mesh (Disk.createMesh, 20 segments
- * by default).  Lights are used in the order TriLights, DiskLights. */
+ * by default). */
 typedef struct {
     float P[3], up[3], lookat[3];
     float radius;
@@ -292,6 +298,18 @@ typedef struct {
     uint32_t shader;
     uint32_t geom;
 } vmr_disk_light;
+
+/* SphereLight (builtin/light/sphere.go:14-28): cone sampling toward the
+ * sphere (pdf q_2 of Shirley et al. 1996); geom is its sphere geom
+ * (vmr_sphere_add).  Lights are used in the order TriLights, DiskLights,
+ * SphereLights. */
+typedef struct {
+    float P[3];
+    float radius;
+    int samples;
+    uint32_t shader;
+    uint32_t geom;
+} vmr_sphere_light;
 
 /* Camera (builtin/camera/camera.go): m = LocalToWorld, column-major;
  * tan_theta_focal = tan(fov/2) * focal; radius > 0 is a thin lens sampled
@@ -323,6 +341,7 @@ int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, u
                          const float* normals);
 int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n);
 int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n);
+int vmr_set_sphere_lights(vmr_ctx* ctx, const vmr_sphere_light* lights, uint32_t n);
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* camera);
 /* core.Render in reference mode (core/render.go:140-218 with ShaderStd's
  * direct lighting): iterations iter_begin..iter_begin+iter_count-1 of every

@@ -150,7 +150,19 @@ typedef struct {
     uint32_t shader, mesh;
 } orc_disklight;
 
+/* SphereLight (builtin/light/sphere.go:14-28); mesh = its sphere geom. */
+typedef struct {
+    float P[3];
+    float radius;
+    int samples;
+    uint32_t shader, mesh;
+} orc_spherelight;
+
 typedef struct orc_render orc_render;
+
+/* An analytic sphere geom (builtin/geom/sphere): usable wherever a mesh is
+ * (scenes, renders); its shader is the mesh's shader 0. */
+orc_mesh* orc_sphere_create(const float center[3], float radius);
 
 /* Per-mesh shading data: shader index per face (face order, may be NULL)
  * and per-vertex normals of key 0 (may be NULL). */
@@ -165,6 +177,8 @@ orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, u
 void orc_render_destroy(orc_render* r);
 /* Append DiskLights to the light list (after the TriLights). */
 int orc_render_add_disk_lights(orc_render* r, const orc_disklight* lights, uint32_t n);
+/* Append SphereLights (after the DiskLights). */
+int orc_render_add_sphere_lights(orc_render* r, const orc_spherelight* lights, uint32_t n);
 /* Runs core.Render iterations iter_begin .. iter_begin+iter_count-1 (the
  * reference's 0-based loop variable; each renders sample iter+1 and folds
  * it into fb as buf = (buf*(iter+1) + c)/(iter+2), core/render.go:127-129).

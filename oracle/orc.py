@@ -102,6 +102,11 @@ class OrcDiskLight(ctypes.Structure):
                 ("mesh", ctypes.c_uint32)]
 
 
+class OrcSphereLight(ctypes.Structure):
+    _fields_ = [("P", ctypes.c_float * 3), ("radius", ctypes.c_float), ("samples", ctypes.c_int),
+                ("shader", ctypes.c_uint32), ("mesh", ctypes.c_uint32)]
+
+
 class OrcCamera(ctypes.Structure):
     _fields_ = [("m", ctypes.c_float * 16), ("tan_theta_focal", ctypes.c_float), ("aspect", ctypes.c_float),
                 ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
@@ -121,6 +126,10 @@ def _register_render(L):
     L.orc_render_destroy.argtypes = [P]
     L.orc_render_add_disk_lights.restype = ctypes.c_int
     L.orc_render_add_disk_lights.argtypes = [P, P, ctypes.c_uint32]
+    L.orc_render_add_sphere_lights.restype = ctypes.c_int
+    L.orc_render_add_sphere_lights.argtypes = [P, P, ctypes.c_uint32]
+    L.orc_sphere_create.restype = P
+    L.orc_sphere_create.argtypes = [P, ctypes.c_float]
     L.orc_render_run.restype = ctypes.c_int
     L.orc_render_run.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                  ctypes.c_uint64, P, ctypes.c_int]
@@ -211,6 +220,9 @@ class Render:
     def __init__(self, scene):
         self.meshes = []
         for m in scene["meshes"]:
+            if "sphere" in m:
+                self.meshes.append(Sphere(m["sphere"][:3], m["sphere"][3]))
+                continue
             om = Mesh(m["verts"], m["idxp"])
             fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
             nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
@@ -267,6 +279,15 @@ class Render:
                 darr[i].radius = float(d["radius"])
                 darr[i].samples, darr[i].shader, darr[i].mesh = int(d.get("samples", 1)), int(d["shader"]), int(d["mesh"])
             lib().orc_render_add_disk_lights(self.h, darr, len(dls))
+        sls = scene.get("sphere_lights", [])
+        if sls:
+            sarr = (OrcSphereLight * len(sls))()
+            for i, d in enumerate(sls):
+                for c in range(3):
+                    sarr[i].P[c] = float(d["P"][c])
+                sarr[i].radius = float(d["radius"])
+                sarr[i].samples, sarr[i].shader, sarr[i].mesh = int(d.get("samples", 1)), int(d["shader"]), int(d["mesh"])
+            lib().orc_render_add_sphere_lights(self.h, sarr, len(sls))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -359,6 +380,21 @@ class Mesh:
         if counters:
             out["counters"] = cnt
         return out
+
+
+class Sphere:
+    """An analytic sphere geom (builtin/geom/sphere), usable as a scene
+    member like Mesh."""
+
+    def __init__(self, center, radius):
+        c = np.ascontiguousarray(center, np.float32)
+        self.h = lib().orc_sphere_create(_ptr(c), float(radius))
+        self._keep = c
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mesh_destroy(self.h)
+            self.h = None
 
 
 class Scene:

@@ -363,9 +363,15 @@ struct Mesh {
   Box bounds;
   std::vector<uint8_t> shaderidx;  // leaf order (static) / face order (motion)
   std::vector<float> normals;      // per vertex, key 0
+  // An analytic sphere geom (builtin/geom/sphere) instead of triangles.
+  bool sphere = false;
+  float sc[3] = {0, 0, 0}, sr = 0;
 
   const float* vert(uint32_t i, int key) const { return &verts[((size_t)key * nverts + i) * 3]; }
-  int motion_keys() const { return nodes.empty() ? (int)mboxes.size() : 1; }  // polymesh.go:103-112
+  int motion_keys() const {  // polymesh.go:103-112; a sphere has one key (sphere.go:58-60)
+    if (sphere) return 1;
+    return nodes.empty() ? (int)mboxes.size() : 1;
+  }
   // PolyMesh.Bounds (builtin/geom/polymesh/bounds.go:25-53).
   Box bounds_at(float time) const {
     if (!nodes.empty() || mboxes.empty()) return bounds;
@@ -666,7 +672,46 @@ bool qbvh_trace_motion(const orc_mnode* nodes, const std::vector<std::vector<flo
 }
 
 // PolyMesh.Trace without a transform (trace.go:57-101).
+// solveQuadratic and raySphereIntersect (builtin/geom/sphere/trace.go).
+bool ray_sphere(const float Ro[3], const float Rd[3], const float P[3], float radius, float& t) {
+  const float L[3] = {Ro[0] - P[0], Ro[1] - P[1], Ro[2] - P[2]};
+  const float a = Rd[0] * Rd[0] + Rd[1] * Rd[1] + Rd[2] * Rd[2];
+  const float b = 2 * (Rd[0] * L[0] + Rd[1] * L[1] + Rd[2] * L[2]);
+  const float c = (L[0] * L[0] + L[1] * L[1] + L[2] * L[2]) - radius * radius;
+  float x0, x1;
+  const float discr = b * b - 4 * a * c;
+  if (discr < 0) return false;
+  if (discr == 0) {
+    x1 = -0.5f * b / a;
+    x0 = x1;
+  } else {
+    const float q = b > 0 ? -0.5f * (b + std::sqrt(discr)) : -0.5f * (b - std::sqrt(discr));
+    x0 = q / a;
+    x1 = c / q;
+  }
+  if (x0 > x1) std::swap(x0, x1);
+  if (x0 > x1) std::swap(x0, x1);  // raySphereIntersect orders them again
+  if (x0 < 0) {
+    x0 = x1;
+    if (x0 < 0) return false;
+  }
+  t = x0;
+  return true;
+}
+
+// Sphere.Trace (sphere/trace.go): the closest root if below Tclosest.
+bool sphere_trace(const Mesh& m, Ray& r, Task& tk) {
+  float t;
+  if (!ray_sphere(r.P, r.D, m.sc, m.sr, t)) return false;
+  if (!(t < r.Tclosest)) return false;
+  r.Tclosest = t;
+  tk.elem = 0;
+  tk.bu = tk.bv = tk.bw = 0.0f;
+  return true;
+}
+
 bool mesh_trace(const Mesh& m, Ray& r, Task& tk) {
+  if (m.sphere) return sphere_trace(m, r, tk);
   if (!m.nodes.empty()) {
     return qbvh_trace(m.nodes.data(), r, tk, [&](Ray& rr, Task& t, int b, int c) {
       return mesh_trace_elems(m, rr, t, b, c);
@@ -838,6 +883,9 @@ MeshView mesh_view(const orc_mesh* om) {
   v.shaderidx = m.shaderidx.empty() ? nullptr : m.shaderidx.data();
   v.normals = m.normals.empty() ? nullptr : m.normals.data();
   v.motion = m.keys > 1;
+  v.sphere = m.sphere;
+  for (int k = 0; k < 3; ++k) v.sc[k] = m.sc[k];
+  v.sr = m.sr;
   return v;
 }
 
@@ -874,6 +922,19 @@ void orc_mesh_destroy(orc_mesh* m) { delete m; }
 // Shading data as PolyMesh holds it after initAccel (buildqbvh.go:98-104):
 // shader indices permuted to leaf order for a static mesh, face order for a
 // motion mesh; normals indexed by vertex (NormalIdx = FaceIdx).
+orc_mesh* orc_sphere_create(const float center[3], float radius) {
+  orc_mesh* om = new orc_mesh();
+  Mesh& m = om->m;
+  m.sphere = true;
+  for (int k = 0; k < 3; ++k) {
+    m.sc[k] = center[k];
+    m.bounds.b[0][k] = center[k] - radius;  // Sphere.Bounds (sphere.go:62-72)
+    m.bounds.b[1][k] = center[k] + radius;
+  }
+  m.sr = radius;
+  return om;
+}
+
 int orc_mesh_set_shading(orc_mesh* om, const uint8_t* face_shader, const float* normals) {
   Mesh& m = om->m;
   m.shaderidx.clear();

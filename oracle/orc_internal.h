@@ -26,6 +26,8 @@ struct MeshView {
   const uint8_t* shaderidx; // indexed by ElemID, or null
   const float* normals;     // per vertex, or null
   bool motion;
+  bool sphere;              // analytic sphere geom: centre sc, radius sr
+  float sc[3], sr;
 };
 MeshView mesh_view(const orc_mesh* m);
 

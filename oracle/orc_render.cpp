@@ -524,9 +524,70 @@ struct Renderer {
     }
   }
 
+  // raySphereIntersect (builtin/light/sphere.go:96-124), the same as the geom's.
+  static bool sphere_hit(V3 Ro, V3 Rd, V3 C, float radius, float& t) {
+    const float ro[3] = {Ro.x, Ro.y, Ro.z}, rd[3] = {Rd.x, Rd.y, Rd.z}, c[3] = {C.x, C.y, C.z};
+    const float L[3] = {ro[0] - c[0], ro[1] - c[1], ro[2] - c[2]};
+    const float a = rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2];
+    const float b = 2 * (rd[0] * L[0] + rd[1] * L[1] + rd[2] * L[2]);
+    const float cc = (L[0] * L[0] + L[1] * L[1] + L[2] * L[2]) - radius * radius;
+    float x0, x1;
+    const float discr = b * b - 4 * a * cc;
+    if (discr < 0) return false;
+    if (discr == 0) {
+      x1 = -0.5f * b / a;
+      x0 = x1;
+    } else {
+      const float q = b > 0 ? -0.5f * (b + std::sqrt(discr)) : -0.5f * (b - std::sqrt(discr));
+      x0 = q / a;
+      x1 = cc / q;
+    }
+    if (x0 > x1) std::swap(x0, x1);
+    if (x0 > x1) std::swap(x0, x1);
+    if (x0 < 0) {
+      x0 = x1;
+      if (x0 < 0) return false;
+    }
+    t = x0;
+    return true;
+  }
+
+  // Sphere.SampleArea (builtin/light/sphere.go:178-254): a cone toward the
+  // sphere, pdf q_2 of Shirley et al. 1996.
+  void sample_area_sphere(const Light& L, const Ctx& sc, int n, std::vector<LightSample>& out) const {
+    const V3 V = sub(L.P, sc.P);
+    const float l = length(V);
+    const V3 w = normalize(V);
+    const V3 v = normalize(cross(w, sc.Ng));
+    const V3 u = cross(w, v);
+    for (int i = 0; i < n; ++i) {
+      const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;  // + sg.Sample, which is 0
+      const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
+      const float theta = gacos(1 - (float)r0 + (float)r0 * std::sqrt(1 - sqr(L.radius / l)));
+      const float phi = 2 * kPi * (float)r1;
+      const V3 a = v3(gcos(phi) * gsin(theta), gsin(phi) * gsin(theta), gcos(theta));
+      const V3 omega = expand(u, v, w, a);
+      if (dot(omega, sc.Ng) < 0) continue;
+      float t;
+      if (!sphere_hit(sc.P, omega, L.P, L.radius, t)) continue;
+      const V3 x = add(sc.P, scale(t, omega));
+      const V3 D = sub(x, sc.P);
+      LightSample ls;
+      ls.Ldist = length(D);
+      ls.Ld = normalize(D);
+      ls.Liu = light_liu(L, sc);
+      ls.pdf = 1 / (2 * kPi * (1 - std::sqrt(1 - sqr(L.radius / l))));
+      out.push_back(ls);
+    }
+  }
+
   void sample_area(const Light& LL, const Ctx& sc, int n, std::vector<LightSample>& out) const {
     if (LL.kind == 1) {
       sample_area_disk(LL, sc, n, out);
+      return;
+    }
+    if (LL.kind == 2) {
+      sample_area_sphere(LL, sc, n, out);
       return;
     }
     const orc_trilight& L = LL.tri;
@@ -583,8 +644,24 @@ struct Renderer {
   }
 
   // Tri.ValidSample (triangle.go:136-230).
+  // Sphere.ValidSample (builtin/light/sphere.go:126-176).
+  bool valid_sample_sphere(const Light& L, const Ctx& sc, BsdfSample& s) const {
+    float t;
+    if (!sphere_hit(sc.P, s.D, L.P, L.radius, t)) return false;
+    const V3 x = add(sc.P, scale(t, s.D));
+    const V3 D = sub(x, sc.P);
+    s.Ldist = length(D);
+    s.Ld = normalize(D);
+    s.Liu = light_liu(L, sc);
+    const V3 V = sub(L.P, sc.P);
+    const float l = length(V);
+    s.pdf_light = 1 / (2 * kPi * (1 - std::sqrt(1 - sqr(L.radius / l))));
+    return true;
+  }
+
   bool valid_sample(const Light& LL, const Ctx& sc, BsdfSample& s) const {
     if (LL.kind == 1) return valid_sample_disk(LL, sc, s);
+    if (LL.kind == 2) return valid_sample_sphere(LL, sc, s);
     const orc_trilight& L = LL.tri;
     const V3 p0 = v3(L.p0[0], L.p0[1], L.p0[2]), p1 = v3(L.p1[0], L.p1[1], L.p1[2]), p2 = v3(L.p2[0], L.p2[1], L.p2[2]);
     V3 P;
@@ -677,10 +754,26 @@ struct Renderer {
     return col;
   }
 
-  // Hit attributes for a static mesh (trace.go:276-515) followed by
-  // ShaderContext.ApplyTransform with the identity (core/shader.go:129-135).
-  bool hit_context(const Hit& h, Ctx& sc) const {
+  // Hit attributes for a static mesh (trace.go:276-515) or an analytic sphere
+  // (sphere/trace.go), followed by ShaderContext.ApplyTransform with the
+  // identity (core/shader.go:129-135).
+  bool hit_context(const Hit& h, Ctx& sc, V3 Ro, V3 Rd) const {
     const orc_internal::MeshView& m = R.meshes[h.geom];
+    if (m.sphere) {
+      const auto& list = R.mesh_shaders[h.geom];
+      if (list.empty()) return false;
+      sc.shader = &R.shaders[list[0]];
+      const V3 P = add(Ro, scale(h.t, Rd));  // Vec3Mad(ray.P, ray.D, t)
+      const V3 N = normalize(sub(P, v3(m.sc[0], m.sc[1], m.sc[2])));
+      sc.Poffset = scale(0.001f, N);
+      sc.P = P;
+      sc.N = normalize(N);
+      sc.Ng = normalize(N);
+      sc.DdPdu = normalize(v3(1, 0, 0));
+      sc.DdPdv = normalize(v3(0, 0, 1));
+      sc.geom = h.geom;
+      return true;
+    }
     const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
     auto vert = [&](uint32_t i) { return v3(m.verts[i * 3], m.verts[i * 3 + 1], m.verts[i * 3 + 2]); };
     const V3 V0 = vert(i0), V1 = vert(i1), V2 = vert(i2);
@@ -726,7 +819,7 @@ struct Renderer {
     Ctx sc = parent;
     sc.level = level;
     sc.Rd = D;
-    if (!hit_context(h, sc)) return false;
+    if (!hit_context(h, sc, P, D)) return false;
     out = shade(sc);
     return true;
   }
@@ -959,6 +1052,20 @@ int orc_render_add_disk_lights(orc_render* o, const orc_disklight* lights, uint3
     L.samples = d.samples;
     L.shader = d.shader;
     L.mesh = d.mesh;
+    o->r.lights.push_back(L);
+  }
+  return 0;
+}
+
+int orc_render_add_sphere_lights(orc_render* o, const orc_spherelight* lights, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) {
+    Light L{};
+    L.kind = 2;
+    L.P = v3(lights[i].P[0], lights[i].P[1], lights[i].P[2]);
+    L.radius = lights[i].radius;
+    L.samples = lights[i].samples;
+    L.shader = lights[i].shader;
+    L.mesh = lights[i].mesh;
     o->r.lights.push_back(L);
   }
   return 0;

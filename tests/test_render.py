@@ -165,3 +165,23 @@ def test_render_mirror_recursion_matches_oracle(ctx, orc, samples):
     frac, mean_abs = _compare(got, ref)
     assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)
     assert st["camera_rays"] == 48 * 48 * 3
+
+
+# ------------------------------------------- sphere geoms and SphereLight ----
+def test_oracle_sphere_room_sane(orc):
+    sc = scenes.small_room_spheres(2048, seed=8)
+    fb = orc.Render(sc).run(32, 32, 0, 4, 5)
+    assert np.isfinite(fb).all() and (fb >= 0).all() and fb.mean() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("samples", [0, 1])
+def test_render_spheres_match_oracle(ctx, orc, samples):
+    """Analytic sphere geoms (Lambert, GGX, mirror) and a SphereLight (cone
+    sampling, ValidSample) next to the TriLights."""
+    sc = scenes.small_room_spheres(2048, seed=8, light_samples=samples)
+    ctx.load_scene(sc)
+    ref = orc.Render(sc).run(48, 48, 0, 3, 17)
+    got, _ = ctx.render(48, 48, 0, 3, 17)
+    frac, mean_abs = _compare(got, ref)
+    assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)

@@ -193,3 +193,37 @@ def test_two_level_scene_every_tuning(ctx, orc, tuning):
                               what=f"scene tuning={tuning} shadow={shadow}")
     finally:
         ctx.set_tuning(13, 0, 0, 0, 4)
+
+
+
+@pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (0, 0, 0, 4, 4)])
+def test_scene_with_sphere_geoms(ctx, orc, tuning):
+    """Analytic sphere geoms among triangle meshes (Sphere.Trace: the nearer
+    non-negative root below Tclosest), in both scene kernels."""
+    rng = np.random.default_rng(91)
+    ms, oms, ids = [], [], []
+    for i in range(12):
+        v, ip = scenes.triangle_soup(int(rng.integers(100, 3000)), 900 + i, edge=0.01)
+        off = rng.uniform(-1, 1, 3).astype(np.float32)
+        v = (v * 0.6 + off).astype(np.float32)
+        oms.append(orc.Mesh(v, ip))
+        ids.append(ctx.mesh_build(v, ip))
+    for i in range(8):
+        c = rng.uniform(-1, 1, 3).astype(np.float32)
+        r = float(rng.uniform(0.05, 0.4))
+        oms.append(orc.Sphere(c, r))
+        ids.append(ctx.sphere_add(c, r))
+    osc = orc.Scene(oms)
+    ctx.scene_build(ids)
+    rays = np.concatenate([scenes.incoherent_rays(70000, 92, lo=-1.5, hi=1.5),
+                           scenes.incoherent_rays(20000, 93, lo=-0.2, hi=0.2)])
+    try:
+        ctx.set_tuning(*tuning)
+        for shadow in (False, True):
+            got = ctx.trace_scene(rays, shadow=shadow)
+            ref = osc.trace(rays, shadow=shadow)
+            ref["geom"] = np.where(ref["geom"] >= 0, np.asarray(ids, np.int32)[np.maximum(ref["geom"], 0)], -1)
+            assert_hits_equal(got, ref, keys=("prim", "geom", "t", "u", "v", "w"), what=f"spheres shadow={shadow}")
+        assert (got["geom"] >= ids[12]).any()  # some rays end on spheres
+    finally:
+        ctx.set_tuning(13, 0, 0, 0, 4)

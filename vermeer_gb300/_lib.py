@@ -77,6 +77,11 @@ class DiskLight(ctypes.Structure):
                 ("radius", ctypes.c_float), ("samples", ctypes.c_int), ("shader", U32), ("geom", U32)]
 
 
+class SphereLight(ctypes.Structure):
+    _fields_ = [("P", ctypes.c_float * 3), ("radius", ctypes.c_float), ("samples", ctypes.c_int), ("shader", U32),
+                ("geom", U32)]
+
+
 class Camera(ctypes.Structure):
     _fields_ = [("m", ctypes.c_float * 16), ("tan_theta_focal", ctypes.c_float), ("aspect", ctypes.c_float),
                 ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
@@ -152,6 +157,8 @@ SIGNATURES = {
     "vmr_mesh_set_shading": (ctypes.c_int, [P, U32, P, U32, P]),
     "vmr_set_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_disk_lights": (ctypes.c_int, [P, P, U32]),
+    "vmr_set_sphere_lights": (ctypes.c_int, [P, P, U32]),
+    "vmr_sphere_add": (ctypes.c_int, [P, P, ctypes.c_float, ctypes.POINTER(U32)]),
     "vmr_set_camera": (ctypes.c_int, [P, ctypes.POINTER(Camera)]),
     "vmr_render": (ctypes.c_int, [P, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
     "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),

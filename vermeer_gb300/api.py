@@ -267,6 +267,23 @@ class Context:
             arr[i].samples, arr[i].shader, arr[i].geom = int(d.get("samples", 1)), int(d["shader"]), int(d["geom"])
         self._check(self.L.vmr_set_lights(self.h, arr, len(lights)))
 
+    def sphere_add(self, center, radius: float) -> int:
+        """An analytic sphere geom (vmr_sphere_add); returns its geom id."""
+        c = (ctypes.c_float * 3)(*[float(x) for x in center])
+        g = ctypes.c_uint32()
+        self._check(self.L.vmr_sphere_add(self.h, c, float(radius), ctypes.byref(g)))
+        return g.value
+
+    def set_sphere_lights(self, lights):
+        """SphereLights: dicts with P, radius, samples, shader, geom."""
+        arr = (_lib.SphereLight * len(lights))()
+        for i, d in enumerate(lights):
+            for c in range(3):
+                arr[i].P[c] = float(d["P"][c])
+            arr[i].radius = float(d["radius"])
+            arr[i].samples, arr[i].shader, arr[i].geom = int(d.get("samples", 1)), int(d["shader"]), int(d["geom"])
+        self._check(self.L.vmr_set_sphere_lights(self.h, arr, len(lights)))
+
     def set_disk_lights(self, lights):
         """DiskLights: dicts with P, up, lookat, radius, samples, shader, geom."""
         arr = (_lib.DiskLight * len(lights))()
@@ -383,7 +400,10 @@ class Context:
         Returns the geom ids."""
         ids = []
         for m in scene["meshes"]:
-            g = self.mesh_build(m["verts"], m["idxp"], shader_idx=m.get("face_shader"))
+            if "sphere" in m:  # an analytic sphere geom: (cx, cy, cz, radius)
+                g = self.sphere_add(m["sphere"][:3], m["sphere"][3])
+            else:
+                g = self.mesh_build(m["verts"], m["idxp"], shader_idx=m.get("face_shader"))
             ids.append(g)
         self.scene_build(ids)
         self.set_shaders(scene["shaders"])
@@ -391,6 +411,7 @@ class Context:
             self.mesh_set_shading(g, m["shaders"], m.get("normals"))
         self.set_lights([dict(l, geom=ids[l["mesh"]]) for l in scene["lights"]])
         self.set_disk_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("disk_lights", [])])
+        self.set_sphere_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("sphere_lights", [])])
         self.set_quad_lights([dict(q, geom=ids[q["mesh"]]) for q in scene.get("quad_lights", [])])
         self.set_env_light(scene.get("env", (0.0, 0.0, 0.0)))
         self.set_camera(scene["camera"])

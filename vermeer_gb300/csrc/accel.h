@@ -32,6 +32,8 @@ struct HostMesh {
   std::vector<Bounds> key_bounds;    // PolyMesh.motionBounds (motion only)
   Bounds bounds{};                   // PolyMesh.bounds
   std::vector<uint8_t> shader_idx;   // leaf order (static) / face order (motion)
+  bool sphere = false;               // an analytic sphere geom (centre, radius)
+  float sphere_c[3] = {0, 0, 0}, sphere_r = 0;
 
   bool motion() const { return keys > 1; }
   int motion_keys() const { return motion() ? (int)keys : 1; }

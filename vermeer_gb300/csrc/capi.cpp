@@ -462,6 +462,31 @@ int vmr_mesh_build(vmr_ctx* ctx, const vmr_mesh_input* in, uint32_t* out_geom) {
   return VMR_OK;
 }
 
+int vmr_sphere_add(vmr_ctx* ctx, const float center[3], float radius, uint32_t* out_geom) {
+  if (!ctx || !center) return VMR_ERR_INVALID;
+  if (!(radius > 0.0f) || std::isinf(radius)) return fail(ctx, VMR_ERR_INVALID, "sphere radius must be positive");
+  auto rec = std::make_unique<MeshRec>();
+  HostMesh& m = rec->host;
+  m.sphere = true;
+  for (int k = 0; k < 3; ++k) {
+    m.sphere_c[k] = center[k];
+    m.bounds.lo[k] = center[k] - radius;  // Sphere.Bounds (builtin/geom/sphere/sphere.go:62-72)
+    m.bounds.hi[k] = center[k] + radius;
+    rec->bounds6[k] = m.bounds.lo[k];
+    rec->bounds6[3 + k] = m.bounds.hi[k];
+  }
+  m.sphere_r = radius;
+  DMesh& d = rec->dmesh;
+  d = DMesh{};
+  d.keys = 1;
+  d.kind = 1;
+  for (int k = 0; k < 3; ++k) d.sphere[k] = center[k];
+  d.sphere[3] = radius;
+  if (out_geom) *out_geom = (uint32_t)ctx->meshes.size();
+  ctx->meshes.push_back(std::move(rec));
+  return VMR_OK;
+}
+
 int vmr_mesh_upload(vmr_ctx* ctx, const vmr_mesh_desc* d, uint32_t* out_geom) {
   if (!ctx || !d) return VMR_ERR_INVALID;
   if (d->motion_keys < 1 || (d->n_tris && (!d->verts || !d->idxp || !d->accel_idx)))
@@ -602,6 +627,8 @@ int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, 
   if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
   cudaSetDevice(ctx->device);
   const DMesh* m = &ctx->meshes[geom]->dmesh;
+  if (ctx->meshes[geom]->host.sphere)
+    return fail(ctx, VMR_ERR_UNSUPPORTED, "a sphere geom is traced through the scene (vmr_trace_scene)");
   if (ctx->meshes[geom]->host.n_tris == 0) return fail(ctx, VMR_ERR_INVALID, "empty mesh");
   if (flags & VMR_TRACE_DEVICE) return run_trace(ctx, m, *rays, n, flags, *hits, stats);
   return trace_host(ctx, m, rays, n, flags, hits, stats);

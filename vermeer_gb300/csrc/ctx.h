@@ -64,6 +64,7 @@ struct RenderState {
   std::vector<vmr_shader_std> shaders;
   std::vector<vmr_tri_light> lights;
   std::vector<vmr_disk_light> disks;
+  std::vector<vmr_sphere_light> spheres;
   std::vector<vmr_quad_light> quads;
   float env[3] = {0.f, 0.f, 0.f};
   vmr_camera camera{};

@@ -61,7 +61,9 @@ struct DMesh {
   float lower_static;       // EpsilonFloat32 + RayBias (trace.go:182)
   float ray_bias;           // motion lower bound (trace.go:612)
   uint32_t iter_cap;        // 4 * nodes + 2: a traversal pops each entry once
-  uint32_t pad[2];
+  uint32_t kind;            // 0 triangles, 1 analytic sphere (builtin/geom/sphere)
+  float sphere[4];          // centre, radius
+  uint32_t pad[3];
 };
 
 // Top level of a scene (builtin/scene): static GNodes or motion MNodes with

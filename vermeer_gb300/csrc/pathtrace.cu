@@ -339,7 +339,9 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
     if (prim >= 0) {
       Ctx sc;
       uint32_t shid = 0;
-      if (hit_attributes(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], sc, shid)) {
+      const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
+      const V3 Rd = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
+      if (surface_attributes(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i], sc, shid)) {
         wi = v3(-q[3 * (size_t)b.cap + i], -q[4 * (size_t)b.cap + i], -q[5 * (size_t)b.cap + i]);
         P = sc.P;
         N = dot(sc.Ng, wi) > 0.0f ? sc.N : v3(-sc.N.x, -sc.N.y, -sc.N.z);
@@ -407,7 +409,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
         const int32_t geom = b.hgeom[i];
         Ctx sc;
         uint32_t shid = 0;
-        if (hit_attributes(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], sc, shid)) {
+        const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
+        if (surface_attributes(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], sc, shid)) {
           const vmr_shader_std& sh = b.shaders[shid];
           const V3 wi = v3(-D.x, -D.y, -D.z);
           const bool front = dot(sc.Ng, wi) > 0.0f;
@@ -879,6 +882,9 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     rm[g].sidx = mr.host.shader_idx.empty() ? nullptr : mr.sidx.as<uint8_t>();
     rm[g].shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
     rm[g].n_shaders = (uint32_t)mr.shader_list.size();
+    rm[g].kind = mr.host.sphere ? 1u : 0u;
+    for (int k = 0; k < 3; ++k) rm[g].sphere[k] = mr.host.sphere_c[k];
+    rm[g].sphere[3] = mr.host.sphere_r;
   }
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;

@@ -64,9 +64,64 @@ __device__ Cand disk_sample(const RLight& L, const Ctx& sc, int n, int i) {
   return c;
 }
 
+// raySphereIntersect (builtin/light/sphere.go:96-124).
+__device__ bool light_sphere_hit(V3 Ro, V3 Rd, V3 C, float radius, float& t) {
+  const V3 Lv = sub(Ro, C);
+  const float a = dot(Rd, Rd);
+  const float b = 2 * dot(Rd, Lv);
+  const float c = dot(Lv, Lv) - radius * radius;
+  const float discr = b * b - 4 * a * c;
+  if (discr < 0) return false;
+  float x0, x1;
+  if (discr == 0) {
+    x1 = -0.5f * b / a;
+    x0 = x1;
+  } else {
+    const float q = b > 0 ? -0.5f * (b + sqrtf(discr)) : -0.5f * (b - sqrtf(discr));
+    x0 = q / a;
+    x1 = c / q;
+  }
+  if (x0 > x1) { const float tt = x0; x0 = x1; x1 = tt; }
+  if (x0 > x1) { const float tt = x0; x0 = x1; x1 = tt; }
+  if (x0 < 0) {
+    x0 = x1;
+    if (x0 < 0) return false;
+  }
+  t = x0;
+  return true;
+}
+
+// Sphere.SampleArea, sample i of n (builtin/light/sphere.go:178-254).
+__device__ Cand sphere_sample(const RLight& L, const Ctx& sc, int n, int i) {
+  Cand c{};
+  const V3 C = v3(L.P[0], L.P[1], L.P[2]);
+  const V3 V = sub(C, sc.P);
+  const float l = length(V);
+  const V3 w = normalize(V);
+  const V3 v = normalize(cross(w, sc.Ng));
+  const V3 u = cross(w, v);
+  const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;
+  const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
+  const float theta = gacos(1 - (float)r0 + (float)r0 * sqrtf(1 - sqr(L.radius / l)));
+  const float phi = 2 * kPi * (float)r1;
+  const V3 a = v3(gcos(phi) * gsin(theta), gsin(phi) * gsin(theta), gcos(theta));
+  const V3 omega = expand(u, v, w, a);
+  if (dot(omega, sc.Ng) < 0) return c;
+  float t;
+  if (!light_sphere_hit(sc.P, omega, C, L.radius, t)) return c;
+  const V3 x = add(sc.P, scale(t, omega));
+  const V3 D = sub(x, sc.P);
+  c.Ldist = length(D);
+  c.Ld = normalize(D);
+  c.pdf_own = 1 / (2 * kPi * (1 - sqrtf(1 - sqr(L.radius / l))));
+  c.ok = true;
+  return c;
+}
+
 // Tri.SampleArea, sample i of n (triangle.go:232-343).
 __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
   if (L.kind == 1) return disk_sample(L, sc, n, i);
+  if (L.kind == 2) return sphere_sample(L, sc, n, i);
   Cand c{};
   const V3 p0 = lp(L, 0), p1 = lp(L, 1), p2 = lp(L, 2);
   const V3 N = normalize(cross(sub(p1, p0), sub(p2, p0)));
@@ -107,6 +162,19 @@ __device__ Cand bsdf_candidate(const RLight& L, const Ctx& sc, const Bsdf& bsdf,
   const V3 D = normalize(bsdf_sample(bsdf, r0, r1));
   c.pdf_bsdf = bsdf_pdf(bsdf, D);
   if (c.pdf_bsdf <= 0) return c;
+  if (L.kind == 2) {  // Sphere.ValidSample (sphere.go:126-176)
+    const V3 C = v3(L.P[0], L.P[1], L.P[2]);
+    float t;
+    if (!light_sphere_hit(sc.P, D, C, L.radius, t)) return c;
+    const V3 x = add(sc.P, scale(t, D));
+    const V3 Dl = sub(x, sc.P);
+    c.Ldist = length(Dl);
+    c.Ld = normalize(Dl);
+    const float l = length(sub(C, sc.P));
+    c.pdf_light = 1 / (2 * kPi * (1 - sqrtf(1 - sqr(L.radius / l))));
+    c.ok = true;
+    return c;
+  }
   if (L.kind == 1) {
     const double pdf = (double)(1.0f / (kPi * L.radius * L.radius));
     const V3 LP = v3(L.P[0], L.P[1], L.P[2]), LN = v3(L.N[0], L.N[1], L.N[2]);
@@ -331,8 +399,10 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
     Ctx sc;
     uint32_t shid;
     const float* hf = reinterpret_cast<const float*>(lv.hit);
-    if (!hit_attributes(m, prim, hf[3 * (size_t)lv.cap + e], hf[4 * (size_t)lv.cap + e], hf[5 * (size_t)lv.cap + e],
-                        sc, shid))
+    const V3 Ro = v3(*ray_f(lv, 0, e), *ray_f(lv, 1, e), *ray_f(lv, 2, e));
+    const V3 Rdir = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
+    if (!surface_attributes(m, prim, hf[3 * (size_t)lv.cap + e], hf[4 * (size_t)lv.cap + e],
+                            hf[5 * (size_t)lv.cap + e], Ro, Rdir, hf[2 * (size_t)lv.cap + e], sc, shid))
       continue;
     const vmr_shader_std& sh = b.shaders[shid];
     sc.Rd = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
@@ -649,6 +719,17 @@ int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n) 
   return VMR_OK;
 }
 
+int vmr_set_sphere_lights(vmr_ctx* ctx, const vmr_sphere_light* lights, uint32_t n) {
+  if (!ctx || (n && !lights)) return VMR_ERR_INVALID;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (lights[i].samples < 0 || (1 << lights[i].samples) > 2 * vmr::kMaxHalf)
+      return rfail(ctx, VMR_ERR_UNSUPPORTED, "SphereLight samples must be in [0, 4]");
+    if (!(lights[i].radius > 0.0f)) return rfail(ctx, VMR_ERR_INVALID, "SphereLight radius must be positive");
+  }
+  ctx->render.spheres.assign(lights, lights + n);
+  return VMR_OK;
+}
+
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* cam) {
   if (!ctx || !cam) return VMR_ERR_INVALID;
   if (!(cam->radius >= 0.0f)) return rfail(ctx, VMR_ERR_INVALID, "camera radius must be >= 0");
@@ -672,6 +753,9 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   for (const auto& L : R.disks)
     if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
       return rfail(ctx, VMR_ERR_INVALID, "disk light shader or geom out of range");
+  for (const auto& L : R.spheres)
+    if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
+      return rfail(ctx, VMR_ERR_INVALID, "sphere light shader or geom out of range");
   for (uint32_t g : ctx->top.host.geom_order) {
     const auto& mr = ctx->meshes[g];
     if (mr->host.motion()) return rfail(ctx, VMR_ERR_UNSUPPORTED, "rendering motion meshes is not supported yet");
@@ -689,8 +773,11 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     rm[g].sidx = mr.host.shader_idx.empty() ? nullptr : mr.sidx.as<uint8_t>();
     rm[g].shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
     rm[g].n_shaders = (uint32_t)mr.shader_list.size();
+    rm[g].kind = mr.host.sphere ? 1u : 0u;
+    for (int k = 0; k < 3; ++k) rm[g].sphere[k] = mr.host.sphere_c[k];
+    rm[g].sphere[3] = mr.host.sphere_r;
   }
-  std::vector<RLight> rl(R.lights.size() + R.disks.size());
+  std::vector<RLight> rl(R.lights.size() + R.disks.size() + R.spheres.size());
   uint32_t ns = 1;
   for (size_t i = 0; i < R.lights.size(); ++i) {
     rl[i] = RLight{};
@@ -728,6 +815,18 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     crs(L.N, d.up, t);
     nrm(t, L.T);
     crs(L.N, L.T, L.B);
+    ns = std::max<uint32_t>(ns, 1u << d.samples);
+  }
+  for (size_t k = 0; k < R.spheres.size(); ++k) {
+    const vmr_sphere_light& d = R.spheres[k];
+    RLight& L = rl[R.lights.size() + R.disks.size() + k];
+    L = RLight{};
+    L.kind = 2;
+    L.samples = d.samples;
+    L.shader = d.shader;
+    L.geom = d.geom;
+    L.radius = d.radius;
+    std::memcpy(L.P, d.P, 12);
     ns = std::max<uint32_t>(ns, 1u << d.samples);
   }
   const uint32_t nl = (uint32_t)rl.size();

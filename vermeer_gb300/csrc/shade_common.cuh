@@ -289,17 +289,18 @@ struct RMesh {
   const float4* tris;      // leaf order, as the traversal holds them
   const float4* nrm;       // per corner (leaf order) or null
   const uint8_t* sidx;     // per leaf-order triangle or null
-  const uint32_t* shaders; // PolyMesh.Shader
+  const uint32_t* shaders; // PolyMesh.Shader (a sphere: its shader first)
   uint32_t n_shaders;
-  uint32_t pad;
+  uint32_t kind;           // 0 triangles, 1 analytic sphere
+  float sphere[4];         // centre, radius
 };
 struct RLight {
   float p[9];        // TriLight: p0, p1, p2
   int samples;
   uint32_t shader;
   uint32_t geom;
-  int kind;          // 0 TriLight, 1 DiskLight
-  float P[3], T[3], B[3], N[3], radius;  // DiskLight frame (Disk.PreRender)
+  int kind;          // 0 TriLight, 1 DiskLight, 2 SphereLight
+  float P[3], T[3], B[3], N[3], radius;  // DiskLight frame (Disk.PreRender); SphereLight centre, radius
 };
 
 struct Ctx {
@@ -494,6 +495,31 @@ __device__ __forceinline__ void camera_primary(const vmr_camera& c, uint32_t wid
   D = normalize(d);
   P = v3(M[0] * e.x + M[4] * e.y + M[8] * e.z + M[12], M[1] * e.x + M[5] * e.y + M[9] * e.z + M[13],
          M[2] * e.x + M[6] * e.y + M[10] * e.z + M[14]);
+}
+
+// Hit attributes of an analytic sphere (builtin/geom/sphere/trace.go):
+// P = ray.P + t*ray.D, N = Ng = normalize(P - centre), Poffset = 0.001*N,
+// dPdu = (1,0,0), dPdv = (0,0,1), then ApplyTransform's renormalisation.
+__device__ __forceinline__ bool sphere_attributes(const RMesh& m, V3 Ro, V3 Rd, float t, Ctx& sc,
+                                                  uint32_t& shader_id) {
+  if (m.n_shaders == 0) return false;
+  shader_id = m.shaders[0];
+  const V3 P = add(Ro, scale(t, Rd));
+  const V3 N = normalize(sub(P, v3(m.sphere[0], m.sphere[1], m.sphere[2])));
+  sc.Poffset = scale(0.001f, N);
+  sc.P = P;
+  sc.N = normalize(N);
+  sc.Ng = normalize(N);
+  sc.DdPdu = normalize(v3(1, 0, 0));
+  sc.DdPdv = normalize(v3(0, 0, 1));
+  return true;
+}
+
+// The hit attributes of either geom kind.
+__device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim, float U, float V, float W, V3 Ro,
+                                                   V3 Rd, float t, Ctx& sc, uint32_t& shader_id) {
+  if (m.kind == 1) return sphere_attributes(m, Ro, Rd, t, sc, shader_id);
+  return hit_attributes(m, prim, U, V, W, sc, shader_id);
 }
 
 }  // namespace

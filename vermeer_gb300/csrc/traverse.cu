@@ -424,9 +424,44 @@ __device__ bool trace_motion(const DMesh& m, TRay& r, int2* stk, int cap, HitRec
   return hit;
 }
 
+// Sphere.Trace with raySphereIntersect (builtin/geom/sphere/trace.go): the
+// nearer non-negative root of the quadratic, taken if below Tclosest.
+__device__ __forceinline__ bool sphere_hit(const DMesh& m, TRay& r, HitRec& h) {
+  const float L[3] = {__fsub_rn(r.ox, m.sphere[0]), __fsub_rn(r.oy, m.sphere[1]), __fsub_rn(r.oz, m.sphere[2])};
+  const float a = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, r.dx), __fmul_rn(r.dy, r.dy)), __fmul_rn(r.dz, r.dz));
+  const float b = __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fmul_rn(r.dx, L[0]), __fmul_rn(r.dy, L[1])),
+                                           __fmul_rn(r.dz, L[2])));
+  const float c = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(L[0], L[0]), __fmul_rn(L[1], L[1])), __fmul_rn(L[2], L[2])),
+                            __fmul_rn(m.sphere[3], m.sphere[3]));
+  const float discr = __fsub_rn(__fmul_rn(b, b), __fmul_rn(__fmul_rn(4.0f, a), c));
+  if (discr < 0.0f) return false;
+  float x0, x1;
+  if (discr == 0.0f) {
+    x1 = __fdiv_rn(__fmul_rn(-0.5f, b), a);
+    x0 = x1;
+  } else {
+    const float sq = __fsqrt_rn(discr);
+    const float q = b > 0.0f ? __fmul_rn(-0.5f, __fadd_rn(b, sq)) : __fmul_rn(-0.5f, __fsub_rn(b, sq));
+    x0 = __fdiv_rn(q, a);
+    x1 = __fdiv_rn(c, q);
+  }
+  if (x0 > x1) { const float t = x0; x0 = x1; x1 = t; }
+  if (x0 > x1) { const float t = x0; x0 = x1; x1 = t; }
+  if (x0 < 0.0f) {
+    x0 = x1;
+    if (x0 < 0.0f) return false;
+  }
+  if (!(x0 < r.tclosest)) return false;
+  r.tclosest = x0;
+  h.elem = 0;
+  h.u = h.v = h.w = 0.0f;
+  return true;
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool trace_any_mesh(const DMesh& m, TRay& r, int2* stk, int cap, HitRec& h,
                                                Counters& cnt, int& status) {
+  if (m.kind == 1) return sphere_hit(m, r, h);
   if (m.n_tris == 0) return false;
   if (m.keys > 1) return trace_motion<ANY, COUNT>(m, r, stk, cap, h, cnt, status);
   return trace_static<ANY, COUNT>(m, r, stk, cap, h, cnt, status);
@@ -1100,6 +1135,17 @@ __global__ void __launch_bounds__(128, 8)
             ++leaf_next;
             --leaf_left;
             const DMesh& M = top.meshes[g];
+            if (M.kind == 1) {  // an analytic sphere: tested here, no stack
+              if (sphere_hit(M, r, h)) {
+                h.geom = (int)g;
+                hit = true;
+                if (ANY) {
+                  node = -1;
+                  break;
+                }
+              }
+              continue;
+            }
             if (M.n_tris == 0) continue;
             base = sp + 1;
             if (base >= kStackCapacity) {
@@ -1172,6 +1218,17 @@ __global__ void __launch_bounds__(128, 8)
               ++leaf_next;
               --leaf_left;
               const DMesh& MM = top.meshes[g];
+              if (MM.kind == 1) {
+                if (sphere_hit(MM, r, h)) {
+                  h.geom = (int)g;
+                  hit = true;
+                  if (ANY) {
+                    node = -1;
+                    break;
+                  }
+                }
+                continue;
+              }
               if (MM.n_tris == 0) continue;
               base = sp + 1;
               geom = (int)g;

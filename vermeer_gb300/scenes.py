@@ -477,3 +477,24 @@ def small_room_mirror(n_tris: int = 4096, seed: int = 1, light_samples: int = 1)
             extra = dict(spec1_colour=(1.0, 1.0, 1.0), spec1_strength=0.4, spec1_roughness=0.0, ior=1.5)
             sh[sid] = dict(sh[sid], **extra)
     return sc
+
+
+def small_room_spheres(n_tris: int = 4096, seed: int = 1, light_samples: int = 1) -> dict:
+    """The small room lit by a SphereLight (radius 0.12 hanging below the
+    ceiling, radiance 10) besides the TriLight panels, with three analytic
+    sphere geoms (builtin/geom/sphere) on the floor: Lambert, diffuse + GGX,
+    and a mirror."""
+    sc = small_room(n_tris, seed=seed, light_samples=light_samples)
+    sh = sc["shaders"]
+    light_shader = sc["lights"][0]["shader"]
+    base = len(sh)
+    sh += [dict(diffuse_colour=(0.8, 0.3, 0.3), diffuse_strength=1.0, diffuse_roughness=0.0),
+           dict(diffuse_colour=(0.3, 0.8, 0.3), diffuse_strength=0.7, diffuse_roughness=0.0,
+                spec1_colour=(1.0, 1.0, 1.0), spec1_strength=0.3, spec1_roughness=0.4, ior=1.5),
+           dict(spec1_colour=(0.9, 0.9, 0.9), spec1_strength=1.0, spec1_roughness=0.0, ior=1.5)]
+    for k, (x, z) in enumerate(((-0.5, 0.3), (0.0, 0.5), (0.5, 0.2))):
+        sc["meshes"].append(dict(sphere=(x, -0.75, z, 0.25), shaders=[base + k]))
+    sc["meshes"].append(dict(sphere=(0.0, 0.6, 0.0, 0.12), shaders=[light_shader]))
+    sc["sphere_lights"] = [dict(P=(0.0, 0.6, 0.0), radius=0.12, samples=light_samples, shader=light_shader,
+                                mesh=len(sc["meshes"]) - 1)]
+    return sc
