@@ -223,7 +223,7 @@ class Render:
             if "sphere" in m:
                 self.meshes.append(Sphere(m["sphere"][:3], m["sphere"][3]))
                 continue
-            om = Mesh(m["verts"], m["idxp"])
+            om = Mesh(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_fixed=m.get("motion_mode", 0) == 1)
             fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
             nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
             lib().orc_mesh_set_shading(om.h, _ptr(fs), _ptr(nr))

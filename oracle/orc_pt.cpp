@@ -307,12 +307,40 @@ struct PT {
 
   // Static-mesh hit attributes (trace.go:276-515; the same expressions as
   // the reference mode).  Returns the shader id or -1.
-  int32_t attributes(const Hit& h, Surf<T>& s) const {
+  int32_t attributes(const Hit& h, Surf<T>& s, const float* Ro, const float* Rd, float time) const {
     const orc_internal::MeshView& m = R.meshes[h.geom];
-    const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
-    const Vec<T> V0 = fromf<T>(m.verts + i0 * 3), V1 = fromf<T>(m.verts + i1 * 3), V2 = fromf<T>(m.verts + i2 * 3);
-    const uint8_t sidx = m.shaderidx ? m.shaderidx[h.elem] : 0;
     const auto& list = R.mesh_shaders[h.geom];
+    if (m.sphere) {  // sphere/trace.go: P = ray.P + t ray.D, N = normalize(P - centre)
+      if (list.empty()) return -1;
+      const float P[3] = {Ro[0] + Rd[0] * h.t, Ro[1] + Rd[1] * h.t, Ro[2] + Rd[2] * h.t};  // float32, as the hit
+      const Vec<T> Pv = fromf<T>(P);
+      const Vec<T> N = nrm(sub(Pv, fromf<T>(m.sc)));
+      s.Poffset = scl(T(0.001f), N);
+      s.P = Pv;
+      s.N = nrm(N);
+      s.Ng = nrm(N);
+      s.dPdu = mk<T>(1, 0, 0);
+      s.dPdv = mk<T>(0, 0, 1);
+      return (int32_t)list[0];
+    }
+    const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
+    float tm = 0.0f;
+    int key = 0, key2 = 0;
+    if (m.motion) {  // TraceMotionElems' lerped vertices (trace.go:520-560)
+      const float k = time * (float)(m.keys - 1);
+      tm = k - std::floor(k);
+      key = (int)std::floor(k);
+      key2 = (int)std::ceil(k);
+    }
+    auto vert = [&](uint32_t i) {
+      const float* a = m.verts + ((size_t)key * m.nverts + i) * 3;
+      if (!m.motion) return fromf<T>(a);
+      const float* b = m.verts + ((size_t)key2 * m.nverts + i) * 3;
+      const float v[3] = {(1.0f - tm) * a[0] + tm * b[0], (1.0f - tm) * a[1] + tm * b[1], (1.0f - tm) * a[2] + tm * b[2]};
+      return fromf<T>(v);
+    };
+    const Vec<T> V0 = vert(i0), V1 = vert(i1), V2 = vert(i2);
+    const uint8_t sidx = m.shaderidx ? m.shaderidx[h.elem] : 0;
     if (sidx >= list.size()) return -1;
     const T U = (T)h.u, V = (T)h.v, W = (T)h.w;
     const T xs = std::fabs(U * V0.x) + std::fabs(V * V1.x) + std::fabs(W * V2.x);
@@ -331,11 +359,17 @@ struct PT {
     const T d = g7 * xs * std::fabs(Ng.x) + g7 * ys * std::fabs(Ng.y) + g7 * zs * std::fabs(Ng.z);
     s.Poffset = scl(d, Ng);
     s.P = mk<T>(U * V0.x + V * V1.x + W * V2.x, U * V0.y + V * V1.y + W * V2.y, U * V0.z + V * V1.z + W * V2.z);
-    Vec<T> axisu = sub(mk<T>(1, 0, 0), scl(dot(mk<T>(1, 0, 0), Ng), Ng));
-    if (len2(axisu) < T(0.1) || std::fabs(dot(axisu, Ng)) > T(0.3))
-      axisu = sub(mk<T>(0, 0, 1), scl(dot(mk<T>(0, 0, 1), Ng), Ng));
-    const Vec<T> dpdu = nrm(axisu);
-    const Vec<T> dpdv = cross(Ng, dpdu);
+    Vec<T> dpdu, dpdv;
+    if (m.motion) {  // raw edges (trace.go:655-661)
+      dpdu = e0;
+      dpdv = e1;
+    } else {
+      Vec<T> axisu = sub(mk<T>(1, 0, 0), scl(dot(mk<T>(1, 0, 0), Ng), Ng));
+      if (len2(axisu) < T(0.1) || std::fabs(dot(axisu, Ng)) > T(0.3))
+        axisu = sub(mk<T>(0, 0, 1), scl(dot(mk<T>(0, 0, 1), Ng), Ng));
+      dpdu = nrm(axisu);
+      dpdv = cross(Ng, dpdu);
+    }
     s.N = nrm(N);
     s.Ng = nrm(Ng);
     s.dPdu = nrm(dpdu);
@@ -366,7 +400,7 @@ struct PT {
         break;
       }
       Surf<T> s;
-      const int32_t shid = attributes(h, s);
+      const int32_t shid = attributes(h, s, Pf, Df, time);
       if (shid < 0) break;
       const orc_shader& sh = R.shaders[shid];
       const Vec<T> wi = neg(D);

@@ -775,7 +775,22 @@ struct Renderer {
       return true;
     }
     const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
-    auto vert = [&](uint32_t i) { return v3(m.verts[i * 3], m.verts[i * 3 + 1], m.verts[i * 3 + 2]); };
+    // static: key 0; motion: the keys around the ray's time, lerped as
+    // TraceMotionElems does (trace.go:520-560, Vec3Lerp math/vec3.go:52-58)
+    float tm = 0.0f;
+    int key = 0, key2 = 0;
+    if (m.motion) {
+      const float k = sc.time * (float)(m.keys - 1);
+      tm = k - std::floor(k);
+      key = (int)std::floor(k);
+      key2 = (int)std::ceil(k);
+    }
+    auto vert = [&](uint32_t i) {
+      const float* a = m.verts + ((size_t)key * m.nverts + i) * 3;
+      if (!m.motion) return v3(a[0], a[1], a[2]);
+      const float* b = m.verts + ((size_t)key2 * m.nverts + i) * 3;
+      return v3((1.0f - tm) * a[0] + tm * b[0], (1.0f - tm) * a[1] + tm * b[1], (1.0f - tm) * a[2] + tm * b[2]);
+    };
     const V3 V0 = vert(i0), V1 = vert(i1), V2 = vert(i2);
     const float U = h.u, V = h.v, W = h.w;
     const float xs = gabs(U * V0.x) + gabs(V * V1.x) + gabs(W * V2.x);
@@ -799,10 +814,16 @@ struct Renderer {
     const float d = g7 * xs * gabs(Ng.x) + g7 * ys * gabs(Ng.y) + g7 * zs * gabs(Ng.z);
     sc.Poffset = scale(d, Ng);
     sc.P = v3(U * V0.x + V * V1.x + W * V2.x, U * V0.y + V * V1.y + W * V2.y, U * V0.z + V * V1.z + W * V2.z);
-    V3 axisu = sub(v3(1, 0, 0), scale(dot(v3(1, 0, 0), Ng), Ng));
-    if (len2(axisu) < 0.1f || gabs(dot(axisu, Ng)) > 0.3f) axisu = sub(v3(0, 0, 1), scale(dot(v3(0, 0, 1), Ng), Ng));
-    const V3 dpdu = normalize(axisu);
-    const V3 dpdv = cross(Ng, dpdu);
+    V3 dpdu, dpdv;
+    if (m.motion) {  // the motion path keeps the raw edges (trace.go:655-661)
+      dpdu = e0;
+      dpdv = e1;
+    } else {
+      V3 axisu = sub(v3(1, 0, 0), scale(dot(v3(1, 0, 0), Ng), Ng));
+      if (len2(axisu) < 0.1f || gabs(dot(axisu, Ng)) > 0.3f) axisu = sub(v3(0, 0, 1), scale(dot(v3(0, 0, 1), Ng), Ng));
+      dpdu = normalize(axisu);
+      dpdv = cross(Ng, dpdu);
+    }
     sc.N = normalize(N);
     sc.Ng = normalize(Ng);
     sc.DdPdu = normalize(dpdu);

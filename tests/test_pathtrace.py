@@ -225,3 +225,21 @@ def test_pt_guided_training_matches_plain(ctx, room):
     se = np.sqrt(np.var(bg - bp) / bg.size)
     assert abs(bg.mean() - bp.mean()) < 5 * se + 1e-6, (bg.mean(), bp.mean(), se)
     assert _block_relmse(g64, p64) < 0.02
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["motion_faithful", "motion_fixed", "spheres"])
+def test_pt_motion_and_spheres_match_float_oracle(ctx, orc, kind):
+    """The extended mode over motion meshes (hit attributes at the ray's
+    time) and analytic sphere geoms."""
+    if kind == "spheres":
+        sc = scenes.small_room_spheres(2048, seed=12)
+    else:
+        sc = scenes.small_room_motion(2048, seed=12, motion_mode=1 if kind == "motion_fixed" else 0)
+    sc = dict(sc, env=(0.1, 0.1, 0.12))
+    ctx.load_scene(sc)
+    ref, _ = orc.Render(sc).run_path(40, 40, 0, 3, 23, max_depth=4, precision=32)
+    got, _ = ctx.render_path(40, 40, 0, 3, 23, max_depth=4)
+    ok = (np.abs(got - ref) <= REL * (1 + np.abs(ref))).all(-1)
+    assert ok.mean() >= FRAC_EQUAL, ok.mean()
+    assert abs(got.mean() - ref.mean()) <= 1e-4 * ref.mean()

@@ -185,3 +185,24 @@ def test_render_spheres_match_oracle(ctx, orc, samples):
     got, _ = ctx.render(48, 48, 0, 3, 17)
     frac, mean_abs = _compare(got, ref)
     assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)
+
+
+# ---------------------------------------------------------- motion blur ----
+def test_oracle_motion_room_sane(orc):
+    sc = scenes.small_room_motion(2048, seed=9)
+    fb = orc.Render(sc).run(32, 32, 0, 4, 5)
+    assert np.isfinite(fb).all() and (fb >= 0).all() and fb.mean() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [0, 1])
+def test_render_motion_blur_matches_oracle(ctx, orc, mode):
+    """A two-key motion soup rendered over the shutter (each sample's VdC
+    time): the motion traversal and the lerped hit attributes of
+    TraceMotionElems, in both leaf-indexing modes."""
+    sc = scenes.small_room_motion(2048, seed=9, motion_mode=mode)
+    ctx.load_scene(sc)
+    ref = orc.Render(sc).run(48, 48, 0, 3, 19)
+    got, _ = ctx.render(48, 48, 0, 3, 19)
+    frac, mean_abs = _compare(got, ref)
+    assert frac >= FRAC_EQUAL and mean_abs <= MEAN_ABS, (frac, mean_abs)

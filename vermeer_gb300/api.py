@@ -403,7 +403,9 @@ class Context:
             if "sphere" in m:  # an analytic sphere geom: (cx, cy, cz, radius)
                 g = self.sphere_add(m["sphere"][:3], m["sphere"][3])
             else:
-                g = self.mesh_build(m["verts"], m["idxp"], shader_idx=m.get("face_shader"))
+                g = self.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1),
+                                    motion_mode=m.get("motion_mode", MOTION_FAITHFUL),
+                                    shader_idx=m.get("face_shader"))
             ids.append(g)
         self.scene_build(ids)
         self.set_shaders(scene["shaders"])

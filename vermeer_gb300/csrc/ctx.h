@@ -47,6 +47,7 @@ struct MeshRec {
   std::vector<uint32_t> shader_list;
   bool has_normals = false;
   DevBuf shlist, sidx, nrm;
+  DevBuf avert, aidx;  // motion meshes: key-major vertices (float4) and face-order idxp for hit attributes
   // the autotuner's choice for this mesh (vmr_autotune)
   bool tuned = false;
   vmr_tuning tuning{};

@@ -341,7 +341,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
       uint32_t shid = 0;
       const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
       const V3 Rd = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
-      if (surface_attributes(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i], sc, shid)) {
+      if (surface_attributes(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i],
+                             q[7 * (size_t)b.cap + i], sc, shid)) {
         wi = v3(-q[3 * (size_t)b.cap + i], -q[4 * (size_t)b.cap + i], -q[5 * (size_t)b.cap + i]);
         P = sc.P;
         N = dot(sc.Ng, wi) > 0.0f ? sc.N : v3(-sc.N.x, -sc.N.y, -sc.N.z);
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
         Ctx sc;
         uint32_t shid = 0;
         const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
-        if (surface_attributes(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], sc, shid)) {
+        if (surface_attributes(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], time, sc, shid)) {
           const vmr_shader_std& sh = b.shaders[shid];
           const V3 wi = v3(-D.x, -D.y, -D.z);
           const bool front = dot(sc.Ng, wi) > 0.0f;
@@ -825,7 +826,8 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   auto& R = ctx->render;
   for (uint32_t g : ctx->top.host.geom_order) {
     const auto& mr = ctx->meshes[g];
-    if (mr->host.motion()) return pfail(ctx, VMR_ERR_UNSUPPORTED, "rendering motion meshes is not supported yet");
+    if (mr->host.motion() && mr->aidx.p == nullptr)
+      return pfail(ctx, VMR_ERR_INVALID, "a motion mesh in the scene has no shading (vmr_mesh_set_shading)");
     for (uint32_t sid : mr->shader_list)
       if (sid >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "mesh shader id out of range");
   }
@@ -885,6 +887,10 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     rm[g].kind = mr.host.sphere ? 1u : 0u;
     for (int k = 0; k < 3; ++k) rm[g].sphere[k] = mr.host.sphere_c[k];
     rm[g].sphere[3] = mr.host.sphere_r;
+    rm[g].keys = mr.host.motion() ? mr.host.keys : 1u;
+    rm[g].n_verts = mr.host.n_verts;
+    rm[g].mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
+    rm[g].midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
   }
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;

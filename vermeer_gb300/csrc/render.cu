@@ -402,7 +402,8 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
     const V3 Ro = v3(*ray_f(lv, 0, e), *ray_f(lv, 1, e), *ray_f(lv, 2, e));
     const V3 Rdir = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
     if (!surface_attributes(m, prim, hf[3 * (size_t)lv.cap + e], hf[4 * (size_t)lv.cap + e],
-                            hf[5 * (size_t)lv.cap + e], Ro, Rdir, hf[2 * (size_t)lv.cap + e], sc, shid))
+                            hf[5 * (size_t)lv.cap + e], Ro, Rdir, hf[2 * (size_t)lv.cap + e], *ray_f(lv, 7, e), sc,
+                            shid))
       continue;
     const vmr_shader_std& sh = b.shaders[shid];
     sc.Rd = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
@@ -675,7 +676,8 @@ int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n) {
 int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, uint32_t n_shaders, const float* normals) {
   if (!ctx || geom >= ctx->meshes.size() || (n_shaders && !shaders)) return VMR_ERR_INVALID;
   MeshRec& rec = *ctx->meshes[geom];
-  if (rec.host.motion()) return rfail(ctx, VMR_ERR_UNSUPPORTED, "rendering motion meshes is not supported yet");
+  if (rec.host.motion() && normals)
+    return rfail(ctx, VMR_ERR_UNSUPPORTED, "normals of motion meshes are not supported");
   rec.shader_list.assign(shaders, shaders + n_shaders);
   rec.has_normals = normals != nullptr;
   if (ctx->device < 0) return VMR_OK;
@@ -693,6 +695,14 @@ int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, u
     }
     RCUDA(rec.nrm.ensure(nrm.size() * sizeof(float4)));
     RCUDA(cudaMemcpy(rec.nrm.p, nrm.data(), nrm.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  }
+  if (m.motion()) {  // vertices and face-order idxp for the hit attributes
+    std::vector<float4> av((size_t)m.keys * m.n_verts);
+    for (size_t i = 0; i < av.size(); ++i) av[i] = make_float4(m.verts[i * 3], m.verts[i * 3 + 1], m.verts[i * 3 + 2], 0.f);
+    RCUDA(rec.avert.ensure(av.size() * sizeof(float4)));
+    RCUDA(cudaMemcpy(rec.avert.p, av.data(), av.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    RCUDA(rec.aidx.ensure(m.idxp.size() * 4));
+    RCUDA(cudaMemcpy(rec.aidx.p, m.idxp.data(), m.idxp.size() * 4, cudaMemcpyHostToDevice));
   }
   RCUDA(rec.shlist.ensure(std::max<size_t>(1, n_shaders) * 4));
   if (n_shaders) RCUDA(cudaMemcpy(rec.shlist.p, shaders, n_shaders * 4, cudaMemcpyHostToDevice));
@@ -758,7 +768,8 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
       return rfail(ctx, VMR_ERR_INVALID, "sphere light shader or geom out of range");
   for (uint32_t g : ctx->top.host.geom_order) {
     const auto& mr = ctx->meshes[g];
-    if (mr->host.motion()) return rfail(ctx, VMR_ERR_UNSUPPORTED, "rendering motion meshes is not supported yet");
+    if (mr->host.motion() && mr->aidx.p == nullptr)
+      return rfail(ctx, VMR_ERR_INVALID, "a motion mesh in the scene has no shading (vmr_mesh_set_shading)");
     for (uint32_t sid : mr->shader_list)
       if (sid >= R.shaders.size()) return rfail(ctx, VMR_ERR_INVALID, "mesh shader id out of range");
   }
@@ -776,6 +787,10 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     rm[g].kind = mr.host.sphere ? 1u : 0u;
     for (int k = 0; k < 3; ++k) rm[g].sphere[k] = mr.host.sphere_c[k];
     rm[g].sphere[3] = mr.host.sphere_r;
+    rm[g].keys = mr.host.motion() ? mr.host.keys : 1u;
+    rm[g].n_verts = mr.host.n_verts;
+    rm[g].mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
+    rm[g].midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
   }
   std::vector<RLight> rl(R.lights.size() + R.disks.size() + R.spheres.size());
   uint32_t ns = 1;

@@ -293,6 +293,10 @@ struct RMesh {
   uint32_t n_shaders;
   uint32_t kind;           // 0 triangles, 1 analytic sphere
   float sphere[4];         // centre, radius
+  // motion meshes: vertices [keys][n_verts] and idxp in face order
+  const float4* mverts;
+  const uint32_t* midxp;
+  uint32_t keys, n_verts;
 };
 struct RLight {
   float p[9];        // TriLight: p0, p1, p2
@@ -515,10 +519,46 @@ __device__ __forceinline__ bool sphere_attributes(const RMesh& m, V3 Ro, V3 Rd, 
   return true;
 }
 
-// The hit attributes of either geom kind.
+// Hit attributes of a motion mesh (TraceMotionElems, trace.go:520-719): the
+// face's vertices idxp[ElemID*3 + j] lerped between the keys around the ray
+// time (Vec3Lerp, math/vec3.go:52-58), dPdu/dPdv the raw edges, then
+// ApplyTransform's renormalisation; no normals (N = Ng).
+__device__ __forceinline__ bool motion_attributes(const RMesh& m, int32_t elem, float U, float V, float W, float time,
+                                                  Ctx& sc, uint32_t& shader_id) {
+  const uint32_t sidx = m.sidx ? m.sidx[elem] : 0u;
+  if (sidx >= m.n_shaders) return false;
+  shader_id = m.shaders[sidx];
+  const float k = time * (float)(m.keys - 1);
+  const float tm = k - floorf(k);
+  const uint32_t key = (uint32_t)floorf(k), key2 = (uint32_t)ceilf(k);
+  V3 Vx[3];
+  for (int j = 0; j < 3; ++j) {
+    const uint32_t i = m.midxp[(size_t)elem * 3 + j];
+    const float4 a = m.mverts[(size_t)key * m.n_verts + i], c = m.mverts[(size_t)key2 * m.n_verts + i];
+    Vx[j] = v3((1.0f - tm) * a.x + tm * c.x, (1.0f - tm) * a.y + tm * c.y, (1.0f - tm) * a.z + tm * c.z);
+  }
+  const V3 V0 = Vx[0], V1 = Vx[1], V2 = Vx[2];
+  const float xs = fabsf(U * V0.x) + fabsf(V * V1.x) + fabsf(W * V2.x);
+  const float ys = fabsf(U * V0.y) + fabsf(V * V1.y) + fabsf(W * V2.y);
+  const float zs = fabsf(U * V0.z) + fabsf(V * V1.z) + fabsf(W * V2.z);
+  const V3 e0 = sub(V1, V0), e1 = sub(V2, V0);
+  const V3 Ng = normalize(v3(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x));
+  const float g7 = (7.0f * 5.96046448e-08f) / (1 - 7.0f * 5.96046448e-08f);  // Gamma(7)
+  const float d = g7 * xs * fabsf(Ng.x) + g7 * ys * fabsf(Ng.y) + g7 * zs * fabsf(Ng.z);
+  sc.Poffset = scale(d, Ng);
+  sc.P = v3(U * V0.x + V * V1.x + W * V2.x, U * V0.y + V * V1.y + W * V2.y, U * V0.z + V * V1.z + W * V2.z);
+  sc.N = normalize(Ng);
+  sc.Ng = normalize(Ng);
+  sc.DdPdu = normalize(e0);
+  sc.DdPdv = normalize(e1);
+  return true;
+}
+
+// The hit attributes of any geom kind.
 __device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim, float U, float V, float W, V3 Ro,
-                                                   V3 Rd, float t, Ctx& sc, uint32_t& shader_id) {
+                                                   V3 Rd, float t, float time, Ctx& sc, uint32_t& shader_id) {
   if (m.kind == 1) return sphere_attributes(m, Ro, Rd, t, sc, shader_id);
+  if (m.keys > 1) return motion_attributes(m, prim, U, V, W, time, sc, shader_id);
   return hit_attributes(m, prim, U, V, W, sc, shader_id);
 }
 

@@ -498,3 +498,19 @@ def small_room_spheres(n_tris: int = 4096, seed: int = 1, light_samples: int = 1
     sc["sphere_lights"] = [dict(P=(0.0, 0.6, 0.0), radius=0.12, samples=light_samples, shader=light_shader,
                                 mesh=len(sc["meshes"]) - 1)]
     return sc
+
+
+def small_room_motion(n_tris: int = 4096, seed: int = 1, motion_mode: int = 0, velocity: float = 0.08) -> dict:
+    """The small room with its soup moving: two motion keys (key 1 = key 0 +
+    a per-triangle velocity in a ball of the given radius), sampled over the
+    shutter by each camera ray's VdC time; motion_mode 0 reproduces
+    TraceMotionElems' leaf indexing, 1 the face the leaf boxes bound."""
+    sc = small_room(n_tris, seed=seed)
+    soup = sc["meshes"][1]
+    v0 = soup["verts"].reshape(n_tris, 3, 3).astype(np.float64)
+    d = unit_sphere(seed, n_tris, 40) * (velocity * np.cbrt(uniform(seed, n_tris, 42)))[:, None]
+    v1 = (v0 + d[:, None, :]).astype(np.float32).reshape(-1, 3)
+    soup["verts"] = np.concatenate([soup["verts"], v1], axis=0)
+    soup["keys"] = 2
+    soup["motion_mode"] = motion_mode
+    return sc
