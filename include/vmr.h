@@ -66,7 +66,9 @@ typedef struct {
                             L1 prefetch of the next node; bit 2: 64-register
                             cap (while-while only); bit 3: reorder rays by
                             permutation class and origin cell before a mesh
-                            trace of >= 65536 rays.  Default 13. */
+                            trace of >= 65536 rays; bit 4: the top 16
+                            entries of the traversal stack in shared memory
+                            (while-while).  Default 13. */
     int block;           /* threads per block, multiple of 32, <= 256 (128) */
     int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
     int refill_min;      /* step-scheduled: idle lanes that trigger a warp
@@ -156,6 +158,13 @@ int vmr_sphere_add(vmr_ctx* ctx, const float center[3], float radius, uint32_t* 
 /* Build the mesh's QBVH on the host exactly as PolyMesh.initAccel does
  * (binned SAH, qbvh/build.go:28-307, leafMax 16) and upload it. */
 int vmr_mesh_build(vmr_ctx* ctx, const vmr_mesh_input* in, uint32_t* out_geom);
+/* Which builder vmr_mesh_build uses.  Both give the same node arrays, leaf
+ * order and bounds, bit for bit.  AUTO (the default) builds meshes of 16384
+ * or more triangles on the device and smaller ones on the host; DEVICE
+ * always builds on the device (VMR_ERR_UNSUPPORTED for build geometry that
+ * is not finite); HOST always on the host (threads per upper-level subtree). */
+typedef enum { VMR_BUILD_AUTO = 0, VMR_BUILD_HOST = 1, VMR_BUILD_DEVICE = 2 } vmr_builder;
+int vmr_set_builder(vmr_ctx* ctx, int builder);
 /* Upload a caller-built (reference-built) accelerator; the data is copied. */
 int vmr_mesh_upload(vmr_ctx* ctx, const vmr_mesh_desc* desc, uint32_t* out_geom);
 /* Sizes of a mesh's accelerator: static node count, motion node count. */

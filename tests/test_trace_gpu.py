@@ -140,7 +140,9 @@ def test_full_size_soup_parity(ctx, orc):
 
 @pytest.mark.parametrize("tuning", [(0, 0, 0, 0), (1, 0, 0, 0), (3, 0, 0, 0), (5, 0, 0, 0), (8, 0, 0, 4),
                                     (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0), (13, 0, 0, 0, 4), (9, 0, 0, 0, 12),
-                                    (13, 0, 0, 0, 4, 3), (13, 0, 0, 0, 4, 5), (8, 256, 0, 4, 4, 5)])
+                                    (13, 0, 0, 0, 4, 3), (13, 0, 0, 0, 4, 5), (8, 256, 0, 4, 4, 5),
+                                    (29, 0, 0, 0, 4), (17, 0, 0, 0, 0), (25, 256, 0, 0, 8, 3), (21, 64, 0, 0, 2),
+                                    (16, 0, 0, 0)])
 def test_every_tuning_is_bit_exact(ctx, orc, tuning):
     """Launch parameters (kernel variant, ray reordering and its key width,
     block size, resident blocks) only change scheduling: hits stay

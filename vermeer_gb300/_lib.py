@@ -143,6 +143,7 @@ SIGNATURES = {
     "vmr_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
     "vmr_trace_timing": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "vmr_mesh_build": (ctypes.c_int, [P, ctypes.POINTER(MeshInput), ctypes.POINTER(U32)]),
+    "vmr_set_builder": (ctypes.c_int, [P, ctypes.c_int]),
     "vmr_mesh_upload": (ctypes.c_int, [P, ctypes.POINTER(MeshDesc), ctypes.POINTER(U32)]),
     "vmr_mesh_info": (ctypes.c_int, [P, U32, P, P, P, P]),
     "vmr_mesh_export": (ctypes.c_int, [P, U32, P, P, P, P, P, P]),

@@ -23,6 +23,7 @@ STATUS = {0: "VMR_OK", -1: "VMR_ERR_INVALID", -2: "VMR_ERR_CUDA", -3: "VMR_ERR_O
           -5: "VMR_ERR_STACK_OVERFLOW", -6: "VMR_ERR_QUEUE_OVERFLOW", -7: "VMR_ERR_UNSUPPORTED"}
 TRACE_ANY_HIT, TRACE_DEVICE, TRACE_COUNT = 1, 2, 4
 MOTION_FAITHFUL, MOTION_FIXED = 0, 1
+BUILD_AUTO, BUILD_HOST, BUILD_DEVICE = 0, 1, 2
 
 NODE_DTYPE = np.dtype([("boxes", "<f4", (24,)), ("axis", "<u4", (3,)), ("children", "<i4", (4,)),
                        ("parent", "<i4")])
@@ -137,6 +138,11 @@ class Context:
                     walk_tail=t.walk_tail, sort_bits=t.sort_bits)
 
     # ------------------------------------------------------------ meshes
+    def set_builder(self, builder: int):
+        """BUILD_AUTO (device for meshes of >= 16384 triangles), BUILD_HOST or
+        BUILD_DEVICE: the QBVH builder of mesh_build (same result either way)."""
+        self._check(self.L.vmr_set_builder(self.h, builder))
+
     def mesh_build(self, verts, idxp, keys: int = 1, ray_bias: float = 0.0, motion_mode: int = MOTION_FAITHFUL,
                    shader_idx=None) -> int:
         verts = np.ascontiguousarray(verts, np.float32)

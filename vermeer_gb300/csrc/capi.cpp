@@ -16,9 +16,13 @@
 #include "accel.h"
 #include "ctx.h"
 #include "device.h"
+#include "gpubuild.h"
 #include "vmr.h"
 
 namespace {
+
+// Smallest mesh vmr_mesh_build builds on the device under VMR_BUILD_AUTO.
+constexpr uint32_t kDeviceBuildMin = 16384;
 
 int fail(vmr_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -108,8 +112,9 @@ bool repack_mnodes(const std::vector<vmr_mqbvh_node>& in, uint32_t n_elems, std:
 
 struct F4 { float x, y, z, w; };
 
-// Host accelerator -> device arrays (layout in device.h).
-int upload_mesh(vmr_ctx* ctx, MeshRec& rec) {
+// Host accelerator -> device arrays (layout in device.h).  tris_ready: the
+// device builder already wrote the static triangle table into rec.tris.
+int upload_mesh(vmr_ctx* ctx, MeshRec& rec, bool tris_ready = false) {
   HostMesh& m = rec.host;
   if (ctx->device < 0) return VMR_OK;
   DMesh d{};
@@ -120,13 +125,15 @@ int upload_mesh(vmr_ctx* ctx, MeshRec& rec) {
   if (!m.motion()) {
     std::vector<GNode> g;
     if (!repack_nodes(m.nodes, m.n_tris, g)) return fail(ctx, VMR_ERR_INVALID, "malformed QBVH nodes");
-    std::vector<F4> tris((size_t)m.n_tris * 3);
-    for (size_t i = 0; i < (size_t)m.n_tris * 3; ++i) {
-      const float* v = &m.verts[(size_t)m.idxp[i] * 3];
-      tris[i] = F4{v[0], v[1], v[2], 0.0f};
-    }
     VMR_CUDA(ctx, upload(ctx, rec.nodes, g));
-    VMR_CUDA(ctx, upload(ctx, rec.tris, tris));
+    if (!tris_ready) {
+      std::vector<F4> tris((size_t)m.n_tris * 3);
+      for (size_t i = 0; i < (size_t)m.n_tris * 3; ++i) {
+        const float* v = &m.verts[(size_t)m.idxp[i] * 3];
+        tris[i] = F4{v[0], v[1], v[2], 0.0f};
+      }
+      VMR_CUDA(ctx, upload(ctx, rec.tris, tris));
+    }
     d.nodes = rec.nodes.as<GNode>();
     d.tris = rec.tris.p;
     d.iter_cap = 4u * (uint32_t)m.nodes.size() + 2u;
@@ -396,7 +403,7 @@ const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
   if (!ctx || !t) return VMR_ERR_INVALID;
-  if (t->kernel < 0 || t->kernel > 15) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 15]");
+  if (t->kernel < 0 || t->kernel > 31) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 31]");
   if (t->walk_tail < 0 || t->walk_tail > 31) return fail(ctx, VMR_ERR_INVALID, "tuning.walk_tail must be in [0, 31]");
   if (t->block != 0 && (t->block < 32 || t->block > 256 || t->block % 32 != 0))
     return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
@@ -454,11 +461,32 @@ int vmr_mesh_build(vmr_ctx* ctx, const vmr_mesh_input* in, uint32_t* out_geom) {
   m.ray_bias = in->ray_bias;
   m.motion_mode = in->motion_mode;
   if (in->shader_idx) m.shader_idx.assign(in->shader_idx, in->shader_idx + in->n_tris);
-  if (!vmr::build_mesh_accel(m, why)) return fail(ctx, VMR_ERR_INVALID, why);
-  int st = upload_mesh(ctx, *rec);
+  // The device builder gives the host builder's result; AUTO takes it for
+  // meshes large enough to gain from it.
+  bool on_device = false;
+  const bool want_device = ctx->device >= 0 && (ctx->builder == VMR_BUILD_DEVICE ||
+                                                (ctx->builder == VMR_BUILD_AUTO && in->n_tris >= kDeviceBuildMin));
+  if (want_device) {
+    int r = vmr::device_build_mesh(m, rec->tris, ctx->stream, why);
+    if (r == vmr::kBuildError) return fail(ctx, VMR_ERR_INVALID, why);
+    if (r == vmr::kBuildDeclined && ctx->builder == VMR_BUILD_DEVICE && in->n_tris > 0)
+      return fail(ctx, VMR_ERR_UNSUPPORTED, "the device builder declined this mesh (non-finite build geometry)");
+    on_device = r == vmr::kBuildOk;
+  }
+  if (!on_device && !vmr::build_mesh_accel(m, why)) return fail(ctx, VMR_ERR_INVALID, why);
+  int st = upload_mesh(ctx, *rec, on_device && !m.motion());
   if (st != VMR_OK) return st;
   if (out_geom) *out_geom = (uint32_t)ctx->meshes.size();
   ctx->meshes.push_back(std::move(rec));
+  return VMR_OK;
+}
+
+int vmr_set_builder(vmr_ctx* ctx, int builder) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (builder < VMR_BUILD_AUTO || builder > VMR_BUILD_DEVICE) return fail(ctx, VMR_ERR_INVALID, "unknown builder");
+  if (builder == VMR_BUILD_DEVICE && ctx->device < 0)
+    return fail(ctx, VMR_ERR_INVALID, "a host-only context has no device builder");
+  ctx->builder = builder;
   return VMR_OK;
 }
 
@@ -675,7 +703,7 @@ int vmr_autotune(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, in
   // candidates: while-while (with/without reordering, register cap, tail
   // cutoff, key width) and the step-scheduled kernel
   std::vector<vmr_tuning> cands;
-  for (int k : {13, 9})
+  for (int k : {13, 9, 29})
     for (int tail : {0, 2, 4, 8})
       for (int bits : {3, 4, 5}) cands.push_back(vmr_tuning{k, 0, 0, 0, tail, bits});
   for (int k : {5, 1})

@@ -118,7 +118,9 @@ enum TraceKernel : int {
   kKernelPrefetch = 2,
   kKernelRegCap = 4,
   kKernelSort = 8,
+  kKernelSharedStack = 16,  // while-while: the top of the stack in shared memory
 };
+constexpr int kSharedStackEntries = 16;
 
 // Ray reordering (raysort.cu): 6 permutation classes x (2^b)^3 origin cells,
 // b = 3..5 (default 4: 16^3 cells).

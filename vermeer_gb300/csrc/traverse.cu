@@ -724,6 +724,60 @@ __device__ __forceinline__ void fetch_mnode(const DMesh& m, int node, unsigned o
   rk = (((oct & 4u) ? meta.z : meta.y) >> ((oct & 3u) * 8u)) & 0xffu;
 }
 
+// A traversal stack whose first SS entries per thread live in shared memory
+// (entry-major, so the 32 lanes of a warp always touch 32 different banks)
+// and the rest in local memory; SS = 0 keeps the whole stack local.
+template <int SS>
+struct SplitStack {
+  int* sn;     // shared node ids: entry k of this thread at sn[k * stride]
+  float* st;   // shared T values
+  int stride;  // threads per block
+  int2 loc[kStackCapacity - SS];
+  __device__ __forceinline__ void set(int i, int node, float T) {
+    if (SS > 0 && i < SS) {
+      sn[i * stride] = node;
+      st[i * stride] = T;
+    } else {
+      loc[i - SS] = make_int2(node, __float_as_int(T));
+    }
+  }
+  __device__ __forceinline__ int2 get(int i) const {
+    if (SS > 0 && i < SS) return make_int2(sn[i * stride], __float_as_int(st[i * stride]));
+    return loc[i - SS];
+  }
+};
+
+// push_ranked for a SplitStack.
+template <class S>
+__device__ __forceinline__ bool push_ranked_s(S& stk, int& sp, unsigned mask, const int4& ch, const float (&tn)[4],
+                                              unsigned rk, int& next, float& nextT, int& status) {
+  if (mask == 0) return false;
+  const unsigned r0 = rk & 3u, r1 = (rk >> 2) & 3u, r2 = (rk >> 4) & 3u, r3 = (rk >> 6) & 3u;
+  const unsigned rmask = ((mask & 1u) << r0) | (((mask >> 1) & 1u) << r1) | (((mask >> 2) & 1u) << r2) |
+                         (((mask >> 3) & 1u) << r3);
+  const unsigned rtop = 31u - __clz(rmask);
+  const int npush = __popc(rmask) - 1;
+  if (sp + npush > kStackCapacity) {
+    status = kStatusStackOverflow;
+    return false;
+  }
+  const unsigned rr[4] = {r0, r1, r2, r3};
+  const int cv[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (mask & (1u << c)) {
+      if (rr[c] == rtop) {
+        next = cv[c];
+        nextT = tn[c];
+      } else {
+        stk.set(sp + __popc(rmask & ((1u << rr[c]) - 1u)), cv[c], tn[c]);
+      }
+    }
+  }
+  sp += npush;
+  return true;
+}
+
 // Push the hit children in rank order (rank r_c = bits 2c..2c+1 of rk);
 // the highest-ranked child is returned as the next entry instead.
 __device__ __forceinline__ bool push_ranked(int2* stk, int& sp, unsigned mask, const int4& ch, const float (&tn)[4],
@@ -807,11 +861,17 @@ __device__ __forceinline__ int32_t leaf_scan_dispatch(const DMesh& m, TRay& r, u
   return leaf_scan<MOTION, -1>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
 }
 
-template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB>
+template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB, int SS>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order,
                     int walk_tail) {
-  int2 stk[kStackCapacity];
+  extern __shared__ int stack_smem[];
+  SplitStack<SS> stk;
+  if (SS > 0) {
+    stk.stride = blockDim.x;
+    stk.sn = stack_smem + threadIdx.x;
+    stk.st = reinterpret_cast<float*>(stack_smem + SS * blockDim.x) + threadIdx.x;
+  }
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lanes_below = (1u << lane) - 1u;
   TRay r;
@@ -908,7 +968,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
             node = -1;
             walking = false;
           } else {
-            const int2 e = stk[--sp];
+            const int2 e = stk.get(--sp);
             node = e.x;
             nodeT = __int_as_float(e.y);
           }
@@ -932,7 +992,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         if (ch.w == kEmptyChild || r.tclosest < tn[3]) mask &= ~8u;
         int next = 0;
         float nextT = 0.f;
-        if (push_ranked(stk, sp, mask, ch, tn, rk, next, nextT, status)) {
+        if (push_ranked_s(stk, sp, mask, ch, tn, rk, next, nextT, status)) {
           node = next;
           nodeT = nextT;
         } else if (status != kStatusOk) {
@@ -942,7 +1002,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
           node = -1;
           walking = false;
         } else {
-          const int2 e = stk[--sp];
+          const int2 e = stk.get(--sp);
           node = e.x;
           nodeT = __int_as_float(e.y);
         }
@@ -965,7 +1025,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         if ((ANY && idx != -1) || sp == 0) {  // shadow rays stop at the first hit leaf (intersect.go:231-236)
           done = true;
         } else {
-          const int2 e = stk[--sp];
+          const int2 e = stk.get(--sp);
           node = e.x;
           nodeT = __int_as_float(e.y);
           if (PF && !MOTION && node >= 0) prefetch_l1(m.nodes + node);
@@ -1478,13 +1538,31 @@ int launch_persistent(K k, const TraceLaunch& l, int block, A... args) {
 // tuning.kernel: bit 0 = while-while (else step-scheduled), bit 1 = L1
 // prefetch of the next node, bit 2 = 64-register cap (while-while, 128
 // threads, 8 resident blocks), bit 3 = ray reordering (host side).
+template <class K, class... A>
+int launch_persistent_smem(K k, const TraceLaunch& l, int block, size_t smem, A... args) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(&per_sm, k, block, smem, cudaOccupancyDefault);
+  if (per_sm < 1) per_sm = 1;
+  if (l.grid > 0 && l.grid < per_sm) per_sm = l.grid;
+  k<<<sms * per_sm, block, smem, (cudaStream_t)l.stream>>>(args...);
+  return (int)cudaGetLastError();
+}
+
 template <bool MOTION, bool ANY, bool COUNT, int MINB>
 int launch_ww(const DMesh& mesh, const TraceLaunch& l, int block) {
   const int tail = l.walk_tail;
+  if (l.kernel & kKernelSharedStack) {
+    constexpr int SS = kSharedStackEntries;
+    return launch_persistent_smem(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, SS>, l, block,
+                                  (size_t)SS * block * 8, mesh, l.rays, l.hits, l.n, l.scratch, l.order, tail);
+  }
   if (l.kernel & kKernelPrefetch)
-    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, MINB>, l, block, mesh, l.rays, l.hits, l.n,
+    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, MINB, 0>, l, block, mesh, l.rays, l.hits, l.n,
                              l.scratch, l.order, tail);
-  return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB>, l, block, mesh, l.rays, l.hits, l.n,
+  return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, 0>, l, block, mesh, l.rays, l.hits, l.n,
                            l.scratch, l.order, tail);
 }
 
