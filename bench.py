@@ -329,10 +329,39 @@ def render_extras(ctx, args):
       guided_slit            equal-wall-time relMSE on the slit-light room
                              against a 4096-spp float64 plain render, at
                              256x256 instead of 1024x1024 so that the reference
-                             render fits the benchmark's time"""
+                             render fits the benchmark's time
+      qbvh_build             the 2,097,152-triangle QBVH build (BuildAccel,
+                             leafMax 16) by the device builder and by the host
+                             builder, with the oracle's single-threaded
+                             restatement of the reference builder timed beside
+                             them; the two product builds must be identical"""
     from oracle import orc
     from vermeer_gb300 import scenes
+    import vermeer_gb300 as vg
     out = {}
+    # QBVH build
+    bv, bip = scenes.triangle_soup(1 << 21, 3)
+    res = {}
+    for b, name in ((vg.BUILD_DEVICE, "device"), (vg.BUILD_HOST, "host")):
+        ctx.set_builder(b)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            g = ctx.mesh_build(bv, bip)
+            ctx.sync()
+            ts.append(time.perf_counter() - t0)
+        res[name] = (min(ts), ctx.mesh_export(g)["nodes"].tobytes())
+    ctx.set_builder(vg.BUILD_AUTO)
+    t0 = time.perf_counter()
+    orc.Mesh(bv, bip)
+    odt = time.perf_counter() - t0
+    out["qbvh_build"] = {
+        "workload": "2,097,152-triangle soup (seed 3), QBVH leafMax 16, wall time of vmr_mesh_build (upload, build, "
+                    "device tables)",
+        "device_ms": round(res["device"][0] * 1e3, 2), "host_ms": round(res["host"][0] * 1e3, 2),
+        "host_threads": cpu_threads(), "identical": res["device"][1] == res["host"][1],
+        "cpu_baseline": {"ms": round(odt * 1e3, 2), "cores": 1, "kind": "port",
+                         "sample": "the whole build, oracle/orc_core.cpp (C++ restatement of qbvh.BuildAccel)"}}
     # reference mode, small room
     sc = scenes.small_room(16384, seed=1)
     ctx.load_scene(sc)

@@ -700,8 +700,9 @@ int vmr_autotune(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, in
     if (src[k]) VMR_CUDA(ctx, cudaMemcpyAsync(f + k * nf, src[k], n * 4, kind, st));
   int32_t* hb = reinterpret_cast<int32_t*>(f + 8 * nf);
   vmr_hits dh{hb, nullptr, f + 9 * nf, f + 10 * nf, f + 11 * nf, f + 12 * nf};
-  // candidates: while-while (with/without reordering, register cap, tail
-  // cutoff, key width) and the step-scheduled kernel
+  // candidates: while-while (with/without reordering, register cap, the
+  // shared-memory stack top, tail cutoff, key width) and the step-scheduled
+  // kernel
   std::vector<vmr_tuning> cands;
   for (int k : {13, 9, 29})
     for (int tail : {0, 2, 4, 8})

@@ -29,6 +29,7 @@
 //    come out as in the reference.
 // Input whose build geometry is not finite is declined (the host builder
 // takes it).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -41,6 +42,8 @@
 
 namespace vmr {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr int kLeafMax = 16;
 constexpr int kMaxLevels = 4096;
@@ -80,12 +83,42 @@ struct Smem {
   static constexpr int W = BS / 32;
   float part[W][8][6];
   int pcnt[W][8];
+  float wcb[W][6];
+  int wsum[W][2];
+  // this CTA's partial results, read by the other CTAs of the cluster
+  float cb[6];
   float bin[8][6];
   int cnt[8];
-  float cb[W][6];
-  int wsum[W][2];
+  int sw_count[2];
   float scale, origin;
   int axis, flat, plane, nL, P;
+};
+
+// The CTAs that build one node: a thread-block cluster of CL CTAs (CL = 1:
+// a single CTA).  Each CTA owns a contiguous slice of every range; partial
+// results are exchanged through distributed shared memory in rank order, so
+// all CTAs derive identical split decisions.
+template <int CL>
+struct Team {
+  int rank;
+  __device__ Team() {
+    if constexpr (CL > 1) rank = (int)cg::this_cluster().block_rank();
+    else rank = 0;
+  }
+  __device__ __forceinline__ void sync() const {
+    if constexpr (CL > 1) cg::this_cluster().sync();  // barrier.cluster arrive.release / wait.acquire
+    else __syncthreads();
+  }
+  template <class T>
+  __device__ __forceinline__ T* peer(T* p, int r) const {
+    if constexpr (CL > 1) return cg::this_cluster().map_shared_rank(p, r);
+    else return p;
+  }
+  // [lo, hi) of an n-element range owned by this CTA
+  __device__ __forceinline__ void slice(int n, int& lo, int& hi) const {
+    lo = (int)(((long long)n * rank) / CL);
+    hi = (int)(((long long)n * (rank + 1)) / CL);
+  }
 };
 
 __device__ __forceinline__ float warp_min(float v) {
@@ -107,8 +140,8 @@ __device__ __forceinline__ int warp_sum(int v) {
 template <int BS>
 __device__ void copy_range(const float4* __restrict__ SA, const float4* __restrict__ SB,
                            const float4* __restrict__ SC, float4* __restrict__ DA, float4* __restrict__ DB,
-                           float4* __restrict__ DC, int f, int n) {
-  for (int i = threadIdx.x; i < n; i += BS) {
+                           float4* __restrict__ DC, int f, int lo, int hi) {
+  for (int i = lo + (int)threadIdx.x; i < hi; i += BS) {
     DA[f + i] = SA[f + i];
     DB[f + i] = SB[f + i];
     DC[f + i] = SC[f + i];
@@ -120,40 +153,55 @@ __device__ __forceinline__ int bin_of(float c, float scale, float origin) {
 }
 
 // binarySplit + calcMinCost (build.go:28-178) over [f, f+n) of S, the
-// partitioned range written to D.  Returns (axis, pivot).
-template <int BS>
+// partitioned range written to D.  Returns (axis, pivot) in every thread of
+// every CTA of the team.
+template <int BS, int CL>
 __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ SB, const float4* __restrict__ SC,
                       float4* __restrict__ DA, float4* __restrict__ DB, float4* __restrict__ DC, int* __restrict__ sw,
-                      int* __restrict__ rk, int f, int n, int* err, Smem<BS>& sh) {
+                      int* __restrict__ rk, int f, int n, int* err, Smem<BS>& sh, const Team<CL>& team) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  __syncthreads();  // shared state of a previous split is no longer read
+  constexpr int W = Smem<BS>::W;
+  const float inf = __int_as_float(0x7f800000);
+  int lo, hi;
+  team.slice(n, lo, hi);
+  team.sync();  // shared state of a previous split is no longer read, here or by peers
   if (n <= kLeafMax) {
-    copy_range<BS>(SA, SB, SC, DA, DB, DC, f, n);
+    copy_range<BS>(SA, SB, SC, DA, DB, DC, f, lo, hi);
     return make_int2(0, n);
   }
   // Centroid bounds.
-  float lo0 = __int_as_float(0x7f800000), lo1 = lo0, lo2 = lo0;
-  float hi0 = -lo0, hi1 = -lo0, hi2 = -lo0;
-  for (int i = tid; i < n; i += BS) {
+  float l0 = inf, l1 = inf, l2 = inf, h0 = -inf, h1 = -inf, h2 = -inf;
+  for (int i = lo + tid; i < hi; i += BS) {
     const float4 c = SC[f + i];
-    lo0 = gmin(c.x, lo0); lo1 = gmin(c.y, lo1); lo2 = gmin(c.z, lo2);
-    hi0 = gmax(c.x, hi0); hi1 = gmax(c.y, hi1); hi2 = gmax(c.z, hi2);
+    l0 = gmin(c.x, l0); l1 = gmin(c.y, l1); l2 = gmin(c.z, l2);
+    h0 = gmax(c.x, h0); h1 = gmax(c.y, h1); h2 = gmax(c.z, h2);
   }
-  lo0 = warp_min(lo0); lo1 = warp_min(lo1); lo2 = warp_min(lo2);
-  hi0 = warp_max(hi0); hi1 = warp_max(hi1); hi2 = warp_max(hi2);
+  l0 = warp_min(l0); l1 = warp_min(l1); l2 = warp_min(l2);
+  h0 = warp_max(h0); h1 = warp_max(h1); h2 = warp_max(h2);
   if (lane == 0) {
-    sh.cb[warp][0] = lo0; sh.cb[warp][1] = lo1; sh.cb[warp][2] = lo2;
-    sh.cb[warp][3] = hi0; sh.cb[warp][4] = hi1; sh.cb[warp][5] = hi2;
+    sh.wcb[warp][0] = l0; sh.wcb[warp][1] = l1; sh.wcb[warp][2] = l2;
+    sh.wcb[warp][3] = h0; sh.wcb[warp][4] = h1; sh.wcb[warp][5] = h2;
   }
   __syncthreads();
   if (tid == 0) {
-    float b[6];
-    for (int k = 0; k < 6; ++k) b[k] = sh.cb[0][k];
-    for (int w = 1; w < Smem<BS>::W; ++w)
+    float b[6] = {inf, inf, inf, -inf, -inf, -inf};
+    for (int w = 0; w < W; ++w)
       for (int k = 0; k < 3; ++k) {
-        b[k] = gmin(sh.cb[w][k], b[k]);
-        b[3 + k] = gmax(sh.cb[w][3 + k], b[3 + k]);
+        b[k] = gmin(sh.wcb[w][k], b[k]);
+        b[3 + k] = gmax(sh.wcb[w][3 + k], b[3 + k]);
       }
+    for (int k = 0; k < 6; ++k) sh.cb[k] = b[k];
+  }
+  team.sync();
+  if (tid == 0) {
+    float b[6] = {inf, inf, inf, -inf, -inf, -inf};
+    for (int r = 0; r < CL; ++r) {
+      const float* pc = team.peer(sh.cb, r);
+      for (int k = 0; k < 3; ++k) {
+        b[k] = gmin(pc[k], b[k]);
+        b[3 + k] = gmax(pc[3 + k], b[3 + k]);
+      }
+    }
     // BoundingBox.MaxDim (math/boundingbox.go:54-70)
     const float e0 = __fsub_rn(b[3], b[0]), e1 = __fsub_rn(b[4], b[1]), e2 = __fsub_rn(b[5], b[2]);
     int axis;
@@ -167,7 +215,7 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
   __syncthreads();
   const int axis = sh.axis;
   if (sh.flat) {  // build.go:34-43
-    copy_range<BS>(SA, SB, SC, DA, DB, DC, f, n);
+    copy_range<BS>(SA, SB, SC, DA, DB, DC, f, lo, hi);
     return make_int2(axis, n / 2 + 1);
   }
   const float scale = sh.scale, origin = sh.origin;
@@ -178,10 +226,10 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
   for (int k = 0; k < 8; ++k) {
     bc[k] = 0;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { bl[k][a] = __int_as_float(0x7f800000); bh[k][a] = -__int_as_float(0x7f800000); }
+    for (int a = 0; a < 3; ++a) { bl[k][a] = inf; bh[k][a] = -inf; }
   }
   bool bad = false;
-  for (int i = tid; i < n; i += BS) {
+  for (int i = lo + tid; i < hi; i += BS) {
     const float4 c = SC[f + i], a = SA[f + i], b = SB[f + i];
     int bin = bin_of(comp(c, axis), scale, origin);
     if (bin < 0 || bin > 7) { bad = true; bin = bin < 0 ? 0 : 7; }
@@ -209,10 +257,9 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
   __syncthreads();
   if (tid < 8) {
     const int k = tid;
-    int c = sh.pcnt[0][k];
-    float v[6];
-    for (int a = 0; a < 6; ++a) v[a] = sh.part[0][k][a];
-    for (int w = 1; w < Smem<BS>::W; ++w) {
+    int c = 0;
+    float v[6] = {inf, inf, inf, -inf, -inf, -inf};
+    for (int w = 0; w < W; ++w) {
       c += sh.pcnt[w][k];
       for (int a = 0; a < 3; ++a) {
         v[a] = gmin(v[a], sh.part[w][k][a]);
@@ -222,26 +269,42 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
     sh.cnt[k] = c;
     for (int a = 0; a < 6; ++a) sh.bin[k][a] = v[a];
   }
-  __syncthreads();
+  team.sync();
   if (tid == 0) {
+    float bin[8][6];
+    int cnt8[8];
+    for (int k = 0; k < 8; ++k) {
+      cnt8[k] = 0;
+      for (int a = 0; a < 3; ++a) { bin[k][a] = inf; bin[k][3 + a] = -inf; }
+    }
+    for (int r = 0; r < CL; ++r) {
+      const float* pb = &team.peer(&sh.bin[0][0], r)[0];
+      const int* pn = team.peer(&sh.cnt[0], r);
+      for (int k = 0; k < 8; ++k) {
+        cnt8[k] += pn[k];
+        for (int a = 0; a < 3; ++a) {
+          bin[k][a] = gmin(bin[k][a], pb[k * 6 + a]);
+          bin[k][3 + a] = gmax(bin[k][3 + a], pb[k * 6 + 3 + a]);
+        }
+      }
+    }
     // Costs from the left and from the right (build.go:68-107).
     float lb[8][6], rb[8][6];
     int ln[8], rn[8];
     float acc[6];
-    const float inf = __int_as_float(0x7f800000);
     for (int a = 0; a < 3; ++a) { acc[a] = inf; acc[3 + a] = -inf; }
     int cnt = 0;
     for (int i = 0; i < 8; ++i) {
-      for (int a = 0; a < 3; ++a) { acc[a] = gmin(acc[a], sh.bin[i][a]); acc[3 + a] = gmax(acc[3 + a], sh.bin[i][3 + a]); }
-      cnt += sh.cnt[i];
+      for (int a = 0; a < 3; ++a) { acc[a] = gmin(acc[a], bin[i][a]); acc[3 + a] = gmax(acc[3 + a], bin[i][3 + a]); }
+      cnt += cnt8[i];
       for (int a = 0; a < 6; ++a) lb[i][a] = acc[a];
       ln[i] = cnt;
     }
     for (int a = 0; a < 3; ++a) { acc[a] = inf; acc[3 + a] = -inf; }
     cnt = 0;
     for (int i = 7; i >= 0; --i) {
-      for (int a = 0; a < 3; ++a) { acc[a] = gmin(acc[a], sh.bin[i][a]); acc[3 + a] = gmax(acc[3 + a], sh.bin[i][3 + a]); }
-      cnt += sh.cnt[i];
+      for (int a = 0; a < 3; ++a) { acc[a] = gmin(acc[a], bin[i][a]); acc[3 + a] = gmax(acc[3 + a], bin[i][3 + a]); }
+      cnt += cnt8[i];
       for (int a = 0; a < 6; ++a) rb[i][a] = acc[a];
       rn[i] = cnt;
     }
@@ -262,7 +325,7 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
     }
     int nL = 0;
     for (int k = 0; k < 8; ++k)
-      if (k < plane) nL += sh.cnt[k];
+      if (k < plane) nL += cnt8[k];
     int P = nL;
     if (nL < n && bin_of(comp(SC[f + nL], axis), scale, origin) >= plane) P = nL + 1;
     sh.plane = plane;
@@ -271,13 +334,40 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
   }
   __syncthreads();
   const int plane = sh.plane, nL = sh.nL, P = sh.P;
-  // Ranks of the switch elements.
-  int runL = 0, runR = 0;
   const unsigned below = (1u << lane) - 1u;
-  for (int base = 0; base < n; base += BS) {
+  // Switch elements of this CTA's slice, then the slices before it.
+  int baseL = 0, baseR = 0, kL = 0, kR = 0;
+  if constexpr (CL > 1) {
+    int cl = 0, cr = 0;
+    for (int i = lo + tid; i < hi; i += BS) {
+      const bool right = bin_of(comp(SC[f + i], axis), scale, origin) >= plane;
+      cl += (i < P && right);
+      cr += (i >= P && !right);
+    }
+    cl = warp_sum(cl);
+    cr = warp_sum(cr);
+    if (lane == 0) { sh.wsum[warp][0] = cl; sh.wsum[warp][1] = cr; }
+    __syncthreads();
+    if (tid == 0) {
+      int a = 0, b2 = 0;
+      for (int w = 0; w < W; ++w) { a += sh.wsum[w][0]; b2 += sh.wsum[w][1]; }
+      sh.sw_count[0] = a;
+      sh.sw_count[1] = b2;
+    }
+    team.sync();
+    for (int r = 0; r < CL; ++r) {
+      const int* pc = team.peer(sh.sw_count, r);
+      if (r < team.rank) { baseL += pc[0]; baseR += pc[1]; }
+      kL += pc[0];
+      kR += pc[1];
+    }
+    __syncthreads();  // wsum is reused below
+  }
+  int runL = baseL, runR = baseR;
+  for (int base = lo; base < hi; base += BS) {
     const int i = base + tid;
     bool fl = false, fr = false;
-    if (i < n) {
+    if (i < hi) {
       const bool right = bin_of(comp(SC[f + i], axis), scale, origin) >= plane;
       fl = i < P && right;
       fr = i >= P && !right;
@@ -286,7 +376,7 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
     if (lane == 0) { sh.wsum[warp][0] = __popc(ml); sh.wsum[warp][1] = __popc(mr); }
     __syncthreads();
     int offL = 0, offR = 0, totL = 0, totR = 0;
-    for (int w = 0; w < Smem<BS>::W; ++w) {
+    for (int w = 0; w < W; ++w) {
       const int a = sh.wsum[w][0], b = sh.wsum[w][1];
       if (w < warp) { offL += a; offR += b; }
       totL += a;
@@ -306,10 +396,14 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
     runR += totR;
     __syncthreads();
   }
-  const int kL = runL, kR = runR;
-  if (tid == 0 && kL - kR != P - nL) atomicOr(err, kErrPartition);
+  if constexpr (CL == 1) {
+    kL = runL;
+    kR = runR;
+  }
+  if (tid == 0 && team.rank == 0 && kL - kR != P - nL) atomicOr(err, kErrPartition);
+  team.sync();  // every switch position of the range is written
   // Scatter to the partitioned order.
-  for (int i = tid; i < n; i += BS) {
+  for (int i = lo + tid; i < hi; i += BS) {
     const float4 a = SA[f + i], b = SB[f + i], c = SC[f + i];
     const bool right = bin_of(comp(c, axis), scale, origin) >= plane;
     int d;
@@ -336,17 +430,21 @@ __device__ int2 split(const float4* __restrict__ SA, const float4* __restrict__ 
   return make_int2(axis, nL);
 }
 
-// One tree level: each CTA builds the node of one task (build.go:180-192)
-// and appends its inner children to the next level.
-template <int BS>
+// One tree level: each team (a CTA or a cluster) builds the node of one
+// task (build.go:180-192) and appends its inner children to the next level.
+template <int BS, int CL>
 __global__ void __launch_bounds__(BS) k_build_level(Bufs b, int t0) {
   __shared__ Smem<BS> sh;
-  const int t = t0 + blockIdx.x;
+  const Team<CL> team;
+  const int t = t0 + (int)blockIdx.x / CL;
   const int f = b.tasks[t].first, n = b.tasks[t].n;
-  const int2 s0 = split<BS>(b.A, b.B, b.C, b.TA, b.TB, b.TC, b.sw, b.rk, f, n, b.err, sh);
-  const int2 s1 = split<BS>(b.TA, b.TB, b.TC, b.A, b.B, b.C, b.sw, b.rk, f, s0.y, b.err, sh);
-  const int2 s2 = split<BS>(b.TA, b.TB, b.TC, b.A, b.B, b.C, b.sw, b.rk, f + s0.y, n - s0.y, b.err, sh);
-  if (threadIdx.x == 0) {
+  const int2 s0 = split<BS, CL>(b.A, b.B, b.C, b.TA, b.TB, b.TC, b.sw, b.rk, f, n, b.err, sh, team);
+  // split 1 and 2 read the whole of split 0's output
+  team.sync();
+  const int2 s1 = split<BS, CL>(b.TA, b.TB, b.TC, b.A, b.B, b.C, b.sw, b.rk, f, s0.y, b.err, sh, team);
+  const int2 s2 = split<BS, CL>(b.TA, b.TB, b.TC, b.A, b.B, b.C, b.sw, b.rk, f + s0.y, n - s0.y, b.err, sh, team);
+  team.sync();  // no CTA leaves while a peer may still read its shared memory
+  if (threadIdx.x == 0 && team.rank == 0) {
     BTask& T = b.tasks[t];
     T.p0 = s0.y;
     T.p1 = s1.y;
@@ -572,6 +670,54 @@ __global__ void k_leaf_order(const float4* __restrict__ A, const uint32_t* __res
 
 int blocks(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+template <int BS, int CL>
+cudaError_t launch_cluster_level(const Bufs& b, int t0, int count, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(count * CL));
+  cfg.blockDim = dim3(BS);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (CL > 8) {
+    cudaError_t e = cudaFuncSetAttribute(k_build_level<BS, CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaLaunchKernelEx(&cfg, k_build_level<BS, CL>, b, t0);
+}
+
+// Team shape per level: clusters of 16 and 8 CTAs for the few large nodes of
+// the upper levels, one CTA per node below.
+cudaError_t launch_level(const Bufs& b, int t0, int count, cudaStream_t s) {
+  if (count <= 2) {
+    int clusters = 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(512);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    // 16-CTA clusters where the device schedules them, else 8
+    if (cudaFuncSetAttribute(k_build_level<512, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess &&
+        cudaOccupancyMaxActiveClusters(&clusters, k_build_level<512, 16>, &cfg) == cudaSuccess && clusters > 0)
+      return launch_cluster_level<512, 16>(b, t0, count, s);
+    cudaGetLastError();
+    return launch_cluster_level<512, 8>(b, t0, count, s);
+  }
+  if (count <= 64) return launch_cluster_level<512, 8>(b, t0, count, s);
+  k_build_level<128, 1><<<count, 128, 0, s>>>(b, t0);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 int device_build_mesh(HostMesh& m, DevBuf& tris_out, cudaStream_t s, std::string& err) {
@@ -638,9 +784,7 @@ int device_build_mesh(HostMesh& m, DevBuf& tris_out, cudaStream_t s, std::string
   while (lb < le) {
     if ((int)levels.size() >= kMaxLevels) { err = "QBVH build recursion does not terminate"; return kBuildError; }
     const int count = le - lb;
-    if (count <= 64) k_build_level<512><<<count, 512, 0, s>>>(b, lb);
-    else k_build_level<128><<<count, 128, 0, s>>>(b, lb);
-    VB_CHECK(cudaGetLastError());
+    VB_CHECK(launch_level(b, lb, count, s));
     VB_CHECK(cudaMemcpyAsync(hc, b.n_tasks, sizeof(hc), cudaMemcpyDeviceToHost, s));
     VB_CHECK(cudaStreamSynchronize(s));
     if (hc[1] & kErrBin) { err = "QBVH build: centroid bin out of range"; return kBuildError; }

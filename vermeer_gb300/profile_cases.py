@@ -7,6 +7,7 @@
     python -m vermeer_gb300.profile_cases render_ref   reference-mode render, small room,
                                                        256x256, 16 iterations
     python -m vermeer_gb300.profile_cases jobs         64 uneven jobs in one launch
+    python -m vermeer_gb300.profile_cases build        device QBVH build of the 1M-triangle soup
 
 Inputs are the seeded synthetic scenes of vermeer_gb300.scenes.
 """
@@ -63,7 +64,15 @@ def jobs(ctx):
     ctx.trace_jobs(js)
 
 
-CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "jobs": jobs}
+def build(ctx):
+    from . import scenes
+    from .api import BUILD_DEVICE
+    v, ip = scenes.triangle_soup(1 << 20, 2)
+    ctx.set_builder(BUILD_DEVICE)
+    ctx.mesh_build(v, ip)
+
+
+CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "jobs": jobs, "build": build}
 
 
 def main(argv):
