@@ -396,14 +396,15 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideTrain tr, const __nv_b
     float weight = 0.f, om[3] = {0.f, 0.f, 1.f};
     if (valid) {
       const GuideRows& in = tr.rows;
-      const float p[3] = {in.px[row], in.py[row], in.pz[row]};
-      const float nn[3] = {in.nx[row], in.ny[row], in.nz[row]};
-      const float wo[3] = {in.wx[row], in.wy[row], in.wz[row]};
+      const uint64_t e = row * in.rstride;
+      const float p[3] = {in.px[e], in.py[e], in.pz[e]};
+      const float nn[3] = {in.nx[e], in.ny[e], in.nz[e]};
+      const float wo[3] = {in.wx[e], in.wy[e], in.wz[e]};
       features(p, nn, wo, in.lo, in.inv_ext, f);
-      weight = tr.weight[row];
-      om[0] = tr.ox[row];
-      om[1] = tr.oy[row];
-      om[2] = tr.oz[row];
+      weight = tr.weight[e];
+      om[0] = tr.ox[e];
+      om[1] = tr.oy[e];
+      om[2] = tr.oz[e];
       for (int k = 0; k < 80; ++k) save[(size_t)k * B + row] = __float2bfloat16_rn(f[k]);
     } else {
       for (int k = 0; k < 80; ++k) f[k] = 0.f;
@@ -814,7 +815,12 @@ int vmr_guide_init(vmr_ctx* ctx, uint64_t seed) {
     const float bound = std::sqrt(6.0f / (float)kin[l]) * (l == 4 ? 0.1f : 1.0f);
     for (int i = off[l]; i < off[l + 1]; ++i) {
       const double u = (double)(smix(seed * 0x9E3779B97F4A7C15ull + (uint64_t)i + 1) >> 11) * (1.0 / 9007199254740992.0);
-      w[i] = (float)((2.0 * u - 1.0) * bound);
+      // First layer: the weights of encoding frequency 2^k start scaled by
+      // 0.7^k, so the untrained network varies smoothly over the scene and
+      // the high frequencies grow only where the data ask for them.
+      const int col = (i - off[l]) % 80;
+      const double damp = (l == 0 && col < 72) ? std::pow(0.7, (double)((col % 24) / 2)) : 1.0;
+      w[i] = (float)((2.0 * u - 1.0) * bound * damp);
     }
   }
   rc = guide_upload(ctx, w.data());

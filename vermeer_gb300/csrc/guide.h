@@ -12,12 +12,15 @@ constexpr int kGuideWeights = 19968;  // W0 64x80, W1..W3 64x64, W4 40x64
 constexpr uint32_t kSaveRows = 640;   // feature-major rows saved per training record
 
 // Path vertices (SoA, device pointers): hit point, shading normal, direction
-// toward the previous vertex; n rows, or *n_dev rows when n_dev is set.
+// toward the previous vertex; n rows, or *n_dev rows when n_dev is set.  The
+// training kernel reads row r at element r * rstride of every array
+// (inference reads rows contiguously).
 struct GuideRows {
   const float *px, *py, *pz, *nx, *ny, *nz, *wx, *wy, *wz;
   uint64_t n;
   const unsigned long long* n_dev;
   float lo[3], inv_ext[3];  // scene bounds: q = (p - lo) * inv_ext
+  uint32_t rstride = 1;
 };
 
 // Training records: the rows plus the sampled direction and its weight

@@ -106,6 +106,9 @@ struct PtBatch {
   uint32_t rcap;
   unsigned long long* rcount;  // [2]: records this batch, records in total
   uint32_t* last_rec;          // per path: its last record awaiting L_mark
+  float* snee;                 // 7 * cap: per shadow slot, the vertex's normal and
+                               // direction toward the previous vertex, and the
+                               // light sample's training weight (0: no record)
 };
 
 // Training record columns: vertex (p, n, wo), sampled direction, weight
@@ -113,6 +116,7 @@ struct PtBatch {
 // radiance before the next vertex, path.
 constexpr int kRecCols = 21;
 enum RecCol { kRP = 0, kRN = 3, kRWo = 6, kROm = 9, kRW = 12, kRQ = 13, kRBeta = 14, kRMark = 17, kRPath = 20 };
+constexpr uint32_t kNoPath = 0xffffffffu;  // path column of a light-sample record
 
 // ------------------------------------------------------------- random ----
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
@@ -382,6 +386,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
     bool want_rec = false;
     V3 rP = v3(0, 0, 0), rN = v3(0, 0, 0), rWi = v3(0, 0, 0);
     float rQ = 0.f;
+    float nee_w = 0.f;  // TRAIN: the light sample's record weight
     if (active) {
       p = qp[i];
       const V3 D = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
@@ -502,6 +507,17 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
                   }
                   sc3 = c;
                   want_shadow = true;
+                  if (TRAIN && guided) {
+                    // incident radiance x |cos| over the light's density, with
+                    // the light's MIS weight: summed with the continuation
+                    // records (whose emission carries the other weight) it
+                    // estimates the product the guide is fitted to
+                    const float lum = 0.2126f * l.Le[0] + 0.7152f * l.Le[1] + 0.0722f * l.Le[2];
+                    const float wt = lum * w * fabsf(dot(sc.N, Ld)) / pl;
+                    nee_w = isfinite(wt) ? fminf(wt, 1e4f) : 0.f;
+                    rN = sc.N;
+                    rWi = wi;
+                  }
                 }
               }
             }
@@ -584,6 +600,12 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
       b.scontrib[si] = sc3.x;
       b.scontrib[b.cap + si] = sc3.y;
       b.scontrib[2 * (size_t)b.cap + si] = sc3.z;
+      if (TRAIN) {
+        const size_t c = b.cap;
+        b.snee[si] = rN.x; b.snee[c + si] = rN.y; b.snee[2 * c + si] = rN.z;
+        b.snee[3 * c + si] = rWi.x; b.snee[4 * c + si] = rWi.y; b.snee[5 * c + si] = rWi.z;
+        b.snee[6 * c + si] = nee_w;
+      }
     }
     const unsigned long long ni = warp_append(&b.qlen[d + 1], want_next);
     if (want_next && ni < b.cap) {
@@ -613,6 +635,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_targets(PtBatch b) {
   const size_t c = b.rcap;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t p = __float_as_uint(b.rec[(size_t)kRPath * c + i]);
+    if (p == kNoPath) continue;  // a light-sample record: weight already set
     const float Lf[3] = {b.lx[p], b.ly[p], b.lz[p]};
     float lin[3];
     for (int k = 0; k < 3; ++k) {
@@ -633,24 +656,51 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_targets(PtBatch b) {
 }
 
 // Records of training step s: [s*B, s*B + B) clipped to the batch's count.
-__global__ void k_pt_train_count(const unsigned long long* rcount, uint32_t rcap, uint64_t off, uint64_t B,
-                                 unsigned long long* out) {
+// Training step s of S takes records s, s + S, s + 2S, ... (every depth and
+// pixel of the batch, not one block of queue order), at most B of them.
+__global__ void k_pt_train_count(const unsigned long long* rcount, uint32_t rcap, uint64_t s, uint64_t S,
+                                 uint64_t B, unsigned long long* out) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const uint64_t n = rcount[0] < rcap ? rcount[0] : rcap;
-  const uint64_t m = n > off ? n - off : 0;
+  const uint64_t m = n > s ? (n - s + S - 1) / S : 0;
   *out = m < B ? m : B;
 }
 
 // Unoccluded shadow rays add their contribution, in queue order (each path
 // has at most one shadow ray per bounce, so no two threads touch one path).
+// TRAIN: an unoccluded light sample of a guided vertex becomes a training
+// record (direction toward the light, weight from the shade kernel; its path
+// column is the marker kNoPath so the targets pass keeps the weight).
+template <bool TRAIN>
 __global__ void __launch_bounds__(kPtBlock) k_pt_resolve(PtBatch b, uint32_t d) {
   const uint64_t n = b.slen[d] < b.cap ? b.slen[d] : b.cap;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    if (b.shit[i] >= 0) continue;
-    const uint32_t p = b.spath[i];
-    b.lx[p] = b.lx[p] + b.scontrib[i];
-    b.ly[p] = b.ly[p] + b.scontrib[b.cap + i];
-    b.lz[p] = b.lz[p] + b.scontrib[2 * (size_t)b.cap + i];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t nround = (n + stride - 1) / stride;
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  for (uint64_t r = 0; r < nround; ++r) {
+    const uint64_t i = r * stride + tid;
+    const bool lit = i < n && b.shit[i] < 0;
+    if (lit) {
+      const uint32_t p = b.spath[i];
+      b.lx[p] = b.lx[p] + b.scontrib[i];
+      b.ly[p] = b.ly[p] + b.scontrib[b.cap + i];
+      b.lz[p] = b.lz[p] + b.scontrib[2 * (size_t)b.cap + i];
+    }
+    if (TRAIN) {
+      const size_t c = b.cap;
+      const float wt = lit ? b.snee[6 * c + i] : 0.f;
+      const unsigned long long ri = warp_append(&b.rcount[0], wt > 0.f);
+      if (wt > 0.f && ri < b.rcap) {
+        const float* sr = b.sray;
+        const V3 dir = normalize(v3(sr[3 * c + i], sr[4 * c + i], sr[5 * c + i]));
+        const float v[13] = {sr[i], sr[c + i], sr[2 * c + i], b.snee[i], b.snee[c + i], b.snee[2 * c + i],
+                             b.snee[3 * c + i], b.snee[4 * c + i], b.snee[5 * c + i], dir.x, dir.y, dir.z, wt};
+        float* R = b.rec;
+        const size_t rc = b.rcap;
+        for (int k = 0; k < 13; ++k) R[(size_t)k * rc + ri] = v[k];
+        R[(size_t)kRPath * rc + ri] = __uint_as_float(kNoPath);
+      }
+    }
   }
 }
 
@@ -778,7 +828,8 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool g
       s.kernel = ctx->tuning.kernel;
       s.walk_tail = ctx->tuning.walk_tail;
       if (launch_trace_scene(ctx->top.dtop, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
-      k_pt_resolve<<<grid, kPtBlock, 0, st>>>(b, d);
+      if (train) k_pt_resolve<true><<<grid, kPtBlock, 0, st>>>(b, d);
+      else k_pt_resolve<false><<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
     }
   }
@@ -909,7 +960,8 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   }
   const float alpha = p->guide_fraction > 0.0f ? p->guide_fraction : 0.5f;
   if (guided && !(alpha < 1.0f)) return pfail(ctx, VMR_ERR_INVALID, "guide_fraction must be below 1");
-  const uint64_t rcap = train ? std::min<uint64_t>(cap * std::max<uint32_t>(1, p->max_depth), 0xffffffffull) : 0;
+  // continuation and light-sample records: at most two per vertex
+  const uint64_t rcap = train ? std::min<uint64_t>(2 * cap * std::max<uint32_t>(1, p->max_depth), 0xffffffffull) : 0;
   const uint32_t tsteps = p->train_steps ? p->train_steps : 4;
   const uint32_t tbatch = p->train_batch ? p->train_batch : 65536;
   const float tlr = p->train_lr > 0.0f ? p->train_lr : 1e-3f;
@@ -935,7 +987,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
                o_shader = carve(std::max<size_t>(1, R.shaders.size()) * sizeof(vmr_shader_std)),
                o_log = carve(log.size() * 4), o_grow = carve(guided ? cap * 9 * 4 : 0),
                o_gout = carve(guided ? cap * 40 * 4 : 0), o_rec = carve(rcap * kRecCols * 4),
-               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32);
+               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32), o_snee = carve(train ? cap * 7 * 4 : 0);
   PCUDA(R.ptbuf.ensure(bytes));
   char* base = R.ptbuf.as<char>();
   uint64_t fwd[52], inv[52];
@@ -1007,6 +1059,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   b.rcap = (uint32_t)rcap;
   b.rcount = train ? reinterpret_cast<unsigned long long*>(base + o_rcnt) : nullptr;
   b.last_rec = train ? reinterpret_cast<uint32_t*>(base + o_last) : nullptr;
+  b.snee = train ? reinterpret_cast<float*>(base + o_snee) : nullptr;
   if (train) PCUDA(cudaMemsetAsync(b.rcount, 0, 32, st));
   guide::GuideRows grows{};
   if (guided) {
@@ -1098,8 +1151,8 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
       }
       unsigned long long* ncount = b.rcount + 2;
       for (uint32_t s = 0; s < tsteps; ++s) {
-        const uint64_t off = (uint64_t)s * tbatch;
-        k_pt_train_count<<<1, 32, 0, st>>>(b.rcount, b.rcap, off, tbatch, ncount);
+        const uint64_t off = s;
+        k_pt_train_count<<<1, 32, 0, st>>>(b.rcount, b.rcap, off, tsteps, tbatch, ncount);
         PCUDA(cudaGetLastError());
         guide::GuideTrain tr{};
         tr.rows = grows;
@@ -1110,6 +1163,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
         tr.rows.wx = R + kRWo * c + off; tr.rows.wy = R + (kRWo + 1) * c + off; tr.rows.wz = R + (kRWo + 2) * c + off;
         tr.rows.n = tbatch;
         tr.rows.n_dev = ncount;
+        tr.rows.rstride = tsteps;
         tr.ox = R + kROm * c + off; tr.oy = R + (kROm + 1) * c + off; tr.oz = R + (kROm + 2) * c + off;
         tr.weight = R + kRW * c + off;
         tr.stride = stride;

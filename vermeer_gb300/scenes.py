@@ -43,7 +43,8 @@ def unit_sphere(seed: int, n: int, stream: int) -> np.ndarray:
 
 
 def triangle_soup(n_tris: int, seed: int, lo=0.0, hi=1.0, edge=0.005) -> tuple[np.ndarray, np.ndarray]:
-    """A soup of n_tris triangles: centroid uniform in [lo,hi)^3, each vertex
+    """A soup of n_tris triangles: centroid uniform in [lo,hi)^3 (lo and hi
+    scalars or per-axis triples), each vertex
     at centroid + edge * (a direction uniform on the sphere).  Returns
     (verts float32 [3n,3], idxp uint32 [3n]) - the PolyMesh form without
     FaceIdx, whose face i uses vertices 3i..3i+2 (polymesh/init.go:108-130)."""
@@ -381,9 +382,12 @@ def slit_room(n_tris: int = 200_000, seed: int = 5, width: int = 1024, height: i
     room, sits in a 0.4-deep chamber behind the x = 2 wall; the wall is cut
     by a horizontal slit 0.06 high across its whole depth (2% of its area),
     the only way the light reaches the room.  n_tris random diffuse
-    triangles (centroids uniform in the room's interior, vertices at
-    centroid + 0.03 x a direction on the sphere), every surface Lambert with
-    albedo 0.7, pinhole camera inside the room at the image's aspect."""
+    triangles built like the small room's soup (centroids uniform in the
+    room's interior, vertices at centroid + 0.02 x a direction on the
+    sphere, in world units: a ray from the interior runs a median 0.4 before
+    it meets one, and the slit is in view from about a sixth of the
+    interior), every surface Lambert with albedo 0.7, pinhole camera inside
+    the room at the image's aspect."""
     f = np.float32
     tris = _box_faces((-2.0, 0.0, 0.0), (2.0, 3.0, 3.0), skip=("x1",))
     # the x = 2 wall below and above the slit (normals toward -x)
@@ -392,10 +396,8 @@ def slit_room(n_tris: int = 200_000, seed: int = 5, width: int = 1024, height: i
     # the light chamber (open toward the room)
     tris += _box_faces((2.0, 0.0, 0.0), (2.4, 3.0, 3.0), skip=("x0",))
     room = np.asarray(tris, f)
-    sv, sidx = triangle_soup(n_tris, seed, lo=0.0, hi=1.0, edge=0.03)
-    c = np.asarray([[-1.8, 0.2, 0.3]], f)
-    e = np.asarray([[3.6, 2.6, 2.5]], f)
-    sv = (c + sv * e).astype(f)  # centroids spread over the interior box
+    c = np.asarray([-1.8, 0.2, 0.3])
+    sv, sidx = triangle_soup(n_tris, seed, lo=c, hi=c + np.asarray([3.6, 2.6, 2.5]), edge=0.02)
     shaders = [dict(diffuse_colour=(0.7, 0.7, 0.7), diffuse_strength=1.0, diffuse_roughness=0.0),
                dict(emission_colour=(1.0, 1.0, 1.0), emission_strength=200.0, diffuse_colour=(0.0, 0.0, 0.0),
                     diffuse_strength=1.0, diffuse_roughness=0.0)]
