@@ -352,6 +352,56 @@ int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n);
 int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n);
 int vmr_set_sphere_lights(vmr_ctx* ctx, const vmr_sphere_light* lights, uint32_t n);
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* camera);
+
+/* Pixel filters for filter importance sampling: replaces core.Init of a
+ * PixelFilter node (core/core.go:88-89, core/pixelfilter.go:8-10) with the
+ * GaussianFilter and AiryFilter nodes (builtin/filter/gauss.go, airy.go).
+ * The sample's position inside its pixel (the fractional part of the
+ * RasterXY coordinates) is warped by the filter's tabulated distribution
+ * (Sampler.WarpSample, builtin/filter/filter.go:40-80, tables built as
+ * CreateSampler does, filter.go:87-166) before the camera ray is made
+ * (core/render.go:99-107); the sample still lands in its own pixel's
+ * running mean.  Applies to vmr_render and vmr_render_path.  res, width
+ * and peak <= 0 take the nodes' defaults (Gaussian res 17, width 2; Airy
+ * res 49, width 6, peak 4).  Note: the Airy filter at an odd res samples its
+ * centre, where 2 J1(v)/v is 0/0; as in the reference, the table is then
+ * NaN and every sample stays at its pixel's centre. */
+enum {
+    VMR_FILTER_BOX = 0,       /* no warp (no PixelFilter node) */
+    VMR_FILTER_GAUSSIAN = 1,
+    VMR_FILTER_AIRY = 2
+};
+typedef struct {
+    int kind;
+    int res;       /* table resolution (Res), >= 2 */
+    float width;   /* Width */
+    float peak;    /* Peak (Airy only) */
+} vmr_pixel_filter;
+int vmr_set_pixel_filter(vmr_ctx* ctx, const vmr_pixel_filter* filter);
+/* The filter's Sampler.WarpSample (builtin/filter/filter.go:40-80,
+ * core.PixelFilter.WarpSample, core/pixelfilter.go:8-10) on the host, for n
+ * sample pairs (r0, r1) in [0, 1): the offsets (u, v) from the pixel centre
+ * that the camera kernels apply.  Needs no context or GPU. */
+int vmr_pixel_filter_warp(const vmr_pixel_filter* filter, const double* r0, const double* r1, size_t n, double* u,
+                          double* v);
+
+/* ------------------------------------------------------- output drivers */
+/* The OutputHDR driver's pixel bytes, encoded on the device: replaces the
+ * loop of image/hdr/writer.go:58-82 (called by OutputHDR.PostRender,
+ * builtin/driver/outputhdr.go:26-55) over core.FrameBuf().  rgb: the
+ * width*height*3 float framebuffer (row-major, top row first, as vmr_render
+ * and vmr_render_path write it); rgbe: width*height*4 bytes in the file's
+ * order, scanline j = image row height-1-j, each pixel convertRGBToRGBE's
+ * (r, g, b, e) (image/hdr/hdr.go:28-55, float32 arithmetic, Go's byte
+ * conversions).  The caller writes the text header ("#?RADIANCE",
+ * "FORMAT=32-bit_rle_rgbe", "+Y h +X w") and then these bytes.  Flags:
+ * VMR_IO_DEVICE_IN / VMR_IO_DEVICE_OUT mark rgb / rgbe as device pointers
+ * (otherwise host memory, copied inside the call). */
+enum {
+    VMR_IO_DEVICE_IN = 1,
+    VMR_IO_DEVICE_OUT = 2
+};
+int vmr_encode_rgbe(vmr_ctx* ctx, const float* rgb, uint32_t width, uint32_t height, int flags, uint8_t* rgbe);
 /* core.Render in reference mode (core/render.go:140-218 with ShaderStd's
  * direct lighting): iterations iter_begin..iter_begin+iter_count-1 of every
  * pixel, folded into fb (host, width*height*3 floats, in/out) as

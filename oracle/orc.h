@@ -160,6 +160,24 @@ typedef struct {
 
 typedef struct orc_render orc_render;
 
+/* Pixel filter for filter importance sampling (builtin/filter/filter.go):
+ * kind 0 none (box), 1 GaussianFilter (gauss.go; defaults res 17, width 2),
+ * 2 AiryFilter (airy.go; defaults res 49, width 6, peak 4). */
+typedef struct {
+    int kind;
+    int res;
+    float width;
+    float peak;
+} orc_pixel_filter;
+/* Sampler.WarpSample (filter.go:40-80) of n sample pairs. */
+int orc_filter_warp(const orc_pixel_filter* f, const double* r0, const double* r1, size_t n, double* u, double* v);
+/* CreateSampler's cdfV (res) and cdfVU (res x res, row j = cdfVU[j]). */
+int orc_filter_tables(const orc_pixel_filter* f, double* cdfV, double* cdfVU);
+
+/* OutputHDR's pixel bytes (image/hdr/writer.go:58-82, convertRGBToRGBE,
+ * image/hdr/hdr.go:28-55): out = w*h*4 bytes, scanline j = row h-1-j. */
+int orc_encode_rgbe(const float* rgb, uint32_t w, uint32_t h, uint8_t* out);
+
 /* An analytic sphere geom (builtin/geom/sphere): usable wherever a mesh is
  * (scenes, renders); its shader is the mesh's shader 0. */
 orc_mesh* orc_sphere_create(const float center[3], float radius);
@@ -175,6 +193,10 @@ orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, u
                               const uint32_t* shader_list, const orc_shader* shaders, uint32_t n_shaders,
                               const orc_trilight* lights, uint32_t n_lights, const orc_camera* cam);
 void orc_render_destroy(orc_render* r);
+/* The render's pixel filter (core.Init of a PixelFilter node, core/core.go:88-89):
+ * the RasterXY sample's position in its pixel is warped before the camera
+ * ray is made (core/render.go:99-107).  kind 0 removes it. */
+int orc_render_set_filter(orc_render* r, const orc_pixel_filter* f);
 /* Append DiskLights to the light list (after the TriLights). */
 int orc_render_add_disk_lights(orc_render* r, const orc_disklight* lights, uint32_t n);
 /* Append SphereLights (after the DiskLights). */

@@ -36,9 +36,9 @@ assert ORC_NODE_DTYPE.itemsize == 128 and ORC_MNODE_DTYPE.itemsize == 40
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (g++, -ffp-contract=off)."""
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (g++, -ffp-contract=off); make
+    rebuilds only when a source is newer than the library."""
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 
@@ -147,6 +147,62 @@ def _register_render(L):
     L.orc_guide_out_grad.argtypes = [P, P, ctypes.c_double, P, P]
     L.orc_guide_loss_grad.restype = ctypes.c_double
     L.orc_guide_loss_grad.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, P]
+    L.orc_filter_warp.restype = ctypes.c_int
+    L.orc_filter_warp.argtypes = [P, P, P, ctypes.c_size_t, P, P]
+    L.orc_filter_tables.restype = ctypes.c_int
+    L.orc_filter_tables.argtypes = [P, P, P]
+    L.orc_render_set_filter.restype = ctypes.c_int
+    L.orc_render_set_filter.argtypes = [P, P]
+    L.orc_encode_rgbe.restype = ctypes.c_int
+    L.orc_encode_rgbe.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, P]
+
+
+class OrcPixelFilter(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("res", ctypes.c_int), ("width", ctypes.c_float), ("peak", ctypes.c_float)]
+
+
+FILTER_DEFAULTS = {1: dict(res=17, width=2.0, peak=0.0), 2: dict(res=49, width=6.0, peak=4.0)}
+
+
+def _pixel_filter(d):
+    """A pixel-filter dict (kind 1 GaussianFilter, 2 AiryFilter; res, width,
+    peak default to the nodes' defaults) as the C struct."""
+    kind = int(d["kind"])
+    dflt = FILTER_DEFAULTS.get(kind, dict(res=0, width=0.0, peak=0.0))
+    return OrcPixelFilter(kind, int(d.get("res", dflt["res"])), float(d.get("width", dflt["width"])),
+                          float(d.get("peak", dflt["peak"])))
+
+
+def filter_warp(f, r0, r1):
+    """Sampler.WarpSample over arrays r0, r1 in [0, 1): returns (u, v)."""
+    r0 = np.ascontiguousarray(r0, np.float64)
+    r1 = np.ascontiguousarray(r1, np.float64)
+    u = np.empty_like(r0)
+    v = np.empty_like(r0)
+    pf = _pixel_filter(f)
+    if lib().orc_filter_warp(ctypes.byref(pf), _ptr(r0), _ptr(r1), r0.size, _ptr(u), _ptr(v)) != 0:
+        raise ValueError("bad pixel filter")
+    return u, v
+
+
+def encode_rgbe(fb):
+    """OutputHDR's pixel bytes of a float framebuffer [h, w, 3]: [h, w, 4]
+    uint8 in file order (bottom row first)."""
+    fb = np.ascontiguousarray(fb, np.float32)
+    h, w = fb.shape[:2]
+    out = np.empty((h, w, 4), np.uint8)
+    lib().orc_encode_rgbe(_ptr(fb), w, h, _ptr(out))
+    return out
+
+
+def filter_tables(f):
+    """CreateSampler's (cdfV [res], cdfVU [res, res])."""
+    pf = _pixel_filter(f)
+    a = np.empty(pf.res, np.float64)
+    b = np.empty((pf.res, pf.res), np.float64)
+    if lib().orc_filter_tables(ctypes.byref(pf), _ptr(a), _ptr(b)) != 0:
+        raise ValueError("bad pixel filter")
+    return a, b
 
 
 class Guide:
@@ -288,6 +344,10 @@ class Render:
                 sarr[i].radius = float(d["radius"])
                 sarr[i].samples, sarr[i].shader, sarr[i].mesh = int(d.get("samples", 1)), int(d["shader"]), int(d["mesh"])
             lib().orc_render_add_sphere_lights(self.h, sarr, len(sls))
+        if scene.get("pixel_filter"):
+            self._filter = _pixel_filter(scene["pixel_filter"])
+            if lib().orc_render_set_filter(self.h, ctypes.byref(self._filter)) != 0:
+                raise ValueError("bad pixel filter")
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -31,6 +31,15 @@ struct MeshView {
 };
 MeshView mesh_view(const orc_mesh* m);
 
+// A pixel filter's sampling tables (filter.go Sampler): n = 0 is no filter.
+struct FilterTable {
+  int n = 0;
+  double w = 0.0;
+  std::vector<double> cdfV, cdfVU;  // cdfVU row-major, row j = cdfVU[j]
+};
+FilterTable make_filter(const orc_pixel_filter& f);
+void warp_sample(const FilterTable& t, double r0, double r1, double& u, double& v);
+
 // What orc_render_create was given, for the extended path tracer (orc_pt.cpp).
 struct RenderScene {
   const orc_scene* scene;
@@ -39,13 +48,15 @@ struct RenderScene {
   std::vector<orc_shader> shaders;
   std::vector<orc_trilight> lights;
   orc_camera cam;
+  FilterTable filter;
 };
 RenderScene render_scene(const orc_render* r);
 
 // core.Render's per-sample setup and the pinhole Camera.ComputeRay
 // (core/render.go:89-120, builtin/camera/camera.go:244-284) for iteration j
-// (render(iter+1)) of pixel pix: ray origin, direction and time.
+// (render(iter+1)) of pixel pix: ray origin, direction and time; filt (may
+// be null or empty) warps the sample inside its pixel first.
 void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uint64_t pix, uint64_t seed, float P[3],
-                    float D[3], float* time);
+                    float D[3], float* time, const FilterTable* filt = nullptr);
 
 }  // namespace orc_internal

@@ -378,6 +378,7 @@ struct Render {
   std::vector<orc_trilight> tri_lights;
   std::vector<Light> lights;
   orc_camera cam;
+  orc_internal::FilterTable filter;
 };
 
 // EvalEmission (std.go:299-316).
@@ -943,11 +944,18 @@ struct orc_render {
 namespace orc_internal {
 
 void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uint64_t pix, uint64_t seed, float Po[3],
-                    float Do[3], float* time) {
+                    float Do[3], float* time, const FilterTable* filt) {
   const uint32_t x = (uint32_t)(pix % w), y = (uint32_t)(pix / w);
   double rx, ry;
   orc_raster_xy(12, j, x, y, 0, 0, &rx, &ry);  // render.go:89
   *time = (float)vdc(j, scramble(seed, pix, 2));
+  if (filt && filt->n > 0) {  // filter importance sampling (render.go:99-107)
+    const double fx = std::floor(rx), fy = std::floor(ry);
+    double u, v;
+    warp_sample(*filt, rx - fx, ry - fy, u, v);
+    rx = fx + 0.5 + u;
+    ry = fy + 0.5 + v;
+  }
   const float Sx = (float)(-1.0 + 2.0 * (rx / (double)w));
   const float Sy = -(float)(-1.0 + 2.0 * (ry / (double)h));
   // Camera.ComputeRay (camera.go:244-284): pinhole, or a thin lens of
@@ -983,6 +991,7 @@ RenderScene render_scene(const orc_render* o) {
   for (const Shader& sh : r.shaders) s.shaders.push_back(sh.p);
   s.lights = r.tri_lights;
   s.cam = r.cam;
+  s.filter = r.filter;
   return s;
 }
 
@@ -991,6 +1000,13 @@ RenderScene render_scene(const orc_render* o) {
 extern "C" {
 
 uint64_t orc_scramble(uint64_t seed, uint64_t pix, uint32_t k) { return scramble(seed, pix, k); }
+
+int orc_render_set_filter(orc_render* r, const orc_pixel_filter* f) {
+  if (!r || !f) return -1;
+  if (f->kind != 0 && f->res < 2) return -1;
+  r->r.filter = orc_internal::make_filter(*f);
+  return 0;
+}
 
 orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, uint32_t n_meshes,
                               const uint32_t* off, const uint32_t* cnt, const uint32_t* list, const orc_shader* shaders,
@@ -1034,7 +1050,7 @@ int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, u
         if (s >= npix) break;
         for (size_t pix = s; pix < std::min(npix, s + 256); ++pix) {
           float Pf[3], Df[3], tf;
-          orc_internal::camera_primary(R.cam, w, h, j, pix, seed, Pf, Df, &tf);
+          orc_internal::camera_primary(R.cam, w, h, j, pix, seed, Pf, Df, &tf, &R.filter);
           const V3 P = v3(Pf[0], Pf[1], Pf[2]), D = v3(Df[0], Df[1], Df[2]);
           const double time = (double)tf;
           const double lambda = (720.0 - 450.0) * vdc(j, scramble(seed, pix, 3)) + 450.0;

@@ -87,6 +87,14 @@ class Camera(ctypes.Structure):
                 ("focal", ctypes.c_float), ("radius", ctypes.c_float)]
 
 
+class PixelFilter(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("res", ctypes.c_int), ("width", ctypes.c_float), ("peak", ctypes.c_float)]
+
+
+FILTER_BOX, FILTER_GAUSSIAN, FILTER_AIRY = 0, 1, 2
+IO_DEVICE_IN, IO_DEVICE_OUT = 1, 2
+
+
 class RenderParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
                 ("seed", ctypes.c_uint64), ("max_batch_samples", U32)]
@@ -161,6 +169,9 @@ SIGNATURES = {
     "vmr_set_sphere_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_sphere_add": (ctypes.c_int, [P, P, ctypes.c_float, ctypes.POINTER(U32)]),
     "vmr_set_camera": (ctypes.c_int, [P, ctypes.POINTER(Camera)]),
+    "vmr_set_pixel_filter": (ctypes.c_int, [P, ctypes.POINTER(PixelFilter)]),
+    "vmr_pixel_filter_warp": (ctypes.c_int, [ctypes.POINTER(PixelFilter), P, P, ctypes.c_size_t, P, P]),
+    "vmr_encode_rgbe": (ctypes.c_int, [P, P, U32, U32, ctypes.c_int, P]),
     "vmr_render": (ctypes.c_int, [P, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
     "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_env_light": (ctypes.c_int, [P, P]),

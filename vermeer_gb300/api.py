@@ -37,6 +37,30 @@ class VmrError(RuntimeError):
         self.code = code
 
 
+FILTER_BOX, FILTER_GAUSSIAN, FILTER_AIRY = _lib.FILTER_BOX, _lib.FILTER_GAUSSIAN, _lib.FILTER_AIRY
+
+
+def pixel_filter_warp(kind: int, r0, r1, res: int = 0, width: float = 0.0, peak: float = 0.0):
+    """The pixel filter's Sampler.WarpSample on the host (no GPU): offsets
+    (u, v) from the pixel centre for sample positions (r0, r1) in [0, 1)."""
+    L = _lib.load()
+    r0 = np.ascontiguousarray(r0, np.float64)
+    r1 = np.ascontiguousarray(r1, np.float64)
+    u = np.empty_like(r0)
+    v = np.empty_like(r0)
+    f = _lib.PixelFilter(int(kind), int(res), float(width), float(peak))
+    rc = L.vmr_pixel_filter_warp(ctypes.byref(f), _p(r0), _p(r1), r0.size, _p(u), _p(v))
+    if rc != 0:
+        raise VmrError(rc, "bad pixel filter")
+    return u, v
+
+
+def write_float(path: str, fb):
+    """The OutputFloat driver (builtin/driver/outputfloat.go): the float32
+    framebuffer [h, w, 3] as raw little-endian floats."""
+    np.ascontiguousarray(fb, "<f4").tofile(path)
+
+
 def _p(a):
     if a is None:
         return None
@@ -423,4 +447,41 @@ class Context:
         self.set_quad_lights([dict(q, geom=ids[q["mesh"]]) for q in scene.get("quad_lights", [])])
         self.set_env_light(scene.get("env", (0.0, 0.0, 0.0)))
         self.set_camera(scene["camera"])
+        self.set_pixel_filter(**scene.get("pixel_filter", {"kind": _lib.FILTER_BOX}))
         return ids
+
+    def encode_rgbe(self, fb):
+        """OutputHDR's pixel bytes of a float framebuffer [h, w, 3] (numpy
+        on the host, or a CUDA torch tensor), encoded on the GPU: uint8
+        [h, w, 4] in file order (scanline 0 = the bottom image row)."""
+        if hasattr(fb, "is_cuda") and fb.is_cuda:
+            import torch
+            t = fb.contiguous().float()
+            h, w = t.shape[:2]
+            out = torch.empty((h, w, 4), dtype=torch.uint8, device=t.device)
+            self._check(self.L.vmr_encode_rgbe(self.h, ctypes.c_void_p(t.data_ptr()), w, h,
+                                               _lib.IO_DEVICE_IN | _lib.IO_DEVICE_OUT, ctypes.c_void_p(out.data_ptr())))
+            return out
+        fb = np.ascontiguousarray(fb, np.float32)
+        h, w = fb.shape[:2]
+        out = np.empty((h, w, 4), np.uint8)
+        self._check(self.L.vmr_encode_rgbe(self.h, _p(fb), w, h, 0, _p(out)))
+        return out
+
+    def write_hdr(self, path: str, fb):
+        """The OutputHDR driver (builtin/driver/outputhdr.go): a Radiance
+        .hdr file of the framebuffer, pixels encoded on the GPU."""
+        px = self.encode_rgbe(fb)
+        if not isinstance(px, np.ndarray):
+            px = px.cpu().numpy()
+        h, w = px.shape[:2]
+        with open(path, "wb") as f:
+            f.write(f"#?RADIANCE\n# vermeer_gb300\nFORMAT=32-bit_rle_rgbe\n\n+Y {h} +X {w}\n".encode())
+            f.write(px.tobytes())
+
+    def set_pixel_filter(self, kind: int, res: int = 0, width: float = 0.0, peak: float = 0.0):
+        """The render's pixel filter (GaussianFilter / AiryFilter node):
+        kind FILTER_BOX (none), FILTER_GAUSSIAN or FILTER_AIRY; res, width
+        and peak <= 0 take the nodes' defaults."""
+        f = _lib.PixelFilter(int(kind), int(res), float(width), float(peak))
+        self._check(self.L.vmr_set_pixel_filter(self.h, ctypes.byref(f)))

@@ -70,6 +70,13 @@ struct RenderState {
   float env[3] = {0.f, 0.f, 0.f};
   vmr_camera camera{};
   bool has_camera = false;
+  // pixel filter (vmr_set_pixel_filter): filter_n = 0 is none; the device
+  // table holds cdfV (n) then cdfVU (n x n) as float64
+  uint32_t filter_n = 0;
+  double filter_w = 0.0;
+  std::vector<double> filter_host;
+  DevBuf filter;
+  DevBuf outbuf;   // vmr_encode_rgbe staging for host framebuffers
   DevBuf buf;      // reference mode batch buffers
   DevBuf ptbuf;    // extended mode batch buffers
   void* pt_host = nullptr;  // pinned per-batch parameters (extended mode)

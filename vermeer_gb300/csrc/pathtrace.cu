@@ -69,6 +69,7 @@ struct PtBatch {
   float sel;          // 1/nl
   uint64_t seed;
   vmr_camera cam;
+  PixFilter filt;     // pixel filter tables (n = 0: none)
   const PtIter* it;
   const vmr_shader_std* shaders;
   const PtLight* lights;
@@ -319,7 +320,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
     const uint32_t j = b.it->iter0 + (uint32_t)(s / b.npix) + 1;
     V3 P, D;
     float time, lambda;
-    camera_primary(b.cam, b.width, b.height, j, pix, b.seed, P, D, time, lambda);
+    camera_primary(b.cam, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
     const float o[3] = {P.x, P.y, P.z};
     put_ray(b.qray[0], b.cap, s, o, D, __int_as_float(0x7f800000), time);
     b.qpath[0][s] = (uint32_t)s;
@@ -1016,6 +1017,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   b.sel = nl > 0 ? 1.0f / (float)nl : 0.0f;
   b.seed = p->seed;
   b.cam = R.camera;
+  b.filt = PixFilter{R.filter_n ? R.filter.as<const double>() : nullptr, R.filter_n, R.filter_w};
   b.it = reinterpret_cast<const PtIter*>(base + o_it);
   b.shaders = reinterpret_cast<const vmr_shader_std*>(base + o_shader);
   b.lights = reinterpret_cast<const PtLight*>(base + o_light);
@@ -1104,6 +1106,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
       for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
     };
     fold(&b.cam, sizeof(b.cam));
+    fold(&b.filt, sizeof(b.filt));
     fold(b.env, sizeof(b.env));
     fold(&b.sel, sizeof(b.sel));
     fold(&ctx->top.dtop, sizeof(ctx->top.dtop));

@@ -8,8 +8,9 @@
 // exclusive scan, scatter) gathers the rays into key order: warps then trace
 // rays that start close together and head into the same sixth of the
 // sphere, and the triangle test can use one compile-time permutation per
-// warp.  Order inside a bucket is whatever the atomics give; every ray is
-// traced independently, so results do not depend on it.
+// warp.  Inside a bucket, each warp's rays keep their input order and warps
+// follow the atomics' order; every ray is traced independently, so results
+// do not depend on it.
 #include <cuda_runtime.h>
 
 #include "device.h"
@@ -44,16 +45,40 @@ __device__ __forceinline__ uint32_t ray_class(float dx, float dy, float dz) {
   return 2u * (uint32_t)kz + (dkz < 0.0f ? 1u : 0u);
 }
 
+// Lanes of a warp that share a key take one atomic: the lowest such lane
+// adds their count and hands each its slot in lane order (so a bucket that
+// holds most rays, e.g. camera primaries from one eye, costs one atomic per
+// warp rather than one per ray, and each warp's rays stay together in input
+// order).  Every lane of the warp calls this; invalid lanes pass kNoKey.
+constexpr uint32_t kNoKey = 0xffffffffu;
+__device__ __forceinline__ uint32_t warp_bucket_add(uint32_t* counters, uint32_t key) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t peers = __match_any_sync(0xffffffffu, key);
+  const uint32_t leader = (uint32_t)__ffs(peers) - 1u;
+  uint32_t base = 0;
+  if (lane == leader && key != kNoKey) base = atomicAdd(counters + key, (uint32_t)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, (int)leader);
+  return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// Grid-stride loops below run whole warps (blockDim.x is a multiple of 32)
+// for the same number of rounds, so every lane reaches the warp collectives.
 __global__ void k_ray_keys(RaySoA rays, uint64_t n, float3 lo, float3 inv, uint32_t bits, uint32_t* keys,
                            uint32_t* hist) {
   const float top = (float)((1u << bits) - 1u);
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = ray_class(rays.dx[i], rays.dy[i], rays.dz[i]);
-    const uint32_t m = spread5(cell(rays.px[i], lo.x, inv.x, top)) << 2 | spread5(cell(rays.py[i], lo.y, inv.y, top)) << 1 |
-                       spread5(cell(rays.pz[i], lo.z, inv.z, top));
-    const uint32_t k = (c << (3 * bits)) + m;
-    keys[i] = k;
-    atomicAdd(hist + k, 1u);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t rounds = (n + stride - 1) / stride;
+  for (uint64_t r = 0; r < rounds; ++r) {
+    const uint64_t i = r * stride + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    uint32_t k = kNoKey;
+    if (i < n) {
+      const uint32_t c = ray_class(rays.dx[i], rays.dy[i], rays.dz[i]);
+      const uint32_t m = spread5(cell(rays.px[i], lo.x, inv.x, top)) << 2 |
+                         spread5(cell(rays.py[i], lo.y, inv.y, top)) << 1 | spread5(cell(rays.pz[i], lo.z, inv.z, top));
+      k = (c << (3 * bits)) + m;
+      keys[i] = k;
+    }
+    warp_bucket_add(hist, k);
   }
 }
 
@@ -97,8 +122,12 @@ __global__ void k_ray_scatter(RaySoA rays, uint64_t n, const uint32_t* keys, uin
   float* dz = const_cast<float*>(sorted_out.dz);
   float* tm = const_cast<float*>(sorted_out.tmax);
   float* ti = const_cast<float*>(sorted_out.time);
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t pos = atomicAdd(offsets + keys[i], 1u);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t rounds = (n + stride - 1) / stride;
+  for (uint64_t r = 0; r < rounds; ++r) {
+    const uint64_t i = r * stride + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint32_t pos = warp_bucket_add(offsets, i < n ? keys[i] : kNoKey);
+    if (i >= n) continue;
     order[pos] = (uint32_t)i;
     px[pos] = rays.px[i];
     py[pos] = rays.py[i];

@@ -252,6 +252,7 @@ struct RenderBatch {
   uint32_t pad;
   uint64_t seed;
   vmr_camera cam;
+  PixFilter filt;     // pixel filter tables (n = 0: none)
   const vmr_shader_std* shaders;
   const RLight* lights;
   const RMesh* meshes;
@@ -275,7 +276,7 @@ __global__ void k_generate(RenderBatch b) {
   const uint32_t j = b.iter0 + (uint32_t)(s / b.npix) + 1;  // render(iter+1)
   V3 P, D;
   float time, lambda;
-  camera_primary(b.cam, b.width, b.height, j, pix, b.seed, P, D, time, lambda);
+  camera_primary(b.cam, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
   const Level& L = b.lv[0];
   *ray_f(L, 0, s) = P.x; *ray_f(L, 1, s) = P.y; *ray_f(L, 2, s) = P.z;
   *ray_f(L, 3, s) = D.x; *ray_f(L, 4, s) = D.y; *ray_f(L, 5, s) = D.z;
@@ -902,6 +903,7 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   b.levels = levels;
   b.seed = p->seed;
   b.cam = R.camera;
+  b.filt = PixFilter{R.filter_n ? R.filter.as<const double>() : nullptr, R.filter_n, R.filter_w};
   b.shaders = reinterpret_cast<const vmr_shader_std*>(base + o_shaders);
   b.lights = reinterpret_cast<const RLight*>(base + o_lights);
   b.meshes = reinterpret_cast<const RMesh*>(base + o_meshes);

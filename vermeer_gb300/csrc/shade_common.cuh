@@ -15,6 +15,7 @@
 #include <cstdint>
 
 #include "colour_tables.h"
+#include "pixfilter.h"
 #include "vmr.h"
 
 namespace vmr {
@@ -473,11 +474,18 @@ __device__ __forceinline__ void uniform_disk(float radius, float r0, float r1, f
 // (render(iter+1)) of pixel pix: RasterXY position, VdC time and hero
 // wavelength with the pixel's scrambles, the ray through LocalToWorld.
 __device__ __forceinline__ void camera_primary(const vmr_camera& c, uint32_t width, uint32_t height, uint32_t j,
-                                               uint32_t pix, uint64_t seed, V3& P, V3& D, float& time,
-                                               float& lambda) {
+                                               uint32_t pix, uint64_t seed, const PixFilter& filt, V3& P, V3& D,
+                                               float& time, float& lambda) {
   const uint32_t x = pix % width, y = pix / width;
   double rx, ry;
   raster_xy(j, x, y, rx, ry);
+  if (filt.n > 0) {  // filter importance sampling (core/render.go:99-107)
+    const double fx = floor(rx), fy = floor(ry);
+    double u, v;
+    warp_sample(filt, rx - fx, ry - fy, u, v);
+    rx = fx + 0.5 + u;
+    ry = fy + 0.5 + v;
+  }
   time = (float)vdc(j, scramble(seed, pix, 2));
   lambda = (float)((720.0 - 450.0) * vdc(j, scramble(seed, pix, 3)) + 450.0);
   const float Sx = (float)(-1.0 + 2.0 * (rx / (double)width));
