@@ -385,6 +385,38 @@ int vmr_set_pixel_filter(vmr_ctx* ctx, const vmr_pixel_filter* filter);
 int vmr_pixel_filter_warp(const vmr_pixel_filter* filter, const double* r0, const double* r1, size_t n, double* u,
                           double* v);
 
+/* ------------------------------------------------------------ scene files */
+/* A .vnf scene file into ctx: replaces nodes.Parse (nodes/lex.go,
+ * nodes/parser.go) and core.PreRender (core/core.go:29-104) for the node
+ * types the GPU path renders: Globals, Camera (LookAt, or LocalToWorld),
+ * PolyMesh (PolyCount/FaceIdx fan triangulation, ShaderIdx, Normals and
+ * NormalIdx, motion keys in Verts; polymesh/init.go), Sphere, ShaderStd
+ * (rgb and float maps), TriLight, DiskLight, SphereLight, QuadLight (the
+ * extended mode's quad light; the reference's panics), GaussianFilter,
+ * AiryFilter, OutputHDR, OutputFloat.  Geoms are taken in file order, then
+ * the lights' own meshes in light order, as the reference adds them; each
+ * goes through vmr_mesh_build / vmr_sphere_add and then vmr_scene_build,
+ * the material, light, camera and filter setters.  Lights are grouped by
+ * kind (TriLights, DiskLights, SphereLights) in file order within a kind.
+ * Errors the reference prints and skips stop the load here:
+ * VMR_ERR_INVALID with "file:line: message" in vmr_last_error; DebugShader,
+ * Proc, GeomInstance, rgbtex textures, non-identity PolyMesh transforms and
+ * camera motion keys give VMR_ERR_UNSUPPORTED.  flags: VMR_VNF_MOTION_FIXED
+ * builds motion meshes in VMR_MOTION_FIXED mode (default: faithful).
+ * Works on host-only contexts too (parsing and accelerator builds). */
+enum { VMR_VNF_MOTION_FIXED = 1 };
+typedef struct {
+    uint32_t width, height;   /* Globals XRes, YRes (1024 x 1024 without a Globals node) */
+    int max_iter;             /* Globals MaxIter (16 without a Globals node; 0 = until stopped) */
+    uint32_t n_geoms, n_shaders, n_lights;
+    char camera[64];          /* the render's camera node */
+    char output_hdr[256];     /* OutputHDR Filename ("" if none) */
+    char output_float[256];   /* OutputFloat Filename ("" if none) */
+} vmr_vnf_info;
+int vmr_load_vnf(vmr_ctx* ctx, const char* path, int flags, vmr_vnf_info* info);
+/* The camera the context renders with (as set or loaded). */
+int vmr_get_camera(vmr_ctx* ctx, vmr_camera* camera);
+
 /* ------------------------------------------------------- output drivers */
 /* The OutputHDR driver's pixel bytes, encoded on the device: replaces the
  * loop of image/hdr/writer.go:58-82 (called by OutputHDR.PostRender,

@@ -1,0 +1,166 @@
+""".vnf scene files (vmr_load_vnf): the reference's node syntax
+(nodes/lex.go, nodes/parser.go) and the PreRender steps that turn nodes into
+geometry (polymesh/init.go triangulation, the lights' meshes, the camera).
+
+A scene written by scenes.to_vnf and loaded back must be the scene
+scenes.vnf_order describes (the same geoms in the loader's order), bit for
+bit: CPU tests compare the host-side accelerators, camera and parse
+results on a host-only context; GPU tests compare renders, which must be
+identical images.
+"""
+import numpy as np
+import pytest
+
+import vermeer_gb300 as vg
+from vermeer_gb300 import scenes
+
+INVALID, UNSUPPORTED = -1, -7
+
+
+def _same(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return a.shape == b.shape and a.dtype == b.dtype and a.tobytes() == b.tobytes()
+
+
+def _write(tmp_path, name, text):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+def _load_err(ctx, path):
+    with pytest.raises(vg.VmrError) as e:
+        ctx.load_vnf(path)
+    return e.value.code, str(e.value)
+
+
+MINI = """# a one-triangle scene
+ShaderStd { Name "white" DiffuseColour rgb 1 1 1 DiffuseStrength float 1 }
+PolyMesh {
+  Name "tri"
+  Verts 1 4 point 0 0 0  1 0 0  1 1 0  0 1 0   # a quad
+  PolyCount 1 int 4
+  FaceIdx 4 int 0 1 2 3
+  Shader 1 string "white"
+}
+Camera { Name "camera" Type "LookAt" From 1 1 point 0 0 -3 To 1 1 point 0 0 0 Roll 1 1 float 0 Up 0 1 0 Fov 40 }
+Globals { XRes 32 YRes 16 }
+OutputHDR { Filename "out.hdr" }
+"""
+
+
+def test_vnf_minimal_scene(tmp_path):
+    host_ctx = vg.Context(-1)  # its own context: geom ids start at 0
+    info = host_ctx.load_vnf(_write(tmp_path, "mini.vnf", MINI))
+    assert (info["width"], info["height"], info["max_iter"]) == (32, 16, 0)  # a Globals node's own defaults
+    assert info["n_geoms"] == 1 and info["n_shaders"] == 1 and info["n_lights"] == 0
+    assert info["camera"] == "camera" and info["output_hdr"] == "out.hdr" and info["output_float"] == ""
+    # PolyCount 4 fans into (0,1,2), (0,2,3) (polymesh/init.go)
+    exp = host_ctx.mesh_export(0)
+    assert sorted(map(tuple, np.asarray(exp["idxp"]).reshape(-1, 3).tolist())) == [(0, 1, 2), (0, 2, 3)]
+    # LookAt (camera.go:113-190) with Roll 0 and the aspect from Globals
+    cam = host_ctx.get_camera()
+    ref = scenes.lookat_camera((0, 0, -3), (0, 0, 0), (0, 1, 0), 40.0, 32 / 16)
+    assert np.array_equal(cam["m"], ref["m"])
+    for k in ("tan_theta_focal", "aspect", "focal"):
+        assert cam[k] == ref[k], k
+    host_ctx.close()
+
+
+def test_vnf_defaults_without_globals(host_ctx, tmp_path):
+    text = MINI.replace("Globals { XRes 32 YRes 16 }", "")
+    info = host_ctx.load_vnf(_write(tmp_path, "noglobals.vnf", text))
+    assert (info["width"], info["height"], info["max_iter"]) == (1024, 1024, 16)  # core.Init's defaults
+
+
+@pytest.mark.parametrize("bad,code,what", [
+    (MINI.replace("  Shader 1 string \"white\"\n", ""), INVALID, "required field Shader"),
+    (MINI.replace("PolyCount", "PolyCnt"), INVALID, "PolyCnt"),
+    (MINI.replace("Globals {", "Proc {"), UNSUPPORTED, "Proc"),
+    (MINI.replace("rgb 1 1 1", "rgbtex \"wood.tga\""), UNSUPPORTED, "rgbtex"),
+    (MINI.replace("\"white\"\n}", "\"black\"\n}"), INVALID, "shader black"),
+    (MINI.replace("Name \"camera\"", "Name \"cam2\""), INVALID, "no camera"),
+    (MINI.replace("FaceIdx 4 int 0 1 2 3", "FaceIdx 4 int 0 1 2 7"), INVALID, "out of range"),
+    (MINI.replace("Verts 1 4 point", "Verts 1 4 vec3"), INVALID, "point"),
+    (MINI.replace("Fov 40", "Fov 40 Fov 41"), INVALID, "already"),
+    (MINI + "Bogus {\n}\n", INVALID, "unknown node type Bogus"),
+])
+def test_vnf_errors(host_ctx, tmp_path, bad, code, what):
+    c, msg = _load_err(host_ctx, _write(tmp_path, "bad.vnf", bad))
+    assert c == code and what in msg, msg
+    assert "bad.vnf:" in msg
+
+
+def test_vnf_error_names_the_line(host_ctx, tmp_path):
+    text = MINI.replace("  FaceIdx 4 int 0 1 2 3", "  FaceIdx 4 int 0 1 2 3\n  Colour 1")
+    _, msg = _load_err(host_ctx, _write(tmp_path, "line.vnf", text))
+    assert "line.vnf:8:" in msg, msg  # line 1 is the comment
+
+
+SCENES = {
+    "small_room": lambda: scenes.small_room(1024, seed=3),
+    "disk_thin_lens": lambda: scenes.small_room_disk(1024, seed=4),
+    "spheres": lambda: scenes.small_room_spheres(1024, seed=5),
+    "motion": lambda: scenes.small_room_motion(1024, seed=6, motion_mode=1),
+    "quads_filter": lambda: dict(scenes.small_room_ext(1024, seed=7), pixel_filter={"kind": 1}),
+}
+
+
+def _host_pair(name, tmp_path, w=40, h=30):
+    import vermeer_gb300 as vg_
+    sc = SCENES[name]()
+    path = _write(tmp_path, name + ".vnf", scenes.to_vnf(sc, w, h))
+    motion_fixed = any(m.get("motion_mode", 0) == 1 for m in sc["meshes"])
+    return sc, path, motion_fixed, vg_
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_vnf_round_trip_builds_the_same_scene(tmp_path, name):
+    """Host-only contexts: every accelerator, the top level and the camera
+    of the loaded file equal those of the scene built directly."""
+    sc, path, mf, vg_ = _host_pair(name, tmp_path)
+    a = vg_.Context(-1)
+    b = vg_.Context(-1)
+    try:
+        info = a.load_vnf(path, motion_fixed=mf)
+        ref = scenes.vnf_order(sc)
+        ids = b.load_scene(ref)
+        assert info["n_geoms"] == len(ids)
+        for g in range(len(ids)):
+            if "sphere" in ref["meshes"][g]:
+                continue
+            ea, eb = a.mesh_export(g), b.mesh_export(ids[g])
+            for k in ea:
+                assert _same(ea[k], eb[k]), (g, k)
+        sa, sb = a.scene_export(len(ids)), b.scene_export(len(ids))
+        for k in sa:
+            assert _same(sa[k], sb[k]), k
+        ca, cb = a.get_camera(), b.get_camera()
+        for k in ca:
+            assert _same(ca[k], cb[k]), k
+    finally:
+        a.close()
+        b.close()
+
+
+# ------------------------------------------------------------------ GPU ----
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["small_room", "disk_thin_lens", "spheres", "motion"])
+def test_vnf_render_equals_direct_scene(ctx, tmp_path, name):
+    sc, path, mf, _ = _host_pair(name, tmp_path)
+    ctx.load_scene(scenes.vnf_order(sc))
+    ref, _ = ctx.render(40, 30, 0, 3, 5)
+    info = ctx.load_vnf(path, motion_fixed=mf)
+    got, _ = ctx.render(info["width"], info["height"], 0, 3, 5)
+    assert got.tobytes() == ref.tobytes()
+
+
+@pytest.mark.gpu
+def test_vnf_path_render_with_quads_and_filter(ctx, tmp_path):
+    sc, path, _, _ = _host_pair("quads_filter", tmp_path)
+    ctx.load_scene(scenes.vnf_order(sc))
+    ref, _ = ctx.render_path(40, 30, 0, 4, 5, max_depth=4)
+    ctx.load_vnf(path)
+    got, _ = ctx.render_path(40, 30, 0, 4, 5, max_depth=4)
+    assert got.tobytes() == ref.tobytes()
+    assert float(got.mean()) > 0.0

@@ -95,6 +95,15 @@ FILTER_BOX, FILTER_GAUSSIAN, FILTER_AIRY = 0, 1, 2
 IO_DEVICE_IN, IO_DEVICE_OUT = 1, 2
 
 
+class VnfInfo(ctypes.Structure):
+    _fields_ = [("width", U32), ("height", U32), ("max_iter", ctypes.c_int), ("n_geoms", U32),
+                ("n_shaders", U32), ("n_lights", U32), ("camera", ctypes.c_char * 64),
+                ("output_hdr", ctypes.c_char * 256), ("output_float", ctypes.c_char * 256)]
+
+
+VNF_MOTION_FIXED = 1
+
+
 class RenderParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
                 ("seed", ctypes.c_uint64), ("max_batch_samples", U32)]
@@ -172,6 +181,8 @@ SIGNATURES = {
     "vmr_set_pixel_filter": (ctypes.c_int, [P, ctypes.POINTER(PixelFilter)]),
     "vmr_pixel_filter_warp": (ctypes.c_int, [ctypes.POINTER(PixelFilter), P, P, ctypes.c_size_t, P, P]),
     "vmr_encode_rgbe": (ctypes.c_int, [P, P, U32, U32, ctypes.c_int, P]),
+    "vmr_load_vnf": (ctypes.c_int, [P, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(VnfInfo)]),
+    "vmr_get_camera": (ctypes.c_int, [P, ctypes.POINTER(Camera)]),
     "vmr_render": (ctypes.c_int, [P, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
     "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_env_light": (ctypes.c_int, [P, P]),

@@ -450,6 +450,23 @@ class Context:
         self.set_pixel_filter(**scene.get("pixel_filter", {"kind": _lib.FILTER_BOX}))
         return ids
 
+    def load_vnf(self, path: str, motion_fixed: bool = False) -> dict:
+        """Load a .vnf scene file (vmr_load_vnf): geometry, materials,
+        lights, camera and pixel filter.  Returns the Globals and output
+        settings the file gives (width, height, max_iter, outputs)."""
+        info = _lib.VnfInfo()
+        self._check(self.L.vmr_load_vnf(self.h, str(path).encode(), _lib.VNF_MOTION_FIXED if motion_fixed else 0,
+                                        ctypes.byref(info)))
+        return dict(width=info.width, height=info.height, max_iter=info.max_iter, n_geoms=info.n_geoms,
+                    n_shaders=info.n_shaders, n_lights=info.n_lights, camera=info.camera.decode(),
+                    output_hdr=info.output_hdr.decode(), output_float=info.output_float.decode())
+
+    def get_camera(self) -> dict:
+        c = _lib.Camera()
+        self._check(self.L.vmr_get_camera(self.h, ctypes.byref(c)))
+        return dict(m=np.array(c.m[:], np.float32), tan_theta_focal=np.float32(c.tan_theta_focal),
+                    aspect=np.float32(c.aspect), focal=np.float32(c.focal), radius=np.float32(c.radius))
+
     def encode_rgbe(self, fb):
         """OutputHDR's pixel bytes of a float framebuffer [h, w, 3] (numpy
         on the host, or a CUDA torch tensor), encoded on the GPU: uint8

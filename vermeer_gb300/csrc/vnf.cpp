@@ -1,0 +1,898 @@
+// vnf.cpp - .vnf scene files into a context (vmr_load_vnf).
+//
+// Replaces, for the node types the GPU path renders, what the reference's
+// command does between reading a scene and core.Render: nodes.Parse
+// (nodes/lex.go, nodes/parser.go: the token rules and the typed field
+// syntax), core.AddNode / core.PreRender (core/core.go:29-104: geoms in file
+// order, then the geoms lights create in their PreRender, in light order),
+// PolyMesh.init (builtin/geom/polymesh/init.go: fan triangulation of
+// PolyCount/FaceIdx, per-face ShaderIdx, NormalIdx), the lights' meshes
+// (builtin/light/{triangle,disk,sphere,quad}.go createMesh / PreRender) and
+// Camera.PreRender (builtin/camera/camera.go:80-98, 109-193).  The result is
+// handed to the same C-ABI calls a host binding makes (vmr_mesh_build,
+// vmr_sphere_add, vmr_scene_build, vmr_set_shaders, vmr_mesh_set_shading,
+// the light setters, vmr_set_camera, vmr_set_pixel_filter).
+//
+// Numbers follow the reference: a token with '.', 'e' or 'E' is read as a
+// float64 and rounded to float32 where the field is float32; integer tokens
+// in float fields are converted exactly.  Vector arithmetic for light
+// meshes and the camera is float32 without contraction; normalisation is
+// a * (1/sqrt((x*x + y*y) + z*z)) (an exact reciprocal square root where the
+// reference uses RSQRTSS and one Newton step), the same form the rest of
+// libvmr and the project's scene generator use.
+//
+// Where the reference tolerates an error (prints it and skips the field or
+// node), the loader stops with VMR_ERR_INVALID and the file:line in
+// vmr_last_error; nodes the GPU path does not render (DebugShader, Proc,
+// GeomInstance, textures, non-identity PolyMesh transforms, camera motion
+// keys) give VMR_ERR_UNSUPPORTED.
+#include <cerrno>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+#include "vmr.h"
+
+namespace {
+
+// ------------------------------------------------------------------ lexer
+enum Tk { kEof, kIdent, kStr, kFloat, kInt, kLBr, kRBr, kLCurl, kRCurl, kComma, kBadNum };
+
+struct Token {
+  Tk k = kEof;
+  std::string s;
+  double f = 0.0;
+  int64_t i = 0;
+  int line = 0;
+};
+
+// nodes/lex.go: identifiers start with a letter or '_' and run to white
+// space or one of " [ ] { } , (which is kept); numbers start with '-' or a
+// digit and take digits, '-', '.', 'e', 'E'; "#" ends the line; any other
+// character is skipped.
+class Lexer {
+ public:
+  explicit Lexer(std::string src) : src_(std::move(src)) {}
+  Token next() {
+    if (have_peek_) {
+      have_peek_ = false;
+      return peek_;
+    }
+    return lex();
+  }
+  const Token& peek() {
+    if (!have_peek_) {
+      peek_ = lex();
+      have_peek_ = true;
+    }
+    return peek_;
+  }
+  int line() const { return line_; }
+
+ private:
+  int get() {
+    if (pushed_ >= 0) {
+      const int c = pushed_;
+      pushed_ = -1;
+      return c;
+    }
+    if (pos_ >= src_.size()) return -1;
+    const int c = (unsigned char)src_[pos_++];
+    if (c == '\n') ++line_;
+    if (c == '#') {  // comment: the rest of the line reads as one newline
+      while (pos_ < src_.size() && src_[pos_] != '\n') ++pos_;
+      if (pos_ < src_.size()) {
+        ++pos_;
+        ++line_;
+      }
+      return '\n';
+    }
+    return c;
+  }
+  static bool alpha(int c) { return c == '_' || (c >= 'a' && c <= 'z') || (c >= 'A' && c <= 'Z') || c >= 0x80; }
+
+  Token lex() {
+    for (;;) {
+      const int c = get();
+      Token t;
+      t.line = line_;
+      if (c < 0) return t;
+      if (alpha(c)) {
+        t.k = kIdent;
+        t.s.push_back((char)c);
+        for (;;) {
+          const int d = get();
+          if (d < 0) return Token{kEof, "", 0, 0, line_};
+          if (d == '"' || d == '[' || d == ']' || d == '{' || d == '}' || d == ',') {
+            pushed_ = d;
+            break;
+          }
+          if (d == ' ' || d == '\t' || d == '\r' || d == '\n') break;
+          t.s.push_back((char)d);
+        }
+        return t;
+      }
+      if (c == '-' || (c >= '0' && c <= '9')) {
+        std::string b(1, (char)c);
+        bool is_float = false;
+        int d;
+        for (;;) {
+          d = get();
+          if ((d >= '0' && d <= '9') || d == '-') {
+            b.push_back((char)d);
+          } else if (d == '.' || d == 'e' || d == 'E') {
+            is_float = true;
+            b.push_back((char)d);
+          } else {
+            break;
+          }
+        }
+        if (d >= 0) pushed_ = d;
+        char* end = nullptr;
+        if (is_float) {
+          t.f = std::strtod(b.c_str(), &end);
+          t.k = (end && *end == 0) ? kFloat : kBadNum;
+        } else {
+          errno = 0;
+          t.i = std::strtoll(b.c_str(), &end, 10);
+          t.k = (end && *end == 0 && errno == 0) ? kInt : kBadNum;
+        }
+        t.s = b;
+        return t;
+      }
+      switch (c) {
+        case '[': t.k = kLBr; return t;
+        case ']': t.k = kRBr; return t;
+        case '{': t.k = kLCurl; return t;
+        case '}': t.k = kRCurl; return t;
+        case ',': t.k = kComma; return t;
+        case '"': {
+          t.k = kStr;
+          for (;;) {
+            const int d = get();
+            if (d < 0) return Token{kEof, "", 0, 0, line_};
+            if (d == '"') break;
+            t.s.push_back((char)d);
+          }
+          return t;
+        }
+        default: break;  // white space and unknown characters
+      }
+    }
+  }
+
+  std::string src_;
+  size_t pos_ = 0;
+  int line_ = 1;
+  int pushed_ = -1;
+  bool have_peek_ = false;
+  Token peek_;
+};
+
+// ---------------------------------------------------------- node schemas
+enum Ft {
+  fInt, fFloat, fBool, fString, fVec3, fMatrix, fPoints, fVec3s, fVec2s, fFloats, fMatrices, fInts, fStrings, fMap
+};
+
+struct FieldSpec {
+  const char* name;
+  Ft t;
+  bool required;
+};
+
+struct NodeSpec {
+  const char* type;
+  std::vector<FieldSpec> fields;
+};
+
+// The node structs' parseable fields (tag "-" skipped; no ",opt" = required).
+const std::vector<NodeSpec>& specs() {
+  static const std::vector<NodeSpec> s = {
+      {"Globals", {{"XRes", fInt, false}, {"YRes", fInt, false}, {"UseProgress", fBool, false},
+                   {"MaxGoRoutines", fInt, false}, {"Camera", fString, false}, {"MaxIter", fInt, false},
+                   {"Output", fString, false}}},
+      {"Camera", {{"Name", fString, true}, {"Type", fString, true}, {"From", fPoints, true}, {"To", fPoints, true},
+                  {"Roll", fFloats, true}, {"Up", fVec3, true}, {"Aspect", fFloat, false}, {"Fov", fFloat, false},
+                  {"Focal", fFloat, false}, {"WorldToLocal", fMatrices, false}, {"LocalToWorld", fMatrices, false},
+                  {"L", fFloat, false}, {"R", fFloat, false}, {"T", fFloat, false}, {"B", fFloat, false},
+                  {"Radius", fFloat, false}}},
+      {"PolyMesh", {{"Name", fString, true}, {"RayBias", fFloat, false}, {"Verts", fPoints, true},
+                    {"PolyCount", fInts, false}, {"FaceIdx", fInts, false}, {"Shader", fStrings, true},
+                    {"ShaderIdx", fInts, false}, {"CalcNormals", fBool, false}, {"IsVisible", fBool, false},
+                    {"Transform", fMatrices, false}, {"UV", fVec2s, false}, {"UVIdx", fInts, false},
+                    {"Normals", fVec3s, false}, {"NormalIdx", fInts, false}}},
+      {"ShaderStd", {{"Name", fString, true}, {"EmissionColour", fMap, false}, {"EmissionStrength", fMap, false},
+                     {"Sides", fInt, false}, {"DiffuseColour", fMap, false}, {"DiffuseStrength", fMap, false},
+                     {"DiffuseRoughness", fMap, false}, {"Spec1Colour", fMap, false}, {"Spec1Strength", fMap, false},
+                     {"Spec1Roughness", fMap, false}, {"Spec1FresnelModel", fString, false},
+                     {"Spec1FresnelRefl", fMap, false}, {"Spec1FresnelEdge", fMap, false}, {"IOR", fMap, false}}},
+      {"TriLight", {{"Name", fString, true}, {"P0", fVec3, true}, {"P1", fVec3, true}, {"P2", fVec3, true},
+                    {"Shader", fString, true}, {"Samples", fInt, true}}},
+      {"DiskLight", {{"Name", fString, true}, {"P", fVec3, true}, {"Up", fVec3, true}, {"LookAt", fVec3, true},
+                     {"Radius", fFloat, true}, {"Shader", fString, true}, {"Segments", fInt, false},
+                     {"Samples", fInt, false}}},
+      {"SphereLight", {{"Name", fString, true}, {"P", fVec3, true}, {"Radius", fFloat, true},
+                       {"Shader", fString, true}, {"Samples", fInt, false}}},
+      {"QuadLight", {{"Name", fString, true}, {"P", fVec3, true}, {"U", fVec3, true}, {"V", fVec3, true},
+                     {"Shader", fString, true}, {"Samples", fInt, false}}},
+      {"Sphere", {{"Name", fString, true}, {"RayBias", fFloat, false}, {"P", fVec3, true}, {"Radius", fFloat, true},
+                  {"Shader", fString, true}}},
+      {"GaussianFilter", {{"Name", fString, true}, {"Width", fFloat, true}, {"Res", fInt, true}}},
+      {"AiryFilter", {{"Name", fString, true}, {"Width", fFloat, false}, {"Res", fInt, false},
+                      {"Peak", fFloat, false}}},
+      {"OutputHDR", {{"Filename", fString, true}}},
+      {"OutputFloat", {{"Filename", fString, true}}},
+  };
+  return s;
+}
+
+// Node types of the reference that this loader does not render.
+bool unsupported_type(const std::string& t) {
+  return t == "DebugShader" || t == "Proc" || t == "GeomInstance" || t == "Instance";
+}
+
+struct Value {
+  Ft t = fInt;
+  int64_t i = 0;
+  double f = 0.0;
+  bool b = false;
+  std::string s;
+  std::vector<float> v;  // vec3, matrix (column-major), arrays (key-major elements)
+  int keys = 0, per = 0;  // arrays: MotionKeys as written, elements per key
+  std::vector<int32_t> ints;
+  std::vector<std::string> strs;
+  float c[3] = {0.f, 0.f, 0.f};  // maps (maps.Constant)
+};
+
+struct Node {
+  std::string type;
+  int line = 0;
+  std::map<std::string, Value> f;
+  bool has(const char* n) const { return f.count(n) != 0; }
+  const Value& at(const char* n) const { return f.at(n); }
+};
+
+struct LoadError {
+  int code;
+  std::string msg;
+};
+
+class Parser {
+ public:
+  Parser(std::string src, std::string name) : lx_(std::move(src)), name_(std::move(name)) {}
+
+  std::vector<Node> parse() {
+    std::vector<Node> out;
+    for (;;) {
+      Token t = lx_.next();
+      if (t.k == kEof) break;
+      if (t.k != kIdent) fail(t.line, "expected a node name");
+      Token b = lx_.next();
+      if (b.k != kLCurl) fail(b.line, "expected '{' after node name " + t.s);
+      if (unsupported_type(t.s))
+        throw LoadError{VMR_ERR_UNSUPPORTED, where(t.line) + "node type " + t.s + " is not rendered by libvmr"};
+      const NodeSpec* spec = nullptr;
+      for (const NodeSpec& s : specs())
+        if (t.s == s.type) spec = &s;
+      if (!spec) fail(t.line, "unknown node type " + t.s);
+      out.push_back(node(*spec, t.line));
+    }
+    return out;
+  }
+
+ private:
+  [[noreturn]] void fail(int line, const std::string& m) { throw LoadError{VMR_ERR_INVALID, where(line) + m}; }
+  std::string where(int line) const { return name_ + ":" + std::to_string(line) + ": "; }
+
+  double number(const char* what) {
+    Token t = lx_.next();
+    if (t.k == kInt) return (double)t.i;
+    if (t.k == kFloat) return t.f;
+    fail(t.line, std::string("expected ") + what);
+  }
+  int64_t integer(const char* what) {
+    Token t = lx_.next();
+    if (t.k != kInt) fail(t.line, std::string("expected ") + what);
+    return t.i;
+  }
+  void keyword(const char* kw) {
+    Token t = lx_.next();
+    if (t.k != kIdent || t.s != kw) fail(t.line, std::string("expected type keyword ") + kw);
+  }
+  // A Matrix4 as written (row after row) stored transposed (Matrix4Transpose).
+  void matrix(std::vector<float>& out) {
+    float m[16];
+    for (int i = 0; i < 16; ++i) m[i] = (float)number("matrix component");
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) out.push_back(m[c * 4 + r]);
+  }
+  // PointArray / Vec3Array / Vec2Array / Float32Array: keys, count, type,
+  // then max(keys, 1) * count elements.
+  void array(Value& v, const char* kw, int comps) {
+    v.keys = (int)integer("number of motion keys");
+    v.per = (int)integer("number of elements");
+    if (v.keys < 0 || v.per < 0) fail(lx_.line(), "negative array size");
+    keyword(kw);
+    const int64_t k = v.keys == 0 ? 1 : v.keys;
+    const int64_t n = k * (int64_t)v.per * comps;
+    if (n > (int64_t)1 << 32) fail(lx_.line(), "array too large");
+    v.v.reserve((size_t)n);
+    for (int64_t j = 0; j < n; ++j) v.v.push_back((float)number("array element"));
+  }
+
+  Value field(Ft t) {
+    Value v;
+    v.t = t;
+    switch (t) {
+      case fInt: {
+        Token a = lx_.next();
+        if (a.k == kFloat) v.i = (int64_t)a.f;
+        else if (a.k == kInt) v.i = a.i;
+        else fail(a.line, "expected a number");
+        break;
+      }
+      case fFloat: v.f = number("a number"); break;
+      case fBool: v.b = integer("0 or 1") != 0; break;
+      case fString: {
+        Token a = lx_.next();
+        if (a.k != kStr) fail(a.line, "expected a string");
+        v.s = a.s;
+        break;
+      }
+      case fVec3:
+        for (int i = 0; i < 3; ++i) v.v.push_back((float)number("vector component"));
+        break;
+      case fMatrix:
+        keyword("matrix");
+        matrix(v.v);
+        break;
+      case fPoints: array(v, "point", 3); break;
+      case fVec3s: array(v, "vec3", 3); break;
+      case fVec2s: array(v, "vec2", 2); break;
+      case fFloats: array(v, "float", 1); break;
+      case fMatrices: {
+        v.keys = (int)integer("number of motion keys");
+        if (v.keys < 0) fail(lx_.line(), "negative key count");
+        keyword("matrix");
+        const int k = v.keys == 0 ? 1 : v.keys;
+        for (int j = 0; j < k; ++j) matrix(v.v);
+        break;
+      }
+      case fInts: {
+        const int64_t n = integer("slice length");
+        if (n < 0 || n > ((int64_t)1 << 31)) fail(lx_.line(), "bad slice length");
+        keyword("int");
+        v.ints.reserve((size_t)n);
+        for (int64_t j = 0; j < n; ++j) v.ints.push_back((int32_t)integer("int"));
+        break;
+      }
+      case fStrings: {
+        const int64_t n = integer("slice length");
+        if (n < 0 || n > ((int64_t)1 << 20)) fail(lx_.line(), "bad slice length");
+        keyword("string");
+        for (int64_t j = 0; j < n; ++j) {
+          Token a = lx_.next();
+          if (a.k != kStr) fail(a.line, "expected a string");
+          v.strs.push_back(a.s);
+        }
+        break;
+      }
+      case fMap: {  // maps.Constant: "rgb r g b" or "float f" (nodes/parser.go rgb, floatmap)
+        Token a = lx_.next();
+        if (a.k == kIdent && a.s == "rgb") {
+          for (int i = 0; i < 3; ++i) v.c[i] = (float)number("RGB component");
+        } else if (a.k == kIdent && a.s == "float") {
+          const float x = (float)number("float component");
+          v.c[0] = v.c[1] = v.c[2] = x;
+        } else if (a.k == kIdent && a.s == "rgbtex") {
+          throw LoadError{VMR_ERR_UNSUPPORTED, where(a.line) + "texture maps (rgbtex) are not supported"};
+        } else {
+          fail(a.line, "expected rgb or float");
+        }
+        break;
+      }
+    }
+    return v;
+  }
+
+  Node node(const NodeSpec& spec, int line) {
+    Node n;
+    n.type = spec.type;
+    n.line = line;
+    for (;;) {
+      Token t = lx_.next();
+      if (t.k == kRCurl) break;
+      if (t.k != kIdent) fail(t.line, "expected a field name in " + n.type);
+      const FieldSpec* fs = nullptr;
+      for (const FieldSpec& f : spec.fields)
+        if (t.s == f.name) fs = &f;
+      if (!fs) fail(t.line, "field \"" + t.s + "\" not found in node " + n.type);
+      if (n.f.count(t.s)) fail(t.line, "field " + t.s + " already found in " + n.type);
+      n.f[t.s] = field(fs->t);
+    }
+    for (const FieldSpec& f : spec.fields)
+      if (f.required && !n.f.count(f.name))
+        fail(line, std::string("required field ") + f.name + " not found in " + n.type);
+    return n;
+  }
+
+  Lexer lx_;
+  std::string name_;
+};
+
+// ------------------------------------------------------ float32 helpers
+struct F3 {
+  float x, y, z;
+};
+F3 f3(const std::vector<float>& v, size_t o = 0) { return F3{v[o], v[o + 1], v[o + 2]}; }
+F3 sub(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+F3 add(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+F3 scl(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
+F3 cross(F3 a, F3 b) { return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+F3 nrm(F3 a) {
+  float s = a.x * a.x + a.y * a.y;
+  s = s + a.z * a.z;
+  const float r = 1.0f / std::sqrt(s);
+  return F3{a.x * r, a.y * r, a.z * r};
+}
+
+// A mesh as the loader hands it to vmr_mesh_build / vmr_mesh_set_shading.
+struct MeshOut {
+  std::vector<float> verts;  // key-major
+  uint32_t n_verts = 0, keys = 1;
+  std::vector<uint32_t> idxp;
+  std::vector<uint8_t> sidx;
+  std::vector<float> normals;  // per vertex (key 0), or empty
+  std::vector<uint32_t> shaders;
+  float ray_bias = 0.0f;
+  bool sphere = false;
+  float centre[3] = {0, 0, 0}, radius = 0.f;
+};
+
+struct Scene {
+  std::vector<vmr_shader_std> shaders;
+  std::map<std::string, uint32_t> shader_id;
+  std::vector<MeshOut> geoms;
+  std::vector<vmr_tri_light> tris;
+  std::vector<vmr_disk_light> disks;
+  std::vector<vmr_sphere_light> spheres;
+  std::vector<vmr_quad_light> quads;
+  vmr_camera cam{};
+  bool has_filter = false;
+  vmr_pixel_filter filter{};
+  vmr_vnf_info info{};
+};
+
+void copy_name(char* dst, size_t cap, const std::string& s) {
+  const size_t n = s.size() < cap - 1 ? s.size() : cap - 1;
+  std::memcpy(dst, s.data(), n);
+  dst[n] = 0;
+}
+
+uint32_t shader_of(const Scene& sc, const Node& n, const std::string& name, const std::string& file) {
+  auto it = sc.shader_id.find(name);
+  if (it == sc.shader_id.end())
+    throw LoadError{VMR_ERR_INVALID, file + ":" + std::to_string(n.line) + ": unable to find shader " + name};
+  return it->second;
+}
+
+// ShaderStd: each field present sets its flag (the reference tests for nil).
+vmr_shader_std shader_std(const Node& n) {
+  vmr_shader_std s{};
+  auto col = [&](const char* f, uint32_t bit, float* dst) {
+    if (!n.has(f)) return;
+    s.flags |= bit;
+    for (int k = 0; k < 3; ++k) dst[k] = n.at(f).c[k];
+  };
+  auto flt = [&](const char* f, uint32_t bit, float* dst) {
+    if (!n.has(f)) return;
+    s.flags |= bit;
+    *dst = n.at(f).c[0];  // maps.Constant.Float32 reads channel 0
+  };
+  col("EmissionColour", VMR_SH_EMISSION_COLOUR, s.emission_colour);
+  flt("EmissionStrength", VMR_SH_EMISSION_STRENGTH, &s.emission_strength);
+  col("DiffuseColour", VMR_SH_DIFFUSE_COLOUR, s.diffuse_colour);
+  flt("DiffuseStrength", VMR_SH_DIFFUSE_STRENGTH, &s.diffuse_strength);
+  flt("DiffuseRoughness", VMR_SH_DIFFUSE_ROUGHNESS, &s.diffuse_roughness);
+  col("Spec1Colour", VMR_SH_SPEC1_COLOUR, s.spec1_colour);
+  flt("Spec1Strength", VMR_SH_SPEC1_STRENGTH, &s.spec1_strength);
+  flt("Spec1Roughness", VMR_SH_SPEC1_ROUGHNESS, &s.spec1_roughness);
+  col("Spec1FresnelRefl", VMR_SH_FRESNEL_REFL, s.spec1_fresnel_refl);
+  col("Spec1FresnelEdge", VMR_SH_FRESNEL_EDGE, s.spec1_fresnel_edge);
+  flt("IOR", VMR_SH_IOR, &s.ior);
+  s.spec1_fresnel = (n.has("Spec1FresnelModel") && n.at("Spec1FresnelModel").s == "Metal") ? 1 : 0;
+  return s;
+}
+
+bool identity(const float* m) {
+  for (int i = 0; i < 16; ++i)
+    if (m[i] != ((i % 5 == 0) ? 1.0f : 0.0f)) return false;
+  return true;
+}
+
+// PolyMesh.init (init.go): fan triangulation, per-face shader index,
+// normal indices; normals with their own index are de-indexed (each
+// triangle corner its own vertex), which leaves every triangle's vertices,
+// and so the accelerator, unchanged.
+MeshOut poly_mesh(const Node& n, const Scene& sc, const std::string& file) {
+  auto where = [&](const std::string& m) { return file + ":" + std::to_string(n.line) + ": PolyMesh: " + m; };
+  MeshOut o;
+  const Value& V = n.at("Verts");
+  o.keys = V.keys == 0 ? 1 : (uint32_t)V.keys;
+  o.n_verts = (uint32_t)V.per;
+  o.verts = V.v;
+  if (n.has("RayBias")) o.ray_bias = (float)n.at("RayBias").f;
+  if (n.has("Transform")) {
+    const Value& T = n.at("Transform");
+    for (size_t k = 0; k * 16 < T.v.size(); ++k)
+      if (!identity(T.v.data() + 16 * k))
+        throw LoadError{VMR_ERR_UNSUPPORTED, where("transformed meshes are not supported")};
+  }
+  for (const std::string& s : n.at("Shader").strs) o.shaders.push_back(shader_of(sc, n, s, file));
+  const std::vector<int32_t> none;
+  const std::vector<int32_t>& fi = n.has("FaceIdx") ? n.at("FaceIdx").ints : none;
+  const std::vector<int32_t>& ni = n.has("NormalIdx") ? n.at("NormalIdx").ints : none;
+  const std::vector<int32_t>& si = n.has("ShaderIdx") ? n.at("ShaderIdx").ints : none;
+  const bool has_n = n.has("Normals") && !n.at("Normals").v.empty();
+  std::vector<uint32_t> nidx;
+  auto chk = [&](const std::vector<int32_t>& a, size_t i) -> uint32_t {
+    if (i >= a.size()) throw LoadError{VMR_ERR_INVALID, where("index array shorter than the polygons need")};
+    return (uint32_t)a[i];
+  };
+  if (n.has("PolyCount")) {
+    uint32_t base = 0;
+    const std::vector<int32_t>& pc = n.at("PolyCount").ints;
+    for (size_t k = 0; k < pc.size(); ++k) {
+      uint32_t i = 0;
+      for (int j = 0; j < (int)pc[k] - 2; ++j) {
+        ++i;
+        const uint32_t c[3] = {base, base + i, base + i + 1};
+        for (uint32_t q : c) o.idxp.push_back(chk(fi, q));
+        if (has_n)
+          for (uint32_t q : c) nidx.push_back(ni.empty() ? chk(fi, q) : chk(ni, q));
+        if (!si.empty()) o.sidx.push_back((uint8_t)chk(si, k));
+      }
+      base += (uint32_t)pc[k];
+    }
+  } else {
+    if (!fi.empty()) {
+      for (size_t j = 0; j < fi.size(); ++j) {
+        o.idxp.push_back((uint32_t)fi[j]);
+        if (has_n) nidx.push_back(ni.empty() ? (uint32_t)fi[j] : chk(ni, j));
+      }
+    } else {
+      for (uint32_t j = 0; j < o.n_verts; ++j) {
+        o.idxp.push_back(j);
+        if (has_n) nidx.push_back(ni.empty() ? j : chk(ni, j));
+      }
+    }
+    for (int32_t s : si) o.sidx.push_back((uint8_t)s);
+  }
+  if (o.idxp.size() % 3) throw LoadError{VMR_ERR_INVALID, where("face indices are not whole triangles")};
+  for (uint32_t v : o.idxp)
+    if (v >= o.n_verts) throw LoadError{VMR_ERR_INVALID, where("face index out of range")};
+  if (!o.sidx.empty() && o.sidx.size() != o.idxp.size() / 3)
+    throw LoadError{VMR_ERR_INVALID, where("ShaderIdx does not give one shader per face")};
+  if (has_n) {
+    const Value& N = n.at("Normals");
+    const size_t nn = (size_t)N.per;
+    for (uint32_t q : nidx)
+      if (q >= nn) throw LoadError{VMR_ERR_INVALID, where("normal index out of range")};
+    if (o.keys > 1) throw LoadError{VMR_ERR_UNSUPPORTED, where("normals of motion meshes are not supported")};
+    bool same = true;
+    for (size_t c = 0; c < nidx.size() && same; ++c) same = nidx[c] == o.idxp[c];
+    if (same && nn >= o.n_verts) {
+      o.normals.assign(N.v.begin(), N.v.begin() + 3 * (size_t)o.n_verts);
+    } else {  // de-index: corner c becomes vertex c
+      std::vector<float> nv, nn3;
+      for (size_t c = 0; c < o.idxp.size(); ++c) {
+        for (int k = 0; k < 3; ++k) nv.push_back(o.verts[3 * (size_t)o.idxp[c] + k]);
+        for (int k = 0; k < 3; ++k) nn3.push_back(N.v[3 * (size_t)nidx[c] + k]);
+      }
+      o.verts = nv;
+      o.normals = nn3;
+      o.n_verts = (uint32_t)o.idxp.size();
+      for (size_t c = 0; c < o.idxp.size(); ++c) o.idxp[c] = (uint32_t)c;
+    }
+  }
+  if ((size_t)o.keys * o.n_verts * 3 != o.verts.size())
+    throw LoadError{VMR_ERR_INVALID, where("Verts holds the wrong number of values")};
+  return o;
+}
+
+MeshOut tri_light_mesh(F3 p0, F3 p1, F3 p2, uint32_t shader) {  // triangle.go:537-565
+  MeshOut o;
+  const F3 N = nrm(cross(sub(p1, p0), sub(p2, p0)));
+  o.verts = {p0.x, p0.y, p0.z, p1.x, p1.y, p1.z, p2.x, p2.y, p2.z};
+  o.n_verts = 3;
+  o.idxp = {0, 1, 2};
+  o.normals = {N.x, N.y, N.z, N.x, N.y, N.z, N.x, N.y, N.z};
+  o.shaders = {shader};
+  return o;
+}
+
+MeshOut disk_light_mesh(F3 P, F3 up, F3 at, float R, int segments, uint32_t shader) {  // disk.go:88-90, 224-258
+  MeshOut o;
+  const F3 N = nrm(sub(at, P));
+  const F3 T = nrm(cross(N, up));
+  const F3 B = cross(N, T);
+  const float pi = 3.14159265358f;
+  const float dv = (2.0f * pi) / (float)segments;
+  float ang = 0.0f;
+  for (int s = 0; s < segments; ++s) {
+    const float a1 = ang + dv;
+    const float c0 = (float)std::cos((double)ang), s0 = (float)std::sin((double)ang);
+    const float c1 = (float)std::cos((double)a1), s1 = (float)std::sin((double)a1);
+    const F3 q0 = add(P, add(scl(R * c0, B), scl(R * s0, T)));
+    const F3 q1 = add(P, add(scl(R * c1, B), scl(R * s1, T)));
+    for (F3 q : {P, q0, q1}) {
+      o.verts.insert(o.verts.end(), {q.x, q.y, q.z});
+      o.normals.insert(o.normals.end(), {N.x, N.y, N.z});
+    }
+    ang = ang + dv;
+  }
+  o.n_verts = (uint32_t)(o.verts.size() / 3);
+  for (uint32_t i = 0; i < o.n_verts; ++i) o.idxp.push_back(i);
+  o.shaders = {shader};
+  return o;
+}
+
+MeshOut quad_light_mesh(F3 P, F3 U, F3 V, uint32_t shader) {  // quad.go:41-66, 174-207
+  MeshOut o;
+  const F3 c[4] = {P, add(P, U), add(add(P, U), V), add(P, V)};
+  const F3 N = nrm(cross(U, V));
+  for (const F3& q : c) {
+    o.verts.insert(o.verts.end(), {q.x, q.y, q.z});
+    o.normals.insert(o.normals.end(), {N.x, N.y, N.z});
+  }
+  o.n_verts = 4;
+  o.idxp = {0, 1, 2, 0, 2, 3};  // PolyCount 4, FaceIdx 0 1 2 3 through init's fan
+  o.shaders = {shader};
+  return o;
+}
+
+// Camera.PreRender for one key (camera.go:80-98, 109-193).
+vmr_camera camera(const Node& n, const vmr_vnf_info& info, const std::string& file) {
+  auto where = [&](const std::string& m) { return file + ":" + std::to_string(n.line) + ": Camera: " + m; };
+  vmr_camera c{};
+  const float fov = n.has("Fov") ? (float)n.at("Fov").f : 90.0f;
+  const float focal = n.has("Focal") ? (float)n.at("Focal").f : 12.0f;
+  float aspect = n.has("Aspect") ? (float)n.at("Aspect").f : 0.0f;
+  if (aspect == 0.0f) aspect = (float)info.width / (float)info.height;  // core.FrameAspect
+  const float pi = 3.14159265358f;
+  const float half = fov / 2.0f;
+  c.tan_theta_focal = (float)std::tan((double)(half * pi / 180.0f)) * focal;
+  c.aspect = aspect;
+  c.focal = focal;
+  c.radius = n.has("Radius") ? (float)n.at("Radius").f : 0.0f;
+  const std::string& type = n.at("Type").s;
+  if (type == "LookAt") {
+    const Value& from = n.at("From");
+    const Value& to = n.at("To");
+    const Value& roll = n.at("Roll");
+    if (from.keys > 1 || to.keys > 1 || roll.keys > 1 || from.v.size() < 3 || to.v.size() < 3)
+      throw LoadError{VMR_ERR_UNSUPPORTED, where("one From/To key is supported (no camera motion)")};
+    const F3 P = f3(from.v), T = f3(to.v), Up = f3(n.at("Up").v);
+    const F3 W = nrm(sub(P, T));  // W points away from the target
+    const F3 u = nrm(cross(Up, W));
+    const F3 v = nrm(cross(u, W));
+    F3 U = u, Vv = v;
+    if (!roll.v.empty()) {
+      const float r = roll.v[0];
+      const float cr = (float)std::cos((double)r), sr = (float)std::sin((double)r);
+      U = add(scl(cr, u), scl(sr, v));
+      Vv = add(scl(-sr, u), scl(cr, v));
+    }
+    const float m[16] = {U.x, U.y, U.z, 0.f, Vv.x, Vv.y, Vv.z, 0.f, W.x, W.y, W.z, 0.f, P.x, P.y, P.z, 1.f};
+    std::memcpy(c.m, m, sizeof(m));
+  } else {
+    if (n.has("WorldToLocal"))
+      throw LoadError{VMR_ERR_UNSUPPORTED, where("WorldToLocal (a matrix inverse) is not supported; give LocalToWorld")};
+    if (!n.has("LocalToWorld")) throw LoadError{VMR_ERR_INVALID, where("a matrix camera needs LocalToWorld")};
+    const Value& M = n.at("LocalToWorld");
+    if (M.keys > 1) throw LoadError{VMR_ERR_UNSUPPORTED, where("one LocalToWorld key is supported")};
+    std::memcpy(c.m, M.v.data(), sizeof(c.m));
+  }
+  return c;
+}
+
+Scene build_scene(const std::vector<Node>& nodes, const std::string& file, int flags) {
+  Scene sc;
+  // core.Init's defaults; a Globals node starts from its own (256 x 256, MaxIter 0)
+  sc.info.width = 1024;
+  sc.info.height = 1024;
+  sc.info.max_iter = 16;
+  std::string cam_name = "camera";
+  for (const Node& n : nodes) {
+    if (n.type == "Globals") {
+      sc.info.width = n.has("XRes") ? (uint32_t)n.at("XRes").i : 256;
+      sc.info.height = n.has("YRes") ? (uint32_t)n.at("YRes").i : 256;
+      sc.info.max_iter = n.has("MaxIter") ? (int)n.at("MaxIter").i : 0;
+      cam_name = n.has("Camera") && !n.at("Camera").s.empty() ? n.at("Camera").s : "camera";
+    } else if (n.type == "ShaderStd") {
+      sc.shader_id[n.at("Name").s] = (uint32_t)sc.shaders.size();
+      sc.shaders.push_back(shader_std(n));
+    } else if (n.type == "OutputHDR") {
+      copy_name(sc.info.output_hdr, sizeof(sc.info.output_hdr), n.at("Filename").s);
+    } else if (n.type == "OutputFloat") {
+      copy_name(sc.info.output_float, sizeof(sc.info.output_float), n.at("Filename").s);
+    } else if (n.type == "GaussianFilter" || n.type == "AiryFilter") {
+      sc.has_filter = true;
+      sc.filter = vmr_pixel_filter{n.type == "GaussianFilter" ? VMR_FILTER_GAUSSIAN : VMR_FILTER_AIRY,
+                                   n.has("Res") ? (int)n.at("Res").i : 49,
+                                   n.has("Width") ? (float)n.at("Width").f : 6.0f,
+                                   n.has("Peak") ? (float)n.at("Peak").f : 4.0f};
+    }
+  }
+  if (sc.info.width == 0 || sc.info.height == 0 || sc.info.width > 4096 || sc.info.height > 4096)
+    throw LoadError{VMR_ERR_INVALID, file + ": Globals XRes/YRes must be in [1, 4096]"};
+  // geoms in file order (core.AddNode)
+  for (const Node& n : nodes) {
+    if (n.type == "PolyMesh") {
+      sc.geoms.push_back(poly_mesh(n, sc, file));
+    } else if (n.type == "Sphere") {
+      MeshOut o;
+      o.sphere = true;
+      for (int k = 0; k < 3; ++k) o.centre[k] = n.at("P").v[k];
+      o.radius = (float)n.at("Radius").f;
+      o.shaders = {shader_of(sc, n, n.at("Shader").s, file)};
+      sc.geoms.push_back(o);
+    }
+  }
+  // lights, each adding its geom in PreRender (core.PreRender's first pass)
+  for (const Node& n : nodes) {
+    if (n.type != "TriLight" && n.type != "DiskLight" && n.type != "SphereLight" && n.type != "QuadLight") continue;
+    const uint32_t sh = shader_of(sc, n, n.at("Shader").s, file);
+    const int samples = n.has("Samples") ? (int)n.at("Samples").i : 1;
+    const uint32_t geom = (uint32_t)sc.geoms.size();
+    if (n.type == "TriLight") {
+      const F3 p0 = f3(n.at("P0").v), p1 = f3(n.at("P1").v), p2 = f3(n.at("P2").v);
+      sc.geoms.push_back(tri_light_mesh(p0, p1, p2, sh));
+      vmr_tri_light l{};
+      std::memcpy(l.p0, &p0, 12);
+      std::memcpy(l.p1, &p1, 12);
+      std::memcpy(l.p2, &p2, 12);
+      l.samples = samples;
+      l.shader = sh;
+      l.geom = geom;
+      sc.tris.push_back(l);
+    } else if (n.type == "DiskLight") {
+      const F3 P = f3(n.at("P").v), up = f3(n.at("Up").v), at = f3(n.at("LookAt").v);
+      const float R = (float)n.at("Radius").f;
+      const int seg = n.has("Segments") ? (int)n.at("Segments").i : 20;
+      if (seg < 1 || seg > 65536) throw LoadError{VMR_ERR_INVALID, file + ": DiskLight Segments out of range"};
+      sc.geoms.push_back(disk_light_mesh(P, up, at, R, seg, sh));
+      vmr_disk_light l{};
+      std::memcpy(l.P, &P, 12);
+      std::memcpy(l.up, &up, 12);
+      std::memcpy(l.lookat, &at, 12);
+      l.radius = R;
+      l.samples = samples;
+      l.shader = sh;
+      l.geom = geom;
+      sc.disks.push_back(l);
+    } else if (n.type == "SphereLight") {
+      MeshOut o;
+      o.sphere = true;
+      for (int k = 0; k < 3; ++k) o.centre[k] = n.at("P").v[k];
+      o.radius = (float)n.at("Radius").f;
+      o.shaders = {sh};
+      sc.geoms.push_back(o);
+      vmr_sphere_light l{};
+      std::memcpy(l.P, o.centre, 12);
+      l.radius = o.radius;
+      l.samples = samples;
+      l.shader = sh;
+      l.geom = geom;
+      sc.spheres.push_back(l);
+    } else {
+      const F3 P = f3(n.at("P").v), U = f3(n.at("U").v), V = f3(n.at("V").v);
+      sc.geoms.push_back(quad_light_mesh(P, U, V, sh));
+      vmr_quad_light l{};
+      std::memcpy(l.p0, &P, 12);
+      std::memcpy(l.e1, &U, 12);
+      std::memcpy(l.e2, &V, 12);
+      l.shader = sh;
+      l.geom = geom;
+      sc.quads.push_back(l);
+    }
+  }
+  // the render's camera (core/render.go:147-162)
+  const Node* cam = nullptr;
+  for (const Node& n : nodes)
+    if (n.type == "Camera" && n.at("Name").s == cam_name) cam = &n;
+  if (!cam) throw LoadError{VMR_ERR_INVALID, file + ": no camera named " + cam_name};
+  sc.cam = camera(*cam, sc.info, file);
+  copy_name(sc.info.camera, sizeof(sc.info.camera), cam_name);
+  (void)flags;
+  return sc;
+}
+
+int fail(vmr_ctx* ctx, int code, const std::string& m) {
+  ctx->err = m;
+  return code;
+}
+
+}  // namespace
+
+extern "C" int vmr_get_camera(vmr_ctx* ctx, vmr_camera* camera) {
+  if (!ctx || !camera) return VMR_ERR_INVALID;
+  if (!ctx->render.has_camera) return fail(ctx, VMR_ERR_INVALID, "no camera set");
+  *camera = ctx->render.camera;
+  return VMR_OK;
+}
+
+extern "C" int vmr_load_vnf(vmr_ctx* ctx, const char* path, int flags, vmr_vnf_info* info) {
+  if (!ctx || !path) return VMR_ERR_INVALID;
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return fail(ctx, VMR_ERR_INVALID, std::string("cannot open ") + path);
+  std::stringstream ss;
+  ss << in.rdbuf();
+  Scene sc;
+  try {
+    Parser p(ss.str(), path);
+    const std::vector<Node> nodes = p.parse();
+    sc = build_scene(nodes, path, flags);
+  } catch (const LoadError& e) {
+    return fail(ctx, e.code, e.msg);
+  } catch (const std::exception& e) {
+    return fail(ctx, VMR_ERR_INVALID, std::string(path) + ": " + e.what());
+  }
+  // upload through the C ABI, as a host binding would
+  const int mode = (flags & VMR_VNF_MOTION_FIXED) ? VMR_MOTION_FIXED : VMR_MOTION_FAITHFUL;
+  std::vector<uint32_t> ids;
+  for (const MeshOut& g : sc.geoms) {
+    uint32_t id = 0;
+    int rc;
+    if (g.sphere) {
+      rc = vmr_sphere_add(ctx, g.centre, g.radius, &id);
+    } else {
+      vmr_mesh_input mi{};
+      mi.verts = g.verts.data();
+      mi.n_verts = g.n_verts;
+      mi.motion_keys = g.keys;
+      mi.idxp = g.idxp.data();
+      mi.n_tris = (uint32_t)(g.idxp.size() / 3);
+      mi.ray_bias = g.ray_bias;
+      mi.motion_mode = mode;
+      mi.shader_idx = g.sidx.empty() ? nullptr : g.sidx.data();
+      rc = vmr_mesh_build(ctx, &mi, &id);
+    }
+    if (rc != VMR_OK) return rc;
+    ids.push_back(id);
+  }
+  int rc = vmr_scene_build(ctx, ids.data(), (uint32_t)ids.size());
+  if (rc == VMR_OK) rc = vmr_set_shaders(ctx, sc.shaders.data(), (uint32_t)sc.shaders.size());
+  for (size_t g = 0; g < sc.geoms.size() && rc == VMR_OK; ++g)
+    rc = vmr_mesh_set_shading(ctx, ids[g], sc.geoms[g].shaders.data(), (uint32_t)sc.geoms[g].shaders.size(),
+                              sc.geoms[g].normals.empty() ? nullptr : sc.geoms[g].normals.data());
+  auto remap = [&](uint32_t g) { return ids[g]; };
+  for (auto& l : sc.tris) l.geom = remap(l.geom);
+  for (auto& l : sc.disks) l.geom = remap(l.geom);
+  for (auto& l : sc.spheres) l.geom = remap(l.geom);
+  for (auto& l : sc.quads) l.geom = remap(l.geom);
+  if (rc == VMR_OK) rc = vmr_set_lights(ctx, sc.tris.data(), (uint32_t)sc.tris.size());
+  if (rc == VMR_OK) rc = vmr_set_disk_lights(ctx, sc.disks.data(), (uint32_t)sc.disks.size());
+  if (rc == VMR_OK) rc = vmr_set_sphere_lights(ctx, sc.spheres.data(), (uint32_t)sc.spheres.size());
+  if (rc == VMR_OK) rc = vmr_set_quad_lights(ctx, sc.quads.data(), (uint32_t)sc.quads.size());
+  const float black[3] = {0.f, 0.f, 0.f};
+  if (rc == VMR_OK) rc = vmr_set_env_light(ctx, black);
+  if (rc == VMR_OK) rc = vmr_set_camera(ctx, &sc.cam);
+  if (rc == VMR_OK) {
+    vmr_pixel_filter none{VMR_FILTER_BOX, 0, 0.f, 0.f};
+    rc = vmr_set_pixel_filter(ctx, sc.has_filter ? &sc.filter : &none);
+  }
+  if (rc != VMR_OK) return rc;
+  sc.info.n_geoms = (uint32_t)ids.size();
+  sc.info.n_shaders = (uint32_t)sc.shaders.size();
+  sc.info.n_lights = (uint32_t)(sc.tris.size() + sc.disks.size() + sc.spheres.size() + sc.quads.size());
+  if (info) *info = sc.info;
+  return VMR_OK;
+}

@@ -103,6 +103,26 @@ def motion_soup(n_tris: int, seed: int, velocity=0.05, edge=0.005):
 
 
 # ---------------------------------------------------------------- renders ---
+def _cross32(a, b):
+    """a x b in float32 scalar operations (the order libvmr's scene loader
+    uses, so a scene written to .vnf and loaded back gets the same bits)."""
+    f = np.float32
+    a, b = np.asarray(a, f), np.asarray(b, f)
+    return np.array([f(a[1] * b[2]) - f(a[2] * b[1]), f(a[2] * b[0]) - f(a[0] * b[2]),
+                     f(a[0] * b[1]) - f(a[1] * b[0])], f)
+
+
+def _norm32(a):
+    """a * (1 / sqrt((x*x + y*y) + z*z)) in float32 (Vec3Normalize with an
+    exact reciprocal square root)."""
+    f = np.float32
+    a = np.asarray(a, f)
+    s = f(f(a[0] * a[0]) + f(a[1] * a[1]))
+    s = f(s + f(a[2] * a[2]))
+    r = f(f(1.0) / np.sqrt(s))
+    return (a * r).astype(f)
+
+
 def lookat_camera(eye, target, up, fov_deg: float, aspect: float, focal: float = 12.0) -> dict:
     """Camera node of type LookAt with one key (builtin/camera/camera.go:
     80-98, 109-193): W = normalize(From - To), u = normalize(Up x W),
@@ -111,27 +131,23 @@ def lookat_camera(eye, target, up, fov_deg: float, aspect: float, focal: float =
     f32 = np.float32
     eye, target, up = (np.asarray(a, f32) for a in (eye, target, up))
 
-    def norm(a):
-        a = a.astype(f32)
-        return (a * (f32(1.0) / np.sqrt(np.dot(a, a), dtype=f32))).astype(f32)
-
-    W = norm(eye - target)
-    u = norm(np.cross(up, W).astype(f32))
-    v = norm(np.cross(u, W).astype(f32))
+    W = _norm32(eye - target)
+    u = _norm32(_cross32(up, W))
+    v = _norm32(_cross32(u, W))
     m = np.zeros(16, f32)
     m[0:3], m[4:7], m[8:11], m[12:15], m[15] = u, v, W, eye, 1.0
     pi = f32(3.14159265358)
     half = f32(fov_deg) / f32(2)
     tan = f32(np.tan(np.float64(half * pi / f32(180.0))))
-    return dict(m=m, tan_theta_focal=f32(tan * f32(focal)), aspect=f32(aspect), focal=f32(focal), radius=f32(0))
+    return dict(m=m, tan_theta_focal=f32(tan * f32(focal)), aspect=f32(aspect), focal=f32(focal), radius=f32(0),
+                fov=f32(fov_deg))
 
 
 def _tri_light_mesh(p0, p1, p2):
     """The emissive mesh a TriLight adds (builtin/light/triangle.go:537-565):
     three vertices with the face normal at each."""
     p = np.asarray([p0, p1, p2], np.float32)
-    n = np.cross(p[1] - p[0], p[2] - p[0]).astype(np.float32)
-    n = n / np.sqrt(np.dot(n, n), dtype=np.float32)
+    n = _norm32(_cross32(p[1] - p[0], p[2] - p[0]))
     return p, np.arange(3, dtype=np.uint32), np.tile(n, (3, 1)).astype(np.float32)
 
 
@@ -418,15 +434,10 @@ def disk_light_mesh(P, up, lookat, radius: float, segments: int = 20):
     the angle advanced in float32, every vertex normal N; N, T, B from
     Disk.PreRender (disk.go:88-90) in float32."""
     f = np.float32
-
-    def norm(a):
-        a = np.asarray(a, f)
-        return (a * (f(1.0) / np.sqrt(np.dot(a, a), dtype=f))).astype(f)
-
     P, up, lookat = (np.asarray(a, f) for a in (P, up, lookat))
-    N = norm(lookat - P)
-    T = norm(np.cross(N, up).astype(f))
-    B = np.cross(N, T).astype(f)
+    N = _norm32(lookat - P)
+    T = _norm32(_cross32(N, up))
+    B = _cross32(N, T)
     R = f(radius)
     pi = f(3.14159265358)
     dv = f(f(2) * pi) / f(segments)
@@ -516,3 +527,127 @@ def small_room_motion(n_tris: int = 4096, seed: int = 1, motion_mode: int = 0, v
     soup["keys"] = 2
     soup["motion_mode"] = motion_mode
     return sc
+
+
+# ------------------------------------------------------------ .vnf files ---
+def _vnf_num(x) -> str:
+    """A float32 value as the decimal of its exact double (read back through
+    float64, as the reference's lexer does, it gives the same float32)."""
+    return repr(float(np.float32(x)))
+
+
+def _light_mesh_ids(scene: dict) -> set:
+    ids = set()
+    for k in ("lights", "disk_lights", "sphere_lights", "quad_lights"):
+        ids |= {int(l["mesh"]) for l in scene.get(k, [])}
+    return ids
+
+
+def to_vnf(scene: dict, width: int, height: int, max_iter: int = 16) -> str:
+    """The scene as a .vnf file the reference's parser (nodes/parser.go) and
+    vmr_load_vnf read: ShaderStd nodes "sh<i>", a PolyMesh or Sphere node per
+    geom that is not a light's own mesh, the lights (which create their
+    meshes when loaded), a matrix Camera "camera" with the scene camera's
+    LocalToWorld, Fov and Focal, Globals, and the pixel filter if any.  The
+    environment light has no node in the reference and is not written."""
+    out = []
+    for i, d in enumerate(scene["shaders"]):
+        out.append(f'ShaderStd {{\n  Name "sh{i}"')
+        names = {"emission_colour": "EmissionColour", "emission_strength": "EmissionStrength",
+                 "diffuse_colour": "DiffuseColour", "diffuse_strength": "DiffuseStrength",
+                 "diffuse_roughness": "DiffuseRoughness", "spec1_colour": "Spec1Colour",
+                 "spec1_strength": "Spec1Strength", "spec1_roughness": "Spec1Roughness",
+                 "spec1_fresnel_refl": "Spec1FresnelRefl", "spec1_fresnel_edge": "Spec1FresnelEdge", "ior": "IOR"}
+        for k, node in names.items():
+            if k in d:
+                v = d[k]
+                if np.ndim(v) == 0:
+                    out.append(f"  {node} float {_vnf_num(v)}")
+                else:
+                    out.append(f"  {node} rgb " + " ".join(_vnf_num(x) for x in v))
+        if "spec1_fresnel" in d:
+            out.append(f'  Spec1FresnelModel "{d["spec1_fresnel"]}"')
+        out.append("}")
+    lights = _light_mesh_ids(scene)
+    for gi, m in enumerate(scene["meshes"]):
+        if gi in lights:
+            continue
+        if "sphere" in m:
+            c = m["sphere"]
+            out.append(f'Sphere {{\n  Name "geom{gi}"\n  P {_vnf_num(c[0])} {_vnf_num(c[1])} {_vnf_num(c[2])}\n'
+                       f'  Radius {_vnf_num(c[3])}\n  Shader "sh{m["shaders"][0]}"\n}}')
+            continue
+        keys = int(m.get("keys", 1))
+        v = np.asarray(m["verts"], np.float32).reshape(-1, 3)
+        per = v.shape[0] // keys
+        idx = np.asarray(m["idxp"], np.uint32)
+        lines = [f'PolyMesh {{\n  Name "geom{gi}"',
+                 f"  Verts {keys} {per} point " + " ".join(_vnf_num(x) for x in v.ravel()),
+                 f"  FaceIdx {idx.size} int " + " ".join(str(int(x)) for x in idx),
+                 f"  Shader {len(m['shaders'])} string " + " ".join(f'"sh{s}"' for s in m["shaders"])]
+        if m.get("face_shader") is not None:
+            fs = np.asarray(m["face_shader"], np.uint8)
+            lines.append(f"  ShaderIdx {fs.size} int " + " ".join(str(int(x)) for x in fs))
+        if m.get("normals") is not None:
+            nr = np.asarray(m["normals"], np.float32).reshape(-1, 3)
+            lines.append(f"  Normals 1 {nr.shape[0]} vec3 " + " ".join(_vnf_num(x) for x in nr.ravel()))
+        out.append("\n".join(lines) + "\n}")
+    vec = lambda a: " ".join(_vnf_num(x) for x in a)  # noqa: E731
+    for i, l in enumerate(scene.get("lights", [])):
+        out.append(f'TriLight {{\n  Name "tri{i}"\n  P0 {vec(l["p0"])}\n  P1 {vec(l["p1"])}\n  P2 {vec(l["p2"])}\n'
+                   f'  Shader "sh{l["shader"]}"\n  Samples {int(l.get("samples", 1))}\n}}')
+    for i, l in enumerate(scene.get("disk_lights", [])):
+        out.append(f'DiskLight {{\n  Name "disk{i}"\n  P {vec(l["P"])}\n  Up {vec(l["up"])}\n'
+                   f'  LookAt {vec(l["lookat"])}\n  Radius {_vnf_num(l["radius"])}\n  Shader "sh{l["shader"]}"\n'
+                   f'  Samples {int(l.get("samples", 1))}\n}}')
+    for i, l in enumerate(scene.get("sphere_lights", [])):
+        out.append(f'SphereLight {{\n  Name "sphere{i}"\n  P {vec(l["P"])}\n  Radius {_vnf_num(l["radius"])}\n'
+                   f'  Shader "sh{l["shader"]}"\n  Samples {int(l.get("samples", 1))}\n}}')
+    for i, l in enumerate(scene.get("quad_lights", [])):
+        out.append(f'QuadLight {{\n  Name "quad{i}"\n  P {vec(l["p0"])}\n  U {vec(l["e1"])}\n  V {vec(l["e2"])}\n'
+                   f'  Shader "sh{l["shader"]}"\n}}')
+    c = scene["camera"]
+    m44 = np.asarray(c["m"], np.float32).reshape(4, 4).T  # written row by row; the reader transposes
+    out.append('Camera {\n  Name "camera"\n  Type "matrix"\n  From 1 1 point 0 0 0\n  To 1 1 point 0 0 -1\n'
+               '  Roll 1 1 float 0\n  Up 0 1 0\n'
+               f'  Fov {_vnf_num(c.get("fov", 90.0))}\n  Focal {_vnf_num(c["focal"])}\n'
+               f'  Aspect {_vnf_num(c["aspect"])}\n  Radius {_vnf_num(c["radius"])}\n'
+               f"  LocalToWorld 1 matrix {vec(m44.ravel())}\n}}")
+    out.append(f"Globals {{\n  XRes {int(width)}\n  YRes {int(height)}\n  MaxIter {int(max_iter)}\n}}")
+    pf = scene.get("pixel_filter")
+    if pf:
+        if int(pf["kind"]) == 1:
+            out.append(f'GaussianFilter {{\n  Name "filter"\n  Width {_vnf_num(pf.get("width", 2.0))}\n'
+                       f'  Res {int(pf.get("res", 17))}\n}}')
+        else:
+            out.append(f'AiryFilter {{\n  Name "filter"\n  Width {_vnf_num(pf.get("width", 6.0))}\n'
+                       f'  Res {int(pf.get("res", 49))}\n  Peak {_vnf_num(pf.get("peak", 4.0))}\n}}')
+    return "# written by vermeer_gb300.scenes.to_vnf\n" + "\n".join(out) + "\n"
+
+
+def vnf_order(scene: dict) -> dict:
+    """The scene as vmr_load_vnf builds it from to_vnf's file: the geoms that
+    are not lights' meshes in their order, then the lights' meshes in the
+    order TriLights, DiskLights, SphereLights, QuadLights (each quad as the
+    reference's 4-vertex polygon with its normal, quad.go:174-207), the
+    light tables pointing at the new positions, and no environment."""
+    lights = _light_mesh_ids(scene)
+    order = [g for g in range(len(scene["meshes"])) if g not in lights]
+    meshes = [scene["meshes"][g] for g in order]
+    out = dict(scene, env=(0.0, 0.0, 0.0))
+    for key in ("lights", "disk_lights", "sphere_lights", "quad_lights"):
+        new = []
+        for l in scene.get(key, []):
+            m = scene["meshes"][int(l["mesh"])]
+            if key == "quad_lights":
+                f = np.float32
+                P, U, V = (np.asarray(l[k], f) for k in ("p0", "e1", "e2"))
+                c = np.stack([P, (P + U).astype(f), ((P + U).astype(f) + V).astype(f), (P + V).astype(f)]).astype(f)
+                N = _norm32(_cross32(U, V))
+                m = dict(verts=c, idxp=np.array([0, 1, 2, 0, 2, 3], np.uint32), shaders=[int(l["shader"])],
+                         normals=np.tile(N, (4, 1)).astype(f))
+            new.append(dict(l, mesh=len(meshes)))
+            meshes.append(m)
+        out[key] = new
+    out["meshes"] = meshes
+    return out
