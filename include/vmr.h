@@ -68,14 +68,17 @@ typedef struct {
                             permutation class and origin cell before a mesh
                             trace of >= 65536 rays; bit 4: the top 16
                             entries of the traversal stack in shared memory
-                            (while-while).  Default 13. */
+                            (while-while); bit 5: warp-cooperative leaf
+                            scan (while-while, static meshes: the warp's
+                            leaves tested as one list, one triangle per
+                            lane).  Default 45. */
     int block;           /* threads per block, multiple of 32, <= 256 (128) */
     int blocks_per_sm;   /* resident blocks per SM (occupancy maximum) */
     int refill_min;      /* step-scheduled: idle lanes that trigger a warp
                             refill, 1..32 (4) */
     int walk_tail;       /* while-while: end a node walk early once at most
                             this many lanes still walk and a lane holds a
-                            leaf, 0..31 (default 4; 0 = wait for every lane) */
+                            leaf, 0..31 (default 8; 0 = wait for every lane) */
     int sort_bits;       /* sort-key width: the ray reordering groups origins
                             in (2^b)^3 cells, b = 3, 4 or 5 (0: 4) */
 } vmr_tuning;

@@ -69,7 +69,7 @@ def test_autotune_picks_a_config_and_stays_exact(ctx, orc):
     g = ctx.mesh_build(v, ip)
     best, ms, tried = ctx.autotune(g, rays)
     assert tried >= 20 and ms > 0
-    assert best["kernel"] in (0, 1, 5, 8, 9, 13) and best["sort_bits"] in (0, 3, 4, 5)
+    assert best["kernel"] in (0, 1, 5, 8, 9, 13, 29, 41, 45) and best["sort_bits"] in (0, 3, 4, 5)
     try:
         assert_hits_equal(ctx.trace_mesh(g, rays), orc.Mesh(v, ip).trace(rays), what="after autotune")
     finally:

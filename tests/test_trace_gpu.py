@@ -142,7 +142,8 @@ def test_full_size_soup_parity(ctx, orc):
                                     (9, 0, 0, 0), (13, 0, 0, 0), (9, 64, 0, 0), (9, 256, 2, 0), (13, 0, 0, 0, 4), (9, 0, 0, 0, 12),
                                     (13, 0, 0, 0, 4, 3), (13, 0, 0, 0, 4, 5), (8, 256, 0, 4, 4, 5),
                                     (29, 0, 0, 0, 4), (17, 0, 0, 0, 0), (25, 256, 0, 0, 8, 3), (21, 64, 0, 0, 2),
-                                    (16, 0, 0, 0)])
+                                    (16, 0, 0, 0), (45, 0, 0, 0, 4), (45, 0, 0, 0, 0), (33, 0, 0, 0, 8),
+                                    (41, 256, 0, 0, 4, 3), (37, 0, 0, 0, 2)])
 def test_every_tuning_is_bit_exact(ctx, orc, tuning):
     """Launch parameters (kernel variant, ray reordering and its key width,
     block size, resident blocks) only change scheduling: hits stay
@@ -163,10 +164,11 @@ def test_every_tuning_is_bit_exact(ctx, orc, tuning):
         assert_hits_equal(ctx.trace_mesh(mg, mrays), orc.Mesh(mv, mip, keys=2, motion_fixed=True).trace(mrays),
                           what=f"motion tuning={tuning}")
     finally:
-        ctx.set_tuning(13, 0, 0, 0, 4)
+        ctx.set_tuning(45, 0, 0, 0, 8)
 
 
-@pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (1, 0, 0, 0, 0), (5, 0, 0, 0, 8), (0, 0, 0, 4, 4),
+@pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (45, 0, 0, 0, 8), (45, 0, 0, 0, 0), (1, 0, 0, 0, 0),
+                                    (5, 0, 0, 0, 8), (0, 0, 0, 4, 4),
                                     (13, 0, 0, 0, 2, 5)])
 def test_two_level_scene_every_tuning(ctx, orc, tuning):
     """The static two-level scene traced by the while-while scene kernel (with
@@ -194,11 +196,11 @@ def test_two_level_scene_every_tuning(ctx, orc, tuning):
             assert_hits_equal(got, ref, keys=("prim", "geom", "t", "u", "v", "w"),
                               what=f"scene tuning={tuning} shadow={shadow}")
     finally:
-        ctx.set_tuning(13, 0, 0, 0, 4)
+        ctx.set_tuning(45, 0, 0, 0, 8)
 
 
 
-@pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (0, 0, 0, 4, 4)])
+@pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (45, 0, 0, 0, 8), (0, 0, 0, 4, 4)])
 def test_scene_with_sphere_geoms(ctx, orc, tuning):
     """Analytic sphere geoms among triangle meshes (Sphere.Trace: the nearer
     non-negative root below Tclosest), in both scene kernels."""
@@ -228,4 +230,4 @@ def test_scene_with_sphere_geoms(ctx, orc, tuning):
             assert_hits_equal(got, ref, keys=("prim", "geom", "t", "u", "v", "w"), what=f"spheres shadow={shadow}")
         assert (got["geom"] >= ids[12]).any()  # some rays end on spheres
     finally:
-        ctx.set_tuning(13, 0, 0, 0, 4)
+        ctx.set_tuning(45, 0, 0, 0, 8)

@@ -99,8 +99,8 @@ class Context:
     def sync(self):
         self._check(self.L.vmr_sync(self.h))
 
-    def set_tuning(self, kernel: int = 13, block: int = 0, blocks_per_sm: int = 0, refill_min: int = 0,
-                   walk_tail: int = 4, sort_bits: int = 0):
+    def set_tuning(self, kernel: int = 45, block: int = 0, blocks_per_sm: int = 0, refill_min: int = 0,
+                   walk_tail: int = 8, sort_bits: int = 0):
         """Launch parameters of the traversal kernels (vmr_set_tuning)."""
         t = _lib.Tuning(kernel, block, blocks_per_sm, refill_min, walk_tail, sort_bits)
         self._check(self.L.vmr_set_tuning(self.h, ctypes.byref(t)))

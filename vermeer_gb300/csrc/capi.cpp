@@ -403,7 +403,7 @@ const char* vmr_last_error(const vmr_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 int vmr_set_tuning(vmr_ctx* ctx, const vmr_tuning* t) {
   if (!ctx || !t) return VMR_ERR_INVALID;
-  if (t->kernel < 0 || t->kernel > 31) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 31]");
+  if (t->kernel < 0 || t->kernel > 63) return fail(ctx, VMR_ERR_INVALID, "tuning.kernel must be in [0, 63]");
   if (t->walk_tail < 0 || t->walk_tail > 31) return fail(ctx, VMR_ERR_INVALID, "tuning.walk_tail must be in [0, 31]");
   if (t->block != 0 && (t->block < 32 || t->block > 256 || t->block % 32 != 0))
     return fail(ctx, VMR_ERR_INVALID, "tuning.block must be a multiple of 32 in [32, 256]");
@@ -704,7 +704,7 @@ int vmr_autotune(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, in
   // shared-memory stack top, tail cutoff, key width) and the step-scheduled
   // kernel
   std::vector<vmr_tuning> cands;
-  for (int k : {13, 9, 29})
+  for (int k : {13, 9, 29, 45, 41})
     for (int tail : {0, 2, 4, 8})
       for (int bits : {3, 4, 5}) cands.push_back(vmr_tuning{k, 0, 0, 0, tail, bits});
   for (int k : {5, 1})

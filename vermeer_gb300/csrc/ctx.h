@@ -123,7 +123,7 @@ struct vmr_ctx {
   TopRec top;
   vmr::RenderState render;
   vmr::GuideState guide;
-  vmr_tuning tuning{13, 0, 0, 0, 4, 0};
+  vmr_tuning tuning{45, 0, 0, 0, 8, 0};
   int builder = VMR_BUILD_AUTO;   // vmr_set_builder
   DevBuf jobs;                    // vmr_trace_jobs tables
   // Bounds (min xyz, max xyz) of the mesh a DMesh belongs to.

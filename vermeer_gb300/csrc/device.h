@@ -119,6 +119,7 @@ enum TraceKernel : int {
   kKernelRegCap = 4,
   kKernelSort = 8,
   kKernelSharedStack = 16,  // while-while: the top of the stack in shared memory
+  kKernelCoopLeaf = 32,     // while-while, static meshes: warp-cooperative leaf scan
 };
 constexpr int kSharedStackEntries = 16;
 

@@ -167,11 +167,14 @@ __device__ __forceinline__ float kcomp(const TRay& r, const float4& v) {
   }
 }
 
-// The watertight test (trace.go:123-193).  STRICT: static idxp path
+// The watertight test (trace.go:123-193), in two parts.  tri_prepare: the
+// part that does not depend on Tclosest (edge functions with the FP64
+// fallback, the sign test, det, T and the lower bound); false when the
+// triangle cannot be hit at any Tclosest.  STRICT: static idxp path
 // (xT < lower*xdet); otherwise the motion path (xT <= lower*xdet).
 template <bool STRICT, int C = -1>
-__device__ __forceinline__ bool tri_test(TRay& r, float4 v0, float4 v1, float4 v2, float lower, float& U,
-                                         float& V, float& W) {
+__device__ __forceinline__ bool tri_prepare(const TRay& r, float4 v0, float4 v1, float4 v2, float lower, float& fU,
+                                            float& fV, float& fW, float& det, float& T) {
   const float AKz = __fsub_rn(kcomp<C, 2>(r, v0), r.pkz);
   const float BKz = __fsub_rn(kcomp<C, 2>(r, v1), r.pkz);
   const float CKz = __fsub_rn(kcomp<C, 2>(r, v2), r.pkz);
@@ -181,9 +184,9 @@ __device__ __forceinline__ bool tri_test(TRay& r, float4 v0, float4 v1, float4 v
   const float Bx = __fsub_rn(__fsub_rn(kcomp<C, 0>(r, v1), r.pkx), __fmul_rn(r.s0, BKz));
   const float Ax = __fsub_rn(__fsub_rn(kcomp<C, 0>(r, v0), r.pkx), __fmul_rn(r.s0, AKz));
   const float Ay = __fsub_rn(__fsub_rn(kcomp<C, 1>(r, v0), r.pky), __fmul_rn(r.s1, AKz));
-  float fU = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-  float fV = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-  float fW = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+  fU = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+  fV = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+  fW = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
   if (fU == 0.0f || fV == 0.0f || fW == 0.0f) {
     // FP64 fallback (trace.go:142-155): exact products, one rounding in the
     // double subtraction, one in the conversion.
@@ -192,21 +195,37 @@ __device__ __forceinline__ bool tri_test(TRay& r, float4 v0, float4 v1, float4 v
     fW = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
   }
   if ((fU < 0.0f || fV < 0.0f || fW < 0.0f) && (fU > 0.0f || fV > 0.0f || fW > 0.0f)) return false;
-  const float det = __fadd_rn(__fadd_rn(fU, fV), fW);
+  det = __fadd_rn(__fadd_rn(fU, fV), fW);
   if (det == 0.0f) return false;
-  const float T = __fmul_rn(r.s2, __fadd_rn(__fadd_rn(__fmul_rn(fU, AKz), __fmul_rn(fV, BKz)), __fmul_rn(fW, CKz)));
+  T = __fmul_rn(r.s2, __fadd_rn(__fadd_rn(__fmul_rn(fU, AKz), __fmul_rn(fV, BKz)), __fmul_rn(fW, CKz)));
   const unsigned sgn = __float_as_uint(det) & 0x80000000u;
   const float xT = __uint_as_float(__float_as_uint(T) ^ sgn);
   const float xdet = __uint_as_float(__float_as_uint(det) ^ sgn);
   const float lo = __fmul_rn(lower, xdet);
-  const bool below = STRICT ? (xT < lo) : (xT <= lo);
-  if (below || xT > __fmul_rn(r.tclosest, xdet)) return false;
+  return !(STRICT ? (xT < lo) : (xT <= lo));
+}
+
+// The Tclosest test and the hit update of a prepared triangle.
+__device__ __forceinline__ bool tri_accept(TRay& r, float fU, float fV, float fW, float det, float T, float& U,
+                                           float& V, float& W) {
+  const unsigned sgn = __float_as_uint(det) & 0x80000000u;
+  const float xT = __uint_as_float(__float_as_uint(T) ^ sgn);
+  const float xdet = __uint_as_float(__float_as_uint(det) ^ sgn);
+  if (xT > __fmul_rn(r.tclosest, xdet)) return false;
   const float rcp = __frcp_rn(det);
   U = __fmul_rn(fU, rcp);
   V = __fmul_rn(fV, rcp);
   W = __fmul_rn(fW, rcp);
   r.tclosest = __fmul_rn(T, rcp);
   return true;
+}
+
+template <bool STRICT, int C = -1>
+__device__ __forceinline__ bool tri_test(TRay& r, float4 v0, float4 v1, float4 v2, float lower, float& U,
+                                         float& V, float& W) {
+  float fU, fV, fW, det, T;
+  if (!tri_prepare<STRICT, C>(r, v0, v1, v2, lower, fU, fV, fW, det, T)) return false;
+  return tri_accept(r, fU, fV, fW, det, T, U, V, W);
 }
 
 struct Counters {
@@ -861,7 +880,102 @@ __device__ __forceinline__ int32_t leaf_scan_dispatch(const DMesh& m, TRay& r, u
   return leaf_scan<MOTION, -1>(m, r, first, count, tr0, tr1, tm, omt, U, V, W);
 }
 
-template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB, int SS>
+// Warp-cooperative leaf scan of a static mesh.  The leaves the lanes hold
+// are laid end to end as one list of (ray, triangle) pairs and tested 32 per
+// round, one pair per lane: consecutive lanes read consecutive triangles of
+// a leaf (a leaf is one contiguous run) and no lane idles while another
+// still has triangles.  tri_prepare does not depend on Tclosest, so it can
+// run in any order; the Tclosest-dependent acceptance then runs on the
+// owning lane, over its candidates in the reference's triangle order (a
+// round's candidates in lane order, rounds in order), exactly as the
+// sequential scan.  Called by all 32 lanes; has: the lane holds a leaf.
+// tris, lower: the lane's mesh (its triangles and lower bound); the tester
+// uses its owner's (one mesh per launch in the mesh kernel, one per lane in
+// the scene kernel).
+template <int C>
+__device__ __forceinline__ int32_t coop_leaf(const float4* tris, float lower, TRay& r, bool has, uint32_t first,
+                                             uint32_t count, float& U, float& V, float& W) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t cnt = has ? count : 0u;
+  uint32_t incl = cnt;  // inclusive prefix of the leaf sizes
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= (unsigned)o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  const uint32_t excl = incl - cnt;
+  int32_t idx = -1;
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t g = base + lane;
+    // owner: the lowest lane whose inclusive prefix exceeds g
+    int lo = 0, hi = 31;
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {
+      const int mid = (lo + hi) >> 1;
+      if (__shfl_sync(kFull, incl, mid) > g) hi = mid;
+      else lo = mid + 1;
+    }
+    const int o = lo;
+    const uint32_t i = __shfl_sync(kFull, first, o) + (g - __shfl_sync(kFull, excl, o));
+    TRay q;  // the owner's ray: the fields tri_prepare reads
+    q.pkx = __shfl_sync(kFull, r.pkx, o);
+    q.pky = __shfl_sync(kFull, r.pky, o);
+    q.pkz = __shfl_sync(kFull, r.pkz, o);
+    q.s0 = __shfl_sync(kFull, r.s0, o);
+    q.s1 = __shfl_sync(kFull, r.s1, o);
+    q.s2 = __shfl_sync(kFull, r.s2, o);
+    if (C < 0) {
+      q.kx = __shfl_sync(kFull, r.kx, o);
+      q.ky = __shfl_sync(kFull, r.ky, o);
+      q.kz = __shfl_sync(kFull, r.kz, o);
+    }
+    const float4* ot = reinterpret_cast<const float4*>(
+        __shfl_sync(kFull, (unsigned long long)reinterpret_cast<uintptr_t>(tris), o));
+    const float olower = __shfl_sync(kFull, lower, o);
+    float fU = 0.f, fV = 0.f, fW = 0.f, det = 0.f, T = 0.f;
+    bool cand = false;
+    if (g < total) {
+      const float4 v0 = __ldg(ot + 3 * (size_t)i);
+      const float4 v1 = __ldg(ot + 3 * (size_t)i + 1);
+      const float4 v2 = __ldg(ot + 3 * (size_t)i + 2);
+      cand = tri_prepare<true, C>(q, v0, v1, v2, olower, fU, fV, fW, det, T);
+    }
+    unsigned cm = __ballot_sync(kFull, cand);
+    while (cm != 0u) {  // candidates in lane order, i.e. in each owner's triangle order
+      const int c = __ffs(cm) - 1;
+      cm &= cm - 1u;
+      const int oc = __shfl_sync(kFull, o, c);
+      const float cU = __shfl_sync(kFull, fU, c), cV = __shfl_sync(kFull, fV, c), cW = __shfl_sync(kFull, fW, c);
+      const float cdet = __shfl_sync(kFull, det, c), cT = __shfl_sync(kFull, T, c);
+      const uint32_t ci = __shfl_sync(kFull, i, c);
+      if ((int)lane == oc && tri_accept(r, cU, cV, cW, cdet, cT, U, V, W)) idx = (int32_t)ci;
+    }
+  }
+  return idx;
+}
+
+// The class the lanes holding a leaf share picks the compile-time instance;
+// mixed classes take the run-time-select one.  All 32 lanes call this.
+__device__ __forceinline__ int32_t coop_leaf_dispatch(const float4* tris, float lower, TRay& r, bool has,
+                                                      uint32_t first, uint32_t count, float& U, float& V, float& W) {
+  const unsigned hm = __ballot_sync(kFull, has);
+  if (hm == 0u) return -1;
+  const int c0 = __shfl_sync(kFull, r.cls, __ffs(hm) - 1);
+  if (__all_sync(kFull, !has || r.cls == c0)) {
+    switch (c0) {
+      case 0: return coop_leaf<0>(tris, lower, r, has, first, count, U, V, W);
+      case 1: return coop_leaf<1>(tris, lower, r, has, first, count, U, V, W);
+      case 2: return coop_leaf<2>(tris, lower, r, has, first, count, U, V, W);
+      case 3: return coop_leaf<3>(tris, lower, r, has, first, count, U, V, W);
+      case 4: return coop_leaf<4>(tris, lower, r, has, first, count, U, V, W);
+      default: return coop_leaf<5>(tris, lower, r, has, first, count, U, V, W);
+    }
+  }
+  return coop_leaf<-1>(tris, lower, r, has, first, count, U, V, W);
+}
+
+template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB, int SS, bool COOP = false>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order,
                     int walk_tail) {
@@ -941,14 +1055,15 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
       if (!more) break;
       continue;
     }
+    constexpr bool kCoop = COOP && !MOTION;
+    bool done = false, walking = false;
     if (alive) {
-      bool done = false;
       // ---- node phase: one entry per step (a cull-pop, a leaf found, or an
       // inner-node visit) for every lane still walking.  The warp steps in
       // lock-step; it stops when no lane walks, or when at most walk_tail
       // lanes walk and some lane holds a leaf (the stragglers resume in the
       // next node phase).
-      bool walking = node != -1;
+      walking = node != -1;
       for (;;) {
         const unsigned wmask = __ballot_sync(alive_mask, walking);
         if (wmask == 0u) break;
@@ -1009,7 +1124,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
       }
       // ---- leaf phase: lanes whose current entry is a leaf scan it, in the
       // order the reference pops it, then pop the next entry.
-      if (!done && !walking && node < -1) {
+      if (!kCoop && !done && !walking && node < -1) {
         uint32_t first, count;
         leaf_decode(node, first, count);
         if (COUNT) { cnt.leafs++; cnt.tris += count; }
@@ -1031,6 +1146,35 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
           if (PF && !MOTION && node >= 0) prefetch_l1(m.nodes + node);
         }
       }
+    }
+    if (kCoop) {  // the leaf phase as one warp-wide list of triangle tests
+      const bool has = alive && !done && !walking && node < -1;
+      uint32_t first = 0, count = 0;
+      if (has) {
+        leaf_decode(node, first, count);
+        if (COUNT) { cnt.leafs++; cnt.tris += count; }
+      }
+      float U = 0.f, V = 0.f, W = 0.f;
+      const int32_t idx = coop_leaf_dispatch(reinterpret_cast<const float4*>(m.tris), m.lower_static, r, has, first,
+                                             count, U, V, W);
+      if (has) {
+        if (idx != -1) {
+          h.elem = idx;
+          h.u = U;
+          h.v = V;
+          h.w = W;
+          hit = true;
+        }
+        if ((ANY && idx != -1) || sp == 0) {
+          done = true;
+        } else {
+          const int2 e = stk.get(--sp);
+          node = e.x;
+          nodeT = __int_as_float(e.y);
+        }
+      }
+    }
+    if (alive) {
       if (!walking && node == -1) done = true;
       if (done) {
         store_hit(hits, rid, r, hit, h);
@@ -1056,7 +1200,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
 // intersect.go:226) and ends when its part of the stack is empty, after
 // which the next geom of the leaf, or the top level, continues.  Node
 // visits, pops, culls and triangle tests per ray are the reference's.
-template <bool ANY>
+template <bool ANY, bool COOP = false>
 __global__ void __launch_bounds__(128, 8)
     k_trace_scene_ww(const DTop top, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch,
                      const unsigned long long* n_dev, const uint32_t* order, int walk_tail) {
@@ -1115,9 +1259,9 @@ __global__ void __launch_bounds__(128, 8)
       if (!more) break;
       continue;
     }
+    bool done = false, walking = false;
     if (alive) {
-      bool done = false;
-      bool walking = node != -1;
+      walking = node != -1;
       for (;;) {
         const unsigned wmask = __ballot_sync(alive_mask, walking);
         if (wmask == 0u) break;
@@ -1244,14 +1388,28 @@ __global__ void __launch_bounds__(128, 8)
         (void)need_pop;
         if (node == -1) walking = false;
       }
-      // ---- leaf phase: a mesh leaf, scanned in the reference's order
-      if (!done && !walking && node < -1 && geom >= 0) {
+    }
+    // ---- leaf phase: a mesh leaf, scanned in the reference's order (COOP:
+    // the warp's leaves as one list of triangle tests, all lanes)
+    const bool has_leaf = alive && !done && !walking && node < -1 && geom >= 0;
+    int32_t cidx = -1;
+    float cU = 0.f, cV = 0.f, cW = 0.f;
+    if (COOP) {
+      uint32_t first = 0, count = 0;
+      if (has_leaf) leaf_decode(node, first, count);
+      cidx = coop_leaf_dispatch(mtris, lower, r, has_leaf, first, count, cU, cV, cW);
+    }
+    if (alive) {
+      if (has_leaf) {
         uint32_t first, count;
         leaf_decode(node, first, count);
-        float U = 0.f, V = 0.f, W = 0.f;
-        DMesh M;
-        M.lower_static = lower;
-        const int32_t idx = leaf_scan_dispatch<false>(M, r, first, count, mtris, mtris, 0.f, 1.f, U, V, W);
+        float U = cU, V = cV, W = cW;
+        int32_t idx = cidx;
+        if (!COOP) {
+          DMesh M;
+          M.lower_static = lower;
+          idx = leaf_scan_dispatch<false>(M, r, first, count, mtris, mtris, 0.f, 1.f, U, V, W);
+        }
         if (idx != -1) {
           h.elem = idx;
           h.geom = geom;
@@ -1554,6 +1712,9 @@ int launch_persistent_smem(K k, const TraceLaunch& l, int block, size_t smem, A.
 template <bool MOTION, bool ANY, bool COUNT, int MINB>
 int launch_ww(const DMesh& mesh, const TraceLaunch& l, int block) {
   const int tail = l.walk_tail;
+  if (!MOTION && (l.kernel & kKernelCoopLeaf) && !(l.kernel & (kKernelSharedStack | kKernelPrefetch)))
+    return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, 0, true>, l, block, mesh, l.rays, l.hits,
+                             l.n, l.scratch, l.order, tail);
   if (l.kernel & kKernelSharedStack) {
     constexpr int SS = kSharedStackEntries;
     return launch_persistent_smem(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, SS>, l, block,
@@ -1589,7 +1750,7 @@ int launch_mesh_m(const DMesh& mesh, const TraceLaunch& l) {
 template <bool ANY, bool COUNT>
 int launch_scene_t(const DTop& top, const TraceLaunch& l) {
   if (!COUNT && top.all_static && (l.kernel & kKernelWhileWhile)) {
-    auto k = k_trace_scene_ww<ANY>;
+    auto k = (l.kernel & kKernelCoopLeaf) ? k_trace_scene_ww<ANY, true> : k_trace_scene_ww<ANY, false>;
     const int grid = persistent_grid(k, 128, l.grid);
     k<<<grid, 128, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order, l.walk_tail);
     return (int)cudaGetLastError();
