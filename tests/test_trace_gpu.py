@@ -231,3 +231,26 @@ def test_scene_with_sphere_geoms(ctx, orc, tuning):
         assert (got["geom"] >= ids[12]).any()  # some rays end on spheres
     finally:
         ctx.set_tuning(45, 0, 0, 0, 8)
+
+
+def test_host_trace_equals_device_trace(ctx, orc):
+    """A host-pointer trace (rays staged in, hits copied out inside the call)
+    of 2,500,001 rays equals the device-pointer trace of the same rays bit
+    for bit, and its visit counters equal the oracle's."""
+    import torch
+    v, ip = scenes.triangle_soup(100000, 41, edge=0.006)
+    geom = ctx.mesh_build(v, ip)
+    rays = scenes.incoherent_rays(2_500_001, 42)
+    dev = torch.from_numpy(np.ascontiguousarray(rays.T)).cuda()
+    for shadow in (False, True):
+        host = ctx.trace_mesh(geom, rays, shadow=shadow, counters=True)
+        d = ctx.trace_mesh(geom, dev, shadow=shadow)
+        ctx.sync()  # device-pointer traces are asynchronous on the context's stream
+        d = {k: d[k].cpu().numpy() for k in ("prim", "t", "u", "v", "w")}
+        assert_hits_equal(host, d, what=f"host vs device shadow={shadow}")
+        assert host["stats"]["rays"] == rays.shape[0]
+        if not shadow:
+            ref = orc.Mesh(v, ip).trace(rays, counters=True)
+            c = np.asarray(ref["counters"], np.uint64)
+            assert host["stats"]["node_visits"] == int(c[:, 0].sum())
+            assert host["stats"]["tri_tests"] == int(c[:, 2].sum())

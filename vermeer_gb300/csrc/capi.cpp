@@ -249,9 +249,13 @@ int read_status(vmr_ctx* ctx, vmr_trace_stats* stats) {
   return VMR_OK;
 }
 
-// One traversal launch: rays/hits are device pointers here.
-int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int flags, const vmr_hits& h,
-              vmr_trace_stats* stats) {
+// Sort (when the tuning asks) and traversal of n device rays, queued on
+// ctx->stream.  reset: zero the whole scratch (ray counter, status, visit
+// counters); otherwise only the ray counter, so consecutive launches add up
+// their counters and statuses.  first/last: record the timing events (ev0,
+// evm around the sort of the first launch; ev1 after the last traversal).
+int launch_trace_chunk(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int flags, const vmr_hits& h,
+                       bool reset, bool first, bool last) {
   vmr::TraceLaunch l{};
   l.rays = vmr::RaySoA{r.px, r.py, r.pz, r.dx, r.dy, r.dz, r.tmax, r.time};
   l.hits = vmr::HitSoA{h.prim, h.geom, h.t, h.u, h.v, h.w};
@@ -266,8 +270,9 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   l.grid = tn.blocks_per_sm;
   l.refill_min = tn.refill_min;
   l.walk_tail = tn.walk_tail;
-  VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
-  VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  if (reset) VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
+  else VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(unsigned long long), ctx->stream));  // next_ray
+  if (first) VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   const bool scene_sort = !mesh && ctx->top.dtop.all_static && !(flags & VMR_TRACE_COUNT);
   if ((mesh || scene_sort) && (tn.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
     // Key-ordered copy of the rays (raysort.cu); hits go back through order[].
@@ -288,10 +293,18 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
     l.rays = sorted;
     l.order = order;
   }
-  VMR_CUDA(ctx, cudaEventRecord(ctx->evm, ctx->stream));
+  if (first) VMR_CUDA(ctx, cudaEventRecord(ctx->evm, ctx->stream));
   int e = mesh ? vmr::launch_trace_mesh(*mesh, l) : vmr::launch_trace_scene(ctx->top.dtop, l);
   if (e != 0) return cuda_fail(ctx, (cudaError_t)e, "trace kernel launch");
-  VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  if (last) VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  return VMR_OK;
+}
+
+// One traversal launch: rays/hits are device pointers here.
+int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int flags, const vmr_hits& h,
+              vmr_trace_stats* stats) {
+  int rc = launch_trace_chunk(ctx, mesh, r, n, flags, h, true, true, true);
+  if (rc != VMR_OK) return rc;
   if (stats) stats->rays = n;
   if (flags & VMR_TRACE_DEVICE) return VMR_OK;
   int st = read_status(ctx, stats);
@@ -303,7 +316,12 @@ int run_trace(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_t n, int 
   return st;
 }
 
-// Host-pointer trace: stage rays in, run, copy hits out.
+// Host-pointer trace: stage rays in, sort and trace, copy hits out, all
+// queued on ctx->stream; the status read after the downloads is the one
+// synchronisation.  (Splitting the call into chunks whose copies overlap the
+// neighbouring chunks' traversal measured slower on GB300: every persistent
+// launch ends with a tail in which SMs drain, and sorting smaller batches
+// groups rays less well, which cost more than the overlapped copies saved.)
 int trace_host(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays* rays, size_t n, int flags, const vmr_hits* hits,
                vmr_trace_stats* stats) {
   const size_t fb = n * sizeof(float);
@@ -316,22 +334,31 @@ int trace_host(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays* rays, size_t n, 
   for (int k = 0; k < n_in; ++k) {
     dst[k] = reinterpret_cast<float*>(base + fb * k);
     if (!src[k]) return fail(ctx, VMR_ERR_INVALID, "null ray array");
-    if (n) VMR_CUDA(ctx, cudaMemcpyAsync(dst[k], src[k], fb, cudaMemcpyHostToDevice, ctx->stream));
   }
-  vmr_rays dr{dst[0], dst[1], dst[2], dst[3], dst[4], dst[5], dst[6], n_in == 8 ? dst[7] : nullptr};
+  for (int k = 0; k < n_in; ++k)
+    if (n) VMR_CUDA(ctx, cudaMemcpyAsync(dst[k], src[k], fb, cudaMemcpyHostToDevice, ctx->stream));
   char* hb = base + fb * n_in;
-  vmr_hits dh{hits->prim ? reinterpret_cast<int32_t*>(hb) : nullptr,
-              hits->geom ? reinterpret_cast<int32_t*>(hb + fb) : nullptr,
-              hits->t ? reinterpret_cast<float*>(hb + 2 * fb) : nullptr,
-              hits->u ? reinterpret_cast<float*>(hb + 3 * fb) : nullptr,
-              hits->v ? reinterpret_cast<float*>(hb + 4 * fb) : nullptr,
-              hits->w ? reinterpret_cast<float*>(hb + 5 * fb) : nullptr};
-  int st = run_trace(ctx, mesh, dr, n, flags & ~VMR_TRACE_DEVICE, dh, stats);
   void* outs[6] = {hits->prim, hits->geom, hits->t, hits->u, hits->v, hits->w};
-  void* douts[6] = {dh.prim, dh.geom, dh.t, dh.u, dh.v, dh.w};
+  char* douts[6];
+  for (int k = 0; k < 6; ++k) douts[k] = outs[k] ? hb + (size_t)k * fb : nullptr;
+  vmr_rays dr{dst[0], dst[1], dst[2], dst[3], dst[4], dst[5], dst[6], n_in == 8 ? dst[7] : nullptr};
+  vmr_hits dh{reinterpret_cast<int32_t*>(douts[0]), reinterpret_cast<int32_t*>(douts[1]),
+              reinterpret_cast<float*>(douts[2]), reinterpret_cast<float*>(douts[3]),
+              reinterpret_cast<float*>(douts[4]), reinterpret_cast<float*>(douts[5])};
+  int rc = launch_trace_chunk(ctx, mesh, dr, n, flags & ~VMR_TRACE_DEVICE, dh, true, true, true);
+  if (rc != VMR_OK) {
+    cudaStreamSynchronize(ctx->stream);
+    return rc;
+  }
   for (int k = 0; k < 6; ++k)
     if (outs[k] && n) VMR_CUDA(ctx, cudaMemcpyAsync(outs[k], douts[k], fb, cudaMemcpyDeviceToHost, ctx->stream));
-  VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (stats) stats->rays = n;
+  const int st = read_status(ctx, stats);  // synchronises ctx->stream, hence the downloads
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->evm, ctx->ev1);
+    stats->kernel_ms = ms;
+  }
   return st;
 }
 
