@@ -2,8 +2,9 @@
 //
 // No reference counterpart.  The network (80 inputs, 4 hidden ReLU layers
 // of 64, 40 outputs = 8 vMF lobes; no biases, input 78 is the constant 1)
-// runs fused per tile of 128 rows: one CTA of 128 threads holds the bf16
-// weights in shared memory, thread r owns row r, and each layer is
+// runs fused per tile of 128 rows: a group of 128 threads works on a tile
+// with the bf16 weights in shared memory (inference: two groups per CTA
+// share one copy), thread r owns row r, and each layer is
 //   A (128 x K activations, smem) * B (N x K weights, smem) -> D (TMEM, fp32)
 // issued as K/16 tcgen05.mma (kind::f16, bf16 inputs, fp32 accumulate) by
 // one thread and committed to an mbarrier; every thread then reads its row of
@@ -308,28 +309,101 @@ __device__ void out_grad(const float* o, const float* w, float weight, float* g,
   }
 }
 
-__global__ void __launch_bounds__(128) k_guide_infer(GuideRows in, const __nv_bfloat16* wf, float* out, int* err) {
+// Inference runs two tile streams per CTA: 256 threads in two groups of
+// four warps share one copy of the weights; each group has its own
+// activation tiles, mbarrier, named barrier (ids 1 and 2) and 64 TMEM
+// columns (the 32x32b loads reach TMEM lanes 32*(warp % 4) .. +31, so the
+// second group's warps read the same 128 lanes in their own columns).  One
+// group's epilogue (TMEM -> ReLU -> bf16 -> shared memory) overlaps the
+// other group's MMAs, and the SM holds twice the warps of a one-tile CTA.
+constexpr uint32_t kGroups = 2;
+constexpr uint32_t kSAGroup = 128 * 80 * 2 + 128 * 64 * 2;  // A0 + A1 of one group: 36864
+// Dynamic shared memory: weights, the groups' tiles, then the control block
+// (no static shared memory, so two CTAs fit an SM's 228 KB).
+constexpr uint32_t kInferCtl = kSWEnd + kGroups * kSAGroup;
+constexpr uint32_t kInferSmem2 = kInferCtl + 64;
+
+__device__ __forceinline__ void group_sync(uint32_t id) {
+  asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+}
+// OR over the group's 128 threads (barrier.red on the group's named barrier).
+__device__ __forceinline__ bool group_any(bool v, uint32_t id) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id)
+      : "memory");
+  return r != 0;
+}
+
+struct GroupShared {
+  uint64_t bar;
+  int abort;
+};
+
+// The forward pass of one tile by one group (features already in its A0):
+// false if a wait ran out.  The output layer ends in the group's TMEM
+// columns 0..47.
+__device__ bool forward_tile_group(char* sm, char* a0, char* a1, GroupShared& gs, uint32_t tmem, uint32_t bid,
+                                   uint32_t r, uint32_t& phase) {
+  const uint32_t lane_base = (r & ~31u) << 16;
+  const uint32_t Ks[5] = {80, 64, 64, 64, 64};
+  const uint32_t Ns[5] = {64, 64, 64, 64, 48};
+  const uint32_t Ws[5] = {kSW0, kSW1, kSW2, kSW3, kSW4};
+  for (int l = 0; l < 5; ++l) {
+    const char* A = (l & 1) ? a1 : a0;
+    fence_async_smem();
+    group_sync(bid);
+    if (r == 0) gemm_issue(tmem, A, sm + Ws[l], Ks[l], Ns[l], &gs.bar);
+    const bool ok = bar_wait(&gs.bar, phase);
+    phase ^= 1u;
+    if (group_any(!ok, bid)) {
+      if (r == 0) gs.abort = 1;
+      return false;
+    }
+    fence_after();
+    if (l == 4) return true;
+    float h[64];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tmem_ld16(tmem + lane_base + 16 * q, h + 16 * q);
+#pragma unroll
+    for (int j = 0; j < 64; ++j) h[j] = h[j] > 0.0f ? h[j] : 0.0f;
+    fence_before();
+    put_row((l & 1) ? a0 : a1, r, 64, h);
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(256) k_guide_infer(GuideRows in, const __nv_bfloat16* wf, float* out, int* err) {
   extern __shared__ __align__(1024) char sm[];
-  __shared__ Shared sh;
-  const uint32_t r = threadIdx.x;
+  GroupShared* gsh = reinterpret_cast<GroupShared*>(sm + kInferCtl);
+  uint32_t& tmem_base = *reinterpret_cast<uint32_t*>(sm + kInferCtl + kGroups * sizeof(GroupShared));
+  const uint32_t g = threadIdx.x / 128u, r = threadIdx.x % 128u;
+  const uint32_t bid = 1u + g;
   const uint64_t n = in.n_dev ? *in.n_dev : in.n;
   if (r == 0) {
-    bar_init(&sh.bar);
-    sh.abort = 0;
+    bar_init(&gsh[g].bar);
+    gsh[g].abort = 0;
   }
   load_tile(sm + kSW0, wf + kWf0, 64, 80);
   load_tile(sm + kSW1, wf + kWf1, 64, 64);
   load_tile(sm + kSW2, wf + kWf2, 64, 64);
   load_tile(sm + kSW3, wf + kWf3, 64, 64);
   load_tile(sm + kSW4, wf + kWf4, 48, 64);
-  if (r < 32) tmem_alloc(&sh.tmem, 64);
+  if (threadIdx.x < 32) tmem_alloc(&tmem_base, 64 * kGroups);
   fence_before();
   __syncthreads();
   fence_after();
-  uint32_t phase = 0;
+  GroupShared& gs = gsh[g];
+  char* a0 = sm + kSWEnd + g * kSAGroup;
+  char* a1 = a0 + 128 * 80 * 2;
+  const uint32_t tmem = tmem_base + 64u * g;
   const uint32_t lane_base = (r & ~31u) << 16;
+  uint32_t phase = 0;
   const uint64_t ntiles = (n + 127) / 128;
-  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  for (uint64_t t = (uint64_t)blockIdx.x * kGroups + g; t < ntiles; t += (uint64_t)gridDim.x * kGroups) {
     const uint64_t row = t * 128 + r;
     float f[80];
     const bool valid = row < n;
@@ -341,20 +415,23 @@ __global__ void __launch_bounds__(128) k_guide_infer(GuideRows in, const __nv_bf
     } else {
       for (int k = 0; k < 80; ++k) f[k] = 0.f;
     }
-    put_row(sm + kSA0, r, 80, f);
-    uint32_t mask[8];
-    if (!forward_tile(sm, sh, phase, mask, false, nullptr, 0, 0, false)) break;
+    put_row(a0, r, 80, f);
+    if (!forward_tile_group(sm, a0, a1, gs, tmem, bid, r, phase)) break;
     float o[48];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) tmem_ld16(sh.tmem + lane_base + 16 * q, o + 16 * q);
+    for (int q = 0; q < 3; ++q) tmem_ld16(tmem + lane_base + 16 * q, o + 16 * q);
     fence_before();
-    if (valid)
-      for (int k = 0; k < 40; ++k) out[(size_t)row * 40 + k] = o[k];
+    if (valid) {
+      float4* dst = reinterpret_cast<float4*>(out + (size_t)row * 40);
+#pragma unroll
+      for (int k = 0; k < 10; ++k) dst[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    }
   }
+  // a group that stopped early waits (bounded) for its MMAs still in flight
+  if (gs.abort) (void)bar_wait(&gs.bar, phase ^ 1u);
   __syncthreads();
-  drain(sh, phase);
-  if (sh.abort && r == 0) atomicExch(err, 1);
-  if (r < 32) tmem_free(sh.tmem, 64);
+  if (r == 0 && gs.abort) atomicExch(err, 1);
+  if (threadIdx.x < 32) tmem_free(tmem_base, 64 * kGroups);
 }
 
 // Forward + loss gradient + backward-data over one tile per iteration.
@@ -608,13 +685,13 @@ __global__ void k_guide_adam(float* W, float* m, float* v, float* grad, const fl
 }  // namespace
 
 void prepare_kernels() {
-  cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+  cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem2);
   cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
   cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgradSmem);
 }
 
 int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int grid, cudaStream_t st) {
-  k_guide_infer<<<grid, 128, kInferSmem, st>>>(rows, static_cast<const __nv_bfloat16*>(wf), out, err);
+  k_guide_infer<<<grid, 256, kInferSmem2, st>>>(rows, static_cast<const __nv_bfloat16*>(wf), out, err);
   return (int)cudaGetLastError();
 }
 
