@@ -374,6 +374,10 @@ def render_extras(ctx, args):
       batched_jobs           64 uneven static/motion jobs traced in one launch,
                              against one launch per job (default and
                              autotuned launch parameters)
+      batched_path_jobs      64 uneven static/motion soups path traced as
+                             one batched render (each job its own scene),
+                             256x256, 32 spp, depth 5, against one render
+                             call per job
       guided_slit            equal-wall-time relMSE (mean and median over
                              pixels) on the slit-light room against a
                              4096-spp float64 plain render, at 512x512
@@ -489,6 +493,45 @@ def render_extras(ctx, args):
         "per_job_launches_mrays_per_s": round(nrays / (seq_default / 1e3) / 1e6, 2),
         "per_job_autotuned_mrays_per_s": round(nrays / (seq_tuned / 1e3) / 1e6, 2),
         "autotune_s": round(tune_s, 2)}
+    # batched path-traced jobs: one launch per stage for all jobs, against one
+    # vmr_render_path call per job (each job its own one-mesh scene)
+    bj = scenes.batched_jobs()
+    ids = [ctx.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_mode=m.get("motion_mode", 0))
+           for m in bj["meshes"]]
+    ctx.set_shaders(bj["shaders"])
+    for g in ids:
+        ctx.mesh_set_shading(g, [0])
+    ctx.set_lights([])
+    ctx.set_disk_lights([])
+    ctx.set_sphere_lights([])
+    ctx.set_quad_lights([])
+    ctx.set_env_light(bj["env"])
+    ctx.set_pixel_filter(vg.FILTER_BOX)
+    W, H = bj["width"], bj["height"]
+    jobs = [dict(geom=g, width=W, height=H, camera=c) for g, c in zip(ids, bj["cameras"])]
+    ctx.render_path_jobs(jobs, 0, 1, 5, max_depth=5)
+    t0 = time.perf_counter()
+    _, jst = ctx.render_path_jobs(jobs, 0, 32, 5, max_depth=5)
+    jwall = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sep_ms = 0.0
+    for g, c in zip(ids, bj["cameras"]):
+        ctx.scene_build([g])
+        ctx.set_camera(c)
+        _, s1 = ctx.render_path(W, H, 0, 32, 5, max_depth=5)
+        sep_ms += s1["ms"]
+    sep_wall = time.perf_counter() - t0
+    n_samp = len(jobs) * W * H * 32
+    out["batched_path_jobs"] = {
+        "workload": "64 jobs: triangle soups of log-uniform [1k, 200k] triangles (seed 4), every other one with "
+                    "two-key linear motion (velocity in a 0.05 ball, shutter [0, 1]); each job 256x256, 32 spp, "
+                    "depth 5, RR from 3, Lambert 0.7 under a constant white environment",
+        "triangles": int(np.sum(bj["sizes"])),
+        "one_call": {"samples_per_s": round(n_samp / (jst["ms"] / 1e3), 1),
+                     "mrays_per_s": round((jst["rays"] + jst["shadow_rays"]) / (jst["ms"] / 1e3) / 1e6, 2),
+                     "device_ms": round(jst["ms"], 2), "wall_s": round(jwall, 3)},
+        "per_job_calls": {"samples_per_s": round(n_samp / (sep_ms / 1e3), 1), "device_ms": round(sep_ms, 2),
+                          "wall_s": round(sep_wall, 3)}}
     # guided vs plain, equal wall time
     W = H = 512
     sc = scenes.slit_room(200_000, width=W, height=H)

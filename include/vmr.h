@@ -523,6 +523,25 @@ typedef struct {
  * fold starts at i+1 and so counts the initial buffer as a sample, F6). */
 int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* params, float* fb, vmr_path_stats* stats);
 
+/* Batched path-traced jobs (no reference counterpart: the reference renders
+ * one scene per process).  Every job is its own one-mesh scene: its mesh
+ * (static or motion, with its shading set by vmr_mesh_set_shading), camera
+ * and image; the jobs share the material table and the environment light
+ * (their only light).  The static jobs' paths run through one set of
+ * wavefront launches (one per stage and bounce), the motion jobs' through a
+ * second; a path's rays trace only its job's mesh.  Each job's image equals vmr_render_path of that mesh alone as the
+ * scene, with the same params (seed, iterations, depths), bit for bit.
+ * params: width/height are ignored (per job), GUIDED and fb64 are not
+ * supported.  fb: width*height*3 floats per job (host), in/out. */
+typedef struct {
+    uint32_t geom;
+    uint32_t width, height;
+    vmr_camera camera;
+    float* fb;
+} vmr_path_job;
+int vmr_render_path_jobs(vmr_ctx* ctx, const vmr_path_job* jobs, uint32_t n_jobs, const vmr_path_params* params,
+                         vmr_path_stats* stats);
+
 /* ------------------------------------------------------------ path guide */
 /* No counterpart in the reference.  A small MLP proposes directions at path
  * vertices: inputs = the hit point normalised to the scene bounds [lo, hi]

@@ -276,3 +276,38 @@ def test_pt_motion_and_spheres_match_float_oracle(ctx, orc, kind):
     ok = (np.abs(got - ref) <= REL * (1 + np.abs(ref))).all(-1)
     assert ok.mean() >= FRAC_EQUAL, ok.mean()
     assert abs(got.mean() - ref.mean()) <= 1e-4 * ref.mean()
+
+
+# -------------------------------------------------------- batched jobs ----
+@pytest.mark.gpu
+def test_path_jobs_equal_one_scene_renders(ctx):
+    """vmr_render_path_jobs: each job's image equals vmr_render_path of its
+    mesh alone as the scene (same seed, iterations, depths), bit for bit,
+    static and motion meshes, images of different sizes, in one call."""
+    bj = scenes.batched_jobs(n_jobs=5, seed=9, width=40, height=32, lo=500, hi=6000)
+    ids = []
+    for m in bj["meshes"]:
+        g = ctx.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_mode=m.get("motion_mode", 0))
+        ids.append(g)
+    ctx.set_shaders(bj["shaders"])
+    for g in ids:
+        ctx.mesh_set_shading(g, [0])
+    ctx.set_lights([])
+    ctx.set_quad_lights([])
+    ctx.set_env_light(bj["env"])
+    sizes = [(40, 32), (24, 24), (40, 32), (17, 9), (33, 40)]
+    jobs = [dict(geom=g, width=w, height=h, camera=bj["cameras"][k]) for k, (g, (w, h)) in enumerate(zip(ids, sizes))]
+    imgs, st = ctx.render_path_jobs(jobs, 0, 3, 13, max_depth=5)
+    assert st["samples"] == 3 * sum(w * h for w, h in sizes)
+    for k, (g, (w, h)) in enumerate(zip(ids, sizes)):
+        ctx.scene_build([g])
+        ctx.set_camera(bj["cameras"][k])
+        ref, _ = ctx.render_path(w, h, 0, 3, 13, max_depth=5)
+        assert imgs[k].tobytes() == ref.tobytes(), k
+        assert float(imgs[k].mean()) > 0.0
+    # split over calls, one iteration of all jobs per batch
+    part, _ = ctx.render_path_jobs(jobs, 0, 1, 13, max_depth=5)
+    part, _ = ctx.render_path_jobs([dict(j, fb=f) for j, f in zip(jobs, part)], 1, 2, 13, max_depth=5,
+                                   max_batch_samples=1000)
+    for k in range(len(jobs)):
+        assert part[k].tobytes() == imgs[k].tobytes(), k

@@ -132,6 +132,10 @@ class PathStats(ctypes.Structure):
                 ("train_steps", U32), ("train_loss", ctypes.c_float)]
 
 
+class PathJob(ctypes.Structure):
+    _fields_ = [("geom", U32), ("width", U32), ("height", U32), ("camera", Camera), ("fb", P)]
+
+
 PATH_NO_GRAPH = 1
 PATH_GUIDED = 2
 PATH_TRAIN = 4
@@ -187,6 +191,7 @@ SIGNATURES = {
     "vmr_set_quad_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_env_light": (ctypes.c_int, [P, P]),
     "vmr_render_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, ctypes.POINTER(PathStats)]),
+    "vmr_render_path_jobs": (ctypes.c_int, [P, P, U32, ctypes.POINTER(PathParams), ctypes.POINTER(PathStats)]),
     "vmr_guide_init": (ctypes.c_int, [P, ctypes.c_uint64]),
     "vmr_guide_set_weights": (ctypes.c_int, [P, P]),
     "vmr_guide_get_weights": (ctypes.c_int, [P, P]),

@@ -404,13 +404,41 @@ class Context:
                                                 pos.shape[0], _p(lo), _p(hi), ctypes.byref(a), ctypes.byref(loss)))
         return loss.value
 
-    def set_camera(self, cam: dict):
+    @staticmethod
+    def _camera(cam: dict):
         c = _lib.Camera()
         for i in range(16):
             c.m[i] = float(cam["m"][i])
         c.tan_theta_focal, c.aspect, c.focal, c.radius = (float(cam[k]) for k in
                                                          ("tan_theta_focal", "aspect", "focal", "radius"))
+        return c
+
+    def set_camera(self, cam: dict):
+        c = self._camera(cam)
         self._check(self.L.vmr_set_camera(self.h, ctypes.byref(c)))
+
+    def render_path_jobs(self, jobs, iter_begin: int, iter_count: int, seed: int, max_depth: int = 4,
+                         rr_depth: int = 3, max_batch_samples: int = 0, graph: bool = True):
+        """Batched path-traced jobs (vmr_render_path_jobs): jobs are dicts
+        with geom, width, height, camera and optionally fb (float32
+        [height, width, 3], folded into).  Returns (images, stats)."""
+        arr = (_lib.PathJob * len(jobs))()
+        fbs = []
+        for i, j in enumerate(jobs):
+            fb = j.get("fb")
+            if fb is None:
+                fb = np.zeros((j["height"], j["width"], 3), np.float32)
+            fb = np.ascontiguousarray(fb, np.float32)
+            fbs.append(fb)
+            arr[i].geom, arr[i].width, arr[i].height = int(j["geom"]), int(j["width"]), int(j["height"])
+            arr[i].camera = self._camera(j["camera"])
+            arr[i].fb = _p(fb)
+        p = _lib.PathParams(0, 0, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
+                            0 if graph else _lib.PATH_NO_GRAPH, None, 0.0, 0, 0, 0.0)
+        st = _lib.PathStats()
+        self._check(self.L.vmr_render_path_jobs(self.h, arr, len(jobs), ctypes.byref(p), ctypes.byref(st)))
+        return fbs, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,
+                         graph_replays=st.graph_replays, ms=st.ms)
 
     def render(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, fb=None,
                max_batch_samples: int = 0):

@@ -77,6 +77,7 @@ struct RenderState {
   std::vector<double> filter_host;
   DevBuf filter;
   DevBuf outbuf;   // vmr_encode_rgbe staging for host framebuffers
+  DevBuf jobmesh;  // batched path jobs: the mesh table the traversal reads
   DevBuf buf;      // reference mode batch buffers
   DevBuf ptbuf;    // extended mode batch buffers
   void* pt_host = nullptr;  // pinned per-batch parameters (extended mode)

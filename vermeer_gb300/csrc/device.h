@@ -150,6 +150,10 @@ struct TraceLaunch {
   int refill_min;
   int walk_tail;
   void* stream;
+  // scene traces in job mode (batched renders): no top level; ray i enters
+  // mesh path_geom[ray_path[i]] directly (both set or both null)
+  const uint32_t* ray_path;
+  const uint32_t* path_geom;
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);
 int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int bits, uint32_t* keys, uint32_t* hist,

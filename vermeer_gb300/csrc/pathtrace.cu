@@ -59,6 +59,16 @@ struct PtIter {
   unsigned long long n;  // paths = iters * npix
 };
 
+// One job of a batched render (vmr_render_path_jobs): its mesh, camera and
+// image; pix0 is the first pixel of the job in the batch's pixel arena (the
+// jobs' images end to end, in job order).
+struct PtJob {
+  vmr_camera cam;
+  uint32_t width, height, npix, geom;
+  uint32_t pix0;
+  uint32_t pad[3];
+};
+
 struct PtBatch {
   uint32_t width, height, npix;
   uint32_t nl;        // lights
@@ -107,6 +117,10 @@ struct PtBatch {
   uint32_t rcap;
   unsigned long long* rcount;  // [2]: records this batch, records in total
   uint32_t* last_rec;          // per path: its last record awaiting L_mark
+  // batched jobs (n_jobs > 0): the job table and each path's mesh
+  const PtJob* jobs;
+  uint32_t n_jobs;
+  uint32_t* pgeom;             // cap: path -> its job's geom
   float* snee;                 // 7 * cap: per shadow slot, the vertex's normal and
                                // direction toward the previous vertex, and the
                                // light sample's training weight (0: no record)
@@ -316,11 +330,24 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
   const uint64_t n = b.it->n < b.cap ? b.it->n : b.cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) b.qlen[0] = n;
   for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t pix = (uint32_t)(s % b.npix);
+    uint32_t pix = (uint32_t)(s % b.npix);
     const uint32_t j = b.it->iter0 + (uint32_t)(s / b.npix) + 1;
     V3 P, D;
     float time, lambda;
-    camera_primary(b.cam, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+    if (b.n_jobs) {  // the job holding arena pixel pix (jobs sorted by pix0)
+      uint32_t lo = 0, hi = b.n_jobs - 1;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (b.jobs[mid].pix0 <= pix) lo = mid;
+        else hi = mid - 1;
+      }
+      const PtJob& job = b.jobs[lo];
+      pix -= job.pix0;
+      b.pgeom[s] = job.geom;
+      camera_primary(job.cam, job.width, job.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+    } else {
+      camera_primary(b.cam, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+    }
     const float o[3] = {P.x, P.y, P.z};
     put_ray(b.qray[0], b.cap, s, o, D, __int_as_float(0x7f800000), time);
     b.qpath[0][s] = (uint32_t)s;
@@ -778,7 +805,7 @@ int pfail(vmr_ctx* ctx, int code, const std::string& msg) {
 
 // Launches one batch's stages on the context's stream (also used while
 // capturing the graph).  Every count is read on the device.
-int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool guided, bool train,
+int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr, int grid, bool guided, bool train,
                  const guide::GuideRows& grows) {
   cudaStream_t st = ctx->stream;
   const size_t nq = kPtMaxDepth + 2, ns = kPtMaxDepth + 1;
@@ -801,7 +828,11 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool g
     l.stream = st;
     l.kernel = ctx->tuning.kernel;
     l.walk_tail = ctx->tuning.walk_tail;
-    if (launch_trace_scene(ctx->top.dtop, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+    if (b.n_jobs) {
+      l.ray_path = b.qpath[d & 1];
+      l.path_geom = b.pgeom;
+    }
+    if (launch_trace_scene(top, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
     if (guided) {
       k_pt_prep<<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
@@ -828,7 +859,11 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, DScratch* scr, int grid, bool g
       s.stream = st;
       s.kernel = ctx->tuning.kernel;
       s.walk_tail = ctx->tuning.walk_tail;
-      if (launch_trace_scene(ctx->top.dtop, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+      if (b.n_jobs) {
+        s.ray_path = b.spath;
+        s.path_geom = b.pgeom;
+      }
+      if (launch_trace_scene(top, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
       if (train) k_pt_resolve<true><<<grid, kPtBlock, 0, st>>>(b, d);
       else k_pt_resolve<false><<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
@@ -866,17 +901,41 @@ int vmr_set_env_light(vmr_ctx* ctx, const float radiance[3]) {
   return VMR_OK;
 }
 
-int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_stats* stats) {
+// The extended path tracer over the context's scene (jobs == nullptr) or
+// over batched jobs (each path traces only its job's mesh; lights: the
+// environment).  fb: the scene's image; jobs: each job's own image.
+static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_stats* stats,
+                            const vmr_path_job* jobs, uint32_t n_jobs) {
   using namespace vmr;
-  if (!ctx || !p || !fb) return VMR_ERR_INVALID;
+  if (!ctx || !p || (!fb && !jobs)) return VMR_ERR_INVALID;
   if (ctx->device < 0) return pfail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot render");
-  if (!ctx->top.valid) return pfail(ctx, VMR_ERR_INVALID, "no scene: call vmr_scene_build first");
-  if (!ctx->render.has_camera) return pfail(ctx, VMR_ERR_INVALID, "no camera");
-  if (p->width == 0 || p->height == 0 || p->width > 4096 || p->height > 4096)
-    return pfail(ctx, VMR_ERR_INVALID, "image size must be in [1, 4096] (RasterXY uses m = 12)");
+  std::vector<uint32_t> used_geoms;
+  uint64_t npix_jobs = 0;
+  if (!jobs) {
+    if (!ctx->top.valid) return pfail(ctx, VMR_ERR_INVALID, "no scene: call vmr_scene_build first");
+    if (!ctx->render.has_camera) return pfail(ctx, VMR_ERR_INVALID, "no camera");
+    if (p->width == 0 || p->height == 0 || p->width > 4096 || p->height > 4096)
+      return pfail(ctx, VMR_ERR_INVALID, "image size must be in [1, 4096] (RasterXY uses m = 12)");
+    used_geoms = ctx->top.host.geom_order;
+  } else {
+    if (n_jobs == 0) return VMR_OK;
+    if (p->flags & VMR_PATH_GUIDED) return pfail(ctx, VMR_ERR_UNSUPPORTED, "batched jobs render without the guide");
+    if (p->fb64) return pfail(ctx, VMR_ERR_UNSUPPORTED, "batched jobs have no float64 images");
+    for (uint32_t k = 0; k < n_jobs; ++k) {
+      const vmr_path_job& jb = jobs[k];
+      if (!jb.fb) return pfail(ctx, VMR_ERR_INVALID, "a job has no image buffer");
+      if (jb.width == 0 || jb.height == 0 || jb.width > 4096 || jb.height > 4096)
+        return pfail(ctx, VMR_ERR_INVALID, "job image size must be in [1, 4096] (RasterXY uses m = 12)");
+      if (jb.geom >= ctx->meshes.size()) return pfail(ctx, VMR_ERR_INVALID, "job geom out of range");
+      if (!(jb.camera.radius >= 0.0f)) return pfail(ctx, VMR_ERR_INVALID, "job camera radius must be >= 0");
+      used_geoms.push_back(jb.geom);
+      npix_jobs += (uint64_t)jb.width * jb.height;
+    }
+    if (npix_jobs > 0xffffffffull) return pfail(ctx, VMR_ERR_INVALID, "too many job pixels");
+  }
   if (p->max_depth > (uint32_t)kPtMaxDepth) return pfail(ctx, VMR_ERR_INVALID, "max_depth must be <= 32");
   auto& R = ctx->render;
-  for (uint32_t g : ctx->top.host.geom_order) {
+  for (uint32_t g : used_geoms) {
     const auto& mr = ctx->meshes[g];
     if (mr->host.motion() && mr->aidx.p == nullptr)
       return pfail(ctx, VMR_ERR_INVALID, "a motion mesh in the scene has no shading (vmr_mesh_set_shading)");
@@ -888,6 +947,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   std::vector<PtLight> lights;
   std::vector<int32_t> log(std::max<uint32_t>(1, n_geoms), -1);
   for (const auto& t : R.lights) {
+    if (jobs) break;  // batched jobs: the environment only
     if (t.shader >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "light shader out of range");
     PtLight l{};
     l.kind = 0;
@@ -904,6 +964,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     lights.push_back(l);
   }
   for (const auto& qd : R.quads) {
+    if (jobs) break;
     if (qd.shader >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "quad light shader out of range");
     PtLight l{};
     l.kind = 1;
@@ -946,8 +1007,11 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   }
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
-  const uint32_t npix = p->width * p->height;
-  const uint32_t per_batch = p->max_batch_samples ? p->max_batch_samples : (2u << 20);
+  const uint32_t npix = jobs ? (uint32_t)npix_jobs : p->width * p->height;
+  // batched jobs default to larger batches: with many images per iteration a
+  // 2M-path batch holds about one iteration, and each bounce's launch ends
+  // in a longer tail relative to its work
+  const uint32_t per_batch = p->max_batch_samples ? p->max_batch_samples : (jobs ? (8u << 20) : (2u << 20));
   uint32_t ipb = std::max<uint32_t>(1, per_batch / npix);
   if (p->iter_count > 0 && ipb > p->iter_count) ipb = p->iter_count;
   const uint64_t cap = (uint64_t)ipb * npix;
@@ -988,7 +1052,8 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
                o_shader = carve(std::max<size_t>(1, R.shaders.size()) * sizeof(vmr_shader_std)),
                o_log = carve(log.size() * 4), o_grow = carve(guided ? cap * 9 * 4 : 0),
                o_gout = carve(guided ? cap * 40 * 4 : 0), o_rec = carve(rcap * kRecCols * 4),
-               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32), o_snee = carve(train ? cap * 7 * 4 : 0);
+               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32), o_snee = carve(train ? cap * 7 * 4 : 0),
+               o_jobs = carve(jobs ? n_jobs * sizeof(PtJob) : 0), o_pgeom = carve(jobs ? cap * 4 : 0);
   PCUDA(R.ptbuf.ensure(bytes));
   char* base = R.ptbuf.as<char>();
   uint64_t fwd[52], inv[52];
@@ -1002,7 +1067,29 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     PCUDA(cudaMemcpyAsync(base + o_shader, R.shaders.data(), R.shaders.size() * sizeof(vmr_shader_std),
                           cudaMemcpyHostToDevice, st));
   PCUDA(cudaMemcpyAsync(base + o_log, log.data(), log.size() * 4, cudaMemcpyHostToDevice, st));
-  PCUDA(cudaMemcpyAsync(base + o_fb, fb, (size_t)npix * 3 * 4, cudaMemcpyHostToDevice, st));
+  // batched jobs: their images end to end in the pixel arena, and the job table
+  std::vector<float> arena;
+  std::vector<PtJob> jtab;
+  if (jobs) {
+    arena.resize((size_t)npix * 3);
+    uint32_t pix0 = 0;
+    for (uint32_t k = 0; k < n_jobs; ++k) {
+      PtJob j{};
+      j.cam = jobs[k].camera;
+      j.width = jobs[k].width;
+      j.height = jobs[k].height;
+      j.npix = j.width * j.height;
+      j.geom = jobs[k].geom;
+      j.pix0 = pix0;
+      std::memcpy(arena.data() + (size_t)pix0 * 3, jobs[k].fb, (size_t)j.npix * 12);
+      pix0 += j.npix;
+      jtab.push_back(j);
+    }
+    PCUDA(cudaMemcpyAsync(base + o_jobs, jtab.data(), jtab.size() * sizeof(PtJob), cudaMemcpyHostToDevice, st));
+    PCUDA(cudaMemcpyAsync(base + o_fb, arena.data(), arena.size() * 4, cudaMemcpyHostToDevice, st));
+  } else {
+    PCUDA(cudaMemcpyAsync(base + o_fb, fb, (size_t)npix * 3 * 4, cudaMemcpyHostToDevice, st));
+  }
   if (p->fb64) PCUDA(cudaMemcpyAsync(base + o_fb64, p->fb64, (size_t)npix * 3 * 8, cudaMemcpyHostToDevice, st));
   PtBatch b{};
   b.width = p->width;
@@ -1062,6 +1149,25 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   b.rcount = train ? reinterpret_cast<unsigned long long*>(base + o_rcnt) : nullptr;
   b.last_rec = train ? reinterpret_cast<uint32_t*>(base + o_last) : nullptr;
   b.snee = train ? reinterpret_cast<float*>(base + o_snee) : nullptr;
+  b.jobs = jobs ? reinterpret_cast<const PtJob*>(base + o_jobs) : nullptr;
+  b.n_jobs = jobs ? n_jobs : 0u;
+  b.pgeom = jobs ? reinterpret_cast<uint32_t*>(base + o_pgeom) : nullptr;
+  // the traversal's view: the scene's top level, or for jobs only the mesh
+  // table (each ray enters its own mesh)
+  DTop top = ctx->top.dtop;
+  if (jobs) {
+    std::vector<DMesh> table(ctx->meshes.size());
+    for (size_t g = 0; g < table.size(); ++g) table[g] = ctx->meshes[g]->dmesh;
+    PCUDA(R.jobmesh.ensure(table.size() * sizeof(DMesh)));
+    PCUDA(cudaMemcpyAsync(R.jobmesh.p, table.data(), table.size() * sizeof(DMesh), cudaMemcpyHostToDevice, st));
+    top = DTop{};
+    top.meshes = R.jobmesh.as<DMesh>();
+    top.n_geoms = (uint32_t)table.size();
+    top.keys = 1;
+    top.all_static = 1u;
+    for (uint32_t g : used_geoms)
+      if (ctx->meshes[g]->host.motion()) top.all_static = 0u;
+  }
   if (train) PCUDA(cudaMemsetAsync(b.rcount, 0, 32, st));
   guide::GuideRows grows{};
   if (guided) {
@@ -1109,7 +1215,9 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     fold(&b.filt, sizeof(b.filt));
     fold(b.env, sizeof(b.env));
     fold(&b.sel, sizeof(b.sel));
-    fold(&ctx->top.dtop, sizeof(ctx->top.dtop));
+    fold(&top, sizeof(top));
+    const uint64_t nj = b.n_jobs;
+    fold(&nj, sizeof(nj));
     fold(&b.alpha, sizeof(b.alpha));
     fold(b.glo, sizeof(b.glo));
     fold(grows.inv_ext, sizeof(grows.inv_ext));
@@ -1123,7 +1231,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     }
     cudaGraph_t g = nullptr;
     PCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-    const int rc = launch_batch(ctx, b, scr, grid, guided, train, grows);
+    const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows);
     const cudaError_t ec = cudaStreamEndCapture(st, &g);
     if (rc != VMR_OK) {
       if (g) cudaGraphDestroy(g);
@@ -1142,7 +1250,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
       PCUDA(cudaGraphLaunch(R.graph.exec, st));
       ++replays;
     } else {
-      const int rc = launch_batch(ctx, b, scr, grid, guided, train, grows);
+      const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows);
       if (rc != VMR_OK) return rc;
     }
     if (train) {  // online training on this batch's records (device counts)
@@ -1187,7 +1295,7 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     }
   }
   PCUDA(cudaEventRecord(ctx->ev1, st));
-  PCUDA(cudaMemcpyAsync(fb, b.fb, (size_t)npix * 3 * 4, cudaMemcpyDeviceToHost, st));
+  PCUDA(cudaMemcpyAsync(jobs ? arena.data() : fb, b.fb, (size_t)npix * 3 * 4, cudaMemcpyDeviceToHost, st));
   if (p->fb64) PCUDA(cudaMemcpyAsync(p->fb64, b.fb64, (size_t)npix * 3 * 8, cudaMemcpyDeviceToHost, st));
   unsigned long long tot[2] = {0, 0};
   PCUDA(cudaMemcpyAsync(tot, b.totals, 16, cudaMemcpyDeviceToHost, st));
@@ -1207,6 +1315,9 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     cudaMemsetAsync(ctx->guide.err.p, 0, 4, st);
     return pfail(ctx, VMR_ERR_TIMEOUT, "a guide kernel's tensor-core wait ran out");
   }
+  if (jobs)
+    for (uint32_t k = 0; k < n_jobs; ++k)
+      std::memcpy(jobs[k].fb, arena.data() + (size_t)jtab[k].pix0 * 3, (size_t)jtab[k].npix * 12);
   if (stats) {
     stats->samples = (uint64_t)npix * p->iter_count;
     stats->rays = tot[0];
@@ -1219,6 +1330,39 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     stats->ms = ms;
   }
+  return VMR_OK;
+}
+
+int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_stats* stats) {
+  if (!fb) return VMR_ERR_INVALID;
+  return render_path_impl(ctx, p, fb, stats, nullptr, 0);
+}
+
+// Static and motion jobs run as two batched renders: the static ones through
+// the while-while scene kernel, the motion ones through the single-loop
+// kernel that handles motion meshes (one kernel per launch; every job is
+// independent, so the split changes no result).
+int vmr_render_path_jobs(vmr_ctx* ctx, const vmr_path_job* jobs, uint32_t n_jobs, const vmr_path_params* p,
+                         vmr_path_stats* stats) {
+  if (!ctx || !p || (n_jobs && !jobs)) return VMR_ERR_INVALID;
+  std::vector<vmr_path_job> groups[2];
+  for (uint32_t k = 0; k < n_jobs; ++k) {
+    if (jobs[k].geom >= ctx->meshes.size()) return vmr::pfail(ctx, VMR_ERR_INVALID, "job geom out of range");
+    groups[ctx->meshes[jobs[k].geom]->host.motion() ? 1 : 0].push_back(jobs[k]);
+  }
+  vmr_path_stats total{};
+  for (const auto& gr : groups) {
+    if (gr.empty()) continue;
+    vmr_path_stats st{};
+    const int rc = render_path_impl(ctx, p, nullptr, &st, gr.data(), (uint32_t)gr.size());
+    if (rc != VMR_OK) return rc;
+    total.samples += st.samples;
+    total.rays += st.rays;
+    total.shadow_rays += st.shadow_rays;
+    total.graph_replays += st.graph_replays;
+    total.ms += st.ms;
+  }
+  if (stats) *stats = total;
   return VMR_OK;
 }
 

@@ -623,7 +623,8 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
 
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays, HitSoA hits, uint64_t n,
-                                                     DScratch* scratch, const unsigned long long* n_dev) {
+                                                     DScratch* scratch, const unsigned long long* n_dev,
+                                                     const uint32_t* ray_path, const uint32_t* path_geom) {
   if (n_dev) {
     const uint64_t nd = *n_dev;
     n = nd < n ? nd : n;
@@ -646,7 +647,18 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
       TRay r;
       load_ray(rays, i, r);
       HitRec h{-1, -1, 0.f, 0.f, 0.f};
-      bool hit = trace_scene_ray<ANY, COUNT>(top, r, stk, h, cnt, status);
+      bool hit;
+      if (ray_path) {  // job mode: the ray's own mesh, one stack slot above the (absent) top level
+        const uint32_t g = __ldg(path_geom + __ldg(ray_path + i));
+        HitRec hm = h;
+        hit = trace_any_mesh<ANY, COUNT>(top.meshes[g], r, stk + 1, kStackCapacity - 1, hm, cnt, status);
+        if (hit) {
+          h = hm;
+          h.geom = (int32_t)g;
+        }
+      } else {
+        hit = trace_scene_ray<ANY, COUNT>(top, r, stk, h, cnt, status);
+      }
       store_hit(hits, i, r, hit, h);
       if (status != kStatusOk) {
         atomicMax(&scratch->status, status);
@@ -1203,7 +1215,8 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
 template <bool ANY, bool COOP = false>
 __global__ void __launch_bounds__(128, 8)
     k_trace_scene_ww(const DTop top, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch,
-                     const unsigned long long* n_dev, const uint32_t* order, int walk_tail) {
+                     const unsigned long long* n_dev, const uint32_t* order, int walk_tail,
+                     const uint32_t* ray_path, const uint32_t* path_geom) {
   if (n_dev) {
     const uint64_t nd = *n_dev;
     n = nd < n ? nd : n;
@@ -1251,6 +1264,28 @@ __global__ void __launch_bounds__(128, 8)
           geom = -1;
           leaf_left = 0;
           alive = true;
+          if (ray_path) {  // job mode: enter the ray's own mesh, as a top-level leaf would
+            const uint32_t g = __ldg(path_geom + __ldg(ray_path + i));
+            const DMesh& M = top.meshes[g];
+            if (M.kind == 1) {  // an analytic sphere: tested here
+              if (sphere_hit(M, r, h)) {
+                h.geom = (int)g;
+                hit = true;
+              }
+              node = -1;
+            } else if (M.n_tris == 0) {
+              node = -1;
+            } else {
+              base = 1;
+              geom = (int)g;
+              mnodes = M.nodes;
+              mtris = reinterpret_cast<const float4*>(M.tris);
+              lower = M.lower_static;
+              mcap = M.iter_cap;
+              miter = 0;
+              sp = base;
+            }
+          }
         }
       }
     }
@@ -1752,13 +1787,15 @@ int launch_scene_t(const DTop& top, const TraceLaunch& l) {
   if (!COUNT && top.all_static && (l.kernel & kKernelWhileWhile)) {
     auto k = (l.kernel & kKernelCoopLeaf) ? k_trace_scene_ww<ANY, true> : k_trace_scene_ww<ANY, false>;
     const int grid = persistent_grid(k, 128, l.grid);
-    k<<<grid, 128, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order, l.walk_tail);
+    k<<<grid, 128, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order, l.walk_tail,
+                                                l.ray_path, l.path_geom);
     return (int)cudaGetLastError();
   }
   auto k = k_trace_scene<ANY, COUNT>;
   const int block = 128;
   const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
-  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev);
+  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.ray_path,
+                                                l.path_geom);
   return (int)cudaGetLastError();
 }
 

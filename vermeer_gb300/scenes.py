@@ -651,3 +651,28 @@ def vnf_order(scene: dict) -> dict:
         out[key] = new
     out["meshes"] = meshes
     return out
+
+
+def batched_jobs(n_jobs: int = 64, seed: int = 4, width: int = 256, height: int = 256,
+                 lo: int = 1000, hi: int = 200_000) -> dict:
+    """The batched-jobs configuration: n_jobs triangle soups (the raw-traversal
+    soup's construction: centroids in the unit cube, 0.005 edges) with sizes
+    log-uniform in [lo, hi] (seed), every other one with two-key linear
+    motion (per-triangle velocity uniform in a 0.05 ball, shutter [0, 1]);
+    each job renders its soup alone through a pinhole looking into the cube,
+    Lambert albedo 0.7 under a constant white environment (the configuration
+    names no material or light).  Returns dict(meshes, shaders, env, cameras,
+    width, height): meshes[j] is job j's mesh, cameras[j] its camera."""
+    sizes = np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * uniform(seed, n_jobs, 0)).astype(int)
+    meshes = []
+    for j, nt in enumerate(sizes):
+        if j % 2 == 1:
+            v, ip = motion_soup(int(nt), 400 + j, velocity=0.05)
+            meshes.append(dict(verts=v, idxp=ip, keys=2, motion_mode=1, shaders=[0]))
+        else:
+            v, ip = triangle_soup(int(nt), 400 + j)
+            meshes.append(dict(verts=v, idxp=ip, shaders=[0]))
+    cam = lookat_camera((0.5, 0.5, -1.2), (0.5, 0.5, 0.5), (0.0, 1.0, 0.0), 40.0, width / height)
+    return dict(meshes=meshes, shaders=[dict(diffuse_colour=(0.7, 0.7, 0.7), diffuse_strength=1.0,
+                                             diffuse_roughness=0.0)],
+                env=(1.0, 1.0, 1.0), cameras=[cam] * n_jobs, width=width, height=height, sizes=sizes)
