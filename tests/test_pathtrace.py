@@ -280,10 +280,23 @@ def test_pt_motion_and_spheres_match_float_oracle(ctx, orc, kind):
 
 # -------------------------------------------------------- batched jobs ----
 @pytest.mark.gpu
-def test_path_jobs_equal_one_scene_renders(ctx):
+@pytest.mark.parametrize("tuning", [(45, 0, 0, 0, 8), (13, 0, 0, 0, 4), (0, 0, 0, 0, 0)])
+def test_path_jobs_equal_one_scene_renders(ctx, tuning):
     """vmr_render_path_jobs: each job's image equals vmr_render_path of its
     mesh alone as the scene (same seed, iterations, depths), bit for bit,
-    static and motion meshes, images of different sizes, in one call."""
+    static and motion meshes, images of different sizes, in one call.  Job
+    rays enter their mesh without a top level, so motion jobs run the
+    while-while scene kernel's motion instantiation (tunings 45, 13) or the
+    single-loop kernel (0), while the one-scene renders of motion meshes
+    traverse a motion top level in the single-loop kernel."""
+    ctx.set_tuning(*tuning)
+    try:
+        _path_jobs_equal_one_scene_renders(ctx)
+    finally:
+        ctx.set_tuning(45, 0, 0, 0, 8)
+
+
+def _path_jobs_equal_one_scene_renders(ctx):
     bj = scenes.batched_jobs(n_jobs=5, seed=9, width=40, height=32, lo=500, hi=6000)
     ids = []
     for m in bj["meshes"]:

@@ -99,8 +99,21 @@ def test_motion_parity(ctx, orc, n, seed, fixed):
                           what=f"motion fixed={fixed} shadow={shadow}")
 
 
-@pytest.mark.parametrize("motion_every", [0, 2])
-def test_two_level_scene_parity(ctx, orc, motion_every):
+@pytest.mark.parametrize("motion_every,tuning", [(0, (45, 0, 0, 0, 8)), (2, (45, 0, 0, 0, 8)), (2, (45, 0, 0, 0, 0)),
+                                                 (2, (13, 0, 0, 0, 4)), (2, (0, 0, 0, 0, 0)), (3, (41, 0, 0, 0, 8))])
+def test_two_level_scene_parity(ctx, orc, motion_every, tuning):
+    """Two-level scenes, static and with motion meshes (which give the top
+    level motion keys): the while-while scene kernel (its motion
+    instantiation lerps the top-level and mesh boxes, motion leaves scanned
+    per lane) and the single-loop kernel (tuning 0) equal the oracle."""
+    ctx.set_tuning(*tuning)
+    try:
+        _two_level_scene_parity(ctx, orc, motion_every)
+    finally:
+        ctx.set_tuning(45, 0, 0, 0, 8)
+
+
+def _two_level_scene_parity(ctx, orc, motion_every):
     rng = np.random.default_rng(5 + motion_every)
     ms = []
     for i in range(24):

@@ -736,7 +736,7 @@ __device__ __forceinline__ void fetch_node(const DMesh& m, int node, unsigned oc
 
 // Fetch a motion node: boxes of both keys lerped per float
 // ((1.0-time)*Boxes[key] + time*Boxes[key2], motionintersect.go:47-49).
-__device__ __forceinline__ void fetch_mnode(const DMesh& m, int node, unsigned oct, const float4* bx0,
+__device__ __forceinline__ void fetch_mnode(const MNode* mnodes, int node, unsigned oct, const float4* bx0,
                                             const float4* bx1, float tm, float omt, float4 (&b)[6], int4& ch,
                                             unsigned& rk) {
 #pragma unroll
@@ -748,7 +748,7 @@ __device__ __forceinline__ void fetch_mnode(const DMesh& m, int node, unsigned o
     b[q].z = __fadd_rn(__fmul_rn(omt, a.z), __fmul_rn(tm, c.z));
     b[q].w = __fadd_rn(__fmul_rn(omt, a.w), __fmul_rn(tm, c.w));
   }
-  const uint4* mn = reinterpret_cast<const uint4*>(m.mnodes + node);
+  const uint4* mn = reinterpret_cast<const uint4*>(mnodes + node);
   const uint4 c4 = __ldg(mn);
   ch = make_int4((int)c4.x, (int)c4.y, (int)c4.z, (int)c4.w);
   const uint4 meta = __ldg(mn + 1);
@@ -1109,7 +1109,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         float4 b[6];
         int4 ch;
         unsigned rk;
-        if (MOTION) fetch_mnode(m, node, r.oct, bx0, bx1, tm, omt, b, ch, rk);
+        if (MOTION) fetch_mnode(m.mnodes, node, r.oct, bx0, bx1, tm, omt, b, ch, rk);
         else fetch_node(m, node, r.oct, b, ch, rk);
         float tn[4];
         unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
@@ -1212,7 +1212,20 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
 // intersect.go:226) and ends when its part of the stack is empty, after
 // which the next geom of the leaf, or the top level, continues.  Node
 // visits, pops, culls and triangle tests per ray are the reference's.
-template <bool ANY, bool COOP = false>
+// The key pair and lerp weight of a motion mesh at the ray's time
+// (builtin/geom/polymesh/trace.go:79-84); false outside the key range (the
+// reference would index out of bounds: a miss, as the mesh kernels treat it).
+__device__ __forceinline__ bool motion_keys(uint32_t keys, float time, float& tm, float& omt, int& key, int& key2) {
+  const float k = __fmul_rn(time, (float)(keys - 1));
+  const float fk = floorf(k);
+  tm = __fsub_rn(k, fk);
+  omt = __fsub_rn(1.0f, tm);
+  key = (int)fk;
+  key2 = (int)ceilf(k);
+  return !(key < 0 || key2 >= (int)keys);
+}
+
+template <bool ANY, bool COOP = false, bool MOT = false>
 __global__ void __launch_bounds__(128, 8)
     k_trace_scene_ww(const DTop top, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch,
                      const unsigned long long* n_dev, const uint32_t* order, int walk_tail,
@@ -1239,6 +1252,9 @@ __global__ void __launch_bounds__(128, 8)
   const float4* mtris = nullptr;
   float lower = 0.f;
   uint32_t mcap = 0;
+  bool mmot = false;  // the current mesh has motion keys (its key data is re-read from top.meshes)
+  float tm_unused = 0.f, omt_unused = 1.f;
+  int key_unused = 0, key2_unused = 0;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !alive);
     if (need != 0u && more) {
@@ -1275,9 +1291,12 @@ __global__ void __launch_bounds__(128, 8)
               node = -1;
             } else if (M.n_tris == 0) {
               node = -1;
+            } else if (MOT && M.keys > 1 && !motion_keys(M.keys, r.time, tm_unused, omt_unused, key_unused, key2_unused)) {
+              node = -1;
             } else {
               base = 1;
               geom = (int)g;
+              mmot = MOT && M.keys > 1;
               mnodes = M.nodes;
               mtris = reinterpret_cast<const float4*>(M.tris);
               lower = M.lower_static;
@@ -1285,6 +1304,9 @@ __global__ void __launch_bounds__(128, 8)
               miter = 0;
               sp = base;
             }
+          } else if (MOT && top.keys > 1 && !motion_keys(top.keys, r.time, tm_unused, omt_unused, key_unused,
+                                                         key2_unused)) {
+            node = -1;  // outside the top level's key range: a miss
           }
         }
       }
@@ -1301,7 +1323,9 @@ __global__ void __launch_bounds__(128, 8)
         const unsigned wmask = __ballot_sync(alive_mask, walking);
         if (wmask == 0u) break;
         if (walk_tail > 0 && __popc(wmask) <= walk_tail) {
-          const unsigned leafy = __ballot_sync(alive_mask, !walking && node < -1 && geom >= 0);
+          // only a static leaf ends the walk early: a motion leaf is scanned
+          // by its own lane, so a walk cut short for it idles the warp
+          const unsigned leafy = __ballot_sync(alive_mask, !walking && node < -1 && geom >= 0 && !(MOT && mmot));
           if (leafy != 0u) break;
         }
         if (!walking) continue;
@@ -1316,16 +1340,33 @@ __global__ void __launch_bounds__(128, 8)
         if (r.tclosest < nodeT) {  // pop-time cull (intersect.go:106)
           need_pop = true;
         } else if (node >= 0) {
-          const GNode* nb = geom < 0 ? top.nodes : mnodes;
           float4 b[6];
           int4 ch;
           unsigned rk;
-          const float4* np = reinterpret_cast<const float4*>(nb + node);
+          if (MOT && geom >= 0 && mmot) {  // a motion mesh: boxes lerped at the ray's time
+            const DMesh& M = top.meshes[geom];
+            float tm, omt;
+            int key, key2;
+            motion_keys(M.keys, r.time, tm, omt, key, key2);
+            const float4* bx = reinterpret_cast<const float4*>(M.mboxes);
+            fetch_mnode(M.mnodes, node, r.oct, bx + (size_t)key * M.n_mnodes * 6, bx + (size_t)key2 * M.n_mnodes * 6, tm,
+                        omt, b, ch, rk);
+          } else if (MOT && geom < 0 && top.keys > 1) {  // a motion top level
+            float tm, omt;
+            int key, key2;
+            motion_keys(top.keys, r.time, tm, omt, key, key2);
+            const float4* bx = reinterpret_cast<const float4*>(top.mboxes);
+            fetch_mnode(top.mnodes, node, r.oct, bx + (size_t)key * top.n_mnodes * 6,
+                        bx + (size_t)key2 * top.n_mnodes * 6, tm, omt, b, ch, rk);
+          } else {
+            const GNode* nb = geom < 0 ? top.nodes : mnodes;
+            const float4* np = reinterpret_cast<const float4*>(nb + node);
 #pragma unroll
-          for (int k = 0; k < 6; ++k) b[k] = __ldg(np + k);
-          ch = __ldg(reinterpret_cast<const int4*>(np + 6));
-          const uint4 meta = __ldg(reinterpret_cast<const uint4*>(np + 7));
-          rk = (((r.oct & 4u) ? meta.z : meta.y) >> ((r.oct & 3u) * 8u)) & 0xffu;
+            for (int k = 0; k < 6; ++k) b[k] = __ldg(np + k);
+            ch = __ldg(reinterpret_cast<const int4*>(np + 6));
+            const uint4 meta = __ldg(reinterpret_cast<const uint4*>(np + 7));
+            rk = (((r.oct & 4u) ? meta.z : meta.y) >> ((r.oct & 3u) * 8u)) & 0xffu;
+          }
           float tn[4];
           unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
           if (ch.x == kEmptyChild || r.tclosest < tn[0]) mask &= ~1u;
@@ -1386,12 +1427,14 @@ __global__ void __launch_bounds__(128, 8)
               continue;
             }
             if (M.n_tris == 0) continue;
+            if (MOT && M.keys > 1 && !motion_keys(M.keys, r.time, tm_unused, omt_unused, key_unused, key2_unused)) continue;
             base = sp + 1;
             if (base >= kStackCapacity) {
               status = kStatusStackOverflow;
               break;
             }
             geom = (int)g;
+            mmot = MOT && M.keys > 1;
             mnodes = M.nodes;
             mtris = reinterpret_cast<const float4*>(M.tris);
             lower = M.lower_static;
@@ -1426,7 +1469,8 @@ __global__ void __launch_bounds__(128, 8)
     }
     // ---- leaf phase: a mesh leaf, scanned in the reference's order (COOP:
     // the warp's leaves as one list of triangle tests, all lanes)
-    const bool has_leaf = alive && !done && !walking && node < -1 && geom >= 0;
+    const bool any_leaf = alive && !done && !walking && node < -1 && geom >= 0;
+    const bool has_leaf = any_leaf && !(MOT && mmot);  // static leaves: the cooperative scan (COOP)
     int32_t cidx = -1;
     float cU = 0.f, cV = 0.f, cW = 0.f;
     if (COOP) {
@@ -1435,18 +1479,29 @@ __global__ void __launch_bounds__(128, 8)
       cidx = coop_leaf_dispatch(mtris, lower, r, has_leaf, first, count, cU, cV, cW);
     }
     if (alive) {
-      if (has_leaf) {
+      if (any_leaf) {
         uint32_t first, count;
         leaf_decode(node, first, count);
         float U = cU, V = cV, W = cW;
         int32_t idx = cidx;
-        if (!COOP) {
+        int32_t elem = idx;
+        if (MOT && mmot) {  // a motion leaf: vertices lerped at the ray's time, scanned by its lane
+          const DMesh& M = top.meshes[geom];
+          float tm, omt;
+          int key, key2;
+          motion_keys(M.keys, r.time, tm, omt, key, key2);
+          const float4* tr = reinterpret_cast<const float4*>(M.mtris);
+          idx = leaf_scan_dispatch<true>(M, r, first, count, tr + (size_t)key * M.n_tris * 3,
+                                         tr + (size_t)key2 * M.n_tris * 3, tm, omt, U, V, W);
+          elem = idx != -1 ? __ldg(M.elem + idx) : -1;
+        } else if (!COOP) {
           DMesh M;
           M.lower_static = lower;
           idx = leaf_scan_dispatch<false>(M, r, first, count, mtris, mtris, 0.f, 1.f, U, V, W);
+          elem = idx;
         }
         if (idx != -1) {
-          h.elem = idx;
+          h.elem = elem;
           h.geom = geom;
           h.u = U;
           h.v = V;
@@ -1483,8 +1538,10 @@ __global__ void __launch_bounds__(128, 8)
                 continue;
               }
               if (MM.n_tris == 0) continue;
+              if (MOT && MM.keys > 1 && !motion_keys(MM.keys, r.time, tm_unused, omt_unused, key_unused, key2_unused)) continue;
               base = sp + 1;
               geom = (int)g;
+              mmot = MOT && MM.keys > 1;
               mnodes = MM.nodes;
               mtris = reinterpret_cast<const float4*>(MM.tris);
               lower = MM.lower_static;
@@ -1676,7 +1733,7 @@ __global__ void __launch_bounds__(256) k_trace_mesh_sched(const DMesh m, RaySoA 
         float4 b[6];
         int4 ch;
         unsigned rk;
-        if (MOTION) fetch_mnode(m, node, r.oct, bx0, bx1, tm, omt, b, ch, rk);
+        if (MOTION) fetch_mnode(m.mnodes, node, r.oct, bx0, bx1, tm, omt, b, ch, rk);
         else fetch_node(m, node, r.oct, b, ch, rk);
         float tn[4];
         unsigned mask = r.exact ? box4<true>(r, b, tn) : box4<false>(r, b, tn);
@@ -1784,8 +1841,13 @@ int launch_mesh_m(const DMesh& mesh, const TraceLaunch& l) {
 
 template <bool ANY, bool COUNT>
 int launch_scene_t(const DTop& top, const TraceLaunch& l) {
-  if (!COUNT && top.all_static && (l.kernel & kKernelWhileWhile)) {
-    auto k = (l.kernel & kKernelCoopLeaf) ? k_trace_scene_ww<ANY, true> : k_trace_scene_ww<ANY, false>;
+  if (!COUNT && (l.kernel & kKernelWhileWhile)) {
+    // Motion meshes and motion top levels take the MOT instantiation (lerped
+    // node boxes, per-lane motion leaves); only-static scenes keep the leaner
+    // kernel.
+    const bool coop = (l.kernel & kKernelCoopLeaf) != 0;
+    auto k = top.all_static ? (coop ? k_trace_scene_ww<ANY, true, false> : k_trace_scene_ww<ANY, false, false>)
+                            : (coop ? k_trace_scene_ww<ANY, true, true> : k_trace_scene_ww<ANY, false, true>);
     const int grid = persistent_grid(k, 128, l.grid);
     k<<<grid, 128, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order, l.walk_tail,
                                                 l.ray_path, l.path_geom);
