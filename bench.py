@@ -447,6 +447,14 @@ def render_extras(ctx, args):
         "mrays_per_s": round((st["rays"] + st["shadow_rays"]) / (st["ms"] / 1e3) / 1e6, 2),
         "device_ms": round(st["ms"], 3), "rays": st["rays"], "shadow_rays": st["shadow_rays"],
         "graph_replays": st["graph_replays"]}
+    # bounce and shadow queues traced in ray-key order (VMR_PATH_SORT_QUEUES)
+    # against queue order, 16 spp each
+    qs = {}
+    for srt in (False, True):
+        ctx.render_path(W, H, 0, 2, 3, max_depth=8, sort_queues=srt)
+        _, s16 = ctx.render_path(W, H, 0, 16, 3, max_depth=8, sort_queues=srt)
+        qs["sorted" if srt else "queue_order"] = round(W * H * 16 / (s16["ms"] / 1e3), 1)
+    out["extended_sphere_grid"]["queue_sort_samples_per_s_16spp"] = qs
     # batched uneven jobs: one launch vs one launch per job
     import torch
     rng_sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)

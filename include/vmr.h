@@ -502,9 +502,13 @@ enum {
                                BSDF at every non-mirror vertex; the density of
                                the mixture enters the NEE and emission weights,
                                so the estimator stays unbiased */
-    VMR_PATH_TRAIN = 4      /* record (vertex, sampled direction, density,
+    VMR_PATH_TRAIN = 4,     /* record (vertex, sampled direction, density,
                                incident radiance) and train the guide on them
                                after each batch (online) */
+    VMR_PATH_SORT_QUEUES = 8 /* batches of >= 65,536 paths: trace each bounce
+                               and shadow queue in ray-key order (direction
+                               class + Morton cell of the origin, the
+                               tuning's sort-key width); images unchanged */
 };
 
 typedef struct {

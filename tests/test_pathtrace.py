@@ -145,6 +145,36 @@ def test_pt_graph_batches_and_calls_are_exact(ctx, room):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scene", ["room", "motion", "guided"])
+def test_pt_queue_reordering_is_exact(ctx, room, scene):
+    """With VMR_PATH_SORT_QUEUES, batches of at least 65,536 paths trace
+    their bounce and shadow queues in key order and write each hit back at
+    its queue position: images and ray counts equal the unsorted run's bit
+    for bit, under several tunings (sort-key widths, the single-loop scene
+    kernel), and a tuning change between two equal calls is not hidden by
+    the cached bounce-loop graph."""
+    sc = room if scene != "motion" else scenes.small_room_motion(2048, seed=12, motion_mode=1)
+    ctx.load_scene(sc)
+    kw = dict(max_depth=5)
+    if scene == "guided":
+        ctx.guide_init(3)
+        kw.update(guided=True, guide_fraction=0.3)
+    out = {}
+    try:
+        for tn, srt in (((45, 0, 0, 0, 8), False), ((45, 0, 0, 0, 8), True), ((37, 0, 0, 0, 8), True),
+                        ((45, 0, 0, 0, 8, 5), True), ((12, 0, 0, 0, 0), True), ((4, 0, 0, 0, 0), True)):
+            ctx.set_tuning(*tn)
+            out[tn, srt] = ctx.render_path(160, 128, 0, 4, 8, sort_queues=srt, **kw)
+    finally:
+        ctx.set_tuning(45, 0, 0, 0, 8)
+    (img0, st0), *rest = out.values()
+    assert st0["samples"] >= 65536
+    for tn, (img, st) in zip(list(out)[1:], rest):
+        assert img.tobytes() == img0.tobytes(), tn
+        assert (st["rays"], st["shadow_rays"]) == (st0["rays"], st0["shadow_rays"]), tn
+
+
+@pytest.mark.gpu
 def test_pt_fp64_accumulation(ctx, room):
     ctx.load_scene(room)
     fb64 = np.zeros((16, 16, 3), np.float64)

@@ -182,11 +182,13 @@ def test_every_tuning_is_bit_exact(ctx, orc, tuning):
 
 @pytest.mark.parametrize("tuning", [(13, 0, 0, 0, 4), (45, 0, 0, 0, 8), (45, 0, 0, 0, 0), (1, 0, 0, 0, 0),
                                     (5, 0, 0, 0, 8), (0, 0, 0, 4, 4),
-                                    (13, 0, 0, 0, 2, 5)])
+                                    (13, 0, 0, 0, 2, 5), (8, 0, 0, 4, 4), (12, 0, 0, 0, 0, 3)])
 def test_two_level_scene_every_tuning(ctx, orc, tuning):
     """The static two-level scene traced by the while-while scene kernel (with
     and without ray reordering, several tail cutoffs) and by the single-loop
-    kernel: all bit-exact with the oracle, closest and any hit."""
+    kernel (unsorted, and sorted: tunings 8 and 12 write each hit back
+    through the order array): all bit-exact with the oracle, closest and any
+    hit."""
     rng = np.random.default_rng(77)
     ms = []
     for i in range(30):

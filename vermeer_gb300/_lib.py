@@ -139,6 +139,7 @@ class PathJob(ctypes.Structure):
 PATH_NO_GRAPH = 1
 PATH_GUIDED = 2
 PATH_TRAIN = 4
+PATH_SORT_QUEUES = 8
 
 GUIDE_WEIGHTS = 19968
 

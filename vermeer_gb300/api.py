@@ -342,18 +342,19 @@ class Context:
     def render_path(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, max_depth: int = 4,
                     rr_depth: int = 3, fb=None, fb64=None, max_batch_samples: int = 0, graph: bool = True,
                     guided: bool = False, train: bool = False, guide_fraction: float = 0.0, train_steps: int = 0,
-                    train_batch: int = 0, train_lr: float = 0.0):
+                    train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False):
         """The extended path tracer: iterations [iter_begin, iter_begin +
         iter_count) folded into fb (float32 [height, width, 3]) and, when
         given, fb64 (float64).  guided: sample the guide network too; train:
-        train it online.  Returns (fb, stats)."""
+        train it online; sort_queues: trace each queue in ray-key order.
+        Returns (fb, stats)."""
         if fb is None:
             fb = np.zeros((height, width, 3), np.float32)
         fb = np.ascontiguousarray(fb, np.float32)
         if fb64 is not None:
             assert fb64.dtype == np.float64 and fb64.flags.c_contiguous and fb64.shape == (height, width, 3)
         flags = (0 if graph else _lib.PATH_NO_GRAPH) | (_lib.PATH_GUIDED if guided else 0) | \
-                (_lib.PATH_TRAIN if train else 0)
+                (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0)
         p = _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
                             flags, None if fb64 is None else _p(fb64), guide_fraction, train_steps, train_batch,
                             train_lr)

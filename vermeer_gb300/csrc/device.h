@@ -156,8 +156,11 @@ struct TraceLaunch {
   const uint32_t* path_geom;
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);
+// n_dev (optional): the ray count on the device, at most n (a wavefront queue
+// length); the grid is sized for n.
 int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int bits, uint32_t* keys, uint32_t* hist,
-                    uint32_t* order, const RaySoA& sorted_out, void* stream);
+                    uint32_t* order, const RaySoA& sorted_out, void* stream,
+                    const unsigned long long* n_dev = nullptr);
 int launch_trace_scene(const DTop& top, const TraceLaunch& l);
 int device_sm_count();
 

@@ -805,9 +805,34 @@ int pfail(vmr_ctx* ctx, int code, const std::string& msg) {
 
 // Launches one batch's stages on the context's stream (also used while
 // capturing the graph).  Every count is read on the device.
+// Reordering of the wavefront's queues before their traces
+// (VMR_PATH_SORT_QUEUES, batches of at least kSortMinRays paths): the rays of
+// a queue are gathered
+// into a key-ordered copy (direction class + Morton cell of the origin,
+// raysort.cu) and the traversal writes each hit back at its queue position,
+// so nothing downstream sees the order.
+struct PtSort {
+  bool on = false;
+  int bits = 4;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};
+  uint32_t* keys = nullptr;
+  uint32_t* order = nullptr;
+  uint32_t* hist = nullptr;
+  float* rays = nullptr;  // 8 * cap floats
+};
+
 int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr, int grid, bool guided, bool train,
-                 const guide::GuideRows& grows) {
+                 const guide::GuideRows& grows, const PtSort& srt) {
   cudaStream_t st = ctx->stream;
+  auto sort_queue = [&](TraceLaunch& l) -> int {
+    const size_t c = b.cap;
+    const float* f = srt.rays;
+    const RaySoA sorted{f, f + c, f + 2 * c, f + 3 * c, f + 4 * c, f + 5 * c, f + 6 * c, f + 7 * c};
+    const int e = launch_ray_sort(l.rays, c, srt.bounds, srt.bits, srt.keys, srt.hist, srt.order, sorted, st, l.n_dev);
+    l.rays = sorted;
+    l.order = srt.order;
+    return e;
+  };
   const size_t nq = kPtMaxDepth + 2, ns = kPtMaxDepth + 1;
   PCUDA(cudaMemsetAsync(b.qlen, 0, nq * sizeof(unsigned long long), st));
   PCUDA(cudaMemsetAsync(b.slen, 0, ns * sizeof(unsigned long long), st));
@@ -832,6 +857,8 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
       l.ray_path = b.qpath[d & 1];
       l.path_geom = b.pgeom;
     }
+    // camera rays are traced in pixel order (already coherent)
+    if (srt.on && d > 0 && sort_queue(l) != 0) return pfail(ctx, VMR_ERR_CUDA, "ray sort launch failed");
     if (launch_trace_scene(top, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
     if (guided) {
       k_pt_prep<<<grid, kPtBlock, 0, st>>>(b, d);
@@ -863,6 +890,7 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
         s.ray_path = b.spath;
         s.path_geom = b.pgeom;
       }
+      if (srt.on && sort_queue(s) != 0) return pfail(ctx, VMR_ERR_CUDA, "ray sort launch failed");
       if (launch_trace_scene(top, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
       if (train) k_pt_resolve<true><<<grid, kPtBlock, 0, st>>>(b, d);
       else k_pt_resolve<false><<<grid, kPtBlock, 0, st>>>(b, d);
@@ -1054,6 +1082,10 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
                o_gout = carve(guided ? cap * 40 * 4 : 0), o_rec = carve(rcap * kRecCols * 4),
                o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32), o_snee = carve(train ? cap * 7 * 4 : 0),
                o_jobs = carve(jobs ? n_jobs * sizeof(PtJob) : 0), o_pgeom = carve(jobs ? cap * 4 : 0);
+  // queue reordering (not for jobs: a key-ordered queue would mix the jobs'
+  // meshes inside a warp)
+  const bool sort_on = !jobs && (p->flags & VMR_PATH_SORT_QUEUES) && cap >= kSortMinRays;
+  const size_t o_sort = carve(sort_on ? cap * 4 * (2 + 8) + sizeof(uint32_t) * kSortBucketsMax : 0);
   PCUDA(R.ptbuf.ensure(bytes));
   char* base = R.ptbuf.as<char>();
   uint64_t fwd[52], inv[52];
@@ -1152,6 +1184,19 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   b.jobs = jobs ? reinterpret_cast<const PtJob*>(base + o_jobs) : nullptr;
   b.n_jobs = jobs ? n_jobs : 0u;
   b.pgeom = jobs ? reinterpret_cast<uint32_t*>(base + o_pgeom) : nullptr;
+  PtSort srt;
+  if (sort_on) {
+    srt.on = true;
+    srt.bits = ctx->tuning.sort_bits ? ctx->tuning.sort_bits : 4;
+    for (int k = 0; k < 3; ++k) {
+      srt.bounds[k] = glo[k];
+      srt.bounds[3 + k] = ghi[k];
+    }
+    srt.keys = reinterpret_cast<uint32_t*>(base + o_sort);
+    srt.order = srt.keys + cap;
+    srt.rays = reinterpret_cast<float*>(srt.order + cap);
+    srt.hist = reinterpret_cast<uint32_t*>(srt.rays + cap * 8);
+  }
   // the traversal's view: the scene's top level, or for jobs only the mesh
   // table (each ray enters its own mesh)
   DTop top = ctx->top.dtop;
@@ -1204,7 +1249,9 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   std::vector<uint64_t> key = {(uint64_t)(uintptr_t)base, bytes, cap, npix, p->width, p->height, nl, p->max_depth,
                                p->rr_depth, p->seed, (uint64_t)(p->fb64 != nullptr), (uint64_t)(uintptr_t)st,
                                (uint64_t)(uintptr_t)ctx->top.nodes.p, (uint64_t)grid, (uint64_t)guided,
-                               (uint64_t)train, (uint64_t)(uintptr_t)ctx->guide.wf.p, rcap};
+                               (uint64_t)train, (uint64_t)(uintptr_t)ctx->guide.wf.p, rcap,
+                               (uint64_t)ctx->tuning.kernel, (uint64_t)ctx->tuning.walk_tail,
+                               (uint64_t)ctx->tuning.sort_bits, (uint64_t)sort_on};
   {
     uint64_t h = 1469598103934665603ull;
     auto fold = [&](const void* d, size_t nb) {
@@ -1231,7 +1278,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     }
     cudaGraph_t g = nullptr;
     PCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-    const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows);
+    const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows, srt);
     const cudaError_t ec = cudaStreamEndCapture(st, &g);
     if (rc != VMR_OK) {
       if (g) cudaGraphDestroy(g);
@@ -1250,7 +1297,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
       PCUDA(cudaGraphLaunch(R.graph.exec, st));
       ++replays;
     } else {
-      const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows);
+      const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows, srt);
       if (rc != VMR_OK) return rc;
     }
     if (train) {  // online training on this batch's records (device counts)

@@ -63,8 +63,9 @@ __device__ __forceinline__ uint32_t warp_bucket_add(uint32_t* counters, uint32_t
 
 // Grid-stride loops below run whole warps (blockDim.x is a multiple of 32)
 // for the same number of rounds, so every lane reaches the warp collectives.
-__global__ void k_ray_keys(RaySoA rays, uint64_t n, float3 lo, float3 inv, uint32_t bits, uint32_t* keys,
-                           uint32_t* hist) {
+__global__ void k_ray_keys(RaySoA rays, uint64_t n, const unsigned long long* n_dev, float3 lo, float3 inv,
+                           uint32_t bits, uint32_t* keys, uint32_t* hist) {
+  if (n_dev && *n_dev < n) n = *n_dev;
   const float top = (float)((1u << bits) - 1u);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t rounds = (n + stride - 1) / stride;
@@ -112,8 +113,9 @@ __global__ void __launch_bounds__(1024) k_bucket_scan(uint32_t* hist, uint32_t n
   }
 }
 
-__global__ void k_ray_scatter(RaySoA rays, uint64_t n, const uint32_t* keys, uint32_t* offsets, uint32_t* order,
-                              RaySoA sorted_out) {
+__global__ void k_ray_scatter(RaySoA rays, uint64_t n, const unsigned long long* n_dev, const uint32_t* keys,
+                              uint32_t* offsets, uint32_t* order, RaySoA sorted_out) {
+  if (n_dev && *n_dev < n) n = *n_dev;
   float* px = const_cast<float*>(sorted_out.px);
   float* py = const_cast<float*>(sorted_out.py);
   float* pz = const_cast<float*>(sorted_out.pz);
@@ -143,7 +145,7 @@ __global__ void k_ray_scatter(RaySoA rays, uint64_t n, const uint32_t* keys, uin
 }  // namespace
 
 int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int bits, uint32_t* keys, uint32_t* hist,
-                    uint32_t* order, const RaySoA& sorted_out, void* stream) {
+                    uint32_t* order, const RaySoA& sorted_out, void* stream, const unsigned long long* n_dev) {
   cudaStream_t s = (cudaStream_t)stream;
   if (bits < 3 || bits > kSortMaxBits) bits = 4;
   const uint32_t nb = sort_buckets(bits);
@@ -161,9 +163,9 @@ int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int b
   const int cap = device_sm_count() * 16;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
-  k_ray_keys<<<grid, block, 0, s>>>(rays, n, lo, inv, (uint32_t)bits, keys, hist);
+  k_ray_keys<<<grid, block, 0, s>>>(rays, n, n_dev, lo, inv, (uint32_t)bits, keys, hist);
   k_bucket_scan<<<1, 1024, 0, s>>>(hist, nb);
-  k_ray_scatter<<<grid, block, 0, s>>>(rays, n, keys, hist, order, sorted_out);
+  k_ray_scatter<<<grid, block, 0, s>>>(rays, n, n_dev, keys, hist, order, sorted_out);
   return (int)cudaGetLastError();
 }
 

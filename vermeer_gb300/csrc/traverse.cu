@@ -624,7 +624,8 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays, HitSoA hits, uint64_t n,
                                                      DScratch* scratch, const unsigned long long* n_dev,
-                                                     const uint32_t* ray_path, const uint32_t* path_geom) {
+                                                     const uint32_t* order, const uint32_t* ray_path,
+                                                     const uint32_t* path_geom) {
   if (n_dev) {
     const uint64_t nd = *n_dev;
     n = nd < n ? nd : n;
@@ -644,12 +645,14 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
     if (base >= n) break;
     const uint64_t i = base + lane;
     if (i < n) {
+      // reordered rays: position i of the sorted copy is input ray order[i]
+      const uint64_t rid = order ? (uint64_t)__ldg(order + i) : i;
       TRay r;
       load_ray(rays, i, r);
       HitRec h{-1, -1, 0.f, 0.f, 0.f};
       bool hit;
       if (ray_path) {  // job mode: the ray's own mesh, one stack slot above the (absent) top level
-        const uint32_t g = __ldg(path_geom + __ldg(ray_path + i));
+        const uint32_t g = __ldg(path_geom + __ldg(ray_path + rid));
         HitRec hm = h;
         hit = trace_any_mesh<ANY, COUNT>(top.meshes[g], r, stk + 1, kStackCapacity - 1, hm, cnt, status);
         if (hit) {
@@ -659,7 +662,7 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
       } else {
         hit = trace_scene_ray<ANY, COUNT>(top, r, stk, h, cnt, status);
       }
-      store_hit(hits, i, r, hit, h);
+      store_hit(hits, rid, r, hit, h);
       if (status != kStatusOk) {
         atomicMax(&scratch->status, status);
         status = kStatusOk;
@@ -1281,7 +1284,7 @@ __global__ void __launch_bounds__(128, 8)
           leaf_left = 0;
           alive = true;
           if (ray_path) {  // job mode: enter the ray's own mesh, as a top-level leaf would
-            const uint32_t g = __ldg(path_geom + __ldg(ray_path + i));
+            const uint32_t g = __ldg(path_geom + __ldg(ray_path + rid));
             const DMesh& M = top.meshes[g];
             if (M.kind == 1) {  // an analytic sphere: tested here
               if (sphere_hit(M, r, h)) {
@@ -1856,8 +1859,8 @@ int launch_scene_t(const DTop& top, const TraceLaunch& l) {
   auto k = k_trace_scene<ANY, COUNT>;
   const int block = 128;
   const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
-  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.ray_path,
-                                                l.path_geom);
+  k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order,
+                                                l.ray_path, l.path_geom);
   return (int)cudaGetLastError();
 }
 
