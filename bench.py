@@ -455,6 +455,15 @@ def render_extras(ctx, args):
         _, s16 = ctx.render_path(W, H, 0, 16, 3, max_depth=8, sort_queues=srt)
         qs["sorted" if srt else "queue_order"] = round(W * H * 16 / (s16["ms"] / 1e3), 1)
     out["extended_sphere_grid"]["queue_sort_samples_per_s_16spp"] = qs
+    # queue capacity chosen by the path autotuner (8 spp per candidate)
+    t0 = time.perf_counter()
+    best, table = ctx.autotune_path(W, H, 8, seed=3, max_depth=8)
+    tune_s = time.perf_counter() - t0
+    _, s16 = ctx.render_path(W, H, 0, 16, 3, max_depth=8)
+    ctx.set_path_batch(0)
+    out["extended_sphere_grid"]["queue_capacity_autotune"] = {
+        "candidates_ms_8spp": {str(k): round(v, 2) for k, v in table.items()}, "best_paths": best,
+        "autotune_s": round(tune_s, 2), "tuned_samples_per_s_16spp": round(W * H * 16 / (s16["ms"] / 1e3), 1)}
     # batched uneven jobs: one launch vs one launch per job
     import torch
     rng_sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)

@@ -483,7 +483,8 @@ typedef struct {
     uint64_t seed;
     uint32_t max_depth;               /* scattering events per path */
     uint32_t rr_depth;                /* Russian roulette from this event on */
-    uint32_t max_batch_samples;       /* paths per wavefront batch (0: 2M) */
+    uint32_t max_batch_samples;       /* paths per wavefront batch (0: the
+                                         context's, vmr_set_path_batch) */
     uint32_t flags;                   /* VMR_PATH_* */
     double* fb64;                     /* optional host width*height*3: the same
                                          running mean folded in float64 */
@@ -527,6 +528,20 @@ typedef struct {
  * i = the 0-based iteration: the exact mean of the samples (the reference's
  * fold starts at i+1 and so counts the initial buffer as a sample, F6). */
 int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* params, float* fb, vmr_path_stats* stats);
+
+/* Queue capacity (paths per wavefront batch, whole iterations) of the
+ * context's one-scene renders when params.max_batch_samples is 0.
+ * vmr_set_path_batch: set it (0: the default, 8M paths; else >= 1024).
+ * vmr_autotune_path: render params' iterations (GUIDED sampled, TRAIN and
+ * fb64 ignored; no framebuffer of the caller is touched) at candidate
+ * capacities of 256K..32M paths, each after an untimed call, and keep the
+ * fastest; candidates/ms (optional, room for 8) receive the capacities
+ * timed and their device times.  A tuned capacity changes no image: any
+ * batch split gives the same bits. */
+int vmr_set_path_batch(vmr_ctx* ctx, uint32_t paths);
+int vmr_get_path_batch(vmr_ctx* ctx, uint32_t* paths);
+int vmr_autotune_path(vmr_ctx* ctx, const vmr_path_params* params, uint32_t* candidates, float* ms,
+                      uint32_t* n_candidates, uint32_t* best);
 
 /* Batched path-traced jobs (no reference counterpart: the reference renders
  * one scene per process).  Every job is its own one-mesh scene: its mesh

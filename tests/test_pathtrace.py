@@ -175,6 +175,33 @@ def test_pt_queue_reordering_is_exact(ctx, room, scene):
 
 
 @pytest.mark.gpu
+def test_pt_autotune_path_queue_capacity(ctx, room):
+    """vmr_autotune_path times whole-iteration queue capacities, keeps the
+    fastest as the context's default, and the image rendered at it equals
+    the default capacity's bit for bit; vmr_set_path_batch sets and resets
+    it and rejects capacities below 1,024 paths."""
+    ctx.load_scene(room)
+    W, H = 256, 192
+    ref, _ = ctx.render_path(W, H, 0, 24, 6, max_depth=5)
+    try:
+        best, table = ctx.autotune_path(W, H, 24, seed=6, max_depth=5)
+        assert best in table and len(table) >= 3
+        assert all(c % (W * H) == 0 for c in table)
+        assert ctx.get_path_batch() == best
+        got, st = ctx.render_path(W, H, 0, 24, 6, max_depth=5)
+        assert got.tobytes() == ref.tobytes()
+        assert st["graph_replays"] == -(-24 // (best // (W * H)))
+        ctx.set_path_batch(W * H * 5)
+        got, st = ctx.render_path(W, H, 0, 24, 6, max_depth=5)
+        assert got.tobytes() == ref.tobytes() and st["graph_replays"] == 5
+        with pytest.raises(RuntimeError):
+            ctx.set_path_batch(500)
+    finally:
+        ctx.set_path_batch(0)
+    assert ctx.get_path_batch() == 0
+
+
+@pytest.mark.gpu
 def test_pt_fp64_accumulation(ctx, room):
     ctx.load_scene(room)
     fb64 = np.zeros((16, 16, 3), np.float64)

@@ -193,6 +193,10 @@ SIGNATURES = {
     "vmr_set_env_light": (ctypes.c_int, [P, P]),
     "vmr_render_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, ctypes.POINTER(PathStats)]),
     "vmr_render_path_jobs": (ctypes.c_int, [P, P, U32, ctypes.POINTER(PathParams), ctypes.POINTER(PathStats)]),
+    "vmr_set_path_batch": (ctypes.c_int, [P, U32]),
+    "vmr_get_path_batch": (ctypes.c_int, [P, ctypes.POINTER(U32)]),
+    "vmr_autotune_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, P, ctypes.POINTER(U32),
+                                         ctypes.POINTER(U32)]),
     "vmr_guide_init": (ctypes.c_int, [P, ctypes.c_uint64]),
     "vmr_guide_set_weights": (ctypes.c_int, [P, P]),
     "vmr_guide_get_weights": (ctypes.c_int, [P, P]),

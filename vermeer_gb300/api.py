@@ -418,6 +418,31 @@ class Context:
         c = self._camera(cam)
         self._check(self.L.vmr_set_camera(self.h, ctypes.byref(c)))
 
+    def set_path_batch(self, paths: int):
+        """Paths per wavefront batch of later render_path calls that give no
+        max_batch_samples (0: the default)."""
+        self._check(self.L.vmr_set_path_batch(self.h, int(paths)))
+
+    def get_path_batch(self) -> int:
+        v = ctypes.c_uint32()
+        self._check(self.L.vmr_get_path_batch(self.h, ctypes.byref(v)))
+        return v.value
+
+    def autotune_path(self, width: int, height: int, iter_count: int, seed: int = 0, max_depth: int = 4,
+                      rr_depth: int = 3, guided: bool = False, guide_fraction: float = 0.0, sort_queues: bool = False):
+        """vmr_autotune_path: time the render at each candidate queue
+        capacity and keep the fastest for this context.  Returns (best,
+        {capacity: device ms})."""
+        flags = (_lib.PATH_GUIDED if guided else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0)
+        p = _lib.PathParams(width, height, 0, iter_count, seed, max_depth, rr_depth, 0, flags, None,
+                            guide_fraction, 0, 0, 0.0)
+        cand = np.zeros(8, np.uint32)  # room for the 8 candidates
+        ms = np.zeros(8, np.float32)
+        n, best = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.L.vmr_autotune_path(self.h, ctypes.byref(p), _p(cand), _p(ms), ctypes.byref(n),
+                                             ctypes.byref(best)))
+        return best.value, {int(c): float(m) for c, m in zip(cand[:n.value], ms[:n.value])}
+
     def render_path_jobs(self, jobs, iter_begin: int, iter_count: int, seed: int, max_depth: int = 4,
                          rr_depth: int = 3, max_batch_samples: int = 0, graph: bool = True):
         """Batched path-traced jobs (vmr_render_path_jobs): jobs are dicts

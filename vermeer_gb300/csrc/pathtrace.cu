@@ -1036,10 +1036,13 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
   const uint32_t npix = jobs ? (uint32_t)npix_jobs : p->width * p->height;
-  // batched jobs default to larger batches: with many images per iteration a
-  // 2M-path batch holds about one iteration, and each bounce's launch ends
-  // in a longer tail relative to its work
-  const uint32_t per_batch = p->max_batch_samples ? p->max_batch_samples : (jobs ? (8u << 20) : (2u << 20));
+  // Default 8M paths per batch: every bounce's launches end in a tail of
+  // long paths, which a larger batch amortises (sphere grid 1920x1080, 8 spp:
+  // 80.7 ms at 2M, 66.5 ms at 8M); a one-scene render uses the context's
+  // tuned capacity when it has one (vmr_autotune_path, vmr_set_path_batch).
+  const uint32_t per_batch = p->max_batch_samples     ? p->max_batch_samples
+                             : (!jobs && ctx->render.path_batch) ? ctx->render.path_batch
+                                                                 : (8u << 20);
   uint32_t ipb = std::max<uint32_t>(1, per_batch / npix);
   if (p->iter_count > 0 && ipb > p->iter_count) ipb = p->iter_count;
   const uint64_t cap = (uint64_t)ipb * npix;
@@ -1385,9 +1388,9 @@ int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* p, float* fb, vmr_path_
   return render_path_impl(ctx, p, fb, stats, nullptr, 0);
 }
 
-// Static and motion jobs run as two batched renders: the static ones through
-// the while-while scene kernel, the motion ones through the single-loop
-// kernel that handles motion meshes (one kernel per launch; every job is
+// Static and motion jobs run as two batched renders, so that the static ones
+// keep the while-while scene kernel's leaner static instantiation and only
+// the motion ones pay for its motion instantiation (every job is
 // independent, so the split changes no result).
 int vmr_render_path_jobs(vmr_ctx* ctx, const vmr_path_job* jobs, uint32_t n_jobs, const vmr_path_params* p,
                          vmr_path_stats* stats) {
@@ -1410,6 +1413,64 @@ int vmr_render_path_jobs(vmr_ctx* ctx, const vmr_path_job* jobs, uint32_t n_jobs
     total.ms += st.ms;
   }
   if (stats) *stats = total;
+  return VMR_OK;
+}
+
+int vmr_set_path_batch(vmr_ctx* ctx, uint32_t paths) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (paths != 0 && paths < 1024) return vmr::pfail(ctx, VMR_ERR_INVALID, "path batch must be 0 or >= 1024");
+  ctx->render.path_batch = paths;
+  return VMR_OK;
+}
+
+int vmr_get_path_batch(vmr_ctx* ctx, uint32_t* paths) {
+  if (!ctx || !paths) return VMR_ERR_INVALID;
+  *paths = ctx->render.path_batch;
+  return VMR_OK;
+}
+
+// Queue capacity per scene: the render of p (its size, depths, flags; the
+// guide is sampled but never trained here) timed at each candidate batch
+// size, after one untimed call that captures that size's bounce-loop graph;
+// the fastest becomes the context's default.  Candidates that round to the
+// same whole number of iterations per batch are timed once.
+int vmr_autotune_path(vmr_ctx* ctx, const vmr_path_params* p, uint32_t* candidates, float* ms,
+                      uint32_t* n_candidates, uint32_t* best) {
+  if (!ctx || !p || !p->width || !p->height || !p->iter_count) return VMR_ERR_INVALID;
+  static const uint32_t kCand[] = {256u << 10, 512u << 10, 1u << 20, 2u << 20, 4u << 20, 8u << 20, 16u << 20,
+                                   32u << 20};
+  const uint64_t npix = (uint64_t)p->width * p->height;
+  std::vector<float> fb((size_t)npix * 3);
+  vmr_path_params q = *p;
+  q.flags &= ~(uint32_t)VMR_PATH_TRAIN;
+  q.fb64 = nullptr;
+  uint32_t n = 0, win = 0, last_ipb = 0;
+  float win_ms = INFINITY;
+  for (uint32_t c : kCand) {
+    uint64_t ipb = std::max<uint64_t>(1, c / npix);
+    if (ipb > p->iter_count) ipb = p->iter_count;
+    if (ipb == last_ipb) continue;
+    last_ipb = (uint32_t)ipb;
+    if ((uint64_t)ipb * npix > 0xffffffffull) break;
+    q.max_batch_samples = (uint32_t)(ipb * npix);
+    vmr_path_stats st{};
+    std::fill(fb.begin(), fb.end(), 0.0f);
+    int rc = render_path_impl(ctx, &q, fb.data(), &st, nullptr, 0);
+    if (rc != VMR_OK) return rc;
+    std::fill(fb.begin(), fb.end(), 0.0f);
+    rc = render_path_impl(ctx, &q, fb.data(), &st, nullptr, 0);
+    if (rc != VMR_OK) return rc;
+    if (candidates) candidates[n] = q.max_batch_samples;
+    if (ms) ms[n] = st.ms;
+    ++n;
+    if (st.ms < win_ms) {
+      win_ms = st.ms;
+      win = q.max_batch_samples;
+    }
+  }
+  ctx->render.path_batch = win;
+  if (n_candidates) *n_candidates = n;
+  if (best) *best = win;
   return VMR_OK;
 }
 
