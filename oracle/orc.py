@@ -139,6 +139,7 @@ def _register_render(L):
     L.orc_pt_run.argtypes = [P, P, ctypes.c_uint32, P, P, P, ctypes.c_int, ctypes.c_int]
     L.orc_pt_rnd.restype = ctypes.c_float
     L.orc_pt_rnd.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
+    L.orc_sincos_turns.argtypes = [P, ctypes.c_size_t, P, P]
     L.orc_guide_n_weights.restype = ctypes.c_int
     L.orc_guide_features.argtypes = [P, P, P, P, P, ctypes.c_int, P]
     L.orc_guide_forward.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P]
@@ -171,6 +172,16 @@ def _pixel_filter(d):
     dflt = FILTER_DEFAULTS.get(kind, dict(res=0, width=0.0, peak=0.0))
     return OrcPixelFilter(kind, int(d.get("res", dflt["res"])), float(d.get("width", dflt["width"])),
                           float(d.get("peak", dflt["peak"])))
+
+
+def sincos_turns(u):
+    """sin and cos of 2*pi*u (float32 u in [0, 1)) as the extended path
+    tracer's sampling computes them: (sin, cos) float32 arrays."""
+    u = np.ascontiguousarray(u, np.float32)
+    s = np.empty_like(u)
+    c = np.empty_like(u)
+    lib().orc_sincos_turns(_ptr(u), u.size, _ptr(s), _ptr(c))
+    return s, c
 
 
 def filter_warp(f, r0, r1):

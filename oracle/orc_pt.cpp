@@ -25,12 +25,14 @@
 //
 // Precision: the template parameter T is the arithmetic of everything but
 // the traversal.  T = float restates the CUDA kernels' float32 operation
-// order (no contraction; transcendentals in float64 rounded to float32), so
-// the two agree sample for sample.  T = double is the float64 oracle the
+// order (no contraction; the sampling angles through sincos_turns, the same
+// float32 quarter-turn reduction and Taylor series as the kernels), so the
+// two agree sample for sample.  T = double is the float64 oracle the
 // converged images are checked against (same random numbers, float64
 // shading, float64 accumulation).  Traversal is the float32 watertight test
 // of orc_core.cpp in both: ray origins and directions are rounded to float32
 // before tracing.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -72,12 +74,36 @@ template <class T> inline Vec<T> expand(Vec<T> U, Vec<T> V, Vec<T> W, Vec<T> s) 
 template <class T> inline Vec<T> fromf(const float* p) { return mk<T>((T)p[0], (T)p[1], (T)p[2]); }
 template <class T> inline T tmax3(T a, T b, T c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
 
-// Transcendentals: float64 evaluation, rounded to T.
-template <class T> inline T tsin(T x) { return (T)std::sin((double)x); }
-template <class T> inline T tcos(T x) { return (T)std::cos((double)x); }
-template <class T> inline T ttan(T x) { return (T)std::tan((double)x); }
-template <class T> inline T tatan2(T y, T x) { return (T)std::atan2((double)y, (double)x); }
-template <class T> inline T tacos(T x) { return (T)std::acos((double)(x > T(1) ? T(1) : (x < T(-1) ? T(-1) : x))); }
+// sin and cos of 2*pi*u, u in [0, 1).  float: u*4 split exactly into a
+// quarter turn and a fraction f, f > 1/2 reflected (sin and cos swapped),
+// x = (pi/2) f in [0, pi/4] through the Taylor series of sin to x^9 and cos
+// to x^10, then the quarter-turn rotation; every operation rounds to float32
+// in this order (compiled without contraction), as the CUDA kernels do.
+// double: std::sin/std::cos of the float64 angle.
+inline void sincos_turns_f(float u, float& s, float& c) {
+  const float q = u * 4.0f;
+  int k = (int)q;
+  float f = q - (float)k;
+  const bool refl = f > 0.5f;
+  if (refl) f = 1.0f - f;
+  const float x = f * 1.57079632679f;
+  const float x2 = x * x;
+  const float sp = x * (1.0f + x2 * (-0.166666667f + x2 * (8.33333333e-3f + x2 * (-1.98412698e-4f +
+                                                                                 x2 * 2.75573192e-6f))));
+  const float cp = 1.0f + x2 * (-0.5f + x2 * (4.16666667e-2f + x2 * (-1.38888889e-3f + x2 * (2.48015873e-5f +
+                                                                                            x2 * -2.75573192e-7f))));
+  const float s0 = refl ? cp : sp, c0 = refl ? sp : cp;
+  k &= 3;
+  s = k == 0 ? s0 : (k == 1 ? c0 : (k == 2 ? -s0 : -c0));
+  c = k == 0 ? c0 : (k == 1 ? -s0 : (k == 2 ? -c0 : s0));
+}
+template <class T> inline void sincos_turns(T u, T& s, T& c);
+template <> inline void sincos_turns<float>(float u, float& s, float& c) { sincos_turns_f(u, s, c); }
+template <> inline void sincos_turns<double>(double u, double& s, double& c) {
+  const double th = 2 * 3.14159265358979323846 * u;
+  s = std::sin(th);
+  c = std::cos(th);
+}
 
 template <class T> struct Consts;
 template <> struct Consts<float> {
@@ -211,14 +237,15 @@ Vec<T> bsdf_f(const Mat<T>& m, Vec<T> wi, Vec<T> wo) {
     if (m.rd == T(0)) {
       s = wo.z / pi;  // Lambert
     } else {  // OrenNayar (bsdf/orennayar.go:42-73), sigma = roughness^2
+      // sin(max theta) * tan(min theta) and cos(phiO - phiI) from the
+      // direction components (no angles)
       const T sigma = m.rd * m.rd;
       const T A = 1 - (T(0.5) * (sigma * sigma) / ((sigma * sigma) + T(0.57)));
       const T B = T(0.45) * (sigma * sigma) / ((sigma * sigma) + T(0.09));
-      const T phiI = tatan2(wi.y, wi.x), phiO = tatan2(wo.y, wo.x);
-      const T thetaI = tacos(wi.z), thetaO = tacos(wo.z);
-      const T al = thetaI > thetaO ? thetaI : thetaO, be = thetaI < thetaO ? thetaI : thetaO;
-      const T C = tsin(al) * ttan(be);
-      const T gm = tcos(phiO - phiI);
+      const T sI = std::sqrt(std::max(T(0), T(1) - wi.z * wi.z)), sO = std::sqrt(std::max(T(0), T(1) - wo.z * wo.z));
+      const T C = wi.z < wo.z ? sI * (sO / wo.z) : sO * (sI / wi.z);
+      const T den = sI * sO;
+      const T gm = den > T(1e-6f) ? (wi.x * wo.x + wi.y * wo.y) / den : T(0);
       s = wo.z * (A + (B * (gm > T(0) ? gm : T(0)) * C)) / pi;
     }
     const T k = m.dw * s;
@@ -383,7 +410,6 @@ struct PT {
 
   // One path; returns L.
   Vec<T> path(uint64_t key, const float P0[3], const float D0[3], float time) const {
-    const T pi = Consts<T>::pi;
     Vec<T> beta = mk<T>(1, 1, 1), L = mk<T>(0, 0, 0);
     T pdf_prev = 0;
     float Pf[3] = {P0[0], P0[1], P0[2]}, Df[3] = {D0[0], D0[1], D0[2]};
@@ -446,8 +472,9 @@ struct PT {
         if (l.kind == 2) {
           const T z = 1 - 2 * u0;
           const T rr = std::sqrt((1 - z * z) > T(0) ? (1 - z * z) : T(0));
-          const T phi = 2 * pi * u1;
-          Ld = mk<T>(rr * tcos(phi), rr * tsin(phi), z);
+          T sp, cp;
+          sincos_turns(u1, sp, cp);
+          Ld = mk<T>(rr * cp, rr * sp, z);
           pl = sel * Consts<T>::inv4pi;
         } else {
           Vec<T> Pl;
@@ -491,20 +518,24 @@ struct PT {
       }
       // ---- BSDF sample
       const T ul = (T)rnd(key, base + 3);
-      const double r0 = (double)rnd(key, base + 4), r1 = (double)rnd(key, base + 5);
+      const T r0 = (T)rnd(key, base + 4), r1 = (T)rnd(key, base + 5);
       Vec<T> wol;
       bool delta = false;
       if (ul < m.dw) {  // CosineHemisphere (math/sample/sample.go:18-27)
-        const double r = std::sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
-        wol = mk<T>((T)(r * std::cos(th)), (T)(r * std::sin(th)), (T)std::sqrt(r0));
+        const T r = std::sqrt(T(1) - r0);
+        T sp, cp;
+        sincos_turns(r1, sp, cp);
+        wol = mk<T>(r * cp, r * sp, std::sqrt(r0));
       } else if (m.mirror) {
         wol = mk<T>(-wil.x, -wil.y, wil.z);
         delta = true;
-      } else {  // GGX: theta_m = atan(alpha sqrt(r0) / sqrt(1-r0)) (microfacetggx.go:82-100)
-        const double thetaM = std::atan2((double)m.alpha * std::sqrt(r0), std::sqrt(1 - r0));
-        const double phiM = 2.0 * 3.14159265358979323846 * r1;
-        const T st = tsin((T)thetaM), ct = tcos((T)thetaM);
-        const Vec<T> mh = mk<T>(st * tcos((T)phiM), st * tsin((T)phiM), ct);
+      } else {  // GGX: tan(theta_m) = alpha sqrt(r0) / sqrt(1-r0) (microfacetggx.go:82-100)
+        const T a = m.alpha * std::sqrt(r0), bq = std::sqrt(T(1) - r0);
+        const T hyp = std::sqrt(a * a + bq * bq);
+        const T st = a / hyp, ct = bq / hyp;
+        T sp, cp;
+        sincos_turns(r1, sp, cp);
+        const Vec<T> mh = mk<T>(st * cp, st * sp, ct);
         wol = nrm(sub(scl(2 * std::fabs(dot(mh, wil)), mh), wil));
       }
       const Vec<T> wo = expand(Ut, Vt, s.N, wol);
@@ -621,6 +652,10 @@ int run(const orc_render* r, const orc_quad_light* quads, uint32_t nq, const orc
 extern "C" {
 
 float orc_pt_rnd(uint64_t seed, uint64_t pix, uint32_t j, uint32_t dim) { return rnd(sample_key(seed, pix, j), dim); }
+
+void orc_sincos_turns(const float* u, size_t n, float* s, float* c) {
+  for (size_t i = 0; i < n; ++i) sincos_turns_f(u[i], s[i], c[i]);
+}
 
 int orc_pt_run(const orc_render* r, const orc_quad_light* quads, uint32_t n_quads, const orc_pt_params* p, float* fb,
                double* fb64, int precision, int nthreads) {

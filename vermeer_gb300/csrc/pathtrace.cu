@@ -150,6 +150,32 @@ __device__ __forceinline__ float rnd(uint64_t key, uint32_t dim) {
 
 constexpr float kInv4Pi = 0.0795774715f;  // float32(1/(4 pi))
 
+// sin and cos of 2*pi*u for u in [0, 1) in float32 arithmetic only (GB300's
+// float64 pipe is narrow, and these sit in every bounce's sampling):
+// u*4 splits exactly into a quarter turn k and a fraction f (u has 24
+// fraction bits), f > 1/2 is reflected to 1-f with sin and cos swapped, and
+// the remaining angle x = (pi/2)*f in [0, pi/4] goes through the Taylor
+// series of sin to x^9 and of cos to x^10 (truncation below 2e-9 there);
+// the quarter turn rotates the pair.  The oracle evaluates the same
+// operations in the same order, so both give the same bits.
+__device__ __forceinline__ void sincos_turns(float u, float& s, float& c) {
+  const float q = u * 4.0f;
+  int k = (int)q;
+  float f = q - (float)k;
+  const bool refl = f > 0.5f;
+  if (refl) f = 1.0f - f;
+  const float x = f * 1.57079632679f;
+  const float x2 = x * x;
+  const float sp = x * (1.0f + x2 * (-0.166666667f + x2 * (8.33333333e-3f + x2 * (-1.98412698e-4f +
+                                                                                 x2 * 2.75573192e-6f))));
+  const float cp = 1.0f + x2 * (-0.5f + x2 * (4.16666667e-2f + x2 * (-1.38888889e-3f + x2 * (2.48015873e-5f +
+                                                                                            x2 * -2.75573192e-7f))));
+  const float s0 = refl ? cp : sp, c0 = refl ? sp : cp;
+  k &= 3;
+  s = k == 0 ? s0 : (k == 1 ? c0 : (k == 2 ? -s0 : -c0));
+  c = k == 0 ? c0 : (k == 1 ? -s0 : (k == 2 ? -c0 : s0));
+}
+
 // ----------------------------------------------------------- material ----
 struct Mat {
   float dw, sw;
@@ -200,14 +226,18 @@ __device__ V3 bsdf_f(const Mat& m, V3 wi, V3 wo) {
     if (m.rd == 0.0f) {
       s = wo.z / kPi;
     } else {  // OrenNayar (bsdf/orennayar.go:42-73), sigma = roughness^2
+      // without angles: alpha = max(theta), beta = min(theta) of the two
+      // directions, so sin(alpha) = sin(theta) of the smaller cos and
+      // tan(beta) = sin/cos of the larger; cos(phiO - phiI) from the
+      // tangent-plane components (0 when a direction is along the normal)
       const float sigma = m.rd * m.rd;
       const float A = 1 - (0.5f * (sigma * sigma) / ((sigma * sigma) + 0.57f));
       const float B = 0.45f * (sigma * sigma) / ((sigma * sigma) + 0.09f);
-      const float phiI = gatan2(wi.y, wi.x), phiO = gatan2(wo.y, wo.x);
-      const float thetaI = gacos(wi.z), thetaO = gacos(wo.z);
-      const float al = thetaI > thetaO ? thetaI : thetaO, be = thetaI < thetaO ? thetaI : thetaO;
-      const float C = gsin(al) * gtan(be);
-      const float gm = gcos(phiO - phiI);
+      const float sI = sqrtf(fmaxf(0.0f, 1.0f - wi.z * wi.z)), sO = sqrtf(fmaxf(0.0f, 1.0f - wo.z * wo.z));
+      const bool iLow = wi.z < wo.z;  // theta_i is the larger angle
+      const float C = iLow ? sI * (sO / wo.z) : sO * (sI / wi.z);
+      const float den = sI * sO;
+      const float gm = den > 1e-6f ? (wi.x * wo.x + wi.y * wo.y) / den : 0.0f;
       s = wo.z * (A + (B * (gm > 0.0f ? gm : 0.0f) * C)) / kPi;
     }
     const float k = m.dw * s;
@@ -493,8 +523,9 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
               if (l.kind == 2) {
                 const float z = 1 - 2 * u0;
                 const float rr = sqrtf((1 - z * z) > 0.0f ? (1 - z * z) : 0.0f);
-                const float phi = 2 * kPi * u1;
-                Ld = v3(rr * gcos(phi), rr * gsin(phi), z);
+                float sp, cp;
+                sincos_turns(u1, sp, cp);
+                Ld = v3(rr * cp, rr * sp, z);
                 pl = b.sel * kInv4Pi;
               } else {
                 const V3 p0 = v3(l.p0[0], l.p0[1], l.p0[2]), la = v3(l.a[0], l.a[1], l.a[2]),
@@ -551,24 +582,28 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
             }
             // ---- continuation: the guide (probability alpha) or the BSDF
             const float ul = rnd(key, base + 3);
-            const double r0 = (double)rnd(key, base + 4), r1 = (double)rnd(key, base + 5);
+            const float r0 = rnd(key, base + 4), r1 = rnd(key, base + 5);
             V3 wol, wo;
             bool delta = false;
             const bool from_guide = guided && rnd(key, base + 7) < b.alpha;
             if (from_guide) {
-              wo = gmix_sample(gm, ul, (float)r0, (float)r1);
+              wo = gmix_sample(gm, ul, r0, r1);
               wol = project(Ut, Vt, sc.N, wo);
-            } else if (ul < m.dw) {  // CosineHemisphere (math/sample/sample.go:18-27)
-              const double r = sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
-              wol = v3((float)(r * cos(th)), (float)(r * sin(th)), (float)sqrt(r0));
+            } else if (ul < m.dw) {  // CosineHemisphere (math/sample/sample.go:18-27), float32
+              const float r = sqrtf(1.0f - r0);
+              float sp, cp;
+              sincos_turns(r1, sp, cp);
+              wol = v3(r * cp, r * sp, sqrtf(r0));
             } else if (m.mirror) {
               wol = v3(-wil.x, -wil.y, wil.z);
               delta = true;
-            } else {  // GGX D(m)cos(m) (microfacetggx.go:82-100)
-              const double thetaM = atan2((double)m.alpha * sqrt(r0), sqrt(1 - r0));
-              const double phiM = 2.0 * 3.14159265358979323846 * r1;
-              const float st = gsin((float)thetaM), ct = gcos((float)thetaM);
-              const V3 mh = v3(st * gcos((float)phiM), st * gsin((float)phiM), ct);
+            } else {  // GGX D(m)cos(m) (microfacetggx.go:82-100): tan(theta_m) = alpha sqrt(r0) / sqrt(1-r0)
+              const float a = m.alpha * sqrtf(r0), bq = sqrtf(1.0f - r0);
+              const float hyp = sqrtf(a * a + bq * bq);
+              const float st = a / hyp, ct = bq / hyp;
+              float sp, cp;
+              sincos_turns(r1, sp, cp);
+              const V3 mh = v3(st * cp, st * sp, ct);
               wol = normalize(sub(scale(2 * fabsf(dot(mh, wil)), mh), wil));
             }
             if (!from_guide) wo = expand(Ut, Vt, sc.N, wol);
