@@ -127,7 +127,7 @@ inline uint64_t sample_key(uint64_t seed, uint64_t pix, uint64_t j) {
 }
 // 24 random bits as a float in [0, 1) (exact in float32).
 inline float rnd(uint64_t key, uint32_t dim) {
-  return (float)(mix64(key + kGold * (uint64_t)(dim + 1)) >> 40) * 5.9604644775390625e-08f;
+  return (float)(uint32_t)(mix64(key + kGold * (uint64_t)(dim + 1)) >> 40) * 5.9604644775390625e-08f;
 }
 
 // ------------------------------------------------------------ offsets ----

@@ -145,7 +145,9 @@ __device__ __forceinline__ uint64_t sample_key(uint64_t seed, uint64_t pix, uint
 }
 // 24 random bits as a float in [0, 1), exact in float32.
 __device__ __forceinline__ float rnd(uint64_t key, uint32_t dim) {
-  return (float)(mix64(key + kGold * (uint64_t)(dim + 1)) >> 40) * 5.9604644775390625e-08f;
+  // 24 bits: converted through uint32 (a 64-bit conversion would take the
+  // narrow float64 pipe); the same value either way
+  return (float)(uint32_t)(mix64(key + kGold * (uint64_t)(dim + 1)) >> 40) * 5.9604644775390625e-08f;
 }
 
 constexpr float kInv4Pi = 0.0795774715f;  // float32(1/(4 pi))
@@ -888,6 +890,7 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
     l.stream = st;
     l.kernel = ctx->tuning.kernel;
     l.walk_tail = ctx->tuning.walk_tail;
+    l.grid = ctx->tuning.blocks_per_sm;
     if (b.n_jobs) {
       l.ray_path = b.qpath[d & 1];
       l.path_geom = b.pgeom;
@@ -921,6 +924,7 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
       s.stream = st;
       s.kernel = ctx->tuning.kernel;
       s.walk_tail = ctx->tuning.walk_tail;
+      s.grid = ctx->tuning.blocks_per_sm;
       if (b.n_jobs) {
         s.ray_path = b.spath;
         s.path_geom = b.pgeom;
@@ -1289,6 +1293,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
                                (uint64_t)(uintptr_t)ctx->top.nodes.p, (uint64_t)grid, (uint64_t)guided,
                                (uint64_t)train, (uint64_t)(uintptr_t)ctx->guide.wf.p, rcap,
                                (uint64_t)ctx->tuning.kernel, (uint64_t)ctx->tuning.walk_tail,
+                               (uint64_t)ctx->tuning.blocks_per_sm,
                                (uint64_t)ctx->tuning.sort_bits, (uint64_t)sort_on};
   {
     uint64_t h = 1469598103934665603ull;

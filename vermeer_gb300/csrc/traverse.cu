@@ -1858,7 +1858,7 @@ int launch_scene_t(const DTop& top, const TraceLaunch& l) {
   }
   auto k = k_trace_scene<ANY, COUNT>;
   const int block = 128;
-  const int grid = l.grid > 0 ? l.grid : persistent_grid(k, block);
+  const int grid = persistent_grid(k, block, l.grid);  // l.grid: resident blocks per SM
   k<<<grid, block, 0, (cudaStream_t)l.stream>>>(top, l.rays, l.hits, l.n, l.scratch, l.n_dev, l.order,
                                                 l.ray_path, l.path_geom);
   return (int)cudaGetLastError();
