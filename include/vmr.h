@@ -494,6 +494,10 @@ typedef struct {
                                          batch (0: 4) */
     uint32_t train_batch;             /* training records per step (0: 65536) */
     float train_lr;                   /* Adam learning rate (0: 1e-3) */
+    uint32_t guide_depth;             /* VMR_PATH_GUIDED: guide (and, with TRAIN,
+                                         record) only the first guide_depth
+                                         vertices of a path; deeper vertices
+                                         sample the BSDF alone (0: all) */
 } vmr_path_params;
 
 enum {

@@ -123,7 +123,7 @@ class PathParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
                 ("seed", ctypes.c_uint64), ("max_depth", U32), ("rr_depth", U32), ("max_batch_samples", U32),
                 ("flags", U32), ("fb64", P), ("guide_fraction", ctypes.c_float), ("train_steps", U32),
-                ("train_batch", U32), ("train_lr", ctypes.c_float)]
+                ("train_batch", U32), ("train_lr", ctypes.c_float), ("guide_depth", U32)]
 
 
 class PathStats(ctypes.Structure):

@@ -342,11 +342,12 @@ class Context:
     def render_path(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, max_depth: int = 4,
                     rr_depth: int = 3, fb=None, fb64=None, max_batch_samples: int = 0, graph: bool = True,
                     guided: bool = False, train: bool = False, guide_fraction: float = 0.0, train_steps: int = 0,
-                    train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False):
+                    train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False, guide_depth: int = 0):
         """The extended path tracer: iterations [iter_begin, iter_begin +
         iter_count) folded into fb (float32 [height, width, 3]) and, when
         given, fb64 (float64).  guided: sample the guide network too; train:
-        train it online; sort_queues: trace each queue in ray-key order.
+        train it online; guide_depth: guide only the first vertices of each
+        path (0: all); sort_queues: trace each queue in ray-key order.
         Returns (fb, stats)."""
         if fb is None:
             fb = np.zeros((height, width, 3), np.float32)
@@ -357,7 +358,7 @@ class Context:
                 (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0)
         p = _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
                             flags, None if fb64 is None else _p(fb64), guide_fraction, train_steps, train_batch,
-                            train_lr)
+                            train_lr, guide_depth)
         st = _lib.PathStats()
         self._check(self.L.vmr_render_path(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,

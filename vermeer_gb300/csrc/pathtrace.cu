@@ -110,6 +110,7 @@ struct PtBatch {
   double* fb64;
   // path guiding
   float alpha;                 // probability of sampling the guide at a vertex
+  uint32_t gdepth;             // guided vertices: the first gdepth of a path (host side)
   float glo[3];                // scene bounds for the guide's inputs
   float* grow;                 // 9 * cap: guide input rows per queue entry
   float* gout;                 // 40 * cap: guide outputs per queue entry
@@ -898,7 +899,9 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
     // camera rays are traced in pixel order (already coherent)
     if (srt.on && d > 0 && sort_queue(l) != 0) return pfail(ctx, VMR_ERR_CUDA, "ray sort launch failed");
     if (launch_trace_scene(top, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
-    if (guided) {
+    // vertices past the guided depth sample the BSDF alone (and record nothing)
+    const bool gd = guided && d < b.gdepth;
+    if (gd) {
       k_pt_prep<<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
       guide::GuideRows r = grows;
@@ -931,7 +934,7 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
       }
       if (srt.on && sort_queue(s) != 0) return pfail(ctx, VMR_ERR_CUDA, "ray sort launch failed");
       if (launch_trace_scene(top, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
-      if (train) k_pt_resolve<true><<<grid, kPtBlock, 0, st>>>(b, d);
+      if (train && gd) k_pt_resolve<true><<<grid, kPtBlock, 0, st>>>(b, d);
       else k_pt_resolve<false><<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
     }
@@ -1215,6 +1218,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   DScratch* scr = reinterpret_cast<DScratch*>(base + o_scr);
   b.scr = scr;
   b.alpha = alpha;
+  b.gdepth = p->guide_depth ? p->guide_depth : 0xffffffffu;
   std::memcpy(b.glo, glo, 12);
   b.grow = guided ? reinterpret_cast<float*>(base + o_grow) : nullptr;
   b.gout = guided ? reinterpret_cast<float*>(base + o_gout) : nullptr;
@@ -1309,6 +1313,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     const uint64_t nj = b.n_jobs;
     fold(&nj, sizeof(nj));
     fold(&b.alpha, sizeof(b.alpha));
+    fold(&b.gdepth, sizeof(b.gdepth));
     fold(b.glo, sizeof(b.glo));
     fold(grows.inv_ext, sizeof(grows.inv_ext));
     key.push_back(h);
