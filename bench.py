@@ -563,9 +563,11 @@ def render_extras(ctx, args):
         t0 = time.perf_counter()
         plain, _ = ctx.render_path(W, H, 8 * k, 8, 1, max_depth=8, fb=plain)
         tp += time.perf_counter() - t0
+    GD = 1  # guide the first vertex of each path (the others sample the BSDF alone)
     ctx.guide_init(7)
-    ctx.render_path(W, H, 0, 1, 2, max_depth=8, guided=True, train=True, guide_fraction=0.5, train_steps=1)
-    ctx.render_path(W, H, 0, 1, 2, max_depth=8, guided=True, guide_fraction=0.2)
+    ctx.render_path(W, H, 0, 1, 2, max_depth=8, guided=True, train=True, guide_fraction=0.5, train_steps=1,
+                    guide_depth=GD)
+    ctx.render_path(W, H, 0, 1, 2, max_depth=8, guided=True, guide_fraction=0.2, guide_depth=GD)
     ctx.guide_init(7)
     g = np.zeros((H, W, 3), np.float32)
     spp, tg, t_hit, k = 0, 0.0, None, 0
@@ -575,23 +577,27 @@ def render_extras(ctx, args):
         t0 = time.perf_counter()
         g, gst = ctx.render_path(W, H, spp, n, 1, max_depth=8, fb=g, guided=True, train=train,
                                  guide_fraction=0.5 if train else 0.2, train_steps=32, train_batch=65536,
-                                 train_lr=3e-3)
+                                 train_lr=3e-3, guide_depth=GD)
         tg += time.perf_counter() - t0
         spp += n
         k += 1
         if t_hit is None and not train and _relmse(g, ref) <= _relmse(plain, ref):
             t_hit = tg
+    # per sample: the trained guide at the plain arm's 256 spp (untimed)
+    g256, _ = ctx.render_path(W, H, 0, 256, 11, max_depth=8, guided=True, guide_fraction=0.2, guide_depth=GD)
     out["guided_slit"] = {
         "workload": "slit-light room, 200,000 diffuse triangles, 512x512 (not 1024x1024: the 4096-spp float64 "
                     "reference at 1024x1024 alone would take about 90 s), depth 8; plain 256 spp vs guided "
                     "for the same wall time: online training on 24 one-sample batches (guide fraction 0.5, "
                     "32 Adam steps of up to 65,536 continuation and light-sample records each), then the frozen "
-                    "guide at fraction 0.2 in 8-spp batches; both images keep every sample",
+                    "guide at fraction 0.2 in 8-spp batches; the guide samples the first vertex of each path "
+                    "(guide_depth 1); both images keep every sample",
         "plain": {"spp": 256, "wall_s": round(tp, 4), "relmse": round(_relmse(plain, ref), 5),
                   "median_rel_sq_err": round(_median_rel(plain, ref), 6)},
         "guided": {"spp": spp, "wall_s": round(tg, 4), "relmse": round(_relmse(g, ref), 5),
                    "median_rel_sq_err": round(_median_rel(g, ref), 6)},
         "guided_time_to_plain_relmse": None if t_hit is None else round(t_hit / tp, 3),
+        "guided_256spp": {"relmse": round(_relmse(g256, ref), 5), "median_rel_sq_err": round(_median_rel(g256, ref), 6)},
         "reference_spp": 4096}
     return out
 
