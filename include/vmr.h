@@ -184,6 +184,23 @@ int vmr_mesh_export(vmr_ctx* ctx, uint32_t geom, vmr_qbvh_node* nodes, int32_t* 
  * over the listed geoms (Scene.initAccel, scene.go:135-203).  Replaces any
  * previous scene of ctx. */
 int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n_geoms);
+/* PolyMesh.Transform with one matrix (builtin/geom/polymesh/trace.go:15-101):
+ * m = the 4x4 object-to-world matrix, column-major as math.Matrix4 (m[12..14]
+ * the translation); NULL removes it.  A scene trace that enters the mesh
+ * maps the ray into object space with Matrix4Inverse(m) (the same float32
+ * cofactor expansion; a singular m gives the zero matrix, as the reference
+ * ignores its ok flag), re-runs Ray.Setup, walks the mesh and restores the
+ * world ray, keeping Tclosest.  As in the reference the top level keeps the
+ * mesh's object-space bounds (PolyMesh.Bounds ignores the transform) and a
+ * direct vmr_trace_mesh ignores the transform (qbvh.Trace).  Renders apply
+ * the hit mesh's transform as core.Trace does after the trace
+ * (ShaderContext.ApplyTransform over the mesh's P = M Po, N = M^-T N):
+ * P = M Po, N = normalize(M^-T M^-T N), Ng = normalize(M^-T Ng),
+ * dPdu/dPdv = normalize(M dPdu/dPdv); Poffset stays in object space.  Not
+ * reproduced: the reference also rewrites the context with the transform
+ * of every other transformed mesh the ray enters (a leak across geoms).
+ * Analytic spheres take no transform.  Takes effect in the scene at once. */
+int vmr_mesh_set_transform(vmr_ctx* ctx, uint32_t geom, const float* m);
 /* Caller-built top level: static nodes, or motion nodes + boxes; geom_order
  * maps leaf position -> geom id. */
 int vmr_scene_upload(vmr_ctx* ctx, const vmr_qbvh_node* nodes, uint32_t n_nodes,

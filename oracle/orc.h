@@ -232,6 +232,9 @@ int orc_pt_run(const orc_render* r, const orc_quad_light* quads, uint32_t n_quad
                float* fb, double* fb64, int precision, int nthreads);
 /* Random number `dim` of pixel sample (pix, j = iteration + 1). */
 float orc_pt_rnd(uint64_t seed, uint64_t pix, uint32_t j, uint32_t dim);
+/* PolyMesh.Transform of a mesh (column-major 4x4, NULL: none); scenes and
+ * renders created after the call see it. */
+void orc_mesh_set_transform(orc_mesh* m, const float* xf);
 /* sin and cos of 2*pi*u[i] (u in [0, 1)) in the float32 operations of the
  * extended path tracer's sampling. */
 void orc_sincos_turns(const float* u, size_t n, float* s, float* c);

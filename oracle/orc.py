@@ -140,6 +140,7 @@ def _register_render(L):
     L.orc_pt_rnd.restype = ctypes.c_float
     L.orc_pt_rnd.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
     L.orc_sincos_turns.argtypes = [P, ctypes.c_size_t, P, P]
+    L.orc_mesh_set_transform.argtypes = [P, P]
     L.orc_guide_n_weights.restype = ctypes.c_int
     L.orc_guide_features.argtypes = [P, P, P, P, P, ctypes.c_int, P]
     L.orc_guide_forward.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P]
@@ -294,6 +295,8 @@ class Render:
             fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
             nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
             lib().orc_mesh_set_shading(om.h, _ptr(fs), _ptr(nr))
+            if m.get("transform") is not None:
+                om.set_transform(m["transform"])
             self.meshes.append(om)
         self.scene = Scene(self.meshes)
         counts = np.asarray([len(m["shaders"]) for m in scene["meshes"]], np.uint32)
@@ -416,6 +419,14 @@ class Mesh:
         if getattr(self, "h", None):
             lib().orc_mesh_destroy(self.h)
             self.h = None
+
+    def set_transform(self, m):
+        """PolyMesh.Transform: a column-major 4x4 (16 floats) or None."""
+        if m is None:
+            lib().orc_mesh_set_transform(self.h, None)
+        else:
+            self._xf = np.ascontiguousarray(m, np.float32).reshape(16)
+            lib().orc_mesh_set_transform(self.h, _ptr(self._xf))
 
     def info(self):
         n = ctypes.c_uint32()

@@ -366,6 +366,9 @@ struct Mesh {
   // An analytic sphere geom (builtin/geom/sphere) instead of triangles.
   bool sphere = false;
   float sc[3] = {0, 0, 0}, sr = 0;
+  // PolyMesh.Transform (one matrix, column-major) and Matrix4Inverse of it
+  bool has_xf = false;
+  float xf[16] = {}, xinv[16] = {};
 
   const float* vert(uint32_t i, int key) const { return &verts[((size_t)key * nverts + i) * 3]; }
   int motion_keys() const {  // polymesh.go:103-112; a sphere has one key (sphere.go:58-60)
@@ -796,11 +799,77 @@ void scene_init(Scene& s, Mesh* const* meshes, uint32_t n) {
   }
 }
 
+// math.Matrix4Inverse (math/matrix4.go:116-160).  Each adjugate element is
+// six signed triple products in the order listed (one string per element:
+// sign and three matrix indices per term); each product rounds as
+// (m[a]*m[b])*m[c] and the terms add left to right, in float32.
+void matrix4_inverse(const float m[16], float c[16]) {
+  static const char* kTerms[16] = {
+      "+5,10,15 -5,11,14 -9,6,15 +9,7,14 +13,6,11 -13,7,10",   // 0
+      "-1,10,15 +1,11,14 +9,2,15 -9,3,14 -13,2,11 +13,3,10",   // 1
+      "+1,6,15 -1,7,14 -5,2,15 +5,3,14 +13,2,7 -13,3,6",       // 2
+      "-1,6,11 +1,7,10 +5,2,11 -5,3,10 -9,2,7 +9,3,6",         // 3
+      "-4,10,15 +4,11,14 +8,6,15 -8,7,14 -12,6,11 +12,7,10",   // 4
+      "+0,10,15 -0,11,14 -8,2,15 +8,3,14 +12,2,11 -12,3,10",   // 5
+      "-0,6,15 +0,7,14 +4,2,15 -4,3,14 -12,2,7 +12,3,6",       // 6
+      "+0,6,11 -0,7,10 -4,2,11 +4,3,10 +8,2,7 -8,3,6",         // 7
+      "+4,9,15 -4,11,13 -8,5,15 +8,7,13 +12,5,11 -12,7,9",     // 8
+      "-0,9,15 +0,11,13 +8,1,15 -8,3,13 -12,1,11 +12,3,9",     // 9
+      "+0,5,15 -0,7,13 -4,1,15 +4,3,13 +12,1,7 -12,3,5",       // 10
+      "-0,5,11 +0,7,9 +4,1,11 -4,3,9 -8,1,7 +8,3,5",           // 11
+      "-4,9,14 +4,10,13 +8,5,14 -8,6,13 -12,5,10 +12,6,9",     // 12
+      "+0,9,14 -0,10,13 -8,1,14 +8,2,13 +12,1,10 -12,2,9",     // 13
+      "-0,5,14 +0,6,13 +4,1,14 -4,2,13 -12,1,6 +12,2,5",       // 14
+      "+0,5,10 -0,6,9 -4,1,10 +4,2,9 +8,1,6 -8,2,5",           // 15
+  };
+  float inv[16];
+  for (int e = 0; e < 16; ++e) {
+    const char* p = kTerms[e];
+    float acc = 0.0f;
+    for (int k = 0; k < 6; ++k) {
+      while (*p == ' ') ++p;
+      const bool neg = *p++ == '-';
+      int idx[3];
+      for (int q = 0; q < 3; ++q) {
+        idx[q] = 0;
+        while (*p >= '0' && *p <= '9') idx[q] = idx[q] * 10 + (*p++ - '0');
+        if (*p == ',') ++p;
+      }
+      const float v = (m[idx[0]] * m[idx[1]]) * m[idx[2]];
+      acc = k == 0 ? (neg ? -v : v) : (neg ? acc - v : acc + v);
+    }
+    inv[e] = acc;
+  }
+  float det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+  for (int i = 0; i < 16; ++i) c[i] = 0.0f;  // Matrix4Inverse's c when det == 0
+  if (det == 0.0f) return;
+  det = 1.0f / det;
+  for (int i = 0; i < 16; ++i) c[i] = inv[i] * det;
+}
+
+// PolyMesh.Trace's transform (builtin/geom/polymesh/trace.go:22-55, 64-69):
+// the ray mapped by Matrix4MulPoint/Matrix4MulVec of the inverse
+// (math/matrix4.go:177-218), Ray.Setup, the walk, then the world ray again
+// with the walk's Tclosest.
+bool mesh_trace_xf(const Mesh& m, Ray& r, Task& tk) {
+  if (!m.has_xf) return mesh_trace(m, r, tk);
+  const float* a = m.xinv;
+  Ray ro = r;
+  for (int i = 0; i < 3; ++i) {
+    ro.P[i] = a[i] * r.P[0] + a[4 + i] * r.P[1] + a[8 + i] * r.P[2] + a[12 + i];
+    ro.D[i] = a[i] * r.D[0] + a[4 + i] * r.D[1] + a[8 + i] * r.D[2];
+  }
+  ray_setup(ro);
+  const bool hit = mesh_trace(m, ro, tk);
+  r.Tclosest = ro.Tclosest;
+  return hit;
+}
+
 // Scene.TraceElems / TraceMotionElems (scene.go:61-97).
 bool scene_trace_elems(const Scene& s, Ray& r, Task& tk, int base, int count) {
   bool hit = false;
   for (int i = base; i < base + count; ++i) {
-    if (mesh_trace(*s.geoms[i], r, tk)) {
+    if (mesh_trace_xf(*s.geoms[i], r, tk)) {
       tk.geom = s.geom_order[i];
       hit = true;
       if (r.shadow) return true;
@@ -886,6 +955,11 @@ MeshView mesh_view(const orc_mesh* om) {
   v.sphere = m.sphere;
   for (int k = 0; k < 3; ++k) v.sc[k] = m.sc[k];
   v.sr = m.sr;
+  v.has_xf = m.has_xf;
+  for (int k = 0; k < 16; ++k) {
+    v.xf[k] = m.xf[k];
+    v.xinv[k] = m.xinv[k];
+  }
   return v;
 }
 
@@ -918,6 +992,13 @@ orc_mesh* orc_mesh_create(const float* verts, uint32_t nverts, uint32_t keys, co
 }
 
 void orc_mesh_destroy(orc_mesh* m) { delete m; }
+
+void orc_mesh_set_transform(orc_mesh* om, const float* m) {
+  Mesh& me = om->m;
+  me.has_xf = m != nullptr;
+  for (int k = 0; k < 16; ++k) me.xf[k] = m ? m[k] : 0.0f;
+  if (m) matrix4_inverse(me.xf, me.xinv);
+}
 
 // Shading data as PolyMesh holds it after initAccel (buildqbvh.go:98-104):
 // shader indices permuted to leaf order for a static mesh, face order for a

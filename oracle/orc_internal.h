@@ -28,6 +28,8 @@ struct MeshView {
   bool motion;
   bool sphere;              // analytic sphere geom: centre sc, radius sr
   float sc[3], sr;
+  bool has_xf;              // PolyMesh.Transform and its inverse (column-major)
+  float xf[16], xinv[16];
 };
 MeshView mesh_view(const orc_mesh* m);
 

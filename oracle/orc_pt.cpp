@@ -401,6 +401,30 @@ struct PT {
     s.Ng = nrm(Ng);
     s.dPdu = nrm(dpdu);
     s.dPdv = nrm(dpdv);
+    if (m.has_xf) {  // to world space as the reference mode does (trace.go:67-74, core/shader.go:129-135)
+      const float* M = m.xf;
+      const float* I = m.xinv;
+      auto pt = [&](Vec<T> b) {
+        return mk<T>((T)M[0] * b.x + (T)M[4] * b.y + (T)M[8] * b.z + (T)M[12],
+                     (T)M[1] * b.x + (T)M[5] * b.y + (T)M[9] * b.z + (T)M[13],
+                     (T)M[2] * b.x + (T)M[6] * b.y + (T)M[10] * b.z + (T)M[14]);
+      };
+      auto vec = [&](Vec<T> b) {
+        return mk<T>((T)M[0] * b.x + (T)M[4] * b.y + (T)M[8] * b.z, (T)M[1] * b.x + (T)M[5] * b.y + (T)M[9] * b.z,
+                     (T)M[2] * b.x + (T)M[6] * b.y + (T)M[10] * b.z);
+      };
+      auto inv_t = [&](Vec<T> b) {  // the inverse transposed
+        return mk<T>((T)I[0] * b.x + (T)I[1] * b.y + (T)I[2] * b.z, (T)I[4] * b.x + (T)I[5] * b.y + (T)I[6] * b.z,
+                     (T)I[8] * b.x + (T)I[9] * b.y + (T)I[10] * b.z);
+      };
+      const Vec<T> Po = s.P;
+      s.N = inv_t(s.N);
+      s.P = pt(Po);
+      s.N = nrm(inv_t(s.N));
+      s.Ng = nrm(inv_t(s.Ng));
+      s.dPdu = nrm(vec(s.dPdu));
+      s.dPdv = nrm(vec(s.dPdv));
+    }
     return (int32_t)list[sidx];
   }
 

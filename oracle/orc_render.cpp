@@ -830,6 +830,39 @@ struct Renderer {
     sc.DdPdu = normalize(dpdu);
     sc.DdPdv = normalize(dpdv);
     sc.geom = h.geom;
+    if (m.has_xf) {
+      // PolyMesh.Trace after its walk (trace.go:67-74): P = M Po, N = M^-T N;
+      // then core.Trace's ApplyTransform (core/shader.go:129-135) with the
+      // same matrices: P = M Po, N = normalize(M^-T N), Ng = normalize(M^-T
+      // Ng), dPdu/dPdv = normalize(M dPdu/dPdv).  Matrix4MulPoint/MulVec
+      // (math/matrix4.go:177-218) sum left to right; M^-T indexes the
+      // inverse transposed (Matrix4Transpose, :105-113).
+      const float* T = m.xf;
+      const float* I = m.xinv;
+      auto mul_point = [&](V3 b) {
+        return v3(T[0] * b.x + T[4] * b.y + T[8] * b.z + T[12], T[1] * b.x + T[5] * b.y + T[9] * b.z + T[13],
+                  T[2] * b.x + T[6] * b.y + T[10] * b.z + T[14]);
+      };
+      auto mul_vec = [&](V3 b) {
+        return v3(T[0] * b.x + T[4] * b.y + T[8] * b.z, T[1] * b.x + T[5] * b.y + T[9] * b.z,
+                  T[2] * b.x + T[6] * b.y + T[10] * b.z);
+      };
+      auto mul_inv_t = [&](V3 b) {
+        float t[16];
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) t[i * 4 + j] = I[j * 4 + i];
+        return v3(t[0] * b.x + t[4] * b.y + t[8] * b.z, t[1] * b.x + t[5] * b.y + t[9] * b.z,
+                  t[2] * b.x + t[6] * b.y + t[10] * b.z);
+      };
+      const V3 Po = sc.P;
+      sc.P = mul_point(Po);
+      sc.N = mul_inv_t(sc.N);
+      sc.P = mul_point(Po);
+      sc.N = normalize(mul_inv_t(sc.N));
+      sc.Ng = normalize(mul_inv_t(sc.Ng));
+      sc.DdPdu = normalize(mul_vec(sc.DdPdu));
+      sc.DdPdv = normalize(mul_vec(sc.DdPdv));
+    }
     return true;
   }
 

@@ -103,7 +103,18 @@ SCENES = {
     "spheres": lambda: scenes.small_room_spheres(1024, seed=5),
     "motion": lambda: scenes.small_room_motion(1024, seed=6, motion_mode=1),
     "quads_filter": lambda: dict(scenes.small_room_ext(1024, seed=7), pixel_filter={"kind": 1}),
+    "transformed": lambda: _transformed(scenes.small_room(1024, seed=8)),
 }
+
+
+def _transformed(sc):
+    """The soup with a PolyMesh Transform (a turn about y and a lift)."""
+    c, s_ = np.cos(0.3), np.sin(0.3)
+    m = np.array([[c, 0, s_, 0], [0, 1, 0, 0.02], [-s_, 0, c, 0], [0, 0, 0, 1]], np.float32)
+    meshes = [dict(mm) for mm in sc["meshes"]]
+    soup = max(range(len(meshes)), key=lambda g: len(meshes[g].get("idxp", ())))
+    meshes[soup]["transform"] = m.T.reshape(16)  # column-major
+    return dict(sc, meshes=meshes)
 
 
 def _host_pair(name, tmp_path, w=40, h=30):
@@ -145,7 +156,7 @@ def test_vnf_round_trip_builds_the_same_scene(tmp_path, name):
 
 # ------------------------------------------------------------------ GPU ----
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["small_room", "disk_thin_lens", "spheres", "motion"])
+@pytest.mark.parametrize("name", ["small_room", "disk_thin_lens", "spheres", "motion", "transformed"])
 def test_vnf_render_equals_direct_scene(ctx, tmp_path, name):
     sc, path, mf, _ = _host_pair(name, tmp_path)
     ctx.load_scene(scenes.vnf_order(sc))

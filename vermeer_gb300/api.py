@@ -479,6 +479,15 @@ class Context:
         self._check(self.L.vmr_render(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, camera_rays=st.camera_rays, shadow_rays=st.shadow_rays, ms=st.ms)
 
+    def mesh_set_transform(self, geom: int, m):
+        """PolyMesh.Transform (vmr_mesh_set_transform): a column-major 4x4
+        as 16 floats (math.Matrix4 order), or None to remove it."""
+        if m is None:
+            self._check(self.L.vmr_mesh_set_transform(self.h, geom, None))
+            return
+        a = np.ascontiguousarray(m, np.float32).reshape(16)
+        self._check(self.L.vmr_mesh_set_transform(self.h, geom, _p(a)))
+
     def load_scene(self, scene: dict):
         """Upload a render scene (vermeer_gb300.scenes format): meshes with
         their shading, the two-level scene, materials, lights, camera.
@@ -491,6 +500,8 @@ class Context:
                 g = self.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1),
                                     motion_mode=m.get("motion_mode", MOTION_FAITHFUL),
                                     shader_idx=m.get("face_shader"))
+                if m.get("transform") is not None:
+                    self.mesh_set_transform(g, m["transform"])
             ids.append(g)
         self.scene_build(ids)
         self.set_shaders(scene["shaders"])

@@ -112,6 +112,13 @@ bool repack_mnodes(const std::vector<vmr_mqbvh_node>& in, uint32_t n_elems, std:
 
 struct F4 { float x, y, z, w; };
 
+// The device copy of a mesh's transform (its inverse, columns 0..3 of rows 0..2).
+void fill_xf(const MeshRec& rec, DMesh& d) {
+  static const int kCols[12] = {0, 1, 2, 4, 5, 6, 8, 9, 10, 12, 13, 14};
+  d.has_xf = rec.has_xf ? 1u : 0u;
+  for (int k = 0; k < 12; ++k) d.xf_inv[k] = rec.has_xf ? rec.xf_inv[kCols[k]] : 0.0f;
+}
+
 // Host accelerator -> device arrays (layout in device.h).  tris_ready: the
 // device builder already wrote the static triangle table into rec.tris.
 int upload_mesh(vmr_ctx* ctx, MeshRec& rec, bool tris_ready = false) {
@@ -166,6 +173,7 @@ int upload_mesh(vmr_ctx* ctx, MeshRec& rec, bool tris_ready = false) {
     d.iter_cap = 4u * (uint32_t)m.mnodes.size() + 2u;
   }
   VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  fill_xf(rec, d);
   rec.dmesh = d;
   for (int a = 0; a < 3; ++a) {
     rec.bounds6[a] = m.bounds.lo[a];
@@ -181,6 +189,50 @@ bool valid_mesh_input(const vmr_mesh_input* in, std::string& why) {
   for (size_t i = 0; i < (size_t)in->n_tris * 3; ++i)
     if (in->idxp[i] >= in->n_verts) { why = "vertex index out of range"; return false; }
   return true;
+}
+
+// math.Matrix4Inverse (math/matrix4.go:116-160): every element of the
+// adjugate is six triple products (m[a]*m[b])*m[c] summed left to right with
+// the cofactor signs, then det = ((m0 i0 + m1 i4) + m2 i8) + m3 i12 and
+// c = i * (1/det), all in float32 (host code built without contraction).
+// The term table keeps the reference's term order, which fixes the rounding;
+// a zero determinant leaves c all zero (the reference returns its zero c).
+struct InvTerm { int8_t s, a, b, c; };
+const int8_t kInvOut[16] = {0, 4, 8, 12, 1, 5, 9, 13, 2, 6, 10, 14, 3, 7, 11, 15};
+const InvTerm kInvTerms[16][6] = {
+    {{1, 5, 10, 15}, {-1, 5, 11, 14}, {-1, 9, 6, 15}, {1, 9, 7, 14}, {1, 13, 6, 11}, {-1, 13, 7, 10}},
+    {{-1, 4, 10, 15}, {1, 4, 11, 14}, {1, 8, 6, 15}, {-1, 8, 7, 14}, {-1, 12, 6, 11}, {1, 12, 7, 10}},
+    {{1, 4, 9, 15}, {-1, 4, 11, 13}, {-1, 8, 5, 15}, {1, 8, 7, 13}, {1, 12, 5, 11}, {-1, 12, 7, 9}},
+    {{-1, 4, 9, 14}, {1, 4, 10, 13}, {1, 8, 5, 14}, {-1, 8, 6, 13}, {-1, 12, 5, 10}, {1, 12, 6, 9}},
+    {{-1, 1, 10, 15}, {1, 1, 11, 14}, {1, 9, 2, 15}, {-1, 9, 3, 14}, {-1, 13, 2, 11}, {1, 13, 3, 10}},
+    {{1, 0, 10, 15}, {-1, 0, 11, 14}, {-1, 8, 2, 15}, {1, 8, 3, 14}, {1, 12, 2, 11}, {-1, 12, 3, 10}},
+    {{-1, 0, 9, 15}, {1, 0, 11, 13}, {1, 8, 1, 15}, {-1, 8, 3, 13}, {-1, 12, 1, 11}, {1, 12, 3, 9}},
+    {{1, 0, 9, 14}, {-1, 0, 10, 13}, {-1, 8, 1, 14}, {1, 8, 2, 13}, {1, 12, 1, 10}, {-1, 12, 2, 9}},
+    {{1, 1, 6, 15}, {-1, 1, 7, 14}, {-1, 5, 2, 15}, {1, 5, 3, 14}, {1, 13, 2, 7}, {-1, 13, 3, 6}},
+    {{-1, 0, 6, 15}, {1, 0, 7, 14}, {1, 4, 2, 15}, {-1, 4, 3, 14}, {-1, 12, 2, 7}, {1, 12, 3, 6}},
+    {{1, 0, 5, 15}, {-1, 0, 7, 13}, {-1, 4, 1, 15}, {1, 4, 3, 13}, {1, 12, 1, 7}, {-1, 12, 3, 5}},
+    {{-1, 0, 5, 14}, {1, 0, 6, 13}, {1, 4, 1, 14}, {-1, 4, 2, 13}, {-1, 12, 1, 6}, {1, 12, 2, 5}},
+    {{-1, 1, 6, 11}, {1, 1, 7, 10}, {1, 5, 2, 11}, {-1, 5, 3, 10}, {-1, 9, 2, 7}, {1, 9, 3, 6}},
+    {{1, 0, 6, 11}, {-1, 0, 7, 10}, {-1, 4, 2, 11}, {1, 4, 3, 10}, {1, 8, 2, 7}, {-1, 8, 3, 6}},
+    {{-1, 0, 5, 11}, {1, 0, 7, 9}, {1, 4, 1, 11}, {-1, 4, 3, 9}, {-1, 8, 1, 7}, {1, 8, 3, 5}},
+    {{1, 0, 5, 10}, {-1, 0, 6, 9}, {-1, 4, 1, 10}, {1, 4, 2, 9}, {1, 8, 1, 6}, {-1, 8, 2, 5}},
+};
+void matrix4_inverse(const float m[16], float c[16]) {
+  float inv[16];
+  for (int e = 0; e < 16; ++e) {
+    float acc = 0.0f;
+    for (int k = 0; k < 6; ++k) {
+      const InvTerm& t = kInvTerms[e][k];
+      const float v = (m[t.a] * m[t.b]) * m[t.c];
+      acc = k == 0 ? (t.s > 0 ? v : -v) : (t.s > 0 ? acc + v : acc - v);
+    }
+    inv[kInvOut[e]] = acc;
+  }
+  float det = ((m[0] * inv[0] + m[1] * inv[4]) + m[2] * inv[8]) + m[3] * inv[12];
+  for (int i = 0; i < 16; ++i) c[i] = 0.0f;
+  if (det == 0.0f) return;
+  det = 1.0f / det;
+  for (int i = 0; i < 16; ++i) c[i] = inv[i] * det;
 }
 
 int refresh_top(vmr_ctx* ctx) {
@@ -222,7 +274,7 @@ int refresh_top(vmr_ctx* ctx) {
     t.bounds6[3 + k] = -INFINITY;
   }
   for (uint32_t g : t.host.geom_order) {
-    if (ctx->meshes[g]->host.motion()) d.all_static = 0u;
+    if (ctx->meshes[g]->host.motion() || ctx->meshes[g]->has_xf) d.all_static = 0u;
     for (int k = 0; k < 3; ++k) {
       t.bounds6[k] = std::min(t.bounds6[k], ctx->meshes[g]->bounds6[k]);
       t.bounds6[3 + k] = std::max(t.bounds6[3 + k], ctx->meshes[g]->bounds6[3 + k]);
@@ -638,6 +690,21 @@ int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n) {
   if (!vmr::build_top_level(ms, ids, top, why)) return fail(ctx, VMR_ERR_INVALID, why);
   ctx->top.host = std::move(top);
   return refresh_top(ctx);
+}
+
+int vmr_mesh_set_transform(vmr_ctx* ctx, uint32_t geom, const float* m) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+  MeshRec& rec = *ctx->meshes[geom];
+  if (m && rec.host.sphere) return fail(ctx, VMR_ERR_UNSUPPORTED, "an analytic sphere takes no transform");
+  rec.has_xf = m != nullptr;
+  if (m) {
+    std::memcpy(rec.xf, m, sizeof(rec.xf));
+    matrix4_inverse(rec.xf, rec.xf_inv);
+  }
+  fill_xf(rec, rec.dmesh);
+  if (ctx->top.valid) return refresh_top(ctx);
+  return VMR_OK;
 }
 
 int vmr_scene_upload(vmr_ctx* ctx, const vmr_qbvh_node* nodes, uint32_t n_nodes, const vmr_mqbvh_node* mnodes,

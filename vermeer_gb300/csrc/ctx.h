@@ -48,6 +48,9 @@ struct MeshRec {
   bool has_normals = false;
   DevBuf shlist, sidx, nrm;
   DevBuf avert, aidx;  // motion meshes: key-major vertices (float4) and face-order idxp for hit attributes
+  // PolyMesh.Transform (one matrix, column-major) and its Matrix4Inverse
+  bool has_xf = false;
+  float xf[16] = {}, xf_inv[16] = {};
   // the autotuner's choice for this mesh (vmr_autotune)
   bool tuned = false;
   vmr_tuning tuning{};

@@ -63,7 +63,11 @@ struct DMesh {
   uint32_t iter_cap;        // 4 * nodes + 2: a traversal pops each entry once
   uint32_t kind;            // 0 triangles, 1 analytic sphere (builtin/geom/sphere)
   float sphere[4];          // centre, radius
-  uint32_t pad[3];
+  uint32_t has_xf;          // PolyMesh.Transform: rays enter through xf_inv
+  uint32_t pad[2];
+  // Matrix4Inverse of the transform, columns 0..3 rows 0..2 (column-major
+  // elements 0,1,2, 4,5,6, 8,9,10, 12,13,14)
+  float xf_inv[12];
 };
 
 // Top level of a scene (builtin/scene): static GNodes or motion MNodes with

@@ -1074,6 +1074,9 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     rm[g].n_verts = mr.host.n_verts;
     rm[g].mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
     rm[g].midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
+    rm[g].has_xf = mr.has_xf ? 1u : 0u;
+    std::memcpy(rm[g].xf, mr.xf, sizeof(mr.xf));
+    std::memcpy(rm[g].xf_inv, mr.xf_inv, sizeof(mr.xf_inv));
   }
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
@@ -1257,7 +1260,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     top.keys = 1;
     top.all_static = 1u;
     for (uint32_t g : used_geoms)
-      if (ctx->meshes[g]->host.motion()) top.all_static = 0u;
+      if (ctx->meshes[g]->host.motion() || ctx->meshes[g]->has_xf) top.all_static = 0u;
   }
   if (train) PCUDA(cudaMemsetAsync(b.rcount, 0, 32, st));
   guide::GuideRows grows{};

@@ -792,6 +792,9 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     rm[g].n_verts = mr.host.n_verts;
     rm[g].mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
     rm[g].midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
+    rm[g].has_xf = mr.has_xf ? 1u : 0u;
+    std::memcpy(rm[g].xf, mr.xf, sizeof(mr.xf));
+    std::memcpy(rm[g].xf_inv, mr.xf_inv, sizeof(mr.xf_inv));
   }
   std::vector<RLight> rl(R.lights.size() + R.disks.size() + R.spheres.size());
   uint32_t ns = 1;

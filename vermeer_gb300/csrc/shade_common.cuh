@@ -298,6 +298,9 @@ struct RMesh {
   const float4* mverts;
   const uint32_t* midxp;
   uint32_t keys, n_verts;
+  // PolyMesh.Transform: the matrix and its Matrix4Inverse, column-major
+  uint32_t has_xf;
+  float xf[16], xf_inv[16];
 };
 struct RLight {
   float p[9];        // TriLight: p0, p1, p2
@@ -562,12 +565,42 @@ __device__ __forceinline__ bool motion_attributes(const RMesh& m, int32_t elem, 
   return true;
 }
 
-// The hit attributes of any geom kind.
+// Matrix4MulPoint / Matrix4MulVec (math/matrix4.go:177-218) of a
+// column-major matrix, and Matrix4MulVec of its transpose.
+__device__ __forceinline__ V3 xf_point(const float* a, V3 b) {
+  return v3(a[0] * b.x + a[4] * b.y + a[8] * b.z + a[12], a[1] * b.x + a[5] * b.y + a[9] * b.z + a[13],
+            a[2] * b.x + a[6] * b.y + a[10] * b.z + a[14]);
+}
+__device__ __forceinline__ V3 xf_vec(const float* a, V3 b) {
+  return v3(a[0] * b.x + a[4] * b.y + a[8] * b.z, a[1] * b.x + a[5] * b.y + a[9] * b.z,
+            a[2] * b.x + a[6] * b.y + a[10] * b.z);
+}
+__device__ __forceinline__ V3 xf_vec_t(const float* a, V3 b) {
+  return v3(a[0] * b.x + a[1] * b.y + a[2] * b.z, a[4] * b.x + a[5] * b.y + a[6] * b.z,
+            a[8] * b.x + a[9] * b.y + a[10] * b.z);
+}
+
+// The hit attributes of any geom kind.  A transformed mesh's object-space
+// attributes go to world space as the reference does after the mesh walk
+// and again in core.Trace: PolyMesh.Trace sets P = M Po and N = M^-T N
+// (builtin/geom/polymesh/trace.go:67-74), then ShaderContext.ApplyTransform
+// (core/shader.go:129-135) sets P = M Po, N = normalize(M^-T N) (a second
+// time), Ng = normalize(M^-T Ng), dPdu/dPdv = normalize(M dPdu/dPdv).
 __device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim, float U, float V, float W, V3 Ro,
                                                    V3 Rd, float t, float time, Ctx& sc, uint32_t& shader_id) {
   if (m.kind == 1) return sphere_attributes(m, Ro, Rd, t, sc, shader_id);
-  if (m.keys > 1) return motion_attributes(m, prim, U, V, W, time, sc, shader_id);
-  return hit_attributes(m, prim, U, V, W, sc, shader_id);
+  const bool ok = m.keys > 1 ? motion_attributes(m, prim, U, V, W, time, sc, shader_id)
+                             : hit_attributes(m, prim, U, V, W, sc, shader_id);
+  if (ok && m.has_xf) {
+    const V3 Po = sc.P;
+    sc.N = xf_vec_t(m.xf_inv, sc.N);
+    sc.P = xf_point(m.xf, Po);
+    sc.N = normalize(xf_vec_t(m.xf_inv, sc.N));
+    sc.Ng = normalize(xf_vec_t(m.xf_inv, sc.Ng));
+    sc.DdPdu = normalize(xf_vec(m.xf, sc.DdPdu));
+    sc.DdPdv = normalize(xf_vec(m.xf, sc.DdPdv));
+  }
+  return ok;
 }
 
 }  // namespace

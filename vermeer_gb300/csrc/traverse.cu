@@ -486,6 +486,29 @@ __device__ __forceinline__ bool trace_any_mesh(const DMesh& m, TRay& r, int2* st
   return trace_static<ANY, COUNT>(m, r, stk, cap, h, cnt, status);
 }
 
+// PolyMesh.Trace with a Transform (builtin/geom/polymesh/trace.go:22-55): the
+// ray in object space, P' = Matrix4MulPoint(inv, P), D' = Matrix4MulVec(inv,
+// D) (math/matrix4.go:177-218, sums left to right), then Ray.Setup; time and
+// Tclosest stay.  x: the inverse's columns 0..3, rows 0..2.
+__device__ __forceinline__ void ray_to_object(TRay& r, const float* x) {
+  const float px = r.ox, py = r.oy, pz = r.oz, dx = r.dx, dy = r.dy, dz = r.dz;
+  r.ox = ((x[0] * px + x[3] * py) + x[6] * pz) + x[9];
+  r.oy = ((x[1] * px + x[4] * py) + x[7] * pz) + x[10];
+  r.oz = ((x[2] * px + x[5] * py) + x[8] * pz) + x[11];
+  r.dx = (x[0] * dx + x[3] * dy) + x[6] * dz;
+  r.dy = (x[1] * dx + x[4] * dy) + x[7] * dz;
+  r.dz = (x[2] * dx + x[5] * dy) + x[8] * dz;
+  ray_setup(r);
+}
+
+// The world ray again after an object-space walk: P and D from the ray
+// stream and Ray.Setup, Tclosest and time kept.
+__device__ __forceinline__ void load_ray_pd(const RaySoA& rs, uint64_t i, TRay& r) {
+  r.ox = __ldg(rs.px + i); r.oy = __ldg(rs.py + i); r.oz = __ldg(rs.pz + i);
+  r.dx = __ldg(rs.dx + i); r.dy = __ldg(rs.dy + i); r.dz = __ldg(rs.dz + i);
+  ray_setup(r);
+}
+
 __device__ __forceinline__ void load_ray(const RaySoA& rs, uint64_t i, TRay& r) {
   r.ox = __ldg(rs.px + i); r.oy = __ldg(rs.py + i); r.oz = __ldg(rs.pz + i);
   r.dx = __ldg(rs.dx + i); r.dy = __ldg(rs.dy + i); r.dz = __ldg(rs.dz + i);
@@ -597,7 +620,17 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
           // as Traversal.StackTop = stackTop + 1 does (intersect.go:226).
           const int base = sp + 1;
           if (base >= kStackCapacity) { status = kStatusStackOverflow; break; }
-          if (trace_any_mesh<ANY, COUNT>(top.meshes[g], r, stk + base, kStackCapacity - base, hm, cnt, status)) {
+          const DMesh& M = top.meshes[g];
+          bool mh;
+          if (M.has_xf) {  // the object-space copy walks the mesh; the world ray keeps its Tclosest
+            TRay ro = r;
+            ray_to_object(ro, M.xf_inv);
+            mh = trace_any_mesh<ANY, COUNT>(M, ro, stk + base, kStackCapacity - base, hm, cnt, status);
+            r.tclosest = ro.tclosest;
+          } else {
+            mh = trace_any_mesh<ANY, COUNT>(M, r, stk + base, kStackCapacity - base, hm, cnt, status);
+          }
+          if (mh) {
             h = hm;
             h.geom = (int32_t)g;
             leaf_hit = true;
@@ -654,6 +687,7 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
       if (ray_path) {  // job mode: the ray's own mesh, one stack slot above the (absent) top level
         const uint32_t g = __ldg(path_geom + __ldg(ray_path + rid));
         HitRec hm = h;
+        if (top.meshes[g].has_xf) ray_to_object(r, top.meshes[g].xf_inv);  // no world-space work follows
         hit = trace_any_mesh<ANY, COUNT>(top.meshes[g], r, stk + 1, kStackCapacity - 1, hm, cnt, status);
         if (hit) {
           h = hm;
@@ -1256,6 +1290,8 @@ __global__ void __launch_bounds__(128, 8)
   float lower = 0.f;
   uint32_t mcap = 0;
   bool mmot = false;  // the current mesh has motion keys (its key data is re-read from top.meshes)
+  bool mxf = false;   // the current mesh has a transform: r is its object-space ray
+  uint32_t li = 0;    // the ray's position in rays (the world ray is reloaded from it)
   float tm_unused = 0.f, omt_unused = 1.f;
   int key_unused = 0, key2_unused = 0;
   for (;;) {
@@ -1273,6 +1309,7 @@ __global__ void __launch_bounds__(128, 8)
         const uint64_t i = b0 + __popc(need & lanes_below);
         if (i < n) {
           rid = order ? (uint64_t)__ldg(order + i) : i;
+          li = (uint32_t)i;
           load_ray(rays, i, r);
           h = HitRec{-1, -1, 0.f, 0.f, 0.f};
           hit = false;
@@ -1300,6 +1337,7 @@ __global__ void __launch_bounds__(128, 8)
               base = 1;
               geom = (int)g;
               mmot = MOT && M.keys > 1;
+              if (MOT && M.has_xf) ray_to_object(r, M.xf_inv);  // the mesh is the ray's whole walk
               mnodes = M.nodes;
               mtris = reinterpret_cast<const float4*>(M.tris);
               lower = M.lower_static;
@@ -1412,6 +1450,10 @@ __global__ void __launch_bounds__(128, 8)
           if (geom >= 0) {  // the mesh traversal is done
             geom = -1;
             sp = base - 1;
+            if (MOT && mxf) {  // back to the world ray (Tclosest kept)
+              load_ray_pd(rays, li, r);
+              mxf = false;
+            }
           }
           if (leaf_left > 0) {  // enter the next geom of the top-level leaf
             const uint32_t g = __ldg(top.geom_order + leaf_next);
@@ -1438,6 +1480,8 @@ __global__ void __launch_bounds__(128, 8)
             }
             geom = (int)g;
             mmot = MOT && M.keys > 1;
+            mxf = MOT && M.has_xf;
+            if (mxf) ray_to_object(r, M.xf_inv);
             mnodes = M.nodes;
             mtris = reinterpret_cast<const float4*>(M.tris);
             lower = M.lower_static;
@@ -1524,6 +1568,10 @@ __global__ void __launch_bounds__(128, 8)
             }
             geom = -1;
             sp = base - 1;
+            if (MOT && mxf) {  // back to the world ray (Tclosest kept)
+              load_ray_pd(rays, li, r);
+              mxf = false;
+            }
             if (leaf_left > 0) {
               const uint32_t g = __ldg(top.geom_order + leaf_next);
               ++leaf_next;
@@ -1545,6 +1593,8 @@ __global__ void __launch_bounds__(128, 8)
               base = sp + 1;
               geom = (int)g;
               mmot = MOT && MM.keys > 1;
+              mxf = MOT && MM.has_xf;
+              if (mxf) ray_to_object(r, MM.xf_inv);
               mnodes = MM.nodes;
               mtris = reinterpret_cast<const float4*>(MM.tris);
               lower = MM.lower_static;

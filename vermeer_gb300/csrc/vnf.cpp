@@ -24,8 +24,9 @@
 // Where the reference tolerates an error (prints it and skips the field or
 // node), the loader stops with VMR_ERR_INVALID and the file:line in
 // vmr_last_error; nodes the GPU path does not render (DebugShader, Proc,
-// GeomInstance, textures, non-identity PolyMesh transforms, camera motion
-// keys) give VMR_ERR_UNSUPPORTED.
+// GeomInstance, textures, PolyMesh transforms with several motion keys,
+// camera motion keys) give VMR_ERR_UNSUPPORTED; a PolyMesh Transform of one
+// matrix goes to vmr_mesh_set_transform.
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -454,6 +455,8 @@ struct MeshOut {
   float ray_bias = 0.0f;
   bool sphere = false;
   float centre[3] = {0, 0, 0}, radius = 0.f;
+  bool has_xf = false;  // PolyMesh.Transform with one non-identity matrix (column-major)
+  float xf[16] = {};
 };
 
 struct Scene {
@@ -529,11 +532,18 @@ MeshOut poly_mesh(const Node& n, const Scene& sc, const std::string& file) {
   o.n_verts = (uint32_t)V.per;
   o.verts = V.v;
   if (n.has("RayBias")) o.ray_bias = (float)n.at("RayBias").f;
-  if (n.has("Transform")) {
+  if (n.has("Transform")) {  // an identity changes nothing (the same ray after Setup)
     const Value& T = n.at("Transform");
-    for (size_t k = 0; k * 16 < T.v.size(); ++k)
-      if (!identity(T.v.data() + 16 * k))
-        throw LoadError{VMR_ERR_UNSUPPORTED, where("transformed meshes are not supported")};
+    const size_t nk = T.v.size() / 16;
+    bool all_identity = true;
+    for (size_t k = 0; k < nk; ++k) all_identity = all_identity && identity(T.v.data() + 16 * k);
+    if (!all_identity) {
+      if (nk != 1)
+        throw LoadError{VMR_ERR_UNSUPPORTED,
+                        where("transform motion keys (TransformDecompLerp) are not supported; give one matrix")};
+      o.has_xf = true;
+      std::memcpy(o.xf, T.v.data(), sizeof(o.xf));
+    }
   }
   for (const std::string& s : n.at("Shader").strs) o.shaders.push_back(shader_of(sc, n, s, file));
   const std::vector<int32_t> none;
@@ -864,6 +874,7 @@ extern "C" int vmr_load_vnf(vmr_ctx* ctx, const char* path, int flags, vmr_vnf_i
       mi.motion_mode = mode;
       mi.shader_idx = g.sidx.empty() ? nullptr : g.sidx.data();
       rc = vmr_mesh_build(ctx, &mi, &id);
+      if (rc == VMR_OK && g.has_xf) rc = vmr_mesh_set_transform(ctx, id, g.xf);
     }
     if (rc != VMR_OK) return rc;
     ids.push_back(id);

@@ -591,6 +591,9 @@ def to_vnf(scene: dict, width: int, height: int, max_iter: int = 16) -> str:
         if m.get("normals") is not None:
             nr = np.asarray(m["normals"], np.float32).reshape(-1, 3)
             lines.append(f"  Normals 1 {nr.shape[0]} vec3 " + " ".join(_vnf_num(x) for x in nr.ravel()))
+        if m.get("transform") is not None:  # column-major; written row by row, the reader transposes
+            xt = np.asarray(m["transform"], np.float32).reshape(4, 4).T
+            lines.append("  Transform 1 matrix " + " ".join(_vnf_num(x) for x in xt.ravel()))
         out.append("\n".join(lines) + "\n}")
     vec = lambda a: " ".join(_vnf_num(x) for x in a)  # noqa: E731
     for i, l in enumerate(scene.get("lights", [])):
