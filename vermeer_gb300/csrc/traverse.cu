@@ -1291,7 +1291,7 @@ __global__ void __launch_bounds__(128, 8)
   uint32_t mcap = 0;
   bool mmot = false;  // the current mesh has motion keys (its key data is re-read from top.meshes)
   bool mxf = false;   // the current mesh has a transform: r is its object-space ray
-  uint32_t li = 0;    // the ray's position in rays (the world ray is reloaded from it)
+  uint64_t li = 0;    // the ray's position in rays (the world ray is reloaded from it)
   float tm_unused = 0.f, omt_unused = 1.f;
   int key_unused = 0, key2_unused = 0;
   for (;;) {
@@ -1309,7 +1309,7 @@ __global__ void __launch_bounds__(128, 8)
         const uint64_t i = b0 + __popc(need & lanes_below);
         if (i < n) {
           rid = order ? (uint64_t)__ldg(order + i) : i;
-          li = (uint32_t)i;
+          li = i;
           load_ray(rays, i, r);
           h = HitRec{-1, -1, 0.f, 0.f, 0.f};
           hit = false;
