@@ -64,3 +64,56 @@ def test_null_context_is_rejected():
     L = _lib.load()
     assert L.vmr_destroy(None) == -1
     assert L.vmr_sync(None) == -1
+
+
+@pytest.mark.gpu
+def test_contexts_run_concurrently(orc):
+    """One context per host thread (the Go wrapper's goroutine rule): two
+    threads tracing and path tracing at the same time on their own contexts
+    get the results of running alone, bit for bit."""
+    import threading
+
+    import vermeer_gb300 as vg
+    from vermeer_gb300 import scenes
+
+    v, ip = scenes.triangle_soup(50000, 91, edge=0.01)
+    rays = scenes.incoherent_rays(300000, 92)
+    room = scenes.small_room_ext(2048, seed=93)
+
+    def work(ctx):
+        g = ctx.mesh_build(v, ip)
+        hits = ctx.trace_mesh(g, rays)
+        ctx.load_scene(room)
+        img, _ = ctx.render_path(64, 48, 0, 4, 7, max_depth=4)
+        return hits, img
+
+    alone = vg.Context(0)
+    try:
+        ref_hits, ref_img = work(alone)
+    finally:
+        alone.close()
+    ctxs = [vg.Context(0), vg.Context(0)]
+    out = [None, None]
+    errs = []
+
+    def run(k):
+        try:
+            for _ in range(3):
+                out[k] = work(ctxs[k])
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    try:
+        th = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        assert not errs, errs
+        for hits, img in out:
+            for key in ("prim", "t", "u", "v", "w"):
+                assert np.asarray(hits[key]).tobytes() == np.asarray(ref_hits[key]).tobytes(), key
+            assert img.tobytes() == ref_img.tobytes()
+    finally:
+        for c in ctxs:
+            c.close()
