@@ -602,6 +602,13 @@ typedef struct {
 /* He-uniform initial weights from a seed (the output layer scaled by 0.1);
  * resets the optimiser. */
 int vmr_guide_init(vmr_ctx* ctx, uint64_t seed);
+/* Self-test of the kernels' failure path: a one-block kernel waits, with the
+ * guide kernels' bounded mbarrier wait, on a barrier that nothing arrives
+ * at.  The wait runs out (about a quarter of a second), the kernel sets the
+ * error word and returns, and the call reports VMR_ERR_TIMEOUT with the
+ * kernel's duration in *ms (optional); the context stays usable.  Any other
+ * status means the bound did not work as designed. */
+int vmr_selftest_wait(vmr_ctx* ctx, float* ms);
 int vmr_guide_set_weights(vmr_ctx* ctx, const float* weights);
 int vmr_guide_get_weights(vmr_ctx* ctx, float* weights);
 /* The 40 outputs of n vertices (out: n x 40 floats). */

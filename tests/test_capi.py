@@ -117,3 +117,35 @@ def test_contexts_run_concurrently(orc):
     finally:
         for c in ctxs:
             c.close()
+
+
+@pytest.mark.gpu
+def test_bounded_wait_runs_out_and_the_context_stays_usable(orc):
+    """The failure path of the kernels' bounded waits, on purpose: a wait on
+    an mbarrier that nothing arrives at gives up after its bound, the kernel
+    reports through the error word (VMR_ERR_TIMEOUT) and returns; the same
+    context then traces and runs the guide network as before."""
+    import vermeer_gb300 as vg
+    from vermeer_gb300 import scenes
+
+    ctx = vg.Context(0)
+    try:
+        ms = ctypes.c_float()
+        rc = ctx.L.vmr_selftest_wait(ctx.h, ctypes.byref(ms))
+        assert rc == -4, rc  # VMR_ERR_TIMEOUT
+        assert 1.0 < ms.value < 5000.0, ms.value
+        v, ip = scenes.triangle_soup(4096, 94, edge=0.02)
+        rays = scenes.incoherent_rays(8192, 95)
+        g = ctx.mesh_build(v, ip)
+        got = ctx.trace_mesh(g, rays)
+        ref = orc.Mesh(v, ip).trace(rays)
+        assert np.array_equal(got["prim"], ref["prim"])
+        ctx.guide_init(1)
+        rng = np.random.default_rng(96)
+        pos = rng.random((1000, 3)).astype(np.float32)
+        nrm = rng.standard_normal((1000, 3)).astype(np.float32)
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+        out = ctx.guide_forward(pos, nrm, nrm, np.zeros(3, np.float32), np.ones(3, np.float32))
+        assert np.isfinite(np.asarray(out)).all()
+    finally:
+        ctx.close()

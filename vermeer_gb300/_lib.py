@@ -195,6 +195,7 @@ SIGNATURES = {
     "vmr_render_path_jobs": (ctypes.c_int, [P, P, U32, ctypes.POINTER(PathParams), ctypes.POINTER(PathStats)]),
     "vmr_set_path_batch": (ctypes.c_int, [P, U32]),
     "vmr_mesh_set_transform": (ctypes.c_int, [P, U32, P]),
+    "vmr_selftest_wait": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float)]),
     "vmr_get_path_batch": (ctypes.c_int, [P, ctypes.POINTER(U32)]),
     "vmr_autotune_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, P, ctypes.POINTER(U32),
                                          ctypes.POINTER(U32)]),

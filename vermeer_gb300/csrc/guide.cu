@@ -690,6 +690,19 @@ void prepare_kernels() {
   cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgradSmem);
 }
 
+// The failure path of the bounded waits, exercised on purpose: one block
+// waits with bar_wait on an mbarrier that nothing arrives at; the wait runs
+// out after its bound (2^22 polls), the block agrees on the outcome and
+// thread 0 sets the error word, as the guide kernels do before returning.
+// No tensor memory is held.
+__global__ void k_wait_selftest(int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) bar_init(&bar);
+  __syncthreads();
+  const bool ok = bar_wait(&bar, 0u);
+  if (__syncthreads_or(ok ? 0 : 1) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
 int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int grid, cudaStream_t st) {
   k_guide_infer<<<grid, 256, kInferSmem2, st>>>(rows, static_cast<const __nv_bfloat16*>(wf), out, err);
   return (int)cudaGetLastError();
@@ -878,6 +891,28 @@ uint64_t smix(uint64_t z) {
 }  // namespace
 
 extern "C" {
+
+int vmr_selftest_wait(vmr_ctx* ctx, float* ms) {
+  if (!ctx) return VMR_ERR_INVALID;
+  if (ctx->device < 0) return gfail(ctx, VMR_ERR_UNSUPPORTED, "host-only context");
+  cudaSetDevice(ctx->device);
+  int rc = guide_alloc(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->stream;
+  GCUDA(cudaMemsetAsync(ctx->guide.err.p, 0, 4, st));
+  GCUDA(cudaEventRecord(ctx->ev0, st));
+  vmr::guide::k_wait_selftest<<<1, 64, 0, st>>>(ctx->guide.err.as<int>());
+  GCUDA(cudaGetLastError());
+  GCUDA(cudaEventRecord(ctx->ev1, st));
+  int err = 0;
+  GCUDA(cudaMemcpyAsync(&err, ctx->guide.err.p, 4, cudaMemcpyDeviceToHost, st));
+  GCUDA(cudaStreamSynchronize(st));
+  GCUDA(cudaMemsetAsync(ctx->guide.err.p, 0, 4, st));
+  float t = 0.f;
+  cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1);
+  if (ms) *ms = t;
+  return err ? VMR_ERR_TIMEOUT : VMR_OK;
+}
 
 int vmr_guide_init(vmr_ctx* ctx, uint64_t seed) {
   if (!ctx) return VMR_ERR_INVALID;
