@@ -78,8 +78,9 @@ typedef struct {
                             refill, 1..32 (4) */
     int walk_tail;       /* while-while: end a node walk early once at most
                             this many lanes still walk and a lane holds a
-                            static leaf, 0..31 (default 8; 0 = wait for
-                            every lane) */
+                            leaf for the cooperative scan (any leaf with bit
+                            5, a static leaf without it), 0..31 (default 8;
+                            0 = wait for every lane) */
     int sort_bits;       /* sort-key width: the ray reordering groups origins
                             in (2^b)^3 cells, b = 3, 4 or 5 (0: 4) */
 } vmr_tuning;

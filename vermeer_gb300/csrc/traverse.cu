@@ -1004,6 +1004,112 @@ __device__ __forceinline__ int32_t coop_leaf(const float4* tris, float lower, TR
   return idx;
 }
 
+// The cooperative scan over leaves of static and motion meshes (the scene
+// kernel's motion instantiation).  A tester takes its owner's mesh mode with
+// the ray: a static pair is TraceElems' test (trace.go:123-193) on the
+// stored vertices above EpsilonFloat32 + RayBias; a motion pair is
+// TraceMotionElems' (trace.go:563-612) on the vertices of the two keys
+// lerped at the owner's time, Vec3Lerp (math/vec3.go:52-58), above RayBias.
+// Acceptance on the owner in triangle order, as in coop_leaf.  t1, tm, omt
+// are unused by static owners.
+template <int C>
+__device__ __forceinline__ int32_t coop_leaf_mix(const float4* t0, const float4* t1, float tm, float omt, bool mot,
+                                                 float lower, TRay& r, bool has, uint32_t first, uint32_t count,
+                                                 float& U, float& V, float& W) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t cnt = has ? count : 0u;
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= (unsigned)o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  const uint32_t excl = incl - cnt;
+  int32_t idx = -1;
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t g = base + lane;
+    int lo = 0, hi = 31;
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {
+      const int mid = (lo + hi) >> 1;
+      if (__shfl_sync(kFull, incl, mid) > g) hi = mid;
+      else lo = mid + 1;
+    }
+    const int o = lo;
+    const uint32_t i = __shfl_sync(kFull, first, o) + (g - __shfl_sync(kFull, excl, o));
+    TRay q;
+    q.pkx = __shfl_sync(kFull, r.pkx, o);
+    q.pky = __shfl_sync(kFull, r.pky, o);
+    q.pkz = __shfl_sync(kFull, r.pkz, o);
+    q.s0 = __shfl_sync(kFull, r.s0, o);
+    q.s1 = __shfl_sync(kFull, r.s1, o);
+    q.s2 = __shfl_sync(kFull, r.s2, o);
+    if (C < 0) {
+      q.kx = __shfl_sync(kFull, r.kx, o);
+      q.ky = __shfl_sync(kFull, r.ky, o);
+      q.kz = __shfl_sync(kFull, r.kz, o);
+    }
+    const float4* a0 = reinterpret_cast<const float4*>(
+        __shfl_sync(kFull, (unsigned long long)reinterpret_cast<uintptr_t>(t0), o));
+    const float4* a1 = reinterpret_cast<const float4*>(
+        __shfl_sync(kFull, (unsigned long long)reinterpret_cast<uintptr_t>(t1), o));
+    const float otm = __shfl_sync(kFull, tm, o), oomt = __shfl_sync(kFull, omt, o);
+    const bool omot = __shfl_sync(kFull, mot ? 1 : 0, o) != 0;
+    const float olower = __shfl_sync(kFull, lower, o);
+    float fU = 0.f, fV = 0.f, fW = 0.f, det = 0.f, T = 0.f;
+    bool cand = false;
+    if (g < total) {
+      if (omot) {
+        float4 v[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float4 a = __ldg(a0 + 3 * (size_t)i + j), c = __ldg(a1 + 3 * (size_t)i + j);
+          v[j] = make_float4(__fadd_rn(__fmul_rn(oomt, a.x), __fmul_rn(otm, c.x)),
+                             __fadd_rn(__fmul_rn(oomt, a.y), __fmul_rn(otm, c.y)),
+                             __fadd_rn(__fmul_rn(oomt, a.z), __fmul_rn(otm, c.z)), 0.f);
+        }
+        cand = tri_prepare<false, C>(q, v[0], v[1], v[2], olower, fU, fV, fW, det, T);
+      } else {
+        const float4 v0 = __ldg(a0 + 3 * (size_t)i);
+        const float4 v1 = __ldg(a0 + 3 * (size_t)i + 1);
+        const float4 v2 = __ldg(a0 + 3 * (size_t)i + 2);
+        cand = tri_prepare<true, C>(q, v0, v1, v2, olower, fU, fV, fW, det, T);
+      }
+    }
+    unsigned cm = __ballot_sync(kFull, cand);
+    while (cm != 0u) {
+      const int c = __ffs(cm) - 1;
+      cm &= cm - 1u;
+      const int oc = __shfl_sync(kFull, o, c);
+      const float cU = __shfl_sync(kFull, fU, c), cV = __shfl_sync(kFull, fV, c), cW = __shfl_sync(kFull, fW, c);
+      const float cdet = __shfl_sync(kFull, det, c), cT = __shfl_sync(kFull, T, c);
+      const uint32_t ci = __shfl_sync(kFull, i, c);
+      if ((int)lane == oc && tri_accept(r, cU, cV, cW, cdet, cT, U, V, W)) idx = (int32_t)ci;
+    }
+  }
+  return idx;
+}
+
+__device__ __forceinline__ int32_t coop_leaf_mix_dispatch(const float4* t0, const float4* t1, float tm, float omt,
+                                                          bool mot, float lower, TRay& r, bool has, uint32_t first,
+                                                          uint32_t count, float& U, float& V, float& W) {
+  const unsigned hm = __ballot_sync(kFull, has);
+  if (hm == 0u) return -1;
+  const int c0 = __shfl_sync(kFull, r.cls, __ffs(hm) - 1);
+  if (__all_sync(kFull, !has || r.cls == c0)) {
+    switch (c0) {
+      case 0: return coop_leaf_mix<0>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+      case 1: return coop_leaf_mix<1>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+      case 2: return coop_leaf_mix<2>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+      case 3: return coop_leaf_mix<3>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+      case 4: return coop_leaf_mix<4>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+      default: return coop_leaf_mix<5>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+    }
+  }
+  return coop_leaf_mix<-1>(t0, t1, tm, omt, mot, lower, r, has, first, count, U, V, W);
+}
+
 // The class the lanes holding a leaf share picks the compile-time instance;
 // mixed classes take the run-time-select one.  All 32 lanes call this.
 __device__ __forceinline__ int32_t coop_leaf_dispatch(const float4* tris, float lower, TRay& r, bool has,
@@ -1364,9 +1470,10 @@ __global__ void __launch_bounds__(128, 8)
         const unsigned wmask = __ballot_sync(alive_mask, walking);
         if (wmask == 0u) break;
         if (walk_tail > 0 && __popc(wmask) <= walk_tail) {
-          // only a static leaf ends the walk early: a motion leaf is scanned
-          // by its own lane, so a walk cut short for it idles the warp
-          const unsigned leafy = __ballot_sync(alive_mask, !walking && node < -1 && geom >= 0 && !(MOT && mmot));
+          // a leaf for the cooperative scan ends the walk early; without it
+          // (COOP off) a motion leaf is scanned by its own lane, and a walk
+          // cut short for it idles the warp
+          const unsigned leafy = __ballot_sync(alive_mask, !walking && node < -1 && geom >= 0 && !(MOT && mmot && !COOP));
           if (leafy != 0u) break;
         }
         if (!walking) continue;
@@ -1517,13 +1624,30 @@ __global__ void __launch_bounds__(128, 8)
     // ---- leaf phase: a mesh leaf, scanned in the reference's order (COOP:
     // the warp's leaves as one list of triangle tests, all lanes)
     const bool any_leaf = alive && !done && !walking && node < -1 && geom >= 0;
-    const bool has_leaf = any_leaf && !(MOT && mmot);  // static leaves: the cooperative scan (COOP)
     int32_t cidx = -1;
     float cU = 0.f, cV = 0.f, cW = 0.f;
-    if (COOP) {
+    if (COOP && MOT) {  // static and motion leaves in one cooperative list
       uint32_t first = 0, count = 0;
-      if (has_leaf) leaf_decode(node, first, count);
-      cidx = coop_leaf_dispatch(mtris, lower, r, has_leaf, first, count, cU, cV, cW);
+      const float4* t0 = mtris;
+      const float4* t1 = mtris;
+      float tm = 0.f, omt = 1.f, lo = lower;
+      if (any_leaf) {
+        leaf_decode(node, first, count);
+        if (mmot) {
+          const DMesh& M = top.meshes[geom];
+          int key, key2;
+          motion_keys(M.keys, r.time, tm, omt, key, key2);
+          const float4* tr = reinterpret_cast<const float4*>(M.mtris);
+          t0 = tr + (size_t)key * M.n_tris * 3;
+          t1 = tr + (size_t)key2 * M.n_tris * 3;
+          lo = M.ray_bias;
+        }
+      }
+      cidx = coop_leaf_mix_dispatch(t0, t1, tm, omt, any_leaf && mmot, lo, r, any_leaf, first, count, cU, cV, cW);
+    } else if (COOP) {
+      uint32_t first = 0, count = 0;
+      if (any_leaf) leaf_decode(node, first, count);
+      cidx = coop_leaf_dispatch(mtris, lower, r, any_leaf, first, count, cU, cV, cW);
     }
     if (alive) {
       if (any_leaf) {
@@ -1532,7 +1656,9 @@ __global__ void __launch_bounds__(128, 8)
         float U = cU, V = cV, W = cW;
         int32_t idx = cidx;
         int32_t elem = idx;
-        if (MOT && mmot) {  // a motion leaf: vertices lerped at the ray's time, scanned by its lane
+        if (COOP && MOT && mmot) {  // scanned cooperatively: the leaf position to ElemID
+          elem = idx != -1 ? __ldg(top.meshes[geom].elem + idx) : -1;
+        } else if (MOT && mmot) {  // a motion leaf: vertices lerped at the ray's time, scanned by its lane
           const DMesh& M = top.meshes[geom];
           float tm, omt;
           int key, key2;
