@@ -7,6 +7,8 @@
     python -m vermeer_gb300.profile_cases render_ref   reference-mode render, small room,
                                                        256x256, 16 iterations
     python -m vermeer_gb300.profile_cases jobs         64 uneven jobs in one launch
+    python -m vermeer_gb300.profile_cases path_jobs    64 uneven static/motion jobs path traced
+                                                       in one call, 256x256, 2 spp, depth 5
     python -m vermeer_gb300.profile_cases build        device QBVH build of the 1M-triangle soup
 
 Inputs are the seeded synthetic scenes of vermeer_gb300.scenes.
@@ -64,6 +66,21 @@ def jobs(ctx):
     ctx.trace_jobs(js)
 
 
+def path_jobs(ctx):
+    from . import scenes
+    bj = scenes.batched_jobs()
+    ids = [ctx.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_mode=m.get("motion_mode", 0))
+           for m in bj["meshes"]]
+    ctx.set_shaders(bj["shaders"])
+    for g in ids:
+        ctx.mesh_set_shading(g, [0])
+    ctx.set_lights([])
+    ctx.set_quad_lights([])
+    ctx.set_env_light(bj["env"])
+    jobs = [dict(geom=g, width=bj["width"], height=bj["height"], camera=c) for g, c in zip(ids, bj["cameras"])]
+    ctx.render_path_jobs(jobs, 0, 2, 5, max_depth=5)
+
+
 def build(ctx):
     from . import scenes
     from .api import BUILD_DEVICE
@@ -72,7 +89,8 @@ def build(ctx):
     ctx.mesh_build(v, ip)
 
 
-CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "jobs": jobs, "build": build}
+CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "jobs": jobs, "path_jobs": path_jobs,
+         "build": build}
 
 
 def main(argv):
