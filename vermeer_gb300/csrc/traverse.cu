@@ -1210,7 +1210,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
       if (!more) break;
       continue;
     }
-    constexpr bool kCoop = COOP && !MOTION;
+    constexpr bool kCoop = COOP;
     bool done = false, walking = false;
     if (alive) {
       // ---- node phase: one entry per step (a cull-pop, a leaf found, or an
@@ -1310,11 +1310,14 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
         if (COUNT) { cnt.leafs++; cnt.tris += count; }
       }
       float U = 0.f, V = 0.f, W = 0.f;
-      const int32_t idx = coop_leaf_dispatch(reinterpret_cast<const float4*>(m.tris), m.lower_static, r, has, first,
-                                             count, U, V, W);
+      // motion: every tester lerps its owner's two keys at the owner's time
+      const int32_t idx =
+          MOTION ? coop_leaf_mix_dispatch(tr0, tr1, tm, omt, true, m.ray_bias, r, has, first, count, U, V, W)
+                 : coop_leaf_dispatch(reinterpret_cast<const float4*>(m.tris), m.lower_static, r, has, first, count,
+                                      U, V, W);
       if (has) {
         if (idx != -1) {
-          h.elem = idx;
+          h.elem = MOTION ? __ldg(m.elem + idx) : idx;
           h.u = U;
           h.v = V;
           h.w = W;
@@ -1983,7 +1986,7 @@ int launch_persistent_smem(K k, const TraceLaunch& l, int block, size_t smem, A.
 template <bool MOTION, bool ANY, bool COUNT, int MINB>
 int launch_ww(const DMesh& mesh, const TraceLaunch& l, int block) {
   const int tail = l.walk_tail;
-  if (!MOTION && (l.kernel & kKernelCoopLeaf) && !(l.kernel & (kKernelSharedStack | kKernelPrefetch)))
+  if ((l.kernel & kKernelCoopLeaf) && !(l.kernel & (kKernelSharedStack | kKernelPrefetch)))
     return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, 0, true>, l, block, mesh, l.rays, l.hits,
                              l.n, l.scratch, l.order, tail);
   if (l.kernel & kKernelSharedStack) {
