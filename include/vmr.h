@@ -262,11 +262,13 @@ int vmr_trace_scene(vmr_ctx* ctx, const vmr_rays* rays, size_t n, int flags,
 
 /* Batched jobs (no reference counterpart: the reference renders one scene
  * per process).  Each job traces n rays against one mesh, static or motion;
- * all jobs of the call run in a single persistent launch whose warps take
- * 32-ray chunks of any job from one work counter, so jobs of very uneven size
- * share the GPU without one launch each.  Results equal vmr_trace_mesh per
- * job.  Rays and hits are device pointers (the call is asynchronous unless
- * stats is given). */
+ * the jobs' rays are gathered into one stream with a per-ray job index, one
+ * persistent traversal launch (the scene kernel's job mode: each ray enters
+ * its job's mesh directly; the context's tuning) traces them all, and the
+ * hits are scattered back, so jobs of very uneven size share the GPU
+ * without one launch each.  Results equal vmr_trace_mesh per job (a mesh's
+ * transform is not applied, as there).  Rays and hits are device pointers
+ * (the call is asynchronous unless stats is given). */
 typedef struct {
     uint32_t geom;
     uint32_t pad;

@@ -852,7 +852,9 @@ int vmr_trace_jobs(vmr_ctx* ctx, const vmr_trace_job* jobs, uint32_t n_jobs, int
   if (flags & VMR_TRACE_COUNT) return fail(ctx, VMR_ERR_UNSUPPORTED, "vmr_trace_jobs has no visit counters");
   cudaSetDevice(ctx->device);
   std::vector<vmr::JobDesc> t(n_jobs);
-  uint64_t chunks = 0, rays = 0;
+  std::vector<uint32_t> job_geom(n_jobs);
+  uint64_t rays = 0;
+  bool motion = false;
   for (uint32_t j = 0; j < n_jobs; ++j) {
     const vmr_trace_job& J = jobs[j];
     if (J.geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "job geom out of range");
@@ -860,28 +862,66 @@ int vmr_trace_jobs(vmr_ctx* ctx, const vmr_trace_job* jobs, uint32_t n_jobs, int
     const vmr_hits& h = J.hits;
     if (J.n && (!r.px || !r.py || !r.pz || !r.dx || !r.dy || !r.dz || !r.tmax))
       return fail(ctx, VMR_ERR_INVALID, "job rays need px..tmax");
-    t[j].mesh = ctx->meshes[J.geom]->dmesh;
     t[j].rays = vmr::RaySoA{r.px, r.py, r.pz, r.dx, r.dy, r.dz, r.tmax, r.time};
     t[j].hits = vmr::HitSoA{h.prim, h.geom, h.t, h.u, h.v, h.w};
     t[j].n = J.n;
-    t[j].chunk0 = chunks;
-    t[j].geom = (int32_t)J.geom;
-    chunks += (J.n + 31) / 32;
+    t[j].ray0 = rays;
+    job_geom[j] = J.geom;
+    if (ctx->meshes[J.geom]->host.motion()) motion = true;
     rays += J.n;
   }
   if (stats) *stats = vmr_trace_stats{rays, 0, 0, 0, 0.f};
-  if (chunks == 0) return VMR_OK;
-  // The table is read by the launch; a pending launch of an earlier call may
-  // still read the old one, so wait before overwriting it.
+  if (rays == 0) return VMR_OK;
+  // Each job is a mesh trace (qbvh.Trace on its mesh): the table the scene
+  // kernel reads holds the meshes without their transforms.
+  std::vector<DMesh> table(ctx->meshes.size());
+  for (size_t g = 0; g < table.size(); ++g) {
+    table[g] = ctx->meshes[g]->dmesh;
+    table[g].has_xf = 0u;
+  }
+  // Gathered rays (8 floats) and hits (6 words) per ray, the ray -> job
+  // index, the job -> geom table, the job table and the mesh table.
+  const size_t nr = (size_t)rays;
+  const size_t o_rays = 0, o_hits = o_rays + nr * 8 * 4, o_rj = o_hits + nr * 6 * 4, o_jg = o_rj + nr * 4,
+               o_jobs = (o_jg + (size_t)n_jobs * 4 + 255) / 256 * 256,
+               o_tab = (o_jobs + (size_t)n_jobs * sizeof(vmr::JobDesc) + 255) / 256 * 256,
+               bytes = o_tab + table.size() * sizeof(DMesh);
+  // The buffer is read by the launch; a pending launch of an earlier call may
+  // still read it, so wait before overwriting it.
   VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  VMR_CUDA(ctx, ctx->jobs.ensure(t.size() * sizeof(vmr::JobDesc)));
-  VMR_CUDA(ctx, cudaMemcpyAsync(ctx->jobs.p, t.data(), t.size() * sizeof(vmr::JobDesc), cudaMemcpyHostToDevice,
+  VMR_CUDA(ctx, ctx->jobs.ensure(bytes));
+  char* base = ctx->jobs.as<char>();
+  VMR_CUDA(ctx, cudaMemcpyAsync(base + o_jg, job_geom.data(), job_geom.size() * 4, cudaMemcpyHostToDevice,
                                 ctx->stream));
+  VMR_CUDA(ctx, cudaMemcpyAsync(base + o_jobs, t.data(), t.size() * sizeof(vmr::JobDesc), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  VMR_CUDA(ctx, cudaMemcpyAsync(base + o_tab, table.data(), table.size() * sizeof(DMesh), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  float* rf = reinterpret_cast<float*>(base + o_rays);
+  float* hf = reinterpret_cast<float*>(base + o_hits);
+  vmr::JobWork w;
+  w.rays = vmr::RaySoA{rf, rf + nr, rf + 2 * nr, rf + 3 * nr, rf + 4 * nr, rf + 5 * nr, rf + 6 * nr, rf + 7 * nr};
+  w.hits = vmr::HitSoA{reinterpret_cast<int32_t*>(hf), reinterpret_cast<int32_t*>(hf + nr), hf + 2 * nr,
+                       hf + 3 * nr, hf + 4 * nr, hf + 5 * nr};
+  w.ray_job = reinterpret_cast<uint32_t*>(base + o_rj);
+  w.job_geom = reinterpret_cast<uint32_t*>(base + o_jg);
+  DTop top{};
+  top.meshes = reinterpret_cast<const DMesh*>(base + o_tab);
+  top.n_geoms = (uint32_t)table.size();
+  top.keys = 1;
+  top.all_static = motion ? 0u : 1u;
+  const vmr_tuning& tn = ctx->tuning;
+  vmr::TraceLaunch l{};
+  l.any_hit = (flags & VMR_TRACE_ANY_HIT) ? 1 : 0;
+  l.scratch = ctx->scratch.as<DScratch>();
+  l.grid = tn.blocks_per_sm;
+  l.kernel = tn.kernel;
+  l.walk_tail = tn.walk_tail;
+  l.stream = ctx->stream;
   VMR_CUDA(ctx, cudaMemsetAsync(ctx->scratch.p, 0, sizeof(DScratch), ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   VMR_CUDA(ctx, cudaEventRecord(ctx->evm, ctx->stream));
-  const int e = vmr::launch_trace_jobs(ctx->jobs.as<vmr::JobDesc>(), n_jobs, chunks,
-                                       (flags & VMR_TRACE_ANY_HIT) ? 1 : 0, ctx->scratch.as<DScratch>(), ctx->stream);
+  const int e = vmr::launch_trace_jobs(reinterpret_cast<const vmr::JobDesc*>(base + o_jobs), n_jobs, rays, top, w, l);
   if (e != 0) return cuda_fail(ctx, (cudaError_t)e, "jobs kernel launch");
   VMR_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
   if (!stats) return VMR_OK;

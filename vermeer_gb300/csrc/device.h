@@ -171,15 +171,22 @@ int device_sm_count();
 // One job of a batched trace (vmr_trace_jobs): its mesh, rays, hits, and the
 // first 32-ray chunk it owns in the launch's chunk sequence.
 struct JobDesc {
-  DMesh mesh;
   RaySoA rays;
   HitSoA hits;
   uint64_t n;
-  uint64_t chunk0;
-  int32_t geom;
-  int32_t pad;
+  uint64_t ray0;  // the job's first position in the gathered ray stream
 };
-int launch_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_chunks, int any_hit, DScratch* scratch,
-                      void* stream);
+// Gathered rays and hits of a batched trace, the per-ray job index and the
+// job -> geom table (the scene kernel's job mode reads job_geom[ray_job[i]]).
+struct JobWork {
+  RaySoA rays;
+  HitSoA hits;
+  uint32_t* ray_job;
+  uint32_t* job_geom;
+};
+// l: the launch settings (stream, kernel, walk tail, scratch, any_hit); top:
+// the mesh table indexed by geom id (keys = 1, no top level).
+int launch_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_rays, const DTop& top, const JobWork& w,
+                      TraceLaunch l);
 
 }  // namespace vmr

@@ -706,45 +706,52 @@ __global__ void __launch_bounds__(128) k_trace_scene(const DTop top, RaySoA rays
   flush_counters<COUNT>(scratch, cnt);
 }
 
-// Batched jobs: persistent warps take 32-ray chunks of the launch's chunk
-// sequence; a chunk belongs to one job (found by binary search over the
-// jobs' first chunks), so the warp's mesh and its static/motion path are
-// uniform.  Each lane runs the per-ray traversal of its ray.
-template <bool ANY>
-__global__ void __launch_bounds__(128) k_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_chunks,
-                                                    DScratch* scratch) {
-  int2 stk[kStackCapacity];
-  Counters cnt{0, 0, 0};
-  const unsigned lane = threadIdx.x & 31u;
-  int status = kStatusOk;
-  for (;;) {
-    unsigned long long c = 0;
-    if (lane == 0) {
-      c = atomicAdd(&scratch->next_ray, 1ull);
-      if (*reinterpret_cast<volatile int*>(&scratch->status) != kStatusOk) c = n_chunks;
-    }
-    c = __shfl_sync(kFull, c, 0);
-    if (c >= n_chunks) break;
-    uint32_t lo = 0, hi = n_jobs - 1;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) / 2;
-      if (jobs[mid].chunk0 <= c) lo = mid;
-      else hi = mid - 1;
-    }
-    const JobDesc& J = jobs[lo];
-    const uint64_t i = (c - J.chunk0) * 32 + lane;
-    if (i < J.n) {
-      TRay r;
-      load_ray(J.rays, i, r);
-      HitRec h{-1, J.geom, 0.f, 0.f, 0.f};
-      const bool hit = trace_any_mesh<ANY, false>(J.mesh, r, stk, kStackCapacity, h, cnt, status);
-      h.geom = J.geom;
-      store_hit(J.hits, i, r, hit, h);
-      if (status != kStatusOk) {
-        atomicMax(&scratch->status, status);
-        status = kStatusOk;
-      }
-    }
+// Batched jobs (vmr_trace_jobs): the jobs' rays are gathered into one ray
+// stream with a per-ray job index, traced by the scene kernel's job mode
+// (each ray enters its job's mesh directly, in the while-while schedule with
+// the cooperative leaf phase), and the hits are scattered back.  The job of
+// stream position g: the last job whose first ray (ray0) is <= g.
+__device__ __forceinline__ uint32_t job_of(const JobDesc* jobs, uint32_t n_jobs, uint64_t g) {
+  uint32_t lo = 0, hi = n_jobs - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) / 2;
+    if (jobs[mid].ray0 <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_jobs_gather(const JobDesc* jobs, uint32_t n_jobs, uint64_t n, RaySoA out, uint32_t* ray_job) {
+  float* px = const_cast<float*>(out.px);
+  float* py = const_cast<float*>(out.py);
+  float* pz = const_cast<float*>(out.pz);
+  float* dx = const_cast<float*>(out.dx);
+  float* dy = const_cast<float*>(out.dy);
+  float* dz = const_cast<float*>(out.dz);
+  float* tm = const_cast<float*>(out.tmax);
+  float* ti = const_cast<float*>(out.time);
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t j = job_of(jobs, n_jobs, g);
+    const JobDesc& J = jobs[j];
+    const uint64_t i = g - J.ray0;
+    px[g] = J.rays.px[i]; py[g] = J.rays.py[i]; pz[g] = J.rays.pz[i];
+    dx[g] = J.rays.dx[i]; dy[g] = J.rays.dy[i]; dz[g] = J.rays.dz[i];
+    tm[g] = J.rays.tmax[i];
+    ti[g] = J.rays.time ? J.rays.time[i] : 0.0f;
+    ray_job[g] = j;
+  }
+}
+
+__global__ void k_jobs_scatter(const JobDesc* jobs, uint32_t n_jobs, uint64_t n, HitSoA in) {
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
+    const JobDesc& J = jobs[job_of(jobs, n_jobs, g)];
+    const uint64_t i = g - J.ray0;
+    if (J.hits.prim) J.hits.prim[i] = in.prim[g];
+    if (J.hits.geom) J.hits.geom[i] = in.geom[g];
+    if (J.hits.t) J.hits.t[i] = in.t[g];
+    if (J.hits.u) J.hits.u[i] = in.u[g];
+    if (J.hits.v) J.hits.v[i] = in.v[g];
+    if (J.hits.w) J.hits.w[i] = in.w[g];
   }
 }
 
@@ -2054,17 +2061,24 @@ int launch_trace_scene(const DTop& top, const TraceLaunch& l) {
   return l.count ? launch_scene_t<false, true>(top, l) : launch_scene_t<false, false>(top, l);
 }
 
-int launch_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_chunks, int any_hit, DScratch* scratch,
-                      void* stream) {
-  if (n_jobs == 0 || n_chunks == 0) return 0;
-  const int block = 128;
-  if (any_hit) {
-    const int grid = persistent_grid(k_trace_jobs<true>, block);
-    k_trace_jobs<true><<<grid, block, 0, (cudaStream_t)stream>>>(jobs, n_jobs, n_chunks, scratch);
-  } else {
-    const int grid = persistent_grid(k_trace_jobs<false>, block);
-    k_trace_jobs<false><<<grid, block, 0, (cudaStream_t)stream>>>(jobs, n_jobs, n_chunks, scratch);
-  }
+int launch_trace_jobs(const JobDesc* jobs, uint32_t n_jobs, uint64_t n_rays, const DTop& top, const JobWork& w,
+                      TraceLaunch l) {
+  if (n_jobs == 0 || n_rays == 0) return 0;
+  cudaStream_t st = (cudaStream_t)l.stream;
+  const int block = 256;
+  const uint64_t want = (n_rays + block - 1) / block, cap = (uint64_t)device_sm_count() * 16;
+  const int grid = (int)(want < cap ? want : cap);
+  k_jobs_gather<<<grid, block, 0, st>>>(jobs, n_jobs, n_rays, w.rays, w.ray_job);
+  int e = (int)cudaGetLastError();
+  if (e != 0) return e;
+  l.rays = w.rays;
+  l.hits = w.hits;
+  l.n = n_rays;
+  l.ray_path = w.ray_job;
+  l.path_geom = w.job_geom;
+  e = launch_trace_scene(top, l);
+  if (e != 0) return e;
+  k_jobs_scatter<<<grid, block, 0, st>>>(jobs, n_jobs, n_rays, w.hits);
   return (int)cudaGetLastError();
 }
 
