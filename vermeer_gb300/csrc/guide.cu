@@ -189,7 +189,7 @@ constexpr uint32_t kSW0 = 0, kSW1 = kSW0 + 64 * 80 * 2, kSW2 = kSW1 + 8192, kSW3
 constexpr uint32_t kSA0 = kSWEnd, kSA1 = kSA0 + 128 * 80 * 2, kSAEnd = kSA1 + 128 * 64 * 2;  // 77824
 constexpr uint32_t kSB1 = kSAEnd, kSB2 = kSB1 + 8192, kSB3 = kSB2 + 8192, kSB4 = kSB3 + 8192,
                    kSBEnd = kSB4 + 64 * 48 * 2;  // 108544
-constexpr uint32_t kInferSmem = kSAEnd + 64, kTrainSmem = kSBEnd + 64;
+constexpr uint32_t kTrainSmem = kSBEnd + 64;
 
 constexpr int kLobes = 8;
 
