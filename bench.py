@@ -144,6 +144,25 @@ def launches_per_step(ctx, n):
     return 1 + (3 if (t["kernel"] & 8) and n >= (1 << 16) else 0)
 
 
+def max_over_ranks(values, world, device):
+    """The timed durations of a step loop as the job sees them: with N
+    replicas (one rank per GPU, no data-path collective) the slowest rank's
+    (an all-reduce MAX); one rank: unchanged."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_value(units_per_rank_step, steps, world, seconds):
+    """Whole-job throughput in millions of units per second: every rank
+    processes its own units (weak scaling) in the max-over-ranks time."""
+    return units_per_rank_step * steps * world / seconds / 1e6
+
+
 def make_workload():
     from vermeer_gb300 import scenes
     v, ip = scenes.triangle_soup(N_TRIS, SEED)
@@ -264,11 +283,8 @@ def run_gpu(args):
     ctx.sync()
     kernel_ms = [a.elapsed_time(b) for a, b in ev]
     dev_s = sum(kernel_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s, wall], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall = t.tolist()
-    value = N_RAYS * args.steps * world / dev_s / 1e6
+    dev_s, wall = max_over_ranks([dev_s, wall], world, dev)
+    value = job_value(N_RAYS, args.steps, world, dev_s)
     avg_launch_s = sum(traverse_ms) / len(traverse_ms) / 1e3  # dominant kernel
 
     peak, peak_kind = measured_peaks()
@@ -625,13 +641,17 @@ def measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world):
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         e2e_step()
     e2e_s = time.perf_counter() - t0
-    e2e_value = N_RAYS * args.steps * world / e2e_s / 1e6
+    e2e_s = max_over_ranks([e2e_s], world, torch.device("cuda", torch.cuda.current_device()))[0]
+    e2e_value = job_value(N_RAYS, args.steps, world, e2e_s)
     ok = np.array_equal(pin_out["prim"].numpy(), hbuf["prim"])
     return {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 7 * 4,
             "d2h_bytes_per_step": N_RAYS * 5 * 4, "hits_match_device_path": bool(ok)}
