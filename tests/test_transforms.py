@@ -175,3 +175,31 @@ def test_path_render_with_transform_matches_float_oracle(ctx, orc):
     got, _ = ctx.render_path(40, 32, 0, 3, 9, max_depth=4)
     ok = (np.abs(got - ref) <= 1e-5 * (1 + np.abs(ref))).all(-1)
     assert ok.mean() >= 0.995, ok.mean()
+
+
+@pytest.mark.gpu
+def test_path_jobs_with_a_transformed_mesh_equal_one_scene_renders(ctx):
+    """A job whose mesh has a transform renders as that mesh alone in a
+    scene does (the job-mode entry maps the ray as the top-level leaf
+    would), static and motion meshes, bit for bit."""
+    bj = scenes.batched_jobs(n_jobs=4, seed=11, width=32, height=24, lo=800, hi=3000)
+    ids = []
+    for k, m in enumerate(bj["meshes"]):
+        g = ctx.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_mode=m.get("motion_mode", 0))
+        if k < 2:  # one static and one motion job transformed
+            c = np.asarray(m["verts"], np.float32).reshape(-1, 3).mean(0)
+            ctx.mesh_set_transform(g, _matrix(0.4, (1, 1, 0), (1.1, 0.9, 1.0), c, (0.0, 0.01, 0.0)))
+        ids.append(g)
+    ctx.set_shaders(bj["shaders"])
+    for g in ids:
+        ctx.mesh_set_shading(g, [0])
+    ctx.set_lights([])
+    ctx.set_quad_lights([])
+    ctx.set_env_light(bj["env"])
+    jobs = [dict(geom=g, width=32, height=24, camera=bj["cameras"][k]) for k, g in enumerate(ids)]
+    imgs, _ = ctx.render_path_jobs(jobs, 0, 2, 17, max_depth=4)
+    for k, g in enumerate(ids):
+        ctx.scene_build([g])
+        ctx.set_camera(bj["cameras"][k])
+        ref, _ = ctx.render_path(32, 24, 0, 2, 17, max_depth=4)
+        assert imgs[k].tobytes() == ref.tobytes(), k
