@@ -67,6 +67,23 @@ def test_vnf_minimal_scene(tmp_path):
     host_ctx.close()
 
 
+def test_vnf_one_transform_is_loaded(tmp_path):
+    """A PolyMesh Transform of one matrix (rows as written) loads; the
+    accelerator stays the object-space one, as PolyMesh builds it."""
+    text = MINI.replace('  Shader 1 string "white"\n', '  Shader 1 string "white"\n  Transform 1 matrix '
+                        '1 0 0 0.25 0 1 0 0 0 0 1 0 0 0 0 1\n')
+    a, b = vg.Context(-1), vg.Context(-1)
+    try:
+        a.load_vnf(_write(tmp_path, "xf.vnf", text))
+        b.load_vnf(_write(tmp_path, "plain.vnf", MINI))
+        ea, eb = a.mesh_export(0), b.mesh_export(0)
+        for k in ea:
+            assert _same(ea[k], eb[k]), k
+    finally:
+        a.close()
+        b.close()
+
+
 def test_vnf_defaults_without_globals(host_ctx, tmp_path):
     text = MINI.replace("Globals { XRes 32 YRes 16 }", "")
     info = host_ctx.load_vnf(_write(tmp_path, "noglobals.vnf", text))
@@ -77,6 +94,9 @@ def test_vnf_defaults_without_globals(host_ctx, tmp_path):
     (MINI.replace("  Shader 1 string \"white\"\n", ""), INVALID, "required field Shader"),
     (MINI.replace("PolyCount", "PolyCnt"), INVALID, "PolyCnt"),
     (MINI.replace("Globals {", "Proc {"), UNSUPPORTED, "Proc"),
+    (MINI.replace('  Shader 1 string "white"\n', '  Shader 1 string "white"\n  Transform 2 matrix '
+                  '1 0 0 0 0 1 0 0 0 0 1 0 0 0 0 1  1 0 0 0.5 0 1 0 0 0 0 1 0 0 0 0 1\n'),
+     UNSUPPORTED, "transform motion keys"),
     (MINI.replace("rgb 1 1 1", "rgbtex \"wood.tga\""), UNSUPPORTED, "rgbtex"),
     (MINI.replace("\"white\"\n}", "\"black\"\n}"), INVALID, "shader black"),
     (MINI.replace("Name \"camera\"", "Name \"cam2\""), INVALID, "no camera"),
