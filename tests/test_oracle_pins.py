@@ -67,6 +67,19 @@ def test_sobol_02_net(orc):
         assert len(cells) == 1 << k, (a, b)
 
 
+def test_vdc_sobol_histogram_is_flat(orc):
+    """The histogram check of the reference's QMC test (core/qmc_test.go:
+    10-35 bins (RadicalInvVdC(k), RadicalInvSobol(k)) on a grid and writes
+    the counts out): for a power-of-two point count the (0,2)-sequence
+    makes every cell hold the same number of points; here 2^18 points on a
+    256 x 256 grid, 4 per cell."""
+    n, res = 1 << 18, 256
+    x = np.array([orc.vdc(i, 0) for i in range(n)], np.uint64) >> np.uint64(52 - 8)
+    y = np.array([orc.sobol(i, 0) for i in range(n)], np.uint64) >> np.uint64(52 - 8)
+    counts = np.bincount((x + y * np.uint64(res)).astype(np.int64), minlength=res * res)
+    assert counts.min() == counts.max() == 4
+
+
 @pytest.mark.parametrize("m", [3, 5, 12])
 def test_raster_xy_lands_in_pixel(orc, m):
     """RasterXY(m, frame, px, py) returns the frame-th sample of pixel
