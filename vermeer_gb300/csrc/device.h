@@ -168,8 +168,8 @@ int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int b
 int launch_trace_scene(const DTop& top, const TraceLaunch& l);
 int device_sm_count();
 
-// One job of a batched trace (vmr_trace_jobs): its mesh, rays, hits, and the
-// first 32-ray chunk it owns in the launch's chunk sequence.
+// One job of a batched trace (vmr_trace_jobs): its rays and hits (device
+// SoA, its own buffers) and its first position in the gathered ray stream.
 struct JobDesc {
   RaySoA rays;
   HitSoA hits;

@@ -19,9 +19,16 @@
 // next stays in registers instead of a stack round trip.
 //
 // Execution model: persistent warps (grid = SMs x resident blocks) pull
-// 32-ray batches from a global counter with one atomic per warp; each lane
-// owns one ray and a private stack in local memory (L1-resident, interleaved
-// per lane by the hardware so same-depth accesses coalesce).
+// rays from a global counter with one warp-aggregated atomic per refill;
+// each lane owns one ray and a private stack in local memory (L1-resident,
+// interleaved per lane by the hardware so same-depth accesses coalesce).
+// The while-while kernels alternate a warp-synchronous node walk with a
+// leaf phase in which the warp scans all its lanes' leaves as one list of
+// (ray, triangle) tests.  Kernels: k_trace_mesh_ww (one mesh, static or
+// motion), k_trace_scene_ww (two-level scenes, and job mode: each ray enters
+// its own mesh), k_trace_mesh_sched and k_trace_scene (the step-scheduled
+// and single-loop kernels the tuning can select), k_jobs_gather and
+// k_jobs_scatter (vmr_trace_jobs).
 #include <cuda_runtime.h>
 
 #include "device.h"
