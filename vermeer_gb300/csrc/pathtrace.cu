@@ -8,16 +8,25 @@
 // pixel)):
 //   k_pt_generate            camera rays (the reference mode's) into queue 0
 //   for d = 0 .. max_depth:
+//     [ray sort]             VMR_PATH_SORT_QUEUES, d > 0: queue d in key order
 //     trace                  closest hit of queue d (count read on the device)
+//     [k_pt_prep, guide]     guided vertices (d < guide_depth): network rows
+//                            and the tcgen05 inference over the queue
 //     k_pt_shade<d>          emission / environment with MIS, light sample +
 //                            shadow ray into the shadow queue, BSDF sample +
 //                            continuation into queue d+1 (warp-aggregated
 //                            appends), Russian roulette
-//     trace (d < max_depth)  any hit of the shadow queue
+//     trace (d < max_depth)  any hit of the shadow queue (sorted first with
+//                            VMR_PATH_SORT_QUEUES)
 //     k_pt_resolve           unoccluded shadow rays add their contribution
 //   k_pt_accumulate          per pixel, the batch's iterations in order:
 //                            buf = (buf*i + L)/(i+1), i the 0-based iteration
 //                            (float, optional float64)
+//   [k_pt_targets, training] VMR_PATH_TRAIN: the guide's records and Adam steps
+// A batch holds the context's queue capacity (8M paths by default,
+// vmr_set_path_batch / vmr_autotune_path).  Batched jobs put many one-mesh
+// images end to end in one pixel arena; their rays enter their own mesh
+// (the scene kernels' job mode).
 // Every queue length lives in device memory and every kernel reads it there,
 // so a batch runs without host synchronisation; the whole sequence is
 // captured once as a CUDA graph and replayed per batch (the batch's first
