@@ -632,19 +632,22 @@ int vmr_guide_train_step(vmr_ctx* ctx, const float* pos, const float* nrm, const
 /* No counterpart in the reference.  For callers that must not have a library
  * allocate device memory while they run (they manage the whole device
  * themselves, or cannot afford an allocation's synchronisation in their
- * loop): the same trace as vmr_trace_mesh with device pointers, but every
- * scratch buffer (work counter, status word, ray-reordering buffers) lives in
- * one static device array of about 10 MB, present on every GPU that loads
- * libvmr until the process exits.  The call allocates nothing.
- *   - rays and hits are device pointers; at most VMR_NOALLOC_MAX_RAYS rays per
- *     call (larger batches fail with VMR_ERR_INVALID); flags may hold only
- *     VMR_TRACE_ANY_HIT and VMR_TRACE_DEVICE;
- *   - the first call on a device looks up the array's device address, so make
- *     that first call before any stream capture;
+ * loop): the same trace as vmr_trace_mesh with device pointers (the mesh's
+ * own tuning, autotuned or the context's), but every scratch buffer (work
+ * counter, status word, ray-reordering buffers) lives in one static device
+ * array of about 11 MB that stays on the GPU until the process exits.
+ * vmr_create resolves that array on its device (this is where the array is
+ * loaded onto the GPU); the call itself allocates nothing.
+ *   - flags must hold VMR_TRACE_DEVICE (rays and hits are device or managed
+ *     memory; anything else fails with VMR_ERR_INVALID before any launch) and
+ *     may add VMR_TRACE_ANY_HIT;
+ *   - at most VMR_NOALLOC_MAX_RAYS rays per call (larger batches fail with
+ *     VMR_ERR_INVALID);
  *   - all calls share the one array: calls that overlap on the GPU (other
  *     host threads, other streams, other contexts of the process on the same
  *     device) race and corrupt each other's results;
- *   - the call returns when the trace has finished. */
+ *   - the call waits on the context's stream and returns when the trace has
+ *     finished. */
 #define VMR_NOALLOC_MAX_RAYS 262144
 int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags,
                            const vmr_hits* hits);

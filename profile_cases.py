@@ -1,15 +1,15 @@
 """Named workloads for kernel profiling (each runs once and exits 0):
 
-    python -m vermeer_gb300.profile_cases guide        guide inference on 1M vertices
+    python profile_cases.py guide        guide inference on 1M vertices
                                                        and one training step of 256K
-    python -m vermeer_gb300.profile_cases render_ext   extended path tracer, sphere grid,
+    python profile_cases.py render_ext   extended path tracer, sphere grid,
                                                        1920x1080, 2 spp, depth 8
-    python -m vermeer_gb300.profile_cases render_ref   reference-mode render, small room,
+    python profile_cases.py render_ref   reference-mode render, small room,
                                                        256x256, 16 iterations
-    python -m vermeer_gb300.profile_cases jobs         64 uneven jobs in one launch
-    python -m vermeer_gb300.profile_cases path_jobs    64 uneven static/motion jobs path traced
+    python profile_cases.py jobs         64 uneven jobs in one launch
+    python profile_cases.py path_jobs    64 uneven static/motion jobs path traced
                                                        in one call, 256x256, 2 spp, depth 5
-    python -m vermeer_gb300.profile_cases build        device QBVH build of the 1M-triangle soup
+    python profile_cases.py build        device QBVH build of the 1M-triangle soup
 
 Inputs are the seeded synthetic scenes of vermeer_gb300.scenes.
 """

@@ -426,10 +426,11 @@ bool ctx_noalloc_view(vmr_ctx* ctx, uint32_t geom, const DMesh** mesh, const flo
   *bounds = ctx->meshes[geom]->bounds6;
   *stream = ctx->stream;
   *device = ctx->device;
-  *tuning = ctx->tuning;
+  *tuning = ctx->tuning_for(*mesh);
   return ctx->meshes[geom]->host.n_tris > 0;
 }
 int ctx_fail(vmr_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
+int noalloc_setup(int device);  // noalloc.cu
 }  // namespace vmr
 
 extern "C" {
@@ -460,6 +461,10 @@ int vmr_create(int device, vmr_ctx** out) {
     return VMR_ERR_CUDA;
   }
   ctx->stream = ctx->own_stream;
+  // Load vmr_trace_mesh_noalloc's static scratch array on this device now, so
+  // that the no-alloc call itself never triggers a module load.  A failure
+  // here is reported by that call, not by vmr_create.
+  vmr::noalloc_setup(device);
   *out = ctx;
   return VMR_OK;
 }

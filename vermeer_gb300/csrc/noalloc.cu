@@ -7,8 +7,10 @@
 // context grows its ray-reordering buffers to the largest batch seen.  This
 // entry point runs the same reordering and traversal kernels on a fixed
 // scratch area instead: one file-scope device array, sized for
-// VMR_NOALLOC_MAX_RAYS rays and loaded with the library on every GPU that
-// uses it, where it stays until the process exits.
+// VMR_NOALLOC_MAX_RAYS rays and a histogram of any key width, where it stays
+// until the process exits.  vmr_create resolves the array's device address
+// for its device (noalloc_setup below), which is where the array is loaded
+// onto that GPU; the entry point itself only reads the cached address.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -20,16 +22,17 @@ namespace vmr {
 bool ctx_noalloc_view(vmr_ctx* ctx, uint32_t geom, const DMesh** mesh, const float** bounds, void** stream,
                       int* device, vmr_tuning* tuning);
 int ctx_fail(vmr_ctx* ctx, int code, const char* msg);
+int noalloc_setup(int device);
 }  // namespace vmr
 
 namespace {
 
 constexpr size_t kMaxRays = VMR_NOALLOC_MAX_RAYS;
-// Layout: work counter / status / visit counters, bucket histogram, ray keys,
-// order, key-ordered rays (8 float fields).  Every part starts on a 256-byte
-// boundary.
+// Layout: work counter / status / visit counters, bucket histogram (sized for
+// the widest sort key a tuning may select), ray keys, order, key-ordered rays
+// (8 float fields).  Every part starts on a 256-byte boundary.
 constexpr size_t kHeaderBytes = 256;
-constexpr size_t kHistBytes = ((sizeof(uint32_t) * vmr::kSortBuckets + 255) / 256) * 256;
+constexpr size_t kHistBytes = ((sizeof(uint32_t) * vmr::kSortBucketsMax + 255) / 256) * 256;
 constexpr size_t kKeyBytes = sizeof(uint32_t) * kMaxRays;
 constexpr size_t kOrderBytes = sizeof(uint32_t) * kMaxRays;
 constexpr size_t kRayBytes = sizeof(float) * 8 * kMaxRays;
@@ -42,9 +45,9 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
 
-// The device address of g_noalloc_scratch on the current device (resolved on
-// the first call for that device; host code only sees a stand-in for the
-// symbol, never its device address).
+// The device address of g_noalloc_scratch on the current device.  Host code
+// only sees a stand-in for the symbol, never its device address, so the
+// address is looked up once per device with that device current.
 cudaError_t scratch_address(int device, unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_setup_mu);
   if (!g_scratch_addr[device]) {
@@ -57,11 +60,51 @@ cudaError_t scratch_address(int device, unsigned char** out) {
   return cudaSuccess;
 }
 
+unsigned char* cached_address(int device) {
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  return g_scratch_addr[device];
+}
+
+// True when p is memory the GPU addresses directly (device or managed).
+bool device_pointer(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
 }  // namespace
+
+namespace vmr {
+// Called by vmr_create with the context's device current: resolves (and so
+// loads) the scratch array on that device.  Returns the CUDA error, 0 on
+// success; a failure leaves later no-alloc calls on the device to report it.
+int noalloc_setup(int device) {
+  if (device < 0 || device >= kMaxDevices) return 0;
+  unsigned char* base = nullptr;
+  const cudaError_t e = scratch_address(device, &base);
+  if (e != cudaSuccess) cudaGetLastError();
+  return (int)e;
+}
+}  // namespace vmr
 
 extern "C" int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, int flags,
                                       const vmr_hits* hits) {
   if (!ctx || !rays || !hits) return VMR_ERR_INVALID;
+  // Checked before anything touches the GPU: the kernels read rays and write
+  // hits in place, so host arrays must never reach them.
+  if (!(flags & VMR_TRACE_DEVICE))
+    return vmr::ctx_fail(ctx, VMR_ERR_INVALID,
+                         "vmr_trace_mesh_noalloc: rays and hits must be device pointers; set VMR_TRACE_DEVICE");
+  if (flags & ~(VMR_TRACE_ANY_HIT | VMR_TRACE_DEVICE))
+    return vmr::ctx_fail(ctx, VMR_ERR_INVALID, "vmr_trace_mesh_noalloc: only VMR_TRACE_ANY_HIT and VMR_TRACE_DEVICE");
+  if (n > kMaxRays)
+    return vmr::ctx_fail(ctx, VMR_ERR_INVALID,
+                         "vmr_trace_mesh_noalloc: batch larger than VMR_NOALLOC_MAX_RAYS (262144 rays); "
+                         "split it or use vmr_trace_mesh");
   const vmr::DMesh* mesh = nullptr;
   const float* bounds = nullptr;
   void* stream = nullptr;
@@ -69,19 +112,23 @@ extern "C" int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_ray
   vmr_tuning tuning{};
   if (!vmr::ctx_noalloc_view(ctx, geom, &mesh, &bounds, &stream, &device, &tuning))
     return vmr::ctx_fail(ctx, VMR_ERR_INVALID, "vmr_trace_mesh_noalloc: bad geom id, empty mesh or host-only context");
-  if (n > kMaxRays)
-    return vmr::ctx_fail(ctx, VMR_ERR_INVALID,
-                         "vmr_trace_mesh_noalloc: batch larger than VMR_NOALLOC_MAX_RAYS (262144 rays); "
-                         "split it or use vmr_trace_mesh");
-  if (flags & ~(VMR_TRACE_ANY_HIT | VMR_TRACE_DEVICE))
-    return vmr::ctx_fail(ctx, VMR_ERR_INVALID, "vmr_trace_mesh_noalloc: only VMR_TRACE_ANY_HIT and VMR_TRACE_DEVICE");
   if (device >= kMaxDevices) return vmr::ctx_fail(ctx, VMR_ERR_UNSUPPORTED, "vmr_trace_mesh_noalloc: device >= 64");
   if (n == 0) return VMR_OK;
-  cudaError_t e = cudaSetDevice(device);
-  unsigned char* base = nullptr;
-  if (e == cudaSuccess) e = scratch_address(device, &base);
-  if (e != cudaSuccess)
-    return vmr::ctx_fail(ctx, VMR_ERR_CUDA, "vmr_trace_mesh_noalloc: cannot resolve the scratch address");
+  if (cudaSetDevice(device) != cudaSuccess)
+    return vmr::ctx_fail(ctx, VMR_ERR_CUDA, "vmr_trace_mesh_noalloc: cannot select the context's device");
+  const void* ptrs[14] = {rays->px, rays->py, rays->pz, rays->dx, rays->dy, rays->dz, rays->tmax, rays->time,
+                          hits->prim, hits->geom, hits->t, hits->u, hits->v, hits->w};
+  for (const void* p : ptrs)
+    if (!device_pointer(p))
+      return vmr::ctx_fail(ctx, VMR_ERR_INVALID,
+                           "vmr_trace_mesh_noalloc: a ray or hit array is not device memory");
+  if (!rays->px || !rays->py || !rays->pz || !rays->dx || !rays->dy || !rays->dz || !rays->tmax)
+    return vmr::ctx_fail(ctx, VMR_ERR_INVALID, "vmr_trace_mesh_noalloc: null ray array");
+  unsigned char* base = cached_address(device);
+  if (!base)
+    return vmr::ctx_fail(ctx, VMR_ERR_CUDA,
+                         "vmr_trace_mesh_noalloc: the scratch array could not be resolved when the context was created");
+  cudaError_t e = cudaSuccess;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   auto* scratch = reinterpret_cast<vmr::DScratch*>(base);
   auto* hist = reinterpret_cast<uint32_t*>(base + kHeaderBytes);
@@ -109,7 +156,10 @@ extern "C" int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_ray
   if ((tuning.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
     const vmr::RaySoA sorted{f, f + kMaxRays, f + 2 * kMaxRays, f + 3 * kMaxRays, f + 4 * kMaxRays,
                              f + 5 * kMaxRays, f + 6 * kMaxRays, rays->time ? f + 7 * kMaxRays : nullptr};
-    if (vmr::launch_ray_sort(l.rays, n, bounds, 4, keys, hist, order, sorted, stream) != 0)
+    const int bits = tuning.sort_bits ? tuning.sort_bits : 4;
+    if (bits > vmr::kSortMaxBits)
+      return vmr::ctx_fail(ctx, VMR_ERR_INVALID, "vmr_trace_mesh_noalloc: sort key wider than the histogram");
+    if (vmr::launch_ray_sort(l.rays, n, bounds, bits, keys, hist, order, sorted, stream) != 0)
       return vmr::ctx_fail(ctx, VMR_ERR_CUDA, "vmr_trace_mesh_noalloc: ray reordering launch failed");
     l.rays = sorted;
     l.order = order;
