@@ -202,6 +202,41 @@ int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n_geoms);
  * of every other transformed mesh the ray enters (a leak across geoms).
  * Analytic spheres take no transform.  Takes effect in the scene at once. */
 int vmr_mesh_set_transform(vmr_ctx* ctx, uint32_t geom, const float* m);
+/* PolyMesh.Transform with motion keys (builtin/geom/polymesh/init.go:14-16,
+ * trace.go:33-48): n_keys column-major 4x4 matrices.  One key is
+ * vmr_mesh_set_transform; with two or more each key is decomposed
+ * (TransformDecompMatrix4, math/animdecomp.go:20-62) and a scene trace
+ * entering the mesh blends the keys around the ray's time
+ * (TransformDecompLerp, animdecomp.go:74-80), rebuilds the matrix
+ * (TransformDecompToMatrix4) and maps the ray by its Matrix4Inverse; renders
+ * take that matrix for the hit.  Scenes holding such a mesh are traced by
+ * the single-loop scene kernel; the extended path tracer and batched jobs do
+ * not take them.  n_keys = 0 removes the transform. */
+int vmr_mesh_set_transform_keys(vmr_ctx* ctx, uint32_t geom, const float* keys16, uint32_t n_keys);
+
+/* GeomInstance (builtin/geom/instance/instance.go:40-160): a new geom that
+ * traces geom `of` (a mesh or sphere, itself also a geom of the scene or not)
+ * through n_keys transform keys.  Every key is decomposed, and a ray's
+ * transform is TransformSRTArray.TimeKey's (one key as it is, else the keys
+ * around the ray's time blended), rebuilt, inverted (Matrix4Inverse); the
+ * ray is mapped and re-set-up, the geom traced (through its own transform
+ * too), the world ray restored.  bmin/bmax: the instance's bounds at every
+ * time (BMin/BMax of key 0, instance.go:64-68); its motion keys for the top
+ * level are the instanced geom's (instance.go:144-148).  Hits report the
+ * instance's id (vmr_trace_scene's geom) and shade as the instanced geom with
+ * the instance's transform applied to the shading context (P = T Po with Po
+ * the hit point in instance space, normals by T^-T, as core.Trace's
+ * ApplyTransform).  Instances of instances or Procs are not supported. */
+int vmr_instance_add(vmr_ctx* ctx, uint32_t of, const float* keys16, uint32_t n_keys, const float bmin[3],
+                     const float bmax[3], uint32_t* out_geom);
+/* Proc (builtin/geom/proc/proc.go:50-190): a new geom holding n child geoms
+ * (meshes or spheres made for it: they join no scene themselves), traced in
+ * order through the Proc's transform keys (n_keys 0: the identity, as
+ * Proc.PreRender sets); a closest-hit ray stops at the first child that hits
+ * (proc.go:117-124), a shadow ray goes on.  A hit reports the child's id.
+ * Its motion keys for the top level are its transform keys. */
+int vmr_proc_add(vmr_ctx* ctx, const uint32_t* children, uint32_t n, const float* keys16, uint32_t n_keys,
+                 const float bmin[3], const float bmax[3], uint32_t* out_geom);
 /* Caller-built top level: static nodes, or motion nodes + boxes; geom_order
  * maps leaf position -> geom id. */
 int vmr_scene_upload(vmr_ctx* ctx, const vmr_qbvh_node* nodes, uint32_t n_nodes,
@@ -299,7 +334,11 @@ enum {
     VMR_SH_EMISSION_COLOUR = 1, VMR_SH_EMISSION_STRENGTH = 2,
     VMR_SH_DIFFUSE_COLOUR = 4, VMR_SH_DIFFUSE_STRENGTH = 8, VMR_SH_DIFFUSE_ROUGHNESS = 16,
     VMR_SH_SPEC1_COLOUR = 32, VMR_SH_SPEC1_STRENGTH = 64, VMR_SH_SPEC1_ROUGHNESS = 128,
-    VMR_SH_FRESNEL_REFL = 256, VMR_SH_FRESNEL_EDGE = 512, VMR_SH_IOR = 1024
+    VMR_SH_FRESNEL_REFL = 256, VMR_SH_FRESNEL_EDGE = 512, VMR_SH_IOR = 1024,
+    /* DebugShader (builtin/shader/debug.go:16-57) instead of ShaderStd: the
+     * surface's colour is diffuse_colour (Colour) and nothing else (no
+     * lights, no emission); reference mode (vmr_render) only */
+    VMR_SH_DEBUG = 2048
 };
 typedef struct {
     uint32_t flags;
@@ -375,7 +414,25 @@ int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, u
 int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n);
 int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n);
 int vmr_set_sphere_lights(vmr_ctx* ctx, const vmr_sphere_light* lights, uint32_t n);
+/* The camera (Camera node, builtin/camera/camera.go): m is LocalToWorld.  As
+ * the reference does, the ray is made with the matrix rebuilt from m's
+ * decomposition (TransformDecompMatrix4, then TransformDecompToMatrix4 of
+ * TransformDecompLerp of that key with itself, camera.go:207-236), which is
+ * close to m but not equal to it. */
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* camera);
+/* Camera motion keys: LocalToWorld as n_keys column-major 4x4 matrices
+ * (after vmr_set_camera, whose other fields stay).  Each key is decomposed;
+ * a sample at time t (the VdC time of core/render.go:94) takes
+ * k = t*(n-1) and blends keys floor(k), ceil(k) at k - floor(k)
+ * (camera.go:223-236).  vmr_get_camera returns key 0 in m. */
+int vmr_set_camera_keys(vmr_ctx* ctx, const float* keys16, uint32_t n_keys);
+/* The matrix libvmr uses for n_keys transform keys at a time: each key
+ * decomposed (TransformDecompMatrix4), the keys around time blended
+ * (TransformDecompLerp), the matrix rebuilt (TransformDecompToMatrix4); one
+ * key is rebuilt as it is unless blend_one (the camera blends it with
+ * itself).  Host-side, needs no context or GPU; VMR_ERR_INVALID if time
+ * falls outside the keys. */
+int vmr_transform_keys_at(const float* keys16, uint32_t n_keys, float time, int blend_one, float* out16);
 
 /* Pixel filters for filter importance sampling: replaces core.Init of a
  * PixelFilter node (core/core.go:88-89, core/pixelfilter.go:8-10) with the

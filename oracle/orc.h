@@ -114,7 +114,8 @@ enum {
     ORC_SH_EMISSION_COLOUR = 1, ORC_SH_EMISSION_STRENGTH = 2,
     ORC_SH_DIFFUSE_COLOUR = 4, ORC_SH_DIFFUSE_STRENGTH = 8, ORC_SH_DIFFUSE_ROUGHNESS = 16,
     ORC_SH_SPEC1_COLOUR = 32, ORC_SH_SPEC1_STRENGTH = 64, ORC_SH_SPEC1_ROUGHNESS = 128,
-    ORC_SH_FRESNEL_REFL = 256, ORC_SH_FRESNEL_EDGE = 512, ORC_SH_IOR = 1024
+    ORC_SH_FRESNEL_REFL = 256, ORC_SH_FRESNEL_EDGE = 512, ORC_SH_IOR = 1024,
+    ORC_SH_DEBUG = 2048  /* DebugShader (builtin/shader/debug.go): OutRGB = diffuse_colour */
 };
 typedef struct {
     uint32_t flags;
@@ -235,6 +236,35 @@ float orc_pt_rnd(uint64_t seed, uint64_t pix, uint32_t j, uint32_t dim);
 /* PolyMesh.Transform of a mesh (column-major 4x4, NULL: none); scenes and
  * renders created after the call see it. */
 void orc_mesh_set_transform(orc_mesh* m, const float* xf);
+/* PolyMesh.Transform of n keys (16 floats each): one key is the matrix as
+ * it is; two or more are decomposed and blended at each ray's time
+ * (builtin/geom/polymesh/trace.go:33-48). */
+void orc_mesh_set_transform_keys(orc_mesh* m, const float* keys16, uint32_t n);
+/* GeomInstance (builtin/geom/instance/instance.go): a geom tracing `of`
+ * through n_keys transform keys (always decomposed, TimeKey), with the given
+ * bounds (BMin/BMax of key 0).  Its hits report the instance's own id. */
+orc_mesh* orc_instance_create(const orc_mesh* of, const float* keys16, uint32_t n_keys, const float bmin[3],
+                              const float bmax[3]);
+/* Proc (builtin/geom/proc/proc.go) holding n child geoms (meshes or
+ * spheres, traced in order); a hit in child i reports child_ids[i].  n_keys
+ * 0 means the identity (Proc.PreRender). */
+orc_mesh* orc_proc_create(orc_mesh* const* children, const int32_t* child_ids, uint32_t n, const float* keys16,
+                          uint32_t n_keys, const float bmin[3], const float bmax[3]);
+/* orc_scene_create whose hits report ids[i] for meshes[i] (default i). */
+orc_scene* orc_scene_create_ids(orc_mesh* const* meshes, const int32_t* ids, uint32_t n);
+/* TransformDecompMatrix4 of a matrix: out = T[3], R[4] (x y z w), S[16]. */
+void orc_decompose(const float* m, float* trs23);
+/* The keyed transform at a time (keys decomposed, blended, rebuilt);
+ * blend_one: blend a single key with itself as Camera.ComputeRay does. */
+int orc_keyed_matrix(const float* keys16, uint32_t n, float time, int blend_one, float* out16);
+/* Camera.LocalToWorld keys of a render (decomposed; camera.go:207-236).
+ * orc_render_create decomposes the camera's m as the single key. */
+int orc_render_set_camera_keys(orc_render* r, const float* keys16, uint32_t n);
+/* Vec3Normalize in the reference-mode renderer: 0 exact (default), 1 an
+ * emulation of the RSQRTSS estimate plus Newton step of
+ * math/vec3_amd64.s:11-42, the estimate's error drawn from a hash of the
+ * input and seed within the documented 1.5*2^-12 bound.  Process-wide. */
+void orc_set_normalize_mode(int mode, uint64_t seed);
 /* sin and cos of 2*pi*u[i] (u in [0, 1)) in the float32 operations of the
  * extended path tracer's sampling. */
 void orc_sincos_turns(const float* u, size_t n, float* s, float* c);

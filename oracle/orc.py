@@ -76,6 +76,19 @@ def lib():
                                     ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_double)]
         L.orc_vdc_sobol_tables.argtypes = [ctypes.c_uint32, P, P]
+        L.orc_scene_create_ids.restype = P
+        L.orc_scene_create_ids.argtypes = [P, P, ctypes.c_uint32]
+        L.orc_mesh_set_transform_keys.argtypes = [P, P, ctypes.c_uint32]
+        L.orc_instance_create.restype = P
+        L.orc_instance_create.argtypes = [P, P, ctypes.c_uint32, P, P]
+        L.orc_proc_create.restype = P
+        L.orc_proc_create.argtypes = [P, P, ctypes.c_uint32, P, ctypes.c_uint32, P, P]
+        L.orc_decompose.argtypes = [P, P]
+        L.orc_keyed_matrix.restype = ctypes.c_int
+        L.orc_keyed_matrix.argtypes = [P, ctypes.c_uint32, ctypes.c_float, ctypes.c_int, P]
+        L.orc_render_set_camera_keys.restype = ctypes.c_int
+        L.orc_render_set_camera_keys.argtypes = [P, P, ctypes.c_uint32]
+        L.orc_set_normalize_mode.argtypes = [ctypes.c_int, ctypes.c_uint64]
         _register_render(L)
         _lib = L
     return _lib
@@ -115,6 +128,34 @@ class OrcCamera(ctypes.Structure):
 _SH_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
              "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
              "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
+_SH_DEBUG = 2048  # DebugShader: {"debug": True, "diffuse_colour": Colour}
+
+
+def _keys16(keys):
+    a = np.ascontiguousarray(keys, np.float32).reshape(-1, 16)
+    return a, a.shape[0]
+
+
+def decompose(m):
+    """TransformDecompMatrix4 of a column-major 4x4: (T[3], R[4] xyzw, S[16])."""
+    out = np.zeros(23, np.float32)
+    lib().orc_decompose(_ptr(np.ascontiguousarray(m, np.float32).reshape(16)), _ptr(out))
+    return out[:3], out[3:7], out[7:]
+
+
+def keyed_matrix(keys, time, blend_one=False):
+    """The decomposed keys blended at time and rebuilt (column-major 16)."""
+    a, n = _keys16(keys)
+    out = np.zeros(16, np.float32)
+    if lib().orc_keyed_matrix(_ptr(a), n, float(time), int(bool(blend_one)), _ptr(out)) != 0:
+        raise ValueError("time outside the keys")
+    return out
+
+
+def set_normalize_mode(mode, seed=0):
+    """Vec3Normalize of the reference-mode renderer: 0 exact, 1 the RSQRTSS
+    emulation (process-wide)."""
+    lib().orc_set_normalize_mode(int(mode), int(seed))
 
 
 def _register_render(L):
@@ -286,19 +327,8 @@ class Render:
     (vermeer_gb300.scenes format)."""
 
     def __init__(self, scene):
-        self.meshes = []
-        for m in scene["meshes"]:
-            if "sphere" in m:
-                self.meshes.append(Sphere(m["sphere"][:3], m["sphere"][3]))
-                continue
-            om = Mesh(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_fixed=m.get("motion_mode", 0) == 1)
-            fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
-            nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
-            lib().orc_mesh_set_shading(om.h, _ptr(fs), _ptr(nr))
-            if m.get("transform") is not None:
-                om.set_transform(m["transform"])
-            self.meshes.append(om)
-        self.scene = Scene(self.meshes)
+        self.meshes = build_geoms(scene["meshes"])
+        self.scene = scene_of(scene["meshes"], self.meshes)
         counts = np.asarray([len(m["shaders"]) for m in scene["meshes"]], np.uint32)
         offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32)
         lst = np.asarray([s for m in scene["meshes"] for s in m["shaders"]], np.uint32)
@@ -313,7 +343,7 @@ class Render:
                     else:
                         for c in range(3):
                             getattr(shs[i], k)[c] = float(d[k][c])
-            shs[i].flags = fl
+            shs[i].flags = fl | (_SH_DEBUG if d.get("debug") else 0)
             shs[i].spec1_fresnel = 1 if d.get("spec1_fresnel") == "Metal" else 0
         lts = (OrcTriLight * len(scene["lights"]))()
         for i, d in enumerate(scene["lights"]):
@@ -339,6 +369,9 @@ class Render:
         self._keep = (counts, offs, lst, shs, lts, cam, arr)
         self.h = lib().orc_render_create(self.scene.h, arr, len(self.meshes), _ptr(offs), _ptr(counts), _ptr(lst),
                                          shs, len(scene["shaders"]), lts, len(scene["lights"]), ctypes.byref(cam))
+        if scene["camera"].get("keys") is not None:
+            self._cam_keys, nk = _keys16(scene["camera"]["keys"])
+            lib().orc_render_set_camera_keys(self.h, _ptr(self._cam_keys), nk)
         dls = scene.get("disk_lights", [])
         if dls:
             darr = (OrcDiskLight * len(dls))()
@@ -399,6 +432,80 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+def build_geoms(entries):
+    """Oracle geoms for a scene's mesh list (vermeer_gb300.scenes format):
+    meshes (optionally 'transform' or 'transform_keys'), spheres, instances
+    ({'instance': i, 'keys', 'bmin', 'bmax'}) and Procs ({'proc': [child
+    indices], 'keys' (optional), 'bmin', 'bmax'}); entry i reports id i."""
+    geoms = [None] * len(entries)
+    for i, m in enumerate(entries):
+        if "sphere" in m:
+            geoms[i] = Sphere(m["sphere"][:3], m["sphere"][3])
+        elif "verts" in m:
+            om = Mesh(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_fixed=m.get("motion_mode", 0) == 1)
+            fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
+            nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
+            lib().orc_mesh_set_shading(om.h, _ptr(fs), _ptr(nr))
+            if m.get("transform_keys") is not None:
+                om.set_transform_keys(m["transform_keys"])
+            elif m.get("transform") is not None:
+                om.set_transform(m["transform"])
+            geoms[i] = om
+    for i, m in enumerate(entries):
+        if "instance" in m:
+            geoms[i] = Instance(geoms[m["instance"]], m["keys"], m["bmin"], m["bmax"])
+        elif "proc" in m:
+            geoms[i] = Proc([geoms[c] for c in m["proc"]], m["proc"], m.get("keys"), m["bmin"], m["bmax"])
+    return geoms
+
+
+def scene_of(entries, geoms):
+    """The scene's top level: every geom but a Proc's children, each
+    reporting its index in the list."""
+    children = {c for m in entries if "proc" in m for c in m["proc"]}
+    top = [i for i in range(len(entries)) if i not in children]
+    return Scene([geoms[i] for i in top], ids=top)
+
+
+class Instance:
+    """GeomInstance (builtin/geom/instance/instance.go) of an oracle geom."""
+
+    def __init__(self, of, keys, bmin, bmax):
+        self.of = of
+        self._k, n = _keys16(keys)
+        self._b = (np.asarray(bmin, np.float32), np.asarray(bmax, np.float32))
+        self.h = lib().orc_instance_create(of.h, _ptr(self._k), n, _ptr(self._b[0]), _ptr(self._b[1]))
+        if not self.h:
+            raise ValueError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mesh_destroy(self.h)
+            self.h = None
+
+
+class Proc:
+    """Proc (builtin/geom/proc/proc.go) over oracle geoms; a hit in child k
+    reports ids[k]."""
+
+    def __init__(self, children, ids, keys, bmin, bmax):
+        self.children = list(children)
+        arr = (ctypes.c_void_p * len(children))(*[c.h for c in children])
+        self._ids = np.ascontiguousarray(ids, np.int32)
+        self._k, n = (None, 0) if keys is None else _keys16(keys)
+        self._b = (np.asarray(bmin, np.float32), np.asarray(bmax, np.float32))
+        self._arr = arr
+        self.h = lib().orc_proc_create(arr, _ptr(self._ids), len(children), _ptr(self._k), n, _ptr(self._b[0]),
+                                       _ptr(self._b[1]))
+        if not self.h:
+            raise ValueError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mesh_destroy(self.h)
+            self.h = None
+
+
 class Mesh:
     """A PolyMesh with its accelerator built by the oracle."""
 
@@ -419,6 +526,11 @@ class Mesh:
         if getattr(self, "h", None):
             lib().orc_mesh_destroy(self.h)
             self.h = None
+
+    def set_transform_keys(self, keys):
+        """PolyMesh.Transform of n keys ([n, 16] column-major)."""
+        self._xk, n = _keys16(keys)
+        lib().orc_mesh_set_transform_keys(self.h, _ptr(self._xk), n)
 
     def set_transform(self, m):
         """PolyMesh.Transform: a column-major 4x4 (16 floats) or None."""
@@ -480,12 +592,14 @@ class Sphere:
 
 
 class Scene:
-    """The two-level scene of builtin/scene over oracle meshes."""
+    """The two-level scene of builtin/scene over oracle meshes (hits report
+    ids[i] for meshes[i], default i)."""
 
-    def __init__(self, meshes):
+    def __init__(self, meshes, ids=None):
         self.meshes = list(meshes)
         arr = (ctypes.c_void_p * len(self.meshes))(*[m.h for m in self.meshes])
-        self.h = lib().orc_scene_create(arr, len(self.meshes))
+        self._ids = None if ids is None else np.ascontiguousarray(ids, np.int32)
+        self.h = lib().orc_scene_create_ids(arr, _ptr(self._ids), len(self.meshes))
         if not self.h:
             raise ValueError(lib().orc_last_error().decode())
 

@@ -5,6 +5,7 @@
 // algorithms, written for readability and compiled with -ffp-contract=off.
 // Every function names the reference file:line it restates.
 #include "orc.h"
+#include "orc_internal.h"
 
 #include <algorithm>
 #include <atomic>
@@ -369,14 +370,31 @@ struct Mesh {
   // PolyMesh.Transform (one matrix, column-major) and Matrix4Inverse of it
   bool has_xf = false;
   float xf[16] = {}, xinv[16] = {};
+  // PolyMesh.Transform of two or more keys, decomposed (init.go:14-16)
+  std::vector<orc_internal::Decomp> xkeys;
+  // A GeomInstance (group 1, builtin/geom/instance) or Proc (group 2,
+  // builtin/geom/proc): its transform keys (always decomposed), its given
+  // bounds (BMin/BMax of key 0), the geoms it traces and, for a Proc, the id
+  // each child's hits report.
+  int group = 0;
+  std::vector<orc_internal::Decomp> gkeys;
+  std::vector<const Mesh*> children;
+  std::vector<int32_t> child_ids;
+  Box user_bounds;
+  // Set on a Proc's children: the Proc's transform keys (used in shading).
+  const std::vector<orc_internal::Decomp>* outer = nullptr;
 
   const float* vert(uint32_t i, int key) const { return &verts[((size_t)key * nverts + i) * 3]; }
   int motion_keys() const {  // polymesh.go:103-112; a sphere has one key (sphere.go:58-60)
+    if (group == 1) return children[0]->motion_keys();  // Instance.MotionKeys (instance.go:144-148)
+    if (group == 2) return (int)gkeys.size();           // Proc.MotionKeys (proc.go:181-185)
     if (sphere) return 1;
     return nodes.empty() ? (int)mboxes.size() : 1;
   }
-  // PolyMesh.Bounds (builtin/geom/polymesh/bounds.go:25-53).
+  // PolyMesh.Bounds (builtin/geom/polymesh/bounds.go:25-53); an instance or
+  // a Proc returns its key-0 bounds at every time (instance.go:64-68).
   Box bounds_at(float time) const {
+    if (group) return user_bounds;
     if (!nodes.empty() || mboxes.empty()) return bounds;
     float k = time * (float)(motion_bounds.size() - 1);
     float t = k - std::floor(k);
@@ -847,21 +865,59 @@ void matrix4_inverse(const float m[16], float c[16]) {
   for (int i = 0; i < 16; ++i) c[i] = inv[i] * det;
 }
 
-// PolyMesh.Trace's transform (builtin/geom/polymesh/trace.go:22-55, 64-69):
-// the ray mapped by Matrix4MulPoint/Matrix4MulVec of the inverse
-// (math/matrix4.go:177-218), Ray.Setup, the walk, then the world ray again
-// with the walk's Tclosest.
-bool mesh_trace_xf(const Mesh& m, Ray& r, Task& tk) {
-  if (!m.has_xf) return mesh_trace(m, r, tk);
-  const float* a = m.xinv;
-  Ray ro = r;
+// The ray mapped by Matrix4MulPoint/Matrix4MulVec of an inverse
+// (math/matrix4.go:177-218), then Ray.Setup.
+void ray_to_space(Ray& ro, const Ray& r, const float* a) {
   for (int i = 0; i < 3; ++i) {
     ro.P[i] = a[i] * r.P[0] + a[4 + i] * r.P[1] + a[8 + i] * r.P[2] + a[12 + i];
     ro.D[i] = a[i] * r.D[0] + a[4 + i] * r.D[1] + a[8 + i] * r.D[2];
   }
   ray_setup(ro);
+}
+
+// PolyMesh.Trace's transform (builtin/geom/polymesh/trace.go:22-55, 64-69):
+// one key used as it is, two or more blended (TransformDecompLerp of the
+// keys around the ray's time, rebuilt), Matrix4Inverse, the ray mapped into
+// object space, the walk, then the world ray again with the walk's Tclosest.
+bool mesh_trace_xf(const Mesh& m, Ray& r, Task& tk) {
+  if (!m.has_xf && m.xkeys.empty()) return mesh_trace(m, r, tk);
+  float inv[16];
+  if (!m.xkeys.empty()) {
+    float M[16];
+    if (!orc_internal::decomp_at(m.xkeys, r.Time, false, M)) return false;  // the reference panics
+    orc_internal::matrix_inverse(M, inv);
+  } else {
+    for (int i = 0; i < 16; ++i) inv[i] = m.xinv[i];
+  }
+  Ray ro = r;
+  ray_to_space(ro, r, inv);
   const bool hit = mesh_trace(m, ro, tk);
   r.Tclosest = ro.Tclosest;
+  return hit;
+}
+
+// Instance.Trace (builtin/geom/instance/instance.go:72-115) and Proc.Trace
+// (builtin/geom/proc/proc.go:88-140): the transform at the ray's time
+// (TransformSRTArray.TimeKey, rebuilt), Matrix4Inverse, the ray mapped and
+// Ray.Setup, then the children in order, each through its own
+// PolyMesh.Trace; a Proc stops at the first child that hits unless the ray
+// is a shadow ray (proc.go:117-124).  hit_id: the id the hit reports.
+bool group_trace(const Mesh& m, Ray& r, Task& tk, int32_t& hit_id) {
+  float M[16], inv[16];
+  if (!orc_internal::decomp_at(m.gkeys, r.Time, false, M)) return false;
+  orc_internal::matrix_inverse(M, inv);
+  Ray rg = r;
+  ray_to_space(rg, r, inv);
+  bool hit = false;
+  for (size_t c = 0; c < m.children.size(); ++c) {
+    if (mesh_trace_xf(*m.children[c], rg, tk)) {
+      hit = true;
+      hit_id = m.group == 2 ? m.child_ids[c] : -1;
+      if (!r.shadow) break;
+    }
+    if (tk.overflow) break;
+  }
+  r.Tclosest = rg.Tclosest;
   return hit;
 }
 
@@ -869,8 +925,11 @@ bool mesh_trace_xf(const Mesh& m, Ray& r, Task& tk) {
 bool scene_trace_elems(const Scene& s, Ray& r, Task& tk, int base, int count) {
   bool hit = false;
   for (int i = base; i < base + count; ++i) {
-    if (mesh_trace_xf(*s.geoms[i], r, tk)) {
-      tk.geom = s.geom_order[i];
+    const Mesh& g = *s.geoms[i];
+    int32_t hid = -1;
+    const bool gh = g.group ? group_trace(g, r, tk, hid) : mesh_trace_xf(g, r, tk);
+    if (gh) {
+      tk.geom = hid >= 0 ? hid : s.geom_order[i];
       hit = true;
       if (r.shadow) return true;
     }
@@ -943,7 +1002,8 @@ Hit trace(const orc_scene* s, const float P[3], const float D[3], float tmax, fl
 }
 
 MeshView mesh_view(const orc_mesh* om) {
-  const Mesh& m = om->m;
+  // An instance shades as the geom it traces, through its own transform.
+  const Mesh& m = om->m.group == 1 ? *om->m.children[0] : om->m;
   MeshView v;
   v.verts = m.verts.data();
   v.nverts = m.nverts;
@@ -960,6 +1020,8 @@ MeshView mesh_view(const orc_mesh* om) {
     v.xf[k] = m.xf[k];
     v.xinv[k] = m.xinv[k];
   }
+  v.xkeys = m.xkeys.empty() ? nullptr : &m.xkeys;
+  v.outer = om->m.group == 1 ? &om->m.gkeys : m.outer;
   return v;
 }
 
@@ -992,6 +1054,54 @@ orc_mesh* orc_mesh_create(const float* verts, uint32_t nverts, uint32_t keys, co
 }
 
 void orc_mesh_destroy(orc_mesh* m) { delete m; }
+
+void orc_mesh_set_transform_keys(orc_mesh* om, const float* keys16, uint32_t n) {
+  Mesh& me = om->m;
+  me.xkeys.clear();
+  if (n <= 1) {
+    orc_mesh_set_transform(om, n == 1 ? keys16 : nullptr);
+    return;
+  }
+  me.has_xf = false;
+  me.xkeys.resize(n);
+  for (uint32_t i = 0; i < n; ++i) orc_internal::decomp_matrix(keys16 + 16 * i, me.xkeys[i]);
+}
+
+static orc_mesh* make_group(int kind, const float* keys16, uint32_t n_keys, const float bmin[3], const float bmax[3]) {
+  orc_mesh* om = new orc_mesh();
+  Mesh& g = om->m;
+  g.group = kind;
+  g.gkeys.resize(n_keys);
+  for (uint32_t i = 0; i < n_keys; ++i) orc_internal::decomp_matrix(keys16 + 16 * i, g.gkeys[i]);
+  box_reset(g.user_bounds);  // BoundingBox.GrowVec3 of BMin and BMax (instance.go:123-128)
+  box_grow(g.user_bounds, bmin);
+  box_grow(g.user_bounds, bmax);
+  return om;
+}
+
+orc_mesh* orc_instance_create(const orc_mesh* of, const float* keys16, uint32_t n_keys, const float bmin[3],
+                              const float bmax[3]) {
+  if (!of || of->m.group || n_keys < 1 || !keys16) { g_err = "bad instance arguments"; return nullptr; }
+  orc_mesh* om = make_group(1, keys16, n_keys, bmin, bmax);
+  om->m.children.push_back(&of->m);
+  return om;
+}
+
+orc_mesh* orc_proc_create(orc_mesh* const* children, const int32_t* child_ids, uint32_t n, const float* keys16,
+                          uint32_t n_keys, const float bmin[3], const float bmax[3]) {
+  if (n == 0 || !children || !child_ids) { g_err = "a Proc needs geoms"; return nullptr; }
+  for (uint32_t i = 0; i < n; ++i)
+    if (!children[i] || children[i]->m.group) { g_err = "a Proc's children are meshes or spheres"; return nullptr; }
+  static const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  // Proc.PreRender: no Transform means one identity key (proc.go:157-160)
+  orc_mesh* om = n_keys ? make_group(2, keys16, n_keys, bmin, bmax) : make_group(2, kIdentity, 1, bmin, bmax);
+  for (uint32_t i = 0; i < n; ++i) {
+    om->m.children.push_back(&children[i]->m);
+    om->m.child_ids.push_back(child_ids[i]);
+    children[i]->m.outer = &om->m.gkeys;
+  }
+  return om;
+}
 
 void orc_mesh_set_transform(orc_mesh* om, const float* m) {
   Mesh& me = om->m;
@@ -1078,7 +1188,9 @@ int orc_trace_mesh(const orc_mesh* om, const float* rays, size_t n, int shadow, 
   return status.load();
 }
 
-orc_scene* orc_scene_create(orc_mesh* const* meshes, uint32_t n) {
+orc_scene* orc_scene_create(orc_mesh* const* meshes, uint32_t n) { return orc_scene_create_ids(meshes, nullptr, n); }
+
+orc_scene* orc_scene_create_ids(orc_mesh* const* meshes, const int32_t* ids, uint32_t n) {
   std::vector<Mesh*> ms(n);
   for (uint32_t i = 0; i < n; ++i) {
     if (!meshes[i]) { g_err = "null mesh"; return nullptr; }
@@ -1091,6 +1203,8 @@ orc_scene* orc_scene_create(orc_mesh* const* meshes, uint32_t n) {
     delete os;
     return nullptr;
   }
+  if (ids)
+    for (auto& g : os->s.geom_order) g = ids[g];
   return os;
 }
 

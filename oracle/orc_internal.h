@@ -19,6 +19,21 @@ struct Hit {
 // Scene.Trace of one ray (builtin/scene/scene.go:30-58); shadow = RayTypeShadow.
 Hit trace(const orc_scene* s, const float P[3], const float D[3], float tmax, float time, bool shadow);
 
+// A decomposed transform (math/animdecomp.go:14-18): translation, rotation
+// quaternion (x, y, z, w), stretch matrix (column-major); orc_anim.cpp.
+struct Decomp {
+  float T[3];
+  float R[4];
+  float S[16];
+};
+void decomp_matrix(const float* m, Decomp& d);                       // TransformDecompMatrix4
+void decomp_to_matrix(const Decomp& d, float* m);                    // TransformDecompToMatrix4
+void decomp_lerp(const Decomp& a, const Decomp& b, float t, Decomp& o);  // TransformDecompLerp
+// The keyed matrix at a time: one key as it is (TimeKey) unless blend_one
+// (the camera blends it with itself), else the two keys around time blended.
+bool decomp_at(const std::vector<Decomp>& keys, float time, bool blend_one, float* m);
+bool matrix_inverse(const float* m, float* c);                       // Matrix4Inverse
+
 struct MeshView {
   const float* verts;       // keys * nverts * 3
   uint32_t nverts, keys;
@@ -30,6 +45,11 @@ struct MeshView {
   float sc[3], sr;
   bool has_xf;              // PolyMesh.Transform and its inverse (column-major)
   float xf[16], xinv[16];
+  const std::vector<Decomp>* xkeys;   // PolyMesh.Transform of >= 2 keys (else null)
+  // The GeomInstance / Proc that reaches this mesh (its hits report this
+  // view's id): ApplyTransform then uses that geom's transform at the ray's
+  // time instead of the mesh's own (core/trace.go:69, instance.go:105-110).
+  const std::vector<Decomp>* outer;   // null: none
 };
 MeshView mesh_view(const orc_mesh* m);
 
@@ -50,6 +70,7 @@ struct RenderScene {
   std::vector<orc_shader> shaders;
   std::vector<orc_trilight> lights;
   orc_camera cam;
+  std::vector<Decomp> cam_keys;  // Camera.LocalToWorld keys, decomposed (camera.go:207-236)
   FilterTable filter;
 };
 RenderScene render_scene(const orc_render* r);
@@ -58,7 +79,10 @@ RenderScene render_scene(const orc_render* r);
 // (core/render.go:89-120, builtin/camera/camera.go:244-284) for iteration j
 // (render(iter+1)) of pixel pix: ray origin, direction and time; filt (may
 // be null or empty) warps the sample inside its pixel first.
-void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uint64_t pix, uint64_t seed, float P[3],
-                    float D[3], float* time, const FilterTable* filt = nullptr);
+// M = TransformDecompToMatrix4(TransformDecompLerp(...)) of the camera keys at
+// the sample's time (camera.go:223-236).
+void camera_primary(const orc_camera& c, const std::vector<Decomp>& keys, uint32_t w, uint32_t h, uint32_t j,
+                    uint64_t pix, uint64_t seed, float P[3], float D[3], float* time,
+                    const FilterTable* filt = nullptr);
 
 }  // namespace orc_internal

@@ -654,7 +654,7 @@ int run(const orc_render* r, const orc_quad_light* quads, uint32_t nq, const orc
         if (s0 >= npix) break;
         for (size_t pix = s0; pix < std::min(npix, s0 + 64); ++pix) {
           float P[3], D[3], time;
-          orc_internal::camera_primary(pt.R.cam, w, h, j, pix, p->seed, P, D, &time, &pt.R.filter);
+          orc_internal::camera_primary(pt.R.cam, pt.R.cam_keys, w, h, j, pix, p->seed, P, D, &time, &pt.R.filter);
           const Vec<T> L = pt.path(sample_key(p->seed, pix, j), P, D, time);
           const T Lc[3] = {L.x, L.y, L.z};
           for (int k = 0; k < 3; ++k) {  // exact running mean over iterations 0..it

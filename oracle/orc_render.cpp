@@ -13,12 +13,17 @@
 // same, so the two agree closely):
 //  * Vec3Normalize is a * (1/sqrt(a.a)) with IEEE sqrt and division; the
 //    reference's RSQRTSS estimate is machine-dependent (math/vec3_amd64.s).
+//    orc_set_normalize_mode(1, seed) switches to an emulation of the
+//    assembly (an estimate within RSQRTSS's documented relative error of
+//    1.5*2^-12, then its Newton step in its operation order) so that the
+//    size of this departure can be measured on whole images.
 //  * acos arguments are clamped to [-1, 1]: a normalised dot product can
 //    exceed 1 by an ulp, where the reference yields NaN.
 //  * per-pixel scrambles come from a hash of (seed, pixel) instead of the
 //    unseeded math/rand stream (core/render.go:166-176).
-//  * the camera uses LocalToWorld directly instead of its SRT decomposition
-//    round trip (camera.go:223-236), which is not exact for one key.
+// The camera goes through the reference's SRT decomposition round trip
+// (TransformDecompMatrix4 of each LocalToWorld key, then per sample
+// TransformDecompToMatrix4 of TransformDecompLerp; camera.go:223-236).
 // Transcendentals follow math/sincos.go: evaluated in float64, rounded to
 // float32.
 #include <atomic>
@@ -48,7 +53,32 @@ inline V3 cross(V3 a, V3 b) {  // Vec3Cross (math/vec3.go:69-74)
 }
 inline float len2(V3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
 inline float gabs(float x) { return std::fabs(x); }
+// Vec3Normalize.  Mode 0: a * (1/sqrt(a.a)).  Mode 1 emulates
+// math/vec3_amd64.s:11-42: s = (x*x + y*y) + z*z; g = RSQRTSS(s), here the
+// exact 1/sqrt(s) times (1 + e) with e a hash of (s, seed) uniform in
+// [-1.5*2^-12, 1.5*2^-12] (the instruction's documented error bound);
+// g' = (1.5 - (g*g)*(0.5*s)) * g; result a * g'.
+int g_norm_mode = 0;
+uint64_t g_norm_seed = 0;
+inline float rsqrtss_estimate(float s) {
+  uint32_t bits;
+  std::memcpy(&bits, &s, 4);
+  uint64_t z = g_norm_seed + 0x9E3779B97F4A7C15ull * ((uint64_t)bits + 1ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
+  const double e = (2.0 * u - 1.0) * 1.5 / 4096.0;
+  return (float)((1.0 / std::sqrt((double)s)) * (1.0 + e));
+}
 inline V3 normalize(V3 a) {
+  if (g_norm_mode == 1) {
+    const float s = (a.x * a.x + a.y * a.y) + a.z * a.z;
+    const float g = rsqrtss_estimate(s);
+    const float h = 0.5f * s;
+    const float g2 = (1.5f - (g * g) * h) * g;
+    return v3(a.x * g2, a.y * g2, a.z * g2);
+  }
   const float r = 1.0f / std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
   return v3(a.x * r, a.y * r, a.z * r);
 }
@@ -378,6 +408,7 @@ struct Render {
   std::vector<orc_trilight> tri_lights;
   std::vector<Light> lights;
   orc_camera cam;
+  std::vector<orc_internal::Decomp> cam_keys;  // LocalToWorld keys, decomposed
   orc_internal::FilterTable filter;
 };
 
@@ -756,10 +787,26 @@ struct Renderer {
   }
 
   // Hit attributes for a static mesh (trace.go:276-515) or an analytic sphere
-  // (sphere/trace.go), followed by ShaderContext.ApplyTransform with the
-  // identity (core/shader.go:129-135).
+  // (sphere/trace.go), then the transforms: a transformed mesh's
+  // PolyMesh.Trace sets P = M Po and N = M^-T N (trace.go:67-74) and makes M
+  // the context's transform; a GeomInstance or Proc around the geom makes
+  // its own transform the context's on a hit (instance.go:105-110,
+  // proc.go:133-138); core.Trace then calls ShaderContext.ApplyTransform with
+  // the context's transform (core/shader.go:129-135; the identity when none
+  // was set).  Keyed transforms are taken at the ray's time.
   bool hit_context(const Hit& h, Ctx& sc, V3 Ro, V3 Rd) const {
     const orc_internal::MeshView& m = R.meshes[h.geom];
+    float OT[16], OI[16];  // the instance's / Proc's transform and inverse
+    if (m.outer) {
+      orc_internal::decomp_at(*m.outer, sc.time, false, OT);
+      orc_internal::matrix_inverse(OT, OI);
+      // the ray its children were traced with (instance.go:91-93)
+      const V3 P0 = Ro, D0 = Rd;
+      Ro = v3(OI[0] * P0.x + OI[4] * P0.y + OI[8] * P0.z + OI[12], OI[1] * P0.x + OI[5] * P0.y + OI[9] * P0.z + OI[13],
+              OI[2] * P0.x + OI[6] * P0.y + OI[10] * P0.z + OI[14]);
+      Rd = v3(OI[0] * D0.x + OI[4] * D0.y + OI[8] * D0.z, OI[1] * D0.x + OI[5] * D0.y + OI[9] * D0.z,
+              OI[2] * D0.x + OI[6] * D0.y + OI[10] * D0.z);
+    }
     if (m.sphere) {
       const auto& list = R.mesh_shaders[h.geom];
       if (list.empty()) return false;
@@ -773,6 +820,7 @@ struct Renderer {
       sc.DdPdu = normalize(v3(1, 0, 0));
       sc.DdPdv = normalize(v3(0, 0, 1));
       sc.geom = h.geom;
+      if (m.outer) apply_transform(sc, OT, OI);
       return true;
     }
     const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
@@ -830,40 +878,50 @@ struct Renderer {
     sc.DdPdu = normalize(dpdu);
     sc.DdPdv = normalize(dpdv);
     sc.geom = h.geom;
-    if (m.has_xf) {
-      // PolyMesh.Trace after its walk (trace.go:67-74): P = M Po, N = M^-T N;
-      // then core.Trace's ApplyTransform (core/shader.go:129-135) with the
-      // same matrices: P = M Po, N = normalize(M^-T N), Ng = normalize(M^-T
-      // Ng), dPdu/dPdv = normalize(M dPdu/dPdv).  Matrix4MulPoint/MulVec
-      // (math/matrix4.go:177-218) sum left to right; M^-T indexes the
-      // inverse transposed (Matrix4Transpose, :105-113).
-      const float* T = m.xf;
-      const float* I = m.xinv;
-      auto mul_point = [&](V3 b) {
-        return v3(T[0] * b.x + T[4] * b.y + T[8] * b.z + T[12], T[1] * b.x + T[5] * b.y + T[9] * b.z + T[13],
-                  T[2] * b.x + T[6] * b.y + T[10] * b.z + T[14]);
-      };
-      auto mul_vec = [&](V3 b) {
-        return v3(T[0] * b.x + T[4] * b.y + T[8] * b.z, T[1] * b.x + T[5] * b.y + T[9] * b.z,
-                  T[2] * b.x + T[6] * b.y + T[10] * b.z);
-      };
-      auto mul_inv_t = [&](V3 b) {
-        float t[16];
-        for (int i = 0; i < 4; ++i)
-          for (int j = 0; j < 4; ++j) t[i * 4 + j] = I[j * 4 + i];
-        return v3(t[0] * b.x + t[4] * b.y + t[8] * b.z, t[1] * b.x + t[5] * b.y + t[9] * b.z,
-                  t[2] * b.x + t[6] * b.y + t[10] * b.z);
-      };
-      const V3 Po = sc.P;
-      sc.P = mul_point(Po);
-      sc.N = mul_inv_t(sc.N);
-      sc.P = mul_point(Po);
-      sc.N = normalize(mul_inv_t(sc.N));
-      sc.Ng = normalize(mul_inv_t(sc.Ng));
-      sc.DdPdu = normalize(mul_vec(sc.DdPdu));
-      sc.DdPdv = normalize(mul_vec(sc.DdPdv));
+    float MT[16], MI[16];  // the mesh's own transform and inverse
+    const bool own = m.has_xf || m.xkeys;
+    if (m.xkeys) {
+      orc_internal::decomp_at(*m.xkeys, sc.time, false, MT);
+      orc_internal::matrix_inverse(MT, MI);
+    } else if (m.has_xf) {
+      for (int i = 0; i < 16; ++i) {
+        MT[i] = m.xf[i];
+        MI[i] = m.xinv[i];
+      }
     }
+    if (own) sc.N = mul_inv_t(MI, sc.N);  // PolyMesh.Trace (its P is replaced below)
+    if (m.outer) apply_transform(sc, OT, OI);
+    else if (own) apply_transform(sc, MT, MI);
     return true;
+  }
+
+  // Matrix4MulPoint / Matrix4MulVec (math/matrix4.go:177-218, sums left to
+  // right) and Matrix4MulVec of the inverse transposed (Matrix4Transpose,
+  // :100-108).
+  static V3 mul_point(const float* T, V3 b) {
+    return v3(T[0] * b.x + T[4] * b.y + T[8] * b.z + T[12], T[1] * b.x + T[5] * b.y + T[9] * b.z + T[13],
+              T[2] * b.x + T[6] * b.y + T[10] * b.z + T[14]);
+  }
+  static V3 mul_vec(const float* T, V3 b) {
+    return v3(T[0] * b.x + T[4] * b.y + T[8] * b.z, T[1] * b.x + T[5] * b.y + T[9] * b.z,
+              T[2] * b.x + T[6] * b.y + T[10] * b.z);
+  }
+  static V3 mul_inv_t(const float* I, V3 b) {
+    float t[16];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) t[i * 4 + j] = I[j * 4 + i];
+    return v3(t[0] * b.x + t[4] * b.y + t[8] * b.z, t[1] * b.x + t[5] * b.y + t[9] * b.z,
+              t[2] * b.x + t[6] * b.y + t[10] * b.z);
+  }
+  // ShaderContext.ApplyTransform (core/shader.go:129-135); Po is the hit
+  // point in the space the geom was traced in.
+  static void apply_transform(Ctx& sc, const float* T, const float* I) {
+    const V3 Po = sc.P;
+    sc.P = mul_point(T, Po);
+    sc.N = normalize(mul_inv_t(I, sc.N));
+    sc.Ng = normalize(mul_inv_t(I, sc.Ng));
+    sc.DdPdu = normalize(mul_vec(T, sc.DdPdu));
+    sc.DdPdv = normalize(mul_vec(T, sc.DdPdv));
   }
 
   // core.Trace (core/trace.go:40-83).
@@ -884,6 +942,8 @@ struct Renderer {
     RGB zero{{0, 0, 0}};
     if (sg.level > 3) return zero;
     const Shader& sh = *sg.shader;
+    if (sh.has(ORC_SH_DEBUG))  // Debug.Eval (builtin/shader/debug.go:47-49)
+      return RGB{{sh.p.diffuse_colour[0], sh.p.diffuse_colour[1], sh.p.diffuse_colour[2]}};
     V3 Vt = cross(sg.N, sg.DdPdu);
     if (len2(Vt) < 0.1f) Vt = cross(sg.N, sg.DdPdv);
     Vt = normalize(Vt);
@@ -976,7 +1036,8 @@ struct orc_render {
 
 namespace orc_internal {
 
-void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uint64_t pix, uint64_t seed, float Po[3],
+void camera_primary(const orc_camera& c, const std::vector<Decomp>& keys, uint32_t w, uint32_t h, uint32_t j,
+                    uint64_t pix, uint64_t seed, float Po[3],
                     float Do[3], float* time, const FilterTable* filt) {
   const uint32_t x = (uint32_t)(pix % w), y = (uint32_t)(pix / w);
   double rx, ry;
@@ -996,7 +1057,9 @@ void camera_primary(const orc_camera& c, uint32_t w, uint32_t h, uint32_t j, uin
   const float camu = Sx * c.tan_theta_focal;
   const float camv = Sy * (c.tan_theta_focal / c.aspect);
   const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
-  const float* M = c.m;
+  float M[16];  // Matrix4Identity without keys (camera.go:223-236)
+  for (int i = 0; i < 16; ++i) M[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+  if (!keys.empty()) decomp_at(keys, *time, true, M);
   V3 e = v3(0, 0, 0);
   V3 sv = s3;
   if (c.radius > 0.0f) {
@@ -1024,6 +1087,7 @@ RenderScene render_scene(const orc_render* o) {
   for (const Shader& sh : r.shaders) s.shaders.push_back(sh.p);
   s.lights = r.tri_lights;
   s.cam = r.cam;
+  s.cam_keys = r.cam_keys;
   s.filter = r.filter;
   return s;
 }
@@ -1063,7 +1127,21 @@ orc_render* orc_render_create(const orc_scene* scene, orc_mesh* const* meshes, u
     r.lights.push_back(L);
   }
   r.cam = *cam;
+  r.cam_keys.resize(1);
+  orc_internal::decomp_matrix(cam->m, r.cam_keys[0]);
   return o;
+}
+
+int orc_render_set_camera_keys(orc_render* o, const float* keys16, uint32_t n) {
+  if (!o || (n > 0 && !keys16)) return -1;
+  o->r.cam_keys.resize(n);
+  for (uint32_t i = 0; i < n; ++i) orc_internal::decomp_matrix(keys16 + 16 * i, o->r.cam_keys[i]);
+  return 0;
+}
+
+void orc_set_normalize_mode(int mode, uint64_t seed) {
+  g_norm_mode = mode;
+  g_norm_seed = seed;
 }
 
 void orc_render_destroy(orc_render* r) { delete r; }
@@ -1083,7 +1161,7 @@ int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, u
         if (s >= npix) break;
         for (size_t pix = s; pix < std::min(npix, s + 256); ++pix) {
           float Pf[3], Df[3], tf;
-          orc_internal::camera_primary(R.cam, w, h, j, pix, seed, Pf, Df, &tf, &R.filter);
+          orc_internal::camera_primary(R.cam, R.cam_keys, w, h, j, pix, seed, Pf, Df, &tf, &R.filter);
           const V3 P = v3(Pf[0], Pf[1], Pf[2]), D = v3(Df[0], Df[1], Df[2]);
           const double time = (double)tf;
           const double lambda = (720.0 - 450.0) * vdc(j, scramble(seed, pix, 3)) + 450.0;

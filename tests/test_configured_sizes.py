@@ -1,0 +1,82 @@
+"""Parity at the stated sizes of the small-room render and the batched-jobs
+trace (the raw-traversal configuration's full-size traces are in
+test_trace_gpu.test_full_size_soup_parity).
+
+* Small room as configured: 5 axis-aligned quads plus 16,384 random
+  triangles (seed 1), 256x256, 16 iterations of core.Render in reference
+  mode, against the oracle's image computed on all host threads.  The
+  tolerance is the render tests' (per channel |a-b| <= 1e-5 (1+|b|) on
+  99.9% of the pixels, mean |a-b| <= 1e-6) and the benchmark spec's: mean
+  relative pixel error <= 1e-3, with the per-pixel maximum asserted too.
+* Batched jobs as configured: 64 soups of 1k-200k triangles (seed 4),
+  every other one with two-key motion, 65,536 camera rays each, in one
+  vmr_trace_jobs launch; every job's hits against the oracle's trace of
+  that job's mesh, bit for bit (closest hit), hit/miss for any hit.
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_hits_equal
+from vermeer_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+MEAN_REL = 1e-3      # the benchmark spec's mean relative pixel error
+MAX_REL = 1e-4       # per-pixel maximum stated for the configured image
+
+
+def _pixel_rel(got, ref):
+    """Relative error per pixel: channel-summed |a-b| over channel-summed
+    |b|, with a floor of 1e-3 in the denominator for black pixels."""
+    num = np.abs(got - ref).sum(-1)
+    den = np.maximum(np.abs(ref).sum(-1), 1e-3)
+    return num / den
+
+
+def test_small_room_as_configured_matches_oracle(ctx, orc):
+    room = scenes.small_room(16384, seed=1, res=256)
+    ctx.load_scene(room)
+    ref = orc.Render(room).run(256, 256, 0, 16, 1, nthreads=0)
+    got, st = ctx.render(256, 256, 0, 16, 1)
+    assert st["samples"] == 256 * 256 * 16
+    assert not np.isnan(got).any() and not np.isnan(ref).any()
+    ok = np.abs(got - ref) <= 1e-5 * (1.0 + np.abs(ref))
+    assert ok.all(-1).mean() >= 0.999
+    assert np.abs(got - ref).mean() <= 1e-6
+    rel = _pixel_rel(got, ref)
+    assert rel.mean() <= MEAN_REL, rel.mean()
+    assert rel.max() <= MAX_REL, rel.max()
+
+
+def _c4_jobs(ctx):
+    import torch
+    sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)
+    cam = scenes.coherent_rays(256)
+    work = []
+    for j, nt in enumerate(sizes):
+        motion = j % 2 == 1
+        if motion:
+            v, ip = scenes.motion_soup(int(nt), 400 + j, velocity=0.05)
+        else:
+            v, ip = scenes.triangle_soup(int(nt), 400 + j)
+        g = ctx.mesh_build(v, ip, keys=2 if motion else 1, motion_mode=1)
+        rays = cam.copy()
+        rays[:, 7] = scenes.uniform(500 + j, rays.shape[0], 7).astype(np.float32) if motion else 0.0
+        work.append((v, ip, motion, rays, g, torch.from_numpy(np.ascontiguousarray(rays.T)).cuda()))
+    return work
+
+
+def test_batched_jobs_as_configured_match_oracle(ctx, orc):
+    work = _c4_jobs(ctx)
+    jobs = [(g, d) for *_, g, d in work]
+    for shadow in (False, True):
+        outs, st = ctx.trace_jobs(jobs, shadow=shadow)
+        assert st["rays"] == 64 * 256 * 256
+        for j, (v, ip, motion, rays, _, _) in enumerate(work):
+            om = orc.Mesh(v, ip, keys=2 if motion else 1, motion_fixed=motion)
+            ref = om.trace(rays, shadow=shadow)
+            got = {k: outs[j][k].cpu().numpy() for k in ("prim", "t", "u", "v", "w")}
+            if shadow:
+                assert np.array_equal(got["prim"] >= 0, ref["prim"] >= 0), f"job {j} any hit"
+            else:
+                assert_hits_equal(got, ref, what=f"job {j} ({'motion' if motion else 'static'}, {len(ip) // 3} tris)")

@@ -140,15 +140,18 @@ def _two_level_scene_parity(ctx, orc, motion_every):
 
 
 def test_full_size_soup_parity(ctx, orc):
-    """The benchmark workload: 1,048,576-triangle soup, 4M incoherent rays,
-    every hit compared with the oracle (multithreaded on the host)."""
+    """The raw-traversal configuration at its stated size: the 1,048,576-
+    triangle soup (seed 2) under all 4,194,304 incoherent rays and the
+    4,194,304 coherent primaries of a 2048x2048 pinhole, closest hit and any
+    hit, every hit compared with the oracle (multithreaded on the host)."""
     v, ip = scenes.triangle_soup(1 << 20, 2)
     geom = ctx.mesh_build(v, ip)
-    rays = scenes.incoherent_rays(1 << 22, 2)
     om = orc.Mesh(v, ip)
-    assert_hits_equal(ctx.trace_mesh(geom, rays), om.trace(rays), what="1M soup closest")
-    sub = rays[: 1 << 20]
-    assert_hits_equal(ctx.trace_mesh(geom, sub, shadow=True), om.trace(sub, shadow=True), what="1M soup any")
+    for name, rays in (("incoherent", scenes.incoherent_rays(1 << 22, 2)), ("coherent", scenes.coherent_rays(2048))):
+        assert rays.shape[0] == 1 << 22
+        for shadow in (False, True):
+            assert_hits_equal(ctx.trace_mesh(geom, rays, shadow=shadow), om.trace(rays, shadow=shadow),
+                              what=f"1M soup {name} shadow={shadow}")
 
 
 @pytest.mark.parametrize("tuning", [(0, 0, 0, 0), (1, 0, 0, 0), (3, 0, 0, 0), (5, 0, 0, 0), (8, 0, 0, 4),

@@ -150,6 +150,7 @@ class Adam(ctypes.Structure):
 SHADER_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
                 "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
                 "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
+SH_DEBUG = 2048  # DebugShader: a shader dict with "debug": True and diffuse_colour = Colour
 
 assert ctypes.sizeof(QbvhNode) == 128 and ctypes.sizeof(MqbvhNode) == 40
 
@@ -195,6 +196,11 @@ SIGNATURES = {
     "vmr_render_path_jobs": (ctypes.c_int, [P, P, U32, ctypes.POINTER(PathParams), ctypes.POINTER(PathStats)]),
     "vmr_set_path_batch": (ctypes.c_int, [P, U32]),
     "vmr_mesh_set_transform": (ctypes.c_int, [P, U32, P]),
+    "vmr_mesh_set_transform_keys": (ctypes.c_int, [P, U32, P, U32]),
+    "vmr_instance_add": (ctypes.c_int, [P, U32, P, U32, P, P, ctypes.POINTER(U32)]),
+    "vmr_proc_add": (ctypes.c_int, [P, P, U32, P, U32, P, P, ctypes.POINTER(U32)]),
+    "vmr_set_camera_keys": (ctypes.c_int, [P, P, U32]),
+    "vmr_transform_keys_at": (ctypes.c_int, [P, U32, ctypes.c_float, ctypes.c_int, P]),
     "vmr_selftest_wait": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float)]),
     "vmr_get_path_batch": (ctypes.c_int, [P, ctypes.POINTER(U32)]),
     "vmr_autotune_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, P, ctypes.POINTER(U32),
@@ -251,7 +257,7 @@ def shader_struct(d: dict) -> ShaderStd:
             else:
                 for i in range(3):
                     getattr(sh, k)[i] = float(v[i])
-    sh.flags = flags
+    sh.flags = flags | (SH_DEBUG if d.get("debug") else 0)
     sh.spec1_fresnel = 1 if d.get("spec1_fresnel") == "Metal" else 0
     return sh
 

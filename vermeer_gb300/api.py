@@ -55,6 +55,19 @@ def pixel_filter_warp(kind: int, r0, r1, res: int = 0, width: float = 0.0, peak:
     return u, v
 
 
+def transform_keys_at(keys, time: float, blend_one: bool = False):
+    """libvmr's matrix for decomposed transform keys ([n, 16] column-major)
+    at a time, on the host (no GPU): TransformDecompMatrix4 per key,
+    TransformDecompLerp of the keys around time, TransformDecompToMatrix4."""
+    L = _lib.load()
+    k = np.ascontiguousarray(keys, np.float32).reshape(-1, 16)
+    out = np.zeros(16, np.float32)
+    rc = L.vmr_transform_keys_at(_p(k), k.shape[0], float(time), int(bool(blend_one)), _p(out))
+    if rc != 0:
+        raise VmrError(rc, "time outside the keys")
+    return out
+
+
 def write_float(path: str, fb):
     """The OutputFloat driver (builtin/driver/outputfloat.go): the float32
     framebuffer [h, w, 3] as raw little-endian floats."""
@@ -416,8 +429,13 @@ class Context:
         return c
 
     def set_camera(self, cam: dict):
+        """vmr_set_camera; cam may carry 'keys' ([n, 16] LocalToWorld motion
+        keys, vmr_set_camera_keys)."""
         c = self._camera(cam)
         self._check(self.L.vmr_set_camera(self.h, ctypes.byref(c)))
+        if cam.get("keys") is not None:
+            k = np.ascontiguousarray(cam["keys"], np.float32).reshape(-1, 16)
+            self._check(self.L.vmr_set_camera_keys(self.h, _p(k), k.shape[0]))
 
     def set_path_batch(self, paths: int):
         """Paths per wavefront batch of later render_path calls that give no
@@ -488,25 +506,61 @@ class Context:
         a = np.ascontiguousarray(m, np.float32).reshape(16)
         self._check(self.L.vmr_mesh_set_transform(self.h, geom, _p(a)))
 
+    def mesh_set_transform_keys(self, geom: int, keys):
+        """PolyMesh.Transform with motion keys (vmr_mesh_set_transform_keys):
+        [n, 16] column-major matrices."""
+        k = np.ascontiguousarray(keys, np.float32).reshape(-1, 16)
+        self._check(self.L.vmr_mesh_set_transform_keys(self.h, geom, _p(k), k.shape[0]))
+
+    def instance_add(self, of: int, keys, bmin, bmax) -> int:
+        """GeomInstance of geom `of` (vmr_instance_add); returns its geom id."""
+        k = np.ascontiguousarray(keys, np.float32).reshape(-1, 16)
+        lo, hi = np.asarray(bmin, np.float32), np.asarray(bmax, np.float32)
+        out = ctypes.c_uint32()
+        self._check(self.L.vmr_instance_add(self.h, of, _p(k), k.shape[0], _p(lo), _p(hi), ctypes.byref(out)))
+        return out.value
+
+    def proc_add(self, children, keys, bmin, bmax) -> int:
+        """Proc over the child geoms (vmr_proc_add); keys None: identity."""
+        ch = np.ascontiguousarray(children, np.uint32)
+        k = None if keys is None else np.ascontiguousarray(keys, np.float32).reshape(-1, 16)
+        lo, hi = np.asarray(bmin, np.float32), np.asarray(bmax, np.float32)
+        out = ctypes.c_uint32()
+        self._check(self.L.vmr_proc_add(self.h, _p(ch), ch.size, None if k is None else _p(k),
+                                        0 if k is None else k.shape[0], _p(lo), _p(hi), ctypes.byref(out)))
+        return out.value
+
     def load_scene(self, scene: dict):
         """Upload a render scene (vermeer_gb300.scenes format): meshes with
-        their shading, the two-level scene, materials, lights, camera.
-        Returns the geom ids."""
-        ids = []
-        for m in scene["meshes"]:
+        their shading (and 'transform' or 'transform_keys'), spheres,
+        instances ({'instance': i, 'keys', 'bmin', 'bmax'}) and Procs
+        ({'proc': [child indices], 'keys', 'bmin', 'bmax'}), the two-level
+        scene over every entry but a Proc's children, materials, lights,
+        camera.  Returns the geom ids (one per entry)."""
+        ids = [None] * len(scene["meshes"])
+        for i, m in enumerate(scene["meshes"]):
             if "sphere" in m:  # an analytic sphere geom: (cx, cy, cz, radius)
-                g = self.sphere_add(m["sphere"][:3], m["sphere"][3])
-            else:
+                ids[i] = self.sphere_add(m["sphere"][:3], m["sphere"][3])
+            elif "verts" in m:
                 g = self.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1),
                                     motion_mode=m.get("motion_mode", MOTION_FAITHFUL),
                                     shader_idx=m.get("face_shader"))
-                if m.get("transform") is not None:
+                if m.get("transform_keys") is not None:
+                    self.mesh_set_transform_keys(g, m["transform_keys"])
+                elif m.get("transform") is not None:
                     self.mesh_set_transform(g, m["transform"])
-            ids.append(g)
-        self.scene_build(ids)
+                ids[i] = g
+        for i, m in enumerate(scene["meshes"]):
+            if "instance" in m:
+                ids[i] = self.instance_add(ids[m["instance"]], m["keys"], m["bmin"], m["bmax"])
+            elif "proc" in m:
+                ids[i] = self.proc_add([ids[c] for c in m["proc"]], m.get("keys"), m["bmin"], m["bmax"])
+        children = {c for m in scene["meshes"] if "proc" in m for c in m["proc"]}
+        self.scene_build([g for i, g in enumerate(ids) if i not in children])
         self.set_shaders(scene["shaders"])
         for g, m in zip(ids, scene["meshes"]):
-            self.mesh_set_shading(g, m["shaders"], m.get("normals"))
+            if "instance" not in m and "proc" not in m:
+                self.mesh_set_shading(g, m["shaders"], m.get("normals"))
         self.set_lights([dict(l, geom=ids[l["mesh"]]) for l in scene["lights"]])
         self.set_disk_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("disk_lights", [])])
         self.set_sphere_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("sphere_lights", [])])

@@ -34,9 +34,16 @@ struct HostMesh {
   std::vector<uint8_t> shader_idx;   // leaf order (static) / face order (motion)
   bool sphere = false;               // an analytic sphere geom (centre, radius)
   float sphere_c[3] = {0, 0, 0}, sphere_r = 0;
+  // A GeomInstance (group 1) or Proc (group 2): no triangles of its own; its
+  // bounds are the given BMin/BMax of key 0 at every time
+  // (builtin/geom/instance/instance.go:64-68) and its motion keys those of
+  // the geom it instances or the number of its transform keys
+  // (instance.go:144-148, proc.go:181-185).
+  int group = 0;
+  int group_keys = 1;
 
   bool motion() const { return keys > 1; }
-  int motion_keys() const { return motion() ? (int)keys : 1; }
+  int motion_keys() const { return group ? group_keys : (motion() ? (int)keys : 1); }
   // PolyMesh.Bounds (builtin/geom/polymesh/bounds.go:25-53).
   Bounds bounds_at(float time) const;
 };

@@ -117,6 +117,9 @@ void fill_xf(const MeshRec& rec, DMesh& d) {
   static const int kCols[12] = {0, 1, 2, 4, 5, 6, 8, 9, 10, 12, 13, 14};
   d.has_xf = rec.has_xf ? 1u : 0u;
   for (int k = 0; k < 12; ++k) d.xf_inv[k] = rec.has_xf ? rec.xf_inv[kCols[k]] : 0.0f;
+  const bool keyed = rec.xkeys.size() >= 2;
+  d.xf_nkeys = keyed ? (uint32_t)rec.xkeys.size() : 0u;
+  d.xf_keys = keyed ? rec.dxkeys.as<vmr::anim::Decomp>() : nullptr;
 }
 
 // Host accelerator -> device arrays (layout in device.h).  tris_ready: the
@@ -191,49 +194,9 @@ bool valid_mesh_input(const vmr_mesh_input* in, std::string& why) {
   return true;
 }
 
-// math.Matrix4Inverse (math/matrix4.go:116-160): every element of the
-// adjugate is six triple products (m[a]*m[b])*m[c] summed left to right with
-// the cofactor signs, then det = ((m0 i0 + m1 i4) + m2 i8) + m3 i12 and
-// c = i * (1/det), all in float32 (host code built without contraction).
-// The term table keeps the reference's term order, which fixes the rounding;
+// math.Matrix4Inverse (math/matrix4.go:116-160), restated in animdecomp.h;
 // a zero determinant leaves c all zero (the reference returns its zero c).
-struct InvTerm { int8_t s, a, b, c; };
-const int8_t kInvOut[16] = {0, 4, 8, 12, 1, 5, 9, 13, 2, 6, 10, 14, 3, 7, 11, 15};
-const InvTerm kInvTerms[16][6] = {
-    {{1, 5, 10, 15}, {-1, 5, 11, 14}, {-1, 9, 6, 15}, {1, 9, 7, 14}, {1, 13, 6, 11}, {-1, 13, 7, 10}},
-    {{-1, 4, 10, 15}, {1, 4, 11, 14}, {1, 8, 6, 15}, {-1, 8, 7, 14}, {-1, 12, 6, 11}, {1, 12, 7, 10}},
-    {{1, 4, 9, 15}, {-1, 4, 11, 13}, {-1, 8, 5, 15}, {1, 8, 7, 13}, {1, 12, 5, 11}, {-1, 12, 7, 9}},
-    {{-1, 4, 9, 14}, {1, 4, 10, 13}, {1, 8, 5, 14}, {-1, 8, 6, 13}, {-1, 12, 5, 10}, {1, 12, 6, 9}},
-    {{-1, 1, 10, 15}, {1, 1, 11, 14}, {1, 9, 2, 15}, {-1, 9, 3, 14}, {-1, 13, 2, 11}, {1, 13, 3, 10}},
-    {{1, 0, 10, 15}, {-1, 0, 11, 14}, {-1, 8, 2, 15}, {1, 8, 3, 14}, {1, 12, 2, 11}, {-1, 12, 3, 10}},
-    {{-1, 0, 9, 15}, {1, 0, 11, 13}, {1, 8, 1, 15}, {-1, 8, 3, 13}, {-1, 12, 1, 11}, {1, 12, 3, 9}},
-    {{1, 0, 9, 14}, {-1, 0, 10, 13}, {-1, 8, 1, 14}, {1, 8, 2, 13}, {1, 12, 1, 10}, {-1, 12, 2, 9}},
-    {{1, 1, 6, 15}, {-1, 1, 7, 14}, {-1, 5, 2, 15}, {1, 5, 3, 14}, {1, 13, 2, 7}, {-1, 13, 3, 6}},
-    {{-1, 0, 6, 15}, {1, 0, 7, 14}, {1, 4, 2, 15}, {-1, 4, 3, 14}, {-1, 12, 2, 7}, {1, 12, 3, 6}},
-    {{1, 0, 5, 15}, {-1, 0, 7, 13}, {-1, 4, 1, 15}, {1, 4, 3, 13}, {1, 12, 1, 7}, {-1, 12, 3, 5}},
-    {{-1, 0, 5, 14}, {1, 0, 6, 13}, {1, 4, 1, 14}, {-1, 4, 2, 13}, {-1, 12, 1, 6}, {1, 12, 2, 5}},
-    {{-1, 1, 6, 11}, {1, 1, 7, 10}, {1, 5, 2, 11}, {-1, 5, 3, 10}, {-1, 9, 2, 7}, {1, 9, 3, 6}},
-    {{1, 0, 6, 11}, {-1, 0, 7, 10}, {-1, 4, 2, 11}, {1, 4, 3, 10}, {1, 8, 2, 7}, {-1, 8, 3, 6}},
-    {{-1, 0, 5, 11}, {1, 0, 7, 9}, {1, 4, 1, 11}, {-1, 4, 3, 9}, {-1, 8, 1, 7}, {1, 8, 3, 5}},
-    {{1, 0, 5, 10}, {-1, 0, 6, 9}, {-1, 4, 1, 10}, {1, 4, 2, 9}, {1, 8, 1, 6}, {-1, 8, 2, 5}},
-};
-void matrix4_inverse(const float m[16], float c[16]) {
-  float inv[16];
-  for (int e = 0; e < 16; ++e) {
-    float acc = 0.0f;
-    for (int k = 0; k < 6; ++k) {
-      const InvTerm& t = kInvTerms[e][k];
-      const float v = (m[t.a] * m[t.b]) * m[t.c];
-      acc = k == 0 ? (t.s > 0 ? v : -v) : (t.s > 0 ? acc + v : acc - v);
-    }
-    inv[kInvOut[e]] = acc;
-  }
-  float det = ((m[0] * inv[0] + m[1] * inv[4]) + m[2] * inv[8]) + m[3] * inv[12];
-  for (int i = 0; i < 16; ++i) c[i] = 0.0f;
-  if (det == 0.0f) return;
-  det = 1.0f / det;
-  for (int i = 0; i < 16; ++i) c[i] = inv[i] * det;
-}
+void matrix4_inverse(const float m[16], float c[16]) { vmr::anim::inverse(m, c); }
 
 int refresh_top(vmr_ctx* ctx) {
   TopRec& t = ctx->top;
@@ -269,12 +232,17 @@ int refresh_top(vmr_ctx* ctx) {
   d.meshes = t.meshes.as<DMesh>();
   d.n_geoms = (uint32_t)t.host.geom_order.size();
   d.all_static = d.keys == 1 ? 1u : 0u;
+  d.simple_only = 0u;
   for (int k = 0; k < 3; ++k) {
     t.bounds6[k] = INFINITY;
     t.bounds6[3 + k] = -INFINITY;
   }
   for (uint32_t g : t.host.geom_order) {
     if (ctx->meshes[g]->host.motion() || ctx->meshes[g]->has_xf) d.all_static = 0u;
+    if (ctx->meshes[g]->host.group || ctx->meshes[g]->xkeys.size() >= 2) {
+      d.simple_only = 1u;
+      d.all_static = 0u;
+    }
     for (int k = 0; k < 3; ++k) {
       t.bounds6[k] = std::min(t.bounds6[k], ctx->meshes[g]->bounds6[k]);
       t.bounds6[3 + k] = std::max(t.bounds6[3 + k], ctx->meshes[g]->bounds6[3 + k]);
@@ -687,6 +655,8 @@ int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n) {
   std::vector<uint32_t> ids(geoms, geoms + n);
   for (uint32_t i = 0; i < n; ++i) {
     if (geoms[i] >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+    if (ctx->meshes[geoms[i]]->owner >= 0)
+      return fail(ctx, VMR_ERR_INVALID, "a Proc's child geom is traced through its Proc, not from the scene");
     ms[i] = &ctx->meshes[geoms[i]]->host;
   }
   if (ctx->device >= 0) cudaSetDevice(ctx->device);
@@ -697,11 +667,123 @@ int vmr_scene_build(vmr_ctx* ctx, const uint32_t* geoms, uint32_t n) {
   return refresh_top(ctx);
 }
 
+namespace {
+// Decomposes n transform keys into rec.xkeys and uploads them (device
+// contexts).  Returns a CUDA error or cudaSuccess.
+cudaError_t set_keys(vmr_ctx* ctx, MeshRec& rec, const float* keys16, uint32_t n) {
+  rec.xkeys.resize(n);
+  for (uint32_t i = 0; i < n; ++i) vmr::anim::decompose(keys16 + 16 * i, rec.xkeys[i]);
+  if (ctx->device < 0 || n < 2) return cudaSuccess;
+  cudaError_t e = rec.dxkeys.ensure(sizeof(vmr::anim::Decomp) * n);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(rec.dxkeys.p, rec.xkeys.data(), sizeof(vmr::anim::Decomp) * n, cudaMemcpyHostToDevice);
+  return e;
+}
+
+// A new GeomInstance / Proc record: its transform keys (one key: the matrix
+// rebuilt from the decomposition, as TimeKey returns it), the given bounds
+// grown as BoundingBox.GrowVec3 does (BMin, then BMax), its children.
+int add_group(vmr_ctx* ctx, int group, const uint32_t* children, uint32_t n_children, const float* keys16,
+              uint32_t n_keys, const float bmin[3], const float bmax[3], int motion_keys, uint32_t* out_geom) {
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  auto rec = std::make_unique<MeshRec>();
+  const uint32_t id = (uint32_t)ctx->meshes.size();
+  HostMesh& h = rec->host;
+  h.group = group;
+  h.group_keys = motion_keys;
+  for (int k = 0; k < 3; ++k) {
+    float lo = INFINITY, hi = -INFINITY;
+    lo = bmin[k] < lo ? bmin[k] : lo;
+    hi = bmin[k] > hi ? bmin[k] : hi;
+    lo = bmax[k] < lo ? bmax[k] : lo;
+    hi = bmax[k] > hi ? bmax[k] : hi;
+    h.bounds.lo[k] = lo;
+    h.bounds.hi[k] = hi;
+    rec->bounds6[k] = lo;
+    rec->bounds6[3 + k] = hi;
+  }
+  VMR_CUDA(ctx, set_keys(ctx, *rec, keys16, n_keys));
+  if (n_keys == 1) {
+    rec->has_xf = true;
+    vmr::anim::compose(rec->xkeys[0], rec->xf);
+    vmr::anim::inverse(rec->xf, rec->xf_inv);
+  }
+  rec->children.assign(children, children + n_children);
+  for (uint32_t i = 0; i < n_children; ++i) rec->child_hit.push_back(group == 1 ? (int32_t)id : (int32_t)children[i]);
+  DMesh d{};
+  d.kind = vmr::kGroup;
+  d.group = (uint32_t)group;
+  d.keys = 1;
+  d.iter_cap = 2;
+  if (ctx->device >= 0) {
+    VMR_CUDA(ctx, upload(ctx, rec->dchildren, rec->children));
+    VMR_CUDA(ctx, upload(ctx, rec->dchild_hit, rec->child_hit));
+    VMR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    d.children = rec->dchildren.as<uint32_t>();
+    d.child_hit = rec->dchild_hit.as<int32_t>();
+  }
+  d.n_children = n_children;
+  fill_xf(*rec, d);
+  rec->dmesh = d;
+  ctx->meshes.push_back(std::move(rec));
+  if (out_geom) *out_geom = id;
+  return VMR_OK;
+}
+}  // namespace
+
+int vmr_instance_add(vmr_ctx* ctx, uint32_t of, const float* keys16, uint32_t n_keys, const float bmin[3],
+                     const float bmax[3], uint32_t* out_geom) {
+  if (!ctx || !keys16 || n_keys < 1 || !bmin || !bmax) return VMR_ERR_INVALID;
+  if (of >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+  const MeshRec& c = *ctx->meshes[of];
+  if (c.host.group) return fail(ctx, VMR_ERR_UNSUPPORTED, "an instance of an instance or Proc is not supported");
+  if (c.owner >= 0) return fail(ctx, VMR_ERR_INVALID, "a Proc's child geom cannot be instanced");
+  // Instance.MotionKeys is the instanced geom's (instance.go:144-148)
+  return add_group(ctx, 1, &of, 1, keys16, n_keys, bmin, bmax, c.host.motion_keys(), out_geom);
+}
+
+int vmr_proc_add(vmr_ctx* ctx, const uint32_t* children, uint32_t n, const float* keys16, uint32_t n_keys,
+                 const float bmin[3], const float bmax[3], uint32_t* out_geom) {
+  if (!ctx || !children || n == 0 || (n_keys && !keys16) || !bmin || !bmax) return VMR_ERR_INVALID;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (children[i] >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+    const MeshRec& c = *ctx->meshes[children[i]];
+    if (c.host.group) return fail(ctx, VMR_ERR_UNSUPPORTED, "a Proc's children are meshes or spheres");
+    if (c.owner >= 0) return fail(ctx, VMR_ERR_INVALID, "a geom belongs to one Proc at most");
+    for (uint32_t j = 0; j < i; ++j)
+      if (children[j] == children[i]) return fail(ctx, VMR_ERR_INVALID, "a Proc lists a geom twice");
+  }
+  static const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  // Proc.PreRender: no Transform is one identity key (proc.go:157-160)
+  const uint32_t nk = n_keys ? n_keys : 1u;
+  int rc = add_group(ctx, 2, children, n, n_keys ? keys16 : kIdentity, nk, bmin, bmax, (int)nk, out_geom);
+  if (rc != VMR_OK) return rc;
+  for (uint32_t i = 0; i < n; ++i) ctx->meshes[children[i]]->owner = (int32_t)*out_geom;
+  return VMR_OK;
+}
+
+int vmr_mesh_set_transform_keys(vmr_ctx* ctx, uint32_t geom, const float* keys16, uint32_t n_keys) {
+  if (!ctx || (n_keys && !keys16)) return VMR_ERR_INVALID;
+  if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
+  if (n_keys <= 1) return vmr_mesh_set_transform(ctx, geom, n_keys ? keys16 : nullptr);
+  MeshRec& rec = *ctx->meshes[geom];
+  if (rec.host.sphere || rec.host.group)
+    return fail(ctx, VMR_ERR_UNSUPPORTED, "transform keys apply to meshes (PolyMesh.Transform)");
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  rec.has_xf = false;
+  VMR_CUDA(ctx, set_keys(ctx, rec, keys16, n_keys));
+  fill_xf(rec, rec.dmesh);
+  if (ctx->top.valid) return refresh_top(ctx);
+  return VMR_OK;
+}
+
 int vmr_mesh_set_transform(vmr_ctx* ctx, uint32_t geom, const float* m) {
   if (!ctx) return VMR_ERR_INVALID;
   if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
   MeshRec& rec = *ctx->meshes[geom];
   if (m && rec.host.sphere) return fail(ctx, VMR_ERR_UNSUPPORTED, "an analytic sphere takes no transform");
+  if (rec.host.group) return fail(ctx, VMR_ERR_UNSUPPORTED, "an instance or Proc takes its transform when added");
+  rec.xkeys.clear();
   rec.has_xf = m != nullptr;
   if (m) {
     std::memcpy(rec.xf, m, sizeof(rec.xf));
@@ -754,8 +836,8 @@ int vmr_trace_mesh(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, 
   if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "bad geom id");
   cudaSetDevice(ctx->device);
   const DMesh* m = &ctx->meshes[geom]->dmesh;
-  if (ctx->meshes[geom]->host.sphere)
-    return fail(ctx, VMR_ERR_UNSUPPORTED, "a sphere geom is traced through the scene (vmr_trace_scene)");
+  if (ctx->meshes[geom]->host.sphere || ctx->meshes[geom]->host.group)
+    return fail(ctx, VMR_ERR_UNSUPPORTED, "sphere, instance and Proc geoms are traced through the scene (vmr_trace_scene)");
   if (ctx->meshes[geom]->host.n_tris == 0) return fail(ctx, VMR_ERR_INVALID, "empty mesh");
   if (flags & VMR_TRACE_DEVICE) return run_trace(ctx, m, *rays, n, flags, *hits, stats);
   return trace_host(ctx, m, rays, n, flags, hits, stats);
@@ -784,6 +866,7 @@ int vmr_autotune(vmr_ctx* ctx, uint32_t geom, const vmr_rays* rays, size_t n, in
   if (ctx->device < 0) return fail(ctx, VMR_ERR_UNSUPPORTED, "host-only context cannot trace");
   if (geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "no such geom");
   MeshRec& mr = *ctx->meshes[geom];
+  if (mr.host.group) return fail(ctx, VMR_ERR_UNSUPPORTED, "instances and Procs are not autotuned");
   if (mr.host.n_tris == 0) return fail(ctx, VMR_ERR_INVALID, "empty mesh");
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
@@ -863,6 +946,8 @@ int vmr_trace_jobs(vmr_ctx* ctx, const vmr_trace_job* jobs, uint32_t n_jobs, int
   for (uint32_t j = 0; j < n_jobs; ++j) {
     const vmr_trace_job& J = jobs[j];
     if (J.geom >= ctx->meshes.size()) return fail(ctx, VMR_ERR_INVALID, "job geom out of range");
+    if (ctx->meshes[J.geom]->host.group || ctx->meshes[J.geom]->xkeys.size() >= 2)
+      return fail(ctx, VMR_ERR_UNSUPPORTED, "job geoms are meshes (instances, Procs and keyed transforms are not)");
     const vmr_rays& r = J.rays;
     const vmr_hits& h = J.hits;
     if (J.n && (!r.px || !r.py || !r.pz || !r.dx || !r.dy || !r.dz || !r.tmax))

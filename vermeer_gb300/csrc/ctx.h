@@ -48,9 +48,22 @@ struct MeshRec {
   bool has_normals = false;
   DevBuf shlist, sidx, nrm;
   DevBuf avert, aidx;  // motion meshes: key-major vertices (float4) and face-order idxp for hit attributes
-  // PolyMesh.Transform (one matrix, column-major) and its Matrix4Inverse
+  // PolyMesh.Transform (one matrix, column-major) and its Matrix4Inverse;
+  // a GeomInstance's or Proc's transform when it has one key (the matrix
+  // rebuilt from its decomposition, as TimeKey returns it)
   bool has_xf = false;
   float xf[16] = {}, xf_inv[16] = {};
+  // Transform keys decomposed (two or more keys: blended at each ray's time)
+  std::vector<anim::Decomp> xkeys;
+  DevBuf dxkeys;
+  // GeomInstance / Proc (host.group != 0): the geoms it traces and the id
+  // a hit in each reports
+  std::vector<uint32_t> children;
+  std::vector<int32_t> child_hit;
+  DevBuf dchildren, dchild_hit;
+  // A Proc's child: the Proc's geom id (such a geom is traced only through
+  // its Proc, never from the top level); -1 otherwise
+  int32_t owner = -1;
   // the autotuner's choice for this mesh (vmr_autotune)
   bool tuned = false;
   vmr_tuning tuning{};
@@ -73,6 +86,13 @@ struct RenderState {
   float env[3] = {0.f, 0.f, 0.f};
   vmr_camera camera{};
   bool has_camera = false;
+  // Camera.LocalToWorld keys decomposed (camera.go:207-236); cam_used is the
+  // camera the kernels see: m rebuilt from the decomposition for one key
+  // (the reference's round trip), key 0 otherwise (the kernels blend
+  // dcam_keys per sample)
+  std::vector<anim::Decomp> cam_keys;
+  DevBuf dcam_keys;
+  vmr_camera cam_used{};
   // pixel filter (vmr_set_pixel_filter): filter_n = 0 is none; the device
   // table holds cdfV (n) then cdfVU (n x n) as float64
   uint32_t filter_n = 0;
@@ -108,6 +128,10 @@ struct TopRec {
   float bounds6[6] = {0, 0, 0, 0, 0, 0};  // union of the geoms' bounds (ray reordering)
   bool valid = false;
 };
+
+// The camera the kernels see for a vmr_camera: m replaced by the matrix the
+// reference rebuilds from its decomposition (render.cu).
+vmr_camera camera_round_trip(const vmr_camera& c);
 
 }  // namespace vmr
 

@@ -17,6 +17,8 @@
 #pragma once
 #include <cstdint>
 
+#include "animdecomp.h"
+
 #ifndef __CUDACC__
 struct float4_host { float x, y, z, w; };
 #endif
@@ -61,14 +63,24 @@ struct DMesh {
   float lower_static;       // EpsilonFloat32 + RayBias (trace.go:182)
   float ray_bias;           // motion lower bound (trace.go:612)
   uint32_t iter_cap;        // 4 * nodes + 2: a traversal pops each entry once
-  uint32_t kind;            // 0 triangles, 1 analytic sphere (builtin/geom/sphere)
+  uint32_t kind;            // kTriangles, kSphere, or kGroup
   float sphere[4];          // centre, radius
   uint32_t has_xf;          // PolyMesh.Transform: rays enter through xf_inv
-  uint32_t pad[2];
+  uint32_t xf_nkeys;        // >= 2: the transform is blended per ray from xf_keys
+  uint32_t pad;
   // Matrix4Inverse of the transform, columns 0..3 rows 0..2 (column-major
   // elements 0,1,2, 4,5,6, 8,9,10, 12,13,14)
   float xf_inv[12];
+  const anim::Decomp* xf_keys;  // decomposed transform keys (xf_nkeys >= 2)
+  // kGroup (GeomInstance: group 1, Proc: group 2): the transform (has_xf /
+  // xf_keys as above), the geoms traced in order and the geom id a hit in
+  // each reports
+  const uint32_t* children;
+  const int32_t* child_hit;
+  uint32_t n_children;
+  uint32_t group;
 };
+enum MeshKind : uint32_t { kTriangles = 0, kSphere = 1, kGroup = 2 };
 
 // Top level of a scene (builtin/scene): static GNodes or motion MNodes with
 // boxes; leaves index geom_order (leaf position -> geom id).
@@ -84,7 +96,8 @@ struct DTop {
   uint32_t iter_cap;
   uint32_t all_static;  // static top level and only static meshes: the
                         // while-while scene kernel applies
-  uint32_t pad;
+  uint32_t simple_only; // instances, Procs or keyed transforms: the
+                        // single-loop scene kernel only
 };
 
 struct RaySoA {

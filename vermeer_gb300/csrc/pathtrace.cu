@@ -88,6 +88,8 @@ struct PtBatch {
   float sel;          // 1/nl
   uint64_t seed;
   vmr_camera cam;
+  const anim::Decomp* cam_keys;  // camera motion keys (cam_nkeys >= 2), else null
+  uint32_t cam_nkeys;
   PixFilter filt;     // pixel filter tables (n = 0: none)
   const PtIter* it;
   const vmr_shader_std* shaders;
@@ -386,9 +388,10 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
       const PtJob& job = b.jobs[lo];
       pix -= job.pix0;
       b.pgeom[s] = job.geom;
-      camera_primary(job.cam, job.width, job.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+      camera_primary(job.cam, nullptr, 0, job.width, job.height, j, pix, b.seed, b.filt, P, D, time, lambda);
     } else {
-      camera_primary(b.cam, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+      camera_primary(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D, time,
+                     lambda);
     }
     const float o[3] = {P.x, P.y, P.z};
     put_ray(b.qray[0], b.cap, s, o, D, __int_as_float(0x7f800000), time);
@@ -1016,10 +1019,17 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   auto& R = ctx->render;
   for (uint32_t g : used_geoms) {
     const auto& mr = ctx->meshes[g];
+    if (mr->host.group || mr->xkeys.size() >= 2)
+      return pfail(ctx, VMR_ERR_UNSUPPORTED,
+                   "the extended path tracer takes meshes, spheres and one-matrix transforms "
+                   "(instances, Procs and transform keys render in reference mode, vmr_render)");
     if (mr->host.motion() && mr->aidx.p == nullptr)
       return pfail(ctx, VMR_ERR_INVALID, "a motion mesh in the scene has no shading (vmr_mesh_set_shading)");
-    for (uint32_t sid : mr->shader_list)
+    for (uint32_t sid : mr->shader_list) {
       if (sid >= R.shaders.size()) return pfail(ctx, VMR_ERR_INVALID, "mesh shader id out of range");
+      if (R.shaders[sid].flags & VMR_SH_DEBUG)
+        return pfail(ctx, VMR_ERR_UNSUPPORTED, "DebugShader renders in reference mode (vmr_render)");
+    }
   }
   // Light list: TriLights, quad lights, environment.
   const uint32_t n_geoms = (uint32_t)ctx->meshes.size();
@@ -1068,25 +1078,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     lights.push_back(l);
   }
   const uint32_t nl = (uint32_t)lights.size();
-  std::vector<RMesh> rm(ctx->meshes.size());
-  for (size_t g = 0; g < ctx->meshes.size(); ++g) {
-    MeshRec& mr = *ctx->meshes[g];
-    rm[g].tris = reinterpret_cast<const float4*>(mr.tris.p);
-    rm[g].nrm = mr.has_normals ? reinterpret_cast<const float4*>(mr.nrm.p) : nullptr;
-    rm[g].sidx = mr.host.shader_idx.empty() ? nullptr : mr.sidx.as<uint8_t>();
-    rm[g].shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
-    rm[g].n_shaders = (uint32_t)mr.shader_list.size();
-    rm[g].kind = mr.host.sphere ? 1u : 0u;
-    for (int k = 0; k < 3; ++k) rm[g].sphere[k] = mr.host.sphere_c[k];
-    rm[g].sphere[3] = mr.host.sphere_r;
-    rm[g].keys = mr.host.motion() ? mr.host.keys : 1u;
-    rm[g].n_verts = mr.host.n_verts;
-    rm[g].mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
-    rm[g].midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
-    rm[g].has_xf = mr.has_xf ? 1u : 0u;
-    std::memcpy(rm[g].xf, mr.xf, sizeof(mr.xf));
-    std::memcpy(rm[g].xf_inv, mr.xf_inv, sizeof(mr.xf_inv));
-  }
+  const std::vector<RMesh> rm = rmesh_table(ctx);
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
   const uint32_t npix = jobs ? (uint32_t)npix_jobs : p->width * p->height;
@@ -1164,7 +1156,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     uint32_t pix0 = 0;
     for (uint32_t k = 0; k < n_jobs; ++k) {
       PtJob j{};
-      j.cam = jobs[k].camera;
+      j.cam = camera_round_trip(jobs[k].camera);
       j.width = jobs[k].width;
       j.height = jobs[k].height;
       j.npix = j.width * j.height;
@@ -1192,7 +1184,9 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   std::memcpy(b.env, R.env, 12);
   b.sel = nl > 0 ? 1.0f / (float)nl : 0.0f;
   b.seed = p->seed;
-  b.cam = R.camera;
+  b.cam = R.cam_used;
+  b.cam_nkeys = R.cam_keys.size() >= 2 ? (uint32_t)R.cam_keys.size() : 0u;
+  b.cam_keys = b.cam_nkeys ? R.dcam_keys.as<const anim::Decomp>() : nullptr;
   b.filt = PixFilter{R.filter_n ? R.filter.as<const double>() : nullptr, R.filter_n, R.filter_w};
   b.it = reinterpret_cast<const PtIter*>(base + o_it);
   b.shaders = reinterpret_cast<const vmr_shader_std*>(base + o_shader);
@@ -1318,6 +1312,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
       for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
     };
     fold(&b.cam, sizeof(b.cam));
+    fold(&b.cam_keys, sizeof(b.cam_keys));
+    fold(&b.cam_nkeys, sizeof(b.cam_nkeys));
     fold(&b.filt, sizeof(b.filt));
     fold(b.env, sizeof(b.env));
     fold(&b.sel, sizeof(b.sel));

@@ -252,6 +252,8 @@ struct RenderBatch {
   uint32_t pad;
   uint64_t seed;
   vmr_camera cam;
+  const anim::Decomp* cam_keys;  // camera motion keys (cam_nkeys >= 2), else null
+  uint32_t cam_nkeys;
   PixFilter filt;     // pixel filter tables (n = 0: none)
   const vmr_shader_std* shaders;
   const RLight* lights;
@@ -276,7 +278,7 @@ __global__ void k_generate(RenderBatch b) {
   const uint32_t j = b.iter0 + (uint32_t)(s / b.npix) + 1;  // render(iter+1)
   V3 P, D;
   float time, lambda;
-  camera_primary(b.cam, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+  camera_primary(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
   const Level& L = b.lv[0];
   *ray_f(L, 0, s) = P.x; *ray_f(L, 1, s) = P.y; *ray_f(L, 2, s) = P.z;
   *ray_f(L, 3, s) = D.x; *ray_f(L, 4, s) = D.y; *ray_f(L, 5, s) = D.z;
@@ -416,6 +418,12 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
     sc.scr1 = scramble(b.seed, pix, 5);
     sc.geom = geom;
     lv.shader[e] = (int32_t)shid;
+    if (sh.flags & VMR_SH_DEBUG) {  // Debug.Eval: OutRGB = Colour (debug.go:47-49)
+      em[0] = sh.diffuse_colour[0];
+      em[1] = sh.diffuse_colour[1];
+      em[2] = sh.diffuse_colour[2];
+      continue;
+    }
     const RGB ec = emission(sh);
     em[0] = ec.c[0];
     em[1] = ec.c[1];
@@ -666,6 +674,19 @@ int rfail(vmr_ctx* ctx, int code, const std::string& msg) {
 
 }  // namespace
 
+namespace vmr {
+// The camera as the kernels see it: m replaced by the matrix the reference
+// computes from it, TransformDecompToMatrix4(TransformDecompLerp(d, d, 0))
+// of d = TransformDecompMatrix4(m) (camera.go:207-236), which is not m.
+vmr_camera camera_round_trip(const vmr_camera& c) {
+  vmr_camera o = c;
+  anim::Decomp d;
+  anim::decompose(c.m, d);
+  anim::at_time(&d, 1, 0.0f, true, o.m);
+  return o;
+}
+}  // namespace vmr
+
 extern "C" {
 
 int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n) {
@@ -677,6 +698,7 @@ int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n) {
 int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, uint32_t n_shaders, const float* normals) {
   if (!ctx || geom >= ctx->meshes.size() || (n_shaders && !shaders)) return VMR_ERR_INVALID;
   MeshRec& rec = *ctx->meshes[geom];
+  if (rec.host.group) return rfail(ctx, VMR_ERR_UNSUPPORTED, "an instance or Proc shades through its geoms");
   if (rec.host.motion() && normals)
     return rfail(ctx, VMR_ERR_UNSUPPORTED, "normals of motion meshes are not supported");
   rec.shader_list.assign(shaders, shaders + n_shaders);
@@ -741,11 +763,41 @@ int vmr_set_sphere_lights(vmr_ctx* ctx, const vmr_sphere_light* lights, uint32_t
   return VMR_OK;
 }
 
+
 int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* cam) {
   if (!ctx || !cam) return VMR_ERR_INVALID;
   if (!(cam->radius >= 0.0f)) return rfail(ctx, VMR_ERR_INVALID, "camera radius must be >= 0");
-  ctx->render.camera = *cam;
-  ctx->render.has_camera = true;
+  auto& R = ctx->render;
+  R.camera = *cam;
+  R.has_camera = true;
+  R.cam_keys.resize(1);
+  vmr::anim::decompose(cam->m, R.cam_keys[0]);
+  R.cam_used = vmr::camera_round_trip(*cam);
+  return VMR_OK;
+}
+
+int vmr_transform_keys_at(const float* keys16, uint32_t n_keys, float time, int blend_one, float* out16) {
+  if (!keys16 || !out16 || n_keys < 1) return VMR_ERR_INVALID;
+  std::vector<vmr::anim::Decomp> k(n_keys);
+  for (uint32_t i = 0; i < n_keys; ++i) vmr::anim::decompose(keys16 + 16 * i, k[i]);
+  return vmr::anim::at_time(k.data(), n_keys, time, blend_one != 0, out16) ? VMR_OK : VMR_ERR_INVALID;
+}
+
+int vmr_set_camera_keys(vmr_ctx* ctx, const float* keys16, uint32_t n_keys) {
+  if (!ctx || !keys16 || n_keys < 1) return VMR_ERR_INVALID;
+  auto& R = ctx->render;
+  if (!R.has_camera) return rfail(ctx, VMR_ERR_INVALID, "set the camera (vmr_set_camera) before its keys");
+  vmr_camera c = R.camera;
+  std::memcpy(c.m, keys16, sizeof(c.m));
+  int rc = vmr_set_camera(ctx, &c);
+  if (rc != VMR_OK || n_keys == 1) return rc;
+  R.cam_keys.resize(n_keys);
+  for (uint32_t i = 0; i < n_keys; ++i) vmr::anim::decompose(keys16 + 16 * i, R.cam_keys[i]);
+  if (ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    RCUDA(R.dcam_keys.ensure(sizeof(vmr::anim::Decomp) * n_keys));
+    RCUDA(cudaMemcpy(R.dcam_keys.p, R.cam_keys.data(), sizeof(vmr::anim::Decomp) * n_keys, cudaMemcpyHostToDevice));
+  }
   return VMR_OK;
 }
 
@@ -767,35 +819,23 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   for (const auto& L : R.spheres)
     if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
       return rfail(ctx, VMR_ERR_INVALID, "sphere light shader or geom out of range");
+  std::vector<uint32_t> shaded;  // the geoms whose shading data hits read
   for (uint32_t g : ctx->top.host.geom_order) {
-    const auto& mr = ctx->meshes[g];
-    if (mr->host.motion() && mr->aidx.p == nullptr)
+    const MeshRec& gr = *ctx->meshes[g];
+    if (gr.host.group == 2) shaded.insert(shaded.end(), gr.children.begin(), gr.children.end());
+    else shaded.push_back(g);
+  }
+  for (uint32_t g : shaded) {
+    const MeshRec& mr = shading_rec(ctx, g);
+    if (mr.host.motion() && mr.aidx.p == nullptr)
       return rfail(ctx, VMR_ERR_INVALID, "a motion mesh in the scene has no shading (vmr_mesh_set_shading)");
-    for (uint32_t sid : mr->shader_list)
+    for (uint32_t sid : mr.shader_list)
       if (sid >= R.shaders.size()) return rfail(ctx, VMR_ERR_INVALID, "mesh shader id out of range");
   }
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
   // Scene tables.
-  std::vector<RMesh> rm(ctx->meshes.size());
-  for (size_t g = 0; g < ctx->meshes.size(); ++g) {
-    MeshRec& mr = *ctx->meshes[g];
-    rm[g].tris = reinterpret_cast<const float4*>(mr.tris.p);
-    rm[g].nrm = mr.has_normals ? reinterpret_cast<const float4*>(mr.nrm.p) : nullptr;
-    rm[g].sidx = mr.host.shader_idx.empty() ? nullptr : mr.sidx.as<uint8_t>();
-    rm[g].shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
-    rm[g].n_shaders = (uint32_t)mr.shader_list.size();
-    rm[g].kind = mr.host.sphere ? 1u : 0u;
-    for (int k = 0; k < 3; ++k) rm[g].sphere[k] = mr.host.sphere_c[k];
-    rm[g].sphere[3] = mr.host.sphere_r;
-    rm[g].keys = mr.host.motion() ? mr.host.keys : 1u;
-    rm[g].n_verts = mr.host.n_verts;
-    rm[g].mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
-    rm[g].midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
-    rm[g].has_xf = mr.has_xf ? 1u : 0u;
-    std::memcpy(rm[g].xf, mr.xf, sizeof(mr.xf));
-    std::memcpy(rm[g].xf_inv, mr.xf_inv, sizeof(mr.xf_inv));
-  }
+  const std::vector<RMesh> rm = rmesh_table(ctx);
   std::vector<RLight> rl(R.lights.size() + R.disks.size() + R.spheres.size());
   uint32_t ns = 1;
   for (size_t i = 0; i < R.lights.size(); ++i) {
@@ -905,7 +945,9 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   b.nl = nl;
   b.levels = levels;
   b.seed = p->seed;
-  b.cam = R.camera;
+  b.cam = R.cam_used;
+  b.cam_nkeys = R.cam_keys.size() >= 2 ? (uint32_t)R.cam_keys.size() : 0u;
+  b.cam_keys = b.cam_nkeys ? R.dcam_keys.as<const anim::Decomp>() : nullptr;
   b.filt = PixFilter{R.filter_n ? R.filter.as<const double>() : nullptr, R.filter_n, R.filter_w};
   b.shaders = reinterpret_cast<const vmr_shader_std*>(base + o_shaders);
   b.lights = reinterpret_cast<const RLight*>(base + o_lights);

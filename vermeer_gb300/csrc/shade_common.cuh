@@ -14,7 +14,9 @@
 
 #include <cstdint>
 
+#include "animdecomp.h"
 #include "colour_tables.h"
+#include "ctx.h"
 #include "pixfilter.h"
 #include "vmr.h"
 
@@ -301,6 +303,16 @@ struct RMesh {
   // PolyMesh.Transform: the matrix and its Matrix4Inverse, column-major
   uint32_t has_xf;
   float xf[16], xf_inv[16];
+  // PolyMesh.Transform of two or more keys (blended at the ray's time)
+  const anim::Decomp* xf_keys;
+  uint32_t xf_nkeys;
+  // The GeomInstance or Proc through which this geom's hits are reached:
+  // on a hit its transform becomes the shading context's
+  // (instance.go:105-110, proc.go:133-138).  outer_nkeys 0: none; 1: the
+  // matrix and inverse below; >= 2: blended from outer_keys at the ray's time.
+  uint32_t outer_nkeys;
+  const anim::Decomp* outer_keys;
+  float outer_xf[16], outer_inv[16];
 };
 struct RLight {
   float p[9];        // TriLight: p0, p1, p2
@@ -472,13 +484,25 @@ __device__ __forceinline__ void uniform_disk(float radius, float r0, float r1, f
   yo = radius * r * gsin(theta);
 }
 
+// The camera matrix of a sample with camera motion keys
+// (Camera.ComputeRay, camera.go:223-236): the keys around the sample's time
+// blended and rebuilt.  Not inlined: once per camera ray.
+__device__ __noinline__ void camera_keyed(const anim::Decomp* keys, uint32_t n, float time, float* M) {
+  if (!anim::at_time(keys, n, time, true, M))
+    for (int i = 0; i < 16; ++i) M[i] = 0.0f;
+}
+
 // core.Render's per-sample setup (core/render.go:89-120) and a pinhole
 // Camera.ComputeRay (builtin/camera/camera.go:244-284) for iteration j
 // (render(iter+1)) of pixel pix: RasterXY position, VdC time and hero
-// wavelength with the pixel's scrambles, the ray through LocalToWorld.
-__device__ __forceinline__ void camera_primary(const vmr_camera& c, uint32_t width, uint32_t height, uint32_t j,
-                                               uint32_t pix, uint64_t seed, const PixFilter& filt, V3& P, V3& D,
-                                               float& time, float& lambda) {
+// wavelength with the pixel's scrambles, the ray through the camera matrix:
+// c.m (the host rebuilt it from its decomposition, as the reference does
+// for one key) or, with two or more keys (ckeys, cnk), the keys blended at
+// the sample's time.
+__device__ __forceinline__ void camera_primary(const vmr_camera& c, const anim::Decomp* ckeys, uint32_t cnk,
+                                               uint32_t width, uint32_t height, uint32_t j, uint32_t pix,
+                                               uint64_t seed, const PixFilter& filt, V3& P, V3& D, float& time,
+                                               float& lambda) {
   const uint32_t x = pix % width, y = pix / width;
   double rx, ry;
   raster_xy(j, x, y, rx, ry);
@@ -496,7 +520,12 @@ __device__ __forceinline__ void camera_primary(const vmr_camera& c, uint32_t wid
   const float camu = Sx * c.tan_theta_focal;
   const float camv = Sy * (c.tan_theta_focal / c.aspect);
   const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
+  float Mk[16];
   const float* M = c.m;
+  if (cnk >= 2) {
+    camera_keyed(ckeys, cnk, time, Mk);
+    M = Mk;
+  }
   V3 e = v3(0, 0, 0), sv = s3;
   if (c.radius > 0.0f) {  // thin lens: UniformDisk2D at (lensU, lensV)
     const double lensU = vdc(j, scramble(seed, pix, 0)), lensV = sobol(j, scramble(seed, pix, 1));
@@ -580,27 +609,120 @@ __device__ __forceinline__ V3 xf_vec_t(const float* a, V3 b) {
             a[8] * b.x + a[9] * b.y + a[10] * b.z);
 }
 
-// The hit attributes of any geom kind.  A transformed mesh's object-space
-// attributes go to world space as the reference does after the mesh walk
-// and again in core.Trace: PolyMesh.Trace sets P = M Po and N = M^-T N
-// (builtin/geom/polymesh/trace.go:67-74), then ShaderContext.ApplyTransform
-// (core/shader.go:129-135) sets P = M Po, N = normalize(M^-T N) (a second
-// time), Ng = normalize(M^-T Ng), dPdu/dPdv = normalize(M dPdu/dPdv).
+// A keyed transform at a time and its Matrix4Inverse (not inlined: it runs
+// once per shaded hit on a keyed geom).
+__device__ __noinline__ void keyed_matrix(const anim::Decomp* keys, uint32_t n, float time, float* M, float* I) {
+  if (!anim::at_time(keys, n, time, false, M))
+    for (int i = 0; i < 16; ++i) M[i] = 0.0f;
+  anim::inverse(M, I);
+}
+
+// ShaderContext.ApplyTransform (core/shader.go:129-135): sc.P still holds
+// Po, the hit point in the space the geom was traced in.
+__device__ __forceinline__ void apply_transform(Ctx& sc, const float* T, const float* I) {
+  const V3 Po = sc.P;
+  sc.P = xf_point(T, Po);
+  sc.N = normalize(xf_vec_t(I, sc.N));
+  sc.Ng = normalize(xf_vec_t(I, sc.Ng));
+  sc.DdPdu = normalize(xf_vec(T, sc.DdPdu));
+  sc.DdPdv = normalize(xf_vec(T, sc.DdPdv));
+}
+
+// The hit attributes of any geom kind.  A transformed mesh's PolyMesh.Trace
+// sets P = M Po and N = M^-T N (builtin/geom/polymesh/trace.go:67-74) and
+// makes M the context's transform; a GeomInstance or Proc around the geom
+// makes its own transform the context's on a hit (instance.go:105-110,
+// proc.go:133-138); core.Trace then calls ShaderContext.ApplyTransform with
+// the context's transform (core/shader.go:129-135): P = T Po,
+// N = normalize(T^-T N), Ng = normalize(T^-T Ng), dPdu/dPdv =
+// normalize(T dPdu/dPdv).  Keyed transforms are taken at the ray's time.  A
+// sphere inside an instance or Proc takes the ray as its group mapped it.
 __device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim, float U, float V, float W, V3 Ro,
                                                    V3 Rd, float t, float time, Ctx& sc, uint32_t& shader_id) {
-  if (m.kind == 1) return sphere_attributes(m, Ro, Rd, t, sc, shader_id);
+  float OT[16], OI[16];
+  const float* ot = m.outer_xf;
+  const float* oi = m.outer_inv;
+  if (m.outer_nkeys >= 2) {
+    keyed_matrix(m.outer_keys, m.outer_nkeys, time, OT, OI);
+    ot = OT;
+    oi = OI;
+  }
+  if (m.outer_nkeys && m.kind == 1) {  // the ray its group traced (instance.go:91-93)
+    Ro = xf_point(oi, Ro);
+    Rd = xf_vec(oi, Rd);
+  }
+  if (m.kind == 1) {
+    const bool ok = sphere_attributes(m, Ro, Rd, t, sc, shader_id);
+    if (ok && m.outer_nkeys) apply_transform(sc, ot, oi);
+    return ok;
+  }
   const bool ok = m.keys > 1 ? motion_attributes(m, prim, U, V, W, time, sc, shader_id)
                              : hit_attributes(m, prim, U, V, W, sc, shader_id);
-  if (ok && m.has_xf) {
-    const V3 Po = sc.P;
-    sc.N = xf_vec_t(m.xf_inv, sc.N);
-    sc.P = xf_point(m.xf, Po);
-    sc.N = normalize(xf_vec_t(m.xf_inv, sc.N));
-    sc.Ng = normalize(xf_vec_t(m.xf_inv, sc.Ng));
-    sc.DdPdu = normalize(xf_vec(m.xf, sc.DdPdu));
-    sc.DdPdv = normalize(xf_vec(m.xf, sc.DdPdv));
+  if (!ok) return false;
+  float MT[16], MI[16];
+  const float* mt = m.xf;
+  const float* mi = m.xf_inv;
+  const bool own = m.has_xf || m.xf_nkeys >= 2;
+  if (m.xf_nkeys >= 2) {
+    keyed_matrix(m.xf_keys, m.xf_nkeys, time, MT, MI);
+    mt = MT;
+    mi = MI;
   }
-  return ok;
+  if (own) sc.N = xf_vec_t(mi, sc.N);  // PolyMesh.Trace (its P is replaced by ApplyTransform)
+  if (m.outer_nkeys) apply_transform(sc, ot, oi);
+  else if (own) apply_transform(sc, mt, mi);
+  return true;
+}
+
+// The shading table indexed by geom id (host side).  A GeomInstance shades
+// as the geom it instances, a Proc's child as itself; both with the group's
+// transform as the outer one.  Group ids never reach a shading kernel
+// otherwise (a Proc's hits report its children's ids).
+inline void fill_rmesh_one(const MeshRec& mr, RMesh& r) {
+  r = RMesh{};
+  r.tris = reinterpret_cast<const float4*>(mr.tris.p);
+  r.nrm = mr.has_normals ? reinterpret_cast<const float4*>(mr.nrm.p) : nullptr;
+  r.sidx = mr.host.shader_idx.empty() ? nullptr : mr.sidx.as<uint8_t>();
+  r.shaders = mr.shader_list.empty() ? nullptr : mr.shlist.as<uint32_t>();
+  r.n_shaders = (uint32_t)mr.shader_list.size();
+  r.kind = mr.host.sphere ? 1u : 0u;
+  for (int k = 0; k < 3; ++k) r.sphere[k] = mr.host.sphere_c[k];
+  r.sphere[3] = mr.host.sphere_r;
+  r.keys = mr.host.motion() ? mr.host.keys : 1u;
+  r.n_verts = mr.host.n_verts;
+  r.mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
+  r.midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
+  r.has_xf = mr.has_xf ? 1u : 0u;
+  std::memcpy(r.xf, mr.xf, sizeof(mr.xf));
+  std::memcpy(r.xf_inv, mr.xf_inv, sizeof(mr.xf_inv));
+  r.xf_nkeys = mr.xkeys.size() >= 2 ? (uint32_t)mr.xkeys.size() : 0u;
+  r.xf_keys = r.xf_nkeys ? mr.dxkeys.as<const anim::Decomp>() : nullptr;
+}
+inline void set_outer(const MeshRec& g, RMesh& r) {
+  r.outer_nkeys = (uint32_t)g.xkeys.size();
+  r.outer_keys = g.xkeys.size() >= 2 ? g.dxkeys.as<const anim::Decomp>() : nullptr;
+  std::memcpy(r.outer_xf, g.xf, sizeof(g.xf));
+  std::memcpy(r.outer_inv, g.xf_inv, sizeof(g.xf_inv));
+}
+inline std::vector<RMesh> rmesh_table(const vmr_ctx* ctx) {
+  std::vector<RMesh> rm(ctx->meshes.size());
+  for (size_t g = 0; g < ctx->meshes.size(); ++g) {
+    const MeshRec& mr = *ctx->meshes[g];
+    if (mr.host.group == 1) {
+      fill_rmesh_one(*ctx->meshes[mr.children[0]], rm[g]);
+      set_outer(mr, rm[g]);
+    } else {
+      fill_rmesh_one(mr, rm[g]);
+      if (mr.owner >= 0) set_outer(*ctx->meshes[mr.owner], rm[g]);
+    }
+  }
+  return rm;
+}
+// The geom whose shading data a hit on geom g reads (the instanced geom for
+// an instance), for the render's input checks.
+inline const MeshRec& shading_rec(const vmr_ctx* ctx, uint32_t g) {
+  const MeshRec& mr = *ctx->meshes[g];
+  return mr.host.group == 1 ? *ctx->meshes[mr.children[0]] : mr;
 }
 
 }  // namespace

@@ -508,6 +508,72 @@ __device__ __forceinline__ void ray_to_object(TRay& r, const float* x) {
   ray_setup(r);
 }
 
+// A transform of two or more keys at the ray's time (PolyMesh.Trace,
+// builtin/geom/polymesh/trace.go:33-48; TransformSRTArray.TimeKey,
+// instance.go:20-36): the keys around the time blended
+// (TransformDecompLerp), the matrix rebuilt, Matrix4Inverse; x receives the
+// inverse's columns 0..3, rows 0..2.  Outside the keys (the reference panics)
+// x is zero and the ray misses.  Not inlined: it runs once per entry into a
+// keyed geom and would otherwise bloat the walk's registers.
+__device__ __noinline__ void keyed_inverse(const anim::Decomp* keys, uint32_t n, float time, float* x) {
+  float m[16], inv[16];
+  if (!anim::at_time(keys, n, time, false, m)) {
+    for (int k = 0; k < 12; ++k) x[k] = 0.0f;
+    return;
+  }
+  anim::inverse(m, inv);
+  const int cols[12] = {0, 1, 2, 4, 5, 6, 8, 9, 10, 12, 13, 14};
+  for (int k = 0; k < 12; ++k) x[k] = inv[cols[k]];
+}
+
+// The ray in a geom's object space: its one matrix's inverse or its keyed
+// transform at the ray's time.
+__device__ __forceinline__ void to_object(const DMesh& M, TRay& r) {
+  if (M.xf_nkeys >= 2) {
+    float x[12];
+    keyed_inverse(M.xf_keys, M.xf_nkeys, r.time, x);
+    ray_to_object(r, x);
+  } else {
+    ray_to_object(r, M.xf_inv);
+  }
+}
+
+// Instance.Trace (builtin/geom/instance/instance.go:72-115) and Proc.Trace
+// (builtin/geom/proc/proc.go:88-140): the ray mapped by the group's
+// transform at its time, then its geoms in order on the same stack slice,
+// each through its own PolyMesh transform; a Proc stops at the first geom
+// that hits unless the ray is a shadow ray (proc.go:117-124).  A hit reports
+// the group's id for an instance and the child's id for a Proc (child_hit).
+template <bool ANY, bool COUNT>
+__device__ bool trace_group(const DTop& top, const DMesh& G, TRay& r, int2* stk, int cap, HitRec& h, Counters& cnt,
+                            int& status) {
+  TRay rg = r;
+  to_object(G, rg);
+  bool hit = false;
+  for (uint32_t c = 0; c < G.n_children; ++c) {
+    const DMesh& C = top.meshes[__ldg(G.children + c)];
+    HitRec hc = h;
+    bool ch;
+    if (C.has_xf || C.xf_nkeys >= 2) {
+      TRay ro = rg;
+      to_object(C, ro);
+      ch = trace_any_mesh<ANY, COUNT>(C, ro, stk, cap, hc, cnt, status);
+      rg.tclosest = ro.tclosest;
+    } else {
+      ch = trace_any_mesh<ANY, COUNT>(C, rg, stk, cap, hc, cnt, status);
+    }
+    if (ch) {
+      h = hc;
+      h.geom = __ldg(G.child_hit + c);
+      hit = true;
+      if (!ANY) break;
+    }
+    if (status != kStatusOk) break;
+  }
+  r.tclosest = rg.tclosest;
+  return hit;
+}
+
 // The world ray again after an object-space walk: P and D from the ray
 // stream and Ray.Setup, Tclosest and time kept.
 __device__ __forceinline__ void load_ray_pd(const RaySoA& rs, uint64_t i, TRay& r) {
@@ -629,9 +695,12 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
           if (base >= kStackCapacity) { status = kStatusStackOverflow; break; }
           const DMesh& M = top.meshes[g];
           bool mh;
-          if (M.has_xf) {  // the object-space copy walks the mesh; the world ray keeps its Tclosest
+          if (M.kind == kGroup) {
+            mh = trace_group<ANY, COUNT>(top, M, r, stk + base, kStackCapacity - base, hm, cnt, status);
+          } else if (M.has_xf || M.xf_nkeys >= 2) {
+            // the object-space copy walks the mesh; the world ray keeps its Tclosest
             TRay ro = r;
-            ray_to_object(ro, M.xf_inv);
+            to_object(M, ro);
             mh = trace_any_mesh<ANY, COUNT>(M, ro, stk + base, kStackCapacity - base, hm, cnt, status);
             r.tclosest = ro.tclosest;
           } else {
@@ -639,7 +708,7 @@ __device__ bool trace_scene_ray(const DTop& top, TRay& r, int2* stk, HitRec& h, 
           }
           if (mh) {
             h = hm;
-            h.geom = (int32_t)g;
+            if (M.kind != kGroup) h.geom = (int32_t)g;
             leaf_hit = true;
             if (ANY) break;
           }
@@ -2037,7 +2106,8 @@ int launch_mesh_m(const DMesh& mesh, const TraceLaunch& l) {
 
 template <bool ANY, bool COUNT>
 int launch_scene_t(const DTop& top, const TraceLaunch& l) {
-  if (!COUNT && (l.kernel & kKernelWhileWhile)) {
+  // Instances, Procs and keyed transforms are traced by the single-loop kernel.
+  if (!COUNT && (l.kernel & kKernelWhileWhile) && !top.simple_only) {
     // Motion meshes and motion top levels take the MOT instantiation (lerped
     // node boxes, per-lane motion leaves); only-static scenes keep the leaner
     // kernel.

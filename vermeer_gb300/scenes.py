@@ -529,6 +529,88 @@ def small_room_motion(n_tris: int = 4096, seed: int = 1, motion_mode: int = 0, v
     return sc
 
 
+def xf_matrix(angle, axis, scale, translate) -> np.ndarray:
+    """Column-major 4x4 (math.Matrix4 order) of x -> translate + R(angle,
+    axis) diag(scale) x, as float32."""
+    axis = np.asarray(axis, np.float64) / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    R = np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * K @ K
+    A = np.eye(4)
+    A[:3, :3] = R @ np.diag(scale)
+    A[:3, 3] = translate
+    return A.T.reshape(16).astype(np.float32)
+
+
+def _box_of(verts, keys16, margin=0.02):
+    """A box around the vertices under every key (for BMin/BMax)."""
+    v = np.asarray(verts, np.float64).reshape(-1, 3)
+    lo, hi = np.full(3, np.inf), np.full(3, -np.inf)
+    for k in np.asarray(keys16, np.float64).reshape(-1, 16):
+        A = k.reshape(4, 4).T
+        w = v @ A[:3, :3].T + A[:3, 3]
+        lo, hi = np.minimum(lo, w.min(0)), np.maximum(hi, w.max(0))
+    # keys blend rotations on arcs between the keys: grow the box by its half size
+    pad = 0.5 * (hi - lo) + margin
+    return (lo - pad).astype(np.float32), (hi + pad).astype(np.float32)
+
+
+def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = True) -> dict:
+    """The small room with the node types that reach geometry through
+    transforms: an object (a 600-triangle soup in a 0.3 cube about the
+    origin, itself placed in the room), two GeomInstances of it (one key; two
+    keys moving and turning over the shutter), an instance of an analytic
+    sphere, a Proc of two meshes (one with its own PolyMesh transform) under
+    two transform keys, a mesh with two PolyMesh transform keys, a
+    DebugShader on the first instance's object, and (camera_keys) two
+    camera motion keys."""
+    sc = small_room(n_tris, seed=seed)
+    M = sc["meshes"]
+    shaders = sc["shaders"]
+    debug = len(shaders)
+    shaders.append(dict(debug=True, diffuse_colour=(0.9, 0.2, 0.6)))
+    ov, oi = triangle_soup(600, seed + 90, lo=-0.15, hi=0.15, edge=0.04)
+    obj = dict(verts=ov, idxp=oi, shaders=[5, 6], face_shader=(np.arange(600) % 2).astype(np.uint8),
+               transform=xf_matrix(0.0, (0, 1, 0), (1, 1, 1), (-0.5, -0.55, 0.3)))
+    M.append(obj)
+    i_obj = len(M) - 1
+    ow = ov.reshape(-1, 3) + np.float32([-0.5, -0.55, 0.3])  # the object under its own transform
+    k1 = [xf_matrix(0.7, (0, 1, 0), (1.3, 0.8, 1.0), (0.45, 0.2, -0.2))]
+    lo, hi = _box_of(ow, k1)
+    M.append(dict(instance=i_obj, keys=k1, bmin=lo, bmax=hi, shaders=[]))
+    k2 = [xf_matrix(0.2, (1, 1, 0), (1, 1, 1), (0.4, 0.85, -0.4)),
+          xf_matrix(0.9, (1, 1, 0), (1.2, 1.2, 1.2), (0.52, 0.92, -0.35))]
+    lo, hi = _box_of(ow, k2)
+    M.append(dict(instance=i_obj, keys=k2, bmin=lo, bmax=hi, shaders=[]))
+    M.append(dict(sphere=(0.0, 0.0, 0.0, 0.12), shaders=[7]))
+    i_sph = len(M) - 1
+    k3 = [xf_matrix(0.0, (0, 0, 1), (1.0, 1.5, 1.0), (-0.45, 0.25, -0.45))]
+    lo, hi = _box_of(np.array([[-0.12] * 3, [0.12] * 3]), k3, margin=0.2)
+    M.append(dict(instance=i_sph, keys=k3, bmin=lo, bmax=hi, shaders=[]))
+    # a Proc's children: meshes made for it (they join no scene themselves)
+    av, ai = triangle_soup(400, seed + 91, lo=-0.12, hi=0.12, edge=0.03)
+    bv, bi = triangle_soup(300, seed + 92, lo=-0.1, hi=0.1, edge=0.03)
+    M.append(dict(verts=av, idxp=ai, shaders=[8]))
+    ca = len(M) - 1
+    M.append(dict(verts=bv, idxp=bi, shaders=[9], transform=xf_matrix(0.4, (0, 0, 1), (1, 1, 1), (0.1, 0.05, 0.0))))
+    cb = len(M) - 1
+    k4 = [xf_matrix(0.0, (0, 1, 0), (1, 1, 1), (0.5, 0.3, 0.4)), xf_matrix(0.5, (0, 1, 0), (1, 1, 1), (0.45, 0.3, 0.5))]
+    lo, hi = _box_of(np.concatenate([av, bv + 0.12]), k4, margin=0.1)
+    M.append(dict(proc=[ca, cb], keys=k4, bmin=lo, bmax=hi, shaders=[]))
+    # a mesh with two PolyMesh transform keys
+    tv, ti = triangle_soup(500, seed + 93, lo=-0.12, hi=0.12, edge=0.03)
+    M.append(dict(verts=tv, idxp=ti, shaders=[10, 11], face_shader=(np.arange(500) % 2).astype(np.uint8),
+                  transform_keys=[xf_matrix(0.0, (1, 0, 0), (1, 1, 1), (-0.1, -0.3, -0.6)),
+                                  xf_matrix(0.8, (1, 0, 0), (1.1, 1.1, 1.1), (0.05, -0.25, -0.55))]))
+    obj["shaders"] = [debug, 6]
+    if camera_keys:
+        cam = sc["camera"]
+        m0 = np.asarray(cam["m"], np.float32)
+        m1 = m0.copy()
+        m1[12:15] += np.float32([0.08, 0.03, 0.0])
+        cam["keys"] = np.stack([m0, m1])
+    return sc
+
+
 # ------------------------------------------------------------ .vnf files ---
 def _vnf_num(x) -> str:
     """A float32 value as the decimal of its exact double (read back through
