@@ -433,6 +433,9 @@ int vmr_set_camera_keys(vmr_ctx* ctx, const float* keys16, uint32_t n_keys);
  * itself).  Host-side, needs no context or GPU; VMR_ERR_INVALID if time
  * falls outside the keys. */
 int vmr_transform_keys_at(const float* keys16, uint32_t n_keys, float time, int blend_one, float* out16);
+/* The camera's LocalToWorld keys as set or loaded: *n_keys receives their
+ * number, keys16 (may be NULL) the first min(n, cap) of them. */
+int vmr_get_camera_keys(vmr_ctx* ctx, float* keys16, uint32_t cap, uint32_t* n_keys);
 
 /* Pixel filters for filter importance sampling: replaces core.Init of a
  * PixelFilter node (core/core.go:88-89, core/pixelfilter.go:8-10) with the

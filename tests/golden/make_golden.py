@@ -9,7 +9,10 @@ Run from the repository root:  python tests/golden/make_golden.py [REFERENCE_DIR
 2. colour_tables.npz plus oracle/orc_colour_tables.h and
    vermeer_gb300/csrc/colour_tables.h - the spectral tables of colour/*.go
    (CIE observer bins, Smits spectra, sRGB matrix); same reference checkout.
-3. traversal_small.npz - small triangle soups, rays with awkward directions
+3. quickstart_nodes.vnf - the node examples of the reference's
+   docs/quickstart.rst (the literal blocks that hold a node), each prefixed
+   by a comment naming its source line; same reference checkout.
+4. traversal_small.npz - small triangle soups, rays with awkward directions
    (axis-parallel, zero components, through vertices and edges, finite
    tmax) and the oracle's closest-hit and any-hit answers.  This pins the
    oracle itself, so a rebuild on another machine (x86_64 or aarch64) must
@@ -90,6 +93,29 @@ def write_colour_headers(t):
         open(path, "w").write(txt)
 
 
+def quickstart_nodes(ref_dir: str) -> str:
+    """The literal blocks of docs/quickstart.rst that hold a node (a name
+    followed by '{'), as one file with a comment before each."""
+    lines = open(os.path.join(ref_dir, "docs", "quickstart.rst")).read().split("\n")
+    out, i = [], 0
+    while i < len(lines):
+        if lines[i].rstrip().endswith("::"):
+            j = i + 1
+            while j < len(lines) and not lines[j].strip():
+                j += 1
+            start, block = j, []
+            while j < len(lines) and (not lines[j].strip() or lines[j][:1] in (" ", "\t")):
+                block.append(lines[j])
+                j += 1
+            text = "\n".join(block).strip("\n")
+            if re.match(r"\s*[A-Za-z_]\w*\s*\{", text):
+                out.append(f"# docs/quickstart.rst:{start + 1}\n{text}\n")
+            i = j
+        else:
+            i += 1
+    return "\n".join(out)
+
+
 def edge_rays(verts: np.ndarray, seed: int, n_random: int) -> np.ndarray:
     """Rays aimed at vertices and edge midpoints of the soup, rays with zero
     direction components, and random rays with finite tmax."""
@@ -135,7 +161,9 @@ def main():
         ct = parse_colour_tables(ref)
         np.savez_compressed(os.path.join(HERE, "colour_tables.npz"), **ct)
         write_colour_headers(ct)
-        print("wrote vdc_sobol_tables.npz, colour_tables.npz and the colour table headers")
+        with open(os.path.join(HERE, "quickstart_nodes.vnf"), "w") as fh:
+            fh.write(quickstart_nodes(ref))
+        print("wrote vdc_sobol_tables.npz, colour_tables.npz, the colour table headers and quickstart_nodes.vnf")
     else:
         print("reference checkout not given: keeping vdc_sobol_tables.npz")
 

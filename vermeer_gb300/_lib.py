@@ -201,6 +201,7 @@ SIGNATURES = {
     "vmr_proc_add": (ctypes.c_int, [P, P, U32, P, U32, P, P, ctypes.POINTER(U32)]),
     "vmr_set_camera_keys": (ctypes.c_int, [P, P, U32]),
     "vmr_transform_keys_at": (ctypes.c_int, [P, U32, ctypes.c_float, ctypes.c_int, P]),
+    "vmr_get_camera_keys": (ctypes.c_int, [P, P, U32, ctypes.POINTER(U32)]),
     "vmr_selftest_wait": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float)]),
     "vmr_get_path_batch": (ctypes.c_int, [P, ctypes.POINTER(U32)]),
     "vmr_autotune_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, P, ctypes.POINTER(U32),

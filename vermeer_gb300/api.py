@@ -581,6 +581,14 @@ class Context:
                     n_shaders=info.n_shaders, n_lights=info.n_lights, camera=info.camera.decode(),
                     output_hdr=info.output_hdr.decode(), output_float=info.output_float.decode())
 
+    def get_camera_keys(self) -> np.ndarray:
+        """The camera's LocalToWorld keys ([n, 16] column-major)."""
+        n = ctypes.c_uint32()
+        self._check(self.L.vmr_get_camera_keys(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, 16), np.float32)
+        self._check(self.L.vmr_get_camera_keys(self.h, _p(out), n.value, ctypes.byref(n)))
+        return out
+
     def get_camera(self) -> dict:
         c = _lib.Camera()
         self._check(self.L.vmr_get_camera(self.h, ctypes.byref(c)))

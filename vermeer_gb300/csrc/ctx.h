@@ -91,6 +91,7 @@ struct RenderState {
   // (the reference's round trip), key 0 otherwise (the kernels blend
   // dcam_keys per sample)
   std::vector<anim::Decomp> cam_keys;
+  std::vector<float> cam_key_m;  // the keys as given (16 floats each)
   DevBuf dcam_keys;
   vmr_camera cam_used{};
   // pixel filter (vmr_set_pixel_filter): filter_n = 0 is none; the device

@@ -772,7 +772,18 @@ int vmr_set_camera(vmr_ctx* ctx, const vmr_camera* cam) {
   R.has_camera = true;
   R.cam_keys.resize(1);
   vmr::anim::decompose(cam->m, R.cam_keys[0]);
+  R.cam_key_m.assign(cam->m, cam->m + 16);
   R.cam_used = vmr::camera_round_trip(*cam);
+  return VMR_OK;
+}
+
+int vmr_get_camera_keys(vmr_ctx* ctx, float* keys16, uint32_t cap, uint32_t* n_keys) {
+  if (!ctx || !n_keys) return VMR_ERR_INVALID;
+  const auto& R = ctx->render;
+  if (!R.has_camera) return rfail(ctx, VMR_ERR_INVALID, "no camera set");
+  const uint32_t n = (uint32_t)(R.cam_key_m.size() / 16);
+  *n_keys = n;
+  if (keys16) std::memcpy(keys16, R.cam_key_m.data(), sizeof(float) * 16 * std::min(n, cap));
   return VMR_OK;
 }
 
@@ -793,6 +804,7 @@ int vmr_set_camera_keys(vmr_ctx* ctx, const float* keys16, uint32_t n_keys) {
   if (rc != VMR_OK || n_keys == 1) return rc;
   R.cam_keys.resize(n_keys);
   for (uint32_t i = 0; i < n_keys; ++i) vmr::anim::decompose(keys16 + 16 * i, R.cam_keys[i]);
+  R.cam_key_m.assign(keys16, keys16 + 16 * (size_t)n_keys);
   if (ctx->device >= 0) {
     cudaSetDevice(ctx->device);
     RCUDA(R.dcam_keys.ensure(sizeof(vmr::anim::Decomp) * n_keys));

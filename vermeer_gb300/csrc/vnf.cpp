@@ -23,10 +23,15 @@
 //
 // Where the reference tolerates an error (prints it and skips the field or
 // node), the loader stops with VMR_ERR_INVALID and the file:line in
-// vmr_last_error; nodes the GPU path does not render (DebugShader, Proc,
-// GeomInstance, textures, PolyMesh transforms with several motion keys,
-// camera motion keys) give VMR_ERR_UNSUPPORTED; a PolyMesh Transform of one
-// matrix goes to vmr_mesh_set_transform.
+// vmr_last_error; what the GPU path does not render (textures, the Proc
+// handler "wfobj", instances of instances or Procs, lerped motion normals)
+// gives VMR_ERR_UNSUPPORTED.  A PolyMesh Transform of one matrix goes to
+// vmr_mesh_set_transform, of several keys to vmr_mesh_set_transform_keys;
+// GeomInstance to vmr_instance_add; Proc with the "vnf" handler
+// (builtin/geom/proc/vnf/vnf.go: the Data file's shaders join the scene's,
+// its geoms become the Proc's) to vmr_proc_add; DebugShader to a shader with
+// VMR_SH_DEBUG; camera motion keys (LookAt From/To/Roll keys, WorldToLocal
+// or LocalToWorld keys) to vmr_set_camera_keys.
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -230,13 +235,14 @@ const std::vector<NodeSpec>& specs() {
                       {"Peak", fFloat, false}}},
       {"OutputHDR", {{"Filename", fString, true}}},
       {"OutputFloat", {{"Filename", fString, true}}},
+      {"DebugShader", {{"Name", fString, true}, {"Sides", fInt, false}, {"Colour", fMap, true}}},
+      {"Include", {{"Name", fString, false}, {"Filename", fString, true}}},
+      {"GeomInstance", {{"Name", fString, true}, {"Geom", fString, true}, {"BMin", fPoints, true},
+                        {"BMax", fPoints, true}, {"Transform", fMatrices, true}}},
+      {"Proc", {{"Name", fString, true}, {"Handler", fString, true}, {"Data", fString, true},
+                {"BMin", fPoints, true}, {"BMax", fPoints, true}, {"Transform", fMatrices, false}}},
   };
   return s;
-}
-
-// Node types of the reference that this loader does not render.
-bool unsupported_type(const std::string& t) {
-  return t == "DebugShader" || t == "Proc" || t == "GeomInstance" || t == "Instance";
 }
 
 struct Value {
@@ -277,8 +283,6 @@ class Parser {
       if (t.k != kIdent) fail(t.line, "expected a node name");
       Token b = lx_.next();
       if (b.k != kLCurl) fail(b.line, "expected '{' after node name " + t.s);
-      if (unsupported_type(t.s))
-        throw LoadError{VMR_ERR_UNSUPPORTED, where(t.line) + "node type " + t.s + " is not rendered by libvmr"};
       const NodeSpec* spec = nullptr;
       for (const NodeSpec& s : specs())
         if (t.s == s.type) spec = &s;
@@ -457,6 +461,15 @@ struct MeshOut {
   float centre[3] = {0, 0, 0}, radius = 0.f;
   bool has_xf = false;  // PolyMesh.Transform with one non-identity matrix (column-major)
   float xf[16] = {};
+  std::vector<float> xkeys;  // PolyMesh.Transform of two or more keys (16 floats each)
+  std::string name;
+  // 1 GeomInstance (ref: the geom's name), 2 Proc (children: indices into
+  // Scene::proc_children); keys: the transform keys; bmin/bmax: key 0's box
+  int group = 0;
+  std::string ref;
+  std::vector<size_t> children;
+  std::vector<float> gkeys;
+  float bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
 };
 
 struct Scene {
@@ -467,7 +480,9 @@ struct Scene {
   std::vector<vmr_disk_light> disks;
   std::vector<vmr_sphere_light> spheres;
   std::vector<vmr_quad_light> quads;
+  std::vector<MeshOut> proc_children;  // geoms reached only through their Proc
   vmr_camera cam{};
+  std::vector<float> cam_keys;  // LocalToWorld keys (16 floats each), two or more
   bool has_filter = false;
   vmr_pixel_filter filter{};
   vmr_vnf_info info{};
@@ -514,6 +529,14 @@ vmr_shader_std shader_std(const Node& n) {
   return s;
 }
 
+// DebugShader (builtin/shader/debug.go:16-57): its Colour as diffuse_colour.
+vmr_shader_std debug_shader(const Node& n) {
+  vmr_shader_std s{};
+  s.flags = VMR_SH_DEBUG;
+  for (int k = 0; k < 3; ++k) s.diffuse_colour[k] = n.at("Colour").c[k];
+  return s;
+}
+
 bool identity(const float* m) {
   for (int i = 0; i < 16; ++i)
     if (m[i] != ((i % 5 == 0) ? 1.0f : 0.0f)) return false;
@@ -538,19 +561,26 @@ MeshOut poly_mesh(const Node& n, const Scene& sc, const std::string& file) {
     bool all_identity = true;
     for (size_t k = 0; k < nk; ++k) all_identity = all_identity && identity(T.v.data() + 16 * k);
     if (!all_identity) {
-      if (nk != 1)
-        throw LoadError{VMR_ERR_UNSUPPORTED,
-                        where("transform motion keys (TransformDecompLerp) are not supported; give one matrix")};
-      o.has_xf = true;
-      std::memcpy(o.xf, T.v.data(), sizeof(o.xf));
+      if (nk == 1) {
+        o.has_xf = true;
+        std::memcpy(o.xf, T.v.data(), sizeof(o.xf));
+      } else {
+        o.xkeys.assign(T.v.begin(), T.v.begin() + 16 * nk);
+      }
     }
   }
+  o.name = n.at("Name").s;
   for (const std::string& s : n.at("Shader").strs) o.shaders.push_back(shader_of(sc, n, s, file));
   const std::vector<int32_t> none;
   const std::vector<int32_t>& fi = n.has("FaceIdx") ? n.at("FaceIdx").ints : none;
   const std::vector<int32_t>& ni = n.has("NormalIdx") ? n.at("NormalIdx").ints : none;
   const std::vector<int32_t>& si = n.has("ShaderIdx") ? n.at("ShaderIdx").ints : none;
-  const bool has_n = n.has("Normals") && !n.at("Normals").v.empty();
+  // TraceMotionElems uses the normals only with as many keys as the
+  // vertices (trace.go:694-712), otherwise N = Ng; the static path uses key 0
+  const int nkeys = n.has("Normals") ? (n.at("Normals").keys == 0 ? 1 : n.at("Normals").keys) : 0;
+  if (o.keys > 1 && nkeys == (int)o.keys)
+    throw LoadError{VMR_ERR_UNSUPPORTED, where("motion-keyed normals (lerped per key) are not supported")};
+  const bool has_n = n.has("Normals") && !n.at("Normals").v.empty() && o.keys == 1;
   std::vector<uint32_t> nidx;
   auto chk = [&](const std::vector<int32_t>& a, size_t i) -> uint32_t {
     if (i >= a.size()) throw LoadError{VMR_ERR_INVALID, where("index array shorter than the polygons need")};
@@ -595,7 +625,6 @@ MeshOut poly_mesh(const Node& n, const Scene& sc, const std::string& file) {
     const size_t nn = (size_t)N.per;
     for (uint32_t q : nidx)
       if (q >= nn) throw LoadError{VMR_ERR_INVALID, where("normal index out of range")};
-    if (o.keys > 1) throw LoadError{VMR_ERR_UNSUPPORTED, where("normals of motion meshes are not supported")};
     bool same = true;
     for (size_t c = 0; c < nidx.size() && same; ++c) same = nidx[c] == o.idxp[c];
     if (same && nn >= o.n_verts) {
@@ -668,8 +697,10 @@ MeshOut quad_light_mesh(F3 P, F3 U, F3 V, uint32_t shader) {  // quad.go:41-66, 
   return o;
 }
 
-// Camera.PreRender for one key (camera.go:80-98, 109-193).
-vmr_camera camera(const Node& n, const vmr_vnf_info& info, const std::string& file) {
+// Camera.PreRender (camera.go:80-98): TanThetaFocal, then the LocalToWorld
+// keys, calcLookatMatrices (:109-193) or matrixCalc (:207-216); keys holds
+// them (16 floats each), c.m key 0.
+vmr_camera camera(const Node& n, const vmr_vnf_info& info, const std::string& file, std::vector<float>& keys) {
   auto where = [&](const std::string& m) { return file + ":" + std::to_string(n.line) + ": Camera: " + m; };
   vmr_camera c{};
   const float fov = n.has("Fov") ? (float)n.at("Fov").f : 90.0f;
@@ -682,53 +713,292 @@ vmr_camera camera(const Node& n, const vmr_vnf_info& info, const std::string& fi
   c.aspect = aspect;
   c.focal = focal;
   c.radius = n.has("Radius") ? (float)n.at("Radius").f : 0.0f;
+  keys.clear();
   const std::string& type = n.at("Type").s;
   if (type == "LookAt") {
     const Value& from = n.at("From");
     const Value& to = n.at("To");
     const Value& roll = n.at("Roll");
-    if (from.keys > 1 || to.keys > 1 || roll.keys > 1 || from.v.size() < 3 || to.v.size() < 3)
-      throw LoadError{VMR_ERR_UNSUPPORTED, where("one From/To key is supported (no camera motion)")};
-    const F3 P = f3(from.v), T = f3(to.v), Up = f3(n.at("Up").v);
-    const F3 W = nrm(sub(P, T));  // W points away from the target
-    const F3 u = nrm(cross(Up, W));
-    const F3 v = nrm(cross(u, W));
-    F3 U = u, Vv = v;
-    if (!roll.v.empty()) {
-      const float r = roll.v[0];
+    const int nf = from.keys == 0 ? 1 : from.keys, nt = to.keys == 0 ? 1 : to.keys;
+    const int nr = roll.keys == 0 ? 1 : roll.keys;
+    if ((int)from.v.size() < 3 * nf || (int)to.v.size() < 3 * nt)
+      throw LoadError{VMR_ERR_INVALID, where("From/To hold fewer points than their keys")};
+    const F3 Up = f3(n.at("Up").v);
+    // The array with more keys is walked; the other is lerped at time i/n
+    // (not i/(n-1)); Roll, if given, is lerped at the same time.
+    const bool by_target = nt > nf;
+    const int n_keys = by_target ? nt : nf;
+    auto lerp_key = [](const Value& a, int na, float time) {
+      const float k = time * (float)(na - 1);
+      const float t = k - std::floor(k);
+      const int key = (int)std::floor(k), key2 = (int)std::ceil(k);
+      const float* p = a.v.data() + 3 * key;
+      const float* q = a.v.data() + 3 * key2;
+      return F3{(1.0f - t) * p[0] + t * q[0], (1.0f - t) * p[1] + t * q[1], (1.0f - t) * p[2] + t * q[2]};
+    };
+    for (int i = 0; i < n_keys; ++i) {
+      const float time = (float)i / (float)n_keys;
+      const F3 From = by_target ? lerp_key(from, nf, time) : f3(from.v, 3 * (size_t)i);
+      const F3 To = by_target ? f3(to.v, 3 * (size_t)i) : lerp_key(to, nt, time);
+      const F3 W = nrm(sub(From, To));  // W points away from the target
+      const F3 u = nrm(cross(Up, W));
+      const F3 v = nrm(cross(u, W));
+      float r = 0.0f;
+      if (!roll.v.empty()) {
+        const float k = time * (float)(nr - 1);
+        const float t = k - std::floor(k);
+        const int key = (int)std::floor(k), key2 = (int)std::ceil(k);
+        r = (1.0f - t) * roll.v[key] + t * roll.v[key2];
+      }
       const float cr = (float)std::cos((double)r), sr = (float)std::sin((double)r);
-      U = add(scl(cr, u), scl(sr, v));
-      Vv = add(scl(-sr, u), scl(cr, v));
+      const F3 U = add(scl(cr, u), scl(sr, v));
+      const F3 Vv = add(scl(-sr, u), scl(cr, v));
+      // Matrix4Mul(Matrix4Translate(From), Matrix4Basis(U, V, W))
+      float tr[16], basis[16], m[16];
+      vmr::anim::identity(tr);
+      tr[12] = From.x;
+      tr[13] = From.y;
+      tr[14] = From.z;
+      const float bz[16] = {U.x, U.y, U.z, 0.f, Vv.x, Vv.y, Vv.z, 0.f, W.x, W.y, W.z, 0.f, 0.f, 0.f, 0.f, 1.f};
+      std::memcpy(basis, bz, sizeof(basis));
+      vmr::anim::mul(tr, basis, m);
+      keys.insert(keys.end(), m, m + 16);
     }
-    const float m[16] = {U.x, U.y, U.z, 0.f, Vv.x, Vv.y, Vv.z, 0.f, W.x, W.y, W.z, 0.f, P.x, P.y, P.z, 1.f};
-    std::memcpy(c.m, m, sizeof(m));
   } else {
-    if (n.has("WorldToLocal"))
-      throw LoadError{VMR_ERR_UNSUPPORTED, where("WorldToLocal (a matrix inverse) is not supported; give LocalToWorld")};
-    if (!n.has("LocalToWorld")) throw LoadError{VMR_ERR_INVALID, where("a matrix camera needs LocalToWorld")};
-    const Value& M = n.at("LocalToWorld");
-    if (M.keys > 1) throw LoadError{VMR_ERR_UNSUPPORTED, where("one LocalToWorld key is supported")};
-    std::memcpy(c.m, M.v.data(), sizeof(c.m));
+    // matrixCalc: the given LocalToWorld keys, then the inverse of each
+    // WorldToLocal key (Matrix4Inverse; its ok flag is ignored)
+    if (n.has("LocalToWorld")) {
+      const Value& M = n.at("LocalToWorld");
+      keys.insert(keys.end(), M.v.begin(), M.v.end());
+    }
+    if (n.has("WorldToLocal")) {
+      const Value& M = n.at("WorldToLocal");
+      for (size_t k = 0; k + 16 <= M.v.size(); k += 16) {
+        float inv[16];
+        vmr::anim::inverse(M.v.data() + k, inv);
+        keys.insert(keys.end(), inv, inv + 16);
+      }
+    }
   }
+  if (keys.empty()) {  // no keys: Matrix4Identity (camera.go:223)
+    float I[16];
+    vmr::anim::identity(I);
+    keys.assign(I, I + 16);
+  }
+  std::memcpy(c.m, keys.data(), sizeof(c.m));
   return c;
 }
 
-Scene build_scene(const std::vector<Node>& nodes, const std::string& file, int flags) {
+MeshOut sphere_geom(const Node& n, const Scene& sc, const std::string& file) {
+  MeshOut o;
+  o.sphere = true;
+  o.name = n.at("Name").s;
+  for (int k = 0; k < 3; ++k) o.centre[k] = n.at("P").v[k];
+  o.radius = (float)n.at("Radius").f;
+  o.shaders = {shader_of(sc, n, n.at("Shader").s, file)};
+  return o;
+}
+
+// A file named by a node: relative to the naming file's directory if it
+// exists there, else as given (the reference opens it from the working
+// directory).
+std::string near(const std::string& from, const std::string& name) {
+  const size_t slash = from.find_last_of('/');
+  if (slash == std::string::npos || (!name.empty() && name[0] == '/')) return name;
+  const std::string rel = from.substr(0, slash + 1) + name;
+  std::ifstream probe(rel);
+  return probe ? rel : name;
+}
+
+std::vector<Node> parse_file(const std::string& path);
+
+// Proc.PreRender with the "vnf" handler (builtin/geom/proc/vnf/vnf.go:18-55):
+// the Data file is parsed, its shaders join the scene's (core.AddNode; a
+// name already taken keeps its first shader), its geoms (PolyMesh, Sphere)
+// become the Proc's children in file order; other nodes are skipped, as the
+// handler logs and skips them.  Data is found relative to the scene file's
+// directory, then as given.  The "wfobj" handler (Wavefront OBJ) is not
+// supported.
+void proc_geoms(const Node& n, Scene& sc, const std::string& file, MeshOut& o) {
+  auto where = [&](const std::string& m) { return file + ":" + std::to_string(n.line) + ": Proc: " + m; };
+  const std::string& handler = n.at("Handler").s;
+  if (handler == "wfobj") throw LoadError{VMR_ERR_UNSUPPORTED, where("the wfobj (Wavefront OBJ) handler is not supported")};
+  if (handler != "vnf") throw LoadError{VMR_ERR_INVALID, where("unable to find handler " + handler)};
+  const std::string data = near(file, n.at("Data").s);
+  const std::vector<Node> sub = parse_file(data);
+  for (const Node& c : sub)
+    if ((c.type == "ShaderStd" || c.type == "DebugShader") && !sc.shader_id.count(c.at("Name").s)) {
+      sc.shader_id[c.at("Name").s] = (uint32_t)sc.shaders.size();
+      sc.shaders.push_back(c.type == "ShaderStd" ? shader_std(c) : debug_shader(c));
+    }
+  for (const Node& c : sub) {
+    if (c.type == "PolyMesh") {
+      o.children.push_back(sc.proc_children.size());
+      sc.proc_children.push_back(poly_mesh(c, sc, data));
+    } else if (c.type == "Sphere") {
+      o.children.push_back(sc.proc_children.size());
+      sc.proc_children.push_back(sphere_geom(c, sc, data));
+    } else if (c.type == "GeomInstance" || c.type == "Proc") {
+      throw LoadError{VMR_ERR_UNSUPPORTED, where("instances and Procs inside a Proc are not supported")};
+    }
+  }
+  if (o.children.empty()) throw LoadError{VMR_ERR_INVALID, where("no geoms in " + data)};
+}
+
+bool is_light(const Node& n) {
+  return n.type == "TriLight" || n.type == "DiskLight" || n.type == "SphereLight" || n.type == "QuadLight";
+}
+bool is_geom(const Node& n) {
+  return n.type == "PolyMesh" || n.type == "Sphere" || n.type == "GeomInstance" || n.type == "Proc";
+}
+
+// A node and the file it came from.
+struct Item {
+  const Node* n;
+  std::string file;
+};
+
+// One geom slot of the scene, in core.AddNode / PreRender order: a geom
+// node (added when parsed) or a light's own mesh (added by the light's
+// PreRender).
+struct Slot {
+  Item it;
+  bool light_mesh;
+};
+
+MeshOut geom_of(const Item& it, Scene& sc) {
+  const Node& n = *it.n;
+  if (n.type == "PolyMesh") return poly_mesh(n, sc, it.file);
+  if (n.type == "Sphere") return sphere_geom(n, sc, it.file);
+  MeshOut o;  // GeomInstance or Proc
+  o.name = n.at("Name").s;
+  o.group = n.type == "GeomInstance" ? 1 : 2;
+  const Value &lo = n.at("BMin"), &hi = n.at("BMax");
+  if (lo.v.size() < 3 || hi.v.size() < 3)
+    throw LoadError{VMR_ERR_INVALID, it.file + ":" + std::to_string(n.line) + ": " + n.type + " needs BMin and BMax"};
+  for (int k = 0; k < 3; ++k) {
+    o.bmin[k] = lo.v[k];
+    o.bmax[k] = hi.v[k];
+  }
+  if (n.has("Transform")) o.gkeys = n.at("Transform").v;
+  if (o.group == 1) {
+    o.ref = n.at("Geom").s;
+    if (o.gkeys.empty())
+      throw LoadError{VMR_ERR_INVALID, it.file + ":" + std::to_string(n.line) + ": GeomInstance needs a Transform"};
+  } else {
+    proc_geoms(n, sc, it.file, o);
+  }
+  return o;
+}
+
+// A light's own mesh (its PreRender) and its table entry pointing at geom.
+void light_of(const Item& it, Scene& sc, uint32_t geom) {
+  const Node& n = *it.n;
+  const std::string& file = it.file;
+  const uint32_t sh = shader_of(sc, n, n.at("Shader").s, file);
+  const int samples = n.has("Samples") ? (int)n.at("Samples").i : 1;
+  if (n.type == "TriLight") {
+    const F3 p0 = f3(n.at("P0").v), p1 = f3(n.at("P1").v), p2 = f3(n.at("P2").v);
+    sc.geoms[geom] = tri_light_mesh(p0, p1, p2, sh);
+    vmr_tri_light l{};
+    std::memcpy(l.p0, &p0, 12);
+    std::memcpy(l.p1, &p1, 12);
+    std::memcpy(l.p2, &p2, 12);
+    l.samples = samples;
+    l.shader = sh;
+    l.geom = geom;
+    sc.tris.push_back(l);
+  } else if (n.type == "DiskLight") {
+    const F3 P = f3(n.at("P").v), up = f3(n.at("Up").v), at = f3(n.at("LookAt").v);
+    const float R = (float)n.at("Radius").f;
+    const int seg = n.has("Segments") ? (int)n.at("Segments").i : 20;
+    if (seg < 1 || seg > 65536) throw LoadError{VMR_ERR_INVALID, file + ": DiskLight Segments out of range"};
+    sc.geoms[geom] = disk_light_mesh(P, up, at, R, seg, sh);
+    vmr_disk_light l{};
+    std::memcpy(l.P, &P, 12);
+    std::memcpy(l.up, &up, 12);
+    std::memcpy(l.lookat, &at, 12);
+    l.radius = R;
+    l.samples = samples;
+    l.shader = sh;
+    l.geom = geom;
+    sc.disks.push_back(l);
+  } else if (n.type == "SphereLight") {
+    MeshOut o;
+    o.sphere = true;
+    for (int k = 0; k < 3; ++k) o.centre[k] = n.at("P").v[k];
+    o.radius = (float)n.at("Radius").f;
+    o.shaders = {sh};
+    sc.geoms[geom] = o;
+    vmr_sphere_light l{};
+    std::memcpy(l.P, o.centre, 12);
+    l.radius = o.radius;
+    l.samples = samples;
+    l.shader = sh;
+    l.geom = geom;
+    sc.spheres.push_back(l);
+  } else {
+    const F3 P = f3(n.at("P").v), U = f3(n.at("U").v), V = f3(n.at("V").v);
+    sc.geoms[geom] = quad_light_mesh(P, U, V, sh);
+    vmr_quad_light l{};
+    std::memcpy(l.p0, &P, 12);
+    std::memcpy(l.e1, &U, 12);
+    std::memcpy(l.e2, &V, 12);
+    l.shader = sh;
+    l.geom = geom;
+    sc.quads.push_back(l);
+  }
+}
+
+// core.AddNode and core.PreRender (core/core.go:29-104) over the file's
+// nodes.  Parsing adds every node: geoms join the scene then, in file order.
+// PreRender then runs over the nodes round by round: a light creates its
+// mesh (a new geom), an Include (builtin/misc/include.go) parses its file,
+// whose nodes are added at that point and PreRender'ed in the next round.
+// Shaders, Globals, the pixel filter and the camera are looked up over all
+// nodes once the rounds are done (a later node of a name wins, as core's
+// node map does).
+Scene build_scene(const std::vector<Node>& nodes, const std::string& file, int flags,
+                  std::vector<std::vector<Node>>& included) {
   Scene sc;
+  std::vector<Item> all, round;
+  std::vector<Slot> slots;
+  std::vector<Item> lights;
+  auto add = [&](const Item& it) {
+    all.push_back(it);
+    if (is_geom(*it.n)) slots.push_back(Slot{it, false});
+    round.push_back(it);
+  };
+  for (const Node& n : nodes) add(Item{&n, file});
+  for (int depth = 0; !round.empty(); ++depth) {
+    if (depth > 16) throw LoadError{VMR_ERR_INVALID, file + ": Include nesting deeper than 16"};
+    std::vector<Item> cur;
+    cur.swap(round);
+    for (const Item& it : cur) {
+      if (is_light(*it.n)) {
+        slots.push_back(Slot{it, true});
+      } else if (it.n->type == "Include") {
+        const std::string path = near(it.file, it.n->at("Filename").s);
+        included.push_back(parse_file(path));
+        for (const Node& c : included.back()) add(Item{&c, path});
+      }
+    }
+  }
   // core.Init's defaults; a Globals node starts from its own (256 x 256, MaxIter 0)
   sc.info.width = 1024;
   sc.info.height = 1024;
   sc.info.max_iter = 16;
   std::string cam_name = "camera";
-  for (const Node& n : nodes) {
+  for (const Item& it : all) {
+    const Node& n = *it.n;
     if (n.type == "Globals") {
       sc.info.width = n.has("XRes") ? (uint32_t)n.at("XRes").i : 256;
       sc.info.height = n.has("YRes") ? (uint32_t)n.at("YRes").i : 256;
       sc.info.max_iter = n.has("MaxIter") ? (int)n.at("MaxIter").i : 0;
       cam_name = n.has("Camera") && !n.at("Camera").s.empty() ? n.at("Camera").s : "camera";
-    } else if (n.type == "ShaderStd") {
+    } else if (n.type == "ShaderStd" || n.type == "DebugShader") {
       sc.shader_id[n.at("Name").s] = (uint32_t)sc.shaders.size();
-      sc.shaders.push_back(shader_std(n));
+      sc.shaders.push_back(n.type == "ShaderStd" ? shader_std(n) : debug_shader(n));
     } else if (n.type == "OutputHDR") {
       copy_name(sc.info.output_hdr, sizeof(sc.info.output_hdr), n.at("Filename").s);
     } else if (n.type == "OutputFloat") {
@@ -743,91 +1013,65 @@ Scene build_scene(const std::vector<Node>& nodes, const std::string& file, int f
   }
   if (sc.info.width == 0 || sc.info.height == 0 || sc.info.width > 4096 || sc.info.height > 4096)
     throw LoadError{VMR_ERR_INVALID, file + ": Globals XRes/YRes must be in [1, 4096]"};
-  // geoms in file order (core.AddNode)
-  for (const Node& n : nodes) {
-    if (n.type == "PolyMesh") {
-      sc.geoms.push_back(poly_mesh(n, sc, file));
-    } else if (n.type == "Sphere") {
-      MeshOut o;
-      o.sphere = true;
-      for (int k = 0; k < 3; ++k) o.centre[k] = n.at("P").v[k];
-      o.radius = (float)n.at("Radius").f;
-      o.shaders = {shader_of(sc, n, n.at("Shader").s, file)};
-      sc.geoms.push_back(o);
-    }
-  }
-  // lights, each adding its geom in PreRender (core.PreRender's first pass)
-  for (const Node& n : nodes) {
-    if (n.type != "TriLight" && n.type != "DiskLight" && n.type != "SphereLight" && n.type != "QuadLight") continue;
-    const uint32_t sh = shader_of(sc, n, n.at("Shader").s, file);
-    const int samples = n.has("Samples") ? (int)n.at("Samples").i : 1;
-    const uint32_t geom = (uint32_t)sc.geoms.size();
-    if (n.type == "TriLight") {
-      const F3 p0 = f3(n.at("P0").v), p1 = f3(n.at("P1").v), p2 = f3(n.at("P2").v);
-      sc.geoms.push_back(tri_light_mesh(p0, p1, p2, sh));
-      vmr_tri_light l{};
-      std::memcpy(l.p0, &p0, 12);
-      std::memcpy(l.p1, &p1, 12);
-      std::memcpy(l.p2, &p2, 12);
-      l.samples = samples;
-      l.shader = sh;
-      l.geom = geom;
-      sc.tris.push_back(l);
-    } else if (n.type == "DiskLight") {
-      const F3 P = f3(n.at("P").v), up = f3(n.at("Up").v), at = f3(n.at("LookAt").v);
-      const float R = (float)n.at("Radius").f;
-      const int seg = n.has("Segments") ? (int)n.at("Segments").i : 20;
-      if (seg < 1 || seg > 65536) throw LoadError{VMR_ERR_INVALID, file + ": DiskLight Segments out of range"};
-      sc.geoms.push_back(disk_light_mesh(P, up, at, R, seg, sh));
-      vmr_disk_light l{};
-      std::memcpy(l.P, &P, 12);
-      std::memcpy(l.up, &up, 12);
-      std::memcpy(l.lookat, &at, 12);
-      l.radius = R;
-      l.samples = samples;
-      l.shader = sh;
-      l.geom = geom;
-      sc.disks.push_back(l);
-    } else if (n.type == "SphereLight") {
-      MeshOut o;
-      o.sphere = true;
-      for (int k = 0; k < 3; ++k) o.centre[k] = n.at("P").v[k];
-      o.radius = (float)n.at("Radius").f;
-      o.shaders = {sh};
-      sc.geoms.push_back(o);
-      vmr_sphere_light l{};
-      std::memcpy(l.P, o.centre, 12);
-      l.radius = o.radius;
-      l.samples = samples;
-      l.shader = sh;
-      l.geom = geom;
-      sc.spheres.push_back(l);
-    } else {
-      const F3 P = f3(n.at("P").v), U = f3(n.at("U").v), V = f3(n.at("V").v);
-      sc.geoms.push_back(quad_light_mesh(P, U, V, sh));
-      vmr_quad_light l{};
-      std::memcpy(l.p0, &P, 12);
-      std::memcpy(l.e1, &U, 12);
-      std::memcpy(l.e2, &V, 12);
-      l.shader = sh;
-      l.geom = geom;
-      sc.quads.push_back(l);
-    }
-  }
-  // the render's camera (core/render.go:147-162)
-  const Node* cam = nullptr;
-  for (const Node& n : nodes)
-    if (n.type == "Camera" && n.at("Name").s == cam_name) cam = &n;
+  // the scene's geoms in slot order; the light tables in the order the
+  // lights were added (parse order, then the included files')
+  sc.geoms.resize(slots.size());
+  std::vector<uint32_t> light_slot;
+  std::vector<Item> light_items;
+  for (size_t i = 0; i < slots.size(); ++i)
+    if (!slots[i].light_mesh) sc.geoms[i] = geom_of(slots[i].it, sc);
+  for (const Item& it : all)
+    if (is_light(*it.n))
+      for (size_t i = 0; i < slots.size(); ++i)
+        if (slots[i].light_mesh && slots[i].it.n == it.n) light_of(it, sc, (uint32_t)i);
+  // the render's camera (core/render.go:147-162): the last Camera of the name
+  const Item* cam = nullptr;
+  for (const Item& it : all)
+    if (it.n->type == "Camera" && it.n->at("Name").s == cam_name) cam = &it;
   if (!cam) throw LoadError{VMR_ERR_INVALID, file + ": no camera named " + cam_name};
-  sc.cam = camera(*cam, sc.info, file);
+  sc.cam = camera(*cam->n, sc.info, cam->file, sc.cam_keys);
   copy_name(sc.info.camera, sizeof(sc.info.camera), cam_name);
   (void)flags;
   return sc;
 }
 
+std::vector<Node> parse_file(const std::string& path) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) throw LoadError{VMR_ERR_INVALID, std::string("cannot open ") + path};
+  std::stringstream ss;
+  ss << in.rdbuf();
+  Parser p(ss.str(), path);
+  return p.parse();
+}
+
 int fail(vmr_ctx* ctx, int code, const std::string& m) {
   ctx->err = m;
   return code;
+}
+
+// One mesh or sphere through the C ABI (vmr_mesh_build or vmr_sphere_add,
+// then its transform).
+int upload_geom(vmr_ctx* ctx, const MeshOut& g, int mode, uint32_t* id) {
+  if (g.sphere) return vmr_sphere_add(ctx, g.centre, g.radius, id);
+  vmr_mesh_input mi{};
+  mi.verts = g.verts.data();
+  mi.n_verts = g.n_verts;
+  mi.motion_keys = g.keys;
+  mi.idxp = g.idxp.data();
+  mi.n_tris = (uint32_t)(g.idxp.size() / 3);
+  mi.ray_bias = g.ray_bias;
+  mi.motion_mode = mode;
+  mi.shader_idx = g.sidx.empty() ? nullptr : g.sidx.data();
+  int rc = vmr_mesh_build(ctx, &mi, id);
+  if (rc == VMR_OK && g.has_xf) rc = vmr_mesh_set_transform(ctx, *id, g.xf);
+  if (rc == VMR_OK && !g.xkeys.empty())
+    rc = vmr_mesh_set_transform_keys(ctx, *id, g.xkeys.data(), (uint32_t)(g.xkeys.size() / 16));
+  return rc;
+}
+
+int set_shading(vmr_ctx* ctx, uint32_t id, const MeshOut& g) {
+  return vmr_mesh_set_shading(ctx, id, g.shaders.data(), (uint32_t)g.shaders.size(),
+                              g.normals.empty() ? nullptr : g.normals.data());
 }
 
 }  // namespace
@@ -841,49 +1085,58 @@ extern "C" int vmr_get_camera(vmr_ctx* ctx, vmr_camera* camera) {
 
 extern "C" int vmr_load_vnf(vmr_ctx* ctx, const char* path, int flags, vmr_vnf_info* info) {
   if (!ctx || !path) return VMR_ERR_INVALID;
-  std::ifstream in(path, std::ios::binary);
-  if (!in) return fail(ctx, VMR_ERR_INVALID, std::string("cannot open ") + path);
-  std::stringstream ss;
-  ss << in.rdbuf();
   Scene sc;
+  std::vector<std::vector<Node>> included;  // the Include files' nodes, alive while the scene is built
   try {
-    Parser p(ss.str(), path);
-    const std::vector<Node> nodes = p.parse();
-    sc = build_scene(nodes, path, flags);
+    const std::vector<Node> nodes = parse_file(path);
+    sc = build_scene(nodes, path, flags, included);
   } catch (const LoadError& e) {
     return fail(ctx, e.code, e.msg);
   } catch (const std::exception& e) {
     return fail(ctx, VMR_ERR_INVALID, std::string(path) + ": " + e.what());
   }
-  // upload through the C ABI, as a host binding would
+  // upload through the C ABI, as a host binding would: meshes and spheres
+  // first, then the instances and Procs that reference them
   const int mode = (flags & VMR_VNF_MOTION_FIXED) ? VMR_MOTION_FIXED : VMR_MOTION_FAITHFUL;
-  std::vector<uint32_t> ids;
-  for (const MeshOut& g : sc.geoms) {
-    uint32_t id = 0;
+  std::vector<uint32_t> ids(sc.geoms.size()), child_ids(sc.proc_children.size());
+  std::map<std::string, size_t> by_name;
+  for (size_t i = 0; i < sc.geoms.size(); ++i) {
+    const MeshOut& g = sc.geoms[i];
+    if (!g.name.empty() && !by_name.count(g.name)) by_name[g.name] = i;
+    if (g.group) continue;
+    const int rc = upload_geom(ctx, g, mode, &ids[i]);
+    if (rc != VMR_OK) return rc;
+  }
+  for (size_t i = 0; i < sc.proc_children.size(); ++i) {
+    const int rc = upload_geom(ctx, sc.proc_children[i], mode, &child_ids[i]);
+    if (rc != VMR_OK) return rc;
+  }
+  for (size_t i = 0; i < sc.geoms.size(); ++i) {
+    const MeshOut& g = sc.geoms[i];
+    if (!g.group) continue;
+    const uint32_t nk = (uint32_t)(g.gkeys.size() / 16);
     int rc;
-    if (g.sphere) {
-      rc = vmr_sphere_add(ctx, g.centre, g.radius, &id);
+    if (g.group == 1) {
+      auto it = by_name.find(g.ref);
+      if (it == by_name.end() || sc.geoms[it->second].group)
+        return fail(ctx, it == by_name.end() ? VMR_ERR_INVALID : VMR_ERR_UNSUPPORTED,
+                    std::string(path) + ": GeomInstance " + g.name + ": unable to find geom " + g.ref +
+                        (it == by_name.end() ? "" : " (instances of instances or Procs are not supported)"));
+      rc = vmr_instance_add(ctx, ids[it->second], g.gkeys.data(), nk, g.bmin, g.bmax, &ids[i]);
     } else {
-      vmr_mesh_input mi{};
-      mi.verts = g.verts.data();
-      mi.n_verts = g.n_verts;
-      mi.motion_keys = g.keys;
-      mi.idxp = g.idxp.data();
-      mi.n_tris = (uint32_t)(g.idxp.size() / 3);
-      mi.ray_bias = g.ray_bias;
-      mi.motion_mode = mode;
-      mi.shader_idx = g.sidx.empty() ? nullptr : g.sidx.data();
-      rc = vmr_mesh_build(ctx, &mi, &id);
-      if (rc == VMR_OK && g.has_xf) rc = vmr_mesh_set_transform(ctx, id, g.xf);
+      std::vector<uint32_t> ch;
+      for (size_t c : g.children) ch.push_back(child_ids[c]);
+      rc = vmr_proc_add(ctx, ch.data(), (uint32_t)ch.size(), nk ? g.gkeys.data() : nullptr, nk, g.bmin, g.bmax,
+                        &ids[i]);
     }
     if (rc != VMR_OK) return rc;
-    ids.push_back(id);
   }
   int rc = vmr_scene_build(ctx, ids.data(), (uint32_t)ids.size());
   if (rc == VMR_OK) rc = vmr_set_shaders(ctx, sc.shaders.data(), (uint32_t)sc.shaders.size());
   for (size_t g = 0; g < sc.geoms.size() && rc == VMR_OK; ++g)
-    rc = vmr_mesh_set_shading(ctx, ids[g], sc.geoms[g].shaders.data(), (uint32_t)sc.geoms[g].shaders.size(),
-                              sc.geoms[g].normals.empty() ? nullptr : sc.geoms[g].normals.data());
+    if (!sc.geoms[g].group) rc = set_shading(ctx, ids[g], sc.geoms[g]);
+  for (size_t g = 0; g < sc.proc_children.size() && rc == VMR_OK; ++g)
+    rc = set_shading(ctx, child_ids[g], sc.proc_children[g]);
   auto remap = [&](uint32_t g) { return ids[g]; };
   for (auto& l : sc.tris) l.geom = remap(l.geom);
   for (auto& l : sc.disks) l.geom = remap(l.geom);
@@ -896,6 +1149,8 @@ extern "C" int vmr_load_vnf(vmr_ctx* ctx, const char* path, int flags, vmr_vnf_i
   const float black[3] = {0.f, 0.f, 0.f};
   if (rc == VMR_OK) rc = vmr_set_env_light(ctx, black);
   if (rc == VMR_OK) rc = vmr_set_camera(ctx, &sc.cam);
+  if (rc == VMR_OK && sc.cam_keys.size() > 16)
+    rc = vmr_set_camera_keys(ctx, sc.cam_keys.data(), (uint32_t)(sc.cam_keys.size() / 16));
   if (rc == VMR_OK) {
     vmr_pixel_filter none{VMR_FILTER_BOX, 0, 0.f, 0.f};
     rc = vmr_set_pixel_filter(ctx, sc.has_filter ? &sc.filter : &none);

@@ -581,10 +581,12 @@ def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = Tru
           xf_matrix(0.9, (1, 1, 0), (1.2, 1.2, 1.2), (0.52, 0.92, -0.35))]
     lo, hi = _box_of(ow, k2)
     M.append(dict(instance=i_obj, keys=k2, bmin=lo, bmax=hi, shaders=[]))
-    M.append(dict(sphere=(0.0, 0.0, 0.0, 0.12), shaders=[7]))
+    # (off the origin: two geoms with one box centroid, here the room's, make
+    # the reference's top-level split recurse forever, qbvh/build.go:34-43)
+    M.append(dict(sphere=(0.03, 0.02, -0.01, 0.12), shaders=[7]))
     i_sph = len(M) - 1
-    k3 = [xf_matrix(0.0, (0, 0, 1), (1.0, 1.5, 1.0), (-0.45, 0.25, -0.45))]
-    lo, hi = _box_of(np.array([[-0.12] * 3, [0.12] * 3]), k3, margin=0.2)
+    k3 = [xf_matrix(0.0, (0, 0, 1), (1.0, 1.5, 1.0), (-0.48, 0.23, -0.44))]
+    lo, hi = _box_of(np.array([[-0.09, -0.1, -0.13], [0.15, 0.14, 0.11]]), k3, margin=0.2)
     M.append(dict(instance=i_sph, keys=k3, bmin=lo, bmax=hi, shaders=[]))
     # a Proc's children: meshes made for it (they join no scene themselves)
     av, ai = triangle_soup(400, seed + 91, lo=-0.12, hi=0.12, edge=0.03)
@@ -625,15 +627,56 @@ def _light_mesh_ids(scene: dict) -> set:
     return ids
 
 
-def to_vnf(scene: dict, width: int, height: int, max_iter: int = 16) -> str:
+def _mat_rows(keys) -> str:
+    """Matrices (column-major 16 each) as the parser reads them: row by row
+    (the reader transposes)."""
+    a = np.asarray(keys, np.float32).reshape(-1, 16)
+    return " ".join(_vnf_num(x) for k in a for x in k.reshape(4, 4).T.ravel())
+
+
+def _geom_node(gi: int, m: dict) -> str:
+    if "sphere" in m:
+        c = m["sphere"]
+        return (f'Sphere {{\n  Name "geom{gi}"\n  P {_vnf_num(c[0])} {_vnf_num(c[1])} {_vnf_num(c[2])}\n'
+                f'  Radius {_vnf_num(c[3])}\n  Shader "sh{m["shaders"][0]}"\n}}')
+    keys = int(m.get("keys", 1))
+    v = np.asarray(m["verts"], np.float32).reshape(-1, 3)
+    per = v.shape[0] // keys
+    idx = np.asarray(m["idxp"], np.uint32)
+    lines = [f'PolyMesh {{\n  Name "geom{gi}"',
+             f"  Verts {keys} {per} point " + " ".join(_vnf_num(x) for x in v.ravel()),
+             f"  FaceIdx {idx.size} int " + " ".join(str(int(x)) for x in idx),
+             f"  Shader {len(m['shaders'])} string " + " ".join(f'"sh{s}"' for s in m["shaders"])]
+    if m.get("face_shader") is not None:
+        fs = np.asarray(m["face_shader"], np.uint8)
+        lines.append(f"  ShaderIdx {fs.size} int " + " ".join(str(int(x)) for x in fs))
+    if m.get("normals") is not None:
+        nr = np.asarray(m["normals"], np.float32).reshape(-1, 3)
+        lines.append(f"  Normals 1 {nr.shape[0]} vec3 " + " ".join(_vnf_num(x) for x in nr.ravel()))
+    if m.get("transform_keys") is not None:
+        k = np.asarray(m["transform_keys"], np.float32).reshape(-1, 16)
+        lines.append(f"  Transform {k.shape[0]} matrix " + _mat_rows(k))
+    elif m.get("transform") is not None:
+        lines.append("  Transform 1 matrix " + _mat_rows(m["transform"]))
+    return "\n".join(lines) + "\n}"
+
+
+def to_vnf(scene: dict, width: int, height: int, max_iter: int = 16, extra_files: dict | None = None) -> str:
     """The scene as a .vnf file the reference's parser (nodes/parser.go) and
-    vmr_load_vnf read: ShaderStd nodes "sh<i>", a PolyMesh or Sphere node per
-    geom that is not a light's own mesh, the lights (which create their
-    meshes when loaded), a matrix Camera "camera" with the scene camera's
-    LocalToWorld, Fov and Focal, Globals, and the pixel filter if any.  The
-    environment light has no node in the reference and is not written."""
+    vmr_load_vnf read: ShaderStd (or DebugShader) nodes "sh<i>", a PolyMesh,
+    Sphere, GeomInstance or Proc node per geom that is neither a light's own
+    mesh nor a Proc's child, the lights (which create their meshes when
+    loaded), a matrix Camera "camera" with the scene camera's LocalToWorld
+    keys, Fov and Focal, Globals, and the pixel filter if any.  A Proc's
+    children go to a file of their own that its Data names (Handler "vnf"):
+    extra_files receives {name: text} for those.  The environment light has
+    no node in the reference and is not written."""
     out = []
     for i, d in enumerate(scene["shaders"]):
+        if d.get("debug"):
+            out.append(f'DebugShader {{\n  Name "sh{i}"\n  Colour rgb ' +
+                       " ".join(_vnf_num(x) for x in d["diffuse_colour"]) + "\n}")
+            continue
         out.append(f'ShaderStd {{\n  Name "sh{i}"')
         names = {"emission_colour": "EmissionColour", "emission_strength": "EmissionStrength",
                  "diffuse_colour": "DiffuseColour", "diffuse_strength": "DiffuseStrength",
@@ -651,32 +694,27 @@ def to_vnf(scene: dict, width: int, height: int, max_iter: int = 16) -> str:
             out.append(f'  Spec1FresnelModel "{d["spec1_fresnel"]}"')
         out.append("}")
     lights = _light_mesh_ids(scene)
+    children = {c for m in scene["meshes"] if "proc" in m for c in m["proc"]}
+    pt = lambda a: "1 1 point " + " ".join(_vnf_num(x) for x in a)  # noqa: E731
     for gi, m in enumerate(scene["meshes"]):
-        if gi in lights:
+        if gi in lights or gi in children:
             continue
-        if "sphere" in m:
-            c = m["sphere"]
-            out.append(f'Sphere {{\n  Name "geom{gi}"\n  P {_vnf_num(c[0])} {_vnf_num(c[1])} {_vnf_num(c[2])}\n'
-                       f'  Radius {_vnf_num(c[3])}\n  Shader "sh{m["shaders"][0]}"\n}}')
-            continue
-        keys = int(m.get("keys", 1))
-        v = np.asarray(m["verts"], np.float32).reshape(-1, 3)
-        per = v.shape[0] // keys
-        idx = np.asarray(m["idxp"], np.uint32)
-        lines = [f'PolyMesh {{\n  Name "geom{gi}"',
-                 f"  Verts {keys} {per} point " + " ".join(_vnf_num(x) for x in v.ravel()),
-                 f"  FaceIdx {idx.size} int " + " ".join(str(int(x)) for x in idx),
-                 f"  Shader {len(m['shaders'])} string " + " ".join(f'"sh{s}"' for s in m["shaders"])]
-        if m.get("face_shader") is not None:
-            fs = np.asarray(m["face_shader"], np.uint8)
-            lines.append(f"  ShaderIdx {fs.size} int " + " ".join(str(int(x)) for x in fs))
-        if m.get("normals") is not None:
-            nr = np.asarray(m["normals"], np.float32).reshape(-1, 3)
-            lines.append(f"  Normals 1 {nr.shape[0]} vec3 " + " ".join(_vnf_num(x) for x in nr.ravel()))
-        if m.get("transform") is not None:  # column-major; written row by row, the reader transposes
-            xt = np.asarray(m["transform"], np.float32).reshape(4, 4).T
-            lines.append("  Transform 1 matrix " + " ".join(_vnf_num(x) for x in xt.ravel()))
-        out.append("\n".join(lines) + "\n}")
+        if "instance" in m:
+            k = np.asarray(m["keys"], np.float32).reshape(-1, 16)
+            out.append(f'GeomInstance {{\n  Name "geom{gi}"\n  Geom "geom{m["instance"]}"\n  BMin {pt(m["bmin"])}\n'
+                       f'  BMax {pt(m["bmax"])}\n  Transform {k.shape[0]} matrix {_mat_rows(k)}\n}}')
+        elif "proc" in m:
+            name = f"proc{gi}.vnf"
+            if extra_files is not None:
+                extra_files[name] = "\n".join(_geom_node(c, scene["meshes"][c]) for c in m["proc"]) + "\n"
+            lines = [f'Proc {{\n  Name "geom{gi}"\n  Handler "vnf"\n  Data "{name}"',
+                     f"  BMin {pt(m['bmin'])}\n  BMax {pt(m['bmax'])}"]
+            if m.get("keys") is not None:
+                k = np.asarray(m["keys"], np.float32).reshape(-1, 16)
+                lines.append(f"  Transform {k.shape[0]} matrix {_mat_rows(k)}")
+            out.append("\n".join(lines) + "\n}")
+        else:
+            out.append(_geom_node(gi, m))
     vec = lambda a: " ".join(_vnf_num(x) for x in a)  # noqa: E731
     for i, l in enumerate(scene.get("lights", [])):
         out.append(f'TriLight {{\n  Name "tri{i}"\n  P0 {vec(l["p0"])}\n  P1 {vec(l["p1"])}\n  P2 {vec(l["p2"])}\n'
@@ -692,12 +730,12 @@ def to_vnf(scene: dict, width: int, height: int, max_iter: int = 16) -> str:
         out.append(f'QuadLight {{\n  Name "quad{i}"\n  P {vec(l["p0"])}\n  U {vec(l["e1"])}\n  V {vec(l["e2"])}\n'
                    f'  Shader "sh{l["shader"]}"\n}}')
     c = scene["camera"]
-    m44 = np.asarray(c["m"], np.float32).reshape(4, 4).T  # written row by row; the reader transposes
+    ck = np.asarray(c["keys"] if c.get("keys") is not None else c["m"], np.float32).reshape(-1, 16)
     out.append('Camera {\n  Name "camera"\n  Type "matrix"\n  From 1 1 point 0 0 0\n  To 1 1 point 0 0 -1\n'
                '  Roll 1 1 float 0\n  Up 0 1 0\n'
                f'  Fov {_vnf_num(c.get("fov", 90.0))}\n  Focal {_vnf_num(c["focal"])}\n'
                f'  Aspect {_vnf_num(c["aspect"])}\n  Radius {_vnf_num(c["radius"])}\n'
-               f"  LocalToWorld 1 matrix {vec(m44.ravel())}\n}}")
+               f"  LocalToWorld {ck.shape[0]} matrix {_mat_rows(ck)}\n}}")
     out.append(f"Globals {{\n  XRes {int(width)}\n  YRes {int(height)}\n  MaxIter {int(max_iter)}\n}}")
     pf = scene.get("pixel_filter")
     if pf:
