@@ -396,6 +396,11 @@ typedef struct {
     uint32_t iter_begin, iter_count;  /* core.Render loop iterations */
     uint64_t seed;                    /* per-pixel scrambles */
     uint32_t max_batch_samples;       /* samples per wavefront batch (0: 4M) */
+    /* A band of the image's rows: rows [row_begin, row_begin + row_count) of
+     * the width x height image, fb holding just those rows; each pixel's
+     * samples are the full render's, so the bands of a split render put
+     * together are the one-call image bit for bit.  row_count 0: all rows. */
+    uint32_t row_begin, row_count;
 } vmr_render_params;
 
 typedef struct {
@@ -578,6 +583,9 @@ typedef struct {
                                          record) only the first guide_depth
                                          vertices of a path; deeper vertices
                                          sample the BSDF alone (0: all) */
+    uint32_t row_begin, row_count;    /* a band of rows, as vmr_render_params
+                                         (0: all rows); not with VMR_PATH_TRAIN
+                                         (a band would train on its rows only) */
 } vmr_path_params;
 
 enum {
@@ -612,6 +620,28 @@ typedef struct {
  * i = the 0-based iteration: the exact mean of the samples (the reference's
  * fold starts at i+1 and so counts the initial buffer as a sample, F6). */
 int vmr_render_path(vmr_ctx* ctx, const vmr_path_params* params, float* fb, vmr_path_stats* stats);
+
+/* ------------------------------------------------------- several GPUs */
+/* One image over n contexts (each on its own GPU, each holding the same
+ * scene, camera, lights and settings): the reference's tile split of a
+ * render (core/render.go:184-204) across devices.  The rows are cut into n
+ * contiguous bands (vmr_split_rows); context i renders band i
+ * (row_begin/row_count) on its own host thread straight into its rows of fb
+ * (width*height*3 floats, folded into as vmr_render does).  Every pixel is
+ * sampled and folded by one context only, exactly as in a one-context
+ * render, so the image is that render's bit for bit; no framebuffer
+ * reduction is needed.  params' row_count must be 0.  Stats sum over the
+ * bands; ms is the slowest band's. */
+int vmr_render_split(vmr_ctx* const* ctxs, uint32_t n, const vmr_render_params* params, float* fb,
+                     vmr_render_stats* stats);
+/* The same for the extended path tracer (fb64 split alike); not with
+ * VMR_PATH_TRAIN (each band would train its own guide on its rows); a
+ * guided render needs the same guide weights in every context. */
+int vmr_render_path_split(vmr_ctx* const* ctxs, uint32_t n, const vmr_path_params* params, float* fb,
+                          vmr_path_stats* stats);
+/* The bands of a split: height rows into n contiguous bands, the first
+ * height % n of them one row taller.  Host-side, needs no context or GPU. */
+int vmr_split_rows(uint32_t height, uint32_t n, uint32_t* row_begin, uint32_t* row_count);
 
 /* Queue capacity (paths per wavefront batch, whole iterations) of the
  * context's one-scene renders when params.max_batch_samples is 0.

@@ -208,6 +208,10 @@ int orc_render_add_sphere_lights(orc_render* r, const orc_spherelight* lights, u
  * fb: w*h*3 floats, in/out.  seed: per-pixel scrambles (see orc_scramble). */
 int orc_render_run(orc_render* r, uint32_t w, uint32_t h, uint32_t iter_begin, uint32_t iter_count,
                    uint64_t seed, float* fb, int nthreads);
+/* Rows [row0, row0 + nrows) of the w x h image only (nrows 0: all); fb holds
+ * those rows.  Each pixel is sampled as in the whole render. */
+int orc_render_run_rows(orc_render* r, uint32_t w, uint32_t h, uint32_t row0, uint32_t nrows, uint32_t iter_begin,
+                        uint32_t iter_count, uint64_t seed, float* fb, int nthreads);
 /* The scramble k (0 lensU, 1 lensV, 2 time, 3 lambda, 4 light/glossy 0,
  * 5 light/glossy 1) of pixel pix: replaces the reference's draws from
  * math/rand (core/render.go:166-176). */
@@ -231,6 +235,9 @@ typedef struct {
  * NULL) both receive the running mean buf = (buf*j + L)/(j+1). */
 int orc_pt_run(const orc_render* r, const orc_quad_light* quads, uint32_t n_quads, const orc_pt_params* p,
                float* fb, double* fb64, int precision, int nthreads);
+/* orc_pt_run over rows [row0, row0 + nrows) only (nrows 0: all). */
+int orc_pt_run_rows(const orc_render* r, const orc_quad_light* quads, uint32_t n_quads, const orc_pt_params* p,
+                    uint32_t row0, uint32_t nrows, float* fb, double* fb64, int precision, int nthreads);
 /* Random number `dim` of pixel sample (pix, j = iteration + 1). */
 float orc_pt_rnd(uint64_t seed, uint64_t pix, uint32_t j, uint32_t dim);
 /* PolyMesh.Transform of a mesh (column-major 4x4, NULL: none); scenes and

@@ -178,6 +178,12 @@ def _register_render(L):
     L.orc_scramble.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32]
     L.orc_pt_run.restype = ctypes.c_int
     L.orc_pt_run.argtypes = [P, P, ctypes.c_uint32, P, P, P, ctypes.c_int, ctypes.c_int]
+    L.orc_pt_run_rows.restype = ctypes.c_int
+    L.orc_pt_run_rows.argtypes = [P, P, ctypes.c_uint32, P, ctypes.c_uint32, ctypes.c_uint32, P, P, ctypes.c_int,
+                                  ctypes.c_int]
+    L.orc_render_run_rows.restype = ctypes.c_int
+    L.orc_render_run_rows.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, P, ctypes.c_int]
     L.orc_pt_rnd.restype = ctypes.c_float
     L.orc_pt_rnd.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
     L.orc_sincos_turns.argtypes = [P, ctypes.c_size_t, P, P]
@@ -329,9 +335,12 @@ class Render:
     def __init__(self, scene):
         self.meshes = build_geoms(scene["meshes"])
         self.scene = scene_of(scene["meshes"], self.meshes)
-        counts = np.asarray([len(m["shaders"]) for m in scene["meshes"]], np.uint32)
+        # an instance shades with the shaders of the geom it instances
+        lists = [scene["meshes"][m["instance"]]["shaders"] if "instance" in m else m["shaders"]
+                 for m in scene["meshes"]]
+        counts = np.asarray([len(x) for x in lists], np.uint32)
         offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32)
-        lst = np.asarray([s for m in scene["meshes"] for s in m["shaders"]], np.uint32)
+        lst = np.asarray([s for x in lists for s in x], np.uint32)
         shs = (OrcShader * len(scene["shaders"]))()
         for i, d in enumerate(scene["shaders"]):
             fl = 0
@@ -402,29 +411,37 @@ class Render:
             self.h = None
 
     def run_path(self, width, height, iter_begin, iter_count, seed, max_depth=4, rr_depth=3, precision=32, fb=None,
-                 fb64=None, nthreads=0):
+                 fb64=None, nthreads=0, rows=None):
         """The extended path tracer (orc_pt.cpp) over this scene plus its
-        'quad_lights' and 'env'.  Returns (fb float32, fb64 float64)."""
+        'quad_lights' and 'env'; rows = (row_begin, row_count): that band
+        only.  Returns (fb float32, fb64 float64)."""
+        r0, nr = rows if rows is not None else (0, 0)
+        hb = nr if rows is not None else height
         if fb is None:
-            fb = np.zeros((height, width, 3), np.float32)
+            fb = np.zeros((hb, width, 3), np.float32)
         if fb64 is None:
-            fb64 = np.zeros((height, width, 3), np.float64)
+            fb64 = np.zeros((hb, width, 3), np.float64)
         fb = np.ascontiguousarray(fb, np.float32)
         fb64 = np.ascontiguousarray(fb64, np.float64)
         quads = self._quads
         p = OrcPtParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth,
                         (ctypes.c_float * 3)(*[float(x) for x in self._env]))
-        rc = lib().orc_pt_run(self.h, quads, len(quads), ctypes.byref(p), _ptr(fb), _ptr(fb64), int(precision),
-                              int(nthreads))
+        rc = lib().orc_pt_run_rows(self.h, quads, len(quads), ctypes.byref(p), r0, nr, _ptr(fb), _ptr(fb64),
+                                   int(precision), int(nthreads))
         if rc != 0:
             raise RuntimeError("orc_pt_run failed")
         return fb, fb64
 
-    def run(self, width, height, iter_begin, iter_count, seed, fb=None, nthreads=0):
+    def run(self, width, height, iter_begin, iter_count, seed, fb=None, nthreads=0, rows=None):
+        """Reference-mode render; rows = (row_begin, row_count) renders that
+        band only (fb then holds row_count rows)."""
+        r0, nr = rows if rows is not None else (0, 0)
         if fb is None:
-            fb = np.zeros((height, width, 3), np.float32)
+            fb = np.zeros((nr if rows is not None else height, width, 3), np.float32)
         fb = np.ascontiguousarray(fb, np.float32)
-        lib().orc_render_run(self.h, width, height, iter_begin, iter_count, seed, _ptr(fb), int(nthreads))
+        if lib().orc_render_run_rows(self.h, width, height, r0, nr, iter_begin, iter_count, seed, _ptr(fb),
+                                     int(nthreads)) != 0:
+            raise ValueError("row band outside the image")
         return fb
 
 

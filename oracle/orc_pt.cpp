@@ -637,14 +637,17 @@ void setup(PT<T>& pt, const orc_render* r, const orc_quad_light* quads, uint32_t
   }
 }
 
+// Rows [row0, row0 + nrows) of the image (nrows 0: all); fb and fb64 hold
+// those rows only.
 template <class T>
 int run(const orc_render* r, const orc_quad_light* quads, uint32_t nq, const orc_pt_params* p, float* fb, double* fb64,
-        int nthreads) {
+        int nthreads, uint32_t row0 = 0, uint32_t nrows = 0) {
   PT<T> pt;
   setup(pt, r, quads, nq, p);
   if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
   const uint32_t w = p->width, h = p->height;
-  const size_t npix = (size_t)w * h;
+  if (nrows == 0) nrows = h;
+  const size_t npix = (size_t)w * nrows, pix0 = (size_t)row0 * w;
   for (uint32_t it = p->iter_begin; it < p->iter_begin + p->iter_count; ++it) {
     const uint32_t j = it + 1;
     std::atomic<size_t> next(0);
@@ -652,10 +655,12 @@ int run(const orc_render* r, const orc_quad_light* quads, uint32_t nq, const orc
       for (;;) {
         const size_t s0 = next.fetch_add(64);
         if (s0 >= npix) break;
-        for (size_t pix = s0; pix < std::min(npix, s0 + 64); ++pix) {
+        for (size_t lp = s0; lp < std::min(npix, s0 + 64); ++lp) {
+          const size_t gp = pix0 + lp;  // the image pixel
+          const size_t pix = lp;        // its place in the band
           float P[3], D[3], time;
-          orc_internal::camera_primary(pt.R.cam, pt.R.cam_keys, w, h, j, pix, p->seed, P, D, &time, &pt.R.filter);
-          const Vec<T> L = pt.path(sample_key(p->seed, pix, j), P, D, time);
+          orc_internal::camera_primary(pt.R.cam, pt.R.cam_keys, w, h, j, gp, p->seed, P, D, &time, &pt.R.filter);
+          const Vec<T> L = pt.path(sample_key(p->seed, gp, j), P, D, time);
           const T Lc[3] = {L.x, L.y, L.z};
           for (int k = 0; k < 3; ++k) {  // exact running mean over iterations 0..it
             if (fb) fb[pix * 3 + k] = (fb[pix * 3 + k] * (float)it + (float)Lc[k]) / (float)(it + 1);
@@ -683,9 +688,14 @@ void orc_sincos_turns(const float* u, size_t n, float* s, float* c) {
 
 int orc_pt_run(const orc_render* r, const orc_quad_light* quads, uint32_t n_quads, const orc_pt_params* p, float* fb,
                double* fb64, int precision, int nthreads) {
-  if (!r || !p) return -1;
-  if (precision == 64) return run<double>(r, quads, n_quads, p, fb, fb64, nthreads);
-  return run<float>(r, quads, n_quads, p, fb, fb64, nthreads);
+  return orc_pt_run_rows(r, quads, n_quads, p, 0, 0, fb, fb64, precision, nthreads);
+}
+
+int orc_pt_run_rows(const orc_render* r, const orc_quad_light* quads, uint32_t n_quads, const orc_pt_params* p,
+                    uint32_t row0, uint32_t nrows, float* fb, double* fb64, int precision, int nthreads) {
+  if (!r || !p || row0 + nrows > p->height) return -1;
+  if (precision == 64) return run<double>(r, quads, n_quads, p, fb, fb64, nthreads, row0, nrows);
+  return run<float>(r, quads, n_quads, p, fb, fb64, nthreads, row0, nrows);
 }
 
 }  // extern "C"

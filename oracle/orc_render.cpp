@@ -1148,10 +1148,17 @@ void orc_render_destroy(orc_render* r) { delete r; }
 
 int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, uint32_t iter_count, uint64_t seed,
                    float* fb, int nthreads) {
+  return orc_render_run_rows(o, w, h, 0, 0, iter_begin, iter_count, seed, fb, nthreads);
+}
+
+int orc_render_run_rows(orc_render* o, uint32_t w, uint32_t h, uint32_t row0, uint32_t nrows, uint32_t iter_begin,
+                        uint32_t iter_count, uint64_t seed, float* fb, int nthreads) {
+  if (row0 + nrows > h) return -1;
   const Render& R = o->r;
   Renderer rr{R};
   if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
-  const size_t npix = (size_t)w * h;
+  if (nrows == 0) nrows = h;
+  const size_t npix = (size_t)w * nrows, pix0 = (size_t)row0 * w;
   for (uint32_t it = iter_begin; it < iter_begin + iter_count; ++it) {
     const uint32_t j = it + 1;  // render(iter+1, ...) (core/render.go:192)
     std::atomic<size_t> next(0);
@@ -1159,7 +1166,8 @@ int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, u
       for (;;) {
         const size_t s = next.fetch_add(256);
         if (s >= npix) break;
-        for (size_t pix = s; pix < std::min(npix, s + 256); ++pix) {
+        for (size_t lp = s; lp < std::min(npix, s + 256); ++lp) {
+          const size_t pix = pix0 + lp;  // the image pixel; lp its place in the band
           float Pf[3], Df[3], tf;
           orc_internal::camera_primary(R.cam, R.cam_keys, w, h, j, pix, seed, Pf, Df, &tf, &R.filter);
           const V3 P = v3(Pf[0], Pf[1], Pf[2]), D = v3(Df[0], Df[1], Df[2]);
@@ -1175,7 +1183,7 @@ int orc_render_run(orc_render* o, uint32_t w, uint32_t h, uint32_t iter_begin, u
           RGB col{{0, 0, 0}};
           rr.trace(P, D, 0, sc, col);
           for (int k = 0; k < 3; ++k)
-            fb[pix * 3 + k] = (fb[pix * 3 + k] * (float)j + col.c[k]) / (float)(j + 1);  // render.go:127-129
+            fb[lp * 3 + k] = (fb[lp * 3 + k] * (float)j + col.c[k]) / (float)(j + 1);  // render.go:127-129
         }
       }
     };

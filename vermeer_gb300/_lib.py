@@ -106,7 +106,7 @@ VNF_MOTION_FIXED = 1
 
 class RenderParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
-                ("seed", ctypes.c_uint64), ("max_batch_samples", U32)]
+                ("seed", ctypes.c_uint64), ("max_batch_samples", U32), ("row_begin", U32), ("row_count", U32)]
 
 
 class RenderStats(ctypes.Structure):
@@ -123,7 +123,8 @@ class PathParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
                 ("seed", ctypes.c_uint64), ("max_depth", U32), ("rr_depth", U32), ("max_batch_samples", U32),
                 ("flags", U32), ("fb64", P), ("guide_fraction", ctypes.c_float), ("train_steps", U32),
-                ("train_batch", U32), ("train_lr", ctypes.c_float), ("guide_depth", U32)]
+                ("train_batch", U32), ("train_lr", ctypes.c_float), ("guide_depth", U32), ("row_begin", U32),
+                ("row_count", U32)]
 
 
 class PathStats(ctypes.Structure):
@@ -202,6 +203,9 @@ SIGNATURES = {
     "vmr_set_camera_keys": (ctypes.c_int, [P, P, U32]),
     "vmr_transform_keys_at": (ctypes.c_int, [P, U32, ctypes.c_float, ctypes.c_int, P]),
     "vmr_get_camera_keys": (ctypes.c_int, [P, P, U32, ctypes.POINTER(U32)]),
+    "vmr_render_split": (ctypes.c_int, [P, U32, ctypes.POINTER(RenderParams), P, ctypes.POINTER(RenderStats)]),
+    "vmr_render_path_split": (ctypes.c_int, [P, U32, ctypes.POINTER(PathParams), P, ctypes.POINTER(PathStats)]),
+    "vmr_split_rows": (ctypes.c_int, [U32, U32, P, P]),
     "vmr_selftest_wait": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float)]),
     "vmr_get_path_batch": (ctypes.c_int, [P, ctypes.POINTER(U32)]),
     "vmr_autotune_path": (ctypes.c_int, [P, ctypes.POINTER(PathParams), P, P, ctypes.POINTER(U32),

@@ -68,6 +68,52 @@ def transform_keys_at(keys, time: float, blend_one: bool = False):
     return out
 
 
+def split_rows(height: int, n: int):
+    """The row bands libvmr's split renders use (vmr_split_rows): a list of
+    (row_begin, row_count), one per device."""
+    L = _lib.load()
+    b = np.zeros(n, np.uint32)
+    c = np.zeros(n, np.uint32)
+    rc = L.vmr_split_rows(height, n, _p(b), _p(c))
+    if rc != 0:
+        raise VmrError(rc, "bad split")
+    return [(int(x), int(y)) for x, y in zip(b, c)]
+
+
+def render_split(ctxs, width: int, height: int, iter_begin: int, iter_count: int, seed: int, fb=None,
+                 max_batch_samples: int = 0):
+    """vmr_render_split: one reference-mode image over several contexts (one
+    per GPU, each holding the same scene); returns (fb, stats)."""
+    L = _lib.load()
+    if fb is None:
+        fb = np.zeros((height, width, 3), np.float32)
+    fb = np.ascontiguousarray(fb, np.float32)
+    arr = (ctypes.c_void_p * len(ctxs))(*[c.h for c in ctxs])
+    p = _lib.RenderParams(width, height, iter_begin, iter_count, seed, max_batch_samples, 0, 0)
+    st = _lib.RenderStats()
+    rc = L.vmr_render_split(arr, len(ctxs), ctypes.byref(p), _p(fb), ctypes.byref(st))
+    if rc != 0:
+        raise VmrError(rc, " / ".join(L.vmr_last_error(c.h).decode() for c in ctxs))
+    return fb, dict(samples=st.samples, camera_rays=st.camera_rays, shadow_rays=st.shadow_rays, ms=st.ms)
+
+
+def render_path_split(ctxs, width: int, height: int, iter_begin: int, iter_count: int, seed: int, fb=None,
+                      fb64=None, **kw):
+    """vmr_render_path_split: one path-traced image over several contexts;
+    keyword arguments as Context.render_path (train excluded)."""
+    L = _lib.load()
+    if fb is None:
+        fb = np.zeros((height, width, 3), np.float32)
+    fb = np.ascontiguousarray(fb, np.float32)
+    p = Context._path_params(width, height, iter_begin, iter_count, seed, fb64=fb64, **kw)
+    arr = (ctypes.c_void_p * len(ctxs))(*[c.h for c in ctxs])
+    st = _lib.PathStats()
+    rc = L.vmr_render_path_split(arr, len(ctxs), ctypes.byref(p), _p(fb), ctypes.byref(st))
+    if rc != 0:
+        raise VmrError(rc, " / ".join(L.vmr_last_error(c.h).decode() for c in ctxs))
+    return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays, ms=st.ms)
+
+
 def write_float(path: str, fb):
     """The OutputFloat driver (builtin/driver/outputfloat.go): the float32
     framebuffer [h, w, 3] as raw little-endian floats."""
@@ -355,28 +401,40 @@ class Context:
     def render_path(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, max_depth: int = 4,
                     rr_depth: int = 3, fb=None, fb64=None, max_batch_samples: int = 0, graph: bool = True,
                     guided: bool = False, train: bool = False, guide_fraction: float = 0.0, train_steps: int = 0,
-                    train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False, guide_depth: int = 0):
+                    train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False, guide_depth: int = 0,
+                    rows=None):
         """The extended path tracer: iterations [iter_begin, iter_begin +
         iter_count) folded into fb (float32 [height, width, 3]) and, when
         given, fb64 (float64).  guided: sample the guide network too; train:
         train it online; guide_depth: guide only the first vertices of each
-        path (0: all); sort_queues: trace each queue in ray-key order.
-        Returns (fb, stats)."""
+        path (0: all); sort_queues: trace each queue in ray-key order;
+        rows: (row_begin, row_count), a band of the image (fb then holds
+        row_count rows).  Returns (fb, stats)."""
+        r0, nr = rows if rows is not None else (0, 0)
+        hb = nr if rows is not None else height
         if fb is None:
-            fb = np.zeros((height, width, 3), np.float32)
+            fb = np.zeros((hb, width, 3), np.float32)
         fb = np.ascontiguousarray(fb, np.float32)
         if fb64 is not None:
-            assert fb64.dtype == np.float64 and fb64.flags.c_contiguous and fb64.shape == (height, width, 3)
-        flags = (0 if graph else _lib.PATH_NO_GRAPH) | (_lib.PATH_GUIDED if guided else 0) | \
-                (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0)
-        p = _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
-                            flags, None if fb64 is None else _p(fb64), guide_fraction, train_steps, train_batch,
-                            train_lr, guide_depth)
+            assert fb64.dtype == np.float64 and fb64.flags.c_contiguous and fb64.shape == (hb, width, 3)
+        p = self._path_params(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, fb64,
+                              max_batch_samples, graph, guided, train, guide_fraction, train_steps, train_batch,
+                              train_lr, sort_queues, guide_depth, r0, nr)
         st = _lib.PathStats()
         self._check(self.L.vmr_render_path(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,
                         graph_replays=st.graph_replays, ms=st.ms, train_records=st.train_records,
                         train_steps=st.train_steps, train_loss=st.train_loss)
+
+    @staticmethod
+    def _path_params(width, height, iter_begin, iter_count, seed, max_depth=4, rr_depth=3, fb64=None,
+                     max_batch_samples=0, graph=True, guided=False, train=False, guide_fraction=0.0, train_steps=0,
+                     train_batch=0, train_lr=0.0, sort_queues=False, guide_depth=0, row_begin=0, row_count=0):
+        flags = (0 if graph else _lib.PATH_NO_GRAPH) | (_lib.PATH_GUIDED if guided else 0) | \
+                (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0)
+        return _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
+                               flags, None if fb64 is None else _p(fb64), guide_fraction, train_steps, train_batch,
+                               train_lr, guide_depth, row_begin, row_count)
 
     # ------------------------------------------------------------ guide ---
     def guide_init(self, seed: int = 0):
@@ -486,13 +544,16 @@ class Context:
                          graph_replays=st.graph_replays, ms=st.ms)
 
     def render(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, fb=None,
-               max_batch_samples: int = 0):
+               max_batch_samples: int = 0, rows=None):
         """core.Render iterations [iter_begin, iter_begin+iter_count) folded
-        into fb (float32 [height, width, 3]); returns (fb, stats)."""
+        into fb (float32 [height, width, 3]; with rows = (row_begin,
+        row_count) the band of those rows, [row_count, width, 3]); returns
+        (fb, stats)."""
+        r0, nr = rows if rows is not None else (0, 0)
         if fb is None:
-            fb = np.zeros((height, width, 3), np.float32)
+            fb = np.zeros((nr if rows is not None else height, width, 3), np.float32)
         fb = np.ascontiguousarray(fb, np.float32)
-        p = _lib.RenderParams(width, height, iter_begin, iter_count, seed, max_batch_samples)
+        p = _lib.RenderParams(width, height, iter_begin, iter_count, seed, max_batch_samples, r0, nr)
         st = _lib.RenderStats()
         self._check(self.L.vmr_render(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, camera_rays=st.camera_rays, shadow_rays=st.shadow_rays, ms=st.ms)

@@ -79,7 +79,8 @@ struct PtJob {
 };
 
 struct PtBatch {
-  uint32_t width, height, npix;
+  uint32_t width, height, npix;  // npix: the pixels of the rendered band
+  uint32_t pix0;                 // the band's first pixel in the image (one-scene renders)
   uint32_t nl;        // lights
   uint32_t max_depth, rr_depth;
   uint32_t has_env;
@@ -390,6 +391,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
       b.pgeom[s] = job.geom;
       camera_primary(job.cam, nullptr, 0, job.width, job.height, j, pix, b.seed, b.filt, P, D, time, lambda);
     } else {
+      pix += b.pix0;  // the image pixel: a band samples as the whole image does
       camera_primary(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D, time,
                      lambda);
     }
@@ -998,6 +1000,11 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     if (!ctx->render.has_camera) return pfail(ctx, VMR_ERR_INVALID, "no camera");
     if (p->width == 0 || p->height == 0 || p->width > 4096 || p->height > 4096)
       return pfail(ctx, VMR_ERR_INVALID, "image size must be in [1, 4096] (RasterXY uses m = 12)");
+    if (p->row_count && (p->row_begin >= p->height || p->row_count > p->height - p->row_begin))
+      return pfail(ctx, VMR_ERR_INVALID, "row band outside the image");
+    if (!p->row_count && p->row_begin) return pfail(ctx, VMR_ERR_INVALID, "row_begin without row_count");
+    if (p->row_count && (p->flags & VMR_PATH_TRAIN))
+      return pfail(ctx, VMR_ERR_UNSUPPORTED, "a row band does not train the guide (it would see its rows only)");
     used_geoms = ctx->top.host.geom_order;
   } else {
     if (n_jobs == 0) return VMR_OK;
@@ -1081,7 +1088,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   const std::vector<RMesh> rm = rmesh_table(ctx);
   cudaSetDevice(ctx->device);
   cudaStream_t st = ctx->stream;
-  const uint32_t npix = jobs ? (uint32_t)npix_jobs : p->width * p->height;
+  const uint32_t band = (!jobs && p->row_count) ? p->row_count : p->height;
+  const uint32_t npix = jobs ? (uint32_t)npix_jobs : p->width * band;
   // Default 8M paths per batch: every bounce's launches end in a tail of
   // long paths, which a larger batch amortises (sphere grid 1920x1080, 8 spp:
   // 80.7 ms at 2M, 66.5 ms at 8M); a one-scene render uses the context's
@@ -1176,6 +1184,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   b.width = p->width;
   b.height = p->height;
   b.npix = npix;
+  b.pix0 = (!jobs && p->row_count) ? p->row_begin * p->width : 0u;
   b.nl = nl;
   b.max_depth = p->max_depth;
   b.rr_depth = p->rr_depth;
@@ -1314,6 +1323,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     fold(&b.cam, sizeof(b.cam));
     fold(&b.cam_keys, sizeof(b.cam_keys));
     fold(&b.cam_nkeys, sizeof(b.cam_nkeys));
+    fold(&b.pix0, sizeof(b.pix0));
     fold(&b.filt, sizeof(b.filt));
     fold(b.env, sizeof(b.env));
     fold(&b.sel, sizeof(b.sel));

@@ -244,7 +244,8 @@ struct Level {
 };
 
 struct RenderBatch {
-  uint32_t width, height, npix;
+  uint32_t width, height, npix;  // npix: the pixels of the rendered band
+  uint32_t pix0;                 // the band's first pixel in the image
   uint32_t iter0;  // first core.Render loop iteration of the batch
   uint32_t n;      // samples in the batch
   uint32_t nl;     // lights
@@ -274,7 +275,7 @@ __device__ __forceinline__ float* ray_f(const Level& L, int k, uint64_t e) { ret
 __global__ void k_generate(RenderBatch b) {
   const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (s >= b.n) return;
-  const uint32_t pix = (uint32_t)(s % b.npix);
+  const uint32_t pix = b.pix0 + (uint32_t)(s % b.npix);    // the image pixel
   const uint32_t j = b.iter0 + (uint32_t)(s / b.npix) + 1;  // render(iter+1)
   V3 P, D;
   float time, lambda;
@@ -412,7 +413,7 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
     sc.Rd = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
     sc.lambda = b.lambda[s];
     sc.time = *ray_f(lv, 7, e);
-    const uint32_t pix = (uint32_t)(s % b.npix);
+    const uint32_t pix = b.pix0 + (uint32_t)(s % b.npix);
     sc.I = b.iter0 + (uint64_t)(s / b.npix) + 1;
     sc.scr0 = scramble(b.seed, pix, 4);
     sc.scr1 = scramble(b.seed, pix, 5);
@@ -821,6 +822,10 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   if (!ctx->render.has_camera) return rfail(ctx, VMR_ERR_INVALID, "no camera");
   if (p->width == 0 || p->height == 0 || p->width > 4096 || p->height > 4096)
     return rfail(ctx, VMR_ERR_INVALID, "image size must be in [1, 4096] (RasterXY uses m = 12)");
+  if (p->row_count && (p->row_begin >= p->height || p->row_count > p->height - p->row_begin))
+    return rfail(ctx, VMR_ERR_INVALID, "row band outside the image");
+  if (!p->row_count && p->row_begin) return rfail(ctx, VMR_ERR_INVALID, "row_begin without row_count");
+  const uint32_t row0 = p->row_count ? p->row_begin : 0u, nrows = p->row_count ? p->row_count : p->height;
   auto& R = ctx->render;
   for (const auto& L : R.lights)
     if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
@@ -901,7 +906,7 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     ns = std::max<uint32_t>(ns, 1u << d.samples);
   }
   const uint32_t nl = (uint32_t)rl.size();
-  const uint32_t npix = p->width * p->height;
+  const uint32_t npix = p->width * nrows;
   uint32_t per_batch = p->max_batch_samples ? p->max_batch_samples : (4u << 20);
   uint32_t iters_per_batch = std::max<uint32_t>(1, per_batch / npix);
   if (iters_per_batch > p->iter_count) iters_per_batch = std::max<uint32_t>(1, p->iter_count);
@@ -954,6 +959,7 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   b.width = p->width;
   b.height = p->height;
   b.npix = npix;
+  b.pix0 = row0 * p->width;
   b.nl = nl;
   b.levels = levels;
   b.seed = p->seed;
