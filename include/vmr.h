@@ -401,7 +401,16 @@ typedef struct {
      * samples are the full render's, so the bands of a split render put
      * together are the one-call image bit for bit.  row_count 0: all rows. */
     uint32_t row_begin, row_count;
+    uint32_t flags;                   /* VMR_RENDER_* */
 } vmr_render_params;
+enum {
+    /* The shading's transcendentals (light and BSDF sampling, Oren-Nayar,
+     * the spherical-triangle sampling) in float32 instead of the reference's
+     * float64-rounded-to-float32 (math/sincos.go): off the FP64 pipe, no
+     * longer bit-exact with the oracle; the image stays within the stated
+     * tolerance of the float64 one. */
+    VMR_RENDER_F32 = 1
+};
 
 typedef struct {
     uint64_t samples;      /* pixel samples rendered */

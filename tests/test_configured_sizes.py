@@ -80,3 +80,20 @@ def test_batched_jobs_as_configured_match_oracle(ctx, orc):
                 assert np.array_equal(got["prim"] >= 0, ref["prim"] >= 0), f"job {j} any hit"
             else:
                 assert_hits_equal(got, ref, what=f"job {j} ({'motion' if motion else 'static'}, {len(ip) // 3} tris)")
+
+
+def test_small_room_float32_shading_within_tolerance(ctx):
+    """VMR_RENDER_F32 (float32 transcendentals in the reference-mode shading)
+    against the float64 image of the configured small room: mean relative
+    pixel error <= 1e-3 (the benchmark spec's), 99th percentile <= 1e-3; the
+    figures and the device times are printed."""
+    room = scenes.small_room(16384, seed=1, res=256)
+    ctx.load_scene(room)
+    ref, s64 = ctx.render(256, 256, 0, 16, 1)
+    got, s32 = ctx.render(256, 256, 0, 16, 1, f32=True)
+    assert not np.isnan(got).any()
+    rel = _pixel_rel(got, ref)
+    p99 = np.percentile(rel, 99)
+    print(f"float32 shading: mean relative pixel error {rel.mean():.3e}, 99th percentile {p99:.2e}, "
+          f"max {rel.max():.3f}; device ms float64 {s64['ms']:.2f}, float32 {s32['ms']:.2f}")
+    assert rel.mean() <= MEAN_REL and p99 <= 1e-3

@@ -192,9 +192,11 @@ def test_render_with_groups_keys_and_debug_shader_matches_oracle(ctx, orc, camer
     frac, mean_abs = _compare(got, ref)
     assert frac >= 0.999, (frac, mean_abs)
     assert mean_abs <= 1e-6, (frac, mean_abs)
-    # the DebugShader's colour shows up unlit
-    dbg = np.float32([0.9, 0.2, 0.6])
-    assert (np.abs(got - dbg).max(-1) < 1e-6).any() or camera_keys
+    # the DebugShader's colour shows up unlit on the back wall, folded as
+    # core.Render folds a constant c: buf = (buf*j + c)/(j+1) from j = 1 on
+    # a zero buffer gives c*N/(N+1) after N iterations (core/render.go:127-129)
+    dbg = np.float32([0.9, 0.2, 0.6]) * np.float32(ITERS) / np.float32(ITERS + 1)
+    assert (np.abs(got - dbg).max(-1) < 1e-6).mean() > 0.05
 
 
 @pytest.mark.gpu

@@ -106,7 +106,8 @@ VNF_MOTION_FIXED = 1
 
 class RenderParams(ctypes.Structure):
     _fields_ = [("width", U32), ("height", U32), ("iter_begin", U32), ("iter_count", U32),
-                ("seed", ctypes.c_uint64), ("max_batch_samples", U32), ("row_begin", U32), ("row_count", U32)]
+                ("seed", ctypes.c_uint64), ("max_batch_samples", U32), ("row_begin", U32), ("row_count", U32),
+                ("flags", U32)]
 
 
 class RenderStats(ctypes.Structure):
@@ -151,6 +152,7 @@ class Adam(ctypes.Structure):
 SHADER_FLAGS = {"emission_colour": 1, "emission_strength": 2, "diffuse_colour": 4, "diffuse_strength": 8,
                 "diffuse_roughness": 16, "spec1_colour": 32, "spec1_strength": 64, "spec1_roughness": 128,
                 "spec1_fresnel_refl": 256, "spec1_fresnel_edge": 512, "ior": 1024}
+RENDER_F32 = 1  # vmr_render_params.flags
 SH_DEBUG = 2048  # DebugShader: a shader dict with "debug": True and diffuse_colour = Colour
 
 assert ctypes.sizeof(QbvhNode) == 128 and ctypes.sizeof(MqbvhNode) == 40

@@ -544,16 +544,18 @@ class Context:
                          graph_replays=st.graph_replays, ms=st.ms)
 
     def render(self, width: int, height: int, iter_begin: int, iter_count: int, seed: int, fb=None,
-               max_batch_samples: int = 0, rows=None):
+               max_batch_samples: int = 0, rows=None, f32: bool = False):
         """core.Render iterations [iter_begin, iter_begin+iter_count) folded
         into fb (float32 [height, width, 3]; with rows = (row_begin,
-        row_count) the band of those rows, [row_count, width, 3]); returns
-        (fb, stats)."""
+        row_count) the band of those rows, [row_count, width, 3]); f32: the
+        float32-transcendental shading (VMR_RENDER_F32).  Returns (fb,
+        stats)."""
         r0, nr = rows if rows is not None else (0, 0)
         if fb is None:
             fb = np.zeros((nr if rows is not None else height, width, 3), np.float32)
         fb = np.ascontiguousarray(fb, np.float32)
-        p = _lib.RenderParams(width, height, iter_begin, iter_count, seed, max_batch_samples, r0, nr)
+        p = _lib.RenderParams(width, height, iter_begin, iter_count, seed, max_batch_samples, r0, nr,
+                              _lib.RENDER_F32 if f32 else 0)
         st = _lib.RenderStats()
         self._check(self.L.vmr_render(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, camera_rays=st.camera_rays, shadow_rays=st.shadow_rays, ms=st.ms)

@@ -45,12 +45,15 @@ struct Cand {
 };
 
 // Disk.SampleArea, sample i of n (builtin/light/disk.go:154-204).
+// F32 (in this and the functions below): the VMR_RENDER_F32 precision switch
+// of the transcendentals (shade_common.cuh msin etc.).
+template <bool F32>
 __device__ Cand disk_sample(const RLight& L, const Ctx& sc, int n, int i) {
   Cand c{};
   const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;
   const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
-  const float u = L.radius * sqrtf((float)r0) * gcos(2 * kPi * (float)r1);
-  const float v = L.radius * sqrtf((float)r0) * gsin(2 * kPi * (float)r1);
+  const float u = L.radius * sqrtf((float)r0) * mcos<F32>(2 * kPi * (float)r1);
+  const float v = L.radius * sqrtf((float)r0) * msin<F32>(2 * kPi * (float)r1);
   const double pdf = (double)(1.0f / (kPi * L.radius * L.radius));
   const V3 LP = v3(L.P[0], L.P[1], L.P[2]), LT = v3(L.T[0], L.T[1], L.T[2]), LB = v3(L.B[0], L.B[1], L.B[2]),
            LN = v3(L.N[0], L.N[1], L.N[2]);
@@ -92,6 +95,7 @@ __device__ bool light_sphere_hit(V3 Ro, V3 Rd, V3 C, float radius, float& t) {
 }
 
 // Sphere.SampleArea, sample i of n (builtin/light/sphere.go:178-254).
+template <bool F32>
 __device__ Cand sphere_sample(const RLight& L, const Ctx& sc, int n, int i) {
   Cand c{};
   const V3 C = v3(L.P[0], L.P[1], L.P[2]);
@@ -102,9 +106,9 @@ __device__ Cand sphere_sample(const RLight& L, const Ctx& sc, int n, int i) {
   const V3 u = cross(w, v);
   const uint64_t idx = sc.I * (uint64_t)n + (uint64_t)i;
   const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
-  const float theta = gacos(1 - (float)r0 + (float)r0 * sqrtf(1 - sqr(L.radius / l)));
+  const float theta = macos<F32>(1 - (float)r0 + (float)r0 * sqrtf(1 - sqr(L.radius / l)));
   const float phi = 2 * kPi * (float)r1;
-  const V3 a = v3(gcos(phi) * gsin(theta), gsin(phi) * gsin(theta), gcos(theta));
+  const V3 a = v3(mcos<F32>(phi) * msin<F32>(theta), msin<F32>(phi) * msin<F32>(theta), mcos<F32>(theta));
   const V3 omega = expand(u, v, w, a);
   if (dot(omega, sc.Ng) < 0) return c;
   float t;
@@ -119,9 +123,10 @@ __device__ Cand sphere_sample(const RLight& L, const Ctx& sc, int n, int i) {
 }
 
 // Tri.SampleArea, sample i of n (triangle.go:232-343).
+template <bool F32>
 __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
-  if (L.kind == 1) return disk_sample(L, sc, n, i);
-  if (L.kind == 2) return sphere_sample(L, sc, n, i);
+  if (L.kind == 1) return disk_sample<F32>(L, sc, n, i);
+  if (L.kind == 2) return sphere_sample<F32>(L, sc, n, i);
   Cand c{};
   const V3 p0 = lp(L, 0), p1 = lp(L, 1), p2 = lp(L, 2);
   const V3 N = normalize(cross(sub(p1, p0), sub(p2, p0)));
@@ -130,7 +135,8 @@ __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
   const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
   if (area_only) {
     const double pdf = (double)(1 / tri_area(p0, p1, p2));
-    const float a = (float)(r1 * sqrt(1 - r0)), b = (float)(1 - sqrt(1 - r0));
+    const float a = F32 ? (float)r1 * sqrtf(1.0f - (float)r0) : (float)(r1 * sqrt(1 - r0));
+    const float b = F32 ? 1.0f - sqrtf(1.0f - (float)r0) : (float)(1 - sqrt(1 - r0));
     const V3 P = add(add(p0, scale(a, sub(p1, p0))), scale(b, sub(p2, p0)));
     const V3 D = sub(P, sc.P);
     c.Ldist = length(D);
@@ -139,7 +145,7 @@ __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
     c.pdf_own = (float)pdf * sqr(c.Ldist) / fabsf(dot(c.Ld, N));
   } else {
     double pdf;
-    const V3 x = sample_spherical(p0, p1, p2, sc.P, r0, r1, pdf);
+    const V3 x = sample_spherical<F32>(p0, p1, p2, sc.P, r0, r1, pdf);
     float t;
     ray_plane(sc.P, x, p0, N, t);
     const V3 P = add(sc.P, scale(t, x));
@@ -155,12 +161,13 @@ __device__ Cand light_sample(const RLight& L, const Ctx& sc, int n, int i) {
 
 // BSDF sample i then Tri.ValidSample / Disk.ValidSample (core/shader.go:211-228,
 // triangle.go:136-230, disk.go:119-151).
+template <bool F32>
 __device__ Cand bsdf_candidate(const RLight& L, const Ctx& sc, const Bsdf& bsdf, int half, int i) {
   Cand c{};
   const uint64_t idx = sc.I * (uint64_t)half + (uint64_t)i;
   const double r0 = vdc(idx, sc.scr0), r1 = sobol(idx, sc.scr1);
-  const V3 D = normalize(bsdf_sample(bsdf, r0, r1));
-  c.pdf_bsdf = bsdf_pdf(bsdf, D);
+  const V3 D = normalize(bsdf_sample<F32>(bsdf, r0, r1));
+  c.pdf_bsdf = bsdf_pdf<F32>(bsdf, D);
   if (c.pdf_bsdf <= 0) return c;
   if (L.kind == 2) {  // Sphere.ValidSample (sphere.go:126-176)
     const V3 C = v3(L.P[0], L.P[1], L.P[2]);
@@ -205,9 +212,9 @@ __device__ Cand bsdf_candidate(const RLight& L, const Ctx& sc, const Bsdf& bsdf,
     c.pdf_light = (float)pdf * sqr(c.Ldist) / fabsf(dot(c.Ld, N));
   } else {
     const V3 pa = normalize(sub(p0, sc.P)), pb = normalize(sub(p1, sc.P)), pc = normalize(sub(p2, sc.P));
-    const float a = gacos(dot(pb, pc)), b = gacos(dot(pc, pa)), cc = gacos(dot(pa, pb));
+    const float a = macos<F32>(dot(pb, pc)), b = macos<F32>(dot(pc, pa)), cc = macos<F32>(dot(pa, pb));
     float al, be, ga;
-    sides_to_angles(a, b, cc, al, be, ga);
+    sides_to_angles<F32>(a, b, cc, al, be, ga);
     const float area = al + be + ga - kPi;
     c.pdf_light = (float)(1 / (double)area);
   }
@@ -317,6 +324,7 @@ __device__ void emit_shadow(const RenderBatch& b, const Level& lv, const Ctx& sc
 // EvaluateLightSamples (core/shader.go:203-402) for one (lobe, light):
 // writes the slot contributions, queues their shadow rays and returns the
 // scale the accumulate pass applies.
+template <bool F32>
 __device__ float light_lobe(const RenderBatch& b, const Level& lv, const Ctx& sc, const RLight& L, const Bsdf& bsdf,
                             int NS, uint32_t slot0) {
   const int half = NS > 1 ? NS / 2 : 0;
@@ -324,11 +332,11 @@ __device__ float light_lobe(const RenderBatch& b, const Level& lv, const Ctx& sc
   Cand cl[kMaxHalf], cb[kMaxHalf];
   int n_light = 0, n_bsdf = 0;
   for (int i = 0; i < nls; ++i) {
-    cl[i] = light_sample(L, sc, nls, i);
+    cl[i] = light_sample<F32>(L, sc, nls, i);
     n_light += cl[i].ok ? 1 : 0;
   }
   for (int i = 0; i < half; ++i) {
-    cb[i] = bsdf_candidate(L, sc, bsdf, half, i);
+    cb[i] = bsdf_candidate<F32>(L, sc, bsdf, half, i);
     n_bsdf += cb[i].ok ? 1 : 0;
   }
   const int nB = n_bsdf == 0 ? 0 : half;
@@ -345,13 +353,13 @@ __device__ float light_lobe(const RenderBatch& b, const Level& lv, const Ctx& sc
       float* out = lv.slot_rgb + (size_t)slot * 3;
       out[0] = out[1] = out[2] = 0.0f;
       if (want) {
-        Spec rho = bsdf_eval(bsdf, c.Ld);
+        Spec rho = bsdf_eval<F32>(bsdf, c.Ld);
         for (int k = 0; k < 4; ++k) rho.c[k] *= Liu.c[k];
         float inv;
         if (mis) {
           float p_hat;
           if (pass == 0) {
-            p_hat = (float)nB * (float)bsdf_pdf(bsdf, c.Ld) / (float)total;
+            p_hat = (float)nB * (float)bsdf_pdf<F32>(bsdf, c.Ld) / (float)total;
             p_hat += (float)nL * c.pdf_own / (float)total;
           } else {
             p_hat = (float)nB * (float)c.pdf_bsdf / (float)total;
@@ -383,6 +391,7 @@ __device__ float light_lobe(const RenderBatch& b, const Level& lv, const Ctx& sc
 // level: emission, the diffuse and glossy lobes' light samples, and the
 // mirror (Spec1Roughness 0) reflection queued for the next level with the
 // sample's I and scrambles (a child ShaderContext copies them).
+template <bool F32>
 __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
   const Level& lv = b.lv[level];
   const uint64_t n = level == 0 ? (uint64_t)b.n : (*lv.count < lv.cap ? *lv.count : lv.cap);
@@ -452,7 +461,7 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
         if ((int32_t)L.geom == geom) continue;  // LightsPrepare (scene.go:100-116)
         const int NS = level > 0 ? 1 : 1 << L.samples;  // level > 0: one sample (shader.go:189-191)
         const uint32_t slot0 = (uint32_t)((e * 2 + 0) * b.nl + l) * lv.ns;
-        lv.lscale[(e * 2 + 0) * b.nl + l] = light_lobe(b, lv, sc, L, diff, NS, slot0);
+        lv.lscale[(e * 2 + 0) * b.nl + l] = light_lobe<F32>(b, lv, sc, L, diff, NS, slot0);
       }
     }
     if (sw > 0.0f) {
@@ -472,19 +481,19 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
           if ((int32_t)L.geom == geom) continue;
           const int NS = level > 0 ? 1 : 1 << L.samples;
           const uint32_t slot0 = (uint32_t)((e * 2 + 1) * b.nl + l) * lv.ns;
-          lv.lscale[(e * 2 + 1) * b.nl + l] = light_lobe(b, lv, sc, L, spec, NS, slot0);
+          lv.lscale[(e * 2 + 1) * b.nl + l] = light_lobe<F32>(b, lv, sc, L, spec, NS, slot0);
         }
       } else {
         // the mirror: one sample at idx = I (std.go:216-259)
         const Bsdf spec{2, sc.lambda, project(Ut, Vt, sc.N, wi), rough * rough, fr, Ut, Vt, sc.N};
         const double r0 = vdc(sc.I, sc.scr0), r1 = sobol(sc.I, sc.scr1);
-        const V3 wo = bsdf_sample(spec, r0, r1);
-        const double pdf = bsdf_pdf(spec, wo);
+        const V3 wo = bsdf_sample<F32>(spec, r0, r1);
+        const double pdf = bsdf_pdf<F32>(spec, wo);
         float* w = lv.mw + e * 4;
         w[0] = w[1] = w[2] = 0.0f;
         w[3] = sw;
         if (dot(wo, sc.Ng) > 0.0f) {
-          Spec rho = bsdf_eval(spec, wo);
+          Spec rho = bsdf_eval<F32>(spec, wo);
           const float inv = 1.0f / (float)pdf;
           for (int k = 0; k < 4; ++k) rho.c[k] *= inv;
           const RGB col = to_rgb(rho, sc.lambda);
@@ -826,6 +835,8 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     return rfail(ctx, VMR_ERR_INVALID, "row band outside the image");
   if (!p->row_count && p->row_begin) return rfail(ctx, VMR_ERR_INVALID, "row_begin without row_count");
   const uint32_t row0 = p->row_count ? p->row_begin : 0u, nrows = p->row_count ? p->row_count : p->height;
+  if (p->flags & ~(uint32_t)VMR_RENDER_F32) return rfail(ctx, VMR_ERR_INVALID, "unknown render flags");
+  const bool f32 = (p->flags & VMR_RENDER_F32) != 0;
   auto& R = ctx->render;
   for (const auto& L : R.lights)
     if (L.shader >= R.shaders.size() || L.geom >= ctx->meshes.size())
@@ -1028,7 +1039,8 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
       int rc = vmr_trace_scene(ctx, &rr, ne, VMR_TRACE_DEVICE, &hh, nullptr);
       if (rc != VMR_OK) return rc;
       RCUDA(cudaMemsetAsync(b.queue_len, 0, 8, st));
-      k_shade<<<(int)((ne + blk - 1) / blk), blk, 0, st>>>(b, l);
+      if (f32) k_shade<true><<<(int)((ne + blk - 1) / blk), blk, 0, st>>>(b, l);
+      else k_shade<false><<<(int)((ne + blk - 1) / blk), blk, 0, st>>>(b, l);
       RCUDA(cudaGetLastError());
       unsigned long long nq = 0;
       RCUDA(cudaMemcpyAsync(&nq, b.queue_len, 8, cudaMemcpyDeviceToHost, st));

@@ -52,6 +52,18 @@ __device__ __forceinline__ float gatan2(float y, float x) { return (float)atan2(
 __device__ __forceinline__ float gacos(float x) {
   return (float)acos((double)(x > 1.0f ? 1.0f : (x < -1.0f ? -1.0f : x)));
 }
+// The same functions under the reference-mode precision switch: F32 false
+// is the float64 evaluation above (the reference's math/sincos.go, bit for
+// bit with the oracle); F32 true is CUDA's float32 functions (within 2 ulp),
+// the VMR_RENDER_F32 option, which keeps the shading off the FP64 pipe.
+template <bool F32> __device__ __forceinline__ float msin(float x) { return F32 ? sinf(x) : gsin(x); }
+template <bool F32> __device__ __forceinline__ float mcos(float x) { return F32 ? cosf(x) : gcos(x); }
+template <bool F32> __device__ __forceinline__ float mtan(float x) { return F32 ? tanf(x) : gtan(x); }
+template <bool F32> __device__ __forceinline__ float matan(float x) { return F32 ? atanf(x) : gatan(x); }
+template <bool F32> __device__ __forceinline__ float matan2(float y, float x) { return F32 ? atan2f(y, x) : gatan2(y, x); }
+template <bool F32> __device__ __forceinline__ float macos(float x) {
+  return F32 ? acosf(x > 1.0f ? 1.0f : (x < -1.0f ? -1.0f : x)) : gacos(x);
+}
 __device__ __forceinline__ V3 project(V3 U, V3 V, V3 W, V3 s) { return v3(dot(U, s), dot(V, s), dot(W, s)); }
 __device__ __forceinline__ V3 expand(V3 U, V3 V, V3 W, V3 s) {
   return v3(U.x * s.x + V.x * s.y + W.x * s.z, U.y * s.x + V.y * s.y + W.y * s.z, U.z * s.x + V.z * s.y + W.z * s.z);
@@ -224,19 +236,31 @@ __device__ __forceinline__ V3 reflect_z(V3 w) {
   const float d = 0.0f * w.x + 0.0f * w.y + 1.0f * w.z;
   return sub(scale(2.0f * d, v3(0, 0, 1)), w);
 }
+template <bool F32 = false>
 __device__ V3 bsdf_sample(const Bsdf& b, double r0, double r1) {
   if (b.kind == 2) return expand(b.U, b.V, b.N, normalize(reflect_z(b.wi)));  // Specular.Sample
   if (b.kind == 0) {  // CosineHemisphere (math/sample/sample.go:18-27)
+    if (F32) {
+      const float r = sqrtf(1.0f - (float)r0), th = 2.0f * kPi * (float)r1;
+      return expand(b.U, b.V, b.N, v3(r * cosf(th), r * sinf(th), sqrtf((float)r0)));
+    }
     const double r = sqrt(1 - r0), th = 2 * 3.14159265358979323846 * r1;
     return expand(b.U, b.V, b.N, v3((float)(r * cos(th)), (float)(r * sin(th)), (float)sqrt(r0)));
   }
   const float alpha = sqr(b.rough);  // MicrofacetGGX.Sample
-  const double thetaM = atan2((double)alpha * sqrt(r0), sqrt(1 - r0));
-  const double phiM = 2.0 * 3.14159265358979323846 * r1;
-  const V3 m = v3(gsin((float)thetaM) * gcos((float)phiM), gsin((float)thetaM) * gsin((float)phiM), gcos((float)thetaM));
+  float thetaM, phiM;
+  if (F32) {
+    thetaM = atan2f(alpha * sqrtf((float)r0), sqrtf(1.0f - (float)r0));
+    phiM = 2.0f * kPi * (float)r1;
+  } else {
+    thetaM = (float)atan2((double)alpha * sqrt(r0), sqrt(1 - r0));
+    phiM = (float)(2.0 * 3.14159265358979323846 * r1);
+  }
+  const V3 m = v3(msin<F32>(thetaM) * mcos<F32>(phiM), msin<F32>(thetaM) * msin<F32>(phiM), mcos<F32>(thetaM));
   const V3 wo = sub(scale(2.0f * fabsf(dot(m, b.wi)), m), b.wi);
   return expand(b.U, b.V, b.N, normalize(wo));
 }
+template <bool F32 = false>
 __device__ double bsdf_pdf(const Bsdf& b, V3 wo_world) {
   const V3 wo = project(b.U, b.V, b.N, wo_world);
   if (b.kind == 2) return dot(wo, reflect_z(b.wi)) < 0.9999f ? 0.0 : 1.0;  // Specular.PDF
@@ -246,6 +270,7 @@ __device__ double bsdf_pdf(const Bsdf& b, V3 wo_world) {
   const double pdf = (double)(ggx_d(m, alpha) * m.z);
   return isnan(pdf) ? 0.0 : pdf;
 }
+template <bool F32 = false>
 __device__ Spec bsdf_eval(const Bsdf& b, V3 wo_world) {
   const V3 wo = project(b.U, b.V, b.N, wo_world);
   if (b.kind == 2) {  // Specular.Eval (bsdf/specular.go:77-101)
@@ -261,11 +286,11 @@ __device__ Spec bsdf_eval(const Bsdf& b, V3 wo_world) {
     const float sigma = b.rough;
     const float A = 1 - (0.5f * (sigma * sigma) / ((sigma * sigma) + 0.57f));
     const float B = 0.45f * (sigma * sigma) / ((sigma * sigma) + 0.09f);
-    const float phiI = gatan2(b.wi.y, b.wi.x), phiO = gatan2(wo.y, wo.x);
-    const float thetaI = gacos(b.wi.z), thetaO = gacos(wo.z);
+    const float phiI = matan2<F32>(b.wi.y, b.wi.x), phiO = matan2<F32>(wo.y, wo.x);
+    const float thetaI = macos<F32>(b.wi.z), thetaO = macos<F32>(wo.z);
     const float alpha = gmax(thetaI, thetaO), beta = gmin(thetaI, thetaO);
-    const float C = gsin(alpha) * gtan(beta);
-    const float gamma = gcos(phiO - phiI);
+    const float C = msin<F32>(alpha) * mtan<F32>(beta);
+    const float gamma = mcos<F32>(phiO - phiI);
     const float s = wo.z * (A + (B * gmax(0.0f, gamma) * C));
     Spec rho = from_rgb(RGB{{1, 1, 1}}, b.lambda);
 #pragma unroll
@@ -365,25 +390,27 @@ __device__ V3 offset_p(const Ctx& sc, int dir) {  // OffsetP (core/shader.go:139
 
 __device__ __forceinline__ V3 lp(const RLight& L, int k) { return v3(L.p[3 * k], L.p[3 * k + 1], L.p[3 * k + 2]); }
 __device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) { return 0.5f * length(cross(sub(p1, p0), sub(p2, p0))); }
+template <bool F32 = false>
 __device__ void sides_to_angles(float as, float bs, float cs, float& a, float& b, float& c) {
   const float ssu = (as + bs + cs) / 2;
-  const float sa = gsin(ssu - as), sb = gsin(ssu - bs), sc2 = gsin(ssu - cs), s = gsin(ssu);
-  a = 2 * gatan(sqrtf(sb * sc2 / (s * sa)));
-  b = 2 * gatan(sqrtf(sa * sc2 / (s * sb)));
-  c = 2 * gatan(sqrtf(sa * sb / (s * sc2)));
+  const float sa = msin<F32>(ssu - as), sb = msin<F32>(ssu - bs), sc2 = msin<F32>(ssu - cs), s = msin<F32>(ssu);
+  a = 2 * matan<F32>(sqrtf(sb * sc2 / (s * sa)));
+  b = 2 * matan<F32>(sqrtf(sa * sc2 / (s * sb)));
+  c = 2 * matan<F32>(sqrtf(sa * sb / (s * sc2)));
 }
 // sampleSphericalTriangle (triangle.go:474-535)
+template <bool F32 = false>
 __device__ V3 sample_spherical(V3 p0, V3 p1, V3 p2, V3 p, double r0, double r1, double& pdf) {
   const V3 pa = normalize(sub(p0, p)), pb = normalize(sub(p1, p)), pc = normalize(sub(p2, p));
-  const float a = gacos(dot(pb, pc)), b = gacos(dot(pc, pa)), c = gacos(dot(pa, pb));
+  const float a = macos<F32>(dot(pb, pc)), b = macos<F32>(dot(pc, pa)), c = macos<F32>(dot(pa, pb));
   float alpha, beta, gamma;
-  sides_to_angles(a, b, c, alpha, beta, gamma);
+  sides_to_angles<F32>(a, b, c, alpha, beta, gamma);
   const float area = alpha + beta + gamma - kPi;
   const float areaHat = (float)r0 * area;
-  const float s = gsin(areaHat - alpha), t = gcos(areaHat - alpha);
-  const float sinA = gsin(alpha), cosA = gcos(alpha);
+  const float s = msin<F32>(areaHat - alpha), t = mcos<F32>(areaHat - alpha);
+  const float sinA = msin<F32>(alpha), cosA = mcos<F32>(alpha);
   const float u = t - cosA;
-  const float v = s + sinA * gcos(c);
+  const float v = s + sinA * mcos<F32>(c);
   float q = ((v * t - u * s) * cosA - v) / ((v * s + u * t) * sinA);
   q = gmax(-1.0f, gmin(q, 1.0f));
   float w = dot(pc, pa);

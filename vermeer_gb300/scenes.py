@@ -561,7 +561,7 @@ def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = Tru
     keys moving and turning over the shutter), an instance of an analytic
     sphere, a Proc of two meshes (one with its own PolyMesh transform) under
     two transform keys, a mesh with two PolyMesh transform keys, a
-    DebugShader on the first instance's object, and (camera_keys) two
+    DebugShader on the instanced object and the back wall, and (camera_keys) two
     camera motion keys."""
     sc = small_room(n_tris, seed=seed)
     M = sc["meshes"]
@@ -604,6 +604,7 @@ def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = Tru
                   transform_keys=[xf_matrix(0.0, (1, 0, 0), (1, 1, 1), (-0.1, -0.3, -0.6)),
                                   xf_matrix(0.8, (1, 0, 0), (1.1, 1.1, 1.1), (0.05, -0.25, -0.55))]))
     obj["shaders"] = [debug, 6]
+    M[0]["shaders"] = [0, 1, debug, 3, 4]  # the back wall too
     if camera_keys:
         cam = sc["camera"]
         m0 = np.asarray(cam["m"], np.float32)
