@@ -122,6 +122,30 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_l2_gbs(dev):
+    """L2 bandwidth on this GPU: a device copy of a 24 MiB buffer into
+    another (48 MiB read + write, resident in the 126 MB L2 after the first
+    pass), timed with CUDA events over 64 copies, best of 5.  The traversal's
+    working set (nodes + triangles, about 57 MB) is L2-resident too, so its
+    algorithmic bytes are reported against this as well as against HBM."""
+    import torch
+    n = (24 << 20) // 4
+    a = torch.ones(n, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(8):
+        b.copy_(a)
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(64):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * 4 * n * 64 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return round(best, 1)
+
+
 def profiled_traffic():
     """DRAM bytes per launch of the traversal kernel from the committed ncu
     summary (profiles/traverse_soup1m_incoherent.md), or None."""
@@ -171,15 +195,19 @@ def make_workload():
 
 
 def cpu_baseline(v, ip, rays, threads, sample):
-    """The oracle port on the host cores over a bounded sample of the rays."""
+    """The oracle port on the host cores over a bounded sample of the rays;
+    returns (Mrays/s, seconds, the sample's closest hits)."""
     from oracle import orc
     m = orc.Mesh(v, ip)
     sub = rays[:sample]
     m.trace(sub[:4096], nthreads=threads)  # warm the caches / thread pool
     t0 = time.perf_counter()
-    m.trace(sub, nthreads=threads)
+    hits = m.trace(sub, nthreads=threads)
     dt = time.perf_counter() - t0
-    return sample / dt / 1e6, dt
+    return sample / dt / 1e6, dt, hits
+
+
+REF_WORKERS = 5  # core.Render's workers: min(Globals.MaxGoRoutines (default 5), 10) (core/render.go:190)
 
 
 def run_reference(args):
@@ -188,24 +216,30 @@ def run_reference(args):
         return 0
     v, ip, rays = make_workload()
     threads = cpu_threads()
-    sample = 1 << 18
     from oracle import orc
     m = orc.Mesh(v, ip)
-    for i in range(args.warmup):
-        m.trace(rays[i * sample % N_RAYS:][:sample], nthreads=threads)
+    m.trace(rays[:1 << 16], nthreads=threads)  # warm the caches / thread pool
+    for _ in range(args.warmup):
+        m.trace(rays[:1 << 18], nthreads=threads)
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        s = (i * sample) % N_RAYS
-        m.trace(rays[s:s + sample], nthreads=threads)
+    for _ in range(args.steps):
+        m.trace(rays, nthreads=threads)  # the whole configured step: all 4,194,304 rays
     dt = time.perf_counter() - t0
-    value = sample * args.steps / dt / 1e6
+    value = N_RAYS * args.steps / dt / 1e6
+    w_sample = 1 << 18
+    t0 = time.perf_counter()
+    m.trace(rays[:w_sample], nthreads=REF_WORKERS)
+    wval = w_sample / (time.perf_counter() - t0) / 1e6
     line = {"metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": dict(CONFIG, rays_per_step=sample), "impl": "reference",
+            "config": dict(CONFIG), "impl": "reference",
             "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": f"{sample} of the {N_RAYS} incoherent rays per step, {threads} threads; "
-                                       "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"},
+                             "sample": f"all {N_RAYS} incoherent rays per step, {threads} threads; C++ restatement "
+                                       "of qbvh.Trace + PolyMesh.TraceElems (oracle/)",
+                             "reference_workers": {"threads": REF_WORKERS, "value": round(wval, 4),
+                                                   "sample": f"{w_sample} rays, the reference's default worker "
+                                                             "count (core/render.go:190)"}},
             "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -289,11 +323,12 @@ def run_gpu(args):
 
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / avg_launch_s / 1e9
+    l2_gbs = measured_l2_gbs(dev)
     traffic = profiled_traffic()
     clocks = clk.summary()
-    e2e = None
+    e2e, e2e_hits = None, None
     if not args.no_e2e:
-        e2e = measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world)
+        e2e, e2e_hits = measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -305,15 +340,27 @@ def run_gpu(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes,
                          "node_visits_per_ray": round(cst.node_visits / N_RAYS, 3),
-                         "tri_tests_per_ray": round(cst.tri_tests / N_RAYS, 3)},
+                         "tri_tests_per_ray": round(cst.tri_tests / N_RAYS, 3),
+                         "l2": {"achieved": round(achieved, 1), "peak": l2_gbs, "unit": "GB/s",
+                                "frac": round(achieved / l2_gbs, 4),
+                                "peak_source": "measured in this run: device copy of a 24 MiB buffer (L2-resident), "
+                                               "best of 5 x 64 copies"}},
             "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
         threads = cpu_threads()
         sample = min(1 << 20, N_RAYS)
-        cval, cdt = cpu_baseline(v, ip, rays, threads, sample)
+        cval, cdt, chits = cpu_baseline(v, ip, rays, threads, sample)
+        wval, _, _ = cpu_baseline(v, ip, rays, REF_WORKERS, sample // 4)
         line["cpu_baseline"] = {"value": round(cval, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
                                 "sample": f"{sample} of the {N_RAYS} incoherent rays ({cdt:.1f} s), "
-                                          "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)"}
+                                          "C++ restatement of qbvh.Trace + PolyMesh.TraceElems (oracle/)",
+                                "reference_workers": {"threads": REF_WORKERS, "value": round(wval, 4),
+                                                      "sample": f"{sample // 4} rays, the reference's default "
+                                                                "worker count (core/render.go:190)"}}
+        if e2e is not None:  # the end-to-end hits against the oracle on the sample
+            ok = all(np.array_equal(np.asarray(chits[k]).view(np.uint32), np.asarray(e2e_hits[k][:sample]).view(np.uint32))
+                     for k in ("prim", "t", "u", "v", "w"))
+            e2e["hits_match_oracle_sample"] = bool(ok)
     if rank == 0 and not args.no_render:
         line["traversal_queries"] = traversal_queries(ctx, geom, d_rays, flush, stream, args)
         line["render"] = render_extras(ctx, args)
@@ -431,25 +478,37 @@ def render_extras(ctx, args):
         "host_threads": cpu_threads(), "identical": res["device"][1] == res["host"][1],
         "cpu_baseline": {"ms": round(odt * 1e3, 2), "cores": 1, "kind": "port",
                          "sample": "the whole build, oracle/orc_core.cpp (C++ restatement of qbvh.BuildAccel)"}}
-    # reference mode, small room
+    # reference mode, small room, as configured
     sc = scenes.small_room(16384, seed=1)
     ctx.load_scene(sc)
     ctx.render(256, 256, 0, 2, 7)
     fb, st = ctx.render(256, 256, 0, 16, 7)
+    ctx.render(256, 256, 0, 2, 7, f32=True)
+    fb32, st32 = ctx.render(256, 256, 0, 16, 7, f32=True)
+    rel32 = np.abs(fb32 - fb).sum(-1) / np.maximum(np.abs(fb).sum(-1), 1e-3)
     r = orc.Render(sc)
-    ref = r.run(64, 64, 0, 2, 7)
-    got, _ = ctx.render(64, 64, 0, 2, 7)
     threads = cpu_threads()
     t0 = time.perf_counter()
-    r.run(128, 128, 0, 4, 7, nthreads=threads)
+    ref = r.run(256, 256, 0, 16, 7, nthreads=threads)  # the whole configured image on the host cores
     cdt = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r.run(64, 64, 0, 4, 7, nthreads=REF_WORKERS)
+    wdt = time.perf_counter() - t0
     out["reference_small_room"] = {
         "workload": "small room, 16,384-triangle soup + 10-triangle box, 2 TriLights, 256x256, 16 iterations",
         "samples_per_s": round(256 * 256 * 16 / (st["ms"] / 1e3), 1), "device_ms": round(st["ms"], 3),
         "camera_rays": st["camera_rays"], "shadow_rays": st["shadow_rays"],
-        "bit_equal_to_oracle_frac": float((got.view(np.uint32) == ref.view(np.uint32)).all(-1).mean()),
-        "cpu_baseline": {"samples_per_s": round(128 * 128 * 4 / cdt, 1), "cores": threads, "kind": "port",
-                         "sample": "128x128 x 4 iterations, oracle/orc_render.cpp (C++ restatement of core.Render)"}}
+        "bit_equal_to_oracle_frac": float((fb.view(np.uint32) == ref.view(np.uint32)).all(-1).mean()),
+        "float32_shading": {"samples_per_s": round(256 * 256 * 16 / (st32["ms"] / 1e3), 1),
+                            "device_ms": round(st32["ms"], 3),
+                            "mean_rel_pixel_err_vs_float64": float(rel32.mean()),
+                            "p99_rel_pixel_err_vs_float64": float(np.percentile(rel32, 99))},
+        "cpu_baseline": {"samples_per_s": round(256 * 256 * 16 / cdt, 1), "cores": threads, "kind": "port",
+                         "sample": "the whole 256x256 x 16 image, oracle/orc_render.cpp (C++ restatement of "
+                                   "core.Render)",
+                         "reference_workers": {"threads": REF_WORKERS, "samples_per_s": round(64 * 64 * 4 / wdt, 1),
+                                               "sample": "64x64 x 4 iterations, the reference's default worker "
+                                                         "count (core/render.go:190)"}}}
     # extended mode, sphere grid
     sc = scenes.sphere_grid()
     ctx.load_scene(sc)
@@ -644,17 +703,19 @@ def measure_e2e(args, ctx, geom, host_soa, hbuf, flush, world):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
-    t0 = time.perf_counter()
+    e2e_s = 0.0
     for _ in range(args.steps):
-        flush.zero_()
+        flush.zero_()  # L2 flush, outside the timed region
         torch.cuda.synchronize()
-        e2e_step()
-    e2e_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        e2e_step()  # synchronous: returns once the hits are in the pinned buffers
+        e2e_s += time.perf_counter() - t0
     e2e_s = max_over_ranks([e2e_s], world, torch.device("cuda", torch.cuda.current_device()))[0]
     e2e_value = job_value(N_RAYS, args.steps, world, e2e_s)
     ok = np.array_equal(pin_out["prim"].numpy(), hbuf["prim"])
-    return {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 7 * 4,
-            "d2h_bytes_per_step": N_RAYS * 5 * 4, "hits_match_device_path": bool(ok)}
+    hits = {k: pin_out[k].numpy().copy() for k in ("prim", "t", "u", "v", "w")}
+    return ({"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 7 * 4,
+             "d2h_bytes_per_step": N_RAYS * 5 * 4, "hits_match_device_path": bool(ok)}, hits)
 
 
 def main():
