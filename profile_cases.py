@@ -6,6 +6,7 @@
                                                        1920x1080, 2 spp, depth 8
     python profile_cases.py render_ref   reference-mode render, small room,
                                                        256x256, 16 iterations
+    python profile_cases.py render_ref_f32  the same with float32 shading
     python profile_cases.py jobs         64 uneven jobs in one launch
     python profile_cases.py path_jobs    64 uneven static/motion jobs path traced
                                                        in one call, 256x256, 2 spp, depth 5
@@ -36,22 +37,29 @@ def guide(ctx):
 
 
 def render_ext(ctx):
-    from . import scenes
+    from vermeer_gb300 import scenes
     sc = scenes.sphere_grid()
     ctx.load_scene(sc)
     ctx.render_path(sc["width"], sc["height"], 0, 2, 3, max_depth=8)
 
 
 def render_ref(ctx):
-    from . import scenes
+    from vermeer_gb300 import scenes
     sc = scenes.small_room(16384, seed=1)
     ctx.load_scene(sc)
     ctx.render(256, 256, 0, 16, 7)
 
 
+def render_ref_f32(ctx):
+    from vermeer_gb300 import scenes
+    sc = scenes.small_room(16384, seed=1)
+    ctx.load_scene(sc)
+    ctx.render(256, 256, 0, 16, 7, f32=True)
+
+
 def jobs(ctx):
     import torch
-    from . import scenes
+    from vermeer_gb300 import scenes
     sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)
     cam = scenes.coherent_rays(256)
     js = []
@@ -67,7 +75,7 @@ def jobs(ctx):
 
 
 def path_jobs(ctx):
-    from . import scenes
+    from vermeer_gb300 import scenes
     bj = scenes.batched_jobs()
     ids = [ctx.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1), motion_mode=m.get("motion_mode", 0))
            for m in bj["meshes"]]
@@ -82,15 +90,15 @@ def path_jobs(ctx):
 
 
 def build(ctx):
-    from . import scenes
-    from .api import BUILD_DEVICE
+    from vermeer_gb300 import scenes
+    from vermeer_gb300.api import BUILD_DEVICE
     v, ip = scenes.triangle_soup(1 << 20, 2)
     ctx.set_builder(BUILD_DEVICE)
     ctx.mesh_build(v, ip)
 
 
-CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "jobs": jobs, "path_jobs": path_jobs,
-         "build": build}
+CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "render_ref_f32": render_ref_f32,
+         "jobs": jobs, "path_jobs": path_jobs, "build": build}
 
 
 def main(argv):
