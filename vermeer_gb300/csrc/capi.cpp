@@ -423,7 +423,8 @@ int vmr_create(int device, vmr_ctx** out) {
   ctx->device = device;
   if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
-      cudaEventCreate(&ctx->evm) != cudaSuccess ||
+      cudaEventCreate(&ctx->evm) != cudaSuccess || cudaEventCreate(&ctx->rev0) != cudaSuccess ||
+      cudaEventCreate(&ctx->rev1) != cudaSuccess ||
       ctx->scratch.ensure(sizeof(DScratch)) != cudaSuccess) {
     delete ctx;
     return VMR_ERR_CUDA;
@@ -445,6 +446,8 @@ int vmr_destroy(vmr_ctx* ctx) {
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->evm) cudaEventDestroy(ctx->evm);
+  if (ctx->rev0) cudaEventDestroy(ctx->rev0);
+  if (ctx->rev1) cudaEventDestroy(ctx->rev1);
   cudaStream_t s = ctx->own_stream;
   delete ctx;
   if (s) cudaStreamDestroy(s);

@@ -149,6 +149,8 @@ struct vmr_ctx {
   DevBuf io;                      // rays + hits for host-pointer traces
   DevBuf sortbuf;                 // ray keys, bucket offsets, order, key-ordered rays
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;  // start, after the sort, end
+  // vmr_render's own start/end (its scene traces record ev0/ev1 themselves)
+  cudaEvent_t rev0 = nullptr, rev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
   vmr::RenderState render;

@@ -1010,7 +1010,7 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   b.queue_cap = (uint32_t)std::min<uint64_t>(qcap, 0xffffffffu);
   b.fb = reinterpret_cast<float*>(base + o_fb);
   RCUDA(cudaMemsetAsync(b.status, 0, 4, st));
-  RCUDA(cudaEventRecord(ctx->ev0, st));
+  RCUDA(cudaEventRecord(ctx->rev0, st));
   uint64_t n_shadow = 0, n_cam = 0;
   for (uint32_t it0 = 0; it0 < p->iter_count; it0 += iters_per_batch) {
     const uint32_t iters = std::min(iters_per_batch, p->iter_count - it0);
@@ -1060,7 +1060,7 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     k_accumulate<<<(int)((npix + 127) / 128), 128, 0, st>>>(b, iters);
     RCUDA(cudaGetLastError());
   }
-  RCUDA(cudaEventRecord(ctx->ev1, st));
+  RCUDA(cudaEventRecord(ctx->rev1, st));
   RCUDA(cudaMemcpyAsync(fb, b.fb, (size_t)npix * 3 * fsz, cudaMemcpyDeviceToHost, st));
   int status = 0;
   RCUDA(cudaMemcpyAsync(&status, b.status, 4, cudaMemcpyDeviceToHost, st));
@@ -1073,7 +1073,7 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     stats->camera_rays = n_cam;
     stats->shadow_rays = n_shadow;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&ms, ctx->rev0, ctx->rev1);
     stats->ms = ms;
   }
   return VMR_OK;
