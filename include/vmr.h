@@ -582,8 +582,13 @@ typedef struct {
     uint32_t flags;                   /* VMR_PATH_* */
     double* fb64;                     /* optional host width*height*3: the same
                                          running mean folded in float64 */
-    float guide_fraction;             /* VMR_PATH_GUIDED: probability of sampling
-                                         the guide at a vertex (0: 0.5) */
+    float guide_fraction;             /* VMR_PATH_GUIDED: alpha_max, the largest
+                                         probability of sampling the guide at a
+                                         vertex; each vertex's probability is
+                                         alpha_max * sigmoid(the network's
+                                         selection output) (0: 0.9); with
+                                         VMR_PATH_FIXED_SELECTION the
+                                         probability itself (0: 0.5) */
     uint32_t train_steps;             /* VMR_PATH_TRAIN: Adam steps after each
                                          batch (0: 4) */
     uint32_t train_batch;             /* training records per step (0: 65536) */
@@ -607,10 +612,15 @@ enum {
     VMR_PATH_TRAIN = 4,     /* record (vertex, sampled direction, density,
                                incident radiance) and train the guide on them
                                after each batch (online) */
-    VMR_PATH_SORT_QUEUES = 8 /* batches of >= 65,536 paths: trace each bounce
+    VMR_PATH_SORT_QUEUES = 8, /* batches of >= 65,536 paths: trace each bounce
                                and shadow queue in ray-key order (direction
                                class + Morton cell of the origin, the
                                tuning's sort-key width); images unchanged */
+    VMR_PATH_FIXED_SELECTION = 16 /* VMR_PATH_GUIDED: every vertex samples the
+                               guide with probability guide_fraction (the
+                               network's selection output unused, and with
+                               TRAIN the guide is fitted to the product
+                               alone, not to the vertex's full density) */
 };
 
 typedef struct {
@@ -690,12 +700,15 @@ int vmr_render_path_jobs(vmr_ctx* ctx, const vmr_path_job* jobs, uint32_t n_jobs
  * vertices: inputs = the hit point normalised to the scene bounds [lo, hi]
  * encoded with 12 sin/cos frequencies per axis, the shading normal and the
  * direction toward the previous vertex (78 values, plus a constant 1);
- * 4 hidden ReLU layers of 64; outputs = 8 von Mises-Fisher lobes (direction,
- * concentration, mixture logit).  Weights: W0 [64][80], W1..W3 [64][64],
- * W4 [40][64] row-major, concatenated (VMR_GUIDE_WEIGHTS floats); the
- * kernels run them on the tensor cores in bf16 with float32 accumulation.
- * Vertex arrays are host pointers to n x 3 floats. */
-#define VMR_GUIDE_WEIGHTS 19968
+ * 4 hidden ReLU layers of 64; 41 outputs = 8 von Mises-Fisher lobes
+ * (direction, concentration, mixture logit) and the selection logit s: a
+ * vertex samples the guide with probability alpha = alpha_max * sigmoid(s)
+ * and its BSDF otherwise.  Weights: W0 [64][80], W1..W3 [64][64], W4 [41][64]
+ * row-major, concatenated (VMR_GUIDE_WEIGHTS floats); the kernels run them
+ * on the tensor cores in bf16 with float32 accumulation.  Vertex arrays are
+ * host pointers to n x 3 floats. */
+#define VMR_GUIDE_WEIGHTS 20032
+#define VMR_GUIDE_OUTPUTS 41
 
 typedef struct {
     float lr, beta1, beta2, eps;
@@ -706,26 +719,30 @@ typedef struct {
 int vmr_guide_init(vmr_ctx* ctx, uint64_t seed);
 /* Self-test of the kernels' failure path: a one-block kernel waits, with the
  * guide kernels' bounded mbarrier wait, on a barrier that nothing arrives
- * at.  The wait runs out (about a quarter of a second), the kernel sets the
+ * at.  The wait runs out (after one second), the kernel sets the
  * error word and returns, and the call reports VMR_ERR_TIMEOUT with the
  * kernel's duration in *ms (optional); the context stays usable.  Any other
  * status means the bound did not work as designed. */
 int vmr_selftest_wait(vmr_ctx* ctx, float* ms);
 int vmr_guide_set_weights(vmr_ctx* ctx, const float* weights);
 int vmr_guide_get_weights(vmr_ctx* ctx, float* weights);
-/* The 40 outputs of n vertices (out: n x 40 floats). */
+/* The 41 outputs of n vertices (out: n x 41 floats). */
 int vmr_guide_forward(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, size_t n,
                       const float lo[3], const float hi[3], float* out);
-/* Gradient of sum_i -weight_i * log p_i(omega_i) with respect to the weights
+/* Gradient of sum_i -weight_i * log q_i(omega_i) with respect to the weights
  * (grad: VMR_GUIDE_WEIGHTS floats) and the loss itself; omega: n x 3 unit
- * directions, weight: n floats.  The weights are not changed. */
+ * directions, weight: n floats.  bsdf_pdf (n floats, optional): the BSDF's
+ * density of each omega_i; with it q_i is the vertex's full sampling density
+ * alpha_i p_guide + (1 - alpha_i) p_bsdf, alpha_i = alpha_max * sigmoid(s_i)
+ * (alpha_max in (0, 1)), and the selection logit is trained too; without it
+ * q_i is the guide's own density.  The weights are not changed. */
 int vmr_guide_gradient(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
-                       const float* weight, size_t n, const float lo[3], const float hi[3], float* grad,
-                       float* loss);
+                       const float* weight, const float* bsdf_pdf, float alpha_max, size_t n, const float lo[3],
+                       const float hi[3], float* grad, float* loss);
 /* One Adam step on that loss divided by the sum of the weights. */
 int vmr_guide_train_step(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
-                         const float* weight, size_t n, const float lo[3], const float hi[3], const vmr_adam* opt,
-                         float* loss);
+                         const float* weight, const float* bsdf_pdf, float alpha_max, size_t n, const float lo[3],
+                         const float hi[3], const vmr_adam* opt, float* loss);
 
 /* -------------------------------------------------------------- no-alloc */
 /* No counterpart in the reference.  For callers that must not have a library

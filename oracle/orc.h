@@ -277,17 +277,19 @@ void orc_set_normalize_mode(int mode, uint64_t seed);
 void orc_sincos_turns(const float* u, size_t n, float* s, float* c);
 
 /* Path-guiding network (orc_mlp.cpp; no reference counterpart).  Weights:
- * W0 [64][80], W1..W3 [64][64], W4 [40][64] concatenated, row-major.
+ * W0 [64][80], W1..W3 [64][64], W4 [41][64] concatenated, row-major (the 41st
+ * output is the guide's selection logit).
  * precision: 64, 32, or 16 (the CUDA kernels' bfloat16 roundings with
  * float32 accumulation). */
 int orc_guide_n_weights(void);
 void orc_guide_features(const float* pos, const float* nrm, const float* wo, const float* lo, const float* hi, int n,
                         double* feat);
 void orc_guide_forward(const float* W, const double* feat, int n, int precision, double* out);
-double orc_guide_pdf(const double* out40, const double* w);
-void orc_guide_out_grad(const double* out40, const double* w, double weight, double* g40, double* loss);
-double orc_guide_loss_grad(const float* W, const double* feat, const float* omega, const float* weight, int n,
-                           int precision, double* gW);
+double orc_guide_pdf(const double* out41, const double* w);
+void orc_guide_out_grad(const double* out41, const double* w, double weight, double pb, double amax, double* g41,
+                        double* loss);
+double orc_guide_loss_grad(const float* W, const double* feat, const float* omega, const float* weight,
+                           const float* bsdf_pdf, double amax, int n, int precision, double* gW);
 
 #ifdef __cplusplus
 }

@@ -193,9 +193,9 @@ def _register_render(L):
     L.orc_guide_forward.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P]
     L.orc_guide_pdf.restype = ctypes.c_double
     L.orc_guide_pdf.argtypes = [P, P]
-    L.orc_guide_out_grad.argtypes = [P, P, ctypes.c_double, P, P]
+    L.orc_guide_out_grad.argtypes = [P, P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, P]
     L.orc_guide_loss_grad.restype = ctypes.c_double
-    L.orc_guide_loss_grad.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, P]
+    L.orc_guide_loss_grad.argtypes = [P, P, P, P, P, ctypes.c_double, ctypes.c_int, ctypes.c_int, P]
     L.orc_filter_warp.restype = ctypes.c_int
     L.orc_filter_warp.argtypes = [P, P, P, ctypes.c_size_t, P, P]
     L.orc_filter_tables.restype = ctypes.c_int
@@ -267,7 +267,7 @@ def filter_tables(f):
 class Guide:
     """The path-guiding network's oracle (orc_mlp.cpp)."""
 
-    N_IN, N_OUT = 80, 40
+    N_IN, N_OUT = 80, 41
 
     @staticmethod
     def n_weights():
@@ -286,33 +286,42 @@ class Guide:
     def forward(W, feat, precision=64):
         W = np.ascontiguousarray(W, np.float32)
         feat = np.ascontiguousarray(feat, np.float64)
-        out = np.zeros((feat.shape[0], 40), np.float64)
+        out = np.zeros((feat.shape[0], 41), np.float64)
         lib().orc_guide_forward(_ptr(W), _ptr(feat), feat.shape[0], int(precision), _ptr(out))
         return out
 
     @staticmethod
-    def pdf(out40, w):
-        o = np.ascontiguousarray(out40, np.float64)
+    def pdf(out41, w):
+        """The vMF mixture's density at the unit direction w."""
+        o = np.ascontiguousarray(out41, np.float64)
         w = np.ascontiguousarray(w, np.float64)
         return lib().orc_guide_pdf(_ptr(o), _ptr(w))
 
     @staticmethod
-    def out_grad(out40, w, weight):
-        o = np.ascontiguousarray(out40, np.float64)
+    def alpha(out41, amax):
+        """The probability of sampling the guide: amax * sigmoid(s)."""
+        return amax / (1.0 + np.exp(-np.asarray(out41, np.float64)[..., 40]))
+
+    @staticmethod
+    def out_grad(out41, w, weight, pb=-1.0, amax=0.5):
+        """Loss and its gradient at the outputs; pb < 0: no BSDF density."""
+        o = np.ascontiguousarray(out41, np.float64)
         w = np.ascontiguousarray(w, np.float64)
-        g = np.zeros(40, np.float64)
+        g = np.zeros(41, np.float64)
         loss = ctypes.c_double()
-        lib().orc_guide_out_grad(_ptr(o), _ptr(w), float(weight), _ptr(g), ctypes.byref(loss))
+        lib().orc_guide_out_grad(_ptr(o), _ptr(w), float(weight), float(pb), float(amax), _ptr(g), ctypes.byref(loss))
         return g, loss.value
 
     @staticmethod
-    def loss_grad(W, feat, omega, weight, precision=64):
+    def loss_grad(W, feat, omega, weight, precision=64, bsdf_pdf=None, amax=0.5):
         W = np.ascontiguousarray(W, np.float32)
         feat = np.ascontiguousarray(feat, np.float64)
         omega = np.ascontiguousarray(omega, np.float32)
         weight = np.ascontiguousarray(weight, np.float32)
+        pb = None if bsdf_pdf is None else np.ascontiguousarray(bsdf_pdf, np.float32)
         g = np.zeros(W.size, np.float64)
-        loss = lib().orc_guide_loss_grad(_ptr(W), _ptr(feat), _ptr(omega), _ptr(weight), feat.shape[0],
+        loss = lib().orc_guide_loss_grad(_ptr(W), _ptr(feat), _ptr(omega), _ptr(weight),
+                                         None if pb is None else _ptr(pb), float(amax), feat.shape[0],
                                          int(precision), _ptr(g))
         return loss, g
 

@@ -4,9 +4,10 @@
 // TEST INFRASTRUCTURE ONLY (see orc.h).
 //
 // Network: 80 inputs -> 4 hidden layers of 64 (ReLU, no biases; input 78 is
-// the constant 1) -> 40 outputs = 8 von Mises-Fisher lobes x (direction 3,
-// concentration 1, mixture logit 1).  Weights: W0 [64][80], W1..W3 [64][64],
-// W4 [40][64], row-major, concatenated (19,968 floats).
+// the constant 1) -> 41 outputs = 8 von Mises-Fisher lobes x (direction 3,
+// concentration 1, mixture logit 1), then the selection logit s.  Weights:
+// W0 [64][80], W1..W3 [64][64], W4 [41][64], row-major, concatenated (20,032
+// floats).
 //
 // Inputs of a path vertex: the hit point p normalised to the scene bounds,
 // q = (p - lo)/(hi - lo); for each axis c and frequency f = 0..11,
@@ -16,12 +17,18 @@
 //
 // Lobe k: mu = normalize(o[5k..5k+2]), kappa = min(softplus(o[5k+3]) + 0.01,
 // 1000), pi = softmax over o[5k+4]; vMF density
-// kappa / (2 pi (1 - exp(-2 kappa))) * exp(kappa (mu.w - 1)).
+// kappa / (2 pi (1 - exp(-2 kappa))) * exp(kappa (mu.w - 1)).  The vertex
+// samples the guide with probability alpha = amax * sigmoid(o[40]) and its
+// BSDF otherwise, so its sampling density is q = alpha p_guide + (1 - alpha)
+// p_bsdf.
 //
-// Training loss of a batch: sum_i -weight_i * log p(omega_i), where omega_i is
-// a direction the tracer sampled at the vertex and weight_i its incident
-// radiance (luminance) over the density it was sampled with; the gradient is
-// analytic (the mixture, the lobe parameters, back through the ReLU layers).
+// Training loss of a batch: sum_i -weight_i * log q(omega_i), where omega_i
+// is a direction the tracer sampled at the vertex, weight_i its incident
+// radiance (luminance) x |cos| over the density it was sampled with, and
+// p_bsdf(omega_i) is recorded with it; without a recorded BSDF density the
+// loss is -weight_i * log p_guide(omega_i) and s gets no gradient.  The
+// gradient is analytic (the selection, the mixture, the lobe parameters,
+// back through the ReLU layers).
 //
 // Precision modes: 64 and 32 compute everything in that type; 16 mirrors
 // the CUDA kernels' tensor-core arithmetic: weights, layer inputs and
@@ -36,9 +43,9 @@
 
 namespace {
 
-const int kIn = 80, kHid = 64, kOut = 40, kLobes = 8;
+const int kIn = 80, kHid = 64, kOut = 41, kLobes = 8;
 const int kLayerIn[5] = {80, 64, 64, 64, 64};
-const int kLayerOut[5] = {64, 64, 64, 64, 40};
+const int kLayerOut[5] = {64, 64, 64, 64, 41};
 const int kOffset[5] = {0, 5120, 9216, 13312, 17408};
 
 float bf16(float x) {  // round to nearest even, as __float2bfloat16_rn
@@ -144,9 +151,9 @@ T mixture_pdf(const Lobes<T>& L, const T* w) {
   return p;
 }
 
-// d(-weight * log p)/d(outputs).
+// d(-weight * log q)/d(outputs); pb < 0: no BSDF density, q = p_guide.
 template <class T>
-void loss_grad_out(const T* o, const T* w, T weight, T* g, T& loss) {
+void loss_grad_out(const T* o, const T* w, T weight, T pb, T amax, T* g, T& loss) {
   Lobes<T> L;
   lobes(o, L);
   T v[kLobes];
@@ -155,12 +162,22 @@ void loss_grad_out(const T* o, const T* w, T weight, T* g, T& loss) {
     v[k] = vmf(L, k, w);
     p += L.pi[k] * v[k];
   }
-  loss = -weight * std::log(p);
+  // q, and a = dq/dp_guide (alpha, or 1 without the selection)
+  T q = p, a = T(1);
+  g[40] = T(0);
+  if (pb >= T(0)) {
+    const T sg = T(1) / (T(1) + std::exp(-o[40]));
+    a = amax * sg;
+    q = a * p + (T(1) - a) * pb;
+    g[40] = -weight * (p - pb) / q * (amax * sg * (T(1) - sg));
+  }
+  loss = -weight * std::log(q);
+  const T sc = a * p / q;  // share of the guide in q
   for (int k = 0; k < kLobes; ++k) {
-    const T r = L.pi[k] * v[k] / p;  // responsibility
+    const T r = a * L.pi[k] * v[k] / q;  // responsibility of lobe k in q
     const T d = L.mu[k][0] * w[0] + L.mu[k][1] * w[1] + L.mu[k][2] * w[2];
     const T kap = L.kappa[k];
-    g[5 * k + 4] = -weight * (r - L.pi[k]);
+    g[5 * k + 4] = -weight * (r - sc * L.pi[k]);
     const T dlogv_dk = T(1) / kap - T(2) / std::expm1(T(2) * kap) + (d - T(1));
     g[5 * k + 3] = L.clamped[k] ? T(0) : -weight * r * dlogv_dk * L.sig[k];
     for (int c = 0; c < 3; ++c) g[5 * k + c] = -weight * r * kap * (w[c] - d * L.mu[k][c]) / L.rn[k];
@@ -168,9 +185,9 @@ void loss_grad_out(const T* o, const T* w, T weight, T* g, T& loss) {
 }
 
 template <class T>
-double loss_and_grad(const float* W, const double* feats, const float* omega, const float* weight, int n, int mode,
-                     double* gW) {
-  const int nw = kOffset[4] + 40 * 64;
+double loss_and_grad(const float* W, const double* feats, const float* omega, const float* weight, const float* pb,
+                     double amax, int n, int mode, double* gW) {
+  const int nw = kOffset[4] + kOut * 64;
   std::vector<double> acc(nw, 0.0);
   double total = 0;
   std::vector<std::vector<T>> acts;
@@ -178,7 +195,7 @@ double loss_and_grad(const float* W, const double* feats, const float* omega, co
     T out[kOut], go[kOut], loss;
     forward<T>(W, feats + (size_t)i * kIn, mode, acts, out);
     const T w[3] = {(T)omega[3 * i], (T)omega[3 * i + 1], (T)omega[3 * i + 2]};
-    loss_grad_out<T>(out, w, (T)weight[i], go, loss);
+    loss_grad_out<T>(out, w, (T)weight[i], pb ? (T)pb[i] : T(-1), (T)amax, go, loss);
     total += (double)loss;
     // back-propagate: delta of layer l's output
     std::vector<T> delta(go, go + kOut);
@@ -205,7 +222,7 @@ double loss_and_grad(const float* W, const double* feats, const float* omega, co
 
 extern "C" {
 
-int orc_guide_n_weights(void) { return kOffset[4] + 40 * 64; }
+int orc_guide_n_weights(void) { return kOffset[4] + kOut * 64; }
 
 void orc_guide_features(const float* pos, const float* nrm, const float* wo, const float* lo, const float* hi, int n,
                         double* feat) {
@@ -228,20 +245,21 @@ void orc_guide_forward(const float* W, const double* feat, int n, int precision,
   }
 }
 
-double orc_guide_pdf(const double* out40, const double* w) {
+double orc_guide_pdf(const double* out41, const double* w) {
   Lobes<double> L;
-  lobes(out40, L);
+  lobes(out41, L);
   return mixture_pdf(L, w);
 }
 
-void orc_guide_out_grad(const double* out40, const double* w, double weight, double* g40, double* loss) {
-  loss_grad_out<double>(out40, w, weight, g40, *loss);
+void orc_guide_out_grad(const double* out41, const double* w, double weight, double pb, double amax, double* g41,
+                        double* loss) {
+  loss_grad_out<double>(out41, w, weight, pb, amax, g41, *loss);
 }
 
-double orc_guide_loss_grad(const float* W, const double* feat, const float* omega, const float* weight, int n,
-                           int precision, double* gW) {
-  if (precision == 64) return loss_and_grad<double>(W, feat, omega, weight, n, 64, gW);
-  return loss_and_grad<float>(W, feat, omega, weight, n, precision, gW);
+double orc_guide_loss_grad(const float* W, const double* feat, const float* omega, const float* weight,
+                           const float* bsdf_pdf, double amax, int n, int precision, double* gW) {
+  if (precision == 64) return loss_and_grad<double>(W, feat, omega, weight, bsdf_pdf, amax, n, 64, gW);
+  return loss_and_grad<float>(W, feat, omega, weight, bsdf_pdf, amax, n, precision, gW);
 }
 
 }  // extern "C"

@@ -14,7 +14,8 @@ relative L2 difference <= 3e-2 and cosine >= 0.999.
 import numpy as np
 import pytest
 
-NW = 19968
+NW = 20032
+AMAX = 0.9
 
 
 def _batch(n, seed):
@@ -41,39 +42,56 @@ HI = np.array([1, 1, 1], np.float32)
 
 # ------------------------------------------------------------------ CPU ----
 def test_oracle_layout(orc):
-    assert orc.Guide.n_weights() == NW == 64 * 80 + 3 * 64 * 64 + 40 * 64
+    assert orc.Guide.n_weights() == NW == 64 * 80 + 3 * 64 * 64 + 41 * 64
 
 
-def test_oracle_gradient_matches_finite_differences(orc):
+def _bsdf_pdf(nrm, om):
+    """Cosine-hemisphere density of om about nrm (0 below the surface)."""
+    return np.maximum((nrm * om).sum(1), 0.0).astype(np.float32) / np.float32(np.pi)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_oracle_gradient_matches_finite_differences(orc, mixed):
+    """Without a BSDF density (the guide's own density) and with one (the
+    vertex's full sampling density, which also trains the selection logit)."""
     G = orc.Guide
     pos, nrm, wo, om, wt = _batch(5, 1)
+    pb = _bsdf_pdf(nrm, om) if mixed else None
     f = G.features(pos, nrm, wo, LO, HI)
     W = _weights(2)
-    _, g = G.loss_grad(W, f, om, wt, 64)
+    _, g = G.loss_grad(W, f, om, wt, 64, bsdf_pdf=pb, amax=AMAX)
     rng = np.random.default_rng(3)
     nz = np.nonzero(np.abs(g) > 1e-4)[0]
-    for k in rng.choice(nz, 10, replace=False):
+    picks = list(rng.choice(nz, 10, replace=False))
+    sel = np.arange(17408 + 40 * 64, NW)  # the selection logit's weights
+    if mixed:
+        picks += list(rng.choice(sel[np.abs(g[sel]) > 1e-5], 4, replace=False))
+    else:
+        assert not g[sel].any()
+    for k in picks:
         h = np.float32(1e-3)
         Wp, Wm = W.copy(), W.copy()
         Wp[k] += h
         Wm[k] -= h
-        lp, _ = G.loss_grad(Wp, f, om, wt, 64)
-        lm, _ = G.loss_grad(Wm, f, om, wt, 64)
+        lp, _ = G.loss_grad(Wp, f, om, wt, 64, bsdf_pdf=pb, amax=AMAX)
+        lm, _ = G.loss_grad(Wm, f, om, wt, 64, bsdf_pdf=pb, amax=AMAX)
         fd = (lp - lm) / (float(Wp[k]) - float(Wm[k]))
         assert abs(fd - g[k]) <= 1e-5 + 1e-4 * abs(g[k]), (k, fd, g[k])
 
 
-def test_oracle_matches_torch_autograd(orc):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_oracle_matches_torch_autograd(orc, mixed):
     torch = pytest.importorskip("torch")
     G = orc.Guide
     pos, nrm, wo, om, wt = _batch(7, 4)
+    pb = _bsdf_pdf(nrm, om)
     f = G.features(pos, nrm, wo, LO, HI)
     W = _weights(5)
-    loss_o, g_o = G.loss_grad(W, f, om, wt, 64)
+    loss_o, g_o = G.loss_grad(W, f, om, wt, 64, bsdf_pdf=pb if mixed else None, amax=AMAX)
     out_o = G.forward(W, f, 64)
     # independent model: plain torch ops in float64
     Wt = torch.tensor(W.astype(np.float64), requires_grad=True)
-    shapes = [(64, 80), (64, 64), (64, 64), (64, 64), (40, 64)]
+    shapes = [(64, 80), (64, 64), (64, 64), (64, 64), (41, 64)]
     offs = np.cumsum([0] + [a * b for a, b in shapes])
     x = torch.tensor(f)
     for l, (a, b) in enumerate(shapes):
@@ -83,7 +101,7 @@ def test_oracle_matches_torch_autograd(orc):
             x = torch.relu(x)
     out = x
     assert np.allclose(out.detach().numpy(), out_o, rtol=1e-10, atol=1e-12)
-    o = out.reshape(-1, 8, 5)
+    o = out[:, :40].reshape(-1, 8, 5)
     r = o[:, :, :3]
     mu = r / torch.clamp(r.norm(dim=2, keepdim=True), min=1e-6)
     kap = torch.clamp(torch.nn.functional.softplus(o[:, :, 3]) + 0.01, max=1000.0)
@@ -92,6 +110,9 @@ def test_oracle_matches_torch_autograd(orc):
     d = (mu * w[:, None, :]).sum(2)
     c = kap / (2 * np.pi * (-torch.expm1(-2 * kap)))
     p = (pi * c * torch.exp(kap * (d - 1))).sum(1)
+    if mixed:
+        a = AMAX * torch.sigmoid(out[:, 40])
+        p = a * p + (1 - a) * torch.tensor(pb.astype(np.float64))
     loss = -(torch.tensor(wt.astype(np.float64)) * torch.log(p)).sum()
     loss.backward()
     assert abs(loss.item() - loss_o) <= 1e-9 * abs(loss_o)
@@ -101,7 +122,7 @@ def test_oracle_matches_torch_autograd(orc):
 def test_vmf_mixture_is_a_density(orc):
     G = orc.Guide
     rng = np.random.default_rng(6)
-    out = rng.standard_normal(40) * 1.5
+    out = rng.standard_normal(41) * 1.5
     # midpoint quadrature over (cos theta, phi)
     nt, npf = 400, 400
     ct = (np.arange(nt) + 0.5) / nt * 2 - 1
@@ -140,20 +161,29 @@ def test_guide_forward_matches_oracle(ctx, orc):
 
 
 @pytest.mark.gpu
-def test_guide_gradient_matches_oracle(ctx, orc):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_guide_gradient_matches_oracle(ctx, orc, mixed):
+    """Without and with the BSDF density (the full sampling density's loss,
+    which also trains the selection logit)."""
     G = orc.Guide
     W = _weights(13)
     ctx.guide_set_weights(W)
     pos, nrm, wo, om, wt = _batch(700, 14)
-    g, loss = ctx.guide_gradient(pos, nrm, wo, om, wt, LO, HI)
+    pb = _bsdf_pdf(nrm, om) if mixed else None
+    g, loss = ctx.guide_gradient(pos, nrm, wo, om, wt, LO, HI, bsdf_pdf=pb, alpha_max=AMAX)
     f = G.features(pos, nrm, wo, LO, HI)
-    loss_o, g_o = G.loss_grad(W, f, om, wt, 16)
+    loss_o, g_o = G.loss_grad(W, f, om, wt, 16, bsdf_pdf=pb, amax=AMAX)
     assert abs(loss - loss_o) <= 1e-2 * abs(loss_o)
     rel = np.linalg.norm(g - g_o) / np.linalg.norm(g_o)
     cos = g @ g_o / (np.linalg.norm(g) * np.linalg.norm(g_o))
     assert rel <= 3e-2 and cos >= 0.999, (rel, cos)
-    # per layer too (each has its own kernel instance)
-    for a, b in ((0, 5120), (5120, 9216), (9216, 13312), (13312, 17408), (17408, NW)):
+    # per layer too (each has its own kernel instance), and the selection
+    # logit's row of the output layer on its own
+    sel = 17408 + 40 * 64
+    for a, b in ((0, 5120), (5120, 9216), (9216, 13312), (13312, 17408), (17408, sel), (sel, NW)):
+        if not mixed and a == sel:
+            assert not g[a:b].any()
+            continue
         r = np.linalg.norm(g[a:b] - g_o[a:b]) / max(np.linalg.norm(g_o[a:b]), 1e-12)
         assert r <= 5e-2, (a, r)
 

@@ -142,8 +142,10 @@ PATH_NO_GRAPH = 1
 PATH_GUIDED = 2
 PATH_TRAIN = 4
 PATH_SORT_QUEUES = 8
+PATH_FIXED_SELECTION = 16
 
-GUIDE_WEIGHTS = 19968
+GUIDE_WEIGHTS = 20032
+GUIDE_OUTPUTS = 41
 
 
 class Adam(ctypes.Structure):
@@ -216,10 +218,10 @@ SIGNATURES = {
     "vmr_guide_set_weights": (ctypes.c_int, [P, P]),
     "vmr_guide_get_weights": (ctypes.c_int, [P, P]),
     "vmr_guide_forward": (ctypes.c_int, [P, P, P, P, ctypes.c_size_t, P, P, P]),
-    "vmr_guide_gradient": (ctypes.c_int, [P, P, P, P, P, P, ctypes.c_size_t, P, P, P,
+    "vmr_guide_gradient": (ctypes.c_int, [P, P, P, P, P, P, P, ctypes.c_float, ctypes.c_size_t, P, P, P,
                                           ctypes.POINTER(ctypes.c_float)]),
-    "vmr_guide_train_step": (ctypes.c_int, [P, P, P, P, P, P, ctypes.c_size_t, P, P, ctypes.POINTER(Adam),
-                                            ctypes.POINTER(ctypes.c_float)]),
+    "vmr_guide_train_step": (ctypes.c_int, [P, P, P, P, P, P, P, ctypes.c_float, ctypes.c_size_t, P, P,
+                                            ctypes.POINTER(Adam), ctypes.POINTER(ctypes.c_float)]),
     "vmr_autotune": (ctypes.c_int, [P, U32, ctypes.POINTER(Rays), ctypes.c_size_t, ctypes.c_int,
                                     ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(U32)]),
     "vmr_clear_tuning": (ctypes.c_int, [P, U32]),

@@ -402,12 +402,14 @@ class Context:
                     rr_depth: int = 3, fb=None, fb64=None, max_batch_samples: int = 0, graph: bool = True,
                     guided: bool = False, train: bool = False, guide_fraction: float = 0.0, train_steps: int = 0,
                     train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False, guide_depth: int = 0,
-                    rows=None):
+                    rows=None, fixed_selection: bool = False):
         """The extended path tracer: iterations [iter_begin, iter_begin +
         iter_count) folded into fb (float32 [height, width, 3]) and, when
         given, fb64 (float64).  guided: sample the guide network too; train:
         train it online; guide_depth: guide only the first vertices of each
-        path (0: all); sort_queues: trace each queue in ray-key order;
+        path (0: all); guide_fraction: alpha_max of the learned selection
+        (0: 0.9), or with fixed_selection the guide's probability at every
+        vertex (0: 0.5); sort_queues: trace each queue in ray-key order;
         rows: (row_begin, row_count), a band of the image (fb then holds
         row_count rows).  Returns (fb, stats)."""
         r0, nr = rows if rows is not None else (0, 0)
@@ -419,7 +421,7 @@ class Context:
             assert fb64.dtype == np.float64 and fb64.flags.c_contiguous and fb64.shape == (hb, width, 3)
         p = self._path_params(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, fb64,
                               max_batch_samples, graph, guided, train, guide_fraction, train_steps, train_batch,
-                              train_lr, sort_queues, guide_depth, r0, nr)
+                              train_lr, sort_queues, guide_depth, r0, nr, fixed_selection)
         st = _lib.PathStats()
         self._check(self.L.vmr_render_path(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,
@@ -429,9 +431,11 @@ class Context:
     @staticmethod
     def _path_params(width, height, iter_begin, iter_count, seed, max_depth=4, rr_depth=3, fb64=None,
                      max_batch_samples=0, graph=True, guided=False, train=False, guide_fraction=0.0, train_steps=0,
-                     train_batch=0, train_lr=0.0, sort_queues=False, guide_depth=0, row_begin=0, row_count=0):
+                     train_batch=0, train_lr=0.0, sort_queues=False, guide_depth=0, row_begin=0, row_count=0,
+                     fixed_selection=False):
         flags = (0 if graph else _lib.PATH_NO_GRAPH) | (_lib.PATH_GUIDED if guided else 0) | \
-                (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0)
+                (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0) | \
+                (_lib.PATH_FIXED_SELECTION if fixed_selection else 0)
         return _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
                                flags, None if fb64 is None else _p(fb64), guide_fraction, train_steps, train_batch,
                                train_lr, guide_depth, row_begin, row_count)
@@ -455,26 +459,36 @@ class Context:
         return [np.ascontiguousarray(a, np.float32) for a in arrs]
 
     def guide_forward(self, pos, nrm, wo, lo, hi):
+        """The network's 41 outputs per vertex (8 lobes x 5, then the
+        selection logit)."""
         pos, nrm, wo, lo, hi = self._rows(pos, nrm, wo, lo, hi)
         n = pos.shape[0]
-        out = np.zeros((n, 40), np.float32)
+        out = np.zeros((n, _lib.GUIDE_OUTPUTS), np.float32)
         self._check(self.L.vmr_guide_forward(self.h, _p(pos), _p(nrm), _p(wo), n, _p(lo), _p(hi), _p(out)))
         return out
 
-    def guide_gradient(self, pos, nrm, wo, omega, weight, lo, hi):
+    def guide_gradient(self, pos, nrm, wo, omega, weight, lo, hi, bsdf_pdf=None, alpha_max=0.9):
+        """Gradient and loss of a batch (vmr_guide_gradient); bsdf_pdf: the
+        BSDF's density of each direction, for the full sampling density's
+        loss that also trains the selection."""
         pos, nrm, wo, omega, weight, lo, hi = self._rows(pos, nrm, wo, omega, weight, lo, hi)
+        pb = None if bsdf_pdf is None else np.ascontiguousarray(bsdf_pdf, np.float32)
         g = np.zeros(_lib.GUIDE_WEIGHTS, np.float32)
         loss = ctypes.c_float()
-        self._check(self.L.vmr_guide_gradient(self.h, _p(pos), _p(nrm), _p(wo), _p(omega), _p(weight), pos.shape[0],
-                                              _p(lo), _p(hi), _p(g), ctypes.byref(loss)))
+        self._check(self.L.vmr_guide_gradient(self.h, _p(pos), _p(nrm), _p(wo), _p(omega), _p(weight), _p(pb),
+                                              float(alpha_max), pos.shape[0], _p(lo), _p(hi), _p(g),
+                                              ctypes.byref(loss)))
         return g.astype(np.float64), loss.value
 
-    def guide_train_step(self, pos, nrm, wo, omega, weight, lo, hi, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+    def guide_train_step(self, pos, nrm, wo, omega, weight, lo, hi, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8,
+                         bsdf_pdf=None, alpha_max=0.9):
         pos, nrm, wo, omega, weight, lo, hi = self._rows(pos, nrm, wo, omega, weight, lo, hi)
+        pb = None if bsdf_pdf is None else np.ascontiguousarray(bsdf_pdf, np.float32)
         a = _lib.Adam(lr, beta1, beta2, eps)
         loss = ctypes.c_float()
-        self._check(self.L.vmr_guide_train_step(self.h, _p(pos), _p(nrm), _p(wo), _p(omega), _p(weight),
-                                                pos.shape[0], _p(lo), _p(hi), ctypes.byref(a), ctypes.byref(loss)))
+        self._check(self.L.vmr_guide_train_step(self.h, _p(pos), _p(nrm), _p(wo), _p(omega), _p(weight), _p(pb),
+                                                float(alpha_max), pos.shape[0], _p(lo), _p(hi), ctypes.byref(a),
+                                                ctypes.byref(loss)))
         return loss.value
 
     @staticmethod

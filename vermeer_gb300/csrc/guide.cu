@@ -1,7 +1,8 @@
 // guide.cu - the path-guiding network on the 5th-generation tensor cores.
 //
 // No reference counterpart.  The network (80 inputs, 4 hidden ReLU layers
-// of 64, 40 outputs = 8 vMF lobes; no biases, input 78 is the constant 1)
+// of 64, 41 outputs = 8 vMF lobes and the selection logit; no biases, input
+// 78 is the constant 1)
 // runs fused per tile of 128 rows: a group of 128 threads works on a tile
 // with the bf16 weights in shared memory (inference: two groups per CTA
 // share one copy), thread r owns row r, and each layer is
@@ -80,19 +81,32 @@ __device__ __forceinline__ void bar_init(uint64_t* bar) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(bar)) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-// Bounded wait for the phase `parity` of an mbarrier to complete.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait for the phase `parity` of an mbarrier to complete.  try_wait
+// suspends the thread in hardware until the phase completes (or a short
+// system time limit passes), so waiting threads take no issue slots from
+// the other tile groups' epilogues; the wait gives up after one second of
+// global time (or 2^24 tries, whichever comes first).
+constexpr uint64_t kWaitNs = 1000000000ull;
 __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = saddr(bar);
-  for (uint32_t i = 0; i < (1u << 22); ++i) {
+  uint64_t t0 = 0;
+  for (uint32_t i = 0; i < (1u << 24); ++i) {
     uint32_t ok;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(ok)
         : "r"(a), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (i > 64) __nanosleep(64);
+    const uint64_t t = global_ns();
+    if (i == 0) t0 = t;
+    else if (t - t0 > kWaitNs) return false;
   }
   return false;
 }
@@ -223,18 +237,30 @@ constexpr uint32_t kTrainSmem = kSBEnd + 64;
 constexpr int kLobes = 8;
 
 // Input features of a vertex (the encoding the oracle's guide_features
-// restates).
+// restates).  sin and cos of pi 2^k q are evaluated exactly (sincospif) at
+// k = 0, 4, 8 and carried to the next three frequencies by the double-angle
+// identities sin 2x = 2 sin x cos x, cos 2x = (cos x - sin x)(cos x + sin x):
+// nine calls instead of 36 per row, with an absolute error below 1e-6 after
+// three doublings, far under the bf16 rounding the features then get.
 __device__ void features(const float* p, const float* n, const float* wo, const float* lo, const float* inv_ext,
                          float* f) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float q = (p[c] - lo[c]) * inv_ext[c];
 #pragma unroll
-    for (int k = 0; k < 12; ++k) {
+    for (int a = 0; a < 12; a += 4) {
       float s, co;
-      sincospif(ldexpf(q, k), &s, &co);
-      f[24 * c + 2 * k] = s;
-      f[24 * c + 2 * k + 1] = co;
+      sincospif(ldexpf(q, a), &s, &co);
+      f[24 * c + 2 * a] = s;
+      f[24 * c + 2 * a + 1] = co;
+#pragma unroll
+      for (int k = a + 1; k < a + 4; ++k) {
+        const float s2 = 2.0f * s * co;
+        co = (co - s) * (co + s);
+        s = s2;
+        f[24 * c + 2 * k] = s;
+        f[24 * c + 2 * k + 1] = co;
+      }
     }
   }
 #pragma unroll
@@ -248,7 +274,7 @@ __device__ void features(const float* p, const float* n, const float* wo, const 
 
 // The forward pass of one tile; the caller has written the input features
 // into A0.  Returns false if a wait ran out.  On return the output layer
-// (48 columns, 40 used) is in TMEM columns 0..47; mask[l] holds bit j for
+// (48 columns, 41 used) is in TMEM columns 0..47; mask[l] holds bit j for
 // h_{l+1}[j] > 0 (l = 0..3, two words each).
 __device__ bool forward_tile(char* sm, Shared& sh, uint32_t& phase, uint32_t* mask, bool keep_mask,
                              __nv_bfloat16* save_h, uint32_t save_stride, uint32_t row_global, bool row_valid) {
@@ -292,8 +318,11 @@ __device__ bool forward_tile(char* sm, Shared& sh, uint32_t& phase, uint32_t* ma
 }
 
 // Mixture parameters and loss gradient at the outputs (the oracle's
-// loss_grad_out in float).
-__device__ void out_grad(const float* o, const float* w, float weight, float* g, float& loss) {
+// loss_grad_out in float): the loss is -weight * log q with q the vertex's
+// sampling density alpha p_guide + (1 - alpha) p_bsdf, alpha = amax *
+// sigmoid(o[40]); pb < 0 (no BSDF density recorded): q = p_guide and the
+// selection logit gets no gradient.
+__device__ void out_grad(const float* o, const float* w, float weight, float pb, float amax, float* g, float& loss) {
   float mx = -INFINITY;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) mx = fmaxf(mx, o[5 * k + 4]);
@@ -325,13 +354,22 @@ __device__ void out_grad(const float* o, const float* w, float weight, float* g,
     v[k] = c * expf(kap[k] * (d - 1.f));
     p += pi[k] * v[k];
   }
-  p = fmaxf(p, 1e-30f);
-  loss = -weight * logf(p);
+  float q = p, a = 1.f;
+  g[40] = 0.f;
+  if (pb >= 0.f) {
+    const float sg = 1.f / (1.f + expf(-o[40]));
+    a = amax * sg;
+    q = fmaxf(a * p + (1.f - a) * pb, 1e-30f);
+    g[40] = -weight * (p - pb) / q * (amax * sg * (1.f - sg));
+  }
+  q = fmaxf(q, 1e-30f);
+  loss = -weight * logf(q);
+  const float share = a * p / q;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) {
-    const float rr = pi[k] * v[k] / p;
+    const float rr = a * pi[k] * v[k] / q;
     const float d = mu[k][0] * w[0] + mu[k][1] * w[1] + mu[k][2] * w[2];
-    g[5 * k + 4] = -weight * (rr - pi[k]);
+    g[5 * k + 4] = -weight * (rr - share * pi[k]);
     const float dl = 1.f / kap[k] - 2.f / expm1f(2.f * kap[k]) + (d - 1.f);
     g[5 * k + 3] = cl[k] ? 0.f : -weight * rr * dl * sig[k];
     for (int c = 0; c < 3; ++c) g[5 * k + c] = -weight * rr * kap[k] * (w[c] - d * mu[k][c]) / rn[k];
@@ -451,9 +489,11 @@ __global__ void __launch_bounds__(256) k_guide_infer(GuideRows in, const __nv_bf
     tmem_ld48(tmem + lane_base, o);
     fence_before();
     if (valid) {
-      float4* dst = reinterpret_cast<float4*>(out + (size_t)row * 40);
+      // 44 floats per row (41 outputs; columns 41..43 of the padded layer are 0)
+      float4* dst = reinterpret_cast<float4*>(out + (size_t)row * kGuideOutStride);
 #pragma unroll
-      for (int k = 0; k < 10; ++k) dst[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+      for (int k = 0; k < kGuideOutStride / 4; ++k)
+        dst[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
     }
   }
   // a group that stopped early waits (bounded) for its MMAs still in flight
@@ -525,14 +565,15 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideTrain tr, const __nv_b
 #pragma unroll
     for (int q = 0; q < 3; ++q) tmem_ld16(sh.tmem + lane_base + 16 * q, o + 16 * q);
     float g[48];
-    for (int k = 40; k < 48; ++k) g[k] = 0.f;
+    for (int k = kGuideOut; k < 48; ++k) g[k] = 0.f;
     if (valid) {
       float loss;
-      out_grad(o, om, weight, g, loss);
+      const float pb = tr.pb ? tr.pb[row * tr.rows.rstride] : -1.0f;
+      out_grad(o, om, weight, pb, tr.amax, g, loss);
       loss_acc += loss;
       w_acc += weight;
     } else {
-      for (int k = 0; k < 40; ++k) g[k] = 0.f;
+      for (int k = 0; k < kGuideOut; ++k) g[k] = 0.f;
     }
     fence_before();
     put_row(sm + kSA0, r, 48, g);  // dY, K = 48
@@ -596,7 +637,7 @@ __global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, 
   if (n_dev) n = *n_dev < n ? *n_dev : n;
   const int l = blockIdx.y;
   // layer l: output deltas at row dz0 (M of them), inputs at row in0 (N)
-  const uint32_t M = l == 4 ? 40u : 64u;
+  const uint32_t M = l == 4 ? (uint32_t)kGuideOut : 64u;
   const uint32_t N = l == 0 ? 80u : 64u;
   const uint32_t dz0 = l == 4 ? 336u : 384u + 64u * (3u - (uint32_t)l);
   const uint32_t in0 = l == 0 ? 0u : 80u + 64u * (uint32_t)(l - 1);
@@ -786,6 +827,8 @@ int gfail(vmr_ctx* ctx, int code, const std::string& msg) {
 using vmr::guide::GuideAdam;
 using vmr::guide::GuideRows;
 using vmr::guide::GuideTrain;
+using vmr::guide::kGuideOut;
+using vmr::guide::kGuideOutStride;
 using vmr::guide::kGuideWeights;
 
 int guide_alloc(vmr_ctx* ctx) {
@@ -830,11 +873,13 @@ int guide_check(vmr_ctx* ctx) {
   return VMR_OK;
 }
 
-// Host n x 3 arrays -> device SoA rows in the context's staging buffer.
+// Host n x 3 arrays -> device SoA rows in the context's staging buffer
+// (omega, weight and pb optional), followed by extra_out floats of room.
 int stage_rows(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
-               const float* weight, size_t n, const float lo[3], const float hi[3], GuideTrain& tr, size_t extra_out) {
+               const float* weight, const float* pb, size_t n, const float lo[3], const float hi[3], GuideTrain& tr,
+               size_t extra_out) {
   auto& G = ctx->guide;
-  const size_t cols = 9 + (omega ? 3 : 0) + (weight ? 1 : 0);
+  const size_t cols = 9 + (omega ? 3 : 0) + (weight ? 1 : 0) + (pb ? 1 : 0);
   GCUDA(G.io.ensure((cols * n + extra_out) * sizeof(float) + 256));
   std::vector<float> h(cols * n);
   for (size_t i = 0; i < n; ++i)
@@ -844,8 +889,15 @@ int stage_rows(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo
       h[(6 + c) * n + i] = wo[3 * i + c];
       if (omega) h[(9 + c) * n + i] = omega[3 * i + c];
     }
-  if (weight)
-    for (size_t i = 0; i < n; ++i) h[(cols - 1) * n + i] = weight[i];
+  size_t col = omega ? 12 : 9;
+  const size_t wcol = col;
+  if (weight) {
+    for (size_t i = 0; i < n; ++i) h[col * n + i] = weight[i];
+    ++col;
+  }
+  const size_t pcol = col;
+  if (pb)
+    for (size_t i = 0; i < n; ++i) h[col * n + i] = pb[i];
   float* d = G.io.as<float>();
   GCUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   GCUDA(cudaStreamSynchronize(ctx->stream));  // h goes out of scope
@@ -862,7 +914,8 @@ int stage_rows(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo
   if (omega) {
     tr.ox = d + 9 * n; tr.oy = d + 10 * n; tr.oz = d + 11 * n;
   }
-  if (weight) tr.weight = d + (cols - 1) * n;
+  if (weight) tr.weight = d + wcol * n;
+  tr.pb = pb ? d + pcol * n : nullptr;
   tr.stride = (uint32_t)n;
   return VMR_OK;
 }
@@ -950,7 +1003,7 @@ int vmr_guide_init(vmr_ctx* ctx, uint64_t seed) {
   int rc = guide_alloc(ctx);
   if (rc) return rc;
   std::vector<float> w(kGuideWeights);
-  const int off[6] = {0, 5120, 9216, 13312, 17408, 19968};
+  const int off[6] = {0, 5120, 9216, 13312, 17408, kGuideWeights};
   const int kin[5] = {80, 64, 64, 64, 64};
   for (int l = 0; l < 5; ++l) {
     const float bound = std::sqrt(6.0f / (float)kin[l]) * (l == 4 ? 0.1f : 1.0f);
@@ -999,26 +1052,38 @@ int vmr_guide_forward(vmr_ctx* ctx, const float* pos, const float* nrm, const fl
   if (n == 0) return VMR_OK;
   cudaSetDevice(ctx->device);
   GuideTrain tr{};
-  rc = stage_rows(ctx, pos, nrm, wo, nullptr, nullptr, n, lo, hi, tr, n * 40);
+  // the outputs follow the 9 input columns: 9n floats, a multiple of 16 bytes
+  // when the row count is (padded below)
+  const size_t n4 = (n + 3) / 4 * 4;
+  rc = stage_rows(ctx, pos, nrm, wo, nullptr, nullptr, nullptr, n, lo, hi, tr, 9 * (n4 - n) + n * kGuideOutStride);
   if (rc) return rc;
-  float* dout = ctx->guide.io.as<float>() + 9 * n;
+  float* dout = ctx->guide.io.as<float>() + 9 * n4;
   const uint64_t tiles = (n + 127) / 128;
   const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)guide_sms(ctx) * 2);
   if (vmr::guide::launch_infer(tr.rows, ctx->guide.wf.p, dout, ctx->guide.err.as<int>(), grid, ctx->stream) != 0)
     return gfail(ctx, VMR_ERR_CUDA, "guide inference launch failed");
-  GCUDA(cudaMemcpyAsync(out, dout, n * 40 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-  return guide_status(ctx);
+  std::vector<float> h(n * kGuideOutStride);
+  GCUDA(cudaMemcpyAsync(h.data(), dout, h.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  rc = guide_status(ctx);  // synchronises
+  if (rc) return rc;
+  for (size_t i = 0; i < n; ++i)
+    std::memcpy(out + i * kGuideOut, h.data() + i * kGuideOutStride, kGuideOut * sizeof(float));
+  return VMR_OK;
 }
 
 int vmr_guide_gradient(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
-                       const float* weight, size_t n, const float lo[3], const float hi[3], float* grad, float* loss) {
+                       const float* weight, const float* bsdf_pdf, float alpha_max, size_t n, const float lo[3],
+                       const float hi[3], float* grad, float* loss) {
   int rc = guide_check(ctx);
   if (rc) return rc;
   if (!pos || !nrm || !wo || !omega || !weight || !lo || !hi || !grad) return gfail(ctx, VMR_ERR_INVALID, "null argument");
   if (n == 0 || n > (1u << 24)) return gfail(ctx, VMR_ERR_INVALID, "n must be in [1, 2^24]");
   cudaSetDevice(ctx->device);
   GuideTrain tr{};
-  rc = stage_rows(ctx, pos, nrm, wo, omega, weight, n, lo, hi, tr, 0);
+  if (bsdf_pdf && !(alpha_max > 0.0f && alpha_max < 1.0f))
+    return gfail(ctx, VMR_ERR_INVALID, "alpha_max must be in (0, 1)");
+  rc = stage_rows(ctx, pos, nrm, wo, omega, weight, bsdf_pdf, n, lo, hi, tr, 0);
+  tr.amax = alpha_max;
   if (rc) return rc;
   GCUDA(cudaMemsetAsync(ctx->guide.grad.p, 0, kGuideWeights * sizeof(float), ctx->stream));
   rc = guide_backprop(ctx, tr, n);
@@ -1034,15 +1099,18 @@ int vmr_guide_gradient(vmr_ctx* ctx, const float* pos, const float* nrm, const f
 }
 
 int vmr_guide_train_step(vmr_ctx* ctx, const float* pos, const float* nrm, const float* wo, const float* omega,
-                         const float* weight, size_t n, const float lo[3], const float hi[3], const vmr_adam* opt,
-                         float* loss) {
+                         const float* weight, const float* bsdf_pdf, float alpha_max, size_t n, const float lo[3],
+                         const float hi[3], const vmr_adam* opt, float* loss) {
   int rc = guide_check(ctx);
   if (rc) return rc;
   if (!pos || !nrm || !wo || !omega || !weight || !lo || !hi || !opt) return gfail(ctx, VMR_ERR_INVALID, "null argument");
   if (n == 0 || n > (1u << 24)) return gfail(ctx, VMR_ERR_INVALID, "n must be in [1, 2^24]");
   cudaSetDevice(ctx->device);
   GuideTrain tr{};
-  rc = stage_rows(ctx, pos, nrm, wo, omega, weight, n, lo, hi, tr, 0);
+  if (bsdf_pdf && !(alpha_max > 0.0f && alpha_max < 1.0f))
+    return gfail(ctx, VMR_ERR_INVALID, "alpha_max must be in (0, 1)");
+  rc = stage_rows(ctx, pos, nrm, wo, omega, weight, bsdf_pdf, n, lo, hi, tr, 0);
+  tr.amax = alpha_max;
   if (rc) return rc;
   rc = guide_backprop(ctx, tr, n);
   if (rc) return rc;

@@ -8,7 +8,9 @@
 namespace vmr {
 namespace guide {
 
-constexpr int kGuideWeights = 19968;  // W0 64x80, W1..W3 64x64, W4 40x64
+constexpr int kGuideWeights = 20032;  // W0 64x80, W1..W3 64x64, W4 41x64
+constexpr int kGuideOut = 41;        // 8 lobes x 5, then the selection logit
+constexpr int kGuideOutStride = 44;  // floats per row of an inference output
 constexpr uint32_t kSaveRows = 640;   // feature-major rows saved per training record
 
 // Path vertices (SoA, device pointers): hit point, shading normal, direction
@@ -24,10 +26,15 @@ struct GuideRows {
 };
 
 // Training records: the rows plus the sampled direction and its weight
-// (incident radiance over the density it was sampled with).
+// (incident radiance over the density it was sampled with), and optionally
+// the BSDF's density of that direction: with it the loss is that of the
+// vertex's full sampling density alpha p_guide + (1 - alpha) p_bsdf, alpha =
+// amax * sigmoid(selection logit), which also trains the selection.
 struct GuideTrain {
   GuideRows rows;
   const float *ox, *oy, *oz, *weight;
+  const float* pb;  // nullptr: the guide's own density
+  float amax;
   uint32_t stride;  // rows of the save buffer's feature-major arrays
 };
 

@@ -121,11 +121,15 @@ struct PtBatch {
   float* fb;
   double* fb64;
   // path guiding
-  float alpha;                 // probability of sampling the guide at a vertex
+  float alpha;                 // learned selection: the largest probability of
+                               // sampling the guide at a vertex (alpha_max);
+                               // fixed selection: that probability itself
+  uint32_t learn_sel;          // 1: each vertex's probability is alpha_max *
+                               // sigmoid(the network's selection output)
   uint32_t gdepth;             // guided vertices: the first gdepth of a path (host side)
   float glo[3];                // scene bounds for the guide's inputs
   float* grow;                 // 9 * cap: guide input rows per queue entry
-  float* gout;                 // 40 * cap: guide outputs per queue entry
+  float* gout;                 // 44 * cap: guide outputs per queue entry
   float* rec;                  // kRecCols * rcap training records (SoA)
   uint32_t rcap;
   unsigned long long* rcount;  // [2]: records this batch, records in total
@@ -134,16 +138,19 @@ struct PtBatch {
   const PtJob* jobs;
   uint32_t n_jobs;
   uint32_t* pgeom;             // cap: path -> its job's geom
-  float* snee;                 // 7 * cap: per shadow slot, the vertex's normal and
-                               // direction toward the previous vertex, and the
+  float* snee;                 // 8 * cap: per shadow slot, the vertex's normal and
+                               // direction toward the previous vertex, the
                                // light sample's training weight (0: no record)
+                               // and the BSDF's density of its direction
 };
 
 // Training record columns: vertex (p, n, wo), sampled direction, weight
 // (filled after the bounce loop), density, throughput after the vertex,
-// radiance before the next vertex, path.
-constexpr int kRecCols = 21;
-enum RecCol { kRP = 0, kRN = 3, kRWo = 6, kROm = 9, kRW = 12, kRQ = 13, kRBeta = 14, kRMark = 17, kRPath = 20 };
+// radiance before the next vertex, path, the BSDF's density of the direction.
+constexpr int kRecCols = 22;
+enum RecCol {
+  kRP = 0, kRN = 3, kRWo = 6, kROm = 9, kRW = 12, kRQ = 13, kRBeta = 14, kRMark = 17, kRPath = 20, kRPb = 21
+};
 constexpr uint32_t kNoPath = 0xffffffffu;  // path column of a light-sample record
 
 // ------------------------------------------------------------- random ----
@@ -311,13 +318,17 @@ __device__ __forceinline__ void put_ray(float* q, uint32_t cap, uint64_t i, cons
 }
 
 // ------------------------------------------------------- guide mixture ---
-// The 40 network outputs as 8 vMF lobes (the same decoding the trainer
+// The network outputs 0..39 as 8 vMF lobes (the same decoding the trainer
 // differentiates): mu = normalize, kappa = min(softplus + 0.01, 1000),
-// pi = softmax; c = kappa / (2 pi (1 - exp(-2 kappa))).
+// pi = softmax; c = kappa / (2 pi (1 - exp(-2 kappa))).  Output 40 is the
+// selection logit: with learned selection the vertex samples the guide with
+// probability alpha = alpha_max * sigmoid(o[40]), else with alpha_max.
 struct GMix {
   float mu[8][3], kap[8], c[8], pi[8];
+  float alpha;
 };
-__device__ void gmix_decode(const float* o, GMix& g) {
+__device__ void gmix_decode(const float* o, float amax, bool learned, GMix& g) {
+  g.alpha = learned ? amax / (1.f + expf(-o[40])) : amax;
   float mx = -INFINITY;
   for (int k = 0; k < 8; ++k) mx = fmaxf(mx, o[5 * k + 4]);
   float z = 0.f;
@@ -460,8 +471,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
     float stmax = 0.f, time = 0.f;
     bool want_rec = false;
     V3 rP = v3(0, 0, 0), rN = v3(0, 0, 0), rWi = v3(0, 0, 0);
-    float rQ = 0.f;
-    float nee_w = 0.f;  // TRAIN: the light sample's record weight
+    float rQ = 0.f, rPb = 0.f;
+    float nee_w = 0.f, nee_pb = 0.f;  // TRAIN: the light sample's record weight, BSDF density
     if (active) {
       p = qp[i];
       const V3 D = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
@@ -526,7 +537,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
             const int nL = (int)b.nl;
             const bool guided = GUIDED && (m.dw > 0.0f || !m.mirror);
             GMix gm;
-            if (guided) gmix_decode(b.gout + i * 40, gm);
+            if (guided) gmix_decode(b.gout + i * guide::kGuideOutStride, b.alpha, b.learn_sel != 0, gm);
             // ---- next-event estimation
             if (nL > 0 && (m.dw > 0.0f || !m.mirror)) {
               const float u = rnd(key, base + 0);
@@ -565,8 +576,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
               if (ok && dot(Ld, sc.Ng) > 0.0f && dot(Ld, sc.N) > 0.0f && pl > 0.0f && !isinf(pl)) {
                 const V3 wol = project(Ut, Vt, sc.N, Ld);
                 const V3 f = bsdf_f(m, wil, wol);
-                float pb = bsdf_pdf_pt(m, wil, wol);
-                if (guided) pb = b.alpha * gmix_pdf(gm, Ld) + (1.0f - b.alpha) * pb;
+                const float pbs = bsdf_pdf_pt(m, wil, wol);
+                const float pb = guided ? gm.alpha * gmix_pdf(gm, Ld) + (1.0f - gm.alpha) * pbs : pbs;
                 const float w = power_w(pl, pb);
                 const float k = w / pl;
                 const V3 c = v3(beta.x * f.x * l.Le[0] * k, beta.y * f.y * l.Le[1] * k, beta.z * f.z * l.Le[2] * k);
@@ -593,6 +604,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
                     nee_w = isfinite(wt) ? fminf(wt, 1e4f) : 0.f;
                     rN = sc.N;
                     rWi = wi;
+                    nee_pb = pbs;
                   }
                 }
               }
@@ -602,7 +614,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
             const float r0 = rnd(key, base + 4), r1 = rnd(key, base + 5);
             V3 wol, wo;
             bool delta = false;
-            const bool from_guide = guided && rnd(key, base + 7) < b.alpha;
+            const bool from_guide = guided && rnd(key, base + 7) < gm.alpha;
             if (from_guide) {
               wo = gmix_sample(gm, ul, r0, r1);
               wol = project(Ut, Vt, sc.N, wo);
@@ -631,13 +643,14 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
                 const RGB F = fresnel_kr(m.fr, wil.z);
                 beta = v3(beta.x * (m.cs.x * F.c[0]), beta.y * (m.cs.y * F.c[1]), beta.z * (m.cs.z * F.c[2]));
                 if (guided) {  // the mirror lobe is taken with probability (1-alpha)*sw
-                  const float inv = 1.0f / (1.0f - b.alpha);
+                  const float inv = 1.0f / (1.0f - gm.alpha);
                   beta = v3(beta.x * inv, beta.y * inv, beta.z * inv);
                 }
               } else {
                 const V3 f = bsdf_f(m, wil, wol);
                 pb = bsdf_pdf_pt(m, wil, wol);
-                if (guided) pb = b.alpha * gmix_pdf(gm, wo) + (1.0f - b.alpha) * pb;
+                rPb = pb;
+                if (guided) pb = gm.alpha * gmix_pdf(gm, wo) + (1.0f - gm.alpha) * pb;
                 if (!(pb > 0.0f)) alive = false;
                 else beta = v3(beta.x * (f.x / pb), beta.y * (f.y / pb), beta.z * (f.z / pb));
               }
@@ -685,6 +698,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
         b.snee[si] = rN.x; b.snee[c + si] = rN.y; b.snee[2 * c + si] = rN.z;
         b.snee[3 * c + si] = rWi.x; b.snee[4 * c + si] = rWi.y; b.snee[5 * c + si] = rWi.z;
         b.snee[6 * c + si] = nee_w;
+        b.snee[7 * c + si] = nee_pb;
       }
     }
     const unsigned long long ni = warp_append(&b.qlen[d + 1], want_next);
@@ -701,6 +715,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
                              b.bx[p], b.by[p], b.bz[p], 0.f, 0.f, 0.f};
         for (int k = 0; k < 20; ++k) R[(size_t)k * c + ri] = v[k];
         R[(size_t)kRPath * c + ri] = __uint_as_float(p);
+        R[(size_t)kRPb * c + ri] = rPb;
         b.last_rec[p] = (uint32_t)ri;
       }
     }
@@ -779,6 +794,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_resolve(PtBatch b, uint32_t d) 
         const size_t rc = b.rcap;
         for (int k = 0; k < 13; ++k) R[(size_t)k * rc + ri] = v[k];
         R[(size_t)kRPath * rc + ri] = __uint_as_float(kNoPath);
+        R[(size_t)kRPb * rc + ri] = b.snee[7 * c + i];
       }
     }
   }
@@ -1108,7 +1124,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     if (rc != VMR_OK) return rc;
     guide::prepare_kernels();
   }
-  const float alpha = p->guide_fraction > 0.0f ? p->guide_fraction : 0.5f;
+  const bool learn_sel = !(p->flags & VMR_PATH_FIXED_SELECTION);
+  const float alpha = p->guide_fraction > 0.0f ? p->guide_fraction : (learn_sel ? 0.9f : 0.5f);
   if (guided && !(alpha < 1.0f)) return pfail(ctx, VMR_ERR_INVALID, "guide_fraction must be below 1");
   // continuation and light-sample records: at most two per vertex
   const uint64_t rcap = train ? std::min<uint64_t>(2 * cap * std::max<uint32_t>(1, p->max_depth), 0xffffffffull) : 0;
@@ -1136,8 +1153,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
                o_light = carve(std::max<size_t>(1, lights.size()) * sizeof(PtLight)),
                o_shader = carve(std::max<size_t>(1, R.shaders.size()) * sizeof(vmr_shader_std)),
                o_log = carve(log.size() * 4), o_grow = carve(guided ? cap * 9 * 4 : 0),
-               o_gout = carve(guided ? cap * 40 * 4 : 0), o_rec = carve(rcap * kRecCols * 4),
-               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32), o_snee = carve(train ? cap * 7 * 4 : 0),
+               o_gout = carve(guided ? cap * guide::kGuideOutStride * 4 : 0), o_rec = carve(rcap * kRecCols * 4),
+               o_last = carve(train ? cap * 4 : 0), o_rcnt = carve(32), o_snee = carve(train ? cap * 8 * 4 : 0),
                o_jobs = carve(jobs ? n_jobs * sizeof(PtJob) : 0), o_pgeom = carve(jobs ? cap * 4 : 0);
   // queue reordering (not for jobs: a key-ordered queue would mix the jobs'
   // meshes inside a warp)
@@ -1233,6 +1250,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   DScratch* scr = reinterpret_cast<DScratch*>(base + o_scr);
   b.scr = scr;
   b.alpha = alpha;
+  b.learn_sel = learn_sel ? 1u : 0u;
   b.gdepth = p->guide_depth ? p->guide_depth : 0xffffffffu;
   std::memcpy(b.glo, glo, 12);
   b.grow = guided ? reinterpret_cast<float*>(base + o_grow) : nullptr;
@@ -1331,6 +1349,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     const uint64_t nj = b.n_jobs;
     fold(&nj, sizeof(nj));
     fold(&b.alpha, sizeof(b.alpha));
+    fold(&b.learn_sel, sizeof(b.learn_sel));
     fold(&b.gdepth, sizeof(b.gdepth));
     fold(b.glo, sizeof(b.glo));
     fold(grows.inv_ext, sizeof(grows.inv_ext));
@@ -1390,6 +1409,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
         tr.rows.rstride = tsteps;
         tr.ox = R + kROm * c + off; tr.oy = R + (kROm + 1) * c + off; tr.oz = R + (kROm + 2) * c + off;
         tr.weight = R + kRW * c + off;
+        tr.pb = learn_sel ? R + kRPb * c + off : nullptr;
+        tr.amax = alpha;
         tr.stride = stride;
         if (off >= rcap) break;
         PCUDA(cudaMemsetAsync(G.sums.p, 0, 16, st));
