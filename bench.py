@@ -424,6 +424,89 @@ def _median_rel(a, ref):
     return float(np.median((a - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
+# The guided arm's configuration on the slit-light room (see guided_slit).
+GUIDE = dict(depth=2, alpha_max=0.9, lr=1e-2, train_batches=96, train_steps=32, batch_spp=8)
+
+
+def guided_slit(ctx, width=1024, plain_spp=256):
+    """Equal-time relMSE, guided against plain, on the slit-light room at
+    width x width: the 4096-spp float64 plain reference first (untimed), then
+    each arm in 8-spp batches with its relMSE after every batch (computed
+    outside the timed region) -> a relMSE-versus-wall-time curve per arm.
+    The plain arm runs plain_spp samples; the guided arm trains online on
+    one-sample batches (GUIDE), then renders with the frozen guide until it
+    has used the plain arm's wall time.  guided_time_to_plain_relmse: the
+    guided arm's time to reach the plain arm's final relMSE over the plain
+    arm's time (null if it does not within that time); plain_time_to_guided
+    : the plain time that reaches the guided arm's final relMSE, by
+    interpolating the plain curve (relMSE ~ 1/spp beyond its end)."""
+    from vermeer_gb300 import scenes
+    W = H = width
+    sc = scenes.slit_room(200_000, width=W, height=H)
+    ctx.load_scene(sc)
+    t0 = time.perf_counter()
+    ref = np.zeros((H, W, 3), np.float64)
+    for k in range(16):
+        ctx.render_path(W, H, 256 * k, 256, 99, max_depth=8, fb64=ref)
+    t_ref = time.perf_counter() - t0
+    ctx.render_path(W, H, 0, 4, 1, max_depth=8)  # warm the graphs
+    bs = GUIDE["batch_spp"]
+
+    def curve_point(img, t, spp):
+        return {"spp": spp, "wall_s": round(t, 4), "relmse": round(_relmse(img, ref), 5),
+                "median_rel_sq_err": round(_median_rel(img, ref), 6)}
+
+    plain = np.zeros((H, W, 3), np.float32)
+    tp, pc = 0.0, []
+    for k in range(plain_spp // bs):
+        t0 = time.perf_counter()
+        plain, _ = ctx.render_path(W, H, bs * k, bs, 1, max_depth=8, fb=plain)
+        tp += time.perf_counter() - t0
+        pc.append(curve_point(plain, tp, bs * (k + 1)))
+    # guided: warm its graphs (untimed), then train and render from scratch
+    kw = dict(max_depth=8, guided=True, guide_fraction=GUIDE["alpha_max"], guide_depth=GUIDE["depth"])
+    ctx.guide_init(7)
+    ctx.render_path(W, H, 0, 1, 2, train=True, train_steps=1, **kw)
+    ctx.render_path(W, H, 0, 1, 2, **kw)
+    ctx.guide_init(7)
+    g = np.zeros((H, W, 3), np.float32)
+    gc, spp, tg, t_train = [], 0, 0.0, 0.0
+    for k in range(GUIDE["train_batches"]):
+        t0 = time.perf_counter()
+        g, _ = ctx.render_path(W, H, spp, 1, 1, fb=g, train=True, train_steps=GUIDE["train_steps"],
+                               train_batch=65536, train_lr=GUIDE["lr"], **kw)
+        tg += time.perf_counter() - t0
+        spp += 1
+    t_train = tg
+    gc.append(curve_point(g, tg, spp))
+    while tg < tp:
+        t0 = time.perf_counter()
+        g, _ = ctx.render_path(W, H, spp, bs, 1, fb=g, **kw)
+        tg += time.perf_counter() - t0
+        spp += bs
+        gc.append(curve_point(g, tg, spp))
+    target = pc[-1]["relmse"]
+    t_hit = next((c["wall_s"] for c in gc if c["relmse"] <= target), None)
+    # plain time to the guided arm's final relMSE (relMSE ~ 1/time past the curve's end)
+    gfin = gc[-1]["relmse"]
+    hit = next((c["wall_s"] for c in pc if c["relmse"] <= gfin), None)
+    t_plain_eq = hit if hit is not None else tp * target / gfin
+    return {
+        "workload": f"slit-light room, 200,000 diffuse triangles, {W}x{H}, depth 8; plain {plain_spp} spp in "
+                    f"{bs}-spp batches vs the guided tracer for the same wall time: online training on "
+                    f"{GUIDE['train_batches']} one-sample batches ({GUIDE['train_steps']} Adam steps of up to "
+                    f"65,536 records each, learning rate {GUIDE['lr']}), then the frozen guide in {bs}-spp batches; "
+                    f"the first {GUIDE['depth']} vertices of each path guided, learned selection probability "
+                    f"(at most {GUIDE['alpha_max']}); every image keeps all its samples; relMSE = mean over pixels "
+                    "and channels of (a - r)^2 / (r^2 + 0.01) against the 4096-spp float64 plain render",
+        "reference_spp": 4096, "reference_render_s": round(t_ref, 2),
+        "plain": pc[-1], "guided": dict(gc[-1], train_s=round(t_train, 3)),
+        "guided_time_to_plain_relmse": None if t_hit is None else round(t_hit / tp, 3),
+        "plain_time_to_guided_relmse_over_guided_time": round(t_plain_eq / tg, 3),
+        "curve": {"plain": pc, "guided": gc},
+    }
+
+
 def render_extras(ctx, args):
     """The render configurations, measured on the same GPU after the
     headline (each on its own seeded synthetic scene):
@@ -442,10 +525,9 @@ def render_extras(ctx, args):
                              256x256, 32 spp, depth 5, against one render
                              call per job
       guided_slit            equal-wall-time relMSE (mean and median over
-                             pixels) on the slit-light room against a
-                             4096-spp float64 plain render, at 512x512
-                             instead of 1024x1024 so that the reference
-                             render fits the benchmark's time
+                             pixels) on the slit-light room at 1024x1024
+                             against a 4096-spp float64 plain render, with a
+                             relMSE-versus-wall-time curve for each arm
       qbvh_build             the 2,097,152-triangle QBVH build (BuildAccel,
                              leafMax 16) by the device builder and by the host
                              builder, with the oracle's single-threaded
@@ -624,56 +706,7 @@ def render_extras(ctx, args):
                      "device_ms": round(jst["ms"], 2), "wall_s": round(jwall, 3)},
         "per_job_calls": {"samples_per_s": round(n_samp / (sep_ms / 1e3), 1), "device_ms": round(sep_ms, 2),
                           "wall_s": round(sep_wall, 3)}}
-    # guided vs plain, equal wall time
-    W = H = 512
-    sc = scenes.slit_room(200_000, width=W, height=H)
-    ctx.load_scene(sc)
-    ref = np.zeros((H, W, 3), np.float64)
-    for k in range(16):
-        ctx.render_path(W, H, 256 * k, 256, 99, max_depth=8, fb64=ref)
-    ctx.render_path(W, H, 0, 4, 1, max_depth=8)
-    plain = np.zeros((H, W, 3), np.float32)
-    tp = 0.0
-    for k in range(32):
-        t0 = time.perf_counter()
-        plain, _ = ctx.render_path(W, H, 8 * k, 8, 1, max_depth=8, fb=plain)
-        tp += time.perf_counter() - t0
-    GD = 1  # guide the first vertex of each path (the others sample the BSDF alone)
-    ctx.guide_init(7)
-    ctx.render_path(W, H, 0, 1, 2, max_depth=8, guided=True, train=True, guide_fraction=0.5, train_steps=1,
-                    guide_depth=GD)
-    ctx.render_path(W, H, 0, 1, 2, max_depth=8, guided=True, guide_fraction=0.2, guide_depth=GD)
-    ctx.guide_init(7)
-    g = np.zeros((H, W, 3), np.float32)
-    spp, tg, t_hit, k = 0, 0.0, None, 0
-    while tg < tp:
-        train = k < 24  # training phase: 24 one-sample batches of 32 Adam steps, then the frozen guide
-        n = 1 if train else 8
-        t0 = time.perf_counter()
-        g, gst = ctx.render_path(W, H, spp, n, 1, max_depth=8, fb=g, guided=True, train=train,
-                                 guide_fraction=0.5 if train else 0.2, train_steps=32, train_batch=65536,
-                                 train_lr=3e-3, guide_depth=GD)
-        tg += time.perf_counter() - t0
-        spp += n
-        k += 1
-        if t_hit is None and not train and _relmse(g, ref) <= _relmse(plain, ref):
-            t_hit = tg
-    # per sample: the trained guide at the plain arm's 256 spp (untimed)
-    g256, _ = ctx.render_path(W, H, 0, 256, 11, max_depth=8, guided=True, guide_fraction=0.2, guide_depth=GD)
-    out["guided_slit"] = {
-        "workload": "slit-light room, 200,000 diffuse triangles, 512x512 (not 1024x1024: the 4096-spp float64 "
-                    "reference at 1024x1024 alone would take about 90 s), depth 8; plain 256 spp vs guided "
-                    "for the same wall time: online training on 24 one-sample batches (guide fraction 0.5, "
-                    "32 Adam steps of up to 65,536 continuation and light-sample records each), then the frozen "
-                    "guide at fraction 0.2 in 8-spp batches; the guide samples the first vertex of each path "
-                    "(guide_depth 1); both images keep every sample",
-        "plain": {"spp": 256, "wall_s": round(tp, 4), "relmse": round(_relmse(plain, ref), 5),
-                  "median_rel_sq_err": round(_median_rel(plain, ref), 6)},
-        "guided": {"spp": spp, "wall_s": round(tg, 4), "relmse": round(_relmse(g, ref), 5),
-                   "median_rel_sq_err": round(_median_rel(g, ref), 6)},
-        "guided_time_to_plain_relmse": None if t_hit is None else round(t_hit / tp, 3),
-        "guided_256spp": {"relmse": round(_relmse(g256, ref), 5), "median_rel_sq_err": round(_median_rel(g256, ref), 6)},
-        "reference_spp": 4096}
+    out["guided_slit"] = guided_slit(ctx)
     return out
 
 

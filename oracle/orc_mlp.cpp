@@ -15,20 +15,24 @@
 // shading normal at 72..74; the direction toward the previous vertex at
 // 75..77; 1 at 78; 0 at 79.
 //
-// Lobe k: mu = normalize(o[5k..5k+2]), kappa = min(softplus(o[5k+3]) + 0.01,
-// 1000), pi = softmax over o[5k+4]; vMF density
-// kappa / (2 pi (1 - exp(-2 kappa))) * exp(kappa (mu.w - 1)).  The vertex
-// samples the guide with probability alpha = amax * sigmoid(o[40]) and its
-// BSDF otherwise, so its sampling density is q = alpha p_guide + (1 - alpha)
-// p_bsdf.
+// Lobe k: mu = normalize(o[5k..5k+2]), kappa = exp(o[5k+3]) with the
+// exponent clamped to [-4.6, 6.9] (kappa in [0.01, 992]), pi = softmax over
+// o[5k+4]; vMF density kappa / (2 pi (1 - exp(-2 kappa))) * exp(kappa
+// (mu.w - 1)).  The vertex samples the guide with probability alpha = amax *
+// sigmoid(o[40]) and its BSDF otherwise, so its sampling density is q =
+// alpha p_guide + (1 - alpha) p_bsdf.
 //
-// Training loss of a batch: sum_i -weight_i * log q(omega_i), where omega_i
-// is a direction the tracer sampled at the vertex, weight_i its incident
-// radiance (luminance) x |cos| over the density it was sampled with, and
-// p_bsdf(omega_i) is recorded with it; without a recorded BSDF density the
-// loss is -weight_i * log p_guide(omega_i) and s gets no gradient.  The
-// gradient is analytic (the selection, the mixture, the lobe parameters,
-// back through the ReLU layers).
+// Training, per record (omega_i: a direction the tracer sampled at the
+// vertex; weight_i: its incident radiance (luminance) x |cos| over the
+// density it was sampled with): the lobes descend -weight_i * log
+// p_guide(omega_i), the guide's own fit to the product; with the BSDF's
+// density p_bsdf(omega_i) recorded, the selection logit descends -weight_i *
+// log q(omega_i) with p_guide held fixed (the best mixing weight for the
+// current guide; the lobes do not see alpha, so a small alpha does not stop
+// them from learning).  The reported loss is the sum of -weight_i * log q
+// (of -weight_i * log p_guide without BSDF densities).  The gradients are
+// analytic (the selection, the mixture, the lobe parameters, back through
+// the ReLU layers).
 //
 // Precision modes: 64 and 32 compute everything in that type; 16 mirrors
 // the CUDA kernels' tensor-core arithmetic: weights, layer inputs and
@@ -105,9 +109,11 @@ void forward(const float* W, const double* feat, int mode, std::vector<std::vect
   }
 }
 
+const double kLogKapMin = -4.6, kLogKapMax = 6.9;  // kappa in [0.01, 992]
+
 template <class T>
 struct Lobes {
-  T mu[kLobes][3], rn[kLobes], kappa[kLobes], sig[kLobes], pi[kLobes];
+  T mu[kLobes][3], rn[kLobes], kappa[kLobes], pi[kLobes];
   bool clamped[kLobes];
 };
 
@@ -123,12 +129,8 @@ void lobes(const T* o, Lobes<T>& L) {
     L.rn[k] = n;
     for (int c = 0; c < 3; ++c) L.mu[k][c] = r[c] / n;
     const T s = r[3];
-    const T sp = s > T(20) ? s : std::log1p(std::exp(s));  // softplus
-    T kap = sp + T(0.01);
-    L.clamped[k] = kap > T(1000);
-    if (L.clamped[k]) kap = T(1000);
-    L.kappa[k] = kap;
-    L.sig[k] = T(1) / (T(1) + std::exp(-s));
+    L.clamped[k] = s < T(kLogKapMin) || s > T(kLogKapMax);
+    L.kappa[k] = std::exp(std::min(std::max(s, T(kLogKapMin)), T(kLogKapMax)));
     L.pi[k] = std::exp(r[4] - mx);
     z += L.pi[k];
   }
@@ -151,7 +153,9 @@ T mixture_pdf(const Lobes<T>& L, const T* w) {
   return p;
 }
 
-// d(-weight * log q)/d(outputs); pb < 0: no BSDF density, q = p_guide.
+// Gradient at the outputs: lobes from -weight * log p_guide, the selection
+// logit from -weight * log q with p_guide fixed (pb < 0: no BSDF density,
+// no selection gradient); loss = -weight * log q (or log p_guide).
 template <class T>
 void loss_grad_out(const T* o, const T* w, T weight, T pb, T amax, T* g, T& loss) {
   Lobes<T> L;
@@ -162,24 +166,23 @@ void loss_grad_out(const T* o, const T* w, T weight, T pb, T amax, T* g, T& loss
     v[k] = vmf(L, k, w);
     p += L.pi[k] * v[k];
   }
-  // q, and a = dq/dp_guide (alpha, or 1 without the selection)
-  T q = p, a = T(1);
+  loss = -weight * std::log(p);
   g[40] = T(0);
   if (pb >= T(0)) {
     const T sg = T(1) / (T(1) + std::exp(-o[40]));
-    a = amax * sg;
-    q = a * p + (T(1) - a) * pb;
+    const T a = amax * sg;
+    const T q = a * p + (T(1) - a) * pb;
     g[40] = -weight * (p - pb) / q * (amax * sg * (T(1) - sg));
+    loss = -weight * std::log(q);
   }
-  loss = -weight * std::log(q);
-  const T sc = a * p / q;  // share of the guide in q
   for (int k = 0; k < kLobes; ++k) {
-    const T r = a * L.pi[k] * v[k] / q;  // responsibility of lobe k in q
+    const T r = L.pi[k] * v[k] / p;  // responsibility of lobe k
     const T d = L.mu[k][0] * w[0] + L.mu[k][1] * w[1] + L.mu[k][2] * w[2];
     const T kap = L.kappa[k];
-    g[5 * k + 4] = -weight * (r - sc * L.pi[k]);
+    g[5 * k + 4] = -weight * (r - L.pi[k]);
+    // d log v / d kappa, times d kappa / d s = kappa
     const T dlogv_dk = T(1) / kap - T(2) / std::expm1(T(2) * kap) + (d - T(1));
-    g[5 * k + 3] = L.clamped[k] ? T(0) : -weight * r * dlogv_dk * L.sig[k];
+    g[5 * k + 3] = L.clamped[k] ? T(0) : -weight * r * dlogv_dk * kap;
     for (int c = 0; c < 3; ++c) g[5 * k + c] = -weight * r * kap * (w[c] - d * L.mu[k][c]) / L.rn[k];
   }
 }

@@ -52,8 +52,12 @@ def _bsdf_pdf(nrm, om):
 
 @pytest.mark.parametrize("mixed", [False, True])
 def test_oracle_gradient_matches_finite_differences(orc, mixed):
-    """Without a BSDF density (the guide's own density) and with one (the
-    vertex's full sampling density, which also trains the selection logit)."""
+    """Without a BSDF density every weight descends the guide's own loss
+    -w log p_guide.  With one, the lobe outputs still do (the output layer's
+    lobe rows against finite differences of that loss), and the selection
+    row descends -w log q, q = alpha p_guide + (1 - alpha) p_bsdf (finite
+    differences of that loss; the hidden layers are checked against autograd
+    with p_guide held fixed in q)."""
     G = orc.Guide
     pos, nrm, wo, om, wt = _batch(5, 1)
     pb = _bsdf_pdf(nrm, om) if mixed else None
@@ -61,20 +65,22 @@ def test_oracle_gradient_matches_finite_differences(orc, mixed):
     W = _weights(2)
     _, g = G.loss_grad(W, f, om, wt, 64, bsdf_pdf=pb, amax=AMAX)
     rng = np.random.default_rng(3)
-    nz = np.nonzero(np.abs(g) > 1e-4)[0]
-    picks = list(rng.choice(nz, 10, replace=False))
     sel = np.arange(17408 + 40 * 64, NW)  # the selection logit's weights
+    lobe_rows = np.arange(17408, 17408 + 40 * 64)
+    pool = lobe_rows if mixed else np.arange(NW)
+    nz = pool[np.abs(g[pool]) > 1e-4]
+    checks = [(k, None) for k in rng.choice(nz, 10, replace=False)]
     if mixed:
-        picks += list(rng.choice(sel[np.abs(g[sel]) > 1e-5], 4, replace=False))
+        checks += [(k, pb) for k in rng.choice(sel[np.abs(g[sel]) > 1e-5], 4, replace=False)]
     else:
         assert not g[sel].any()
-    for k in picks:
+    for k, pbk in checks:
         h = np.float32(1e-3)
         Wp, Wm = W.copy(), W.copy()
         Wp[k] += h
         Wm[k] -= h
-        lp, _ = G.loss_grad(Wp, f, om, wt, 64, bsdf_pdf=pb, amax=AMAX)
-        lm, _ = G.loss_grad(Wm, f, om, wt, 64, bsdf_pdf=pb, amax=AMAX)
+        lp, _ = G.loss_grad(Wp, f, om, wt, 64, bsdf_pdf=pbk, amax=AMAX)
+        lm, _ = G.loss_grad(Wm, f, om, wt, 64, bsdf_pdf=pbk, amax=AMAX)
         fd = (lp - lm) / (float(Wp[k]) - float(Wm[k]))
         assert abs(fd - g[k]) <= 1e-5 + 1e-4 * abs(g[k]), (k, fd, g[k])
 
@@ -104,17 +110,22 @@ def test_oracle_matches_torch_autograd(orc, mixed):
     o = out[:, :40].reshape(-1, 8, 5)
     r = o[:, :, :3]
     mu = r / torch.clamp(r.norm(dim=2, keepdim=True), min=1e-6)
-    kap = torch.clamp(torch.nn.functional.softplus(o[:, :, 3]) + 0.01, max=1000.0)
+    kap = torch.exp(torch.clamp(o[:, :, 3], -4.6, 6.9))
     pi = torch.softmax(o[:, :, 4], dim=1)
     w = torch.tensor(om.astype(np.float64))
     d = (mu * w[:, None, :]).sum(2)
     c = kap / (2 * np.pi * (-torch.expm1(-2 * kap)))
     p = (pi * c * torch.exp(kap * (d - 1))).sum(1)
+    wtt = torch.tensor(wt.astype(np.float64))
+    loss = -(wtt * torch.log(p)).sum()
+    objective = loss
     if mixed:
+        # the selection descends the mixture's loss with p_guide held fixed
         a = AMAX * torch.sigmoid(out[:, 40])
-        p = a * p + (1 - a) * torch.tensor(pb.astype(np.float64))
-    loss = -(torch.tensor(wt.astype(np.float64)) * torch.log(p)).sum()
-    loss.backward()
+        pbt = torch.tensor(pb.astype(np.float64))
+        loss = -(wtt * torch.log(a * p + (1 - a) * pbt)).sum()
+        objective = objective - (wtt * torch.log(a * p.detach() + (1 - a) * pbt)).sum()
+    objective.backward()
     assert abs(loss.item() - loss_o) <= 1e-9 * abs(loss_o)
     assert np.allclose(Wt.grad.numpy(), g_o, rtol=1e-7, atol=1e-10)
 

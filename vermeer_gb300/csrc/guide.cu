@@ -2,24 +2,25 @@
 //
 // No reference counterpart.  The network (80 inputs, 4 hidden ReLU layers
 // of 64, 41 outputs = 8 vMF lobes and the selection logit; no biases, input
-// 78 is the constant 1)
-// runs fused per tile of 128 rows: a group of 128 threads works on a tile
-// with the bf16 weights in shared memory (inference: two groups per CTA
-// share one copy), thread r owns row r, and each layer is
+// 78 is the constant 1) runs fused per tile of 128 rows: a group of 128
+// threads works on a tile with the bf16 weights in shared memory (several
+// groups per CTA share one copy), thread r owns row r, and each layer is
 //   A (128 x K activations, smem) * B (N x K weights, smem) -> D (TMEM, fp32)
 // issued as K/16 tcgen05.mma (kind::f16, bf16 inputs, fp32 accumulate) by
-// one thread and committed to an mbarrier; every thread then reads its row of
-// D with tcgen05.ld, applies ReLU, rounds to bf16 and writes the next layer's
-// A tile.  Operands use the no-swizzle K-major canonical layout: 8-row x
-// 16-byte core matrices of 128 contiguous bytes, LBO = 128 (next core matrix
-// along K), SBO = (K/8)*128 (next 8-row group).
+// one thread and committed to the group's mbarrier; every thread then reads
+// its row of D with tcgen05.ld, applies ReLU, rounds to bf16 and writes the
+// next layer's input over the tile the MMA has finished reading.  Operands
+// use the no-swizzle K-major canonical layout: 8-row x 16-byte core matrices
+// of 128 contiguous bytes, LBO = 128 (next core matrix along K), SBO =
+// (K/8)*128 (next 8-row group).
 //
 //   k_guide_infer   forward for path vertices (features computed in-kernel)
 //   k_guide_train   forward, loss gradient at the outputs, backward-data
 //                   (dH = dZ * W through transposed weight copies), storing
 //                   every layer's input and output delta feature-major
-//   k_guide_wgrad   weight gradients dW_l = dZ_{l+1}^T H_l as a tensor-core
-//                   GEMM whose K dimension is the batch (M padded to 128)
+//   k_guide_wgrad   weight gradients dW_l = dZ_{l+1}^T H_l as M = 64
+//                   tensor-core GEMMs whose K dimension is the batch,
+//                   operands double-buffered with cp.async
 //   k_guide_adam    Adam on float32 master weights, then the bf16 copies
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the error word,
@@ -148,35 +149,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// 64 consecutive fp32 columns of this thread's TMEM lane: both 32-column
-// loads are issued before the one wait (a single asm statement, so no use of
-// the registers can be scheduled before the wait).
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float* v) {
-  uint32_t r[64];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n\t"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
-      : "r"(taddr), "r"(taddr + 32u)
-      : "memory");
-#pragma unroll
-  for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
-}
-// 48 columns (the output layer): a 32- and a 16-column load, one wait.
-__device__ __forceinline__ void tmem_ld48(uint32_t taddr, float* v) {
-  uint32_t r[48];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%48];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%49];\n\t"
-      "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47])
-      : "r"(taddr), "r"(taddr + 32u)
-      : "memory");
-#pragma unroll
-  for (int i = 0; i < 48; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // ------------------------------------------------------------ layouts ---
 // Byte offset of the 16-byte chunk (row r, columns 8c..8c+7) of a K-major
 // canonical tile with K columns.
@@ -186,6 +158,14 @@ __device__ __forceinline__ uint32_t chunk_off(uint32_t r, uint32_t c, uint32_t K
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&h);
+}
+// max(a, 0) and max(b, 0) rounded to bf16 and packed (a in the low half) by
+// one conversion: a negative value converts to +0, the same bits as
+// rounding the ReLU's output.
+__device__ __forceinline__ uint32_t pack2_relu(float a, float b) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+  return d;
 }
 // Row r of a K-major tile from K fp32 values (rounded to bf16).
 __device__ __forceinline__ void put_row(char* tile, uint32_t r, uint32_t K, const float* v) {
@@ -226,13 +206,12 @@ constexpr uint32_t kWf0 = 0, kWf1 = 64 * 80, kWf2 = kWf1 + 4096, kWf3 = kWf2 + 4
                    kWfSize = kWf4 + 48 * 64;
 constexpr uint32_t kWb1 = 0, kWb2 = 4096, kWb3 = 8192, kWb4 = 12288, kWbSize = kWb4 + 64 * 48;
 
-// Shared-memory plan (bytes; all tiles 1024-aligned).
+// Shared-memory plan (bytes; all tiles 1024-aligned): the forward weights,
+// then (training) the transposed weights, then the groups' activation tiles.
 constexpr uint32_t kSW0 = 0, kSW1 = kSW0 + 64 * 80 * 2, kSW2 = kSW1 + 8192, kSW3 = kSW2 + 8192, kSW4 = kSW3 + 8192,
                    kSWEnd = kSW4 + 48 * 64 * 2;  // 40960
-constexpr uint32_t kSA0 = kSWEnd, kSA1 = kSA0 + 128 * 80 * 2, kSAEnd = kSA1 + 128 * 64 * 2;  // 77824
-constexpr uint32_t kSB1 = kSAEnd, kSB2 = kSB1 + 8192, kSB3 = kSB2 + 8192, kSB4 = kSB3 + 8192,
-                   kSBEnd = kSB4 + 64 * 48 * 2;  // 108544
-constexpr uint32_t kTrainSmem = kSBEnd + 64;
+constexpr uint32_t kSB1 = kSWEnd, kSB2 = kSB1 + 8192, kSB3 = kSB2 + 8192, kSB4 = kSB3 + 8192,
+                   kSBEnd = kSB4 + 64 * 48 * 2;  // 71680
 
 constexpr int kLobes = 8;
 
@@ -272,61 +251,17 @@ __device__ void features(const float* p, const float* n, const float* wo, const 
   f[79] = 0.0f;
 }
 
-// The forward pass of one tile; the caller has written the input features
-// into A0.  Returns false if a wait ran out.  On return the output layer
-// (48 columns, 41 used) is in TMEM columns 0..47; mask[l] holds bit j for
-// h_{l+1}[j] > 0 (l = 0..3, two words each).
-__device__ bool forward_tile(char* sm, Shared& sh, uint32_t& phase, uint32_t* mask, bool keep_mask,
-                             __nv_bfloat16* save_h, uint32_t save_stride, uint32_t row_global, bool row_valid) {
-  const uint32_t r = threadIdx.x;
-  const uint32_t lane_base = (r & ~31u) << 16;
-  const uint32_t Ks[5] = {80, 64, 64, 64, 64};
-  const uint32_t Ns[5] = {64, 64, 64, 64, 48};
-  const uint32_t Ws[5] = {kSW0, kSW1, kSW2, kSW3, kSW4};
-  for (int l = 0; l < 5; ++l) {
-    const char* A = sm + ((l & 1) ? kSA1 : kSA0);
-    fence_async_smem();
-    __syncthreads();
-    if (r == 0) gemm_issue(sh.tmem, A, sm + Ws[l], Ks[l], Ns[l], &sh.bar);
-    if (!wait_all(sh, phase)) return false;
-    fence_after();
-    if (l == 4) return true;
-    float h[64];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) tmem_ld16(sh.tmem + lane_base + 16 * q, h + 16 * q);
-    uint32_t m0 = 0, m1 = 0;
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-      h[j] = h[j] > 0.0f ? h[j] : 0.0f;
-      if (h[j] > 0.0f) {
-        if (j < 32) m0 |= 1u << j;
-        else m1 |= 1u << (j - 32);
-      }
-    }
-    if (keep_mask) {
-      mask[2 * l] = m0;
-      mask[2 * l + 1] = m1;
-    }
-    fence_before();
-    put_row(sm + ((l & 1) ? kSA0 : kSA1), r, 64, h);
-    if (save_h && row_valid) {  // feature-major copy of h_{l+1} for the weight gradient
-      __nv_bfloat16* dst = save_h + (size_t)(80 + 64 * l) * save_stride + row_global;
-      for (int j = 0; j < 64; ++j) dst[(size_t)j * save_stride] = __float2bfloat16_rn(h[j]);
-    }
-  }
-  return true;
-}
-
 // Mixture parameters and loss gradient at the outputs (the oracle's
-// loss_grad_out in float): the loss is -weight * log q with q the vertex's
-// sampling density alpha p_guide + (1 - alpha) p_bsdf, alpha = amax *
-// sigmoid(o[40]); pb < 0 (no BSDF density recorded): q = p_guide and the
-// selection logit gets no gradient.
+// loss_grad_out in float): the lobes descend -weight * log p_guide; with a
+// BSDF density (pb >= 0) the selection logit descends -weight * log q, q =
+// alpha p_guide + (1 - alpha) p_bsdf, alpha = amax * sigmoid(o[40]), with
+// p_guide held fixed; loss = -weight * log q (or log p_guide).
+constexpr float kLogKapMin = -4.6f, kLogKapMax = 6.9f;  // kappa in [0.01, 992]
 __device__ void out_grad(const float* o, const float* w, float weight, float pb, float amax, float* g, float& loss) {
   float mx = -INFINITY;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) mx = fmaxf(mx, o[5 * k + 4]);
-  float pi[kLobes], v[kLobes], mu[kLobes][3], rn[kLobes], kap[kLobes], sig[kLobes];
+  float pi[kLobes], v[kLobes], mu[kLobes][3], rn[kLobes], kap[kLobes];
   bool cl[kLobes];
   float z = 0.f;
 #pragma unroll
@@ -337,11 +272,8 @@ __device__ void out_grad(const float* o, const float* w, float weight, float pb,
     rn[k] = n;
     for (int c = 0; c < 3; ++c) mu[k][c] = r[c] / n;
     const float s = r[3];
-    const float sp = s > 20.f ? s : log1pf(expf(s));
-    float kk = sp + 0.01f;
-    cl[k] = kk > 1000.f;
-    kap[k] = cl[k] ? 1000.f : kk;
-    sig[k] = 1.f / (1.f + expf(-s));
+    cl[k] = s < kLogKapMin || s > kLogKapMax;
+    kap[k] = expf(fminf(fmaxf(s, kLogKapMin), kLogKapMax));
     pi[k] = expf(r[4] - mx);
     z += pi[k];
   }
@@ -354,41 +286,47 @@ __device__ void out_grad(const float* o, const float* w, float weight, float pb,
     v[k] = c * expf(kap[k] * (d - 1.f));
     p += pi[k] * v[k];
   }
-  float q = p, a = 1.f;
+  p = fmaxf(p, 1e-30f);
+  loss = -weight * logf(p);
   g[40] = 0.f;
   if (pb >= 0.f) {
     const float sg = 1.f / (1.f + expf(-o[40]));
-    a = amax * sg;
-    q = fmaxf(a * p + (1.f - a) * pb, 1e-30f);
+    const float a = amax * sg;
+    const float q = fmaxf(a * p + (1.f - a) * pb, 1e-30f);
     g[40] = -weight * (p - pb) / q * (amax * sg * (1.f - sg));
+    loss = -weight * logf(q);
   }
-  q = fmaxf(q, 1e-30f);
-  loss = -weight * logf(q);
-  const float share = a * p / q;
 #pragma unroll
   for (int k = 0; k < kLobes; ++k) {
-    const float rr = a * pi[k] * v[k] / q;
+    const float rr = pi[k] * v[k] / p;
     const float d = mu[k][0] * w[0] + mu[k][1] * w[1] + mu[k][2] * w[2];
-    g[5 * k + 4] = -weight * (rr - share * pi[k]);
+    g[5 * k + 4] = -weight * (rr - pi[k]);
     const float dl = 1.f / kap[k] - 2.f / expm1f(2.f * kap[k]) + (d - 1.f);
-    g[5 * k + 3] = cl[k] ? 0.f : -weight * rr * dl * sig[k];
+    g[5 * k + 3] = cl[k] ? 0.f : -weight * rr * dl * kap[k];
     for (int c = 0; c < 3; ++c) g[5 * k + c] = -weight * rr * kap[k] * (w[c] - d * mu[k][c]) / rn[k];
   }
 }
 
-// Inference runs two tile streams per CTA: 256 threads in two groups of
-// four warps share one copy of the weights; each group has its own
-// activation tiles, mbarrier, named barrier (ids 1 and 2) and 64 TMEM
-// columns (the 32x32b loads reach TMEM lanes 32*(warp % 4) .. +31, so the
-// second group's warps read the same 128 lanes in their own columns).  One
-// group's epilogue (TMEM -> ReLU -> bf16 -> shared memory) overlaps the
-// other group's MMAs, and the SM holds twice the warps of a one-tile CTA.
-constexpr uint32_t kGroups = 2;
-constexpr uint32_t kSAGroup = 128 * 80 * 2 + 128 * 64 * 2;  // A0 + A1 of one group: 36864
+// Inference: one CTA per SM runs six tile streams.  768 threads in six
+// groups of four warps share one copy of the weights; each group owns one
+// 128 x 80 activation tile (a layer's MMA has completed before its epilogue
+// writes the next layer's input over the same tile), an mbarrier, a named
+// barrier (ids 1..6) and 64 TMEM columns (the 32x32b loads reach TMEM lanes
+// 32*(warp % 4) .. +31, so every group's warps read the same 128 lanes in
+// their own columns).  With six independent five-layer chains per SM the
+// tensor pipe has MMAs from some group while the others run their
+// epilogues (TMEM -> ReLU -> bf16 -> shared memory).  Registers stay within
+// 85 per thread: the input encoding is built one 16-byte chunk (8 features)
+// at a time and the epilogues run in halves of 32 columns.
+constexpr uint32_t kGroups = 6;
+constexpr uint32_t kInferThreads = 128 * kGroups;
+// tcgen05.alloc takes a power of two of columns (>= 32): 64 a group, rounded up
+constexpr uint32_t kInferTmemCols = 64 * kGroups <= 256 ? (64 * kGroups <= 128 ? 128 : 256) : 512;
+static_assert(64 * kGroups <= kInferTmemCols && kInferTmemCols <= 512, "inference tensor memory");
+constexpr uint32_t kSAGroup = 128 * 80 * 2;  // one group's activation tile: 20480
 // Dynamic shared memory: weights, the groups' tiles, then the control block
-// (no static shared memory, so two CTAs fit an SM's 228 KB).
+// (kGroups mbarrier records, then the TMEM address slot).
 constexpr uint32_t kInferCtl = kSWEnd + kGroups * kSAGroup;
-constexpr uint32_t kInferSmem2 = kInferCtl + 64;
 
 __device__ __forceinline__ void group_sync(uint32_t id) {
   asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
@@ -409,21 +347,82 @@ struct GroupShared {
   uint64_t bar;
   int abort;
 };
+constexpr uint32_t kInferSlot = kInferCtl + kGroups * (uint32_t)sizeof(GroupShared);
+constexpr uint32_t kInferSmem2 = kInferSlot + 16;
+static_assert(kInferSmem2 <= 227u * 1024u, "inference shared memory");
 
-// The forward pass of one tile by one group (features already in its A0):
-// false if a wait ran out.  The output layer ends in the group's TMEM
-// columns 0..47.
-__device__ bool forward_tile_group(char* sm, char* a0, char* a1, GroupShared& gs, uint32_t tmem, uint32_t bid,
-                                   uint32_t r, uint32_t& phase) {
+// 32 consecutive fp32 columns of this thread's TMEM lane (one wait).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Features of one axis (chunks 3 ax .. 3 ax + 2 of a row: frequencies
+// 0..11, sin then cos, 8 features a chunk) into the tile (the encoding of
+// features()).  sin and cos of pi 2^k q are exact (sincospif) at k = 0 and
+// 8 and carried by double-angle steps from there: at most seven steps, an
+// absolute error below 2e-5, far under the bf16 rounding the features get.
+__device__ __forceinline__ void put_axis_features(char* tile, uint32_t r, uint32_t ax, float qa, bool valid) {
+  float s = 0.f, co = 1.f;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    if (m == 1) {  // one more step from frequency 3
+      const float s2 = 2.0f * s * co;
+      co = (co - s) * (co + s);
+      s = s2;
+    } else {
+      sincospif(ldexpf(qa, 4 * m), &s, &co);
+    }
+    float f[8];
+    f[0] = s;
+    f[1] = co;
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+      const float s2 = 2.0f * s * co;
+      co = (co - s) * (co + s);
+      s = s2;
+      f[2 * k] = s;
+      f[2 * k + 1] = co;
+    }
+    uint4 w = make_uint4(0, 0, 0, 0);
+    if (valid) {
+      w.x = pack2(f[0], f[1]);
+      w.y = pack2(f[2], f[3]);
+      w.z = pack2(f[4], f[5]);
+      w.w = pack2(f[6], f[7]);
+    }
+    *reinterpret_cast<uint4*>(tile + chunk_off(r, 3 * ax + m, 80)) = w;
+  }
+}
+__device__ __forceinline__ void put_chunk(char* tile, uint32_t r, uint32_t c, uint32_t K, const float* v) {
+  uint4 w;
+  w.x = pack2(v[0], v[1]);
+  w.y = pack2(v[2], v[3]);
+  w.z = pack2(v[4], v[5]);
+  w.w = pack2(v[6], v[7]);
+  *reinterpret_cast<uint4*>(tile + chunk_off(r, c, K)) = w;
+}
+
+// The forward pass of one tile by one group (features already in its
+// tile): false if a wait ran out.  The output layer ends in the group's
+// TMEM columns 0..47.
+__device__ bool forward_tile_group(char* sm, char* a, GroupShared& gs, uint32_t tmem, uint32_t bid, uint32_t r,
+                                   uint32_t& phase) {
   const uint32_t lane_base = (r & ~31u) << 16;
-  const uint32_t Ks[5] = {80, 64, 64, 64, 64};
-  const uint32_t Ns[5] = {64, 64, 64, 64, 48};
-  const uint32_t Ws[5] = {kSW0, kSW1, kSW2, kSW3, kSW4};
+#pragma unroll
   for (int l = 0; l < 5; ++l) {
-    const char* A = (l & 1) ? a1 : a0;
     fence_async_smem();
     group_sync(bid);
-    if (r == 0) gemm_issue(tmem, A, sm + Ws[l], Ks[l], Ns[l], &gs.bar);
+    if (r == 0)
+      gemm_issue(tmem, a, sm + (l == 0 ? kSW0 : (l == 1 ? kSW1 : (l == 2 ? kSW2 : (l == 3 ? kSW3 : kSW4)))),
+                 l == 0 ? 80u : 64u, l == 4 ? 48u : 64u, &gs.bar);
     const bool ok = bar_wait(&gs.bar, phase);
     phase ^= 1u;
     if (group_any(!ok, bid)) {
@@ -432,21 +431,32 @@ __device__ bool forward_tile_group(char* sm, char* a0, char* a1, GroupShared& gs
     }
     fence_after();
     if (l == 4) return true;
-    float h[64];
+    // the MMA has read the tile: the next layer's input goes over it (K = 64)
 #pragma unroll
-    tmem_ld64(tmem + lane_base, h);
+    for (uint32_t hh = 0; hh < 2; ++hh) {
+      float h[32];
+      tmem_ld32(tmem + lane_base + 32u * hh, h);
 #pragma unroll
-    for (int j = 0; j < 64; ++j) h[j] = h[j] > 0.0f ? h[j] : 0.0f;
+      for (uint32_t cc = 0; cc < 4; ++cc) {
+        const float* v = h + 8 * cc;
+        uint4 w;
+        w.x = pack2_relu(v[0], v[1]);
+        w.y = pack2_relu(v[2], v[3]);
+        w.z = pack2_relu(v[4], v[5]);
+        w.w = pack2_relu(v[6], v[7]);
+        *reinterpret_cast<uint4*>(a + chunk_off(r, 4 * hh + cc, 64)) = w;
+      }
+    }
     fence_before();
-    put_row((l & 1) ? a0 : a1, r, 64, h);
   }
   return true;
 }
 
-__global__ void __launch_bounds__(256) k_guide_infer(GuideRows in, const __nv_bfloat16* wf, float* out, int* err) {
+__global__ void __launch_bounds__(kInferThreads, 1) k_guide_infer(GuideRows in, const __nv_bfloat16* wf, float* out,
+                                                                  int* err) {
   extern __shared__ __align__(1024) char sm[];
   GroupShared* gsh = reinterpret_cast<GroupShared*>(sm + kInferCtl);
-  uint32_t& tmem_base = *reinterpret_cast<uint32_t*>(sm + kInferCtl + kGroups * sizeof(GroupShared));
+  uint32_t& tmem_base = *reinterpret_cast<uint32_t*>(sm + kInferSlot);
   const uint32_t g = threadIdx.x / 128u, r = threadIdx.x % 128u;
   const uint32_t bid = 1u + g;
   const uint64_t n = in.n_dev ? *in.n_dev : in.n;
@@ -459,63 +469,104 @@ __global__ void __launch_bounds__(256) k_guide_infer(GuideRows in, const __nv_bf
   load_tile(sm + kSW2, wf + kWf2, 64, 64);
   load_tile(sm + kSW3, wf + kWf3, 64, 64);
   load_tile(sm + kSW4, wf + kWf4, 48, 64);
-  if (threadIdx.x < 32) tmem_alloc(&tmem_base, 64 * kGroups);
+  if (threadIdx.x < 32) tmem_alloc(&tmem_base, kInferTmemCols);
   fence_before();
   __syncthreads();
   fence_after();
   GroupShared& gs = gsh[g];
-  char* a0 = sm + kSWEnd + g * kSAGroup;
-  char* a1 = a0 + 128 * 80 * 2;
+  char* a = sm + kSWEnd + g * kSAGroup;
   const uint32_t tmem = tmem_base + 64u * g;
   const uint32_t lane_base = (r & ~31u) << 16;
   uint32_t phase = 0;
   const uint64_t ntiles = (n + 127) / 128;
   for (uint64_t t = (uint64_t)blockIdx.x * kGroups + g; t < ntiles; t += (uint64_t)gridDim.x * kGroups) {
     const uint64_t row = t * 128 + r;
-    float f[80];
     const bool valid = row < n;
+    float q[3] = {0.f, 0.f, 0.f}, nn[3] = {0.f, 0.f, 0.f}, wo[3] = {0.f, 0.f, 0.f};
     if (valid) {
-      const float p[3] = {in.px[row], in.py[row], in.pz[row]};
-      const float nn[3] = {in.nx[row], in.ny[row], in.nz[row]};
-      const float wo[3] = {in.wx[row], in.wy[row], in.wz[row]};
-      features(p, nn, wo, in.lo, in.inv_ext, f);
-    } else {
-      for (int k = 0; k < 80; ++k) f[k] = 0.f;
+      q[0] = (in.px[row] - in.lo[0]) * in.inv_ext[0];
+      q[1] = (in.py[row] - in.lo[1]) * in.inv_ext[1];
+      q[2] = (in.pz[row] - in.lo[2]) * in.inv_ext[2];
+      nn[0] = in.nx[row]; nn[1] = in.ny[row]; nn[2] = in.nz[row];
+      wo[0] = in.wx[row]; wo[1] = in.wy[row]; wo[2] = in.wz[row];
     }
-    put_row(a0, r, 80, f);
-    if (!forward_tile_group(sm, a0, a1, gs, tmem, bid, r, phase)) break;
-    float o[48];
+#pragma unroll 1
+    for (uint32_t ax = 0; ax < 3; ++ax) put_axis_features(a, r, ax, ax == 0 ? q[0] : (ax == 1 ? q[1] : q[2]), valid);
+    {
+      // chunk 9: normal, direction toward the previous vertex, 1, 0
+      const float f[8] = {nn[0], nn[1], nn[2], wo[0], wo[1], wo[2], valid ? 1.0f : 0.0f, 0.0f};
+      put_chunk(a, r, 9, 80, f);
+    }
+    if (!forward_tile_group(sm, a, gs, tmem, bid, r, phase)) break;
+    // 44 floats per row (41 outputs; columns 41..43 of the padded layer are 0)
+    float4* dst = reinterpret_cast<float4*>(out + (size_t)row * kGuideOutStride);
+    {
+      float o[32];
+      tmem_ld32(tmem + lane_base, o);
+      if (valid)
 #pragma unroll
-    tmem_ld48(tmem + lane_base, o);
+        for (int k = 0; k < 8; ++k) dst[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    }
+    {
+      float o[16];
+      tmem_ld16(tmem + lane_base + 32u, o);
+      if (valid)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dst[8 + k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+    }
     fence_before();
-    if (valid) {
-      // 44 floats per row (41 outputs; columns 41..43 of the padded layer are 0)
-      float4* dst = reinterpret_cast<float4*>(out + (size_t)row * kGuideOutStride);
-#pragma unroll
-      for (int k = 0; k < kGuideOutStride / 4; ++k)
-        dst[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
-    }
   }
   // a group that stopped early waits (bounded) for its MMAs still in flight
   if (gs.abort) (void)bar_wait(&gs.bar, phase ^ 1u);
   __syncthreads();
   if (r == 0 && gs.abort) atomicExch(err, 1);
-  if (threadIdx.x < 32) tmem_free(tmem_base, 64 * kGroups);
+  if (threadIdx.x < 32) tmem_free(tmem_base, kInferTmemCols);
 }
 
-// Forward + loss gradient + backward-data over one tile per iteration.
-// Saved feature-major (stride = batch size B): X rows 0..79, h1..h4 at 80 +
-// 64*l, dY at 336 (48 rows), dZ4..dZ1 at 384 + 64*(4-l) (l = 4..1).
-__global__ void __launch_bounds__(128) k_guide_train(GuideTrain tr, const __nv_bfloat16* wf, const __nv_bfloat16* wb,
-                                                     __nv_bfloat16* save, float* sums, int* err) {
+// Training: forward + loss gradient + backward-data, four tile streams per
+// CTA (512 threads in groups of four warps, one CTA per SM) sharing both
+// weight copies; each group owns one 128 x 80 tile that holds the current
+// layer's input (forward), dY (K = 48) and then each dZ (backward), written
+// over the tile once the MMA that read it has completed.  Saved
+// feature-major (stride = batch size B): X rows 0..79, h1..h4 at 80 + 64*l,
+// dY at 336 (48 rows), dZ4..dZ1 at 384 + 64*(4-l) (l = 4..1).
+constexpr uint32_t kTrainGroups = 4;
+constexpr uint32_t kTrainThreads = 128 * kTrainGroups;
+constexpr uint32_t kTrainCtl = kSBEnd + kTrainGroups * kSAGroup;
+constexpr uint32_t kTrainSlot = kTrainCtl + kTrainGroups * (uint32_t)sizeof(GroupShared);
+constexpr uint32_t kTrainSmem = kTrainSlot + 16;
+static_assert(kTrainSmem <= 227u * 1024u, "training shared memory");
+
+// One MMA of a group (the tile as A, K-major) and its bounded wait; false if
+// the wait ran out (the group agrees; thread 0 marks the abort).
+__device__ __forceinline__ bool group_gemm(uint32_t tmem, const char* A, const char* Bm, uint32_t K, uint32_t N,
+                                           GroupShared& gs, uint32_t bid, uint32_t r, uint32_t& phase) {
+  fence_async_smem();
+  group_sync(bid);
+  if (r == 0) gemm_issue(tmem, A, Bm, K, N, &gs.bar);
+  const bool ok = bar_wait(&gs.bar, phase);
+  phase ^= 1u;
+  if (group_any(!ok, bid)) {
+    if (r == 0) gs.abort = 1;
+    return false;
+  }
+  fence_after();
+  return true;
+}
+
+__global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideTrain tr, const __nv_bfloat16* wf,
+                                                                  const __nv_bfloat16* wb, __nv_bfloat16* save,
+                                                                  float* sums, int* err) {
   extern __shared__ __align__(1024) char sm[];
-  __shared__ Shared sh;
-  const uint32_t r = threadIdx.x;
+  GroupShared* gsh = reinterpret_cast<GroupShared*>(sm + kTrainCtl);
+  uint32_t& tmem_base = *reinterpret_cast<uint32_t*>(sm + kTrainSlot);
+  const uint32_t g = threadIdx.x / 128u, r = threadIdx.x % 128u;
+  const uint32_t bid = 1u + g;
   const uint64_t n = tr.rows.n_dev ? *tr.rows.n_dev : tr.rows.n;
   const uint32_t B = tr.stride;
   if (r == 0) {
-    bar_init(&sh.bar);
-    sh.abort = 0;
+    bar_init(&gsh[g].bar);
+    gsh[g].abort = 0;
   }
   load_tile(sm + kSW0, wf + kWf0, 64, 80);
   load_tile(sm + kSW1, wf + kWf1, 64, 64);
@@ -526,86 +577,115 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideTrain tr, const __nv_b
   load_tile(sm + kSB2, wb + kWb2, 64, 64);
   load_tile(sm + kSB3, wb + kWb3, 64, 64);
   load_tile(sm + kSB4, wb + kWb4, 64, 48);
-  if (r < 32) tmem_alloc(&sh.tmem, 64);
+  if (threadIdx.x < 32) tmem_alloc(&tmem_base, 64 * kTrainGroups);
   fence_before();
   __syncthreads();
   fence_after();
-  uint32_t phase = 0;
+  GroupShared& gs = gsh[g];
+  char* a = sm + kSBEnd + g * kSAGroup;
+  const uint32_t tmem = tmem_base + 64u * g;
   const uint32_t lane_base = (r & ~31u) << 16;
+  uint32_t phase = 0;
   const uint64_t ntiles = (n + 127) / 128;
   float loss_acc = 0.f, w_acc = 0.f;
-  bool ok = true;
-  for (uint64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+  for (uint64_t t = (uint64_t)blockIdx.x * kTrainGroups + g; t < ntiles; t += (uint64_t)gridDim.x * kTrainGroups) {
     const uint64_t row = t * 128 + r;
     const bool valid = row < n;
-    float f[80];
-    float weight = 0.f, om[3] = {0.f, 0.f, 1.f};
-    if (valid) {
-      const GuideRows& in = tr.rows;
-      const uint64_t e = row * in.rstride;
-      const float p[3] = {in.px[e], in.py[e], in.pz[e]};
-      const float nn[3] = {in.nx[e], in.ny[e], in.nz[e]};
-      const float wo[3] = {in.wx[e], in.wy[e], in.wz[e]};
-      features(p, nn, wo, in.lo, in.inv_ext, f);
-      weight = tr.weight[e];
-      om[0] = tr.ox[e];
-      om[1] = tr.oy[e];
-      om[2] = tr.oz[e];
-      for (int k = 0; k < 80; ++k) save[(size_t)k * B + row] = __float2bfloat16_rn(f[k]);
-    } else {
-      for (int k = 0; k < 80; ++k) f[k] = 0.f;
+    float weight = 0.f, om[3] = {0.f, 0.f, 1.f}, pb = -1.0f;
+    {
+      float f[80];
+      if (valid) {
+        const GuideRows& in = tr.rows;
+        const uint64_t e = row * in.rstride;
+        const float p[3] = {in.px[e], in.py[e], in.pz[e]};
+        const float nn[3] = {in.nx[e], in.ny[e], in.nz[e]};
+        const float wo[3] = {in.wx[e], in.wy[e], in.wz[e]};
+        features(p, nn, wo, in.lo, in.inv_ext, f);
+        weight = tr.weight[e];
+        om[0] = tr.ox[e];
+        om[1] = tr.oy[e];
+        om[2] = tr.oz[e];
+        if (tr.pb) pb = tr.pb[e];
+        for (int k = 0; k < 80; ++k) save[(size_t)k * B + row] = __float2bfloat16_rn(f[k]);
+      } else {
+        for (int k = 0; k < 80; ++k) f[k] = 0.f;
+      }
+      put_row(a, r, 80, f);
     }
-    put_row(sm + kSA0, r, 80, f);
+    // forward; mask[l] holds bit j for h_{l+1}[j] > 0 (two words a layer)
     uint32_t mask[8];
-    if (!forward_tile(sm, sh, phase, mask, true, save, B, (uint32_t)row, valid)) {
-      ok = false;
-      break;
-    }
-    float o[48];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) tmem_ld16(sh.tmem + lane_base + 16 * q, o + 16 * q);
-    float g[48];
-    for (int k = kGuideOut; k < 48; ++k) g[k] = 0.f;
-    if (valid) {
-      float loss;
-      const float pb = tr.pb ? tr.pb[row * tr.rows.rstride] : -1.0f;
-      out_grad(o, om, weight, pb, tr.amax, g, loss);
-      loss_acc += loss;
-      w_acc += weight;
-    } else {
-      for (int k = 0; k < kGuideOut; ++k) g[k] = 0.f;
-    }
-    fence_before();
-    put_row(sm + kSA0, r, 48, g);  // dY, K = 48
-    if (valid)
-      for (int k = 0; k < 48; ++k) save[(size_t)(336 + k) * B + row] = __float2bfloat16_rn(g[k]);
-    // dH_l = dZ_{l+1} * W_l, masked by h_l > 0, for l = 4 .. 1
-    const uint32_t Bt[5] = {0, kSB1, kSB2, kSB3, kSB4};
-    for (int l = 4; l >= 1; --l) {
-      const uint32_t K = l == 4 ? 48u : 64u;
-      const char* A = sm + ((l & 1) ? kSA1 : kSA0);  // l=4 reads A0 (dY), l=3 reads A1, ...
-      fence_async_smem();
-      __syncthreads();
-      if (r == 0) gemm_issue(sh.tmem, A, sm + Bt[l], K, 64, &sh.bar);
-      if (!wait_all(sh, phase)) {
+    bool ok = true;
+#pragma unroll 1
+    for (int l = 0; l < 5 && ok; ++l) {
+      const uint32_t W = l == 0 ? kSW0 : (l == 1 ? kSW1 : (l == 2 ? kSW2 : (l == 3 ? kSW3 : kSW4)));
+      if (!group_gemm(tmem, a, sm + W, l == 0 ? 80u : 64u, l == 4 ? 48u : 64u, gs, bid, r, phase)) {
         ok = false;
         break;
       }
-      fence_after();
+      if (l == 4) break;
+      float h[64];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tmem_ld16(tmem + lane_base + 16 * q, h + 16 * q);
+      uint32_t m0 = 0, m1 = 0;
+#pragma unroll
+      for (int j = 0; j < 64; ++j) {
+        h[j] = h[j] > 0.0f ? h[j] : 0.0f;
+        if (h[j] > 0.0f) {
+          if (j < 32) m0 |= 1u << j;
+          else m1 |= 1u << (j - 32);
+        }
+      }
+      mask[2 * l] = m0;
+      mask[2 * l + 1] = m1;
+      put_row(a, r, 64, h);
+      fence_before();
+      if (valid) {  // feature-major copy of h_{l+1} for the weight gradient
+        __nv_bfloat16* dst = save + (size_t)(80 + 64 * l) * B + row;
+        for (int j = 0; j < 64; ++j) dst[(size_t)j * B] = __float2bfloat16_rn(h[j]);
+      }
+    }
+    if (!ok) break;
+    {
+      float o[48], gr[48];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) tmem_ld16(tmem + lane_base + 16 * q, o + 16 * q);
+      for (int k = kGuideOut; k < 48; ++k) gr[k] = 0.f;
+      if (valid) {
+        float loss;
+        out_grad(o, om, weight, pb, tr.amax, gr, loss);
+        loss_acc += loss;
+        w_acc += weight;
+      } else {
+        for (int k = 0; k < kGuideOut; ++k) gr[k] = 0.f;
+      }
+      put_row(a, r, 48, gr);  // dY, K = 48
+      fence_before();
+      if (valid)
+        for (int k = 0; k < 48; ++k) save[(size_t)(336 + k) * B + row] = __float2bfloat16_rn(gr[k]);
+    }
+    // dH_l = dZ_{l+1} * W_l, masked by h_l > 0, for l = 4 .. 1
+#pragma unroll 1
+    for (int l = 4; l >= 1; --l) {
+      const uint32_t Bt = l == 1 ? kSB1 : (l == 2 ? kSB2 : (l == 3 ? kSB3 : kSB4));
+      if (!group_gemm(tmem, a, sm + Bt, l == 4 ? 48u : 64u, 64u, gs, bid, r, phase)) {
+        ok = false;
+        break;
+      }
       float d[64];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmem_ld16(sh.tmem + lane_base + 16 * q, d + 16 * q);
+      for (int q = 0; q < 4; ++q) tmem_ld16(tmem + lane_base + 16 * q, d + 16 * q);
       const uint32_t m0 = mask[2 * (l - 1)], m1 = mask[2 * (l - 1) + 1];
 #pragma unroll
       for (int j = 0; j < 64; ++j) {
         const bool on = j < 32 ? ((m0 >> j) & 1u) : ((m1 >> (j - 32)) & 1u);
         d[j] = on ? d[j] : 0.f;
       }
+      put_row(a, r, 64, d);
       fence_before();
-      put_row(sm + ((l & 1) ? kSA0 : kSA1), r, 64, d);
       if (valid)
         for (int j = 0; j < 64; ++j) save[(size_t)(384 + 64 * (4 - l) + j) * B + row] = __float2bfloat16_rn(d[j]);
     }
+    if (!ok) break;
   }
   // batch sums: loss, weight
 #pragma unroll
@@ -617,18 +697,34 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideTrain tr, const __nv_b
     atomicAdd(&sums[0], loss_acc);
     atomicAdd(&sums[1], w_acc);
   }
+  // a group that stopped early waits (bounded) for its MMAs still in flight
+  if (gs.abort) (void)bar_wait(&gs.bar, phase ^ 1u);
   __syncthreads();
-  drain(sh, phase);
-  if (sh.abort && r == 0) atomicExch(err, 1);
-  if (r < 32) tmem_free(sh.tmem, 64);
+  if (r == 0 && gs.abort) atomicExch(err, 1);
+  if (threadIdx.x < 32) tmem_free(tmem_base, 64 * kTrainGroups);
 }
 
-// Weight gradients: for layer l, D [128 x N] += A [128 x 128] * B [N x 128]^T
-// over chunks of 128 batch rows, A = the output deltas of layer l (M rows of
-// the feature-major save, rows M..127 zero), B = the layer's input (N rows).
-// blockIdx.y = layer, blockIdx.x strides the chunks; partial sums go to the
-// float32 gradient with atomics.
-constexpr uint32_t kGA = 0, kGB = 128 * 128 * 2, kWgradSmem = kGB + 80 * 128 * 2 + 64;
+// Weight gradients: for layer l, D [64 x N] += A [64 x 128] * B [N x 128]^T
+// over chunks of 128 batch records (M = 64: the layer's output deltas, the
+// 41 outputs of the last layer padded with zero rows; N = the layer's 80 or
+// 64 inputs; K = the chunk's records), both operands K-major tiles loaded
+// from the feature-major save with cp.async into two stages: the loads of
+// chunk i+1 run while the MMAs of chunk i do.  blockIdx.y = layer,
+// blockIdx.x strides the chunks; the CTA's sum goes to the float32
+// gradient with atomics.  The M = 64 accumulator sits in TMEM lanes 0-15
+// of each 32-lane quarter (row 16q + j in lane 32q + j).
+constexpr uint32_t kWgStage = 64 * 128 * 2 + 80 * 128 * 2;  // A + B of one stage: 36864
+constexpr uint32_t kWgradSmem = 2 * kWgStage + 64;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, uint32_t B, uint64_t n,
                                                      const unsigned long long* n_dev, float* grad, int* err) {
   extern __shared__ __align__(1024) char sm[];
@@ -636,8 +732,8 @@ __global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, 
   const uint32_t r = threadIdx.x;
   if (n_dev) n = *n_dev < n ? *n_dev : n;
   const int l = blockIdx.y;
-  // layer l: output deltas at row dz0 (M of them), inputs at row in0 (N)
-  const uint32_t M = l == 4 ? (uint32_t)kGuideOut : 64u;
+  // layer l: output deltas at row dz0 (Mr of them), inputs at row in0 (N)
+  const uint32_t Mr = l == 4 ? (uint32_t)kGuideOut : 64u;
   const uint32_t N = l == 0 ? 80u : 64u;
   const uint32_t dz0 = l == 4 ? 336u : 384u + 64u * (3u - (uint32_t)l);
   const uint32_t in0 = l == 0 ? 0u : 80u + 64u * (uint32_t)(l - 1);
@@ -646,64 +742,83 @@ __global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, 
     bar_init(&sh.bar);
     sh.abort = 0;
   }
-  // zero the whole A tile once (rows >= M stay zero)
-  for (uint32_t i = r; i < 128 * 128 * 2 / 16; i += 128) reinterpret_cast<uint4*>(sm + kGA)[i] = make_uint4(0, 0, 0, 0);
+  // zero both stages once (the padding rows Mr..63 of A stay zero)
+  for (uint32_t i = r; i < 2 * kWgStage / 16; i += 128) reinterpret_cast<uint4*>(sm)[i] = make_uint4(0, 0, 0, 0);
   if (r < 32) tmem_alloc(&sh.tmem, 128);
   fence_before();
   __syncthreads();
   fence_after();
-  uint32_t phase = 0;
-  bool any = false, ok = true;
   const uint64_t nchunks = (n + 127) / 128;
-  for (uint64_t c = blockIdx.x; c < nchunks && ok; c += gridDim.x) {
+  // the chunk's operand rows into stage st: 16 pieces of 8 records per row
+  auto issue = [&](uint64_t c, uint32_t st) {
+    char* A = sm + st * kWgStage;
+    char* Bt = A + 64 * 128 * 2;
     const uint64_t b0 = c * 128;
-    // A rows (deltas) and B rows (inputs): 16 chunks of 8 batch values per row
-    for (uint32_t i = r; i < (M + N) * 16; i += 128) {
+    for (uint32_t i = r; i < (Mr + N) * 16; i += 128) {
       const uint32_t row = i / 16, ch = i % 16;
-      const bool isA = row < M;
-      const uint32_t src = isA ? dz0 + row : in0 + (row - M);
-      uint4 q = make_uint4(0, 0, 0, 0);
+      const bool isA = row < Mr;
+      const uint32_t src = isA ? dz0 + row : in0 + (row - Mr);
+      char* dst = isA ? A + chunk_off(row, ch, 128) : Bt + chunk_off(row - Mr, ch, 128);
       const uint64_t col = b0 + 8 * ch;
       if (col + 8 <= n) {
-        q = *reinterpret_cast<const uint4*>(save + (size_t)src * B + col);
-      } else if (col < n) {
+        cp_async16(dst, save + (size_t)src * B + col);
+      } else {
         union {
           uint4 q;
           __nv_bfloat16 h[8];
         } tmp;
         for (int e = 0; e < 8; ++e)
           tmp.h[e] = col + e < n ? save[(size_t)src * B + col + e] : __float2bfloat16_rn(0.f);
-        q = tmp.q;
+        *reinterpret_cast<uint4*>(dst) = tmp.q;
       }
-      char* dst = isA ? sm + kGA + chunk_off(row, ch, 128) : sm + kGB + chunk_off(row - M, ch, 128);
-      *reinterpret_cast<uint4*>(dst) = q;
+    }
+    cp_async_commit();
+  };
+  uint32_t phase = 0;
+  bool ok = true;
+  uint64_t it = 0;
+  const uint64_t first = blockIdx.x, step = gridDim.x;
+  if (first < nchunks) issue(first, 0);
+  for (uint64_t c = first; c < nchunks; c += step, ++it) {
+    const uint32_t st = (uint32_t)(it & 1u);
+    // the MMAs of the previous chunk read the other stage: wait for them
+    if (it > 0 && !wait_all(sh, phase)) {
+      ok = false;
+      break;
+    }
+    const bool more = c + step < nchunks;
+    if (more) {
+      issue(c + step, st ^ 1u);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     fence_async_smem();
     __syncthreads();
     if (r == 0) {
       fence_after();
-      const uint32_t a0 = saddr(sm + kGA), bb = saddr(sm + kGB);
-      const uint32_t id = idesc(128, (int)N);
+      const uint32_t a0 = saddr(sm + st * kWgStage), bb = a0 + 64 * 128 * 2;
+      const uint32_t id = idesc(64, (int)N);
       for (uint32_t kk = 0; kk < 8; ++kk)
         mma(sh.tmem, sdesc(a0 + kk * 256u, 128u, 16u * 128u), sdesc(bb + kk * 256u, 128u, 16u * 128u), id,
-            (any || kk > 0) ? 1u : 0u);
+            (it > 0 || kk > 0) ? 1u : 0u);
       mma_commit(&sh.bar);
     }
-    any = true;
-    if (!wait_all(sh, phase)) {
-      ok = false;
-      break;
-    }
-    fence_after();  // the loop's next __syncthreads orders the operand reuse
   }
-  if (any && ok) {
-    // every warp loads its lane quarter (warp-collective); rows >= M are padding
-    const uint32_t lane_base = (r & ~31u) << 16;
-    for (uint32_t q = 0; q < N / 16; ++q) {
+  cp_async_wait<0>();
+  if (ok && it > 0 && !wait_all(sh, phase)) ok = false;
+  if (ok && it > 0) {
+    fence_after();
+    // every warp loads its lane quarter (warp-collective); row 16q + j is in
+    // lane 32q + j for j < 16
+    const uint32_t q = r >> 5, j = r & 31u;
+    const uint32_t lane_base = (q * 32u) << 16;
+    const uint32_t row = 16u * q + j;
+    for (uint32_t c16 = 0; c16 < N / 16; ++c16) {
       float v[16];
-      tmem_ld16(sh.tmem + lane_base + 16 * q, v);
-      if (r < M)
-        for (int e = 0; e < 16; ++e) atomicAdd(&grad[goff + r * N + 16 * q + e], v[e]);
+      tmem_ld16(sh.tmem + lane_base + 16 * c16, v);
+      if (j < 16 && row < Mr)
+        for (int e = 0; e < 16; ++e) atomicAdd(&grad[goff + row * N + 16 * c16 + e], v[e]);
     }
   }
   fence_before();
@@ -773,14 +888,23 @@ __global__ void k_wait_selftest(int* err) {
   if (__syncthreads_or(ok ? 0 : 1) && threadIdx.x == 0) atomicExch(err, 1);
 }
 
-int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int grid, cudaStream_t st) {
-  k_guide_infer<<<grid, 256, kInferSmem2, st>>>(rows, static_cast<const __nv_bfloat16*>(wf), out, err);
+// One CTA per SM at most (it holds all of the SM's tensor memory): sms = the
+// device's SM count; fewer CTAs when the host knows the row count.
+int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int sms, cudaStream_t st) {
+  uint64_t grid = (uint64_t)(sms > 0 ? sms : 1);
+  if (!rows.n_dev) grid = std::min<uint64_t>(grid, std::max<uint64_t>(1, (rows.n + 128 * kGroups - 1) / (128 * kGroups)));
+  k_guide_infer<<<(int)grid, kInferThreads, kInferSmem2, st>>>(rows, static_cast<const __nv_bfloat16*>(wf), out, err);
   return (int)cudaGetLastError();
 }
 
-int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int grid,
+// One CTA per SM at most; sms = the device's SM count (fewer CTAs for a
+// small batch: rows.n bounds the device count too).
+int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int sms,
                  cudaStream_t st) {
-  k_guide_train<<<grid, 128, kTrainSmem, st>>>(tr, static_cast<const __nv_bfloat16*>(wf),
+  const uint64_t per_cta = 128ull * kTrainGroups;
+  const int grid = (int)std::min<uint64_t>((uint64_t)(sms > 0 ? sms : 1),
+                                           std::max<uint64_t>(1, (tr.rows.n + per_cta - 1) / per_cta));
+  k_guide_train<<<grid, kTrainThreads, kTrainSmem, st>>>(tr, static_cast<const __nv_bfloat16*>(wf),
                                                 static_cast<const __nv_bfloat16*>(wb),
                                                 static_cast<__nv_bfloat16*>(save), sums, err);
   return (int)cudaGetLastError();
@@ -942,8 +1066,7 @@ int guide_backprop(vmr_ctx* ctx, const GuideTrain& tr, size_t n) {
   GCUDA(cudaMemsetAsync(G.sums.p, 0, 16, ctx->stream));
   const int sms = guide_sms(ctx);
   const uint64_t tiles = (n + 127) / 128;
-  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)sms * 2);
-  if (vmr::guide::launch_train(t, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), grid,
+  if (vmr::guide::launch_train(t, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), sms,
                                ctx->stream) != 0)
     return gfail(ctx, VMR_ERR_CUDA, "guide training kernel launch failed");
   const int chunks = (int)std::min<uint64_t>(tiles, (uint64_t)sms);
@@ -1058,9 +1181,8 @@ int vmr_guide_forward(vmr_ctx* ctx, const float* pos, const float* nrm, const fl
   rc = stage_rows(ctx, pos, nrm, wo, nullptr, nullptr, nullptr, n, lo, hi, tr, 9 * (n4 - n) + n * kGuideOutStride);
   if (rc) return rc;
   float* dout = ctx->guide.io.as<float>() + 9 * n4;
-  const uint64_t tiles = (n + 127) / 128;
-  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)guide_sms(ctx) * 2);
-  if (vmr::guide::launch_infer(tr.rows, ctx->guide.wf.p, dout, ctx->guide.err.as<int>(), grid, ctx->stream) != 0)
+  if (vmr::guide::launch_infer(tr.rows, ctx->guide.wf.p, dout, ctx->guide.err.as<int>(), guide_sms(ctx), ctx->stream) !=
+      0)
     return gfail(ctx, VMR_ERR_CUDA, "guide inference launch failed");
   std::vector<float> h(n * kGuideOutStride);
   GCUDA(cudaMemcpyAsync(h.data(), dout, h.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));

@@ -49,8 +49,10 @@ void prepare_kernels();
 // Random initial weights (seed 0) unless the context's guide already has some.
 int ensure_ready(struct ::vmr_ctx* ctx);
 size_t wb_elems();
-int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int grid, cudaStream_t st);
-int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int grid,
+// out: kGuideOutStride floats per row; sms: the device's SM count.
+int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, int sms, cudaStream_t st);
+// sms: the device's SM count (the kernel runs at most one CTA per SM).
+int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int sms,
                  cudaStream_t st);
 int launch_wgrad(const void* save, uint32_t B, uint64_t n, const unsigned long long* n_dev, float* grad, int* err,
                  int chunks, cudaStream_t st);

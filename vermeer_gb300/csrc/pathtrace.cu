@@ -319,8 +319,8 @@ __device__ __forceinline__ void put_ray(float* q, uint32_t cap, uint64_t i, cons
 
 // ------------------------------------------------------- guide mixture ---
 // The network outputs 0..39 as 8 vMF lobes (the same decoding the trainer
-// differentiates): mu = normalize, kappa = min(softplus + 0.01, 1000),
-// pi = softmax; c = kappa / (2 pi (1 - exp(-2 kappa))).  Output 40 is the
+// differentiates): mu = normalize, kappa = exp(s) with s clamped to
+// [-4.6, 6.9], pi = softmax; c = kappa / (2 pi (1 - exp(-2 kappa))).  Output 40 is the
 // selection logit: with learned selection the vertex samples the guide with
 // probability alpha = alpha_max * sigmoid(o[40]), else with alpha_max.
 struct GMix {
@@ -337,9 +337,7 @@ __device__ void gmix_decode(const float* o, float amax, bool learned, GMix& g) {
     float n = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
     n = n < 1e-6f ? 1e-6f : n;
     for (int c = 0; c < 3; ++c) g.mu[k][c] = r[c] / n;
-    const float s = r[3];
-    const float kk = (s > 20.f ? s : log1pf(expf(s))) + 0.01f;
-    g.kap[k] = kk > 1000.f ? 1000.f : kk;
+    g.kap[k] = expf(fminf(fmaxf(r[3], -4.6f), 6.9f));
     g.c[k] = g.kap[k] / (6.28318530718f * (-expm1f(-2.f * g.kap[k])));
     g.pi[k] = expf(r[4] - mx);
     z += g.pi[k];
@@ -936,7 +934,7 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
       PCUDA(cudaGetLastError());
       guide::GuideRows r = grows;
       r.n_dev = &b.qlen[d];
-      if (guide::launch_infer(r, ctx->guide.wf.p, b.gout, ctx->guide.err.as<int>(), grid / 4, st) != 0)
+      if (guide::launch_infer(r, ctx->guide.wf.p, b.gout, ctx->guide.err.as<int>(), grid / 8, st) != 0)
         return pfail(ctx, VMR_ERR_CUDA, "guide inference launch failed");
       if (train) k_pt_shade<true, true><<<grid, kPtBlock, 0, st>>>(b, d);
       else k_pt_shade<true, false><<<grid, kPtBlock, 0, st>>>(b, d);
@@ -1414,8 +1412,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
         tr.stride = stride;
         if (off >= rcap) break;
         PCUDA(cudaMemsetAsync(G.sums.p, 0, 16, st));
-        const int tgrid = std::min<int>(grid / 4, (int)((tbatch + 127) / 128));
-        if (guide::launch_train(tr, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), tgrid, st) != 0)
+        if (guide::launch_train(tr, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), sms, st) != 0)
           return pfail(ctx, VMR_ERR_CUDA, "guide training launch failed");
         if (guide::launch_wgrad(G.save.p, stride, tbatch, ncount, G.grad.as<float>(), G.err.as<int>(),
                                 std::max(1, std::min(sms, (int)((tbatch + 127) / 128))), st) != 0)

@@ -843,14 +843,33 @@ __global__ void k_jobs_scatter(const JobDesc* jobs, uint32_t n_jobs, uint64_t n,
 // count, lanes take base + their rank among the idle lanes), which keeps the
 // warp full until the ray pool runs dry.
 
+// 32 bytes of read-only global memory (32-byte aligned) as two float4, in
+// one 256-bit load: a node of 128 bytes takes four load instructions
+// instead of eight, and each instruction of a warp whose lanes fetch
+// different nodes costs the L1 one pass per lane either way, so the node
+// fetches' share of the L1 passes halves.
+__device__ __forceinline__ void ld256(const void* p, float4& a, float4& c) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(c.x), "=f"(c.y), "=f"(c.z), "=f"(c.w)
+      : "l"(p));
+}
+// A static wide node (128-byte aligned): 6 box float4, children, meta.
+__device__ __forceinline__ void ld_node(const void* p, float4 (&b)[6], int4& ch, uint4& meta) {
+  const float4* q = static_cast<const float4*>(p);
+  ld256(q, b[0], b[1]);
+  ld256(q + 2, b[2], b[3]);
+  ld256(q + 4, b[4], b[5]);
+  float4 c4, m4;
+  ld256(q + 6, c4, m4);
+  ch = make_int4(__float_as_int(c4.x), __float_as_int(c4.y), __float_as_int(c4.z), __float_as_int(c4.w));
+  meta = make_uint4(__float_as_uint(m4.x), __float_as_uint(m4.y), __float_as_uint(m4.z), __float_as_uint(m4.w));
+}
+
 // Fetch a static node: 6 box float4, children, and this octant's push ranks.
 __device__ __forceinline__ void fetch_node(const DMesh& m, int node, unsigned oct, float4 (&b)[6], int4& ch,
                                            unsigned& rk) {
-  const float4* nb = reinterpret_cast<const float4*>(m.nodes + node);
-#pragma unroll
-  for (int k = 0; k < 6; ++k) b[k] = __ldg(nb + k);
-  ch = __ldg(reinterpret_cast<const int4*>(nb + 6));
-  const uint4 meta = __ldg(reinterpret_cast<const uint4*>(nb + 7));
+  uint4 meta;
+  ld_node(m.nodes + node, b, ch, meta);
   rk = (((oct & 4u) ? meta.z : meta.y) >> ((oct & 3u) * 8u)) & 0xffu;
 }
 
@@ -1594,11 +1613,8 @@ __global__ void __launch_bounds__(128, 8)
                         bx + (size_t)key2 * top.n_mnodes * 6, tm, omt, b, ch, rk);
           } else {
             const GNode* nb = geom < 0 ? top.nodes : mnodes;
-            const float4* np = reinterpret_cast<const float4*>(nb + node);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) b[k] = __ldg(np + k);
-            ch = __ldg(reinterpret_cast<const int4*>(np + 6));
-            const uint4 meta = __ldg(reinterpret_cast<const uint4*>(np + 7));
+            uint4 meta;
+            ld_node(nb + node, b, ch, meta);
             rk = (((r.oct & 4u) ? meta.z : meta.y) >> ((r.oct & 3u) * 8u)) & 0xffu;
           }
           float tn[4];
