@@ -425,7 +425,7 @@ def _median_rel(a, ref):
 
 
 # The guided arm's configuration on the slit-light room (see guided_slit).
-GUIDE = dict(depth=2, alpha_max=0.9, lr=1e-2, train_batches=96, train_steps=32, batch_spp=8)
+GUIDE = dict(depth=2, alpha_max=0.5, lr=1e-2, train_batches=32, train_steps=32, batch_spp=8)
 
 
 def guided_slit(ctx, width=1024, plain_spp=256):
