@@ -625,7 +625,7 @@ def render_extras(ctx, args):
     import torch
     rng_sizes = np.exp(np.log(1000) + (np.log(200000) - np.log(1000)) * scenes.uniform(4, 64, 0)).astype(int)
     cam = scenes.coherent_rays(256)
-    jobs = []
+    jobs, host_jobs = [], []
     for j, nt in enumerate(rng_sizes):
         motion = j % 2 == 1
         if motion:
@@ -636,6 +636,7 @@ def render_extras(ctx, args):
         rays = cam.copy()
         rays[:, 7] = scenes.uniform(500 + j, rays.shape[0], 7).astype(np.float32) if motion else 0.0
         jobs.append((g, torch.from_numpy(np.ascontiguousarray(rays.T)).cuda()))
+        host_jobs.append((v, ip, motion, rays))
     nrays = sum(r.shape[1] for _, r in jobs)
     ctx.trace_jobs(jobs)
     _, jst = ctx.trace_jobs(jobs)
@@ -658,6 +659,23 @@ def render_extras(ctx, args):
     seq_tuned = per_job_ms()
     for g, _ in jobs:
         ctx.clear_tuning(g)
+    # the reference algorithm on the host: the oracle's restatement of
+    # qbvh.Trace / motion traversal, every job's rays one job at a time
+    # (traces timed, builds not), on all host threads and on the reference's
+    # default worker count
+    cpu = {}
+    meshes = [(orc.Mesh(v, ip, keys=2 if motion else 1, motion_fixed=motion), rays)
+              for v, ip, motion, rays in host_jobs]
+    for label, nt in (("all_threads", 0), ("reference_workers", REF_WORKERS)):
+        sample = meshes if nt == 0 else meshes[:8]
+        t0 = time.perf_counter()
+        nr = 0
+        for m, rays in sample:
+            m.trace(rays, nthreads=nt)
+            nr += rays.shape[0]
+        cpu[label] = {"mrays_per_s": round(nr / (time.perf_counter() - t0) / 1e6, 3),
+                      "threads": cpu_threads() if nt == 0 else nt, "jobs": len(sample), "rays": nr}
+    del meshes
     out["batched_jobs"] = {
         "workload": "64 triangle soups, sizes log-uniform in [1k, 200k] (seed 4), every other one with two-key "
                     "linear motion (velocity in a 0.05 ball), 256x256 camera rays each (times uniform in [0, 1) "
@@ -666,7 +684,11 @@ def render_extras(ctx, args):
         "one_launch_mrays_per_s": round(nrays / (jst["kernel_ms"] / 1e3) / 1e6, 2),
         "per_job_launches_mrays_per_s": round(nrays / (seq_default / 1e3) / 1e6, 2),
         "per_job_autotuned_mrays_per_s": round(nrays / (seq_tuned / 1e3) / 1e6, 2),
-        "autotune_s": round(tune_s, 2)}
+        "autotune_s": round(tune_s, 2),
+        "cpu_baseline": dict(cpu, kind="port",
+                             sample="all 64 jobs on all host threads; the first 8 jobs (4 static, 4 motion) on the "
+                                    "reference's default worker count; oracle/orc_core.cpp, C++ restatement of "
+                                    "qbvh.Trace and the motion traversal, one job after another")}
     # batched path-traced jobs: one launch per stage for all jobs, against one
     # vmr_render_path call per job (each job its own one-mesh scene)
     bj = scenes.batched_jobs()
