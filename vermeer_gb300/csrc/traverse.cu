@@ -878,25 +878,19 @@ __device__ __forceinline__ void fetch_node(const DMesh& m, int node, unsigned oc
 __device__ __forceinline__ void fetch_mnode(const MNode* mnodes, int node, unsigned oct, const float4* bx0,
                                             const float4* bx1, float tm, float omt, float4 (&b)[6], int4& ch,
                                             unsigned& rk) {
-  // each key's 6 box float4 (96 bytes, 32-byte aligned) in three 256-bit loads
-  float4 a[6], c[6];
-#pragma unroll
-  for (int q = 0; q < 6; q += 2) {
-    ld256(bx0 + (size_t)node * 6 + q, a[q], a[q + 1]);
-    ld256(bx1 + (size_t)node * 6 + q, c[q], c[q + 1]);
-  }
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
-    b[q].x = __fadd_rn(__fmul_rn(omt, a[q].x), __fmul_rn(tm, c[q].x));
-    b[q].y = __fadd_rn(__fmul_rn(omt, a[q].y), __fmul_rn(tm, c[q].y));
-    b[q].z = __fadd_rn(__fmul_rn(omt, a[q].z), __fmul_rn(tm, c[q].z));
-    b[q].w = __fadd_rn(__fmul_rn(omt, a[q].w), __fmul_rn(tm, c[q].w));
+    const float4 a = __ldg(bx0 + (size_t)node * 6 + q);
+    const float4 c = __ldg(bx1 + (size_t)node * 6 + q);
+    b[q].x = __fadd_rn(__fmul_rn(omt, a.x), __fmul_rn(tm, c.x));
+    b[q].y = __fadd_rn(__fmul_rn(omt, a.y), __fmul_rn(tm, c.y));
+    b[q].z = __fadd_rn(__fmul_rn(omt, a.z), __fmul_rn(tm, c.z));
+    b[q].w = __fadd_rn(__fmul_rn(omt, a.w), __fmul_rn(tm, c.w));
   }
-  float4 c4f, m4f;
-  ld256(mnodes + node, c4f, m4f);  // MNode: 32 bytes, 32-byte aligned
-  ch = make_int4(__float_as_int(c4f.x), __float_as_int(c4f.y), __float_as_int(c4f.z), __float_as_int(c4f.w));
-  const uint4 meta = make_uint4(__float_as_uint(m4f.x), __float_as_uint(m4f.y), __float_as_uint(m4f.z),
-                                __float_as_uint(m4f.w));
+  const uint4* mn = reinterpret_cast<const uint4*>(mnodes + node);
+  const uint4 c4 = __ldg(mn);
+  ch = make_int4((int)c4.x, (int)c4.y, (int)c4.z, (int)c4.w);
+  const uint4 meta = __ldg(mn + 1);
   rk = (((oct & 4u) ? meta.z : meta.y) >> ((oct & 3u) * 8u)) & 0xffu;
 }
 
