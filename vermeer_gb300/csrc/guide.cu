@@ -17,10 +17,11 @@
 //   k_guide_infer   forward for path vertices (features computed in-kernel)
 //   k_guide_train   forward, loss gradient at the outputs, backward-data
 //                   (dH = dZ * W through transposed weight copies), storing
-//                   every layer's input and output delta feature-major
+//                   every layer's input and output delta chunk-blocked
 //   k_guide_wgrad   weight gradients dW_l = dZ_{l+1}^T H_l as M = 64
-//                   tensor-core GEMMs whose K dimension is the batch,
-//                   operands double-buffered with cp.async
+//                   tensor-core GEMMs whose K dimension is the batch; each
+//                   chunk's operands are one bulk async copy each
+//                   (cp.async.bulk) through a 3-stage mbarrier pipeline
 //   k_guide_adam    Adam on float32 master weights, then the bf16 copies
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the error word,
@@ -111,30 +112,6 @@ __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
   }
   return false;
 }
-struct Shared {
-  uint64_t bar;
-  uint32_t tmem;
-  int abort;
-};
-
-// Every thread waits for the commit; the outcome is agreed by a block vote so
-// that all threads leave together (the loads that follow are warp-collective).
-__device__ __forceinline__ bool wait_all(Shared& sh, uint32_t& phase) {
-  const bool ok = bar_wait(&sh.bar, phase);
-  phase ^= 1u;
-  if (__syncthreads_or(ok ? 0 : 1)) {
-    if (threadIdx.x == 0) sh.abort = 1;
-    return false;
-  }
-  return true;
-}
-
-// After an abort: a second bounded wait for the MMAs still in flight, so
-// that the tensor memory they write is not freed under them.
-__device__ __forceinline__ void drain(Shared& sh, uint32_t phase) {
-  if (sh.abort) (void)bar_wait(&sh.bar, phase ^ 1u);
-}
-
 // 16 consecutive fp32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
@@ -523,13 +500,38 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_guide_infer(GuideRows in, 
   if (threadIdx.x < 32) tmem_free(tmem_base, kInferTmemCols);
 }
 
+// The saved activations and deltas, per section of R rows starting at
+// row0 (X: rows 0..79; h1..h4: 80 + 64 (l - 1); dY: 336, 48 rows; dZ4..dZ1:
+// 384 + 64 (4 - l)), are stored chunk-blocked: the 128 records of chunk c
+// form one block of R x 128 bf16 laid out [row group (R / 8)][record (128)]
+// [row % 8 (8)], a record's 8 consecutive rows in one 16-byte vector (one
+// store of the training kernel, consecutive across a warp's records).  The
+// block is the no-swizzle MN-major operand layout of a weight-gradient MMA
+// whose M (or N) is the section's rows and K the chunk's records: core
+// matrices of 8 records x 16 bytes (128 contiguous bytes), the next 8
+// records 128 bytes on (LBO), the next 8 rows 2048 bytes on (SBO).  A
+// chunk's operand is one contiguous block of 256 R bytes, moved by one bulk
+// copy.  The record stride B is a multiple of 128.  save_vec: the element
+// index of the vector holding rows 8 g .. 8 g + 7 of record b.
+__device__ __forceinline__ size_t save_vec(uint32_t row0, uint32_t R, uint32_t g, uint64_t b, uint32_t B) {
+  return (size_t)row0 * B + (size_t)(b >> 7) * (R * 128u) + (g * 128u + ((uint32_t)b & 127u)) * 8u;
+}
+// 8 fp32 values as 8 bf16 in one 16-byte store.
+__device__ __forceinline__ void save8(__nv_bfloat16* save, size_t at, const float* v) {
+  uint4 w;
+  w.x = pack2(v[0], v[1]);
+  w.y = pack2(v[2], v[3]);
+  w.z = pack2(v[4], v[5]);
+  w.w = pack2(v[6], v[7]);
+  *reinterpret_cast<uint4*>(save + at) = w;
+}
+
 // Training: forward + loss gradient + backward-data, four tile streams per
 // CTA (512 threads in groups of four warps, one CTA per SM) sharing both
 // weight copies; each group owns one 128 x 80 tile that holds the current
 // layer's input (forward), dY (K = 48) and then each dZ (backward), written
-// over the tile once the MMA that read it has completed.  Saved
-// feature-major (stride = batch size B): X rows 0..79, h1..h4 at 80 + 64*l,
-// dY at 336 (48 rows), dZ4..dZ1 at 384 + 64*(4-l) (l = 4..1).
+// over the tile once the MMA that read it has completed.  Every layer's
+// input and output delta is saved chunk-blocked (save_vec).
 constexpr uint32_t kTrainGroups = 4;
 constexpr uint32_t kTrainThreads = 128 * kTrainGroups;
 constexpr uint32_t kTrainCtl = kSBEnd + kTrainGroups * kSAGroup;
@@ -606,10 +608,13 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideTrain tr,
         om[1] = tr.oy[e];
         om[2] = tr.oz[e];
         if (tr.pb) pb = tr.pb[e];
-        for (int k = 0; k < 80; ++k) save[(size_t)k * B + row] = __float2bfloat16_rn(f[k]);
       } else {
         for (int k = 0; k < 80; ++k) f[k] = 0.f;
       }
+      // every row of the tile is saved (an invalid row as zeros), so the
+      // weight gradient reads whole 128-record chunks
+#pragma unroll
+      for (int g8 = 0; g8 < 10; ++g8) save8(save, save_vec(0, 80, g8, row, B), f + 8 * g8);
       put_row(a, r, 80, f);
     }
     // forward; mask[l] holds bit j for h_{l+1}[j] > 0 (two words a layer)
@@ -639,10 +644,9 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideTrain tr,
       mask[2 * l + 1] = m1;
       put_row(a, r, 64, h);
       fence_before();
-      if (valid) {  // feature-major copy of h_{l+1} for the weight gradient
-        __nv_bfloat16* dst = save + (size_t)(80 + 64 * l) * B + row;
-        for (int j = 0; j < 64; ++j) dst[(size_t)j * B] = __float2bfloat16_rn(h[j]);
-      }
+#pragma unroll
+      for (int g8 = 0; g8 < 8; ++g8)  // h_{l+1} for the weight gradient
+        save8(save, save_vec(80 + 64 * l, 64, g8, row, B), h + 8 * g8);
     }
     if (!ok) break;
     {
@@ -660,8 +664,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideTrain tr,
       }
       put_row(a, r, 48, gr);  // dY, K = 48
       fence_before();
-      if (valid)
-        for (int k = 0; k < 48; ++k) save[(size_t)(336 + k) * B + row] = __float2bfloat16_rn(gr[k]);
+#pragma unroll
+      for (int g8 = 0; g8 < 6; ++g8) save8(save, save_vec(336, 48, g8, row, B), gr + 8 * g8);
     }
     // dH_l = dZ_{l+1} * W_l, masked by h_l > 0, for l = 4 .. 1
 #pragma unroll 1
@@ -682,8 +686,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideTrain tr,
       }
       put_row(a, r, 64, d);
       fence_before();
-      if (valid)
-        for (int j = 0; j < 64; ++j) save[(size_t)(384 + 64 * (4 - l) + j) * B + row] = __float2bfloat16_rn(d[j]);
+#pragma unroll
+      for (int g8 = 0; g8 < 8; ++g8) save8(save, save_vec(384 + 64 * (4 - l), 64, g8, row, B), d + 8 * g8);
     }
     if (!ok) break;
   }
@@ -705,109 +709,123 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_guide_train(GuideTrain tr,
 }
 
 // Weight gradients: for layer l, D [64 x N] += A [64 x 128] * B [N x 128]^T
-// over chunks of 128 batch records (M = 64: the layer's output deltas, the
-// 41 outputs of the last layer padded with zero rows; N = the layer's 80 or
-// 64 inputs; K = the chunk's records), both operands K-major tiles loaded
-// from the feature-major save with cp.async into two stages: the loads of
-// chunk i+1 run while the MMAs of chunk i do.  blockIdx.y = layer,
-// blockIdx.x strides the chunks; the CTA's sum goes to the float32
-// gradient with atomics.  The M = 64 accumulator sits in TMEM lanes 0-15
-// of each 32-lane quarter (row 16q + j in lane 32q + j).
+// over chunks of 128 records (M = 64: the layer's output deltas, the last
+// layer's 48 saved dY rows read as 64 with rows 48..63 unused; N = the
+// layer's 80 or 64 inputs; K = the chunk's records).  Each operand of a
+// chunk is one contiguous block of the chunk-blocked save, fetched by one
+// bulk async copy (cp.async.bulk, completion counted on the stage's
+// mbarrier) into one of kWgStages stages; one thread issues the copies
+// kWgStages chunks ahead and the MMAs, whose commit frees the stage.
+// blockIdx.y = layer, blockIdx.x strides the chunks; the CTA's sum goes to
+// the float32 gradient with atomics.  The M = 64 accumulator sits in TMEM
+// lanes 0-15 of each 32-lane quarter (row 16q + j in lane 32q + j).
+constexpr uint32_t kWgStages = 3;
 constexpr uint32_t kWgStage = 64 * 128 * 2 + 80 * 128 * 2;  // A + B of one stage: 36864
-constexpr uint32_t kWgradSmem = 2 * kWgStage + 64;
+constexpr uint32_t kWgCtl = kWgStages * kWgStage;
+constexpr uint32_t kWgradSmem = kWgCtl + 2 * kWgStages * 8 + 16;
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(dst)), "l"(src) : "memory");
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   saddr(dst)),
+               "l"(src), "r"(bytes), "r"(saddr(bar))
+               : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+__device__ __forceinline__ void bar_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
 }
 
 __global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, uint32_t B, uint64_t n,
                                                      const unsigned long long* n_dev, float* grad, int* err) {
   extern __shared__ __align__(1024) char sm[];
-  __shared__ Shared sh;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + kWgCtl);
+  uint64_t* empty = full + kWgStages;
   const uint32_t r = threadIdx.x;
   if (n_dev) n = *n_dev < n ? *n_dev : n;
   const int l = blockIdx.y;
-  // layer l: output deltas at row dz0 (Mr of them), inputs at row in0 (N)
-  const uint32_t Mr = l == 4 ? (uint32_t)kGuideOut : 64u;
+  // layer l: output deltas (A, RA rows saved, 64 read) and inputs (B, N rows)
+  const uint32_t RA = l == 4 ? 48u : 64u;
   const uint32_t N = l == 0 ? 80u : 64u;
-  const uint32_t dz0 = l == 4 ? 336u : 384u + 64u * (3u - (uint32_t)l);
-  const uint32_t in0 = l == 0 ? 0u : 80u + 64u * (uint32_t)(l - 1);
+  const uint32_t a_row0 = l == 4 ? 336u : 384u + 64u * (3u - (uint32_t)l);
+  const uint32_t b_row0 = l == 0 ? 0u : 80u + 64u * (uint32_t)(l - 1);
+  const uint32_t Mr = l == 4 ? (uint32_t)kGuideOut : 64u;
   const uint32_t goff = l == 0 ? 0u : (l == 4 ? 17408u : 5120u + 4096u * (uint32_t)(l - 1));
+  const uint32_t a_bytes = RA * 256u, b_bytes = N * 256u;
   if (r == 0) {
-    bar_init(&sh.bar);
-    sh.abort = 0;
+    for (uint32_t st = 0; st < kWgStages; ++st) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(full + st)) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(empty + st)) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
   }
-  // zero both stages once (the padding rows Mr..63 of A stay zero)
-  for (uint32_t i = r; i < 2 * kWgStage / 16; i += 128) reinterpret_cast<uint4*>(sm)[i] = make_uint4(0, 0, 0, 0);
-  if (r < 32) tmem_alloc(&sh.tmem, 128);
+  // the A region of every stage is 64 rows: rows RA..63 of a 48-row block
+  // read the stage's other bytes, which only reach D rows >= 48 (unused)
+  for (uint32_t i = r; i < kWgStages * kWgStage / 16; i += 128) reinterpret_cast<uint4*>(sm)[i] = make_uint4(0, 0, 0, 0);
+  fence_async_smem();
+  if (r < 32) tmem_alloc(&tmem_slot, 128);
   fence_before();
   __syncthreads();
   fence_after();
   const uint64_t nchunks = (n + 127) / 128;
-  // the chunk's operand rows into stage st: 16 pieces of 8 records per row
-  auto issue = [&](uint64_t c, uint32_t st) {
-    char* A = sm + st * kWgStage;
-    char* Bt = A + 64 * 128 * 2;
-    const uint64_t b0 = c * 128;
-    for (uint32_t i = r; i < (Mr + N) * 16; i += 128) {
-      const uint32_t row = i / 16, ch = i % 16;
-      const bool isA = row < Mr;
-      const uint32_t src = isA ? dz0 + row : in0 + (row - Mr);
-      char* dst = isA ? A + chunk_off(row, ch, 128) : Bt + chunk_off(row - Mr, ch, 128);
-      const uint64_t col = b0 + 8 * ch;
-      if (col + 8 <= n) {
-        cp_async16(dst, save + (size_t)src * B + col);
-      } else {
-        union {
-          uint4 q;
-          __nv_bfloat16 h[8];
-        } tmp;
-        for (int e = 0; e < 8; ++e)
-          tmp.h[e] = col + e < n ? save[(size_t)src * B + col + e] : __float2bfloat16_rn(0.f);
-        *reinterpret_cast<uint4*>(dst) = tmp.q;
-      }
-    }
-    cp_async_commit();
-  };
-  uint32_t phase = 0;
-  bool ok = true;
-  uint64_t it = 0;
   const uint64_t first = blockIdx.x, step = gridDim.x;
-  if (first < nchunks) issue(first, 0);
-  for (uint64_t c = first; c < nchunks; c += step, ++it) {
-    const uint32_t st = (uint32_t)(it & 1u);
-    // the MMAs of the previous chunk read the other stage: wait for them
-    if (it > 0 && !wait_all(sh, phase)) {
-      ok = false;
-      break;
-    }
-    const bool more = c + step < nchunks;
-    if (more) {
-      issue(c + step, st ^ 1u);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    fence_async_smem();
-    __syncthreads();
-    if (r == 0) {
+  const uint64_t nloc = first < nchunks ? (nchunks - first + step - 1) / step : 0;
+  const __nv_bfloat16* a_src = save + (size_t)a_row0 * B;
+  const __nv_bfloat16* b_src = save + (size_t)b_row0 * B;
+  uint64_t issued = 0, done_mma = 0;
+  if (r == 0 && nloc > 0) {
+    auto issue = [&](uint64_t i) {
+      const uint32_t st = (uint32_t)(i % kWgStages);
+      const uint64_t c = first + i * step;
+      char* A = sm + st * kWgStage;
+      char* Bt = A + 64 * 128 * 2;
+      bar_expect(full + st, a_bytes + b_bytes);
+      bulk_copy(A, a_src + (size_t)c * (RA * 128u), a_bytes, full + st);
+      bulk_copy(Bt, b_src + (size_t)c * (N * 128u), b_bytes, full + st);
+    };
+    for (; issued < nloc && issued < kWgStages; ++issued) issue(issued);
+    const uint32_t id = idesc(64, (int)N) | (1u << 15) | (1u << 16);  // A and B MN-major
+    for (uint64_t i = 0; i < nloc; ++i) {
+      const uint32_t st = (uint32_t)(i % kWgStages);
+      const uint32_t par = (uint32_t)((i / kWgStages) & 1u);
+      if (!bar_wait(full + st, par)) {
+        abort_flag = 1;
+        break;
+      }
       fence_after();
       const uint32_t a0 = saddr(sm + st * kWgStage), bb = a0 + 64 * 128 * 2;
-      const uint32_t id = idesc(64, (int)N);
-      for (uint32_t kk = 0; kk < 8; ++kk)
-        mma(sh.tmem, sdesc(a0 + kk * 256u, 128u, 16u * 128u), sdesc(bb + kk * 256u, 128u, 16u * 128u), id,
-            (it > 0 || kk > 0) ? 1u : 0u);
-      mma_commit(&sh.bar);
+      for (uint32_t kk = 0; kk < 8; ++kk)  // K = 16: records 16 kk .. 16 kk + 15
+        mma(tmem_slot, sdesc(a0 + kk * 256u, 128u, 2048u), sdesc(bb + kk * 256u, 128u, 2048u), id,
+            (i > 0 || kk > 0) ? 1u : 0u);
+      mma_commit(empty + st);
+      done_mma = i + 1;
+      if (issued < nloc) {  // refill this stage once its MMAs have read it
+        if (!bar_wait(empty + st, par)) {
+          abort_flag = 1;
+          break;
+        }
+        issue(issued);
+        ++issued;
+      }
+    }
+    // the last commit of each stage still pending: wait for the final one
+    if (!abort_flag && done_mma > 0) {
+      const uint64_t i = done_mma - 1;
+      if (!bar_wait(empty + (uint32_t)(i % kWgStages), (uint32_t)((i / kWgStages) & 1u))) abort_flag = 1;
+    }
+    if (abort_flag) {
+      // bounded waits for the copies and MMAs still in flight
+      for (uint64_t i = done_mma; i < issued; ++i)
+        (void)bar_wait(full + (uint32_t)(i % kWgStages), (uint32_t)((i / kWgStages) & 1u));
+      if (done_mma > 0) {
+        const uint64_t i = done_mma - 1;
+        (void)bar_wait(empty + (uint32_t)(i % kWgStages), (uint32_t)((i / kWgStages) & 1u));
+      }
     }
   }
-  cp_async_wait<0>();
-  if (ok && it > 0 && !wait_all(sh, phase)) ok = false;
-  if (ok && it > 0) {
+  __syncthreads();
+  if (!abort_flag && nloc > 0) {
     fence_after();
     // every warp loads its lane quarter (warp-collective); row 16q + j is in
     // lane 32q + j for j < 16
@@ -816,16 +834,15 @@ __global__ void __launch_bounds__(128) k_guide_wgrad(const __nv_bfloat16* save, 
     const uint32_t row = 16u * q + j;
     for (uint32_t c16 = 0; c16 < N / 16; ++c16) {
       float v[16];
-      tmem_ld16(sh.tmem + lane_base + 16 * c16, v);
+      tmem_ld16(tmem_slot + lane_base + 16 * c16, v);
       if (j < 16 && row < Mr)
         for (int e = 0; e < 16; ++e) atomicAdd(&grad[goff + row * N + 16 * c16 + e], v[e]);
     }
   }
   fence_before();
   __syncthreads();
-  drain(sh, phase);
-  if (sh.abort && r == 0) atomicExch(err, 1);
-  if (r < 32) tmem_free(sh.tmem, 128);
+  if (abort_flag && r == 0) atomicExch(err, 1);
+  if (r < 32) tmem_free(tmem_slot, 128);
 }
 
 // Adam on the float32 masters (gradient divided by the batch's weight sum),
@@ -910,9 +927,14 @@ int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* sav
   return (int)cudaGetLastError();
 }
 
+// Two CTAs per SM (110 KB of stages each) over the five layers: about
+// 2 * sms / 5 CTAs per layer, fewer for a small batch (n bounds the device
+// count too).
 int launch_wgrad(const void* save, uint32_t B, uint64_t n, const unsigned long long* n_dev, float* grad, int* err,
-                 int chunks, cudaStream_t st) {
-  dim3 g(chunks, 5);
+                 int sms, cudaStream_t st) {
+  const uint64_t per_layer = std::max<uint64_t>(1, (uint64_t)(sms > 0 ? sms : 1) * 2 / 5);
+  const uint64_t chunks = std::max<uint64_t>(1, std::min<uint64_t>(per_layer, (n + 127) / 128));
+  dim3 g((unsigned)chunks, 5);
   k_guide_wgrad<<<g, 128, kWgradSmem, st>>>(static_cast<const __nv_bfloat16*>(save), B, n, n_dev, grad, err);
   return (int)cudaGetLastError();
 }
@@ -1065,12 +1087,10 @@ int guide_backprop(vmr_ctx* ctx, const GuideTrain& tr, size_t n) {
   t.stride = (uint32_t)stride;
   GCUDA(cudaMemsetAsync(G.sums.p, 0, 16, ctx->stream));
   const int sms = guide_sms(ctx);
-  const uint64_t tiles = (n + 127) / 128;
   if (vmr::guide::launch_train(t, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), sms,
                                ctx->stream) != 0)
     return gfail(ctx, VMR_ERR_CUDA, "guide training kernel launch failed");
-  const int chunks = (int)std::min<uint64_t>(tiles, (uint64_t)sms);
-  if (vmr::guide::launch_wgrad(G.save.p, (uint32_t)stride, n, nullptr, G.grad.as<float>(), G.err.as<int>(), chunks,
+  if (vmr::guide::launch_wgrad(G.save.p, (uint32_t)stride, n, nullptr, G.grad.as<float>(), G.err.as<int>(), sms,
                                ctx->stream) != 0)
     return gfail(ctx, VMR_ERR_CUDA, "guide weight-gradient kernel launch failed");
   return VMR_OK;

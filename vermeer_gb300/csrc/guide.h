@@ -11,7 +11,7 @@ namespace guide {
 constexpr int kGuideWeights = 20032;  // W0 64x80, W1..W3 64x64, W4 41x64
 constexpr int kGuideOut = 41;        // 8 lobes x 5, then the selection logit
 constexpr int kGuideOutStride = 44;  // floats per row of an inference output
-constexpr uint32_t kSaveRows = 640;   // feature-major rows saved per training record
+constexpr uint32_t kSaveRows = 640;   // values saved per training record (chunk-blocked)
 
 // Path vertices (SoA, device pointers): hit point, shading normal, direction
 // toward the previous vertex; n rows, or *n_dev rows when n_dev is set.  The
@@ -54,8 +54,10 @@ int launch_infer(const GuideRows& rows, const void* wf, float* out, int* err, in
 // sms: the device's SM count (the kernel runs at most one CTA per SM).
 int launch_train(const GuideTrain& tr, const void* wf, const void* wb, void* save, float* sums, int* err, int sms,
                  cudaStream_t st);
+// save: the training kernel's chunk-blocked activations (record stride B,
+// a multiple of 128); sms: the device's SM count.
 int launch_wgrad(const void* save, uint32_t B, uint64_t n, const unsigned long long* n_dev, float* grad, int* err,
-                 int chunks, cudaStream_t st);
+                 int sms, cudaStream_t st);
 int launch_adam(float* W, float* m, float* v, float* grad, const float* sums, const GuideAdam& a, void* wf, void* wb,
                 cudaStream_t st);
 

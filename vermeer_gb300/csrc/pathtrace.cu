@@ -1414,8 +1414,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
         PCUDA(cudaMemsetAsync(G.sums.p, 0, 16, st));
         if (guide::launch_train(tr, G.wf.p, G.wb.p, G.save.p, G.sums.as<float>(), G.err.as<int>(), sms, st) != 0)
           return pfail(ctx, VMR_ERR_CUDA, "guide training launch failed");
-        if (guide::launch_wgrad(G.save.p, stride, tbatch, ncount, G.grad.as<float>(), G.err.as<int>(),
-                                std::max(1, std::min(sms, (int)((tbatch + 127) / 128))), st) != 0)
+        if (guide::launch_wgrad(G.save.p, stride, tbatch, ncount, G.grad.as<float>(), G.err.as<int>(), sms, st) !=
+            0)
           return pfail(ctx, VMR_ERR_CUDA, "guide weight-gradient launch failed");
         guide::GuideAdam a{tlr, 0.9f, 0.999f, 1e-8f, ++G.step};
         if (guide::launch_adam(G.W.as<float>(), G.m.as<float>(), G.v.as<float>(), G.grad.as<float>(),
