@@ -258,17 +258,19 @@ def test_pt_converges_to_fp64_oracle(ctx, room, oracle_room):
 
 # --------------------------------------------------------- guided mode ----
 @pytest.mark.gpu
-@pytest.mark.parametrize("guide_depth", [0, 1, 3])
-def test_pt_guided_furnace_unbiased(ctx, guide_depth):
+@pytest.mark.parametrize("guide_depth,fixed", [(0, False), (1, False), (3, False), (0, True)])
+def test_pt_guided_furnace_unbiased(ctx, guide_depth, fixed):
     """One-sample MIS of an untrained (random) guide and the BSDF stays
     unbiased: the furnace still converges to albedo x environment, with
     every vertex guided and with only the first one or three (deeper
-    vertices sample the BSDF alone)."""
+    vertices sample the BSDF alone), with the network's per-vertex selection
+    probability and with one fixed probability."""
     sc = scenes.furnace(0.5, 1.0, subdiv=12)
     ctx.load_scene(sc)
     ctx.guide_init(3)
     fb64 = np.zeros((64, 64, 3), np.float64)
-    ctx.render_path(64, 64, 0, 512, 19, max_depth=8, rr_depth=1, fb64=fb64, guided=True, guide_depth=guide_depth)
+    ctx.render_path(64, 64, 0, 512, 19, max_depth=8, rr_depth=1, fb64=fb64, guided=True, guide_depth=guide_depth,
+                    fixed_selection=fixed)
     on, off = _disc_masks(64, 64)
     v = fb64[on][:, 0]
     assert abs(v.mean() - 0.5) < 5 * v.std() / np.sqrt(v.size), (v.mean(), v.std())
