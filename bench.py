@@ -599,7 +599,7 @@ def render_extras(ctx, args):
     fb, st = ctx.render_path(W, H, 0, 64, 3, max_depth=8)
     out["extended_sphere_grid"] = {
         "workload": "16x16 displaced spheres x 8,192 tris + ground, 4 quad lights + environment, 1920x1080, "
-                    "depth 8, RR from 3, 64 spp",
+                    "depth 8, RR from 3, 64 spp; the scene traced flattened (one mesh over all triangles)",
         "samples_per_s": round(W * H * 64 / (st["ms"] / 1e3), 1),
         "mrays_per_s": round((st["rays"] + st["shadow_rays"]) / (st["ms"] / 1e3) / 1e6, 2),
         "device_ms": round(st["ms"], 3), "rays": st["rays"], "shadow_rays": st["shadow_rays"],
@@ -612,6 +612,11 @@ def render_extras(ctx, args):
         _, s16 = ctx.render_path(W, H, 0, 16, 3, max_depth=8, sort_queues=srt)
         qs["sorted" if srt else "queue_order"] = round(W * H * 16 / (s16["ms"] / 1e3), 1)
     out["extended_sphere_grid"]["queue_sort_samples_per_s_16spp"] = qs
+    # the two-level traversal (VMR_PATH_TWO_LEVEL) against the flattened
+    # scene the renders above trace, 16 spp each
+    ctx.render_path(W, H, 0, 2, 3, max_depth=8, two_level=True)
+    _, s16 = ctx.render_path(W, H, 0, 16, 3, max_depth=8, two_level=True)
+    out["extended_sphere_grid"]["two_level_samples_per_s_16spp"] = round(W * H * 16 / (s16["ms"] / 1e3), 1)
     # queue capacity chosen by the path autotuner (8 spp per candidate)
     t0 = time.perf_counter()
     best, table = ctx.autotune_path(W, H, 8, seed=3, max_depth=8)

@@ -616,11 +616,20 @@ enum {
                                and shadow queue in ray-key order (direction
                                class + Morton cell of the origin, the
                                tuning's sort-key width); images unchanged */
-    VMR_PATH_FIXED_SELECTION = 16 /* VMR_PATH_GUIDED: every vertex samples the
+    VMR_PATH_FIXED_SELECTION = 16, /* VMR_PATH_GUIDED: every vertex samples the
                                guide with probability guide_fraction (the
                                network's selection output unused, and with
                                TRAIN the guide is fitted to the product
                                alone, not to the vertex's full density) */
+    VMR_PATH_TWO_LEVEL = 32 /* trace the two-level scene even when it can be
+                               flattened: by default a scene of static,
+                               untransformed triangle meshes with one ray bias
+                               is traced as one mesh over all its triangles
+                               (built once per scene by the device builder),
+                               its hits mapped back to (geom, triangle); the
+                               closest hit is the same triangle either way
+                               (only exact ties in t between two triangles may
+                               resolve differently) */
 };
 
 typedef struct {

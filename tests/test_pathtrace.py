@@ -256,6 +256,28 @@ def test_pt_converges_to_fp64_oracle(ctx, room, oracle_room):
     assert _block_relmse(g64, o64) < 0.01
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["room", "spheres"])
+def test_pt_flattened_scene_equals_two_level(ctx, kind):
+    """A scene of static, untransformed triangle meshes is traced as one flat
+    mesh over all its triangles, hits mapped back to (geom, triangle): the
+    image equals the two-level traversal's (VMR_PATH_TWO_LEVEL) pixel for
+    pixel, but for the rare path whose closest hit is an exact tie in t
+    between two triangles."""
+    if kind == "room":
+        sc = scenes.small_room_ext(4096, seed=8)
+        W, H = 64, 48
+    else:
+        sc = scenes.sphere_grid(per_side=4, subdiv=8, width=96, height=64)
+        W, H = 96, 64
+    ctx.load_scene(sc)
+    a, sa = ctx.render_path(W, H, 0, 8, 5, max_depth=6)
+    b, sb = ctx.render_path(W, H, 0, 8, 5, max_depth=6, two_level=True)
+    same = np.all(a == b, axis=-1).mean()
+    assert same >= 0.999, same
+    assert abs(sa["rays"] - sb["rays"]) <= 0.001 * sb["rays"]
+
+
 # --------------------------------------------------------- guided mode ----
 @pytest.mark.gpu
 @pytest.mark.parametrize("guide_depth,fixed", [(0, False), (1, False), (3, False), (0, True)])

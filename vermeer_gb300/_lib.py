@@ -143,6 +143,7 @@ PATH_GUIDED = 2
 PATH_TRAIN = 4
 PATH_SORT_QUEUES = 8
 PATH_FIXED_SELECTION = 16
+PATH_TWO_LEVEL = 32
 
 GUIDE_WEIGHTS = 20032
 GUIDE_OUTPUTS = 41

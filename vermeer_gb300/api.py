@@ -402,7 +402,7 @@ class Context:
                     rr_depth: int = 3, fb=None, fb64=None, max_batch_samples: int = 0, graph: bool = True,
                     guided: bool = False, train: bool = False, guide_fraction: float = 0.0, train_steps: int = 0,
                     train_batch: int = 0, train_lr: float = 0.0, sort_queues: bool = False, guide_depth: int = 0,
-                    rows=None, fixed_selection: bool = False):
+                    rows=None, fixed_selection: bool = False, two_level: bool = False):
         """The extended path tracer: iterations [iter_begin, iter_begin +
         iter_count) folded into fb (float32 [height, width, 3]) and, when
         given, fb64 (float64).  guided: sample the guide network too; train:
@@ -410,6 +410,7 @@ class Context:
         path (0: all); guide_fraction: alpha_max of the learned selection
         (0: 0.9), or with fixed_selection the guide's probability at every
         vertex (0: 0.5); sort_queues: trace each queue in ray-key order;
+        two_level: trace the two-level scene even when it can be flattened;
         rows: (row_begin, row_count), a band of the image (fb then holds
         row_count rows).  Returns (fb, stats)."""
         r0, nr = rows if rows is not None else (0, 0)
@@ -421,7 +422,7 @@ class Context:
             assert fb64.dtype == np.float64 and fb64.flags.c_contiguous and fb64.shape == (hb, width, 3)
         p = self._path_params(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, fb64,
                               max_batch_samples, graph, guided, train, guide_fraction, train_steps, train_batch,
-                              train_lr, sort_queues, guide_depth, r0, nr, fixed_selection)
+                              train_lr, sort_queues, guide_depth, r0, nr, fixed_selection, two_level)
         st = _lib.PathStats()
         self._check(self.L.vmr_render_path(self.h, ctypes.byref(p), _p(fb), ctypes.byref(st)))
         return fb, dict(samples=st.samples, rays=st.rays, shadow_rays=st.shadow_rays,
@@ -432,10 +433,10 @@ class Context:
     def _path_params(width, height, iter_begin, iter_count, seed, max_depth=4, rr_depth=3, fb64=None,
                      max_batch_samples=0, graph=True, guided=False, train=False, guide_fraction=0.0, train_steps=0,
                      train_batch=0, train_lr=0.0, sort_queues=False, guide_depth=0, row_begin=0, row_count=0,
-                     fixed_selection=False):
+                     fixed_selection=False, two_level=False):
         flags = (0 if graph else _lib.PATH_NO_GRAPH) | (_lib.PATH_GUIDED if guided else 0) | \
                 (_lib.PATH_TRAIN if train else 0) | (_lib.PATH_SORT_QUEUES if sort_queues else 0) | \
-                (_lib.PATH_FIXED_SELECTION if fixed_selection else 0)
+                (_lib.PATH_FIXED_SELECTION if fixed_selection else 0) | (_lib.PATH_TWO_LEVEL if two_level else 0)
         return _lib.PathParams(width, height, iter_begin, iter_count, seed, max_depth, rr_depth, max_batch_samples,
                                flags, None if fb64 is None else _p(fb64), guide_fraction, train_steps, train_batch,
                                train_lr, guide_depth, row_begin, row_count)

@@ -200,6 +200,8 @@ void matrix4_inverse(const float m[16], float c[16]) { vmr::anim::inverse(m, c);
 
 int refresh_top(vmr_ctx* ctx) {
   TopRec& t = ctx->top;
+  ctx->flat.tried = false;  // a flattened copy of the old top level is stale
+  ctx->flat.rec.reset();
   if (ctx->device < 0) return VMR_OK;
   // Device mesh table indexed by geom id.
   std::vector<DMesh> table(ctx->meshes.size());
@@ -383,6 +385,82 @@ int trace_host(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays* rays, size_t n, 
 }
 
 }  // namespace
+
+namespace vmr {
+const DMesh* flat_scene(vmr_ctx* ctx, const uint32_t** map, uint32_t* n, int* status) {
+  *status = VMR_OK;
+  FlatScene& F = ctx->flat;
+  if (F.tried) {
+    if (!F.rec) return nullptr;
+    *map = F.map.as<uint32_t>();
+    *n = F.n;
+    return &F.rec->dmesh;
+  }
+  F.tried = true;
+  F.rec.reset();
+  const TopRec& top = ctx->top;
+  if (ctx->device < 0 || !top.valid || !top.dtop.all_static || top.dtop.simple_only || top.host.keys > 1) return nullptr;
+  const std::vector<uint32_t>& order = top.host.geom_order;
+  if (order.size() < 2) return nullptr;
+  float bias = 0.0f;
+  uint64_t total = 0;
+  for (size_t i = 0; i < order.size(); ++i) {
+    const MeshRec& r = *ctx->meshes[order[i]];
+    const HostMesh& m = r.host;
+    if (m.sphere || m.group || m.motion() || r.has_xf || r.xkeys.size() >= 2 || m.n_tris == 0) return nullptr;
+    if (i == 0) bias = m.ray_bias;
+    else if (m.ray_bias != bias) return nullptr;
+    total += m.n_tris;
+  }
+  if (total >= (1u << 23)) return nullptr;  // a mesh's leaf base limit (qbvh.LeafBase)
+  const uint32_t T = (uint32_t)total;
+  auto rec = std::make_unique<MeshRec>();
+  HostMesh& fm = rec->host;
+  fm.keys = 1;
+  fm.n_tris = T;
+  fm.n_verts = 3 * T;
+  fm.ray_bias = bias;
+  fm.verts.resize((size_t)9 * T);
+  fm.idxp.resize((size_t)3 * T);
+  std::vector<uint32_t> fgeom(T), fprim(T);
+  uint32_t c = 0;
+  for (uint32_t g : order) {
+    const HostMesh& m = ctx->meshes[g]->host;
+    for (uint32_t j = 0; j < m.n_tris; ++j, ++c) {  // the geom's leaf order
+      for (int k = 0; k < 3; ++k) {
+        const float* v = &m.verts[(size_t)m.idxp[(size_t)3 * j + k] * 3];
+        std::memcpy(&fm.verts[((size_t)3 * c + k) * 3], v, 12);
+        fm.idxp[(size_t)3 * c + k] = 3 * c + (uint32_t)k;
+      }
+      fgeom[c] = g;
+      fprim[c] = j;
+    }
+  }
+  std::string why;
+  if (vmr::device_build_mesh(fm, rec->tris, ctx->stream, why) != vmr::kBuildOk) return nullptr;
+  if ((*status = upload_mesh(ctx, *rec, true)) != VMR_OK) return nullptr;
+  std::vector<uint32_t> tab((size_t)2 * T);
+  for (uint32_t e = 0; e < T; ++e) {
+    const uint32_t f = (uint32_t)fm.accel_idx[e];
+    tab[e] = fgeom[f];
+    tab[(size_t)T + e] = fprim[f];
+  }
+  cudaError_t ce = upload(ctx, F.map, tab);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  if (ce != cudaSuccess) {
+    *status = cuda_fail(ctx, ce, "flattened scene upload");
+    return nullptr;
+  }
+  // the host copies are not needed again
+  std::vector<float>().swap(fm.verts);
+  std::vector<uint32_t>().swap(fm.idxp);
+  F.rec = std::move(rec);
+  F.n = T;
+  *map = F.map.as<uint32_t>();
+  *n = T;
+  return &F.rec->dmesh;
+}
+}  // namespace vmr
 
 namespace vmr {
 // Read-only view of a context's mesh and settings for vmr_trace_mesh_noalloc

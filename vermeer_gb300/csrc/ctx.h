@@ -134,6 +134,19 @@ struct TopRec {
 // reference rebuilds from its decomposition (render.cu).
 vmr_camera camera_round_trip(const vmr_camera& c);
 
+// A static scene flattened into one mesh for the extended path tracer's
+// traces: every triangle of every top-level geom (each geom's triangles in
+// its leaf order) in one QBVH, and per leaf position of that QBVH the geom
+// and the geom's own leaf position the hit reports (map[e], map[n + e]).
+// Built once per scene, on the first render that can use it; any change of
+// the top level drops it.
+struct FlatScene {
+  bool tried = false;  // the current top level was examined
+  std::unique_ptr<MeshRec> rec;  // nullptr: the scene does not qualify
+  DevBuf map;
+  uint32_t n = 0;
+};
+
 }  // namespace vmr
 
 using vmr::DevBuf;
@@ -153,6 +166,7 @@ struct vmr_ctx {
   cudaEvent_t rev0 = nullptr, rev1 = nullptr;
   std::vector<std::unique_ptr<MeshRec>> meshes;
   TopRec top;
+  vmr::FlatScene flat;
   vmr::RenderState render;
   vmr::GuideState guide;
   vmr_tuning tuning{45, 0, 0, 0, 8, 0};
@@ -173,3 +187,13 @@ struct vmr_ctx {
   }
 };
 
+
+namespace vmr {
+// The context's flattened scene (capi.cpp), built on the first call that
+// asks for it: the flat mesh, or nullptr when the scene does not qualify
+// (a motion, transformed, sphere, instance or Proc geom, geoms with
+// different ray biases, fewer than two geoms, or a build the device
+// builder declines).  *map / *n: the leaf position -> (geom, leaf position)
+// table on the device and its length.  Returns a VMR status in *status.
+const DMesh* flat_scene(vmr_ctx* ctx, const uint32_t** map, uint32_t* n, int* status);
+}  // namespace vmr

@@ -155,9 +155,10 @@ struct TraceLaunch {
   HitSoA hits;
   const uint32_t* order;  // rays[i] is input ray order[i] (nullptr: identity)
   uint64_t n;
-  const unsigned long long* n_dev;  // scene traces: if set, the ray count is read
-                                    // from device memory when the kernel starts
-                                    // (wavefront queues; n is then a capacity)
+  const unsigned long long* n_dev;  // if set, the ray count is read from device
+                                    // memory when the kernel starts (wavefront
+                                    // queues; n is then a capacity); scene
+                                    // traces and the while-while mesh kernels
   int any_hit;
   int count;
   DScratch* scratch;

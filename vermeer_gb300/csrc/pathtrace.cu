@@ -887,8 +887,34 @@ struct PtSort {
   float* rays = nullptr;  // 8 * cap floats
 };
 
+// The flattened scene (vmr::flat_scene) the bounce loop traces instead of
+// the two-level scene: one mesh over every triangle, its hits mapped back to
+// (geom, the geom's leaf position) by k_flat_remap.
+struct PtFlat {
+  const DMesh* mesh = nullptr;
+  const uint32_t* map = nullptr;  // [2 * n]: geom, then the geom's leaf position
+  uint32_t n = 0;
+};
+
+// Closest hits of a flattened-scene trace back to the scene's ids: the flat
+// mesh's leaf position e becomes geom map[e] and triangle map[n + e].
+__global__ void __launch_bounds__(kPtBlock) k_flat_remap(const uint32_t* __restrict__ map, uint32_t n,
+                                                          int32_t* prim, int32_t* geom,
+                                                          const unsigned long long* qlen, uint64_t cap) {
+  const uint64_t m = *qlen < cap ? *qlen : cap;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int32_t e = prim[i];
+    if (e >= 0 && (uint32_t)e < n) {
+      geom[i] = (int32_t)__ldg(map + e);
+      prim[i] = (int32_t)__ldg(map + n + e);
+    } else {
+      geom[i] = -1;
+    }
+  }
+}
+
 int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr, int grid, bool guided, bool train,
-                 const guide::GuideRows& grows, const PtSort& srt) {
+                 const guide::GuideRows& grows, const PtSort& srt, const PtFlat& flat) {
   cudaStream_t st = ctx->stream;
   auto sort_queue = [&](TraceLaunch& l) -> int {
     const size_t c = b.cap;
@@ -926,7 +952,13 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
     }
     // camera rays are traced in pixel order (already coherent)
     if (srt.on && d > 0 && sort_queue(l) != 0) return pfail(ctx, VMR_ERR_CUDA, "ray sort launch failed");
-    if (launch_trace_scene(top, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+    if (flat.mesh) {
+      if (launch_trace_mesh(*flat.mesh, l) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+      k_flat_remap<<<grid, kPtBlock, 0, st>>>(flat.map, flat.n, b.hprim, b.hgeom, &b.qlen[d], b.cap);
+      PCUDA(cudaGetLastError());
+    } else if (launch_trace_scene(top, l) != 0) {
+      return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+    }
     // vertices past the guided depth sample the BSDF alone (and record nothing)
     const bool gd = guided && d < b.gdepth;
     if (gd) {
@@ -961,7 +993,9 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
         s.path_geom = b.pgeom;
       }
       if (srt.on && sort_queue(s) != 0) return pfail(ctx, VMR_ERR_CUDA, "ray sort launch failed");
-      if (launch_trace_scene(top, s) != 0) return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
+      // shadow rays need hit or miss only: the flat mesh's prim is enough
+      if ((flat.mesh ? launch_trace_mesh(*flat.mesh, s) : launch_trace_scene(top, s)) != 0)
+        return pfail(ctx, VMR_ERR_CUDA, "trace launch failed");
       if (train && gd) k_pt_resolve<true><<<grid, kPtBlock, 0, st>>>(b, d);
       else k_pt_resolve<false><<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
@@ -1261,6 +1295,12 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   b.jobs = jobs ? reinterpret_cast<const PtJob*>(base + o_jobs) : nullptr;
   b.n_jobs = jobs ? n_jobs : 0u;
   b.pgeom = jobs ? reinterpret_cast<uint32_t*>(base + o_pgeom) : nullptr;
+  PtFlat flat;
+  if (!jobs && !(p->flags & VMR_PATH_TWO_LEVEL) && (ctx->tuning.kernel & kKernelWhileWhile)) {
+    int fs = VMR_OK;
+    flat.mesh = flat_scene(ctx, &flat.map, &flat.n, &fs);
+    if (fs != VMR_OK) return fs;
+  }
   PtSort srt;
   if (sort_on) {
     srt.on = true;
@@ -1329,7 +1369,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
                                (uint64_t)train, (uint64_t)(uintptr_t)ctx->guide.wf.p, rcap,
                                (uint64_t)ctx->tuning.kernel, (uint64_t)ctx->tuning.walk_tail,
                                (uint64_t)ctx->tuning.blocks_per_sm,
-                               (uint64_t)ctx->tuning.sort_bits, (uint64_t)sort_on};
+                               (uint64_t)ctx->tuning.sort_bits, (uint64_t)sort_on,
+                               (uint64_t)(uintptr_t)flat.mesh, (uint64_t)(uintptr_t)flat.map};
   {
     uint64_t h = 1469598103934665603ull;
     auto fold = [&](const void* d, size_t nb) {
@@ -1361,7 +1402,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
     }
     cudaGraph_t g = nullptr;
     PCUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-    const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows, srt);
+    const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows, srt, flat);
     const cudaError_t ec = cudaStreamEndCapture(st, &g);
     if (rc != VMR_OK) {
       if (g) cudaGraphDestroy(g);
@@ -1380,7 +1421,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
       PCUDA(cudaGraphLaunch(R.graph.exec, st));
       ++replays;
     } else {
-      const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows, srt);
+      const int rc = launch_batch(ctx, b, top, scr, grid, guided, train, grows, srt, flat);
       if (rc != VMR_OK) return rc;
     }
     if (train) {  // online training on this batch's records (device counts)

@@ -1235,7 +1235,8 @@ __device__ __forceinline__ int32_t coop_leaf_dispatch(const float4* tris, float 
 template <bool MOTION, bool ANY, bool COUNT, bool PF, int MINB, int SS, bool COOP = false>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
     k_trace_mesh_ww(const DMesh m, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch, const uint32_t* order,
-                    int walk_tail) {
+                    int walk_tail, const unsigned long long* n_dev) {
+  if (n_dev) n = *n_dev < n ? *n_dev : n;  // a wavefront queue's length
   extern __shared__ int stack_smem[];
   SplitStack<SS> stk;
   if (SS > 0) {
@@ -2087,17 +2088,17 @@ int launch_ww(const DMesh& mesh, const TraceLaunch& l, int block) {
   const int tail = l.walk_tail;
   if ((l.kernel & kKernelCoopLeaf) && !(l.kernel & (kKernelSharedStack | kKernelPrefetch)))
     return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, 0, true>, l, block, mesh, l.rays, l.hits,
-                             l.n, l.scratch, l.order, tail);
+                             l.n, l.scratch, l.order, tail, l.n_dev);
   if (l.kernel & kKernelSharedStack) {
     constexpr int SS = kSharedStackEntries;
     return launch_persistent_smem(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, SS>, l, block,
-                                  (size_t)SS * block * 8, mesh, l.rays, l.hits, l.n, l.scratch, l.order, tail);
+                                  (size_t)SS * block * 8, mesh, l.rays, l.hits, l.n, l.scratch, l.order, tail, l.n_dev);
   }
   if (l.kernel & kKernelPrefetch)
     return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, true, MINB, 0>, l, block, mesh, l.rays, l.hits, l.n,
-                             l.scratch, l.order, tail);
+                             l.scratch, l.order, tail, l.n_dev);
   return launch_persistent(k_trace_mesh_ww<MOTION, ANY, COUNT, false, MINB, 0>, l, block, mesh, l.rays, l.hits, l.n,
-                           l.scratch, l.order, tail);
+                           l.scratch, l.order, tail, l.n_dev);
 }
 
 template <bool MOTION, bool ANY, bool COUNT>
