@@ -117,7 +117,7 @@ struct GuideState {
   bool ready = false;
   int step = 0;
   DevBuf W, m, v, grad, wf, wb, sums, err;
-  DevBuf save;          // bf16 feature-major activations and deltas
+  DevBuf save;          // bf16 activations and deltas, chunk-blocked (guide.cu save_vec)
   uint32_t save_rows = 0;
   DevBuf io;            // host-call staging (SoA rows, outputs)
 };

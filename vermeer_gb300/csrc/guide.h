@@ -35,7 +35,7 @@ struct GuideTrain {
   const float *ox, *oy, *oz, *weight;
   const float* pb;  // nullptr: the guide's own density
   float amax;
-  uint32_t stride;  // rows of the save buffer's feature-major arrays
+  uint32_t stride;  // records the save buffer holds (a multiple of 128)
 };
 
 struct GuideAdam {
