@@ -278,6 +278,19 @@ def test_pt_flattened_scene_equals_two_level(ctx, kind):
     assert abs(sa["rays"] - sb["rays"]) <= 0.001 * sb["rays"]
 
 
+@pytest.mark.gpu
+def test_pt_scene_that_cannot_be_flattened_is_traced_two_level(ctx):
+    """A scene whose meshes have different ray biases (or a transform, motion
+    keys, spheres, instances) is not flattened: the default render is the
+    two-level render bit for bit."""
+    sc = scenes.small_room_ext(4096, seed=9)
+    sc["meshes"][1] = dict(sc["meshes"][1], ray_bias=1e-4)
+    ctx.load_scene(sc)
+    a, _ = ctx.render_path(48, 40, 0, 4, 6, max_depth=5)
+    b, _ = ctx.render_path(48, 40, 0, 4, 6, max_depth=5, two_level=True)
+    assert a.tobytes() == b.tobytes()
+
+
 # --------------------------------------------------------- guided mode ----
 @pytest.mark.gpu
 @pytest.mark.parametrize("guide_depth,fixed", [(0, False), (1, False), (3, False), (0, True)])

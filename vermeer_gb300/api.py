@@ -621,6 +621,7 @@ class Context:
                 ids[i] = self.sphere_add(m["sphere"][:3], m["sphere"][3])
             elif "verts" in m:
                 g = self.mesh_build(m["verts"], m["idxp"], keys=m.get("keys", 1),
+                                    ray_bias=m.get("ray_bias", 0.0),
                                     motion_mode=m.get("motion_mode", MOTION_FAITHFUL),
                                     shader_idx=m.get("face_shader"))
                 if m.get("transform_keys") is not None:
