@@ -4,6 +4,9 @@
                                                        and one training step of 256K
     python profile_cases.py render_ext   extended path tracer, sphere grid,
                                                        1920x1080, 2 spp, depth 8
+    python profile_cases.py render_ext_flat / render_ext_two_level
+                                         the same render twice, the scene
+                                                       flattened or two-level
     python profile_cases.py render_ref   reference-mode render, small room,
                                                        256x256, 16 iterations
     python profile_cases.py render_ref_f32  the same with float32 shading
@@ -41,6 +44,22 @@ def render_ext(ctx):
     sc = scenes.sphere_grid()
     ctx.load_scene(sc)
     ctx.render_path(sc["width"], sc["height"], 0, 2, 3, max_depth=8)
+
+
+def _render_ext_twice(ctx, two_level):
+    from vermeer_gb300 import scenes
+    sc = scenes.sphere_grid()
+    ctx.load_scene(sc)
+    for _ in range(2):
+        ctx.render_path(sc["width"], sc["height"], 0, 2, 3, max_depth=8, two_level=two_level)
+
+
+def render_ext_flat(ctx):
+    _render_ext_twice(ctx, False)
+
+
+def render_ext_two_level(ctx):
+    _render_ext_twice(ctx, True)
 
 
 def render_ref(ctx):
@@ -97,7 +116,8 @@ def build(ctx):
     ctx.mesh_build(v, ip)
 
 
-CASES = {"guide": guide, "render_ext": render_ext, "render_ref": render_ref, "render_ref_f32": render_ref_f32,
+CASES = {"guide": guide, "render_ext": render_ext, "render_ext_flat": render_ext_flat,
+         "render_ext_two_level": render_ext_two_level, "render_ref": render_ref, "render_ref_f32": render_ref_f32,
          "jobs": jobs, "path_jobs": path_jobs, "build": build}
 
 

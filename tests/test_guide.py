@@ -200,6 +200,21 @@ def test_guide_gradient_matches_oracle(ctx, orc, mixed):
 
 
 @pytest.mark.gpu
+def test_guide_selection_bound_is_checked(ctx):
+    """With BSDF densities the selection's bound alpha_max must lie in
+    (0, 1); the call is refused before any launch otherwise."""
+    import vermeer_gb300 as vg
+    ctx.guide_init(1)
+    pos, nrm, wo, om, wt = _batch(64, 3)
+    pb = _bsdf_pdf(nrm, om)
+    for bad in (0.0, 1.0, 1.5):
+        with pytest.raises(vg.VmrError):
+            ctx.guide_gradient(pos, nrm, wo, om, wt, LO, HI, bsdf_pdf=pb, alpha_max=bad)
+    g, loss = ctx.guide_gradient(pos, nrm, wo, om, wt, LO, HI, bsdf_pdf=pb, alpha_max=0.5)
+    assert np.isfinite(loss) and np.isfinite(g).all()
+
+
+@pytest.mark.gpu
 def test_guide_training_fits_a_lobe(ctx):
     """Directions drawn around one axis: Adam steps on the guide's loss make
     the mixture put its mass there."""
