@@ -193,30 +193,29 @@ constexpr uint32_t kSB1 = kSWEnd, kSB2 = kSB1 + 8192, kSB3 = kSB2 + 8192, kSB4 =
 constexpr int kLobes = 8;
 
 // Input features of a vertex (the encoding the oracle's guide_features
-// restates).  sin and cos of pi 2^k q are evaluated exactly (sincospif) at
-// k = 0, 4, 8 and carried to the next three frequencies by the double-angle
-// identities sin 2x = 2 sin x cos x, cos 2x = (cos x - sin x)(cos x + sin x):
-// nine calls instead of 36 per row, with an absolute error below 1e-6 after
-// three doublings, far under the bf16 rounding the features then get.
+// restates), for the training kernel.  sin and cos of pi 2^k q are exact
+// (sincospif) at k = 0 and 8 and carried to the other frequencies by the
+// double-angle identities sin 2x = 2 sin x cos x, cos 2x = (cos x - sin x)
+// (cos x + sin x): at most seven steps, an absolute error below 2e-5, far
+// under the bf16 rounding the features then get (the inference kernel
+// builds the same values in freq_words).
 __device__ void features(const float* p, const float* n, const float* wo, const float* lo, const float* inv_ext,
                          float* f) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float q = (p[c] - lo[c]) * inv_ext[c];
+    float s = 0.f, co = 1.f;
 #pragma unroll
-    for (int a = 0; a < 12; a += 4) {
-      float s, co;
-      sincospif(ldexpf(q, a), &s, &co);
-      f[24 * c + 2 * a] = s;
-      f[24 * c + 2 * a + 1] = co;
-#pragma unroll
-      for (int k = a + 1; k < a + 4; ++k) {
+    for (int k = 0; k < 12; ++k) {
+      if (k == 0 || k == 8) {
+        sincospif(ldexpf(q, k), &s, &co);
+      } else {
         const float s2 = 2.0f * s * co;
         co = (co - s) * (co + s);
         s = s2;
-        f[24 * c + 2 * k] = s;
-        f[24 * c + 2 * k + 1] = co;
       }
+      f[24 * c + 2 * k] = s;
+      f[24 * c + 2 * k + 1] = co;
     }
   }
 #pragma unroll
