@@ -380,6 +380,8 @@ __device__ V3 gmix_sample(const GMix& g, float u, float u1, float u2) {
                       w * mu.z + st * (cp * t1.z + sp * t2.z)));
 }
 
+// CKEYS: the camera has motion keys (b.cam_nkeys >= 2).
+template <bool CKEYS>
 __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
   const uint64_t n = b.it->n < b.cap ? b.it->n : b.cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) b.qlen[0] = n;
@@ -398,11 +400,11 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
       const PtJob& job = b.jobs[lo];
       pix -= job.pix0;
       b.pgeom[s] = job.geom;
-      camera_primary(job.cam, nullptr, 0, job.width, job.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+      camera_primary<false>(job.cam, nullptr, 0, job.width, job.height, j, pix, b.seed, b.filt, P, D, time, lambda);
     } else {
       pix += b.pix0;  // the image pixel: a band samples as the whole image does
-      camera_primary(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D, time,
-                     lambda);
+      camera_primary<CKEYS>(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D,
+                            time, lambda);
     }
     const float o[3] = {P.x, P.y, P.z};
     put_ray(b.qray[0], b.cap, s, o, D, __int_as_float(0x7f800000), time);
@@ -429,7 +431,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
       uint32_t shid = 0;
       const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
       const V3 Rd = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
-      if (surface_attributes(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i],
+      if (surface_attributes<false>(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i],
                              q[7 * (size_t)b.cap + i], sc, shid)) {
         wi = v3(-q[3 * (size_t)b.cap + i], -q[4 * (size_t)b.cap + i], -q[5 * (size_t)b.cap + i]);
         P = sc.P;
@@ -446,9 +448,11 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
 
 // One bounce of every path in queue d.  GUIDED: one-sample MIS of the guide
 // (probability alpha) and the BSDF at non-mirror vertices; TRAIN: training
-// records of the guided continuations.
+// records of the guided continuations.  Registers capped for 3 resident
+// blocks per SM (2 guided): measured faster than the uncapped 121 (166)
+// registers despite a few spilled words.
 template <bool GUIDED, bool TRAIN>
-__global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
+__global__ void __launch_bounds__(kPtBlock, GUIDED ? 2 : 3) k_pt_shade(PtBatch b, uint32_t d) {
   const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
   const float* q = b.qray[d & 1];
   const uint32_t* qp = b.qpath[d & 1];
@@ -500,7 +504,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_shade(PtBatch b, uint32_t d) {
         Ctx sc;
         uint32_t shid = 0;
         const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
-        if (surface_attributes(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], time, sc, shid)) {
+        if (surface_attributes<false>(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], time, sc, shid)) {
           const vmr_shader_std& sh = b.shaders[shid];
           const V3 wi = v3(-D.x, -D.y, -D.z);
           const bool front = dot(sc.Ng, wi) > 0.0f;
@@ -930,7 +934,8 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
   PCUDA(cudaMemsetAsync(b.slen, 0, ns * sizeof(unsigned long long), st));
   PCUDA(cudaMemsetAsync(scr, 0, sizeof(DScratch) * 2 * (b.max_depth + 1), st));
   if (train) PCUDA(cudaMemsetAsync(b.rcount, 0, sizeof(unsigned long long), st));
-  k_pt_generate<<<grid, kPtBlock, 0, st>>>(b);
+  if (b.cam_nkeys >= 2) k_pt_generate<true><<<grid, kPtBlock, 0, st>>>(b);
+  else k_pt_generate<false><<<grid, kPtBlock, 0, st>>>(b);
   PCUDA(cudaGetLastError());
   for (uint32_t d = 0; d <= b.max_depth; ++d) {
     TraceLaunch l{};

@@ -279,6 +279,8 @@ struct RenderBatch {
 
 __device__ __forceinline__ float* ray_f(const Level& L, int k, uint64_t e) { return L.ray + (size_t)k * L.cap + e; }
 
+// CKEYS: the camera has motion keys (b.cam_nkeys >= 2).
+template <bool CKEYS>
 __global__ void k_generate(RenderBatch b) {
   const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (s >= b.n) return;
@@ -286,7 +288,8 @@ __global__ void k_generate(RenderBatch b) {
   const uint32_t j = b.iter0 + (uint32_t)(s / b.npix) + 1;  // render(iter+1)
   V3 P, D;
   float time, lambda;
-  camera_primary(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D, time, lambda);
+  camera_primary<CKEYS>(b.cam, b.cam_keys, b.cam_nkeys, b.width, b.height, j, pix, b.seed, b.filt, P, D, time,
+                        lambda);
   const Level& L = b.lv[0];
   *ray_f(L, 0, s) = P.x; *ray_f(L, 1, s) = P.y; *ray_f(L, 2, s) = P.z;
   *ray_f(L, 3, s) = D.x; *ray_f(L, 4, s) = D.y; *ray_f(L, 5, s) = D.z;
@@ -391,7 +394,7 @@ __device__ float light_lobe(const RenderBatch& b, const Level& lv, const Ctx& sc
 // level: emission, the diffuse and glossy lobes' light samples, and the
 // mirror (Spec1Roughness 0) reflection queued for the next level with the
 // sample's I and scrambles (a child ShaderContext copies them).
-template <bool F32>
+template <bool F32, bool GROUPS>
 __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
   const Level& lv = b.lv[level];
   const uint64_t n = level == 0 ? (uint64_t)b.n : (*lv.count < lv.cap ? *lv.count : lv.cap);
@@ -414,7 +417,7 @@ __global__ void __launch_bounds__(128) k_shade(RenderBatch b, uint32_t level) {
     const float* hf = reinterpret_cast<const float*>(lv.hit);
     const V3 Ro = v3(*ray_f(lv, 0, e), *ray_f(lv, 1, e), *ray_f(lv, 2, e));
     const V3 Rdir = v3(*ray_f(lv, 3, e), *ray_f(lv, 4, e), *ray_f(lv, 5, e));
-    if (!surface_attributes(m, prim, hf[3 * (size_t)lv.cap + e], hf[4 * (size_t)lv.cap + e],
+    if (!surface_attributes<GROUPS>(m, prim, hf[3 * (size_t)lv.cap + e], hf[4 * (size_t)lv.cap + e],
                             hf[5 * (size_t)lv.cap + e], Ro, Rdir, hf[2 * (size_t)lv.cap + e], *ray_f(lv, 7, e), sc,
                             shid))
       continue;
@@ -864,6 +867,10 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
   cudaStream_t st = ctx->stream;
   // Scene tables.
   const std::vector<RMesh> rm = rmesh_table(ctx);
+  // Instances, Procs or keyed transforms in the scene: the shading kernel
+  // with the group and keyed-transform helpers (and their registers).
+  bool groups = false;
+  for (const RMesh& r : rm) groups = groups || r.outer_nkeys != 0 || r.xf_nkeys >= 2;
   std::vector<RLight> rl(R.lights.size() + R.disks.size() + R.spheres.size());
   uint32_t ns = 1;
   for (size_t i = 0; i < R.lights.size(); ++i) {
@@ -1019,7 +1026,8 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
     const int blk = 128;
     const int grid = (int)((b.n + blk - 1) / blk);
     RCUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(unsigned long long) * (kMaxLevel + 1), st));
-    k_generate<<<grid, blk, 0, st>>>(b);
+    if (b.cam_nkeys >= 2) k_generate<true><<<grid, blk, 0, st>>>(b);
+    else k_generate<false><<<grid, blk, 0, st>>>(b);
     RCUDA(cudaGetLastError());
     for (uint32_t l = 0; l < levels; ++l) {
       const Level& L = b.lv[l];
@@ -1039,8 +1047,14 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
       int rc = vmr_trace_scene(ctx, &rr, ne, VMR_TRACE_DEVICE, &hh, nullptr);
       if (rc != VMR_OK) return rc;
       RCUDA(cudaMemsetAsync(b.queue_len, 0, 8, st));
-      if (f32) k_shade<true><<<(int)((ne + blk - 1) / blk), blk, 0, st>>>(b, l);
-      else k_shade<false><<<(int)((ne + blk - 1) / blk), blk, 0, st>>>(b, l);
+      const int nblk = (int)((ne + blk - 1) / blk);
+      if (f32) {
+        if (groups) k_shade<true, true><<<nblk, blk, 0, st>>>(b, l);
+        else k_shade<true, false><<<nblk, blk, 0, st>>>(b, l);
+      } else {
+        if (groups) k_shade<false, true><<<nblk, blk, 0, st>>>(b, l);
+        else k_shade<false, false><<<nblk, blk, 0, st>>>(b, l);
+      }
       RCUDA(cudaGetLastError());
       unsigned long long nq = 0;
       RCUDA(cudaMemcpyAsync(&nq, b.queue_len, 8, cudaMemcpyDeviceToHost, st));

@@ -525,7 +525,9 @@ __device__ __noinline__ void camera_keyed(const anim::Decomp* keys, uint32_t n, 
 // wavelength with the pixel's scrambles, the ray through the camera matrix:
 // c.m (the host rebuilt it from its decomposition, as the reference does
 // for one key) or, with two or more keys (ckeys, cnk), the keys blended at
-// the sample's time.
+// the sample's time.  KEYS false: the caller has no camera keys, and the
+// blend (whose registers a kernel that calls it must hold) is left out.
+template <bool KEYS = true>
 __device__ __forceinline__ void camera_primary(const vmr_camera& c, const anim::Decomp* ckeys, uint32_t cnk,
                                                uint32_t width, uint32_t height, uint32_t j, uint32_t pix,
                                                uint64_t seed, const PixFilter& filt, V3& P, V3& D, float& time,
@@ -549,7 +551,7 @@ __device__ __forceinline__ void camera_primary(const vmr_camera& c, const anim::
   const V3 s3 = sub(add(scale(camu, v3(1, 0, 0)), scale(camv, v3(0, 1, 0))), scale(c.focal, v3(0, 0, 1)));
   float Mk[16];
   const float* M = c.m;
-  if (cnk >= 2) {
+  if (KEYS && cnk >= 2) {
     camera_keyed(ckeys, cnk, time, Mk);
     M = Mk;
   }
@@ -644,29 +646,40 @@ __device__ __noinline__ void keyed_matrix(const anim::Decomp* keys, uint32_t n, 
   anim::inverse(M, I);
 }
 
-// ShaderContext.ApplyTransform (core/shader.go:129-135): sc.P still holds
-// Po, the hit point in the space the geom was traced in.
-__device__ __forceinline__ void apply_transform(Ctx& sc, const float* T, const float* I) {
-  const V3 Po = sc.P;
-  sc.P = xf_point(T, Po);
-  sc.N = normalize(xf_vec_t(I, sc.N));
-  sc.Ng = normalize(xf_vec_t(I, sc.Ng));
-  sc.DdPdu = normalize(xf_vec(T, sc.DdPdu));
-  sc.DdPdv = normalize(xf_vec(T, sc.DdPdv));
+// The five vectors of a shading context that a transform changes.
+struct XfFrame {
+  V3 P, N, Ng, DdPdu, DdPdv;
+};
+__device__ __forceinline__ XfFrame frame_of(const Ctx& sc) { return XfFrame{sc.P, sc.N, sc.Ng, sc.DdPdu, sc.DdPdv}; }
+__device__ __forceinline__ void set_frame(Ctx& sc, const XfFrame& f) {
+  sc.P = f.P;
+  sc.N = f.N;
+  sc.Ng = f.Ng;
+  sc.DdPdu = f.DdPdu;
+  sc.DdPdv = f.DdPdv;
 }
 
-// The hit attributes of any geom kind.  A transformed mesh's PolyMesh.Trace
-// sets P = M Po and N = M^-T N (builtin/geom/polymesh/trace.go:67-74) and
-// makes M the context's transform; a GeomInstance or Proc around the geom
-// makes its own transform the context's on a hit (instance.go:105-110,
-// proc.go:133-138); core.Trace then calls ShaderContext.ApplyTransform with
-// the context's transform (core/shader.go:129-135): P = T Po,
-// N = normalize(T^-T N), Ng = normalize(T^-T Ng), dPdu/dPdv =
-// normalize(T dPdu/dPdv).  Keyed transforms are taken at the ray's time.  A
-// sphere inside an instance or Proc takes the ray as its group mapped it.
-__device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim, float U, float V, float W, V3 Ro,
-                                                   V3 Rd, float t, float time, Ctx& sc, uint32_t& shader_id) {
-  float OT[16], OI[16];
+// ShaderContext.ApplyTransform (core/shader.go:129-135): f.P still holds
+// Po, the hit point in the space the geom was traced in.
+__device__ __forceinline__ void apply_transform(XfFrame& f, const float* T, const float* I) {
+  const V3 Po = f.P;
+  f.P = xf_point(T, Po);
+  f.N = normalize(xf_vec_t(I, f.N));
+  f.Ng = normalize(xf_vec_t(I, f.Ng));
+  f.DdPdu = normalize(xf_vec(T, f.DdPdu));
+  f.DdPdv = normalize(xf_vec(T, f.DdPdv));
+}
+
+// The transforms of a mesh hit: a transformed mesh's PolyMesh.Trace sets
+// N = M^-T N (builtin/geom/polymesh/trace.go:67-74; its P = M Po is replaced
+// by ApplyTransform) and makes M the context's transform; a GeomInstance or
+// Proc around the geom makes its own transform the context's instead
+// (instance.go:105-110, proc.go:133-138); core.Trace then applies the
+// context's transform.  Keyed transforms are taken at the ray's time.  Not
+// inlined, like the keyed matrices: the matrices live in this frame only, so
+// an untransformed hit, the common case, keeps its registers.
+__device__ __noinline__ XfFrame mesh_transform(const RMesh& m, float time, XfFrame f) {
+  float OT[16], OI[16], MT[16], MI[16];
   const float* ot = m.outer_xf;
   const float* oi = m.outer_inv;
   if (m.outer_nkeys >= 2) {
@@ -674,19 +687,6 @@ __device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim,
     ot = OT;
     oi = OI;
   }
-  if (m.outer_nkeys && m.kind == 1) {  // the ray its group traced (instance.go:91-93)
-    Ro = xf_point(oi, Ro);
-    Rd = xf_vec(oi, Rd);
-  }
-  if (m.kind == 1) {
-    const bool ok = sphere_attributes(m, Ro, Rd, t, sc, shader_id);
-    if (ok && m.outer_nkeys) apply_transform(sc, ot, oi);
-    return ok;
-  }
-  const bool ok = m.keys > 1 ? motion_attributes(m, prim, U, V, W, time, sc, shader_id)
-                             : hit_attributes(m, prim, U, V, W, sc, shader_id);
-  if (!ok) return false;
-  float MT[16], MI[16];
   const float* mt = m.xf;
   const float* mi = m.xf_inv;
   const bool own = m.has_xf || m.xf_nkeys >= 2;
@@ -695,9 +695,78 @@ __device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim,
     mt = MT;
     mi = MI;
   }
-  if (own) sc.N = xf_vec_t(mi, sc.N);  // PolyMesh.Trace (its P is replaced by ApplyTransform)
-  if (m.outer_nkeys) apply_transform(sc, ot, oi);
-  else if (own) apply_transform(sc, mt, mi);
+  if (own) f.N = xf_vec_t(mi, f.N);
+  if (m.outer_nkeys) apply_transform(f, ot, oi);
+  else if (own) apply_transform(f, mt, mi);
+  return f;
+}
+
+// An analytic sphere inside a GeomInstance or Proc: the ray as its group
+// mapped it (instance.go:91-93), the sphere's attributes, then the group's
+// transform applied.  Not inlined, for the same reason.
+struct GroupSphere {
+  XfFrame f;
+  V3 Poffset;
+  uint32_t shader_id;
+  bool ok;
+};
+__device__ __noinline__ GroupSphere grouped_sphere_attributes(const RMesh& m, V3 Ro, V3 Rd, float t, float time) {
+  float OT[16], OI[16];
+  const float* ot = m.outer_xf;
+  const float* oi = m.outer_inv;
+  if (m.outer_nkeys >= 2) {
+    keyed_matrix(m.outer_keys, m.outer_nkeys, time, OT, OI);
+    ot = OT;
+    oi = OI;
+  }
+  Ro = xf_point(oi, Ro);
+  Rd = xf_vec(oi, Rd);
+  Ctx sc{};
+  GroupSphere g{};
+  g.ok = sphere_attributes(m, Ro, Rd, t, sc, g.shader_id);
+  g.f = frame_of(sc);
+  g.Poffset = sc.Poffset;
+  if (g.ok) apply_transform(g.f, ot, oi);
+  return g;
+}
+
+// A mesh's own one-matrix PolyMesh.Transform (the reference's steps as in
+// mesh_transform, inlined for the kernels that take no groups or keys).
+__device__ __forceinline__ XfFrame own_transform(const RMesh& m, XfFrame f) {
+  f.N = xf_vec_t(m.xf_inv, f.N);
+  apply_transform(f, m.xf, m.xf_inv);
+  return f;
+}
+
+// The hit attributes of any geom kind, with the transforms above applied
+// (P = T Po, N = normalize(T^-T N), Ng = normalize(T^-T Ng), dPdu/dPdv =
+// normalize(T dPdu/dPdv), core/shader.go:129-135).  GROUPS false: the
+// caller's scenes hold no GeomInstance, Proc or keyed transform (the
+// extended path tracer refuses them on the host), so only a mesh's own
+// one-matrix transform is applied and the keyed and group helpers, whose
+// registers a kernel that calls them must hold, are left out.
+template <bool GROUPS = true>
+__device__ __forceinline__ bool surface_attributes(const RMesh& m, int32_t prim, float U, float V, float W, V3 Ro,
+                                                   V3 Rd, float t, float time, Ctx& sc, uint32_t& shader_id) {
+  if (m.kind == 1) {
+    if (GROUPS && m.outer_nkeys) {
+      const GroupSphere g = grouped_sphere_attributes(m, Ro, Rd, t, time);
+      if (!g.ok) return false;
+      set_frame(sc, g.f);
+      sc.Poffset = g.Poffset;
+      shader_id = g.shader_id;
+      return true;
+    }
+    return sphere_attributes(m, Ro, Rd, t, sc, shader_id);
+  }
+  const bool ok = m.keys > 1 ? motion_attributes(m, prim, U, V, W, time, sc, shader_id)
+                             : hit_attributes(m, prim, U, V, W, sc, shader_id);
+  if (!ok) return false;
+  if (GROUPS) {
+    if (m.outer_nkeys || m.has_xf || m.xf_nkeys >= 2) set_frame(sc, mesh_transform(m, time, frame_of(sc)));
+  } else if (m.has_xf) {
+    set_frame(sc, own_transform(m, frame_of(sc)));
+  }
   return true;
 }
 
