@@ -425,6 +425,17 @@ int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n);
  * shader_idx given at build) and optional per-vertex normals (key 0). */
 int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, uint32_t n_shaders,
                          const float* normals);
+/* Per-key normals of a motion mesh: PolyMesh.Normals with as many motion
+ * keys as the vertices (builtin/geom/polymesh/trace.go:694-712).
+ * normals[key][i] are 3 floats, n_per_key entries a key, keys = the mesh's
+ * keys.  A hit on element e reads entries 3e .. 3e + 2 of the two keys
+ * around the ray's time (directly, not through NormalIdx), lerps them and
+ * interpolates them with the hit's barycentrics; without them a motion
+ * hit's N is Ng.  n_per_key must be at least 3 x the mesh's triangles.
+ * NULL removes them.  VMR_ERR_INVALID for a static mesh, another key count
+ * or too few entries. */
+int vmr_mesh_set_motion_normals(vmr_ctx* ctx, uint32_t geom, const float* normals, uint32_t n_per_key,
+                                uint32_t keys);
 int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n);
 int vmr_set_disk_lights(vmr_ctx* ctx, const vmr_disk_light* lights, uint32_t n);
 int vmr_set_sphere_lights(vmr_ctx* ctx, const vmr_sphere_light* lights, uint32_t n);

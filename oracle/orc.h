@@ -186,6 +186,12 @@ orc_mesh* orc_sphere_create(const float center[3], float radius);
 /* Per-mesh shading data: shader index per face (face order, may be NULL)
  * and per-vertex normals of key 0 (may be NULL). */
 int orc_mesh_set_shading(orc_mesh* m, const uint8_t* face_shader, const float* normals);
+/* Per-key normals of a motion mesh (PolyMesh.Normals with as many keys as
+ * the vertices): normals[key][i][3], n_per_key >= 3 x triangles; a hit on
+ * element e reads entries 3e .. 3e+2 of the two keys around the ray's time
+ * (builtin/geom/polymesh/trace.go:694-712).  NULL clears them; -1 when the
+ * mesh is static, keys differ or n_per_key is short. */
+int orc_mesh_set_motion_normals(orc_mesh* m, const float* normals, uint32_t n_per_key, uint32_t keys);
 
 /* shader_list[mesh_shader_offset[m] .. + mesh_shader_count[m]] are the
  * shaders of mesh m (PolyMesh.Shader). */

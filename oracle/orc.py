@@ -162,6 +162,8 @@ def _register_render(L):
     P = ctypes.c_void_p
     L.orc_mesh_set_shading.restype = ctypes.c_int
     L.orc_mesh_set_shading.argtypes = [P, P, P]
+    L.orc_mesh_set_motion_normals.restype = ctypes.c_int
+    L.orc_mesh_set_motion_normals.argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32]
     L.orc_render_create.restype = P
     L.orc_render_create.argtypes = [P, P, ctypes.c_uint32, P, P, P, P, ctypes.c_uint32, P, ctypes.c_uint32, P]
     L.orc_render_destroy.argtypes = [P]
@@ -472,6 +474,8 @@ def build_geoms(entries):
             fs = None if m.get("face_shader") is None else np.ascontiguousarray(m["face_shader"], np.uint8)
             nr = None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32)
             lib().orc_mesh_set_shading(om.h, _ptr(fs), _ptr(nr))
+            if m.get("motion_normals") is not None:
+                om.set_motion_normals(m["motion_normals"])
             if m.get("transform_keys") is not None:
                 om.set_transform_keys(m["transform_keys"])
             elif m.get("transform") is not None:
@@ -557,6 +561,18 @@ class Mesh:
         """PolyMesh.Transform of n keys ([n, 16] column-major)."""
         self._xk, n = _keys16(keys)
         lib().orc_mesh_set_transform_keys(self.h, _ptr(self._xk), n)
+
+    def set_motion_normals(self, normals):
+        """PolyMesh.Normals of a motion mesh with as many keys as its
+        vertices: [keys, n, 3], n >= 3 x triangles; a hit on element e reads
+        rows 3e .. 3e + 2 of each key (trace.go:694-712).  None clears them."""
+        if normals is None:
+            lib().orc_mesh_set_motion_normals(self.h, None, 0, 0)
+            return
+        a = np.ascontiguousarray(normals, np.float32)
+        assert a.ndim == 3 and a.shape[2] == 3
+        if lib().orc_mesh_set_motion_normals(self.h, _ptr(a), a.shape[1], a.shape[0]) != 0:
+            raise ValueError("motion normals need the mesh's key count and at least 3 rows per triangle")
 
     def set_transform(self, m):
         """PolyMesh.Transform: a column-major 4x4 (16 floats) or None."""

@@ -364,6 +364,10 @@ struct Mesh {
   Box bounds;
   std::vector<uint8_t> shaderidx;  // leaf order (static) / face order (motion)
   std::vector<float> normals;      // per vertex, key 0
+  // PolyMesh.Normals with as many keys as the vertices (motion meshes):
+  // [key][mnormals_per_key][3], read at ElemID*3 + corner
+  std::vector<float> mnormals;
+  uint32_t mnormals_per_key = 0;
   // An analytic sphere geom (builtin/geom/sphere) instead of triangles.
   bool sphere = false;
   float sc[3] = {0, 0, 0}, sr = 0;
@@ -1011,6 +1015,8 @@ MeshView mesh_view(const orc_mesh* om) {
   v.idxp = m.idxp.data();
   v.shaderidx = m.shaderidx.empty() ? nullptr : m.shaderidx.data();
   v.normals = m.normals.empty() ? nullptr : m.normals.data();
+  v.mnormals = m.mnormals.empty() ? nullptr : m.mnormals.data();
+  v.mnormals_per_key = m.mnormals_per_key;
   v.motion = m.keys > 1;
   v.sphere = m.sphere;
   for (int k = 0; k < 3; ++k) v.sc[k] = m.sc[k];
@@ -1136,6 +1142,21 @@ int orc_mesh_set_shading(orc_mesh* om, const uint8_t* face_shader, const float* 
   }
   m.normals.clear();
   if (normals) m.normals.assign(normals, normals + (size_t)m.nverts * 3);
+  return 0;
+}
+
+// PolyMesh.Normals of a motion mesh with as many keys as its vertices: the
+// motion hit reads Normals.Elems[idx*3 + j + ElemsPerKey*key] directly, idx
+// being the element the hit reports (trace.go:694-712), not through
+// NormalIdx.
+int orc_mesh_set_motion_normals(orc_mesh* om, const float* normals, uint32_t n_per_key, uint32_t keys) {
+  Mesh& m = om->m;
+  m.mnormals.clear();
+  m.mnormals_per_key = 0;
+  if (!normals) return 0;
+  if (m.keys < 2 || keys != m.keys || (uint64_t)n_per_key < 3ull * m.ntris) return -1;
+  m.mnormals.assign(normals, normals + (size_t)keys * n_per_key * 3);
+  m.mnormals_per_key = n_per_key;
   return 0;
 }
 

@@ -40,6 +40,8 @@ struct MeshView {
   const uint32_t* idxp;     // leaf order (static) / face order (motion)
   const uint8_t* shaderidx; // indexed by ElemID, or null
   const float* normals;     // per vertex, or null
+  const float* mnormals;    // motion meshes: [key][mnormals_per_key][3], or null
+  uint32_t mnormals_per_key;
   bool motion;
   bool sphere;              // analytic sphere geom: centre sc, radius sr
   float sc[3], sr;

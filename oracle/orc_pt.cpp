@@ -376,9 +376,18 @@ struct PT {
     const Vec<T> e0 = sub(V1, V0), e1 = sub(V2, V0);
     const Vec<T> Ng = nrm(mk<T>(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x));
     Vec<T> N = Ng;
-    if (m.normals) {
-      const Vec<T> N0 = fromf<T>(m.normals + i0 * 3), N1 = fromf<T>(m.normals + i1 * 3),
-                   N2 = fromf<T>(m.normals + i2 * 3);
+    if (m.motion ? m.mnormals != nullptr : m.normals != nullptr) {
+      // static: per-vertex normals; motion: the element's corner normals of
+      // the two keys lerped at the ray's time (trace.go:694-712)
+      auto cn = [&](uint32_t i, uint32_t j) {
+        if (!m.motion) return fromf<T>(m.normals + i * 3);
+        const size_t c = (size_t)h.elem * 3 + j;
+        const float* a = m.mnormals + ((size_t)key * m.mnormals_per_key + c) * 3;
+        const float* b = m.mnormals + ((size_t)key2 * m.mnormals_per_key + c) * 3;
+        const float v[3] = {(1.0f - tm) * a[0] + tm * b[0], (1.0f - tm) * a[1] + tm * b[1], (1.0f - tm) * a[2] + tm * b[2]};
+        return fromf<T>(v);
+      };
+      const Vec<T> N0 = cn(i0, 0), N1 = cn(i1, 1), N2 = cn(i2, 2);
       N = nrm(mk<T>(U * N0.x + V * N1.x + W * N2.x, U * N0.y + V * N1.y + W * N2.y, U * N0.z + V * N1.z + W * N2.z));
     }
     const float g7f = (7.0f * 5.96046448e-08f) / (1 - 7.0f * 5.96046448e-08f);  // Gamma(7) of float32 data

@@ -852,9 +852,18 @@ struct Renderer {
     const V3 e0 = sub(V1, V0), e1 = sub(V2, V0);
     V3 Ng = normalize(v3(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x));
     V3 N;
-    if (m.normals) {
-      auto nrm = [&](uint32_t i) { return v3(m.normals[i * 3], m.normals[i * 3 + 1], m.normals[i * 3 + 2]); };
-      const V3 N0 = nrm(i0), N1 = nrm(i1), N2 = nrm(i2);
+    if (m.motion ? m.mnormals != nullptr : m.normals != nullptr) {
+      // static: per-vertex normals; motion: the element's corner normals of
+      // the two keys lerped at the ray's time (trace.go:694-712), N = Ng
+      // when the mesh has none with as many keys as its vertices
+      auto nrm = [&](uint32_t i, uint32_t j) {
+        if (!m.motion) return v3(m.normals[i * 3], m.normals[i * 3 + 1], m.normals[i * 3 + 2]);
+        const size_t c = (size_t)h.elem * 3 + j;
+        const float* a = m.mnormals + ((size_t)key * m.mnormals_per_key + c) * 3;
+        const float* b = m.mnormals + ((size_t)key2 * m.mnormals_per_key + c) * 3;
+        return v3((1.0f - tm) * a[0] + tm * b[0], (1.0f - tm) * a[1] + tm * b[1], (1.0f - tm) * a[2] + tm * b[2]);
+      };
+      const V3 N0 = nrm(i0, 0), N1 = nrm(i1, 1), N2 = nrm(i2, 2);
       N = normalize(v3(U * N0.x + V * N1.x + W * N2.x, U * N0.y + V * N1.y + W * N2.y, U * N0.z + V * N1.z + W * N2.z));
     } else {
       N = Ng;

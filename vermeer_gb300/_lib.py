@@ -185,6 +185,7 @@ SIGNATURES = {
                                        ctypes.POINTER(Hits), ctypes.POINTER(TraceStats)]),
     "vmr_set_shaders": (ctypes.c_int, [P, P, U32]),
     "vmr_mesh_set_shading": (ctypes.c_int, [P, U32, P, U32, P]),
+    "vmr_mesh_set_motion_normals": (ctypes.c_int, [P, U32, P, U32, U32]),
     "vmr_set_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_disk_lights": (ctypes.c_int, [P, P, U32]),
     "vmr_set_sphere_lights": (ctypes.c_int, [P, P, U32]),

@@ -346,6 +346,17 @@ class Context:
         nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
         self._check(self.L.vmr_mesh_set_shading(self.h, geom, _p(ids), ids.size, _p(nrm)))
 
+    def mesh_set_motion_normals(self, geom: int, normals):
+        """vmr_mesh_set_motion_normals: [keys, n, 3] corner normals of a motion
+        mesh (n >= 3 x triangles; a hit on element e reads rows 3e .. 3e + 2
+        of each key), or None to remove them."""
+        if normals is None:
+            self._check(self.L.vmr_mesh_set_motion_normals(self.h, geom, None, 0, 0))
+            return
+        a = np.ascontiguousarray(normals, np.float32)
+        assert a.ndim == 3 and a.shape[2] == 3
+        self._check(self.L.vmr_mesh_set_motion_normals(self.h, geom, _p(a), a.shape[1], a.shape[0]))
+
     def set_lights(self, lights):
         """TriLights: dicts with p0, p1, p2, samples, shader, geom."""
         arr = (_lib.TriLight * len(lights))()
@@ -640,6 +651,8 @@ class Context:
         for g, m in zip(ids, scene["meshes"]):
             if "instance" not in m and "proc" not in m:
                 self.mesh_set_shading(g, m["shaders"], m.get("normals"))
+                if m.get("motion_normals") is not None:
+                    self.mesh_set_motion_normals(g, m["motion_normals"])
         self.set_lights([dict(l, geom=ids[l["mesh"]]) for l in scene["lights"]])
         self.set_disk_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("disk_lights", [])])
         self.set_sphere_lights([dict(d, geom=ids[d["mesh"]]) for d in scene.get("sphere_lights", [])])

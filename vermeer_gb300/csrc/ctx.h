@@ -48,6 +48,10 @@ struct MeshRec {
   bool has_normals = false;
   DevBuf shlist, sidx, nrm;
   DevBuf avert, aidx;  // motion meshes: key-major vertices (float4) and face-order idxp for hit attributes
+  // motion meshes: per-key corner normals (vmr_mesh_set_motion_normals),
+  // float4 [keys][mnrm_n]; mnrm_n = 0: none
+  DevBuf mnrm;
+  uint32_t mnrm_n = 0;
   // PolyMesh.Transform (one matrix, column-major) and its Matrix4Inverse;
   // a GeomInstance's or Proc's transform when it has one key (the matrix
   // rebuilt from its decomposition, as TimeKey returns it)

@@ -745,6 +745,32 @@ int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, u
   return VMR_OK;
 }
 
+int vmr_mesh_set_motion_normals(vmr_ctx* ctx, uint32_t geom, const float* normals, uint32_t n_per_key,
+                                uint32_t keys) {
+  if (!ctx || geom >= ctx->meshes.size()) return VMR_ERR_INVALID;
+  MeshRec& rec = *ctx->meshes[geom];
+  if (!normals) {
+    rec.mnrm_n = 0;
+    return VMR_OK;
+  }
+  const HostMesh& m = rec.host;
+  if (!m.motion() || m.group || m.sphere) return rfail(ctx, VMR_ERR_INVALID, "motion normals need a motion mesh");
+  if (keys != m.keys) return rfail(ctx, VMR_ERR_INVALID, "motion normals need as many keys as the mesh's vertices");
+  if ((uint64_t)n_per_key < 3ull * m.n_tris)
+    return rfail(ctx, VMR_ERR_INVALID, "motion normals: fewer than three entries per triangle");
+  if (ctx->device < 0) {
+    rec.mnrm_n = n_per_key;
+    return VMR_OK;
+  }
+  cudaSetDevice(ctx->device);
+  std::vector<float4> nv((size_t)keys * n_per_key);
+  for (size_t i = 0; i < nv.size(); ++i) nv[i] = make_float4(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2], 0.f);
+  RCUDA(rec.mnrm.ensure(nv.size() * sizeof(float4)));
+  RCUDA(cudaMemcpy(rec.mnrm.p, nv.data(), nv.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  rec.mnrm_n = n_per_key;
+  return VMR_OK;
+}
+
 int vmr_set_lights(vmr_ctx* ctx, const vmr_tri_light* lights, uint32_t n) {
   if (!ctx || (n && !lights)) return VMR_ERR_INVALID;
   for (uint32_t i = 0; i < n; ++i)

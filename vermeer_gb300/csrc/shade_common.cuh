@@ -325,6 +325,10 @@ struct RMesh {
   const float4* mverts;
   const uint32_t* midxp;
   uint32_t keys, n_verts;
+  // motion meshes: per-key corner normals [keys][mnrm_n] (entry 3e + j is
+  // corner j of element e), or null
+  const float4* mnrm;
+  uint32_t mnrm_n;
   // PolyMesh.Transform: the matrix and its Matrix4Inverse, column-major
   uint32_t has_xf;
   float xf[16], xf_inv[16];
@@ -591,7 +595,8 @@ __device__ __forceinline__ bool sphere_attributes(const RMesh& m, V3 Ro, V3 Rd, 
 // Hit attributes of a motion mesh (TraceMotionElems, trace.go:520-719): the
 // face's vertices idxp[ElemID*3 + j] lerped between the keys around the ray
 // time (Vec3Lerp, math/vec3.go:52-58), dPdu/dPdv the raw edges, then
-// ApplyTransform's renormalisation; no normals (N = Ng).
+// ApplyTransform's renormalisation; N from the per-key corner normals when
+// the mesh has them (trace.go:694-712), else N = Ng.
 __device__ __forceinline__ bool motion_attributes(const RMesh& m, int32_t elem, float U, float V, float W, float time,
                                                   Ctx& sc, uint32_t& shader_id) {
   const uint32_t sidx = m.sidx ? m.sidx[elem] : 0u;
@@ -616,7 +621,18 @@ __device__ __forceinline__ bool motion_attributes(const RMesh& m, int32_t elem, 
   const float d = g7 * xs * fabsf(Ng.x) + g7 * ys * fabsf(Ng.y) + g7 * zs * fabsf(Ng.z);
   sc.Poffset = scale(d, Ng);
   sc.P = v3(U * V0.x + V * V1.x + W * V2.x, U * V0.y + V * V1.y + W * V2.y, U * V0.z + V * V1.z + W * V2.z);
-  sc.N = normalize(Ng);
+  V3 N = Ng;
+  if (m.mnrm) {  // the element's corner normals of the two keys, lerped, then weighted by U, V, W
+    V3 Nc[3];
+    for (int j = 0; j < 3; ++j) {
+      const size_t c = (size_t)elem * 3 + j;
+      const float4 a = m.mnrm[(size_t)key * m.mnrm_n + c], b = m.mnrm[(size_t)key2 * m.mnrm_n + c];
+      Nc[j] = v3((1.0f - tm) * a.x + tm * b.x, (1.0f - tm) * a.y + tm * b.y, (1.0f - tm) * a.z + tm * b.z);
+    }
+    N = normalize(v3(U * Nc[0].x + V * Nc[1].x + W * Nc[2].x, U * Nc[0].y + V * Nc[1].y + W * Nc[2].y,
+                     U * Nc[0].z + V * Nc[1].z + W * Nc[2].z));
+  }
+  sc.N = normalize(N);
   sc.Ng = normalize(Ng);
   sc.DdPdu = normalize(e0);
   sc.DdPdv = normalize(e1);
@@ -788,6 +804,8 @@ inline void fill_rmesh_one(const MeshRec& mr, RMesh& r) {
   r.n_verts = mr.host.n_verts;
   r.mverts = mr.host.motion() ? mr.avert.as<float4>() : nullptr;
   r.midxp = mr.host.motion() ? mr.aidx.as<uint32_t>() : nullptr;
+  r.mnrm = mr.host.motion() && mr.mnrm_n ? mr.mnrm.as<float4>() : nullptr;
+  r.mnrm_n = r.mnrm ? mr.mnrm_n : 0u;
   r.has_xf = mr.has_xf ? 1u : 0u;
   std::memcpy(r.xf, mr.xf, sizeof(mr.xf));
   std::memcpy(r.xf_inv, mr.xf_inv, sizeof(mr.xf_inv));

@@ -455,6 +455,10 @@ struct MeshOut {
   std::vector<uint32_t> idxp;
   std::vector<uint8_t> sidx;
   std::vector<float> normals;  // per vertex (key 0), or empty
+  // a motion mesh's Normals with as many keys as its vertices (key-major,
+  // mnormals_per_key a key), or empty
+  std::vector<float> mnormals;
+  uint32_t mnormals_per_key = 0;
   std::vector<uint32_t> shaders;
   float ray_bias = 0.0f;
   bool sphere = false;
@@ -578,8 +582,12 @@ MeshOut poly_mesh(const Node& n, const Scene& sc, const std::string& file) {
   // TraceMotionElems uses the normals only with as many keys as the
   // vertices (trace.go:694-712), otherwise N = Ng; the static path uses key 0
   const int nkeys = n.has("Normals") ? (n.at("Normals").keys == 0 ? 1 : n.at("Normals").keys) : 0;
-  if (o.keys > 1 && nkeys == (int)o.keys)
-    throw LoadError{VMR_ERR_UNSUPPORTED, where("motion-keyed normals (lerped per key) are not supported")};
+  if (o.keys > 1 && nkeys == (int)o.keys) {  // read at ElemID*3 + corner of each key, not through NormalIdx
+    const Value& N = n.at("Normals");
+    if (N.v.size() != (size_t)nkeys * N.per * 3) throw LoadError{VMR_ERR_INVALID, where("Normals keys are not whole")};
+    o.mnormals = N.v;
+    o.mnormals_per_key = (uint32_t)N.per;
+  }
   const bool has_n = n.has("Normals") && !n.at("Normals").v.empty() && o.keys == 1;
   std::vector<uint32_t> nidx;
   auto chk = [&](const std::vector<int32_t>& a, size_t i) -> uint32_t {
@@ -1070,8 +1078,11 @@ int upload_geom(vmr_ctx* ctx, const MeshOut& g, int mode, uint32_t* id) {
 }
 
 int set_shading(vmr_ctx* ctx, uint32_t id, const MeshOut& g) {
-  return vmr_mesh_set_shading(ctx, id, g.shaders.data(), (uint32_t)g.shaders.size(),
-                              g.normals.empty() ? nullptr : g.normals.data());
+  int rc = vmr_mesh_set_shading(ctx, id, g.shaders.data(), (uint32_t)g.shaders.size(),
+                                g.normals.empty() ? nullptr : g.normals.data());
+  if (rc == VMR_OK && !g.mnormals.empty())
+    rc = vmr_mesh_set_motion_normals(ctx, id, g.mnormals.data(), g.mnormals_per_key, g.keys);
+  return rc;
 }
 
 }  // namespace

@@ -513,11 +513,15 @@ def small_room_spheres(n_tris: int = 4096, seed: int = 1, light_samples: int = 1
     return sc
 
 
-def small_room_motion(n_tris: int = 4096, seed: int = 1, motion_mode: int = 0, velocity: float = 0.08) -> dict:
+def small_room_motion(n_tris: int = 4096, seed: int = 1, motion_mode: int = 0, velocity: float = 0.08,
+                      normals: bool = False) -> dict:
     """The small room with its soup moving: two motion keys (key 1 = key 0 +
     a per-triangle velocity in a ball of the given radius), sampled over the
     shutter by each camera ray's VdC time; motion_mode 0 reproduces
-    TraceMotionElems' leaf indexing, 1 the face the leaf boxes bound."""
+    TraceMotionElems' leaf indexing, 1 the face the leaf boxes bound.
+    normals: per-key corner normals for the soup (motion_normals [2, 3n, 3]:
+    each key's face normal tilted by a seeded random vector of length 0.5 per
+    corner, unit length)."""
     sc = small_room(n_tris, seed=seed)
     soup = sc["meshes"][1]
     v0 = soup["verts"].reshape(n_tris, 3, 3).astype(np.float64)
@@ -526,6 +530,14 @@ def small_room_motion(n_tris: int = 4096, seed: int = 1, motion_mode: int = 0, v
     soup["verts"] = np.concatenate([soup["verts"], v1], axis=0)
     soup["keys"] = 2
     soup["motion_mode"] = motion_mode
+    if normals:
+        keys = []
+        for k, vk in enumerate((v0, v1.reshape(n_tris, 3, 3).astype(np.float64))):
+            fn = np.cross(vk[:, 1] - vk[:, 0], vk[:, 2] - vk[:, 0])
+            fn /= np.maximum(np.linalg.norm(fn, axis=1, keepdims=True), 1e-30)
+            c = np.repeat(fn, 3, axis=0) + 0.5 * unit_sphere(seed, 3 * n_tris, 50 + k)
+            keys.append(c / np.maximum(np.linalg.norm(c, axis=1, keepdims=True), 1e-30))
+        soup["motion_normals"] = np.stack(keys).astype(np.float32)
     return sc
 
 
@@ -651,7 +663,10 @@ def _geom_node(gi: int, m: dict) -> str:
     if m.get("face_shader") is not None:
         fs = np.asarray(m["face_shader"], np.uint8)
         lines.append(f"  ShaderIdx {fs.size} int " + " ".join(str(int(x)) for x in fs))
-    if m.get("normals") is not None:
+    if m.get("motion_normals") is not None:  # as many keys as the vertices
+        nr = np.asarray(m["motion_normals"], np.float32)
+        lines.append(f"  Normals {nr.shape[0]} {nr.shape[1]} vec3 " + " ".join(_vnf_num(x) for x in nr.ravel()))
+    elif m.get("normals") is not None:
         nr = np.asarray(m["normals"], np.float32).reshape(-1, 3)
         lines.append(f"  Normals 1 {nr.shape[0]} vec3 " + " ".join(_vnf_num(x) for x in nr.ravel()))
     if m.get("transform_keys") is not None:
