@@ -210,8 +210,8 @@ int vmr_mesh_set_transform(vmr_ctx* ctx, uint32_t geom, const float* m);
  * (TransformDecompLerp, animdecomp.go:74-80), rebuilds the matrix
  * (TransformDecompToMatrix4) and maps the ray by its Matrix4Inverse; renders
  * take that matrix for the hit.  Scenes holding such a mesh are traced by
- * the single-loop scene kernel; the extended path tracer and batched jobs do
- * not take them.  n_keys = 0 removes the transform. */
+ * the single-loop scene kernel (both render modes); batched jobs do not
+ * take them.  n_keys = 0 removes the transform. */
 int vmr_mesh_set_transform_keys(vmr_ctx* ctx, uint32_t geom, const float* keys16, uint32_t n_keys);
 
 /* GeomInstance (builtin/geom/instance/instance.go:40-160): a new geom that

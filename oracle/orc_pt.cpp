@@ -332,11 +332,54 @@ struct PT {
   bool has_env = false;
   uint32_t max_depth = 4, rr_depth = 3;
 
-  // Static-mesh hit attributes (trace.go:276-515; the same expressions as
-  // the reference mode).  Returns the shader id or -1.
+  // Matrix4MulPoint / Matrix4MulVec of a column-major matrix (sums left to
+  // right) and Matrix4MulVec of the inverse transposed, in T.
+  static Vec<T> xf_pt(const float* M, Vec<T> b) {
+    return mk<T>((T)M[0] * b.x + (T)M[4] * b.y + (T)M[8] * b.z + (T)M[12],
+                 (T)M[1] * b.x + (T)M[5] * b.y + (T)M[9] * b.z + (T)M[13],
+                 (T)M[2] * b.x + (T)M[6] * b.y + (T)M[10] * b.z + (T)M[14]);
+  }
+  static Vec<T> xf_vec(const float* M, Vec<T> b) {
+    return mk<T>((T)M[0] * b.x + (T)M[4] * b.y + (T)M[8] * b.z, (T)M[1] * b.x + (T)M[5] * b.y + (T)M[9] * b.z,
+                 (T)M[2] * b.x + (T)M[6] * b.y + (T)M[10] * b.z);
+  }
+  static Vec<T> inv_t(const float* I, Vec<T> b) {
+    return mk<T>((T)I[0] * b.x + (T)I[1] * b.y + (T)I[2] * b.z, (T)I[4] * b.x + (T)I[5] * b.y + (T)I[6] * b.z,
+                 (T)I[8] * b.x + (T)I[9] * b.y + (T)I[10] * b.z);
+  }
+  // ShaderContext.ApplyTransform (core/shader.go:129-135); s.P holds Po.
+  static void apply_transform(Surf<T>& s, const float* M, const float* I) {
+    const Vec<T> Po = s.P;
+    s.P = xf_pt(M, Po);
+    s.N = nrm(inv_t(I, s.N));
+    s.Ng = nrm(inv_t(I, s.Ng));
+    s.dPdu = nrm(xf_vec(M, s.dPdu));
+    s.dPdv = nrm(xf_vec(M, s.dPdv));
+  }
+
+  // Hit attributes (trace.go:276-515 and :520-719, sphere/trace.go; the
+  // same expressions as the reference mode).  Returns the shader id or -1.
   int32_t attributes(const Hit& h, Surf<T>& s, const float* Ro, const float* Rd, float time) const {
     const orc_internal::MeshView& m = R.meshes[h.geom];
     const auto& list = R.mesh_shaders[h.geom];
+    // the GeomInstance / Proc transform that reaches this geom, at the ray's
+    // time (instance.go:105-110, proc.go:133-138); a sphere inside one takes
+    // the ray as its group mapped it (instance.go:91-93), in float32 as the
+    // traversal does
+    float OT[16], OI[16];
+    if (m.outer) {
+      orc_internal::decomp_at(*m.outer, time, false, OT);
+      orc_internal::matrix_inverse(OT, OI);
+    }
+    float Rog[3], Rdg[3];
+    if (m.sphere && m.outer) {
+      for (int k = 0; k < 3; ++k) {
+        Rog[k] = OI[k] * Ro[0] + OI[4 + k] * Ro[1] + OI[8 + k] * Ro[2] + OI[12 + k];
+        Rdg[k] = OI[k] * Rd[0] + OI[4 + k] * Rd[1] + OI[8 + k] * Rd[2];
+      }
+      Ro = Rog;
+      Rd = Rdg;
+    }
     if (m.sphere) {  // sphere/trace.go: P = ray.P + t ray.D, N = normalize(P - centre)
       if (list.empty()) return -1;
       const float P[3] = {Ro[0] + Rd[0] * h.t, Ro[1] + Rd[1] * h.t, Ro[2] + Rd[2] * h.t};  // float32, as the hit
@@ -348,6 +391,7 @@ struct PT {
       s.Ng = nrm(N);
       s.dPdu = mk<T>(1, 0, 0);
       s.dPdv = mk<T>(0, 0, 1);
+      if (m.outer) apply_transform(s, OT, OI);
       return (int32_t)list[0];
     }
     const uint32_t i0 = m.idxp[h.elem * 3 + 0], i1 = m.idxp[h.elem * 3 + 1], i2 = m.idxp[h.elem * 3 + 2];
@@ -410,30 +454,22 @@ struct PT {
     s.Ng = nrm(Ng);
     s.dPdu = nrm(dpdu);
     s.dPdv = nrm(dpdv);
-    if (m.has_xf) {  // to world space as the reference mode does (trace.go:67-74, core/shader.go:129-135)
-      const float* M = m.xf;
-      const float* I = m.xinv;
-      auto pt = [&](Vec<T> b) {
-        return mk<T>((T)M[0] * b.x + (T)M[4] * b.y + (T)M[8] * b.z + (T)M[12],
-                     (T)M[1] * b.x + (T)M[5] * b.y + (T)M[9] * b.z + (T)M[13],
-                     (T)M[2] * b.x + (T)M[6] * b.y + (T)M[10] * b.z + (T)M[14]);
-      };
-      auto vec = [&](Vec<T> b) {
-        return mk<T>((T)M[0] * b.x + (T)M[4] * b.y + (T)M[8] * b.z, (T)M[1] * b.x + (T)M[5] * b.y + (T)M[9] * b.z,
-                     (T)M[2] * b.x + (T)M[6] * b.y + (T)M[10] * b.z);
-      };
-      auto inv_t = [&](Vec<T> b) {  // the inverse transposed
-        return mk<T>((T)I[0] * b.x + (T)I[1] * b.y + (T)I[2] * b.z, (T)I[4] * b.x + (T)I[5] * b.y + (T)I[6] * b.z,
-                     (T)I[8] * b.x + (T)I[9] * b.y + (T)I[10] * b.z);
-      };
-      const Vec<T> Po = s.P;
-      s.N = inv_t(s.N);
-      s.P = pt(Po);
-      s.N = nrm(inv_t(s.N));
-      s.Ng = nrm(inv_t(s.Ng));
-      s.dPdu = nrm(vec(s.dPdu));
-      s.dPdv = nrm(vec(s.dPdv));
+    // to world space as the reference mode does: a transformed mesh's
+    // PolyMesh.Trace sets N = M^-T N (trace.go:67-74), then ApplyTransform
+    // with the group's transform when one reaches the geom, else the mesh's
+    // own (core/shader.go:129-135); keyed transforms at the ray's time
+    float MT[16], MI[16];
+    const bool own = m.has_xf || m.xkeys;
+    if (m.xkeys) {
+      orc_internal::decomp_at(*m.xkeys, time, false, MT);
+      orc_internal::matrix_inverse(MT, MI);
+    } else if (m.has_xf) {
+      std::memcpy(MT, m.xf, sizeof(MT));
+      std::memcpy(MI, m.xinv, sizeof(MI));
     }
+    if (own) s.N = inv_t(MI, s.N);
+    if (m.outer) apply_transform(s, OT, OI);
+    else if (own) apply_transform(s, MT, MI);
     return (int32_t)list[sidx];
   }
 

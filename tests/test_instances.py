@@ -220,9 +220,32 @@ def test_one_key_camera_uses_the_rebuilt_matrix(ctx, orc):
 
 
 @pytest.mark.gpu
-def test_path_tracer_refuses_groups(ctx):
-    sc = scenes.small_room_groups(1024, seed=4, camera_keys=False)
+@pytest.mark.parametrize("camera_keys", [False, True])
+def test_path_tracer_with_groups_matches_float_oracle(ctx, orc, camera_keys):
+    """The extended mode over the room with instances (one key and two), an
+    instanced sphere, a Proc with a transformed child, a mesh with transform
+    keys and (camera_keys) camera keys: the traversal takes the single-loop
+    scene kernel and the shading applies each hit's group or keyed
+    transform at the ray's time, as the float oracle does."""
+    sc = dict(scenes.small_room_groups(2048, seed=4, camera_keys=camera_keys, debug=False), env=(0.1, 0.1, 0.12))
     ctx.load_scene(sc)
+    ref, _ = orc.Render(sc).run_path(40, 40, 0, 3, 23, max_depth=4, precision=32)
+    got, _ = ctx.render_path(40, 40, 0, 3, 23, max_depth=4)
+    ok = (np.abs(got - ref) <= 1e-5 * (1 + np.abs(ref))).all(-1)
+    assert ok.mean() >= 0.999, ok.mean()
+    assert abs(got.mean() - ref.mean()) <= 1e-4 * ref.mean()
+
+
+@pytest.mark.gpu
+def test_path_tracer_refuses_debug_shader_and_grouped_jobs(ctx):
+    """A DebugShader renders in reference mode only; batched path jobs take
+    plain meshes (an instance as a job is refused)."""
+    sc = scenes.small_room_groups(1024, seed=4, camera_keys=False)
+    ids = ctx.load_scene(sc)
     with pytest.raises(vg.VmrError) as e:
         ctx.render_path(16, 16, 0, 1, 1)
+    assert e.value.code == -7
+    inst = next(ids[i] for i, m in enumerate(sc["meshes"]) if "instance" in m)
+    with pytest.raises(vg.VmrError) as e:
+        ctx.render_path_jobs([dict(geom=inst, width=16, height=16, camera=sc["camera"])], 0, 1, 1, max_depth=2)
     assert e.value.code == -7

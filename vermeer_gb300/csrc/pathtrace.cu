@@ -80,6 +80,9 @@ struct PtJob {
 
 struct PtBatch {
   uint32_t width, height, npix;  // npix: the pixels of the rendered band
+  // GeomInstances, Procs or keyed mesh transforms in the scene: the shading
+  // kernels' GROUPS instantiation applies their transforms at each hit
+  uint32_t groups;
   uint32_t pix0;                 // the band's first pixel in the image (one-scene renders)
   uint32_t nl;        // lights
   uint32_t max_depth, rr_depth;
@@ -420,6 +423,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_generate(PtBatch b) {
 // Guide inputs of queue d: the hit point, the shading normal facing the
 // incoming ray and the direction toward the previous vertex (misses and
 // faces without a shader get a placeholder row the shade kernel ignores).
+template <bool GROUPS>
 __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
   const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
   const float* q = b.qray[d & 1];
@@ -431,7 +435,7 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
       uint32_t shid = 0;
       const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
       const V3 Rd = v3(q[3 * (size_t)b.cap + i], q[4 * (size_t)b.cap + i], q[5 * (size_t)b.cap + i]);
-      if (surface_attributes<false>(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i],
+      if (surface_attributes<GROUPS>(b.meshes[b.hgeom[i]], prim, b.hu[i], b.hv[i], b.hw[i], Ro, Rd, b.ht[i],
                              q[7 * (size_t)b.cap + i], sc, shid)) {
         wi = v3(-q[3 * (size_t)b.cap + i], -q[4 * (size_t)b.cap + i], -q[5 * (size_t)b.cap + i]);
         P = sc.P;
@@ -451,8 +455,8 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
 // records of the guided continuations.  Registers capped for 3 resident
 // blocks per SM (2 guided): measured faster than the uncapped 121 (166)
 // registers despite a few spilled words.
-template <bool GUIDED, bool TRAIN>
-__global__ void __launch_bounds__(kPtBlock, GUIDED ? 2 : 3) k_pt_shade(PtBatch b, uint32_t d) {
+template <bool GUIDED, bool TRAIN, bool GROUPS>
+__global__ void __launch_bounds__(kPtBlock, GROUPS ? 1 : (GUIDED ? 2 : 3)) k_pt_shade(PtBatch b, uint32_t d) {
   const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
   const float* q = b.qray[d & 1];
   const uint32_t* qp = b.qpath[d & 1];
@@ -504,7 +508,7 @@ __global__ void __launch_bounds__(kPtBlock, GUIDED ? 2 : 3) k_pt_shade(PtBatch b
         Ctx sc;
         uint32_t shid = 0;
         const V3 Ro = v3(q[i], q[(size_t)b.cap + i], q[2 * (size_t)b.cap + i]);
-        if (surface_attributes<false>(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], time, sc, shid)) {
+        if (surface_attributes<GROUPS>(b.meshes[geom], prim, b.hu[i], b.hv[i], b.hw[i], Ro, D, b.ht[i], time, sc, shid)) {
           const vmr_shader_std& sh = b.shaders[shid];
           const V3 wi = v3(-D.x, -D.y, -D.z);
           const bool front = dot(sc.Ng, wi) > 0.0f;
@@ -967,16 +971,24 @@ int launch_batch(vmr_ctx* ctx, const PtBatch& b, const DTop& top, DScratch* scr,
     // vertices past the guided depth sample the BSDF alone (and record nothing)
     const bool gd = guided && d < b.gdepth;
     if (gd) {
-      k_pt_prep<<<grid, kPtBlock, 0, st>>>(b, d);
+      if (b.groups) k_pt_prep<true><<<grid, kPtBlock, 0, st>>>(b, d);
+      else k_pt_prep<false><<<grid, kPtBlock, 0, st>>>(b, d);
       PCUDA(cudaGetLastError());
       guide::GuideRows r = grows;
       r.n_dev = &b.qlen[d];
       if (guide::launch_infer(r, ctx->guide.wf.p, b.gout, ctx->guide.err.as<int>(), grid / 8, st) != 0)
         return pfail(ctx, VMR_ERR_CUDA, "guide inference launch failed");
-      if (train) k_pt_shade<true, true><<<grid, kPtBlock, 0, st>>>(b, d);
-      else k_pt_shade<true, false><<<grid, kPtBlock, 0, st>>>(b, d);
+      if (b.groups) {
+        if (train) k_pt_shade<true, true, true><<<grid, kPtBlock, 0, st>>>(b, d);
+        else k_pt_shade<true, false, true><<<grid, kPtBlock, 0, st>>>(b, d);
+      } else {
+        if (train) k_pt_shade<true, true, false><<<grid, kPtBlock, 0, st>>>(b, d);
+        else k_pt_shade<true, false, false><<<grid, kPtBlock, 0, st>>>(b, d);
+      }
+    } else if (b.groups) {
+      k_pt_shade<false, false, true><<<grid, kPtBlock, 0, st>>>(b, d);
     } else {
-      k_pt_shade<false, false><<<grid, kPtBlock, 0, st>>>(b, d);
+      k_pt_shade<false, false, false><<<grid, kPtBlock, 0, st>>>(b, d);
     }
     PCUDA(cudaGetLastError());
     if (d < b.max_depth) {
@@ -1077,12 +1089,21 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   }
   if (p->max_depth > (uint32_t)kPtMaxDepth) return pfail(ctx, VMR_ERR_INVALID, "max_depth must be <= 32");
   auto& R = ctx->render;
+  // The geoms whose shading a hit reads: a GeomInstance shades as the geom
+  // it instances, a Proc's hits report its children.
+  std::vector<uint32_t> shaded;
   for (uint32_t g : used_geoms) {
     const auto& mr = ctx->meshes[g];
-    if (mr->host.group || mr->xkeys.size() >= 2)
+    if (jobs && (mr->host.group || mr->xkeys.size() >= 2))
       return pfail(ctx, VMR_ERR_UNSUPPORTED,
-                   "the extended path tracer takes meshes, spheres and one-matrix transforms "
-                   "(instances, Procs and transform keys render in reference mode, vmr_render)");
+                   "batched path jobs take meshes, spheres and one-matrix transforms (instances, Procs and "
+                   "transform keys render in one-scene calls)");
+    if (mr->host.group == 1) shaded.push_back(mr->children[0]);
+    else if (mr->host.group == 2) shaded.insert(shaded.end(), mr->children.begin(), mr->children.end());
+    else shaded.push_back(g);
+  }
+  for (uint32_t g : shaded) {
+    const auto& mr = ctx->meshes[g];
     if (mr->host.motion() && mr->aidx.p == nullptr)
       return pfail(ctx, VMR_ERR_INVALID, "a motion mesh in the scene has no shading (vmr_mesh_set_shading)");
     for (uint32_t sid : mr->shader_list) {
@@ -1246,6 +1267,8 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   b.cap = (uint32_t)cap;
   std::memcpy(b.env, R.env, 12);
   b.sel = nl > 0 ? 1.0f / (float)nl : 0.0f;
+  b.groups = 0u;
+  for (const RMesh& r : rm) b.groups |= (r.outer_nkeys != 0 || r.xf_nkeys >= 2) ? 1u : 0u;
   b.seed = p->seed;
   b.cam = R.cam_used;
   b.cam_nkeys = R.cam_keys.size() >= 2 ? (uint32_t)R.cam_keys.size() : 0u;
@@ -1382,6 +1405,7 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
       const unsigned char* c = static_cast<const unsigned char*>(d);
       for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
     };
+    fold(&b.groups, sizeof(b.groups));
     fold(&b.cam, sizeof(b.cam));
     fold(&b.cam_keys, sizeof(b.cam_keys));
     fold(&b.cam_nkeys, sizeof(b.cam_nkeys));

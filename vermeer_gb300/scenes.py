@@ -566,19 +566,19 @@ def _box_of(verts, keys16, margin=0.02):
     return (lo - pad).astype(np.float32), (hi + pad).astype(np.float32)
 
 
-def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = True) -> dict:
+def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = True, debug: bool = True) -> dict:
     """The small room with the node types that reach geometry through
     transforms: an object (a 600-triangle soup in a 0.3 cube about the
     origin, itself placed in the room), two GeomInstances of it (one key; two
     keys moving and turning over the shutter), an instance of an analytic
     sphere, a Proc of two meshes (one with its own PolyMesh transform) under
     two transform keys, a mesh with two PolyMesh transform keys, a
-    DebugShader on the instanced object and the back wall, and (camera_keys) two
-    camera motion keys."""
+    DebugShader on the instanced object and the back wall (debug; else their
+    ShaderStd shaders), and (camera_keys) two camera motion keys."""
     sc = small_room(n_tris, seed=seed)
     M = sc["meshes"]
     shaders = sc["shaders"]
-    debug = len(shaders)
+    debug_id = len(shaders)
     shaders.append(dict(debug=True, diffuse_colour=(0.9, 0.2, 0.6)))
     ov, oi = triangle_soup(600, seed + 90, lo=-0.15, hi=0.15, edge=0.04)
     obj = dict(verts=ov, idxp=oi, shaders=[5, 6], face_shader=(np.arange(600) % 2).astype(np.uint8),
@@ -615,8 +615,9 @@ def small_room_groups(n_tris: int = 4096, seed: int = 1, camera_keys: bool = Tru
     M.append(dict(verts=tv, idxp=ti, shaders=[10, 11], face_shader=(np.arange(500) % 2).astype(np.uint8),
                   transform_keys=[xf_matrix(0.0, (1, 0, 0), (1, 1, 1), (-0.1, -0.3, -0.6)),
                                   xf_matrix(0.8, (1, 0, 0), (1.1, 1.1, 1.1), (0.05, -0.25, -0.55))]))
-    obj["shaders"] = [debug, 6]
-    M[0]["shaders"] = [0, 1, debug, 3, 4]  # the back wall too
+    if debug:
+        obj["shaders"] = [debug_id, 6]
+        M[0]["shaders"] = [0, 1, debug_id, 3, 4]  # the back wall too
     if camera_keys:
         cam = sc["camera"]
         m0 = np.asarray(cam["m"], np.float32)
