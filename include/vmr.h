@@ -422,7 +422,9 @@ typedef struct {
 /* Material table (index = shader id). */
 int vmr_set_shaders(vmr_ctx* ctx, const vmr_shader_std* shaders, uint32_t n);
 /* PolyMesh.Shader (the mesh's shader ids; faces pick one through the
- * shader_idx given at build) and optional per-vertex normals (key 0). */
+ * shader_idx given at build) and optional per-vertex normals (key 0) of a
+ * static mesh; a motion mesh's normals go through
+ * vmr_mesh_set_motion_normals (VMR_ERR_UNSUPPORTED here). */
 int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, uint32_t n_shaders,
                          const float* normals);
 /* Per-key normals of a motion mesh: PolyMesh.Normals with as many motion

@@ -713,7 +713,9 @@ int vmr_mesh_set_shading(vmr_ctx* ctx, uint32_t geom, const uint32_t* shaders, u
   MeshRec& rec = *ctx->meshes[geom];
   if (rec.host.group) return rfail(ctx, VMR_ERR_UNSUPPORTED, "an instance or Proc shades through its geoms");
   if (rec.host.motion() && normals)
-    return rfail(ctx, VMR_ERR_UNSUPPORTED, "normals of motion meshes are not supported");
+    return rfail(ctx, VMR_ERR_UNSUPPORTED,
+                 "a motion mesh takes keyed normals through vmr_mesh_set_motion_normals (its hits ignore "
+                 "one-key normals, trace.go:694-712)");
   rec.shader_list.assign(shaders, shaders + n_shaders);
   rec.has_normals = normals != nullptr;
   if (ctx->device < 0) return VMR_OK;

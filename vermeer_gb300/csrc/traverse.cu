@@ -2132,8 +2132,8 @@ int launch_scene_t(const DTop& top, const TraceLaunch& l) {
   // Instances, Procs and keyed transforms are traced by the single-loop kernel.
   if (!COUNT && (l.kernel & kKernelWhileWhile) && !top.simple_only) {
     // Motion meshes and motion top levels take the MOT instantiation (lerped
-    // node boxes, per-lane motion leaves); only-static scenes keep the leaner
-    // kernel.
+    // node boxes, motion leaves in the cooperative phase with both keys'
+    // vertices lerped); only-static scenes keep the leaner kernel.
     const bool coop = (l.kernel & kKernelCoopLeaf) != 0;
     auto k = top.all_static ? (coop ? k_trace_scene_ww<ANY, true, false> : k_trace_scene_ww<ANY, false, false>)
                             : (coop ? k_trace_scene_ww<ANY, true, true> : k_trace_scene_ww<ANY, false, true>);
