@@ -686,7 +686,7 @@ int vmr_split_rows(uint32_t height, uint32_t n, uint32_t* row_begin, uint32_t* r
 
 /* Queue capacity (paths per wavefront batch, whole iterations) of the
  * context's one-scene renders when params.max_batch_samples is 0.
- * vmr_set_path_batch: set it (0: the default, 8M paths; else >= 1024).
+ * vmr_set_path_batch: set it (0: the default, 16M paths; else >= 1024).
  * vmr_autotune_path: render params' iterations (GUIDED sampled, TRAIN and
  * fb64 ignored; no framebuffer of the caller is touched) at candidate
  * capacities of 256K..32M paths, each after an untimed call, and keep the

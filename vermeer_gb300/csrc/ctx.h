@@ -108,7 +108,7 @@ struct RenderState {
   DevBuf jobmesh;  // batched path jobs: the mesh table the traversal reads
   DevBuf buf;      // reference mode batch buffers
   DevBuf ptbuf;    // extended mode batch buffers
-  uint32_t path_batch = 0;  // paths per batch of a one-scene render when the call gives none (0: 8M)
+  uint32_t path_batch = 0;  // paths per batch of a one-scene render when the call gives none (0: 16M)
   void* pt_host = nullptr;  // pinned per-batch parameters (extended mode)
   size_t pt_host_bytes = 0;
   PathGraph graph;

@@ -23,7 +23,7 @@
 //                            buf = (buf*i + L)/(i+1), i the 0-based iteration
 //                            (float, optional float64)
 //   [k_pt_targets, training] VMR_PATH_TRAIN: the guide's records and Adam steps
-// A batch holds the context's queue capacity (8M paths by default,
+// A batch holds the context's queue capacity (16M paths by default,
 // vmr_set_path_batch / vmr_autotune_path).  Batched jobs put many one-mesh
 // images end to end in one pixel arena; their rays enter their own mesh
 // (the scene kernels' job mode).
@@ -1164,13 +1164,15 @@ static int render_path_impl(vmr_ctx* ctx, const vmr_path_params* p, float* fb, v
   cudaStream_t st = ctx->stream;
   const uint32_t band = (!jobs && p->row_count) ? p->row_count : p->height;
   const uint32_t npix = jobs ? (uint32_t)npix_jobs : p->width * band;
-  // Default 8M paths per batch: every bounce's launches end in a tail of
-  // long paths, which a larger batch amortises (sphere grid 1920x1080, 8 spp:
-  // 80.7 ms at 2M, 66.5 ms at 8M); a one-scene render uses the context's
-  // tuned capacity when it has one (vmr_autotune_path, vmr_set_path_batch).
+  // Default 16M paths per batch (about 3 GB of queues, allocated only when
+  // a call has that many paths): every bounce's launches end in a tail of
+  // long paths, which a larger batch amortises (sphere grid 1920x1080, 8
+  // spp: 80.7 ms at 2M, 66.5 ms at 8M, 16M 3-4% faster than 8M); a one-scene
+  // render uses the context's tuned capacity when it has one
+  // (vmr_autotune_path, vmr_set_path_batch).
   const uint32_t per_batch = p->max_batch_samples     ? p->max_batch_samples
                              : (!jobs && ctx->render.path_batch) ? ctx->render.path_batch
-                                                                 : (8u << 20);
+                                                                 : (16u << 20);
   uint32_t ipb = std::max<uint32_t>(1, per_batch / npix);
   if (p->iter_count > 0 && ipb > p->iter_count) ipb = p->iter_count;
   const uint64_t cap = (uint64_t)ipb * npix;
