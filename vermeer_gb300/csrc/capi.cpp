@@ -308,7 +308,10 @@ int launch_trace_chunk(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_
     uint32_t* hist = reinterpret_cast<uint32_t*>(f + nf * nfield);
     vmr::RaySoA sorted{f, f + nf, f + 2 * nf, f + 3 * nf, f + 4 * nf, f + 5 * nf, f + 6 * nf,
                        nfield == 8 ? f + 7 * nf : nullptr};
+    // a context mesh's own bounds; the scene's (the flattened scene's mesh,
+    // which is no context mesh, covers exactly the scene's geoms)
     const float* mb = mesh ? ctx->mesh_bounds_of(mesh) : ctx->top.bounds6;
+    if (!mb) mb = ctx->top.bounds6;
     int se = vmr::launch_ray_sort(l.rays, n, mb, tn.sort_bits ? tn.sort_bits : 4, keys, hist, order, sorted,
                                   ctx->stream);
     if (se != 0) return cuda_fail(ctx, (cudaError_t)se, "ray sort launch");
@@ -387,6 +390,18 @@ int trace_host(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays* rays, size_t n, 
 }  // namespace
 
 namespace vmr {
+int trace_flat_any_hit(vmr_ctx* ctx, const vmr_rays& r, size_t n, const vmr_hits& h, bool* used) {
+  *used = false;
+  if (!(ctx->tuning.kernel & kKernelWhileWhile)) return VMR_OK;
+  const uint32_t* map = nullptr;
+  uint32_t nmap = 0;
+  int st = VMR_OK;
+  const DMesh* flat = flat_scene(ctx, &map, &nmap, &st);
+  if (st != VMR_OK || !flat) return st;
+  *used = true;
+  return launch_trace_chunk(ctx, flat, r, n, VMR_TRACE_DEVICE | VMR_TRACE_ANY_HIT, h, true, true, true);
+}
+
 const DMesh* flat_scene(vmr_ctx* ctx, const uint32_t** map, uint32_t* n, int* status) {
   *status = VMR_OK;
   FlatScene& F = ctx->flat;

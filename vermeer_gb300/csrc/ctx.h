@@ -200,4 +200,11 @@ namespace vmr {
 // builder declines).  *map / *n: the leaf position -> (geom, leaf position)
 // table on the device and its length.  Returns a VMR status in *status.
 const DMesh* flat_scene(vmr_ctx* ctx, const uint32_t** map, uint32_t* n, int* status);
+// Any-hit trace of n device rays against the flattened scene (capi.cpp):
+// whether each ray hits something within its tmax is the same whichever
+// tree holds the triangles, so shadow rays may take it wherever the scene
+// flattens.  h.prim >= 0 marks a hit (a leaf position of the flat mesh).
+// *used false (nothing launched): the scene does not flatten, or the
+// context's kernel is not the while-while one.
+int trace_flat_any_hit(vmr_ctx* ctx, const vmr_rays& r, size_t n, const vmr_hits& h, bool* used);
 }  // namespace vmr

@@ -1091,7 +1091,13 @@ int vmr_render(vmr_ctx* ctx, const vmr_render_params* p, float* fb, vmr_render_s
       if (nq) {
         vmr_rays sr{b.sx, b.sy, b.sz, b.sdx, b.sdy, b.sdz, b.stmax, b.stime};
         vmr_hits sh{b.shit, nullptr, nullptr, nullptr, nullptr, nullptr};
-        rc = vmr_trace_scene(ctx, &sr, nq, VMR_TRACE_DEVICE | VMR_TRACE_ANY_HIT, &sh, nullptr);
+        // EvaluateLightSamples uses only TraceProbe's yes/no for its shadow
+        // rays (core/shader.go:276,317,380; core/trace.go:23-35), which does
+        // not depend on the traversal order: a scene that flattens answers
+        // it from one tree
+        bool flat = false;
+        rc = vmr::trace_flat_any_hit(ctx, sr, nq, sh, &flat);
+        if (rc == VMR_OK && !flat) rc = vmr_trace_scene(ctx, &sr, nq, VMR_TRACE_DEVICE | VMR_TRACE_ANY_HIT, &sh, nullptr);
         if (rc != VMR_OK) return rc;
         k_resolve<<<(int)((nq + 255) / 256), 256, 0, st>>>(b, l, (uint32_t)nq);
         RCUDA(cudaGetLastError());
