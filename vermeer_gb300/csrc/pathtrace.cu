@@ -452,9 +452,12 @@ __global__ void __launch_bounds__(kPtBlock) k_pt_prep(PtBatch b, uint32_t d) {
 
 // One bounce of every path in queue d.  GUIDED: one-sample MIS of the guide
 // (probability alpha) and the BSDF at non-mirror vertices; TRAIN: training
-// records of the guided continuations.  Registers capped for 3 resident
-// blocks per SM (2 guided): measured faster than the uncapped 121 (166)
-// registers despite a few spilled words.
+// records of the guided continuations; GROUPS: the scene has GeomInstances,
+// Procs or keyed mesh transforms (their transforms applied at each hit).
+// Registers capped for 3 resident blocks per SM (2 guided): measured faster
+// than the uncapped 121 (166) registers despite a few spilled words; the
+// GROUPS instantiation, which holds the keyed-transform helpers' registers,
+// is left uncapped.
 template <bool GUIDED, bool TRAIN, bool GROUPS>
 __global__ void __launch_bounds__(kPtBlock, GROUPS ? 1 : (GUIDED ? 2 : 3)) k_pt_shade(PtBatch b, uint32_t d) {
   const uint64_t n = b.qlen[d] < b.cap ? b.qlen[d] : b.cap;
