@@ -312,11 +312,16 @@ int launch_trace_chunk(vmr_ctx* ctx, const DMesh* mesh, const vmr_rays& r, size_
     // which is no context mesh, covers exactly the scene's geoms)
     const float* mb = mesh ? ctx->mesh_bounds_of(mesh) : ctx->top.bounds6;
     if (!mb) mb = ctx->top.bounds6;
+    // A static mesh in the while-while kernel reads the copy as 32-byte
+    // records (two 16-byte loads a ray, its input index inside), written
+    // over the order and array regions (4 + 28 bytes a ray).
+    const bool recs = mesh && mesh->keys <= 1 && !r.time && (tn.kernel & vmr::kKernelWhileWhile);
+    if (recs) sorted = vmr::RaySoA{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, order};
     int se = vmr::launch_ray_sort(l.rays, n, mb, tn.sort_bits ? tn.sort_bits : 4, keys, hist, order, sorted,
                                   ctx->stream);
     if (se != 0) return cuda_fail(ctx, (cudaError_t)se, "ray sort launch");
     l.rays = sorted;
-    l.order = order;
+    l.order = recs ? nullptr : order;
   }
   if (first) VMR_CUDA(ctx, cudaEventRecord(ctx->evm, ctx->stream));
   int e = mesh ? vmr::launch_trace_mesh(*mesh, l) : vmr::launch_trace_scene(ctx->top.dtop, l);

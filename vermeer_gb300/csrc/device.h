@@ -102,6 +102,10 @@ struct DTop {
 
 struct RaySoA {
   const float *px, *py, *pz, *dx, *dy, *dz, *tmax, *time;
+  // If set: the rays as two 16-byte records each, (px, py, pz, dx) and
+  // (dy, dz, tmax, input index as bits), the key-ordered copy of a static
+  // mesh trace (the arrays above are then unused; time is 0)
+  const void* rec = nullptr;
 };
 struct HitSoA {
   int32_t* prim;
@@ -175,7 +179,9 @@ struct TraceLaunch {
 };
 int launch_trace_mesh(const DMesh& mesh, const TraceLaunch& l);
 // n_dev (optional): the ray count on the device, at most n (a wavefront queue
-// length); the grid is sized for n.
+// length); the grid is sized for n.  sorted_out.rec set: the key-ordered copy
+// is written as records (RaySoA::rec, 32 bytes a ray) and order is not
+// written; else as arrays, with order[i] = the input index of position i.
 int launch_ray_sort(const RaySoA& rays, uint64_t n, const float bounds[6], int bits, uint32_t* keys, uint32_t* hist,
                     uint32_t* order, const RaySoA& sorted_out, void* stream,
                     const unsigned long long* n_dev = nullptr);

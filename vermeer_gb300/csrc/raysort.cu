@@ -124,12 +124,18 @@ __global__ void k_ray_scatter(RaySoA rays, uint64_t n, const unsigned long long*
   float* dz = const_cast<float*>(sorted_out.dz);
   float* tm = const_cast<float*>(sorted_out.tmax);
   float* ti = const_cast<float*>(sorted_out.time);
+  float4* rec = static_cast<float4*>(const_cast<void*>(sorted_out.rec));
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const uint64_t rounds = (n + stride - 1) / stride;
   for (uint64_t r = 0; r < rounds; ++r) {
     const uint64_t i = r * stride + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint32_t pos = warp_bucket_add(offsets, i < n ? keys[i] : kNoKey);
     if (i >= n) continue;
+    if (rec) {  // one ray = two 16-byte stores instead of eight scattered 4-byte ones
+      rec[2 * (size_t)pos] = make_float4(rays.px[i], rays.py[i], rays.pz[i], rays.dx[i]);
+      rec[2 * (size_t)pos + 1] = make_float4(rays.dy[i], rays.dz[i], rays.tmax[i], __uint_as_float((uint32_t)i));
+      continue;
+    }
     order[pos] = (uint32_t)i;
     px[pos] = rays.px[i];
     py[pos] = rays.py[i];

@@ -1277,8 +1277,19 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : 256, MINB > 0 ? MINB : 1)
       if (!alive) {
         const uint64_t i = base + __popc(need & lanes_below);
         if (i < n) {
-          rid = order ? (uint64_t)__ldg(order + i) : i;
-          load_ray(rays, i, r);
+          if (!MOTION && rays.rec) {  // the key-ordered copy as records (RaySoA::rec)
+            const float4* A = static_cast<const float4*>(rays.rec);
+            const float4 a = __ldg(A + 2 * i), b = __ldg(A + 2 * i + 1);
+            r.ox = a.x; r.oy = a.y; r.oz = a.z;
+            r.dx = a.w; r.dy = b.x; r.dz = b.y;
+            r.tclosest = b.z;
+            r.time = 0.0f;
+            ray_setup(r);
+            rid = __float_as_uint(b.w);
+          } else {
+            rid = order ? (uint64_t)__ldg(order + i) : i;
+            load_ray(rays, i, r);
+          }
           h = HitRec{-1, -1, 0.f, 0.f, 0.f};
           hit = false;
           node = 0;  // the root, pushed with T = Tclosest (intersect.go:93-95)
@@ -2109,10 +2120,12 @@ int launch_mesh_t(const DMesh& mesh, const TraceLaunch& l) {
   const int block = l.block > 0 ? l.block : 128;
   const int v = l.kernel;
   if (v & kKernelWhileWhile) {
-    // the register cap: 64 registers (8 resident blocks per SM) for static
-    // meshes; motion meshes hold both keys' boxes and vertices and run
-    // fastest at 5 blocks (96 registers: 130 against 100 Mrays/s at 8)
-    if (v & kKernelRegCap) return launch_ww<MOTION, ANY, COUNT, MOTION ? 5 : 8>(mesh, l, 128);
+    // the register cap: 7 resident blocks per SM (72 registers) for static
+    // meshes (with the record fetch, 8 blocks at 64 registers spilled 108 B
+    // and ran 5% slower); motion meshes hold both keys' boxes and vertices
+    // and run fastest at 5 blocks (96 registers: 130 against 100 Mrays/s
+    // at 8)
+    if (v & kKernelRegCap) return launch_ww<MOTION, ANY, COUNT, MOTION ? 5 : 7>(mesh, l, 128);
     return launch_ww<MOTION, ANY, COUNT, 0>(mesh, l, block);
   }
   const int refill = l.refill_min > 0 ? l.refill_min : 4;
