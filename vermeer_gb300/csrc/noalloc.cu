@@ -30,7 +30,8 @@ namespace {
 constexpr size_t kMaxRays = VMR_NOALLOC_MAX_RAYS;
 // Layout: work counter / status / visit counters, bucket histogram (sized for
 // the widest sort key a tuning may select), ray keys, order, key-ordered rays
-// (8 float fields).  Every part starts on a 256-byte boundary.
+// (8 float fields, or 32-byte records for static meshes).  Every part starts
+// on a 256-byte boundary.
 constexpr size_t kHeaderBytes = 256;
 constexpr size_t kHistBytes = ((sizeof(uint32_t) * vmr::kSortBucketsMax + 255) / 256) * 256;
 constexpr size_t kKeyBytes = sizeof(uint32_t) * kMaxRays;
@@ -154,15 +155,19 @@ extern "C" int vmr_trace_mesh_noalloc(vmr_ctx* ctx, uint32_t geom, const vmr_ray
   l.refill_min = tuning.refill_min;
   l.walk_tail = tuning.walk_tail;
   if ((tuning.kernel & vmr::kKernelSort) && n >= vmr::kSortMinRays) {
-    const vmr::RaySoA sorted{f, f + kMaxRays, f + 2 * kMaxRays, f + 3 * kMaxRays, f + 4 * kMaxRays,
-                             f + 5 * kMaxRays, f + 6 * kMaxRays, rays->time ? f + 7 * kMaxRays : nullptr};
+    // a static mesh in the while-while kernel reads the copy as 32-byte
+    // records (RaySoA::rec), which fill the ray region exactly
+    const bool recs = mesh->keys <= 1 && !rays->time && (tuning.kernel & vmr::kKernelWhileWhile);
+    vmr::RaySoA sorted{f, f + kMaxRays, f + 2 * kMaxRays, f + 3 * kMaxRays, f + 4 * kMaxRays,
+                       f + 5 * kMaxRays, f + 6 * kMaxRays, rays->time ? f + 7 * kMaxRays : nullptr};
+    if (recs) sorted = vmr::RaySoA{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, f};
     const int bits = tuning.sort_bits ? tuning.sort_bits : 4;
     if (bits > vmr::kSortMaxBits)
       return vmr::ctx_fail(ctx, VMR_ERR_INVALID, "vmr_trace_mesh_noalloc: sort key wider than the histogram");
     if (vmr::launch_ray_sort(l.rays, n, bounds, bits, keys, hist, order, sorted, stream) != 0)
       return vmr::ctx_fail(ctx, VMR_ERR_CUDA, "vmr_trace_mesh_noalloc: ray reordering launch failed");
     l.rays = sorted;
-    l.order = order;
+    l.order = recs ? nullptr : order;
   }
   if (vmr::launch_trace_mesh(*mesh, l) != 0)
     return vmr::ctx_fail(ctx, VMR_ERR_CUDA, "vmr_trace_mesh_noalloc: traversal launch failed");
