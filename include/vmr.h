@@ -63,8 +63,10 @@ int vmr_abi_version(void);
  * the defaults. */
 typedef struct {
     int kernel;          /* bit 0: while-while (else step-scheduled); bit 1:
-                            L1 prefetch of the next node; bit 2: 64-register
-                            cap (while-while only); bit 3: reorder rays by
+                            L1 prefetch of the next node; bit 2: register
+                            cap for 7 resident 128-thread blocks per SM (5
+                            for motion meshes; while-while only); bit 3:
+                            reorder rays by
                             permutation class and origin cell before a mesh
                             trace of >= 65536 rays; bit 4: the top 16
                             entries of the traversal stack in shared memory
