@@ -1485,11 +1485,12 @@ __device__ __forceinline__ bool motion_keys(uint32_t keys, float time, float& tm
   return !(key < 0 || key2 >= (int)keys);
 }
 
-// MOT (motion meshes and top levels) holds more state: capped for 5
-// resident blocks per SM (96 registers) instead of 8, which spilled 1 KB
-// per thread and measured 27% slower on the batched jobs.
+// Capped for 7 resident blocks per SM (72 registers; the two-level sphere
+// grid 1% faster than at 8).  MOT (motion meshes and top levels) holds more
+// state: capped for 5 (96 registers) instead, as at 8 it spilled 1 KB per
+// thread and measured 27% slower on the batched jobs.
 template <bool ANY, bool COOP = false, bool MOT = false>
-__global__ void __launch_bounds__(128, MOT ? 5 : 8)
+__global__ void __launch_bounds__(128, MOT ? 5 : 7)
     k_trace_scene_ww(const DTop top, RaySoA rays, HitSoA hits, uint64_t n, DScratch* scratch,
                      const unsigned long long* n_dev, const uint32_t* order, int walk_tail,
                      const uint32_t* ray_path, const uint32_t* path_geom) {
